@@ -1,0 +1,183 @@
+/*
+ * fbgpu.h -- C ABI of the GB300 (sm_103a) FIREBALL Harris matrix-element
+ * assembly library, libfbgpu.so.
+ *
+ * The library replaces, as a drop-in, the table-driven assembly path of the
+ * reference (thunder-dft/thunder-master, Fortran):
+ *
+ *   module M_Fdata_2c / M_Fdata_3c   read_Fdata_2c / read_Fdata_3c
+ *   module M_species                 read_info
+ *   subroutine make_cells
+ *   module M_neighbors               driver_neighbors (find_neighbors,
+ *                                    find_common_neighbors)
+ *   module M_assemble_2c             assemble_S, assemble_T, assemble_vna_2c
+ *   module M_assemble_3c             assemble_vna_3c
+ *   module M_Dassemble_2c            Dassemble_S, Dassemble_T, Dassemble_vna_2c
+ *   module M_Dassemble_3c            Dassemble_vna_3c
+ *   module M_build_forces            build_forces (the kinetic, vna, f3na and
+ *                                    Pulay terms)
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (FB_OK = 0) and never aborts the process; fb_last_error() gives the text.
+ * Where the reference would `stop`, the library returns the matching status.
+ *
+ * Data layout (identical to the Fortran per-neighbor block types):
+ *   positions   ratom[3*i + k], Angstrom, i = 0..natoms-1
+ *   species     imass[i], 1-based species number (order of nZ in
+ *               fb_load_fdata, as in Fdata.inp)
+ *   lattice     lattice[3*a + k] = component k of lattice vector a+1
+ *   pairs       pair p = pair_off[i] + (ineigh-1), atoms in order, each
+ *               atom's neighbors in the reference order (mbeta outer, jatom
+ *               inner, c.SYSTEM/M_neighbors.f90:409-437)
+ *   blocks      block of pair p at blk_off[p], column-major norb_i x norb_j:
+ *               s%overlap(i)%neighbors(ineigh)%block(mu,nu) is
+ *               S[blk_off[p] + (mu-1) + norb_i*(nu-1)]
+ *   Dblocks     Dblock(ix,mu,nu) at 3*blk_off[p] + (ix-1) + 3*((mu-1) +
+ *               norb_i*(nu-1))
+ *   per-pair 3-vectors   vna_ontop(:,ineigh), vna_atom(:,ineigh) at 3*p
+ *   per-atom 3-vectors   forces(i)%ftot(:) at 3*i
+ * Neighbor indices returned to the caller are 1-based like the Fortran
+ * arrays (neigh_j, neigh_back, neigh_self, iatom_common_j, jatom_common_j,
+ * neigh_common); cell indices mbeta are 0-based as in the reference.
+ *
+ * Threading: one context per thread; calls on a context are ordered on its
+ * CUDA stream and return after the work completes unless stated otherwise.
+ */
+#ifndef FBGPU_H
+#define FBGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FB_OK 0
+#define FB_ERR_ARG 1           /* bad argument */
+#define FB_ERR_IO 2            /* Fdata file missing or unparsable */
+#define FB_ERR_TABLE 3         /* interaction cell or ME map missing */
+#define FB_ERR_X_NEGATIVE 4    /* getMEs: negative distance */
+#define FB_ERR_X_TOO_LARGE 5   /* getMEs: x > xmax*(1+1e-5) */
+#define FB_ERR_ATOMS_CLOSE 6   /* find_neighbors: two atoms < 0.5 A apart */
+#define FB_ERR_NEIGH_SELF 7    /* neigh_self missing or found twice */
+#define FB_ERR_NEIGH_BACK 8    /* neigh_back missing or found twice */
+#define FB_ERR_CUDA 9          /* CUDA runtime error */
+#define FB_ERR_WATCHDOG 10     /* a device wait ran out of its budget */
+#define FB_ERR_STATE 11        /* call out of order (e.g. no neighbors yet) */
+#define FB_ERR_CAPACITY 12     /* size beyond a stated maximum */
+#define FB_ERR_UNSUPPORTED 13  /* basis or map this build does not handle */
+
+/* assembly selection bits for fb_assemble / fb_dassemble */
+#define FB_S 1u        /* overlap           (assemble_S / Dassemble_S) */
+#define FB_T 2u        /* kinetic           (assemble_T / Dassemble_T) */
+#define FB_VNA2C 4u    /* neutral atom 2c   (assemble_vna_2c / Dassemble_vna_2c) */
+#define FB_VNA3C 8u    /* neutral atom 3c   (assemble_vna_3c / Dassemble_vna_3c) */
+#define FB_ALL 15u
+#define FB_KEEP_DBLOCKS 16u  /* fb_dassemble: also keep dS, dT Dblocks */
+
+/* block sets for fb_get_blocks / fb_device_blocks */
+#define FB_BLOCK_S 0       /* s%overlap(i)%neighbors(k)%block */
+#define FB_BLOCK_T 1       /* s%kinetic(i)%neighbors(k)%block */
+#define FB_BLOCK_VNA 2     /* s%vna(i)%neighbors(k)%block  (atom + 3c) */
+#define FB_BLOCK_VNAO 3    /* s%vna(i)%neighbors(k)%blocko (ontop L + R) */
+#define FB_BLOCK_DS 4      /* s%overlap(i)%neighbors(k)%Dblock */
+#define FB_BLOCK_DT 5      /* s%kinetic(i)%neighbors(k)%Dblock */
+#define FB_BLOCK_RHO 6     /* s%denmat(i)%neighbors(k)%block (input) */
+#define FB_BLOCK_CAPE 7    /* s%capemat(i)%neighbors(k)%block (input) */
+
+/* force arrays for fb_get_forces */
+#define FB_F_TOT 0         /* ftot: kinetic + vna + f3na(a+b+c) - pulay */
+#define FB_F_KINETIC 1     /* forces(i)%kinetic */
+#define FB_F_VNA 2         /* forces(i)%vna (atom + ontop pair sums) */
+#define FB_F_PULAY 3       /* forces(i)%pulay */
+#define FB_F_F3NAA 4       /* forces(i)%f3naa */
+#define FB_F_F3NAB 5       /* forces(i)%f3nab */
+#define FB_F_F3NAC 6       /* forces(i)%f3nac */
+#define FB_F_VNA_ONTOP 7   /* forces(i)%vna_ontop(3, neighn), per pair */
+#define FB_F_VNA_ATOM 8    /* forces(i)%vna_atom(3, neighn), per pair */
+
+typedef struct fb_ctx fb_ctx;
+
+/* Create a context on CUDA device `device`.  Replaces the module state that
+ * M_species, M_Fdata_2c/3c and the structure type hold in the reference. */
+int fb_create(int device, fb_ctx **out);
+void fb_destroy(fb_ctx *ctx);
+const char *fb_last_error(const fb_ctx *ctx);
+const char *fb_version(void);
+
+/* Run the context's work on `stream` (a cudaStream_t, or NULL for the
+ * context's own stream).  The caller keeps ownership of the stream. */
+int fb_set_stream(fb_ctx *ctx, void *stream);
+
+/* read_info (c.SYSTEM/M_species.f90:1057) + read_Fdata_2c
+ * (e.FDATA/M_Fdata_2c.f90:149) + read_Fdata_3c (e.FDATA/M_Fdata_3c.f90:143):
+ * parse the Fdata directory and stage every table in device memory.
+ * nZ[k] is the atomic number of species k+1 (the Fdata.inp list). */
+int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies,
+                  const int *nZ);
+/* species layout after fb_load_fdata: norb_max of species isp (1-based) */
+int fb_species_norb(const fb_ctx *ctx, int isp);
+
+/* Structure: positions, species, lattice; make_cells
+ * (c.SYSTEM/make_cells.f90:51).  icluster = 1 disables periodic images. */
+int fb_set_structure(fb_ctx *ctx, int natoms, const double *ratom,
+                     const int *imass, const double *lattice, int icluster);
+/* New positions for the same atoms (an MD step); neighbor maps must be
+ * rebuilt by fb_neighbors before the next assembly. */
+int fb_update_positions(fb_ctx *ctx, const double *ratom);
+
+/* driver_neighbors (c.SYSTEM/M_neighbors.f90:93): find_neighbors,
+ * neigh_self, neigh_back, find_common_neighbors, built on the GPU in the
+ * reference order. */
+int fb_neighbors(fb_ctx *ctx);
+/* Adopt neighbor maps computed by the caller (e.g. read_NEIGHBORS,
+ * M_neighbors.f90:171).  Arrays are 1-based as returned by
+ * fb_get_neighbors; common-neighbor maps are rebuilt on the GPU. */
+int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j,
+                     const int *neigh_b);
+int fb_get_sizes(const fb_ctx *ctx, int *npairs, int *ntriplets,
+                 long long *nblock);
+/* copy the maps out (any pointer may be NULL) */
+int fb_get_neighbors(fb_ctx *ctx, int *neighn, int *neigh_j, int *neigh_b,
+                     int *neigh_back, int *neigh_self, long long *blk_off);
+int fb_get_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j,
+                  int *iatom_common_b, int *jatom_common_j,
+                  int *jatom_common_b, int *neigh_common);
+
+/* assemble_S/T/vna_2c (j.ASSEMBLERS/M_assemble_2c_Harris.f90:89,233,435)
+ * and assemble_vna_3c (j.ASSEMBLERS/M_assemble_3c_Harris.f90:82), selected
+ * by `what`.  Blocks stay in device memory until fetched. FB_VNA3C
+ * accumulates onto the vna blocks, so it requires FB_VNA2C in the same call
+ * or an earlier one (the reference's call order). */
+int fb_assemble(fb_ctx *ctx, unsigned what);
+/* copy one block set to the host (nblock doubles; 3*nblock for Dblocks) */
+int fb_get_blocks(fb_ctx *ctx, int which, double *out);
+/* device address of a block set (valid until the next fb_neighbors) */
+int fb_device_blocks(fb_ctx *ctx, int which, void **dptr);
+
+/* Density matrix and energy-weighted density matrix blocks (host, nblock
+ * doubles each, layout as the blocks); cape may be NULL (zero Pulay). */
+int fb_set_denmat(fb_ctx *ctx, const double *rho, const double *cape);
+
+/* Dassemble_S/T/vna_2c (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:96,289,538),
+ * Dassemble_vna_3c (k.DASSEMBLERS/M_Dassemble_3c_Harris.f90:136) and the
+ * assembly terms of build_forces (c.SYSTEM/M_build_forces.f90:172). */
+int fb_dassemble(fb_ctx *ctx, unsigned what);
+/* copy one force array to the host (3*natoms, or 3*npairs for the per-pair
+ * vna_ontop / vna_atom arrays) */
+int fb_get_forces(fb_ctx *ctx, int which, double *out);
+
+/* End-to-end H/S step through host buffers: upload positions, build the
+ * neighbor maps, assemble S, T, vna (2c + 3c) and copy the four block sets
+ * back.  Any output may be NULL. */
+int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T,
+                     double *vna, double *vnao);
+
+/* Number of kernels this context launched since creation (diagnostics). */
+long long fb_kernel_launches(const fb_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

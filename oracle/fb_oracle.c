@@ -1,0 +1,1673 @@
+/*
+ * fb_oracle.c -- CPU oracle: plain-C restatement of the FIREBALL Harris
+ * matrix-element assembly (reference: thunder-dft/thunder-master, Fortran).
+ *
+ * TEST INFRASTRUCTURE ONLY (see fb_oracle.h).  Parity status: UNPINNED --
+ * the reference has no tests or golden data and cannot be compiled here.
+ *
+ * Every routine below names the reference file:line range it restates.  The
+ * floating-point expressions keep the reference's operation order; the file
+ * is compiled with -ffp-contract=off so no fused multiply-adds are formed.
+ * Fortran 1-based indices are kept where they appear in arithmetic (grid
+ * points, orbital numbers) and converted to 0-based only for storage.
+ */
+#include "fb_oracle.h"
+
+#include <ctype.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* status codes, identical to include/fbgpu.h */
+enum {
+  OK = 0, E_ARG = 1, E_IO = 2, E_TABLE = 3, E_XNEG = 4, E_XLARGE = 5,
+  E_CLOSE = 6, E_SELF = 7, E_BACK = 8, E_UNSUP = 13
+};
+
+/* include/constants.h:2,4 */
+#define P_abohr 0.529177
+#define P_eq2 14.39975
+
+/* include/interactions_2c.h:2-3, interactions_3c.h:2-4 */
+#define P_MAXTYPE2 25
+#define P_MAXSUB2 9
+#define P_MAXTYPE3 4
+#define P_MAXSUB3 6
+#define P_MAXTHETA 5
+#define P_overlap 1
+#define P_kinetic 2
+#define P_vna_ontopL 3
+#define P_vna_ontopR 4
+#define P_vna_atom 5
+#define P_bcna 3
+#define P_mbox 4 /* c.SYSTEM/M_configuraciones.f90:359 */
+
+#define MAXSP 8
+#define MAXSH 8
+#define MAXORB 16
+
+static __thread char g_err[512];
+static int g_threads = 1;
+
+static void seterr(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+const char *or_last_error(void) { return g_err; }
+void or_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+
+/* ------------------------------------------------------------------------ */
+/* data types: T_Fdata_cell_2c/bundle (e.FDATA/M_Fdata_2c.f90:83-109),       */
+/* T_Fdata_cell_3c/bundle (e.FDATA/M_Fdata_3c.f90:77-103), T_species         */
+/* (c.SYSTEM/M_species.f90:116-164)                                          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int nME, nx;
+  double dx, xmax;
+  int *mu, *nu, *mvalue;
+  double *F; /* F[(ix-1) + nx*(iME-1)] */
+} cell2c;
+
+typedef struct {
+  int ncell;
+  int index[P_MAXTYPE2 + 1][P_MAXSUB2 + 1];
+  cell2c *cells;
+} bundle2c;
+
+typedef struct {
+  int nME, nx, ny;
+  double xmax, ymax;
+  int *mu, *nu, *mvalue;
+  double *F; /* F[(ix-1) + nx*((iy-1) + ny*(iME-1))] */
+} cell3c;
+
+typedef struct {
+  int ncell;
+  int index[P_MAXTYPE3 + 1][P_MAXSUB3 + 1][P_MAXTHETA + 1];
+  cell3c *cells;
+} bundle3c;
+
+typedef struct {
+  int nZ, nssh, nssh_PP, norb_max;
+  int lssh[MAXSH];
+  double rcutoffA[MAXSH];
+  double rcutoffA_max;
+} species_t;
+
+struct or_fdata {
+  int nspecies, have_dorbitals;
+  species_t sp[MAXSP + 1]; /* 1-based */
+  bundle2c b2[MAXSP + 1][MAXSP + 1];
+  bundle3c b3[MAXSP + 1][MAXSP + 1][MAXSP + 1];
+};
+
+struct or_sys {
+  or_fdata *fd;
+  int natoms, icluster, mbeta_max;
+  double *ratom; /* 3N */
+  int *imass;
+  double lattice[3][3];
+  double (*xl)[3];
+  /* neighbors */
+  int *neighn, *pair_off, *neigh_j, *neigh_b, *neigh_back, *neigh_self;
+  long long *blk_off;
+  long long nblock;
+  int npairs;
+  int *ncommon, *trip_off, *ci_j, *ci_b, *cj_j, *cj_b, *cneigh;
+  int ntrip;
+};
+
+/* ------------------------------------------------------------------------ */
+/* list-directed text input                                                  */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  char *buf;
+  size_t len, pos; /* pos = start of the next record */
+} txt;
+
+static int txt_open(txt *t, const char *path) {
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    seterr("cannot open %s", path);
+    return E_IO;
+  }
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  t->buf = (char *)malloc((size_t)n + 1);
+  t->len = fread(t->buf, 1, (size_t)n, f);
+  t->buf[t->len] = 0;
+  t->pos = 0;
+  fclose(f);
+  return OK;
+}
+static void txt_close(txt *t) {
+  free(t->buf);
+  t->buf = NULL;
+}
+
+/* One list-directed READ of ntok tokens: starts at the next record, may span
+ * records, and leaves the file at the record after the last one touched.
+ * Tokens are separated by blanks or commas.  Returns number of tokens read. */
+static int txt_read(txt *t, int ntok, char tok[][64]) {
+  int got = 0;
+  size_t p = t->pos;
+  if (p >= t->len) return 0;
+  while (got < ntok && p < t->len) {
+    /* scan this record */
+    while (p < t->len && t->buf[p] != '\n') {
+      while (p < t->len && (t->buf[p] == ' ' || t->buf[p] == '\t' ||
+                            t->buf[p] == ',' || t->buf[p] == '\r'))
+        p++;
+      if (p >= t->len || t->buf[p] == '\n') break;
+      size_t q = p;
+      while (q < t->len && !isspace((unsigned char)t->buf[q]) && t->buf[q] != ',')
+        q++;
+      if (got < ntok) {
+        size_t L = q - p < 63 ? q - p : 63;
+        memcpy(tok[got], t->buf + p, L);
+        tok[got][L] = 0;
+        got++;
+      }
+      p = q;
+      if (got == ntok) break;
+    }
+    /* advance to the next record */
+    while (p < t->len && t->buf[p] != '\n') p++;
+    if (p < t->len) p++;
+  }
+  t->pos = p;
+  return got;
+}
+
+/* skip one record (READ with empty list) */
+static int txt_skip(txt *t) {
+  if (t->pos >= t->len) return 0;
+  while (t->pos < t->len && t->buf[t->pos] != '\n') t->pos++;
+  if (t->pos < t->len) t->pos++;
+  return 1;
+}
+
+/* raw record (formatted A read) */
+static int txt_line(txt *t, char *out, int n) {
+  if (t->pos >= t->len) return 0;
+  size_t q = t->pos;
+  int k = 0;
+  while (q < t->len && t->buf[q] != '\n') {
+    if (k < n - 1) out[k++] = t->buf[q];
+    q++;
+  }
+  out[k] = 0;
+  t->pos = q < t->len ? q + 1 : q;
+  return 1;
+}
+
+static double tok_d(const char *s) {
+  char b[64];
+  int i;
+  for (i = 0; s[i] && i < 63; i++) b[i] = (s[i] == 'D' || s[i] == 'd') ? 'E' : s[i];
+  b[i] = 0;
+  return strtod(b, NULL);
+}
+
+static int read_ints(txt *t, int n, int *out) {
+  char tok[64][64];
+  if (n > 64 || txt_read(t, n, tok) != n) return E_IO;
+  for (int i = 0; i < n; i++) out[i] = atoi(tok[i]);
+  return OK;
+}
+static int read_dbls(txt *t, int n, double *out) {
+  static __thread char tok[128][64];
+  if (n > 128 || txt_read(t, n, tok) != n) return E_IO;
+  for (int i = 0; i < n; i++) out[i] = tok_d(tok[i]);
+  return OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* read_info (c.SYSTEM/M_species.f90:1057-1251) -- species block structure   */
+/* ------------------------------------------------------------------------ */
+static int read_info(or_fdata *fd, const char *dir, const int *nZreq) {
+  char path[1024], line[256];
+  txt t;
+  snprintf(path, sizeof path, "%s/info.dat", dir);
+  if (txt_open(&t, path)) return E_IO;
+  int nsf;
+  txt_line(&t, line, sizeof line); /* signature (2x, a70) */
+  if (read_ints(&t, 1, &nsf)) goto bad;
+  for (int k = 1; k <= fd->nspecies; k++) fd->sp[k].nZ = nZreq[k - 1], fd->sp[k].nssh = 0;
+  for (int iskip = 0; iskip < nsf; iskip++) {
+    int nZ, isp = 0;
+    txt_skip(&t);
+    txt_skip(&t);
+    txt_line(&t, line, sizeof line); /* symbol (2x, a2) */
+    if (read_ints(&t, 1, &nZ)) goto bad;
+    for (int k = 1; k <= fd->nspecies; k++)
+      if (fd->sp[k].nZ == nZ) { isp = k; break; }
+    if (!isp) {
+      for (int l = 0; l < 12; l++) txt_skip(&t);
+      continue;
+    }
+    species_t *s = &fd->sp[isp];
+    double xmass, qn[MAXSH], rc[MAXSH], rcpp, atomicE;
+    int nssh, lpp[MAXSH];
+    if (read_dbls(&t, 1, &xmass) || read_ints(&t, 1, &nssh) || nssh < 1 || nssh > MAXSH) goto bad;
+    s->nssh = nssh;
+    if (read_ints(&t, nssh, s->lssh) || read_dbls(&t, nssh, qn) || read_dbls(&t, nssh, rc)) goto bad;
+    if (read_ints(&t, 1, &s->nssh_PP) || s->nssh_PP < 0 || s->nssh_PP > MAXSH) goto bad;
+    if (s->nssh_PP > 0 && read_ints(&t, s->nssh_PP, lpp)) goto bad;
+    if (read_dbls(&t, 1, &rcpp)) goto bad;
+    txt_skip(&t); /* wffile names */
+    txt_skip(&t); /* na files */
+    if (read_dbls(&t, 1, &atomicE)) goto bad;
+    txt_skip(&t);
+    /* :1164-1193 cutoffs in Angstrom, norb_max = sum(2l+1) */
+    s->norb_max = 0;
+    s->rcutoffA_max = -99.0;
+    for (int i = 0; i < nssh; i++) {
+      s->rcutoffA[i] = rc[i] * P_abohr;
+      s->norb_max += 2 * s->lssh[i] + 1;
+      if (s->lssh[i] < 0 || s->lssh[i] > 2) { seterr("unsupported l=%d", s->lssh[i]); txt_close(&t); return E_UNSUP; }
+    }
+  }
+  txt_close(&t);
+  fd->have_dorbitals = 0; /* :1212-1221 */
+  for (int k = 1; k <= fd->nspecies; k++) {
+    if (fd->sp[k].nssh == 0) { seterr("species nZ=%d not in info.dat", fd->sp[k].nZ); return E_IO; }
+    for (int i = 0; i < fd->sp[k].nssh; i++) {
+      if (fd->sp[k].lssh[i] == 2) fd->have_dorbitals = 1;
+      if (fd->sp[k].rcutoffA[i] > fd->sp[k].rcutoffA_max) fd->sp[k].rcutoffA_max = fd->sp[k].rcutoffA[i];
+    }
+    if (fd->sp[k].norb_max > MAXORB) { seterr("norb %d > %d", fd->sp[k].norb_max, MAXORB); return E_UNSUP; }
+  }
+  return OK;
+bad:
+  seterr("parse error in %s", path);
+  txt_close(&t);
+  return E_IO;
+}
+
+/* munu file state: a unit re-opened on the same file keeps its position */
+typedef struct {
+  char name[1024];
+  txt t;
+  int open;
+} unit_t;
+
+static int unit_open(unit_t *u, const char *path) {
+  if (u->open && strcmp(u->name, path) == 0) return OK;
+  if (u->open) txt_close(&u->t);
+  u->open = 0;
+  if (txt_open(&u->t, path)) return E_IO;
+  snprintf(u->name, sizeof u->name, "%s", path);
+  u->open = 1;
+  return OK;
+}
+static void unit_close(unit_t *u) {
+  if (u->open) txt_close(&u->t);
+  u->open = 0;
+}
+
+/* read_Fdata_2c (e.FDATA/M_Fdata_2c.f90:149-272) */
+static int read_fdata_2c(or_fdata *fd, const char *dir) {
+  char path[1024], tok[8][64];
+  for (int is = 1; is <= fd->nspecies; is++) {
+    for (int js = 1; js <= fd->nspecies; js++) {
+      bundle2c *b = &fd->b2[is][js];
+      txt t;
+      snprintf(path, sizeof path, "%s/2c.%02d.%02d.dat", dir, fd->sp[is].nZ, fd->sp[js].nZ);
+      if (txt_open(&t, path)) return E_IO;
+      if (read_ints(&t, 1, &b->ncell) || b->ncell < 1) { txt_close(&t); seterr("bad %s", path); return E_IO; }
+      txt_close(&t);
+      b->cells = (cell2c *)calloc((size_t)b->ncell, sizeof(cell2c));
+      for (int a = 0; a <= P_MAXTYPE2; a++)
+        for (int c = 0; c <= P_MAXSUB2; c++) b->index[a][c] = -1;
+      snprintf(path, sizeof path, "%s/2c.%02d.%02d.dir", dir, fd->sp[is].nZ, fd->sp[js].nZ);
+      txt tdir;
+      if (txt_open(&tdir, path)) return E_IO;
+      unit_t u14 = {0};
+      for (int icell = 1; icell <= b->ncell; icell++) {
+        cell2c *c = &b->cells[icell - 1];
+        if (txt_read(&tdir, 7, tok) != 7) { seterr("short %s", path); txt_close(&tdir); return E_IO; }
+        int iindex = atoi(tok[0]), itype = atoi(tok[1]), isub = atoi(tok[2]);
+        c->nME = atoi(tok[4]);
+        c->nx = atoi(tok[5]);
+        c->xmax = tok_d(tok[6]);
+        if (itype < 1 || itype > P_MAXTYPE2 || isub < 0 || isub > P_MAXSUB2 || c->nME < 1 || c->nx < 7) {
+          seterr("bad dir entry in %s", path); txt_close(&tdir); return E_IO;
+        }
+        c->F = (double *)malloc(sizeof(double) * (size_t)c->nx * c->nME);
+        c->mu = (int *)malloc(sizeof(int) * c->nME);
+        c->nu = (int *)malloc(sizeof(int) * c->nME);
+        c->mvalue = (int *)malloc(sizeof(int) * c->nME);
+        b->index[itype][isub] = iindex;                 /* :221 */
+        c->dx = c->xmax / (c->nx - 1);                  /* :222 */
+        char dpath[1200];
+        snprintf(dpath, sizeof dpath, "%s/%s", dir, tok[3]);
+        txt td;
+        if (txt_open(&td, dpath)) { txt_close(&tdir); return E_IO; }
+        double row[128];
+        if (c->nME > 128) { seterr("nME too large"); return E_UNSUP; }
+        for (int ix = 1; ix <= c->nx; ix++) {         /* :230-232 */
+          if (read_dbls(&td, c->nME, row)) { seterr("short data %s", dpath); txt_close(&td); txt_close(&tdir); return E_IO; }
+          for (int m = 0; m < c->nME; m++) c->F[(ix - 1) + (size_t)c->nx * m] = row[m];
+        }
+        txt_close(&td);
+        snprintf(dpath, sizeof dpath, "%s/%02d_munu_2c.%02d.%02d.dat", dir, itype, fd->sp[is].nZ, fd->sp[js].nZ);
+        if (unit_open(&u14, dpath) || read_ints(&u14.t, c->nME, c->mu) ||
+            read_ints(&u14.t, c->nME, c->nu) || read_ints(&u14.t, c->nME, c->mvalue)) {
+          seterr("bad munu %s", dpath); unit_close(&u14); txt_close(&tdir); return E_IO;
+        }
+      }
+      txt_close(&tdir);
+      unit_close(&u14);
+    }
+    /* :252-258 Kleinman-Bylander coefficients, read unconditionally */
+    txt t;
+    snprintf(path, sizeof path, "%s/clPP.%02d.dat", dir, fd->sp[is].nZ);
+    if (txt_open(&t, path)) return E_IO;
+    for (int k = 0; k < fd->sp[is].nssh_PP; k++) {
+      double cl;
+      if (read_dbls(&t, 1, &cl)) { txt_close(&t); seterr("short %s", path); return E_IO; }
+    }
+    txt_close(&t);
+  }
+  return OK;
+}
+
+/* read_Fdata_3c (e.FDATA/M_Fdata_3c.f90:143-264) */
+static int read_fdata_3c(or_fdata *fd, const char *dir) {
+  char path[1024], tok[12][64];
+  for (int is = 1; is <= fd->nspecies; is++)
+    for (int js = 1; js <= fd->nspecies; js++)
+      for (int ks = 1; ks <= fd->nspecies; ks++) {
+        bundle3c *b = &fd->b3[is][js][ks];
+        txt t;
+        snprintf(path, sizeof path, "%s/3c.%02d.%02d.%02d.dat", dir, fd->sp[is].nZ, fd->sp[js].nZ, fd->sp[ks].nZ);
+        if (txt_open(&t, path)) return E_IO;
+        if (read_ints(&t, 1, &b->ncell) || b->ncell < 1) { txt_close(&t); seterr("bad %s", path); return E_IO; }
+        txt_close(&t);
+        b->cells = (cell3c *)calloc((size_t)b->ncell, sizeof(cell3c));
+        for (int a = 0; a <= P_MAXTYPE3; a++)
+          for (int c = 0; c <= P_MAXSUB3; c++)
+            for (int d = 0; d <= P_MAXTHETA; d++) b->index[a][c][d] = -1;
+        snprintf(path, sizeof path, "%s/3c.%02d.%02d.%02d.dir", dir, fd->sp[is].nZ, fd->sp[js].nZ, fd->sp[ks].nZ);
+        txt tdir;
+        if (txt_open(&tdir, path)) return E_IO;
+        unit_t u13 = {0};
+        for (int icell = 1; icell <= b->ncell; icell++) {
+          cell3c *c = &b->cells[icell - 1];
+          if (txt_read(&tdir, 10, tok) != 10) { seterr("short %s", path); txt_close(&tdir); return E_IO; }
+          int iindex = atoi(tok[0]), itype = atoi(tok[1]), isub = atoi(tok[2]), ith = atoi(tok[3]);
+          c->nME = atoi(tok[5]);
+          c->nx = atoi(tok[6]);
+          c->xmax = tok_d(tok[7]);
+          c->ny = atoi(tok[8]);
+          c->ymax = tok_d(tok[9]);
+          if (itype < 1 || itype > P_MAXTYPE3 || isub < 0 || isub > P_MAXSUB3 || ith < 1 ||
+              ith > P_MAXTHETA || c->nME < 1 || c->nME > 128 || c->nx < 4 || c->ny < 4) {
+            seterr("bad dir entry in %s", path); txt_close(&tdir); return E_IO;
+          }
+          size_t n = (size_t)c->nx * c->ny * c->nME;
+          c->F = (double *)malloc(sizeof(double) * n);
+          c->mu = (int *)malloc(sizeof(int) * c->nME);
+          c->nu = (int *)malloc(sizeof(int) * c->nME);
+          c->mvalue = (int *)malloc(sizeof(int) * c->nME);
+          b->index[itype][isub][ith] = iindex;          /* :221 */
+          char dpath[1200];
+          snprintf(dpath, sizeof dpath, "%s/%s", dir, tok[4]);
+          txt td;
+          if (txt_open(&td, dpath)) { txt_close(&tdir); return E_IO; }
+          double row[128];
+          for (int iy = 1; iy <= c->ny; iy++)           /* :227-231 */
+            for (int ix = 1; ix <= c->nx; ix++) {
+              if (read_dbls(&td, c->nME, row)) { seterr("short data %s", dpath); txt_close(&td); txt_close(&tdir); return E_IO; }
+              for (int m = 0; m < c->nME; m++)
+                c->F[(ix - 1) + (size_t)c->nx * ((iy - 1) + (size_t)c->ny * m)] = row[m];
+            }
+          txt_close(&td);
+          snprintf(dpath, sizeof dpath, "%s/%02d_munu_3c.%02d.%02d.%02d.dat", dir, itype, fd->sp[is].nZ,
+                   fd->sp[js].nZ, fd->sp[ks].nZ);
+          if (unit_open(&u13, dpath) || read_ints(&u13.t, c->nME, c->mu) ||
+              read_ints(&u13.t, c->nME, c->nu) || read_ints(&u13.t, c->nME, c->mvalue)) {
+            seterr("bad munu %s", dpath); unit_close(&u13); txt_close(&tdir); return E_IO;
+          }
+        }
+        txt_close(&tdir);
+        unit_close(&u13);
+      }
+  return OK;
+}
+
+or_fdata *or_load_fdata(const char *dir, int nspecies, const int *nZ, char *err, int errlen) {
+  if (nspecies < 1 || nspecies > MAXSP) {
+    if (err) snprintf(err, (size_t)errlen, "nspecies out of range");
+    return NULL;
+  }
+  or_fdata *fd = (or_fdata *)calloc(1, sizeof(or_fdata));
+  fd->nspecies = nspecies;
+  int st = read_info(fd, dir, nZ);
+  if (!st) st = read_fdata_2c(fd, dir);
+  if (!st) st = read_fdata_3c(fd, dir);
+  if (st) {
+    if (err) snprintf(err, (size_t)errlen, "%s", g_err);
+    or_free_fdata(fd);
+    return NULL;
+  }
+  return fd;
+}
+
+void or_free_fdata(or_fdata *fd) {
+  if (!fd) return;
+  for (int a = 1; a <= fd->nspecies; a++)
+    for (int b = 1; b <= fd->nspecies; b++) {
+      bundle2c *B = &fd->b2[a][b];
+      for (int k = 0; B->cells && k < B->ncell; k++) {
+        free(B->cells[k].F); free(B->cells[k].mu); free(B->cells[k].nu); free(B->cells[k].mvalue);
+      }
+      free(B->cells);
+      for (int c = 1; c <= fd->nspecies; c++) {
+        bundle3c *C = &fd->b3[a][b][c];
+        for (int k = 0; C->cells && k < C->ncell; k++) {
+          free(C->cells[k].F); free(C->cells[k].mu); free(C->cells[k].nu); free(C->cells[k].mvalue);
+        }
+        free(C->cells);
+      }
+    }
+  free(fd);
+}
+
+int or_species_norb(const or_fdata *fd, int isp) { return fd->sp[isp].norb_max; }
+
+/* ------------------------------------------------------------------------ */
+/* interpolators                                                             */
+/* ------------------------------------------------------------------------ */
+static cell2c *get_cell2c(or_fdata *fd, int isp, int jsp, int iint, int isub) {
+  bundle2c *b = &fd->b2[isp][jsp];
+  if (iint < 1 || iint > P_MAXTYPE2 || isub < 0 || isub > P_MAXSUB2) return NULL;
+  int k = b->index[iint][isub];
+  if (k < 1 || k > b->ncell) return NULL;
+  return &b->cells[k - 1];
+}
+
+/* getMEs_Fdata_2c (e.FDATA/M_Fdata_2c.f90:302-415) */
+int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x, int norb_mu, int norb_nu,
+                 double *hmbox) {
+  const double P_tolerance = 1.0e-5;
+  cell2c *c = get_cell2c(fd, isp, jsp, iint, isub);
+  if (!c) { seterr("missing 2c cell (%d,%d) for species %d,%d", iint, isub, isp, jsp); return E_TABLE; }
+  double Fdata[128], xx[7], pdenom[7];
+  if (x < 0.0) { seterr("negative x"); return E_XNEG; }            /* :347-348 */
+  if (x > c->xmax * (1.0 + P_tolerance)) {                          /* :349-353 */
+    seterr("x too large: x=%.17g xmax=%.17g", x, c->xmax);
+    return E_XLARGE;
+  }
+  /* :354-362 the x < tolerance branch fills hmbox but falls through, so the
+   * interpolation below overwrites it; nothing to do here */
+  int imid = (int)(x / c->dx) + 1;                                  /* :366-375 */
+  int ileft = imid - 3, iright = imid + 3;
+  if (ileft < 1) { ileft = 1; iright = 7; }
+  else if (iright > c->nx) { ileft = c->nx - 6; iright = c->nx; }
+  for (int ip = ileft; ip <= iright; ip++) xx[ip - ileft] = (double)(ip - 1) * c->dx;
+  for (int m = 0; m < c->nME; m++) Fdata[m] = 0.0;
+  for (int isum = ileft; isum <= iright; isum++) {                  /* :382-393 */
+    double prod = 1.0;
+    pdenom[isum - ileft] = 1.0;
+    for (int iprod = ileft; iprod <= iright; iprod++) {
+      if (iprod != isum) {
+        double pden = 1.0 / (xx[isum - ileft] - xx[iprod - ileft]);
+        pdenom[isum - ileft] = pdenom[isum - ileft] * pden;
+        prod = prod * (x - xx[iprod - ileft]) * pden;
+      }
+    }
+    for (int m = 0; m < c->nME; m++) Fdata[m] = Fdata[m] + c->F[(isum - 1) + (size_t)c->nx * m] * prod;
+  }
+  for (int k = 0; k < norb_mu * norb_nu; k++) hmbox[k] = 0.0;       /* :396-401 */
+  for (int m = 0; m < c->nME; m++) {
+    int imu = c->mu[m], inu = c->nu[m];
+    if (imu < 1 || imu > norb_mu || inu < 1 || inu > norb_nu) { seterr("munu out of block"); return E_TABLE; }
+    hmbox[(imu - 1) + norb_mu * (inu - 1)] = Fdata[m];
+  }
+  return OK;
+}
+
+/* getDMEs_Fdata_2c (e.FDATA/M_Fdata_2c.f90:446-600) */
+int or_getDMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x, int norb_mu, int norb_nu,
+                  double *hmbox, double *dhmbox) {
+  const double P_tolerance = 1.0e-5;
+  cell2c *c = get_cell2c(fd, isp, jsp, iint, isub);
+  if (!c) { seterr("missing 2c cell (%d,%d)", iint, isub); return E_TABLE; }
+  double Fdata[128], dF[128], xx[7] = {0}, pdenom[7] = {0};
+  for (int m = 0; m < c->nME; m++) Fdata[m] = dF[m] = 0.0;
+  if (x < 0.0) { seterr("negative x"); return E_XNEG; }
+  if (x > c->xmax * (1.0 + P_tolerance)) {
+    seterr("x too large: x=%.17g xmax=%.17g", x, c->xmax);
+    return E_XLARGE;
+  }
+  if (x < P_tolerance) {                                            /* :510-520 early return */
+    for (int k = 0; k < norb_mu * norb_nu; k++) hmbox[k] = 0.0;
+    for (int m = 0; m < c->nME; m++) {
+      int imu = c->mu[m], inu = c->nu[m];
+      hmbox[(imu - 1) + norb_mu * (inu - 1)] = c->F[0 + (size_t)c->nx * m];
+      dhmbox[(imu - 1) + norb_mu * (inu - 1)] = 0.0;
+    }
+    return OK;
+  }
+  int imid = (int)(x / c->dx) + 1;
+  int ileft = imid - 3, iright = imid + 3;
+  if (ileft < 1) { ileft = 1; iright = 7; }
+  else if (iright > c->nx) { ileft = c->nx - 6; iright = c->nx; }
+  for (int ip = ileft; ip <= iright; ip++) xx[ip - ileft] = (double)(ip - 1) * c->dx;
+  for (int isum = ileft; isum <= iright; isum++) {
+    double prod = 1.0;
+    pdenom[isum - ileft] = 1.0;
+    for (int iprod = ileft; iprod <= iright; iprod++) {
+      if (iprod != isum) {
+        double pden = 1.0 / (xx[isum - ileft] - xx[iprod - ileft]);
+        pdenom[isum - ileft] = pdenom[isum - ileft] * pden;
+        prod = prod * (x - xx[iprod - ileft]) * pden;
+      }
+    }
+    for (int m = 0; m < c->nME; m++) Fdata[m] = Fdata[m] + c->F[(isum - 1) + (size_t)c->nx * m] * prod;
+  }
+  for (int k = 0; k < norb_mu * norb_nu; k++) hmbox[k] = 0.0;
+  for (int m = 0; m < c->nME; m++) hmbox[(c->mu[m] - 1) + norb_mu * (c->nu[m] - 1)] = Fdata[m];
+  for (int m = 0; m < c->nME; m++) dF[m] = 0.0;                     /* :561-577 */
+  for (int ip = ileft; ip <= iright; ip++) {
+    double xsumoverj = 0.0;
+    for (int jp = ileft; jp <= iright; jp++) {
+      if (ip == jp) continue;
+      double xprod = 1.0;
+      for (int kp = ileft; kp <= iright; kp++) {
+        if (kp == jp) continue;
+        if (kp == ip) continue;
+        xprod = xprod * (x - xx[kp - ileft]);
+      }
+      xsumoverj = xsumoverj + xprod;
+    }
+    for (int m = 0; m < c->nME; m++)
+      dF[m] = dF[m] + c->F[(ip - 1) + (size_t)c->nx * m] * pdenom[ip - ileft] * xsumoverj;
+  }
+  for (int k = 0; k < norb_mu * norb_nu; k++) dhmbox[k] = 0.0;      /* :580-585 */
+  for (int m = 0; m < c->nME; m++) dhmbox[(c->mu[m] - 1) + norb_mu * (c->nu[m] - 1)] = dF[m];
+  return OK;
+}
+
+static cell3c *get_cell3c(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub, int ith) {
+  bundle3c *b = &fd->b3[isp][jsp][ksp];
+  if (iint < 1 || iint > P_MAXTYPE3 || isub < 0 || isub > P_MAXSUB3) return NULL;
+  int k = b->index[iint][isub][ith];
+  if (k < 1 || k > b->ncell) return NULL;
+  return &b->cells[k - 1];
+}
+
+#define F3(c, ix, iy, m) ((c)->F[((ix)-1) + (size_t)(c)->nx * (((iy)-1) + (size_t)(c)->ny * (m))])
+
+/* getMEs_Fdata_3c (e.FDATA/M_Fdata_3c.f90:293-517) and getDMEs_Fdata_3c
+ * (:549-846) share one body; deriv selects the derivative outputs. */
+static int getMEs_3c_body(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub, double x, double y,
+                          int norb_mu, int norb_nu, double cost, double *hmbox, double *dph, double *dxh,
+                          double *dyh, int deriv) {
+  const double P_tiny = 1.0e-6;
+  const double P_small = 1.0 - 4; /* :317 "1.0d0-4" evaluates to -3 */
+  double p[5], Dp[5];
+  double cost2 = cost * cost;                                       /* :348-354 */
+  double sint = sqrt(fmax(1.0e-5, 1.0 - cost2));
+  p[0] = 1.0;
+  p[1] = cost;
+  p[2] = 0.5 * (3.0 * cost2 - 1.0);
+  p[3] = 0.5 * cost * (5.0 * cost2 - 3.0);
+  p[4] = 0.125 * (3.0 - cost2 * (30.0 - 35.0 * cost2));
+  Dp[0] = 0.0;                                                      /* :625-629 */
+  Dp[1] = 1.0;
+  Dp[2] = 3.0 * cost;
+  Dp[3] = (15.0 * cost2 - 3.0) / 2.0;
+  Dp[4] = 0.5 * cost * (35.0 * cost2 - 15.0);
+  cell3c *c = get_cell3c(fd, isp, jsp, ksp, iint, isub, 1);
+  if (!c) { seterr("missing 3c cell"); return E_TABLE; }
+  int nME = c->nME;
+  double Fd[128], DpF[128], DxF[128], DyF[128], interim[128];
+  for (int m = 0; m < nME; m++) Fd[m] = DpF[m] = DxF[m] = DyF[m] = 0.0;
+  double dx = c->xmax / (c->nx - 1.0);                              /* :367-379 */
+  double dy = c->ymax / (c->ny - 1.0);
+  int ix = (int)(x / dx) + 1;
+  int iy = (int)(y / dy) + 1;
+  if (ix < 2) ix = 2;
+  if (iy < 2) iy = 2;
+  if (ix > c->nx - 2) ix = c->nx - 2;
+  if (iy > c->ny - 2) iy = c->ny - 2;
+  double px = x / dx - ix + 1.0;
+  double py = y / dy - iy + 1.0;
+  double gx = (F3(c, ix + 1, iy, 0) - F3(c, ix, iy, 0)) / dx;      /* :383-385 */
+  double gy = (F3(c, ix, iy + 1, 0) - F3(c, ix, iy, 0)) / dy;
+  double gg = gx * gx + gy * gy;
+  for (int it = 1; it <= P_MAXTHETA; it++) {
+    c = get_cell3c(fd, isp, jsp, ksp, iint, isub, it);
+    if (!c || c->nME != nME) { seterr("missing 3c theta cell %d", it); return E_TABLE; }
+    double pt = p[it - 1], Dpt = Dp[it - 1];
+    if (gg < P_tiny) {                                              /* :406-410, :684-691 */
+      for (int m = 0; m < nME; m++) {
+        interim[m] = ((1.0 - px - py) * F3(c, ix, iy, m) + px * F3(c, ix + 1, iy, m) + py * F3(c, ix, iy + 1, m));
+        Fd[m] = Fd[m] + pt * interim[m];
+        if (deriv) {
+          DpF[m] = DpF[m] + Dpt * interim[m];
+          DxF[m] = DxF[m] + pt * gx;
+          DyF[m] = DyF[m] + pt * gy;
+        }
+      }
+    } else if (gg <= P_small) {                                     /* :415-422 dead: P_small = -3 */
+      for (int m = 0; m < nME; m++) {
+        interim[m] = (py * (py - 1) * 0.5 * F3(c, ix, iy - 1, m) + px * (px - 1) * 0.5 * F3(c, ix - 1, iy, m) +
+                      (1.0 + px * py - px * px - py * py) * F3(c, ix, iy, m) +
+                      px * (px - 2.0 * py + 1.0) * 0.5 * F3(c, ix + 1, iy, m) +
+                      py * (py - 2.0 * px + 1.0) * 0.5 * F3(c, ix, iy + 1, m) + px * py * F3(c, ix + 1, iy + 1, m));
+        Fd[m] = Fd[m] + pt * interim[m];
+        if (deriv) {
+          DpF[m] = DpF[m] + Dpt * interim[m];
+          DxF[m] = DxF[m] + pt * (((F3(c, ix + 1, iy + 1, m) - F3(c, ix + 1, iy, m) - F3(c, ix, iy + 1, m) +
+                                    F3(c, ix, iy, m)) * py +
+                                   (F3(c, ix - 1, iy, m) + F3(c, ix + 1, iy, m) - 2.0 * F3(c, ix, iy, m)) * px -
+                                   0.5 * (F3(c, ix - 1, iy, m) - F3(c, ix + 1, iy, m))) / dx);
+          DyF[m] = DyF[m] + pt * (((F3(c, ix + 1, iy + 1, m) - F3(c, ix + 1, iy, m) - F3(c, ix, iy + 1, m) +
+                                    F3(c, ix, iy, m)) * px +
+                                   (F3(c, ix, iy - 1, m) + F3(c, ix, iy + 1, m) - 2.0 * F3(c, ix, iy, m)) * py -
+                                   0.5 * (F3(c, ix, iy - 1, m) - F3(c, ix, iy + 1, m))) / dy);
+        }
+      }
+    } else {                                                        /* :425-481, :721-798 */
+      for (int m = 0; m < nME; m++) {
+        double g[4], gp[4], f1m1, f1m2, f1m3, f0p3, f0p6, f1p3, f1p6, f2p1, bb0, bb1, bb2, bb3;
+        for (int k = -1; k <= 2; k++) {
+          f1m1 = F3(c, ix + k, iy - 1, m);
+          f1m2 = 2.0 * f1m1;
+          f1m3 = 3.0 * f1m1;
+          f0p3 = 3.0 * F3(c, ix + k, iy, m);
+          f0p6 = 2.0 * f0p3;
+          f1p3 = 3.0 * F3(c, ix + k, iy + 1, m);
+          f1p6 = 2.0 * f1p3;
+          f2p1 = F3(c, ix + k, iy + 2, m);
+          bb3 = -f1m1 + f0p3 - f1p3 + f2p1;
+          bb2 = f1m3 - f0p6 + f1p3;
+          bb1 = -f1m2 - f0p3 + f1p6 - f2p1;
+          bb0 = f0p6;
+          g[k + 1] = ((bb3 * py + bb2) * py + bb1) * py + bb0;
+          gp[k + 1] = ((3 * bb3 * py + 2 * bb2) * py + bb1);
+        }
+        f1m1 = g[0];
+        f1m2 = 2.0 * f1m1;
+        f1m3 = 3.0 * f1m1;
+        f0p3 = 3.0 * g[1];
+        f0p6 = 2.0 * f0p3;
+        f1p3 = 3.0 * g[2];
+        f1p6 = 2.0 * f1p3;
+        f2p1 = g[3];
+        bb3 = -f1m1 + f0p3 - f1p3 + f2p1;
+        bb2 = f1m3 - f0p6 + f1p3;
+        bb1 = -f1m2 - f0p3 + f1p6 - f2p1;
+        bb0 = f0p6;
+        interim[m] = (((bb3 * px + bb2) * px + bb1) * px + bb0) / 36.0;
+        Fd[m] = Fd[m] + pt * interim[m];
+        if (deriv) {
+          DpF[m] = DpF[m] + Dpt * interim[m];
+          DxF[m] = DxF[m] + pt * ((3 * bb3 * px + 2 * bb2) * px + bb1) / (36.0 * dx);
+          f1m1 = gp[0];
+          f1m2 = 2 * f1m1;
+          f1m3 = 3 * f1m1;
+          f0p3 = 3 * gp[1];
+          f0p6 = 2 * f0p3;
+          f1p3 = 3 * gp[2];
+          f1p6 = 2 * f1p3;
+          f2p1 = gp[3];
+          bb3 = -f1m1 + f0p3 - f1p3 + f2p1;
+          bb2 = f1m3 - f0p6 + f1p3;
+          bb1 = -f1m2 - f0p3 + f1p6 - f2p1;
+          bb0 = f0p6;
+          DyF[m] = DyF[m] + pt * (((bb3 * px + bb2) * px + bb1) * px + bb0) / (36.0 * dy);
+        }
+      }
+    }
+  }
+  /* recover matrices (:497-507, :814-833); nME and the maps are taken from
+   * the last theta cell */
+  int nb = norb_mu * norb_nu;
+  for (int k = 0; k < nb; k++) {
+    hmbox[k] = 0.0;
+    if (deriv) dph[k] = dxh[k] = dyh[k] = 0.0;
+  }
+  for (int m = 0; m < c->nME; m++) {
+    int imu = c->mu[m], inu = c->nu[m];
+    if (imu < 1 || imu > norb_mu || inu < 1 || inu > norb_nu) { seterr("munu out of block"); return E_TABLE; }
+    int k = (imu - 1) + norb_mu * (inu - 1);
+    if (c->mvalue[m] != 1) {
+      hmbox[k] = Fd[m];
+      if (deriv) { dph[k] = DpF[m]; dxh[k] = DxF[m]; dyh[k] = DyF[m]; }
+    } else {
+      hmbox[k] = Fd[m] * sint;
+      if (deriv) {
+        dph[k] = DpF[m] * sint - cost * Fd[m] / sint;
+        dxh[k] = DxF[m] * sint;
+        dyh[k] = DyF[m] * sint;
+      }
+    }
+  }
+  return OK;
+}
+
+int or_getMEs_3c(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub, double x, double y, int norb_mu,
+                 int norb_nu, double cost, double *hmbox) {
+  return getMEs_3c_body(fd, isp, jsp, ksp, iint, isub, x, y, norb_mu, norb_nu, cost, hmbox, NULL, NULL, NULL, 0);
+}
+int or_getDMEs_3c(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub, double x, double y, int norb_mu,
+                  int norb_nu, double cost, double *hmbox, double *dph, double *dxh, double *dyh) {
+  return getMEs_3c_body(fd, isp, jsp, ksp, iint, isub, x, y, norb_mu, norb_nu, cost, hmbox, dph, dxh, dyh, 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* vector helpers: distance (b.FUNCTIONS/distance.f90:51-80), magnitude      */
+/* (magnitude.f90:50-77), a_cross_b (a_cross_b.f90:49-79)                     */
+/* ------------------------------------------------------------------------ */
+static double distance3(const double *a, const double *b) {
+  return sqrt((b[0] - a[0]) * (b[0] - a[0]) + (b[1] - a[1]) * (b[1] - a[1]) + (b[2] - a[2]) * (b[2] - a[2]));
+}
+static double magnitude3(const double *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+static void cross3(const double *a, const double *b, double *c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* eps and deps storage: eps[i + 3*j] = spe(i+1, j+1);                       */
+/* deps[ix + 3*(imu + 3*k)] = deps(ix+1, imu+1, k+1)                          */
+#define E2(a, i, j) (a)[(i) + 3 * (j)]
+#define E3(a, i, j, k) (a)[(i) + 3 * ((j) + 3 * (k))]
+
+/* epsilon_function (b.FUNCTIONS/epsilon.f90:73-202); the WARNINGS-file side
+ * effects are not reproduced */
+void or_epsilon(const double *r1, const double *r2, double *spe) {
+  double r1_mag = magnitude3(r1), r2_mag = magnitude3(r2);
+  double r1_hat[3], xp[3], yp[3] = {0, 0, 0}, zp[3], yp_mag;
+  if (r2_mag < 1.0e-4) {                                            /* :123-133 */
+    for (int k = 0; k < 9; k++) spe[k] = 0.0;
+    for (int k = 0; k < 3; k++) E2(spe, k, k) = 1.0;
+    return;
+  }
+  for (int k = 0; k < 3; k++) zp[k] = r2[k] / r2_mag;
+  yp_mag = 0;
+  if (r1_mag > 1.0e-4) {                                            /* :139-145 */
+    for (int k = 0; k < 3; k++) r1_hat[k] = r1[k] / r1_mag;
+    cross3(zp, r1_hat, yp);
+    yp_mag = magnitude3(yp);
+  }
+  if (yp_mag < 1.0e-4) {                                            /* :148-168 */
+    if (fabs(zp[0]) > 1.0e-4) {
+      yp[0] = -(zp[1] + zp[2]) / zp[0];
+      yp[1] = 1.0;
+      yp[2] = 1.0;
+    } else if (fabs(zp[1]) > 1.0e-4) {
+      yp[0] = 1.0;
+      yp[1] = -(zp[0] + zp[2]) / zp[1];
+      yp[2] = 1.0;
+    } else {
+      yp[0] = 1.0;
+      yp[1] = 1.0;
+      yp[2] = -(zp[0] + zp[1]) / zp[2];
+    }
+    yp_mag = magnitude3(yp);
+  }
+  for (int k = 0; k < 3; k++) yp[k] = yp[k] / yp_mag;
+  cross3(yp, zp, xp);
+  for (int k = 0; k < 3; k++) {
+    E2(spe, k, 0) = xp[k];
+    E2(spe, k, 1) = yp[k];
+    E2(spe, k, 2) = zp[k];
+  }
+}
+
+/* constants.h:18-21 (delk), :24-28 (xlevi) */
+static double delk(int i, int j) { return i == j ? 1.0 : 0.0; }
+static double xlevi(int i, int j, int k) {
+  if (i == j || j == k || i == k) return 0.0;
+  if ((i == 0 && j == 1 && k == 2) || (i == 1 && j == 2 && k == 0) || (i == 2 && j == 0 && k == 1)) return 1.0;
+  return -1.0;
+}
+
+/* Depsilon_2c (b.FUNCTIONS/Depsilon_2c.f90:46-140) */
+void or_depsilon_2c(const double *r1, const double *r2, double z, const double *eps, double *deps) {
+  for (int k = 0; k < 27; k++) deps[k] = 0.0;
+  if (z < 1.0e-5) return;
+  double crossa[3];
+  crossa[0] = r2[1] * r1[2] - r2[2] * r1[1];
+  crossa[1] = r2[2] * r1[0] - r2[0] * r1[2];
+  crossa[2] = r2[0] * r1[1] - r2[1] * r1[0];
+  double crossmag = sqrt(crossa[0] * crossa[0] + crossa[1] * crossa[1] + crossa[2] * crossa[2]);
+  if (fabs(crossmag) < 1.0e-3) return;
+  double r2mag2 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+  double r1dotr2 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+  for (int ix = 0; ix < 3; ix++)
+    for (int imu = 0; imu < 3; imu++) {
+      double sum = xlevi(ix, imu, 0) * r2[0] + xlevi(ix, imu, 1) * r2[1] + xlevi(ix, imu, 2) * r2[2];
+      E3(deps, ix, imu, 0) = (E2(eps, imu, 0) * E2(eps, ix, 2) * (1.0 / z)) -
+                             (E2(eps, imu, 0) * (1.0 / crossmag) * (1.0 / crossmag)) *
+                                 (r2mag2 * r1[ix] - r1dotr2 * r2[ix]) +
+                             (1.0 / z) * (1.0 / crossmag) *
+                                 (delk(imu, ix) * (r2mag2 - r1dotr2) - r1[imu] * r2[ix] - r2[imu] * r2[ix] +
+                                  2.0 * r1[ix] * r2[imu]);
+      E3(deps, ix, imu, 1) =
+          (1.0 / crossmag) * (sum + (E2(eps, imu, 1) * (1.0 / crossmag)) * (r1dotr2 * r2[ix] - r2mag2 * r1[ix]));
+      E3(deps, ix, imu, 2) = -(delk(imu, ix) - E2(eps, imu, 2) * E2(eps, ix, 2)) * (1.0 / z);
+    }
+}
+
+/* Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189) */
+void or_depsilon_3c(const double *r1, const double *r2, const double *r21, double z, const double *ratm,
+                    const double *rnabc, const double *eps3, double *dera3, double *der13) {
+  for (int k = 0; k < 27; k++) dera3[k] = der13[k] = 0.0;
+  double crossa[3];
+  crossa[0] = r21[1] * rnabc[2] - r21[2] * rnabc[1];
+  crossa[1] = r21[2] * rnabc[0] - r21[0] * rnabc[2];
+  crossa[2] = r21[0] * rnabc[1] - r21[1] * rnabc[0];
+  double crossmag = sqrt(crossa[0] * crossa[0] + crossa[1] * crossa[1] + crossa[2] * crossa[2]);
+  if (fabs(crossmag) < 1.0e-3) return;
+  double r2mag2 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+  double r1mag2 = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+  double ratmmag2 = ratm[0] * ratm[0] + ratm[1] * ratm[1] + ratm[2] * ratm[2];
+  double r1dotr2 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+  double r2dotratm = r2[0] * ratm[0] + r2[1] * ratm[1] + r2[2] * ratm[2];
+  double r1dotratm = r1[0] * ratm[0] + r1[1] * ratm[1] + r1[2] * ratm[2];
+  for (int ix = 0; ix < 3; ix++)
+    for (int imu = 0; imu < 3; imu++) {
+      E3(dera3, ix, imu, 2) = 0.0;
+      double sum = xlevi(ix, imu, 0) * (r2[0] - r1[0]) + xlevi(ix, imu, 1) * (r2[1] - r1[1]) +
+                   xlevi(ix, imu, 2) * (r2[2] - r1[2]);
+      E3(dera3, ix, imu, 1) =
+          (1.0 / crossmag) *
+          (sum - (E2(eps3, imu, 1) / crossmag) * ((r1mag2 + r2mag2 - 2.0 * r1dotr2) * ratm[ix] +
+                                                  (r1dotr2 - r1mag2 - r2dotratm + r1dotratm) * r2[ix] +
+                                                  (r1dotr2 - r2mag2 + r2dotratm - r1dotratm) * r1[ix]));
+    }
+  for (int a = 0; a < 3; a++) {
+    E3(dera3, a, 0, 0) = E2(eps3, 2, 2) * E3(dera3, a, 1, 1) - E2(eps3, 1, 2) * E3(dera3, a, 2, 1);
+    E3(dera3, a, 1, 0) = E2(eps3, 0, 2) * E3(dera3, a, 2, 1) - E2(eps3, 2, 2) * E3(dera3, a, 0, 1);
+    E3(dera3, a, 2, 0) = E2(eps3, 1, 2) * E3(dera3, a, 0, 1) - E2(eps3, 0, 2) * E3(dera3, a, 1, 1);
+  }
+  for (int ix = 0; ix < 3; ix++)
+    for (int imu = 0; imu < 3; imu++) {
+      E3(der13, ix, imu, 2) = (1.0 / z) * (E2(eps3, imu, 2) * E2(eps3, ix, 2) - delk(imu, ix));
+      double sum = xlevi(ix, imu, 0) * (ratm[0] - r2[0]) + xlevi(ix, imu, 1) * (ratm[1] - r2[1]) +
+                   xlevi(ix, imu, 2) * (ratm[2] - r2[2]);
+      E3(der13, ix, imu, 1) =
+          (1.0 / crossmag) *
+          (sum - (E2(eps3, imu, 1) / crossmag) * ((r2dotratm - r1dotratm + r1dotr2 - r2mag2) * ratm[ix] +
+                                                  (r2dotratm + r1dotratm - r1dotr2 - ratmmag2) * r2[ix] +
+                                                  (ratmmag2 - 2.0 * r2dotratm + r2mag2) * r1[ix]));
+    }
+  for (int a = 0; a < 3; a++) {
+    E3(der13, a, 0, 0) = E2(eps3, 2, 2) * E3(der13, a, 1, 1) - E2(eps3, 2, 1) * E3(der13, a, 1, 2) -
+                         E2(eps3, 1, 2) * E3(der13, a, 2, 1) + E2(eps3, 1, 1) * E3(der13, a, 2, 2);
+    E3(der13, a, 1, 0) = E2(eps3, 0, 2) * E3(der13, a, 2, 1) - E2(eps3, 0, 1) * E3(der13, a, 2, 2) -
+                         E2(eps3, 2, 2) * E3(der13, a, 0, 1) + E2(eps3, 2, 1) * E3(der13, a, 0, 2);
+    E3(der13, a, 2, 0) = E2(eps3, 1, 2) * E3(der13, a, 0, 1) - E2(eps3, 1, 1) * E3(der13, a, 0, 2) -
+                         E2(eps3, 0, 2) * E3(der13, a, 1, 1) + E2(eps3, 0, 1) * E3(der13, a, 1, 2);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* rotations: twister/chooser (c.SYSTEM/M_rotations.f90:221-382), rotate     */
+/* (:98-177), Dtwister/Dchooser/Dmatrix/Drotate (M_Drotations.f90:102-482)   */
+/* ------------------------------------------------------------------------ */
+/* amat(3,3,5) of include/constants.h:30-38, stored amat[imu][ix][jx] */
+static double amat(int ix, int jx, int imu) {
+  static const double v = 0.28867513459481287; /* 1/(2*sqrt(3)) */
+  switch (imu) {
+  case 0: return ((ix == 0 && jx == 1) || (ix == 1 && jx == 0)) ? 0.5 : 0.0;
+  case 1: return ((ix == 1 && jx == 2) || (ix == 2 && jx == 1)) ? 0.5 : 0.0;
+  case 2: return (ix == jx) ? (ix == 2 ? 2.0 * v : -v) : 0.0;
+  case 3: return ((ix == 0 && jx == 2) || (ix == 2 && jx == 0)) ? 0.5 : 0.0;
+  case 4: return (ix == jx && ix < 2) ? (ix == 0 ? 0.5 : -0.5) : 0.0;
+  }
+  return 0.0;
+}
+
+/* dmat[a + 5*b] = dmat(a+1, b+1); pmat[a + 3*b] = pmat(a+1,b+1) */
+static void twister(const double *eps, int have_d, double *dmat, double *pmat) {
+  pmat[0 + 3 * 0] = E2(eps, 1, 1);
+  pmat[0 + 3 * 1] = E2(eps, 1, 2);
+  pmat[0 + 3 * 2] = E2(eps, 1, 0);
+  pmat[1 + 3 * 0] = E2(eps, 2, 1);
+  pmat[1 + 3 * 1] = E2(eps, 2, 2);
+  pmat[1 + 3 * 2] = E2(eps, 2, 0);
+  pmat[2 + 3 * 0] = E2(eps, 0, 1);
+  pmat[2 + 3 * 1] = E2(eps, 0, 2);
+  pmat[2 + 3 * 2] = E2(eps, 0, 0);
+  if (!have_d) return;
+  for (int imu = 0; imu < 5; imu++) {
+    double l11 = 0, l12 = 0, l13 = 0, l32 = 0, l33 = 0;
+    for (int jx = 0; jx < 3; jx++)
+      for (int ix = 0; ix < 3; ix++) {
+        double a = amat(ix, jx, imu);
+        if (a != 0.0) {
+          l11 = l11 + a * E2(eps, jx, 0) * E2(eps, ix, 0);
+          l12 = l12 + a * E2(eps, jx, 0) * E2(eps, ix, 1);
+          l13 = l13 + a * E2(eps, jx, 0) * E2(eps, ix, 2);
+          l32 = l32 + a * E2(eps, jx, 2) * E2(eps, ix, 1);
+          l33 = l33 + a * E2(eps, jx, 2) * E2(eps, ix, 2);
+        }
+      }
+    dmat[imu + 5 * 0] = 2.0 * l12;
+    dmat[imu + 5 * 1] = 2.0 * l32;
+    dmat[imu + 5 * 2] = sqrt(3.0) * l33;
+    dmat[imu + 5 * 3] = 2.0 * l13;
+    dmat[imu + 5 * 4] = 2.0 * l11 + l33;
+  }
+}
+
+/* chooser: rm[a + 5*b] */
+static void chooser(int l, const double *dmat, const double *pmat, double *rm) {
+  for (int k = 0; k < 25; k++) rm[k] = 0.0;
+  if (l == 0) rm[0] = 1.0;
+  else if (l == 1) {
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) rm[a + 5 * b] = pmat[a + 3 * b];
+  } else if (l == 2) {
+    for (int k = 0; k < 25; k++) rm[k] = dmat[k];
+  }
+}
+
+void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu, int norb_nu, const double *mm,
+               double *xm) {
+  double dmat[25] = {0}, pmat[9], left[25], right[25];
+  twister(eps, fd->have_dorbitals, dmat, pmat);
+  for (int k = 0; k < norb_mu * norb_nu; k++) xm[k] = 0.0;
+  int n1 = 0;
+  for (int issh = 0; issh < fd->sp[in1].nssh; issh++) {
+    int l1 = fd->sp[in1].lssh[issh];
+    chooser(l1, dmat, pmat, left);
+    int n2 = 0;
+    for (int jssh = 0; jssh < fd->sp[in3].nssh; jssh++) {
+      int l2 = fd->sp[in3].lssh[jssh];
+      chooser(l2, dmat, pmat, right);
+      for (int m2 = 0; m2 < 2 * l2 + 1; m2++)
+        for (int m1 = 0; m1 < 2 * l1 + 1; m1++)
+          for (int k2 = 0; k2 < 2 * l2 + 1; k2++)
+            for (int k1 = 0; k1 < 2 * l1 + 1; k1++)
+              xm[(n1 + k1) + norb_mu * (n2 + k2)] = xm[(n1 + k1) + norb_mu * (n2 + k2)] +
+                                                    left[k1 + 5 * m1] * mm[(n1 + m1) + norb_mu * (n2 + m2)] *
+                                                        right[k2 + 5 * m2];
+      n2 += 2 * l2 + 1;
+    }
+    n1 += 2 * l1 + 1;
+  }
+}
+
+/* Dtwister: Ddmat[ix + 3*(a + 5*b)], Dpmat[ix + 3*(a + 3*b)] */
+static void dtwister(const double *eps, const double *deps, double *Ddmat, double *Dpmat) {
+  for (int k = 0; k < 3; k++) {
+    Dpmat[k + 3 * (0 + 3 * 0)] = E3(deps, k, 1, 1);
+    Dpmat[k + 3 * (0 + 3 * 1)] = E3(deps, k, 1, 2);
+    Dpmat[k + 3 * (0 + 3 * 2)] = E3(deps, k, 1, 0);
+    Dpmat[k + 3 * (1 + 3 * 0)] = E3(deps, k, 2, 1);
+    Dpmat[k + 3 * (1 + 3 * 1)] = E3(deps, k, 2, 2);
+    Dpmat[k + 3 * (1 + 3 * 2)] = E3(deps, k, 2, 0);
+    Dpmat[k + 3 * (2 + 3 * 0)] = E3(deps, k, 0, 1);
+    Dpmat[k + 3 * (2 + 3 * 1)] = E3(deps, k, 0, 2);
+    Dpmat[k + 3 * (2 + 3 * 2)] = E3(deps, k, 0, 0);
+  }
+  for (int imu = 0; imu < 5; imu++)
+    for (int kx = 0; kx < 3; kx++) {
+      double a12 = 0, a32 = 0, a33 = 0, a13 = 0, a11 = 0;
+      for (int ix = 0; ix < 3; ix++)
+        for (int jx = 0; jx < 3; jx++) {
+          double a = amat(jx, ix, imu);
+          if (a != 0.0) {
+            a12 = a12 + a * (E3(deps, kx, ix, 0) * E2(eps, jx, 1) + E2(eps, ix, 0) * E3(deps, kx, jx, 1));
+            a32 = a32 + a * (E3(deps, kx, ix, 2) * E2(eps, jx, 1) + E2(eps, ix, 2) * E3(deps, kx, jx, 1));
+            a33 = a33 + a * (E3(deps, kx, ix, 2) * E2(eps, jx, 2) + E2(eps, ix, 2) * E3(deps, kx, jx, 2));
+            a13 = a13 + a * (E3(deps, kx, ix, 0) * E2(eps, jx, 2) + E2(eps, ix, 0) * E3(deps, kx, jx, 2));
+            a11 = a11 + a * (E3(deps, kx, ix, 0) * E2(eps, jx, 0) + E2(eps, ix, 0) * E3(deps, kx, jx, 0));
+          }
+        }
+      Ddmat[kx + 3 * (imu + 5 * 0)] = 2.0 * a12;
+      Ddmat[kx + 3 * (imu + 5 * 1)] = 2.0 * a32;
+      Ddmat[kx + 3 * (imu + 5 * 2)] = sqrt(3.0) * a33;
+      Ddmat[kx + 3 * (imu + 5 * 3)] = 2.0 * a13;
+      Ddmat[kx + 3 * (imu + 5 * 4)] = 2.0 * a11 + a33;
+    }
+}
+
+static void dchooser(int l, const double *Ddmat, const double *Dpmat, double *Dm) {
+  for (int k = 0; k < 75; k++) Dm[k] = 0.0;
+  if (l == 1) {
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++)
+        for (int x = 0; x < 3; x++) Dm[x + 3 * (a + 5 * b)] = Dpmat[x + 3 * (a + 3 * b)];
+  } else if (l == 2) {
+    for (int k = 0; k < 75; k++) Dm[k] = Ddmat[k];
+  }
+}
+
+/* Drotate = twister + Dtwister + Dmatrix; matm (norb_mu,norb_nu), Dmatm and
+ * Dmatx (3,norb_mu,norb_nu) */
+static void drotate(or_fdata *fd, int in1, int in2, const double *eps, const double *deps, int norb_mu,
+                    int norb_nu, const double *matm, const double *Dmatm, double *term) {
+  double dmat[25] = {0}, pmat[9], Ddmat[75], Dpmat[27];
+  double left[25], right[25], Dleft[75], Dright[75];
+  twister(eps, fd->have_dorbitals, dmat, pmat);
+  dtwister(eps, deps, Ddmat, Dpmat);
+  int n1 = 0;
+  for (int issh = 0; issh < fd->sp[in1].nssh; issh++) {
+    int l1 = fd->sp[in1].lssh[issh];
+    chooser(l1, dmat, pmat, left);
+    dchooser(l1, Ddmat, Dpmat, Dleft);
+    int n2 = 0;
+    for (int jssh = 0; jssh < fd->sp[in2].nssh; jssh++) {
+      int l2 = fd->sp[in2].lssh[jssh];
+      chooser(l2, dmat, pmat, right);
+      dchooser(l2, Ddmat, Dpmat, Dright);
+      for (int k2 = 0; k2 < 2 * l2 + 1; k2++)
+        for (int k1 = 0; k1 < 2 * l1 + 1; k1++)
+          for (int x = 0; x < 3; x++) term[x + 3 * ((n1 + k1) + norb_mu * (n2 + k2))] = 0.0;
+      for (int m2 = 0; m2 < 2 * l2 + 1; m2++)
+        for (int k2 = 0; k2 < 2 * l2 + 1; k2++)
+          for (int m1 = 0; m1 < 2 * l1 + 1; m1++)
+            for (int k1 = 0; k1 < 2 * l1 + 1; k1++)
+              for (int x = 0; x < 3; x++) {
+                double mv = matm[(n1 + m1) + norb_mu * (n2 + m2)];
+                size_t ko = x + 3 * ((n1 + k1) + norb_mu * (n2 + k2));
+                term[ko] = term[ko] + Dleft[x + 3 * (k1 + 5 * m1)] * right[k2 + 5 * m2] * mv +
+                           left[k1 + 5 * m1] * Dright[x + 3 * (k2 + 5 * m2)] * mv +
+                           left[k1 + 5 * m1] * right[k2 + 5 * m2] * Dmatm[x + 3 * ((n1 + m1) + norb_mu * (n2 + m2))];
+              }
+      n2 += 2 * l2 + 1;
+    }
+    n1 += 2 * l1 + 1;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* structure and neighbor maps                                               */
+/* ------------------------------------------------------------------------ */
+or_sys *or_create_system(or_fdata *fd, int natoms, const double *ratom, const int *imass, const double *lattice,
+                         int icluster) {
+  if (!fd || natoms < 1) return NULL;
+  or_sys *s = (or_sys *)calloc(1, sizeof(or_sys));
+  s->fd = fd;
+  s->natoms = natoms;
+  s->icluster = icluster;
+  s->ratom = (double *)malloc(sizeof(double) * 3 * natoms);
+  s->imass = (int *)malloc(sizeof(int) * natoms);
+  memcpy(s->ratom, ratom, sizeof(double) * 3 * natoms);
+  memcpy(s->imass, imass, sizeof(int) * natoms);
+  for (int i = 0; i < natoms; i++)
+    if (imass[i] < 1 || imass[i] > fd->nspecies) { free(s->ratom); free(s->imass); free(s); return NULL; }
+  memcpy(s->lattice, lattice, sizeof(double) * 9);
+  /* make_cells (c.SYSTEM/make_cells.f90:112-144) */
+  if (icluster == 1) {
+    s->mbeta_max = 0;
+    s->xl = (double(*)[3])calloc(1, sizeof(double[3]));
+  } else {
+    int mbox = P_mbox;
+    s->mbeta_max = (2 * P_mbox + 1) * (2 * P_mbox + 1) * (2 * P_mbox + 1) - 1;
+    s->xl = (double(*)[3])calloc((size_t)s->mbeta_max + 1, sizeof(double[3]));
+    int mbeta = 1;
+    for (int iz = -mbox; iz <= mbox; iz++)
+      for (int iy = -mbox; iy <= mbox; iy++)
+        for (int ix = -mbox; ix <= mbox; ix++)
+          if (!(ix == 0 && iy == 0 && iz == 0)) {
+            for (int k = 0; k < 3; k++)
+              s->xl[mbeta][k] = (double)ix * lattice[0 * 3 + k] + (double)iy * lattice[1 * 3 + k] +
+                                (double)iz * lattice[2 * 3 + k];
+            mbeta++;
+          }
+  }
+  return s;
+}
+
+static void free_neigh(or_sys *s) {
+  free(s->neighn); free(s->pair_off); free(s->neigh_j); free(s->neigh_b); free(s->neigh_back);
+  free(s->neigh_self); free(s->blk_off); free(s->ncommon); free(s->trip_off); free(s->ci_j);
+  free(s->ci_b); free(s->cj_j); free(s->cj_b); free(s->cneigh);
+  s->neighn = s->pair_off = s->neigh_j = s->neigh_b = s->neigh_back = s->neigh_self = NULL;
+  s->ncommon = s->trip_off = s->ci_j = s->ci_b = s->cj_j = s->cj_b = s->cneigh = NULL;
+  s->blk_off = NULL;
+}
+
+void or_free_system(or_sys *s) {
+  if (!s) return;
+  free_neigh(s);
+  free(s->ratom); free(s->imass); free(s->xl);
+  free(s);
+}
+
+static double rcut_of(const or_sys *s, int iatom) { return s->fd->sp[s->imass[iatom]].rcutoffA_max; }
+#define RAT(s, i) (&(s)->ratom[3 * (i)])
+
+/* find_neigh_max + find_neighbors + neigh_self/neigh_back
+ * (c.SYSTEM/M_neighbors.f90:246-519), then find_common_max +
+ * find_common_neighbors (:548-812) */
+int or_neighbors(or_sys *s) {
+  free_neigh(s);
+  int N = s->natoms;
+  s->neighn = (int *)calloc((size_t)N, sizeof(int));
+  s->pair_off = (int *)calloc((size_t)N + 1, sizeof(int));
+  s->neigh_self = (int *)malloc(sizeof(int) * N);
+  /* counting pass (find_neigh_max :289-330) */
+  for (int i = 0; i < N; i++) {
+    int num = 0;
+    double rci = rcut_of(s, i), r2[3];
+    for (int mb = 0; mb <= s->mbeta_max; mb++)
+      for (int j = 0; j < N; j++) {
+        for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[mb][k];
+        double z = distance3(RAT(s, i), r2);
+        double range_max = rci + rcut_of(s, j) - 0.01;
+        if (z < range_max) num++;
+      }
+    s->neighn[i] = num;
+    s->pair_off[i + 1] = s->pair_off[i] + num;
+  }
+  int P = s->pair_off[N];
+  s->npairs = P;
+  s->neigh_j = (int *)malloc(sizeof(int) * (P ? P : 1));
+  s->neigh_b = (int *)malloc(sizeof(int) * (P ? P : 1));
+  s->neigh_back = (int *)malloc(sizeof(int) * (P ? P : 1));
+  for (int i = 0; i < N; i++) {                                     /* :392-439 */
+    int num = 0;
+    double rci = rcut_of(s, i), r2[3];
+    for (int mb = 0; mb <= s->mbeta_max; mb++)
+      for (int j = 0; j < N; j++) {
+        for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[mb][k];
+        double z = distance3(RAT(s, i), r2);
+        double range_max = rci + rcut_of(s, j) - 0.01;
+        if (i != j && z < 0.5) {
+          seterr("atoms dangerously close: %d %d z=%g mbeta=%d", i + 1, j + 1, z, mb);
+          return E_CLOSE;
+        }
+        if (z < range_max) {
+          s->neigh_j[s->pair_off[i] + num] = j;
+          s->neigh_b[s->pair_off[i] + num] = mb;
+          num++;
+        }
+      }
+  }
+  for (int i = 0; i < N; i++) s->neigh_self[i] = -999;              /* :456-505 */
+  for (int i = 0; i < N; i++) {
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, mb = s->neigh_b[p], j = s->neigh_j[p];
+      s->neigh_back[p] = -999;
+      if (i == j && mb == 0) {
+        if (s->neigh_self[i] != -999) { seterr("neigh_self found twice for %d", i + 1); return E_SELF; }
+        s->neigh_self[i] = in;
+      }
+      for (int jn = 0; jn < s->neighn[j]; jn++) {
+        int q = s->pair_off[j] + jn, jb = s->neigh_b[q], k = s->neigh_j[q];
+        if (i != k || fabs(s->xl[mb][0] + s->xl[jb][0]) > 1.0e-3 || fabs(s->xl[mb][1] + s->xl[jb][1]) > 1.0e-3 ||
+            fabs(s->xl[mb][2] + s->xl[jb][2]) > 1.0e-3) {
+        } else {
+          if (s->neigh_back[p] != -999) { seterr("neigh_back found twice for %d", i + 1); return E_BACK; }
+          s->neigh_back[p] = jn;
+        }
+      }
+    }
+    for (int in = 0; in < s->neighn[i]; in++)
+      if (s->neigh_back[s->pair_off[i] + in] == -999) { seterr("no neigh_back for %d", i + 1); return E_BACK; }
+  }
+  for (int i = 0; i < N; i++)
+    if (s->neigh_self[i] == -999) { seterr("no neigh_self for %d", i + 1); return E_SELF; }
+  /* block offsets */
+  s->blk_off = (long long *)malloc(sizeof(long long) * (P + 1));
+  long long off = 0;
+  for (int i = 0; i < N; i++)
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in;
+      s->blk_off[p] = off;
+      off += (long long)s->fd->sp[s->imass[i]].norb_max * s->fd->sp[s->imass[s->neigh_j[p]]].norb_max;
+    }
+  s->blk_off[P] = off;
+  s->nblock = off;
+  /* common neighbors (:681-812) */
+  s->ncommon = (int *)calloc((size_t)N, sizeof(int));
+  s->trip_off = (int *)calloc((size_t)N + 1, sizeof(int));
+  int cap = 1024, nt = 0;
+  s->ci_j = (int *)malloc(sizeof(int) * cap);
+  s->ci_b = (int *)malloc(sizeof(int) * cap);
+  s->cj_j = (int *)malloc(sizeof(int) * cap);
+  s->cj_b = (int *)malloc(sizeof(int) * cap);
+  s->cneigh = (int *)malloc(sizeof(int) * cap);
+  for (int ia = 0; ia < N; ia++) {
+    int num = 0;
+    for (int in = 0; in < s->neighn[ia]; in++) {
+      int p = s->pair_off[ia] + in, iat = s->neigh_j[p], ib = s->neigh_b[p];
+      if (iat == ia && ib == 0) continue;
+      double r1[3], r2[3], r3[3];
+      for (int k = 0; k < 3; k++) r1[k] = RAT(s, iat)[k] + s->xl[ib][k];
+      double rci = rcut_of(s, iat);
+      for (int jn = 0; jn < s->neighn[ia]; jn++) {
+        int q = s->pair_off[ia] + jn, jat = s->neigh_j[q], jb = s->neigh_b[q];
+        if ((jat == ia && jb == 0) || in == jn) continue;
+        for (int k = 0; k < 3; k++) r2[k] = RAT(s, jat)[k] + s->xl[jb][k];
+        double z = distance3(r1, r2);
+        double range_max = rci + rcut_of(s, jat) - 0.01;
+        if (z < range_max) {
+          int found = -9999;
+          for (int kn = 0; kn < s->neighn[iat]; kn++) {
+            int r = s->pair_off[iat] + kn, kat = s->neigh_j[r], kb = s->neigh_b[r];
+            for (int k = 0; k < 3; k++) r3[k] = s->xl[kb][k] + RAT(s, kat)[k] - RAT(s, iat)[k];
+            if ((fabs(r3[0] - r2[0] + r1[0]) < 1.0e-4) && (fabs(r3[1] - r2[1] + r1[1]) < 1.0e-4) &&
+                (fabs(r3[2] - r2[2] + r1[2]) < 1.0e-4)) {
+              found = kn;
+              break;
+            }
+          }
+          if (found == -9999) continue;
+          if (nt == cap) {
+            cap *= 2;
+            s->ci_j = (int *)realloc(s->ci_j, sizeof(int) * cap);
+            s->ci_b = (int *)realloc(s->ci_b, sizeof(int) * cap);
+            s->cj_j = (int *)realloc(s->cj_j, sizeof(int) * cap);
+            s->cj_b = (int *)realloc(s->cj_b, sizeof(int) * cap);
+            s->cneigh = (int *)realloc(s->cneigh, sizeof(int) * cap);
+          }
+          s->ci_j[nt] = iat;
+          s->ci_b[nt] = ib;
+          s->cj_j[nt] = jat;
+          s->cj_b[nt] = jb;
+          s->cneigh[nt] = found;
+          nt++;
+          num++;
+        }
+      }
+    }
+    s->ncommon[ia] = num;
+    s->trip_off[ia + 1] = s->trip_off[ia] + num;
+  }
+  s->ntrip = nt;
+  return OK;
+}
+
+int or_npairs(const or_sys *s) { return s->npairs; }
+int or_ntriplets(const or_sys *s) { return s->ntrip; }
+long long or_nblock(const or_sys *s) { return s->nblock; }
+
+void or_get_pairs(const or_sys *s, int *pair_off, int *neigh_j, int *neigh_b, int *neigh_back, int *neigh_self,
+                  long long *blk_off) {
+  int N = s->natoms, P = s->npairs;
+  if (pair_off) memcpy(pair_off, s->pair_off, sizeof(int) * (N + 1));
+  if (neigh_j) memcpy(neigh_j, s->neigh_j, sizeof(int) * P);
+  if (neigh_b) memcpy(neigh_b, s->neigh_b, sizeof(int) * P);
+  if (neigh_back) memcpy(neigh_back, s->neigh_back, sizeof(int) * P);
+  if (neigh_self) memcpy(neigh_self, s->neigh_self, sizeof(int) * N);
+  if (blk_off) memcpy(blk_off, s->blk_off, sizeof(long long) * (P + 1));
+}
+
+void or_get_triplets(const or_sys *s, int *trip_off, int *iatom_j, int *iatom_b, int *jatom_j, int *jatom_b,
+                     int *neigh_common) {
+  int N = s->natoms, T = s->ntrip;
+  if (trip_off) memcpy(trip_off, s->trip_off, sizeof(int) * (N + 1));
+  if (iatom_j) memcpy(iatom_j, s->ci_j, sizeof(int) * T);
+  if (iatom_b) memcpy(iatom_b, s->ci_b, sizeof(int) * T);
+  if (jatom_j) memcpy(jatom_j, s->cj_j, sizeof(int) * T);
+  if (jatom_b) memcpy(jatom_b, s->cj_b, sizeof(int) * T);
+  if (neigh_common) memcpy(neigh_common, s->cneigh, sizeof(int) * T);
+}
+
+/* ------------------------------------------------------------------------ */
+/* assemblers                                                                */
+/* ------------------------------------------------------------------------ */
+/* pair set-up shared by all 2c assemblers: z, sighat, eps = epsilon(r2,
+ * sighat) (e.g. j.ASSEMBLERS/M_assemble_2c_Harris.f90:170-177) */
+static void pair_frame(const or_sys *s, int i, int p, double *r1, double *r2, double *z, double *eps) {
+  double sighat[3];
+  int j = s->neigh_j[p], mb = s->neigh_b[p];
+  for (int k = 0; k < 3; k++) {
+    r1[k] = RAT(s, i)[k];
+    r2[k] = RAT(s, j)[k] + s->xl[mb][k];
+  }
+  *z = distance3(r1, r2);
+  if (*z < 1.0e-05) {
+    sighat[0] = 0.0;
+    sighat[1] = 0.0;
+    sighat[2] = 1.0;
+  } else {
+    for (int k = 0; k < 3; k++) sighat[k] = (r2[k] - r1[k]) / *z;
+  }
+  or_epsilon(r2, sighat, eps);
+}
+
+/* assemble_S (:89-209), assemble_T (:233-353), assemble_vna_2c (:435-649) of
+ * j.ASSEMBLERS/M_assemble_2c_Harris.f90 */
+int or_assemble_2c(or_sys *s, double *S, double *T, double *vb, double *vbo) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
+  for (int i = 0; i < N; i++) {
+    double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      long long o = s->blk_off[p];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      if (S) {
+        if ((st = or_getMEs_2c(fd, in1, in2, P_overlap, 0, z, nmu, nnu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        memcpy(S + o, xm, sizeof(double) * nmu * nnu);
+      }
+      if (T) {
+        if ((st = or_getMEs_2c(fd, in1, in2, P_kinetic, 0, z, nmu, nnu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        memcpy(T + o, xm, sizeof(double) * nmu * nnu);
+      }
+      if (vb) {
+        for (int k = 0; k < nmu * nnu; k++) vb[o + k] = 0.0, vbo[o + k] = 0.0;
+        if (!(i == j && s->neigh_b[p] == 0)) {
+          if ((st = or_getMEs_2c(fd, in1, in2, P_vna_ontopL, 0, z, nmu, nnu, mm))) { err = st; continue; }
+          or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+          for (int k = 0; k < nmu * nnu; k++) vbo[o + k] = vbo[o + k] + xm[k] * P_eq2;
+          if ((st = or_getMEs_2c(fd, in1, in2, P_vna_ontopR, 0, z, nmu, nnu, mm))) { err = st; continue; }
+          or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+          for (int k = 0; k < nmu * nnu; k++) vbo[o + k] = vbo[o + k] + xm[k] * P_eq2;
+        }
+      }
+    }
+    if (vb) {
+      /* atom case (:584-636): <i|v(j)|i> summed into block(neigh_self(i)) */
+      long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+      for (int k = 0; k < nmu * nmu; k++) vb[os + k] = 0.0;
+      for (int in = 0; in < s->neighn[i]; in++) {
+        int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+        pair_frame(s, i, p, r1, r2, &z, eps);
+        if ((st = or_getMEs_2c(fd, in1, in2, P_vna_atom, 0, z, nmu, nmu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in1, eps, nmu, nmu, mm, xm);
+        for (int k = 0; k < nmu * nmu; k++) vb[os + k] = vb[os + k] + xm[k] * P_eq2;
+      }
+    }
+  }
+  return err;
+}
+
+/* triplet set-up shared by assemble_vna_3c and Dassemble_vna_3c
+ * (j.ASSEMBLERS/M_assemble_3c_Harris.f90:154-189) */
+typedef struct {
+  double r1[3], r2[3], rna[3], r21[3], rnabc[3], sighat[3], rhat[3], z, x, cost, eps[9];
+  int iatom, jatom, in1, in2, indna, mneigh;
+} trip_t;
+
+static void trip_frame(const or_sys *s, int ia, int t, trip_t *g) {
+  g->indna = s->imass[ia];
+  for (int k = 0; k < 3; k++) g->rna[k] = RAT(s, ia)[k];
+  g->mneigh = s->cneigh[t];
+  g->iatom = s->ci_j[t];
+  g->jatom = s->cj_j[t];
+  for (int k = 0; k < 3; k++) {
+    g->r1[k] = RAT(s, g->iatom)[k] + s->xl[s->ci_b[t]][k];
+    g->r2[k] = RAT(s, g->jatom)[k] + s->xl[s->cj_b[t]][k];
+  }
+  g->in1 = s->imass[g->iatom];
+  g->in2 = s->imass[g->jatom];
+  for (int k = 0; k < 3; k++) g->r21[k] = g->r2[k] - g->r1[k];
+  g->z = distance3(g->r1, g->r2);
+  if (g->z < 1.0e-05) {
+    g->sighat[0] = 0.0; g->sighat[1] = 0.0; g->sighat[2] = 1.0;
+  } else {
+    for (int k = 0; k < 3; k++) g->sighat[k] = g->r21[k] / g->z;
+  }
+  for (int k = 0; k < 3; k++) g->rnabc[k] = g->rna[k] - (g->r1[k] + g->r21[k] / 2.0);
+  g->x = sqrt(g->rnabc[0] * g->rnabc[0] + g->rnabc[1] * g->rnabc[1] + g->rnabc[2] * g->rnabc[2]);
+  if (g->x < 1.0e-05) {
+    g->rhat[0] = g->rhat[1] = g->rhat[2] = 0.0;
+  } else {
+    for (int k = 0; k < 3; k++) g->rhat[k] = g->rnabc[k] / g->x;
+  }
+  g->cost = g->sighat[0] * g->rhat[0] + g->sighat[1] * g->rhat[1] + g->sighat[2] * g->rhat[2];
+  or_epsilon(g->rhat, g->sighat, g->eps);
+}
+
+/* assemble_vna_3c (j.ASSEMBLERS/M_assemble_3c_Harris.f90:82-227) */
+int or_assemble_3c(or_sys *s, double *vb) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK, nthr = g_threads;
+  long long nb = s->nblock;
+  double *acc = NULL;
+  if (nthr > 1) acc = (double *)calloc((size_t)nthr * nb, sizeof(double));
+#pragma omp parallel num_threads(nthr) if (nthr > 1)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double *dst = nthr > 1 ? acc + (size_t)tid * nb : vb;
+#pragma omp for schedule(dynamic, 2)
+    for (int ia = 0; ia < N; ia++) {
+      double mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+      for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+        trip_t g;
+        trip_frame(s, ia, t, &g);
+        int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+        int st = or_getMEs_3c(fd, g.in1, g.in2, g.indna, P_bcna, 0, g.x, g.z, nmu, nnu, g.cost, mm);
+        if (st) { err = st; continue; }
+        or_rotate(fd, g.in1, g.in2, g.eps, nmu, nnu, mm, xm);
+        long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+        for (int k = 0; k < nmu * nnu; k++) dst[o + k] = dst[o + k] + xm[k] * P_eq2;
+      }
+    }
+  }
+  if (nthr > 1) {
+    for (int t = 0; t < nthr; t++)
+#pragma omp parallel for num_threads(nthr)
+      for (long long k = 0; k < nb; k++) vb[k] += acc[(size_t)t * nb + k];
+    free(acc);
+  }
+  return err;
+}
+
+/* Dassemble_S/T (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:96-263, :289-456)
+ * and Dassemble_vna_2c (:538-869) */
+int or_dassemble_2c(or_sys *s, const double *rho, double *dS, double *dT, double *vna_ontop, double *vna_atom) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
+  for (int i = 0; i < N; i++) {
+    double r1[3], r2[3], z, eps[9], deps[27], eta[3];
+    double mm[MAXORB * MAXORB], dm[MAXORB * MAXORB], vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    const int ints[2] = {P_overlap, P_kinetic};
+    double *outs[2] = {dS, dT};
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      long long o = s->blk_off[p];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      for (int w = 0; w < 2; w++) {
+        if (!outs[w]) continue;
+        for (int k = 0; k < nmu * nnu; k++) mm[k] = dm[k] = 0.0;
+        if ((st = or_getDMEs_2c(fd, in1, in2, ints[w], 0, z, nmu, nnu, mm, dm))) { err = st; continue; }
+        for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = 0.0;
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            if (z > 1.0e-3)
+              for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+        drotate(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+        memcpy(outs[w] + 3 * o, vdx, sizeof(double) * 3 * nmu * nnu);
+      }
+      if (vna_ontop) {
+        double *f = vna_ontop + 3 * (size_t)p;
+        f[0] = f[1] = f[2] = 0.0;
+        if (!(i == j && s->neigh_b[p] == 0)) {
+          const int vi[2] = {P_vna_ontopL, P_vna_ontopR};
+          for (int w = 0; w < 2; w++) {
+            for (int k = 0; k < nmu * nnu; k++) mm[k] = dm[k] = 0.0;
+            for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = vdx[k] = 0.0;
+            if ((st = or_getDMEs_2c(fd, in1, in2, vi[w], 0, z, nmu, nnu, mm, dm))) { err = st; continue; }
+            for (int inu = 0; inu < nnu; inu++)
+              for (int imu = 0; imu < nmu; imu++)
+                if (z > 1.0e-3)
+                  for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+            drotate(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+            for (int inu = 0; inu < nnu; inu++)
+              for (int imu = 0; imu < nmu; imu++)
+                for (int c = 0; c < 3; c++)
+                  f[c] = f[c] - rho[o + imu + nmu * inu] * vdx[c + 3 * (imu + nmu * inu)] * P_eq2;
+          }
+        }
+      }
+    }
+    if (vna_atom) {
+      /* atom case (:784-859), contracted with the self block of rho */
+      long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+      for (int in = 0; in < s->neighn[i]; in++) {
+        int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+        double *f = vna_atom + 3 * (size_t)p;
+        f[0] = f[1] = f[2] = 0.0;
+        pair_frame(s, i, p, r1, r2, &z, eps);
+        or_depsilon_2c(r1, r2, z, eps, deps);
+        for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+        for (int k = 0; k < nmu * nmu; k++) mm[k] = dm[k] = 0.0;
+        for (int k = 0; k < 3 * nmu * nmu; k++) vdm[k] = vdx[k] = 0.0;
+        if ((st = or_getDMEs_2c(fd, in1, in2, P_vna_atom, 0, z, nmu, nmu, mm, dm))) { err = st; continue; }
+        for (int inu = 0; inu < nmu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            if (z > 1.0e-3)
+              for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+        drotate(fd, in1, in1, eps, deps, nmu, nmu, mm, vdm, vdx);
+        for (int inu = 0; inu < nmu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            for (int c = 0; c < 3; c++)
+              f[c] = f[c] - rho[os + imu + nmu * inu] * vdx[c + 3 * (imu + nmu * inu)] * P_eq2;
+      }
+    }
+  }
+  return err;
+}
+
+/* Dassemble_vna_3c (k.DASSEMBLERS/M_Dassemble_3c_Harris.f90:136-408) */
+int or_dassemble_3c(or_sys *s, const double *rho, double *f3naa, double *f3nab, double *f3nac) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK, nthr = g_threads;
+  double *acc = (double *)calloc((size_t)nthr * 9 * N, sizeof(double));
+#pragma omp parallel num_threads(nthr) if (nthr > 1)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double *fa = acc + (size_t)tid * 9 * N, *fb = fa + 3 * N, *fc = fb + 3 * N;
+#pragma omp for schedule(dynamic, 2)
+    for (int ia = 0; ia < N; ia++) {
+      double mm[MAXORB * MAXORB], dpm[MAXORB * MAXORB], dxm[MAXORB * MAXORB], dym[MAXORB * MAXORB];
+      double Ma[3 * MAXORB * MAXORB], Mb[3 * MAXORB * MAXORB], Xa[3 * MAXORB * MAXORB], Xb[3 * MAXORB * MAXORB];
+      double depsA[27], depsB[27], amt[3], bmt[3];
+      for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+        trip_t g;
+        trip_frame(s, ia, t, &g);
+        int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+        or_depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.eps, depsA, depsB);
+        if (g.x > 1.0e-5)                                           /* :285-292 */
+          for (int k = 0; k < 3; k++) amt[k] = (g.sighat[k] - g.cost * g.rhat[k]) / g.x;
+        else
+          amt[0] = amt[1] = amt[2] = 0.0;
+        for (int k = 0; k < 3; k++) bmt[k] = (g.cost * g.sighat[k] - g.rhat[k]) / g.z;
+        int st = or_getDMEs_3c(fd, g.in1, g.in2, g.indna, P_bcna, 0, g.x, g.z, nmu, nnu, g.cost, mm, dpm, dxm, dym);
+        if (st) { err = st; continue; }
+        for (int k = 0; k < 3 * nmu * nnu; k++) Ma[k] = Mb[k] = 0.0;
+        cell3c *c = get_cell3c(fd, g.in1, g.in2, g.indna, P_bcna, 0, 1);
+        for (int m = 0; m < c->nME; m++) {                          /* :330-345 */
+          int k = (c->mu[m] - 1) + nmu * (c->nu[m] - 1);
+          for (int q = 0; q < 3; q++) Ma[q + 3 * k] = g.rhat[q] * dxm[k] + amt[q] * dpm[k];
+          for (int q = 0; q < 3; q++) Mb[q + 3 * k] = -g.sighat[q] * dym[k] + bmt[q] * dpm[k] - Ma[q + 3 * k] / 2.0;
+        }
+        drotate(fd, g.in1, g.in2, g.eps, depsA, nmu, nnu, mm, Ma, Xa);
+        drotate(fd, g.in1, g.in2, g.eps, depsB, nmu, nnu, mm, Mb, Xb);
+        long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+        for (int inu = 0; inu < nnu; inu++)                         /* :379-388 */
+          for (int imu = 0; imu < nmu; imu++) {
+            double r = rho[o + imu + nmu * inu];
+            for (int q = 0; q < 3; q++) {
+              double xa = Xa[q + 3 * (imu + nmu * inu)], xb = Xb[q + 3 * (imu + nmu * inu)];
+              double xc = -xa - xb;
+              fa[3 * ia + q] = fa[3 * ia + q] - r * xa * P_eq2;
+              fb[3 * g.iatom + q] = fb[3 * g.iatom + q] - r * xb * P_eq2;
+              fc[3 * g.jatom + q] = fc[3 * g.jatom + q] - r * xc * P_eq2;
+            }
+          }
+      }
+    }
+  }
+  for (int k = 0; k < 3 * N; k++) {
+    double a = 0, b = 0, cc = 0;
+    for (int t = 0; t < nthr; t++) {
+      a += acc[(size_t)t * 9 * N + k];
+      b += acc[(size_t)t * 9 * N + 3 * N + k];
+      cc += acc[(size_t)t * 9 * N + 6 * N + k];
+    }
+    if (f3naa) f3naa[k] = a;
+    if (f3nab) f3nab[k] = b;
+    if (f3nac) f3nac[k] = cc;
+  }
+  free(acc);
+  return err;
+}
+
+/* build_forces (c.SYSTEM/M_build_forces.f90:172-588), assembly terms only:
+ * kinetic (:234-301), vna atom/ontop (:310-345), f3na (:444-451), Pulay
+ * (:473-537).  The vxc, ewald, vnl, usr and vdW terms belong to assemblers
+ * outside this library and are left to the caller. */
+int or_build_forces(or_sys *s, const double *rho, const double *cape, const double *dS, const double *dT,
+                    const double *vna_ontop, const double *vna_atom, const double *f3naa, const double *f3nab,
+                    const double *f3nac, double *kinetic, double *vna, double *pulay, double *ftot) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  for (int k = 0; k < 3 * N; k++) kinetic[k] = vna[k] = pulay[k] = ftot[k] = 0.0;
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      long long o = s->blk_off[p];
+      for (int ix = 0; ix < 3; ix++) {
+        double sumT = 0.0;
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            sumT = sumT + rho[o + imu + nmu * inu] * dT[3 * (o + imu + nmu * inu) + ix];
+        kinetic[3 * i + ix] = kinetic[3 * i + ix] + (-1.0) * sumT;
+        kinetic[3 * j + ix] = kinetic[3 * j + ix] - (-1.0) * sumT;
+      }
+    }
+  }
+  for (int k = 0; k < 3 * N; k++) ftot[k] = ftot[k] + kinetic[k];
+  for (int i = 0; i < N; i++)
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p];
+      for (int q = 0; q < 3; q++) {
+        vna[3 * i + q] = vna[3 * i + q] + vna_atom[3 * p + q];
+        vna[3 * j + q] = vna[3 * j + q] - vna_atom[3 * p + q];
+        ftot[3 * i + q] = ftot[3 * i + q] + vna_atom[3 * p + q];
+        ftot[3 * j + q] = ftot[3 * j + q] - vna_atom[3 * p + q];
+        vna[3 * i + q] = vna[3 * i + q] + vna_ontop[3 * p + q];
+        vna[3 * j + q] = vna[3 * j + q] - vna_ontop[3 * p + q];
+        ftot[3 * i + q] = ftot[3 * i + q] + vna_ontop[3 * p + q];
+        ftot[3 * j + q] = ftot[3 * j + q] - vna_ontop[3 * p + q];
+      }
+    }
+  for (int k = 0; k < 3 * N; k++) ftot[k] = ftot[k] + f3naa[k] + f3nab[k] + f3nac[k];
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      long long o = s->blk_off[p];
+      for (int ix = 0; ix < 3; ix++) {
+        double sumT = 0.0;
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            sumT = sumT + cape[o + imu + nmu * inu] * dS[3 * (o + imu + nmu * inu) + ix];
+        pulay[3 * i + ix] = pulay[3 * i + ix] + (-1.0) * sumT;
+        pulay[3 * j + ix] = pulay[3 * j + ix] - (-1.0) * sumT;
+      }
+    }
+  }
+  for (int k = 0; k < 3 * N; k++) ftot[k] = ftot[k] - pulay[k];
+  return OK;
+}

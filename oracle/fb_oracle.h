@@ -1,0 +1,107 @@
+/*
+ * fb_oracle.h -- CPU oracle for the FIREBALL Harris matrix-element assembly.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * Fortran routines on the assembly path.  Only the test suite, the smoke check
+ * and the CPU-baseline leg of the benchmark load it, and only as the checker
+ * or the timed CPU baseline; the GPU library never links or calls it.
+ *
+ * Parity status: UNPINNED.  The reference ships no tests, golden vectors or
+ * Fdata, and its Fortran cannot be compiled where this project is built (no
+ * Fortran compiler), so this restatement is checked by property tests
+ * (polynomial exactness of the interpolators, Hermiticity through neigh_back,
+ * rotation invariance, finite differences of the derivative paths) rather
+ * than against outputs of the reference itself.
+ *
+ * Layout conventions (shared with the GPU library):
+ *   pairs   p = pair_off[i] + ineigh, CSR by atom i, reference order
+ *   blocks  block p at blk_off[p], column-major norb_i x norb_j (Fortran
+ *           block(mu,nu) of T_assemble_block, a.GLOBAL/M_assemble_blocks.f90:44)
+ *   Dblocks 3 * blk_off[p], layout Dblock(3,mu,nu) column-major
+ *   per-pair 3-vectors (vna_ontop, vna_atom) at 3*p
+ *   per-atom 3-vectors at 3*i
+ */
+#ifndef FB_ORACLE_H
+#define FB_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct or_fdata or_fdata;
+typedef struct or_sys or_sys;
+
+/* read_info + read_Fdata_2c + read_Fdata_3c.  Returns NULL on failure and
+ * writes a message into err. */
+or_fdata *or_load_fdata(const char *dir, int nspecies, const int *nZ,
+                        char *err, int errlen);
+void or_free_fdata(or_fdata *fd);
+int or_species_norb(const or_fdata *fd, int ispecies /* 1-based */);
+
+/* structure + make_cells; positions (natoms,3) row-major Angstrom,
+ * imass 1-based species, lattice rows a1,a2,a3 */
+or_sys *or_create_system(or_fdata *fd, int natoms, const double *ratom,
+                         const int *imass, const double *lattice, int icluster);
+void or_free_system(or_sys *s);
+
+/* driver_neighbors: find_neigh_max/find_neighbors/find_common_* */
+int or_neighbors(or_sys *s);
+int or_npairs(const or_sys *s);
+int or_ntriplets(const or_sys *s);
+long long or_nblock(const or_sys *s);        /* total doubles of one block set */
+/* copy out neighbor maps (caller allocates) */
+void or_get_pairs(const or_sys *s, int *pair_off, int *neigh_j, int *neigh_b,
+                  int *neigh_back, int *neigh_self, long long *blk_off);
+void or_get_triplets(const or_sys *s, int *trip_off, int *iatom_j,
+                     int *iatom_b, int *jatom_j, int *jatom_b,
+                     int *neigh_common);
+
+/* assemblers (j.ASSEMBLERS Harris): outputs are full block sets */
+int or_assemble_2c(or_sys *s, double *S, double *T, double *vna_block,
+                   double *vna_blocko);
+int or_assemble_3c(or_sys *s, double *vna_block);   /* accumulates */
+
+/* derivative assemblers (k.DASSEMBLERS Harris); rho = denmat block set */
+int or_dassemble_2c(or_sys *s, const double *rho, double *dS, double *dT,
+                    double *vna_ontop, double *vna_atom);
+int or_dassemble_3c(or_sys *s, const double *rho, double *f3naa,
+                    double *f3nab, double *f3nac);
+/* build_forces, assembly terms only: kinetic, vna, f3na, pulay, ftot */
+int or_build_forces(or_sys *s, const double *rho, const double *cape,
+                    const double *dS, const double *dT,
+                    const double *vna_ontop, const double *vna_atom,
+                    const double *f3naa, const double *f3nab,
+                    const double *f3nac, double *kinetic, double *vna,
+                    double *pulay, double *ftot);
+
+/* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
+ * norb_mu x norb_nu column-major */
+int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x,
+                 int norb_mu, int norb_nu, double *hmbox);
+int or_getDMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub,
+                  double x, int norb_mu, int norb_nu, double *hmbox,
+                  double *dhmbox);
+int or_getMEs_3c(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub,
+                 double x, double y, int norb_mu, int norb_nu, double cost,
+                 double *hmbox);
+int or_getDMEs_3c(or_fdata *fd, int isp, int jsp, int ksp, int iint, int isub,
+                  double x, double y, int norb_mu, int norb_nu, double cost,
+                  double *hmbox, double *dphmbox, double *dxhmbox,
+                  double *dyhmbox);
+void or_epsilon(const double *r1, const double *r2, double *spe);
+void or_depsilon_2c(const double *r1, const double *r2, double z,
+                    const double *eps, double *deps);
+void or_depsilon_3c(const double *r1, const double *r2, const double *r21,
+                    double z, const double *ratm, const double *rnabc,
+                    const double *eps3, double *dera3, double *der13);
+void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu,
+               int norb_nu, const double *mmatrix, double *xmatrix);
+
+/* OpenMP thread count for the assemblers (1 = serial reference order) */
+void or_set_threads(int n);
+const char *or_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,217 @@
+"""ctypes wrapper of the C oracle (oracle/fb_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by the tests, by the smoke check and by
+the CPU-baseline leg of the benchmark, always as the checker or the timed CPU
+baseline, never as part of the GPU product path.  Parity status: unpinned
+(the reference has no golden data and its Fortran cannot be built here).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "fb_oracle.c")):
+            build()
+        L = C.CDLL(LIB)
+        L.or_load_fdata.restype = C.c_void_p
+        L.or_load_fdata.argtypes = [C.c_char_p, C.c_int, _ip, C.c_char_p, C.c_int]
+        L.or_free_fdata.argtypes = [C.c_void_p]
+        L.or_species_norb.argtypes = [C.c_void_p, C.c_int]
+        L.or_create_system.restype = C.c_void_p
+        L.or_create_system.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _dp, C.c_int]
+        L.or_free_system.argtypes = [C.c_void_p]
+        L.or_neighbors.argtypes = [C.c_void_p]
+        L.or_npairs.argtypes = [C.c_void_p]
+        L.or_ntriplets.argtypes = [C.c_void_p]
+        L.or_nblock.argtypes = [C.c_void_p]
+        L.or_nblock.restype = C.c_longlong
+        L.or_get_pairs.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip, _ip, _lp]
+        L.or_get_triplets.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip, _ip, _ip]
+        L.or_assemble_2c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.or_assemble_3c.argtypes = [C.c_void_p, _dp]
+        L.or_dassemble_2c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+        L.or_dassemble_3c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.or_build_forces.argtypes = [C.c_void_p] + [_dp] * 13
+        L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
+        L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                    _dp, _dp]
+        L.or_getMEs_3c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                   C.c_int, C.c_int, C.c_double, _dp]
+        L.or_getDMEs_3c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                    C.c_double, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp]
+        L.or_epsilon.argtypes = [_dp, _dp, _dp]
+        L.or_depsilon_2c.argtypes = [_dp, _dp, C.c_double, _dp, _dp]
+        L.or_depsilon_3c.argtypes = [_dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp]
+        L.or_rotate.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, C.c_int, _dp, _dp]
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("oracle status %d: %s" % (code, msg))
+        self.code = code
+
+
+def _check(st):
+    if st != 0:
+        raise OracleError(st, lib().or_last_error().decode())
+
+
+class Fdata:
+    def __init__(self, path, nZ):
+        L = lib()
+        err = C.create_string_buffer(512)
+        nz = np.ascontiguousarray(nZ, dtype=np.int32)
+        self.h = L.or_load_fdata(path.encode(), len(nz), nz, err, 512)
+        if not self.h:
+            raise OracleError(2, err.value.decode())
+        self.nZ = list(nZ)
+
+    def norb(self, isp):
+        return lib().or_species_norb(self.h, isp)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_free_fdata(self.h)
+            self.h = None
+
+
+class System:
+    """One structure with its neighbor maps, mirroring T_structure."""
+
+    def __init__(self, fd: Fdata, ratom, imass, lattice, icluster=0, threads=1):
+        L = lib()
+        self.fd = fd
+        self.ratom = np.ascontiguousarray(ratom, dtype=np.float64).reshape(-1, 3)
+        self.imass = np.ascontiguousarray(imass, dtype=np.int32)
+        self.lattice = np.ascontiguousarray(lattice, dtype=np.float64).reshape(3, 3)
+        self.h = L.or_create_system(fd.h, len(self.imass), self.ratom.ravel(), self.imass,
+                                    self.lattice.ravel(), icluster)
+        if not self.h:
+            raise OracleError(1, "bad system")
+        self.threads = threads
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_free_system(self.h)
+            self.h = None
+
+    def neighbors(self):
+        L = lib()
+        _check(L.or_neighbors(self.h))
+        N = len(self.imass)
+        P = L.or_npairs(self.h)
+        T = L.or_ntriplets(self.h)
+        self.npairs, self.ntrip, self.nblock = P, T, L.or_nblock(self.h)
+        self.pair_off = np.zeros(N + 1, np.int32)
+        self.neigh_j = np.zeros(max(P, 1), np.int32)
+        self.neigh_b = np.zeros(max(P, 1), np.int32)
+        self.neigh_back = np.zeros(max(P, 1), np.int32)
+        self.neigh_self = np.zeros(N, np.int32)
+        self.blk_off = np.zeros(P + 1, np.int64)
+        L.or_get_pairs(self.h, self.pair_off, self.neigh_j, self.neigh_b, self.neigh_back, self.neigh_self,
+                       self.blk_off)
+        self.trip_off = np.zeros(N + 1, np.int32)
+        self.ci_j = np.zeros(max(T, 1), np.int32)
+        self.ci_b = np.zeros(max(T, 1), np.int32)
+        self.cj_j = np.zeros(max(T, 1), np.int32)
+        self.cj_b = np.zeros(max(T, 1), np.int32)
+        self.cneigh = np.zeros(max(T, 1), np.int32)
+        L.or_get_triplets(self.h, self.trip_off, self.ci_j, self.ci_b, self.cj_j, self.cj_b, self.cneigh)
+        return self
+
+    def assemble(self, with3c=True):
+        L = lib()
+        L.or_set_threads(self.threads)
+        nb = self.nblock
+        S, T, vb, vbo = (np.zeros(nb) for _ in range(4))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        if with3c:
+            _check(L.or_assemble_3c(self.h, vb))
+        return S, T, vb, vbo
+
+    def assemble_3c_only(self):
+        L = lib()
+        L.or_set_threads(self.threads)
+        vb = np.zeros(self.nblock)
+        _check(L.or_assemble_3c(self.h, vb))
+        return vb
+
+    def dassemble(self, rho, cape):
+        L = lib()
+        L.or_set_threads(self.threads)
+        nb, P, N = self.nblock, self.npairs, len(self.imass)
+        rho = np.ascontiguousarray(rho, np.float64)
+        cape = np.ascontiguousarray(cape, np.float64)
+        dS, dT = np.zeros(3 * nb), np.zeros(3 * nb)
+        ontop, atom = np.zeros(3 * P), np.zeros(3 * P)
+        _check(L.or_dassemble_2c(self.h, rho, dS, dT, ontop, atom))
+        fa, fb, fc = np.zeros(3 * N), np.zeros(3 * N), np.zeros(3 * N)
+        _check(L.or_dassemble_3c(self.h, rho, fa, fb, fc))
+        kin, vna, pul, ftot = (np.zeros(3 * N) for _ in range(4))
+        _check(L.or_build_forces(self.h, rho, cape, dS, dT, ontop, atom, fa, fb, fc, kin, vna, pul, ftot))
+        return dict(dS=dS, dT=dT, vna_ontop=ontop, vna_atom=atom, f3naa=fa, f3nab=fb, f3nac=fc,
+                    kinetic=kin, vna=vna, pulay=pul, ftot=ftot)
+
+
+def getMEs_2c(fd, isp, jsp, iint, x, nmu, nnu, isub=0):
+    out = np.zeros(nmu * nnu)
+    _check(lib().or_getMEs_2c(fd.h, isp, jsp, iint, isub, float(x), nmu, nnu, out))
+    return out.reshape(nnu, nmu).T
+
+
+def getDMEs_2c(fd, isp, jsp, iint, x, nmu, nnu, isub=0):
+    h, d = np.zeros(nmu * nnu), np.zeros(nmu * nnu)
+    _check(lib().or_getDMEs_2c(fd.h, isp, jsp, iint, isub, float(x), nmu, nnu, h, d))
+    return h.reshape(nnu, nmu).T, d.reshape(nnu, nmu).T
+
+
+def getMEs_3c(fd, isp, jsp, ksp, x, y, cost, nmu, nnu, iint=3, isub=0):
+    out = np.zeros(nmu * nnu)
+    _check(lib().or_getMEs_3c(fd.h, isp, jsp, ksp, iint, isub, float(x), float(y), nmu, nnu, float(cost), out))
+    return out.reshape(nnu, nmu).T
+
+
+def getDMEs_3c(fd, isp, jsp, ksp, x, y, cost, nmu, nnu, iint=3, isub=0):
+    h, dp, dx, dy = (np.zeros(nmu * nnu) for _ in range(4))
+    _check(lib().or_getDMEs_3c(fd.h, isp, jsp, ksp, iint, isub, float(x), float(y), nmu, nnu, float(cost),
+                               h, dp, dx, dy))
+    return tuple(a.reshape(nnu, nmu).T for a in (h, dp, dx, dy))
+
+
+def epsilon(r1, r2):
+    out = np.zeros(9)
+    lib().or_epsilon(np.ascontiguousarray(r1, np.float64), np.ascontiguousarray(r2, np.float64), out)
+    return out.reshape(3, 3).T  # spe(i, j)
+
+
+def rotate(fd, in1, in3, eps, mm):
+    nmu, nnu = mm.shape
+    out = np.zeros(nmu * nnu)
+    e = np.ascontiguousarray(np.asarray(eps).T.ravel())
+    lib().or_rotate(fd.h, in1, in3, e, nmu, nnu, np.ascontiguousarray(mm.T.ravel()), out)
+    return out.reshape(nnu, nmu).T

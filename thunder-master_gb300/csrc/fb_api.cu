@@ -1,0 +1,707 @@
+// fb_api.cu -- context, memory and the C ABI of libfbgpu (include/fbgpu.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fbgpu.h"
+#include "fb_fdata.h"
+#include "fb_launch.h"
+
+using namespace fb;
+
+namespace {
+
+// device buffer that grows on demand and never shrinks
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    if (cudaMalloc(&p, want) != cudaSuccess) return FB_ERR_CUDA;
+    cap = want;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+}  // namespace
+
+struct fb_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  std::string err;
+  long long launches = 0;
+  // Fdata
+  bool have_fdata = false;
+  FdataHost fdh;
+  DevBuf d_fd, d_tab2, d_tab3, d_lin, d_gxy;
+  // structure
+  int N = 0, icluster = 0, mbeta_max = 0;
+  std::vector<double> h_xl;
+  std::vector<int> h_isp, h_imgs;
+  double lattice[9] = {0};
+  DevBuf d_ratom, d_ratomf, d_isp, d_xl, d_xlf, d_imgs;
+  // neighbors
+  bool have_neigh = false;
+  int P = 0, T = 0;
+  long long nblock = 0;
+  std::vector<int> h_pair_off, h_trip_off;
+  DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v, d_r3f,
+      d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
+  DevBuf d_status, d_errinfo;
+  // blocks
+  DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT;
+  bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
+  unsigned assembled = 0, dassembled = 0;
+  // forces
+  DevBuf d_sumT, d_sumS, d_ontop, d_atomf, d_f3a, d_f3b, d_f3c, d_kin, d_vna, d_pul, d_ftot;
+};
+
+static int fail(fb_ctx *c, int code, const char *fmt, ...) {
+  char b[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(b, sizeof b, fmt, ap);
+  va_end(ap);
+  if (c) c->err = b;
+  return code;
+}
+
+#define CU(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(ctx, FB_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+#define CHK(call)                                                               \
+  do {                                                                          \
+    int st_ = (call);                                                           \
+    if (st_) return st_ == FB_ERR_CUDA ? fail(ctx, FB_ERR_CUDA, "allocation failed: %s", #call) : st_; \
+  } while (0)
+#define KL(call)                                                                                        \
+  do {                                                                                                  \
+    int e_ = (call);                                                                                    \
+    ctx->launches++;                                                                                    \
+    if (e_) return fail(ctx, FB_ERR_CUDA, "launch %s: %s", #call, cudaGetErrorString((cudaError_t)e_)); \
+  } while (0)
+
+static int sync_status(fb_ctx *ctx, unsigned *st) {
+  CU(cudaMemcpyAsync(st, ctx->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FB_OK;
+}
+
+static int status_error(fb_ctx *ctx, unsigned st) {
+  if (st & DEVERR_CLOSE) {
+    int info[3] = {0, 0, 0};
+    cudaMemcpy(info, ctx->d_errinfo.p, sizeof info, cudaMemcpyDeviceToHost);
+    return fail(ctx, FB_ERR_ATOMS_CLOSE, "atoms dangerously close: iatom %d jatom %d mbeta %d", info[0] + 1,
+                info[1] + 1, info[2]);
+  }
+  if (st & DEVERR_SELF) return fail(ctx, FB_ERR_NEIGH_SELF, "neigh_self missing");
+  if (st & DEVERR_BACK) return fail(ctx, FB_ERR_NEIGH_BACK, "neigh_back missing or found twice");
+  if (st & DEVERR_XLARGE) return fail(ctx, FB_ERR_X_TOO_LARGE, "interaction distance beyond table range");
+  if (st & DEVERR_TABLE) return fail(ctx, FB_ERR_TABLE, "table missing");
+  return FB_OK;
+}
+
+extern "C" {
+
+const char *fb_version(void) { return "fbgpu 0.1 sm_103a fp64"; }
+
+int fb_create(int device, fb_ctx **out) {
+  if (!out) return FB_ERR_ARG;
+  *out = nullptr;
+  fb_ctx *ctx = new fb_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return FB_ERR_CUDA;
+  }
+  ctx->stream = ctx->own;
+  if (ctx->d_status.ensure(sizeof(unsigned)) || ctx->d_errinfo.ensure(4 * sizeof(int))) {
+    delete ctx;
+    return FB_ERR_CUDA;
+  }
+  cudaMemset(ctx->d_status.p, 0, sizeof(unsigned));
+  *out = ctx;
+  return FB_OK;
+}
+
+void fb_destroy(fb_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  DevBuf *bufs[] = {&ctx->d_fd, &ctx->d_tab2, &ctx->d_tab3, &ctx->d_lin, &ctx->d_gxy, &ctx->d_ratom,
+                    &ctx->d_ratomf, &ctx->d_isp, &ctx->d_xl, &ctx->d_xlf, &ctx->d_imgs, &ctx->d_cnt,
+                    &ctx->d_pair_off, &ctx->d_neigh_j, &ctx->d_neigh_b, &ctx->d_neigh_self, &ctx->d_neigh_back,
+                    &ctx->d_pair_owner, &ctx->d_r3v, &ctx->d_r3f, &ctx->d_blk_off, &ctx->d_tcnt,
+                    &ctx->d_trip_off, &ctx->d_ci_j, &ctx->d_ci_b, &ctx->d_cj_j, &ctx->d_cj_b, &ctx->d_cneigh,
+                    &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
+                    &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
+                    &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
+                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot};
+  for (DevBuf *b : bufs) b->release();
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+}
+
+const char *fb_last_error(const fb_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+long long fb_kernel_launches(const fb_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int fb_set_stream(fb_ctx *ctx, void *stream) {
+  if (!ctx) return FB_ERR_ARG;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+  return FB_OK;
+}
+
+int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies, const int *nZ) {
+  if (!ctx || !fdata_dir || !nZ) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = fdata_read(fdata_dir, nspecies, nZ, ctx->fdh, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  FdataHost &f = ctx->fdh;
+  CHK(ctx->d_fd.ensure(sizeof(FdataDev)));
+  CHK(ctx->d_tab2.ensure(f.table2c.size() * sizeof(double)));
+  CHK(ctx->d_tab3.ensure(f.table3c.size() * sizeof(double)));
+  CHK(ctx->d_lin.ensure(f.lin.size()));
+  CHK(ctx->d_gxy.ensure(f.gxy.size() * sizeof(double)));
+  CU(cudaMemcpy(ctx->d_fd.p, &f.dev, sizeof(FdataDev), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_tab2.p, f.table2c.data(), f.table2c.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_tab3.p, f.table3c.data(), f.table3c.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_lin.p, f.lin.data(), f.lin.size(), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_gxy.p, f.gxy.data(), f.gxy.size() * sizeof(double), cudaMemcpyHostToDevice));
+  ctx->have_fdata = true;
+  ctx->have_neigh = false;
+  return FB_OK;
+}
+
+int fb_species_norb(const fb_ctx *ctx, int isp) {
+  if (!ctx || !ctx->have_fdata || isp < 1 || isp > ctx->fdh.nspecies) return -1;
+  return ctx->fdh.sp[isp - 1].norb;
+}
+
+// image list: every cell mbeta whose translation can bring some atom within
+// range of another; kept in increasing mbeta (the reference loop order)
+static void make_images(fb_ctx *ctx, const double *ratom) {
+  ctx->h_imgs.clear();
+  if (ctx->icluster == 1) {
+    ctx->h_imgs.push_back(0);
+    return;
+  }
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < ctx->N; i++)
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], ratom[3 * i + k]);
+      hi[k] = std::max(hi[k], ratom[3 * i + k]);
+    }
+  double D = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                       (hi[2] - lo[2]) * (hi[2] - lo[2]));
+  double rmax = 0.0;
+  for (int k = 0; k < ctx->fdh.nspecies; k++) rmax = std::max(rmax, ctx->fdh.sp[k].rcA);
+  double reach = std::max(2.0 * rmax, 0.5) + D + 1.0;
+  for (int mb = 0; mb <= ctx->mbeta_max; mb++) {
+    const double *L = &ctx->h_xl[3 * mb];
+    double l = std::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+    if (l < reach) ctx->h_imgs.push_back(mb);
+  }
+}
+
+int fb_set_structure(fb_ctx *ctx, int natoms, const double *ratom, const int *imass, const double *lattice,
+                     int icluster) {
+  if (!ctx || natoms < 1 || !ratom || !imass || (!lattice && icluster != 1)) return FB_ERR_ARG;
+  if (!ctx->have_fdata) return fail(ctx, FB_ERR_STATE, "fb_load_fdata first");
+  CU(cudaSetDevice(ctx->device));
+  ctx->N = natoms;
+  ctx->icluster = icluster;
+  ctx->h_isp.resize(natoms);
+  for (int i = 0; i < natoms; i++) {
+    if (imass[i] < 1 || imass[i] > ctx->fdh.nspecies)
+      return fail(ctx, FB_ERR_ARG, "imass(%d) = %d out of range", i + 1, imass[i]);
+    ctx->h_isp[i] = imass[i] - 1;
+  }
+  if (lattice) std::memcpy(ctx->lattice, lattice, sizeof ctx->lattice);
+  // make_cells (c.SYSTEM/make_cells.f90:112-144)
+  if (icluster == 1) {
+    ctx->mbeta_max = 0;
+    ctx->h_xl.assign(3, 0.0);
+  } else {
+    ctx->mbeta_max = (2 * P_mbox + 1) * (2 * P_mbox + 1) * (2 * P_mbox + 1) - 1;
+    ctx->h_xl.assign(3 * (ctx->mbeta_max + 1), 0.0);
+    int mb = 1;
+    for (int iz = -P_mbox; iz <= P_mbox; iz++)
+      for (int iy = -P_mbox; iy <= P_mbox; iy++)
+        for (int ix = -P_mbox; ix <= P_mbox; ix++)
+          if (!(ix == 0 && iy == 0 && iz == 0)) {
+            for (int k = 0; k < 3; k++)
+              ctx->h_xl[3 * mb + k] = (double)ix * ctx->lattice[k] + (double)iy * ctx->lattice[3 + k] +
+                                      (double)iz * ctx->lattice[6 + k];
+            mb++;
+          }
+  }
+  std::vector<float> xlf(ctx->h_xl.begin(), ctx->h_xl.end());
+  CHK(ctx->d_xl.ensure(ctx->h_xl.size() * sizeof(double)));
+  CHK(ctx->d_xlf.ensure(xlf.size() * sizeof(float)));
+  CHK(ctx->d_isp.ensure(natoms * sizeof(int)));
+  CU(cudaMemcpy(ctx->d_xl.p, ctx->h_xl.data(), ctx->h_xl.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_xlf.p, xlf.data(), xlf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_isp.p, ctx->h_isp.data(), natoms * sizeof(int), cudaMemcpyHostToDevice));
+  ctx->have_neigh = false;
+  return fb_update_positions(ctx, ratom);
+}
+
+int fb_update_positions(fb_ctx *ctx, const double *ratom) {
+  if (!ctx || !ratom) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N;
+  make_images(ctx, ratom);
+  std::vector<float> rf(ratom, ratom + 3 * N);
+  CHK(ctx->d_ratom.ensure(3 * N * sizeof(double)));
+  CHK(ctx->d_ratomf.ensure(3 * N * sizeof(float)));
+  CHK(ctx->d_imgs.ensure(ctx->h_imgs.size() * sizeof(int)));
+  CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_ratomf.p, rf.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_imgs.p, ctx->h_imgs.data(), ctx->h_imgs.size() * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_neigh = false;
+  return FB_OK;
+}
+
+static NeighArgs neigh_args(fb_ctx *ctx) {
+  NeighArgs a{};
+  a.N = ctx->N;
+  a.P = ctx->P;
+  a.nimg = (int)ctx->h_imgs.size();
+  a.ratom = ctx->d_ratom.as<double>();
+  a.ratomf = ctx->d_ratomf.as<float>();
+  a.isp = ctx->d_isp.as<int>();
+  a.fd = ctx->d_fd.as<FdataDev>();
+  a.xl = ctx->d_xl.as<double>();
+  a.xlf = ctx->d_xlf.as<float>();
+  a.imgs = ctx->d_imgs.as<int>();
+  a.cnt = ctx->d_cnt.as<int>();
+  a.pair_off = ctx->d_pair_off.as<int>();
+  a.neigh_j = ctx->d_neigh_j.as<int>();
+  a.neigh_b = ctx->d_neigh_b.as<int>();
+  a.neigh_self = ctx->d_neigh_self.as<int>();
+  a.neigh_back = ctx->d_neigh_back.as<int>();
+  a.pair_owner = ctx->d_pair_owner.as<int>();
+  a.r3v = ctx->d_r3v.as<double>();
+  a.r3f = ctx->d_r3f.as<float>();
+  a.tcnt = ctx->d_tcnt.as<int>();
+  a.trip_off = ctx->d_trip_off.as<int>();
+  a.ci_j = ctx->d_ci_j.as<int>();
+  a.ci_b = ctx->d_ci_b.as<int>();
+  a.cj_j = ctx->d_cj_j.as<int>();
+  a.cj_b = ctx->d_cj_b.as<int>();
+  a.cneigh = ctx->d_cneigh.as<int>();
+  a.tdst = ctx->d_tdst.as<int>();
+  a.status = ctx->d_status.as<unsigned>();
+  a.errinfo = ctx->d_errinfo.as<int>();
+  return a;
+}
+
+// everything after the pair lists exist on the device: neigh_back, block
+// offsets, common neighbors, block storage
+static int finish_neighbors(fb_ctx *ctx) {
+  int N = ctx->N, P = ctx->P;
+  // pair owner and block offsets from the host copy of the lists
+  std::vector<int> nj(P), owner(P), self(N);
+  CU(cudaMemcpyAsync(nj.data(), ctx->d_neigh_j.p, P * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(self.data(), ctx->d_neigh_self.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  std::vector<long long> blk(P + 1);
+  long long off = 0;
+  for (int i = 0; i < N; i++) {
+    if (self[i] < 0) return fail(ctx, FB_ERR_NEIGH_SELF, "no neigh_self for atom %d", i + 1);
+    int ni = ctx->fdh.sp[ctx->h_isp[i]].norb;
+    for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
+      owner[p] = i;
+      blk[p] = off;
+      off += (long long)ni * ctx->fdh.sp[ctx->h_isp[nj[p]]].norb;
+    }
+  }
+  blk[P] = off;
+  ctx->nblock = off;
+  CHK(ctx->d_pair_owner.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_blk_off.ensure((P + 1) * sizeof(long long)));
+  CHK(ctx->d_neigh_back.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
+  CHK(ctx->d_r3f.ensure(3 * P * sizeof(float) + 8));
+  CU(cudaMemcpyAsync(ctx->d_pair_owner.p, owner.data(), P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_blk_off.p, blk.data(), (P + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  NeighArgs a = neigh_args(ctx);
+  KL(launch_neigh_back(a, ctx->stream));
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  // common neighbors
+  CHK(ctx->d_tcnt.ensure(N * sizeof(int)));
+  a = neigh_args(ctx);
+  KL(launch_common(a, false, ctx->stream));
+  std::vector<int> tc(N);
+  CU(cudaMemcpyAsync(tc.data(), ctx->d_tcnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->h_trip_off.assign(N + 1, 0);
+  for (int i = 0; i < N; i++) ctx->h_trip_off[i + 1] = ctx->h_trip_off[i] + tc[i];
+  int T = ctx->h_trip_off[N];
+  ctx->T = T;
+  std::vector<int> talpha(T);
+  for (int i = 0; i < N; i++)
+    for (int t = ctx->h_trip_off[i]; t < ctx->h_trip_off[i + 1]; t++) talpha[t] = i;
+  size_t tb = (size_t)T * sizeof(int) + 4;
+  CHK(ctx->d_trip_off.ensure((N + 1) * sizeof(int)));
+  CHK(ctx->d_ci_j.ensure(tb));
+  CHK(ctx->d_ci_b.ensure(tb));
+  CHK(ctx->d_cj_j.ensure(tb));
+  CHK(ctx->d_cj_b.ensure(tb));
+  CHK(ctx->d_cneigh.ensure(tb));
+  CHK(ctx->d_tdst.ensure(tb));
+  CHK(ctx->d_talpha.ensure(tb));
+  CU(cudaMemcpyAsync(ctx->d_trip_off.p, ctx->h_trip_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_talpha.p, talpha.data(), T * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  a = neigh_args(ctx);
+  KL(launch_common(a, true, ctx->stream));
+  // block storage
+  size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
+  CHK(ctx->d_S.ensure(bb));
+  CHK(ctx->d_T.ensure(bb));
+  CHK(ctx->d_vb.ensure(bb));
+  CHK(ctx->d_vbo.ensure(bb));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_neigh = true;
+  ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = false;
+  ctx->assembled = ctx->dassembled = 0;
+  return FB_OK;
+}
+
+int fb_neighbors(fb_ctx *ctx) {
+  if (!ctx) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N;
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  CHK(ctx->d_cnt.ensure(N * sizeof(int)));
+  NeighArgs a = neigh_args(ctx);
+  KL(launch_neigh(a, false, ctx->stream));
+  std::vector<int> cnt(N);
+  CU(cudaMemcpyAsync(cnt.data(), ctx->d_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  ctx->h_pair_off.assign(N + 1, 0);
+  for (int i = 0; i < N; i++) ctx->h_pair_off[i + 1] = ctx->h_pair_off[i] + cnt[i];
+  int P = ctx->h_pair_off[N];
+  ctx->P = P;
+  CHK(ctx->d_pair_off.ensure((N + 1) * sizeof(int)));
+  CHK(ctx->d_neigh_j.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_neigh_b.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_neigh_self.ensure(N * sizeof(int)));
+  CU(cudaMemcpyAsync(ctx->d_pair_off.p, ctx->h_pair_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_neigh_self.p, 0xff, N * sizeof(int), ctx->stream));
+  a = neigh_args(ctx);
+  KL(launch_neigh(a, true, ctx->stream));
+  return finish_neighbors(ctx);
+}
+
+int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const int *neigh_b) {
+  if (!ctx || !neighn || !neigh_j || !neigh_b) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N;
+  ctx->h_pair_off.assign(N + 1, 0);
+  for (int i = 0; i < N; i++) {
+    if (neighn[i] < 0) return fail(ctx, FB_ERR_ARG, "neighn(%d) < 0", i + 1);
+    ctx->h_pair_off[i + 1] = ctx->h_pair_off[i] + neighn[i];
+  }
+  int P = ctx->h_pair_off[N];
+  ctx->P = P;
+  std::vector<int> nj(P), self(N, -1);
+  for (int i = 0; i < N; i++)
+    for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
+      if (neigh_j[p] < 1 || neigh_j[p] > N || neigh_b[p] < 0 || neigh_b[p] > ctx->mbeta_max)
+        return fail(ctx, FB_ERR_ARG, "neighbor %d of atom %d out of range", p - ctx->h_pair_off[i] + 1, i + 1);
+      nj[p] = neigh_j[p] - 1;
+      if (nj[p] == i && neigh_b[p] == 0) {
+        if (self[i] >= 0) return fail(ctx, FB_ERR_NEIGH_SELF, "neigh_self found twice for atom %d", i + 1);
+        self[i] = p - ctx->h_pair_off[i];
+      }
+    }
+  CHK(ctx->d_pair_off.ensure((N + 1) * sizeof(int)));
+  CHK(ctx->d_neigh_j.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_neigh_b.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_neigh_self.ensure(N * sizeof(int)));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_pair_off.p, ctx->h_pair_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_neigh_j.p, nj.data(), P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_neigh_b.p, neigh_b, P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_neigh_self.p, self.data(), N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  return finish_neighbors(ctx);
+}
+
+int fb_get_sizes(const fb_ctx *ctx, int *npairs, int *ntriplets, long long *nblock) {
+  if (!ctx || !ctx->have_neigh) return FB_ERR_STATE;
+  if (npairs) *npairs = ctx->P;
+  if (ntriplets) *ntriplets = ctx->T;
+  if (nblock) *nblock = ctx->nblock;
+  return FB_OK;
+}
+
+static int d2h_int(fb_ctx *ctx, int *dst, const DevBuf &src, size_t n, int add) {
+  if (!dst) return FB_OK;
+  CU(cudaMemcpyAsync(dst, src.p, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (add)
+    for (size_t k = 0; k < n; k++) dst[k] += add;
+  return FB_OK;
+}
+
+int fb_get_neighbors(fb_ctx *ctx, int *neighn, int *neigh_j, int *neigh_b, int *neigh_back, int *neigh_self,
+                     long long *blk_off) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (neighn)
+    for (int i = 0; i < ctx->N; i++) neighn[i] = ctx->h_pair_off[i + 1] - ctx->h_pair_off[i];
+  CHK(d2h_int(ctx, neigh_j, ctx->d_neigh_j, ctx->P, 1));
+  CHK(d2h_int(ctx, neigh_b, ctx->d_neigh_b, ctx->P, 0));
+  CHK(d2h_int(ctx, neigh_back, ctx->d_neigh_back, ctx->P, 1));
+  CHK(d2h_int(ctx, neigh_self, ctx->d_neigh_self, ctx->N, 1));
+  if (blk_off) {
+    CU(cudaMemcpy(blk_off, ctx->d_blk_off.p, (ctx->P + 1) * sizeof(long long), cudaMemcpyDeviceToHost));
+  }
+  return FB_OK;
+}
+
+int fb_get_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_common_b, int *jatom_common_j,
+                  int *jatom_common_b, int *neigh_common) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (ncommon)
+    for (int i = 0; i < ctx->N; i++) ncommon[i] = ctx->h_trip_off[i + 1] - ctx->h_trip_off[i];
+  CHK(d2h_int(ctx, iatom_common_j, ctx->d_ci_j, ctx->T, 1));
+  CHK(d2h_int(ctx, iatom_common_b, ctx->d_ci_b, ctx->T, 0));
+  CHK(d2h_int(ctx, jatom_common_j, ctx->d_cj_j, ctx->T, 1));
+  CHK(d2h_int(ctx, jatom_common_b, ctx->d_cj_b, ctx->T, 0));
+  CHK(d2h_int(ctx, neigh_common, ctx->d_cneigh, ctx->T, 1));
+  return FB_OK;
+}
+
+static AsmArgs asm_args(fb_ctx *ctx) {
+  AsmArgs a{};
+  a.N = ctx->N;
+  a.ntrip = ctx->T;
+  a.have_d = ctx->fdh.have_d;
+  a.ratom = ctx->d_ratom.as<double>();
+  a.isp = ctx->d_isp.as<int>();
+  a.fd = ctx->d_fd.as<FdataDev>();
+  a.table2c = ctx->d_tab2.as<double>();
+  a.table3c = ctx->d_tab3.as<double>();
+  a.lin = ctx->d_lin.as<unsigned char>();
+  a.gxy = ctx->d_gxy.as<double>();
+  a.xl = ctx->d_xl.as<double>();
+  a.pair_off = ctx->d_pair_off.as<int>();
+  a.neigh_j = ctx->d_neigh_j.as<int>();
+  a.neigh_b = ctx->d_neigh_b.as<int>();
+  a.neigh_self = ctx->d_neigh_self.as<int>();
+  a.neigh_back = ctx->d_neigh_back.as<int>();
+  a.blk_off = ctx->d_blk_off.as<long long>();
+  a.trip_alpha = ctx->d_talpha.as<int>();
+  a.ci_j = ctx->d_ci_j.as<int>();
+  a.ci_b = ctx->d_ci_b.as<int>();
+  a.cj_j = ctx->d_cj_j.as<int>();
+  a.cj_b = ctx->d_cj_b.as<int>();
+  a.tdst = ctx->d_tdst.as<int>();
+  a.S = ctx->d_S.as<double>();
+  a.T = ctx->d_T.as<double>();
+  a.vb = ctx->d_vb.as<double>();
+  a.vbo = ctx->d_vbo.as<double>();
+  a.rho = ctx->d_rho.as<double>();
+  a.cape = ctx->d_cape.as<double>();
+  a.dS = ctx->d_dS.as<double>();
+  a.dT = ctx->d_dT.as<double>();
+  a.sumT = ctx->d_sumT.as<double>();
+  a.sumS = ctx->d_sumS.as<double>();
+  a.ontop = ctx->d_ontop.as<double>();
+  a.atomf = ctx->d_atomf.as<double>();
+  a.f3naa = ctx->d_f3a.as<double>();
+  a.f3nab = ctx->d_f3b.as<double>();
+  a.f3nac = ctx->d_f3c.as<double>();
+  a.kin = ctx->d_kin.as<double>();
+  a.vna = ctx->d_vna.as<double>();
+  a.pul = ctx->d_pul.as<double>();
+  a.ftot = ctx->d_ftot.as<double>();
+  a.status = ctx->d_status.as<unsigned>();
+  return a;
+}
+
+int fb_assemble(fb_ctx *ctx, unsigned what) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if ((what & FB_VNA3C) && !(what & FB_VNA2C) && !ctx->have_vna2c)
+    return fail(ctx, FB_ERR_STATE, "assemble_vna_3c accumulates onto assemble_vna_2c blocks: assemble FB_VNA2C first");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  AsmArgs a = asm_args(ctx);
+  unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+  if (w2) KL(launch_assemble_2c(a, w2, ctx->stream));
+  if (what & FB_VNA3C) KL(launch_assemble_3c(a, ctx->stream));
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  if (what & FB_VNA2C) ctx->have_vna2c = true;
+  ctx->assembled |= what;
+  return FB_OK;
+}
+
+static DevBuf *block_buf(fb_ctx *ctx, int which, size_t *n) {
+  *n = (size_t)ctx->nblock;
+  switch (which) {
+    case FB_BLOCK_S: return &ctx->d_S;
+    case FB_BLOCK_T: return &ctx->d_T;
+    case FB_BLOCK_VNA: return &ctx->d_vb;
+    case FB_BLOCK_VNAO: return &ctx->d_vbo;
+    case FB_BLOCK_DS: *n *= 3; return ctx->have_dblocks ? &ctx->d_dS : nullptr;
+    case FB_BLOCK_DT: *n *= 3; return ctx->have_dblocks ? &ctx->d_dT : nullptr;
+    case FB_BLOCK_RHO: return ctx->have_rho ? &ctx->d_rho : nullptr;
+    case FB_BLOCK_CAPE: return ctx->have_rho ? &ctx->d_cape : nullptr;
+  }
+  return nullptr;
+}
+
+int fb_get_blocks(fb_ctx *ctx, int which, double *out) {
+  if (!ctx || !out) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  size_t n;
+  DevBuf *b = block_buf(ctx, which, &n);
+  if (!b) return fail(ctx, FB_ERR_STATE, "block set %d not available", which);
+  CU(cudaMemcpyAsync(out, b->p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FB_OK;
+}
+
+int fb_device_blocks(fb_ctx *ctx, int which, void **dptr) {
+  if (!ctx || !dptr) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  size_t n;
+  DevBuf *b = block_buf(ctx, which, &n);
+  if (!b) return fail(ctx, FB_ERR_STATE, "block set %d not available", which);
+  *dptr = b->p;
+  return FB_OK;
+}
+
+int fb_set_denmat(fb_ctx *ctx, const double *rho, const double *cape) {
+  if (!ctx || !rho) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  CU(cudaSetDevice(ctx->device));
+  size_t bb = (size_t)ctx->nblock * sizeof(double);
+  CHK(ctx->d_rho.ensure(bb + 8));
+  CHK(ctx->d_cape.ensure(bb + 8));
+  CU(cudaMemcpyAsync(ctx->d_rho.p, rho, bb, cudaMemcpyHostToDevice, ctx->stream));
+  if (cape) CU(cudaMemcpyAsync(ctx->d_cape.p, cape, bb, cudaMemcpyHostToDevice, ctx->stream));
+  else CU(cudaMemsetAsync(ctx->d_cape.p, 0, bb, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_rho = true;
+  return FB_OK;
+}
+
+int fb_dassemble(fb_ctx *ctx, unsigned what) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N, P = ctx->P;
+  size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
+  CHK(ctx->d_sumT.ensure(pb));
+  CHK(ctx->d_sumS.ensure(pb));
+  CHK(ctx->d_ontop.ensure(pb));
+  CHK(ctx->d_atomf.ensure(pb));
+  DevBuf *ab_bufs[] = {&ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c, &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot};
+  for (DevBuf *b : ab_bufs) CHK(b->ensure(ab));
+  bool keep = (what & FB_KEEP_DBLOCKS) != 0;
+  if (keep) {
+    size_t db = (size_t)3 * ctx->nblock * sizeof(double) + 8;
+    CHK(ctx->d_dS.ensure(db));
+    CHK(ctx->d_dT.ensure(db));
+  }
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_f3a.p, 0, ab, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_f3b.p, 0, ab, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_f3c.p, 0, ab, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_sumT.p, 0, pb, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_sumS.p, 0, pb, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_ontop.p, 0, pb, ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_atomf.p, 0, pb, ctx->stream));
+  AsmArgs a = asm_args(ctx);
+  a.keep_dblocks = keep;
+  unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+  if (w2) KL(launch_dassemble_2c(a, w2, ctx->stream));
+  if (what & FB_VNA3C) KL(launch_dassemble_3c(a, ctx->stream));
+  KL(launch_build_forces(a, what & FB_ALL, ctx->stream));
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
+  ctx->dassembled = what;
+  return FB_OK;
+}
+
+int fb_get_forces(fb_ctx *ctx, int which, double *out) {
+  if (!ctx || !out) return FB_ERR_ARG;
+  if (!ctx->dassembled) return fail(ctx, FB_ERR_STATE, "fb_dassemble first");
+  DevBuf *b = nullptr;
+  size_t n = (size_t)3 * ctx->N;
+  switch (which) {
+    case FB_F_TOT: b = &ctx->d_ftot; break;
+    case FB_F_KINETIC: b = &ctx->d_kin; break;
+    case FB_F_VNA: b = &ctx->d_vna; break;
+    case FB_F_PULAY: b = &ctx->d_pul; break;
+    case FB_F_F3NAA: b = &ctx->d_f3a; break;
+    case FB_F_F3NAB: b = &ctx->d_f3b; break;
+    case FB_F_F3NAC: b = &ctx->d_f3c; break;
+    case FB_F_VNA_ONTOP: b = &ctx->d_ontop; n = (size_t)3 * ctx->P; break;
+    case FB_F_VNA_ATOM: b = &ctx->d_atomf; n = (size_t)3 * ctx->P; break;
+    default: return fail(ctx, FB_ERR_ARG, "unknown force array %d", which);
+  }
+  CU(cudaMemcpyAsync(out, b->p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FB_OK;
+}
+
+int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T, double *vna, double *vnao) {
+  if (!ctx) return FB_ERR_ARG;
+  int st;
+  if (ratom && (st = fb_update_positions(ctx, ratom))) return st;
+  if ((st = fb_neighbors(ctx))) return st;
+  if ((st = fb_assemble(ctx, FB_ALL))) return st;
+  if (S && (st = fb_get_blocks(ctx, FB_BLOCK_S, S))) return st;
+  if (T && (st = fb_get_blocks(ctx, FB_BLOCK_T, T))) return st;
+  if (vna && (st = fb_get_blocks(ctx, FB_BLOCK_VNA, vna))) return st;
+  if (vnao && (st = fb_get_blocks(ctx, FB_BLOCK_VNAO, vnao))) return st;
+  return FB_OK;
+}
+
+}  // extern "C"

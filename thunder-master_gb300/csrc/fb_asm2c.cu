@@ -1,0 +1,173 @@
+// fb_asm2c.cu -- sm_103a kernel of the 2c assembly (S, T, vna 2c) and the force reduction.
+#include "fb_common.cuh"
+
+namespace fb {
+
+template <int PA, int PB, bool HASD>
+__device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned what, double *Xatom) {
+  using PL = Plan<PA, PB, K2C>;
+  using PLA = Plan<PA, PA, K2C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
+  int j = c.neigh_j[p];
+  int in1 = c.isp[i], in2 = c.isp[j];
+  double r1[3], r2[3], z, e[3][3];
+  pair_geom(c, i, p, r1, r2, z, e);
+  RotM R;
+  twister<HASD>(e, R);
+  const FdataDev &fd = *c.fd;
+  long long o = c.blk_off[p];
+  bool self = (i == j && c.neigh_b[p] == 0);
+  double w[7], v[NE > NEA ? NE : NEA], X[NA * NB];
+  int i0 = 0;
+  const Cell2cDev *last = nullptr;
+  auto weights = [&](const Cell2cDev &cell) {
+    if (z > cell.xmax * (1.0 + 1.0e-5)) atomicOr(c.status, DEVERR_XLARGE);
+    if (!last || !same_grid(*last, cell)) lagrange7(z, cell, i0, w, nullptr);
+    last = &cell;
+  };
+  if (what & 1u) {  // overlap
+    const Cell2cDev &cell = fd.c2[in1][in2][0];
+    weights(cell);
+    interp2c<NE>(c.table2c, cell, i0, w, v);
+    rotate_plan<PA, PB, K2C>(R, v, X);
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) c.S[o + q] = X[q];
+  }
+  if (what & 2u) {  // kinetic
+    const Cell2cDev &cell = fd.c2[in1][in2][1];
+    weights(cell);
+    interp2c<NE>(c.table2c, cell, i0, w, v);
+    rotate_plan<PA, PB, K2C>(R, v, X);
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) c.T[o + q] = X[q];
+  }
+  if (what & 4u) {  // vna: ontop L + R into blocko; zero block
+    double acc[NA * NB];
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) acc[q] = 0.0;
+    if (!self) {
+      const Cell2cDev &cL = fd.c2[in1][in2][2];
+      weights(cL);
+      interp2c<NE>(c.table2c, cL, i0, w, v);
+      rotate_plan<PA, PB, K2C>(R, v, X);
+#pragma unroll
+      for (int q = 0; q < NA * NB; q++) acc[q] = X[q] * P_eq2;
+      const Cell2cDev &cR = fd.c2[in1][in2][3];
+      weights(cR);
+      interp2c<NE>(c.table2c, cR, i0, w, v);
+      rotate_plan<PA, PB, K2C>(R, v, X);
+#pragma unroll
+      for (int q = 0; q < NA * NB; q++) acc[q] = acc[q] + X[q] * P_eq2;
+    }
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) c.vbo[o + q] = acc[q];
+    if (!self) {
+#pragma unroll
+      for (int q = 0; q < NA * NB; q++) c.vb[o + q] = 0.0;
+    }
+    // atom case <i|v(j)|i>, rotated with (in1, in1)
+    const Cell2cDev &cA = fd.c2[in1][in2][4];
+    weights(cA);
+    interp2c<NEA>(c.table2c, cA, i0, w, v);
+    double XA[NA * NA];
+    rotate_plan<PA, PA, K2C>(R, v, XA);
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) Xatom[q] = fma(XA[q], P_eq2, Xatom[q]);
+  }
+}
+
+template <int PA, bool HASD>
+__device__ __forceinline__ void pair_2c_dispatch(const Ctx2c &c, int i, int p, unsigned what, double *Xatom) {
+  int pb = c.fd->sp[c.isp[c.neigh_j[p]]].pattern;
+  if (pb == PAT_SP) pair_2c<PA, PAT_SP, HASD>(c, i, p, what, Xatom);
+  else if (pb == PAT_S) pair_2c<PA, PAT_S, HASD>(c, i, p, what, Xatom);
+  else if constexpr (HASD) pair_2c<PA, PAT_SPD, HASD>(c, i, p, what, Xatom);
+}
+
+template <int PA, bool HASD>
+__device__ void atom_2c(const Ctx2c &c, int i, int lane, unsigned what) {
+  constexpr int NA = pat_norb(PA);
+  double Xatom[NA * NA];
+#pragma unroll
+  for (int q = 0; q < NA * NA; q++) Xatom[q] = 0.0;
+  int p0 = c.pair_off[i], p1 = c.pair_off[i + 1];
+  for (int p = p0 + lane; p < p1; p += 32) pair_2c_dispatch<PA, HASD>(c, i, p, what, Xatom);
+  if (what & 4u) {
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) {
+      double v = Xatom[q];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      Xatom[q] = v;
+    }
+    if (lane == 0) {
+      long long os = c.blk_off[p0 + c.neigh_self[i]];
+#pragma unroll
+      for (int q = 0; q < NA * NA; q++) c.vb[os + q] = Xatom[q];
+    }
+  }
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_assemble_2c(Ctx2c c, unsigned what) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= c.N) return;
+  int pa = c.fd->sp[c.isp[warp]].pattern;
+  if (pa == PAT_SP) atom_2c<PAT_SP, HASD>(c, warp, lane, what);
+  else if (pa == PAT_S) atom_2c<PAT_S, HASD>(c, warp, lane, what);
+  else if constexpr (HASD) atom_2c<PAT_SPD, HASD>(c, warp, lane, what);
+}
+
+// build_forces, assembly terms (c.SYSTEM/M_build_forces.f90:172-588).  The
+// j-side contribution of pair (i -> j) is gathered by atom j through
+// neigh_back, which maps j's own pair list one-to-one onto the pairs whose
+// neighbor is j, so no atomics are needed.
+__global__ void k_build_forces(int N, const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
+                               const int *__restrict__ neigh_back, const double *__restrict__ sumT,
+                               const double *__restrict__ sumS, const double *__restrict__ ontop,
+                               const double *__restrict__ atomf, const double *__restrict__ f3a,
+                               const double *__restrict__ f3b, const double *__restrict__ f3c,
+                               double *__restrict__ kin, double *__restrict__ vna, double *__restrict__ pul,
+                               double *__restrict__ ftot, unsigned what) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double k[3] = {0, 0, 0}, v[3] = {0, 0, 0}, pu[3] = {0, 0, 0};
+  for (int p = pair_off[i]; p < pair_off[i + 1]; p++) {
+    int j = neigh_j[p];
+    int pb = pair_off[j] + neigh_back[p];  // pair (j -> i)
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      if (what & 2u) k[q] += -sumT[3 * p + q] + sumT[3 * pb + q];
+      if (what & 1u) pu[q] += -sumS[3 * p + q] + sumS[3 * pb + q];
+      if (what & 4u) v[q] += atomf[3 * p + q] + ontop[3 * p + q] - atomf[3 * pb + q] - ontop[3 * pb + q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    kin[3 * i + q] = k[q];
+    vna[3 * i + q] = v[q];
+    pul[3 * i + q] = pu[q];
+    double f3 = (what & 8u) ? f3a[3 * i + q] + f3b[3 * i + q] + f3c[3 * i + q] : 0.0;
+    ftot[3 * i + q] = k[q] + v[q] + f3 - pu[q];
+  }
+}
+
+int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
+  Ctx2c c = make2c(a);
+  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
+  if (a.have_d) k_assemble_2c<true><<<blocks, threads, 0, s>>>(c, what);
+  else k_assemble_2c<false><<<blocks, threads, 0, s>>>(c, what);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s) {
+  int threads = 128, blocks = (a.N + threads - 1) / threads;
+  k_build_forces<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_back, a.sumT, a.sumS, a.ontop,
+                                            a.atomf, a.f3naa, a.f3nab, a.f3nac, a.kin, a.vna, a.pul, a.ftot, what);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+}  // namespace fb

@@ -1,0 +1,367 @@
+// fb_common.cuh -- device contexts and shared per-pair / per-triplet
+// routines of the libfbgpu assembly kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "fb_device.cuh"
+#include "fb_launch.h"
+
+namespace fb {
+
+#define FB_LAUNCH_CHECK()                         \
+  do {                                            \
+    cudaError_t e_ = cudaGetLastError();          \
+    if (e_ != cudaSuccess) return (int)e_;        \
+  } while (0)
+
+// ===========================================================================
+// 2c assembly: assemble_S, assemble_T, assemble_vna_2c
+// (j.ASSEMBLERS/M_assemble_2c_Harris.f90:89-649).  One warp per atom i,
+// one lane per neighbor pair; the vna_atom terms of i's pairs are summed by
+// a warp reduction into i's self block.
+// ===========================================================================
+struct Ctx2c {
+  int N;
+  const double *ratom;
+  const int *isp;
+  const FdataDev *fd;
+  const double *table2c;
+  const double *xl;
+  const int *pair_off, *neigh_j, *neigh_b, *neigh_self;
+  const long long *blk_off;
+  double *S, *T, *vb, *vbo;
+  unsigned *status;
+};
+
+__device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
+                                          double e[3][3]) {
+  int j = c.neigh_j[p], mb = c.neigh_b[p];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r1[k] = c.ratom[3 * i + k];
+    r2[k] = __dadd_rn(c.ratom[3 * j + k], c.xl[3 * mb + k]);
+  }
+  z = dist_rn(r1, r2);
+  double sig[3];
+  if (z < 1.0e-05) {
+    sig[0] = 0.0;
+    sig[1] = 0.0;
+    sig[2] = 1.0;
+  } else {
+    double iz = 1.0 / z;
+#pragma unroll
+    for (int k = 0; k < 3; k++) sig[k] = (r2[k] - r1[k]) * iz;
+  }
+  epsilon_fn(r2, sig, e);
+}
+
+// interpolate one 2c cell at the weights (getMEs_Fdata_2c :378-401)
+template <int NE>
+__device__ __forceinline__ void interp2c(const double *__restrict__ tab, const Cell2cDev &cell, int i0,
+                                         const double w[7], double *v) {
+  const double *F = tab + cell.off + (long long)i0 * NE;
+#pragma unroll
+  for (int e = 0; e < NE; e++) v[e] = w[0] * __ldg(F + e);
+#pragma unroll
+  for (int s = 1; s < 7; s++)
+#pragma unroll
+    for (int e = 0; e < NE; e++) v[e] = fma(w[s], __ldg(F + s * NE + e), v[e]);
+}
+
+__device__ __forceinline__ bool same_grid(const Cell2cDev &a, const Cell2cDev &b) {
+  return a.nx == b.nx && a.dx == b.dx;
+}
+
+// ===========================================================================
+// 3c assembly: assemble_vna_3c (j.ASSEMBLERS/M_assemble_3c_Harris.f90:82-227)
+// One thread per triplet; bcna blocks accumulate by FP64 atomics into the
+// vna block of pair (iatom, mneigh).
+// ===========================================================================
+struct Ctx3c {
+  int N, T;
+  const double *ratom;
+  const int *isp;
+  const FdataDev *fd;
+  const double *table3c;
+  const unsigned char *lin;
+  const double *gxy;
+  const double *xl;
+  const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
+  const long long *blk_off;
+  double *vb;
+  // force pass
+  const double *rho;
+  double *f3naa, *f3nab, *f3nac;
+};
+
+struct TripGeom {
+  double r1[3], r2[3], rna[3], r21[3], rnabc[3], sighat[3], rhat[3], z, x, cost;
+  double e[3][3];
+};
+
+// set-up of M_assemble_3c_Harris.f90:154-189
+__device__ __forceinline__ void trip_geom(const Ctx3c &c, int t, int &ia, int &iat, int &jat, TripGeom &g) {
+  ia = c.trip_alpha[t];
+  iat = c.ci_j[t];
+  jat = c.cj_j[t];
+  int ib = c.ci_b[t], jb = c.cj_b[t];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    g.rna[k] = c.ratom[3 * ia + k];
+    g.r1[k] = __dadd_rn(c.ratom[3 * iat + k], c.xl[3 * ib + k]);
+    g.r2[k] = __dadd_rn(c.ratom[3 * jat + k], c.xl[3 * jb + k]);
+    g.r21[k] = __dsub_rn(g.r2[k], g.r1[k]);
+  }
+  g.z = dist_rn(g.r1, g.r2);
+  if (g.z < 1.0e-05) {
+    g.sighat[0] = 0.0;
+    g.sighat[1] = 0.0;
+    g.sighat[2] = 1.0;
+  } else {
+    double iz = 1.0 / g.z;
+#pragma unroll
+    for (int k = 0; k < 3; k++) g.sighat[k] = g.r21[k] * iz;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) g.rnabc[k] = __dsub_rn(g.rna[k], __dadd_rn(g.r1[k], g.r21[k] * 0.5));
+  g.x = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(g.rnabc[0], g.rnabc[0]), __dmul_rn(g.rnabc[1], g.rnabc[1])),
+                             __dmul_rn(g.rnabc[2], g.rnabc[2])));
+  if (g.x < 1.0e-05) {
+    g.rhat[0] = g.rhat[1] = g.rhat[2] = 0.0;
+  } else {
+    double ix = 1.0 / g.x;
+#pragma unroll
+    for (int k = 0; k < 3; k++) g.rhat[k] = g.rnabc[k] * ix;
+  }
+  g.cost = g.sighat[0] * g.rhat[0] + g.sighat[1] * g.rhat[1] + g.sighat[2] * g.rhat[2];
+  epsilon_fn(g.rhat, g.sighat, g.e);
+}
+
+// getMEs_Fdata_3c / getDMEs_Fdata_3c (e.FDATA/M_Fdata_3c.f90:293-846):
+// Legendre sum over the 5 theta tables of a bicubic (or, where the table is
+// flat, three-point linear) interpolation.  F, and with DERIV DpF, DxF, DyF,
+// are returned before the sin(theta) factor of the mvalue = 1 channels.
+template <int NE, bool DERIV>
+__device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, double x, double y, double cost,
+                                         double *F, double *DpF, double *DxF, double *DyF) {
+  double cost2 = cost * cost;
+  double pl[5] = {1.0, cost, 0.5 * (3.0 * cost2 - 1.0), 0.5 * cost * (5.0 * cost2 - 3.0),
+                  0.125 * (3.0 - cost2 * (30.0 - 35.0 * cost2))};
+  double dpl[5] = {0.0, 1.0, 3.0 * cost, (15.0 * cost2 - 3.0) * 0.5, 0.5 * cost * (35.0 * cost2 - 15.0)};
+  int ix = (int)(x / cell.dx) + 1;
+  int iy = (int)(y / cell.dy) + 1;
+  if (ix < 2) ix = 2;
+  if (iy < 2) iy = 2;
+  if (ix > cell.nx - 2) ix = cell.nx - 2;
+  if (iy > cell.ny - 2) iy = cell.ny - 2;
+  double px = x / cell.dx - ix + 1.0;
+  double py = y / cell.dy - iy + 1.0;
+  int nx = cell.nx;
+  long long node0 = (long long)(iy - 1) * nx + (ix - 1);  // 0-based node of (ix, iy)
+  const double *tab = c.table3c + cell.off;
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    F[e] = 0.0;
+    if (DERIV) DpF[e] = DxF[e] = DyF[e] = 0.0;
+  }
+  if (c.lin[cell.node_off + node0]) {
+    // METHOD 1, three-point linear (:406-410, :684-691)
+    double gx = c.gxy[2 * (cell.node_off + node0)], gy = c.gxy[2 * (cell.node_off + node0) + 1];
+    double w00 = 1.0 - px - py;
+    const double *T00 = tab + node0 * NTHETA * NE;
+    const double *T10 = tab + (node0 + 1) * NTHETA * NE;
+    const double *T01 = tab + (node0 + nx) * NTHETA * NE;
+#pragma unroll
+    for (int th = 0; th < NTHETA; th++)
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        double I = w00 * __ldg(T00 + th * NE + e) + px * __ldg(T10 + th * NE + e) + py * __ldg(T01 + th * NE + e);
+        F[e] = fma(pl[th], I, F[e]);
+        if (DERIV) {
+          DpF[e] = fma(dpl[th], I, DpF[e]);
+          DxF[e] = fma(pl[th], gx, DxF[e]);
+          DyF[e] = fma(pl[th], gy, DyF[e]);
+        }
+      }
+    return;
+  }
+  // METHOD 3, 16-point bicubic (:425-481, :721-798) as a tensor product of
+  // 4-point Lagrange weights
+  double wx[4], wy[4], dwx[4], dwy[4];
+  lagrange4(px, wx, DERIV ? dwx : nullptr);
+  lagrange4(py, wy, DERIV ? dwy : nullptr);
+  double W[16], Wx[16], Wy[16];
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      W[4 * j + k] = wx[k] * wy[j];
+      if (DERIV) {
+        Wx[4 * j + k] = dwx[k] * wy[j] / cell.dx;
+        Wy[4 * j + k] = wx[k] * dwy[j] / cell.dy;
+      }
+    }
+  const double *Tb = tab + (node0 - nx - 1) * NTHETA * NE;  // node (ix-1, iy-1)
+#pragma unroll
+  for (int th = 0; th < NTHETA; th++) {
+    double I[NE], Ix[NE], Iy[NE];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const double *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          double tv = __ldg(Tn + e);
+          if (j == 0 && k == 0) {
+            I[e] = W[0] * tv;
+            if (DERIV) {
+              Ix[e] = Wx[0] * tv;
+              Iy[e] = Wy[0] * tv;
+            }
+          } else {
+            I[e] = fma(W[4 * j + k], tv, I[e]);
+            if (DERIV) {
+              Ix[e] = fma(Wx[4 * j + k], tv, Ix[e]);
+              Iy[e] = fma(Wy[4 * j + k], tv, Iy[e]);
+            }
+          }
+        }
+      }
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      F[e] = fma(pl[th], I[e], F[e]);
+      if (DERIV) {
+        DpF[e] = fma(dpl[th], I[e], DpF[e]);
+        DxF[e] = fma(pl[th], Ix[e], DxF[e]);
+        DyF[e] = fma(pl[th], Iy[e], DyF[e]);
+      }
+    }
+  }
+}
+
+// ===========================================================================
+// 2c forces: Dassemble_S, Dassemble_T, Dassemble_vna_2c
+// (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:96-869).  One warp per atom, one
+// lane per pair.  Produces per pair: the kinetic and Pulay contractions
+// sum rho.dT and sum cape.dS (build_forces :234-301, :473-537), vna_ontop
+// and vna_atom; optionally the dS, dT Dblocks.
+// ===========================================================================
+struct CtxD2c {
+  Ctx2c b;
+  const double *rho, *cape;
+  double *dS, *dT;        // optional Dblocks
+  double *sumT, *sumS;    // per pair 3-vectors
+  double *ontop, *atomf;  // per pair 3-vectors
+  bool keep;
+};
+
+// value and x-derivative of one 2c cell (getDMEs_Fdata_2c, :446-600)
+template <int NE>
+__device__ __forceinline__ void interp2c_d(const double *__restrict__ tab, const Cell2cDev &cell, double z, bool tiny,
+                                           double *v, double *dv, unsigned *status) {
+  if (z > cell.xmax * (1.0 + 1.0e-5)) atomicOr(status, DEVERR_XLARGE);
+  if (tiny) {
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      v[e] = __ldg(tab + cell.off + e);
+      dv[e] = 0.0;
+    }
+    return;
+  }
+  int i0;
+  double w[7], dw[7];
+  lagrange7(z, cell, i0, w, dw);
+  const double *F = tab + cell.off + (long long)i0 * NE;
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    double f = __ldg(F + e);
+    v[e] = w[0] * f;
+    dv[e] = dw[0] * f;
+  }
+#pragma unroll
+  for (int s = 1; s < 7; s++)
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      double f = __ldg(F + s * NE + e);
+      v[e] = fma(w[s], f, v[e]);
+      dv[e] = fma(dw[s], f, dv[e]);
+    }
+}
+
+// vdsm(:,mu,nu) = -eta(:) dsm(mu,nu) when z > 1e-3
+// (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:237-241)
+template <int NE>
+__device__ __forceinline__ void vec2c(double z, const double *eta, const double *dv, double *vd) {
+  bool on = z > 1.0e-3;
+#pragma unroll
+  for (int e = 0; e < NE; e++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) vd[k + 3 * e] = on ? -eta[k] * dv[e] : 0.0;
+}
+
+template <int PA, int PB, int K, bool HASD>
+__device__ __forceinline__ void contract(const RotM &R, const DRotM &D, const double *blk, const double *v,
+                                         const double *vd, double out[3]) {
+  MolRho<PA, PB, K> G;
+  mol_rho<PA, PB, K>(R, D, blk, G);
+  constexpr int NE = Plan<PA, PB, K>::m.n;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    double s = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      s = fma(v[e], G.H[q][e], s);
+      s = fma(vd[q + 3 * e], G.G[e], s);
+    }
+    out[q] = s;
+  }
+}
+
+inline Ctx2c make2c(const AsmArgs &a) {
+  Ctx2c c;
+  c.N = a.N;
+  c.ratom = a.ratom;
+  c.isp = a.isp;
+  c.fd = a.fd;
+  c.table2c = a.table2c;
+  c.xl = a.xl;
+  c.pair_off = a.pair_off;
+  c.neigh_j = a.neigh_j;
+  c.neigh_b = a.neigh_b;
+  c.neigh_self = a.neigh_self;
+  c.blk_off = a.blk_off;
+  c.S = a.S;
+  c.T = a.T;
+  c.vb = a.vb;
+  c.vbo = a.vbo;
+  c.status = a.status;
+  return c;
+}
+
+inline Ctx3c make3c(const AsmArgs &a) {
+  Ctx3c c;
+  c.N = a.N;
+  c.T = a.ntrip;
+  c.ratom = a.ratom;
+  c.isp = a.isp;
+  c.fd = a.fd;
+  c.table3c = a.table3c;
+  c.lin = a.lin;
+  c.gxy = a.gxy;
+  c.xl = a.xl;
+  c.trip_alpha = a.trip_alpha;
+  c.ci_j = a.ci_j;
+  c.ci_b = a.ci_b;
+  c.cj_j = a.cj_j;
+  c.cj_b = a.cj_b;
+  c.tdst = a.tdst;
+  c.blk_off = a.blk_off;
+  c.vb = a.vb;
+  c.rho = a.rho;
+  c.f3naa = a.f3naa;
+  c.f3nab = a.f3nab;
+  c.f3nac = a.f3nac;
+  return c;
+}
+
+}  // namespace fb

@@ -1,0 +1,504 @@
+// fb_device.cuh -- device math of libfbgpu: local frames, Slater-Koster
+// rotations and their derivatives, and table interpolation weights.
+// Every routine names the reference routine whose mathematics it computes.
+#pragma once
+#include <utility>
+#include <type_traits>
+#include "fb_internal.h"
+
+namespace fb {
+
+// ---------------------------------------------------------------------------
+// compile-time loops
+// ---------------------------------------------------------------------------
+template <class F, int... I>
+__device__ __forceinline__ void sfor_impl(F &&f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void sfor(F &&f) {
+  sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+enum { K2C = 0, K3C = 1 };
+template <int PA, int PB, int K>
+struct Plan {
+  static constexpr MEMap m = (K == K3C) ? make_munu_3c(PA, PB) : make_munu(PA, PB);
+  static constexpr int NA = pat_norb(PA);
+  static constexpr int NB = pat_norb(PB);
+  // is ME e the first one feeding row mu of Y, block column shell sb?
+  static constexpr bool first_y(int e) {
+    for (int q = 0; q < e; q++)
+      if (m.mu[q] == m.mu[e] && orb_shell(m.nu[q]) == orb_shell(m.nu[e])) return false;
+    return true;
+  }
+  // is Y(mu, k2) structurally nonzero?
+  static constexpr bool ynz(int mu, int k2) {
+    for (int q = 0; q < m.n; q++)
+      if (m.mu[q] == mu && orb_shell(m.nu[q]) == orb_shell(k2)) return true;
+    return false;
+  }
+  // is X(k1, k2) structurally nonzero?
+  static constexpr bool xnz(int k1, int k2) {
+    int s1 = orb_shell(k1);
+    for (int mu = shell_off(s1); mu < shell_off(s1) + 2 * s1 + 1; mu++)
+      if (ynz(mu, k2)) return true;
+    return false;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// exact (uncontracted) FP64 helpers for integer-valued decisions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dist_rn(const double *a, const double *b) {
+  double d0 = __dsub_rn(b[0], a[0]), d1 = __dsub_rn(b[1], a[1]), d2 = __dsub_rn(b[2], a[2]);
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+}
+
+// ---------------------------------------------------------------------------
+// epsilon_function (b.FUNCTIONS/epsilon.f90:73-202): e[i][j] = spe(i+1,j+1)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void epsilon_fn(const double *r1, const double *r2, double e[3][3]) {
+  double r1m = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+  double r2m = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+  if (r2m < 1.0e-4) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) e[i][j] = (i == j) ? 1.0 : 0.0;
+    return;
+  }
+  double inv2 = 1.0 / r2m;
+  double zp[3] = {r2[0] * inv2, r2[1] * inv2, r2[2] * inv2};
+  double yp[3] = {0.0, 0.0, 0.0}, ypm = 0.0;
+  if (r1m > 1.0e-4) {
+    double inv1 = 1.0 / r1m;
+    double h0 = r1[0] * inv1, h1 = r1[1] * inv1, h2 = r1[2] * inv1;
+    yp[0] = zp[1] * h2 - zp[2] * h1;
+    yp[1] = zp[2] * h0 - zp[0] * h2;
+    yp[2] = zp[0] * h1 - zp[1] * h0;
+    ypm = sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]);
+  }
+  if (ypm < 1.0e-4) {
+    if (fabs(zp[0]) > 1.0e-4) {
+      yp[0] = -(zp[1] + zp[2]) / zp[0];
+      yp[1] = 1.0;
+      yp[2] = 1.0;
+    } else if (fabs(zp[1]) > 1.0e-4) {
+      yp[0] = 1.0;
+      yp[1] = -(zp[0] + zp[2]) / zp[1];
+      yp[2] = 1.0;
+    } else {
+      yp[0] = 1.0;
+      yp[1] = 1.0;
+      yp[2] = -(zp[0] + zp[1]) / zp[2];
+    }
+    ypm = sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]);
+  }
+  double iy = 1.0 / ypm;
+  yp[0] *= iy;
+  yp[1] *= iy;
+  yp[2] *= iy;
+  double xp[3] = {yp[1] * zp[2] - yp[2] * zp[1], yp[2] * zp[0] - yp[0] * zp[2], yp[0] * zp[1] - yp[1] * zp[0]};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    e[k][0] = xp[k];
+    e[k][1] = yp[k];
+    e[k][2] = zp[k];
+  }
+}
+
+__device__ __forceinline__ constexpr double levi(int i, int j, int k) {
+  return (i == j || j == k || i == k) ? 0.0
+         : ((i == 0 && j == 1) || (i == 1 && j == 2) || (i == 2 && j == 0)) ? 1.0
+                                                                            : -1.0;
+}
+
+// Depsilon_2c (b.FUNCTIONS/Depsilon_2c.f90:46-140): d[ix][imu][k]
+__device__ __forceinline__ void depsilon_2c(const double *r1, const double *r2, double z, const double e[3][3],
+                                            double d[3][3][3]) {
+#pragma unroll
+  for (int a = 0; a < 27; a++) (&d[0][0][0])[a] = 0.0;
+  if (z < 1.0e-5) return;
+  double c0 = r2[1] * r1[2] - r2[2] * r1[1];
+  double c1 = r2[2] * r1[0] - r2[0] * r1[2];
+  double c2 = r2[0] * r1[1] - r2[1] * r1[0];
+  double cm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  if (fabs(cm) < 1.0e-3) return;
+  double r2m2 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+  double r12 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+  double iz = 1.0 / z, ic = 1.0 / cm;
+#pragma unroll
+  for (int ix = 0; ix < 3; ix++)
+#pragma unroll
+    for (int imu = 0; imu < 3; imu++) {
+      double sum = levi(ix, imu, 0) * r2[0] + levi(ix, imu, 1) * r2[1] + levi(ix, imu, 2) * r2[2];
+      double dk = (ix == imu) ? 1.0 : 0.0;
+      d[ix][imu][0] = e[imu][0] * e[ix][2] * iz - e[imu][0] * ic * ic * (r2m2 * r1[ix] - r12 * r2[ix]) +
+                      iz * ic * (dk * (r2m2 - r12) - r1[imu] * r2[ix] - r2[imu] * r2[ix] + 2.0 * r1[ix] * r2[imu]);
+      d[ix][imu][1] = ic * (sum + e[imu][1] * ic * (r12 * r2[ix] - r2m2 * r1[ix]));
+      d[ix][imu][2] = -(dk - e[imu][2] * e[ix][2]) * iz;
+    }
+}
+
+// Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189): dA = deps/dratm,
+// dB = deps/dr1
+__device__ __forceinline__ void depsilon_3c(const double *r1, const double *r2, const double *r21, double z,
+                                            const double *ratm, const double *rnabc, const double e[3][3],
+                                            double dA[3][3][3], double dB[3][3][3]) {
+#pragma unroll
+  for (int a = 0; a < 27; a++) (&dA[0][0][0])[a] = 0.0, (&dB[0][0][0])[a] = 0.0;
+  double c0 = r21[1] * rnabc[2] - r21[2] * rnabc[1];
+  double c1 = r21[2] * rnabc[0] - r21[0] * rnabc[2];
+  double c2 = r21[0] * rnabc[1] - r21[1] * rnabc[0];
+  double cm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  if (fabs(cm) < 1.0e-3) return;
+  double r2m2 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+  double r1m2 = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+  double ram2 = ratm[0] * ratm[0] + ratm[1] * ratm[1] + ratm[2] * ratm[2];
+  double r12 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+  double r2a = r2[0] * ratm[0] + r2[1] * ratm[1] + r2[2] * ratm[2];
+  double r1a = r1[0] * ratm[0] + r1[1] * ratm[1] + r1[2] * ratm[2];
+  double ic = 1.0 / cm, iz = 1.0 / z;
+  double A1 = r1m2 + r2m2 - 2.0 * r12, A2 = r12 - r1m2 - r2a + r1a, A3 = r12 - r2m2 + r2a - r1a;
+  double B1 = r2a - r1a + r12 - r2m2, B2 = r2a + r1a - r12 - ram2, B3 = ram2 - 2.0 * r2a + r2m2;
+#pragma unroll
+  for (int ix = 0; ix < 3; ix++)
+#pragma unroll
+    for (int imu = 0; imu < 3; imu++) {
+      double sum = levi(ix, imu, 0) * (r2[0] - r1[0]) + levi(ix, imu, 1) * (r2[1] - r1[1]) +
+                   levi(ix, imu, 2) * (r2[2] - r1[2]);
+      dA[ix][imu][1] = ic * (sum - (e[imu][1] * ic) * (A1 * ratm[ix] + A2 * r2[ix] + A3 * r1[ix]));
+      double dk = (ix == imu) ? 1.0 : 0.0;
+      dB[ix][imu][2] = iz * (e[imu][2] * e[ix][2] - dk);
+      double sb = levi(ix, imu, 0) * (ratm[0] - r2[0]) + levi(ix, imu, 1) * (ratm[1] - r2[1]) +
+                  levi(ix, imu, 2) * (ratm[2] - r2[2]);
+      dB[ix][imu][1] = ic * (sb - (e[imu][1] * ic) * (B1 * ratm[ix] + B2 * r2[ix] + B3 * r1[ix]));
+    }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    dA[a][0][0] = e[2][2] * dA[a][1][1] - e[1][2] * dA[a][2][1];
+    dA[a][1][0] = e[0][2] * dA[a][2][1] - e[2][2] * dA[a][0][1];
+    dA[a][2][0] = e[1][2] * dA[a][0][1] - e[0][2] * dA[a][1][1];
+    dB[a][0][0] = e[2][2] * dB[a][1][1] - e[2][1] * dB[a][1][2] - e[1][2] * dB[a][2][1] + e[1][1] * dB[a][2][2];
+    dB[a][1][0] = e[0][2] * dB[a][2][1] - e[0][1] * dB[a][2][2] - e[2][2] * dB[a][0][1] + e[2][1] * dB[a][0][2];
+    dB[a][2][0] = e[1][2] * dB[a][0][1] - e[1][1] * dB[a][0][2] - e[0][2] * dB[a][1][1] + e[0][1] * dB[a][1][2];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// twister / Dtwister (c.SYSTEM/M_rotations.f90:221-313,
+// M_Drotations.f90:203-298).  p-orbital order (y, z, x).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr double amat_v(int ix, int jx, int imu) {
+  // include/constants.h:30-38 (symmetric in ix, jx)
+  return imu == 0   ? (((ix == 0 && jx == 1) || (ix == 1 && jx == 0)) ? 0.5 : 0.0)
+         : imu == 1 ? (((ix == 1 && jx == 2) || (ix == 2 && jx == 1)) ? 0.5 : 0.0)
+         : imu == 2 ? ((ix == jx) ? (ix == 2 ? 0.57735026918962573 : -0.28867513459481287) : 0.0)
+         : imu == 3 ? (((ix == 0 && jx == 2) || (ix == 2 && jx == 0)) ? 0.5 : 0.0)
+                    : ((ix == jx && ix < 2) ? (ix == 0 ? 0.5 : -0.5) : 0.0);
+}
+__host__ __device__ constexpr int pperm(int a) { return a == 0 ? 1 : (a == 1 ? 2 : 0); }
+
+struct RotM {
+  double p[3][3];
+  double d[5][5];
+};
+struct DRotM {
+  double p[3][3][3];  // [c][a][b]
+  double d[3][5][5];
+};
+
+template <bool HASD>
+__device__ __forceinline__ void twister(const double e[3][3], RotM &R) {
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b < 3; b++) R.p[a][b] = e[pperm(a)][pperm(b)];
+  if constexpr (HASD) {
+#pragma unroll
+    for (int imu = 0; imu < 5; imu++) {
+      double l11 = 0, l12 = 0, l13 = 0, l32 = 0, l33 = 0;
+#pragma unroll
+      for (int jx = 0; jx < 3; jx++)
+#pragma unroll
+        for (int ix = 0; ix < 3; ix++) {
+          constexpr double dummy = 0.0;
+          (void)dummy;
+          double a = amat_v(ix, jx, imu);
+          if (a != 0.0) {
+            l11 += a * e[jx][0] * e[ix][0];
+            l12 += a * e[jx][0] * e[ix][1];
+            l13 += a * e[jx][0] * e[ix][2];
+            l32 += a * e[jx][2] * e[ix][1];
+            l33 += a * e[jx][2] * e[ix][2];
+          }
+        }
+      R.d[imu][0] = 2.0 * l12;
+      R.d[imu][1] = 2.0 * l32;
+      R.d[imu][2] = 1.7320508075688772 * l33;
+      R.d[imu][3] = 2.0 * l13;
+      R.d[imu][4] = 2.0 * l11 + l33;
+    }
+  }
+}
+
+template <bool HASD>
+__device__ __forceinline__ void dtwister(const double e[3][3], const double dd[3][3][3], DRotM &D) {
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) D.p[c][a][b] = dd[c][pperm(a)][pperm(b)];
+  if constexpr (HASD) {
+#pragma unroll
+    for (int imu = 0; imu < 5; imu++)
+#pragma unroll
+      for (int kx = 0; kx < 3; kx++) {
+        double a12 = 0, a32 = 0, a33 = 0, a13 = 0, a11 = 0;
+#pragma unroll
+        for (int ix = 0; ix < 3; ix++)
+#pragma unroll
+          for (int jx = 0; jx < 3; jx++) {
+            double a = amat_v(jx, ix, imu);
+            if (a != 0.0) {
+              a12 += a * (dd[kx][ix][0] * e[jx][1] + e[ix][0] * dd[kx][jx][1]);
+              a32 += a * (dd[kx][ix][2] * e[jx][1] + e[ix][2] * dd[kx][jx][1]);
+              a33 += a * (dd[kx][ix][2] * e[jx][2] + e[ix][2] * dd[kx][jx][2]);
+              a13 += a * (dd[kx][ix][0] * e[jx][2] + e[ix][0] * dd[kx][jx][2]);
+              a11 += a * (dd[kx][ix][0] * e[jx][0] + e[ix][0] * dd[kx][jx][0]);
+            }
+          }
+        D.d[kx][imu][0] = 2.0 * a12;
+        D.d[kx][imu][1] = 2.0 * a32;
+        D.d[kx][imu][2] = 1.7320508075688772 * a33;
+        D.d[kx][imu][3] = 2.0 * a13;
+        D.d[kx][imu][4] = 2.0 * a11 + a33;
+      }
+  }
+}
+
+// element (k, m) of the rotation block of shell s (chooser,
+// M_rotations.f90:341-382); s = 0 gives the literal 1
+template <int S>
+__device__ __forceinline__ double Lrot(const RotM &R, int k, int m) {
+  if constexpr (S == 0) return 1.0;
+  else if constexpr (S == 1) return R.p[k][m];
+  else return R.d[k][m];
+}
+template <int S>
+__device__ __forceinline__ double DLrot(const DRotM &D, int c, int k, int m) {
+  if constexpr (S == 0) return 0.0;
+  else if constexpr (S == 1) return D.p[c][k][m];
+  else return D.d[c][k][m];
+}
+
+// rotate (M_rotations.f90:98-177): X = L M R^T with M given only at the ME
+// positions of the plan (v[e]), computed as Y = M R^T then X = L Y while
+// skipping every structurally zero product.
+template <int PA, int PB, int K>
+__device__ __forceinline__ void rotate_plan(const RotM &R, const double *v, double *X) {
+  using PL = Plan<PA, PB, K>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  double Y[NA * NB];
+  sfor<PL::m.n>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    constexpr int mu = PL::m.mu[e], nu = PL::m.nu[e];
+    constexpr int sb = orb_shell(nu), mb = orb_m(nu), ob = shell_off(sb);
+    constexpr bool first = PL::first_y(e);
+    sfor<2 * sb + 1>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      double r = Lrot<sb>(R, k, mb);
+      if constexpr (first) Y[mu * NB + ob + k] = v[e] * r;
+      else Y[mu * NB + ob + k] = fma(v[e], r, Y[mu * NB + ob + k]);
+    });
+  });
+  sfor<NA>([&](auto K1) {
+    constexpr int k1 = decltype(K1)::value;
+    constexpr int s1 = orb_shell(k1), m1 = orb_m(k1), o1 = shell_off(s1);
+    sfor<NB>([&](auto K2) {
+      constexpr int k2 = decltype(K2)::value;
+      if constexpr (!PL::xnz(k1, k2)) {
+        X[k1 + NA * k2] = 0.0;
+      } else {
+        double acc = 0.0;
+        bool have = false;
+        sfor<2 * s1 + 1>([&](auto MM) {
+          constexpr int mm = decltype(MM)::value;
+          if constexpr (PL::ynz(o1 + mm, k2)) {
+            double l = Lrot<s1>(R, m1, mm);
+            if (!have) acc = l * Y[(o1 + mm) * NB + k2];
+            else acc = fma(l, Y[(o1 + mm) * NB + k2], acc);
+            have = true;
+          }
+        });
+        X[k1 + NA * k2] = acc;
+      }
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Contraction of a rotated derivative with a density block, in the molecular
+// frame.  For X_c = dL_c M R^T + L M dR_c^T + L Md_c R^T (Dmatrix,
+// M_Drotations.f90:389-482), sum_{mu,nu} rho(mu,nu) X_c(mu,nu) equals
+//   sum_e [ M_e H_c(e) + Md_c(e) G(e) ]
+// with G = L^T rho R and H_c = dL_c^T rho R + L^T rho dR_c evaluated at the
+// ME positions e only.  This is the same sum in a different order.
+// ---------------------------------------------------------------------------
+template <int PA, int PB, int K>
+struct MolRho {
+  static constexpr int NA = pat_norb(PA), NB = pat_norb(PB), NE = Plan<PA, PB, K>::m.n;
+  double G[NE];
+  double H[3][NE];
+};
+
+template <int PA, int PB, int K>
+__device__ __forceinline__ void mol_rho(const RotM &R, const DRotM &D, const double *rho, MolRho<PA, PB, K> &out) {
+  using PL = Plan<PA, PB, K>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  // rhoR(mu, b) = sum_nu rho(mu, nu) R(nu, b) over the shell of b
+  double rR[NA * NB];
+  sfor<NA>([&](auto MU) {
+    constexpr int mu = decltype(MU)::value;
+    sfor<NB>([&](auto B) {
+      constexpr int b = decltype(B)::value;
+      constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
+      double acc = 0.0;
+      sfor<2 * sb + 1>([&](auto NU) {
+        constexpr int k = decltype(NU)::value;
+        double t = rho[mu + NA * (ob + k)] * Lrot<sb>(R, k, mb);
+        acc = (k == 0) ? t : acc + t;
+      });
+      rR[mu + NA * b] = acc;
+    });
+  });
+  sfor<PL::m.n>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
+    constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
+    double g = 0.0;
+    sfor<2 * sa + 1>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      g = fma(Lrot<sa>(R, k, ma), rR[(oa + k) + NA * b], g);
+    });
+    out.G[e] = g;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double h = 0.0;
+      if constexpr (sa > 0) {
+        sfor<2 * sa + 1>([&](auto KK) {
+          constexpr int k = decltype(KK)::value;
+          h = fma(DLrot<sa>(D, c, k, ma), rR[(oa + k) + NA * b], h);
+        });
+      }
+      if constexpr (sb > 0) {
+        // L^T rho dR at (a, b): sum_k L(k, ma) sum_nu rho(oa+k, nu) dR(nu, mb)
+        sfor<2 * sa + 1>([&](auto KK) {
+          constexpr int k = decltype(KK)::value;
+          double t = 0.0;
+          sfor<2 * sb + 1>([&](auto NU) {
+            constexpr int q = decltype(NU)::value;
+            t = fma(rho[(oa + k) + NA * (ob + q)], DLrot<sb>(D, c, q, mb), t);
+          });
+          h = fma(Lrot<sa>(R, k, ma), t, h);
+        });
+      }
+      out.H[c][e] = h;
+    }
+  });
+}
+
+// Explicit Drotate (M_Drotations.f90:102-153, Dmatrix :389-482):
+// Xd[c + 3*(mu + NA*nu)]
+template <int PA, int PB, int K>
+__device__ __forceinline__ void drotate_plan(const RotM &R, const DRotM &D, const double *v, const double *vd,
+                                             double *Xd) {
+  using PL = Plan<PA, PB, K>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+#pragma unroll
+  for (int q = 0; q < 3 * NA * NB; q++) Xd[q] = 0.0;
+  sfor<PL::m.n>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
+    constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
+    sfor<2 * sa + 1>([&](auto K1) {
+      constexpr int k1 = decltype(K1)::value;
+      sfor<2 * sb + 1>([&](auto K2) {
+        constexpr int k2 = decltype(K2)::value;
+        double l = Lrot<sa>(R, k1, ma), r = Lrot<sb>(R, k2, mb);
+        double lr = l * r;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          double t = lr * vd[c + 3 * e];
+          if constexpr (sa > 0) t = fma(DLrot<sa>(D, c, k1, ma) * r, v[e], t);
+          if constexpr (sb > 0) t = fma(l * DLrot<sb>(D, c, k2, mb), v[e], t);
+          Xd[c + 3 * ((oa + k1) + NA * (ob + k2))] += t;
+        }
+      });
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation weights
+// ---------------------------------------------------------------------------
+// 7-point Lagrange weights of getMEs_Fdata_2c (e.FDATA/M_Fdata_2c.f90:366-393)
+// with the stencil choice of the reference; i0 = 0-based first point.
+__device__ __forceinline__ void lagrange7(double x, const Cell2cDev &c, int &i0, double w[7], double *dw) {
+  int imid = (int)(x / c.dx) + 1;
+  int ileft = imid - 3;
+  if (ileft < 1) ileft = 1;
+  else if (imid + 3 > c.nx) ileft = c.nx - 6;
+  i0 = ileft - 1;
+  double t[7];
+#pragma unroll
+  for (int p = 0; p < 7; p++) t[p] = x - (double)(ileft - 1 + p) * c.dx;
+  // C_k = 1 / prod_{p != k} (k - p)
+  constexpr double Ck[7] = {1.0 / 720, -1.0 / 120, 1.0 / 48, -1.0 / 36, 1.0 / 48, -1.0 / 120, 1.0 / 720};
+  double pre[7], suf[7];
+  pre[0] = 1.0;
+#pragma unroll
+  for (int p = 1; p < 7; p++) pre[p] = pre[p - 1] * t[p - 1];
+  suf[6] = 1.0;
+#pragma unroll
+  for (int p = 5; p >= 0; p--) suf[p] = suf[p + 1] * t[p + 1];
+#pragma unroll
+  for (int k = 0; k < 7; k++) w[k] = pre[k] * suf[k] * (Ck[k] * c.inv_dx6);
+  if (dw) {
+    // derivative of prod_{p != k} t_p by running (value, derivative) pairs
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+      double P = 1.0, dP = 0.0;
+#pragma unroll
+      for (int p = 0; p < 7; p++)
+        if (p != k) {
+          dP = fma(dP, t[p], P);
+          P = P * t[p];
+        }
+      dw[k] = dP * (Ck[k] * c.inv_dx6);
+    }
+  }
+}
+
+// 4-point Lagrange weights on nodes -1, 0, 1, 2 (Abramowitz-Stegun 25.2.13,
+// the bicubic of getMEs_Fdata_3c, M_Fdata_3c.f90:425-481) and derivatives
+__device__ __forceinline__ void lagrange4(double p, double w[4], double *dw) {
+  double pm1 = p - 1.0, pm2 = p - 2.0, pp1 = p + 1.0;
+  w[0] = -p * pm1 * pm2 * (1.0 / 6.0);
+  w[1] = pp1 * pm1 * pm2 * 0.5;
+  w[2] = -pp1 * p * pm2 * 0.5;
+  w[3] = pp1 * p * pm1 * (1.0 / 6.0);
+  if (dw) {
+    double p2 = p * p;
+    dw[0] = -(3.0 * p2 - 6.0 * p + 2.0) * (1.0 / 6.0);
+    dw[1] = (3.0 * p2 - 4.0 * p - 1.0) * 0.5;
+    dw[2] = -(3.0 * p2 - 2.0 * p - 2.0) * 0.5;
+    dw[3] = (3.0 * p2 - 1.0) * (1.0 / 6.0);
+  }
+}
+
+}  // namespace fb

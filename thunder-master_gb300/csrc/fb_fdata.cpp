@@ -1,0 +1,466 @@
+// fb_fdata.cpp -- host reader of FIREBALL Fdata (libfbgpu).
+//
+// Parses the text files read by read_info (c.SYSTEM/M_species.f90:1057-1251),
+// read_Fdata_2c (e.FDATA/M_Fdata_2c.f90:149-272) and read_Fdata_3c
+// (e.FDATA/M_Fdata_3c.f90:143-264) with Fortran list-directed semantics:
+// every READ starts on a new record, may continue over records until its
+// item list is satisfied, and discards the rest of its last record.  A munu
+// unit that is re-opened on the file it already has open keeps its position
+// (the reference re-opens it once per cell), so a 3c munu file holds one
+// (mu, nu, mvalue) triple of records per theta cell.
+//
+// The tables are then repacked for the GPU: 2c values point-major (all MEs of
+// a grid point contiguous), 3c values node-major with the five theta terms
+// and all MEs of a grid node contiguous, and the gradient switch of
+// getMEs_Fdata_3c (M_Fdata_3c.f90:383-385) precomputed per node.  This file
+// is compiled with -ffp-contract=off so that switch is decided exactly as in
+// the reference.
+#include "fb_fdata.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "../../include/fbgpu.h"
+
+namespace fb {
+
+namespace {
+
+struct Text {
+  std::vector<std::string> rec;
+  size_t pos = 0;
+  bool load(const std::string &path) {
+    std::ifstream f(path);
+    if (!f) return false;
+    std::string line;
+    rec.clear();
+    while (std::getline(f, line)) {
+      if (!line.empty() && line.back() == '\r') line.pop_back();
+      rec.push_back(line);
+    }
+    pos = 0;
+    return true;
+  }
+  // one list-directed READ of n items
+  bool read(size_t n, std::vector<std::string> &out) {
+    out.clear();
+    while (out.size() < n) {
+      if (pos >= rec.size()) return false;
+      const std::string &r = rec[pos++];
+      size_t i = 0;
+      while (i < r.size() && out.size() < n) {
+        while (i < r.size() && (r[i] == ' ' || r[i] == '\t' || r[i] == ',')) i++;
+        if (i >= r.size()) break;
+        size_t j = i;
+        while (j < r.size() && r[j] != ' ' && r[j] != '\t' && r[j] != ',') j++;
+        out.push_back(r.substr(i, j - i));
+        i = j;
+      }
+    }
+    return true;
+  }
+  bool skip() {
+    if (pos >= rec.size()) return false;
+    pos++;
+    return true;
+  }
+  bool line(std::string &s) {
+    if (pos >= rec.size()) return false;
+    s = rec[pos++];
+    return true;
+  }
+};
+
+double to_d(const std::string &t) {
+  std::string s = t;
+  for (char &ch : s)
+    if (ch == 'D' || ch == 'd') ch = 'E';
+  return std::strtod(s.c_str(), nullptr);
+}
+
+bool read_ints(Text &t, size_t n, int *v) {
+  std::vector<std::string> tok;
+  if (!t.read(n, tok)) return false;
+  for (size_t k = 0; k < n; k++) v[k] = std::atoi(tok[k].c_str());
+  return true;
+}
+bool read_dbls(Text &t, size_t n, double *v) {
+  std::vector<std::string> tok;
+  if (!t.read(n, tok)) return false;
+  for (size_t k = 0; k < n; k++) v[k] = to_d(tok[k]);
+  return true;
+}
+
+std::string zz(int a) {
+  char b[8];
+  std::snprintf(b, sizeof b, "%02d", a);
+  return b;
+}
+
+struct Cell2 {
+  int nME = 0, nx = 0;
+  double xmax = 0;
+  std::vector<int> mu, nu, mv;
+  std::vector<double> F;  // F[ix + nx*e]
+};
+struct Cell3 {
+  int nME = 0, nx = 0, ny = 0;
+  double xmax = 0, ymax = 0;
+  std::vector<int> mu, nu, mv;
+  std::vector<double> F;  // F[ix + nx*(iy + ny*e)]
+};
+
+// a munu unit: re-opening the file already open keeps the position
+struct Unit {
+  std::string name;
+  Text t;
+  bool open(const std::string &path) {
+    if (path == name) return true;
+    name = path;
+    return t.load(path);
+  }
+};
+
+bool map_equal(const Cell2 &c, const MEMap &m) {
+  if (c.nME != m.n) return false;
+  for (int e = 0; e < m.n; e++)
+    if (c.mu[e] - 1 != m.mu[e] || c.nu[e] - 1 != m.nu[e]) return false;
+  return true;
+}
+bool map_equal3(const Cell3 &c, const MEMap &m) {
+  if (c.nME != m.n) return false;
+  for (int e = 0; e < m.n; e++)
+    if (c.mu[e] - 1 != m.mu[e] || c.nu[e] - 1 != m.nu[e] || c.mv[e] != m.mv[e]) return false;
+  return true;
+}
+
+}  // namespace
+
+int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &out, std::string &err) {
+  if (nspecies < 1 || nspecies > MAXSP) {
+    err = "nspecies out of range";
+    return FB_ERR_ARG;
+  }
+  out = FdataHost();
+  out.nspecies = nspecies;
+  for (int k = 0; k < nspecies; k++) out.sp[k].nZ = nZ[k];
+
+  // ---- read_info ----------------------------------------------------------
+  {
+    Text t;
+    std::string path = dir + "/info.dat", s;
+    if (!t.load(path)) {
+      err = "cannot open " + path;
+      return FB_ERR_IO;
+    }
+    int nsf = 0;
+    t.line(s);  // signature
+    if (!read_ints(t, 1, &nsf)) goto bad_info;
+    for (int b = 0; b < nsf; b++) {
+      int z = 0;
+      t.skip();
+      t.skip();
+      t.line(s);  // symbol
+      if (!read_ints(t, 1, &z)) goto bad_info;
+      int isp = -1;
+      for (int k = 0; k < nspecies; k++)
+        if (out.sp[k].nZ == z) {
+          isp = k;
+          break;
+        }
+      if (isp < 0) {
+        for (int l = 0; l < 12; l++) t.skip();
+        continue;
+      }
+      SpeciesHost &sp = out.sp[isp];
+      double xmass, q[8], rc[8], rcpp, ae;
+      int lpp[8];
+      if (!read_dbls(t, 1, &xmass) || !read_ints(t, 1, &sp.nssh) || sp.nssh < 1 || sp.nssh > 8) goto bad_info;
+      if (!read_ints(t, sp.nssh, sp.lssh) || !read_dbls(t, sp.nssh, q) || !read_dbls(t, sp.nssh, rc)) goto bad_info;
+      if (!read_ints(t, 1, &sp.nssh_pp) || sp.nssh_pp < 0 || sp.nssh_pp > 8) goto bad_info;
+      if (sp.nssh_pp > 0 && !read_ints(t, sp.nssh_pp, lpp)) goto bad_info;
+      if (!read_dbls(t, 1, &rcpp)) goto bad_info;
+      t.skip();
+      t.skip();
+      if (!read_dbls(t, 1, &ae)) goto bad_info;
+      t.skip();
+      sp.rcA = -99.0;
+      sp.norb = 0;
+      for (int k = 0; k < sp.nssh; k++) {
+        double r = rc[k] * P_abohr;  // M_species.f90:1164-1167
+        if (r > sp.rcA) sp.rcA = r;
+        sp.norb += 2 * sp.lssh[k] + 1;
+      }
+    }
+    for (int k = 0; k < nspecies; k++) {
+      SpeciesHost &sp = out.sp[k];
+      if (sp.nssh == 0) {
+        err = "species nZ=" + std::to_string(sp.nZ) + " not in info.dat";
+        return FB_ERR_IO;
+      }
+      if (sp.nssh == 1 && sp.lssh[0] == 0) sp.pattern = PAT_S;
+      else if (sp.nssh == 2 && sp.lssh[0] == 0 && sp.lssh[1] == 1) sp.pattern = PAT_SP;
+      else if (sp.nssh == 3 && sp.lssh[0] == 0 && sp.lssh[1] == 1 && sp.lssh[2] == 2) sp.pattern = PAT_SPD;
+      else {
+        err = "basis of species nZ=" + std::to_string(sp.nZ) + " is not s, sp or spd";
+        return FB_ERR_UNSUPPORTED;
+      }
+      if (sp.pattern == PAT_SPD) out.have_d = 1;
+    }
+    goto info_done;
+  bad_info:
+    err = "parse error in " + path;
+    return FB_ERR_IO;
+  }
+info_done:
+
+  // ---- read_Fdata_2c --------------------------------------------------------
+  for (int is = 0; is < nspecies; is++) {
+    for (int js = 0; js < nspecies; js++) {
+      std::string pz = zz(out.sp[is].nZ) + "." + zz(out.sp[js].nZ);
+      Text t;
+      std::string path = dir + "/2c." + pz + ".dat";
+      int ncell = 0;
+      if (!t.load(path)) {
+        err = "cannot open " + path;
+        return FB_ERR_IO;
+      }
+      if (!read_ints(t, 1, &ncell) || ncell < 1) {
+        err = "bad " + path;
+        return FB_ERR_IO;
+      }
+      std::vector<Cell2> cells(ncell);
+      int index[26][10];
+      for (auto &r : index)
+        for (int &v : r) v = -1;
+      Text td;
+      path = dir + "/2c." + pz + ".dir";
+      if (!td.load(path)) {
+        err = "cannot open " + path;
+        return FB_ERR_IO;
+      }
+      Unit u14;
+      for (int ic = 0; ic < ncell; ic++) {
+        std::vector<std::string> tok;
+        if (!td.read(7, tok)) {
+          err = "short " + path;
+          return FB_ERR_IO;
+        }
+        int iindex = std::atoi(tok[0].c_str()), itype = std::atoi(tok[1].c_str()), isub = std::atoi(tok[2].c_str());
+        Cell2 &c = cells[ic];
+        c.nME = std::atoi(tok[4].c_str());
+        c.nx = std::atoi(tok[5].c_str());
+        c.xmax = to_d(tok[6]);
+        if (itype < 1 || itype > 25 || isub < 0 || isub > 9 || c.nME < 1 || c.nx < 7) {
+          err = "bad entry in " + path;
+          return FB_ERR_IO;
+        }
+        index[itype][isub] = iindex;
+        c.F.resize((size_t)c.nx * c.nME);
+        Text tf;
+        std::string fpath = dir + "/" + tok[3];
+        if (!tf.load(fpath)) {
+          err = "cannot open " + fpath;
+          return FB_ERR_IO;
+        }
+        std::vector<double> row(c.nME);
+        for (int ix = 0; ix < c.nx; ix++) {
+          if (!read_dbls(tf, c.nME, row.data())) {
+            err = "short data " + fpath;
+            return FB_ERR_IO;
+          }
+          for (int e = 0; e < c.nME; e++) c.F[ix + (size_t)c.nx * e] = row[e];
+        }
+        std::string mpath = dir + "/" + zz(itype) + "_munu_2c." + pz + ".dat";
+        c.mu.resize(c.nME);
+        c.nu.resize(c.nME);
+        c.mv.resize(c.nME);
+        if (!u14.open(mpath) || !read_ints(u14.t, c.nME, c.mu.data()) || !read_ints(u14.t, c.nME, c.nu.data()) ||
+            !read_ints(u14.t, c.nME, c.mv.data())) {
+          err = "bad munu " + mpath;
+          return FB_ERR_IO;
+        }
+      }
+      // stage the five Harris interactions (isub = 0)
+      int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
+      for (int it = 1; it <= 5; it++) {
+        int k = index[it][0];
+        Cell2cDev &d = out.dev.c2[is][js][it - 1];
+        if (k < 1 || k > ncell) {
+          err = "2c table " + pz + " lacks interaction " + std::to_string(it);
+          return FB_ERR_TABLE;
+        }
+        const Cell2 &c = cells[k - 1];
+        MEMap m = make_munu(PA, it == 5 ? PA : PB);
+        if (!map_equal(c, m)) {
+          err = "2c table " + pz + " interaction " + std::to_string(it) + " has a non-canonical ME map";
+          return FB_ERR_UNSUPPORTED;
+        }
+        d.nx = c.nx;
+        d.nME = c.nME;
+        d.xmax = c.xmax;
+        d.dx = c.xmax / (c.nx - 1);  // M_Fdata_2c.f90:222
+        double dx3 = d.dx * d.dx * d.dx;
+        d.inv_dx6 = 1.0 / (dx3 * dx3);
+        d.off = (long long)out.table2c.size();
+        for (int ix = 0; ix < c.nx; ix++)
+          for (int e = 0; e < c.nME; e++) out.table2c.push_back(c.F[ix + (size_t)c.nx * e]);
+      }
+    }
+    // clPP.ZZ.dat is opened unconditionally (M_Fdata_2c.f90:252-258)
+    Text t;
+    std::string path = dir + "/clPP." + zz(out.sp[is].nZ) + ".dat";
+    if (!t.load(path)) {
+      err = "cannot open " + path;
+      return FB_ERR_IO;
+    }
+    for (int k = 0; k < out.sp[is].nssh_pp; k++) {
+      double cl;
+      if (!read_dbls(t, 1, &cl)) {
+        err = "short " + path;
+        return FB_ERR_IO;
+      }
+    }
+  }
+
+  // ---- read_Fdata_3c --------------------------------------------------------
+  for (int is = 0; is < nspecies; is++)
+    for (int js = 0; js < nspecies; js++)
+      for (int ks = 0; ks < nspecies; ks++) {
+        std::string pz = zz(out.sp[is].nZ) + "." + zz(out.sp[js].nZ) + "." + zz(out.sp[ks].nZ);
+        Text t;
+        std::string path = dir + "/3c." + pz + ".dat";
+        int ncell = 0;
+        if (!t.load(path)) {
+          err = "cannot open " + path;
+          return FB_ERR_IO;
+        }
+        if (!read_ints(t, 1, &ncell) || ncell < 1) {
+          err = "bad " + path;
+          return FB_ERR_IO;
+        }
+        std::vector<Cell3> cells(ncell);
+        int index[5][7][6];
+        for (auto &a : index)
+          for (auto &b : a)
+            for (int &v : b) v = -1;
+        Text td;
+        path = dir + "/3c." + pz + ".dir";
+        if (!td.load(path)) {
+          err = "cannot open " + path;
+          return FB_ERR_IO;
+        }
+        Unit u13;
+        for (int ic = 0; ic < ncell; ic++) {
+          std::vector<std::string> tok;
+          if (!td.read(10, tok)) {
+            err = "short " + path;
+            return FB_ERR_IO;
+          }
+          int iindex = std::atoi(tok[0].c_str()), itype = std::atoi(tok[1].c_str());
+          int isub = std::atoi(tok[2].c_str()), ith = std::atoi(tok[3].c_str());
+          Cell3 &c = cells[ic];
+          c.nME = std::atoi(tok[5].c_str());
+          c.nx = std::atoi(tok[6].c_str());
+          c.xmax = to_d(tok[7]);
+          c.ny = std::atoi(tok[8].c_str());
+          c.ymax = to_d(tok[9]);
+          if (itype < 1 || itype > 4 || isub < 0 || isub > 6 || ith < 1 || ith > 5 || c.nME < 1 || c.nx < 4 ||
+              c.ny < 4) {
+            err = "bad entry in " + path;
+            return FB_ERR_IO;
+          }
+          index[itype][isub][ith] = iindex;
+          c.F.resize((size_t)c.nx * c.ny * c.nME);
+          Text tf;
+          std::string fpath = dir + "/" + tok[4];
+          if (!tf.load(fpath)) {
+            err = "cannot open " + fpath;
+            return FB_ERR_IO;
+          }
+          std::vector<double> row(c.nME);
+          for (int iy = 0; iy < c.ny; iy++)
+            for (int ix = 0; ix < c.nx; ix++) {
+              if (!read_dbls(tf, c.nME, row.data())) {
+                err = "short data " + fpath;
+                return FB_ERR_IO;
+              }
+              for (int e = 0; e < c.nME; e++) c.F[ix + (size_t)c.nx * (iy + (size_t)c.ny * e)] = row[e];
+            }
+          std::string mpath = dir + "/" + zz(itype) + "_munu_3c." + pz + ".dat";
+          c.mu.resize(c.nME);
+          c.nu.resize(c.nME);
+          c.mv.resize(c.nME);
+          if (!u13.open(mpath) || !read_ints(u13.t, c.nME, c.mu.data()) || !read_ints(u13.t, c.nME, c.nu.data()) ||
+              !read_ints(u13.t, c.nME, c.mv.data())) {
+            err = "bad munu " + mpath;
+            return FB_ERR_IO;
+          }
+        }
+        // stage bcna (interaction 3, isub 0), theta 1..5
+        int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
+        MEMap m = make_munu_3c(PA, PB);
+        const Cell3 *th[NTHETA];
+        for (int it = 1; it <= NTHETA; it++) {
+          int k = index[3][0][it];
+          if (k < 1 || k > ncell) {
+            err = "3c table " + pz + " lacks bcna theta " + std::to_string(it);
+            return FB_ERR_TABLE;
+          }
+          th[it - 1] = &cells[k - 1];
+          if (!map_equal3(*th[it - 1], m)) {
+            err = "3c table " + pz + " has a non-canonical ME map";
+            return FB_ERR_UNSUPPORTED;
+          }
+          if (th[it - 1]->nx != th[0]->nx || th[it - 1]->ny != th[0]->ny) {
+            err = "3c table " + pz + ": theta cells on different grids";
+            return FB_ERR_UNSUPPORTED;
+          }
+        }
+        const Cell3 &c1 = *th[0];
+        Cell3cDev &d = out.dev.c3[is][js][ks];
+        d.nx = c1.nx;
+        d.ny = c1.ny;
+        d.nME = c1.nME;
+        d.xmax = c1.xmax;
+        d.ymax = c1.ymax;
+        d.dx = c1.xmax / (c1.nx - 1.0);  // M_Fdata_3c.f90:367-368
+        d.dy = c1.ymax / (c1.ny - 1.0);
+        d.off = (long long)out.table3c.size();
+        d.node_off = (long long)out.lin.size();
+        for (int iy = 0; iy < c1.ny; iy++)
+          for (int ix = 0; ix < c1.nx; ix++) {
+            for (int it = 0; it < NTHETA; it++)
+              for (int e = 0; e < c1.nME; e++)
+                out.table3c.push_back(th[it]->F[ix + (size_t)c1.nx * (iy + (size_t)c1.ny * e)]);
+            // gradient switch from theta 1, ME 1 (M_Fdata_3c.f90:383-385)
+            double gx = 0.0, gy = 0.0;
+            unsigned char lin = 0;
+            if (ix + 1 < c1.nx && iy + 1 < c1.ny) {
+              double f00 = c1.F[ix + (size_t)c1.nx * iy];
+              gx = (c1.F[(ix + 1) + (size_t)c1.nx * iy] - f00) / d.dx;
+              gy = (c1.F[ix + (size_t)c1.nx * (iy + 1)] - f00) / d.dy;
+              double gg = gx * gx + gy * gy;
+              lin = gg < 1.0e-6 ? 1 : 0;
+            }
+            out.lin.push_back(lin);
+            out.gxy.push_back(gx);
+            out.gxy.push_back(gy);
+          }
+      }
+
+  out.dev.nspecies = nspecies;
+  out.dev.have_d = out.have_d;
+  for (int k = 0; k < nspecies; k++) {
+    out.dev.sp[k].pattern = out.sp[k].pattern;
+    out.dev.sp[k].norb = out.sp[k].norb;
+    out.dev.sp[k].rcA = out.sp[k].rcA;
+  }
+  return FB_OK;
+}
+
+}  // namespace fb

@@ -1,0 +1,26 @@
+// fb_fdata.h -- host reader of the FIREBALL Fdata text format (libfbgpu).
+#pragma once
+#include <string>
+#include <vector>
+#include "fb_internal.h"
+
+namespace fb {
+
+struct SpeciesHost {
+  int nZ = 0, nssh = 0, norb = 0, pattern = -1, nssh_pp = 0;
+  int lssh[8] = {0};
+  double rcA = 0.0;
+};
+
+struct FdataHost {
+  int nspecies = 0, have_d = 0;
+  SpeciesHost sp[MAXSP];
+  std::vector<double> table2c, table3c, gxy;
+  std::vector<unsigned char> lin;
+  FdataDev dev{};
+};
+
+// read_info + read_Fdata_2c + read_Fdata_3c; returns an FB_ERR_* status
+int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &out, std::string &err);
+
+}  // namespace fb

@@ -1,0 +1,60 @@
+// fb_launch.h -- kernel launchers of libfbgpu (host side of fb_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "fb_internal.h"
+
+namespace fb {
+
+struct NeighArgs {
+  int N, P, nimg;
+  const double *ratom;
+  const float *ratomf;
+  const int *isp;
+  const FdataDev *fd;
+  const double *xl;
+  const float *xlf;
+  const int *imgs;
+  int *cnt;
+  const int *pair_off;
+  int *neigh_j, *neigh_b, *neigh_self, *neigh_back;
+  const int *pair_owner;
+  double *r3v;
+  float *r3f;
+  int *tcnt;
+  const int *trip_off;
+  int *ci_j, *ci_b, *cj_j, *cj_b, *cneigh, *tdst;
+  unsigned *status;
+  int *errinfo;
+};
+
+struct AsmArgs {
+  int N, ntrip, have_d;
+  const double *ratom;
+  const int *isp;
+  const FdataDev *fd;
+  const double *table2c, *table3c, *gxy;
+  const unsigned char *lin;
+  const double *xl;
+  const int *pair_off, *neigh_j, *neigh_b, *neigh_self, *neigh_back;
+  const long long *blk_off;
+  const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
+  double *S, *T, *vb, *vbo;
+  const double *rho, *cape;
+  double *dS, *dT;
+  bool keep_dblocks;
+  double *sumT, *sumS, *ontop, *atomf;
+  double *f3naa, *f3nab, *f3nac;
+  double *kin, *vna, *pul, *ftot;
+  unsigned *status;
+};
+
+int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s);
+int launch_neigh_back(const NeighArgs &a, cudaStream_t s);
+int launch_common(const NeighArgs &a, bool fill, cudaStream_t s);
+int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
+int launch_assemble_3c(const AsmArgs &a, cudaStream_t s);
+int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
+int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s);
+int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s);
+
+}  // namespace fb

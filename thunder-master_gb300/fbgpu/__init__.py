@@ -1,0 +1,245 @@
+"""fbgpu -- GB300 (sm_103a) FIREBALL Harris matrix-element assembly.
+
+Python host mirror of the reference's assembler interfaces over the C ABI of
+``libfbgpu.so`` (include/fbgpu.h).  The procedure names follow the Fortran
+modules they replace:
+
+=====================  =============================================  ====================================
+this module            reference procedure                            reference file
+=====================  =============================================  ====================================
+Context.read_Fdata     read_info + read_Fdata_2c + read_Fdata_3c      c.SYSTEM/M_species.f90:1057,
+                                                                      e.FDATA/M_Fdata_2c.f90:149,
+                                                                      e.FDATA/M_Fdata_3c.f90:143
+Context.set_structure  read_positions + make_cells                    c.SYSTEM/make_cells.f90:51
+Context.driver_neighbors  driver_neighbors                            c.SYSTEM/M_neighbors.f90:93
+Context.assemble_S     assemble_S                                     j.ASSEMBLERS/M_assemble_2c_Harris.f90:89
+Context.assemble_T     assemble_T                                     j.ASSEMBLERS/M_assemble_2c_Harris.f90:233
+Context.assemble_vna_2c  assemble_vna_2c                              j.ASSEMBLERS/M_assemble_2c_Harris.f90:435
+Context.assemble_vna_3c  assemble_vna_3c                              j.ASSEMBLERS/M_assemble_3c_Harris.f90:82
+Context.Dassemble_*    Dassemble_S / _T / _vna_2c / _vna_3c           k.DASSEMBLERS/M_Dassemble_{2c,3c}_Harris.f90
+Context.build_forces   build_forces (assembly terms)                  c.SYSTEM/M_build_forces.f90:172
+=====================  =============================================  ====================================
+
+There is no CPU fallback: every call runs on the GPU through the native
+library, and a missing library or GPU raises FBError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
+
+FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS = 1, 2, 4, 8, 15, 16
+BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7}
+FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
+         "vna_ontop": 7, "vna_atom": 8}
+STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
+          6: "ATOMS_CLOSE", 7: "NEIGH_SELF", 8: "NEIGH_BACK", 9: "CUDA", 10: "WATCHDOG",
+          11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED"}
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+# every symbol include/fbgpu.h declares, with its ctypes signature
+_SIGS = {
+    "fb_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "fb_destroy": (None, [C.c_void_p]),
+    "fb_last_error": (C.c_char_p, [C.c_void_p]),
+    "fb_version": (C.c_char_p, []),
+    "fb_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fb_load_fdata": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, _ip]),
+    "fb_species_norb": (C.c_int, [C.c_void_p, C.c_int]),
+    "fb_set_structure": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip, _dp, C.c_int]),
+    "fb_update_positions": (C.c_int, [C.c_void_p, _dp]),
+    "fb_neighbors": (C.c_int, [C.c_void_p]),
+    "fb_set_neighbors": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "fb_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "fb_get_neighbors": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
+    "fb_get_common": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
+    "fb_assemble": (C.c_int, [C.c_void_p, C.c_uint]),
+    "fb_get_blocks": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "fb_device_blocks": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "fb_set_denmat": (C.c_int, [C.c_void_p, _dp, C.c_void_p]),
+    "fb_dassemble": (C.c_int, [C.c_void_p, C.c_uint]),
+    "fb_get_forces": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "fb_assemble_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_kernel_launches": (C.c_longlong, [C.c_void_p]),
+}
+
+
+class FBError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("fbgpu status %d (%s): %s" % (code, STATUS.get(code, "?"), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path=LIBPATH):
+    """Load libfbgpu.so (raises FBError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FBError(9, "native library %s is missing: build it with fbgpu.build.build()" % path)
+    L = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One GPU assembly context: Fdata, one structure, its neighbor maps and
+    block sets (the parts of T_structure the assembly path owns)."""
+
+    def __init__(self, device=0):
+        L = load_library()
+        h = C.c_void_p()
+        st = L.fb_create(device, C.byref(h))
+        if st != 0:
+            raise FBError(st, "fb_create(device=%d) failed (no usable GPU?)" % device)
+        self.h = h
+        self.L = L
+        self.nspecies = 0
+        self.natoms = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            raise FBError(st, self.L.fb_last_error(self.h).decode())
+
+    # ---- setup -------------------------------------------------------------
+    def set_stream(self, stream_ptr):
+        self._check(self.L.fb_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def read_Fdata(self, fdata_dir, nZ):
+        nz = np.ascontiguousarray(nZ, np.int32)
+        self._check(self.L.fb_load_fdata(self.h, fdata_dir.encode(), len(nz), nz))
+        self.nspecies = len(nz)
+        self.norb_species = [self.L.fb_species_norb(self.h, k + 1) for k in range(len(nz))]
+
+    def set_structure(self, ratom, imass, lattice, icluster=0):
+        r = np.ascontiguousarray(ratom, np.float64).reshape(-1)
+        im = np.ascontiguousarray(imass, np.int32)
+        lat = np.ascontiguousarray(lattice if lattice is not None else np.eye(3), np.float64).reshape(-1)
+        self._check(self.L.fb_set_structure(self.h, len(im), r, im, lat, int(icluster)))
+        self.natoms = len(im)
+        self.imass = im.copy()
+
+    def update_positions(self, ratom):
+        self._check(self.L.fb_update_positions(self.h, np.ascontiguousarray(ratom, np.float64).reshape(-1)))
+
+    def driver_neighbors(self):
+        self._check(self.L.fb_neighbors(self.h))
+        return self.sizes()
+
+    def set_neighbors(self, neighn, neigh_j, neigh_b):
+        self._check(self.L.fb_set_neighbors(self.h, np.ascontiguousarray(neighn, np.int32),
+                                            np.ascontiguousarray(neigh_j, np.int32),
+                                            np.ascontiguousarray(neigh_b, np.int32)))
+        return self.sizes()
+
+    def sizes(self):
+        p, t, n = C.c_int(), C.c_int(), C.c_longlong()
+        self._check(self.L.fb_get_sizes(self.h, C.byref(p), C.byref(t), C.byref(n)))
+        self.npairs, self.ntrip, self.nblock = p.value, t.value, n.value
+        return self.npairs, self.ntrip, self.nblock
+
+    def neighbors(self):
+        """Neighbor maps with the reference's 1-based indices."""
+        N, P = self.natoms, self.npairs
+        neighn = np.zeros(N, np.int32)
+        nj, nb, nback = (np.zeros(max(P, 1), np.int32) for _ in range(3))
+        nself = np.zeros(N, np.int32)
+        blk = np.zeros(P + 1, np.int64)
+        self._check(self.L.fb_get_neighbors(self.h, _ptr(neighn), _ptr(nj), _ptr(nb), _ptr(nback), _ptr(nself),
+                                            _ptr(blk)))
+        return dict(neighn=neighn, neigh_j=nj[:P], neigh_b=nb[:P], neigh_back=nback[:P], neigh_self=nself,
+                    blk_off=blk)
+
+    def common_neighbors(self):
+        N, T = self.natoms, self.ntrip
+        nc = np.zeros(N, np.int32)
+        arrs = [np.zeros(max(T, 1), np.int32) for _ in range(5)]
+        self._check(self.L.fb_get_common(self.h, _ptr(nc), *[_ptr(a) for a in arrs]))
+        names = ["iatom_common_j", "iatom_common_b", "jatom_common_j", "jatom_common_b", "neigh_common"]
+        out = {k: a[:T] for k, a in zip(names, arrs)}
+        out["ncommon"] = nc
+        return out
+
+    # ---- assembly (j.ASSEMBLERS) ---------------------------------------------
+    def assemble(self, what=FB_ALL):
+        self._check(self.L.fb_assemble(self.h, what))
+
+    def assemble_S(self):
+        self.assemble(FB_S)
+
+    def assemble_T(self):
+        self.assemble(FB_T)
+
+    def assemble_vna_2c(self):
+        self.assemble(FB_VNA2C)
+
+    def assemble_vna_3c(self):
+        self.assemble(FB_VNA3C)
+
+    def blocks(self, which):
+        n = self.nblock * (3 if which in ("dS", "dT") else 1)
+        out = np.zeros(max(n, 1))
+        self._check(self.L.fb_get_blocks(self.h, BLOCK[which], out))
+        return out[:n]
+
+    def device_blocks(self, which):
+        p = C.c_void_p()
+        self._check(self.L.fb_device_blocks(self.h, BLOCK[which], C.byref(p)))
+        return p.value
+
+    # ---- forces (k.DASSEMBLERS, build_forces) --------------------------------
+    def set_denmat(self, rho, cape=None):
+        rho = np.ascontiguousarray(rho, np.float64)
+        cape = None if cape is None else np.ascontiguousarray(cape, np.float64)
+        self._check(self.L.fb_set_denmat(self.h, rho, _ptr(cape)))
+        self._cape_keep = cape
+
+    def Dassemble(self, what=FB_ALL, keep_dblocks=False):
+        self._check(self.L.fb_dassemble(self.h, what | (FB_KEEP_DBLOCKS if keep_dblocks else 0)))
+
+    def forces(self, which):
+        n = 3 * (self.npairs if which in ("vna_ontop", "vna_atom") else self.natoms)
+        out = np.zeros(max(n, 1))
+        self._check(self.L.fb_get_forces(self.h, FORCE[which], out))
+        return out[:n]
+
+    def build_forces(self):
+        """All force arrays of the assembly terms (after Dassemble)."""
+        return {k: self.forces(k) for k in FORCE}
+
+    def assemble_step(self, ratom, S, T, vna, vnao):
+        self._check(self.L.fb_assemble_step(self.h, _ptr(ratom), _ptr(S), _ptr(T), _ptr(vna), _ptr(vnao)))
+
+    def kernel_launches(self):
+        return int(self.L.fb_kernel_launches(self.h))

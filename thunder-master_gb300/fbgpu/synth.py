@@ -1,0 +1,536 @@
+"""Seeded synthetic Fdata and structures in FIREBALL's own on-disk formats.
+
+The reference ships no Fdata and no example inputs, so every workload is
+generated here, deterministically from a seed, and written in exactly the text
+formats the reference readers parse:
+
+* ``info.dat``          -- read by ``read_info`` (c.SYSTEM/M_species.f90:1057-1251)
+* ``2c.ZZ.ZZ.dat/.dir`` -- read by ``read_Fdata_2c`` (e.FDATA/M_Fdata_2c.f90:149-272)
+* ``NN_munu_2c.ZZ.ZZ.dat`` (mu, nu, mvalue lines, M_Fdata_2c.f90:236-245)
+* ``clPP.ZZ.dat``       -- opened unconditionally by read_Fdata_2c (:252-258)
+* ``3c.ZZ.ZZ.ZZ.dat/.dir`` and the data files, iy outer / ix inner
+  (e.FDATA/M_Fdata_3c.f90:192-231)
+* ``03_munu_3c.ZZ.ZZ.ZZ.dat`` holding one (mu, nu, mvalue) triple of lines per
+  theta cell, because the create step appends it once per theta
+  (p.THEORY/M_bcna_Harris.f90:258-273) and the reader re-opens the unit
+  without rewinding (M_Fdata_3c.f90:239-245).
+
+Matrix-element index maps follow ``make_munu`` / ``make_munu_atom``
+(c.SYSTEM/M_integrals_2c.f90:232-488) and ``make_munu_3c``
+(c.SYSTEM/M_integrals_3c.f90:230-587).
+
+Table values: every channel is a sum of three Gaussians times cubic
+polynomials with seeded coefficients.  The two pi channels (m = -1, +1) of a
+two-center table share coefficients so the physics is rotation invariant; the
+three-center channels are independent.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+P_ABOHR = 0.529177  # include/constants.h:2
+
+# interaction ids (include/interactions_2c.h:5-9, interactions_3c.h:8)
+P_OVERLAP, P_KINETIC, P_VNA_ONTOPL, P_VNA_ONTOPR, P_VNA_ATOM = 1, 2, 3, 4, 5
+P_BCNA = 3
+P_NTHETA = 5
+
+
+@dataclass
+class Species:
+    symbol: str
+    nZ: int
+    xmass: float
+    lssh: list            # angular momentum per shell
+    rcutoff: list         # bohr, per shell
+    qneutral: list
+    lssh_pp: list = field(default_factory=lambda: [0, 1])
+    rcutoff_pp: float = 1.5
+
+    @property
+    def norb(self) -> int:
+        return sum(2 * l + 1 for l in self.lssh)
+
+    @property
+    def rcA(self) -> float:
+        """Largest shell cutoff in Angstrom (M_species.f90:1180-1183)."""
+        return max(r * P_ABOHR for r in self.rcutoff)
+
+
+def si(rc=5.0):
+    return Species("Si", 14, 28.0855, [0, 1], [rc, rc], [2.0, 2.0])
+
+
+def c(rc=5.0):
+    return Species("C", 6, 12.011, [0, 1], [rc, rc], [2.0, 2.0])
+
+
+def o(rc=4.0):
+    return Species("O", 8, 15.999, [0, 1], [rc, rc], [2.0, 4.0])
+
+
+def h(rc=4.0):
+    return Species("H", 1, 1.008, [0], [rc], [1.0], lssh_pp=[0])
+
+
+def ti(rc=5.0):
+    """A transition-metal-like species with an s, p, d basis (9 orbitals),
+    used only to exercise the d-orbital rotation paths."""
+    return Species("Ti", 22, 47.867, [0, 1, 2], [rc, rc, rc], [2.0, 0.0, 2.0],
+                   lssh_pp=[0, 1, 2])
+
+
+# ---------------------------------------------------------------------------
+# matrix-element maps
+# ---------------------------------------------------------------------------
+def make_munu(ls_i, ls_j):
+    """(mu, nu, mvalue) lists of the 2c sigma/pi/delta map.
+
+    Follows make_munu (c.SYSTEM/M_integrals_2c.f90:232-340): for every shell
+    pair the channels m = -min(l1,l2)..min(l1,l2) sit at n1 + m, n2 + m where
+    n1, n2 are the m=0 positions of the two shells.
+    """
+    mu, nu, mv = [], [], []
+    n1 = 0
+    for l1 in ls_i:
+        n1 += l1 + 1
+        n2 = 0
+        for l2 in ls_j:
+            n2 += l2 + 1
+            for m in range(-min(l1, l2), min(l1, l2) + 1):
+                mu.append(n1 + m)
+                nu.append(n2 + m)
+                mv.append(0)
+            n2 += l2
+        n1 += l1
+    return mu, nu, mv
+
+
+def make_munu_3c(ls_i, ls_j):
+    """(mu, nu, mvalue) lists of the 3c map (c.SYSTEM/M_integrals_3c.f90:230-587):
+    the 2c map with mvalue 0, then the mvalue 1 and mvalue 2 channels."""
+    mu, nu, mv = make_munu(ls_i, ls_j)
+    n1 = 0
+    for l1 in ls_i:
+        n1 += l1 + 1
+        n2 = 0
+        for l2 in ls_j:
+            n2 += l2 + 1
+            if l1 == 0 and l2 != 0:
+                mu.append(n1); nu.append(n2 + 1); mv.append(1)
+            if l1 == 1:
+                mu.append(n1 + 1); nu.append(n2); mv.append(1)
+                if l2 != 0:
+                    mu.append(n1); nu.append(n2 + 1); mv.append(1)
+                if l2 == 2:
+                    mu.append(n1 + 1); nu.append(n2 + 2); mv.append(1)
+                    mu.append(n1 - 1); nu.append(n2 - 2); mv.append(1)
+            if l1 == 2:
+                mu.append(n1 + 1); nu.append(n2); mv.append(1)
+                if l2 != 0:
+                    mu.append(n1); nu.append(n2 + 1); mv.append(1)
+                    mu.append(n1 - 2); nu.append(n2 - 1); mv.append(1)
+                    mu.append(n1 + 2); nu.append(n2 + 1); mv.append(1)
+                if l2 == 2:
+                    mu.append(n1 + 1); nu.append(n2 + 2); mv.append(1)
+                    mu.append(n1 - 1); nu.append(n2 - 2); mv.append(1)
+            n2 += l2
+        n1 += l1
+    n1 = 0
+    for l1 in ls_i:
+        n1 += l1 + 1
+        n2 = 0
+        for l2 in ls_j:
+            n2 += l2 + 1
+            if l1 == 2:
+                mu.append(n1 + 2); nu.append(n2); mv.append(2)
+            if l2 == 2:
+                mu.append(n1); nu.append(n2 + 2); mv.append(2)
+            n2 += l2
+        n1 += l1
+    return mu, nu, mv
+
+
+def _orbital_lm(ls):
+    """(shell index, l, m) for each orbital of a species, m = -l..l."""
+    out = []
+    for issh, l in enumerate(ls):
+        for m in range(-l, l + 1):
+            out.append((issh, l, m))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# table functions
+# ---------------------------------------------------------------------------
+_ALPHA = (3.0, 7.0, 16.0)
+
+# Sign of each real orbital under a rotation by pi about the molecular x
+# axis (x -> x, y -> -y, z -> -z); this maps the frame of pair (A, B) onto
+# the frame of the reversed pair (B, A).  Orbital order in a shell is
+# m = -l..l: p = (y, z, x), d = (xy, yz, z^2, xz, x^2-y^2).
+_FLIP = {0: (1,), 1: (-1, -1, 1), 2: (-1, 1, 1, -1, 1)}
+
+
+def _flip_sign(orb):
+    _, l, m = orb
+    return _FLIP[l][m + l]
+
+
+def _f1d(coef, t, odd):
+    """Sum of three Gaussians times cubics in t in [0, 1]."""
+    val = np.zeros_like(t)
+    for g, a in enumerate(_ALPHA):
+        c0, c1, c2, c3 = coef[4 * g: 4 * g + 4]
+        val += (c0 + c1 * t + c2 * t * t + c3 * t ** 3) * np.exp(-a * t * t)
+    if odd:
+        val = val * t
+    return val
+
+
+def _f2d(coef, u, v, scale):
+    val = np.zeros(np.broadcast(u, v).shape)
+    for g in range(3):
+        cc = coef[10 * g: 10 * g + 10]
+        poly = (cc[0] + cc[1] * u + cc[2] * v + cc[3] * u * u + cc[4] * u * v
+                + cc[5] * v * v + cc[6] * u ** 3 + cc[7] * u * u * v
+                + cc[8] * u * v * v + cc[9] * v ** 3)
+        val = val + poly * np.exp(-_ALPHA[g] * u * u - 0.6 * _ALPHA[g] * v * v)
+    return scale * val
+
+
+def _seed_of(*keys):
+    h = 1469598103934665603
+    for k in keys:
+        for ch in str(k).encode():
+            h = ((h ^ ch) * 1099511628211) & ((1 << 63) - 1)
+        h = ((h ^ 0x2C) * 1099511628211) & ((1 << 63) - 1)
+    return h
+
+
+_AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P_VNA_ATOM: 0.3}
+
+
+def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi):
+    """Seeded channel function of the canonical orientation."""
+    sa, la, ma = oa
+    sb, lb, mb = ob
+    mkey = ma if asym_pi else abs(ma)
+    rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey))
+    coef = rng.normal(0.0, 1.0, 12)
+    return _AMP2[itype] * _f1d(coef, t, (la + lb) % 2 == 1)
+
+
+def _canonical(zA, oa, zB, ob):
+    return (zA, oa[0], oa[1]) <= (zB, ob[0], ob[1])
+
+
+def table2c(seed, itype, A, B, oa, ob, t, asym_pi=False):
+    """Values of one 2c channel <A oa| O |B ob> on the grid t.
+
+    Channels of the reversed pair are generated from the canonical ones with
+    f^{BA}[nu, mu] = s(mu) s(nu) f^{AB}[mu, nu] (s = _flip_sign), so that
+    S, T and the ontop potentials are Hermitian across neigh_back, and
+    vna_ontopL of (B, A) is the transpose of vna_ontopR of (A, B)."""
+    if itype == P_VNA_ATOM:   # both orbitals on A: symmetric in (mu, nu)
+        if (oa[0], oa[1]) > (ob[0], ob[1]):
+            oa, ob = ob, oa
+        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi)
+    if _canonical(A.nZ, oa, B.nZ, ob):
+        if itype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
+            itype = P_VNA_ONTOPL
+        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi)
+    sign = _flip_sign(oa) * _flip_sign(ob)
+    rtype = {P_VNA_ONTOPL: P_VNA_ONTOPR, P_VNA_ONTOPR: P_VNA_ONTOPL}.get(itype, itype)
+    if rtype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
+        rtype = P_VNA_ONTOPL
+    return sign * _base2c(seed, rtype, B.nZ, A.nZ, ob, oa, t, asym_pi)
+
+
+def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0):
+    """Legendre coefficient itheta of the bcna channel <A oa| V_K |B ob>.
+
+    c^{BAK}_l[nu, mu] = (-1)^l s(mu) s(nu) c^{ABK}_l[mu, nu] with l = itheta-1
+    (reversing the bond flips cos(theta)), so the three-center blocks are
+    Hermitian across neigh_back as well."""
+    l = itheta - 1
+    if (A.nZ, oa) == (B.nZ, ob):
+        if l % 2 == 1:
+            return np.zeros(np.broadcast(u, v).shape)
+        key = (A.nZ, B.nZ, oa, ob)
+        sign = 1.0
+    elif (A.nZ, oa) < (B.nZ, ob):
+        key = (A.nZ, B.nZ, oa, ob)
+        sign = 1.0
+    else:
+        key = (B.nZ, A.nZ, ob, oa)
+        sign = (-1.0) ** l * _flip_sign(oa) * _flip_sign(ob)
+    rng = np.random.default_rng(_seed_of(seed, "3c", key, K.nZ, mval, itheta))
+    coef = rng.normal(0.0, 1.0, 30)
+    return sign * _f2d(coef, u, v, 0.5 / (itheta ** theta_decay))
+
+
+# ---------------------------------------------------------------------------
+# writers
+# ---------------------------------------------------------------------------
+def _fmt(vals):
+    return " ".join("%24.16E" % v for v in vals)
+
+
+def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
+                asym_pi=False, theta_decay=1.0):
+    """Write a complete Harris Fdata set for ``species`` into ``path``.
+
+    nx2c: 2c grid points on [0, rcA_i + rcA_j] (200 points over 10 bohr for
+    the rc = 5 bohr species).  n3c: 3c grid points on both axes.
+    asym_pi: give the two pi channels of 2c tables different coefficients
+    (breaks rotation invariance; used only to sharpen frame tests).
+    """
+    os.makedirs(path, exist_ok=True)
+    ns = len(species)
+    # Fdata.inp (M_species.f90:227-233)
+    with open(os.path.join(path, "Fdata.inp"), "w") as f:
+        f.write("%d\n" % ns)
+        for s in species:
+            f.write("%d\n" % s.nZ)
+        f.write("%s\n" % path)
+    # info.dat (M_species.f90:1094-1160): signature, count, 16 lines/species
+    with open(os.path.join(path, "info.dat"), "w") as f:
+        f.write("  synthetic seeded Fdata (gaussian-polynomial tables)\n")
+        f.write("%12d\n" % ns)
+        for isp, s in enumerate(species):
+            f.write("  " + "=" * 70 + "\n")
+            f.write("%12d  - Information for this species \n" % (isp + 1))
+            f.write("  %-2s          - Element \n" % s.symbol)
+            f.write("%12d  - Nuclear Z \n" % s.nZ)
+            f.write("%12.4f  - Atomic Mass \n" % s.xmass)
+            f.write("%12d  - Number of shells; L for each shell \n" % len(s.lssh))
+            f.write("  " + " ".join("%d" % l for l in s.lssh) + "\n")
+            f.write("  " + " ".join("%5.2f" % q for q in s.qneutral) + "\n")
+            f.write("  " + " ".join("%7.4f" % r for r in s.rcutoff) + "\n")
+            f.write("%12d  - Number of shells (PP) \n" % len(s.lssh_pp))
+            f.write("  " + " ".join("%d" % l for l in s.lssh_pp) + "\n")
+            f.write("%12.4f  - Radial cutoffs (PP) \n" % s.rcutoff_pp)
+            f.write("  " + "  ".join("%-20s" % ("%03d_%02d.wf%d" % (s.nZ, int(10 * s.rcutoff[k]) % 100, k + 1))
+                                       for k in range(len(s.lssh))) + "\n")
+            f.write("  " + "  ".join("%-20s" % ("%03d_%02d.na%d" % (s.nZ, int(10 * s.rcutoff[0]) % 100, k))
+                                       for k in range(len(s.lssh) + 1)) + "\n")
+            f.write("%12.4f  - Atomic energy \n" % (-100.0 - s.nZ))
+            f.write("  " + "=" * 70 + "\n")
+    for s in species:
+        with open(os.path.join(path, "clPP.%02d.dat" % s.nZ), "w") as f:
+            for k in range(len(s.lssh_pp)):
+                f.write("%22.14E\n" % (0.5 + 0.1 * k))
+
+    # two-center tables
+    for si_ in species:
+        for sj in species:
+            zz = "%02d.%02d" % (si_.nZ, sj.nZ)
+            xmax = si_.rcA + sj.rcA
+            x = np.linspace(0.0, xmax, nx2c)
+            t = x / xmax
+            cells = [
+                (P_OVERLAP, "overlap", make_munu(si_.lssh, sj.lssh)),
+                (P_KINETIC, "kinetic", make_munu(si_.lssh, sj.lssh)),
+                (P_VNA_ONTOPL, "vna_ontopl_00", make_munu(si_.lssh, sj.lssh)),
+                (P_VNA_ONTOPR, "vna_ontopr_00", make_munu(si_.lssh, sj.lssh)),
+                (P_VNA_ATOM, "vna_atom_00", make_munu(si_.lssh, si_.lssh)),
+            ]
+            with open(os.path.join(path, "2c.%s.dat" % zz), "w") as f:
+                f.write("%d\n" % len(cells))
+            with open(os.path.join(path, "2c.%s.dir" % zz), "w") as fd:
+                for icell, (itype, stem, (mu, nu, mv)) in enumerate(cells, start=1):
+                    fname = "%s.%s.dat" % (stem, zz)
+                    ls_b = si_.lssh if itype == P_VNA_ATOM else sj.lssh
+                    orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(ls_b)
+                    data = np.zeros((nx2c, len(mu)))
+                    for ime in range(len(mu)):
+                        data[:, ime] = table2c(seed, itype, si_, sj, orb_a[mu[ime] - 1],
+                                               orb_b[nu[ime] - 1], t, asym_pi)
+                    with open(os.path.join(path, fname), "w") as f:
+                        for ix in range(nx2c):
+                            f.write(_fmt(data[ix]) + "\n")
+                        f.write("\n")
+                    fd.write("  %3d %3d %3d %-29s %3d %4d %9.6f\n"
+                             % (icell, itype, 0, fname, len(mu), nx2c, xmax))
+                    with open(os.path.join(path, "%02d_munu_2c.%s.dat" % (itype, zz)), "w") as f:
+                        f.write(" ".join("%d" % v for v in mu) + "\n")
+                        f.write(" ".join("%d" % v for v in nu) + "\n")
+                        f.write(" ".join("%d" % v for v in mv) + "\n")
+
+    # three-center tables (bcna, isorp = 0, theta = 1..5)
+    for si_ in species:
+        for sj in species:
+            for sk in species:
+                zzz = "%02d.%02d.%02d" % (si_.nZ, sj.nZ, sk.nZ)
+                ymax = si_.rcA + sj.rcA                       # dbc
+                xmax = sk.rcA + max(si_.rcA, sj.rcA)          # dna
+                mu, nu, mv = make_munu_3c(si_.lssh, sj.lssh)
+                orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(sj.lssh)
+                u = np.linspace(0.0, 1.0, n3c)[None, :]       # x fastest
+                v = np.linspace(0.0, 1.0, n3c)[:, None]
+                with open(os.path.join(path, "3c.%s.dat" % zzz), "w") as f:
+                    f.write("%d\n" % P_NTHETA)
+                with open(os.path.join(path, "3c.%s.dir" % zzz), "w") as fd, \
+                        open(os.path.join(path, "%02d_munu_3c.%s.dat" % (P_BCNA, zzz)), "w") as fm:
+                    for itheta in range(1, P_NTHETA + 1):
+                        fname = "bcna_%02d_%02d.%s.dat" % (itheta, 0, zzz)
+                        data = np.zeros((n3c, n3c, len(mu)))
+                        for ime in range(len(mu)):
+                            data[:, :, ime] = table3c(seed, si_, sj, sk, orb_a[mu[ime] - 1],
+                                                      orb_b[nu[ime] - 1], mv[ime], itheta, u, v,
+                                                      theta_decay)
+                        with open(os.path.join(path, fname), "w") as f:
+                            for iy in range(n3c):
+                                for ix in range(n3c):
+                                    f.write(_fmt(data[iy, ix]) + "\n")
+                        fd.write("  %2d %2d %2d %3d %-29s %3d %4d %9.6f %4d %9.6f\n"
+                                 % (itheta, P_BCNA, 0, itheta, fname, len(mu),
+                                    n3c, xmax, n3c, ymax))
+                        fm.write(" " + " ".join("%d" % q for q in mu) + "\n")
+                        fm.write(" " + " ".join("%d" % q for q in nu) + "\n")
+                        fm.write(" " + " ".join("%d" % q for q in mv) + "\n")
+    return path
+
+
+# ---------------------------------------------------------------------------
+# structures
+# ---------------------------------------------------------------------------
+@dataclass
+class Structure:
+    ratom: np.ndarray          # (N, 3) Angstrom
+    imass: np.ndarray          # (N,) 1-based species index
+    lattice: np.ndarray        # (3, 3) rows a1, a2, a3
+    icluster: int = 0
+    name: str = ""
+
+    @property
+    def natoms(self):
+        return len(self.imass)
+
+
+_DIAMOND_BASIS = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0],
+                           [.25, .25, .25], [.25, .75, .75], [.75, .25, .75], [.75, .75, .25]])
+
+
+def diamond(n, a, sigma, seed, sp_a=1, sp_b=1, vacancy=0.0, name=""):
+    """n = (n1, n2, n3) conventional cells of diamond (sp_a == sp_b) or
+    zincblende; Gaussian jitter sigma (Angstrom); random vacancy fraction."""
+    rng = np.random.default_rng(seed)
+    n1, n2, n3 = n
+    pos, sp = [], []
+    for i in range(n1):
+        for j in range(n2):
+            for k in range(n3):
+                for b, fr in enumerate(_DIAMOND_BASIS):
+                    pos.append((np.array([i, j, k]) + fr) * a)
+                    sp.append(sp_a if b < 4 else sp_b)
+    pos = np.array(pos, dtype=np.float64)
+    sp = np.array(sp, dtype=np.int32)
+    pos += rng.normal(0.0, sigma, pos.shape)
+    if vacancy > 0:
+        nvac = int(round(vacancy * len(sp)))
+        keep = np.sort(rng.permutation(len(sp))[nvac:])
+        pos, sp = pos[keep], sp[keep]
+    lat = np.diag([n1 * a, n2 * a, n3 * a]).astype(np.float64)
+    return Structure(pos, sp, lat, 0, name)
+
+
+def random_box(counts, box, dmin, seed, name=""):
+    """Uniform random positions in a cubic periodic box with a minimum image
+    distance dmin (random sequential addition); counts = list of atoms per
+    species (1-based species order)."""
+    rng = np.random.default_rng(seed)
+    total = sum(counts)
+    sp = np.concatenate([np.full(cnt, isp + 1, np.int32) for isp, cnt in enumerate(counts)])
+    sp = sp[rng.permutation(total)]
+    pos = np.zeros((total, 3))
+    ncell = max(1, int(box // dmin))
+    grid = {}
+    placed = 0
+    while placed < total:
+        trial = rng.uniform(0.0, box, 3)
+        cidx = tuple((trial / box * ncell).astype(int) % ncell)
+        ok = True
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    key = ((cidx[0] + dx) % ncell, (cidx[1] + dy) % ncell, (cidx[2] + dz) % ncell)
+                    for q in grid.get(key, ()):
+                        d = trial - pos[q]
+                        d -= box * np.round(d / box)
+                        if d @ d < dmin * dmin:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if not ok:
+                break
+        if ok:
+            pos[placed] = trial
+            grid.setdefault(cidx, []).append(placed)
+            placed += 1
+    return Structure(pos, sp, np.diag([box] * 3).astype(np.float64), 0, name)
+
+
+# Workload definitions (synthetic, seeded)
+SEED_SI64, SEED_SI512, SEED_CHO, SEED_BATCH, SEED_SIC = 1001, 1002, 1003, 1004, 1005
+
+
+def species_for(workload):
+    if workload in ("si64", "si512"):
+        return [si(5.0)]
+    if workload == "cho1536":
+        return [c(4.5), h(4.0), o(4.0)]
+    if workload in ("sic4096", "batch256"):
+        return [si(5.0), c(5.0)]
+    raise ValueError(workload)
+
+
+def structure_for(workload):
+    if workload == "si64":
+        return diamond((2, 2, 2), 5.43, 0.05, SEED_SI64, name="Si64")
+    if workload == "si512":
+        return diamond((4, 4, 4), 5.43, 0.15, SEED_SI512, name="Si512")
+    if workload == "cho1536":
+        return random_box([384, 768, 384], 24.0, 1.0, SEED_CHO, name="CHO1536")
+    if workload == "sic4096":
+        return diamond((8, 8, 8), 4.36, 0.1, SEED_SIC, sp_a=1, sp_b=2, name="SiC4096")
+    raise ValueError(workload)
+
+
+def batch_structures(nstruct=256, seed=SEED_BATCH):
+    """Independent Si / SiC structures of 32..512 atoms with 0-5 % vacancies."""
+    rng = np.random.default_rng(seed)
+    dims = [(a, b, cc) for a in range(1, 5) for b in range(1, 5) for cc in range(1, 5)
+            if 32 <= 8 * a * b * cc <= 512]
+    out = []
+    for k in range(nstruct):
+        target = int(rng.integers(32, 513))
+        best = min(dims, key=lambda d: abs(8 * d[0] * d[1] * d[2] - target))
+        zinc = bool(rng.integers(0, 2))
+        a = 4.36 if zinc else 5.43
+        vac = float(rng.uniform(0.0, 0.05))
+        out.append(diamond(best, a, 0.1, int(rng.integers(1 << 30)), sp_a=1,
+                           sp_b=2 if zinc else 1, vacancy=vac, name="batch%03d" % k))
+    return out
+
+
+def fdata_dir_for(workload, root=None):
+    """Generate (once) and return the Fdata directory of a workload."""
+    root = root or os.environ.get("FBGPU_FDATA_ROOT") or os.path.join(
+        os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "_fdata")
+    key = {"si64": "Si_rc50", "si512": "Si_rc50", "cho1536": "CHO_rc45_40_40",
+           "sic4096": "SiC_rc50", "batch256": "SiC_rc50"}[workload]
+    path = os.path.join(root, key)
+    stamp = os.path.join(path, ".complete")
+    if not os.path.exists(stamp):
+        write_fdata(path, species_for(workload))
+        with open(stamp, "w") as f:
+            f.write("ok\n")
+    return path
