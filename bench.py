@@ -1,0 +1,372 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 FIREBALL Harris assembly hot path.
+
+One step = one pass of the path over one structure: the neighbor maps
+(driver_neighbors), the 2c + 3c H/S assembly (assemble_S, assemble_T,
+assemble_vna_2c, assemble_vna_3c) and the force derivatives with the force
+reduction (Dassemble_S/T/vna_2c/vna_3c, build_forces), all in FP64.
+The density matrices the solver would supply are seeded synthetic blocks.
+
+Default workload: 512-atom Si (4x4x4 diamond cells, a = 5.43 A, N(0, 0.15 A)
+jitter, sp3, rc = 5.0 bohr), synthetic Gaussian-polynomial Fdata.
+
+  value  neighbor blocks/s with inputs resident in HBM (device timing, CUDA
+         events on the library's stream, L2 flushed between steps)
+  e2e    the same metric through the C ABI with host buffers: positions and
+         density matrices copied in from pinned memory, S, T, vna, vnao
+         blocks and ftot copied out, every step
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, OpenMP on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "thunder-master_gb300")
+for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = ("H/S assembly ms/step & neighbor blocks/s: table vs MLP-3c, 1 GB300, |ΔH|<1e-5 Ha")
+UNIT = "neighbor blocks/s"
+WORKLOADS = {
+    "si512": "Si512: 4x4x4 diamond Si, a=5.43 A, N(0,0.15 A) jitter, sp3, rc=5.0 bohr; neighbors + 2c + 3c "
+             "H/S + forces, FP64",
+    "si64": "Si64: 2x2x2 diamond Si, a=5.43 A, N(0,0.05 A) jitter, sp3, rc=5.0 bohr; neighbors + 2c + 3c H/S "
+            "+ forces, FP64",
+    "cho1536": "C/H/O 1536 atoms (1:2:1), 24 A box, dmin 1.0 A, rc C 4.5 / O 4.0 / H 4.0 bohr; neighbors + "
+               "2c + 3c H/S + forces, FP64",
+    "sic4096": "SiC4096: 8x8x8 zincblende SiC, a=4.36 A, N(0,0.1 A) jitter, sp3, rc=5.0 bohr; neighbors + 2c "
+               "+ 3c H/S + forces, FP64",
+}
+
+
+def fdata_root():
+    return os.environ.get("FBGPU_FDATA_ROOT") or os.path.join(ROOT, "_fdata")
+
+
+def load_workload(name):
+    from fbgpu import synth
+    path = synth.fdata_dir_for(name, root=fdata_root())
+    st = synth.structure_for(name)
+    nZ = [s.nZ for s in synth.species_for(name)]
+    return path, nZ, st
+
+
+def denmat_for(ctx_or_sys, st, nZ, norb_of, seed=42):
+    """Seeded density matrices symmetric across neigh_back."""
+    rng = np.random.default_rng(seed)
+    nb = ctx_or_sys["blk_off"]
+    P = len(ctx_or_sys["neigh_j"])
+    rho = np.zeros(int(nb[-1]))
+    cape = np.zeros(int(nb[-1]))
+    pair_off = np.concatenate([[0], np.cumsum(ctx_or_sys["neighn"])])
+    owner = np.repeat(np.arange(len(ctx_or_sys["neighn"])), ctx_or_sys["neighn"])
+    for p in range(P):
+        i = owner[p]
+        j = ctx_or_sys["neigh_j"][p] - 1
+        q = pair_off[j] + ctx_or_sys["neigh_back"][p] - 1
+        if q < p:
+            continue
+        ni, nj = norb_of[i], norb_of[j]
+        a = rng.normal(0.0, 0.1, (ni, nj))
+        b = rng.normal(0.0, 0.05, (ni, nj))
+        if p == q:
+            a = 0.5 * (a + a.T)
+            b = 0.5 * (b + b.T)
+        rho[nb[p]:nb[p + 1]] = a.T.ravel()
+        cape[nb[p]:nb[p + 1]] = b.T.ravel()
+        rho[nb[q]:nb[q + 1]] = a.ravel()
+        cape[nb[q]:nb[q + 1]] = b.ravel()
+    return rho, cape
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % device)
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        if sm:
+            out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work per unit
+# ---------------------------------------------------------------------------
+def flops_dassemble_3c(nme):
+    # value + x + y derivative table contractions (5 theta x 16 nodes x nME FMA
+    # each), Legendre and theta-derivative combination (4 x 5 x nME FMA), and
+    # ~1800 FLOP of geometry, frame derivatives and molecular-frame contraction
+    return 2.0 * (3 * 5 * 16 * nme + 4 * 5 * nme) + 1800.0
+
+
+def flops_assemble_3c(nme):
+    return 2.0 * (5 * 16 * nme + 5 * nme) + 600.0
+
+
+def bytes_dassemble_3c(T, P, N, nb_per_pair, table_bytes):
+    # triplet list (6 int32 per triplet), rho blocks once per pair, positions,
+    # three per-atom force vectors written, tables once
+    return T * 24 + P * nb_per_pair * 8 + N * 24 + 3 * N * 24 + table_bytes
+
+
+def run_gpu(args):
+    import torch
+    import fbgpu
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    path, nZ, st = load_workload(args.workload)
+    ctx = fbgpu.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    P, T, NB = ctx.driver_neighbors()
+    nbm = ctx.neighbors()
+    norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
+    rho, cape = denmat_for(nbm, st, nZ, norb_of)
+    d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
+    d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def device_step():
+        ctx.driver_neighbors()
+        ctx.assemble(fbgpu.FB_ALL)
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.Dassemble(fbgpu.FB_ALL)
+
+    # pinned host buffers for the end-to-end leg
+    pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    h_pos = pin(3 * st.natoms)
+    h_pos[:] = st.ratom.ravel()
+    h_rho, h_cape = pin(NB), pin(NB)
+    h_rho[:] = rho
+    h_cape[:] = cape
+    h_out = [pin(NB) for _ in range(4)]
+    h_f = pin(3 * st.natoms)
+
+    def e2e_step():
+        ctx.update_positions(h_pos)
+        ctx.driver_neighbors()
+        ctx.assemble(fbgpu.FB_ALL)
+        for key, buf in zip(("S", "T", "vna", "vnao"), h_out):
+            ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
+        ctx.set_denmat(h_rho, h_cape)
+        ctx.Dassemble(fbgpu.FB_ALL)
+        ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
+
+    h2d = 3 * st.natoms * 8 + 2 * NB * 8
+    d2h = 4 * NB * 8 + 3 * st.natoms * 8
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(step, nsteps, timing=False):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        barrier()
+        if timing:
+            ctx.set_timing(True)
+        l0 = ctx.kernel_launches()
+        for k in range(nsteps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+        barrier()
+        launches = ctx.kernel_launches() - l0
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches
+
+    for _ in range(args.warmup):
+        device_step()
+        e2e_step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, launches = timed(device_step, args.steps, timing=True)
+    ktimes = ctx.timing()
+    ms_e2e, _ = timed(e2e_step, args.steps)
+    clk = clocks.stop()
+    ctx.set_timing(False)
+    fp64_peak = ctx.probe_fp64()
+
+    per_step = ms / args.steps
+    value = ws * P * args.steps / (ms * 1e-3)
+    e2e_value = ws * P * args.steps / (ms_e2e * 1e-3)
+    # dominant kernel and its roofline
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms = ktimes[dom][0] / max(1, ktimes[dom][1])
+    from fbgpu import synth
+    nme = len(synth.make_munu_3c([0, 1], [0, 1])[0])
+    fl = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
+    roof = None
+    if fl is not None:
+        ach = fl / (dom_ms * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp64_peak, 4),
+                "unit": "TFLOP/s", "frac": round(ach / fp64_peak, 4), "traffic": None,
+                "peak_source": "measured in this run (fb_probe_fp64 DFMA chains)",
+                "flops_per_launch": fl, "avg_launch_ms": round(dom_ms, 4)}
+        table_bytes = 8 * 31 * 31 * 5 * nme * len(nZ) ** 3
+        by = bytes_dassemble_3c(T, P, st.natoms, 16, table_bytes)
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f)["hbm_gbs"]
+        roof["hbm"] = {"achieved": round(by / (dom_ms * 1e-3) / 1e9, 3), "peak": hbm_peak, "unit": "GB/s",
+                       "frac": round(by / (dom_ms * 1e-3) / 1e9 / hbm_peak, 6), "bytes_per_launch": by,
+                       "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "flushed between steps (256 MiB write)", "forces": True},
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(ms_e2e / args.steps, 4)},
+        "gpu_launches": launches,
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+        "roofline": roof,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.workload, path, nZ, st, P)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(workload, path, nZ, st, P_expect=None, steps=1):
+    """The oracle (C restatement, OpenMP on every host core) on one full step
+    of the same workload: neighbors, 2c + 3c assembly, forces."""
+    from oracle import oracle as orc
+    from conftest import symmetric_denmat
+    cores = os.cpu_count() or 1
+    fd = orc.Fdata(path, nZ)
+    times = []
+    P = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        s = orc.System(fd, st.ratom, st.imass, st.lattice, threads=cores).neighbors()
+        s.assemble()
+        t1 = time.perf_counter()
+        norb = np.array([fd.norb(int(k)) for k in st.imass])
+        rho, cape = symmetric_denmat(s, norb, 42)
+        t2 = time.perf_counter()
+        s.dassemble(rho, cape)
+        t3 = time.perf_counter()
+        times.append((t1 - t0) + (t3 - t2))
+        P = s.npairs
+    t = float(np.median(times))
+    return {"value": round(P / t, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d full step(s) of the same workload (neighbors + 2c + 3c assembly + forces), median "
+                      "%.3f s/step" % (steps, t)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    path, nZ, st = load_workload(args.workload)
+    cb = None
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, path, nZ, st)
+    t0 = time.perf_counter()
+    cb = cpu_baseline(args.workload, path, nZ, st, steps=args.steps)
+    wall = time.perf_counter() - t0
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fbgpu", choices=["fbgpu", "reference"])
+    ap.add_argument("--workload", default="si512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

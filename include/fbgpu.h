@@ -160,6 +160,11 @@ int fb_device_blocks(fb_ctx *ctx, int which, void **dptr);
  * doubles each, layout as the blocks); cape may be NULL (zero Pulay). */
 int fb_set_denmat(fb_ctx *ctx, const double *rho, const double *cape);
 
+/* Same, from device memory (a GPU solver's output): device-to-device copy
+ * on the context's stream; cape_dev may be NULL. */
+int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev,
+                         const void *cape_dev);
+
 /* Dassemble_S/T/vna_2c (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:96,289,538),
  * Dassemble_vna_3c (k.DASSEMBLERS/M_Dassemble_3c_Harris.f90:136) and the
  * assembly terms of build_forces (c.SYSTEM/M_build_forces.f90:172). */
@@ -176,6 +181,22 @@ int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T,
 
 /* Number of kernels this context launched since creation (diagnostics). */
 long long fb_kernel_launches(const fb_ctx *ctx);
+
+/* Per-kernel timing with CUDA events recorded on the context's stream
+ * around every launch.  fb_set_timing(ctx, 1) resets and enables it;
+ * fb_get_timing returns the accumulated device time and launch count of one
+ * kernel: "neigh_count", "neigh_fill", "neigh_back", "common_count",
+ * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
+ * "dassemble_3c", "build_forces".  No reference counterpart (the reference
+ * has no timers on this path). */
+int fb_set_timing(fb_ctx *ctx, int enable);
+int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,
+                  long long *launches);
+
+/* Measured FP64 FMA throughput of this GPU in TFLOP/s (a DFMA-chain kernel,
+ * about 0.1 s); the denominator of the FP64 roofline.  No reference
+ * counterpart. */
+int fb_probe_fp64(fb_ctx *ctx, double *tflops);
 
 #ifdef __cplusplus
 }

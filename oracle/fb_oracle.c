@@ -1156,7 +1156,9 @@ int or_neighbors(or_sys *s) {
   s->neighn = (int *)calloc((size_t)N, sizeof(int));
   s->pair_off = (int *)calloc((size_t)N + 1, sizeof(int));
   s->neigh_self = (int *)malloc(sizeof(int) * N);
-  /* counting pass (find_neigh_max :289-330) */
+  /* counting pass (find_neigh_max :289-330); atoms are independent, so the
+   * CPU baseline runs this loop on all threads */
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
   for (int i = 0; i < N; i++) {
     int num = 0;
     double rci = rcut_of(s, i), r2[3];
@@ -1168,13 +1170,15 @@ int or_neighbors(or_sys *s) {
         if (z < range_max) num++;
       }
     s->neighn[i] = num;
-    s->pair_off[i + 1] = s->pair_off[i] + num;
   }
+  for (int i = 0; i < N; i++) s->pair_off[i + 1] = s->pair_off[i] + s->neighn[i];
   int P = s->pair_off[N];
   s->npairs = P;
   s->neigh_j = (int *)malloc(sizeof(int) * (P ? P : 1));
   s->neigh_b = (int *)malloc(sizeof(int) * (P ? P : 1));
   s->neigh_back = (int *)malloc(sizeof(int) * (P ? P : 1));
+  int close_err = 0;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
   for (int i = 0; i < N; i++) {                                     /* :392-439 */
     int num = 0;
     double rci = rcut_of(s, i), r2[3];
@@ -1184,8 +1188,11 @@ int or_neighbors(or_sys *s) {
         double z = distance3(RAT(s, i), r2);
         double range_max = rci + rcut_of(s, j) - 0.01;
         if (i != j && z < 0.5) {
-          seterr("atoms dangerously close: %d %d z=%g mbeta=%d", i + 1, j + 1, z, mb);
-          return E_CLOSE;
+#pragma omp critical
+          {
+            if (!close_err) seterr("atoms dangerously close: %d %d z=%g mbeta=%d", i + 1, j + 1, z, mb);
+            close_err = 1;
+          }
         }
         if (z < range_max) {
           s->neigh_j[s->pair_off[i] + num] = j;
@@ -1194,6 +1201,7 @@ int or_neighbors(or_sys *s) {
         }
       }
   }
+  if (close_err) return E_CLOSE;
   for (int i = 0; i < N; i++) s->neigh_self[i] = -999;              /* :456-505 */
   for (int i = 0; i < N; i++) {
     for (int in = 0; in < s->neighn[i]; in++) {
@@ -1229,62 +1237,63 @@ int or_neighbors(or_sys *s) {
     }
   s->blk_off[P] = off;
   s->nblock = off;
-  /* common neighbors (:681-812) */
+  /* common neighbors (:681-812): a counting pass and a filling pass, both
+   * parallel over ialpha, give the reference order */
   s->ncommon = (int *)calloc((size_t)N, sizeof(int));
   s->trip_off = (int *)calloc((size_t)N + 1, sizeof(int));
-  int cap = 1024, nt = 0;
-  s->ci_j = (int *)malloc(sizeof(int) * cap);
-  s->ci_b = (int *)malloc(sizeof(int) * cap);
-  s->cj_j = (int *)malloc(sizeof(int) * cap);
-  s->cj_b = (int *)malloc(sizeof(int) * cap);
-  s->cneigh = (int *)malloc(sizeof(int) * cap);
-  for (int ia = 0; ia < N; ia++) {
-    int num = 0;
-    for (int in = 0; in < s->neighn[ia]; in++) {
-      int p = s->pair_off[ia] + in, iat = s->neigh_j[p], ib = s->neigh_b[p];
-      if (iat == ia && ib == 0) continue;
-      double r1[3], r2[3], r3[3];
-      for (int k = 0; k < 3; k++) r1[k] = RAT(s, iat)[k] + s->xl[ib][k];
-      double rci = rcut_of(s, iat);
-      for (int jn = 0; jn < s->neighn[ia]; jn++) {
-        int q = s->pair_off[ia] + jn, jat = s->neigh_j[q], jb = s->neigh_b[q];
-        if ((jat == ia && jb == 0) || in == jn) continue;
-        for (int k = 0; k < 3; k++) r2[k] = RAT(s, jat)[k] + s->xl[jb][k];
-        double z = distance3(r1, r2);
-        double range_max = rci + rcut_of(s, jat) - 0.01;
-        if (z < range_max) {
-          int found = -9999;
-          for (int kn = 0; kn < s->neighn[iat]; kn++) {
-            int r = s->pair_off[iat] + kn, kat = s->neigh_j[r], kb = s->neigh_b[r];
-            for (int k = 0; k < 3; k++) r3[k] = s->xl[kb][k] + RAT(s, kat)[k] - RAT(s, iat)[k];
-            if ((fabs(r3[0] - r2[0] + r1[0]) < 1.0e-4) && (fabs(r3[1] - r2[1] + r1[1]) < 1.0e-4) &&
-                (fabs(r3[2] - r2[2] + r1[2]) < 1.0e-4)) {
-              found = kn;
-              break;
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) {
+      for (int ia = 0; ia < N; ia++) s->trip_off[ia + 1] = s->trip_off[ia] + s->ncommon[ia];
+      int T = s->trip_off[N] ? s->trip_off[N] : 1;
+      s->ci_j = (int *)malloc(sizeof(int) * T);
+      s->ci_b = (int *)malloc(sizeof(int) * T);
+      s->cj_j = (int *)malloc(sizeof(int) * T);
+      s->cj_b = (int *)malloc(sizeof(int) * T);
+      s->cneigh = (int *)malloc(sizeof(int) * T);
+    }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
+    for (int ia = 0; ia < N; ia++) {
+      int num = 0;
+      for (int in = 0; in < s->neighn[ia]; in++) {
+        int p = s->pair_off[ia] + in, iat = s->neigh_j[p], ib = s->neigh_b[p];
+        if (iat == ia && ib == 0) continue;
+        double r1[3], r2[3], r3[3];
+        for (int k = 0; k < 3; k++) r1[k] = RAT(s, iat)[k] + s->xl[ib][k];
+        double rci = rcut_of(s, iat);
+        for (int jn = 0; jn < s->neighn[ia]; jn++) {
+          int q = s->pair_off[ia] + jn, jat = s->neigh_j[q], jb = s->neigh_b[q];
+          if ((jat == ia && jb == 0) || in == jn) continue;
+          for (int k = 0; k < 3; k++) r2[k] = RAT(s, jat)[k] + s->xl[jb][k];
+          double z = distance3(r1, r2);
+          double range_max = rci + rcut_of(s, jat) - 0.01;
+          if (z < range_max) {
+            int found = -9999;
+            for (int kn = 0; kn < s->neighn[iat]; kn++) {
+              int r = s->pair_off[iat] + kn, kat = s->neigh_j[r], kb = s->neigh_b[r];
+              for (int k = 0; k < 3; k++) r3[k] = s->xl[kb][k] + RAT(s, kat)[k] - RAT(s, iat)[k];
+              if ((fabs(r3[0] - r2[0] + r1[0]) < 1.0e-4) && (fabs(r3[1] - r2[1] + r1[1]) < 1.0e-4) &&
+                  (fabs(r3[2] - r2[2] + r1[2]) < 1.0e-4)) {
+                found = kn;
+                break;
+              }
             }
+            if (found == -9999) continue;
+            if (pass == 1) {
+              int t = s->trip_off[ia] + num;
+              s->ci_j[t] = iat;
+              s->ci_b[t] = ib;
+              s->cj_j[t] = jat;
+              s->cj_b[t] = jb;
+              s->cneigh[t] = found;
+            }
+            num++;
           }
-          if (found == -9999) continue;
-          if (nt == cap) {
-            cap *= 2;
-            s->ci_j = (int *)realloc(s->ci_j, sizeof(int) * cap);
-            s->ci_b = (int *)realloc(s->ci_b, sizeof(int) * cap);
-            s->cj_j = (int *)realloc(s->cj_j, sizeof(int) * cap);
-            s->cj_b = (int *)realloc(s->cj_b, sizeof(int) * cap);
-            s->cneigh = (int *)realloc(s->cneigh, sizeof(int) * cap);
-          }
-          s->ci_j[nt] = iat;
-          s->ci_b[nt] = ib;
-          s->cj_j[nt] = jat;
-          s->cj_b[nt] = jb;
-          s->cneigh[nt] = found;
-          nt++;
-          num++;
         }
       }
+      if (pass == 0) s->ncommon[ia] = num;
     }
-    s->ncommon[ia] = num;
-    s->trip_off[ia + 1] = s->trip_off[ia] + num;
   }
+  int nt = s->trip_off[N];
   s->ntrip = nt;
   return OK;
 }

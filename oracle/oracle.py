@@ -122,6 +122,7 @@ class System:
 
     def neighbors(self):
         L = lib()
+        L.or_set_threads(self.threads)
         _check(L.or_neighbors(self.h))
         N = len(self.imass)
         P = L.or_npairs(self.h)

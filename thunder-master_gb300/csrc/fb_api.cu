@@ -15,6 +15,13 @@
 
 using namespace fb;
 
+// kernels timed by fb_set_timing / fb_get_timing
+enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
+       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_N };
+static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
+                                     "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
+                                     "build_forces"};
+
 namespace {
 
 // device buffer that grows on demand and never shrinks
@@ -64,6 +71,7 @@ struct fb_ctx {
   int P = 0, T = 0;
   long long nblock = 0;
   std::vector<int> h_pair_off, h_trip_off;
+  DevBuf d_bsum, d_blk_base;
   DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v, d_r3f,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_status, d_errinfo;
@@ -73,6 +81,12 @@ struct fb_ctx {
   unsigned assembled = 0, dassembled = 0;
   // forces
   DevBuf d_sumT, d_sumS, d_ontop, d_atomf, d_f3a, d_f3b, d_f3c, d_kin, d_vna, d_pul, d_ftot;
+  // per-kernel CUDA-event timing (fb_set_timing)
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evpool;
+  std::vector<std::pair<int, int>> pending;  // (kernel id, event index)
+  double kt_ms[KT_N] = {0};
+  long long kt_n[KT_N] = {0};
 };
 
 static int fail(fb_ctx *c, int code, const char *fmt, ...) {
@@ -95,16 +109,48 @@ static int fail(fb_ctx *c, int code, const char *fmt, ...) {
     int st_ = (call);                                                           \
     if (st_) return st_ == FB_ERR_CUDA ? fail(ctx, FB_ERR_CUDA, "allocation failed: %s", #call) : st_; \
   } while (0)
-#define KL(call)                                                                                        \
+static int timing_begin(fb_ctx *ctx) {
+  size_t k = ctx->pending.size();
+  if (k >= ctx->evpool.size()) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return -1;
+    ctx->evpool.push_back({a, b});
+  }
+  cudaEventRecord(ctx->evpool[k].first, ctx->stream);
+  return (int)k;
+}
+
+static void timing_end(fb_ctx *ctx, int kid, int ev) {
+  if (ev < 0) return;
+  cudaEventRecord(ctx->evpool[ev].second, ctx->stream);
+  ctx->pending.push_back({kid, ev});
+}
+
+// fold finished launches into the per-kernel totals (after a stream sync)
+static void timing_drain(fb_ctx *ctx) {
+  for (auto &pe : ctx->pending) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ctx->evpool[pe.second].first, ctx->evpool[pe.second].second) == cudaSuccess) {
+      ctx->kt_ms[pe.first] += ms;
+      ctx->kt_n[pe.first] += 1;
+    }
+  }
+  ctx->pending.clear();
+}
+
+#define KL(kid, call)                                                                                   \
   do {                                                                                                  \
+    int ev_ = ctx->timing ? timing_begin(ctx) : -1;                                                     \
     int e_ = (call);                                                                                    \
     ctx->launches++;                                                                                    \
+    timing_end(ctx, kid, ev_);                                                                          \
     if (e_) return fail(ctx, FB_ERR_CUDA, "launch %s: %s", #call, cudaGetErrorString((cudaError_t)e_)); \
   } while (0)
 
 static int sync_status(fb_ctx *ctx, unsigned *st) {
   CU(cudaMemcpyAsync(st, ctx->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
+  if (ctx->timing) timing_drain(ctx);
   return FB_OK;
 }
 
@@ -156,8 +202,12 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
-                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot};
+                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base};
   for (DevBuf *b : bufs) b->release();
+  for (auto &e : ctx->evpool) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
 }
@@ -300,6 +350,11 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.xlf = ctx->d_xlf.as<float>();
   a.imgs = ctx->d_imgs.as<int>();
   a.cnt = ctx->d_cnt.as<int>();
+  a.bsum = ctx->d_bsum.as<long long>();
+  a.blk_base = ctx->d_blk_base.as<long long>();
+  a.pair_owner_w = ctx->d_pair_owner.as<int>();
+  a.blk_off_w = ctx->d_blk_off.as<long long>();
+  a.talpha = ctx->d_talpha.as<int>();
   a.pair_off = ctx->d_pair_off.as<int>();
   a.neigh_j = ctx->d_neigh_j.as<int>();
   a.neigh_b = ctx->d_neigh_b.as<int>();
@@ -321,55 +376,30 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   return a;
 }
 
-// everything after the pair lists exist on the device: neigh_back, block
-// offsets, common neighbors, block storage
+// everything after the pair lists exist on the device: neigh_back, common
+// neighbors, block storage
 static int finish_neighbors(fb_ctx *ctx) {
   int N = ctx->N, P = ctx->P;
-  // pair owner and block offsets from the host copy of the lists
-  std::vector<int> nj(P), owner(P), self(N);
-  CU(cudaMemcpyAsync(nj.data(), ctx->d_neigh_j.p, P * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(self.data(), ctx->d_neigh_self.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
-  std::vector<long long> blk(P + 1);
-  long long off = 0;
-  for (int i = 0; i < N; i++) {
-    if (self[i] < 0) return fail(ctx, FB_ERR_NEIGH_SELF, "no neigh_self for atom %d", i + 1);
-    int ni = ctx->fdh.sp[ctx->h_isp[i]].norb;
-    for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
-      owner[p] = i;
-      blk[p] = off;
-      off += (long long)ni * ctx->fdh.sp[ctx->h_isp[nj[p]]].norb;
-    }
-  }
-  blk[P] = off;
-  ctx->nblock = off;
-  CHK(ctx->d_pair_owner.ensure(P * sizeof(int) + 4));
-  CHK(ctx->d_blk_off.ensure((P + 1) * sizeof(long long)));
   CHK(ctx->d_neigh_back.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
   CHK(ctx->d_r3f.ensure(3 * P * sizeof(float) + 8));
-  CU(cudaMemcpyAsync(ctx->d_pair_owner.p, owner.data(), P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  CU(cudaMemcpyAsync(ctx->d_blk_off.p, blk.data(), (P + 1) * sizeof(long long), cudaMemcpyHostToDevice,
-                     ctx->stream));
   NeighArgs a = neigh_args(ctx);
-  KL(launch_neigh_back(a, ctx->stream));
+  KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
   // common neighbors
   CHK(ctx->d_tcnt.ensure(N * sizeof(int)));
   a = neigh_args(ctx);
-  KL(launch_common(a, false, ctx->stream));
+  KL(KT_COMMON_COUNT, launch_common(a, false, ctx->stream));
   std::vector<int> tc(N);
   CU(cudaMemcpyAsync(tc.data(), ctx->d_tcnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
+  if (ctx->timing) timing_drain(ctx);
   ctx->h_trip_off.assign(N + 1, 0);
   for (int i = 0; i < N; i++) ctx->h_trip_off[i + 1] = ctx->h_trip_off[i] + tc[i];
   int T = ctx->h_trip_off[N];
   ctx->T = T;
-  std::vector<int> talpha(T);
-  for (int i = 0; i < N; i++)
-    for (int t = ctx->h_trip_off[i]; t < ctx->h_trip_off[i + 1]; t++) talpha[t] = i;
   size_t tb = (size_t)T * sizeof(int) + 4;
   CHK(ctx->d_trip_off.ensure((N + 1) * sizeof(int)));
   CHK(ctx->d_ci_j.ensure(tb));
@@ -381,9 +411,8 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_talpha.ensure(tb));
   CU(cudaMemcpyAsync(ctx->d_trip_off.p, ctx->h_trip_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
                      ctx->stream));
-  CU(cudaMemcpyAsync(ctx->d_talpha.p, talpha.data(), T * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   a = neigh_args(ctx);
-  KL(launch_common(a, true, ctx->stream));
+  KL(KT_COMMON_FILL, launch_common(a, true, ctx->stream));
   // block storage
   size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
   CHK(ctx->d_S.ensure(bb));
@@ -391,6 +420,7 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_vb.ensure(bb));
   CHK(ctx->d_vbo.ensure(bb));
   CU(cudaStreamSynchronize(ctx->stream));
+  if (ctx->timing) timing_drain(ctx);
   ctx->have_neigh = true;
   ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = false;
   ctx->assembled = ctx->dassembled = 0;
@@ -404,26 +434,41 @@ int fb_neighbors(fb_ctx *ctx) {
   int N = ctx->N;
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
   CHK(ctx->d_cnt.ensure(N * sizeof(int)));
+  CHK(ctx->d_bsum.ensure(N * sizeof(long long)));
   NeighArgs a = neigh_args(ctx);
-  KL(launch_neigh(a, false, ctx->stream));
+  KL(KT_NEIGH_COUNT, launch_neigh(a, false, ctx->stream));
   std::vector<int> cnt(N);
+  std::vector<long long> bsum(N), bbase(N);
   CU(cudaMemcpyAsync(cnt.data(), ctx->d_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(bsum.data(), ctx->d_bsum.p, N * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
   ctx->h_pair_off.assign(N + 1, 0);
-  for (int i = 0; i < N; i++) ctx->h_pair_off[i + 1] = ctx->h_pair_off[i] + cnt[i];
+  long long nb = 0;
+  for (int i = 0; i < N; i++) {
+    ctx->h_pair_off[i + 1] = ctx->h_pair_off[i] + cnt[i];
+    bbase[i] = nb;
+    nb += bsum[i];
+  }
   int P = ctx->h_pair_off[N];
   ctx->P = P;
+  ctx->nblock = nb;
   CHK(ctx->d_pair_off.ensure((N + 1) * sizeof(int)));
+  CHK(ctx->d_blk_base.ensure(N * sizeof(long long)));
   CHK(ctx->d_neigh_j.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_neigh_b.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_neigh_self.ensure(N * sizeof(int)));
+  CHK(ctx->d_pair_owner.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_blk_off.ensure((P + 1) * sizeof(long long)));
   CU(cudaMemcpyAsync(ctx->d_pair_off.p, ctx->h_pair_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_blk_base.p, bbase.data(), N * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_blk_off.as<long long>() + P, &ctx->nblock, sizeof(long long), cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaMemsetAsync(ctx->d_neigh_self.p, 0xff, N * sizeof(int), ctx->stream));
   a = neigh_args(ctx);
-  KL(launch_neigh(a, true, ctx->stream));
+  KL(KT_NEIGH_FILL, launch_neigh(a, true, ctx->stream));
   return finish_neighbors(ctx);
 }
 
@@ -460,6 +505,26 @@ int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const i
   CU(cudaMemcpyAsync(ctx->d_neigh_j.p, nj.data(), P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_neigh_b.p, neigh_b, P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_neigh_self.p, self.data(), N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<int> owner(P);
+  std::vector<long long> blk(P + 1);
+  long long off = 0;
+  for (int i = 0; i < N; i++) {
+    if (self[i] < 0) return fail(ctx, FB_ERR_NEIGH_SELF, "no neigh_self for atom %d", i + 1);
+    int ni = ctx->fdh.sp[ctx->h_isp[i]].norb;
+    for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
+      owner[p] = i;
+      blk[p] = off;
+      off += (long long)ni * ctx->fdh.sp[ctx->h_isp[nj[p]]].norb;
+    }
+  }
+  blk[P] = off;
+  ctx->nblock = off;
+  CHK(ctx->d_pair_owner.ensure(P * sizeof(int) + 4));
+  CHK(ctx->d_blk_off.ensure((P + 1) * sizeof(long long)));
+  CU(cudaMemcpyAsync(ctx->d_pair_owner.p, owner.data(), P * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_blk_off.p, blk.data(), (P + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
   return finish_neighbors(ctx);
 }
 
@@ -567,8 +632,8 @@ int fb_assemble(fb_ctx *ctx, unsigned what) {
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
   AsmArgs a = asm_args(ctx);
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
-  if (w2) KL(launch_assemble_2c(a, w2, ctx->stream));
-  if (what & FB_VNA3C) KL(launch_assemble_3c(a, ctx->stream));
+  if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
+  if (what & FB_VNA3C) KL(KT_ASM3C, launch_assemble_3c(a, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
@@ -628,6 +693,20 @@ int fb_set_denmat(fb_ctx *ctx, const double *rho, const double *cape) {
   return FB_OK;
 }
 
+int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev) {
+  if (!ctx || !rho_dev) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  CU(cudaSetDevice(ctx->device));
+  size_t bb = (size_t)ctx->nblock * sizeof(double);
+  CHK(ctx->d_rho.ensure(bb + 8));
+  CHK(ctx->d_cape.ensure(bb + 8));
+  CU(cudaMemcpyAsync(ctx->d_rho.p, rho_dev, bb, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (cape_dev) CU(cudaMemcpyAsync(ctx->d_cape.p, cape_dev, bb, cudaMemcpyDeviceToDevice, ctx->stream));
+  else CU(cudaMemsetAsync(ctx->d_cape.p, 0, bb, ctx->stream));
+  ctx->have_rho = true;
+  return FB_OK;
+}
+
 int fb_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
@@ -658,9 +737,9 @@ int fb_dassemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   a.keep_dblocks = keep;
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
-  if (w2) KL(launch_dassemble_2c(a, w2, ctx->stream));
-  if (what & FB_VNA3C) KL(launch_dassemble_3c(a, ctx->stream));
-  KL(launch_build_forces(a, what & FB_ALL, ctx->stream));
+  if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
+  if (what & FB_VNA3C) KL(KT_DASM3C, launch_dassemble_3c(a, ctx->stream));
+  KL(KT_FORCES, launch_build_forces(a, what & FB_ALL, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
@@ -701,6 +780,42 @@ int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T, dou
   if (T && (st = fb_get_blocks(ctx, FB_BLOCK_T, T))) return st;
   if (vna && (st = fb_get_blocks(ctx, FB_BLOCK_VNA, vna))) return st;
   if (vnao && (st = fb_get_blocks(ctx, FB_BLOCK_VNAO, vnao))) return st;
+  return FB_OK;
+}
+
+int fb_set_timing(fb_ctx *ctx, int enable) {
+  if (!ctx) return FB_ERR_ARG;
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->pending.clear();
+  ctx->timing = enable != 0;
+  for (int k = 0; k < KT_N; k++) {
+    ctx->kt_ms[k] = 0.0;
+    ctx->kt_n[k] = 0;
+  }
+  return FB_OK;
+}
+
+int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms, long long *launches) {
+  if (!ctx || !kernel) return FB_ERR_ARG;
+  CU(cudaStreamSynchronize(ctx->stream));
+  timing_drain(ctx);
+  for (int k = 0; k < KT_N; k++)
+    if (std::strcmp(kernel, kt_names[k]) == 0) {
+      if (total_ms) *total_ms = ctx->kt_ms[k];
+      if (launches) *launches = ctx->kt_n[k];
+      return FB_OK;
+    }
+  return fail(ctx, FB_ERR_ARG, "unknown kernel name %s", kernel);
+}
+
+int fb_probe_fp64(fb_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  double ms = 0.0, flops = 0.0;
+  int st = fb::probe_dfma(ctx->stream, &ms, &flops);
+  if (st) return fail(ctx, FB_ERR_CUDA, "fp64 probe: %s", cudaGetErrorString((cudaError_t)st));
+  ctx->launches += 2;
+  *tflops = flops / (ms * 1e-3) / 1e12;
   return FB_OK;
 }
 

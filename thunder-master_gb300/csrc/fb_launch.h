@@ -15,6 +15,11 @@ struct NeighArgs {
   const float *xlf;
   const int *imgs;
   int *cnt;
+  long long *bsum;
+  const long long *blk_base;
+  int *pair_owner_w;
+  long long *blk_off_w;
+  int *talpha;
   const int *pair_off;
   int *neigh_j, *neigh_b, *neigh_self, *neigh_back;
   const int *pair_owner;
@@ -56,5 +61,7 @@ int launch_assemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s);
+// DFMA throughput probe: one warm-up and one timed launch
+int probe_dfma(cudaStream_t s, double *ms, double *flops);
 
 }  // namespace fb

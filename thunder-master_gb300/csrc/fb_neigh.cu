@@ -15,8 +15,10 @@ template <bool FILL>
 __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__restrict__ ratomf,
                         const int *__restrict__ isp, const FdataDev *__restrict__ fd, const double *__restrict__ xl,
                         const float *__restrict__ xlf, const int *__restrict__ imgs, int nimg, int *__restrict__ cnt,
-                        const int *__restrict__ pair_off, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
-                        int *__restrict__ neigh_self, unsigned *__restrict__ status, int *__restrict__ errinfo) {
+                        long long *__restrict__ bsum, const int *__restrict__ pair_off,
+                        const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
+                        int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
+                        unsigned *__restrict__ status, int *__restrict__ errinfo) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
@@ -25,6 +27,9 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__
   float rfi0 = ratomf[3 * i], rfi1 = ratomf[3 * i + 1], rfi2 = ratomf[3 * i + 2];
   double rci = fd->sp[isp[i]].rcA;
   int num = 0, base = FILL ? pair_off[i] : 0;
+  long long norbsum = 0;  // sum of norb_j over the hits so far
+  long long bbase = FILL ? blk_base[i] : 0;
+  int ni = fd->sp[isp[i]].norb;
   for (int ii = 0; ii < nimg; ii++) {
     int mb = imgs[ii];
     float L0 = xlf[3 * mb], L1 = xlf[3 * mb + 1], L2 = xlf[3 * mb + 2];
@@ -52,16 +57,34 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__
         }
       }
       unsigned m = __ballot_sync(0xffffffffu, hit);
+      // inclusive warp scan of norb_j over the hit lanes -> block offsets
+      int nj = hit ? fd->sp[isp[j]].norb : 0;
+      int incl = nj;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += u;
+      }
       if (FILL && hit) {
         int idx = num + __popc(m & ((1u << lane) - 1u));
         neigh_j[base + idx] = j;
         neigh_b[base + idx] = mb;
+        pair_owner[base + idx] = i;
+        blk_off[base + idx] = bbase + (long long)ni * (norbsum + incl - nj);
         if (j == i && mb == 0) neigh_self[i] = idx;
       }
       num += __popc(m);
+      norbsum += __shfl_sync(0xffffffffu, incl, 31);
     }
   }
-  if (!FILL && lane == 0) cnt[i] = num;
+  if (!FILL && lane == 0) {
+    cnt[i] = num;
+    bsum[i] = (long long)ni * norbsum;
+  }
+  if (FILL) {
+    __syncwarp();
+    if (lane == 0 && neigh_self[i] < 0) atomicOr(status, DEVERR_SELF);
+  }
 }
 
 // neigh_back (M_neighbors.f90:469-486) and the per-pair vectors
@@ -109,7 +132,7 @@ __global__ void k_common(int N, const double *__restrict__ ratom, const int *__r
                          const double *__restrict__ r3v, const float *__restrict__ r3f, int *__restrict__ tcnt,
                          const int *__restrict__ trip_off, int *__restrict__ ci_j, int *__restrict__ ci_b,
                          int *__restrict__ cj_j, int *__restrict__ cj_b, int *__restrict__ cneigh,
-                         int *__restrict__ tdst) {
+                         int *__restrict__ tdst, int *__restrict__ talpha) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
@@ -167,6 +190,7 @@ __global__ void k_common(int N, const double *__restrict__ ratom, const int *__r
         cj_b[t] = jb;
         cneigh[t] = found;
         tdst[t] = q0 + found;
+        talpha[t] = ia;
       }
       num += __popc(m);
     }
@@ -178,11 +202,12 @@ int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   if (fill)
     k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.ratomf, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                             nullptr, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.status,
-                                             a.errinfo);
+                                             nullptr, nullptr, a.pair_off, a.blk_base, a.neigh_j, a.neigh_b,
+                                             a.neigh_self, a.pair_owner_w, a.blk_off_w, a.status, a.errinfo);
   else
     k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.ratomf, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                              a.cnt, nullptr, nullptr, nullptr, nullptr, a.status, a.errinfo);
+                                              a.cnt, a.bsum, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                              nullptr, a.status, a.errinfo);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -201,11 +226,11 @@ int launch_common(const NeighArgs &a, bool fill, cudaStream_t s) {
   if (fill)
     k_common<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j, a.neigh_b,
                                               a.neigh_self, a.r3v, a.r3f, nullptr, a.trip_off, a.ci_j, a.ci_b,
-                                              a.cj_j, a.cj_b, a.cneigh, a.tdst);
+                                              a.cj_j, a.cj_b, a.cneigh, a.tdst, a.talpha);
   else
     k_common<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j, a.neigh_b,
                                                a.neigh_self, a.r3v, a.r3f, a.tcnt, nullptr, nullptr, nullptr,
-                                               nullptr, nullptr, nullptr, nullptr);
+                                               nullptr, nullptr, nullptr, nullptr, nullptr);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -70,7 +70,14 @@ _SIGS = {
     "fb_get_forces": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fb_assemble_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "fb_set_denmat_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "fb_get_timing": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+    "fb_probe_fp64": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
 }
+
+KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
+           "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces")
 
 
 class FBError(RuntimeError):
@@ -225,6 +232,10 @@ class Context:
         self._check(self.L.fb_set_denmat(self.h, rho, _ptr(cape)))
         self._cape_keep = cape
 
+    def set_denmat_device(self, rho_ptr, cape_ptr=None):
+        self._check(self.L.fb_set_denmat_device(self.h, C.c_void_p(rho_ptr),
+                                                None if cape_ptr is None else C.c_void_p(cape_ptr)))
+
     def Dassemble(self, what=FB_ALL, keep_dblocks=False):
         self._check(self.L.fb_dassemble(self.h, what | (FB_KEEP_DBLOCKS if keep_dblocks else 0)))
 
@@ -243,3 +254,21 @@ class Context:
 
     def kernel_launches(self):
         return int(self.L.fb_kernel_launches(self.h))
+
+    def set_timing(self, enable=True):
+        self._check(self.L.fb_set_timing(self.h, int(bool(enable))))
+
+    def timing(self):
+        """{kernel: (total device ms, launches)} since set_timing(True)."""
+        out = {}
+        for k in KERNELS:
+            ms, n = C.c_double(), C.c_longlong()
+            self._check(self.L.fb_get_timing(self.h, k.encode(), C.byref(ms), C.byref(n)))
+            out[k] = (ms.value, n.value)
+        return out
+
+    def probe_fp64(self):
+        """Measured FP64 FMA throughput, TFLOP/s."""
+        t = C.c_double()
+        self._check(self.L.fb_probe_fp64(self.h, C.byref(t)))
+        return t.value
