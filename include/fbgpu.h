@@ -193,6 +193,32 @@ int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,
                   long long *launches);
 
+/* Allocation-free force pass.  No counterpart in the reference: it exists
+ * for callers that cannot allocate GPU memory while they run the force pass,
+ * for example a driver that hands the whole GPU to a pre-sized memory pool,
+ * or an MD loop that must not call the CUDA allocator between steps (an
+ * allocation synchronizes the device and can fail once memory fragments).
+ *
+ * Computes what fb_dassemble(ctx, FB_ALL) + fb_get_forces(ctx, FB_F_TOT)
+ * compute, for the structure and neighbor maps already on the context:
+ *   rho_dev, cape_dev  device pointers, nblock doubles each, block layout;
+ *                      cape_dev may be NULL (no Pulay term)
+ *   ftot_dev           device pointer, 3*natoms doubles, written
+ * The call makes no cudaMalloc, cudaFree or other allocating call.  Its
+ * intermediate per-pair and per-atom terms live in one statically sized
+ * device array of the library, which every GPU that loads the library holds
+ * until the process exits (8.25 MiB); systems with more than
+ * FB_NOALLOC_MAX_PAIRS pairs or FB_NOALLOC_MAX_ATOMS atoms are rejected with
+ * FB_ERR_CAPACITY.  All calls share that array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (two streams, two contexts on
+ * one device) race and must be serialized by the caller.  The first call on
+ * each device looks up the array's device address; make that first call
+ * before any stream capture.  Returns after the work completes. */
+#define FB_NOALLOC_MAX_PAIRS 65536
+#define FB_NOALLOC_MAX_ATOMS 16384
+int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev,
+                         const double *cape_dev, double *ftot_dev);
+
 /* Measured FP64 FMA throughput of this GPU in TFLOP/s (a DFMA-chain kernel,
  * about 0.1 s); the denominator of the FP64 roofline.  No reference
  * counterpart. */

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -820,3 +821,79 @@ int fb_probe_fp64(fb_ctx *ctx, double *tflops) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free force pass (fb_dassemble_noalloc).  Its scratch is this
+// file-scope device array: per pair sumT, sumS, vna_ontop, vna_atom (12
+// doubles), per atom f3naa, f3nab, f3nac, kinetic, vna, pulay (18 doubles).
+// In host code the name g_noalloc_scratch is only a host-side stand-in, so
+// the kernels get the device address from cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double
+    g_noalloc_scratch[12 * FB_NOALLOC_MAX_PAIRS + 18 * FB_NOALLOC_MAX_ATOMS];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[128];  // device address per device ordinal
+
+// once per device, with that device current
+static int noalloc_scratch(fb_ctx *ctx, double **out) {
+  if (ctx->device < 0 || ctx->device >= 128) return fail(ctx, FB_ERR_ARG, "device ordinal %d", ctx->device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[ctx->device]) {
+    double *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ctx, FB_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[ctx->device] = p;
+  }
+  *out = g_noalloc_ptr[ctx->device];
+  return FB_OK;
+}
+
+extern "C" int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev, const double *cape_dev, double *ftot_dev) {
+  if (!ctx || !rho_dev || !ftot_dev) return FB_ERR_ARG;
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  int N = ctx->N, P = ctx->P;
+  if (P > FB_NOALLOC_MAX_PAIRS || N > FB_NOALLOC_MAX_ATOMS)
+    return fail(ctx, FB_ERR_CAPACITY,
+                "fb_dassemble_noalloc handles at most %d pairs and %d atoms; this system has %d pairs, %d atoms",
+                FB_NOALLOC_MAX_PAIRS, FB_NOALLOC_MAX_ATOMS, P, N);
+  CU(cudaSetDevice(ctx->device));
+  double *scr = nullptr;
+  CHK(noalloc_scratch(ctx, &scr));
+  AsmArgs a = asm_args(ctx);
+  a.rho = rho_dev;
+  a.cape = cape_dev;
+  a.keep_dblocks = false;
+  a.dS = a.dT = nullptr;
+  double *pp = scr, *pa = scr + 12 * FB_NOALLOC_MAX_PAIRS;
+  a.sumT = pp;
+  a.sumS = pp + 3 * (size_t)P;
+  a.ontop = pp + 6 * (size_t)P;
+  a.atomf = pp + 9 * (size_t)P;
+  a.f3naa = pa;
+  a.f3nab = pa + 3 * (size_t)N;
+  a.f3nac = pa + 6 * (size_t)N;
+  a.kin = pa + 9 * (size_t)N;
+  a.vna = pa + 12 * (size_t)N;
+  a.pul = pa + 15 * (size_t)N;
+  a.ftot = ftot_dev;
+  // the three-center terms are accumulated with atomics: clear them (the
+  // array keeps the previous call's values); every other term is overwritten
+  CU(cudaMemsetAsync(a.f3naa, 0, 9 * (size_t)N * sizeof(double), ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  unsigned what = cape_dev ? FB_ALL : (FB_ALL & ~FB_S);
+  int e;
+  if ((e = launch_dassemble_2c(a, what & (FB_S | FB_T | FB_VNA2C), ctx->stream)))
+    return fail(ctx, FB_ERR_CUDA, "launch dassemble_2c: %s", cudaGetErrorString((cudaError_t)e));
+  if ((e = launch_dassemble_3c(a, ctx->stream)))
+    return fail(ctx, FB_ERR_CUDA, "launch dassemble_3c: %s", cudaGetErrorString((cudaError_t)e));
+  if ((e = launch_build_forces(a, what, ctx->stream)))
+    return fail(ctx, FB_ERR_CUDA, "launch build_forces: %s", cudaGetErrorString((cudaError_t)e));
+  ctx->launches += 3;
+  unsigned st = 0;
+  CU(cudaMemcpyAsync(&st, ctx->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (st) return status_error(ctx, st);
+  return FB_OK;
+}

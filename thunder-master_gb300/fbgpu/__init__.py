@@ -74,6 +74,7 @@ _SIGS = {
     "fb_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "fb_get_timing": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "fb_probe_fp64": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fb_dassemble_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
