@@ -1,0 +1,148 @@
+"""System-level property tests of the oracle (CPU only): neighbor maps
+against a numpy brute force in the reference order, Hermiticity of the
+assembled blocks, forces against finite differences of the band energy,
+invariance under rigid motions, and the reference's error stops."""
+import numpy as np
+import pytest
+
+from conftest import symmetric_denmat, workload
+from fbgpu import synth
+from oracle import oracle as orc
+
+
+def _system(name, root, threads=1, st=None):
+    path, nZ, st0 = workload(name, root)
+    st = st or st0
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice, threads=threads).neighbors()
+    norb = np.array([fd.norb(int(k)) for k in st.imass])
+    return fd, s, st, norb
+
+
+def _xl(lattice):
+    out = [np.zeros(3)]
+    for iz in range(-4, 5):
+        for iy in range(-4, 5):
+            for ix in range(-4, 5):
+                if ix or iy or iz:
+                    out.append(ix * lattice[0] + iy * lattice[1] + iz * lattice[2])
+    return np.array(out)
+
+
+@pytest.mark.parametrize("name", ["si64", "cho_small", "sic_vac"])
+def test_neighbors_match_brute_force(fdata_root, name):
+    fd, s, st, norb = _system(name, fdata_root)
+    xl = _xl(st.lattice)
+    path, nZ, _ = workload(name, fdata_root)
+    sp = synth.species_for({"si64": "si64", "cho_small": "cho1536", "sic_vac": "sic4096"}[name])
+    rc = np.array([max(r * 0.529177 for r in x.rcutoff) for x in sp])[st.imass - 1]
+    N = st.natoms
+    for i in range(N):
+        want = []
+        for mb in range(len(xl)):
+            d = np.linalg.norm(st.ratom + xl[mb] - st.ratom[i], axis=1)
+            for j in np.nonzero(d < rc[i] + rc - 0.01)[0]:
+                want.append((j, mb))
+        got = list(zip(s.neigh_j[s.pair_off[i]:s.pair_off[i + 1]], s.neigh_b[s.pair_off[i]:s.pair_off[i + 1]]))
+        assert got == want
+    # neigh_self and neigh_back
+    for i in range(N):
+        p = s.pair_off[i] + s.neigh_self[i]
+        assert s.neigh_j[p] == i and s.neigh_b[p] == 0
+        for p in range(s.pair_off[i], s.pair_off[i + 1]):
+            j, q = s.neigh_j[p], s.pair_off[s.neigh_j[p]] + s.neigh_back[p]
+            assert s.neigh_j[q] == i
+            assert np.allclose(xl[s.neigh_b[p]] + xl[s.neigh_b[q]], 0.0, atol=1e-9)
+
+
+def test_common_neighbors_are_pairs_within_cutoff(fdata_root):
+    fd, s, st, norb = _system("si64", fdata_root)
+    xl = _xl(st.lattice)
+    for a in range(st.natoms):
+        for t in range(s.trip_off[a], s.trip_off[a + 1]):
+            i, j = s.ci_j[t], s.cj_j[t]
+            r1 = st.ratom[i] + xl[s.ci_b[t]]
+            r2 = st.ratom[j] + xl[s.cj_b[t]]
+            q = s.pair_off[i] + s.cneigh[t]
+            assert s.neigh_j[q] == j
+            assert np.allclose(st.ratom[j] + xl[s.neigh_b[q]] - st.ratom[i], r2 - r1, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["si64", "cho_small", "sic_small"])
+def test_blocks_hermitian(fdata_root, name):
+    fd, s, st, norb = _system(name, fdata_root)
+    S, T, vb, vbo = s.assemble()
+    H = T + vb + vbo
+    for B, tol in ((S, 1e-13), (T, 1e-12), (H, 1e-11)):
+        for i in range(st.natoms):
+            for p in range(s.pair_off[i], s.pair_off[i + 1]):
+                j = s.neigh_j[p]
+                q = s.pair_off[j] + s.neigh_back[p]
+                a = B[s.blk_off[p]:s.blk_off[p + 1]].reshape(norb[j], norb[i]).T
+                b = B[s.blk_off[q]:s.blk_off[q + 1]].reshape(norb[i], norb[j]).T
+                assert np.abs(a - b.T).max() < tol
+
+
+def _band_energy(fd, st, ratom, rho, cape, layout):
+    s = orc.System(fd, ratom, st.imass, st.lattice).neighbors()
+    assert s.npairs == layout.npairs and np.array_equal(s.neigh_j[:s.npairs], layout.neigh_j[:s.npairs])
+    S, T, vb, vbo = s.assemble()
+    return float(rho @ (T + vb + vbo) - cape @ S)
+
+
+@pytest.mark.parametrize("name", ["si_vac", "cho_small"])
+def test_forces_are_minus_gradient_of_band_energy(fdata_root, name):
+    """ftot = -dE/dR for E = sum rho.(T + vna + vnao) - sum cape.S at fixed
+    density matrices: checks the whole derivative chain of the oracle."""
+    fd, s, st, norb = _system(name, fdata_root)
+    rho, cape = symmetric_denmat(s, norb, 11)
+    f = s.dassemble(rho, cape)["ftot"].reshape(-1, 3)
+    h = 1e-5
+    rng = np.random.default_rng(3)
+    for i in rng.choice(st.natoms, 4, replace=False):
+        for k in range(3):
+            rp, rm = st.ratom.copy(), st.ratom.copy()
+            rp[i, k] += h
+            rm[i, k] -= h
+            g = (_band_energy(fd, st, rp, rho, cape, s) - _band_energy(fd, st, rm, rho, cape, s)) / (2 * h)
+            assert abs(-g - f[i, k]) < 1e-5 * max(1.0, abs(g)), (i, k, -g, f[i, k])
+
+
+def test_rigid_motion_invariance(fdata_root):
+    fd, s, st, norb = _system("si64", fdata_root)
+    S, T, vb, vbo = s.assemble()
+    Q, _ = np.linalg.qr(np.random.default_rng(5).normal(size=(3, 3)))
+    if np.linalg.det(Q) < 0:
+        Q[:, 0] *= -1
+    st2 = synth.Structure(st.ratom @ Q.T + np.array([0.3, -1.1, 2.0]), st.imass, st.lattice @ Q.T)
+    s2 = orc.System(fd, st2.ratom, st2.imass, st2.lattice).neighbors()
+    assert np.array_equal(s.neigh_j, s2.neigh_j) and np.array_equal(s.neigh_b, s2.neigh_b)
+    S2, T2, vb2, vbo2 = s2.assemble()
+    for A, B in ((S, S2), (T, T2), (vb, vb2), (vbo, vbo2)):
+        for p in range(s.npairs):
+            a = A[s.blk_off[p]:s.blk_off[p + 1]]
+            b = B[s.blk_off[p]:s.blk_off[p + 1]]
+            assert abs(np.linalg.norm(a) - np.linalg.norm(b)) < 1e-10 * max(1.0, np.linalg.norm(a))
+
+
+def test_atoms_too_close_is_an_error(fdata_root):
+    path, nZ, st = workload("si64", fdata_root)
+    r = st.ratom.copy()
+    r[1] = r[0] + np.array([0.3, 0.0, 0.0])
+    fd = orc.Fdata(path, nZ)
+    with pytest.raises(orc.OracleError) as ei:
+        orc.System(fd, r, st.imass, st.lattice).neighbors()
+    assert ei.value.code == 6
+
+
+def test_parallel_oracle_matches_serial(fdata_root):
+    fd, s1, st, norb = _system("cho_small", fdata_root, threads=1)
+    _, s4, _, _ = _system("cho_small", fdata_root, threads=4)
+    assert np.array_equal(s1.neigh_j, s4.neigh_j) and np.array_equal(s1.cneigh, s4.cneigh)
+    a1, a4 = s1.assemble(), s4.assemble()
+    for x, y in zip(a1, a4):
+        assert np.abs(x - y).max() < 1e-12
+    rho, cape = symmetric_denmat(s1, norb, 5)
+    f1 = s1.dassemble(rho, cape)["ftot"]
+    f4 = s4.dassemble(rho, cape)["ftot"]
+    assert np.abs(f1 - f4).max() < 1e-11

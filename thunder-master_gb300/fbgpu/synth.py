@@ -215,13 +215,19 @@ _AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P
 
 
 def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi):
-    """Seeded channel function of the canonical orientation."""
+    """Seeded channel function of the canonical orientation.  The m != 0
+    channels equal the m = 0 channel plus t^2 times their own function, so
+    all channels of a shell pair agree at zero separation (on-site blocks are
+    then rotation invariant, as a physical table's are)."""
     sa, la, ma = oa
     sb, lb, mb = ob
+    rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, 0))
+    val = _AMP2[itype] * _f1d(rng.normal(0.0, 1.0, 12), t, (la + lb) % 2 == 1)
     mkey = ma if asym_pi else abs(ma)
-    rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey))
-    coef = rng.normal(0.0, 1.0, 12)
-    return _AMP2[itype] * _f1d(coef, t, (la + lb) % 2 == 1)
+    if mkey != 0:
+        rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey))
+        val = val + t * t * _AMP2[itype] * _f1d(rng.normal(0.0, 1.0, 12), t, False)
+    return val
 
 
 def _canonical(zA, oa, zB, ob):
