@@ -181,6 +181,7 @@ def run_gpu(args):
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
     ctx.read_Fdata(path, nZ)
+    ctx.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
     ctx.set_structure(st.ratom, st.imass, st.lattice)
     P, T, NB = ctx.driver_neighbors()
     nbm = ctx.neighbors()
@@ -287,6 +288,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
+                   "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MiB write)", "forces": True},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -361,6 +363,8 @@ def main():
     ap.add_argument("--impl", default="fbgpu", choices=["fbgpu", "reference"])
     ap.add_argument("--workload", default="si512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    ap.add_argument("--prec", default="df", choices=["df", "fp64"],
+                    help="three-center arithmetic: double-float on the FP32 pipe (default) or FP64")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -179,6 +179,18 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out);
 int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T,
                      double *vna, double *vnao);
 
+/* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
+ * table contractions, rotations, frame derivatives and density contractions
+ * run in double-float arithmetic on the FP32 pipe (two floats per value,
+ * 48-bit significand), while every grid-cell, stencil, cutoff and
+ * interpolation-branch decision is still made in FP64 exactly as the
+ * reference makes it; GB300 executes FP64 at 1/64 of its FP32 rate.
+ * FB_PREC_FP64: every operation in FP64.  Systems with d shells always use
+ * FP64.  No reference counterpart (the reference computes in FP64). */
+#define FB_PREC_FP64 0
+#define FB_PREC_DF 1
+int fb_set_precision(fb_ctx *ctx, int mode);
+
 /* Number of kernels this context launched since creation (diagnostics). */
 long long fb_kernel_launches(const fb_ctx *ctx);
 
@@ -187,7 +199,7 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * fb_get_timing returns the accumulated device time and launch count of one
  * kernel: "neigh_count", "neigh_fill", "neigh_back", "common_count",
  * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
- * "dassemble_3c", "build_forces".  No reference counterpart (the reference
+ * "dassemble_3c", "build_forces", "trip_bins", "split_rho".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,
@@ -223,6 +235,10 @@ int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev,
  * about 0.1 s); the denominator of the FP64 roofline.  No reference
  * counterpart. */
 int fb_probe_fp64(fb_ctx *ctx, double *tflops);
+/* Measured FP32 FMA throughput in TFLOP/s (FFMA chains); the denominator of
+ * the FP32-pipe roofline of the double-float kernels.  No reference
+ * counterpart. */
+int fb_probe_fp32(fb_ctx *ctx, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -58,12 +58,17 @@ def test_neighbors_bit_exact(gpu_ctx, fdata_root, name):
     assert np.array_equal(cm["neigh_common"], s.cneigh[:T] + 1)
 
 
+PRECS = [0, 1]  # FB_PREC_FP64, FB_PREC_DF (double-float three-center kernels)
+
+
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("name", CASES)
-def test_blocks_match_oracle(gpu_ctx, fdata_root, name):
+def test_blocks_match_oracle(gpu_ctx, fdata_root, name, prec):
     path, nZ, st = workload(name, fdata_root)
     fd, s = _oracle(path, nZ, st)
     S0, T0, vb0, vbo0 = s.assemble()
     ctx = gpu_ctx
+    ctx.set_precision(prec)
     ctx.read_Fdata(path, nZ)
     ctx.set_structure(st.ratom, st.imass, st.lattice)
     ctx.driver_neighbors()
@@ -74,17 +79,19 @@ def test_blocks_match_oracle(gpu_ctx, fdata_root, name):
     for key, ref in (("S", S0), ("T", T0), ("vna", vb0), ("vnao", vbo0)):
         got = ctx.blocks(key)
         err = np.abs(got - ref).max()
-        assert err <= TOL_BLOCK, "%s %s max |diff| %.3e" % (name, key, err)
+        assert err <= TOL_BLOCK, "%s prec %d %s max |diff| %.3e" % (name, prec, key, err)
 
 
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("name", CASES)
-def test_forces_match_oracle(gpu_ctx, fdata_root, name):
+def test_forces_match_oracle(gpu_ctx, fdata_root, name, prec):
     path, nZ, st = workload(name, fdata_root)
     fd, s = _oracle(path, nZ, st)
     norb = np.array([fd.norb(int(k)) for k in st.imass])
     rho, cape = symmetric_denmat(s, norb, 42)
     ref = s.dassemble(rho, cape)
     ctx = gpu_ctx
+    ctx.set_precision(prec)
     ctx.read_Fdata(path, nZ)
     ctx.set_structure(st.ratom, st.imass, st.lattice)
     ctx.driver_neighbors()
@@ -93,7 +100,7 @@ def test_forces_match_oracle(gpu_ctx, fdata_root, name):
     for key in ("ftot", "kinetic", "vna", "pulay", "f3naa", "f3nab", "f3nac", "vna_ontop", "vna_atom"):
         got = ctx.forces(key)
         err = np.abs(got - ref[key]).max()
-        assert err <= TOL_FORCE, "%s %s max |diff| %.3e" % (name, key, err)
+        assert err <= TOL_FORCE, "%s prec %d %s max |diff| %.3e" % (name, prec, key, err)
     for key in ("dS", "dT"):
         err = np.abs(ctx.blocks(key) - ref[key]).max()
         assert err <= TOL_FORCE, "%s %s max |diff| %.3e" % (name, key, err)
@@ -112,3 +119,31 @@ def test_step_through_host_buffers(gpu_ctx, fdata_root):
     ctx.assemble_step(np.ascontiguousarray(st.ratom.ravel()), *outs)
     for got, ref in zip(outs, (S0, T0, vb0, vbo0)):
         assert np.abs(got - ref).max() <= TOL_BLOCK
+
+
+@pytest.mark.slow
+def test_si512_full_size_parity(gpu_ctx, fdata_root):
+    """Configuration 2 at full size: neighbor maps bit-exact, blocks and
+    forces within tolerance, both precision modes."""
+    path, nZ, st = workload("si512", fdata_root)
+    fd, s = _oracle(path, nZ, st, threads=16)
+    S0, T0, vb0, vbo0 = s.assemble()
+    norb = np.array([fd.norb(int(k)) for k in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 7)
+    ref = s.dassemble(rho, cape)
+    ctx = gpu_ctx
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    assert ctx.driver_neighbors() == (s.npairs, s.ntrip, s.nblock)
+    nb = ctx.neighbors()
+    assert np.array_equal(nb["neigh_j"], s.neigh_j[:s.npairs] + 1)
+    assert np.array_equal(ctx.common_neighbors()["neigh_common"], s.cneigh[:s.ntrip] + 1)
+    for prec in PRECS:
+        ctx.set_precision(prec)
+        ctx.assemble()
+        for key, r in (("S", S0), ("T", T0), ("vna", vb0), ("vnao", vbo0)):
+            assert np.abs(ctx.blocks(key) - r).max() <= TOL_BLOCK, (prec, key)
+        ctx.set_denmat(rho, cape)
+        ctx.Dassemble()
+        assert np.abs(ctx.forces("ftot") - ref["ftot"]).max() <= TOL_FORCE, prec
+    ctx.set_precision(1)

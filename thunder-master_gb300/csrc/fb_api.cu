@@ -18,10 +18,10 @@ using namespace fb;
 
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
-       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_N };
+       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
-                                     "build_forces"};
+                                     "build_forces", "trip_bins", "split_rho"};
 
 namespace {
 
@@ -60,24 +60,27 @@ struct fb_ctx {
   // Fdata
   bool have_fdata = false;
   FdataHost fdh;
-  DevBuf d_fd, d_tab2, d_tab3, d_lin, d_gxy;
+  DevBuf d_fd, d_tab2, d_tab3, d_tab3df, d_lin, d_gxy;
+  int prec = FB_PREC_DF;
   // structure
   int N = 0, icluster = 0, mbeta_max = 0;
   std::vector<double> h_xl;
   std::vector<int> h_isp, h_imgs;
   double lattice[9] = {0};
-  DevBuf d_ratom, d_ratomf, d_isp, d_xl, d_xlf, d_imgs;
+  float4 bbox_lo{}, bbox_hi{};
+  DevBuf d_ratom, d_pos4, d_isp, d_xl, d_xlf, d_imgs;
   // neighbors
   bool have_neigh = false;
   int P = 0, T = 0;
   long long nblock = 0;
   std::vector<int> h_pair_off, h_trip_off;
   DevBuf d_bsum, d_blk_base;
-  DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v, d_r3f,
+  DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
+  DevBuf d_tkey, d_trank, d_tperm, d_thist;
   DevBuf d_status, d_errinfo;
   // blocks
-  DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT;
+  DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
   // forces
@@ -196,14 +199,15 @@ void fb_destroy(fb_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   DevBuf *bufs[] = {&ctx->d_fd, &ctx->d_tab2, &ctx->d_tab3, &ctx->d_lin, &ctx->d_gxy, &ctx->d_ratom,
-                    &ctx->d_ratomf, &ctx->d_isp, &ctx->d_xl, &ctx->d_xlf, &ctx->d_imgs, &ctx->d_cnt,
+                    &ctx->d_pos4, &ctx->d_isp, &ctx->d_xl, &ctx->d_xlf, &ctx->d_imgs, &ctx->d_cnt,
                     &ctx->d_pair_off, &ctx->d_neigh_j, &ctx->d_neigh_b, &ctx->d_neigh_self, &ctx->d_neigh_back,
-                    &ctx->d_pair_owner, &ctx->d_r3v, &ctx->d_r3f, &ctx->d_blk_off, &ctx->d_tcnt,
+                    &ctx->d_pair_owner, &ctx->d_r3v, &ctx->d_blk_off, &ctx->d_tcnt,
                     &ctx->d_trip_off, &ctx->d_ci_j, &ctx->d_ci_b, &ctx->d_cj_j, &ctx->d_cj_b, &ctx->d_cneigh,
                     &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
-                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base};
+                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm,
+                    &ctx->d_thist};
   for (DevBuf *b : bufs) b->release();
   for (auto &e : ctx->evpool) {
     cudaEventDestroy(e.first);
@@ -233,11 +237,13 @@ int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies, const int *n
   CHK(ctx->d_fd.ensure(sizeof(FdataDev)));
   CHK(ctx->d_tab2.ensure(f.table2c.size() * sizeof(double)));
   CHK(ctx->d_tab3.ensure(f.table3c.size() * sizeof(double)));
+  CHK(ctx->d_tab3df.ensure(f.table3c_df.size() * sizeof(float)));
   CHK(ctx->d_lin.ensure(f.lin.size()));
   CHK(ctx->d_gxy.ensure(f.gxy.size() * sizeof(double)));
   CU(cudaMemcpy(ctx->d_fd.p, &f.dev, sizeof(FdataDev), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_tab2.p, f.table2c.data(), f.table2c.size() * sizeof(double), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_tab3.p, f.table3c.data(), f.table3c.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_tab3df.p, f.table3c_df.data(), f.table3c_df.size() * sizeof(float), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_lin.p, f.lin.data(), f.lin.size(), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_gxy.p, f.gxy.data(), f.gxy.size() * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_fdata = true;
@@ -325,12 +331,27 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
   CU(cudaSetDevice(ctx->device));
   int N = ctx->N;
   make_images(ctx, ratom);
-  std::vector<float> rf(ratom, ratom + 3 * N);
+  // float positions with the species cutoff in .w, and the bounding box
+  std::vector<float4> p4(N);
+  float rcmax = 0.0f;
+  for (int k = 0; k < ctx->fdh.nspecies; k++) rcmax = std::max(rcmax, (float)ctx->fdh.sp[k].rcA);
+  ctx->bbox_lo = make_float4(1e30f, 1e30f, 1e30f, rcmax);
+  ctx->bbox_hi = make_float4(-1e30f, -1e30f, -1e30f, 0.0f);
+  for (int i = 0; i < N; i++) {
+    p4[i] = make_float4((float)ratom[3 * i], (float)ratom[3 * i + 1], (float)ratom[3 * i + 2],
+                        (float)ctx->fdh.sp[ctx->h_isp[i]].rcA);
+    ctx->bbox_lo.x = std::min(ctx->bbox_lo.x, p4[i].x);
+    ctx->bbox_lo.y = std::min(ctx->bbox_lo.y, p4[i].y);
+    ctx->bbox_lo.z = std::min(ctx->bbox_lo.z, p4[i].z);
+    ctx->bbox_hi.x = std::max(ctx->bbox_hi.x, p4[i].x);
+    ctx->bbox_hi.y = std::max(ctx->bbox_hi.y, p4[i].y);
+    ctx->bbox_hi.z = std::max(ctx->bbox_hi.z, p4[i].z);
+  }
   CHK(ctx->d_ratom.ensure(3 * N * sizeof(double)));
-  CHK(ctx->d_ratomf.ensure(3 * N * sizeof(float)));
+  CHK(ctx->d_pos4.ensure(N * sizeof(float4)));
   CHK(ctx->d_imgs.ensure(ctx->h_imgs.size() * sizeof(int)));
   CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CU(cudaMemcpyAsync(ctx->d_ratomf.p, rf.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_pos4.p, p4.data(), N * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_imgs.p, ctx->h_imgs.data(), ctx->h_imgs.size() * sizeof(int), cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -344,7 +365,10 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.P = ctx->P;
   a.nimg = (int)ctx->h_imgs.size();
   a.ratom = ctx->d_ratom.as<double>();
-  a.ratomf = ctx->d_ratomf.as<float>();
+  a.pos4 = ctx->d_pos4.as<float4>();
+  a.bbox_lo = ctx->bbox_lo;
+  a.bbox_hi = ctx->bbox_hi;
+  a.periodic = ctx->icluster != 1;
   a.isp = ctx->d_isp.as<int>();
   a.fd = ctx->d_fd.as<FdataDev>();
   a.xl = ctx->d_xl.as<double>();
@@ -363,7 +387,6 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.neigh_back = ctx->d_neigh_back.as<int>();
   a.pair_owner = ctx->d_pair_owner.as<int>();
   a.r3v = ctx->d_r3v.as<double>();
-  a.r3f = ctx->d_r3f.as<float>();
   a.tcnt = ctx->d_tcnt.as<int>();
   a.trip_off = ctx->d_trip_off.as<int>();
   a.ci_j = ctx->d_ci_j.as<int>();
@@ -383,7 +406,6 @@ static int finish_neighbors(fb_ctx *ctx) {
   int N = ctx->N, P = ctx->P;
   CHK(ctx->d_neigh_back.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
-  CHK(ctx->d_r3f.ensure(3 * P * sizeof(float) + 8));
   NeighArgs a = neigh_args(ctx);
   KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
   unsigned st = 0;
@@ -414,6 +436,21 @@ static int finish_neighbors(fb_ctx *ctx) {
                      ctx->stream));
   a = neigh_args(ctx);
   KL(KT_COMMON_FILL, launch_common(a, true, ctx->stream));
+  // triplet processing order, binned by (species triple, 3c grid cell)
+  {
+    int nsp = ctx->fdh.nspecies, cells = 1;
+    for (int x = 0; x < nsp; x++)
+      for (int y = 0; y < nsp; y++)
+        for (int z = 0; z < nsp; z++)
+          cells = std::max(cells, ctx->fdh.dev.c3[x][y][z].nx * ctx->fdh.dev.c3[x][y][z].ny);
+    size_t nbins = (size_t)nsp * nsp * nsp * cells;
+    CHK(ctx->d_tkey.ensure(tb));
+    CHK(ctx->d_trank.ensure(tb));
+    CHK(ctx->d_tperm.ensure(tb));
+    CHK(ctx->d_thist.ensure(nbins * sizeof(int)));
+    KL(KT_TRIP_BINS, launch_trip_bins(a, T, nsp, cells, ctx->d_tkey.as<int>(), ctx->d_trank.as<int>(),
+                                      ctx->d_thist.as<int>(), ctx->d_tperm.as<int>(), ctx->stream));
+  }
   // block storage
   size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
   CHK(ctx->d_S.ensure(bb));
@@ -601,6 +638,7 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.cj_j = ctx->d_cj_j.as<int>();
   a.cj_b = ctx->d_cj_b.as<int>();
   a.tdst = ctx->d_tdst.as<int>();
+  a.tperm = ctx->d_tperm.as<int>();
   a.S = ctx->d_S.as<double>();
   a.T = ctx->d_T.as<double>();
   a.vb = ctx->d_vb.as<double>();
@@ -621,7 +659,17 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.pul = ctx->d_pul.as<double>();
   a.ftot = ctx->d_ftot.as<double>();
   a.status = ctx->d_status.as<unsigned>();
+  a.table3c_df = ctx->d_tab3df.as<float2>();
+  a.rho_df = ctx->d_rho_df.as<float2>();
   return a;
+}
+
+static bool use_df(const fb_ctx *ctx) { return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d; }
+
+int fb_set_precision(fb_ctx *ctx, int mode) {
+  if (!ctx || (mode != FB_PREC_FP64 && mode != FB_PREC_DF)) return FB_ERR_ARG;
+  ctx->prec = mode;
+  return FB_OK;
 }
 
 int fb_assemble(fb_ctx *ctx, unsigned what) {
@@ -634,7 +682,10 @@ int fb_assemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
-  if (what & FB_VNA3C) KL(KT_ASM3C, launch_assemble_3c(a, ctx->stream));
+  if (what & FB_VNA3C) {
+    if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(a, ctx->stream));
+    else KL(KT_ASM3C, launch_assemble_3c(a, ctx->stream));
+  }
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
@@ -739,7 +790,16 @@ int fb_dassemble(fb_ctx *ctx, unsigned what) {
   a.keep_dblocks = keep;
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
-  if (what & FB_VNA3C) KL(KT_DASM3C, launch_dassemble_3c(a, ctx->stream));
+  if (what & FB_VNA3C) {
+    if (use_df(ctx)) {
+      CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
+      a.rho_df = ctx->d_rho_df.as<float2>();
+      KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
+      KL(KT_DASM3C, launch_dassemble_3c_df(a, ctx->stream));
+    } else {
+      KL(KT_DASM3C, launch_dassemble_3c(a, ctx->stream));
+    }
+  }
   KL(KT_FORCES, launch_build_forces(a, what & FB_ALL, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
@@ -807,6 +867,17 @@ int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms, long long *
       return FB_OK;
     }
   return fail(ctx, FB_ERR_ARG, "unknown kernel name %s", kernel);
+}
+
+int fb_probe_fp32(fb_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  double ms = 0.0, flops = 0.0;
+  int st = fb::probe_ffma(ctx->stream, &ms, &flops);
+  if (st) return fail(ctx, FB_ERR_CUDA, "fp32 probe: %s", cudaGetErrorString((cudaError_t)st));
+  ctx->launches += 2;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return FB_OK;
 }
 
 int fb_probe_fp64(fb_ctx *ctx, double *tflops) {

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "fb_device.cuh"
+#include "fb_df.cuh"
 #include "fb_launch.h"
 
 namespace fb {
@@ -86,11 +87,15 @@ struct Ctx3c {
   const double *gxy;
   const double *xl;
   const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
+  const int *tperm;
   const long long *blk_off;
   double *vb;
   // force pass
   const double *rho;
   double *f3naa, *f3nab, *f3nac;
+  // double-float copies (table values and rho blocks as hi + lo floats)
+  const df *table3c_df;
+  const df *rho_df;
 };
 
 struct TripGeom {
@@ -355,12 +360,15 @@ inline Ctx3c make3c(const AsmArgs &a) {
   c.cj_j = a.cj_j;
   c.cj_b = a.cj_b;
   c.tdst = a.tdst;
+  c.tperm = a.tperm;
   c.blk_off = a.blk_off;
   c.vb = a.vb;
   c.rho = a.rho;
   c.f3naa = a.f3naa;
   c.f3nab = a.f3nab;
   c.f3nac = a.f3nac;
+  c.table3c_df = reinterpret_cast<const df *>(a.table3c_df);
+  c.rho_df = reinterpret_cast<const df *>(a.rho_df);
   return c;
 }
 

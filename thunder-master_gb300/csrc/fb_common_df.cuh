@@ -1,0 +1,313 @@
+// fb_common_df.cuh -- double-float three-center interpolation
+// (getMEs_Fdata_3c / getDMEs_Fdata_3c, e.FDATA/M_Fdata_3c.f90:293-846) on
+// the FP32 pipe.  The grid cell, the stencil origin and the gradient switch
+// are decided in FP64 exactly as the reference does; the Legendre sum of the
+// bicubic (or three-point linear) interpolations runs in df.
+#pragma once
+#include "fb_common.cuh"
+#include "fb_device_df.cuh"
+
+namespace fb {
+
+// reciprocal of a df by one Newton step from the float reciprocal
+__device__ __forceinline__ df df_rcp(df a) {
+  float r = __frcp_rn(a.h);
+  df e = df_one() - a * r;  // 1 - a r, small
+  return df_make(r) + e * r;
+}
+
+// P_eq2 (include/constants.h:4) as hi + lo floats
+__device__ __forceinline__ df peq2_df() { return df_make(14.39975f, 2.4414064e-07f); }
+
+__device__ __forceinline__ df cross_df(const df *a, const df *b, int k) {
+  return k == 0 ? a[1] * b[2] - a[2] * b[1] : (k == 1 ? a[2] * b[0] - a[0] * b[2] : a[0] * b[1] - a[1] * b[0]);
+}
+
+// Triplet set-up (M_assemble_3c_Harris.f90:160-189) with FP64 kept where the
+// reference's integer decisions depend on it -- the bond length z and the
+// distance x that select the table cell -- and everything else (unit
+// vectors, cos(theta), the local frame) in df.
+struct GeomDF {
+  int ia, iat, jat;
+  double x, z;
+  df u[3];    // r21 = r2 - r1
+  df v[3];    // rna - r1
+  df sig[3];  // sighat
+  df rh[3];   // rhat
+  df cost, iz, ix;
+  df e[3][3];  // epsilon(rhat, sighat)
+};
+
+// FP64 part of the set-up: what the table cell depends on, and the exact
+// difference vectors the df quantities are formed from
+struct GeomFP64 {
+  int ia, iat, jat;
+  double x, z;
+  double r21[3], rn[3], v[3];
+};
+
+__device__ __forceinline__ void trip_geom_fp64(const Ctx3c &c, int t, GeomFP64 &h) {
+  h.ia = c.trip_alpha[t];
+  h.iat = c.ci_j[t];
+  h.jat = c.cj_j[t];
+  int ib = c.ci_b[t], jb = c.cj_b[t];
+  double r1[3], r2[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r1[k] = __dadd_rn(c.ratom[3 * h.iat + k], c.xl[3 * ib + k]);
+    r2[k] = __dadd_rn(c.ratom[3 * h.jat + k], c.xl[3 * jb + k]);
+    h.r21[k] = __dsub_rn(r2[k], r1[k]);
+    h.rn[k] = __dsub_rn(c.ratom[3 * h.ia + k], __dadd_rn(r1[k], h.r21[k] * 0.5));
+    h.v[k] = c.ratom[3 * h.ia + k] - r1[k];
+  }
+  h.z = dist_rn(r1, r2);
+  h.x = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(h.rn[0], h.rn[0]), __dmul_rn(h.rn[1], h.rn[1])),
+                             __dmul_rn(h.rn[2], h.rn[2])));
+}
+
+// cos(theta) alone (for the interpolation), in df
+__device__ __forceinline__ df trip_cost_df(const GeomFP64 &h) {
+  if (h.x < 1.0e-05) return df_zero();
+  df s = df_zero();
+#pragma unroll
+  for (int k = 0; k < 3; k++) s = s + df_from(h.r21[k]) * df_from(h.rn[k]);
+  if (h.z < 1.0e-05) return df_from(h.rn[2]) * df_rcp(df_from(h.x));
+  return s * (df_rcp(df_from(h.z)) * df_rcp(df_from(h.x)));
+}
+
+__device__ __forceinline__ void trip_geom_df_from(const GeomFP64 &h, GeomDF &g) {
+  g.ia = h.ia;
+  g.iat = h.iat;
+  g.jat = h.jat;
+  g.x = h.x;
+  g.z = h.z;
+  df rnd[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    g.u[k] = df_from(h.r21[k]);
+    g.v[k] = df_from(h.v[k]);
+    rnd[k] = df_from(h.rn[k]);
+  }
+  if (g.z < 1.0e-05) {
+    g.sig[0] = df_zero();
+    g.sig[1] = df_zero();
+    g.sig[2] = df_one();
+    g.iz = df_zero();
+  } else {
+    g.iz = df_rcp(df_from(g.z));
+#pragma unroll
+    for (int k = 0; k < 3; k++) g.sig[k] = g.u[k] * g.iz;
+  }
+  bool hasr = g.x >= 1.0e-05;
+  if (hasr) {
+    g.ix = df_rcp(df_from(g.x));
+#pragma unroll
+    for (int k = 0; k < 3; k++) g.rh[k] = rnd[k] * g.ix;
+  } else {
+    g.ix = df_zero();
+    g.rh[0] = g.rh[1] = g.rh[2] = df_zero();
+  }
+  g.cost = g.sig[0] * g.rh[0] + g.sig[1] * g.rh[1] + g.sig[2] * g.rh[2];
+  // epsilon_function(rhat, sighat) (b.FUNCTIONS/epsilon.f90:73-202); both
+  // arguments are unit vectors (or rhat = 0), so their normalisations are
+  // the identity to within a few ulps and are omitted
+  df yp[3];
+  float ypm2 = 0.0f;
+  if (hasr) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) yp[k] = cross_df(g.sig, g.rh, k);
+    ypm2 = (yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]).h;
+  }
+  if (!hasr || ypm2 < 1.0e-8f) {
+    // colinear fallback (:148-168), first non-zero component of zphat
+    if (fabsf(g.sig[0].h) > 1.0e-4f) {
+      yp[0] = -(g.sig[1] + g.sig[2]) * df_rcp(g.sig[0]);
+      yp[1] = df_one();
+      yp[2] = df_one();
+    } else if (fabsf(g.sig[1].h) > 1.0e-4f) {
+      yp[0] = df_one();
+      yp[1] = -(g.sig[0] + g.sig[2]) * df_rcp(g.sig[1]);
+      yp[2] = df_one();
+    } else {
+      yp[0] = df_one();
+      yp[1] = df_one();
+      yp[2] = -(g.sig[0] + g.sig[1]) * df_rcp(g.sig[2]);
+    }
+  }
+  df iy = df_rcp(df_sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]));
+#pragma unroll
+  for (int k = 0; k < 3; k++) yp[k] = yp[k] * iy;
+  df xp[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) xp[k] = cross_df(yp, g.sig, k);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    g.e[k][0] = xp[k];
+    g.e[k][1] = yp[k];
+    g.e[k][2] = g.sig[k];
+  }
+}
+
+__device__ __forceinline__ void trip_geom_df(const Ctx3c &c, int t, GeomDF &g) {
+  GeomFP64 h;
+  trip_geom_fp64(c, t, h);
+  trip_geom_df_from(h, g);
+}
+
+__device__ __forceinline__ df sel3(const df *a, int k) {
+  df r = a[0];
+  r = k == 1 ? a[1] : r;
+  r = k == 2 ? a[2] : r;
+  return r;
+}
+
+// element th of a 5-array by selects (keeps the array in registers when th
+// is a loop variable)
+__device__ __forceinline__ df sel5(const df *a, int th) {
+  df r = a[0];
+  r = th == 1 ? a[1] : r;
+  r = th == 2 ? a[2] : r;
+  r = th == 3 ? a[3] : r;
+  r = th == 4 ? a[4] : r;
+  return r;
+}
+
+template <int NE, bool DERIV>
+__device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cell, double x, double y, df cost,
+                                            df *F, df *DpF, df *DxF, df *DyF) {
+  // Legendre P_0..P_4 and their derivatives (:348-354, :625-629)
+  df c2 = cost * cost;
+  df pl[5], dpl[5];
+  pl[0] = df_one();
+  pl[1] = cost;
+  pl[2] = (c2 * 3.0f - df_one()) * 0.5f;
+  pl[3] = (cost * (c2 * 5.0f - df_make(3.0f))) * 0.5f;
+  pl[4] = (df_make(3.0f) - c2 * (df_make(30.0f) - c2 * 35.0f)) * 0.125f;
+  if (DERIV) {
+    dpl[0] = df_zero();
+    dpl[1] = df_one();
+    dpl[2] = cost * 3.0f;
+    dpl[3] = (c2 * 15.0f - df_make(3.0f)) * 0.5f;
+    dpl[4] = (cost * (c2 * 35.0f - df_make(15.0f))) * 0.5f;
+  }
+  // grid cell and offsets, FP64 as the reference (:367-379)
+  double qx = __ddiv_rn(x, cell.dx), qy = __ddiv_rn(y, cell.dy);
+  int ix = (int)qx + 1;
+  int iy = (int)qy + 1;
+  if (ix < 2) ix = 2;
+  if (iy < 2) iy = 2;
+  if (ix > cell.nx - 2) ix = cell.nx - 2;
+  if (iy > cell.ny - 2) iy = cell.ny - 2;
+  df px = df_from(qx - ix + 1.0);
+  df py = df_from(qy - iy + 1.0);
+  int nx = cell.nx;
+  long long node0 = (long long)(iy - 1) * nx + (ix - 1);
+  const df *tab = c.table3c_df + cell.off;
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    F[e] = df_zero();
+    if (DERIV) DpF[e] = DxF[e] = DyF[e] = df_zero();
+  }
+  if (c.lin[cell.node_off + node0]) {
+    // METHOD 1, three-point linear (:406-410, :684-691)
+    df gx = df_from(c.gxy[2 * (cell.node_off + node0)]), gy = df_from(c.gxy[2 * (cell.node_off + node0) + 1]);
+    df w00 = (df_one() - px) - py;
+    const df *T00 = tab + node0 * NTHETA * NE;
+    const df *T10 = tab + (node0 + 1) * NTHETA * NE;
+    const df *T01 = tab + (node0 + nx) * NTHETA * NE;
+#pragma unroll
+    for (int th = 0; th < NTHETA; th++)
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        dacc a;
+        dacc_first(a, w00, T00[th * NE + e]);
+        dacc_add(a, px, T10[th * NE + e]);
+        dacc_add(a, py, T01[th * NE + e]);
+        df I = dacc_val(a);
+        F[e] = F[e] + pl[th] * I;
+        if (DERIV) {
+          DpF[e] = DpF[e] + dpl[th] * I;
+          DxF[e] = DxF[e] + pl[th] * gx;
+          DyF[e] = DyF[e] + pl[th] * gy;
+        }
+      }
+    return;
+  }
+  // METHOD 3, 16-point bicubic as a tensor product of Lagrange weights
+  df wx[4], wy[4], dwx[4], dwy[4];
+  lagrange4_df(px, wx, DERIV ? dwx : nullptr);
+  lagrange4_df(py, wy, DERIV ? dwy : nullptr);
+  if (DERIV) {
+    df idx = df_from(1.0 / cell.dx), idy = df_from(1.0 / cell.dy);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      dwx[k] = dwx[k] * idx;
+      dwy[k] = dwy[k] * idy;
+    }
+  }
+  df W[16];
+  if (!DERIV) {
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) W[4 * j + k] = wx[k] * wy[j];
+  }
+  const df *Tb = tab + (node0 - nx - 1) * NTHETA * NE;
+  // pass 1: the value contraction I_theta -> F and dF/dcos(theta); with
+  // derivatives the theta loop is kept rolled (code size, registers)
+#pragma unroll(DERIV ? 1 : NTHETA)
+  for (int th = 0; th < NTHETA; th++) {
+    const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
+    dacc I[NE];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
+        df w = DERIV ? wx[k] * wy[j] : W[4 * j + k];
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          if (j == 0 && k == 0) dacc_first(I[e], w, Tn[e]);
+          else dacc_add(I[e], w, Tn[e]);
+        }
+      }
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      df iv = dacc_val(I[e]);
+      F[e] = F[e] + plt * iv;
+      if (DERIV) DpF[e] = DpF[e] + dplt * iv;
+    }
+  }
+  if (!DERIV) return;
+  // pass 2: the x and y derivative contractions (fewer live accumulators
+  // than one fused pass; the stencil is re-read from L1)
+#pragma unroll 1
+  for (int th = 0; th < NTHETA; th++) {
+    const df plt = sel5(pl, th);
+    dacc Ix[NE], Iy[NE];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
+        df wxd = dwx[k] * wy[j], wyd = wx[k] * dwy[j];
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          if (j == 0 && k == 0) {
+            dacc_first(Ix[e], wxd, Tn[e]);
+            dacc_first(Iy[e], wyd, Tn[e]);
+          } else {
+            dacc_add(Ix[e], wxd, Tn[e]);
+            dacc_add(Iy[e], wyd, Tn[e]);
+          }
+        }
+      }
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      DxF[e] = DxF[e] + plt * dacc_val(Ix[e]);
+      DyF[e] = DyF[e] + plt * dacc_val(Iy[e]);
+    }
+  }
+}
+
+}  // namespace fb

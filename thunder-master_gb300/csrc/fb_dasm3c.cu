@@ -86,6 +86,7 @@ template <bool HASD>
 __global__ void __launch_bounds__(128) k_dassemble_3c(Ctx3c c) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= c.T) return;
+  if (c.tperm) t = c.tperm[t];
   int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
   int key = pa * 3 + pb;
   switch (key) {

@@ -453,6 +453,15 @@ info_done:
           }
       }
 
+  // double-float copy of the 3c values: hi = nearest float, lo = nearest
+  // float of the remainder (exact in double)
+  out.table3c_df.resize(2 * out.table3c.size());
+  for (size_t k = 0; k < out.table3c.size(); k++) {
+    double v = out.table3c[k];
+    float h = (float)v;
+    out.table3c_df[2 * k] = h;
+    out.table3c_df[2 * k + 1] = (float)(v - (double)h);
+  }
   out.dev.nspecies = nspecies;
   out.dev.have_d = out.have_d;
   for (int k = 0; k < nspecies; k++) {

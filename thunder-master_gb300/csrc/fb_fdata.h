@@ -16,6 +16,7 @@ struct FdataHost {
   int nspecies = 0, have_d = 0;
   SpeciesHost sp[MAXSP];
   std::vector<double> table2c, table3c, gxy;
+  std::vector<float> table3c_df;  // hi, lo float pairs of table3c
   std::vector<unsigned char> lin;
   FdataDev dev{};
 };

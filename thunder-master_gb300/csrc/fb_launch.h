@@ -8,7 +8,9 @@ namespace fb {
 struct NeighArgs {
   int N, P, nimg;
   const double *ratom;
-  const float *ratomf;
+  const float4 *pos4;  // x, y, z, float cutoff of the atom's species
+  float4 bbox_lo, bbox_hi;  // bounding box of the positions; bbox_lo.w = largest cutoff
+  int periodic;
   const int *isp;
   const FdataDev *fd;
   const double *xl;
@@ -24,7 +26,6 @@ struct NeighArgs {
   int *neigh_j, *neigh_b, *neigh_self, *neigh_back;
   const int *pair_owner;
   double *r3v;
-  float *r3f;
   int *tcnt;
   const int *trip_off;
   int *ci_j, *ci_b, *cj_j, *cj_b, *cneigh, *tdst;
@@ -43,6 +44,7 @@ struct AsmArgs {
   const int *pair_off, *neigh_j, *neigh_b, *neigh_self, *neigh_back;
   const long long *blk_off;
   const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
+  const int *tperm;  // triplet processing order (binned), or null
   double *S, *T, *vb, *vbo;
   const double *rho, *cape;
   double *dS, *dT;
@@ -51,17 +53,27 @@ struct AsmArgs {
   double *f3naa, *f3nab, *f3nac;
   double *kin, *vna, *pul, *ftot;
   unsigned *status;
+  const float2 *table3c_df;  // hi, lo float pairs of table3c
+  float2 *rho_df;            // hi, lo float pairs of rho
 };
 
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s);
 int launch_neigh_back(const NeighArgs &a, cudaStream_t s);
 int launch_common(const NeighArgs &a, bool fill, cudaStream_t s);
+// counting sort of the triplets by (species triple, 3c grid cell) -> perm
+int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, int *rank, int *hist, int *perm,
+                     cudaStream_t s);
 int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_assemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s);
+// double-float three-center kernels (s and sp bases) and the rho split
+int launch_assemble_3c_df(const AsmArgs &a, cudaStream_t s);
+int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s);
+int launch_split_rho(const AsmArgs &a, long long nblock, cudaStream_t s);
 // DFMA throughput probe: one warm-up and one timed launch
 int probe_dfma(cudaStream_t s, double *ms, double *flops);
+int probe_ffma(cudaStream_t s, double *ms, double *flops);
 
 }  // namespace fb

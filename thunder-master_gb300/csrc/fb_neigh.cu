@@ -12,20 +12,23 @@ namespace fb {
 // pairs; every candidate is decided by the uncontracted FP64 test of the
 // reference: z = distance(r1, r2) < rc_i + rc_j - 0.01.
 template <bool FILL>
-__global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__restrict__ ratomf,
+__global__ void k_neigh(int N, const double *__restrict__ ratom, const float4 *__restrict__ pos4,
                         const int *__restrict__ isp, const FdataDev *__restrict__ fd, const double *__restrict__ xl,
-                        const float *__restrict__ xlf, const int *__restrict__ imgs, int nimg, int *__restrict__ cnt,
-                        long long *__restrict__ bsum, const int *__restrict__ pair_off,
-                        const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
-                        int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
+                        const float *__restrict__ xlf, const int *__restrict__ imgs, int nimg, float4 bbox_lo,
+                        float4 bbox_hi, int *__restrict__ cnt, long long *__restrict__ bsum,
+                        const int *__restrict__ pair_off, const long long *__restrict__ blk_base,
+                        int *__restrict__ neigh_j, int *__restrict__ neigh_b, int *__restrict__ neigh_self,
+                        int *__restrict__ pair_owner, long long *__restrict__ blk_off,
                         unsigned *__restrict__ status, int *__restrict__ errinfo) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
   int i = warp;
   double ri[3] = {ratom[3 * i], ratom[3 * i + 1], ratom[3 * i + 2]};
-  float rfi0 = ratomf[3 * i], rfi1 = ratomf[3 * i + 1], rfi2 = ratomf[3 * i + 2];
+  float4 pi = pos4[i];  // (x, y, z, float cutoff of species)
   double rci = fd->sp[isp[i]].rcA;
+  // float reach of atom i: its cutoff + the largest cutoff + margin
+  float reach = pi.w + bbox_lo.w + 1.0e-2f;
   int num = 0, base = FILL ? pair_off[i] : 0;
   long long norbsum = 0;  // sum of norb_j over the hits so far
   long long bbase = FILL ? blk_base[i] : 0;
@@ -33,17 +36,22 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__
   for (int ii = 0; ii < nimg; ii++) {
     int mb = imgs[ii];
     float L0 = xlf[3 * mb], L1 = xlf[3 * mb + 1], L2 = xlf[3 * mb + 2];
+    // skip an image whose shifted bounding box lies beyond reach (warp-uniform)
+    float ox = fmaxf(fmaxf(bbox_lo.x + L0 - pi.x, pi.x - (bbox_hi.x + L0)), 0.0f);
+    float oy = fmaxf(fmaxf(bbox_lo.y + L1 - pi.y, pi.y - (bbox_hi.y + L1)), 0.0f);
+    float oz = fmaxf(fmaxf(bbox_lo.z + L2 - pi.z, pi.z - (bbox_hi.z + L2)), 0.0f);
+    if (ox * ox + oy * oy + oz * oz > reach * reach) continue;
     double X0 = xl[3 * mb], X1 = xl[3 * mb + 1], X2 = xl[3 * mb + 2];
     for (int j0 = 0; j0 < N; j0 += 32) {
       int j = j0 + lane;
       bool hit = false;
       if (j < N) {
-        double rcj = fd->sp[isp[j]].rcA;
-        double range = __dsub_rn(__dadd_rn(rci, rcj), 0.01);
-        float d0 = (ratomf[3 * j] + L0) - rfi0, d1 = (ratomf[3 * j + 1] + L1) - rfi1,
-              d2 = (ratomf[3 * j + 2] + L2) - rfi2;
-        float lim = (float)range + 1.0e-2f;
+        float4 pj = pos4[j];
+        float d0 = (pj.x + L0) - pi.x, d1 = (pj.y + L1) - pi.y, d2 = (pj.z + L2) - pi.z;
+        float lim = pi.w + pj.w + 1.0e-2f;
         if (d0 * d0 + d1 * d1 + d2 * d2 < lim * lim) {
+          // the reference's test, uncontracted FP64
+          double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[j]].rcA), 0.01);
           double r2[3] = {__dadd_rn(ratom[3 * j], X0), __dadd_rn(ratom[3 * j + 1], X1),
                           __dadd_rn(ratom[3 * j + 2], X2)};
           double z = dist_rn(ri, r2);
@@ -57,6 +65,7 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__
         }
       }
       unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (m == 0u) continue;
       // inclusive warp scan of norb_j over the hit lanes -> block offsets
       int nj = hit ? fd->sp[isp[j]].norb : 0;
       int incl = nj;
@@ -93,7 +102,7 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float *__
 __global__ void k_neigh_back(int N, int P, const int *__restrict__ pair_owner, const int *__restrict__ pair_off,
                              const int *__restrict__ neigh_j, const int *__restrict__ neigh_b,
                              const double *__restrict__ xl, const double *__restrict__ ratom,
-                             int *__restrict__ neigh_back, double *__restrict__ r3v, float *__restrict__ r3f,
+                             int *__restrict__ neigh_back, double *__restrict__ r3v,
                              unsigned *__restrict__ status) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
@@ -115,24 +124,48 @@ __global__ void k_neigh_back(int N, int P, const int *__restrict__ pair_owner, c
   for (int k = 0; k < 3; k++) {
     double v = __dsub_rn(__dadd_rn(xl[3 * mb + k], ratom[3 * j + k]), ratom[3 * i + k]);
     r3v[3 * p + k] = v;
-    r3f[3 * p + k] = (float)v;
   }
+}
+
+// Integer cell shift (ix, iy, iz) of image mbeta in the make_cells order
+// (c.SYSTEM/make_cells.f90:125-144): iz outer, ix inner, the origin skipped.
+__device__ __forceinline__ void mbeta_shift(int mb, int &sx, int &sy, int &sz) {
+  int L = (mb == 0) ? 364 : (mb <= 364 ? mb - 1 : mb);
+  sx = L % 9 - 4;
+  sy = (L / 9) % 9 - 4;
+  sz = L / 81 - 4;
+}
+__device__ __forceinline__ int shift_mbeta(int sx, int sy, int sz) {
+  int L = (sz + 4) * 81 + (sy + 4) * 9 + (sx + 4);
+  return L == 364 ? 0 : (L < 364 ? L + 1 : L);
+}
+
+// the reference's vector match of find_common_neighbors (:776-779),
+// uncontracted FP64
+__device__ __forceinline__ bool common_match(const double *r3, const double *r1, const double *r2) {
+  return fabs(__dadd_rn(__dsub_rn(r3[0], r2[0]), r1[0])) < 1.0e-4 &&
+         fabs(__dadd_rn(__dsub_rn(r3[1], r2[1]), r1[1])) < 1.0e-4 &&
+         fabs(__dadd_rn(__dsub_rn(r3[2], r2[2]), r1[2])) < 1.0e-4;
 }
 
 // find_common_max / find_common_neighbors: one warp per ialpha; for each
 // non-self ineigh (warp-uniform), lanes sweep jneigh; a candidate (i, j)
 // with |r1 - r2| < rc_i + rc_j - 0.01 is kept only if j is found in i's
-// list by vector match (first kneigh with |r3 - r2 + r1| < 1e-4 per
-// component).  Output order matches the reference loops.
+// list by the reference's vector match (first kneigh with
+// |r3 - r2 + r1| < 1e-4 per component).  The entry that can match is
+// (jatom, shift(jbeta) - shift(ibeta)); i's list is sorted by (mbeta, jatom),
+// so it is found by binary search and then tested exactly.  When that entry
+// is absent or fails the test, the full scan of the reference decides.
+// Output order matches the reference loops.
 template <bool FILL>
-__global__ void k_common(int N, const double *__restrict__ ratom, const int *__restrict__ isp,
+__global__ void k_common(int N, int periodic, const double *__restrict__ ratom, const int *__restrict__ isp,
                          const FdataDev *__restrict__ fd, const double *__restrict__ xl,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                          const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
-                         const double *__restrict__ r3v, const float *__restrict__ r3f, int *__restrict__ tcnt,
-                         const int *__restrict__ trip_off, int *__restrict__ ci_j, int *__restrict__ ci_b,
-                         int *__restrict__ cj_j, int *__restrict__ cj_b, int *__restrict__ cneigh,
-                         int *__restrict__ tdst, int *__restrict__ talpha) {
+                         const double *__restrict__ r3v, int *__restrict__ tcnt, const int *__restrict__ trip_off,
+                         int *__restrict__ ci_j, int *__restrict__ ci_b, int *__restrict__ cj_j,
+                         int *__restrict__ cj_b, int *__restrict__ cneigh, int *__restrict__ tdst,
+                         int *__restrict__ talpha) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
@@ -145,9 +178,10 @@ __global__ void k_common(int N, const double *__restrict__ ratom, const int *__r
     double r1[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
-    float r1f[3] = {(float)r1[0], (float)r1[1], (float)r1[2]};
     double rci = fd->sp[isp[iat]].rcA;
     int q0 = pair_off[iat], qn = pair_off[iat + 1];
+    int ibx, iby, ibz;
+    mbeta_shift(ib, ibx, iby, ibz);
     for (int j0 = 0; j0 < n; j0 += 32) {
       int jn = j0 + lane;
       bool keep = false;
@@ -163,20 +197,36 @@ __global__ void k_common(int N, const double *__restrict__ ratom, const int *__r
         double z = dist_rn(r1, r2);
         double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
         if (z < range) {
-          float r2f[3] = {(float)r2[0], (float)r2[1], (float)r2[2]};
-          for (int q = q0; q < qn; q++) {
-            // float prefilter of the 1e-4 vector match, then the exact test
-            float e0 = fabsf(r3f[3 * q] - r2f[0] + r1f[0]);
-            float e1 = fabsf(r3f[3 * q + 1] - r2f[1] + r1f[1]);
-            float e2 = fabsf(r3f[3 * q + 2] - r2f[2] + r1f[2]);
-            if (e0 < 1.0e-2f && e1 < 1.0e-2f && e2 < 1.0e-2f) {
-              if (fabs(__dadd_rn(__dsub_rn(r3v[3 * q], r2[0]), r1[0])) < 1.0e-4 &&
-                  fabs(__dadd_rn(__dsub_rn(r3v[3 * q + 1], r2[1]), r1[1])) < 1.0e-4 &&
-                  fabs(__dadd_rn(__dsub_rn(r3v[3 * q + 2], r2[2]), r1[2])) < 1.0e-4) {
-                found = q - q0;
+          int tmb = 0;
+          bool inbox = true;
+          if (periodic) {
+            int jbx, jby, jbz;
+            mbeta_shift(jb, jbx, jby, jbz);
+            int tx = jbx - ibx, ty = jby - iby, tz = jbz - ibz;
+            inbox = tx >= -4 && tx <= 4 && ty >= -4 && ty <= 4 && tz >= -4 && tz <= 4;
+            if (inbox) tmb = shift_mbeta(tx, ty, tz);
+          }
+          if (inbox) {
+            long long key = (long long)tmb * N + jat;
+            int lo = q0, hi = qn - 1;
+            while (lo <= hi) {
+              int mid = (lo + hi) >> 1;
+              long long km = (long long)neigh_b[mid] * N + neigh_j[mid];
+              if (km < key) lo = mid + 1;
+              else if (km > key) hi = mid - 1;
+              else {
+                if (common_match(r3v + 3 * mid, r1, r2)) found = mid - q0;
                 break;
               }
             }
+          }
+          if (found < 0) {
+            // rare: candidate at the cutoff edge; decide by the reference scan
+            for (int q = q0; q < qn; q++)
+              if (common_match(r3v + 3 * q, r1, r2)) {
+                found = q - q0;
+                break;
+              }
           }
           keep = found >= 0;
         }
@@ -198,16 +248,103 @@ __global__ void k_common(int N, const double *__restrict__ ratom, const int *__r
   if (!FILL && lane == 0) tcnt[ia] = num;
 }
 
+// ---------------------------------------------------------------------------
+// Triplet binning: a counting sort of the triplets by (species triple, 3c
+// grid cell of the interpolation stencil).  The three-center kernels walk
+// the triplets in this order, so neighboring lanes read the same table
+// stencil (broadcast loads) and take the same interpolation branch.  The
+// cell is computed with the set-up of assemble_vna_3c
+// (M_assemble_3c_Harris.f90:160-186) and the index rule of getMEs_Fdata_3c
+// (M_Fdata_3c.f90:367-376); it only orders the work.
+// ---------------------------------------------------------------------------
+__global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__ ratom, const int *__restrict__ isp,
+                           const FdataDev *__restrict__ fd, const double *__restrict__ xl,
+                           const int *__restrict__ talpha, const int *__restrict__ ci_j, const int *__restrict__ ci_b,
+                           const int *__restrict__ cj_j, const int *__restrict__ cj_b, int *__restrict__ key,
+                           int *__restrict__ rank, int *__restrict__ hist) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  int ia = talpha[t], i = ci_j[t], j = cj_j[t], ib = ci_b[t], jb = cj_b[t];
+  double r1[3], r2[3], rn[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r1[k] = ratom[3 * i + k] + xl[3 * ib + k];
+    r2[k] = ratom[3 * j + k] + xl[3 * jb + k];
+    rn[k] = ratom[3 * ia + k] - 0.5 * (r1[k] + r2[k]);
+  }
+  double z = sqrt((r2[0] - r1[0]) * (r2[0] - r1[0]) + (r2[1] - r1[1]) * (r2[1] - r1[1]) +
+                  (r2[2] - r1[2]) * (r2[2] - r1[2]));
+  double x = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+  int a = isp[i], b = isp[j], c = isp[ia];
+  const Cell3cDev &cell = fd->c3[a][b][c];
+  int ix = (int)(x / cell.dx) + 1, iy = (int)(z / cell.dy) + 1;
+  ix = min(max(ix, 2), cell.nx - 2);
+  iy = min(max(iy, 2), cell.ny - 2);
+  int node = (iy - 1) * cell.nx + (ix - 1);
+  int k = ((a * nsp + b) * nsp + c) * cells + min(node, cells - 1);
+  key[t] = k;
+  rank[t] = atomicAdd(hist + k, 1);
+}
+
+// exclusive scan of the bin counts, one block
+__global__ void k_scan_bins(int nbins, int *__restrict__ hist) {
+  __shared__ int part[1024];
+  int tid = threadIdx.x;
+  int per = (nbins + 1023) / 1024;
+  int lo = tid * per, hi = min(lo + per, nbins);
+  int sum = 0;
+  for (int b = lo; b < hi; b++) sum += hist[b];
+  part[tid] = sum;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {
+    int v = tid >= d ? part[tid - d] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int run = part[tid] - sum;
+  for (int b = lo; b < hi; b++) {
+    int c = hist[b];
+    hist[b] = run;
+    run += c;
+  }
+}
+
+__global__ void k_trip_scatter(int T, const int *__restrict__ key, const int *__restrict__ rank,
+                               const int *__restrict__ start, int *__restrict__ perm) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  perm[start[key[t]] + rank[t]] = t;
+}
+
+int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, int *rank, int *hist, int *perm,
+                     cudaStream_t s) {
+  if (T == 0) return 0;
+  int nbins = nsp * nsp * nsp * cells;
+  cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), s);
+  if (e != cudaSuccess) return (int)e;
+  int threads = 256, blocks = (T + threads - 1) / threads;
+  k_trip_key<<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.isp, a.fd, a.xl, a.talpha, a.ci_j, a.ci_b,
+                                        a.cj_j, a.cj_b, key, rank, hist);
+  FB_LAUNCH_CHECK();
+  k_scan_bins<<<1, 1024, 0, s>>>(nbins, hist);
+  FB_LAUNCH_CHECK();
+  k_trip_scatter<<<blocks, threads, 0, s>>>(T, key, rank, hist, perm);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   if (fill)
-    k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.ratomf, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                             nullptr, nullptr, a.pair_off, a.blk_base, a.neigh_j, a.neigh_b,
-                                             a.neigh_self, a.pair_owner_w, a.blk_off_w, a.status, a.errinfo);
+    k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
+                                             a.bbox_lo, a.bbox_hi, nullptr, nullptr, a.pair_off, a.blk_base,
+                                             a.neigh_j, a.neigh_b, a.neigh_self, a.pair_owner_w, a.blk_off_w,
+                                             a.status, a.errinfo);
   else
-    k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.ratomf, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                              a.cnt, a.bsum, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                                              nullptr, a.status, a.errinfo);
+    k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
+                                              a.bbox_lo, a.bbox_hi, a.cnt, a.bsum, nullptr, nullptr, nullptr,
+                                              nullptr, nullptr, nullptr, nullptr, a.status, a.errinfo);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -216,7 +353,7 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
   if (a.P == 0) return 0;
   int threads = 256, blocks = (a.P + threads - 1) / threads;
   k_neigh_back<<<blocks, threads, 0, s>>>(a.N, a.P, a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.xl, a.ratom,
-                                          a.neigh_back, a.r3v, a.r3f, a.status);
+                                          a.neigh_back, a.r3v, a.status);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -224,13 +361,13 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
 int launch_common(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   if (fill)
-    k_common<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j, a.neigh_b,
-                                              a.neigh_self, a.r3v, a.r3f, nullptr, a.trip_off, a.ci_j, a.ci_b,
+    k_common<true><<<blocks, threads, 0, s>>>(a.N, a.periodic, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j,
+                                              a.neigh_b, a.neigh_self, a.r3v, nullptr, a.trip_off, a.ci_j, a.ci_b,
                                               a.cj_j, a.cj_b, a.cneigh, a.tdst, a.talpha);
   else
-    k_common<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j, a.neigh_b,
-                                               a.neigh_self, a.r3v, a.r3f, a.tcnt, nullptr, nullptr, nullptr,
-                                               nullptr, nullptr, nullptr, nullptr, nullptr);
+    k_common<false><<<blocks, threads, 0, s>>>(a.N, a.periodic, a.ratom, a.isp, a.fd, a.xl, a.pair_off,
+                                               a.neigh_j, a.neigh_b, a.neigh_self, a.r3v, a.tcnt, nullptr,
+                                               nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -45,4 +45,45 @@ int probe_dfma(cudaStream_t s, double *ms, double *flops) {
   return 0;
 }
 
+// FP32 FMA throughput probe: 8 independent FFMA chains per thread
+__global__ void __launch_bounds__(256) k_probe_ffma(int iters, float seed, float *sink) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = seed + 1e-3f * (threadIdx.x + k);
+  const float m = 0.9999f, c = 1e-4f;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = fmaf(a[k], m, c);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += a[k];
+  if (s == -1.2345e30f) sink[0] = s;
+}
+
+int probe_ffma(cudaStream_t s, double *ms, double *flops) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int blocks = nsm * 8, threads = 256, iters = 65536;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_probe_ffma<<<blocks, threads, 0, s>>>(iters / 8, 1.0f, nullptr);
+  cudaEventRecord(a, s);
+  k_probe_ffma<<<blocks, threads, 0, s>>>(iters, 1.0f, nullptr);
+  cudaEventRecord(b, s);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0.0f;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  *ms = t;
+  *flops = 2.0 * 8.0 * (double)iters * (double)blocks * threads;
+  return 0;
+}
+
 }  // namespace fb

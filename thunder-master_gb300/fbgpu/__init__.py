@@ -74,11 +74,15 @@ _SIGS = {
     "fb_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "fb_get_timing": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "fb_probe_fp64": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fb_probe_fp32": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fb_dassemble_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
 }
 
+FB_PREC_FP64, FB_PREC_DF = 0, 1
+
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
-           "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces")
+           "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho")
 
 
 class FBError(RuntimeError):
@@ -141,6 +145,11 @@ class Context:
             raise FBError(st, self.L.fb_last_error(self.h).decode())
 
     # ---- setup -------------------------------------------------------------
+    def set_precision(self, mode):
+        """FB_PREC_DF (default): three-center contractions in double-float
+        on the FP32 pipe; FB_PREC_FP64: everything in FP64."""
+        self._check(self.L.fb_set_precision(self.h, int(mode)))
+
     def set_stream(self, stream_ptr):
         self._check(self.L.fb_set_stream(self.h, C.c_void_p(stream_ptr)))
 
@@ -267,6 +276,12 @@ class Context:
             self._check(self.L.fb_get_timing(self.h, k.encode(), C.byref(ms), C.byref(n)))
             out[k] = (ms.value, n.value)
         return out
+
+    def probe_fp32(self):
+        """Measured FP32 FMA throughput, TFLOP/s."""
+        t = C.c_double()
+        self._check(self.L.fb_probe_fp32(self.h, C.byref(t)))
+        return t.value
 
     def probe_fp64(self):
         """Measured FP64 FMA throughput, TFLOP/s."""
