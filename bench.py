@@ -4,8 +4,15 @@
 One step = one pass of the path over one structure: the neighbor maps
 (driver_neighbors), the 2c + 3c H/S assembly (assemble_S, assemble_T,
 assemble_vna_2c, assemble_vna_3c) and the force derivatives with the force
-reduction (Dassemble_S/T/vna_2c/vna_3c, build_forces), all in FP64.
-The density matrices the solver would supply are seeded synthetic blocks.
+reduction (Dassemble_S/T/vna_2c/vna_3c, build_forces).  The assembly and
+force kernels run as one CUDA graph launch per step, with launch shapes
+picked by the library's autotuner.  The density matrices the solver would
+supply are seeded synthetic blocks.
+
+--workload batch256: 256 independent Si / SiC structures of 32..512 atoms in
+one batch (one neighbor build + one graph launch per step), compared with
+the same 256 structures assembled one after another through the
+single-structure calls.
 
 Default workload: 512-atom Si (4x4x4 diamond cells, a = 5.43 A, N(0, 0.15 A)
 jitter, sp3, rc = 5.0 bohr), synthetic Gaussian-polynomial Fdata.
@@ -47,6 +54,9 @@ WORKLOADS = {
                "2c + 3c H/S + forces, FP64",
     "sic4096": "SiC4096: 8x8x8 zincblende SiC, a=4.36 A, N(0,0.1 A) jitter, sp3, rc=5.0 bohr; neighbors + 2c "
                "+ 3c H/S + forces, FP64",
+    "batch256": "256 independent structures, 32..512 atoms (seeded), diamond Si (a=5.43 A) or zincblende SiC "
+                "(a=4.36 A), N(0,0.1 A) jitter, 0-5% vacancies, sp3, rc=5.0 bohr; one batch: neighbors + 2c + 3c "
+                "H/S + forces",
 }
 
 
@@ -60,6 +70,37 @@ def load_workload(name):
     st = synth.structure_for(name)
     nZ = [s.nZ for s in synth.species_for(name)]
     return path, nZ, st
+
+
+def denmat_fast(neighn, neigh_j0, neigh_back0, blk_off, norb_of, seed=42):
+    """Seeded density matrices symmetric across neigh_back (vectorized):
+    rho_ji(nu, mu) = rho_ij(mu, nu).  neigh_j0 and neigh_back0 are 0-based
+    global indices."""
+    rng = np.random.default_rng(seed)
+    NB = int(blk_off[-1])
+    raw_r = rng.normal(0.0, 0.1, NB)
+    raw_c = rng.normal(0.0, 0.05, NB)
+    P = len(neigh_j0)
+    pair_off = np.concatenate([[0], np.cumsum(neighn)]).astype(np.int64)
+    owner = np.repeat(np.arange(len(neighn)), neighn)
+    ni = norb_of[owner]
+    nj = norb_of[neigh_j0]
+    q = pair_off[neigh_j0] + neigh_back0
+    # every element e of pair p: (mu, nu) column-major, mu fastest
+    size = ni * nj
+    pe = np.repeat(np.arange(P), size)
+    loc = np.arange(NB) - np.repeat(blk_off[:P], size)
+    mu = loc % np.repeat(ni, size)
+    nu = loc // np.repeat(ni, size)
+    # the mirrored element (nu, mu) of pair q (an nj x ni block)
+    mirror = np.repeat(blk_off[q], size) + nu + np.repeat(nj, size) * mu
+    lead = pe <= np.repeat(q, size)  # the pair with the smaller index supplies the values
+    rho = np.where(lead, raw_r, raw_r[mirror])
+    cape = np.where(lead, raw_c, raw_c[mirror])
+    selfp = pe == np.repeat(q, size)
+    rho[selfp] = 0.5 * (raw_r[selfp] + raw_r[mirror[selfp]])
+    cape[selfp] = 0.5 * (raw_c[selfp] + raw_c[mirror[selfp]])
+    return rho, cape
 
 
 def denmat_for(ctx_or_sys, st, nZ, norb_of, seed=42):
@@ -168,6 +209,39 @@ def bytes_dassemble_3c(T, P, N, nb_per_pair, table_bytes):
     return T * 24 + P * nb_per_pair * 8 + N * 24 + 3 * N * 24 + table_bytes
 
 
+def tuned_shapes(ctx, fbgpu, autotune):
+    """Autotune the assembly and force kernels on the current system (or keep
+    the default shapes); returns the chosen shapes for the JSON line."""
+    if autotune:
+        ctx.autotune(fbgpu.FB_ALL | fbgpu.FB_FORCES, reps=2)
+    return {k: ctx.get_launch(k) for k in fbgpu.TUNABLE}
+
+
+def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps):
+    """Roofline of the dominant kernel from its CUDA-event launch times."""
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms = ktimes[dom][0] / max(1, ktimes[dom][1])
+    from fbgpu import synth
+    nme = len(synth.make_munu_3c([0, 1], [0, 1])[0])
+    fl = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
+    if fl is None:
+        return None
+    fp64_peak = ctx.probe_fp64()
+    ach = fl / (dom_ms * 1e-3) / 1e12
+    roof = {"bound": "fp64", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp64_peak, 4),
+            "unit": "TFLOP/s", "frac": round(ach / fp64_peak, 4), "traffic": None,
+            "peak_source": "measured in this run (fb_probe_fp64 DFMA chains)",
+            "flops_per_launch": fl, "avg_launch_ms": round(dom_ms, 4)}
+    table_bytes = 8 * 31 * 31 * 5 * nme * len(nZ) ** 3
+    by = bytes_dassemble_3c(T, P, natoms, 16, table_bytes)
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        hbm_peak = json.load(f)["hbm_gbs"]
+    roof["hbm"] = {"achieved": round(by / (dom_ms * 1e-3) / 1e9, 3), "peak": hbm_peak, "unit": "GB/s",
+                   "frac": round(by / (dom_ms * 1e-3) / 1e9 / hbm_peak, 6), "bytes_per_launch": by,
+                   "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+    return roof
+
+
 def run_gpu(args):
     import torch
     import fbgpu
@@ -176,6 +250,8 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "batch256":
+        return run_batch(args, torch, fbgpu, ws, rank, local)
     path, nZ, st = load_workload(args.workload)
     ctx = fbgpu.Context(local)
     stream = torch.cuda.Stream(device=local)
@@ -186,12 +262,21 @@ def run_gpu(args):
     P, T, NB = ctx.driver_neighbors()
     nbm = ctx.neighbors()
     norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
-    rho, cape = denmat_for(nbm, st, nZ, norb_of)
+    rho, cape = denmat_fast(nbm["neighn"], nbm["neigh_j"] - 1, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
     d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
     d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+    shapes = tuned_shapes(ctx, fbgpu, not args.no_autotune)
+    step_what = fbgpu.FB_ALL | fbgpu.FB_FORCES
 
     def device_step():
+        ctx.driver_neighbors()
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.assemble_graph(step_what)
+
+    def kernel_step():
+        # the same work through the separate calls, for per-kernel timing
         ctx.driver_neighbors()
         ctx.assemble(fbgpu.FB_ALL)
         ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
@@ -210,16 +295,62 @@ def run_gpu(args):
     def e2e_step():
         ctx.update_positions(h_pos)
         ctx.driver_neighbors()
-        ctx.assemble(fbgpu.FB_ALL)
+        ctx.set_denmat(h_rho, h_cape)
+        ctx.assemble_graph(step_what)
         for key, buf in zip(("S", "T", "vna", "vnao"), h_out):
             ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
-        ctx.set_denmat(h_rho, h_cape)
-        ctx.Dassemble(fbgpu.FB_ALL)
         ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
 
     h2d = 3 * st.natoms * 8 + 2 * NB * 8
     d2h = 4 * NB * 8 + 3 * st.natoms * 8
+    timed = make_timer(torch, ctx, stream, flush, ws, local)
 
+    for _ in range(args.warmup):
+        device_step()
+        e2e_step()
+        kernel_step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, launches = timed(device_step, args.steps)
+    ms_e2e, _ = timed(e2e_step, args.steps)
+    clk = clocks.stop()
+    ms_k, _ = timed(kernel_step, args.steps, timing=True)
+    ktimes = ctx.timing()
+    ctx.set_timing(False)
+
+    per_step = ms / args.steps
+    value = ws * P * args.steps / (ms * 1e-3)
+    e2e_value = ws * P * args.steps / (ms_e2e * 1e-3)
+    roof = roofline_for(ctx, ktimes, T, P, st.natoms, nZ, args.steps)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
+                   "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "flushed between steps (256 MiB write)", "forces": True,
+                   "step": "fb_neighbors + one CUDA graph launch (assembly + forces)",
+                   "launch_shapes": shapes, "autotuned": not args.no_autotune},
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(ms_e2e / args.steps, 4)},
+        "gpu_launches": launches,
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+        "separate_calls_ms_per_step": round(ms_k / args.steps, 4),
+        "roofline": roof,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.workload, path, nZ, st, P)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def make_timer(torch, ctx, stream, flush, ws, local):
     def barrier():
         if ws > 1:
             import torch.distributed as dist
@@ -247,65 +378,168 @@ def run_gpu(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
         return ms, launches
+    return timed
 
+
+def batch_inputs(structs, ctx, fbgpu):
+    """Seeded symmetric density matrices of a batch (global numbering)."""
+    nbm = ctx.neighbors()
+    off = ctx.batch_offsets()
+    sid = np.repeat(np.arange(len(structs)), np.diff(off["atom"]))
+    owner = np.repeat(np.arange(len(nbm["neighn"])), nbm["neighn"])
+    jg = nbm["neigh_j"] - 1 + off["atom"][sid[owner]]
+    imass = np.concatenate([st.imass for st in structs])
+    norb_of = np.array([ctx.norb_species[k - 1] for k in imass])
+    return denmat_fast(nbm["neighn"], jg, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
+
+
+def run_batch(args, torch, fbgpu, ws, rank, local):
+    """Config: 256 structures of uneven size in one batch, against the same
+    structures assembled one at a time."""
+    from fbgpu import synth
+    path = synth.fdata_dir_for("batch256", root=fdata_root())
+    nZ = [s.nZ for s in synth.species_for("batch256")]
+    structs = synth.batch_structures(256)
+    ctx = fbgpu.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
+    ctx.set_batch([(st.ratom, st.imass, st.lattice, 0) for st in structs])
+    P, T, NB = ctx.driver_neighbors()
+    off = ctx.batch_offsets()
+    rho, cape = batch_inputs(structs, ctx, fbgpu)
+    dev = f"cuda:{local}"
+    d_rho = torch.from_numpy(rho).to(dev)
+    d_cape = torch.from_numpy(cape).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+    shapes = tuned_shapes(ctx, fbgpu, not args.no_autotune)
+    step_what = fbgpu.FB_ALL | fbgpu.FB_FORCES
+    natoms = int(off["atom"][-1])
+
+    def batch_step():
+        ctx.driver_neighbors()
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.assemble_graph(step_what)
+
+    # the same structures one at a time through the single-structure calls
+    seq = fbgpu.Context(local)
+    seq.set_stream(stream.cuda_stream)
+    seq.read_Fdata(path, nZ)
+    seq.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
+    bo = off["block"]
+
+    def sequential_step():
+        for k, st in enumerate(structs):
+            seq.set_structure(st.ratom, st.imass, st.lattice)
+            seq.driver_neighbors()
+            seq.assemble(fbgpu.FB_ALL)
+            seq.set_denmat_device(d_rho.data_ptr() + 8 * int(bo[k]), d_cape.data_ptr() + 8 * int(bo[k]))
+            seq.Dassemble(fbgpu.FB_ALL)
+
+    pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    h_pos = pin(3 * natoms)
+    h_pos[:] = np.concatenate([st.ratom.ravel() for st in structs])
+    h_rho, h_cape = pin(NB), pin(NB)
+    h_rho[:] = rho
+    h_cape[:] = cape
+    h_out = [pin(NB) for _ in range(4)]
+    h_f = pin(3 * natoms)
+
+    def e2e_step():
+        ctx.update_positions(h_pos)
+        ctx.driver_neighbors()
+        ctx.set_denmat(h_rho, h_cape)
+        ctx.assemble_graph(step_what)
+        for key, buf in zip(("S", "T", "vna", "vnao"), h_out):
+            ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
+        ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
+
+    h2d = 3 * natoms * 8 + 2 * NB * 8
+    d2h = 4 * NB * 8 + 3 * natoms * 8
+    timed = make_timer(torch, ctx, stream, flush, ws, local)
     for _ in range(args.warmup):
-        device_step()
+        batch_step()
         e2e_step()
+    sequential_step()
     clocks = ClockSampler(local)
     clocks.start()
-    ms, launches = timed(device_step, args.steps, timing=True)
-    ktimes = ctx.timing()
+    ms, launches = timed(batch_step, args.steps)
     ms_e2e, _ = timed(e2e_step, args.steps)
     clk = clocks.stop()
+    seq_steps = max(1, min(args.steps, 3))
+    ms_seq, seq_launches = make_timer(torch, seq, stream, flush, ws, local)(sequential_step, seq_steps)
+    # per-kernel times of the batch through the separate calls
+    def kernel_step():
+        ctx.driver_neighbors()
+        ctx.assemble(fbgpu.FB_ALL)
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.Dassemble(fbgpu.FB_ALL)
+    kernel_step()
+    ms_k, _ = timed(kernel_step, args.steps, timing=True)
+    ktimes = ctx.timing()
     ctx.set_timing(False)
-    fp64_peak = ctx.probe_fp64()
-
+    roof = roofline_for(ctx, ktimes, T, P, natoms, nZ, args.steps)
     per_step = ms / args.steps
-    value = ws * P * args.steps / (ms * 1e-3)
-    e2e_value = ws * P * args.steps / (ms_e2e * 1e-3)
-    # dominant kernel and its roofline
-    dom = max(ktimes, key=lambda k: ktimes[k][0])
-    dom_ms = ktimes[dom][0] / max(1, ktimes[dom][1])
-    from fbgpu import synth
-    nme = len(synth.make_munu_3c([0, 1], [0, 1])[0])
-    fl = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
-    roof = None
-    if fl is not None:
-        ach = fl / (dom_ms * 1e-3) / 1e12
-        roof = {"bound": "fp64", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp64_peak, 4),
-                "unit": "TFLOP/s", "frac": round(ach / fp64_peak, 4), "traffic": None,
-                "peak_source": "measured in this run (fb_probe_fp64 DFMA chains)",
-                "flops_per_launch": fl, "avg_launch_ms": round(dom_ms, 4)}
-        table_bytes = 8 * 31 * 31 * 5 * nme * len(nZ) ** 3
-        by = bytes_dassemble_3c(T, P, st.natoms, 16, table_bytes)
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            hbm_peak = json.load(f)["hbm_gbs"]
-        roof["hbm"] = {"achieved": round(by / (dom_ms * 1e-3) / 1e9, 3), "peak": hbm_peak, "unit": "GB/s",
-                       "frac": round(by / (dom_ms * 1e-3) / 1e9 / hbm_peak, 6), "bytes_per_launch": by,
-                       "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+    sizes = np.diff(off["atom"])
     line = {
-        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
+        "metric": METRIC, "value": round(ws * P * args.steps / (ms * 1e-3), 1), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS["batch256"], "structures": len(structs), "natoms": natoms,
+                   "atoms_min_max": [int(sizes.min()), int(sizes.max())], "pairs": P, "triplets": T,
                    "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "flushed between steps (256 MiB write)", "forces": True},
-        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                   "l2": "inputs larger than L2 and flushed between steps (256 MiB write)", "forces": True,
+                   "step": "fb_neighbors over the batch + one CUDA graph launch (assembly + forces)",
+                   "launch_shapes": shapes, "autotuned": not args.no_autotune},
+        "e2e": {"value": round(ws * P * args.steps / (ms_e2e * 1e-3), 1), "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(ms_e2e / args.steps, 4)},
+        "sequential": {"ms_per_step": round(ms_seq / seq_steps, 4),
+                       "value": round(P * seq_steps / (ms_seq * 1e-3), 1), "unit": UNIT,
+                       "gpu_launches_per_step": seq_launches // seq_steps,
+                       "how": "the 256 structures one after another: fb_set_structure + fb_neighbors + "
+                              "fb_assemble + fb_dassemble each (device-resident density matrices)",
+                       "batch_speedup": round((ms_seq / seq_steps) / per_step, 3)},
         "gpu_launches": launches,
         "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+        "separate_calls_ms_per_step": round(ms_k / args.steps, 4),
         "roofline": roof,
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(args.workload, path, nZ, st, P)
+        line["cpu_baseline"] = cpu_baseline_batch(path, nZ, structs, P)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    seq.close()
     ctx.close()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+
+
+def cpu_baseline_batch(path, nZ, structs, P_total, nsample=16):
+    """The oracle on a bounded sample of the batch (the first nsample
+    structures), scaled to blocks/s."""
+    from oracle import oracle as orc
+    from conftest import symmetric_denmat
+    cores = os.cpu_count() or 1
+    fd = orc.Fdata(path, nZ)
+    t_tot, p_tot = 0.0, 0
+    for st in structs[:nsample]:
+        t0 = time.perf_counter()
+        s = orc.System(fd, st.ratom, st.imass, st.lattice, threads=cores).neighbors()
+        s.assemble()
+        t1 = time.perf_counter()
+        norb = np.array([fd.norb(int(k)) for k in st.imass])
+        rho, cape = symmetric_denmat(s, norb, 42)
+        t2 = time.perf_counter()
+        s.dassemble(rho, cape)
+        t3 = time.perf_counter()
+        t_tot += (t1 - t0) + (t3 - t2)
+        p_tot += s.npairs
+    return {"value": round(p_tot / t_tot, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "the first %d of the 256 structures (%d pairs), neighbors + 2c + 3c assembly + forces, "
+                      "%.3f s" % (nsample, p_tot, t_tot)}
 
 
 def cpu_baseline(workload, path, nZ, st, P_expect=None, steps=1):
@@ -339,6 +573,8 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
+    if args.workload == "batch256":
+        return run_reference_batch(args, ws)
     path, nZ, st = load_workload(args.workload)
     cb = None
     for _ in range(args.warmup):
@@ -355,6 +591,27 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_batch(args, ws):
+    from fbgpu import synth
+    path = synth.fdata_dir_for("batch256", root=fdata_root())
+    nZ = [s.nZ for s in synth.species_for("batch256")]
+    structs = synth.batch_structures(256)
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline_batch(path, nZ, structs, None, nsample=2)
+    t0 = time.perf_counter()
+    cbs = [cpu_baseline_batch(path, nZ, structs, None) for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
+    cb = cbs[-1]
+    cb["value"] = round(float(np.median([c["value"] for c in cbs])), 1)
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["batch256"], "structures": 256},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -363,6 +620,7 @@ def main():
     ap.add_argument("--impl", default="fbgpu", choices=["fbgpu", "reference"])
     ap.add_argument("--workload", default="si512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--prec", default="df", choices=["df", "fp64"],
                     help="three-center arithmetic: double-float on the FP32 pipe (default) or FP64")
     args = ap.parse_args()

@@ -75,6 +75,7 @@ extern "C" {
 #define FB_VNA3C 8u    /* neutral atom 3c   (assemble_vna_3c / Dassemble_vna_3c) */
 #define FB_ALL 15u
 #define FB_KEEP_DBLOCKS 16u  /* fb_dassemble: also keep dS, dT Dblocks */
+#define FB_FORCES 32u        /* fb_assemble_graph / fb_autotune: the force pass too */
 
 /* block sets for fb_get_blocks / fb_device_blocks */
 #define FB_BLOCK_S 0       /* s%overlap(i)%neighbors(k)%block */
@@ -123,6 +124,28 @@ int fb_species_norb(const fb_ctx *ctx, int isp);
  * (c.SYSTEM/make_cells.f90:51).  icluster = 1 disables periodic images. */
 int fb_set_structure(fb_ctx *ctx, int natoms, const double *ratom,
                      const int *imass, const double *lattice, int icluster);
+/* Batch of independent structures (MD snapshots or unrelated
+ * configurations of uneven size) assembled together.  No reference
+ * counterpart: the reference handles one structure per process; each
+ * structure here keeps the reference's per-structure semantics (its own
+ * make_cells images, neighbor maps that never cross structures).
+ * natoms[s] atoms of structure s follow one another in ratom (3 per atom)
+ * and imass; lattice holds 9 doubles per structure (rows a1, a2, a3; may be
+ * NULL when every structure is a cluster); icluster[s] = 1 marks a cluster
+ * (NULL: all periodic).  fb_set_structure is the batch of one.  All later
+ * calls act on the whole batch: block arrays, force arrays and pair lists
+ * are the structures' arrays one after another, with the offsets of
+ * fb_get_batch; atom numbers returned by fb_get_neighbors / fb_get_common
+ * are 1-based within each structure, as the reference numbers them. */
+int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms,
+                 const double *ratom, const int *imass, const double *lattice,
+                 const int *icluster);
+/* Per-structure offsets (nstruct + 1 entries each, 0-based, last = total):
+ * first atom, first pair, first common-neighbor triplet and first block
+ * element.  Any pointer may be NULL; pair, triplet and block offsets need
+ * fb_neighbors first. */
+int fb_get_batch(const fb_ctx *ctx, int *atom_off, int *pair_off,
+                 int *trip_off, long long *block_off);
 /* New positions for the same atoms (an MD step); neighbor maps must be
  * rebuilt by fb_neighbors before the next assembly. */
 int fb_update_positions(fb_ctx *ctx, const double *ratom);
@@ -178,6 +201,41 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out);
  * back.  Any output may be NULL. */
 int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T,
                      double *vna, double *vnao);
+
+/* Value pass (what & FB_ALL) and, with FB_FORCES, the force pass of
+ * fb_dassemble (same bits, FB_KEEP_DBLOCKS allowed) as ONE CUDA graph
+ * launch on the context's stream.  The graph is captured on the first call
+ * and replayed while the sizes (atoms, pairs, triplets, block elements),
+ * device buffers, precision, launch shapes, stream and `what` stay the
+ * same, so new positions and rebuilt neighbor maps of unchanged sizes reuse
+ * it; anything else re-captures it.  For a batch (fb_set_batch) every kernel node is one launch over the
+ * whole batch's concatenated pair or triplet list.  Results are the same as
+ * fb_assemble(what & FB_ALL) followed by fb_dassemble(what).  The density
+ * matrix must be set (fb_set_denmat / _device) before a call with
+ * FB_FORCES; its contents may change between calls.  No reference
+ * counterpart. */
+int fb_assemble_graph(fb_ctx *ctx, unsigned what);
+
+/* Launch shape of a tunable kernel ("assemble_2c", "assemble_3c",
+ * "dassemble_2c", "dassemble_3c"): threads per CTA (32..256, a multiple of
+ * 32), ctas_per_sm = 0 for a grid that covers the work (one triplet per
+ * thread, one atom per warp), or > 0 for a persistent grid of
+ * ctas_per_sm CTAs per SM whose warps take `chunk` groups of work (32
+ * triplets, or one atom, per group) at a time from a device counter. */
+int fb_set_launch(fb_ctx *ctx, const char *kernel, int threads,
+                  int ctas_per_sm, int chunk);
+int fb_get_launch(const fb_ctx *ctx, const char *kernel, int *threads,
+                  int *ctas_per_sm, int *chunk);
+/* Autotuner: times every candidate launch shape (covering grids of 64, 128
+ * and 256 threads; persistent grids of 256..2048 threads per SM with chunks
+ * of 1, 4 and 16) of the kernels `what` selects (FB_FORCES adds the force
+ * kernels; they need the density matrix) on the current system with CUDA
+ * events, `reps` launches per shape, and keeps the fastest.  best_ms (may be
+ * NULL) receives 4 doubles: the best time per launch of assemble_2c,
+ * assemble_3c, dassemble_2c, dassemble_3c (0 if not tuned).  The timed
+ * launches overwrite the block and force arrays: assemble again before
+ * reading them.  No reference counterpart. */
+int fb_autotune(fb_ctx *ctx, unsigned what, int reps, double *best_ms);
 
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions

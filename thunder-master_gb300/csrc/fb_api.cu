@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -22,8 +23,15 @@ enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho"};
+// kernels with a tunable launch shape
+enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
+static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
 
 namespace {
+
+// bumped by every device (re)allocation: a captured CUDA graph whose
+// pointers may have moved is re-captured
+std::atomic<long long> g_alloc_gen{0};
 
 // device buffer that grows on demand and never shrinks
 struct DevBuf {
@@ -37,6 +45,7 @@ struct DevBuf {
     size_t want = std::max<size_t>(bytes, 256);
     if (cudaMalloc(&p, want) != cudaSuccess) return FB_ERR_CUDA;
     cap = want;
+    g_alloc_gen++;
     return 0;
   }
   void release() {
@@ -63,17 +72,21 @@ struct fb_ctx {
   DevBuf d_fd, d_tab2, d_tab3, d_tab3df, d_lin, d_gxy;
   int prec = FB_PREC_DF;
   // structure
-  int N = 0, icluster = 0, mbeta_max = 0;
-  std::vector<double> h_xl;
-  std::vector<int> h_isp, h_imgs;
-  double lattice[9] = {0};
-  float4 bbox_lo{}, bbox_hi{};
-  DevBuf d_ratom, d_pos4, d_isp, d_xl, d_xlf, d_imgs;
+  // structures: a batch of nstruct concatenated systems (one structure is a
+  // batch of one); structure s holds atoms h_satom_off[s] .. h_satom_off[s+1]-1
+  int N = 0, nstruct = 0;
+  std::vector<int> h_satom_off, h_sid, h_icl, h_simg_off, h_isp, h_imgs;
+  std::vector<double> h_lat;   // 9 per structure, rows a1, a2, a3
+  std::vector<double> h_xl;    // XL_STRIDE per structure
+  std::vector<float4> h_sbbox; // lo, hi per structure
+  float rcmax = 0.0f;
+  DevBuf d_ratom, d_pos4, d_isp, d_xl, d_xlf, d_imgs, d_sid, d_satom_off, d_simg_off, d_sbbox, d_speriodic;
   // neighbors
   bool have_neigh = false;
   int P = 0, T = 0;
   long long nblock = 0;
   std::vector<int> h_pair_off, h_trip_off;
+  std::vector<long long> h_blk_base;  // first block element of each atom's pairs (+ total)
   DevBuf d_bsum, d_blk_base;
   DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
@@ -85,6 +98,20 @@ struct fb_ctx {
   unsigned assembled = 0, dassembled = 0;
   // forces
   DevBuf d_sumT, d_sumS, d_ontop, d_atomf, d_f3a, d_f3b, d_f3c, d_kin, d_vna, d_pul, d_ftot;
+  // launch shapes of the tunable kernels and their persistent work counters
+  int nsm = 0;
+  KCfg cfg[TK_N];
+  DevBuf d_queue;
+  // CUDA graph of assembly + force pass (fb_assemble_graph).  Its kernel
+  // arguments hold device pointers and the sizes N, P, T, nblock; it stays
+  // valid while none of them changes (new positions and rebuilt neighbor
+  // maps of the same sizes reuse it).
+  cudaGraphExec_t gexec = nullptr;
+  unsigned g_what = 0;
+  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1;
+  long long g_nblock = -1, g_alloc = -1, g_launches = 0;
+  cudaStream_t g_stream = nullptr;
+  KCfg g_cfg[TK_N];
   // per-kernel CUDA-event timing (fb_set_timing)
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evpool;
@@ -191,6 +218,12 @@ int fb_create(int device, fb_ctx **out) {
     return FB_ERR_CUDA;
   }
   cudaMemset(ctx->d_status.p, 0, sizeof(unsigned));
+  if (cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      ctx->d_queue.ensure(TK_N * sizeof(int))) {
+    fb_destroy(ctx);
+    return FB_ERR_CUDA;
+  }
+  for (int k = 0; k < TK_N; k++) ctx->cfg[k] = KCfg{128, 0, 1, ctx->nsm};
   *out = ctx;
   return FB_OK;
 }
@@ -207,8 +240,11 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
                     &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm,
-                    &ctx->d_thist};
+                    &ctx->d_thist, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
+                    &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
+  ctx->d_queue.release();
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   for (auto &e : ctx->evpool) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
@@ -256,16 +292,16 @@ int fb_species_norb(const fb_ctx *ctx, int isp) {
   return ctx->fdh.sp[isp - 1].norb;
 }
 
-// image list: every cell mbeta whose translation can bring some atom within
-// range of another; kept in increasing mbeta (the reference loop order)
-static void make_images(fb_ctx *ctx, const double *ratom) {
-  ctx->h_imgs.clear();
-  if (ctx->icluster == 1) {
+// image list of structure s: every cell mbeta whose translation can bring
+// some atom within range of another; kept in increasing mbeta (the
+// reference loop order)
+static void make_images(fb_ctx *ctx, int s, const double *ratom) {
+  if (ctx->h_icl[s] == 1) {
     ctx->h_imgs.push_back(0);
     return;
   }
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (int i = 0; i < ctx->N; i++)
+  for (int i = ctx->h_satom_off[s]; i < ctx->h_satom_off[s + 1]; i++)
     for (int k = 0; k < 3; k++) {
       lo[k] = std::min(lo[k], ratom[3 * i + k]);
       hi[k] = std::max(hi[k], ratom[3 * i + k]);
@@ -275,84 +311,129 @@ static void make_images(fb_ctx *ctx, const double *ratom) {
   double rmax = 0.0;
   for (int k = 0; k < ctx->fdh.nspecies; k++) rmax = std::max(rmax, ctx->fdh.sp[k].rcA);
   double reach = std::max(2.0 * rmax, 0.5) + D + 1.0;
-  for (int mb = 0; mb <= ctx->mbeta_max; mb++) {
-    const double *L = &ctx->h_xl[3 * mb];
+  const double *X = &ctx->h_xl[(size_t)s * XL_STRIDE];
+  for (int mb = 0; mb < NIMG; mb++) {
+    const double *L = X + 3 * mb;
     double l = std::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
     if (l < reach) ctx->h_imgs.push_back(mb);
   }
 }
 
-int fb_set_structure(fb_ctx *ctx, int natoms, const double *ratom, const int *imass, const double *lattice,
-                     int icluster) {
-  if (!ctx || natoms < 1 || !ratom || !imass || (!lattice && icluster != 1)) return FB_ERR_ARG;
+int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms, const double *ratom, const int *imass,
+                 const double *lattice, const int *icluster) {
+  if (!ctx || nstruct < 1 || !natoms || !ratom || !imass) return FB_ERR_ARG;
   if (!ctx->have_fdata) return fail(ctx, FB_ERR_STATE, "fb_load_fdata first");
+  long long total = 0;
+  for (int s = 0; s < nstruct; s++) {
+    if (natoms[s] < 1) return fail(ctx, FB_ERR_ARG, "structure %d has %d atoms", s + 1, natoms[s]);
+    if ((!icluster || icluster[s] != 1) && !lattice)
+      return fail(ctx, FB_ERR_ARG, "structure %d is periodic but no lattice was given", s + 1);
+    total += natoms[s];
+  }
+  if (total > (1LL << 30)) return fail(ctx, FB_ERR_ARG, "%lld atoms in the batch", total);
   CU(cudaSetDevice(ctx->device));
-  ctx->N = natoms;
-  ctx->icluster = icluster;
-  ctx->h_isp.resize(natoms);
-  for (int i = 0; i < natoms; i++) {
+  int N = (int)total;
+  ctx->N = N;
+  ctx->nstruct = nstruct;
+  ctx->h_isp.resize(N);
+  for (int i = 0; i < N; i++) {
     if (imass[i] < 1 || imass[i] > ctx->fdh.nspecies)
       return fail(ctx, FB_ERR_ARG, "imass(%d) = %d out of range", i + 1, imass[i]);
     ctx->h_isp[i] = imass[i] - 1;
   }
-  if (lattice) std::memcpy(ctx->lattice, lattice, sizeof ctx->lattice);
-  // make_cells (c.SYSTEM/make_cells.f90:112-144)
-  if (icluster == 1) {
-    ctx->mbeta_max = 0;
-    ctx->h_xl.assign(3, 0.0);
-  } else {
-    ctx->mbeta_max = (2 * P_mbox + 1) * (2 * P_mbox + 1) * (2 * P_mbox + 1) - 1;
-    ctx->h_xl.assign(3 * (ctx->mbeta_max + 1), 0.0);
+  ctx->h_satom_off.assign(nstruct + 1, 0);
+  ctx->h_sid.resize(N);
+  ctx->h_icl.assign(nstruct, 0);
+  ctx->h_lat.assign((size_t)9 * nstruct, 0.0);
+  ctx->h_xl.assign((size_t)XL_STRIDE * nstruct, 0.0);
+  for (int s = 0; s < nstruct; s++) {
+    ctx->h_satom_off[s + 1] = ctx->h_satom_off[s] + natoms[s];
+    for (int i = ctx->h_satom_off[s]; i < ctx->h_satom_off[s + 1]; i++) ctx->h_sid[i] = s;
+    ctx->h_icl[s] = icluster ? icluster[s] : 0;
+    if (ctx->h_icl[s] == 1) continue;  // a cluster has mbeta = 0 only
+    double *lat = &ctx->h_lat[(size_t)9 * s];
+    std::memcpy(lat, lattice + (size_t)9 * s, 9 * sizeof(double));
+    // make_cells (c.SYSTEM/make_cells.f90:112-144)
+    double *X = &ctx->h_xl[(size_t)s * XL_STRIDE];
     int mb = 1;
     for (int iz = -P_mbox; iz <= P_mbox; iz++)
       for (int iy = -P_mbox; iy <= P_mbox; iy++)
         for (int ix = -P_mbox; ix <= P_mbox; ix++)
           if (!(ix == 0 && iy == 0 && iz == 0)) {
             for (int k = 0; k < 3; k++)
-              ctx->h_xl[3 * mb + k] = (double)ix * ctx->lattice[k] + (double)iy * ctx->lattice[3 + k] +
-                                      (double)iz * ctx->lattice[6 + k];
+              X[3 * mb + k] = (double)ix * lat[k] + (double)iy * lat[3 + k] + (double)iz * lat[6 + k];
             mb++;
           }
   }
   std::vector<float> xlf(ctx->h_xl.begin(), ctx->h_xl.end());
+  std::vector<int> per(nstruct);
+  for (int s = 0; s < nstruct; s++) per[s] = ctx->h_icl[s] != 1;
   CHK(ctx->d_xl.ensure(ctx->h_xl.size() * sizeof(double)));
   CHK(ctx->d_xlf.ensure(xlf.size() * sizeof(float)));
-  CHK(ctx->d_isp.ensure(natoms * sizeof(int)));
+  CHK(ctx->d_isp.ensure(N * sizeof(int)));
+  CHK(ctx->d_sid.ensure(N * sizeof(int)));
+  CHK(ctx->d_satom_off.ensure((nstruct + 1) * sizeof(int)));
+  CHK(ctx->d_speriodic.ensure(nstruct * sizeof(int)));
   CU(cudaMemcpy(ctx->d_xl.p, ctx->h_xl.data(), ctx->h_xl.size() * sizeof(double), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_xlf.p, xlf.data(), xlf.size() * sizeof(float), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(ctx->d_isp.p, ctx->h_isp.data(), natoms * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_isp.p, ctx->h_isp.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_sid.p, ctx->h_sid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_satom_off.p, ctx->h_satom_off.data(), (nstruct + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_speriodic.p, per.data(), nstruct * sizeof(int), cudaMemcpyHostToDevice));
   ctx->have_neigh = false;
   return fb_update_positions(ctx, ratom);
+}
+
+int fb_set_structure(fb_ctx *ctx, int natoms, const double *ratom, const int *imass, const double *lattice,
+                     int icluster) {
+  if (!ctx || natoms < 1 || !ratom || !imass || (!lattice && icluster != 1)) return FB_ERR_ARG;
+  return fb_set_batch(ctx, 1, &natoms, ratom, imass, lattice, &icluster);
 }
 
 int fb_update_positions(fb_ctx *ctx, const double *ratom) {
   if (!ctx || !ratom) return FB_ERR_ARG;
   if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
   CU(cudaSetDevice(ctx->device));
-  int N = ctx->N;
-  make_images(ctx, ratom);
-  // float positions with the species cutoff in .w, and the bounding box
+  int N = ctx->N, ns = ctx->nstruct;
+  ctx->h_imgs.clear();
+  ctx->h_simg_off.assign(ns + 1, 0);
+  for (int s = 0; s < ns; s++) {
+    make_images(ctx, s, ratom);
+    ctx->h_simg_off[s + 1] = (int)ctx->h_imgs.size();
+  }
+  // float positions with the species cutoff in .w, and the bounding boxes
   std::vector<float4> p4(N);
   float rcmax = 0.0f;
   for (int k = 0; k < ctx->fdh.nspecies; k++) rcmax = std::max(rcmax, (float)ctx->fdh.sp[k].rcA);
-  ctx->bbox_lo = make_float4(1e30f, 1e30f, 1e30f, rcmax);
-  ctx->bbox_hi = make_float4(-1e30f, -1e30f, -1e30f, 0.0f);
-  for (int i = 0; i < N; i++) {
-    p4[i] = make_float4((float)ratom[3 * i], (float)ratom[3 * i + 1], (float)ratom[3 * i + 2],
-                        (float)ctx->fdh.sp[ctx->h_isp[i]].rcA);
-    ctx->bbox_lo.x = std::min(ctx->bbox_lo.x, p4[i].x);
-    ctx->bbox_lo.y = std::min(ctx->bbox_lo.y, p4[i].y);
-    ctx->bbox_lo.z = std::min(ctx->bbox_lo.z, p4[i].z);
-    ctx->bbox_hi.x = std::max(ctx->bbox_hi.x, p4[i].x);
-    ctx->bbox_hi.y = std::max(ctx->bbox_hi.y, p4[i].y);
-    ctx->bbox_hi.z = std::max(ctx->bbox_hi.z, p4[i].z);
+  ctx->rcmax = rcmax;
+  ctx->h_sbbox.assign(2 * (size_t)ns, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  for (int s = 0; s < ns; s++) {
+    float4 lo = make_float4(1e30f, 1e30f, 1e30f, 0.0f), hi = make_float4(-1e30f, -1e30f, -1e30f, 0.0f);
+    for (int i = ctx->h_satom_off[s]; i < ctx->h_satom_off[s + 1]; i++) {
+      p4[i] = make_float4((float)ratom[3 * i], (float)ratom[3 * i + 1], (float)ratom[3 * i + 2],
+                          (float)ctx->fdh.sp[ctx->h_isp[i]].rcA);
+      lo.x = std::min(lo.x, p4[i].x);
+      lo.y = std::min(lo.y, p4[i].y);
+      lo.z = std::min(lo.z, p4[i].z);
+      hi.x = std::max(hi.x, p4[i].x);
+      hi.y = std::max(hi.y, p4[i].y);
+      hi.z = std::max(hi.z, p4[i].z);
+    }
+    ctx->h_sbbox[2 * s] = lo;
+    ctx->h_sbbox[2 * s + 1] = hi;
   }
-  CHK(ctx->d_ratom.ensure(3 * N * sizeof(double)));
+  CHK(ctx->d_ratom.ensure(3 * (size_t)N * sizeof(double)));
   CHK(ctx->d_pos4.ensure(N * sizeof(float4)));
   CHK(ctx->d_imgs.ensure(ctx->h_imgs.size() * sizeof(int)));
-  CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CHK(ctx->d_simg_off.ensure((ns + 1) * sizeof(int)));
+  CHK(ctx->d_sbbox.ensure(2 * (size_t)ns * sizeof(float4)));
+  CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_pos4.p, p4.data(), N * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_imgs.p, ctx->h_imgs.data(), ctx->h_imgs.size() * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_simg_off.p, ctx->h_simg_off.data(), (ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_sbbox.p, ctx->h_sbbox.data(), 2 * (size_t)ns * sizeof(float4), cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_neigh = false;
@@ -363,12 +444,14 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   NeighArgs a{};
   a.N = ctx->N;
   a.P = ctx->P;
-  a.nimg = (int)ctx->h_imgs.size();
   a.ratom = ctx->d_ratom.as<double>();
   a.pos4 = ctx->d_pos4.as<float4>();
-  a.bbox_lo = ctx->bbox_lo;
-  a.bbox_hi = ctx->bbox_hi;
-  a.periodic = ctx->icluster != 1;
+  a.sid = ctx->d_sid.as<int>();
+  a.satom_off = ctx->d_satom_off.as<int>();
+  a.simg_off = ctx->d_simg_off.as<int>();
+  a.sbbox = ctx->d_sbbox.as<float4>();
+  a.speriodic = ctx->d_speriodic.as<int>();
+  a.rcmax = ctx->rcmax;
   a.isp = ctx->d_isp.as<int>();
   a.fd = ctx->d_fd.as<FdataDev>();
   a.xl = ctx->d_xl.as<double>();
@@ -483,12 +566,15 @@ int fb_neighbors(fb_ctx *ctx) {
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
   ctx->h_pair_off.assign(N + 1, 0);
+  ctx->h_blk_base.assign(N + 1, 0);
   long long nb = 0;
   for (int i = 0; i < N; i++) {
     ctx->h_pair_off[i + 1] = ctx->h_pair_off[i] + cnt[i];
     bbase[i] = nb;
+    ctx->h_blk_base[i] = nb;
     nb += bsum[i];
   }
+  ctx->h_blk_base[N] = nb;
   int P = ctx->h_pair_off[N];
   ctx->P = P;
   ctx->nblock = nb;
@@ -522,17 +608,21 @@ int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const i
   }
   int P = ctx->h_pair_off[N];
   ctx->P = P;
+  // neigh_j is numbered within the atom's own structure (1-based)
   std::vector<int> nj(P), self(N, -1);
-  for (int i = 0; i < N; i++)
+  for (int i = 0; i < N; i++) {
+    int s = ctx->h_sid[i], a0 = ctx->h_satom_off[s], ns = ctx->h_satom_off[s + 1] - a0;
+    int bmax = ctx->h_icl[s] == 1 ? 0 : NIMG - 1;
     for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
-      if (neigh_j[p] < 1 || neigh_j[p] > N || neigh_b[p] < 0 || neigh_b[p] > ctx->mbeta_max)
+      if (neigh_j[p] < 1 || neigh_j[p] > ns || neigh_b[p] < 0 || neigh_b[p] > bmax)
         return fail(ctx, FB_ERR_ARG, "neighbor %d of atom %d out of range", p - ctx->h_pair_off[i] + 1, i + 1);
-      nj[p] = neigh_j[p] - 1;
+      nj[p] = a0 + neigh_j[p] - 1;
       if (nj[p] == i && neigh_b[p] == 0) {
         if (self[i] >= 0) return fail(ctx, FB_ERR_NEIGH_SELF, "neigh_self found twice for atom %d", i + 1);
         self[i] = p - ctx->h_pair_off[i];
       }
     }
+  }
   CHK(ctx->d_pair_off.ensure((N + 1) * sizeof(int)));
   CHK(ctx->d_neigh_j.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_neigh_b.ensure(P * sizeof(int) + 4));
@@ -546,8 +636,10 @@ int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const i
   std::vector<int> owner(P);
   std::vector<long long> blk(P + 1);
   long long off = 0;
+  ctx->h_blk_base.assign(N + 1, 0);
   for (int i = 0; i < N; i++) {
     if (self[i] < 0) return fail(ctx, FB_ERR_NEIGH_SELF, "no neigh_self for atom %d", i + 1);
+    ctx->h_blk_base[i] = off;
     int ni = ctx->fdh.sp[ctx->h_isp[i]].norb;
     for (int p = ctx->h_pair_off[i]; p < ctx->h_pair_off[i + 1]; p++) {
       owner[p] = i;
@@ -556,6 +648,7 @@ int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const i
     }
   }
   blk[P] = off;
+  ctx->h_blk_base[N] = off;
   ctx->nblock = off;
   CHK(ctx->d_pair_owner.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_blk_off.ensure((P + 1) * sizeof(long long)));
@@ -583,6 +676,16 @@ static int d2h_int(fb_ctx *ctx, int *dst, const DevBuf &src, size_t n, int add) 
   return FB_OK;
 }
 
+// atom numbers of a per-item list, made 1-based within the structure of the
+// item's owner atom (off[owner] .. off[owner+1]-1 are the owner's items)
+static void local_atoms(const fb_ctx *ctx, int *dst, const std::vector<int> &off) {
+  if (!dst || ctx->nstruct < 2) return;
+  for (int i = 0; i < ctx->N; i++) {
+    int a0 = ctx->h_satom_off[ctx->h_sid[i]];
+    for (int k = off[i]; k < off[i + 1]; k++) dst[k] -= a0;
+  }
+}
+
 int fb_get_neighbors(fb_ctx *ctx, int *neighn, int *neigh_j, int *neigh_b, int *neigh_back, int *neigh_self,
                      long long *blk_off) {
   if (!ctx) return FB_ERR_ARG;
@@ -590,6 +693,7 @@ int fb_get_neighbors(fb_ctx *ctx, int *neighn, int *neigh_j, int *neigh_b, int *
   if (neighn)
     for (int i = 0; i < ctx->N; i++) neighn[i] = ctx->h_pair_off[i + 1] - ctx->h_pair_off[i];
   CHK(d2h_int(ctx, neigh_j, ctx->d_neigh_j, ctx->P, 1));
+  local_atoms(ctx, neigh_j, ctx->h_pair_off);
   CHK(d2h_int(ctx, neigh_b, ctx->d_neigh_b, ctx->P, 0));
   CHK(d2h_int(ctx, neigh_back, ctx->d_neigh_back, ctx->P, 1));
   CHK(d2h_int(ctx, neigh_self, ctx->d_neigh_self, ctx->N, 1));
@@ -606,10 +710,27 @@ int fb_get_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_com
   if (ncommon)
     for (int i = 0; i < ctx->N; i++) ncommon[i] = ctx->h_trip_off[i + 1] - ctx->h_trip_off[i];
   CHK(d2h_int(ctx, iatom_common_j, ctx->d_ci_j, ctx->T, 1));
+  local_atoms(ctx, iatom_common_j, ctx->h_trip_off);
   CHK(d2h_int(ctx, iatom_common_b, ctx->d_ci_b, ctx->T, 0));
   CHK(d2h_int(ctx, jatom_common_j, ctx->d_cj_j, ctx->T, 1));
+  local_atoms(ctx, jatom_common_j, ctx->h_trip_off);
   CHK(d2h_int(ctx, jatom_common_b, ctx->d_cj_b, ctx->T, 0));
   CHK(d2h_int(ctx, neigh_common, ctx->d_cneigh, ctx->T, 1));
+  return FB_OK;
+}
+
+int fb_get_batch(const fb_ctx *ctx, int *atom_off, int *pair_off, int *trip_off, long long *block_off) {
+  if (!ctx) return FB_ERR_ARG;
+  if (ctx->nstruct < 1) return FB_ERR_STATE;
+  if ((pair_off || trip_off || block_off) && !ctx->have_neigh) return FB_ERR_STATE;
+  for (int s = 0; s <= ctx->nstruct; s++) {
+    int a = ctx->h_satom_off[s];
+    if (atom_off) atom_off[s] = a;
+    if (pair_off) pair_off[s] = ctx->h_pair_off[a];
+    if (trip_off) trip_off[s] = ctx->h_trip_off[a];
+  }
+  if (block_off)
+    for (int s = 0; s <= ctx->nstruct; s++) block_off[s] = ctx->h_blk_base[ctx->h_satom_off[s]];
   return FB_OK;
 }
 
@@ -619,6 +740,7 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.ntrip = ctx->T;
   a.have_d = ctx->fdh.have_d;
   a.ratom = ctx->d_ratom.as<double>();
+  a.sid = ctx->d_sid.as<int>();
   a.isp = ctx->d_isp.as<int>();
   a.fd = ctx->d_fd.as<FdataDev>();
   a.table2c = ctx->d_tab2.as<double>();
@@ -661,6 +783,11 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.status = ctx->d_status.as<unsigned>();
   a.table3c_df = ctx->d_tab3df.as<float2>();
   a.rho_df = ctx->d_rho_df.as<float2>();
+  a.cfg_a2c = ctx->cfg[TK_A2C];
+  a.cfg_a3c = ctx->cfg[TK_A3C];
+  a.cfg_d2c = ctx->cfg[TK_D2C];
+  a.cfg_d3c = ctx->cfg[TK_D3C];
+  a.queue = ctx->d_queue.as<int>();
   return a;
 }
 
@@ -672,13 +799,8 @@ int fb_set_precision(fb_ctx *ctx, int mode) {
   return FB_OK;
 }
 
-int fb_assemble(fb_ctx *ctx, unsigned what) {
-  if (!ctx) return FB_ERR_ARG;
-  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
-  if ((what & FB_VNA3C) && !(what & FB_VNA2C) && !ctx->have_vna2c)
-    return fail(ctx, FB_ERR_STATE, "assemble_vna_3c accumulates onto assemble_vna_2c blocks: assemble FB_VNA2C first");
-  CU(cudaSetDevice(ctx->device));
-  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+// launches of the value pass (no synchronization)
+static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
@@ -686,6 +808,22 @@ int fb_assemble(fb_ctx *ctx, unsigned what) {
     if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(a, ctx->stream));
     else KL(KT_ASM3C, launch_assemble_3c(a, ctx->stream));
   }
+  return FB_OK;
+}
+
+static int check_assemble(fb_ctx *ctx, unsigned what) {
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if ((what & FB_VNA3C) && !(what & FB_VNA2C) && !ctx->have_vna2c)
+    return fail(ctx, FB_ERR_STATE, "assemble_vna_3c accumulates onto assemble_vna_2c blocks: assemble FB_VNA2C first");
+  return FB_OK;
+}
+
+int fb_assemble(fb_ctx *ctx, unsigned what) {
+  if (!ctx) return FB_ERR_ARG;
+  CHK(check_assemble(ctx, what));
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  CHK(enqueue_assemble(ctx, what));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
@@ -759,11 +897,11 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
   return FB_OK;
 }
 
-int fb_dassemble(fb_ctx *ctx, unsigned what) {
-  if (!ctx) return FB_ERR_ARG;
+// device storage of the force pass (allocations happen here, never while
+// a graph is being captured)
+static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
-  CU(cudaSetDevice(ctx->device));
   int N = ctx->N, P = ctx->P;
   size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
   CHK(ctx->d_sumT.ensure(pb));
@@ -772,13 +910,19 @@ int fb_dassemble(fb_ctx *ctx, unsigned what) {
   CHK(ctx->d_atomf.ensure(pb));
   DevBuf *ab_bufs[] = {&ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c, &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot};
   for (DevBuf *b : ab_bufs) CHK(b->ensure(ab));
-  bool keep = (what & FB_KEEP_DBLOCKS) != 0;
-  if (keep) {
+  if (what & FB_KEEP_DBLOCKS) {
     size_t db = (size_t)3 * ctx->nblock * sizeof(double) + 8;
     CHK(ctx->d_dS.ensure(db));
     CHK(ctx->d_dT.ensure(db));
   }
-  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  if ((what & FB_VNA3C) && use_df(ctx)) CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
+  return FB_OK;
+}
+
+// clears and launches of the force pass (no synchronization)
+static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
+  int N = ctx->N, P = ctx->P;
+  size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
   CU(cudaMemsetAsync(ctx->d_f3a.p, 0, ab, ctx->stream));
   CU(cudaMemsetAsync(ctx->d_f3b.p, 0, ab, ctx->stream));
   CU(cudaMemsetAsync(ctx->d_f3c.p, 0, ab, ctx->stream));
@@ -787,13 +931,11 @@ int fb_dassemble(fb_ctx *ctx, unsigned what) {
   CU(cudaMemsetAsync(ctx->d_ontop.p, 0, pb, ctx->stream));
   CU(cudaMemsetAsync(ctx->d_atomf.p, 0, pb, ctx->stream));
   AsmArgs a = asm_args(ctx);
-  a.keep_dblocks = keep;
+  a.keep_dblocks = (what & FB_KEEP_DBLOCKS) != 0;
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
   if (what & FB_VNA3C) {
     if (use_df(ctx)) {
-      CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
-      a.rho_df = ctx->d_rho_df.as<float2>();
       KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
       KL(KT_DASM3C, launch_dassemble_3c_df(a, ctx->stream));
     } else {
@@ -801,11 +943,218 @@ int fb_dassemble(fb_ctx *ctx, unsigned what) {
     }
   }
   KL(KT_FORCES, launch_build_forces(a, what & FB_ALL, ctx->stream));
+  return FB_OK;
+}
+
+static void dassemble_done(fb_ctx *ctx, unsigned what) {
+  bool keep = (what & FB_KEEP_DBLOCKS) != 0;
+  ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
+  ctx->dassembled = what & FB_ALL;
+}
+
+int fb_dassemble(fb_ctx *ctx, unsigned what) {
+  if (!ctx) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  CHK(prepare_dassemble(ctx, what));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  CHK(enqueue_dassemble(ctx, what));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
-  ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
-  ctx->dassembled = what;
+  dassemble_done(ctx, what);
+  return FB_OK;
+}
+
+static bool same_cfg(const KCfg *a, const KCfg *b) {
+  for (int k = 0; k < TK_N; k++)
+    if (a[k].threads != b[k].threads || a[k].ctas_per_sm != b[k].ctas_per_sm || a[k].chunk != b[k].chunk)
+      return false;
+  return true;
+}
+
+// capture of the value pass (+ force pass) into one CUDA graph
+static int capture_graph(fb_ctx *ctx, unsigned what) {
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  bool timing = ctx->timing;
+  ctx->timing = false;  // no timing events inside the graph
+  long long l0 = ctx->launches;
+  CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int st = FB_OK;
+  if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
+    st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
+  if (!st && (what & FB_ALL)) st = enqueue_assemble(ctx, what);
+  if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->timing = timing;
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return fail(ctx, FB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    ctx->gexec = nullptr;
+    return fail(ctx, FB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  ctx->g_launches = ctx->launches - l0;
+  ctx->launches = l0;
+  ctx->g_what = what;
+  ctx->g_prec = ctx->prec;
+  ctx->g_N = ctx->N;
+  ctx->g_P = ctx->P;
+  ctx->g_T = ctx->T;
+  ctx->g_nblock = ctx->nblock;
+  ctx->g_have_d = ctx->fdh.have_d;
+  ctx->g_alloc = g_alloc_gen.load();
+  ctx->g_stream = ctx->stream;
+  for (int k = 0; k < TK_N; k++) ctx->g_cfg[k] = ctx->cfg[k];
+  return FB_OK;
+}
+
+int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!(what & (FB_ALL | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
+  CU(cudaSetDevice(ctx->device));
+  if (what & FB_ALL) CHK(check_assemble(ctx, what));
+  if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what));
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_prec == ctx->prec && ctx->g_N == ctx->N &&
+               ctx->g_P == ctx->P && ctx->g_T == ctx->T && ctx->g_nblock == ctx->nblock &&
+               ctx->g_have_d == ctx->fdh.have_d && ctx->g_alloc == g_alloc_gen.load() &&
+               ctx->g_stream == ctx->stream && same_cfg(ctx->g_cfg, ctx->cfg);
+  if (!fresh) CHK(capture_graph(ctx, what));
+  CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+  ctx->launches += ctx->g_launches;
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  if (what & FB_VNA2C) ctx->have_vna2c = true;
+  ctx->assembled |= what & FB_ALL;
+  if (what & FB_FORCES) dassemble_done(ctx, what);
+  return FB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch shapes and the autotuner
+// ---------------------------------------------------------------------------
+static int tk_index(const char *kernel) {
+  if (!kernel) return -1;
+  for (int k = 0; k < TK_N; k++)
+    if (std::strcmp(kernel, tk_names[k]) == 0) return k;
+  return -1;
+}
+
+int fb_set_launch(fb_ctx *ctx, const char *kernel, int threads, int ctas_per_sm, int chunk) {
+  if (!ctx) return FB_ERR_ARG;
+  int k = tk_index(kernel);
+  if (k < 0) return fail(ctx, FB_ERR_ARG, "no tunable kernel named %s", kernel ? kernel : "(null)");
+  if (threads < 32 || threads > 256 || threads % 32 || ctas_per_sm < 0 || ctas_per_sm > 64 || chunk < 1 ||
+      chunk > 4096)
+    return fail(ctx, FB_ERR_ARG, "launch shape (%d threads, %d CTAs/SM, chunk %d) out of range", threads,
+                ctas_per_sm, chunk);
+  ctx->cfg[k] = KCfg{threads, ctas_per_sm, chunk, ctx->nsm};
+  return FB_OK;
+}
+
+int fb_get_launch(const fb_ctx *ctx, const char *kernel, int *threads, int *ctas_per_sm, int *chunk) {
+  if (!ctx) return FB_ERR_ARG;
+  int k = tk_index(kernel);
+  if (k < 0) return FB_ERR_ARG;
+  if (threads) *threads = ctx->cfg[k].threads;
+  if (ctas_per_sm) *ctas_per_sm = ctx->cfg[k].ctas_per_sm;
+  if (chunk) *chunk = ctx->cfg[k].chunk;
+  return FB_OK;
+}
+
+// one launch of tunable kernel k with shape c
+static int tune_launch(fb_ctx *ctx, int k, const KCfg &c, unsigned what) {
+  AsmArgs a = asm_args(ctx);
+  a.keep_dblocks = false;
+  switch (k) {
+    case TK_A2C: a.cfg_a2c = c; return launch_assemble_2c(a, what & (FB_S | FB_T | FB_VNA2C), ctx->stream);
+    case TK_A3C:
+      a.cfg_a3c = c;
+      return use_df(ctx) ? launch_assemble_3c_df(a, ctx->stream) : launch_assemble_3c(a, ctx->stream);
+    case TK_D2C: a.cfg_d2c = c; return launch_dassemble_2c(a, what & (FB_S | FB_T | FB_VNA2C), ctx->stream);
+    case TK_D3C:
+      a.cfg_d3c = c;
+      return use_df(ctx) ? launch_dassemble_3c_df(a, ctx->stream) : launch_dassemble_3c(a, ctx->stream);
+  }
+  return 0;
+}
+
+int fb_autotune(fb_ctx *ctx, unsigned what, int reps, double *best_ms) {
+  if (!ctx) return FB_ERR_ARG;
+  if (reps < 1) reps = 1;
+  CU(cudaSetDevice(ctx->device));
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  bool forces = (what & FB_FORCES) != 0;
+  if (forces) CHK(prepare_dassemble(ctx, what | FB_ALL));
+  if (forces && (what & FB_VNA3C) && use_df(ctx)) {
+    AsmArgs a = asm_args(ctx);
+    KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
+  }
+  if (best_ms)
+    for (int k = 0; k < TK_N; k++) best_ms[k] = 0.0;
+  bool tune[TK_N] = {(what & (FB_S | FB_T | FB_VNA2C)) != 0, (what & FB_VNA3C) != 0,
+                     forces && (what & (FB_S | FB_T | FB_VNA2C)) != 0, forces && (what & FB_VNA3C) != 0};
+  // candidates: a grid that covers the work, and persistent grids filling
+  // 256 .. 2048 threads per SM, each at several chunk sizes
+  std::vector<KCfg> cand;
+  const int ths[3] = {64, 128, 256}, per_sm[4] = {256, 512, 1024, 2048}, chunks[3] = {1, 4, 16};
+  for (int t : ths) {
+    cand.push_back(KCfg{t, 0, 1, ctx->nsm});
+    for (int ps : per_sm)
+      for (int ch : chunks)
+        if (ps >= t) cand.push_back(KCfg{t, ps / t, ch, ctx->nsm});
+  }
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  int rc = FB_OK;
+  for (int k = 0; k < TK_N && rc == FB_OK; k++) {
+    if (!tune[k]) continue;
+    float best = 3.0e38f;
+    KCfg bestc = ctx->cfg[k];
+    for (const KCfg &c : cand) {
+      int e = tune_launch(ctx, k, c, what);  // warm-up
+      for (int r = 0; r < reps && !e; r++) {
+        if (r == 0) cudaEventRecord(e0, ctx->stream);
+        e = tune_launch(ctx, k, c, what);
+      }
+      if (e) {
+        rc = fail(ctx, FB_ERR_CUDA, "autotune %s: %s", tk_names[k], cudaGetErrorString((cudaError_t)e));
+        break;
+      }
+      cudaEventRecord(e1, ctx->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = fail(ctx, FB_ERR_CUDA, "autotune %s: synchronize", tk_names[k]);
+        break;
+      }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ctx->launches += reps + 1;
+      if (ms < best) {
+        best = ms;
+        bestc = c;
+      }
+    }
+    ctx->cfg[k] = bestc;
+    if (best_ms) best_ms[k] = best / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // the timed launches accumulated into the outputs: they must be recomputed
+  ctx->assembled = ctx->dassembled = 0;
+  ctx->have_vna2c = ctx->have_dblocks = false;
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (rc) return rc;
   return FB_OK;
 }
 

@@ -109,14 +109,13 @@ __device__ void atom_2c(const Ctx2c &c, int i, int lane, unsigned what) {
 }
 
 template <bool HASD>
-__global__ void __launch_bounds__(128) k_assemble_2c(Ctx2c c, unsigned what) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= c.N) return;
-  int pa = c.fd->sp[c.isp[warp]].pattern;
-  if (pa == PAT_SP) atom_2c<PAT_SP, HASD>(c, warp, lane, what);
-  else if (pa == PAT_S) atom_2c<PAT_S, HASD>(c, warp, lane, what);
-  else if constexpr (HASD) atom_2c<PAT_SPD, HASD>(c, warp, lane, what);
+__global__ void __launch_bounds__(256) k_assemble_2c(Ctx2c c, unsigned what, Sched q) {
+  for_each_warp_item(c.N, q, [&](int i, int lane) {
+    int pa = c.fd->sp[c.isp[i]].pattern;
+    if (pa == PAT_SP) atom_2c<PAT_SP, HASD>(c, i, lane, what);
+    else if (pa == PAT_S) atom_2c<PAT_S, HASD>(c, i, lane, what);
+    else if constexpr (HASD) atom_2c<PAT_SPD, HASD>(c, i, lane, what);
+  });
 }
 
 // build_forces, assembly terms (c.SYSTEM/M_build_forces.f90:172-588).  The
@@ -155,9 +154,12 @@ __global__ void k_build_forces(int N, const int *__restrict__ pair_off, const in
 
 int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   Ctx2c c = make2c(a);
-  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
-  if (a.have_d) k_assemble_2c<true><<<blocks, threads, 0, s>>>(c, what);
-  else k_assemble_2c<false><<<blocks, threads, 0, s>>>(c, what);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_a2c, (long long)a.N * 32, a.queue ? a.queue + 0 : nullptr, s, grid, block, q);
+  if (e) return e;
+  if (a.have_d) k_assemble_2c<true><<<grid, block, 0, s>>>(c, what, q);
+  else k_assemble_2c<false><<<grid, block, 0, s>>>(c, what, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

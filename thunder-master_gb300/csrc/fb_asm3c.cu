@@ -28,34 +28,37 @@ __device__ __forceinline__ void trip_3c(const Ctx3c &c, int t) {
 }
 
 template <bool HASD>
-__global__ void __launch_bounds__(128) k_assemble_3c(Ctx3c c) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= c.T) return;
-  if (c.tperm) t = c.tperm[t];
-  int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
-  int key = pa * 3 + pb;
-  switch (key) {
-    case PAT_SP * 3 + PAT_SP: trip_3c<PAT_SP, PAT_SP, HASD>(c, t); break;
-    case PAT_SP * 3 + PAT_S: trip_3c<PAT_SP, PAT_S, HASD>(c, t); break;
-    case PAT_S * 3 + PAT_SP: trip_3c<PAT_S, PAT_SP, HASD>(c, t); break;
-    case PAT_S * 3 + PAT_S: trip_3c<PAT_S, PAT_S, HASD>(c, t); break;
-    default:
-      if constexpr (HASD) {
-        if (key == PAT_SPD * 3 + PAT_SPD) trip_3c<PAT_SPD, PAT_SPD, HASD>(c, t);
-        else if (key == PAT_SPD * 3 + PAT_SP) trip_3c<PAT_SPD, PAT_SP, HASD>(c, t);
-        else if (key == PAT_SP * 3 + PAT_SPD) trip_3c<PAT_SP, PAT_SPD, HASD>(c, t);
-        else if (key == PAT_SPD * 3 + PAT_S) trip_3c<PAT_SPD, PAT_S, HASD>(c, t);
-        else if (key == PAT_S * 3 + PAT_SPD) trip_3c<PAT_S, PAT_SPD, HASD>(c, t);
-      }
-  }
+__global__ void __launch_bounds__(256) k_assemble_3c(Ctx3c c, Sched q) {
+  for_each_item(c.T, q, [&](int t) {
+    if (c.tperm) t = c.tperm[t];
+    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+    int key = pa * 3 + pb;
+    switch (key) {
+      case PAT_SP * 3 + PAT_SP: trip_3c<PAT_SP, PAT_SP, HASD>(c, t); break;
+      case PAT_SP * 3 + PAT_S: trip_3c<PAT_SP, PAT_S, HASD>(c, t); break;
+      case PAT_S * 3 + PAT_SP: trip_3c<PAT_S, PAT_SP, HASD>(c, t); break;
+      case PAT_S * 3 + PAT_S: trip_3c<PAT_S, PAT_S, HASD>(c, t); break;
+      default:
+        if constexpr (HASD) {
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_3c<PAT_SPD, PAT_SPD, HASD>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_3c<PAT_SPD, PAT_SP, HASD>(c, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_3c<PAT_SP, PAT_SPD, HASD>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_3c<PAT_SPD, PAT_S, HASD>(c, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_3c<PAT_S, PAT_SPD, HASD>(c, t);
+        }
+    }
+  });
 }
 
 int launch_assemble_3c(const AsmArgs &a, cudaStream_t s) {
   if (a.ntrip == 0) return 0;
   Ctx3c c = make3c(a);
-  int threads = 128, blocks = (a.ntrip + threads - 1) / threads;
-  if (a.have_d) k_assemble_3c<true><<<blocks, threads, 0, s>>>(c);
-  else k_assemble_3c<false><<<blocks, threads, 0, s>>>(c);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_a3c, (long long)a.ntrip, a.queue ? a.queue + 1 : nullptr, s, grid, block, q);
+  if (e) return e;
+  if (a.have_d) k_assemble_3c<true><<<grid, block, 0, s>>>(c, q);
+  else k_assemble_3c<false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -5,6 +5,7 @@
 #include "fb_device.cuh"
 #include "fb_df.cuh"
 #include "fb_launch.h"
+#include "fb_sched.cuh"
 
 namespace fb {
 
@@ -23,6 +24,7 @@ namespace fb {
 struct Ctx2c {
   int N;
   const double *ratom;
+  const int *sid;
   const int *isp;
   const FdataDev *fd;
   const double *table2c;
@@ -36,10 +38,11 @@ struct Ctx2c {
 __device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
                                           double e[3][3]) {
   int j = c.neigh_j[p], mb = c.neigh_b[p];
+  const double *xl = c.xl + (long long)c.sid[i] * XL_STRIDE;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     r1[k] = c.ratom[3 * i + k];
-    r2[k] = __dadd_rn(c.ratom[3 * j + k], c.xl[3 * mb + k]);
+    r2[k] = __dadd_rn(c.ratom[3 * j + k], xl[3 * mb + k]);
   }
   z = dist_rn(r1, r2);
   double sig[3];
@@ -80,6 +83,7 @@ __device__ __forceinline__ bool same_grid(const Cell2cDev &a, const Cell2cDev &b
 struct Ctx3c {
   int N, T;
   const double *ratom;
+  const int *sid;
   const int *isp;
   const FdataDev *fd;
   const double *table3c;
@@ -109,11 +113,12 @@ __device__ __forceinline__ void trip_geom(const Ctx3c &c, int t, int &ia, int &i
   iat = c.ci_j[t];
   jat = c.cj_j[t];
   int ib = c.ci_b[t], jb = c.cj_b[t];
+  const double *xl = c.xl + (long long)c.sid[ia] * XL_STRIDE;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     g.rna[k] = c.ratom[3 * ia + k];
-    g.r1[k] = __dadd_rn(c.ratom[3 * iat + k], c.xl[3 * ib + k]);
-    g.r2[k] = __dadd_rn(c.ratom[3 * jat + k], c.xl[3 * jb + k]);
+    g.r1[k] = __dadd_rn(c.ratom[3 * iat + k], xl[3 * ib + k]);
+    g.r2[k] = __dadd_rn(c.ratom[3 * jat + k], xl[3 * jb + k]);
     g.r21[k] = __dsub_rn(g.r2[k], g.r1[k]);
   }
   g.z = dist_rn(g.r1, g.r2);
@@ -326,6 +331,7 @@ inline Ctx2c make2c(const AsmArgs &a) {
   Ctx2c c;
   c.N = a.N;
   c.ratom = a.ratom;
+  c.sid = a.sid;
   c.isp = a.isp;
   c.fd = a.fd;
   c.table2c = a.table2c;
@@ -348,6 +354,7 @@ inline Ctx3c make3c(const AsmArgs &a) {
   c.N = a.N;
   c.T = a.ntrip;
   c.ratom = a.ratom;
+  c.sid = a.sid;
   c.isp = a.isp;
   c.fd = a.fd;
   c.table3c = a.table3c;

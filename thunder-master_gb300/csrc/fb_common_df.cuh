@@ -51,11 +51,12 @@ __device__ __forceinline__ void trip_geom_fp64(const Ctx3c &c, int t, GeomFP64 &
   h.iat = c.ci_j[t];
   h.jat = c.cj_j[t];
   int ib = c.ci_b[t], jb = c.cj_b[t];
+  const double *xl = c.xl + (long long)c.sid[h.ia] * XL_STRIDE;
   double r1[3], r2[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    r1[k] = __dadd_rn(c.ratom[3 * h.iat + k], c.xl[3 * ib + k]);
-    r2[k] = __dadd_rn(c.ratom[3 * h.jat + k], c.xl[3 * jb + k]);
+    r1[k] = __dadd_rn(c.ratom[3 * h.iat + k], xl[3 * ib + k]);
+    r2[k] = __dadd_rn(c.ratom[3 * h.jat + k], xl[3 * jb + k]);
     h.r21[k] = __dsub_rn(r2[k], r1[k]);
     h.rn[k] = __dsub_rn(c.ratom[3 * h.ia + k], __dadd_rn(r1[k], h.r21[k] * 0.5));
     h.v[k] = c.ratom[3 * h.ia + k] - r1[k];

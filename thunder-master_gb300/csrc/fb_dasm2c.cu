@@ -98,14 +98,13 @@ __device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
 }
 
 template <bool HASD>
-__global__ void __launch_bounds__(128) k_dassemble_2c(CtxD2c c, unsigned what) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= c.b.N) return;
-  int pa = c.b.fd->sp[c.b.isp[warp]].pattern;
-  if (pa == PAT_SP) atom_d2c<PAT_SP, HASD>(c, warp, lane, what);
-  else if (pa == PAT_S) atom_d2c<PAT_S, HASD>(c, warp, lane, what);
-  else if constexpr (HASD) atom_d2c<PAT_SPD, HASD>(c, warp, lane, what);
+__global__ void __launch_bounds__(256) k_dassemble_2c(CtxD2c c, unsigned what, Sched q) {
+  for_each_warp_item(c.b.N, q, [&](int i, int lane) {
+    int pa = c.b.fd->sp[c.b.isp[i]].pattern;
+    if (pa == PAT_SP) atom_d2c<PAT_SP, HASD>(c, i, lane, what);
+    else if (pa == PAT_S) atom_d2c<PAT_S, HASD>(c, i, lane, what);
+    else if constexpr (HASD) atom_d2c<PAT_SPD, HASD>(c, i, lane, what);
+  });
 }
 
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
@@ -120,9 +119,12 @@ int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   c.ontop = a.ontop;
   c.atomf = a.atomf;
   c.keep = a.keep_dblocks;
-  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
-  if (a.have_d) k_dassemble_2c<true><<<blocks, threads, 0, s>>>(c, what);
-  else k_dassemble_2c<false><<<blocks, threads, 0, s>>>(c, what);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_d2c, (long long)a.N * 32, a.queue ? a.queue + 2 : nullptr, s, grid, block, q);
+  if (e) return e;
+  if (a.have_d) k_dassemble_2c<true><<<grid, block, 0, s>>>(c, what, q);
+  else k_dassemble_2c<false><<<grid, block, 0, s>>>(c, what, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

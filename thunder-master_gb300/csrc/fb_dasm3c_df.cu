@@ -193,25 +193,28 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t) {
   }
 }
 
-__global__ void __launch_bounds__(128) k_dassemble_3c_df(Ctx3c c) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= c.T) return;
-  if (c.tperm) t = c.tperm[t];
-  int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
-  switch (pa * 3 + pb) {
-    case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP>(c, t); break;
-    case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S>(c, t); break;
-    case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP>(c, t); break;
-    case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S>(c, t); break;
-    default: break;
-  }
+__global__ void __launch_bounds__(256) k_dassemble_3c_df(Ctx3c c, Sched q) {
+  for_each_item(c.T, q, [&](int t) {
+    if (c.tperm) t = c.tperm[t];
+    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+    switch (pa * 3 + pb) {
+      case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP>(c, t); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S>(c, t); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP>(c, t); break;
+      case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S>(c, t); break;
+      default: break;
+    }
+  });
 }
 
 int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s) {
   if (a.ntrip == 0) return 0;
   Ctx3c c = make3c(a);
-  int threads = 128, blocks = (a.ntrip + threads - 1) / threads;
-  k_dassemble_3c_df<<<blocks, threads, 0, s>>>(c);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
+  if (e) return e;
+  k_dassemble_3c_df<<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

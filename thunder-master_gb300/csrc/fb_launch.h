@@ -1,16 +1,35 @@
-// fb_launch.h -- kernel launchers of libfbgpu (host side of fb_kernels.cu).
+// fb_launch.h -- kernel launchers of libfbgpu and their argument blocks.
 #pragma once
 #include <cuda_runtime.h>
 #include "fb_internal.h"
 
 namespace fb {
 
+// Launch shape of one kernel: threads per CTA; ctas_per_sm > 0 selects the
+// persistent form (nsm * ctas_per_sm CTAs whose warps take `chunk` task
+// groups per grab from a device counter), 0 a grid that covers the work.
+struct KCfg {
+  int threads, ctas_per_sm, chunk, nsm;
+};
+// device side of a launch: the work counter (null: grid covers the work)
+struct Sched {
+  int *ctr;
+  int chunk;
+};
+
+// A batch of structures is one concatenated system: atoms of structure s
+// are satom_off[s] .. satom_off[s+1]-1, sid[atom] = s, and structure s owns
+// XL_STRIDE doubles of image vectors at xl + s * XL_STRIDE.
 struct NeighArgs {
-  int N, P, nimg;
+  int N, P;
   const double *ratom;
-  const float4 *pos4;  // x, y, z, float cutoff of the atom's species
-  float4 bbox_lo, bbox_hi;  // bounding box of the positions; bbox_lo.w = largest cutoff
-  int periodic;
+  const float4 *pos4;     // x, y, z, float cutoff of the atom's species
+  const int *sid;         // structure of each atom
+  const int *satom_off;   // first atom of each structure (+ end)
+  const int *simg_off;    // images of structure s: imgs[simg_off[s] .. simg_off[s+1]-1]
+  const float4 *sbbox;    // bounding box (lo, hi) of each structure's positions
+  const int *speriodic;   // 1 for a periodic structure, 0 for a cluster
+  float rcmax;            // largest species cutoff
   const int *isp;
   const FdataDev *fd;
   const double *xl;
@@ -36,6 +55,7 @@ struct NeighArgs {
 struct AsmArgs {
   int N, ntrip, have_d;
   const double *ratom;
+  const int *sid;  // structure of each atom (image vectors at xl + sid * XL_STRIDE)
   const int *isp;
   const FdataDev *fd;
   const double *table2c, *table3c, *gxy;
@@ -55,6 +75,9 @@ struct AsmArgs {
   unsigned *status;
   const float2 *table3c_df;  // hi, lo float pairs of table3c
   float2 *rho_df;            // hi, lo float pairs of rho
+  // launch shapes (autotuned) and the work counters of persistent launches
+  KCfg cfg_a2c, cfg_a3c, cfg_d2c, cfg_d3c;
+  int *queue;  // 4 counters: assemble_2c, assemble_3c, dassemble_2c, dassemble_3c
 };
 
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s);

@@ -8,44 +8,52 @@ namespace fb {
 // ===========================================================================
 // One warp per atom i; lanes sweep jatom inside each periodic image, images
 // in increasing mbeta, so hits come out in the reference order (mbeta
-// outer, jatom inner).  A float prefilter with a 1e-2 A margin discards far
-// pairs; every candidate is decided by the uncontracted FP64 test of the
-// reference: z = distance(r1, r2) < rc_i + rc_j - 0.01.
+// outer, jatom inner).  In a batch, j runs over the atoms of i's own
+// structure and the images are that structure's.  A float prefilter with a
+// 1e-2 A margin discards far pairs; every candidate is decided by the
+// uncontracted FP64 test of the reference:
+// z = distance(r1, r2) < rc_i + rc_j - 0.01.
 template <bool FILL>
 __global__ void k_neigh(int N, const double *__restrict__ ratom, const float4 *__restrict__ pos4,
-                        const int *__restrict__ isp, const FdataDev *__restrict__ fd, const double *__restrict__ xl,
-                        const float *__restrict__ xlf, const int *__restrict__ imgs, int nimg, float4 bbox_lo,
-                        float4 bbox_hi, int *__restrict__ cnt, long long *__restrict__ bsum,
-                        const int *__restrict__ pair_off, const long long *__restrict__ blk_base,
-                        int *__restrict__ neigh_j, int *__restrict__ neigh_b, int *__restrict__ neigh_self,
-                        int *__restrict__ pair_owner, long long *__restrict__ blk_off,
+                        const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
+                        const int *__restrict__ satom_off, const int *__restrict__ simg_off,
+                        const float4 *__restrict__ sbbox, float rcmax, const double *__restrict__ xl,
+                        const float *__restrict__ xlf, const int *__restrict__ imgs, int *__restrict__ cnt,
+                        long long *__restrict__ bsum, const int *__restrict__ pair_off,
+                        const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
+                        int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
                         unsigned *__restrict__ status, int *__restrict__ errinfo) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
   int i = warp;
+  int s = sid[i];
+  int a0 = satom_off[s], a1 = satom_off[s + 1];
+  const double *X = xl + (long long)s * XL_STRIDE;
+  const float *Xf = xlf + (long long)s * XL_STRIDE;
+  float4 bbox_lo = sbbox[2 * s], bbox_hi = sbbox[2 * s + 1];
   double ri[3] = {ratom[3 * i], ratom[3 * i + 1], ratom[3 * i + 2]};
   float4 pi = pos4[i];  // (x, y, z, float cutoff of species)
   double rci = fd->sp[isp[i]].rcA;
   // float reach of atom i: its cutoff + the largest cutoff + margin
-  float reach = pi.w + bbox_lo.w + 1.0e-2f;
+  float reach = pi.w + rcmax + 1.0e-2f;
   int num = 0, base = FILL ? pair_off[i] : 0;
   long long norbsum = 0;  // sum of norb_j over the hits so far
   long long bbase = FILL ? blk_base[i] : 0;
   int ni = fd->sp[isp[i]].norb;
-  for (int ii = 0; ii < nimg; ii++) {
+  for (int ii = simg_off[s]; ii < simg_off[s + 1]; ii++) {
     int mb = imgs[ii];
-    float L0 = xlf[3 * mb], L1 = xlf[3 * mb + 1], L2 = xlf[3 * mb + 2];
+    float L0 = Xf[3 * mb], L1 = Xf[3 * mb + 1], L2 = Xf[3 * mb + 2];
     // skip an image whose shifted bounding box lies beyond reach (warp-uniform)
     float ox = fmaxf(fmaxf(bbox_lo.x + L0 - pi.x, pi.x - (bbox_hi.x + L0)), 0.0f);
     float oy = fmaxf(fmaxf(bbox_lo.y + L1 - pi.y, pi.y - (bbox_hi.y + L1)), 0.0f);
     float oz = fmaxf(fmaxf(bbox_lo.z + L2 - pi.z, pi.z - (bbox_hi.z + L2)), 0.0f);
     if (ox * ox + oy * oy + oz * oz > reach * reach) continue;
-    double X0 = xl[3 * mb], X1 = xl[3 * mb + 1], X2 = xl[3 * mb + 2];
-    for (int j0 = 0; j0 < N; j0 += 32) {
+    double X0 = X[3 * mb], X1 = X[3 * mb + 1], X2 = X[3 * mb + 2];
+    for (int j0 = a0; j0 < a1; j0 += 32) {
       int j = j0 + lane;
       bool hit = false;
-      if (j < N) {
+      if (j < a1) {
         float4 pj = pos4[j];
         float d0 = (pj.x + L0) - pi.x, d1 = (pj.y + L1) - pi.y, d2 = (pj.z + L2) - pi.z;
         float lim = pi.w + pj.w + 1.0e-2f;
@@ -101,12 +109,14 @@ __global__ void k_neigh(int N, const double *__restrict__ ratom, const float4 *_
 // (:776-779); one thread per pair.
 __global__ void k_neigh_back(int N, int P, const int *__restrict__ pair_owner, const int *__restrict__ pair_off,
                              const int *__restrict__ neigh_j, const int *__restrict__ neigh_b,
-                             const double *__restrict__ xl, const double *__restrict__ ratom,
+                             const int *__restrict__ sid, const double *__restrict__ xl0,
+                             const double *__restrict__ ratom,
                              int *__restrict__ neigh_back, double *__restrict__ r3v,
                              unsigned *__restrict__ status) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   int i = pair_owner[p], j = neigh_j[p], mb = neigh_b[p];
+  const double *xl = xl0 + (long long)sid[i] * XL_STRIDE;
   int found = -999, nfound = 0;
   for (int q = pair_off[j]; q < pair_off[j + 1]; q++) {
     int k = neigh_j[q], jb = neigh_b[q];
@@ -158,8 +168,9 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
 // is absent or fails the test, the full scan of the reference decides.
 // Output order matches the reference loops.
 template <bool FILL>
-__global__ void k_common(int N, int periodic, const double *__restrict__ ratom, const int *__restrict__ isp,
-                         const FdataDev *__restrict__ fd, const double *__restrict__ xl,
+__global__ void k_common(int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
+                         const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
+                         const double *__restrict__ xl0,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                          const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
                          const double *__restrict__ r3v, int *__restrict__ tcnt, const int *__restrict__ trip_off,
@@ -170,6 +181,8 @@ __global__ void k_common(int N, int periodic, const double *__restrict__ ratom, 
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
   int ia = warp;
+  const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
+  int periodic = speriodic[sid[ia]];
   int p0 = pair_off[ia], n = pair_off[ia + 1] - p0, self = neigh_self[ia];
   int num = 0, base = FILL ? trip_off[ia] : 0;
   for (int in = 0; in < n; in++) {
@@ -258,13 +271,15 @@ __global__ void k_common(int N, int periodic, const double *__restrict__ ratom, 
 // (M_Fdata_3c.f90:367-376); it only orders the work.
 // ---------------------------------------------------------------------------
 __global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__ ratom, const int *__restrict__ isp,
-                           const FdataDev *__restrict__ fd, const double *__restrict__ xl,
+                           const FdataDev *__restrict__ fd, const int *__restrict__ sid,
+                           const double *__restrict__ xl0,
                            const int *__restrict__ talpha, const int *__restrict__ ci_j, const int *__restrict__ ci_b,
                            const int *__restrict__ cj_j, const int *__restrict__ cj_b, int *__restrict__ key,
                            int *__restrict__ rank, int *__restrict__ hist) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int ia = talpha[t], i = ci_j[t], j = cj_j[t], ib = ci_b[t], jb = cj_b[t];
+  const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
   double r1[3], r2[3], rn[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -324,7 +339,7 @@ int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, in
   cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
   int threads = 256, blocks = (T + threads - 1) / threads;
-  k_trip_key<<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.isp, a.fd, a.xl, a.talpha, a.ci_j, a.ci_b,
+  k_trip_key<<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.isp, a.fd, a.sid, a.xl, a.talpha, a.ci_j, a.ci_b,
                                         a.cj_j, a.cj_b, key, rank, hist);
   FB_LAUNCH_CHECK();
   k_scan_bins<<<1, 1024, 0, s>>>(nbins, hist);
@@ -337,13 +352,15 @@ int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, in
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   if (fill)
-    k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                             a.bbox_lo, a.bbox_hi, nullptr, nullptr, a.pair_off, a.blk_base,
+    k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
+                                             a.sbbox, a.rcmax, a.xl, a.xlf, a.imgs, nullptr, nullptr, a.pair_off,
+                                             a.blk_base,
                                              a.neigh_j, a.neigh_b, a.neigh_self, a.pair_owner_w, a.blk_off_w,
                                              a.status, a.errinfo);
   else
-    k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.xl, a.xlf, a.imgs, a.nimg,
-                                              a.bbox_lo, a.bbox_hi, a.cnt, a.bsum, nullptr, nullptr, nullptr,
+    k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
+                                              a.sbbox, a.rcmax, a.xl, a.xlf, a.imgs, a.cnt, a.bsum, nullptr, nullptr,
+                                              nullptr,
                                               nullptr, nullptr, nullptr, nullptr, a.status, a.errinfo);
   FB_LAUNCH_CHECK();
   return 0;
@@ -352,8 +369,8 @@ int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
 int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
   if (a.P == 0) return 0;
   int threads = 256, blocks = (a.P + threads - 1) / threads;
-  k_neigh_back<<<blocks, threads, 0, s>>>(a.N, a.P, a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.xl, a.ratom,
-                                          a.neigh_back, a.r3v, a.status);
+  k_neigh_back<<<blocks, threads, 0, s>>>(a.N, a.P, a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.sid, a.xl,
+                                          a.ratom, a.neigh_back, a.r3v, a.status);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -361,11 +378,11 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
 int launch_common(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   if (fill)
-    k_common<true><<<blocks, threads, 0, s>>>(a.N, a.periodic, a.ratom, a.isp, a.fd, a.xl, a.pair_off, a.neigh_j,
+    k_common<true><<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off, a.neigh_j,
                                               a.neigh_b, a.neigh_self, a.r3v, nullptr, a.trip_off, a.ci_j, a.ci_b,
                                               a.cj_j, a.cj_b, a.cneigh, a.tdst, a.talpha);
   else
-    k_common<false><<<blocks, threads, 0, s>>>(a.N, a.periodic, a.ratom, a.isp, a.fd, a.xl, a.pair_off,
+    k_common<false><<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off,
                                                a.neigh_j, a.neigh_b, a.neigh_self, a.r3v, a.tcnt, nullptr,
                                                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   FB_LAUNCH_CHECK();

@@ -11,6 +11,7 @@ Context.read_Fdata     read_info + read_Fdata_2c + read_Fdata_3c      c.SYSTEM/M
                                                                       e.FDATA/M_Fdata_2c.f90:149,
                                                                       e.FDATA/M_Fdata_3c.f90:143
 Context.set_structure  read_positions + make_cells                    c.SYSTEM/make_cells.f90:51
+Context.set_batch      (no counterpart) many structures, one system   --
 Context.driver_neighbors  driver_neighbors                            c.SYSTEM/M_neighbors.f90:93
 Context.assemble_S     assemble_S                                     j.ASSEMBLERS/M_assemble_2c_Harris.f90:89
 Context.assemble_T     assemble_T                                     j.ASSEMBLERS/M_assemble_2c_Harris.f90:233
@@ -33,7 +34,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
-FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS = 1, 2, 4, 8, 15, 16
+FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
+TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
 BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8}
@@ -55,7 +57,13 @@ _SIGS = {
     "fb_load_fdata": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, _ip]),
     "fb_species_norb": (C.c_int, [C.c_void_p, C.c_int]),
     "fb_set_structure": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip, _dp, C.c_int]),
+    "fb_set_batch": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_void_p, C.c_void_p]),
+    "fb_get_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_update_positions": (C.c_int, [C.c_void_p, _dp]),
+    "fb_assemble_graph": (C.c_int, [C.c_void_p, C.c_uint]),
+    "fb_set_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
+    "fb_get_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_autotune": (C.c_int, [C.c_void_p, C.c_uint, C.c_int, C.c_void_p]),
     "fb_neighbors": (C.c_int, [C.c_void_p]),
     "fb_set_neighbors": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
     "fb_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
@@ -166,6 +174,34 @@ class Context:
         self._check(self.L.fb_set_structure(self.h, len(im), r, im, lat, int(icluster)))
         self.natoms = len(im)
         self.imass = im.copy()
+        self.nstruct = 1
+
+    def set_batch(self, structures):
+        """Many independent structures assembled together.  ``structures`` is
+        a list of (ratom (n, 3), imass (n,), lattice (3, 3) or None,
+        icluster) tuples; later calls act on the whole batch and
+        ``batch_offsets`` slices their results per structure."""
+        nat = np.array([len(st[1]) for st in structures], np.int32)
+        r = np.ascontiguousarray(np.concatenate([np.asarray(st[0], np.float64).reshape(-1, 3)
+                                                 for st in structures]).reshape(-1))
+        im = np.ascontiguousarray(np.concatenate([np.asarray(st[1], np.int32) for st in structures]))
+        lat = np.ascontiguousarray(np.concatenate([
+            np.asarray(st[2] if st[2] is not None else np.eye(3), np.float64).reshape(-1)
+            for st in structures]))
+        icl = np.array([int(st[3]) if len(st) > 3 else 0 for st in structures], np.int32)
+        self._check(self.L.fb_set_batch(self.h, len(nat), nat, r, im, _ptr(lat), _ptr(icl)))
+        self.natoms = len(im)
+        self.imass = im.copy()
+        self.nstruct = len(nat)
+
+    def batch_offsets(self):
+        """Per-structure offsets (nstruct + 1 each): atoms, pairs, triplets,
+        block elements."""
+        n = getattr(self, "nstruct", 1) + 1
+        a, p, t = (np.zeros(n, np.int32) for _ in range(3))
+        b = np.zeros(n, np.int64)
+        self._check(self.L.fb_get_batch(self.h, _ptr(a), _ptr(p), _ptr(t), _ptr(b)))
+        return dict(atom=a, pair=p, trip=t, block=b)
 
     def update_positions(self, ratom):
         self._check(self.L.fb_update_positions(self.h, np.ascontiguousarray(ratom, np.float64).reshape(-1)))
@@ -223,6 +259,27 @@ class Context:
 
     def assemble_vna_3c(self):
         self.assemble(FB_VNA3C)
+
+    def assemble_graph(self, what=FB_ALL | FB_FORCES):
+        """Value pass (+ force pass with FB_FORCES) as one CUDA graph launch,
+        captured once and replayed while the system stays the same."""
+        self._check(self.L.fb_assemble_graph(self.h, what))
+
+    def set_launch(self, kernel, threads, ctas_per_sm=0, chunk=1):
+        self._check(self.L.fb_set_launch(self.h, kernel.encode(), threads, ctas_per_sm, chunk))
+
+    def get_launch(self, kernel):
+        t, c, k = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.fb_get_launch(self.h, kernel.encode(), C.byref(t), C.byref(c), C.byref(k)))
+        return dict(threads=t.value, ctas_per_sm=c.value, chunk=k.value)
+
+    def autotune(self, what=FB_ALL | FB_FORCES, reps=3):
+        """Pick the fastest launch shape of each selected kernel; returns
+        {kernel: (best ms per launch, shape)}.  Outputs must be recomputed
+        afterwards."""
+        best = np.zeros(4)
+        self._check(self.L.fb_autotune(self.h, what, reps, _ptr(best)))
+        return {k: (float(best[i]), self.get_launch(k)) for i, k in enumerate(TUNABLE) if best[i] > 0}
 
     def blocks(self, which):
         n = self.nblock * (3 if which in ("dS", "dT") else 1)
