@@ -237,6 +237,44 @@ int fb_get_launch(const fb_ctx *ctx, const char *kernel, int *threads,
  * reading them.  No reference counterpart. */
 int fb_autotune(fb_ctx *ctx, unsigned what, int reps, double *best_ms);
 
+/* ---- MLP-3c surrogate (no reference counterpart) ------------------------
+ * A network that stands in for the three-center table interpolation of the
+ * bcna integrals (getMEs_Fdata_3c, e.FDATA/M_Fdata_3c.f90:293-517): inputs
+ * (2x/xmax - 1, 2y/ymax - 1, cos theta) of a triplet plus a 16-float
+ * embedding of its species triple, three hidden layers of 128 with SiLU, 64
+ * outputs of which output (itheta-1)*10 + ime (itheta = 1..5, ime = 0..9) is
+ * the Legendre coefficient itheta of matrix element ime divided by its
+ * scale (fb_mlp_scales).  BF16 weights and tensor-core inputs, FP32
+ * accumulation.  Species triple index = (in1 * nspecies + in2) * nspecies +
+ * indna, all 0-based.  The parameter vector (FP32) is laid out as
+ * fb_mlp_layout describes: 10 offsets (embedding [ntriple][16], W1 [128][32],
+ * b1, W2 [128][128], b2, W3, b3, W4 [64][128], b4 [64], end); W1 columns
+ * 19..31 and W4 rows 50..63 are padding and stay zero. */
+int fb_mlp_init(fb_ctx *ctx, unsigned long long seed);
+long long fb_mlp_nparams(const fb_ctx *ctx);
+int fb_mlp_layout(const fb_ctx *ctx, long long *offsets);
+int fb_mlp_get_params(fb_ctx *ctx, float *out);
+/* per-triple output scales, [ntriple][64] floats */
+int fb_mlp_scales(fb_ctx *ctx, float *out);
+/* Adam training on the GPU: nsamples points drawn uniformly over the table
+ * domains (x in [0, xmax], y in [0, ymax], cos theta in [-1, 1], a species
+ * triple with a table) and labelled by the FP64 table interpolator; `epochs`
+ * passes in batches of `batch` (a multiple of 64), learning rate lr with
+ * cosine decay; mean loss of each epoch into loss_per_epoch (may be NULL). */
+int fb_mlp_train(fb_ctx *ctx, long long nsamples, int epochs, int batch,
+                 double lr, unsigned long long seed, double *loss_per_epoch);
+/* n training points as the trainer draws them: feat3 [n][3], triple [n],
+ * normalized targets [n][64] */
+int fb_mlp_samples(fb_ctx *ctx, int n, unsigned long long seed, float *feat3,
+                   int *triple, float *target);
+/* loss and gradient (FP32, the parameter layout) of one batch of n rows (a
+ * multiple of 64): loss = sum (out - target)^2 / (50 n) over used outputs */
+int fb_mlp_grad(fb_ctx *ctx, int n, const float *feat3, const int *triple,
+                const float *target, float *grad, double *loss);
+/* forward pass of n rows (a multiple of 64): normalized outputs [n][64] */
+int fb_mlp_forward(fb_ctx *ctx, int n, const float *feat3, const int *triple,
+                   float *out);
+
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions
  * run in double-float arithmetic on the FP32 pipe (two floats per value,

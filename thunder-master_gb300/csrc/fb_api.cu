@@ -14,8 +14,14 @@
 #include "../../include/fbgpu.h"
 #include "fb_fdata.h"
 #include "fb_launch.h"
+#include "fb_devbuf.h"
+#include "fb_mlp.h"
 
 using namespace fb;
+
+namespace fb {
+std::atomic<long long> g_alloc_gen{0};
+}
 
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
@@ -26,40 +32,6 @@ static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", 
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
-
-namespace {
-
-// bumped by every device (re)allocation: a captured CUDA graph whose
-// pointers may have moved is re-captured
-std::atomic<long long> g_alloc_gen{0};
-
-// device buffer that grows on demand and never shrinks
-struct DevBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-  int ensure(size_t bytes) {
-    if (bytes <= cap) return 0;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(bytes, 256);
-    if (cudaMalloc(&p, want) != cudaSuccess) return FB_ERR_CUDA;
-    cap = want;
-    g_alloc_gen++;
-    return 0;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T *as() const {
-    return static_cast<T *>(p);
-  }
-};
-
-}  // namespace
 
 struct fb_ctx {
   int device = 0;
@@ -112,6 +84,8 @@ struct fb_ctx {
   long long g_nblock = -1, g_alloc = -1, g_launches = 0;
   cudaStream_t g_stream = nullptr;
   KCfg g_cfg[TK_N];
+  // MLP-3c surrogate
+  MlpState mlp;
   // per-kernel CUDA-event timing (fb_set_timing)
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evpool;
@@ -244,6 +218,11 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
+  DevBuf *mb[] = {&ctx->mlp.params, &ctx->mlp.grad, &ctx->mlp.adam_m, &ctx->mlp.adam_v, &ctx->mlp.wbf,
+                  &ctx->mlp.scale, &ctx->mlp.tmeta, &ctx->mlp.dX, &ctx->mlp.dXt, &ctx->mlp.dY, &ctx->mlp.dTrip,
+                  &ctx->mlp.Z, &ctx->mlp.H, &ctx->mlp.Ht, &ctx->mlp.O, &ctx->mlp.dO, &ctx->mlp.dOt,
+                  &ctx->mlp.dZ, &ctx->mlp.dZt, &ctx->mlp.dXg, &ctx->mlp.part};
+  for (DevBuf *b : mb) b->release();
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   for (auto &e : ctx->evpool) {
     cudaEventDestroy(e.first);
@@ -1317,3 +1296,95 @@ extern "C" int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev, const do
   if (st) return status_error(ctx, st);
   return FB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// MLP-3c surrogate (fb_mlp_*)
+// ---------------------------------------------------------------------------
+static MlpTables mlp_tables(fb_ctx *ctx) {
+  MlpTables t;
+  t.fd = ctx->d_fd.as<FdataDev>();
+  t.table3c = ctx->d_tab3.as<double>();
+  t.gxy = ctx->d_gxy.as<double>();
+  t.lin = ctx->d_lin.as<unsigned char>();
+  return t;
+}
+
+extern "C" {
+
+int fb_mlp_init(fb_ctx *ctx, unsigned long long seed) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_fdata) return fail(ctx, FB_ERR_STATE, "fb_load_fdata first");
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = mlp_init(ctx->mlp, ctx->fdh, seed, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+long long fb_mlp_nparams(const fb_ctx *ctx) { return ctx && ctx->mlp.ready ? ctx->mlp.nparams : 0; }
+
+int fb_mlp_layout(const fb_ctx *ctx, long long *offsets) {
+  if (!ctx || !offsets) return FB_ERR_ARG;
+  if (!ctx->mlp.ready) return FB_ERR_STATE;
+  const MlpState &m = ctx->mlp;
+  long long o[10] = {m.o_emb, m.o_w1, m.o_b1, m.o_w2, m.o_b2, m.o_w3, m.o_b3, m.o_w4, m.o_b4, m.nparams};
+  std::memcpy(offsets, o, sizeof o);
+  return FB_OK;
+}
+
+int fb_mlp_get_params(fb_ctx *ctx, float *out) {
+  if (!ctx || !out) return FB_ERR_ARG;
+  if (!ctx->mlp.ready) return fail(ctx, FB_ERR_STATE, "fb_mlp_init first");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemcpyAsync(out, ctx->mlp.params.p, ctx->mlp.nparams * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FB_OK;
+}
+
+int fb_mlp_scales(fb_ctx *ctx, float *out) {
+  if (!ctx || !out) return FB_ERR_ARG;
+  if (!ctx->mlp.ready) return fail(ctx, FB_ERR_STATE, "fb_mlp_init first");
+  std::memcpy(out, ctx->mlp.h_scale.data(), ctx->mlp.h_scale.size() * sizeof(float));
+  return FB_OK;
+}
+
+int fb_mlp_train(fb_ctx *ctx, long long nsamples, int epochs, int batch, double lr, unsigned long long seed,
+                 double *loss_per_epoch) {
+  if (!ctx) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = mlp_train(ctx->mlp, mlp_tables(ctx), nsamples, epochs, batch, lr, seed, loss_per_epoch, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  ctx->launches += (long long)epochs * (nsamples / std::max(batch, 1)) * 26;
+  return FB_OK;
+}
+
+int fb_mlp_samples(fb_ctx *ctx, int n, unsigned long long seed, float *feat3, int *triple, float *target) {
+  if (!ctx || n < 1 || !feat3 || !triple || !target) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = mlp_samples(ctx->mlp, mlp_tables(ctx), n, seed, feat3, triple, target, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+int fb_mlp_grad(fb_ctx *ctx, int n, const float *feat3, const int *triple, const float *target, float *grad,
+                double *loss) {
+  if (!ctx || !feat3 || !triple || !target || !grad || !loss) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = mlp_grad(ctx->mlp, n, feat3, triple, target, grad, loss, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+int fb_mlp_forward(fb_ctx *ctx, int n, const float *feat3, const int *triple, float *out) {
+  if (!ctx || !feat3 || !triple || !out) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int st = mlp_forward(ctx->mlp, n, feat3, triple, out, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+}  // extern "C"

@@ -60,6 +60,17 @@ _SIGS = {
     "fb_set_batch": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_void_p, C.c_void_p]),
     "fb_get_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_update_positions": (C.c_int, [C.c_void_p, _dp]),
+    "fb_mlp_init": (C.c_int, [C.c_void_p, C.c_ulonglong]),
+    "fb_mlp_nparams": (C.c_longlong, [C.c_void_p]),
+    "fb_mlp_layout": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fb_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fb_mlp_scales": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fb_mlp_train": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_double, C.c_ulonglong,
+                               C.c_void_p]),
+    "fb_mlp_samples": (C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_mlp_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p]),
+    "fb_mlp_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_assemble_graph": (C.c_int, [C.c_void_p, C.c_uint]),
     "fb_set_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "fb_get_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -280,6 +291,55 @@ class Context:
         best = np.zeros(4)
         self._check(self.L.fb_autotune(self.h, what, reps, _ptr(best)))
         return {k: (float(best[i]), self.get_launch(k)) for i, k in enumerate(TUNABLE) if best[i] > 0}
+
+    # ---- MLP-3c surrogate ------------------------------------------------------
+    def mlp_init(self, seed=1):
+        self._check(self.L.fb_mlp_init(self.h, seed))
+        off = np.zeros(10, np.int64)
+        self._check(self.L.fb_mlp_layout(self.h, _ptr(off)))
+        self.mlp_offsets = off
+        self.mlp_nparams = int(off[-1])
+        self.mlp_ntriple = (int(off[1]) - int(off[0])) // 16
+        return off
+
+    def mlp_params(self):
+        p = np.zeros(self.mlp_nparams, np.float32)
+        self._check(self.L.fb_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def mlp_scales(self):
+        s = np.zeros((self.mlp_ntriple, 64), np.float32)
+        self._check(self.L.fb_mlp_scales(self.h, _ptr(s)))
+        return s
+
+    def mlp_train(self, nsamples=1 << 22, epochs=20, batch=4096, lr=2e-3, seed=7):
+        hist = np.zeros(epochs)
+        self._check(self.L.fb_mlp_train(self.h, int(nsamples), int(epochs), int(batch), float(lr), int(seed),
+                                        _ptr(hist)))
+        return hist
+
+    def mlp_samples(self, n, seed=3):
+        f = np.zeros((n, 3), np.float32)
+        t = np.zeros(n, np.int32)
+        y = np.zeros((n, 64), np.float32)
+        self._check(self.L.fb_mlp_samples(self.h, int(n), int(seed), _ptr(f), _ptr(t), _ptr(y)))
+        return f, t, y
+
+    def mlp_grad(self, feat3, trip, target):
+        f = np.ascontiguousarray(feat3, np.float32)
+        t = np.ascontiguousarray(trip, np.int32)
+        y = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(self.mlp_nparams, np.float32)
+        loss = C.c_double()
+        self._check(self.L.fb_mlp_grad(self.h, len(t), _ptr(f), _ptr(t), _ptr(y), _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def mlp_forward(self, feat3, trip):
+        f = np.ascontiguousarray(feat3, np.float32)
+        t = np.ascontiguousarray(trip, np.int32)
+        out = np.zeros((len(t), 64), np.float32)
+        self._check(self.L.fb_mlp_forward(self.h, len(t), _ptr(f), _ptr(t), _ptr(out)))
+        return out
 
     def blocks(self, which):
         n = self.nblock * (3 if which in ("dS", "dT") else 1)
