@@ -274,6 +274,44 @@ int fb_mlp_grad(fb_ctx *ctx, int n, const float *feat3, const int *triple,
 /* forward pass of n rows (a multiple of 64): normalized outputs [n][64] */
 int fb_mlp_forward(fb_ctx *ctx, int n, const float *feat3, const int *triple,
                    float *out);
+/* Validation against the FP64 table interpolator, per interpolation bin
+ * (species triple x stencil node (ix, iy) of getMEs_Fdata_3c,
+ * M_Fdata_3c.f90:367-376): the largest |network - tables| of a
+ * Legendre-combined matrix element (table units, before the P_eq2 factor)
+ * over samples_per_bin random points of the bin's region and random cos
+ * theta.  max_err (may be NULL) receives the largest over all bins;
+ * fb_mlp_bin_errors copies the per-bin values (out may be NULL to query
+ * nbins). */
+int fb_mlp_validate(fb_ctx *ctx, int samples_per_bin, unsigned long long seed,
+                    double *max_err);
+int fb_mlp_bin_errors(fb_ctx *ctx, float *out, long long *nbins);
+/* Gate: a bin is given to the network only where its validated error keeps
+ * every assembled vna block element of the current neighbor maps within
+ * tol_ha Hartree in the worst case (all of a block's triplets erring the
+ * same way): per-triplet bound tau = tol_ha * P_Hartree / (P_eq2 * 3 * n),
+ * n the most triplets adding into one block.  Elsewhere the table path
+ * runs.  Sets FB_MLP_GATED; tau (table units) and coverage (fraction of the
+ * current triplets given to the network) may be NULL. */
+int fb_mlp_gate(fb_ctx *ctx, double tol_ha, double *tau, double *coverage);
+/* FB_MLP_OFF: tables only.  FB_MLP_GATED: approved bins through the
+ * network (fb_mlp_gate).  FB_MLP_ALL: every three-center triplet through
+ * the network, ungated (to measure the surrogate alone).  Applies to the
+ * value and force passes of fb_assemble, fb_dassemble and
+ * fb_assemble_graph; the network's results enter the same double-float
+ * rotation and density contraction as the table values. */
+#define FB_MLP_OFF 0
+#define FB_MLP_GATED 1
+#define FB_MLP_ALL 2
+int fb_mlp_set_mode(fb_ctx *ctx, int mode);
+/* The assembly's network evaluation at given points (n rows of pts =
+ * (x, y, cos theta), x the neutral-atom and y the bond-charge distance in
+ * Angstrom, and a species triple each): Legendre-combined matrix elements
+ * out[n][10] (before the sin(theta) factor of the mvalue = 1 elements), or
+ * with derivs out[n][4][10] = value, d/dcos, d/dx, d/dy. */
+int fb_mlp_eval_points(fb_ctx *ctx, int n, const float *pts, const int *triple,
+                       int derivs, float *out);
+/* triplets the network takes in the current mode, and all triplets */
+int fb_mlp_routed(const fb_ctx *ctx, int *n_mlp, int *n_total);
 
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions
@@ -295,7 +333,8 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * fb_get_timing returns the accumulated device time and launch count of one
  * kernel: "neigh_count", "neigh_fill", "neigh_back", "common_count",
  * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
- * "dassemble_3c", "build_forces", "trip_bins", "split_rho".  No reference counterpart (the reference
+ * "dassemble_3c", "build_forces", "trip_bins", "split_rho", "mlp_eval",
+ * "assemble_3c_mlp", "dassemble_3c_mlp".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,

@@ -11,6 +11,10 @@ GPU), so that the library's forward pass and gradients can be checked
 against it.  ``exact=True`` drops the roundings (float64 throughout) for
 finite-difference checks of the back-propagation itself.
 
+The three coordinates enter as a BF16 pair: their rounding in columns 0..2
+and the rounding of the remainder in columns 19..21, which share W1's
+columns 0..2.
+
 Parameter vector layout (float32): the 10 offsets of fb_mlp_layout --
 embedding [ntriple][16], W1 [128][32], b1 [128], W2 [128][128], b2,
 W3 [128][128], b3, W4 [64][128], b4 [64], end.
@@ -21,6 +25,7 @@ import numpy as np
 
 N_IN, N_EMB, N_H, N_OUT, N_ME, N_THETA = 32, 16, 128, 64, 10, 5
 N_USED = N_THETA * N_ME
+N_LO = 3 + N_EMB  # columns of the coordinates' low parts (weights tied to columns 0..2)
 
 
 def bf16(x):
@@ -74,10 +79,15 @@ def forward(P, feat3, trip, exact=False):
     X[:, :3] = feat3
     X[:, 3:3 + N_EMB] = P["emb"][trip]
     X = r(X)
+    if not exact:
+        X[:, N_LO:N_LO + 3] = bf16(np.asarray(feat3, np.float32) - X[:, :3].astype(np.float32))
     cache = {"X": X, "Z": [], "H": []}
     h = X
     for l in (1, 2, 3):
-        z = h @ r(P["W%d" % l]).T + P["b%d" % l]
+        W = np.array(P["W%d" % l], dtype=np.float64)
+        if l == 1:
+            W[:, N_LO:N_LO + 3] = W[:, :3]
+        z = h @ r(W).T + P["b%d" % l]
         h = r(silu(z))
         cache["Z"].append(z)
         cache["H"].append(h)
@@ -107,7 +117,11 @@ def loss_and_grad(P, feat3, trip, target, nme, exact=False):
         hin = c["X"] if l == 1 else H[l - 2]
         g["W%d" % l] = dz.T @ hin
         g["b%d" % l] = dz.sum(0)
-        gin, Win = dz, r(P["W%d" % l])
+        W = np.array(P["W%d" % l], dtype=np.float64)
+        if l == 1:
+            W[:, N_LO:N_LO + 3] = W[:, :3]
+        gin, Win = dz, r(W)
+    g["W1"][:, :3] += g["W1"][:, N_LO:N_LO + 3]
     g["W1"][:, 3 + N_EMB:] = 0.0
     dX = gin @ Win
     gemb = np.zeros_like(P["emb"])

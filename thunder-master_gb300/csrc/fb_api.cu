@@ -25,10 +25,11 @@ std::atomic<long long> g_alloc_gen{0};
 
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
-       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_N };
+       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
-                                     "build_forces", "trip_bins", "split_rho"};
+                                     "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
+                                     "dassemble_3c_mlp"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -80,12 +81,19 @@ struct fb_ctx {
   // maps of the same sizes reuse it).
   cudaGraphExec_t gexec = nullptr;
   unsigned g_what = 0;
-  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1;
+  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1;
   long long g_nblock = -1, g_alloc = -1, g_launches = 0;
   cudaStream_t g_stream = nullptr;
   KCfg g_cfg[TK_N];
-  // MLP-3c surrogate
+  // MLP-3c surrogate: mode, per-bin validation errors and approval, the
+  // number of triplets routed to the network (the first mlp_n of tperm)
   MlpState mlp;
+  int mlp_mode = FB_MLP_OFF;
+  int mlp_cells = 0;
+  std::vector<float> h_bin_err;
+  DevBuf d_binok, d_mlpF;
+  int mlp_n = 0;
+  double mlp_tau = 0.0;
   // per-kernel CUDA-event timing (fb_set_timing)
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evpool;
@@ -218,6 +226,8 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
+  ctx->d_binok.release();
+  ctx->d_mlpF.release();
   DevBuf *mb[] = {&ctx->mlp.params, &ctx->mlp.grad, &ctx->mlp.adam_m, &ctx->mlp.adam_v, &ctx->mlp.wbf,
                   &ctx->mlp.scale, &ctx->mlp.tmeta, &ctx->mlp.dX, &ctx->mlp.dXt, &ctx->mlp.dY, &ctx->mlp.dTrip,
                   &ctx->mlp.Z, &ctx->mlp.H, &ctx->mlp.Ht, &ctx->mlp.O, &ctx->mlp.dO, &ctx->mlp.dOt,
@@ -462,6 +472,42 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   return a;
 }
 
+// grid nodes of the largest 3c cell (the bin count per species triple)
+static int trip_cells(const fb_ctx *ctx) {
+  int nsp = ctx->fdh.nspecies, cells = 1;
+  for (int x = 0; x < nsp; x++)
+    for (int y = 0; y < nsp; y++)
+      for (int z = 0; z < nsp; z++) cells = std::max(cells, ctx->fdh.dev.c3[x][y][z].nx * ctx->fdh.dev.c3[x][y][z].ny);
+  return cells;
+}
+
+static bool mlp_routes(const fb_ctx *ctx) { return ctx->mlp.ready && ctx->mlp_mode != FB_MLP_OFF && !ctx->fdh.have_d; }
+
+// counting sort of the triplets by interpolation bin, approved MLP-3c bins
+// first; mlp_n = triplets the network takes
+static int bin_triplets(fb_ctx *ctx) {
+  int T = ctx->T, nsp = ctx->fdh.nspecies, cells = trip_cells(ctx);
+  size_t nbins = (size_t)nsp * nsp * nsp * cells;
+  size_t tb = (size_t)T * sizeof(int) + 4;
+  CHK(ctx->d_tkey.ensure(tb));
+  CHK(ctx->d_trank.ensure(tb));
+  CHK(ctx->d_tperm.ensure(tb));
+  CHK(ctx->d_thist.ensure(2 * nbins * sizeof(int)));
+  bool gated = mlp_routes(ctx) && ctx->mlp_mode == FB_MLP_GATED && ctx->d_binok.p;
+  NeighArgs a = neigh_args(ctx);
+  KL(KT_TRIP_BINS, launch_trip_bins(a, T, nsp, cells, gated ? ctx->d_binok.as<unsigned char>() : nullptr,
+                                    ctx->d_tkey.as<int>(), ctx->d_trank.as<int>(), ctx->d_thist.as<int>(),
+                                    ctx->d_tperm.as<int>(), ctx->stream));
+  ctx->mlp_n = 0;
+  if (mlp_routes(ctx) && ctx->mlp_mode == FB_MLP_ALL) ctx->mlp_n = T;
+  if (gated && T > 0) {
+    CU(cudaMemcpyAsync(&ctx->mlp_n, ctx->d_thist.as<int>() + nbins, sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return FB_OK;
+}
+
 // everything after the pair lists exist on the device: neigh_back, common
 // neighbors, block storage
 static int finish_neighbors(fb_ctx *ctx) {
@@ -498,21 +544,9 @@ static int finish_neighbors(fb_ctx *ctx) {
                      ctx->stream));
   a = neigh_args(ctx);
   KL(KT_COMMON_FILL, launch_common(a, true, ctx->stream));
+  ctx->mlp_cells = trip_cells(ctx);
   // triplet processing order, binned by (species triple, 3c grid cell)
-  {
-    int nsp = ctx->fdh.nspecies, cells = 1;
-    for (int x = 0; x < nsp; x++)
-      for (int y = 0; y < nsp; y++)
-        for (int z = 0; z < nsp; z++)
-          cells = std::max(cells, ctx->fdh.dev.c3[x][y][z].nx * ctx->fdh.dev.c3[x][y][z].ny);
-    size_t nbins = (size_t)nsp * nsp * nsp * cells;
-    CHK(ctx->d_tkey.ensure(tb));
-    CHK(ctx->d_trank.ensure(tb));
-    CHK(ctx->d_tperm.ensure(tb));
-    CHK(ctx->d_thist.ensure(nbins * sizeof(int)));
-    KL(KT_TRIP_BINS, launch_trip_bins(a, T, nsp, cells, ctx->d_tkey.as<int>(), ctx->d_trank.as<int>(),
-                                      ctx->d_thist.as<int>(), ctx->d_tperm.as<int>(), ctx->stream));
-  }
+  CHK(bin_triplets(ctx));
   // block storage
   size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
   CHK(ctx->d_S.ensure(bb));
@@ -778,14 +812,53 @@ int fb_set_precision(fb_ctx *ctx, int mode) {
   return FB_OK;
 }
 
+// MLP-3c evaluation arguments for the first mlp_n triplets of tperm
+static MlpEvalArgs mlp_eval_args(fb_ctx *ctx) {
+  MlpEvalArgs m{};
+  const MlpState &s = ctx->mlp;
+  m.n = ctx->mlp_n;
+  m.list = ctx->d_tperm.as<int>();
+  m.wbf = s.wbf.as<__nv_bfloat16>();
+  m.params = s.params.as<float>();
+  m.o_emb = s.o_emb;
+  m.o_b1 = s.o_b1;
+  m.o_b2 = s.o_b2;
+  m.o_b3 = s.o_b3;
+  m.o_b4 = s.o_b4;
+  m.scale = s.scale.as<float>();
+  m.nsp = s.nsp;
+  m.out = ctx->d_mlpF.as<float>();
+  m.pts = nullptr;
+  m.ptrip = nullptr;
+  return m;
+}
+
+static int prepare_mlp(fb_ctx *ctx, bool forces) {
+  if (mlp_routes(ctx) && ctx->mlp_n > 0)
+    CHK(ctx->d_mlpF.ensure((size_t)ctx->mlp_n * (forces ? 4 : 1) * MLP_ME_STRIDE * sizeof(float)));
+  return FB_OK;
+}
+
 // launches of the value pass (no synchronization)
 static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
   if (what & FB_VNA3C) {
-    if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(a, ctx->stream));
-    else KL(KT_ASM3C, launch_assemble_3c(a, ctx->stream));
+    // triplets of approved bins through the network, the rest through the tables
+    int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
+    AsmArgs at = a;
+    at.tperm = a.tperm + nm;
+    at.ntrip = a.ntrip - nm;
+    if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
+    else KL(KT_ASM3C, launch_assemble_3c(at, ctx->stream));
+    if (nm > 0) {
+      KL(KT_MLP_EVAL, launch_mlp_eval(mlp_eval_args(ctx), a, false, ctx->nsm, ctx->stream));
+      AsmArgs am = a;
+      am.ntrip = nm;
+      am.mlpF = ctx->d_mlpF.as<float>();
+      KL(KT_ASM3C_MLP, launch_assemble_3c_mlp(am, ctx->stream));
+    }
   }
   return FB_OK;
 }
@@ -801,6 +874,7 @@ int fb_assemble(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
   CHK(check_assemble(ctx, what));
   CU(cudaSetDevice(ctx->device));
+  if (what & FB_VNA3C) CHK(prepare_mlp(ctx, false));
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
   CHK(enqueue_assemble(ctx, what));
   unsigned st = 0;
@@ -894,7 +968,9 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
     CHK(ctx->d_dS.ensure(db));
     CHK(ctx->d_dT.ensure(db));
   }
-  if ((what & FB_VNA3C) && use_df(ctx)) CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
+  if ((what & FB_VNA3C) && (use_df(ctx) || mlp_routes(ctx)))
+    CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
+  if (what & FB_VNA3C) CHK(prepare_mlp(ctx, true));
   return FB_OK;
 }
 
@@ -914,11 +990,19 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
   if (what & FB_VNA3C) {
-    if (use_df(ctx)) {
-      KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
-      KL(KT_DASM3C, launch_dassemble_3c_df(a, ctx->stream));
-    } else {
-      KL(KT_DASM3C, launch_dassemble_3c(a, ctx->stream));
+    int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
+    AsmArgs at = a;
+    at.tperm = a.tperm + nm;
+    at.ntrip = a.ntrip - nm;
+    if (use_df(ctx) || nm > 0) KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
+    if (use_df(ctx)) KL(KT_DASM3C, launch_dassemble_3c_df(at, ctx->stream));
+    else KL(KT_DASM3C, launch_dassemble_3c(at, ctx->stream));
+    if (nm > 0) {
+      KL(KT_MLP_EVAL, launch_mlp_eval(mlp_eval_args(ctx), a, true, ctx->nsm, ctx->stream));
+      AsmArgs am = a;
+      am.ntrip = nm;
+      am.mlpF = ctx->d_mlpF.as<float>();
+      KL(KT_DASM3C_MLP, launch_dassemble_3c_mlp(am, ctx->stream));
     }
   }
   KL(KT_FORCES, launch_build_forces(a, what & FB_ALL, ctx->stream));
@@ -989,6 +1073,8 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   ctx->g_T = ctx->T;
   ctx->g_nblock = ctx->nblock;
   ctx->g_have_d = ctx->fdh.have_d;
+  ctx->g_mlp_n = ctx->mlp_n;
+  ctx->g_mlp_mode = ctx->mlp_mode;
   ctx->g_alloc = g_alloc_gen.load();
   ctx->g_stream = ctx->stream;
   for (int k = 0; k < TK_N; k++) ctx->g_cfg[k] = ctx->cfg[k];
@@ -1000,11 +1086,13 @@ int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   if (!(what & (FB_ALL | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
   CU(cudaSetDevice(ctx->device));
   if (what & FB_ALL) CHK(check_assemble(ctx, what));
+  if (what & FB_VNA3C) CHK(prepare_mlp(ctx, (what & FB_FORCES) != 0));
   if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what));
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_prec == ctx->prec && ctx->g_N == ctx->N &&
                ctx->g_P == ctx->P && ctx->g_T == ctx->T && ctx->g_nblock == ctx->nblock &&
                ctx->g_have_d == ctx->fdh.have_d && ctx->g_alloc == g_alloc_gen.load() &&
+               ctx->g_mlp_n == ctx->mlp_n && ctx->g_mlp_mode == ctx->mlp_mode &&
                ctx->g_stream == ctx->stream && same_cfg(ctx->g_cfg, ctx->cfg);
   if (!fresh) CHK(capture_graph(ctx, what));
   CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
@@ -1375,6 +1463,115 @@ int fb_mlp_grad(fb_ctx *ctx, int n, const float *feat3, const int *triple, const
   std::string e;
   int st = mlp_grad(ctx->mlp, n, feat3, triple, target, grad, loss, ctx->stream, e);
   if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+int fb_mlp_validate(fb_ctx *ctx, int samples_per_bin, unsigned long long seed, double *max_err) {
+  if (!ctx || samples_per_bin < 1) return FB_ERR_ARG;
+  if (!ctx->have_fdata) return fail(ctx, FB_ERR_STATE, "fb_load_fdata first");
+  CU(cudaSetDevice(ctx->device));
+  std::string e;
+  int cells = trip_cells(ctx);
+  int st = mlp_validate(ctx->mlp, mlp_tables(ctx), samples_per_bin, cells, seed, ctx->h_bin_err, ctx->stream, e);
+  if (st) return fail(ctx, st, "%s", e.c_str());
+  ctx->mlp_cells = cells;
+  if (max_err) {
+    double m = 0.0;
+    for (float v : ctx->h_bin_err) m = std::max(m, (double)v);
+    *max_err = m;
+  }
+  return FB_OK;
+}
+
+int fb_mlp_bin_errors(fb_ctx *ctx, float *out, long long *nbins) {
+  if (!ctx) return FB_ERR_ARG;
+  if (nbins) *nbins = (long long)ctx->h_bin_err.size();
+  if (out) std::memcpy(out, ctx->h_bin_err.data(), ctx->h_bin_err.size() * sizeof(float));
+  return FB_OK;
+}
+
+int fb_mlp_gate(fb_ctx *ctx, double tol_ha, double *tau, double *coverage) {
+  if (!ctx || !(tol_ha > 0.0)) return FB_ERR_ARG;
+  if (!ctx->mlp.ready) return fail(ctx, FB_ERR_STATE, "fb_mlp_init first");
+  if (ctx->h_bin_err.empty()) return fail(ctx, FB_ERR_STATE, "fb_mlp_validate first");
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  CU(cudaSetDevice(ctx->device));
+  // the most triplets that add into one block: count them per destination pair
+  int T = ctx->T, nmax = 1;
+  if (T > 0) {
+    std::vector<int> tdst(T), cnt(ctx->P, 0);
+    CU(cudaMemcpy(tdst.data(), ctx->d_tdst.p, T * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int t = 0; t < T; t++) nmax = std::max(nmax, ++cnt[tdst[t]]);
+  }
+  // |error of a block element| <= P_eq2 * 3 * nmax * (largest per-triplet
+  // error of a molecular-frame element): rows and columns of a p-shell
+  // rotation have 1-norms of at most sqrt(3) each
+  double t_eV = tol_ha * P_Hartree;
+  ctx->mlp_tau = t_eV / (P_eq2 * 3.0 * (double)nmax);
+  size_t nb = ctx->h_bin_err.size();
+  std::vector<unsigned char> ok(nb);
+  for (size_t b = 0; b < nb; b++) ok[b] = ctx->h_bin_err[b] <= ctx->mlp_tau ? 1 : 0;
+  CHK(ctx->d_binok.ensure(nb));
+  CU(cudaMemcpy(ctx->d_binok.p, ok.data(), nb, cudaMemcpyHostToDevice));
+  ctx->mlp_mode = FB_MLP_GATED;
+  CHK(bin_triplets(ctx));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (tau) *tau = ctx->mlp_tau;
+  if (coverage) *coverage = T > 0 ? (double)ctx->mlp_n / (double)T : 0.0;
+  return FB_OK;
+}
+
+int fb_mlp_set_mode(fb_ctx *ctx, int mode) {
+  if (!ctx || (mode != FB_MLP_OFF && mode != FB_MLP_GATED && mode != FB_MLP_ALL)) return FB_ERR_ARG;
+  if (mode != FB_MLP_OFF && !ctx->mlp.ready) return fail(ctx, FB_ERR_STATE, "fb_mlp_init first");
+  if (mode == FB_MLP_GATED && !ctx->d_binok.p) return fail(ctx, FB_ERR_STATE, "fb_mlp_gate first");
+  if (mode != FB_MLP_OFF && ctx->fdh.have_d)
+    return fail(ctx, FB_ERR_UNSUPPORTED, "MLP-3c covers s and sp bases");
+  CU(cudaSetDevice(ctx->device));
+  ctx->mlp_mode = mode;
+  if (ctx->have_neigh) {
+    CHK(bin_triplets(ctx));
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return FB_OK;
+}
+
+int fb_mlp_eval_points(fb_ctx *ctx, int n, const float *pts, const int *triple, int derivs, float *out) {
+  if (!ctx || n < 1 || !pts || !triple || !out) return FB_ERR_ARG;
+  if (!ctx->mlp.ready) return fail(ctx, FB_ERR_STATE, "fb_mlp_init first");
+  for (int i = 0; i < n; i++)
+    if (triple[i] < 0 || triple[i] >= ctx->mlp.ntrip || ctx->mlp.h_nme[triple[i]] == 0)
+      return fail(ctx, FB_ERR_ARG, "point %d: species triple %d has no table", i, triple[i]);
+  CU(cudaSetDevice(ctx->device));
+  int rows = derivs ? 4 : 1;
+  DevBuf p, t, o;
+  CHK(p.ensure((size_t)n * 3 * sizeof(float)));
+  CHK(t.ensure((size_t)n * sizeof(int)));
+  CHK(o.ensure((size_t)n * rows * MLP_ME_STRIDE * sizeof(float)));
+  CU(cudaMemcpyAsync(p.p, pts, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(t.p, triple, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  int saved = ctx->mlp_n;
+  ctx->mlp_n = n;
+  MlpEvalArgs m = mlp_eval_args(ctx);
+  ctx->mlp_n = saved;
+  m.pts = p.as<float>();
+  m.ptrip = t.as<int>();
+  m.out = o.as<float>();
+  AsmArgs a = asm_args(ctx);
+  KL(KT_MLP_EVAL, launch_mlp_eval(m, a, derivs != 0, ctx->nsm, ctx->stream));
+  CU(cudaMemcpyAsync(out, o.p, (size_t)n * rows * MLP_ME_STRIDE * sizeof(float), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  p.release();
+  t.release();
+  o.release();
+  return FB_OK;
+}
+
+int fb_mlp_routed(const fb_ctx *ctx, int *n_mlp, int *n_total) {
+  if (!ctx) return FB_ERR_ARG;
+  if (n_mlp) *n_mlp = mlp_routes(ctx) ? ctx->mlp_n : 0;
+  if (n_total) *n_total = ctx->T;
   return FB_OK;
 }
 

@@ -5,15 +5,21 @@
 
 namespace fb {
 
-template <int PA, int PB>
-__device__ __forceinline__ void trip_3c_df(const Ctx3c &c, int t) {
+// MLP: F comes from the MLP-3c results of list position i instead of the tables
+template <int PA, int PB, bool MLP>
+__device__ __forceinline__ void trip_3c_df(const Ctx3c &c, int t, int i) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
   GeomDF g;
   trip_geom_df(c, t, g);
-  const Cell3cDev &cell = c.fd->c3[c.isp[g.iat]][c.isp[g.jat]][c.isp[g.ia]];
   df F[NE];
-  interp3c_df<NE, false>(c, cell, g.x, g.z, g.cost, F, nullptr, nullptr, nullptr);
+  if constexpr (MLP) {
+#pragma unroll
+    for (int e = 0; e < NE; e++) F[e] = df_make(c.mlpF[(long long)i * MLP_ME_STRIDE + e]);
+  } else {
+    const Cell3cDev &cell = c.fd->c3[c.isp[g.iat]][c.isp[g.jat]][c.isp[g.ia]];
+    interp3c_df<NE, false>(c, cell, g.x, g.z, g.cost, F, nullptr, nullptr, nullptr);
+  }
   // sint = sqrt(max(1e-5, 1 - cost^2)) (:349) for the mvalue = 1 channels
   df s2 = df_one() - g.cost * g.cost;
   df sint = df_sqrt(s2.h > 1.0e-5f ? s2 : df_make(1.0e-5f, 2.5262125e-13f));
@@ -34,15 +40,17 @@ __device__ __forceinline__ void trip_3c_df(const Ctx3c &c, int t) {
   for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, df_to(X[q] * peq2));
 }
 
+template <bool MLP>
 __global__ void __launch_bounds__(256) k_assemble_3c_df(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
+    int i = t;
     if (c.tperm) t = c.tperm[t];
     int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
     switch (pa * 3 + pb) {
-      case PAT_SP * 3 + PAT_SP: trip_3c_df<PAT_SP, PAT_SP>(c, t); break;
-      case PAT_SP * 3 + PAT_S: trip_3c_df<PAT_SP, PAT_S>(c, t); break;
-      case PAT_S * 3 + PAT_SP: trip_3c_df<PAT_S, PAT_SP>(c, t); break;
-      case PAT_S * 3 + PAT_S: trip_3c_df<PAT_S, PAT_S>(c, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_3c_df<PAT_SP, PAT_SP, MLP>(c, t, i); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_df<PAT_SP, PAT_S, MLP>(c, t, i); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_df<PAT_S, PAT_SP, MLP>(c, t, i); break;
+      case PAT_S * 3 + PAT_S: trip_3c_df<PAT_S, PAT_S, MLP>(c, t, i); break;
       default: break;
     }
   });
@@ -55,7 +63,19 @@ int launch_assemble_3c_df(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_a3c, (long long)a.ntrip, a.queue ? a.queue + 1 : nullptr, s, grid, block, q);
   if (e) return e;
-  k_assemble_3c_df<<<grid, block, 0, s>>>(c, q);
+  k_assemble_3c_df<false><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_assemble_3c_mlp(const AsmArgs &a, cudaStream_t s) {
+  if (a.ntrip == 0) return 0;
+  Ctx3c c = make3c(a);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_a3c, (long long)a.ntrip, a.queue ? a.queue + 1 : nullptr, s, grid, block, q);
+  if (e) return e;
+  k_assemble_3c_df<true><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

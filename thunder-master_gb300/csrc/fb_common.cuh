@@ -100,6 +100,8 @@ struct Ctx3c {
   // double-float copies (table values and rho blocks as hi + lo floats)
   const df *table3c_df;
   const df *rho_df;
+  // MLP-3c results per list position (F or F, dF/dcos, dF/dx, dF/dy; 10 each)
+  const float *mlpF;
 };
 
 struct TripGeom {
@@ -376,6 +378,7 @@ inline Ctx3c make3c(const AsmArgs &a) {
   c.f3nac = a.f3nac;
   c.table3c_df = reinterpret_cast<const df *>(a.table3c_df);
   c.rho_df = reinterpret_cast<const df *>(a.rho_df);
+  c.mlpF = a.mlpF;
   return c;
 }
 

@@ -108,17 +108,30 @@ __device__ __forceinline__ df mol_HM_df(const RotDF &R, const df dP[3][3], const
   return acc;
 }
 
-template <int PA, int PB>
-__device__ void trip_3c_force_df(const Ctx3c &c, int t) {
+// MLP: F and its cos / x / y derivatives come from the MLP-3c results of
+// list position i instead of the tables
+template <int PA, int PB, bool MLP>
+__device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
   // interpolation first: it needs only x, z and cos(theta)
   GeomFP64 h;
   trip_geom_fp64(c, t, h);
   const int ia = h.ia, iat = h.iat, jat = h.jat;
-  const Cell3cDev &cell = c.fd->c3[c.isp[iat]][c.isp[jat]][c.isp[ia]];
   df F[NE], DpF[NE], DxF[NE], DyF[NE];
-  interp3c_df<NE, true>(c, cell, h.x, h.z, trip_cost_df(h), F, DpF, DxF, DyF);
+  if constexpr (MLP) {
+    const float *m = c.mlpF + (long long)i * 4 * MLP_ME_STRIDE;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      F[e] = df_make(m[e]);
+      DpF[e] = df_make(m[MLP_ME_STRIDE + e]);
+      DxF[e] = df_make(m[2 * MLP_ME_STRIDE + e]);
+      DyF[e] = df_make(m[3 * MLP_ME_STRIDE + e]);
+    }
+  } else {
+    const Cell3cDev &cell = c.fd->c3[c.isp[iat]][c.isp[jat]][c.isp[ia]];
+    interp3c_df<NE, true>(c, cell, h.x, h.z, trip_cost_df(h), F, DpF, DxF, DyF);
+  }
   GeomDF g;
   trip_geom_df_from(h, g);
   const df cost = g.cost, iz = g.iz;
@@ -193,15 +206,17 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t) {
   }
 }
 
+template <bool MLP>
 __global__ void __launch_bounds__(256) k_dassemble_3c_df(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
+    int i = t;
     if (c.tperm) t = c.tperm[t];
     int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
     switch (pa * 3 + pb) {
-      case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP>(c, t); break;
-      case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S>(c, t); break;
-      case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP>(c, t); break;
-      case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S>(c, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP, MLP>(c, t, i); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S, MLP>(c, t, i); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP, MLP>(c, t, i); break;
+      case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S, MLP>(c, t, i); break;
       default: break;
     }
   });
@@ -214,7 +229,19 @@ int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  k_dassemble_3c_df<<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c_df<false><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s) {
+  if (a.ntrip == 0) return 0;
+  Ctx3c c = make3c(a);
+  dim3 grid, block;
+  Sched q;
+  int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
+  if (e) return e;
+  k_dassemble_3c_df<true><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -14,12 +14,16 @@ constexpr int MAXSP = 8;         // species per Fdata set
 constexpr int NTHETA = 5;        // Legendre terms of the 3c tables
 constexpr double P_eq2 = 14.39975;   // include/constants.h:4
 constexpr double P_abohr = 0.529177; // include/constants.h:2
+constexpr double P_Hartree = P_eq2 / P_abohr;  // include/constants.h:5 (eV)
 constexpr int P_mbox = 4;            // c.SYSTEM/M_configuraciones.f90:359
 // periodic images of make_cells (c.SYSTEM/make_cells.f90:125-144): a
 // (2 P_mbox + 1)^3 box, mbeta = 0 .. 728.  Every structure of a batch owns
 // XL_STRIDE doubles of image vectors, xl(:, mbeta) at 3 * mbeta.
 constexpr int NIMG = (2 * P_mbox + 1) * (2 * P_mbox + 1) * (2 * P_mbox + 1);
 constexpr int XL_STRIDE = 3 * NIMG;
+// MLP-3c results per triplet: 10 values (the bcna matrix elements of an sp x
+// sp pair), and in the force pass 4 such rows: F, dF/dcos, dF/dx, dF/dy
+constexpr int MLP_ME_STRIDE = 10;
 
 // Basis patterns: the shell lists this build compiles rotation code for.
 // PAT_S = [s], PAT_SP = [s, p], PAT_SPD = [s, p, d]; orbital order inside a

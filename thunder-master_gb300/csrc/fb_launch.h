@@ -75,6 +75,8 @@ struct AsmArgs {
   unsigned *status;
   const float2 *table3c_df;  // hi, lo float pairs of table3c
   float2 *rho_df;            // hi, lo float pairs of rho
+  // MLP-3c: per list position, the network's values (and derivatives)
+  const float *mlpF;
   // launch shapes (autotuned) and the work counters of persistent launches
   KCfg cfg_a2c, cfg_a3c, cfg_d2c, cfg_d3c;
   int *queue;  // 4 counters: assemble_2c, assemble_3c, dassemble_2c, dassemble_3c
@@ -83,9 +85,11 @@ struct AsmArgs {
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s);
 int launch_neigh_back(const NeighArgs &a, cudaStream_t s);
 int launch_common(const NeighArgs &a, bool fill, cudaStream_t s);
-// counting sort of the triplets by (species triple, 3c grid cell) -> perm
-int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, int *rank, int *hist, int *perm,
-                     cudaStream_t s);
+// counting sort of the triplets by (species triple, 3c grid cell) -> perm;
+// bins with binok[bin] set (may be null) come first; hist has 2 x nbins
+// entries and holds the exclusive bin starts afterwards
+int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsigned char *binok, int *key, int *rank,
+                     int *hist, int *perm, cudaStream_t s);
 int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_assemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
@@ -95,6 +99,12 @@ int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_assemble_3c_df(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s);
 int launch_split_rho(const AsmArgs &a, long long nblock, cudaStream_t s);
+// three-center kernels fed by MLP-3c results (a.mlpF) instead of the tables:
+// list positions 0 .. a.ntrip-1 of a.tperm
+int launch_assemble_3c_mlp(const AsmArgs &a, cudaStream_t s);
+int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s);
+struct MlpEvalArgs;
+int launch_mlp_eval(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
 // DFMA throughput probe: one warm-up and one timed launch
 int probe_dfma(cudaStream_t s, double *ms, double *flops);
 int probe_ffma(cudaStream_t s, double *ms, double *flops);

@@ -94,6 +94,72 @@ __global__ void k_mlp_gen(long long n, long long first, unsigned long long seed,
   for (int o = NTHETA * MLP_ME; o < MLP_OUT; o++) Y[s * MLP_OUT + o] = 0.0f;
 }
 
+// Validation samples, stratified by interpolation bin: bin = (triple, node
+// (ix, iy) of the 4 x 4 stencil); the bin's region is the set of (x, y) whose
+// clamped stencil index is (ix, iy) (getMEs_Fdata_3c, :367-376).  Targets as
+// in k_mlp_gen; samples of bins without a table are marked with trip = -1.
+__global__ void k_mlp_gen_bins(long long n, long long first, int per_bin, int cells, unsigned long long seed,
+                               MlpTables tb, int nsp, const float *__restrict__ scale, float *__restrict__ feat3,
+                               int *__restrict__ trip, float *__restrict__ Y) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  long long gs = first + s;
+  int bin = (int)(gs / per_bin);
+  int tr = bin / cells, node = bin % cells;
+  int a = tr / (nsp * nsp), b = (tr / nsp) % nsp, kk = tr % nsp;
+  const Cell3cDev &cell = tb.fd->c3[a][b][kk];
+  bool ok = cell.off >= 0 && node < cell.nx * cell.ny;
+  int ix = ok ? node % cell.nx + 1 : 2, iy = ok ? node / cell.nx + 1 : 2;  // 1-based
+  ok = ok && ix >= 2 && ix <= cell.nx - 2 && iy >= 2 && iy <= cell.ny - 2;
+  if (!ok) {
+    trip[s] = -1;
+    feat3[3 * s] = feat3[3 * s + 1] = feat3[3 * s + 2] = 0.0f;
+    for (int o = 0; o < MLP_OUT; o++) Y[s * MLP_OUT + o] = 0.0f;
+    return;
+  }
+  unsigned long long k = (unsigned long long)gs * 4ull;
+  double xl = ix == 2 ? 0.0 : (ix - 1) * cell.dx, xh = ix == cell.nx - 2 ? cell.xmax : ix * cell.dx;
+  double yl = iy == 2 ? 0.0 : (iy - 1) * cell.dy, yh = iy == cell.ny - 2 ? cell.ymax : iy * cell.dy;
+  double x = xl + (xh - xl) * unit_rand(seed, k), y = yl + (yh - yl) * unit_rand(seed, k + 1);
+  double c = 2.0 * unit_rand(seed, k + 2) - 1.0;
+  double I[NTHETA][MLP_ME];
+  interp3c_terms(tb, cell, x, y, I);
+  feat3[3 * s] = (float)(2.0 * x / cell.xmax - 1.0);
+  feat3[3 * s + 1] = (float)(2.0 * y / cell.ymax - 1.0);
+  feat3[3 * s + 2] = (float)c;
+  trip[s] = tr;
+  for (int th = 0; th < NTHETA; th++)
+    for (int e = 0; e < MLP_ME; e++) {
+      int o = th * MLP_ME + e;
+      Y[s * MLP_OUT + o] = (float)(I[th][e] / (double)scale[tr * MLP_OUT + o]);
+    }
+  for (int o = NTHETA * MLP_ME; o < MLP_OUT; o++) Y[s * MLP_OUT + o] = 0.0f;
+}
+
+// per-bin maximum over samples of max_ime |sum_theta P_theta(cos) (out - target) * scale|
+__global__ void k_mlp_bin_err(long long n, long long first, int per_bin, const float *__restrict__ feat3,
+                              const int *__restrict__ trip, const float *__restrict__ O, const float *__restrict__ Y,
+                              const float *__restrict__ scale, const int *__restrict__ tmeta,
+                              unsigned *__restrict__ bin_err) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int tr = trip[s];
+  if (tr < 0) return;
+  float c = feat3[3 * s + 2], c2 = c * c;
+  float pl[5] = {1.0f, c, 0.5f * (3.0f * c2 - 1.0f), 0.5f * c * (5.0f * c2 - 3.0f),
+                 0.125f * (3.0f - c2 * (30.0f - 35.0f * c2))};
+  float mx = 0.0f;
+  for (int e = 0; e < tmeta[tr]; e++) {
+    float d = 0.0f;
+    for (int th = 0; th < NTHETA; th++) {
+      int o = th * MLP_ME + e;
+      d += pl[th] * (O[s * MLP_OUT + o] - Y[s * MLP_OUT + o]) * scale[tr * MLP_OUT + o];
+    }
+    mx = fmaxf(mx, fabsf(d));
+  }
+  atomicMax(bin_err + (first + s) / per_bin, __float_as_uint(mx));  // non-negative floats order as integers
+}
+
 // input rows: 3 coordinates, the triple's embedding, zeros; plain and transposed
 __global__ void k_mlp_input(int B, const float *__restrict__ feat3, const int *__restrict__ trip,
                             const float *__restrict__ emb, __nv_bfloat16 *__restrict__ X,
@@ -101,10 +167,16 @@ __global__ void k_mlp_input(int B, const float *__restrict__ feat3, const int *_
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= B * MLP_IN) return;
   int r = idx / MLP_IN, k = idx % MLP_IN;
-  float v = 0.0f;
-  if (k < 3) v = feat3[3 * r + k];
-  else if (k < 3 + MLP_EMB) v = emb[trip[r] * MLP_EMB + (k - 3)];
-  __nv_bfloat16 h = __float2bfloat16_rn(v);
+  int tr = trip[r] < 0 ? 0 : trip[r];
+  __nv_bfloat16 h = __float2bfloat16_rn(0.0f);
+  if (k < 3) {
+    h = __float2bfloat16_rn(feat3[3 * r + k]);
+  } else if (k < 3 + MLP_EMB) {
+    h = __float2bfloat16_rn(emb[tr * MLP_EMB + (k - 3)]);
+  } else if (k < MLP_LO + 3) {
+    float f = feat3[3 * r + (k - MLP_LO)];
+    h = __float2bfloat16_rn(f - __bfloat162float(__float2bfloat16_rn(f)));
+  }
   X[idx] = h;
   if (Xt) Xt[(long long)k * B + r] = h;
 }
@@ -222,14 +294,18 @@ __global__ void k_mlp_loss(int B, const float *__restrict__ O, const float *__re
 }
 
 // sum of split-K partials into the gradient; rows >= mrows_used and columns
-// >= ncols_used stay zero (padding of W1 columns and W4 rows)
+// >= ncols_used stay zero (padding of W1 columns and W4 rows); tie > 0:
+// columns tie .. tie+2 share the weights of columns 0..2, so their
+// gradients are added there
 __global__ void k_wgrad_reduce(int M, int N, int S, const float *__restrict__ part, float *__restrict__ g,
-                               int mrows_used, int ncols_used) {
+                               int mrows_used, int ncols_used, int tie) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= M * N) return;
   int m = idx / N, n = idx % N;
   float v = 0.0f;
   for (int s = 0; s < S; s++) v += part[(long long)s * M * N + idx];
+  if (tie > 0 && n < 3)
+    for (int s = 0; s < S; s++) v += part[(long long)s * M * N + m * N + tie + n];
   g[idx] = (m < mrows_used && n < ncols_used) ? v : 0.0f;
 }
 
@@ -264,13 +340,15 @@ __global__ void k_adam(long long n, float *__restrict__ p, const float *__restri
   p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
-// BF16 copies of a weight matrix W[N][K]: plain and transposed (Wt[K][N])
+// BF16 copies of a weight matrix W[N][K]: plain and transposed (Wt[K][N]);
+// tie > 0: columns tie .. tie+2 repeat columns 0..2 (W1's low-part inputs)
 __global__ void k_pack_w(int N, int K, const float *__restrict__ W, __nv_bfloat16 *__restrict__ Wb,
-                         __nv_bfloat16 *__restrict__ Wt) {
+                         __nv_bfloat16 *__restrict__ Wt, int tie) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N * K) return;
   int n = idx / K, k = idx % K;
-  __nv_bfloat16 h = __float2bfloat16_rn(W[idx]);
+  int ks = (tie > 0 && k >= tie && k < tie + 3) ? k - tie : k;
+  __nv_bfloat16 h = __float2bfloat16_rn(W[n * K + ks]);
   Wb[idx] = h;
   Wt[(long long)k * N + n] = h;
 }
@@ -327,7 +405,7 @@ int pack_weights(MlpState &m, cudaStream_t s, std::string &err) {
             {m.o_w4, o.w4, o.w4t, MLP_OUT, MLP_H}};
   for (auto &l : L) {
     int n = l.n * l.k;
-    k_pack_w<<<(n + 255) / 256, 256, 0, s>>>(l.n, l.k, P + l.src, W + l.b, W + l.t);
+    k_pack_w<<<(n + 255) / 256, 256, 0, s>>>(l.n, l.k, P + l.src, W + l.b, W + l.t, l.src == m.o_w1 ? MLP_LO : 0);
   }
   MCU(cudaGetLastError());
   return FB_OK;
@@ -430,7 +508,7 @@ int backward(MlpState &m, int B, const float *Y, const int *trip, double *d_loss
   ep.ldz = MLP_H;
   MCU((cudaError_t)gemm<EPI_STORE>(MLP_OUT, MLP_H, B, dOt, B, a.Ht[2], B, ep, S, s));
   k_wgrad_reduce<<<(MLP_OUT * MLP_H + 255) / 256, 256, 0, s>>>(MLP_OUT, MLP_H, S, part, G + m.o_w4,
-                                                                 NTHETA * MLP_ME, MLP_H);
+                                                                 NTHETA * MLP_ME, MLP_H, 0);
   k_bias_grad<<<(MLP_OUT * 32 + 255) / 256, 256, 0, s>>>(MLP_OUT, B, dOt, G + m.o_b4, NTHETA * MLP_ME);
   MCU(cudaGetLastError());
   const __nv_bfloat16 *gin = dO;
@@ -454,7 +532,7 @@ int backward(MlpState &m, int B, const float *Y, const int *trip, double *d_loss
     ep.ldz = kin;
     MCU((cudaError_t)gemm<EPI_STORE>(MLP_H, kin, B, a.dZt[l], B, hin_t, B, ep, S, s));
     k_wgrad_reduce<<<(MLP_H * kin + 255) / 256, 256, 0, s>>>(MLP_H, kin, S, part, G + wg[l], MLP_H,
-                                                              l == 0 ? 3 + MLP_EMB : kin);
+                                                              l == 0 ? 3 + MLP_EMB : kin, l == 0 ? MLP_LO : 0);
     k_bias_grad<<<(MLP_H * 32 + 255) / 256, 256, 0, s>>>(MLP_H, B, a.dZt[l], G + bg[l], MLP_H);
     MCU(cudaGetLastError());
     gin = a.dZ[l];
@@ -694,6 +772,56 @@ int mlp_grad(MlpState &m, int n, const float *feat3, const int *trip, const floa
   tr.release();
   y.release();
   dl.release();
+  return FB_OK;
+}
+
+int mlp_validate(MlpState &m, const MlpTables &t, int per_bin, int cells, unsigned long long seed,
+                 std::vector<float> &bin_err, cudaStream_t s, std::string &err) {
+  if (!m.ready) {
+    err = "MLP not initialized";
+    return FB_ERR_STATE;
+  }
+  if (per_bin < 1) {
+    err = "per_bin must be positive";
+    return FB_ERR_ARG;
+  }
+  long long nbins = (long long)m.ntrip * cells, total = nbins * per_bin;
+  const int chunk = 1 << 16;
+  int st;
+  if ((st = ensure_batch(m, chunk, err))) return st;
+  DevBuf f, tr, y, be;
+  MCHK(f.ensure((size_t)chunk * 3 * sizeof(float)));
+  MCHK(tr.ensure((size_t)chunk * sizeof(int)));
+  MCHK(y.ensure((size_t)chunk * MLP_OUT * sizeof(float)));
+  MCHK(be.ensure((size_t)nbins * sizeof(unsigned)));
+  MCU(cudaMemsetAsync(be.p, 0, nbins * sizeof(unsigned), s));
+  for (long long first = 0; first < total; first += chunk) {
+    long long n = std::min<long long>(chunk, total - first);
+    int rows = (int)((n + 63) / 64 * 64);
+    if (rows > n) {
+      // pad rows: a valid triple index with zero features; excluded from the error
+      MCU(cudaMemsetAsync(f.p, 0, (size_t)rows * 3 * sizeof(float), s));
+      MCU(cudaMemsetAsync(tr.p, 0xff, (size_t)rows * sizeof(int), s));
+    }
+    k_mlp_gen_bins<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, first, per_bin, cells, seed, t, m.nsp,
+                                                               m.scale.as<float>(), f.as<float>(), tr.as<int>(),
+                                                               y.as<float>());
+    MCU(cudaGetLastError());
+    if ((st = forward(m, rows, f.as<float>(), tr.as<int>(), false, s, err))) return st;
+    k_mlp_bin_err<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, first, per_bin, f.as<float>(), tr.as<int>(),
+                                                              m.O.as<float>(), y.as<float>(), m.scale.as<float>(),
+                                                              m.tmeta.as<int>(), be.as<unsigned>());
+    MCU(cudaGetLastError());
+  }
+  std::vector<unsigned> bits(nbins);
+  MCU(cudaMemcpyAsync(bits.data(), be.p, nbins * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  MCU(cudaStreamSynchronize(s));
+  bin_err.resize(nbins);
+  for (long long b = 0; b < nbins; b++) std::memcpy(&bin_err[b], &bits[b], sizeof(float));
+  f.release();
+  tr.release();
+  y.release();
+  be.release();
   return FB_OK;
 }
 

@@ -4,7 +4,8 @@
 // (getMEs_Fdata_3c, e.FDATA/M_Fdata_3c.f90:293-517).
 //
 // Network: inputs (2 x / xmax - 1, 2 y / ymax - 1, cos theta) of a triplet
-// plus a 16-float embedding of its species triple (in1, in2, indna), three
+// (each as a BF16 pair, high and low part) plus a 16-float embedding of its
+// species triple (in1, in2, indna), three
 // hidden layers of 128 with SiLU, 64 outputs of which 50 are used: the
 // Legendre coefficient itheta = 1..5 of each of the (at most) 10 bcna matrix
 // elements, output = (itheta - 1) * 10 + ime, divided by a per-output scale
@@ -12,6 +13,7 @@
 // and the activations fed to the tensor cores are BF16, accumulation FP32.
 // Training data come from the FP64 table interpolator itself.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -27,6 +29,10 @@ constexpr int MLP_EMB = 16;
 constexpr int MLP_H = 128;
 constexpr int MLP_OUT = 64;   // 5 theta x 10 ME used, padded
 constexpr int MLP_ME = 10;    // matrix elements per Legendre term (sp x sp)
+// the 3 coordinates enter twice: their BF16 roundings in columns 0..2 and the
+// BF16 roundings of the remainders in columns MLP_LO..MLP_LO+2, both through
+// the same (tied) weights, so the products see ~16-bit coordinates
+constexpr int MLP_LO = 3 + MLP_EMB;
 
 struct MlpState {
   bool ready = false;
@@ -48,6 +54,22 @@ struct MlpState {
   long long data_cap = 0;
 };
 
+// MLP-3c evaluation for the assembly (fb_mlp_eval.cu): the first n
+// triplets of the binned order through the network
+struct MlpEvalArgs {
+  int n;                     // triplets in the list
+  const int *list;           // triplet indices (the binned order)
+  const __nv_bfloat16 *wbf;  // BF16 weights: W1 [128][32], W2, W3 [128][128], W4 [64][128]
+  const float *params;       // FP32 parameters (biases, embedding)
+  long long o_emb, o_b1, o_b2, o_b3, o_b4;
+  const float *scale;        // [ntrip][64]
+  int nsp;
+  float *out;                // [n][10] values, or [n][4][10]: F, dF/dcos, dF/dx, dF/dy
+  // points instead of triplets (tests): pts [n][3] = (x, y, cos), ptrip [n]
+  const float *pts;
+  const int *ptrip;
+};
+
 // Device tables the sample generator interpolates (FP64, as assembled).
 struct MlpTables {
   const FdataDev *fd;
@@ -66,6 +88,10 @@ int mlp_grad(MlpState &m, int n, const float *feat3, const int *trip, const floa
 // forward pass of n rows given on the host (normalized outputs, n x MLP_OUT)
 int mlp_forward(MlpState &m, int n, const float *feat3, const int *trip, float *out, cudaStream_t s,
                 std::string &err);
+// per-bin maximum error of the network (table units, Legendre-combined
+// values) over per_bin samples of each interpolation bin (triple x cells)
+int mlp_validate(MlpState &m, const MlpTables &t, int per_bin, int cells, unsigned long long seed,
+                 std::vector<float> &bin_err, cudaStream_t s, std::string &err);
 // table samples as the trainer draws them (for tests): features, triple, normalized targets
 int mlp_samples(MlpState &m, const MlpTables &t, int n, unsigned long long seed, float *feat3, int *trip,
                 float *target, cudaStream_t s, std::string &err);

@@ -263,7 +263,8 @@ __global__ void k_common(int N, const int *__restrict__ speriodic, const double 
 
 // ---------------------------------------------------------------------------
 // Triplet binning: a counting sort of the triplets by (species triple, 3c
-// grid cell of the interpolation stencil).  The three-center kernels walk
+// grid cell of the interpolation stencil), bins approved for the MLP-3c
+// surrogate first.  The three-center kernels walk
 // the triplets in this order, so neighboring lanes read the same table
 // stencil (broadcast loads) and take the same interpolation branch.  The
 // cell is computed with the set-up of assemble_vna_3c
@@ -274,8 +275,9 @@ __global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__
                            const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                            const double *__restrict__ xl0,
                            const int *__restrict__ talpha, const int *__restrict__ ci_j, const int *__restrict__ ci_b,
-                           const int *__restrict__ cj_j, const int *__restrict__ cj_b, int *__restrict__ key,
-                           int *__restrict__ rank, int *__restrict__ hist) {
+                           const int *__restrict__ cj_j, const int *__restrict__ cj_b,
+                           const unsigned char *__restrict__ binok, int *__restrict__ key, int *__restrict__ rank,
+                           int *__restrict__ hist) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int ia = talpha[t], i = ci_j[t], j = cj_j[t], ib = ci_b[t], jb = cj_b[t];
@@ -297,6 +299,8 @@ __global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__
   iy = min(max(iy, 2), cell.ny - 2);
   int node = (iy - 1) * cell.nx + (ix - 1);
   int k = ((a * nsp + b) * nsp + c) * cells + min(node, cells - 1);
+  // bins approved for the MLP-3c surrogate come first
+  if (!(binok && binok[k])) k += nsp * nsp * nsp * cells;
   key[t] = k;
   rank[t] = atomicAdd(hist + k, 1);
 }
@@ -332,15 +336,15 @@ __global__ void k_trip_scatter(int T, const int *__restrict__ key, const int *__
   perm[start[key[t]] + rank[t]] = t;
 }
 
-int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, int *key, int *rank, int *hist, int *perm,
-                     cudaStream_t s) {
+int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsigned char *binok, int *key, int *rank,
+                     int *hist, int *perm, cudaStream_t s) {
   if (T == 0) return 0;
-  int nbins = nsp * nsp * nsp * cells;
+  int nbins = 2 * nsp * nsp * nsp * cells;
   cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
   int threads = 256, blocks = (T + threads - 1) / threads;
   k_trip_key<<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.isp, a.fd, a.sid, a.xl, a.talpha, a.ci_j, a.ci_b,
-                                        a.cj_j, a.cj_b, key, rank, hist);
+                                        a.cj_j, a.cj_b, binok, key, rank, hist);
   FB_LAUNCH_CHECK();
   k_scan_bins<<<1, 1024, 0, s>>>(nbins, hist);
   FB_LAUNCH_CHECK();

@@ -35,6 +35,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
+FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
 BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
@@ -71,6 +72,12 @@ _SIGS = {
     "fb_mlp_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p]),
     "fb_mlp_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_mlp_validate": (C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong, C.c_void_p]),
+    "fb_mlp_bin_errors": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_mlp_gate": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "fb_mlp_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "fb_mlp_routed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_mlp_eval_points": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "fb_assemble_graph": (C.c_int, [C.c_void_p, C.c_uint]),
     "fb_set_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "fb_get_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -340,6 +347,43 @@ class Context:
         out = np.zeros((len(t), 64), np.float32)
         self._check(self.L.fb_mlp_forward(self.h, len(t), _ptr(f), _ptr(t), _ptr(out)))
         return out
+
+    def mlp_validate(self, samples_per_bin=64, seed=17):
+        """Largest per-bin error of the network against the FP64 tables."""
+        m = C.c_double()
+        self._check(self.L.fb_mlp_validate(self.h, int(samples_per_bin), int(seed), C.byref(m)))
+        return m.value
+
+    def mlp_bin_errors(self):
+        n = C.c_longlong()
+        self._check(self.L.fb_mlp_bin_errors(self.h, None, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        self._check(self.L.fb_mlp_bin_errors(self.h, _ptr(out), C.byref(n)))
+        return out
+
+    def mlp_gate(self, tol_ha):
+        """Approve the bins whose error keeps |dH| <= tol_ha (Hartree) in the
+        worst case; returns (tau, coverage)."""
+        tau, cov = C.c_double(), C.c_double()
+        self._check(self.L.fb_mlp_gate(self.h, float(tol_ha), C.byref(tau), C.byref(cov)))
+        return tau.value, cov.value
+
+    def mlp_set_mode(self, mode):
+        self._check(self.L.fb_mlp_set_mode(self.h, int(mode)))
+
+    def mlp_eval_points(self, pts, triple, derivs=True):
+        """The assembly's network evaluation at (x, y, cos) points:
+        [n][4][10] = value, d/dcos, d/dx, d/dy (or [n][10] values)."""
+        p = np.ascontiguousarray(pts, np.float32)
+        t = np.ascontiguousarray(triple, np.int32)
+        out = np.zeros((len(t), 4 if derivs else 1, 10), np.float32)
+        self._check(self.L.fb_mlp_eval_points(self.h, len(t), _ptr(p), _ptr(t), int(bool(derivs)), _ptr(out)))
+        return out if derivs else out[:, 0]
+
+    def mlp_routed(self):
+        a, b = C.c_int(), C.c_int()
+        self._check(self.L.fb_mlp_routed(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def blocks(self, which):
         n = self.nblock * (3 if which in ("dS", "dT") else 1)
