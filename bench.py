@@ -217,29 +217,139 @@ def tuned_shapes(ctx, fbgpu, autotune):
     return {k: ctx.get_launch(k) for k in fbgpu.TUNABLE}
 
 
-def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps):
-    """Roofline of the dominant kernel from its CUDA-event launch times."""
+# Executed FP32 work of the double-float three-center kernels per sp3 x sp3
+# triplet (2 FFMA + FADD + FMUL thread instructions), and the DRAM bytes per
+# triplet of one launch, from ncu on SiC4096 (profiles/): the df
+# formulation's arithmetic is what the FP32 pipe must execute.
+DF_FP32_FLOP = {"dassemble_3c": 55932.0, "assemble_3c": 15224.0}
+DF_DRAM_BYTES = {"dassemble_3c": 93.4, "assemble_3c": 89.7}
+
+
+def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
+    """Roofline of the dominant kernel from its CUDA-event launch times.
+    Double-float kernels run on the FP32 pipe: achieved = executed FP32
+    FLOPs per launch / launch time against the FP32 FFMA peak probed in the
+    same run.  FP64 kernels: the algorithmic FP64 FLOPs against the DFMA
+    peak.  The FP64-equivalent rate (algorithmic FLOPs of the FP64
+    formulation) and the HBM view are reported beside it."""
     dom = max(ktimes, key=lambda k: ktimes[k][0])
     dom_ms = ktimes[dom][0] / max(1, ktimes[dom][1])
     from fbgpu import synth
     nme = len(synth.make_munu_3c([0, 1], [0, 1])[0])
-    fl = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
-    if fl is None:
+    fl64 = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
+    if fl64 is None:
         return None
     fp64_peak = ctx.probe_fp64()
-    ach = fl / (dom_ms * 1e-3) / 1e12
-    roof = {"bound": "fp64", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp64_peak, 4),
-            "unit": "TFLOP/s", "frac": round(ach / fp64_peak, 4), "traffic": None,
-            "peak_source": "measured in this run (fb_probe_fp64 DFMA chains)",
-            "flops_per_launch": fl, "avg_launch_ms": round(dom_ms, 4)}
+    ach64 = fl64 / (dom_ms * 1e-3) / 1e12
     table_bytes = 8 * 31 * 31 * 5 * nme * len(nZ) ** 3
     by = bytes_dassemble_3c(T, P, natoms, 16, table_bytes)
     with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
         hbm_peak = json.load(f)["hbm_gbs"]
-    roof["hbm"] = {"achieved": round(by / (dom_ms * 1e-3) / 1e9, 3), "peak": hbm_peak, "unit": "GB/s",
-                   "frac": round(by / (dom_ms * 1e-3) / 1e9 / hbm_peak, 6), "bytes_per_launch": by,
-                   "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
-    return roof
+    hbm = {"achieved": round(by / (dom_ms * 1e-3) / 1e9, 3), "peak": hbm_peak, "unit": "GB/s",
+           "frac": round(by / (dom_ms * 1e-3) / 1e9 / hbm_peak, 6), "bytes_per_launch": by,
+           "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+    if prec == "df":
+        fp32_peak = ctx.probe_fp32()
+        fl32 = T * DF_FP32_FLOP[dom]
+        ach = fl32 / (dom_ms * 1e-3) / 1e12
+        return {"bound": "fp32", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp32_peak, 4),
+                "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4),
+                "traffic": round(T * DF_DRAM_BYTES[dom]),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on SiC4096, "
+                                  "scaled by triplets",
+                "peak_source": "of measured: fb_probe_fp32 FFMA chains in this run",
+                "flops_per_launch": fl32,
+                "flops_source": "executed FP32 FLOPs of the double-float kernel (2 FFMA + FADD + FMUL per "
+                                "triplet, ncu on SiC4096)",
+                "avg_launch_ms": round(dom_ms, 4),
+                "fp64_equivalent": {"algorithmic_flops_per_launch": fl64, "achieved": round(ach64, 4),
+                                    "fp64_peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+                                    "ratio_to_fp64_peak": round(ach64 / fp64_peak, 4)},
+                "hbm": hbm}
+    return {"bound": "fp64", "kernel": dom, "achieved": round(ach64, 4), "peak": round(fp64_peak, 4),
+            "unit": "TFLOP/s", "frac": round(ach64 / fp64_peak, 4), "traffic": None,
+            "peak_source": "of measured: fb_probe_fp64 DFMA chains in this run",
+            "flops_per_launch": fl64, "avg_launch_ms": round(dom_ms, 4), "hbm": hbm}
+
+
+P_HARTREE = 14.39975 / 0.529177          # eV (P_eq2 / P_abohr)
+HA_PER_BOHR = P_HARTREE / 0.529177       # eV/Angstrom per Ha/bohr
+
+
+def mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T, steps, epochs, tol_ha=1e-5):
+    """Table vs MLP-3c on the current system: train the surrogate on the GPU
+    (2^22 samples of the FP64 table interpolator), validate it per bin, then
+    time the assembly + force step with the table path, the gated MLP path
+    (|dH| <= tol_ha in the worst case) and the ungated MLP path, and measure
+    each one's errors against the table path (which equals the FP64 oracle
+    to 1e-10 eV)."""
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.mlp_init(seed=2026)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = ctx.mlp_train(nsamples=1 << 22, epochs=epochs, batch=4096, lr=2e-3, seed=7)
+    train_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    max_bin_err = ctx.mlp_validate(samples_per_bin=64, seed=11)
+    val_s = time.perf_counter() - t0
+    bins = ctx.mlp_bin_errors()
+    used = bins[bins > 0]
+    what = fbgpu.FB_ALL | fbgpu.FB_FORCES
+    timed = make_timer(torch, ctx, stream, flush, ws, local)
+
+    def step():
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.assemble_graph(what)
+
+    def run(mode, tol=None):
+        info = {}
+        if mode == fbgpu.FB_MLP_GATED:
+            tau, cov = ctx.mlp_gate(tol)
+            info.update(tol_ha=tol, tau_table_units=tau, coverage=round(cov, 6))
+        else:
+            ctx.mlp_set_mode(mode)
+        for _ in range(2):
+            step()
+        ms, launches = timed(step, steps)
+        out = {k: ctx.blocks(k) for k in ("S", "vna")}
+        out["ftot"] = ctx.forces("ftot")
+        info.update(ms_per_step=round(ms / steps, 4), value=round(P * steps / (ms * 1e-3), 1),
+                    gpu_launches_per_step=launches // steps, triplets_to_network=ctx.mlp_routed()[0])
+        return info, out
+
+    table, ref = run(fbgpu.FB_MLP_OFF)
+    res = {"table": table}
+    for name, mode, tol in (("mlp_gated", fbgpu.FB_MLP_GATED, tol_ha), ("mlp_all", fbgpu.FB_MLP_ALL, None)):
+        info, out = run(mode, tol)
+        dH = (out["vna"] - ref["vna"]) / P_HARTREE
+        dS = out["S"] - ref["S"]
+        dF = (out["ftot"] - ref["ftot"]) / HA_PER_BOHR
+        info.update(max_abs_dH_ha=float(np.abs(dH).max()), rms_dH_ha=float(np.sqrt(np.mean(dH * dH))),
+                    max_abs_dS=float(np.abs(dS).max()), rms_dS=float(np.sqrt(np.mean(dS * dS))),
+                    max_abs_dF_ha_per_bohr=float(np.abs(dF).max()),
+                    rms_dF_ha_per_bohr=float(np.sqrt(np.mean(dF * dF))),
+                    speedup_vs_table=round(table["ms_per_step"] / info["ms_per_step"], 4))
+        res[name] = info
+    # per-kernel device times of the ungated MLP path through the separate calls
+    ctx.mlp_set_mode(fbgpu.FB_MLP_ALL)
+
+    def kstep():
+        ctx.assemble(fbgpu.FB_ALL)
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.Dassemble(fbgpu.FB_ALL)
+    kstep()
+    timed(kstep, steps, timing=True)
+    res["mlp_all"]["kernels_ms_per_step"] = {k: round(v[0] / steps, 4) for k, v in ctx.timing().items() if v[1]}
+    ctx.set_timing(False)
+    ctx.mlp_set_mode(fbgpu.FB_MLP_OFF)
+    res["training"] = {"samples": 1 << 22, "epochs": epochs, "batch": 4096, "seconds": round(train_s, 2),
+                       "loss_first_last": [float(hist[0]), float(hist[-1])],
+                       "validation_seconds": round(val_s, 2), "bins": int(len(used)),
+                       "bin_error_table_units": {"max": float(max_bin_err), "median": float(np.median(used)),
+                                                 "p10": float(np.quantile(used, 0.1))}}
+    res["network"] = "3 inputs (each a BF16 hi/lo pair) + 16-float species-triple embedding, 3 x 128 SiLU, " \
+                     "50 Legendre coefficients; BF16 weights, FP32 accumulation (mma.sync m16n8k16)"
+    return res
 
 
 def run_gpu(args):
@@ -321,11 +431,12 @@ def run_gpu(args):
     per_step = ms / args.steps
     value = ws * P * args.steps / (ms * 1e-3)
     e2e_value = ws * P * args.steps / (ms_e2e * 1e-3)
-    roof = roofline_for(ctx, ktimes, T, P, st.natoms, nZ, args.steps)
+    roof = roofline_for(ctx, ktimes, T, P, st.natoms, nZ, args.steps, args.prec)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f64 (three-center: double-float f32x2)",
+        "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
                    "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
@@ -340,6 +451,9 @@ def run_gpu(args):
         "roofline": roof,
         "clocks": clk,
     }
+    if args.mlp_epochs > 0:
+        line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
+                                    args.steps, args.mlp_epochs)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.workload, path, nZ, st, P)
     if rank == 0:
@@ -480,7 +594,7 @@ def run_batch(args, torch, fbgpu, ws, rank, local):
     ms_k, _ = timed(kernel_step, args.steps, timing=True)
     ktimes = ctx.timing()
     ctx.set_timing(False)
-    roof = roofline_for(ctx, ktimes, T, P, natoms, nZ, args.steps)
+    roof = roofline_for(ctx, ktimes, T, P, natoms, nZ, args.steps, args.prec)
     per_step = ms / args.steps
     sizes = np.diff(off["atom"])
     line = {
@@ -621,6 +735,9 @@ def main():
     ap.add_argument("--workload", default="si512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--mlp-epochs", type=int, default=12,
+                    help="train the MLP-3c surrogate this many epochs over 2^22 samples and compare it with the "
+                         "table path (0: skip)")
     ap.add_argument("--prec", default="df", choices=["df", "fp64"],
                     help="three-center arithmetic: double-float on the FP32 pipe (default) or FP64")
     args = ap.parse_args()

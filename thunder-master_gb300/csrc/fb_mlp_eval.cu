@@ -96,9 +96,10 @@ __device__ __forceinline__ void hidden_layer(const __nv_bfloat16 *in, __nv_bfloa
       for (int q = 0; q < 4; q++) {
         int r = g + (q >= 2 ? 8 : 0), n = ng * 32 + 8 * j + 2 * t + (q & 1);
         float z = acc[0][j][q] + b[n];
-        outb[r * WSH + n] = __float2bfloat16_rn(silu(z));
+        float sg = sigmoid(z);
+        outb[r * WSH + n] = __float2bfloat16_rn(z * sg);
         if (MT > 1) {
-          float ds = dsilu(z);
+          float ds = sg * (1.0f + z * (1.0f - sg));
 #pragma unroll
           for (int m = 1; m < MT; m++) outb[(16 * m + r) * WSH + n] = __float2bfloat16_rn(ds * acc[m][j][q]);
         }
@@ -223,9 +224,10 @@ __global__ void __launch_bounds__(32 * EvalShape<NTAN>::warps) k_mlp_eval(MlpEva
         for (int q = 0; q < 4; q++) {
           int h2 = q >= 2 ? 1 : 0, r = g + 8 * h2, n = ng * 32 + 8 * j + 2 * t + (q & 1);
           float z = acc[j][q] + bias[n];
-          act1[r * WSH + n] = __float2bfloat16_rn(silu(z));
+          float sg = sigmoid(z);
+          act1[r * WSH + n] = __float2bfloat16_rn(z * sg);
           if (NTAN) {
-            float ds = dsilu(z);
+            float ds = sg * (1.0f + z * (1.0f - sg));
             act1[(16 + r) * WSH + n] = __float2bfloat16_rn(ds * w1t[n] * sxg[h2]);
             act1[(32 + r) * WSH + n] = __float2bfloat16_rn(ds * w1t[MLP_H + n] * syg[h2]);
             act1[(48 + r) * WSH + n] = __float2bfloat16_rn(ds * w1t[2 * MLP_H + n]);

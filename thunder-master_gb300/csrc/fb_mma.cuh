@@ -32,6 +32,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 }
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + __expf(-z)); }
 // d silu / dz = s (1 + z (1 - s)), s = sigmoid(z)
 __device__ __forceinline__ float dsilu(float z) {
   float s = 1.0f / (1.0f + __expf(-z));

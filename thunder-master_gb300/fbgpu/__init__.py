@@ -108,7 +108,8 @@ _SIGS = {
 FB_PREC_FP64, FB_PREC_DF = 0, 1
 
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
-           "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho")
+           "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
+           "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp")
 
 
 class FBError(RuntimeError):
