@@ -319,8 +319,12 @@ def mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T
 
     table, ref = run(fbgpu.FB_MLP_OFF)
     res = {"table": table}
-    for name, mode, tol in (("mlp_gated", fbgpu.FB_MLP_GATED, tol_ha), ("mlp_all", fbgpu.FB_MLP_ALL, None)):
+    for name, mode, tol, engine in (("mlp_gated", fbgpu.FB_MLP_GATED, tol_ha, fbgpu.FB_MLP_ENGINE_TC),
+                                    ("mlp_all", fbgpu.FB_MLP_ALL, None, fbgpu.FB_MLP_ENGINE_TC),
+                                    ("mlp_all_mma_sync", fbgpu.FB_MLP_ALL, None, fbgpu.FB_MLP_ENGINE_MMA)):
+        ctx.mlp_set_engine(engine)
         info, out = run(mode, tol)
+        info["engine"] = "tcgen05 (TMEM)" if engine == fbgpu.FB_MLP_ENGINE_TC else "mma.sync"
         dH = (out["vna"] - ref["vna"]) / P_HARTREE
         dS = out["S"] - ref["S"]
         dF = (out["ftot"] - ref["ftot"]) / HA_PER_BOHR
@@ -331,6 +335,7 @@ def mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T
                     speedup_vs_table=round(table["ms_per_step"] / info["ms_per_step"], 4))
         res[name] = info
     # per-kernel device times of the ungated MLP path through the separate calls
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_TC)
     ctx.mlp_set_mode(fbgpu.FB_MLP_ALL)
 
     def kstep():
@@ -348,7 +353,8 @@ def mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T
                        "bin_error_table_units": {"max": float(max_bin_err), "median": float(np.median(used)),
                                                  "p10": float(np.quantile(used, 0.1))}}
     res["network"] = "3 inputs (each a BF16 hi/lo pair) + 16-float species-triple embedding, 3 x 128 SiLU, " \
-                     "50 Legendre coefficients; BF16 weights, FP32 accumulation (mma.sync m16n8k16)"
+                     "50 Legendre coefficients; BF16 weights, FP32 accumulation; evaluated on tcgen05 " \
+                     "(UMMA 128xNx16, TMEM accumulators), trained with mma.sync m16n8k16 GEMMs"
     return res
 
 

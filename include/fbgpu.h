@@ -310,6 +310,13 @@ int fb_mlp_set_mode(fb_ctx *ctx, int mode);
  * with derivs out[n][4][10] = value, d/dcos, d/dx, d/dy. */
 int fb_mlp_eval_points(fb_ctx *ctx, int n, const float *pts, const int *triple,
                        int derivs, float *out);
+/* Tensor-core engine of the network evaluation in the assembly:
+ * FB_MLP_ENGINE_MMA (warp-level mma.sync BF16) or FB_MLP_ENGINE_TC (tcgen05
+ * UMMA with TMEM accumulators, one thread per triplet; the default).  Same
+ * contract and results up to FP32 summation order. */
+#define FB_MLP_ENGINE_MMA 0
+#define FB_MLP_ENGINE_TC 1
+int fb_mlp_set_engine(fb_ctx *ctx, int engine);
 /* triplets the network takes in the current mode, and all triplets */
 int fb_mlp_routed(const fb_ctx *ctx, int *n_mlp, int *n_total);
 

@@ -190,3 +190,47 @@ def test_mlp_forces_track_table_forces(mlp_sys):
     f3ref = f["f3naa"] + f["f3nab"] + f["f3nac"]
     rel = np.linalg.norm(f3 - f3ref) / np.linalg.norm(f3ref)
     assert rel < 0.3, rel
+
+
+def test_tcgen05_engine_matches_mma(mlp_sys):
+    """The tcgen05 evaluation (TMEM accumulators) against the mma.sync one:
+    the same network and roundings, FP32 sums in another order."""
+    import fbgpu
+    from fbgpu import synth
+    ctx = mlp_sys["ctx"]
+    sp = synth.species_for("sic4096")
+    rng = np.random.default_rng(12)
+    n = 300   # not a multiple of 128: a partial tile
+    trip = rng.integers(0, 8, n)
+    xmax = np.array([sp[t % 2].rcA + max(sp[t // 4].rcA, sp[(t // 2) % 2].rcA) for t in trip])
+    ymax = np.array([sp[t // 4].rcA + sp[(t // 2) % 2].rcA for t in trip])
+    pts = np.stack([rng.uniform(0.02, 0.98, n) * xmax, rng.uniform(0.02, 0.98, n) * ymax,
+                    rng.uniform(-1, 1, n)], 1)
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_MMA)
+    ref = ctx.mlp_eval_points(pts, trip)
+    ref0 = ctx.mlp_eval_points(pts, trip, derivs=False)
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_TC)
+    got = ctx.mlp_eval_points(pts, trip)
+    got0 = ctx.mlp_eval_points(pts, trip, derivs=False)
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_MMA)
+    for k in range(4):
+        s = np.abs(ref[:, k]).max()
+        assert np.abs(got[:, k] - ref[:, k]).max() <= 2e-2 * s, k
+        assert np.abs(got[:, k] - ref[:, k]).mean() <= 2e-3 * s, k
+    assert np.abs(got0 - ref0).max() <= 2e-2 * np.abs(ref0).max()
+    assert np.abs(got0 - got[:, 0]).max() <= 2e-2 * np.abs(ref0).max()
+
+
+def test_tcgen05_engine_in_the_assembly(mlp_sys):
+    import fbgpu
+    ctx = mlp_sys["ctx"]
+    ctx.mlp_set_mode(fbgpu.FB_MLP_ALL)
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_MMA)
+    a = _run(ctx, mlp_sys["rho"], mlp_sys["cape"])
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_TC)
+    b = _run(ctx, mlp_sys["rho"], mlp_sys["cape"])
+    ctx.mlp_set_engine(fbgpu.FB_MLP_ENGINE_MMA)
+    ctx.mlp_set_mode(fbgpu.FB_MLP_OFF)
+    v0 = mlp_sys["blocks"][2]
+    assert np.abs(b["vna"] - a["vna"]).max() <= 0.05 * np.abs(a["vna"] - v0).max() + 1e-9
+    assert np.linalg.norm(b["ftot"] - a["ftot"]) <= 0.05 * np.linalg.norm(a["ftot"])

@@ -64,6 +64,7 @@ struct fb_ctx {
   DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
+  DevBuf d_slot_off, d_slot_nn, d_slot_found;
   DevBuf d_status, d_errinfo;
   // blocks
   DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df;
@@ -81,7 +82,7 @@ struct fb_ctx {
   // maps of the same sizes reuse it).
   cudaGraphExec_t gexec = nullptr;
   unsigned g_what = 0;
-  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1;
+  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1, g_mlp_engine = -1;
   long long g_nblock = -1, g_alloc = -1, g_launches = 0;
   cudaStream_t g_stream = nullptr;
   KCfg g_cfg[TK_N];
@@ -94,6 +95,7 @@ struct fb_ctx {
   DevBuf d_binok, d_mlpF;
   int mlp_n = 0;
   double mlp_tau = 0.0;
+  int mlp_engine = FB_MLP_ENGINE_TC;
   // per-kernel CUDA-event timing (fb_set_timing)
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evpool;
@@ -178,6 +180,7 @@ static int status_error(fb_ctx *ctx, unsigned st) {
   if (st & DEVERR_BACK) return fail(ctx, FB_ERR_NEIGH_BACK, "neigh_back missing or found twice");
   if (st & DEVERR_XLARGE) return fail(ctx, FB_ERR_X_TOO_LARGE, "interaction distance beyond table range");
   if (st & DEVERR_TABLE) return fail(ctx, FB_ERR_TABLE, "table missing");
+  if (st & DEVERR_WATCHDOG) return fail(ctx, FB_ERR_WATCHDOG, "a tensor-core product did not complete in time");
   return FB_OK;
 }
 
@@ -222,7 +225,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
                     &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm,
-                    &ctx->d_thist, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
+                    &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
@@ -467,6 +470,9 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.cj_b = ctx->d_cj_b.as<int>();
   a.cneigh = ctx->d_cneigh.as<int>();
   a.tdst = ctx->d_tdst.as<int>();
+  a.slot_off = ctx->d_slot_off.as<long long>();
+  a.slot_nn = ctx->d_slot_nn.as<unsigned>();
+  a.slot_found = ctx->d_slot_found.as<int>();
   a.status = ctx->d_status.as<unsigned>();
   a.errinfo = ctx->d_errinfo.as<int>();
   return a;
@@ -516,17 +522,26 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
   NeighArgs a = neigh_args(ctx);
   KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
+  // common neighbors: slots for every ordered pair of ialpha's non-self neighbors
+  std::vector<long long> soff(N + 1, 0);
+  for (int i = 0; i < N; i++) {
+    long long n = ctx->h_pair_off[i + 1] - ctx->h_pair_off[i] - 1;  // non-self neighbors
+    if (n > 65535) return fail(ctx, FB_ERR_CAPACITY, "atom %d has %lld neighbors (at most 65536)", i + 1, n + 1);
+    soff[i + 1] = soff[i] + (n > 1 ? n * (n - 1) : 0);
+  }
+  CHK(ctx->d_tcnt.ensure(N * sizeof(int)));
+  CHK(ctx->d_slot_off.ensure((N + 1) * sizeof(long long)));
+  CHK(ctx->d_slot_nn.ensure((size_t)soff[N] * sizeof(unsigned) + 4));
+  CHK(ctx->d_slot_found.ensure((size_t)soff[N] * sizeof(int) + 4));
+  CU(cudaMemcpyAsync(ctx->d_slot_off.p, soff.data(), (N + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  a = neigh_args(ctx);
+  KL(KT_COMMON_COUNT, launch_common(a, ctx->stream));
+  std::vector<int> tc(N);
+  CU(cudaMemcpyAsync(tc.data(), ctx->d_tcnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
-  // common neighbors
-  CHK(ctx->d_tcnt.ensure(N * sizeof(int)));
-  a = neigh_args(ctx);
-  KL(KT_COMMON_COUNT, launch_common(a, false, ctx->stream));
-  std::vector<int> tc(N);
-  CU(cudaMemcpyAsync(tc.data(), ctx->d_tcnt.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
-  if (ctx->timing) timing_drain(ctx);
   ctx->h_trip_off.assign(N + 1, 0);
   for (int i = 0; i < N; i++) ctx->h_trip_off[i + 1] = ctx->h_trip_off[i] + tc[i];
   int T = ctx->h_trip_off[N];
@@ -543,7 +558,7 @@ static int finish_neighbors(fb_ctx *ctx) {
   CU(cudaMemcpyAsync(ctx->d_trip_off.p, ctx->h_trip_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice,
                      ctx->stream));
   a = neigh_args(ctx);
-  KL(KT_COMMON_FILL, launch_common(a, true, ctx->stream));
+  KL(KT_COMMON_FILL, launch_common_compact(a, ctx->stream));
   ctx->mlp_cells = trip_cells(ctx);
   // triplet processing order, binned by (species triple, 3c grid cell)
   CHK(bin_triplets(ctx));
@@ -553,8 +568,6 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_T.ensure(bb));
   CHK(ctx->d_vb.ensure(bb));
   CHK(ctx->d_vbo.ensure(bb));
-  CU(cudaStreamSynchronize(ctx->stream));
-  if (ctx->timing) timing_drain(ctx);
   ctx->have_neigh = true;
   ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = false;
   ctx->assembled = ctx->dassembled = 0;
@@ -833,6 +846,11 @@ static MlpEvalArgs mlp_eval_args(fb_ctx *ctx) {
   return m;
 }
 
+static int mlp_launch(fb_ctx *ctx, const MlpEvalArgs &m, const AsmArgs &a, bool tangents) {
+  if (ctx->mlp_engine == FB_MLP_ENGINE_TC) return launch_mlp_tc(m, a, tangents, ctx->nsm, ctx->stream);
+  return launch_mlp_eval(m, a, tangents, ctx->nsm, ctx->stream);
+}
+
 static int prepare_mlp(fb_ctx *ctx, bool forces) {
   if (mlp_routes(ctx) && ctx->mlp_n > 0)
     CHK(ctx->d_mlpF.ensure((size_t)ctx->mlp_n * (forces ? 4 : 1) * MLP_ME_STRIDE * sizeof(float)));
@@ -853,7 +871,7 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
     else KL(KT_ASM3C, launch_assemble_3c(at, ctx->stream));
     if (nm > 0) {
-      KL(KT_MLP_EVAL, launch_mlp_eval(mlp_eval_args(ctx), a, false, ctx->nsm, ctx->stream));
+      KL(KT_MLP_EVAL, mlp_launch(ctx, mlp_eval_args(ctx), a, false));
       AsmArgs am = a;
       am.ntrip = nm;
       am.mlpF = ctx->d_mlpF.as<float>();
@@ -998,7 +1016,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     if (use_df(ctx)) KL(KT_DASM3C, launch_dassemble_3c_df(at, ctx->stream));
     else KL(KT_DASM3C, launch_dassemble_3c(at, ctx->stream));
     if (nm > 0) {
-      KL(KT_MLP_EVAL, launch_mlp_eval(mlp_eval_args(ctx), a, true, ctx->nsm, ctx->stream));
+      KL(KT_MLP_EVAL, mlp_launch(ctx, mlp_eval_args(ctx), a, true));
       AsmArgs am = a;
       am.ntrip = nm;
       am.mlpF = ctx->d_mlpF.as<float>();
@@ -1075,6 +1093,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   ctx->g_have_d = ctx->fdh.have_d;
   ctx->g_mlp_n = ctx->mlp_n;
   ctx->g_mlp_mode = ctx->mlp_mode;
+  ctx->g_mlp_engine = ctx->mlp_engine;
   ctx->g_alloc = g_alloc_gen.load();
   ctx->g_stream = ctx->stream;
   for (int k = 0; k < TK_N; k++) ctx->g_cfg[k] = ctx->cfg[k];
@@ -1093,6 +1112,7 @@ int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
                ctx->g_P == ctx->P && ctx->g_T == ctx->T && ctx->g_nblock == ctx->nblock &&
                ctx->g_have_d == ctx->fdh.have_d && ctx->g_alloc == g_alloc_gen.load() &&
                ctx->g_mlp_n == ctx->mlp_n && ctx->g_mlp_mode == ctx->mlp_mode &&
+               ctx->g_mlp_engine == ctx->mlp_engine &&
                ctx->g_stream == ctx->stream && same_cfg(ctx->g_cfg, ctx->cfg);
   if (!fresh) CHK(capture_graph(ctx, what));
   CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
@@ -1558,13 +1578,19 @@ int fb_mlp_eval_points(fb_ctx *ctx, int n, const float *pts, const int *triple, 
   m.ptrip = t.as<int>();
   m.out = o.as<float>();
   AsmArgs a = asm_args(ctx);
-  KL(KT_MLP_EVAL, launch_mlp_eval(m, a, derivs != 0, ctx->nsm, ctx->stream));
+  KL(KT_MLP_EVAL, mlp_launch(ctx, m, a, derivs != 0));
   CU(cudaMemcpyAsync(out, o.p, (size_t)n * rows * MLP_ME_STRIDE * sizeof(float), cudaMemcpyDeviceToHost,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   p.release();
   t.release();
   o.release();
+  return FB_OK;
+}
+
+int fb_mlp_set_engine(fb_ctx *ctx, int engine) {
+  if (!ctx || (engine != FB_MLP_ENGINE_MMA && engine != FB_MLP_ENGINE_TC)) return FB_ERR_ARG;
+  ctx->mlp_engine = engine;
   return FB_OK;
 }
 

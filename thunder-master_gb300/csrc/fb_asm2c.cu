@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(256) k_assemble_2c(Ctx2c c, unsigned what, Sch
 // build_forces, assembly terms (c.SYSTEM/M_build_forces.f90:172-588).  The
 // j-side contribution of pair (i -> j) is gathered by atom j through
 // neigh_back, which maps j's own pair list one-to-one onto the pairs whose
-// neighbor is j, so no atomics are needed.
+// neighbor is j, so no atomics are needed.  One warp per atom, lanes over
+// its pairs, a warp reduction of the nine sums.
 __global__ void k_build_forces(int N, const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                                const int *__restrict__ neigh_back, const double *__restrict__ sumT,
                                const double *__restrict__ sumS, const double *__restrict__ ontop,
@@ -129,10 +130,11 @@ __global__ void k_build_forces(int N, const int *__restrict__ pair_off, const in
                                const double *__restrict__ f3b, const double *__restrict__ f3c,
                                double *__restrict__ kin, double *__restrict__ vna, double *__restrict__ pul,
                                double *__restrict__ ftot, unsigned what) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
   if (i >= N) return;
   double k[3] = {0, 0, 0}, v[3] = {0, 0, 0}, pu[3] = {0, 0, 0};
-  for (int p = pair_off[i]; p < pair_off[i + 1]; p++) {
+  for (int p = pair_off[i] + lane; p < pair_off[i + 1]; p += 32) {
     int j = neigh_j[p];
     int pb = pair_off[j] + neigh_back[p];  // pair (j -> i)
 #pragma unroll
@@ -143,12 +145,22 @@ __global__ void k_build_forces(int N, const int *__restrict__ pair_off, const in
     }
   }
 #pragma unroll
-  for (int q = 0; q < 3; q++) {
-    kin[3 * i + q] = k[q];
-    vna[3 * i + q] = v[q];
-    pul[3 * i + q] = pu[q];
-    double f3 = (what & 8u) ? f3a[3 * i + q] + f3b[3 * i + q] + f3c[3 * i + q] : 0.0;
-    ftot[3 * i + q] = k[q] + v[q] + f3 - pu[q];
+  for (int q = 0; q < 3; q++)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      k[q] += __shfl_xor_sync(0xffffffffu, k[q], off);
+      v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+      pu[q] += __shfl_xor_sync(0xffffffffu, pu[q], off);
+    }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      kin[3 * i + q] = k[q];
+      vna[3 * i + q] = v[q];
+      pul[3 * i + q] = pu[q];
+      double f3 = (what & 8u) ? f3a[3 * i + q] + f3b[3 * i + q] + f3c[3 * i + q] : 0.0;
+      ftot[3 * i + q] = k[q] + v[q] + f3 - pu[q];
+    }
   }
 }
 
@@ -165,7 +177,7 @@ int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
 }
 
 int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s) {
-  int threads = 128, blocks = (a.N + threads - 1) / threads;
+  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   k_build_forces<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_back, a.sumT, a.sumS, a.ontop,
                                             a.atomf, a.f3naa, a.f3nab, a.f3nac, a.kin, a.vna, a.pul, a.ftot, what);
   FB_LAUNCH_CHECK();

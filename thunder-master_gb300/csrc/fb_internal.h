@@ -179,6 +179,7 @@ enum : unsigned {
   DEVERR_BACK = 8u,
   DEVERR_TABLE = 16u,
   DEVERR_CAP = 32u,
+  DEVERR_WATCHDOG = 64u,  // a bounded device wait ran out
 };
 
 }  // namespace fb

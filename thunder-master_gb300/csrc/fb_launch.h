@@ -48,6 +48,10 @@ struct NeighArgs {
   int *tcnt;
   const int *trip_off;
   int *ci_j, *ci_b, *cj_j, *cj_b, *cneigh, *tdst;
+  // common-neighbor slots: ialpha's kept (ineigh, jneigh) pairs and matches
+  const long long *slot_off;
+  unsigned *slot_nn;
+  int *slot_found;
   unsigned *status;
   int *errinfo;
 };
@@ -84,7 +88,10 @@ struct AsmArgs {
 
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s);
 int launch_neigh_back(const NeighArgs &a, cudaStream_t s);
-int launch_common(const NeighArgs &a, bool fill, cudaStream_t s);
+// common neighbors: the search into per-ialpha slots (+ counts), then the
+// compaction into the CSR triplet lists at trip_off
+int launch_common(const NeighArgs &a, cudaStream_t s);
+int launch_common_compact(const NeighArgs &a, cudaStream_t s);
 // counting sort of the triplets by (species triple, 3c grid cell) -> perm;
 // bins with binok[bin] set (may be null) come first; hist has 2 x nbins
 // entries and holds the exclusive bin starts afterwards
@@ -105,6 +112,8 @@ int launch_assemble_3c_mlp(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s);
 struct MlpEvalArgs;
 int launch_mlp_eval(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
+// the same on the tcgen05 tensor cores (TMEM accumulators)
+int launch_mlp_tc(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
 // DFMA throughput probe: one warm-up and one timed launch
 int probe_dfma(cudaStream_t s, double *ms, double *flops);
 int probe_ffma(cudaStream_t s, double *ms, double *flops);

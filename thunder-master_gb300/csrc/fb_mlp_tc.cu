@@ -1,0 +1,326 @@
+// fb_mlp_tc.cu -- MLP-3c evaluation on the Blackwell tensor cores
+// (tcgen05.mma kind::f16, BF16 operands from shared memory, FP32
+// accumulators in TMEM).  Same contract as k_mlp_eval (fb_mlp_eval.cu):
+// per triplet of the list, the Legendre-combined values of getMEs_Fdata_3c
+// (e.FDATA/M_Fdata_3c.f90:293-517) and, with tangents, their cos / x / y
+// derivatives (getDMEs_Fdata_3c, :549-846).
+//
+// A CTA works on tiles of 128 triplets, one thread per triplet: thread t
+// owns row t of every operand and TMEM lane t of every accumulator, so the
+// epilogue of a layer (bias, SiLU, the tangents' silu'(z) factor, BF16
+// conversion into the next layer's operand) needs no data exchange.  The
+// three tangents d/dx, d/dy, d/dcos are three more 128-row operands of the
+// same products; their layer-1 pre-activations are columns of W1 times the
+// input derivative and need no product.  One thread issues the MMAs of a
+// layer and commits them to an mbarrier the CTA waits on (bounded).
+#include "fb_common_df.cuh"
+#include "fb_mlp.h"
+#include "fb_mma.cuh"
+#include "fb_tc.cuh"
+
+namespace fb {
+
+namespace {
+
+// shared-memory plan (bytes): the network's weights, the input rows, the
+// hidden operands, the mbarrier and the TMEM address slot
+template <int NTAN, int TILES>
+struct TcShape {
+  static constexpr int MT = 1 + NTAN;  // operands per tile: primal + tangents
+  static constexpr int w1 = 0;
+  static constexpr int w2 = w1 + MLP_H * MLP_IN * 2;
+  static constexpr int w3 = w2 + MLP_H * MLP_H * 2;
+  static constexpr int w4 = w3 + MLP_H * MLP_H * 2;
+  static constexpr int x = w4 + MLP_OUT * MLP_H * 2;
+  static constexpr int h = x + TILES * 128 * MLP_IN * 2;
+  static constexpr int bar = h + TILES * MT * 128 * MLP_H * 2;
+  static constexpr int smem = bar + 16;
+  static constexpr int threads = 128 * TILES;
+  static constexpr int cols = TILES * MT * 128;  // TMEM columns (a power of 2)
+};
+static_assert(TcShape<3, 1>::smem <= 232448, "tangent plan exceeds 227 KB of shared memory");
+static_assert(TcShape<0, 2>::smem <= 232448, "value plan exceeds 227 KB of shared memory");
+static_assert(TcShape<3, 1>::cols == 512 && TcShape<0, 2>::cols == 256, "TMEM columns");
+
+constexpr long long TC_WAIT_LIMIT = 1LL << 22;  // mbarrier polls before the kernel gives up
+
+}  // namespace
+
+template <int NTAN, int TILES>
+__global__ void __launch_bounds__(128 * TILES, 1) k_mlp_tc(MlpEvalArgs a, Ctx3c c, unsigned *status) {
+  using S = TcShape<NTAN, TILES>;
+  constexpr int MT = S::MT;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __nv_bfloat16 *W1s = reinterpret_cast<__nv_bfloat16 *>(smem + S::w1);
+  __nv_bfloat16 *W2s = reinterpret_cast<__nv_bfloat16 *>(smem + S::w2);
+  __nv_bfloat16 *W3s = reinterpret_cast<__nv_bfloat16 *>(smem + S::w3);
+  __nv_bfloat16 *W4s = reinterpret_cast<__nv_bfloat16 *>(smem + S::w4);
+  __nv_bfloat16 *Xs = reinterpret_cast<__nv_bfloat16 *>(smem + S::x);
+  __nv_bfloat16 *Hs = reinterpret_cast<__nv_bfloat16 *>(smem + S::h);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S::bar);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::bar + 8);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tt = tid >> 7, row = tid & 127;  // tile within the CTA, row within the tile
+
+  // the network in the canonical operand layout
+  const __nv_bfloat16 *gw = a.wbf;
+  for (int i = tid; i < MLP_H * MLP_IN; i += S::threads) W1s[canon_off(i / MLP_IN, i % MLP_IN, MLP_IN)] = gw[i];
+  gw += MLP_H * MLP_IN;
+  for (int i = tid; i < MLP_H * MLP_H; i += S::threads) W2s[canon_off(i / MLP_H, i % MLP_H, MLP_H)] = gw[i];
+  gw += MLP_H * MLP_H;
+  for (int i = tid; i < MLP_H * MLP_H; i += S::threads) W3s[canon_off(i / MLP_H, i % MLP_H, MLP_H)] = gw[i];
+  gw += MLP_H * MLP_H;
+  for (int i = tid; i < MLP_OUT * MLP_H; i += S::threads) W4s[canon_off(i / MLP_H, i % MLP_H, MLP_H)] = gw[i];
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tslot, S::cols);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
+  const float *P = a.params;
+  const float *b1 = P + a.o_b1, *b2 = P + a.o_b2, *b3 = P + a.o_b3, *b4 = P + a.o_b4;
+  const FdataDev &fd = *c.fd;
+  constexpr uint32_t ID128 = umma_idesc_bf16(128, MLP_H), ID64 = umma_idesc_bf16(128, MLP_OUT);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int ntiles = (a.n + 127) / 128;
+
+  for (int t0 = blockIdx.x * TILES; t0 < ntiles; t0 += gridDim.x * TILES) {
+    const int i = (t0 + tt) * 128 + row;
+    const bool valid = i < a.n;
+    // ---- inputs: the triplet's coordinates (BF16 hi/lo pairs) and embedding
+    float f[3] = {0.0f, 0.0f, 0.0f}, sx = 0.0f, sy = 0.0f;
+    int tr = 0;
+    if (valid && a.pts) {
+      tr = a.ptrip[i];
+      const Cell3cDev &cell = fd.c3[tr / (a.nsp * a.nsp)][(tr / a.nsp) % a.nsp][tr % a.nsp];
+      sx = (float)(2.0 / cell.xmax);
+      sy = (float)(2.0 / cell.ymax);
+      f[0] = (float)(a.pts[3 * i] * (2.0 / cell.xmax) - 1.0);
+      f[1] = (float)(a.pts[3 * i + 1] * (2.0 / cell.ymax) - 1.0);
+      f[2] = a.pts[3 * i + 2];
+    } else if (valid) {
+      GeomFP64 h;
+      trip_geom_fp64(c, a.list[i], h);
+      int ka = c.isp[h.iat], kb = c.isp[h.jat], kc = c.isp[h.ia];
+      const Cell3cDev &cell = fd.c3[ka][kb][kc];
+      tr = (ka * a.nsp + kb) * a.nsp + kc;
+      sx = (float)(2.0 / cell.xmax);
+      sy = (float)(2.0 / cell.ymax);
+      f[0] = (float)(h.x * (2.0 / cell.xmax) - 1.0);
+      f[1] = (float)(h.z * (2.0 / cell.ymax) - 1.0);
+      f[2] = trip_cost_df(h).h;
+    }
+    {
+      __nv_bfloat16 *X = Xs + tt * 128 * MLP_IN;
+      const float *em = P + a.o_emb + tr * MLP_EMB;
+#pragma unroll
+      for (int k = 0; k < MLP_IN; k++) {
+        float v = 0.0f;
+        if (k < 3) v = f[k];
+        else if (k < 3 + MLP_EMB) v = em[k - 3];
+        else if (k < MLP_LO + 3) v = f[k - MLP_LO] - __bfloat162float(__float2bfloat16_rn(f[k - MLP_LO]));
+        X[canon_off(row, k, MLP_IN)] = __float2bfloat16_rn(v);
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- layer 1 (K = 32): primal only --------------------------------------
+    if (tid == 0) {
+      for (int q = 0; q < TILES; q++) {
+        uint32_t xa = smem_u32(Xs + q * 128 * MLP_IN), wb = smem_u32(W1s);
+        for (int ks = 0; ks < MLP_IN / 16; ks++)
+          umma_bf16(tmem + q * MT * 128, umma_desc(xa + ks * 256, 128, (MLP_IN / 8) * 128),
+                    umma_desc(wb + ks * 256, 128, (MLP_IN / 8) * 128), ID128, ks > 0);
+      }
+      umma_commit(bar);
+    }
+    ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+    phase ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    __nv_bfloat16 *H = Hs + tt * MT * 128 * MLP_H;
+    const uint32_t dbase = tmem + lane_base + tt * MT * 128;
+#pragma unroll 1
+    for (int c0 = 0; c0 < MLP_H; c0 += 16) {
+      float z[16];
+      tmem_ld16(dbase + c0, z);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        int n = c0 + j;
+        float zz = z[j] + b1[n];
+        float sg = sigmoid(zz);
+        int o = canon_off(row, n, MLP_H);
+        H[o] = __float2bfloat16_rn(zz * sg);
+        if (NTAN) {
+          float ds = sg * (1.0f + zz * (1.0f - sg));
+          const __nv_bfloat16 *w1r = a.wbf + n * MLP_IN;
+          H[1 * 128 * MLP_H + o] = __float2bfloat16_rn(ds * __bfloat162float(w1r[0]) * sx);
+          H[2 * 128 * MLP_H + o] = __float2bfloat16_rn(ds * __bfloat162float(w1r[1]) * sy);
+          H[3 * 128 * MLP_H + o] = __float2bfloat16_rn(ds * __bfloat162float(w1r[2]));
+        }
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- layers 2 and 3 (K = N = 128) ----------------------------------------
+#pragma unroll 1
+    for (int l = 0; l < 2; l++) {
+      const __nv_bfloat16 *W = l == 0 ? W2s : W3s;
+      const float *bl = l == 0 ? b2 : b3;
+      if (tid == 0) {
+        uint32_t wb = smem_u32(W);
+        for (int q = 0; q < TILES; q++)
+          for (int op = 0; op < MT; op++) {
+            uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
+            for (int ks = 0; ks < MLP_H / 16; ks++)
+              umma_bf16(tmem + (q * MT + op) * 128, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
+                        umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID128, ks > 0);
+          }
+        umma_commit(bar);
+      }
+      ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+      phase ^= 1;
+      if (!ok) break;
+      tc_fence_after();
+#pragma unroll 1
+      for (int c0 = 0; c0 < MLP_H; c0 += 16) {
+        float z[16], ds[16];
+        tmem_ld16(dbase + c0, z);
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          float zz = z[j] + bl[c0 + j];
+          float sg = sigmoid(zz);
+          H[canon_off(row, c0 + j, MLP_H)] = __float2bfloat16_rn(zz * sg);
+          ds[j] = sg * (1.0f + zz * (1.0f - sg));
+        }
+#pragma unroll
+        for (int op = 1; op < MT; op++) {
+          float dz[16];
+          tmem_ld16(dbase + op * 128 + c0, dz);
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            H[op * 128 * MLP_H + canon_off(row, c0 + j, MLP_H)] = __float2bfloat16_rn(ds[j] * dz[j]);
+        }
+      }
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+    }
+    if (!ok) break;
+    // ---- layer 4 (N = 64, 50 used) --------------------------------------------
+    if (tid == 0) {
+      uint32_t wb = smem_u32(W4s);
+      for (int q = 0; q < TILES; q++)
+        for (int op = 0; op < MT; op++) {
+          uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
+          for (int ks = 0; ks < MLP_H / 16; ks++)
+            umma_bf16(tmem + (q * MT + op) * MLP_OUT, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
+                      umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID64, ks > 0);
+        }
+      umma_commit(bar);
+    }
+    ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+    phase ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    // ---- Legendre combination (the reference's P_l(cos theta) sum) ------------
+    {
+      float cth = f[2], c2 = cth * cth;
+      float pl[5] = {1.0f, cth, 0.5f * (3.0f * c2 - 1.0f), 0.5f * cth * (5.0f * c2 - 3.0f),
+                     0.125f * (3.0f - c2 * (30.0f - 35.0f * c2))};
+      float dpl[5] = {0.0f, 1.0f, 3.0f * cth, (15.0f * c2 - 3.0f) * 0.5f, 0.5f * cth * (35.0f * c2 - 15.0f)};
+      const float *sc = a.scale + tr * MLP_OUT;
+      float acc[4][MLP_ME];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int e = 0; e < MLP_ME; e++) acc[q][e] = 0.0f;
+      const uint32_t obase = tmem + lane_base + tt * MT * MLP_OUT;
+#pragma unroll
+      for (int op = 0; op < MT; op++) {
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          float v[16];
+          tmem_ld16(obase + op * MLP_OUT + c0, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int o = c0 + j;
+            if (o < NTHETA * MLP_ME) {
+              const int th = o / MLP_ME, e = o % MLP_ME;
+              float val = (op == 0 ? v[j] + b4[o] : v[j]) * sc[o];
+              if (op == 0) {
+                acc[0][e] = fmaf(pl[th], val, acc[0][e]);
+                acc[1][e] = fmaf(dpl[th], val, acc[1][e]);
+              } else if (op == 1) {
+                acc[2][e] = fmaf(pl[th], val, acc[2][e]);
+              } else if (op == 2) {
+                acc[3][e] = fmaf(pl[th], val, acc[3][e]);
+              } else {
+                acc[1][e] = fmaf(pl[th], val, acc[1][e]);
+              }
+            }
+          }
+        }
+      }
+      if (valid) {
+        if (NTAN) {
+          float *o4 = a.out + (long long)i * 4 * MLP_ME;
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int e = 0; e < MLP_ME; e++) o4[q * MLP_ME + e] = acc[q][e];
+        } else {
+#pragma unroll
+          for (int e = 0; e < MLP_ME; e++) a.out[(long long)i * MLP_ME + e] = acc[0][e];
+        }
+      }
+    }
+    // the next tile's MMAs overwrite the accumulators: all reads done first
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  if (!ok) {
+    // a product never completed: report it, give it one more bounded wait, release TMEM
+    if (tid == 0) atomicOr(status, DEVERR_WATCHDOG);
+    mbar_wait(bar, phase ^ 1, TC_WAIT_LIMIT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, S::cols);
+}
+
+int launch_mlp_tc(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s) {
+  if (m.n == 0) return 0;
+  Ctx3c c = make3c(a);
+  int ntiles = (m.n + 127) / 128;
+  if (tangents) {
+    using S = TcShape<3, 1>;
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::smem);
+    if (e != cudaSuccess) return (int)e;
+    int blocks = ntiles < nsm ? ntiles : nsm;
+    k_mlp_tc<3, 1><<<blocks, S::threads, S::smem, s>>>(m, c, a.status);
+  } else {
+    using S = TcShape<0, 2>;
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::smem);
+    if (e != cudaSuccess) return (int)e;
+    int blocks = (ntiles + 1) / 2 < nsm ? (ntiles + 1) / 2 : nsm;
+    k_mlp_tc<0, 2><<<blocks, S::threads, S::smem, s>>>(m, c, a.status);
+  }
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+}  // namespace fb

@@ -166,17 +166,18 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
 // (jatom, shift(jbeta) - shift(ibeta)); i's list is sorted by (mbeta, jatom),
 // so it is found by binary search and then tested exactly.  When that entry
 // is absent or fails the test, the full scan of the reference decides.
-// Output order matches the reference loops.
-template <bool FILL>
+// Output order matches the reference loops.  One pass: every kept pair
+// (ineigh, jneigh) and its match go to ialpha's slots (slot_off[ialpha],
+// room for all ordered pairs of its non-self neighbors) and the count to
+// tcnt; k_common_compact then packs the slots into the CSR triplet lists.
 __global__ void k_common(int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
                          const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                          const double *__restrict__ xl0,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                          const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
-                         const double *__restrict__ r3v, int *__restrict__ tcnt, const int *__restrict__ trip_off,
-                         int *__restrict__ ci_j, int *__restrict__ ci_b, int *__restrict__ cj_j,
-                         int *__restrict__ cj_b, int *__restrict__ cneigh, int *__restrict__ tdst,
-                         int *__restrict__ talpha) {
+                         const double *__restrict__ r3v, int *__restrict__ tcnt,
+                         const long long *__restrict__ slot_off, unsigned *__restrict__ slot_nn,
+                         int *__restrict__ slot_found) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= N) return;
@@ -184,7 +185,8 @@ __global__ void k_common(int N, const int *__restrict__ speriodic, const double 
   const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
   int periodic = speriodic[sid[ia]];
   int p0 = pair_off[ia], n = pair_off[ia + 1] - p0, self = neigh_self[ia];
-  int num = 0, base = FILL ? trip_off[ia] : 0;
+  int num = 0;
+  long long base = slot_off[ia];
   for (int in = 0; in < n; in++) {
     if (in == self) continue;
     int pi = p0 + in, iat = neigh_j[pi], ib = neigh_b[pi];
@@ -245,20 +247,44 @@ __global__ void k_common(int N, const int *__restrict__ speriodic, const double 
         }
       }
       unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (FILL && keep) {
-        int t = base + num + __popc(m & ((1u << lane) - 1u));
-        ci_j[t] = iat;
-        ci_b[t] = ib;
-        cj_j[t] = jat;
-        cj_b[t] = jb;
-        cneigh[t] = found;
-        tdst[t] = q0 + found;
-        talpha[t] = ia;
+      if (keep) {
+        long long t = base + num + __popc(m & ((1u << lane) - 1u));
+        slot_nn[t] = (unsigned)in | ((unsigned)jn << 16);
+        slot_found[t] = found;
       }
       num += __popc(m);
     }
   }
-  if (!FILL && lane == 0) tcnt[ia] = num;
+  if (lane == 0) tcnt[ia] = num;
+}
+
+// slots -> CSR triplet lists in the reference's field layout (one warp per ialpha)
+__global__ void k_common_compact(int N, const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
+                                 const int *__restrict__ neigh_b, const int *__restrict__ tcnt,
+                                 const long long *__restrict__ slot_off, const unsigned *__restrict__ slot_nn,
+                                 const int *__restrict__ slot_found, const int *__restrict__ trip_off,
+                                 int *__restrict__ ci_j, int *__restrict__ ci_b, int *__restrict__ cj_j,
+                                 int *__restrict__ cj_b, int *__restrict__ cneigh, int *__restrict__ tdst,
+                                 int *__restrict__ talpha) {
+  int ia = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (ia >= N) return;
+  int p0 = pair_off[ia], cnt = tcnt[ia], t0 = trip_off[ia];
+  long long s0 = slot_off[ia];
+  for (int k = lane; k < cnt; k += 32) {
+    unsigned nn = slot_nn[s0 + k];
+    int found = slot_found[s0 + k];
+    int pi = p0 + (int)(nn & 0xffffu), pj = p0 + (int)(nn >> 16);
+    int iat = neigh_j[pi];
+    int t = t0 + k;
+    ci_j[t] = iat;
+    ci_b[t] = neigh_b[pi];
+    cj_j[t] = neigh_j[pj];
+    cj_b[t] = neigh_b[pj];
+    cneigh[t] = found;
+    tdst[t] = pair_off[iat] + found;
+    talpha[t] = ia;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -379,16 +405,19 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
   return 0;
 }
 
-int launch_common(const NeighArgs &a, bool fill, cudaStream_t s) {
+int launch_common(const NeighArgs &a, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
-  if (fill)
-    k_common<true><<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off, a.neigh_j,
-                                              a.neigh_b, a.neigh_self, a.r3v, nullptr, a.trip_off, a.ci_j, a.ci_b,
-                                              a.cj_j, a.cj_b, a.cneigh, a.tdst, a.talpha);
-  else
-    k_common<false><<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off,
-                                               a.neigh_j, a.neigh_b, a.neigh_self, a.r3v, a.tcnt, nullptr,
-                                               nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+  k_common<<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off, a.neigh_j,
+                                      a.neigh_b, a.neigh_self, a.r3v, a.tcnt, a.slot_off, a.slot_nn, a.slot_found);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_common_compact(const NeighArgs &a, cudaStream_t s) {
+  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
+  k_common_compact<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_b, a.tcnt, a.slot_off, a.slot_nn,
+                                              a.slot_found, a.trip_off, a.ci_j, a.ci_b, a.cj_j, a.cj_b, a.cneigh,
+                                              a.tdst, a.talpha);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -36,6 +36,7 @@ LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
 FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
+FB_MLP_ENGINE_MMA, FB_MLP_ENGINE_TC = 0, 1
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
 BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
@@ -77,6 +78,7 @@ _SIGS = {
     "fb_mlp_gate": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
     "fb_mlp_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "fb_mlp_routed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_mlp_set_engine": (C.c_int, [C.c_void_p, C.c_int]),
     "fb_mlp_eval_points": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "fb_assemble_graph": (C.c_int, [C.c_void_p, C.c_uint]),
     "fb_set_launch": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
@@ -380,6 +382,10 @@ class Context:
         out = np.zeros((len(t), 4 if derivs else 1, 10), np.float32)
         self._check(self.L.fb_mlp_eval_points(self.h, len(t), _ptr(p), _ptr(t), int(bool(derivs)), _ptr(out)))
         return out if derivs else out[:, 0]
+
+    def mlp_set_engine(self, engine):
+        """FB_MLP_ENGINE_MMA (mma.sync) or FB_MLP_ENGINE_TC (tcgen05 + TMEM)."""
+        self._check(self.L.fb_mlp_set_engine(self.h, int(engine)))
 
     def mlp_routed(self):
         a, b = C.c_int(), C.c_int()
