@@ -457,6 +457,8 @@ def run_gpu(args):
         "roofline": roof,
         "clocks": clk,
     }
+    if rank == 0:
+        line["bloch"] = bloch_measure(ctx, torch, stream, local)
     if args.mlp_epochs > 0:
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
@@ -468,6 +470,32 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def bloch_measure(ctx, torch, stream, local, reps=5):
+    """Bloch sums of the assembled blocks into dense complex H(k) and S(k)
+    at one general k-point (h.SOLVESH/M_kspace_Lowdin.f90), on the device."""
+    import fbgpu
+    ctx.assemble(fbgpu.FB_ALL)
+    n = int(ctx.L.fb_norbitals(ctx.h))
+    hk = torch.empty((n, n), dtype=torch.complex128, device=f"cuda:{local}")
+    sk = torch.empty((n, n), dtype=torch.complex128, device=f"cuda:{local}")
+    k = np.array([[0.11, -0.23, 0.31]])
+    ctx.bloch_device(k, hk.data_ptr(), sk.data_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.bloch_device(k, hk.data_ptr(), sk.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = 2 * n * n * 16
+    herm = float((hk - hk.conj().T).abs().max().item())
+    del hk, sk
+    return {"what": "dense complex H(k) = T + vna + vnao and S(k) at one k-point (Bloch sums of the blocks)",
+            "norbitals": n, "ms": round(ms, 4), "bytes_written": nbytes,
+            "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), "hermiticity_max_abs": herm}
 
 
 def make_timer(torch, ctx, stream, flush, ws, local):

@@ -320,6 +320,23 @@ int fb_mlp_set_engine(fb_ctx *ctx, int engine);
 /* triplets the network takes in the current mode, and all triplets */
 int fb_mlp_routed(const fb_ctx *ctx, int *n_mlp, int *n_total);
 
+/* Bloch sums, the step after the assembly (h.SOLVESH/M_kspace_Lowdin.f90:
+ * 680-708 for S, :796-853 for H): dense complex matrices
+ *   M(jmu, jnu) = sum over pairs of phase(k . (xl(mbeta) + r_j - r_i)) *
+ *                 block(imu, inu),  phase(dot) = cos(dot) + i sin(dot),
+ * jmu / jnu the orbital's position in the structure (iblock_slot order),
+ * for H the T + vna + vnao blocks (the Harris terms of build_Hmatrix,
+ * :253-255) and for S the overlap blocks, one norbitals x norbitals
+ * column-major complex matrix (re, im interleaved) per k-point (kpts: 3
+ * doubles each, 1/Angstrom).  fb_bloch_device writes into device buffers
+ * (either may be NULL) and adds extra_dev (NULL, or nblock doubles on the
+ * device: the caller's other H terms, e.g. vxc) to H; fb_bloch copies to
+ * host buffers.  Needs fb_assemble of the blocks; single structures. */
+long long fb_norbitals(const fb_ctx *ctx);
+int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts,
+                    const void *extra_dev, void *Hk_dev, void *Sk_dev);
+int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
+
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions
  * run in double-float arithmetic on the FP32 pipe (two floats per value,
@@ -341,7 +358,7 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * kernel: "neigh_count", "neigh_fill", "neigh_back", "common_count",
  * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
  * "dassemble_3c", "build_forces", "trip_bins", "split_rho", "mlp_eval",
- * "assemble_3c_mlp", "dassemble_3c_mlp".  No reference counterpart (the reference
+ * "assemble_3c_mlp", "dassemble_3c_mlp", "bloch".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,

@@ -1680,3 +1680,49 @@ int or_build_forces(or_sys *s, const double *rho, const double *cape, const doub
   for (int k = 0; k < 3 * N; k++) ftot[k] = ftot[k] - pulay[k];
   return OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Bloch sums (h.SOLVESH/M_kspace_Lowdin.f90:680-708, :796-853)              */
+/* ------------------------------------------------------------------------ */
+/* out: nk column-major n x n complex matrices (re, im interleaved),
+ * M(jmu,jnu) += phase(dot) * block(imu,inu) over every pair, with
+ * vec = xl(mbeta) + ratom(jatom) - ratom(iatom), dot = k . vec and
+ * phase(dot) = cmplx(cos(dot), sin(dot))
+ * (M_diagonalization_Lowdin_kpoints.f90:413-442); jmu = imu + iblock_slot
+ * (M_configuraciones.f90:778-783). */
+int or_bloch(or_sys *s, int nk, const double *kpts, const double *blocks, double *out) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  int *slot = (int *)malloc(sizeof(int) * (N + 1));
+  if (!slot) return E_ARG;
+  slot[0] = 0;
+  for (int i = 0; i < N; i++) slot[i + 1] = slot[i] + fd->sp[s->imass[i]].norb_max;
+  long long n = slot[N];
+  for (long long q = 0; q < (long long)nk * 2 * n * n; q++) out[q] = 0.0;
+  for (int kk = 0; kk < nk; kk++) {
+    const double *k = kpts + 3 * kk;
+    double *M = out + (long long)kk * 2 * n * n;
+    for (int i = 0; i < N; i++) {
+      int ni = fd->sp[s->imass[i]].norb_max;
+      for (int p = s->pair_off[i]; p < s->pair_off[i + 1]; p++) {
+        int j = s->neigh_j[p], mb = s->neigh_b[p];
+        int nj = fd->sp[s->imass[j]].norb_max;
+        double vec[3], dot = 0.0;
+        for (int c = 0; c < 3; c++) {
+          vec[c] = (s->xl[mb][c] + s->ratom[3 * j + c]) - s->ratom[3 * i + c];
+          dot += k[c] * vec[c];
+        }
+        double cs = cos(dot), sn = sin(dot);
+        for (int nu = 0; nu < nj; nu++)
+          for (int mu = 0; mu < ni; mu++) {
+            double v = blocks[s->blk_off[p] + mu + (long long)ni * nu];
+            long long e = (slot[i] + mu) + n * (long long)(slot[j] + nu);
+            M[2 * e] += cs * v;
+            M[2 * e + 1] += sn * v;
+          }
+      }
+    }
+  }
+  free(slot);
+  return 0;
+}

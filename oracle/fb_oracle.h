@@ -74,6 +74,11 @@ int or_build_forces(or_sys *s, const double *rho, const double *cape,
                     const double *f3nac, double *kinetic, double *vna,
                     double *pulay, double *ftot);
 
+/* Bloch sum of one block set into nk dense n x n complex matrices
+ * (column-major, re/im interleaved) -- h.SOLVESH/M_kspace_Lowdin.f90 */
+int or_bloch(or_sys *s, int nk, const double *kpts, const double *blocks,
+             double *out);
+
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */
 int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x,

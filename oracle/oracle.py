@@ -53,6 +53,7 @@ def lib():
         L.or_dassemble_2c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
         L.or_dassemble_3c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_build_forces.argtypes = [C.c_void_p] + [_dp] * 13
+        L.or_bloch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
         L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     _dp, _dp]
@@ -161,6 +162,17 @@ class System:
         vb = np.zeros(self.nblock)
         _check(L.or_assemble_3c(self.h, vb))
         return vb
+
+    def bloch(self, kpts, blocks):
+        """Dense complex matrices sum_pairs phase(k . vec) block over the
+        k-points (nk, n, n), the reference's Hmatrix / Smatrix."""
+        L = lib()
+        k = np.ascontiguousarray(kpts, np.float64).reshape(-1, 3)
+        n = int(sum(self.fd.norb(int(q)) for q in self.imass))
+        out = np.zeros(len(k) * 2 * n * n)
+        _check(L.or_bloch(self.h, len(k), k.ravel(), np.ascontiguousarray(blocks, np.float64), out))
+        m = out.reshape(len(k), n, n, 2)   # [k][jnu][jmu][re/im] (column-major)
+        return np.transpose(m[..., 0] + 1j * m[..., 1], (0, 2, 1))
 
     def dassemble(self, rho, cape):
         L = lib()

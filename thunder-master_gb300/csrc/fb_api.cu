@@ -25,11 +25,12 @@ std::atomic<long long> g_alloc_gen{0};
 
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
-       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP, KT_N };
+       KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
+       KT_BLOCH, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
-                                     "dassemble_3c_mlp"};
+                                     "dassemble_3c_mlp", "bloch"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -65,6 +66,7 @@ struct fb_ctx {
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
   DevBuf d_slot_off, d_slot_nn, d_slot_found;
+  DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
   DevBuf d_status, d_errinfo;
   // blocks
   DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df;
@@ -1607,6 +1609,82 @@ int fb_mlp_forward(fb_ctx *ctx, int n, const float *feat3, const int *triple, fl
   std::string e;
   int st = mlp_forward(ctx->mlp, n, feat3, triple, out, ctx->stream, e);
   if (st) return fail(ctx, st, "%s", e.c_str());
+  return FB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Bloch sums into dense H(k), S(k) (fb_bloch, fb_bloch_device)
+// ---------------------------------------------------------------------------
+static int bloch_run(fb_ctx *ctx, int nk, const double *kpts, const double *extra_dev, double *Hk, double *Sk) {
+  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "Bloch sums are per structure (a batch of one)");
+  unsigned need = (Hk ? (FB_T | FB_VNA2C) : 0u) | (Sk ? FB_S : 0u);
+  if ((ctx->assembled & need) != need) return fail(ctx, FB_ERR_STATE, "fb_assemble the S / T / vna blocks first");
+  int N = ctx->N;
+  std::vector<int> slot(N);
+  long long n = 0;
+  for (int i = 0; i < N; i++) {
+    slot[i] = (int)n;
+    n += ctx->fdh.sp[ctx->h_isp[i]].norb;
+  }
+  CHK(ctx->d_orb_slot.ensure(N * sizeof(int)));
+  CU(cudaMemcpyAsync(ctx->d_orb_slot.p, slot.data(), N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  DevBuf dk;
+  CHK(dk.ensure((size_t)nk * 3 * sizeof(double)));
+  CU(cudaMemcpyAsync(dk.p, kpts, (size_t)nk * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  size_t bytes = (size_t)nk * 2 * n * n * sizeof(double);
+  AsmArgs a = asm_args(ctx);
+  if (Hk) {
+    CU(cudaMemsetAsync(Hk, 0, bytes, ctx->stream));
+    KL(KT_BLOCH, launch_bloch(a, ctx->P, nk, dk.as<double>(), ctx->d_pair_owner.as<int>(), ctx->d_r3v.as<double>(),
+                              ctx->d_orb_slot.as<int>(), n, ctx->d_T.as<double>(), ctx->d_vb.as<double>(),
+                              ctx->d_vbo.as<double>(), Hk, ctx->stream));
+    if (extra_dev)
+      KL(KT_BLOCH, launch_bloch(a, ctx->P, nk, dk.as<double>(), ctx->d_pair_owner.as<int>(), ctx->d_r3v.as<double>(),
+                                ctx->d_orb_slot.as<int>(), n, extra_dev, nullptr, nullptr, Hk, ctx->stream));
+  }
+  if (Sk) {
+    CU(cudaMemsetAsync(Sk, 0, bytes, ctx->stream));
+    KL(KT_BLOCH, launch_bloch(a, ctx->P, nk, dk.as<double>(), ctx->d_pair_owner.as<int>(), ctx->d_r3v.as<double>(),
+                              ctx->d_orb_slot.as<int>(), n, ctx->d_S.as<double>(), nullptr, nullptr, Sk, ctx->stream));
+  }
+  CU(cudaStreamSynchronize(ctx->stream));
+  dk.release();
+  return FB_OK;
+}
+
+extern "C" {
+
+long long fb_norbitals(const fb_ctx *ctx) {
+  if (!ctx || ctx->N < 1) return 0;
+  long long n = 0;
+  for (int i = 0; i < ctx->N; i++) n += ctx->fdh.sp[ctx->h_isp[i]].norb;
+  return n;
+}
+
+int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts, const void *extra_dev, void *Hk_dev, void *Sk_dev) {
+  if (!ctx || nk < 1 || !kpts || (!Hk_dev && !Sk_dev)) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  return bloch_run(ctx, nk, kpts, static_cast<const double *>(extra_dev), static_cast<double *>(Hk_dev),
+                   static_cast<double *>(Sk_dev));
+}
+
+int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk) {
+  if (!ctx || nk < 1 || !kpts || (!Hk && !Sk)) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  long long n = fb_norbitals(ctx);
+  size_t bytes = (size_t)nk * 2 * n * n * sizeof(double);
+  DevBuf h, sb;
+  if (Hk) CHK(h.ensure(bytes));
+  if (Sk) CHK(sb.ensure(bytes));
+  int st = bloch_run(ctx, nk, kpts, nullptr, Hk ? h.as<double>() : nullptr, Sk ? sb.as<double>() : nullptr);
+  if (st) return st;
+  if (Hk) CU(cudaMemcpy(Hk, h.p, bytes, cudaMemcpyDeviceToHost));
+  if (Sk) CU(cudaMemcpy(Sk, sb.p, bytes, cudaMemcpyDeviceToHost));
+  h.release();
+  sb.release();
   return FB_OK;
 }
 

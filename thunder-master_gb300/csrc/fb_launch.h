@@ -114,6 +114,11 @@ struct MlpEvalArgs;
 int launch_mlp_eval(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
 // the same on the tcgen05 tensor cores (TMEM accumulators)
 int launch_mlp_tc(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
+// Bloch sums of up to three block sets (B, C may be null) into nk dense
+// complex n x n matrices at out (column-major, re/im interleaved)
+int launch_bloch(const AsmArgs &a, int P, int nk, const double *kpts, const int *pair_owner, const double *r3v,
+                 const int *slot, long long n, const double *A, const double *B, const double *C, double *out,
+                 cudaStream_t s);
 // DFMA throughput probe: one warm-up and one timed launch
 int probe_dfma(cudaStream_t s, double *ms, double *flops);
 int probe_ffma(cudaStream_t s, double *ms, double *flops);

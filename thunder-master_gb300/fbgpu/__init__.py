@@ -63,6 +63,9 @@ _SIGS = {
     "fb_get_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_update_positions": (C.c_int, [C.c_void_p, _dp]),
     "fb_mlp_init": (C.c_int, [C.c_void_p, C.c_ulonglong]),
+    "fb_norbitals": (C.c_longlong, [C.c_void_p]),
+    "fb_bloch": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p]),
+    "fb_bloch_device": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_mlp_nparams": (C.c_longlong, [C.c_void_p]),
     "fb_mlp_layout": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fb_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -111,7 +114,7 @@ FB_PREC_FP64, FB_PREC_DF = 0, 1
 
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
            "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
-           "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp")
+           "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch")
 
 
 class FBError(RuntimeError):
@@ -301,6 +304,29 @@ class Context:
         best = np.zeros(4)
         self._check(self.L.fb_autotune(self.h, what, reps, _ptr(best)))
         return {k: (float(best[i]), self.get_launch(k)) for i, k in enumerate(TUNABLE) if best[i] > 0}
+
+    # ---- Bloch sums (h.SOLVESH/M_kspace_Lowdin.f90) ----------------------------
+    def bloch(self, kpts, H=True, S=True):
+        """Dense complex H(k) (T + vna + vnao) and S(k), shape (nk, n, n)."""
+        k = np.ascontiguousarray(kpts, np.float64).reshape(-1, 3)
+        n = int(self.L.fb_norbitals(self.h))
+        hk = np.zeros(len(k) * 2 * n * n) if H else None
+        sk = np.zeros(len(k) * 2 * n * n) if S else None
+        self._check(self.L.fb_bloch(self.h, len(k), k.ravel(), _ptr(hk), _ptr(sk)))
+
+        def cplx(a):
+            if a is None:
+                return None
+            m = a.reshape(len(k), n, n, 2)   # column-major: [k][col][row][re, im]
+            return np.transpose(m[..., 0] + 1j * m[..., 1], (0, 2, 1))
+        return cplx(hk), cplx(sk)
+
+    def bloch_device(self, kpts, hk_ptr, sk_ptr, extra_ptr=None):
+        k = np.ascontiguousarray(kpts, np.float64).reshape(-1, 3)
+        self._check(self.L.fb_bloch_device(self.h, len(k), k.ravel(),
+                                           None if extra_ptr is None else C.c_void_p(extra_ptr),
+                                           None if hk_ptr is None else C.c_void_p(hk_ptr),
+                                           None if sk_ptr is None else C.c_void_p(sk_ptr)))
 
     # ---- MLP-3c surrogate ------------------------------------------------------
     def mlp_init(self, seed=1):

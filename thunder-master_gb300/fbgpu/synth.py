@@ -35,6 +35,7 @@ P_ABOHR = 0.529177  # include/constants.h:2
 
 # interaction ids (include/interactions_2c.h:5-9, interactions_3c.h:8)
 P_OVERLAP, P_KINETIC, P_VNA_ONTOPL, P_VNA_ONTOPR, P_VNA_ATOM = 1, 2, 3, 4, 5
+P_DIPOLE_Z = 10     # include/interactions_2c.h:14
 P_BCNA = 3
 P_NTHETA = 5
 
@@ -211,22 +212,26 @@ def _seed_of(*keys):
     return h
 
 
-_AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P_VNA_ATOM: 0.3}
+_AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P_VNA_ATOM: 0.3,
+         P_DIPOLE_Z: 0.5}
 
 
-def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi):
+def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi, isub=0):
     """Seeded channel function of the canonical orientation.  The m != 0
     channels equal the m = 0 channel plus t^2 times their own function, so
     all channels of a shell pair agree at zero separation (on-site blocks are
-    then rotation invariant, as a physical table's are)."""
+    then rotation invariant, as a physical table's are).  isub > 0: the
+    charged-shell sub-cell isorp = isub (smaller amplitude)."""
     sa, la, ma = oa
     sb, lb, mb = ob
-    rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, 0))
-    val = _AMP2[itype] * _f1d(rng.normal(0.0, 1.0, 12), t, (la + lb) % 2 == 1)
+    sub = () if isub == 0 else ("isorp", isub)
+    amp = _AMP2[itype] * (1.0 if isub == 0 else 0.4)
+    rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, 0, *sub))
+    val = amp * _f1d(rng.normal(0.0, 1.0, 12), t, (la + lb) % 2 == 1)
     mkey = ma if asym_pi else abs(ma)
     if mkey != 0:
-        rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey))
-        val = val + t * t * _AMP2[itype] * _f1d(rng.normal(0.0, 1.0, 12), t, False)
+        rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey, *sub))
+        val = val + t * t * amp * _f1d(rng.normal(0.0, 1.0, 12), t, False)
     return val
 
 
@@ -234,7 +239,7 @@ def _canonical(zA, oa, zB, ob):
     return (zA, oa[0], oa[1]) <= (zB, ob[0], ob[1])
 
 
-def table2c(seed, itype, A, B, oa, ob, t, asym_pi=False):
+def table2c(seed, itype, A, B, oa, ob, t, asym_pi=False, isub=0):
     """Values of one 2c channel <A oa| O |B ob> on the grid t.
 
     Channels of the reversed pair are generated from the canonical ones with
@@ -244,19 +249,19 @@ def table2c(seed, itype, A, B, oa, ob, t, asym_pi=False):
     if itype == P_VNA_ATOM:   # both orbitals on A: symmetric in (mu, nu)
         if (oa[0], oa[1]) > (ob[0], ob[1]):
             oa, ob = ob, oa
-        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi)
+        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi, isub)
     if _canonical(A.nZ, oa, B.nZ, ob):
         if itype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
             itype = P_VNA_ONTOPL
-        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi)
+        return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi, isub)
     sign = _flip_sign(oa) * _flip_sign(ob)
     rtype = {P_VNA_ONTOPL: P_VNA_ONTOPR, P_VNA_ONTOPR: P_VNA_ONTOPL}.get(itype, itype)
     if rtype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
         rtype = P_VNA_ONTOPL
-    return sign * _base2c(seed, rtype, B.nZ, A.nZ, ob, oa, t, asym_pi)
+    return sign * _base2c(seed, rtype, B.nZ, A.nZ, ob, oa, t, asym_pi, isub)
 
 
-def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0):
+def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0, isub=0):
     """Legendre coefficient itheta of the bcna channel <A oa| V_K |B ob>.
 
     c^{BAK}_l[nu, mu] = (-1)^l s(mu) s(nu) c^{ABK}_l[mu, nu] with l = itheta-1
@@ -274,9 +279,11 @@ def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0):
     else:
         key = (B.nZ, A.nZ, ob, oa)
         sign = (-1.0) ** l * _flip_sign(oa) * _flip_sign(ob)
-    rng = np.random.default_rng(_seed_of(seed, "3c", key, K.nZ, mval, itheta))
+    sub = () if isub == 0 else ("isorp", isub)
+    rng = np.random.default_rng(_seed_of(seed, "3c", key, K.nZ, mval, itheta, *sub))
     coef = rng.normal(0.0, 1.0, 30)
-    return sign * _f2d(coef, u, v, 0.5 / (itheta ** theta_decay))
+    amp = 0.5 / (itheta ** theta_decay) * (1.0 if isub == 0 else 0.4)
+    return sign * _f2d(coef, u, v, amp)
 
 
 # ---------------------------------------------------------------------------
@@ -287,13 +294,19 @@ def _fmt(vals):
 
 
 def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
-                asym_pi=False, theta_decay=1.0):
+                asym_pi=False, theta_decay=1.0, dogs=False):
     """Write a complete Harris Fdata set for ``species`` into ``path``.
 
     nx2c: 2c grid points on [0, rcA_i + rcA_j] (200 points over 10 bohr for
     the rc = 5 bohr species).  n3c: 3c grid points on both axes.
     asym_pi: give the two pi channels of 2c tables different coefficients
     (breaks rotation invariance; used only to sharpen frame tests).
+    dogs: also the charged-shell sub-cells isorp = 1..nssh of vna_ontopL
+    (shells of the first atom), vna_ontopR and vna_atom (shells of the
+    second atom) and bcna (shells of the neutral atom), and the z-dipole
+    table, which the DOGS assemblers read.  Cells of one interaction are
+    consecutive and its munu file holds one record triple per cell (the
+    reference re-opens the open unit, which keeps its position).
     """
     os.makedirs(path, exist_ok=True)
     ns = len(species)
@@ -338,36 +351,45 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
             xmax = si_.rcA + sj.rcA
             x = np.linspace(0.0, xmax, nx2c)
             t = x / xmax
-            cells = [
-                (P_OVERLAP, "overlap", make_munu(si_.lssh, sj.lssh)),
-                (P_KINETIC, "kinetic", make_munu(si_.lssh, sj.lssh)),
-                (P_VNA_ONTOPL, "vna_ontopl_00", make_munu(si_.lssh, sj.lssh)),
-                (P_VNA_ONTOPR, "vna_ontopr_00", make_munu(si_.lssh, sj.lssh)),
-                (P_VNA_ATOM, "vna_atom_00", make_munu(si_.lssh, si_.lssh)),
-            ]
+            mm = make_munu(si_.lssh, sj.lssh)
+            ma = make_munu(si_.lssh, si_.lssh)
+            nsub = {P_VNA_ONTOPL: len(si_.lssh), P_VNA_ONTOPR: len(sj.lssh), P_VNA_ATOM: len(sj.lssh)}
+            stems = {P_VNA_ONTOPL: "vna_ontopl", P_VNA_ONTOPR: "vna_ontopr", P_VNA_ATOM: "vna_atom"}
+            cells = [(P_OVERLAP, 0, "overlap", mm), (P_KINETIC, 0, "kinetic", mm)]
+            for itype in (P_VNA_ONTOPL, P_VNA_ONTOPR, P_VNA_ATOM):
+                for isub in range(0, (nsub[itype] if dogs else 0) + 1):
+                    cells.append((itype, isub, "%s_%02d" % (stems[itype], isub),
+                                  ma if itype == P_VNA_ATOM else mm))
+            if dogs:
+                cells.append((P_DIPOLE_Z, 0, "dipole_z", mm))
             with open(os.path.join(path, "2c.%s.dat" % zz), "w") as f:
                 f.write("%d\n" % len(cells))
+            munu_records = {}
             with open(os.path.join(path, "2c.%s.dir" % zz), "w") as fd:
-                for icell, (itype, stem, (mu, nu, mv)) in enumerate(cells, start=1):
+                for icell, (itype, isub, stem, (mu, nu, mv)) in enumerate(cells, start=1):
                     fname = "%s.%s.dat" % (stem, zz)
                     ls_b = si_.lssh if itype == P_VNA_ATOM else sj.lssh
                     orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(ls_b)
                     data = np.zeros((nx2c, len(mu)))
                     for ime in range(len(mu)):
                         data[:, ime] = table2c(seed, itype, si_, sj, orb_a[mu[ime] - 1],
-                                               orb_b[nu[ime] - 1], t, asym_pi)
+                                               orb_b[nu[ime] - 1], t, asym_pi, isub)
                     with open(os.path.join(path, fname), "w") as f:
                         for ix in range(nx2c):
                             f.write(_fmt(data[ix]) + "\n")
                         f.write("\n")
                     fd.write("  %3d %3d %3d %-29s %3d %4d %9.6f\n"
-                             % (icell, itype, 0, fname, len(mu), nx2c, xmax))
-                    with open(os.path.join(path, "%02d_munu_2c.%s.dat" % (itype, zz)), "w") as f:
+                             % (icell, itype, isub, fname, len(mu), nx2c, xmax))
+                    munu_records.setdefault(itype, []).append((mu, nu, mv))
+            for itype, recs in munu_records.items():
+                with open(os.path.join(path, "%02d_munu_2c.%s.dat" % (itype, zz)), "w") as f:
+                    for mu, nu, mv in recs:
                         f.write(" ".join("%d" % v for v in mu) + "\n")
                         f.write(" ".join("%d" % v for v in nu) + "\n")
                         f.write(" ".join("%d" % v for v in mv) + "\n")
 
-    # three-center tables (bcna, isorp = 0, theta = 1..5)
+    # three-center tables (bcna, theta = 1..5; isorp = 0, and with dogs the
+    # neutral atom's shells isorp = 1..nssh)
     for si_ in species:
         for sj in species:
             for sk in species:
@@ -378,27 +400,29 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
                 orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(sj.lssh)
                 u = np.linspace(0.0, 1.0, n3c)[None, :]       # x fastest
                 v = np.linspace(0.0, 1.0, n3c)[:, None]
+                subs = list(range(0, (len(sk.lssh) if dogs else 0) + 1))
                 with open(os.path.join(path, "3c.%s.dat" % zzz), "w") as f:
-                    f.write("%d\n" % P_NTHETA)
+                    f.write("%d\n" % (P_NTHETA * len(subs)))
                 with open(os.path.join(path, "3c.%s.dir" % zzz), "w") as fd, \
                         open(os.path.join(path, "%02d_munu_3c.%s.dat" % (P_BCNA, zzz)), "w") as fm:
-                    for itheta in range(1, P_NTHETA + 1):
-                        fname = "bcna_%02d_%02d.%s.dat" % (itheta, 0, zzz)
-                        data = np.zeros((n3c, n3c, len(mu)))
-                        for ime in range(len(mu)):
-                            data[:, :, ime] = table3c(seed, si_, sj, sk, orb_a[mu[ime] - 1],
-                                                      orb_b[nu[ime] - 1], mv[ime], itheta, u, v,
-                                                      theta_decay)
-                        with open(os.path.join(path, fname), "w") as f:
-                            for iy in range(n3c):
-                                for ix in range(n3c):
-                                    f.write(_fmt(data[iy, ix]) + "\n")
-                        fd.write("  %2d %2d %2d %3d %-29s %3d %4d %9.6f %4d %9.6f\n"
-                                 % (itheta, P_BCNA, 0, itheta, fname, len(mu),
-                                    n3c, xmax, n3c, ymax))
-                        fm.write(" " + " ".join("%d" % q for q in mu) + "\n")
-                        fm.write(" " + " ".join("%d" % q for q in nu) + "\n")
-                        fm.write(" " + " ".join("%d" % q for q in mv) + "\n")
+                    for isub in subs:
+                        for itheta in range(1, P_NTHETA + 1):
+                            fname = "bcna_%02d_%02d.%s.dat" % (itheta, isub, zzz)
+                            data = np.zeros((n3c, n3c, len(mu)))
+                            for ime in range(len(mu)):
+                                data[:, :, ime] = table3c(seed, si_, sj, sk, orb_a[mu[ime] - 1],
+                                                          orb_b[nu[ime] - 1], mv[ime], itheta, u, v,
+                                                          theta_decay, isub)
+                            with open(os.path.join(path, fname), "w") as f:
+                                for iy in range(n3c):
+                                    for ix in range(n3c):
+                                        f.write(_fmt(data[iy, ix]) + "\n")
+                            fd.write("  %2d %2d %2d %3d %-29s %3d %4d %9.6f %4d %9.6f\n"
+                                     % (isub * P_NTHETA + itheta, P_BCNA, isub, itheta, fname, len(mu),
+                                        n3c, xmax, n3c, ymax))
+                            fm.write(" " + " ".join("%d" % q for q in mu) + "\n")
+                            fm.write(" " + " ".join("%d" % q for q in nu) + "\n")
+                            fm.write(" " + " ".join("%d" % q for q in mv) + "\n")
     return path
 
 
@@ -527,16 +551,17 @@ def batch_structures(nstruct=256, seed=SEED_BATCH):
     return out
 
 
-def fdata_dir_for(workload, root=None):
-    """Generate (once) and return the Fdata directory of a workload."""
+def fdata_dir_for(workload, root=None, dogs=False):
+    """Generate (once) and return the Fdata directory of a workload (with
+    the DOGS sub-cells and dipole table when dogs is set)."""
     root = root or os.environ.get("FBGPU_FDATA_ROOT") or os.path.join(
         os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "_fdata")
     key = {"si64": "Si_rc50", "si512": "Si_rc50", "cho1536": "CHO_rc45_40_40",
            "sic4096": "SiC_rc50", "batch256": "SiC_rc50"}[workload]
-    path = os.path.join(root, key)
+    path = os.path.join(root, key + ("_DOGS" if dogs else ""))
     stamp = os.path.join(path, ".complete")
     if not os.path.exists(stamp):
-        write_fdata(path, species_for(workload))
+        write_fdata(path, species_for(workload), dogs=dogs)
         with open(stamp, "w") as f:
             f.write("ok\n")
     return path
