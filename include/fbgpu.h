@@ -76,6 +76,8 @@ extern "C" {
 #define FB_ALL 15u
 #define FB_KEEP_DBLOCKS 16u  /* fb_dassemble: also keep dS, dT Dblocks */
 #define FB_FORCES 32u        /* fb_assemble_graph / fb_autotune: the force pass too */
+#define FB_DIPOLE 64u        /* z-dipole blocks (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499);
+                                with FB_THEORY_DOGS, FB_VNA2C computes them and FB_S as well */
 
 /* block sets for fb_get_blocks / fb_device_blocks */
 #define FB_BLOCK_S 0       /* s%overlap(i)%neighbors(k)%block */
@@ -86,6 +88,7 @@ extern "C" {
 #define FB_BLOCK_DT 5      /* s%kinetic(i)%neighbors(k)%Dblock */
 #define FB_BLOCK_RHO 6     /* s%denmat(i)%neighbors(k)%block (input) */
 #define FB_BLOCK_CAPE 7    /* s%capemat(i)%neighbors(k)%block (input) */
+#define FB_BLOCK_DIP 8     /* s%dipole_z(i)%neighbors(k)%block (FB_DIPOLE) */
 
 /* force arrays for fb_get_forces */
 #define FB_F_TOT 0         /* ftot: kinetic + vna + f3na(a+b+c) - pulay */
@@ -336,6 +339,29 @@ long long fb_norbitals(const fb_ctx *ctx);
 int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts,
                     const void *extra_dev, void *Hk_dev, void *Sk_dev);
 int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
+
+/* Theory of the neutral-atom terms.  FB_THEORY_HARRIS (the default):
+ * assemble_vna_2c / assemble_vna_3c of the Harris functional
+ * (M_assemble_2c_Harris.f90, M_assemble_3c_Harris.f90).  FB_THEORY_DOGS:
+ * the charge-weighted versions (j.ASSEMBLERS/M_assemble_2c_DOGS.f90:640-814,
+ * M_assemble_3c_DOGS.f90:158-322): the vna ontop and atom terms add the
+ * charged-shell sub-cells isorp = 1..nssh weighted by the shell charges
+ * dQ = Qin - Qneutral, the atom and three-center terms smoothed into the
+ * effective monopole of the overlap and z-dipole blocks.  DOGS needs Fdata
+ * with the sub-cells and dipole_z tables (FB_ERR_TABLE otherwise) and
+ * fb_set_charges; it runs the FP64 kernels and the tables only (no MLP-3c
+ * routing).  Its force pass (Dassemble_*_DOGS) is not built: fb_dassemble
+ * and FB_FORCES return FB_ERR_UNSUPPORTED in DOGS. */
+#define FB_THEORY_HARRIS 0
+#define FB_THEORY_DOGS 1
+int fb_set_theory(fb_ctx *ctx, int theory);
+
+/* Shell charges of the DOGS terms, dq[i * nssh_max + k] = Qin(k+1, i+1) -
+ * Qneutral(k+1, imass(i+1)), a row per atom (entries beyond the species'
+ * nssh are ignored; nssh_max <= 3).  Stands for the reference's
+ * s%atom(i)%shell(k)%dQ (M_assemble_2c_DOGS.f90:662, :806,
+ * M_assemble_3c_DOGS.f90:313). */
+int fb_set_charges(fb_ctx *ctx, const double *dq, int nssh_max);
 
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions

@@ -44,6 +44,7 @@ enum {
 #define P_vna_ontopL 3
 #define P_vna_ontopR 4
 #define P_vna_atom 5
+#define P_dipole_z 10
 #define P_bcna 3
 #define P_mbox 4 /* c.SYSTEM/M_configuraciones.f90:359 */
 
@@ -122,6 +123,9 @@ struct or_sys {
   int npairs;
   int *ncommon, *trip_off, *ci_j, *ci_b, *cj_j, *cj_b, *cneigh;
   int ntrip;
+  /* DOGS shell charges dQ[i * nssh_max + isorp - 1] */
+  double *dQ;
+  int nssh_max;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -1140,7 +1144,7 @@ static void free_neigh(or_sys *s) {
 void or_free_system(or_sys *s) {
   if (!s) return;
   free_neigh(s);
-  free(s->ratom); free(s->imass); free(s->xl);
+  free(s->ratom); free(s->imass); free(s->xl); free(s->dQ);
   free(s);
 }
 
@@ -1725,4 +1729,155 @@ int or_bloch(or_sys *s, int nk, const double *kpts, const double *blocks, double
   }
   free(slot);
   return 0;
+}
+/* ------------------------------------------------------------------------ */
+/* DOGS: charge-weighted neutral-atom terms                                  */
+/* ------------------------------------------------------------------------ */
+int or_set_charges(or_sys *s, const double *dq, int nssh_max) {
+  if (!s || !dq || nssh_max < 1) return E_ARG;
+  free(s->dQ);
+  s->dQ = (double *)malloc(sizeof(double) * (size_t)s->natoms * nssh_max);
+  memcpy(s->dQ, dq, sizeof(double) * (size_t)s->natoms * nssh_max);
+  s->nssh_max = nssh_max;
+  return OK;
+}
+
+/* s%atom(iatom)%shell(isorp)%dQ */
+static double shell_dq(const or_sys *s, int iatom, int isorp) {
+  if (!s->dQ || isorp > s->nssh_max) return 0.0;
+  return s->dQ[(size_t)iatom * s->nssh_max + isorp - 1];
+}
+
+/* smoother (b.FUNCTIONS/smoother.f90:100-146), scaler = 1 */
+static double smoother(double r, double rend, double x) {
+  double rbegin = x * rend;
+  if (r > rend) return 0.0;
+  if (r < rbegin) return 1.0;
+  double ratio = (r - rbegin) / (rend - rbegin);
+  double sm = 1.0 - ratio * ratio;
+  return sm * sm;
+}
+
+/* smallest shell cutoff of a species, starting from 99
+ * (j.ASSEMBLERS/M_assemble_2c_DOGS.f90:746-754) */
+static double rcutoff_min(const species_t *sp) {
+  double r = 99.0;
+  for (int k = 0; k < sp->nssh; k++) r = fmin(r, sp->rcutoffA[k]);
+  return r;
+}
+
+/* assemble_dipole_z (j.ASSEMBLERS/M_assemble_2c_DOGS.f90:376-499) */
+int or_assemble_dipole_z(or_sys *s, double *dip) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      if ((st = or_getMEs_2c(fd, in1, in2, P_dipole_z, 0, z, nmu, nnu, mm))) { err = st; continue; }
+      or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+      memcpy(dip + s->blk_off[p], xm, sizeof(double) * nmu * nnu);
+    }
+  }
+  return err;
+}
+
+/* assemble_vna_2c, DOGS (j.ASSEMBLERS/M_assemble_2c_DOGS.f90:640-814): the
+ * Harris ontop and atom terms plus the charged shells -- ontop L weighted by
+ * the shells of iatom, ontop R and atom by those of jatom, the atom terms
+ * smoothed into the effective monopole S(i, self) / z.  S is the overlap
+ * block set. */
+int or_assemble_vna_2c_dogs(or_sys *s, const double *S, double *vb, double *vbo) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      long long o = s->blk_off[p];
+      for (int k = 0; k < nmu * nnu; k++) vb[o + k] = 0.0, vbo[o + k] = 0.0;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      /* ontop L: neutral, then the charged shells of iatom */
+      for (int isorp = 0; isorp <= fd->sp[in1].nssh; isorp++) {
+        if ((st = or_getMEs_2c(fd, in1, in2, P_vna_ontopL, isorp, z, nmu, nnu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        double w = isorp == 0 ? 1.0 : shell_dq(s, i, isorp);
+        for (int k = 0; k < nmu * nnu; k++) vbo[o + k] = vbo[o + k] + w * xm[k] * P_eq2;
+      }
+      /* ontop R: neutral, then the charged shells of jatom */
+      for (int isorp = 0; isorp <= fd->sp[in2].nssh; isorp++) {
+        if ((st = or_getMEs_2c(fd, in1, in2, P_vna_ontopR, isorp, z, nmu, nnu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        double w = isorp == 0 ? 1.0 : shell_dq(s, j, isorp);
+        for (int k = 0; k < nmu * nnu; k++) vbo[o + k] = vbo[o + k] + w * xm[k] * P_eq2;
+      }
+    }
+    /* atom case (:704-814) into block(neigh_self(i)) */
+    long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+    for (int k = 0; k < nmu * nmu; k++) vb[os + k] = 0.0;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      double rend = rcutoff_min(&fd->sp[in1]) + rcutoff_min(&fd->sp[in2]);
+      double smooth = smoother(z, rend, 0.8);
+      double emnpl[MAXORB * MAXORB];
+      for (int k = 0; k < nmu * nmu; k++) emnpl[k] = z > 1.0e-4 ? S[os + k] / z : 0.0;
+      for (int isorp = 0; isorp <= fd->sp[in2].nssh; isorp++) {
+        if ((st = or_getMEs_2c(fd, in1, in2, P_vna_atom, isorp, z, nmu, nmu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in1, eps, nmu, nmu, mm, xm);
+        if (isorp == 0) {
+          for (int k = 0; k < nmu * nmu; k++) vb[os + k] = vb[os + k] + xm[k] * P_eq2;
+        } else {
+          double dq = shell_dq(s, j, isorp);
+          for (int k = 0; k < nmu * nmu; k++)
+            vb[os + k] = vb[os + k] + P_eq2 * dq * ((1.0 - smooth) * emnpl[k] + smooth * xm[k]);
+        }
+      }
+    }
+  }
+  return err;
+}
+
+/* assemble_vna_3c, DOGS (j.ASSEMBLERS/M_assemble_3c_DOGS.f90:158-322),
+ * accumulating: the neutral bcna term plus, for the charged shells of
+ * ialpha, the dQ-weighted sub-cells smoothed (stinky = smoother(d13) *
+ * smoother(d23)) into the effective monopole
+ * emnpl = (S/2 - dip/z)/d13 + (S/2 + dip/z)/d23 of the pair (i, mneigh). */
+int or_assemble_vna_3c_dogs(or_sys *s, const double *S, const double *dip, double *vb) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int ia = 0; ia < s->natoms; ia++) {
+    double mm[MAXORB * MAXORB], xm[MAXORB * MAXORB], emnpl[MAXORB * MAXORB];
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+      double d13 = distance3(g.rna, g.r1), d23 = distance3(g.rna, g.r2);
+      double rc3 = rcutoff_min(&fd->sp[g.indna]);
+      double stinky = smoother(d13, rcutoff_min(&fd->sp[g.in1]) + rc3, 0.8) *
+                      smoother(d23, rcutoff_min(&fd->sp[g.in2]) + rc3, 0.8);
+      for (int k = 0; k < nmu * nnu; k++) {
+        double sterm = S[o + k] / 2.0, dterm = dip[o + k] / g.z;
+        emnpl[k] = (sterm - dterm) / d13 + (sterm + dterm) / d23;
+      }
+      for (int isorp = 0; isorp <= fd->sp[g.indna].nssh; isorp++) {
+        int st = or_getMEs_3c(fd, g.in1, g.in2, g.indna, P_bcna, isorp, g.x, g.z, nmu, nnu, g.cost, mm);
+        if (st) { err = st; continue; }
+        or_rotate(fd, g.in1, g.in2, g.eps, nmu, nnu, mm, xm);
+        if (isorp == 0) {
+          for (int k = 0; k < nmu * nnu; k++) vb[o + k] = vb[o + k] + xm[k] * P_eq2;
+        } else {
+          double dq = shell_dq(s, ia, isorp);
+          for (int k = 0; k < nmu * nnu; k++)
+            vb[o + k] = vb[o + k] + dq * (stinky * xm[k] + (1.0 - stinky) * emnpl[k]) * P_eq2;
+        }
+      }
+    }
+  }
+  return err;
 }

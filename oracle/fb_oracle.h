@@ -79,6 +79,17 @@ int or_build_forces(or_sys *s, const double *rho, const double *cape,
 int or_bloch(or_sys *s, int nk, const double *kpts, const double *blocks,
              double *out);
 
+/* DOGS (j.ASSEMBLERS/M_assemble_2c_DOGS.f90, M_assemble_3c_DOGS.f90):
+ * shell charges dq[i * nssh_max + isorp - 1] = Qin - Qneutral; z-dipole
+ * blocks; the charge-weighted vna 2c (fills vb, vbo from the overlap S) and
+ * vna 3c (accumulates onto vb from S and dip) */
+int or_set_charges(or_sys *s, const double *dq, int nssh_max);
+int or_assemble_dipole_z(or_sys *s, double *dip);
+int or_assemble_vna_2c_dogs(or_sys *s, const double *S, double *vb,
+                            double *vbo);
+int or_assemble_vna_3c_dogs(or_sys *s, const double *S, const double *dip,
+                            double *vb);
+
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */
 int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x,

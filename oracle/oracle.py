@@ -54,6 +54,10 @@ def lib():
         L.or_dassemble_3c.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_build_forces.argtypes = [C.c_void_p] + [_dp] * 13
         L.or_bloch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
+        L.or_set_charges.argtypes = [C.c_void_p, _dp, C.c_int]
+        L.or_assemble_dipole_z.argtypes = [C.c_void_p, _dp]
+        L.or_assemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.or_assemble_vna_3c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
         L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     _dp, _dp]
@@ -155,6 +159,22 @@ class System:
         if with3c:
             _check(L.or_assemble_3c(self.h, vb))
         return S, T, vb, vbo
+
+    def assemble_dogs(self, dQ, with3c=True):
+        """DOGS value pass: S, T, vna (atom + 3c), vnao (ontop) and the
+        z-dipole blocks, with shell charges dQ (natoms, nssh_max)."""
+        L = lib()
+        nb = self.nblock
+        d = np.ascontiguousarray(dQ, np.float64)
+        d = d.reshape(len(self.imass), -1)
+        _check(L.or_set_charges(self.h, np.ascontiguousarray(d.ravel()), d.shape[1]))
+        S, T, vb, vbo, dip = (np.zeros(nb) for _ in range(5))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        _check(L.or_assemble_dipole_z(self.h, dip))
+        _check(L.or_assemble_vna_2c_dogs(self.h, S, vb, vbo))
+        if with3c:
+            _check(L.or_assemble_vna_3c_dogs(self.h, S, dip, vb))
+        return S, T, vb, vbo, dip
 
     def assemble_3c_only(self):
         L = lib()

@@ -26,11 +26,12 @@ def fdata_root():
     return root
 
 
-def workload(name, root):
-    """(fdata dir, nZ list, Structure) of a named synthetic workload."""
+def workload(name, root, dogs=False):
+    """(fdata dir, nZ list, Structure) of a named synthetic workload; dogs:
+    the Fdata set with the DOGS charged-shell sub-cells and z-dipole table."""
     path = synth.fdata_dir_for(name if name in ("si64", "si512", "cho1536", "sic4096") else
                                {"cho_small": "cho1536", "sic_small": "sic4096", "si_vac": "si64",
-                                "sic_vac": "sic4096"}[name], root=root)
+                                "sic_vac": "sic4096"}[name], root=root, dogs=dogs)
     if name in ("si64", "si512", "cho1536", "sic4096"):
         st = synth.structure_for(name)
         nZ = [s.nZ for s in synth.species_for(name)]

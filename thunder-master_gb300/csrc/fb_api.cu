@@ -69,7 +69,12 @@ struct fb_ctx {
   DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
   DevBuf d_status, d_errinfo;
   // blocks
-  DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df;
+  DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df, d_dip;
+  // theory of the neutral-atom terms (FB_THEORY_HARRIS / FB_THEORY_DOGS) and
+  // the DOGS shell charges dq[atom][MAXSUB]
+  int theory = FB_THEORY_HARRIS;
+  DevBuf d_dq;
+  bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
   // forces
@@ -84,7 +89,7 @@ struct fb_ctx {
   // maps of the same sizes reuse it).
   cudaGraphExec_t gexec = nullptr;
   unsigned g_what = 0;
-  int g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1, g_mlp_engine = -1;
+  int g_theory = -1, g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1, g_mlp_engine = -1;
   long long g_nblock = -1, g_alloc = -1, g_launches = 0;
   cudaStream_t g_stream = nullptr;
   KCfg g_cfg[TK_N];
@@ -327,6 +332,7 @@ int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms, const double *rato
   if (total > (1LL << 30)) return fail(ctx, FB_ERR_ARG, "%lld atoms in the batch", total);
   CU(cudaSetDevice(ctx->device));
   int N = (int)total;
+  if (N != ctx->N) ctx->have_charges = false;
   ctx->N = N;
   ctx->nstruct = nstruct;
   ctx->h_isp.resize(N);
@@ -489,7 +495,9 @@ static int trip_cells(const fb_ctx *ctx) {
   return cells;
 }
 
-static bool mlp_routes(const fb_ctx *ctx) { return ctx->mlp.ready && ctx->mlp_mode != FB_MLP_OFF && !ctx->fdh.have_d; }
+static bool mlp_routes(const fb_ctx *ctx) {
+  return ctx->mlp.ready && ctx->mlp_mode != FB_MLP_OFF && !ctx->fdh.have_d && ctx->theory == FB_THEORY_HARRIS;
+}
 
 // counting sort of the triplets by interpolation bin, approved MLP-3c bins
 // first; mlp_n = triplets the network takes
@@ -571,7 +579,7 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_vb.ensure(bb));
   CHK(ctx->d_vbo.ensure(bb));
   ctx->have_neigh = true;
-  ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = false;
+  ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = ctx->have_dip = false;
   ctx->assembled = ctx->dassembled = 0;
   return FB_OK;
 }
@@ -816,10 +824,52 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.cfg_d2c = ctx->cfg[TK_D2C];
   a.cfg_d3c = ctx->cfg[TK_D3C];
   a.queue = ctx->d_queue.as<int>();
+  a.dogs = ctx->theory == FB_THEORY_DOGS;
+  a.dq = ctx->d_dq.as<double>();
+  a.dip = ctx->d_dip.as<double>();
   return a;
 }
 
-static bool use_df(const fb_ctx *ctx) { return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d; }
+// the double-float kernels carry the Harris terms only; DOGS runs in FP64
+static bool use_df(const fb_ctx *ctx) {
+  return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d && ctx->theory == FB_THEORY_HARRIS;
+}
+
+int fb_set_theory(fb_ctx *ctx, int theory) {
+  if (!ctx || (theory != FB_THEORY_HARRIS && theory != FB_THEORY_DOGS)) return FB_ERR_ARG;
+  if (theory == FB_THEORY_DOGS && (!ctx->have_fdata || !ctx->fdh.dev.have_dogs))
+    return fail(ctx, FB_ERR_TABLE, "DOGS: the Fdata has no charged-shell sub-cells or no z-dipole table");
+  if (theory != ctx->theory) {
+    ctx->theory = theory;
+    // vna blocks and forces of the other theory are stale
+    ctx->have_vna2c = false;
+    ctx->assembled &= ~(unsigned)(FB_VNA2C | FB_VNA3C);
+    ctx->dassembled = 0;
+  }
+  return FB_OK;
+}
+
+int fb_set_charges(fb_ctx *ctx, const double *dq, int nssh_max) {
+  if (!ctx || !dq || nssh_max < 1) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  if (nssh_max > MAXSUB) return fail(ctx, FB_ERR_CAPACITY, "nssh_max = %d > %d", nssh_max, MAXSUB);
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N;
+  std::vector<double> h((size_t)N * MAXSUB, 0.0);
+  for (int i = 0; i < N; i++) {
+    int nssh = ctx->fdh.dev.sp[ctx->h_isp[i]].nssh;
+    for (int k = 0; k < nssh_max; k++) {
+      double v = dq[(size_t)i * nssh_max + k];
+      if (!std::isfinite(v)) return fail(ctx, FB_ERR_ARG, "dQ(%d, %d) is not finite", k + 1, i + 1);
+      if (k < nssh) h[(size_t)i * MAXSUB + k] = v;
+    }
+  }
+  CHK(ctx->d_dq.ensure(h.size() * sizeof(double)));
+  CU(cudaMemcpyAsync(ctx->d_dq.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_charges = true;
+  return FB_OK;
+}
 
 int fb_set_precision(fb_ctx *ctx, int mode) {
   if (!ctx || (mode != FB_PREC_FP64 && mode != FB_PREC_DF)) return FB_ERR_ARG;
@@ -862,7 +912,10 @@ static int prepare_mlp(fb_ctx *ctx, bool forces) {
 // launches of the value pass (no synchronization)
 static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
-  unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+  unsigned w2 = what & (FB_S | FB_T | FB_VNA2C | FB_DIPOLE);
+  // DOGS: the vna 2c pass also writes the overlap and z-dipole blocks the
+  // three-center terms read
+  if (a.dogs && (w2 & FB_VNA2C)) w2 |= FB_S | FB_DIPOLE;
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
   if (what & FB_VNA3C) {
     // triplets of approved bins through the network, the rest through the tables
@@ -883,11 +936,26 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   return FB_OK;
 }
 
+// state checks and the storage of the value pass (allocations happen here,
+// never while a graph is being captured)
 static int check_assemble(fb_ctx *ctx, unsigned what) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   if ((what & FB_VNA3C) && !(what & FB_VNA2C) && !ctx->have_vna2c)
     return fail(ctx, FB_ERR_STATE, "assemble_vna_3c accumulates onto assemble_vna_2c blocks: assemble FB_VNA2C first");
+  bool dogs = ctx->theory == FB_THEORY_DOGS;
+  if (dogs && (what & (FB_VNA2C | FB_VNA3C)) && !ctx->have_charges)
+    return fail(ctx, FB_ERR_STATE, "DOGS: fb_set_charges first");
+  if ((what & FB_DIPOLE) && !ctx->fdh.dev.have_dogs)
+    return fail(ctx, FB_ERR_TABLE, "FB_DIPOLE: the Fdata has no z-dipole table (dipole_z)");
+  if ((what & FB_DIPOLE) || (dogs && (what & FB_VNA2C)))
+    CHK(ctx->d_dip.ensure((size_t)ctx->nblock * sizeof(double) + 8));
   return FB_OK;
+}
+
+static void assemble_done(fb_ctx *ctx, unsigned what) {
+  if (what & FB_VNA2C) ctx->have_vna2c = true;
+  if ((what & FB_DIPOLE) || (ctx->theory == FB_THEORY_DOGS && (what & FB_VNA2C))) ctx->have_dip = true;
+  ctx->assembled |= what & (FB_ALL | FB_DIPOLE);
 }
 
 int fb_assemble(fb_ctx *ctx, unsigned what) {
@@ -900,8 +968,7 @@ int fb_assemble(fb_ctx *ctx, unsigned what) {
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
-  if (what & FB_VNA2C) ctx->have_vna2c = true;
-  ctx->assembled |= what;
+  assemble_done(ctx, what);
   return FB_OK;
 }
 
@@ -916,6 +983,7 @@ static DevBuf *block_buf(fb_ctx *ctx, int which, size_t *n) {
     case FB_BLOCK_DT: *n *= 3; return ctx->have_dblocks ? &ctx->d_dT : nullptr;
     case FB_BLOCK_RHO: return ctx->have_rho ? &ctx->d_rho : nullptr;
     case FB_BLOCK_CAPE: return ctx->have_rho ? &ctx->d_cape : nullptr;
+    case FB_BLOCK_DIP: return ctx->have_dip ? &ctx->d_dip : nullptr;
   }
   return nullptr;
 }
@@ -974,6 +1042,8 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
 // a graph is being captured)
 static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (ctx->theory == FB_THEORY_DOGS)
+    return fail(ctx, FB_ERR_UNSUPPORTED, "DOGS: the force pass (Dassemble_*_DOGS) is not built; Harris forces only");
   if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
   int N = ctx->N, P = ctx->P;
   size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
@@ -1068,7 +1138,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   int st = FB_OK;
   if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
     st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
-  if (!st && (what & FB_ALL)) st = enqueue_assemble(ctx, what);
+  if (!st && (what & (FB_ALL | FB_DIPOLE))) st = enqueue_assemble(ctx, what);
   if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -1087,6 +1157,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   ctx->g_launches = ctx->launches - l0;
   ctx->launches = l0;
   ctx->g_what = what;
+  ctx->g_theory = ctx->theory;
   ctx->g_prec = ctx->prec;
   ctx->g_N = ctx->N;
   ctx->g_P = ctx->P;
@@ -1104,13 +1175,13 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
 
 int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
-  if (!(what & (FB_ALL | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
+  if (!(what & (FB_ALL | FB_FORCES | FB_DIPOLE))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
   CU(cudaSetDevice(ctx->device));
-  if (what & FB_ALL) CHK(check_assemble(ctx, what));
+  if (what & (FB_ALL | FB_DIPOLE)) CHK(check_assemble(ctx, what));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, (what & FB_FORCES) != 0));
   if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what));
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
-  bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_prec == ctx->prec && ctx->g_N == ctx->N &&
+  bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_theory == ctx->theory && ctx->g_prec == ctx->prec && ctx->g_N == ctx->N &&
                ctx->g_P == ctx->P && ctx->g_T == ctx->T && ctx->g_nblock == ctx->nblock &&
                ctx->g_have_d == ctx->fdh.have_d && ctx->g_alloc == g_alloc_gen.load() &&
                ctx->g_mlp_n == ctx->mlp_n && ctx->g_mlp_mode == ctx->mlp_mode &&
@@ -1122,8 +1193,7 @@ int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
-  if (what & FB_VNA2C) ctx->have_vna2c = true;
-  ctx->assembled |= what & FB_ALL;
+  assemble_done(ctx, what);
   if (what & FB_FORCES) dassemble_done(ctx, what);
   return FB_OK;
 }
@@ -1165,7 +1235,12 @@ static int tune_launch(fb_ctx *ctx, int k, const KCfg &c, unsigned what) {
   AsmArgs a = asm_args(ctx);
   a.keep_dblocks = false;
   switch (k) {
-    case TK_A2C: a.cfg_a2c = c; return launch_assemble_2c(a, what & (FB_S | FB_T | FB_VNA2C), ctx->stream);
+    case TK_A2C: {
+      a.cfg_a2c = c;
+      unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+      if (a.dogs && (w2 & FB_VNA2C)) w2 |= FB_S | FB_DIPOLE;
+      return launch_assemble_2c(a, w2, ctx->stream);
+    }
     case TK_A3C:
       a.cfg_a3c = c;
       return use_df(ctx) ? launch_assemble_3c_df(a, ctx->stream) : launch_assemble_3c(a, ctx->stream);
@@ -1183,6 +1258,7 @@ int fb_autotune(fb_ctx *ctx, unsigned what, int reps, double *best_ms) {
   CU(cudaSetDevice(ctx->device));
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   bool forces = (what & FB_FORCES) != 0;
+  if (what & FB_ALL) CHK(check_assemble(ctx, (what & FB_ALL) | FB_VNA2C));
   if (forces) CHK(prepare_dassemble(ctx, what | FB_ALL));
   if (forces && (what & FB_VNA3C) && use_df(ctx)) {
     AsmArgs a = asm_args(ctx);
@@ -1362,6 +1438,8 @@ static int noalloc_scratch(fb_ctx *ctx, double **out) {
 extern "C" int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev, const double *cape_dev, double *ftot_dev) {
   if (!ctx || !rho_dev || !ftot_dev) return FB_ERR_ARG;
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+  if (ctx->theory == FB_THEORY_DOGS)
+    return fail(ctx, FB_ERR_UNSUPPORTED, "DOGS: the force pass (Dassemble_*_DOGS) is not built; Harris forces only");
   int N = ctx->N, P = ctx->P;
   if (P > FB_NOALLOC_MAX_PAIRS || N > FB_NOALLOC_MAX_ATOMS)
     return fail(ctx, FB_ERR_CAPACITY,

@@ -3,8 +3,14 @@
 
 namespace fb {
 
-template <int PA, int PB, bool HASD>
-__device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned what, double *Xatom) {
+// what: 1 overlap, 2 kinetic, 4 vna (ontop + atom), 64 z-dipole.  With DOGS
+// the vna terms add the charged shells (M_assemble_2c_DOGS.f90:640-814):
+// ontop L / R the sub-cells of the atom the potential sits on weighted by
+// its shell charges, the atom case the smoothed effective monopole
+// emnpl = S(i, self) / z (Sself, the self overlap block of atom i).
+template <int PA, int PB, bool HASD, bool DOGS>
+__device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned what, double *Xatom,
+                                        const double *Sself) {
   using PL = Plan<PA, PB, K2C>;
   using PLA = Plan<PA, PA, K2C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
@@ -41,6 +47,14 @@ __device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned w
 #pragma unroll
     for (int q = 0; q < NA * NB; q++) c.T[o + q] = X[q];
   }
+  if (what & 64u) {  // z-dipole (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499)
+    const Cell2cDev &cell = fd.c2dip[in1][in2];
+    weights(cell);
+    interp2c<NE>(c.table2c, cell, i0, w, v);
+    rotate_plan<PA, PB, K2C>(R, v, X);
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) c.dip[o + q] = X[q];
+  }
   if (what & 4u) {  // vna: ontop L + R into blocko; zero block
     double acc[NA * NB];
 #pragma unroll
@@ -52,12 +66,36 @@ __device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned w
       rotate_plan<PA, PB, K2C>(R, v, X);
 #pragma unroll
       for (int q = 0; q < NA * NB; q++) acc[q] = X[q] * P_eq2;
+      if constexpr (DOGS) {
+#pragma unroll 1
+        for (int isorp = 1; isorp <= fd.sp[in1].nssh; isorp++) {
+          const Cell2cDev &cs = fd.c2s[in1][in2][0][isorp - 1];
+          weights(cs);
+          interp2c<NE>(c.table2c, cs, i0, w, v);
+          rotate_plan<PA, PB, K2C>(R, v, X);
+          double dq = c.dq[i * MAXSUB + isorp - 1];
+#pragma unroll
+          for (int q = 0; q < NA * NB; q++) acc[q] = acc[q] + dq * X[q] * P_eq2;
+        }
+      }
       const Cell2cDev &cR = fd.c2[in1][in2][3];
       weights(cR);
       interp2c<NE>(c.table2c, cR, i0, w, v);
       rotate_plan<PA, PB, K2C>(R, v, X);
 #pragma unroll
       for (int q = 0; q < NA * NB; q++) acc[q] = acc[q] + X[q] * P_eq2;
+      if constexpr (DOGS) {
+#pragma unroll 1
+        for (int isorp = 1; isorp <= fd.sp[in2].nssh; isorp++) {
+          const Cell2cDev &cs = fd.c2s[in1][in2][1][isorp - 1];
+          weights(cs);
+          interp2c<NE>(c.table2c, cs, i0, w, v);
+          rotate_plan<PA, PB, K2C>(R, v, X);
+          double dq = c.dq[j * MAXSUB + isorp - 1];
+#pragma unroll
+          for (int q = 0; q < NA * NB; q++) acc[q] = acc[q] + dq * X[q] * P_eq2;
+        }
+      }
     }
 #pragma unroll
     for (int q = 0; q < NA * NB; q++) c.vbo[o + q] = acc[q];
@@ -73,25 +111,59 @@ __device__ __forceinline__ void pair_2c(const Ctx2c &c, int i, int p, unsigned w
     rotate_plan<PA, PA, K2C>(R, v, XA);
 #pragma unroll
     for (int q = 0; q < NA * NA; q++) Xatom[q] = fma(XA[q], P_eq2, Xatom[q]);
+    if constexpr (DOGS) {
+      // smoothing of the charged shells (M_assemble_2c_DOGS.f90:744-812)
+      double smooth = smoother(z, fd.sp[in1].rcmin + fd.sp[in2].rcmin, 0.8);
+      double iz = z > 1.0e-4 ? 1.0 / z : 0.0;
+#pragma unroll 1
+      for (int isorp = 1; isorp <= fd.sp[in2].nssh; isorp++) {
+        const Cell2cDev &cs = fd.c2s[in1][in2][2][isorp - 1];
+        weights(cs);
+        interp2c<NEA>(c.table2c, cs, i0, w, v);
+        rotate_plan<PA, PA, K2C>(R, v, XA);
+        double dq = c.dq[j * MAXSUB + isorp - 1];
+#pragma unroll
+        for (int q = 0; q < NA * NA; q++)
+          Xatom[q] = Xatom[q] + P_eq2 * dq * ((1.0 - smooth) * (Sself[q] * iz) + smooth * XA[q]);
+      }
+    }
   }
 }
 
-template <int PA, bool HASD>
-__device__ __forceinline__ void pair_2c_dispatch(const Ctx2c &c, int i, int p, unsigned what, double *Xatom) {
+template <int PA, bool HASD, bool DOGS>
+__device__ __forceinline__ void pair_2c_dispatch(const Ctx2c &c, int i, int p, unsigned what, double *Xatom,
+                                                 const double *Sself) {
   int pb = c.fd->sp[c.isp[c.neigh_j[p]]].pattern;
-  if (pb == PAT_SP) pair_2c<PA, PAT_SP, HASD>(c, i, p, what, Xatom);
-  else if (pb == PAT_S) pair_2c<PA, PAT_S, HASD>(c, i, p, what, Xatom);
-  else if constexpr (HASD) pair_2c<PA, PAT_SPD, HASD>(c, i, p, what, Xatom);
+  if (pb == PAT_SP) pair_2c<PA, PAT_SP, HASD, DOGS>(c, i, p, what, Xatom, Sself);
+  else if (pb == PAT_S) pair_2c<PA, PAT_S, HASD, DOGS>(c, i, p, what, Xatom, Sself);
+  else if constexpr (HASD) pair_2c<PA, PAT_SPD, HASD, DOGS>(c, i, p, what, Xatom, Sself);
 }
 
-template <int PA, bool HASD>
+template <int PA, bool HASD, bool DOGS>
 __device__ void atom_2c(const Ctx2c &c, int i, int lane, unsigned what) {
   constexpr int NA = pat_norb(PA);
   double Xatom[NA * NA];
 #pragma unroll
   for (int q = 0; q < NA * NA; q++) Xatom[q] = 0.0;
   int p0 = c.pair_off[i], p1 = c.pair_off[i + 1];
-  for (int p = p0 + lane; p < p1; p += 32) pair_2c_dispatch<PA, HASD>(c, i, p, what, Xatom);
+  double Sself[DOGS ? NA * NA : 1];
+  if (DOGS && (what & 4u)) {
+    // the self overlap block S(i, neigh_self(i)) the DOGS atom terms scale
+    // (the same interpolation and frame as the overlap pass gives it)
+    using PLA = Plan<PA, PA, K2C>;
+    int ps = p0 + c.neigh_self[i];
+    double r1[3], r2[3], z, e[3][3];
+    pair_geom(c, i, ps, r1, r2, z, e);
+    RotM R;
+    twister<HASD>(e, R);
+    const Cell2cDev &cell = c.fd->c2[c.isp[i]][c.isp[i]][0];
+    double w[7], v[PLA::m.n];
+    int i0 = 0;
+    lagrange7(z, cell, i0, w, nullptr);
+    interp2c<PLA::m.n>(c.table2c, cell, i0, w, v);
+    rotate_plan<PA, PA, K2C>(R, v, Sself);
+  }
+  for (int p = p0 + lane; p < p1; p += 32) pair_2c_dispatch<PA, HASD, DOGS>(c, i, p, what, Xatom, Sself);
   if (what & 4u) {
 #pragma unroll
     for (int q = 0; q < NA * NA; q++) {
@@ -108,13 +180,13 @@ __device__ void atom_2c(const Ctx2c &c, int i, int lane, unsigned what) {
   }
 }
 
-template <bool HASD>
+template <bool HASD, bool DOGS>
 __global__ void __launch_bounds__(256) k_assemble_2c(Ctx2c c, unsigned what, Sched q) {
   for_each_warp_item(c.N, q, [&](int i, int lane) {
     int pa = c.fd->sp[c.isp[i]].pattern;
-    if (pa == PAT_SP) atom_2c<PAT_SP, HASD>(c, i, lane, what);
-    else if (pa == PAT_S) atom_2c<PAT_S, HASD>(c, i, lane, what);
-    else if constexpr (HASD) atom_2c<PAT_SPD, HASD>(c, i, lane, what);
+    if (pa == PAT_SP) atom_2c<PAT_SP, HASD, DOGS>(c, i, lane, what);
+    else if (pa == PAT_S) atom_2c<PAT_S, HASD, DOGS>(c, i, lane, what);
+    else if constexpr (HASD) atom_2c<PAT_SPD, HASD, DOGS>(c, i, lane, what);
   });
 }
 
@@ -170,8 +242,14 @@ int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_a2c, (long long)a.N * 32, a.queue ? a.queue + 0 : nullptr, s, grid, block, q);
   if (e) return e;
-  if (a.have_d) k_assemble_2c<true><<<grid, block, 0, s>>>(c, what, q);
-  else k_assemble_2c<false><<<grid, block, 0, s>>>(c, what, q);
+  bool dogs = a.dogs && (what & 4u);
+  if (a.have_d) {
+    if (dogs) k_assemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
+    else k_assemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
+  } else {
+    if (dogs) k_assemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
+    else k_assemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
+  }
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -33,7 +33,21 @@ struct Ctx2c {
   const long long *blk_off;
   double *S, *T, *vb, *vbo;
   unsigned *status;
+  // DOGS: shell charges dq[atom * MAXSUB + isorp - 1] and the z-dipole blocks
+  int dogs;
+  const double *dq;
+  double *dip;
 };
+
+// smoother (b.FUNCTIONS/smoother.f90:100-146), the scaler = 1 branch
+__device__ __forceinline__ double smoother(double r, double rend, double x) {
+  double rbegin = x * rend;
+  if (r > rend) return 0.0;
+  if (r < rbegin) return 1.0;
+  double ratio = (r - rbegin) / (rend - rbegin);
+  double sm = 1.0 - ratio * ratio;
+  return sm * sm;
+}
 
 __device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
                                           double e[3][3]) {
@@ -102,6 +116,10 @@ struct Ctx3c {
   const df *rho_df;
   // MLP-3c results per list position (F or F, dF/dcos, dF/dx, dF/dy; 10 each)
   const float *mlpF;
+  // DOGS: shell charges, overlap and z-dipole blocks of the pairs
+  int dogs;
+  const double *dq;
+  const double *S, *dip;
 };
 
 struct TripGeom {
@@ -348,6 +366,9 @@ inline Ctx2c make2c(const AsmArgs &a) {
   c.vb = a.vb;
   c.vbo = a.vbo;
   c.status = a.status;
+  c.dogs = a.dogs;
+  c.dq = a.dq;
+  c.dip = a.dip;
   return c;
 }
 
@@ -379,6 +400,10 @@ inline Ctx3c make3c(const AsmArgs &a) {
   c.table3c_df = reinterpret_cast<const df *>(a.table3c_df);
   c.rho_df = reinterpret_cast<const df *>(a.rho_df);
   c.mlpF = a.mlpF;
+  c.dogs = a.dogs;
+  c.dq = a.dq;
+  c.S = a.S;
+  c.dip = a.dip;
   return c;
 }
 

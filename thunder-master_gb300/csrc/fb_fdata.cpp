@@ -189,10 +189,12 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
       if (!read_dbls(t, 1, &ae)) goto bad_info;
       t.skip();
       sp.rcA = -99.0;
+      sp.rcmin = 99.0;
       sp.norb = 0;
       for (int k = 0; k < sp.nssh; k++) {
         double r = rc[k] * P_abohr;  // M_species.f90:1164-1167
         if (r > sp.rcA) sp.rcA = r;
+        sp.rcmin = std::fmin(sp.rcmin, r);  // M_assemble_2c_DOGS.f90:746-754
         sp.norb += 2 * sp.lssh[k] + 1;
       }
     }
@@ -219,6 +221,7 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
 info_done:
 
   // ---- read_Fdata_2c --------------------------------------------------------
+  bool dogs_ok = true;  // every DOGS sub-cell and z-dipole table found
   for (int is = 0; is < nspecies; is++) {
     for (int js = 0; js < nspecies; js++) {
       std::string pz = zz(out.sp[is].nZ) + "." + zz(out.sp[js].nZ);
@@ -285,19 +288,17 @@ info_done:
           return FB_ERR_IO;
         }
       }
-      // stage the five Harris interactions (isub = 0)
+      // stage cell (itype, isub) into d: 0 staged, 1 absent, else an error
       int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
-      for (int it = 1; it <= 5; it++) {
-        int k = index[it][0];
-        Cell2cDev &d = out.dev.c2[is][js][it - 1];
-        if (k < 1 || k > ncell) {
-          err = "2c table " + pz + " lacks interaction " + std::to_string(it);
-          return FB_ERR_TABLE;
-        }
+      auto stage = [&](int it, int isub, Cell2cDev &d) -> int {
+        int k = index[it][isub];
+        d.off = -1;
+        if (k < 1 || k > ncell) return 1;
         const Cell2 &c = cells[k - 1];
         MEMap m = make_munu(PA, it == 5 ? PA : PB);
         if (!map_equal(c, m)) {
-          err = "2c table " + pz + " interaction " + std::to_string(it) + " has a non-canonical ME map";
+          err = "2c table " + pz + " interaction " + std::to_string(it) + " sub " + std::to_string(isub) +
+                " has a non-canonical ME map";
           return FB_ERR_UNSUPPORTED;
         }
         d.nx = c.nx;
@@ -309,6 +310,34 @@ info_done:
         d.off = (long long)out.table2c.size();
         for (int ix = 0; ix < c.nx; ix++)
           for (int e = 0; e < c.nME; e++) out.table2c.push_back(c.F[ix + (size_t)c.nx * e]);
+        return 0;
+      };
+      // the five Harris interactions (isub = 0)
+      for (int it = 1; it <= 5; it++) {
+        int r = stage(it, 0, out.dev.c2[is][js][it - 1]);
+        if (r == 1) {
+          err = "2c table " + pz + " lacks interaction " + std::to_string(it);
+          return FB_ERR_TABLE;
+        }
+        if (r) return r;
+      }
+      // DOGS: charged-shell sub-cells of vna ontop L (shells of the first
+      // species), ontop R and atom (shells of the second), and dipole_z
+      int nsub[3] = {out.sp[is].nssh, out.sp[js].nssh, out.sp[js].nssh};
+      for (int q = 0; q < 3; q++)
+        for (int isorp = 1; isorp <= MAXSUB; isorp++) {
+          Cell2cDev &d = out.dev.c2s[is][js][q][isorp - 1];
+          d.off = -1;
+          if (isorp > nsub[q]) continue;
+          int r = stage(3 + q, isorp, d);
+          if (r == 1) dogs_ok = false;
+          else if (r) return r;
+        }
+      if (nsub[0] > MAXSUB || nsub[1] > MAXSUB) dogs_ok = false;
+      {
+        int r = stage(10, 0, out.dev.c2dip[is][js]);
+        if (r == 1) dogs_ok = false;
+        else if (r) return r;
       }
     }
     // clPP.ZZ.dat is opened unconditionally (M_Fdata_2c.f90:252-258)
@@ -401,56 +430,74 @@ info_done:
             return FB_ERR_IO;
           }
         }
-        // stage bcna (interaction 3, isub 0), theta 1..5
+        // stage bcna (interaction 3) sub-cell isub, theta 1..5: 0 staged,
+        // 1 absent, else an error
         int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
         MEMap m = make_munu_3c(PA, PB);
-        const Cell3 *th[NTHETA];
-        for (int it = 1; it <= NTHETA; it++) {
-          int k = index[3][0][it];
-          if (k < 1 || k > ncell) {
-            err = "3c table " + pz + " lacks bcna theta " + std::to_string(it);
-            return FB_ERR_TABLE;
-          }
-          th[it - 1] = &cells[k - 1];
-          if (!map_equal3(*th[it - 1], m)) {
-            err = "3c table " + pz + " has a non-canonical ME map";
-            return FB_ERR_UNSUPPORTED;
-          }
-          if (th[it - 1]->nx != th[0]->nx || th[it - 1]->ny != th[0]->ny) {
-            err = "3c table " + pz + ": theta cells on different grids";
-            return FB_ERR_UNSUPPORTED;
-          }
-        }
-        const Cell3 &c1 = *th[0];
-        Cell3cDev &d = out.dev.c3[is][js][ks];
-        d.nx = c1.nx;
-        d.ny = c1.ny;
-        d.nME = c1.nME;
-        d.xmax = c1.xmax;
-        d.ymax = c1.ymax;
-        d.dx = c1.xmax / (c1.nx - 1.0);  // M_Fdata_3c.f90:367-368
-        d.dy = c1.ymax / (c1.ny - 1.0);
-        d.off = (long long)out.table3c.size();
-        d.node_off = (long long)out.lin.size();
-        for (int iy = 0; iy < c1.ny; iy++)
-          for (int ix = 0; ix < c1.nx; ix++) {
-            for (int it = 0; it < NTHETA; it++)
-              for (int e = 0; e < c1.nME; e++)
-                out.table3c.push_back(th[it]->F[ix + (size_t)c1.nx * (iy + (size_t)c1.ny * e)]);
-            // gradient switch from theta 1, ME 1 (M_Fdata_3c.f90:383-385)
-            double gx = 0.0, gy = 0.0;
-            unsigned char lin = 0;
-            if (ix + 1 < c1.nx && iy + 1 < c1.ny) {
-              double f00 = c1.F[ix + (size_t)c1.nx * iy];
-              gx = (c1.F[(ix + 1) + (size_t)c1.nx * iy] - f00) / d.dx;
-              gy = (c1.F[ix + (size_t)c1.nx * (iy + 1)] - f00) / d.dy;
-              double gg = gx * gx + gy * gy;
-              lin = gg < 1.0e-6 ? 1 : 0;
+        auto stage3 = [&](int isub, Cell3cDev &d) -> int {
+          d.off = -1;
+          const Cell3 *th[NTHETA];
+          for (int it = 1; it <= NTHETA; it++) {
+            int k = index[3][isub][it];
+            if (k < 1 || k > ncell) return 1;
+            th[it - 1] = &cells[k - 1];
+            if (!map_equal3(*th[it - 1], m)) {
+              err = "3c table " + pz + " sub " + std::to_string(isub) + " has a non-canonical ME map";
+              return FB_ERR_UNSUPPORTED;
             }
-            out.lin.push_back(lin);
-            out.gxy.push_back(gx);
-            out.gxy.push_back(gy);
+            if (th[it - 1]->nx != th[0]->nx || th[it - 1]->ny != th[0]->ny) {
+              err = "3c table " + pz + ": theta cells on different grids";
+              return FB_ERR_UNSUPPORTED;
+            }
           }
+          const Cell3 &c1 = *th[0];
+          d.nx = c1.nx;
+          d.ny = c1.ny;
+          d.nME = c1.nME;
+          d.xmax = c1.xmax;
+          d.ymax = c1.ymax;
+          d.dx = c1.xmax / (c1.nx - 1.0);  // M_Fdata_3c.f90:367-368
+          d.dy = c1.ymax / (c1.ny - 1.0);
+          d.off = (long long)out.table3c.size();
+          d.node_off = (long long)out.lin.size();
+          for (int iy = 0; iy < c1.ny; iy++)
+            for (int ix = 0; ix < c1.nx; ix++) {
+              for (int it = 0; it < NTHETA; it++)
+                for (int e = 0; e < c1.nME; e++)
+                  out.table3c.push_back(th[it]->F[ix + (size_t)c1.nx * (iy + (size_t)c1.ny * e)]);
+              // gradient switch from theta 1, ME 1 (M_Fdata_3c.f90:383-385)
+              double gx = 0.0, gy = 0.0;
+              unsigned char lin = 0;
+              if (ix + 1 < c1.nx && iy + 1 < c1.ny) {
+                double f00 = c1.F[ix + (size_t)c1.nx * iy];
+                gx = (c1.F[(ix + 1) + (size_t)c1.nx * iy] - f00) / d.dx;
+                gy = (c1.F[ix + (size_t)c1.nx * (iy + 1)] - f00) / d.dy;
+                double gg = gx * gx + gy * gy;
+                lin = gg < 1.0e-6 ? 1 : 0;
+              }
+              out.lin.push_back(lin);
+              out.gxy.push_back(gx);
+              out.gxy.push_back(gy);
+            }
+          return 0;
+        };
+        int r = stage3(0, out.dev.c3[is][js][ks]);
+        if (r == 1) {
+          err = "3c table " + pz + " lacks bcna";
+          return FB_ERR_TABLE;
+        }
+        if (r) return r;
+        // DOGS: the neutral atom's charged shells isorp = 1..nssh
+        int nk = out.sp[ks].nssh;
+        if (nk > MAXSUB) dogs_ok = false;
+        for (int isorp = 1; isorp <= MAXSUB; isorp++) {
+          Cell3cDev &dd = out.dev.c3s[is][js][ks][isorp - 1];
+          dd.off = -1;
+          if (isorp > nk) continue;
+          r = stage3(isorp, dd);
+          if (r == 1) dogs_ok = false;
+          else if (r) return r;
+        }
       }
 
   // double-float copy of the 3c values: hi = nearest float, lo = nearest
@@ -468,7 +515,10 @@ info_done:
     out.dev.sp[k].pattern = out.sp[k].pattern;
     out.dev.sp[k].norb = out.sp[k].norb;
     out.dev.sp[k].rcA = out.sp[k].rcA;
+    out.dev.sp[k].nssh = out.sp[k].nssh;
+    out.dev.sp[k].rcmin = out.sp[k].rcmin;
   }
+  out.dev.have_dogs = dogs_ok ? 1 : 0;
   return FB_OK;
 }
 

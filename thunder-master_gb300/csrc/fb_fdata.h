@@ -10,6 +10,7 @@ struct SpeciesHost {
   int nZ = 0, nssh = 0, norb = 0, pattern = -1, nssh_pp = 0;
   int lssh[8] = {0};
   double rcA = 0.0;
+  double rcmin = 99.0;
 };
 
 struct FdataHost {

@@ -24,6 +24,7 @@ constexpr int XL_STRIDE = 3 * NIMG;
 // MLP-3c results per triplet: 10 values (the bcna matrix elements of an sp x
 // sp pair), and in the force pass 4 such rows: F, dF/dcos, dF/dx, dF/dy
 constexpr int MLP_ME_STRIDE = 10;
+constexpr int MAXSUB = 3;        // charged-shell sub-cells (isorp = 1..nssh) of the DOGS tables
 
 // Basis patterns: the shell lists this build compiles rotation code for.
 // PAT_S = [s], PAT_SP = [s, p], PAT_SPD = [s, p, d]; orbital order inside a
@@ -139,7 +140,9 @@ __host__ __device__ constexpr MEMap make_munu_3c(int PA, int PB) {
 struct SpeciesDev {
   int pattern;   // PAT_*
   int norb;
+  int nssh;      // shells
   double rcA;    // max shell cutoff, Angstrom
+  double rcmin;  // min shell cutoff from 99, Angstrom (the DOGS smoothing range)
 };
 
 // One 2c interaction cell (T_Fdata_cell_2c, e.FDATA/M_Fdata_2c.f90:83-96).
@@ -166,9 +169,15 @@ struct Cell3cDev {
 struct FdataDev {
   int nspecies;
   int have_d;
+  int have_dogs;  // the DOGS sub-cells and the z-dipole table are present
   SpeciesDev sp[MAXSP];
   Cell2cDev c2[MAXSP][MAXSP][5];       // itype 1..5 -> [itype-1]
   Cell3cDev c3[MAXSP][MAXSP][MAXSP];   // (in1, in2, indna)
+  // DOGS: charged-shell sub-cells isorp = 1..nssh of vna_ontopL, vna_ontopR,
+  // vna_atom ([0..2][isorp-1]) and bcna, and the z-dipole table (itype 10)
+  Cell2cDev c2s[MAXSP][MAXSP][3][MAXSUB];
+  Cell2cDev c2dip[MAXSP][MAXSP];
+  Cell3cDev c3s[MAXSP][MAXSP][MAXSP][MAXSUB];
 };
 
 // device status flags (bit mask, OR-ed by kernels)

@@ -81,6 +81,10 @@ struct AsmArgs {
   float2 *rho_df;            // hi, lo float pairs of rho
   // MLP-3c: per list position, the network's values (and derivatives)
   const float *mlpF;
+  // DOGS (charge-weighted neutral atom): shell charges [atom][MAXSUB], z-dipole blocks
+  int dogs;
+  const double *dq;
+  double *dip;
   // launch shapes (autotuned) and the work counters of persistent launches
   KCfg cfg_a2c, cfg_a3c, cfg_d2c, cfg_d3c;
   int *queue;  // 4 counters: assemble_2c, assemble_3c, dassemble_2c, dassemble_3c

@@ -19,6 +19,10 @@ Context.assemble_vna_2c  assemble_vna_2c                              j.ASSEMBLE
 Context.assemble_vna_3c  assemble_vna_3c                              j.ASSEMBLERS/M_assemble_3c_Harris.f90:82
 Context.Dassemble_*    Dassemble_S / _T / _vna_2c / _vna_3c           k.DASSEMBLERS/M_Dassemble_{2c,3c}_Harris.f90
 Context.build_forces   build_forces (assembly terms)                  c.SYSTEM/M_build_forces.f90:172
+Context.set_theory     DOGS instead of Harris vna 2c / 3c             j.ASSEMBLERS/M_assemble_2c_DOGS.f90:640,
+                                                                      j.ASSEMBLERS/M_assemble_3c_DOGS.f90:158
+Context.assemble_dipole_z  assemble_dipole_z                          j.ASSEMBLERS/M_assemble_2c_DOGS.f90:376
+Context.bloch          Bloch sums into H(k), S(k)                     h.SOLVESH/M_kspace_Lowdin.f90:680
 =====================  =============================================  ====================================
 
 There is no CPU fallback: every call runs on the GPU through the native
@@ -35,10 +39,12 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
+FB_DIPOLE = 64
+FB_THEORY_HARRIS, FB_THEORY_DOGS = 0, 1
 FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
 FB_MLP_ENGINE_MMA, FB_MLP_ENGINE_TC = 0, 1
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
-BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7}
+BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7, "dip": 8}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8}
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
@@ -108,6 +114,8 @@ _SIGS = {
     "fb_probe_fp32": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fb_dassemble_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
+    "fb_set_theory": (C.c_int, [C.c_void_p, C.c_int]),
+    "fb_set_charges": (C.c_int, [C.c_void_p, _dp, C.c_int]),
 }
 
 FB_PREC_FP64, FB_PREC_DF = 0, 1
@@ -181,6 +189,23 @@ class Context:
         """FB_PREC_DF (default): three-center contractions in double-float
         on the FP32 pipe; FB_PREC_FP64: everything in FP64."""
         self._check(self.L.fb_set_precision(self.h, int(mode)))
+
+    def set_theory(self, theory):
+        """FB_THEORY_HARRIS (default) or FB_THEORY_DOGS: the charge-weighted
+        neutral-atom terms of M_assemble_2c_DOGS.f90 / M_assemble_3c_DOGS.f90
+        (value pass, FP64 kernels)."""
+        self._check(self.L.fb_set_theory(self.h, int(theory)))
+
+    def set_charges(self, dq):
+        """DOGS shell charges Qin - Qneutral, one row per atom (natoms, nssh_max)."""
+        d = np.ascontiguousarray(dq, np.float64)
+        if d.ndim == 1:
+            d = d.reshape(-1, 1)
+        self._check(self.L.fb_set_charges(self.h, np.ascontiguousarray(d.reshape(-1)), int(d.shape[1])))
+
+    def assemble_dipole_z(self):
+        """z-dipole blocks (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499)."""
+        self._check(self.L.fb_assemble(self.h, FB_DIPOLE))
 
     def set_stream(self, stream_ptr):
         self._check(self.L.fb_set_stream(self.h, C.c_void_p(stream_ptr)))
