@@ -350,8 +350,13 @@ int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
  * effective monopole of the overlap and z-dipole blocks.  DOGS needs Fdata
  * with the sub-cells and dipole_z tables (FB_ERR_TABLE otherwise) and
  * fb_set_charges; it runs the FP64 kernels and the tables only (no MLP-3c
- * routing).  Its force pass (Dassemble_*_DOGS) is not built: fb_dassemble
- * and FB_FORCES return FB_ERR_UNSUPPORTED in DOGS. */
+ * routing).  fb_dassemble then computes the DOGS force pass
+ * (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90:679-1199, M_Dassemble_3c_DOGS.f90:
+ * 136-520): the charged ontop and atom derivatives with the smoother and
+ * monopole terms, and the charged three-center terms from the overlap and
+ * z-dipole blocks and their derivatives, into the same force arrays as
+ * Harris (vna_ontop, vna_atom, f3na*, ftot).  fb_dassemble_noalloc stays
+ * Harris-only (FB_ERR_UNSUPPORTED in DOGS). */
 #define FB_THEORY_HARRIS 0
 #define FB_THEORY_DOGS 1
 int fb_set_theory(fb_ctx *ctx, int theory);

@@ -1881,3 +1881,231 @@ int or_assemble_vna_3c_dogs(or_sys *s, const double *S, const double *dip, doubl
   }
   return err;
 }
+
+/* Dsmoother (b.FUNCTIONS/Dsmoother.f90:102-135), scaler = 1 */
+static double dsmoother(double r, double rend, double x) {
+  double rbegin = x * rend;
+  if (r > rend) return 0.0;
+  if (r < rbegin) return 0.0;
+  double ratio = (r - rbegin) / (rend - rbegin);
+  return -2.0 * (1.0 - ratio * ratio) * (2.0 * ratio) / (rend - rbegin);
+}
+
+/* Dassemble_dipole_z (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90:487-655):
+ * Dblock(3, mu, nu) of the z-dipole, layout of dS */
+int or_dassemble_dipole_z(or_sys *s, double *ddip) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    double r1[3], r2[3], z, eps[9], deps[27], eta[3];
+    double mm[MAXORB * MAXORB], dm[MAXORB * MAXORB], vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      for (int k = 0; k < nmu * nnu; k++) mm[k] = dm[k] = 0.0;
+      for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = 0.0;
+      if ((st = or_getDMEs_2c(fd, in1, in2, P_dipole_z, 0, z, nmu, nnu, mm, dm))) { err = st; continue; }
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++)
+          if (z > 1.0e-3)
+            for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+      drotate(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+      memcpy(ddip + 3 * s->blk_off[p], vdx, sizeof(double) * 3 * nmu * nnu);
+    }
+  }
+  return err;
+}
+
+/* Dassemble_vna_2c, DOGS (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90:679-1199):
+ * the Harris ontop and atom derivatives plus the charged shells -- ontop L
+ * weighted by the shells of iatom, ontop R by those of jatom; the atom terms
+ * smoothed, with the derivative of the smoother and of the monopole S/z.
+ * S is the overlap block set. */
+int or_dassemble_vna_2c_dogs(or_sys *s, const double *rho, const double *S, double *vna_ontop, double *vna_atom) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    double r1[3], r2[3], z, eps[9], deps[27], eta[3];
+    double mm[MAXORB * MAXORB], dm[MAXORB * MAXORB], vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+    double xm[MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      long long o = s->blk_off[p];
+      double *f = vna_ontop + 3 * (size_t)p;
+      f[0] = f[1] = f[2] = 0.0;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      const int vi[2] = {P_vna_ontopL, P_vna_ontopR};
+      for (int w = 0; w < 2; w++) {
+        int owner = w == 0 ? i : j, nsh = fd->sp[w == 0 ? in1 : in2].nssh;
+        for (int isorp = 0; isorp <= nsh; isorp++) {
+          double dq = isorp == 0 ? 1.0 : shell_dq(s, owner, isorp);
+          for (int k = 0; k < nmu * nnu; k++) mm[k] = dm[k] = 0.0;
+          for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = vdx[k] = 0.0;
+          if ((st = or_getDMEs_2c(fd, in1, in2, vi[w], isorp, z, nmu, nnu, mm, dm))) { err = st; continue; }
+          for (int inu = 0; inu < nnu; inu++)
+            for (int imu = 0; imu < nmu; imu++)
+              if (z > 1.0e-3)
+                for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+          drotate(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+          for (int inu = 0; inu < nnu; inu++)
+            for (int imu = 0; imu < nmu; imu++)
+              for (int c = 0; c < 3; c++) {
+                double r = rho[o + imu + nmu * inu];
+                if (isorp == 0) f[c] = f[c] - r * vdx[c + 3 * (imu + nmu * inu)] * P_eq2;
+                else f[c] = f[c] - r * dq * vdx[c + 3 * (imu + nmu * inu)] * P_eq2;
+              }
+        }
+      }
+    }
+    /* atom case (:1004-1196), contracted with the self blocks of rho and S */
+    long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      double *f = vna_atom + 3 * (size_t)p;
+      f[0] = f[1] = f[2] = 0.0;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      double rend = rcutoff_min(&fd->sp[in1]) + rcutoff_min(&fd->sp[in2]);
+      double smooth = smoother(z, rend, 0.8), dsmooth = dsmoother(z, rend, 0.8);
+      for (int isorp = 0; isorp <= fd->sp[in2].nssh; isorp++) {
+        for (int k = 0; k < nmu * nmu; k++) mm[k] = dm[k] = xm[k] = 0.0;
+        for (int k = 0; k < 3 * nmu * nmu; k++) vdm[k] = vdx[k] = 0.0;
+        if ((st = or_getDMEs_2c(fd, in1, in2, P_vna_atom, isorp, z, nmu, nmu, mm, dm))) { err = st; continue; }
+        if (isorp == 0) {
+          for (int inu = 0; inu < nmu; inu++)
+            for (int imu = 0; imu < nmu; imu++)
+              if (z > 1.0e-3)
+                for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+          drotate(fd, in1, in1, eps, deps, nmu, nmu, mm, vdm, vdx);
+          for (int inu = 0; inu < nmu; inu++)
+            for (int imu = 0; imu < nmu; imu++)
+              for (int c = 0; c < 3; c++)
+                f[c] = f[c] - rho[os + imu + nmu * inu] * vdx[c + 3 * (imu + nmu * inu)] * P_eq2;
+          continue;
+        }
+        double dq = shell_dq(s, j, isorp);
+        double emnpl[MAXORB * MAXORB], vdemnpl[3 * MAXORB * MAXORB];
+        for (int k = 0; k < nmu * nmu; k++) emnpl[k] = 0.0;
+        for (int k = 0; k < 3 * nmu * nmu; k++) vdemnpl[k] = 0.0;
+        for (int inu = 0; inu < nmu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            if (z > 1.0e-4) {
+              int k = imu + nmu * inu;
+              for (int c = 0; c < 3; c++) vdm[c + 3 * k] = -eta[c] * dm[k];
+              emnpl[k] = S[os + k] / z;
+              for (int c = 0; c < 3; c++) vdemnpl[c + 3 * k] = eta[c] * S[os + k] / (z * z);
+            }
+        or_rotate(fd, in1, in1, eps, nmu, nmu, mm, xm);
+        drotate(fd, in1, in1, eps, deps, nmu, nmu, mm, vdm, vdx);
+        for (int inu = 0; inu < nmu; inu++)
+          for (int imu = 0; imu < nmu; imu++) {
+            int k = imu + nmu * inu;
+            for (int c = 0; c < 3; c++)
+              f[c] = f[c] - rho[os + k] * P_eq2 * dq *
+                                (smooth * vdx[c + 3 * k] - eta[c] * dsmooth * xm[k] +
+                                 (1.0 - smooth) * vdemnpl[c + 3 * k] + eta[c] * dsmooth * emnpl[k]);
+          }
+      }
+    }
+  }
+  return err;
+}
+
+/* Dassemble_vna_3c, DOGS (k.DASSEMBLERS/M_Dassemble_3c_DOGS.f90:136-520):
+ * the Harris (neutral) term plus, for the charged shells of ialpha, the
+ * smoothed sub-cell derivatives with the derivatives of the smoothers
+ * (dstn) and of the effective monopole (demnpl), from the overlap and
+ * z-dipole blocks of the pair (i, mneigh) and their Dblocks dS, ddip. */
+int or_dassemble_vna_3c_dogs(or_sys *s, const double *rho, const double *S, const double *dS, const double *dip,
+                             const double *ddip, double *f3naa, double *f3nab, double *f3nac) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+  if ((err = or_dassemble_3c(s, rho, f3naa, f3nab, f3nac))) return err;
+  for (int ia = 0; ia < N; ia++) {
+    double mm[MAXORB * MAXORB], xm[MAXORB * MAXORB], dpm[MAXORB * MAXORB], dxm[MAXORB * MAXORB],
+        dym[MAXORB * MAXORB];
+    double Ma[3 * MAXORB * MAXORB], Mb[3 * MAXORB * MAXORB], Xa[3 * MAXORB * MAXORB], Xb[3 * MAXORB * MAXORB];
+    double emnpl[MAXORB * MAXORB], dA[3 * MAXORB * MAXORB], dB[3 * MAXORB * MAXORB];
+    double depsA[27], depsB[27], amt[3], bmt[3], rA1[3] = {0, 0, 0}, rA2[3] = {0, 0, 0};
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      or_depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.eps, depsA, depsB);
+      double d13 = distance3(g.rna, g.r1), d23 = distance3(g.rna, g.r2);
+      if (d13 > 1.0e-5)
+        for (int k = 0; k < 3; k++) rA1[k] = (g.rna[k] - g.r1[k]) / d13;
+      if (d23 > 1.0e-5)
+        for (int k = 0; k < 3; k++) rA2[k] = (g.rna[k] - g.r2[k]) / d23;
+      if (g.x > 1.0e-5)
+        for (int k = 0; k < 3; k++) amt[k] = (g.sighat[k] - g.cost * g.rhat[k]) / g.x;
+      else
+        amt[0] = amt[1] = amt[2] = 0.0;
+      for (int k = 0; k < 3; k++) bmt[k] = (g.cost * g.sighat[k] - g.rhat[k]) / g.z;
+      double rc3 = rcutoff_min(&fd->sp[g.indna]);
+      double rend1 = rcutoff_min(&fd->sp[g.in1]) + rc3, rend2 = rcutoff_min(&fd->sp[g.in2]) + rc3;
+      double s13 = smoother(d13, rend1, 0.8), ds13 = dsmoother(d13, rend1, 0.8);
+      double s23 = smoother(d23, rend2, 0.8), ds23 = dsmoother(d23, rend2, 0.8);
+      double stinky = s13 * s23, dstnA[3], dstnB[3], dstnC[3];
+      for (int k = 0; k < 3; k++) {
+        dstnB[k] = -ds13 * s23 * rA1[k];
+        dstnC[k] = -s13 * ds23 * rA2[k];
+        dstnA[k] = -dstnB[k] - dstnC[k];
+      }
+      long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          int k = imu + nmu * inu;
+          double sterm = S[o + k] / 2.0, dterm = dip[o + k] / g.z;
+          emnpl[k] = (sterm - dterm) / d13 + (sterm + dterm) / d23;
+          for (int c = 0; c < 3; c++) {
+            double spterm = dS[3 * (o + k) + c] / 2.0;
+            double dpterm = ddip[3 * (o + k) + c] / g.z + dterm * g.sighat[c] / g.z;
+            dA[c + 3 * k] = -(sterm - dterm) * rA1[c] / (d13 * d13) - (sterm + dterm) * rA2[c] / (d23 * d23);
+            dB[c + 3 * k] = (sterm - dterm) * rA1[c] / (d13 * d13) + (spterm - dpterm) / d13 +
+                            (spterm + dpterm) / d23;
+          }
+        }
+      for (int isorp = 1; isorp <= fd->sp[g.indna].nssh; isorp++) {
+        int st = or_getDMEs_3c(fd, g.in1, g.in2, g.indna, P_bcna, isorp, g.x, g.z, nmu, nnu, g.cost, mm, dpm, dxm,
+                               dym);
+        if (st) { err = st; continue; }
+        or_rotate(fd, g.in1, g.in2, g.eps, nmu, nnu, mm, xm);
+        for (int k = 0; k < 3 * nmu * nnu; k++) Ma[k] = Mb[k] = 0.0;
+        cell3c *c = get_cell3c(fd, g.in1, g.in2, g.indna, P_bcna, isorp, 1);
+        for (int m = 0; m < c->nME; m++) {
+          int k = (c->mu[m] - 1) + nmu * (c->nu[m] - 1);
+          for (int q = 0; q < 3; q++) Ma[q + 3 * k] = g.rhat[q] * dxm[k] + amt[q] * dpm[k];
+          for (int q = 0; q < 3; q++) Mb[q + 3 * k] = -g.sighat[q] * dym[k] + bmt[q] * dpm[k] - Ma[q + 3 * k] / 2.0;
+        }
+        drotate(fd, g.in1, g.in2, g.eps, depsA, nmu, nnu, mm, Ma, Xa);
+        drotate(fd, g.in1, g.in2, g.eps, depsB, nmu, nnu, mm, Mb, Xb);
+        double dq = shell_dq(s, ia, isorp);
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++) {
+            int k = imu + nmu * inu;
+            double r = rho[o + k];
+            for (int q = 0; q < 3; q++) {
+              double xa = Xa[q + 3 * k], xb = Xb[q + 3 * k], xc = -xa - xb;
+              double dC = -dA[q + 3 * k] - dB[q + 3 * k];
+              f3naa[3 * ia + q] = f3naa[3 * ia + q] - P_eq2 * dq * r *
+                  (stinky * xa + dstnA[q] * xm[k] - dstnA[q] * emnpl[k] + (1.0 - stinky) * dA[q + 3 * k]);
+              f3nab[3 * g.iatom + q] = f3nab[3 * g.iatom + q] - P_eq2 * dq * r *
+                  (stinky * xb + dstnB[q] * xm[k] - dstnB[q] * emnpl[k] + (1.0 - stinky) * dB[q + 3 * k]);
+              f3nac[3 * g.jatom + q] = f3nac[3 * g.jatom + q] - P_eq2 * dq * r *
+                  (stinky * xc + dstnC[q] * xm[k] - dstnC[q] * emnpl[k] + (1.0 - stinky) * dC);
+            }
+          }
+      }
+    }
+  }
+  return err;
+}

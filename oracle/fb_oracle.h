@@ -89,6 +89,16 @@ int or_assemble_vna_2c_dogs(or_sys *s, const double *S, double *vb,
                             double *vbo);
 int or_assemble_vna_3c_dogs(or_sys *s, const double *S, const double *dip,
                             double *vb);
+/* DOGS force derivatives (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90,
+ * M_Dassemble_3c_DOGS.f90): z-dipole Dblocks; vna ontop / atom pair terms;
+ * f3na{a,b,c} (neutral + charged; overwrites) from S, dS, dip, ddip */
+int or_dassemble_dipole_z(or_sys *s, double *ddip);
+int or_dassemble_vna_2c_dogs(or_sys *s, const double *rho, const double *S,
+                             double *vna_ontop, double *vna_atom);
+int or_dassemble_vna_3c_dogs(or_sys *s, const double *rho, const double *S,
+                             const double *dS, const double *dip,
+                             const double *ddip, double *f3naa,
+                             double *f3nab, double *f3nac);
 
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */

@@ -58,6 +58,9 @@ def lib():
         L.or_assemble_dipole_z.argtypes = [C.c_void_p, _dp]
         L.or_assemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_assemble_vna_3c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.or_dassemble_dipole_z.argtypes = [C.c_void_p, _dp]
+        L.or_dassemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.or_dassemble_vna_3c_dogs.argtypes = [C.c_void_p] + [_dp] * 8
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
         L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     _dp, _dp]
@@ -208,6 +211,31 @@ class System:
         kin, vna, pul, ftot = (np.zeros(3 * N) for _ in range(4))
         _check(L.or_build_forces(self.h, rho, cape, dS, dT, ontop, atom, fa, fb, fc, kin, vna, pul, ftot))
         return dict(dS=dS, dT=dT, vna_ontop=ontop, vna_atom=atom, f3naa=fa, f3nab=fb, f3nac=fc,
+                    kinetic=kin, vna=vna, pulay=pul, ftot=ftot)
+
+    def dassemble_dogs(self, rho, cape, dQ):
+        """DOGS force pass: the Harris S, T, Pulay and kinetic terms, the DOGS
+        vna ontop / atom and f3na terms, and build_forces, with shell
+        charges dQ (natoms, nssh_max)."""
+        L = lib()
+        nb, P, N = self.nblock, self.npairs, len(self.imass)
+        d = np.ascontiguousarray(dQ, np.float64).reshape(N, -1)
+        _check(L.or_set_charges(self.h, np.ascontiguousarray(d.ravel()), d.shape[1]))
+        rho = np.ascontiguousarray(rho, np.float64)
+        cape = np.ascontiguousarray(cape, np.float64)
+        S, T, vb, vbo, dip = (np.zeros(nb) for _ in range(5))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        _check(L.or_assemble_dipole_z(self.h, dip))
+        dS, dT, ddip = np.zeros(3 * nb), np.zeros(3 * nb), np.zeros(3 * nb)
+        ontop, atom = np.zeros(3 * P), np.zeros(3 * P)
+        _check(L.or_dassemble_2c(self.h, rho, dS, dT, ontop, atom))
+        _check(L.or_dassemble_dipole_z(self.h, ddip))
+        _check(L.or_dassemble_vna_2c_dogs(self.h, rho, S, ontop, atom))
+        fa, fb, fc = np.zeros(3 * N), np.zeros(3 * N), np.zeros(3 * N)
+        _check(L.or_dassemble_vna_3c_dogs(self.h, rho, S, dS, dip, ddip, fa, fb, fc))
+        kin, vna, pul, ftot = (np.zeros(3 * N) for _ in range(4))
+        _check(L.or_build_forces(self.h, rho, cape, dS, dT, ontop, atom, fa, fb, fc, kin, vna, pul, ftot))
+        return dict(dS=dS, dT=dT, ddip=ddip, vna_ontop=ontop, vna_atom=atom, f3naa=fa, f3nab=fb, f3nac=fc,
                     kinetic=kin, vna=vna, pulay=pul, ftot=ftot)
 
 

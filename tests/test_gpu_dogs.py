@@ -1,9 +1,11 @@
-"""DOGS value pass on the GPU (fb_set_theory(FB_THEORY_DOGS)) against the
-oracle's restatement of assemble_vna_2c / assemble_vna_3c / assemble_dipole_z
-of j.ASSEMBLERS/M_assemble_2c_DOGS.f90 and M_assemble_3c_DOGS.f90: every
-block set to 1e-10 eV per element, for one- and two-species systems and for
-a batch; zero charges give the Harris blocks; the call-order and capability
-errors the interface states."""
+"""DOGS on the GPU (fb_set_theory(FB_THEORY_DOGS)) against the oracle's
+restatement of assemble_vna_2c / assemble_vna_3c / assemble_dipole_z
+(j.ASSEMBLERS/M_assemble_{2c,3c}_DOGS.f90) and Dassemble_vna_2c /
+Dassemble_vna_3c (k.DASSEMBLERS/M_Dassemble_{2c,3c}_DOGS.f90): every block
+set to 1e-10 eV per element and every force array to 1e-10 eV/Angstrom per
+component, for one- and two-species systems and for a batch, plain and as
+one CUDA graph; zero charges give the Harris results; the call-order and
+capability errors the interface states."""
 import numpy as np
 import pytest
 
@@ -15,6 +17,8 @@ from oracle import oracle as orc
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-10   # eV per matrix element
+TOL_FORCE = 1e-10   # eV/Angstrom per component
+FORCES = ("ftot", "kinetic", "vna", "pulay", "f3naa", "f3nab", "f3nac", "vna_ontop", "vna_atom")
 
 
 @pytest.fixture(scope="module")
@@ -39,6 +43,36 @@ def gpu_dogs(ctx, path, nZ, st, dq, graph=False):
     else:
         ctx.assemble()
     return [ctx.blocks(w) for w in ("S", "T", "vna", "vnao", "dip")]
+
+
+def gpu_dogs_forces(ctx, rho, cape, graph=False):
+    ctx.set_denmat(rho, cape)
+    if graph:
+        ctx.assemble_graph(fbgpu.FB_ALL | fbgpu.FB_FORCES)
+    else:
+        ctx.Dassemble()
+    return {k: ctx.forces(k) for k in FORCES}
+
+
+@pytest.mark.parametrize("name", ["sic_small", "cho_small", "si64", "sic_vac"])
+def test_dogs_forces_match_oracle(ctx, fdata_root, name):
+    from conftest import symmetric_denmat
+    path, nZ, st = workload(name, fdata_root, dogs=True)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+    norb = np.array([fd.norb(int(q)) for q in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 23)
+    dq = charges(len(st.imass), 29)
+    ref = s.dassemble_dogs(rho, cape, dq)
+    gpu_dogs(ctx, path, nZ, st, dq)
+    got = gpu_dogs_forces(ctx, rho, cape)
+    for k in FORCES:
+        assert np.abs(got[k] - ref[k]).max() <= TOL_FORCE, (k, np.abs(got[k] - ref[k]).max())
+    # the same step as one graph (value and force pass), replayed
+    for _ in range(2):
+        g = gpu_dogs_forces(ctx, rho, cape, graph=True)
+        for k in FORCES:
+            assert np.abs(g[k] - ref[k]).max() <= TOL_FORCE, ("graph", k)
 
 
 @pytest.mark.parametrize("name", ["sic_small", "cho_small", "si64", "sic_vac"])
@@ -126,11 +160,6 @@ def test_dogs_errors(ctx, fdata_root):
     assert e.value.code == 12
     ctx.set_charges(charges(len(st.imass), 1))
     ctx.assemble()
-    rho = np.zeros(ctx.nblock)
-    ctx.set_denmat(rho, rho)
-    with pytest.raises(fbgpu.FBError) as e:      # the DOGS force pass is not built
-        ctx.Dassemble()
-    assert e.value.code == 13
     # the z-dipole blocks alone, in either theory
     ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
     ctx.assemble_dipole_z()

@@ -50,3 +50,68 @@ def test_dipole_finite(systems):
     s, _, st = systems
     D = s.assemble_dogs(np.zeros((len(st.imass), 3)))
     assert np.isfinite(D[4]).all() and np.abs(D[4]).max() > 0
+
+
+def _dogs_energies(s, st, ratom, rho, cape, dq, layout):
+    """(two-center part, three-center part) of E = sum rho.(T + vna + vnao)
+    - sum cape.S of the DOGS value pass at the given positions."""
+    t = orc.System(s.fd, ratom, st.imass, st.lattice).neighbors()
+    assert t.npairs == layout.npairs and np.array_equal(t.neigh_j[:t.npairs], layout.neigh_j[:t.npairs])
+    S, T, vb2, vbo, _ = t.assemble_dogs(dq, with3c=False)
+    vb = t.assemble_dogs(dq)[2]
+    return float(rho @ (T + vb2 + vbo) - cape @ S), float(rho @ (vb - vb2))
+
+
+def test_dogs_forces_are_minus_gradient(systems):
+    """The DOGS force pass against -dE/dR of the DOGS value pass at fixed
+    density matrices and shell charges.  The two-center terms (kinetic,
+    Pulay, vna ontop and atom with the smoother and monopole derivatives of
+    M_Dassemble_2c_DOGS.f90) agree to 1e-5 relative.  The three-center terms
+    agree to a few percent only: where the gradient of theta-cell 1, ME 1 is
+    tiny, getDMEs_Fdata_3c takes its linear branch and gives every ME that
+    one gradient (M_Fdata_3c.f90:684-691), which is not the derivative of
+    the values, and the DOGS sub-cells take that branch at some triplets
+    here.  The restatement keeps the rule, as the GPU path does."""
+    from conftest import symmetric_denmat
+    s, _, st = systems
+    norb = np.array([s.fd.norb(int(q)) for q in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 11)
+    dq = np.random.default_rng(9).uniform(-0.3, 0.3, (len(st.imass), 3))
+    d = s.dassemble_dogs(rho, cape, dq)
+    f2 = (d["kinetic"] + d["vna"] - d["pulay"]).reshape(-1, 3)
+    f3 = (d["f3naa"] + d["f3nab"] + d["f3nac"]).reshape(-1, 3)
+    h = 1e-5
+    rng = np.random.default_rng(4)
+    for i in rng.choice(len(st.imass), 3, replace=False):
+        for k in range(3):
+            rp, rm = st.ratom.copy(), st.ratom.copy()
+            rp[i, k] += h
+            rm[i, k] -= h
+            ep, em = _dogs_energies(s, st, rp, rho, cape, dq, s), _dogs_energies(s, st, rm, rho, cape, dq, s)
+            g2, g3 = -(ep[0] - em[0]) / (2 * h), -(ep[1] - em[1]) / (2 * h)
+            assert abs(g2 - f2[i, k]) < 1e-5 * max(1.0, abs(g2)), (i, k, g2, f2[i, k])
+            assert abs(g3 - f3[i, k]) < 0.05 * max(1.0, abs(g3)), (i, k, g3, f3[i, k])
+
+
+def test_dogs_forces_zero_charges_are_harris(systems):
+    from conftest import symmetric_denmat
+    s, s0, st = systems
+    norb = np.array([s.fd.norb(int(q)) for q in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 11)
+    d = s.dassemble_dogs(rho, cape, np.zeros((len(st.imass), 3)))
+    h = s0.dassemble(rho, cape)
+    for k in ("vna_ontop", "vna_atom", "f3naa", "f3nab", "f3nac", "ftot"):
+        assert np.abs(d[k] - h[k]).max() <= 1e-12 * max(1.0, np.abs(h[k]).max()), k
+
+
+def test_dogs_charged_forces_linear(systems):
+    from conftest import symmetric_denmat
+    s, _, st = systems
+    norb = np.array([s.fd.norb(int(q)) for q in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 11)
+    dq = np.random.default_rng(6).uniform(-0.3, 0.3, (len(st.imass), 3))
+    z = s.dassemble_dogs(rho, cape, np.zeros_like(dq))["ftot"]
+    a = s.dassemble_dogs(rho, cape, dq)["ftot"] - z
+    b = s.dassemble_dogs(rho, cape, 2.0 * dq)["ftot"] - z
+    assert np.abs(a).max() > 1e-3
+    assert np.abs(b - 2.0 * a).max() <= 1e-9 * max(1.0, np.abs(b).max())

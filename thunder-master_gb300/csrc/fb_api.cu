@@ -73,7 +73,7 @@ struct fb_ctx {
   // theory of the neutral-atom terms (FB_THEORY_HARRIS / FB_THEORY_DOGS) and
   // the DOGS shell charges dq[atom][MAXSUB]
   int theory = FB_THEORY_HARRIS;
-  DevBuf d_dq;
+  DevBuf d_dq, d_dogs_ps;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -827,6 +827,7 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.dogs = ctx->theory == FB_THEORY_DOGS;
   a.dq = ctx->d_dq.as<double>();
   a.dip = ctx->d_dip.as<double>();
+  a.dogs_ps = ctx->d_dogs_ps.as<double>();
   return a;
 }
 
@@ -1042,9 +1043,10 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
 // a graph is being captured)
 static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
-  if (ctx->theory == FB_THEORY_DOGS)
-    return fail(ctx, FB_ERR_UNSUPPORTED, "DOGS: the force pass (Dassemble_*_DOGS) is not built; Harris forces only");
   if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
+  bool dogs = ctx->theory == FB_THEORY_DOGS;
+  if (dogs && (what & (FB_VNA2C | FB_VNA3C)) && !ctx->have_charges)
+    return fail(ctx, FB_ERR_STATE, "DOGS: fb_set_charges first");
   int N = ctx->N, P = ctx->P;
   size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
   CHK(ctx->d_sumT.ensure(pb));
@@ -1061,6 +1063,7 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if ((what & FB_VNA3C) && (use_df(ctx) || mlp_routes(ctx)))
     CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, true));
+  if (dogs && (what & FB_VNA3C)) CHK(ctx->d_dogs_ps.ensure((size_t)8 * P * sizeof(double) + 8));
   return FB_OK;
 }
 
@@ -1078,6 +1081,8 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   a.keep_dblocks = (what & FB_KEEP_DBLOCKS) != 0;
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+  // DOGS: the 2c kernel also leaves the per-pair sums the 3c kernel reads
+  if (a.dogs && (what & FB_VNA3C)) w2 |= 8u;
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
   if (what & FB_VNA3C) {
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
@@ -1244,7 +1249,12 @@ static int tune_launch(fb_ctx *ctx, int k, const KCfg &c, unsigned what) {
     case TK_A3C:
       a.cfg_a3c = c;
       return use_df(ctx) ? launch_assemble_3c_df(a, ctx->stream) : launch_assemble_3c(a, ctx->stream);
-    case TK_D2C: a.cfg_d2c = c; return launch_dassemble_2c(a, what & (FB_S | FB_T | FB_VNA2C), ctx->stream);
+    case TK_D2C: {
+      a.cfg_d2c = c;
+      unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+      if (a.dogs && (what & FB_VNA3C)) w2 |= 8u;
+      return launch_dassemble_2c(a, w2, ctx->stream);
+    }
     case TK_D3C:
       a.cfg_d3c = c;
       return use_df(ctx) ? launch_dassemble_3c_df(a, ctx->stream) : launch_dassemble_3c(a, ctx->stream);
@@ -1439,7 +1449,7 @@ extern "C" int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev, const do
   if (!ctx || !rho_dev || !ftot_dev) return FB_ERR_ARG;
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   if (ctx->theory == FB_THEORY_DOGS)
-    return fail(ctx, FB_ERR_UNSUPPORTED, "DOGS: the force pass (Dassemble_*_DOGS) is not built; Harris forces only");
+    return fail(ctx, FB_ERR_UNSUPPORTED, "fb_dassemble_noalloc computes the Harris force pass only; use fb_dassemble for DOGS");
   int N = ctx->N, P = ctx->P;
   if (P > FB_NOALLOC_MAX_PAIRS || N > FB_NOALLOC_MAX_ATOMS)
     return fail(ctx, FB_ERR_CAPACITY,

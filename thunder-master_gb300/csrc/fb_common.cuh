@@ -120,6 +120,7 @@ struct Ctx3c {
   int dogs;
   const double *dq;
   const double *S, *dip;
+  const double *dogs_ps;
 };
 
 struct TripGeom {
@@ -283,7 +284,16 @@ struct CtxD2c {
   double *sumT, *sumS;    // per pair 3-vectors
   double *ontop, *atomf;  // per pair 3-vectors
   bool keep;
+  double *dogs_ps;        // DOGS: 8 rho-weighted sums per pair for the 3c pass
 };
+
+// Dsmoother (b.FUNCTIONS/Dsmoother.f90:102-135), the scaler = 1 branch
+__device__ __forceinline__ double dsmoother(double r, double rend, double x) {
+  double rbegin = x * rend;
+  if (r > rend || r < rbegin) return 0.0;
+  double ratio = (r - rbegin) / (rend - rbegin);
+  return -2.0 * (1.0 - ratio * ratio) * (2.0 * ratio) / (rend - rbegin);
+}
 
 // value and x-derivative of one 2c cell (getDMEs_Fdata_2c, :446-600)
 template <int NE>
@@ -404,6 +414,7 @@ inline Ctx3c make3c(const AsmArgs &a) {
   c.dq = a.dq;
   c.S = a.S;
   c.dip = a.dip;
+  c.dogs_ps = a.dogs_ps;
   return c;
 }
 

@@ -3,8 +3,14 @@
 
 namespace fb {
 
-template <int PA, int PB, bool HASD>
-__device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned what) {
+// what: 1 overlap, 2 kinetic, 4 vna ontop + atom, 8 (DOGS) the pair sums
+// the 3c pass reads.  With DOGS the ontop terms add the charged-shell
+// sub-cells weighted by the shell charges (linear, so the weighted tables
+// go through one derivative rotation), and the atom term adds the smoothed
+// charged shells with the smoother and monopole derivatives
+// (M_Dassemble_2c_DOGS.f90:780-1196); sig = sum rho(i,self) S(i,self).
+template <int PA, int PB, bool HASD, bool DOGS>
+__device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned what, double sig) {
   using PL = Plan<PA, PB, K2C>;
   using PLA = Plan<PA, PA, K2C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
@@ -65,6 +71,20 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
 #pragma unroll
       for (int w2 = 2; w2 <= 3; w2++) {
         interp2c_d<NE>(b.table2c, fd.c2[in1][in2][w2], z, tiny, v, dv, b.status);
+        if constexpr (DOGS) {
+          int owner = w2 == 2 ? i : j, nsh = fd.sp[w2 == 2 ? in1 : in2].nssh;
+          double vs[NE], dvs[NE];
+#pragma unroll 1
+          for (int isorp = 1; isorp <= nsh; isorp++) {
+            interp2c_d<NE>(b.table2c, fd.c2s[in1][in2][w2 - 2][isorp - 1], z, tiny, vs, dvs, b.status);
+            double dq = b.dq[owner * MAXSUB + isorp - 1];
+#pragma unroll
+            for (int e = 0; e < NE; e++) {
+              v[e] = fma(dq, vs[e], v[e]);
+              dv[e] = fma(dq, dvs[e], dv[e]);
+            }
+          }
+        }
         vec2c<NE>(z, eta, dv, vd);
         contract<PA, PB, K2C, HASD>(R, D, rb, v, vd, out);
 #pragma unroll
@@ -81,29 +101,125 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
 #pragma unroll
     for (int q = 0; q < NA * NA; q++) rs[q] = __ldg(c.rho + os + q);
     contract<PA, PA, K2C, HASD>(R, D, rs, v, vd, out);
+    if constexpr (DOGS) {
+      // charged shells of jatom, smoothed: sum of dq * (smooth dX - eta
+      // dsmooth X + (1 - smooth) d(S/z) + eta dsmooth S/z) contracted with
+      // rho(i, self)
+      double rend = fd.sp[in1].rcmin + fd.sp[in2].rcmin;
+      double smooth = smoother(z, rend, 0.8), dsm = dsmoother(z, rend, 0.8);
+      double M[NEA], dM[NEA], vs[NEA], dvs[NEA], dsum = 0.0;
+#pragma unroll
+      for (int e = 0; e < NEA; e++) M[e] = dM[e] = 0.0;
+#pragma unroll 1
+      for (int isorp = 1; isorp <= fd.sp[in2].nssh; isorp++) {
+        interp2c_d<NEA>(b.table2c, fd.c2s[in1][in2][2][isorp - 1], z, tiny, vs, dvs, b.status);
+        double dq = b.dq[j * MAXSUB + isorp - 1];
+        dsum += dq;
+#pragma unroll
+        for (int e = 0; e < NEA; e++) {
+          M[e] = fma(dq, vs[e], M[e]);
+          dM[e] = fma(dq, dvs[e], dM[e]);
+        }
+      }
+      bool on = z > 1.0e-4;
+      double vm[NEA], vdm[3 * NEA];
+#pragma unroll
+      for (int e = 0; e < NEA; e++) {
+        vm[e] = smooth * M[e];
+#pragma unroll
+        for (int k = 0; k < 3; k++) vdm[k + 3 * e] = on ? -eta[k] * (smooth * dM[e]) : 0.0;
+      }
+      MolRho<PA, PA, K2C> Gs;
+      mol_rho<PA, PA, K2C>(R, D, rs, Gs);
+      double cx = 0.0;
+#pragma unroll
+      for (int e = 0; e < NEA; e++) cx = fma(M[e], Gs.G[e], cx);
+      double mono = 0.0, dmono = 0.0;  // sum rho S/z and sum rho S/z^2
+      if (on) {
+        mono = sig / z;
+        dmono = sig / (z * z);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        double s = 0.0;
+#pragma unroll
+        for (int e = 0; e < NEA; e++) {
+          s = fma(vm[e], Gs.H[q][e], s);
+          s = fma(vdm[q + 3 * e], Gs.G[e], s);
+        }
+        s = s - eta[q] * dsm * cx + dsum * ((1.0 - smooth) * eta[q] * dmono + eta[q] * dsm * mono);
+        out[q] += s;
+      }
+    }
 #pragma unroll
     for (int q = 0; q < 3; q++) c.atomf[3 * p + q] = -out[q] * P_eq2;
   }
-}
-
-template <int PA, bool HASD>
-__device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
-  int p0 = c.b.pair_off[i], p1 = c.b.pair_off[i + 1];
-  for (int p = p0 + lane; p < p1; p += 32) {
-    int pb = c.b.fd->sp[c.b.isp[c.b.neigh_j[p]]].pattern;
-    if (pb == PAT_SP) pair_d2c<PA, PAT_SP, HASD>(c, i, p, what);
-    else if (pb == PAT_S) pair_d2c<PA, PAT_S, HASD>(c, i, p, what);
-    else if constexpr (HASD) pair_d2c<PA, PAT_SPD, HASD>(c, i, p, what);
+  if constexpr (DOGS) {
+    if (what & 8u) {
+      // sum rho S, sum rho dip, sum rho dS, sum rho ddip of this pair: the
+      // pieces of the 3c effective monopole and its derivatives
+      MolRho<PA, PB, K2C> G;
+      mol_rho<PA, PB, K2C>(R, D, rb, G);
+      double *ps = c.dogs_ps + 8 * (long long)p;
+#pragma unroll
+      for (int w = 0; w < 2; w++) {
+        const Cell2cDev &cell = w == 0 ? fd.c2[in1][in2][0] : fd.c2dip[in1][in2];
+        interp2c_d<NE>(b.table2c, cell, z, tiny, v, dv, b.status);
+        vec2c<NE>(z, eta, dv, vd);
+        double s0 = 0.0, s3[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          s0 = fma(v[e], G.G[e], s0);
+#pragma unroll
+          for (int q = 0; q < 3; q++) s3[q] = fma(v[e], G.H[q][e], fma(vd[q + 3 * e], G.G[e], s3[q]));
+        }
+        ps[w] = s0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) ps[2 + 3 * w + q] = s3[q];
+      }
+    }
   }
 }
 
-template <bool HASD>
+template <int PA, bool HASD, bool DOGS>
+__device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
+  int p0 = c.b.pair_off[i], p1 = c.b.pair_off[i + 1];
+  double sig = 0.0;
+  if (DOGS && (what & 4u)) {
+    // sum rho(i, self) S(i, self): the self overlap block, interpolated and
+    // rotated as the overlap pass does, contracted with rho of the self block
+    using PLA = Plan<PA, PA, K2C>;
+    constexpr int NA = PLA::NA;
+    int ps = p0 + c.b.neigh_self[i];
+    double r1[3], r2[3], z, e[3][3];
+    pair_geom(c.b, i, ps, r1, r2, z, e);
+    RotM R;
+    twister<HASD>(e, R);
+    const Cell2cDev &cell = c.b.fd->c2[c.b.isp[i]][c.b.isp[i]][0];
+    double w[7], v[PLA::m.n], X[NA * NA];
+    int i0 = 0;
+    lagrange7(z, cell, i0, w, nullptr);
+    interp2c<PLA::m.n>(c.b.table2c, cell, i0, w, v);
+    rotate_plan<PA, PA, K2C>(R, v, X);
+    long long os = c.b.blk_off[ps];
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) sig = fma(__ldg(c.rho + os + q), X[q], sig);
+  }
+  for (int p = p0 + lane; p < p1; p += 32) {
+    int pb = c.b.fd->sp[c.b.isp[c.b.neigh_j[p]]].pattern;
+    if (pb == PAT_SP) pair_d2c<PA, PAT_SP, HASD, DOGS>(c, i, p, what, sig);
+    else if (pb == PAT_S) pair_d2c<PA, PAT_S, HASD, DOGS>(c, i, p, what, sig);
+    else if constexpr (HASD) pair_d2c<PA, PAT_SPD, HASD, DOGS>(c, i, p, what, sig);
+  }
+}
+
+template <bool HASD, bool DOGS>
 __global__ void __launch_bounds__(256) k_dassemble_2c(CtxD2c c, unsigned what, Sched q) {
   for_each_warp_item(c.b.N, q, [&](int i, int lane) {
     int pa = c.b.fd->sp[c.b.isp[i]].pattern;
-    if (pa == PAT_SP) atom_d2c<PAT_SP, HASD>(c, i, lane, what);
-    else if (pa == PAT_S) atom_d2c<PAT_S, HASD>(c, i, lane, what);
-    else if constexpr (HASD) atom_d2c<PAT_SPD, HASD>(c, i, lane, what);
+    if (pa == PAT_SP) atom_d2c<PAT_SP, HASD, DOGS>(c, i, lane, what);
+    else if (pa == PAT_S) atom_d2c<PAT_S, HASD, DOGS>(c, i, lane, what);
+    else if constexpr (HASD) atom_d2c<PAT_SPD, HASD, DOGS>(c, i, lane, what);
   });
 }
 
@@ -119,12 +235,18 @@ int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   c.ontop = a.ontop;
   c.atomf = a.atomf;
   c.keep = a.keep_dblocks;
+  c.dogs_ps = a.dogs_ps;
   dim3 grid, block;
   Sched q;
   int e = sched_launch(a.cfg_d2c, (long long)a.N * 32, a.queue ? a.queue + 2 : nullptr, s, grid, block, q);
   if (e) return e;
-  if (a.have_d) k_dassemble_2c<true><<<grid, block, 0, s>>>(c, what, q);
-  else k_dassemble_2c<false><<<grid, block, 0, s>>>(c, what, q);
+  if (a.have_d) {
+    if (a.dogs) k_dassemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
+    else k_dassemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
+  } else {
+    if (a.dogs) k_dassemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
+    else k_dassemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
+  }
   FB_LAUNCH_CHECK();
   return 0;
 }

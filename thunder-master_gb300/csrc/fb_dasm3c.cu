@@ -6,7 +6,14 @@ namespace fb {
 // ===========================================================================
 // 3c forces: Dassemble_vna_3c (k.DASSEMBLERS/M_Dassemble_3c_Harris.f90:136-408)
 // ===========================================================================
-template <int PA, int PB, bool HASD>
+// With DOGS the charged shells of ialpha add (M_Dassemble_3c_DOGS.f90:
+// 355-520) sum_isorp dq * (stinky dX + dstn X - dstn emnpl + (1 - stinky)
+// demnpl): the sub-cells are linear in their tables, so the dq-weighted sum
+// of the sub-cells goes through the same derivative rotations as the
+// neutral term (scaled by stinky); the smoother and monopole terms are
+// contracted with rho through the per-pair sums of rho S, rho dip, rho dS
+// and rho ddip the 2c kernel left in dogs_ps.
+template <int PA, int PB, bool HASD, bool DOGS>
 __device__ void trip_3c_force(const Ctx3c &c, int t) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
@@ -30,6 +37,58 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   double F[NE], DpF[NE], DxF[NE], DyF[NE];
   interp3c<NE, true>(c, cell, g.x, g.z, g.cost, F, DpF, DxF, DyF);
   double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
+  // DOGS: Fq = sum dq * sub-cell (values, for the smoother term), and
+  // F += stinky * sum dq * sub-cell (values and derivatives)
+  double Fq[DOGS ? NE : 1], stinky = 0.0, dsum = 0.0, dstnA[3], dstnB[3], rA1[3], rA2[3], d13 = 0.0, d23 = 0.0;
+  if constexpr (DOGS) {
+    const FdataDev &fd = *c.fd;
+    int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      d13 += (g.rna[k] - g.r1[k]) * (g.rna[k] - g.r1[k]);
+      d23 += (g.rna[k] - g.r2[k]) * (g.rna[k] - g.r2[k]);
+    }
+    d13 = sqrt(d13);
+    d23 = sqrt(d23);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      rA1[k] = d13 > 1.0e-5 ? (g.rna[k] - g.r1[k]) / d13 : 0.0;
+      rA2[k] = d23 > 1.0e-5 ? (g.rna[k] - g.r2[k]) / d23 : 0.0;
+    }
+    double rc3 = fd.sp[indna].rcmin;
+    double rend1 = fd.sp[in1].rcmin + rc3, rend2 = fd.sp[in2].rcmin + rc3;
+    double s13 = smoother(d13, rend1, 0.8), ds13 = dsmoother(d13, rend1, 0.8);
+    double s23 = smoother(d23, rend2, 0.8), ds23 = dsmoother(d23, rend2, 0.8);
+    stinky = s13 * s23;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      dstnB[k] = -ds13 * s23 * rA1[k];
+      double dstnC = -s13 * ds23 * rA2[k];
+      dstnA[k] = -dstnB[k] - dstnC;
+    }
+    double Gq[NE], Gp[NE], Gx[NE], Gy[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) Fq[e] = 0.0;
+#pragma unroll 1
+    for (int isorp = 1; isorp <= fd.sp[indna].nssh; isorp++) {
+      interp3c<NE, true>(c, fd.c3s[in1][in2][indna][isorp - 1], g.x, g.z, g.cost, Gq, Gp, Gx, Gy);
+      double dq = c.dq[ia * MAXSUB + isorp - 1];
+      dsum += dq;
+      double w = dq * stinky;
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        Fq[e] = fma(dq, Gq[e], Fq[e]);
+        F[e] = fma(w, Gq[e], F[e]);
+        DpF[e] = fma(w, Gp[e], DpF[e]);
+        DxF[e] = fma(w, Gx[e], DxF[e]);
+        DyF[e] = fma(w, Gy[e], DyF[e]);
+      }
+    }
+    sfor<NE>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      if constexpr (PL::m.mv[e] == 1) Fq[e] = Fq[e] * sint;
+    });
+  }
   double M[NE], Ma[3 * NE], Mb[3 * NE];
   sfor<NE>([&](auto E) {
     constexpr int e = decltype(E)::value;
@@ -74,6 +133,28 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
     fa[q] = -sa * P_eq2;
     fb[q] = -sb * P_eq2;
   }
+  if constexpr (DOGS) {
+    // dstn * sum rho rot(Fq), and the effective monopole emnpl =
+    // (S/2 - dip/z)/d13 + (S/2 + dip/z)/d23 with its derivatives, all
+    // contracted with rho of the pair
+    double cx = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) cx = fma(Fq[e], GA.G[e], cx);
+    const double *ps = c.dogs_ps + 8 * (long long)c.tdst[t];
+    double sterm = 0.5 * ps[0], dterm = ps[1] / g.z;
+    double am = sterm - dterm, ap = sterm + dterm;
+    double emnpl = am / d13 + ap / d23;
+    double i13 = 1.0 / (d13 * d13), i23 = 1.0 / (d23 * d23);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double spterm = 0.5 * ps[2 + q];
+      double dpterm = ps[5 + q] / g.z + dterm * g.sighat[q] / g.z;
+      double dA = -am * rA1[q] * i13 - ap * rA2[q] * i23;
+      double dB = am * rA1[q] * i13 + (spterm - dpterm) / d13 + (spterm + dpterm) / d23;
+      fa[q] -= P_eq2 * (dstnA[q] * cx - dsum * dstnA[q] * emnpl + dsum * (1.0 - stinky) * dA);
+      fb[q] -= P_eq2 * (dstnB[q] * cx - dsum * dstnB[q] * emnpl + dsum * (1.0 - stinky) * dB);
+    }
+  }
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     atomicAdd(c.f3naa + 3 * ia + q, fa[q]);
@@ -82,24 +163,24 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   }
 }
 
-template <bool HASD>
+template <bool HASD, bool DOGS>
 __global__ void __launch_bounds__(256) k_dassemble_3c(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
     if (c.tperm) t = c.tperm[t];
     int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
     int key = pa * 3 + pb;
     switch (key) {
-      case PAT_SP * 3 + PAT_SP: trip_3c_force<PAT_SP, PAT_SP, HASD>(c, t); break;
-      case PAT_SP * 3 + PAT_S: trip_3c_force<PAT_SP, PAT_S, HASD>(c, t); break;
-      case PAT_S * 3 + PAT_SP: trip_3c_force<PAT_S, PAT_SP, HASD>(c, t); break;
-      case PAT_S * 3 + PAT_S: trip_3c_force<PAT_S, PAT_S, HASD>(c, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_3c_force<PAT_SP, PAT_SP, HASD, DOGS>(c, t); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_force<PAT_SP, PAT_S, HASD, DOGS>(c, t); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_force<PAT_S, PAT_SP, HASD, DOGS>(c, t); break;
+      case PAT_S * 3 + PAT_S: trip_3c_force<PAT_S, PAT_S, HASD, DOGS>(c, t); break;
       default:
         if constexpr (HASD) {
-          if (key == PAT_SPD * 3 + PAT_SPD) trip_3c_force<PAT_SPD, PAT_SPD, HASD>(c, t);
-          else if (key == PAT_SPD * 3 + PAT_SP) trip_3c_force<PAT_SPD, PAT_SP, HASD>(c, t);
-          else if (key == PAT_SP * 3 + PAT_SPD) trip_3c_force<PAT_SP, PAT_SPD, HASD>(c, t);
-          else if (key == PAT_SPD * 3 + PAT_S) trip_3c_force<PAT_SPD, PAT_S, HASD>(c, t);
-          else if (key == PAT_S * 3 + PAT_SPD) trip_3c_force<PAT_S, PAT_SPD, HASD>(c, t);
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_3c_force<PAT_SPD, PAT_SPD, HASD, DOGS>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_3c_force<PAT_SPD, PAT_SP, HASD, DOGS>(c, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_3c_force<PAT_SP, PAT_SPD, HASD, DOGS>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_3c_force<PAT_SPD, PAT_S, HASD, DOGS>(c, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_3c_force<PAT_S, PAT_SPD, HASD, DOGS>(c, t);
         }
     }
   });
@@ -112,8 +193,13 @@ int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  if (a.have_d) k_dassemble_3c<true><<<grid, block, 0, s>>>(c, q);
-  else k_dassemble_3c<false><<<grid, block, 0, s>>>(c, q);
+  if (a.have_d) {
+    if (a.dogs) k_dassemble_3c<true, true><<<grid, block, 0, s>>>(c, q);
+    else k_dassemble_3c<true, false><<<grid, block, 0, s>>>(c, q);
+  } else {
+    if (a.dogs) k_dassemble_3c<false, true><<<grid, block, 0, s>>>(c, q);
+    else k_dassemble_3c<false, false><<<grid, block, 0, s>>>(c, q);
+  }
   FB_LAUNCH_CHECK();
   return 0;
 }

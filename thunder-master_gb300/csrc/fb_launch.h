@@ -85,6 +85,9 @@ struct AsmArgs {
   int dogs;
   const double *dq;
   double *dip;
+  // DOGS force pass: per pair sum(rho S), sum(rho dip), sum(rho dS)[3],
+  // sum(rho ddip)[3] (8 doubles), written by the 2c and read by the 3c kernel
+  double *dogs_ps;
   // launch shapes (autotuned) and the work counters of persistent launches
   KCfg cfg_a2c, cfg_a3c, cfg_d2c, cfg_d3c;
   int *queue;  // 4 counters: assemble_2c, assemble_3c, dassemble_2c, dassemble_3c
