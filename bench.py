@@ -459,6 +459,7 @@ def run_gpu(args):
     }
     if rank == 0:
         line["bloch"] = bloch_measure(ctx, torch, stream, local)
+        line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
     if args.mlp_epochs > 0:
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
@@ -496,6 +497,73 @@ def bloch_measure(ctx, torch, stream, local, reps=5):
     return {"what": "dense complex H(k) = T + vna + vnao and S(k) at one k-point (Bloch sums of the blocks)",
             "norbitals": n, "ms": round(ms, 4), "bytes_written": nbytes,
             "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), "hermiticity_max_abs": herm}
+
+
+def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=False):
+    """The DOGS step (charge-weighted vna, M_assemble_*_DOGS.f90 and
+    M_Dassemble_*_DOGS.f90) on the same structure with seeded shell charges:
+    fb_neighbors + one graph launch of the value and force pass (FP64
+    kernels), its agreement with the oracle's DOGS restatement, and the
+    oracle's time for the same step on one host core."""
+    from fbgpu import synth
+    path = synth.fdata_dir_for(args.workload, root=fdata_root(), dogs=True)
+    ctx = fbgpu.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    P, T, NB = ctx.driver_neighbors()
+    nbm = ctx.neighbors()
+    norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
+    rho, cape = denmat_fast(nbm["neighn"], nbm["neigh_j"] - 1, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
+    dq = np.random.default_rng(5).uniform(-0.3, 0.3, (st.natoms, 3))
+    ctx.set_theory(fbgpu.FB_THEORY_DOGS)
+    ctx.set_charges(dq)
+    d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
+    d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
+    what = fbgpu.FB_ALL | fbgpu.FB_FORCES
+    shapes = tuned_shapes(ctx, fbgpu, not args.no_autotune)
+
+    def step():
+        ctx.driver_neighbors()
+        ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+        ctx.assemble_graph(what)
+
+    timed = make_timer(torch, ctx, stream, flush, 1, local)
+    for _ in range(max(3, args.warmup)):
+        step()
+    ms, launches = timed(step, args.steps)
+    ms_k, _ = timed(lambda: (ctx.driver_neighbors(), ctx.assemble(fbgpu.FB_ALL),
+                             ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr()),
+                             ctx.Dassemble(fbgpu.FB_ALL)), args.steps, timing=True)
+    ktimes = ctx.timing()
+    ctx.set_timing(False)
+    out = {"what": "DOGS value + force pass (charged-shell sub-cells, smoothed monopoles), FP64 kernels, "
+                   "shell charges U(-0.3, 0.3) seeded",
+           "ms_per_step": round(ms / args.steps, 4), "value": round(P * args.steps / (ms * 1e-3), 1),
+           "unit": UNIT, "gpu_launches_per_step": launches // max(1, args.steps),
+           "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+           "launch_shapes": shapes}
+    # agreement with the oracle and the oracle's single-core time
+    got = {k: ctx.blocks(k) for k in ("vna", "vnao")}
+    ctx.set_denmat(rho, cape)
+    ctx.Dassemble()
+    f_gpu = ctx.forces("ftot")
+    ctx.close()
+    if no_cpu or st.natoms > 1024:
+        out["cpu_oracle"] = "not run (single-core oracle bounded to systems of at most 1024 atoms)"
+    else:
+        from oracle import oracle as orc
+        fd = orc.Fdata(path, nZ)
+        t0 = time.perf_counter()
+        s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+        ref = s.assemble_dogs(dq)
+        d = s.dassemble_dogs(rho, cape, dq)
+        t = time.perf_counter() - t0
+        out["max_abs_dvna_ev"] = float(max(np.abs(got["vna"] - ref[2]).max(), np.abs(got["vnao"] - ref[3]).max()))
+        out["max_abs_dftot_ev_per_A"] = float(np.abs(f_gpu - d["ftot"]).max())
+        out["cpu_oracle"] = {"value": round(P / t, 1), "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "1 DOGS step (neighbors + value + force pass), %.3f s" % t}
+    return out
 
 
 def make_timer(torch, ctx, stream, flush, ws, local):

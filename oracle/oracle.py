@@ -167,6 +167,7 @@ class System:
         """DOGS value pass: S, T, vna (atom + 3c), vnao (ontop) and the
         z-dipole blocks, with shell charges dQ (natoms, nssh_max)."""
         L = lib()
+        L.or_set_threads(self.threads)
         nb = self.nblock
         d = np.ascontiguousarray(dQ, np.float64)
         d = d.reshape(len(self.imass), -1)
@@ -218,6 +219,7 @@ class System:
         vna ontop / atom and f3na terms, and build_forces, with shell
         charges dQ (natoms, nssh_max)."""
         L = lib()
+        L.or_set_threads(self.threads)
         nb, P, N = self.nblock, self.npairs, len(self.imass)
         d = np.ascontiguousarray(dQ, np.float64).reshape(N, -1)
         _check(L.or_set_charges(self.h, np.ascontiguousarray(d.ravel()), d.shape[1]))
