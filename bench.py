@@ -521,6 +521,7 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
     d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
     d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
     what = fbgpu.FB_ALL | fbgpu.FB_FORCES
+    ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
     shapes = tuned_shapes(ctx, fbgpu, not args.no_autotune)
 
     def step():
