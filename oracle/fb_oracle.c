@@ -44,6 +44,7 @@ enum {
 #define P_vna_ontopL 3
 #define P_vna_ontopR 4
 #define P_vna_atom 5
+#define P_vnl 6
 #define P_dipole_z 10
 #define P_bcna 3
 #define P_mbox 4 /* c.SYSTEM/M_configuraciones.f90:359 */
@@ -100,10 +101,13 @@ typedef struct {
   int lssh[MAXSH];
   double rcutoffA[MAXSH];
   double rcutoffA_max;
+  /* pseudopotential projectors: shells, orbitals, cutoff (as read), cl */
+  int lssh_PP[MAXSH], norb_PP_max;
+  double rcutoff_PP, cl_PP[MAXSH];
 } species_t;
 
 struct or_fdata {
-  int nspecies, have_dorbitals;
+  int nspecies, have_dorbitals, have_dorbitals_PP;
   species_t sp[MAXSP + 1]; /* 1-based */
   bundle2c b2[MAXSP + 1][MAXSP + 1];
   bundle3c b3[MAXSP + 1][MAXSP + 1][MAXSP + 1];
@@ -126,6 +130,15 @@ struct or_sys {
   /* DOGS shell charges dQ[i * nssh_max + isorp - 1] */
   double *dQ;
   int nssh_max;
+  /* pseudopotential neighbor maps (c.SYSTEM/M_neighbors_PP.f90), CSR by
+   * atom, 0-based: PP (basis i, projector j), PPx (projector i, basis j),
+   * PPp (pairs sharing a projector), and the PP common-neighbor triplets */
+  int have_pp;
+  int *pp_off, *pp_j, *pp_b, *pp_self, *pp_map;
+  int *ppx_off, *ppx_j, *ppx_b, *ppx_self, *ppx_map, *ppx_point;
+  int *ppp_off, *ppp_j, *ppp_b, *ppp_self;
+  long long *svnl_off, *vnl_off, nsvnl, nvnl;
+  int *ppc_off, *ppc_i, *ppc_ib, *ppc_j, *ppc_jb, *ppc_m, *ppc_m31, *ppc_m32;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -267,6 +280,13 @@ static int read_info(or_fdata *fd, const char *dir, const int *nZreq) {
     if (read_ints(&t, 1, &s->nssh_PP) || s->nssh_PP < 0 || s->nssh_PP > MAXSH) goto bad;
     if (s->nssh_PP > 0 && read_ints(&t, s->nssh_PP, lpp)) goto bad;
     if (read_dbls(&t, 1, &rcpp)) goto bad;
+    s->rcutoff_PP = rcpp; /* :1147, used as read (M_neighbors_PP.f90:469) */
+    s->norb_PP_max = 0;   /* :1188-1194 */
+    for (int i = 0; i < s->nssh_PP; i++) {
+      if (lpp[i] < 0 || lpp[i] > 2) { seterr("unsupported PP l=%d", lpp[i]); txt_close(&t); return E_UNSUP; }
+      s->lssh_PP[i] = lpp[i];
+      s->norb_PP_max += 2 * lpp[i] + 1;
+    }
     txt_skip(&t); /* wffile names */
     txt_skip(&t); /* na files */
     if (read_dbls(&t, 1, &atomicE)) goto bad;
@@ -282,8 +302,11 @@ static int read_info(or_fdata *fd, const char *dir, const int *nZreq) {
   }
   txt_close(&t);
   fd->have_dorbitals = 0; /* :1212-1221 */
+  fd->have_dorbitals_PP = 0;
   for (int k = 1; k <= fd->nspecies; k++) {
     if (fd->sp[k].nssh == 0) { seterr("species nZ=%d not in info.dat", fd->sp[k].nZ); return E_IO; }
+    for (int i = 0; i < fd->sp[k].nssh_PP; i++)
+      if (fd->sp[k].lssh_PP[i] == 2) fd->have_dorbitals_PP = 1;
     for (int i = 0; i < fd->sp[k].nssh; i++) {
       if (fd->sp[k].lssh[i] == 2) fd->have_dorbitals = 1;
       if (fd->sp[k].rcutoffA[i] > fd->sp[k].rcutoffA_max) fd->sp[k].rcutoffA_max = fd->sp[k].rcutoffA[i];
@@ -379,6 +402,7 @@ static int read_fdata_2c(or_fdata *fd, const char *dir) {
     for (int k = 0; k < fd->sp[is].nssh_PP; k++) {
       double cl;
       if (read_dbls(&t, 1, &cl)) { txt_close(&t); seterr("short %s", path); return E_IO; }
+      fd->sp[is].cl_PP[k] = cl;
     }
     txt_close(&t);
   }
@@ -983,18 +1007,21 @@ static void chooser(int l, const double *dmat, const double *pmat, double *rm) {
   }
 }
 
-void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu, int norb_nu, const double *mm,
-               double *xm) {
+/* rotate (M_rotations.f90:98-177) with the shells of in1 on the left and
+ * the shell list (n2sh, l2s) on the right: the basis of in3, or the
+ * projector shells for rotate_PP (c.SYSTEM/rotate_PP.f90:60-156) */
+static void rotate_shells(or_fdata *fd, int in1, int n2sh, const int *l2s, int have_d, const double *eps,
+                          int norb_mu, int norb_nu, const double *mm, double *xm) {
   double dmat[25] = {0}, pmat[9], left[25], right[25];
-  twister(eps, fd->have_dorbitals, dmat, pmat);
+  twister(eps, have_d, dmat, pmat);
   for (int k = 0; k < norb_mu * norb_nu; k++) xm[k] = 0.0;
   int n1 = 0;
   for (int issh = 0; issh < fd->sp[in1].nssh; issh++) {
     int l1 = fd->sp[in1].lssh[issh];
     chooser(l1, dmat, pmat, left);
     int n2 = 0;
-    for (int jssh = 0; jssh < fd->sp[in3].nssh; jssh++) {
-      int l2 = fd->sp[in3].lssh[jssh];
+    for (int jssh = 0; jssh < n2sh; jssh++) {
+      int l2 = l2s[jssh];
       chooser(l2, dmat, pmat, right);
       for (int m2 = 0; m2 < 2 * l2 + 1; m2++)
         for (int m1 = 0; m1 < 2 * l1 + 1; m1++)
@@ -1007,6 +1034,17 @@ void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu, i
     }
     n1 += 2 * l1 + 1;
   }
+}
+
+void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu, int norb_nu, const double *mm,
+               double *xm) {
+  rotate_shells(fd, in1, fd->sp[in3].nssh, fd->sp[in3].lssh, fd->have_dorbitals, eps, norb_mu, norb_nu, mm, xm);
+}
+
+static void rotate_pp(or_fdata *fd, int in1, int in2, const double *eps, int norb_mu, int norb_nu, const double *mm,
+                      double *xm) {
+  rotate_shells(fd, in1, fd->sp[in2].nssh_PP, fd->sp[in2].lssh_PP, fd->have_dorbitals || fd->have_dorbitals_PP, eps,
+                norb_mu, norb_nu, mm, xm);
 }
 
 /* Dtwister: Ddmat[ix + 3*(a + 5*b)], Dpmat[ix + 3*(a + 3*b)] */
@@ -1057,11 +1095,12 @@ static void dchooser(int l, const double *Ddmat, const double *Dpmat, double *Dm
 
 /* Drotate = twister + Dtwister + Dmatrix; matm (norb_mu,norb_nu), Dmatm and
  * Dmatx (3,norb_mu,norb_nu) */
-static void drotate(or_fdata *fd, int in1, int in2, const double *eps, const double *deps, int norb_mu,
-                    int norb_nu, const double *matm, const double *Dmatm, double *term) {
+static void drotate_shells(or_fdata *fd, int in1, int n2sh, const int *l2s, int have_d, const double *eps,
+                           const double *deps, int norb_mu, int norb_nu, const double *matm, const double *Dmatm,
+                           double *term) {
   double dmat[25] = {0}, pmat[9], Ddmat[75], Dpmat[27];
   double left[25], right[25], Dleft[75], Dright[75];
-  twister(eps, fd->have_dorbitals, dmat, pmat);
+  twister(eps, have_d, dmat, pmat);
   dtwister(eps, deps, Ddmat, Dpmat);
   int n1 = 0;
   for (int issh = 0; issh < fd->sp[in1].nssh; issh++) {
@@ -1069,8 +1108,8 @@ static void drotate(or_fdata *fd, int in1, int in2, const double *eps, const dou
     chooser(l1, dmat, pmat, left);
     dchooser(l1, Ddmat, Dpmat, Dleft);
     int n2 = 0;
-    for (int jssh = 0; jssh < fd->sp[in2].nssh; jssh++) {
-      int l2 = fd->sp[in2].lssh[jssh];
+    for (int jssh = 0; jssh < n2sh; jssh++) {
+      int l2 = l2s[jssh];
       chooser(l2, dmat, pmat, right);
       dchooser(l2, Ddmat, Dpmat, Dright);
       for (int k2 = 0; k2 < 2 * l2 + 1; k2++)
@@ -1091,6 +1130,19 @@ static void drotate(or_fdata *fd, int in1, int in2, const double *eps, const dou
     }
     n1 += 2 * l1 + 1;
   }
+}
+
+static void drotate(or_fdata *fd, int in1, int in2, const double *eps, const double *deps, int norb_mu,
+                    int norb_nu, const double *matm, const double *Dmatm, double *term) {
+  drotate_shells(fd, in1, fd->sp[in2].nssh, fd->sp[in2].lssh, fd->have_dorbitals, eps, deps, norb_mu, norb_nu, matm,
+                 Dmatm, term);
+}
+
+/* Drotate_PP (c.SYSTEM/M_Drotations_PP.f90:103-271) */
+static void drotate_pp(or_fdata *fd, int in1, int in2, const double *eps, const double *deps, int norb_mu,
+                       int norb_nu, const double *matm, const double *Dmatm, double *term) {
+  drotate_shells(fd, in1, fd->sp[in2].nssh_PP, fd->sp[in2].lssh_PP, fd->have_dorbitals || fd->have_dorbitals_PP, eps,
+                 deps, norb_mu, norb_nu, matm, Dmatm, term);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1141,9 +1193,23 @@ static void free_neigh(or_sys *s) {
   s->blk_off = NULL;
 }
 
+static void free_pp(or_sys *s) {
+  void *v[] = {s->pp_off, s->pp_j, s->pp_b, s->pp_self, s->pp_map, s->ppx_off, s->ppx_j, s->ppx_b, s->ppx_self,
+               s->ppx_map, s->ppx_point, s->ppp_off, s->ppp_j, s->ppp_b, s->ppp_self, s->svnl_off, s->vnl_off,
+               s->ppc_off, s->ppc_i, s->ppc_ib, s->ppc_j, s->ppc_jb, s->ppc_m, s->ppc_m31, s->ppc_m32};
+  for (size_t k = 0; k < sizeof v / sizeof v[0]; k++) free(v[k]);
+  s->pp_off = s->pp_j = s->pp_b = s->pp_self = s->pp_map = NULL;
+  s->ppx_off = s->ppx_j = s->ppx_b = s->ppx_self = s->ppx_map = s->ppx_point = NULL;
+  s->ppp_off = s->ppp_j = s->ppp_b = s->ppp_self = NULL;
+  s->svnl_off = s->vnl_off = NULL;
+  s->ppc_off = s->ppc_i = s->ppc_ib = s->ppc_j = s->ppc_jb = s->ppc_m = s->ppc_m31 = s->ppc_m32 = NULL;
+  s->have_pp = 0;
+}
+
 void or_free_system(or_sys *s) {
   if (!s) return;
   free_neigh(s);
+  free_pp(s);
   free(s->ratom); free(s->imass); free(s->xl); free(s->dQ);
   free(s);
 }
@@ -2108,4 +2174,503 @@ int or_dassemble_vna_3c_dogs(or_sys *s, const double *rho, const double *S, cons
     }
   }
   return err;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Non-local pseudopotential (vnl)                                           */
+/* ------------------------------------------------------------------------ */
+/* growable int list */
+typedef struct { int *v; int n, cap; } ivec;
+static void ivec_push(ivec *a, int x) {
+  if (a->n == a->cap) {
+    a->cap = a->cap ? 2 * a->cap : 256;
+    a->v = (int *)realloc(a->v, sizeof(int) * a->cap);
+  }
+  a->v[a->n++] = x;
+}
+
+/* pairs (i, j, mbeta) with |r_j + xl - r_i| < rc_i + rc_j - 0.01, mbeta
+ * outer and jatom inner, and the self index; ri / rj the two cutoffs
+ * (find_neighbors_PP, M_neighbors_PP.f90:409-516, ri = basis, rj = PP;
+ * find_neighbors_PPx, :672-778, ri = PP, rj = basis) */
+static int pp_pairs(or_sys *s, int kind, int **off, int **jj, int **bb, int **self) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  ivec J = {0}, B = {0};
+  *off = (int *)malloc(sizeof(int) * (N + 1));
+  *self = (int *)malloc(sizeof(int) * N);
+  (*off)[0] = 0;
+  for (int i = 0; i < N; i++) {
+    const species_t *a = &fd->sp[s->imass[i]];
+    double rci = kind == 0 ? a->rcutoffA_max : a->rcutoff_PP;
+    (*self)[i] = -1;
+    for (int mb = 0; mb <= s->mbeta_max; mb++)
+      for (int j = 0; j < N; j++) {
+        const species_t *b = &fd->sp[s->imass[j]];
+        double rcj = kind == 0 ? b->rcutoff_PP : b->rcutoffA_max;
+        double r2[3];
+        for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[mb][k];
+        double z = distance3(RAT(s, i), r2);
+        if (z < rci + rcj - 0.01) {
+          if (j == i && mb == 0 && (*self)[i] < 0) (*self)[i] = J.n - (*off)[i];
+          ivec_push(&J, j);
+          ivec_push(&B, mb);
+        }
+      }
+    (*off)[i + 1] = J.n;
+    if ((*self)[i] < 0) { seterr("no PP self pair for atom %d", i + 1); return E_SELF; }
+  }
+  *jj = J.v ? J.v : (int *)malloc(sizeof(int));
+  *bb = B.v ? B.v : (int *)malloc(sizeof(int));
+  return OK;
+}
+
+/* the image index of a lattice vector (distance < 1e-4), or -1 */
+static int image_of(const or_sys *s, const double *r) {
+  for (int mb = 0; mb <= s->mbeta_max; mb++)
+    if (distance3(s->xl[mb], r) < 1.0e-04) return mb;
+  return -1;
+}
+
+/* driver_neighbors_PP (c.SYSTEM/M_neighbors_PP.f90:98-151): PP and PPx
+ * pairs, PPp with the PP/PPx maps and the PPx point (find_neighbors_PPp,
+ * :922-1123), and the PP common-neighbor triplets (find_common_neighbors_PP,
+ * :1301-1420) with the svnl indices mpairnay gives
+ * (M_assemble_PP_3c.f90:266-365) */
+int or_neighbors_pp(or_sys *s) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, st;
+  free_pp(s);
+  if ((st = pp_pairs(s, 0, &s->pp_off, &s->pp_j, &s->pp_b, &s->pp_self))) return st;
+  if ((st = pp_pairs(s, 1, &s->ppx_off, &s->ppx_j, &s->ppx_b, &s->ppx_self))) return st;
+  /* PPp: for each PP neighbor alpha of i, each PPx neighbor j of alpha,
+   * image xl(jbeta) + xl(ibeta); first occurrences in that order */
+  ivec J = {0}, B = {0};
+  s->ppp_off = (int *)malloc(sizeof(int) * (N + 1));
+  s->ppp_self = (int *)malloc(sizeof(int) * N);
+  s->ppp_off[0] = 0;
+  for (int i = 0; i < N; i++) {
+    int start = J.n;
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int al = s->pp_j[p], ib = s->pp_b[p];
+      for (int q = s->ppx_off[al]; q < s->ppx_off[al + 1]; q++) {
+        int j = s->ppx_j[q], jb = s->ppx_b[q];
+        double r3[3];
+        for (int k = 0; k < 3; k++) r3[k] = s->xl[jb][k] + s->xl[ib][k];
+        int mb = image_of(s, r3);
+        if (mb < 0) {
+          seterr("PPp image of atom %d outside the %d-image box", j + 1, s->mbeta_max + 1);
+          return E_BACK;
+        }
+        int found = 0;
+        for (int k = start; k < J.n; k++)
+          if (J.v[k] == j && B.v[k] == mb) { found = 1; break; }
+        if (!found) { ivec_push(&J, j); ivec_push(&B, mb); }
+      }
+    }
+    s->ppp_off[i + 1] = J.n;
+    s->ppp_self[i] = -1;
+    for (int k = start; k < J.n; k++)
+      if (J.v[k] == i && B.v[k] == 0) { s->ppp_self[i] = k - start; break; }
+    if (s->ppp_self[i] < 0) { seterr("no PPp self pair for atom %d", i + 1); return E_SELF; }
+  }
+  s->ppp_j = J.v;
+  s->ppp_b = B.v;
+  /* maps of PP and PPx pairs into PPp, and PPx point into PP(j) */
+  s->pp_map = (int *)malloc(sizeof(int) * (s->pp_off[N] + 1));
+  s->ppx_map = (int *)malloc(sizeof(int) * (s->ppx_off[N] + 1));
+  s->ppx_point = (int *)malloc(sizeof(int) * (s->ppx_off[N] + 1));
+  for (int i = 0; i < N; i++) {
+    for (int w = 0; w < 2; w++) {
+      int *off = w ? s->ppx_off : s->pp_off, *jj = w ? s->ppx_j : s->pp_j, *bb = w ? s->ppx_b : s->pp_b;
+      int *map = w ? s->ppx_map : s->pp_map;
+      for (int p = off[i]; p < off[i + 1]; p++) {
+        map[p] = -1;
+        for (int k = s->ppp_off[i]; k < s->ppp_off[i + 1]; k++)
+          if (s->ppp_j[k] == jj[p] && s->ppp_b[k] == bb[p]) { map[p] = k - s->ppp_off[i]; break; }
+        if (map[p] < 0) { seterr("PP map of atom %d not found", i + 1); return E_BACK; }
+      }
+    }
+    for (int p = s->ppx_off[i]; p < s->ppx_off[i + 1]; p++) {
+      int j = s->ppx_j[p], jb = s->ppx_b[p];
+      s->ppx_point[p] = -1;
+      for (int k = s->pp_off[j]; k < s->pp_off[j + 1]; k++) {
+        double r2[3];
+        for (int c = 0; c < 3; c++) r2[c] = RAT(s, s->pp_j[k])[c] + s->xl[s->pp_b[k]][c] + s->xl[jb][c];
+        if (distance3(RAT(s, i), r2) < 1.0e-04) { s->ppx_point[p] = k - s->pp_off[j]; break; }
+      }
+      if (s->ppx_point[p] < 0) { seterr("PPx point of atom %d not found", i + 1); return E_BACK; }
+    }
+  }
+  /* block offsets: svnl norb_i x norb_PP_j per PP pair, vnl norb_i x norb_j per PPp pair */
+  s->svnl_off = (long long *)malloc(sizeof(long long) * (s->pp_off[N] + 1));
+  s->vnl_off = (long long *)malloc(sizeof(long long) * (s->ppp_off[N] + 1));
+  long long o = 0;
+  for (int i = 0; i < N; i++)
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      s->svnl_off[p] = o;
+      o += (long long)fd->sp[s->imass[i]].norb_max * fd->sp[s->imass[s->pp_j[p]]].norb_PP_max;
+    }
+  s->svnl_off[s->pp_off[N]] = o;
+  s->nsvnl = o;
+  o = 0;
+  for (int i = 0; i < N; i++)
+    for (int p = s->ppp_off[i]; p < s->ppp_off[i + 1]; p++) {
+      s->vnl_off[p] = o;
+      o += (long long)fd->sp[s->imass[i]].norb_max * fd->sp[s->imass[s->ppp_j[p]]].norb_max;
+    }
+  s->vnl_off[s->ppp_off[N]] = o;
+  s->nvnl = o;
+  /* common PP triplets of each alpha */
+  ivec CI = {0}, CIB = {0}, CJ = {0}, CJB = {0}, CM = {0}, C31 = {0}, C32 = {0};
+  s->ppc_off = (int *)malloc(sizeof(int) * (N + 1));
+  s->ppc_off[0] = 0;
+  for (int al = 0; al < N; al++) {
+    for (int a = s->ppx_off[al]; a < s->ppx_off[al + 1]; a++) {
+      int i = s->ppx_j[a], ib = s->ppx_b[a];
+      if (i == al && ib == 0) continue;
+      double r1[3];
+      for (int k = 0; k < 3; k++) r1[k] = RAT(s, i)[k] + s->xl[ib][k];
+      for (int b = s->ppx_off[al]; b < s->ppx_off[al + 1]; b++) {
+        int j = s->ppx_j[b], jb = s->ppx_b[b];
+        if ((j == al && jb == 0) || a == b) continue;
+        double r2[3], r[3];
+        for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[jb][k], r[k] = r2[k] - r1[k];
+        int m = -1;
+        for (int k = s->ppp_off[i]; k < s->ppp_off[i + 1]; k++) {
+          double r3[3];
+          for (int c = 0; c < 3; c++) r3[c] = s->xl[s->ppp_b[k]][c] + RAT(s, s->ppp_j[k])[c] - RAT(s, i)[c];
+          if (distance3(r, r3) < 1.0e-4) { m = k - s->ppp_off[i]; break; }
+        }
+        if (m < 0) continue;
+        /* mpairnay: alpha in PP(i) and in PP(j) at the triplet's vectors */
+        int mm[2];
+        for (int w = 0; w < 2; w++) {
+          int at = w ? j : i;
+          const double *rr = w ? r2 : r1;
+          double r12[3];
+          for (int k = 0; k < 3; k++) r12[k] = RAT(s, al)[k] - rr[k];
+          int imatch = 0;
+          mm[w] = -1;
+          for (int k = s->pp_off[at]; k < s->pp_off[at + 1]; k++) {
+            if (s->pp_j[k] != al) continue;
+            double r21[3];
+            for (int c = 0; c < 3; c++) r21[c] = RAT(s, al)[c] + s->xl[s->pp_b[k]][c] - RAT(s, at)[c];
+            if (distance3(r12, r21) < 0.0001) { imatch++; mm[w] = k - s->pp_off[at]; }
+          }
+          if (imatch != 1) { seterr("mpairnay: imatch = %d for atoms %d, %d", imatch, at + 1, al + 1); return E_BACK; }
+        }
+        ivec_push(&CI, i); ivec_push(&CIB, ib); ivec_push(&CJ, j); ivec_push(&CJB, jb);
+        ivec_push(&CM, m); ivec_push(&C31, mm[0]); ivec_push(&C32, mm[1]);
+      }
+    }
+    s->ppc_off[al + 1] = CI.n;
+  }
+  s->ppc_i = CI.v; s->ppc_ib = CIB.v; s->ppc_j = CJ.v; s->ppc_jb = CJB.v;
+  s->ppc_m = CM.v; s->ppc_m31 = C31.v; s->ppc_m32 = C32.v;
+  s->have_pp = 1;
+  return OK;
+}
+
+void or_pp_sizes(const or_sys *s, int *npp, int *nppx, int *nppp, int *ntrip, long long *nsvnl, long long *nvnl) {
+  int N = s->natoms;
+  *npp = s->pp_off[N];
+  *nppx = s->ppx_off[N];
+  *nppp = s->ppp_off[N];
+  *ntrip = s->ppc_off[N];
+  *nsvnl = s->nsvnl;
+  *nvnl = s->nvnl;
+}
+
+/* which: 0 PP (off, j, b, self, map), 1 PPx (off, j, b, self, map, point),
+ * 2 PPp (off, j, b, self); 0-based */
+void or_get_pp(const or_sys *s, int which, int *off, int *jj, int *bb, int *self, int *map, int *point) {
+  int N = s->natoms;
+  const int *o = which == 0 ? s->pp_off : which == 1 ? s->ppx_off : s->ppp_off;
+  const int *J = which == 0 ? s->pp_j : which == 1 ? s->ppx_j : s->ppp_j;
+  const int *B = which == 0 ? s->pp_b : which == 1 ? s->ppx_b : s->ppp_b;
+  const int *S = which == 0 ? s->pp_self : which == 1 ? s->ppx_self : s->ppp_self;
+  memcpy(off, o, sizeof(int) * (N + 1));
+  memcpy(jj, J, sizeof(int) * o[N]);
+  memcpy(bb, B, sizeof(int) * o[N]);
+  memcpy(self, S, sizeof(int) * N);
+  if (map && which < 2) memcpy(map, which == 0 ? s->pp_map : s->ppx_map, sizeof(int) * o[N]);
+  if (point && which == 1) memcpy(point, s->ppx_point, sizeof(int) * o[N]);
+}
+
+void or_get_pp_common(const or_sys *s, int *off, int *ci, int *cib, int *cj, int *cjb, int *m, int *m31, int *m32) {
+  int N = s->natoms, T = s->ppc_off[N];
+  memcpy(off, s->ppc_off, sizeof(int) * (N + 1));
+  memcpy(ci, s->ppc_i, sizeof(int) * T); memcpy(cib, s->ppc_ib, sizeof(int) * T);
+  memcpy(cj, s->ppc_j, sizeof(int) * T); memcpy(cjb, s->ppc_jb, sizeof(int) * T);
+  memcpy(m, s->ppc_m, sizeof(int) * T); memcpy(m31, s->ppc_m31, sizeof(int) * T);
+  memcpy(m32, s->ppc_m32, sizeof(int) * T);
+}
+
+/* the PP pair frame: z, sighat, eps = epsilon(r2, sighat) */
+static void pp_frame(const or_sys *s, int i, int j, int mb, double *r1, double *r2, double *z, double *eps) {
+  double sighat[3];
+  for (int k = 0; k < 3; k++) {
+    r1[k] = RAT(s, i)[k];
+    r2[k] = RAT(s, j)[k] + s->xl[mb][k];
+  }
+  *z = distance3(r1, r2);
+  if (*z < 1.0e-05) {
+    sighat[0] = 0.0; sighat[1] = 0.0; sighat[2] = 1.0;
+  } else {
+    for (int k = 0; k < 3; k++) sighat[k] = (r2[k] - r1[k]) / *z;
+  }
+  or_epsilon(r2, sighat, eps);
+}
+
+/* cl(ispecies) (b.FUNCTIONS/cl.f90:50-90): the shell's cl for each of its
+ * 2l+1 projector orbitals */
+static void cl_values(const species_t *sp, double *cl) {
+  int k = 0;
+  for (int issh = 0; issh < sp->nssh_PP; issh++)
+    for (int m = 0; m < 2 * sp->lssh_PP[issh] + 1; m++) cl[k++] = sp->cl_PP[issh];
+}
+
+/* assemble_svnl (j.ASSEMBLERS/M_assemble_PP_2c.f90:86-206) */
+int or_assemble_svnl(or_sys *s, double *svnl) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int j = s->pp_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_PP_max, st;
+      double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+      pp_frame(s, i, j, s->pp_b[p], r1, r2, &z, eps);
+      if ((st = or_getMEs_2c(fd, in1, in2, P_vnl, 0, z, nmu, nnu, mm))) { err = st; continue; }
+      rotate_pp(fd, in1, in2, eps, nmu, nnu, mm, xm);
+      memcpy(svnl + s->svnl_off[p], xm, sizeof(double) * nmu * nnu);
+    }
+  }
+  return err;
+}
+
+/* PPx(imu, inu) = sum_ncc cl(ncc) A(imu, ncc) B(inu, ncc), A, B column-major
+ * with leading dimensions na, nb */
+static void cl_product(const double *cl, int ncl, const double *A, int na, const double *B, int nb, double *out) {
+  for (int inu = 0; inu < nb; inu++)
+    for (int imu = 0; imu < na; imu++) {
+      double acc = 0.0;
+      for (int ncc = 0; ncc < ncl; ncc++) acc = acc + cl[ncc] * A[imu + na * ncc] * B[inu + nb * ncc];
+      out[imu + na * inu] = acc;
+    }
+}
+
+/* assemble_vnl_2c (j.ASSEMBLERS/M_assemble_PP_2c.f90:232-511): the vnl
+ * blocks over PPp, the atom (both orbitals on i, projector on a PP
+ * neighbor), ontop left (projector on i, PPx pairs) and ontop right
+ * (projector on j, PP pairs) terms */
+int or_assemble_vnl_2c(or_sys *s, const double *svnl, double *vnl) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double cl[MAXORB], PPx[MAXORB * MAXORB];
+  for (long long k = 0; k < s->nvnl; k++) vnl[k] = 0.0;
+  for (int i = 0; i < N; i++) {  /* atom */
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    double *dst = vnl + s->vnl_off[s->ppp_off[i] + s->ppp_self[i]];
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int in2 = s->imass[s->pp_j[p]];
+      cl_values(&fd->sp[in2], cl);
+      const double *b = svnl + s->svnl_off[p];
+      cl_product(cl, fd->sp[in2].norb_PP_max, b, nmu, b, nmu, PPx);
+      for (int k = 0; k < nmu * nmu; k++) dst[k] = dst[k] + PPx[k];
+    }
+  }
+  for (int i = 0; i < N; i++) {  /* ontop left */
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    cl_values(&fd->sp[in1], cl);
+    for (int p = s->ppx_off[i]; p < s->ppx_off[i + 1]; p++) {
+      int j = s->ppx_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      if (j == i && s->ppx_b[p] == 0) continue;
+      const double *b1 = svnl + s->svnl_off[s->pp_off[i] + s->pp_self[i]];
+      const double *b2 = svnl + s->svnl_off[s->pp_off[j] + s->ppx_point[p]];
+      cl_product(cl, fd->sp[in1].norb_PP_max, b1, nmu, b2, nnu, PPx);
+      double *dst = vnl + s->vnl_off[s->ppp_off[i] + s->ppx_map[p]];
+      for (int k = 0; k < nmu * nnu; k++) dst[k] = dst[k] + PPx[k];
+    }
+  }
+  for (int i = 0; i < N; i++) {  /* ontop right */
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int j = s->pp_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      if (j == i && s->pp_b[p] == 0) continue;
+      cl_values(&fd->sp[in2], cl);
+      const double *b1 = svnl + s->svnl_off[p];
+      const double *b2 = svnl + s->svnl_off[s->pp_off[j] + s->pp_self[j]];
+      cl_product(cl, fd->sp[in2].norb_PP_max, b1, nmu, b2, nnu, PPx);
+      double *dst = vnl + s->vnl_off[s->ppp_off[i] + s->pp_map[p]];
+      for (int k = 0; k < nmu * nnu; k++) dst[k] = dst[k] + PPx[k];
+    }
+  }
+  return OK;
+}
+
+/* assemble_vnl_3c (j.ASSEMBLERS/M_assemble_PP_3c.f90:94-229), accumulating */
+int or_assemble_vnl_3c(or_sys *s, const double *svnl, double *vnl) {
+  or_fdata *fd = s->fd;
+  double cl[MAXORB], PPx[MAXORB * MAXORB];
+  for (int al = 0; al < s->natoms; al++) {
+    int indna = s->imass[al];
+    cl_values(&fd->sp[indna], cl);
+    for (int t = s->ppc_off[al]; t < s->ppc_off[al + 1]; t++) {
+      int i = s->ppc_i[t], j = s->ppc_j[t];
+      int nmu = fd->sp[s->imass[i]].norb_max, nnu = fd->sp[s->imass[j]].norb_max;
+      const double *b1 = svnl + s->svnl_off[s->pp_off[i] + s->ppc_m31[t]];
+      const double *b2 = svnl + s->svnl_off[s->pp_off[j] + s->ppc_m32[t]];
+      cl_product(cl, fd->sp[indna].norb_PP_max, b1, nmu, b2, nnu, PPx);
+      double *dst = vnl + s->vnl_off[s->ppp_off[i] + s->ppc_m[t]];
+      for (int k = 0; k < nmu * nnu; k++) dst[k] = dst[k] + PPx[k];
+    }
+  }
+  return OK;
+}
+
+/* Dassemble_svnl (k.DASSEMBLERS/M_Dassemble_PP_2c.f90:296-380): Dblock(3,
+ * mu, ncc) of svnl, the derivative with respect to the basis atom i */
+int or_dassemble_svnl(or_sys *s, double *dsvnl) {
+  or_fdata *fd = s->fd;
+  int err = OK;
+  for (int i = 0; i < s->natoms; i++) {
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int j = s->pp_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_PP_max, st;
+      double r1[3], r2[3], z, eps[9], deps[27], eta[3];
+      double mm[MAXORB * MAXORB], dm[MAXORB * MAXORB], vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+      pp_frame(s, i, j, s->pp_b[p], r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < nmu * nnu; k++) mm[k] = dm[k] = 0.0;
+      for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = 0.0;
+      if ((st = or_getDMEs_2c(fd, in1, in2, P_vnl, 0, z, nmu, nnu, mm, dm))) { err = st; continue; }
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++)
+          if (z > 1.0e-3)
+            for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+      drotate_pp(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+      memcpy(dsvnl + 3 * s->svnl_off[p], vdx, sizeof(double) * 3 * nmu * nnu);
+    }
+  }
+  return err;
+}
+
+/* Dassemble_vnl_2c (k.DASSEMBLERS/M_Dassemble_PP_2c.f90:420-745): vnl_atom
+ * per PP pair (self skipped), vnl_ontop per PPx pair (ontop left; the ontop
+ * right force is commented out in the reference, :737-738, and build_forces
+ * doubles the left one instead); rho_pp is the density over PPp */
+int or_dassemble_vnl_2c(or_sys *s, const double *rho_pp, const double *svnl, const double *dsvnl, double *vnl_atom,
+                        double *vnl_ontop) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double cl[MAXORB];
+  for (int k = 0; k < 3 * s->pp_off[N]; k++) vnl_atom[k] = 0.0;
+  for (int k = 0; k < 3 * s->ppx_off[N]; k++) vnl_ontop[k] = 0.0;
+  for (int i = 0; i < N; i++) {
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max;
+    const double *rs = rho_pp + s->vnl_off[s->ppp_off[i] + s->ppp_self[i]];
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      if (p - s->pp_off[i] == s->pp_self[i]) continue;
+      int in2 = s->imass[s->pp_j[p]], ncl = fd->sp[in2].norb_PP_max;
+      cl_values(&fd->sp[in2], cl);
+      const double *b = svnl + s->svnl_off[p], *D = dsvnl + 3 * s->svnl_off[p];
+      double *f = vnl_atom + 3 * (size_t)p;
+      for (int inu = 0; inu < nmu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          double x[3] = {0, 0, 0};
+          for (int ncc = 0; ncc < ncl; ncc++)
+            for (int c = 0; c < 3; c++)
+              x[c] = x[c] + cl[ncc] * (D[c + 3 * (imu + nmu * ncc)] * b[inu + nmu * ncc] +
+                                       b[imu + nmu * ncc] * D[c + 3 * (inu + nmu * ncc)]);
+          for (int c = 0; c < 3; c++) f[c] = f[c] - rs[imu + nmu * inu] * x[c];
+        }
+    }
+  }
+  for (int i = 0; i < N; i++) {
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, ncl = fd->sp[in1].norb_PP_max;
+    cl_values(&fd->sp[in1], cl);
+    for (int p = s->ppx_off[i]; p < s->ppx_off[i + 1]; p++) {
+      int j = s->ppx_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      if (j == i && s->ppx_b[p] == 0) continue;
+      const double *b1 = svnl + s->svnl_off[s->pp_off[i] + s->pp_self[i]];
+      const double *D2 = dsvnl + 3 * s->svnl_off[s->pp_off[j] + s->ppx_point[p]];
+      const double *r = rho_pp + s->vnl_off[s->ppp_off[i] + s->ppx_map[p]];
+      double *f = vnl_ontop + 3 * (size_t)p;
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          double x[3] = {0, 0, 0};
+          for (int ncc = 0; ncc < ncl; ncc++)
+            for (int c = 0; c < 3; c++)
+              x[c] = x[c] - cl[ncc] * b1[imu + nmu * ncc] * D2[c + 3 * (inu + nnu * ncc)];
+          for (int c = 0; c < 3; c++) f[c] = f[c] - r[imu + nmu * inu] * x[c];
+        }
+    }
+  }
+  return OK;
+}
+
+/* Dassemble_vnl_3c (k.DASSEMBLERS/M_Dassemble_PP_3c.f90:127-265) */
+int or_dassemble_vnl_3c(or_sys *s, const double *rho_pp, const double *svnl, const double *dsvnl, double *f3nla,
+                        double *f3nlb, double *f3nlc) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double cl[MAXORB];
+  for (int k = 0; k < 3 * N; k++) f3nla[k] = f3nlb[k] = f3nlc[k] = 0.0;
+  for (int al = 0; al < N; al++) {
+    int indna = s->imass[al], ncl = fd->sp[indna].norb_PP_max;
+    cl_values(&fd->sp[indna], cl);
+    for (int t = s->ppc_off[al]; t < s->ppc_off[al + 1]; t++) {
+      int i = s->ppc_i[t], j = s->ppc_j[t];
+      int nmu = fd->sp[s->imass[i]].norb_max, nnu = fd->sp[s->imass[j]].norb_max;
+      long long o1 = s->svnl_off[s->pp_off[i] + s->ppc_m31[t]], o2 = s->svnl_off[s->pp_off[j] + s->ppc_m32[t]];
+      const double *b1 = svnl + o1, *b2 = svnl + o2, *D1 = dsvnl + 3 * o1, *D2 = dsvnl + 3 * o2;
+      const double *r = rho_pp + s->vnl_off[s->ppp_off[i] + s->ppc_m[t]];
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          double xb[3] = {0, 0, 0}, xc[3] = {0, 0, 0};
+          for (int ncc = 0; ncc < ncl; ncc++)
+            for (int c = 0; c < 3; c++) {
+              xb[c] = xb[c] + cl[ncc] * D1[c + 3 * (imu + nmu * ncc)] * b2[inu + nnu * ncc];
+              xc[c] = xc[c] + cl[ncc] * b1[imu + nmu * ncc] * D2[c + 3 * (inu + nnu * ncc)];
+            }
+          double rr = r[imu + nmu * inu];
+          for (int c = 0; c < 3; c++) {
+            double xa = -xb[c] - xc[c];
+            f3nla[3 * al + c] = f3nla[3 * al + c] - rr * xa;
+            f3nlb[3 * i + c] = f3nlb[3 * i + c] - rr * xb[c];
+            f3nlc[3 * j + c] = f3nlc[3 * j + c] - rr * xc[c];
+          }
+        }
+    }
+  }
+  return OK;
+}
+
+/* build_forces, vnl terms (c.SYSTEM/M_build_forces.f90:395-461): vnl(i) =
+ * sum of vnl_atom over PP pairs (i +, j -) and 2 vnl_ontop over PPx pairs
+ * (i +, j -); ftot_add = vnl + f3nla + f3nlb + f3nlc */
+int or_build_forces_vnl(or_sys *s, const double *vnl_atom, const double *vnl_ontop, const double *f3nla,
+                        const double *f3nlb, const double *f3nlc, double *vnl, double *ftot_add) {
+  int N = s->natoms;
+  for (int k = 0; k < 3 * N; k++) vnl[k] = 0.0;
+  for (int i = 0; i < N; i++) {
+    for (int p = s->pp_off[i]; p < s->pp_off[i + 1]; p++) {
+      int j = s->pp_j[p];
+      for (int c = 0; c < 3; c++) {
+        vnl[3 * i + c] = vnl[3 * i + c] + vnl_atom[3 * p + c];
+        vnl[3 * j + c] = vnl[3 * j + c] - vnl_atom[3 * p + c];
+      }
+    }
+    for (int p = s->ppx_off[i]; p < s->ppx_off[i + 1]; p++) {
+      int j = s->ppx_j[p];
+      for (int c = 0; c < 3; c++) {
+        vnl[3 * i + c] = vnl[3 * i + c] + 2.0 * vnl_ontop[3 * p + c];
+        vnl[3 * j + c] = vnl[3 * j + c] - 2.0 * vnl_ontop[3 * p + c];
+      }
+    }
+  }
+  for (int k = 0; k < 3 * N; k++) ftot_add[k] = vnl[k] + f3nla[k] + f3nlb[k] + f3nlc[k];
+  return OK;
 }

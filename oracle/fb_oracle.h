@@ -100,6 +100,33 @@ int or_dassemble_vna_3c_dogs(or_sys *s, const double *rho, const double *S,
                              const double *ddip, double *f3naa,
                              double *f3nab, double *f3nac);
 
+/* non-local pseudopotential (vnl): driver_neighbors_PP; sizes (pairs of the
+ * PP, PPx, PPp maps, PP common triplets, svnl and vnl block doubles); the
+ * maps (0-based; which 0 PP, 1 PPx, 2 PPp); assemble_svnl / vnl_2c /
+ * vnl_3c (vnl_3c accumulates); the derivatives and the build_forces vnl
+ * terms.  rho_pp: the density over PPp (s%denmat_PP). */
+int or_neighbors_pp(or_sys *s);
+void or_pp_sizes(const or_sys *s, int *npp, int *nppx, int *nppp, int *ntrip,
+                 long long *nsvnl, long long *nvnl);
+void or_get_pp(const or_sys *s, int which, int *off, int *jj, int *bb,
+               int *self, int *map, int *point);
+void or_get_pp_common(const or_sys *s, int *off, int *ci, int *cib, int *cj,
+                      int *cjb, int *m, int *m31, int *m32);
+int or_assemble_svnl(or_sys *s, double *svnl);
+int or_assemble_vnl_2c(or_sys *s, const double *svnl, double *vnl);
+int or_assemble_vnl_3c(or_sys *s, const double *svnl, double *vnl);
+int or_dassemble_svnl(or_sys *s, double *dsvnl);
+int or_dassemble_vnl_2c(or_sys *s, const double *rho_pp, const double *svnl,
+                        const double *dsvnl, double *vnl_atom,
+                        double *vnl_ontop);
+int or_dassemble_vnl_3c(or_sys *s, const double *rho_pp, const double *svnl,
+                        const double *dsvnl, double *f3nla, double *f3nlb,
+                        double *f3nlc);
+int or_build_forces_vnl(or_sys *s, const double *vnl_atom,
+                        const double *vnl_ontop, const double *f3nla,
+                        const double *f3nlb, const double *f3nlc, double *vnl,
+                        double *ftot_add);
+
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */
 int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x,

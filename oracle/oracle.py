@@ -59,6 +59,20 @@ def lib():
         L.or_assemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_assemble_vna_3c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_dassemble_dipole_z.argtypes = [C.c_void_p, _dp]
+        L.or_neighbors_pp.argtypes = [C.c_void_p]
+        L.or_pp_sizes.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_longlong)] * 2
+        L.or_pp_sizes.restype = None
+        L.or_get_pp.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, C.c_void_p, C.c_void_p]
+        L.or_get_pp.restype = None
+        L.or_get_pp_common.argtypes = [C.c_void_p] + [_ip] * 8
+        L.or_get_pp_common.restype = None
+        L.or_assemble_svnl.argtypes = [C.c_void_p, _dp]
+        L.or_assemble_vnl_2c.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_assemble_vnl_3c.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_dassemble_svnl.argtypes = [C.c_void_p, _dp]
+        L.or_dassemble_vnl_2c.argtypes = [C.c_void_p] + [_dp] * 5
+        L.or_dassemble_vnl_3c.argtypes = [C.c_void_p] + [_dp] * 6
+        L.or_build_forces_vnl.argtypes = [C.c_void_p] + [_dp] * 7
         L.or_dassemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_dassemble_vna_3c_dogs.argtypes = [C.c_void_p] + [_dp] * 8
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
@@ -239,6 +253,69 @@ class System:
         _check(L.or_build_forces(self.h, rho, cape, dS, dT, ontop, atom, fa, fb, fc, kin, vna, pul, ftot))
         return dict(dS=dS, dT=dT, ddip=ddip, vna_ontop=ontop, vna_atom=atom, f3naa=fa, f3nab=fb, f3nac=fc,
                     kinetic=kin, vna=vna, pulay=pul, ftot=ftot)
+
+    # ---- non-local pseudopotential (vnl) --------------------------------
+    def neighbors_pp(self):
+        """driver_neighbors_PP: PP, PPx and PPp maps (0-based) and the PP
+        common-neighbor triplets."""
+        L = lib()
+        _check(L.or_neighbors_pp(self.h))
+        n = [C.c_int() for _ in range(4)]
+        b = [C.c_longlong() for _ in range(2)]
+        L.or_pp_sizes(self.h, *[C.byref(x) for x in n], *[C.byref(x) for x in b])
+        self.npp, self.nppx, self.nppp, self.ntrip_pp = (x.value for x in n)
+        self.nsvnl, self.nvnl = (x.value for x in b)
+        N = len(self.imass)
+        self.pp = {}
+        for which, name, cnt in ((0, "PP", self.npp), (1, "PPx", self.nppx), (2, "PPp", self.nppp)):
+            off = np.zeros(N + 1, np.int32)
+            jj, bb = np.zeros(max(cnt, 1), np.int32), np.zeros(max(cnt, 1), np.int32)
+            self_ = np.zeros(N, np.int32)
+            mp, pt = np.zeros(max(cnt, 1), np.int32), np.zeros(max(cnt, 1), np.int32)
+            L.or_get_pp(self.h, which, off, jj, bb, self_, mp.ctypes.data_as(C.c_void_p) if which < 2 else None,
+                        pt.ctypes.data_as(C.c_void_p) if which == 1 else None)
+            d = dict(off=off, j=jj[:cnt], b=bb[:cnt], self=self_)
+            if which < 2:
+                d["map"] = mp[:cnt]
+            if which == 1:
+                d["point"] = pt[:cnt]
+            self.pp[name] = d
+        T = self.ntrip_pp
+        arrs = [np.zeros(N + 1, np.int32)] + [np.zeros(max(T, 1), np.int32) for _ in range(7)]
+        L.or_get_pp_common(self.h, *arrs)
+        self.pp["common"] = dict(off=arrs[0], i=arrs[1][:T], ib=arrs[2][:T], j=arrs[3][:T], jb=arrs[4][:T],
+                                 m=arrs[5][:T], m31=arrs[6][:T], m32=arrs[7][:T])
+        return self
+
+    def assemble_pp(self, with3c=True):
+        """svnl blocks (PP pairs) and vnl blocks (PPp pairs)."""
+        L = lib()
+        svnl, vnl = np.zeros(max(self.nsvnl, 1)), np.zeros(max(self.nvnl, 1))
+        _check(L.or_assemble_svnl(self.h, svnl))
+        _check(L.or_assemble_vnl_2c(self.h, svnl, vnl))
+        if with3c:
+            _check(L.or_assemble_vnl_3c(self.h, svnl, vnl))
+        return svnl[:self.nsvnl], vnl[:self.nvnl]
+
+    def dassemble_pp(self, rho_pp):
+        """vnl force pass with the density over PPp: dsvnl, vnl_atom (per PP
+        pair), vnl_ontop (per PPx pair), f3nl{a,b,c}, the vnl force and the
+        build_forces addition to ftot."""
+        L = lib()
+        N = len(self.imass)
+        svnl = np.zeros(max(self.nsvnl, 1))
+        _check(L.or_assemble_svnl(self.h, svnl))
+        dsvnl = np.zeros(max(3 * self.nsvnl, 1))
+        _check(L.or_dassemble_svnl(self.h, dsvnl))
+        rho = np.ascontiguousarray(rho_pp, np.float64)
+        va, vo = np.zeros(max(3 * self.npp, 1)), np.zeros(max(3 * self.nppx, 1))
+        _check(L.or_dassemble_vnl_2c(self.h, rho, svnl, dsvnl, va, vo))
+        fa, fb, fc = np.zeros(3 * N), np.zeros(3 * N), np.zeros(3 * N)
+        _check(L.or_dassemble_vnl_3c(self.h, rho, svnl, dsvnl, fa, fb, fc))
+        vnl, add = np.zeros(3 * N), np.zeros(3 * N)
+        _check(L.or_build_forces_vnl(self.h, va, vo, fa, fb, fc, vnl, add))
+        return dict(dsvnl=dsvnl[:3 * self.nsvnl], vnl_atom=va[:3 * self.npp], vnl_ontop=vo[:3 * self.nppx],
+                    f3nla=fa, f3nlb=fb, f3nlc=fc, vnl=vnl, ftot_vnl=add)
 
 
 def getMEs_2c(fd, isp, jsp, iint, x, nmu, nnu, isub=0):

@@ -1,0 +1,158 @@
+"""The oracle's restatement of the non-local pseudopotential path
+(c.SYSTEM/M_neighbors_PP.f90, j.ASSEMBLERS/M_assemble_PP_{2c,3c}.f90,
+k.DASSEMBLERS/M_Dassemble_PP_{2c,3c}.f90, the vnl terms of build_forces):
+the PP and PPx maps against a brute-force search, the PPp map, its maps and
+points against their definitions, Hermitian vnl blocks, and forces equal to
+minus the gradient of sum rho_pp . vnl."""
+import numpy as np
+import pytest
+
+from conftest import workload
+from fbgpu import synth
+from oracle import oracle as orc
+
+
+def _xl(lattice):
+    out = [np.zeros(3)]
+    for iz in range(-4, 5):
+        for iy in range(-4, 5):
+            for ix in range(-4, 5):
+                if ix or iy or iz:
+                    out.append(ix * lattice[0] + iy * lattice[1] + iz * lattice[2])
+    return np.array(out)
+
+
+SPECIES = {"sic_vac": "sic4096", "cho_small": "cho1536", "si_vac": "si64"}
+
+
+@pytest.fixture(scope="module", params=["sic_vac", "cho_small"])
+def pp_system(request, fdata_root):
+    name = request.param
+    path, nZ, st = workload(name, fdata_root)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors().neighbors_pp()
+    return name, fd, s, st
+
+
+def test_pp_maps(pp_system):
+    name, fd, s, st = pp_system
+    sp = synth.species_for(SPECIES[name])
+    rcA = np.array([max(r * 0.529177 for r in x.rcutoff) for x in sp])[st.imass - 1]
+    rcpp = np.array([x.rcutoff_pp for x in sp])[st.imass - 1]
+    xl = _xl(st.lattice)
+    N = len(st.imass)
+    for key, ri, rj in (("PP", rcA, rcpp), ("PPx", rcpp, rcA)):
+        m = s.pp[key]
+        for i in range(N):
+            want = []
+            for mb in range(len(xl)):
+                d = np.linalg.norm(st.ratom + xl[mb] - st.ratom[i], axis=1)
+                for j in np.nonzero(d < ri[i] + rj - 0.01)[0]:
+                    want.append((j, mb))
+            got = list(zip(m["j"][m["off"][i]:m["off"][i + 1]], m["b"][m["off"][i]:m["off"][i + 1]]))
+            assert got == want, (key, i)
+            k = m["off"][i] + m["self"][i]
+            assert m["j"][k] == i and m["b"][k] == 0
+    ppp = s.pp["PPp"]
+    for i in range(N):
+        lst = list(zip(ppp["j"][ppp["off"][i]:ppp["off"][i + 1]], ppp["b"][ppp["off"][i]:ppp["off"][i + 1]]))
+        assert len(set(lst)) == len(lst)
+        for key in ("PP", "PPx"):
+            m = s.pp[key]
+            for p in range(m["off"][i], m["off"][i + 1]):
+                assert lst[m["map"][p]] == (m["j"][p], m["b"][p])
+        m = s.pp["PPx"]
+        for p in range(m["off"][i], m["off"][i + 1]):
+            j, jb = m["j"][p], m["b"][p]
+            k = s.pp["PP"]["off"][j] + m["point"][p]
+            r = st.ratom[s.pp["PP"]["j"][k]] + xl[s.pp["PP"]["b"][k]] + xl[jb]
+            assert np.linalg.norm(r - st.ratom[i]) < 1e-4
+    c = s.pp["common"]
+    assert len(c["i"]) > 0
+
+
+def _back(s, st, xl):
+    """index of (j, i, -xl) in PPp(j) for every PPp pair (i, j, xl)"""
+    ppp = s.pp["PPp"]
+    N = len(st.imass)
+    back = np.zeros(len(ppp["j"]), np.int64)
+    for i in range(N):
+        for p in range(ppp["off"][i], ppp["off"][i + 1]):
+            j, mb = ppp["j"][p], ppp["b"][p]
+            for q in range(ppp["off"][j], ppp["off"][j + 1]):
+                if ppp["j"][q] == i and np.linalg.norm(xl[ppp["b"][q]] + xl[mb]) < 1e-9:
+                    back[p] = q
+                    break
+            else:
+                raise AssertionError("no back pair")
+    return back
+
+
+def _vnl_off(s, fd, st):
+    ppp = s.pp["PPp"]
+    norb = np.array([fd.norb(int(q)) for q in st.imass])
+    off = np.zeros(len(ppp["j"]) + 1, np.int64)
+    for i in range(len(st.imass)):
+        for p in range(ppp["off"][i], ppp["off"][i + 1]):
+            off[p + 1] = off[p] + norb[i] * norb[ppp["j"][p]]
+    return off, norb
+
+
+def test_vnl_hermitian(pp_system):
+    name, fd, s, st = pp_system
+    xl = _xl(st.lattice)
+    _, vnl = s.assemble_pp()
+    back = _back(s, st, xl)
+    off, norb = _vnl_off(s, fd, st)
+    ppp = s.pp["PPp"]
+    assert off[-1] == len(vnl)
+    for i in range(len(st.imass)):
+        for p in range(ppp["off"][i], ppp["off"][i + 1]):
+            j, q = ppp["j"][p], back[p]
+            a = vnl[off[p]:off[p + 1]].reshape(norb[j], norb[i]).T
+            b = vnl[off[q]:off[q + 1]].reshape(norb[i], norb[j]).T
+            assert np.abs(a - b.T).max() < 1e-12
+
+
+def _sym_rho(s, fd, st, seed):
+    xl = _xl(st.lattice)
+    back = _back(s, st, xl)
+    off, norb = _vnl_off(s, fd, st)
+    ppp = s.pp["PPp"]
+    rng = np.random.default_rng(seed)
+    rho = np.zeros(off[-1])
+    done = np.zeros(len(ppp["j"]), bool)
+    for i in range(len(st.imass)):
+        for p in range(ppp["off"][i], ppp["off"][i + 1]):
+            if done[p]:
+                continue
+            j, q = ppp["j"][p], back[p]
+            blk = rng.uniform(-0.5, 0.5, (norb[i], norb[j]))
+            if q == p:
+                blk = 0.5 * (blk + blk.T)
+            rho[off[p]:off[p + 1]] = blk.T.ravel()
+            rho[off[q]:off[q + 1]] = blk.ravel()
+            done[p] = done[q] = True
+    return rho
+
+
+def test_vnl_forces_are_minus_gradient(pp_system):
+    name, fd, s, st = pp_system
+    rho = _sym_rho(s, fd, st, 3)
+    d = s.dassemble_pp(rho)
+    f = d["ftot_vnl"].reshape(-1, 3)
+    h = 1e-5
+
+    def energy(r):
+        t = orc.System(fd, r, st.imass, st.lattice).neighbors().neighbors_pp()
+        assert t.nppp == s.nppp and np.array_equal(t.pp["PPp"]["j"], s.pp["PPp"]["j"])
+        return float(rho @ t.assemble_pp()[1])
+
+    rng = np.random.default_rng(8)
+    for i in rng.choice(len(st.imass), 3, replace=False):
+        for k in range(3):
+            rp, rm = st.ratom.copy(), st.ratom.copy()
+            rp[i, k] += h
+            rm[i, k] -= h
+            g = -(energy(rp) - energy(rm)) / (2 * h)
+            assert abs(g - f[i, k]) < 1e-5 * max(1.0, abs(g)), (i, k, g, f[i, k])

@@ -35,6 +35,7 @@ P_ABOHR = 0.529177  # include/constants.h:2
 
 # interaction ids (include/interactions_2c.h:5-9, interactions_3c.h:8)
 P_OVERLAP, P_KINETIC, P_VNA_ONTOPL, P_VNA_ONTOPR, P_VNA_ATOM = 1, 2, 3, 4, 5
+P_VNL = 6           # include/interactions_2c.h:10
 P_DIPOLE_Z = 10     # include/interactions_2c.h:14
 P_BCNA = 3
 P_NTHETA = 5
@@ -213,7 +214,7 @@ def _seed_of(*keys):
 
 
 _AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P_VNA_ATOM: 0.3,
-         P_DIPOLE_Z: 0.5}
+         P_DIPOLE_Z: 0.5, P_VNL: 0.5}
 
 
 def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi, isub=0):
@@ -231,6 +232,22 @@ def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi, isub=0):
     mkey = ma if asym_pi else abs(ma)
     if mkey != 0:
         rng = np.random.default_rng(_seed_of(seed, "2c", itype, zA, zB, sa, la, sb, lb, mkey, *sub))
+        val = val + t * t * amp * _f1d(rng.normal(0.0, 1.0, 12), t, False)
+    return val
+
+
+def table2c_vnl(seed, A, B, oa, ob, t):
+    """<A oa | projector B ob> (interaction 6): a basis orbital of A against
+    a pseudopotential projector of B.  No transpose symmetry relates it to
+    <B ob | projector A oa>, so every (A, B) pair has its own channels; the
+    m != 0 channels follow the m = 0 one as in _base2c (rotation invariant)."""
+    sa, la, ma = oa
+    sb, lb, mb = ob
+    amp = _AMP2[P_VNL]
+    rng = np.random.default_rng(_seed_of(seed, "vnl", A.nZ, B.nZ, sa, la, sb, lb, 0))
+    val = amp * _f1d(rng.normal(0.0, 1.0, 12), t, (la + lb) % 2 == 1)
+    if ma != 0:
+        rng = np.random.default_rng(_seed_of(seed, "vnl", A.nZ, B.nZ, sa, la, sb, lb, abs(ma)))
         val = val + t * t * amp * _f1d(rng.normal(0.0, 1.0, 12), t, False)
     return val
 
@@ -362,24 +379,31 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
                                   ma if itype == P_VNA_ATOM else mm))
             if dogs:
                 cells.append((P_DIPOLE_Z, 0, "dipole_z", mm))
+            # non-local pseudopotential <basis i | projector j> (every Fdata set)
+            cells.append((P_VNL, 0, "vnl", make_munu(si_.lssh, sj.lssh_pp)))
             with open(os.path.join(path, "2c.%s.dat" % zz), "w") as f:
                 f.write("%d\n" % len(cells))
             munu_records = {}
             with open(os.path.join(path, "2c.%s.dir" % zz), "w") as fd:
                 for icell, (itype, isub, stem, (mu, nu, mv)) in enumerate(cells, start=1):
                     fname = "%s.%s.dat" % (stem, zz)
-                    ls_b = si_.lssh if itype == P_VNA_ATOM else sj.lssh
+                    ls_b = si_.lssh if itype == P_VNA_ATOM else sj.lssh_pp if itype == P_VNL else sj.lssh
                     orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(ls_b)
+                    xm = si_.rcA + sj.rcutoff_pp if itype == P_VNL else xmax
+                    tt = np.linspace(0.0, xm, nx2c) / xm
                     data = np.zeros((nx2c, len(mu)))
                     for ime in range(len(mu)):
-                        data[:, ime] = table2c(seed, itype, si_, sj, orb_a[mu[ime] - 1],
-                                               orb_b[nu[ime] - 1], t, asym_pi, isub)
+                        if itype == P_VNL:
+                            data[:, ime] = table2c_vnl(seed, si_, sj, orb_a[mu[ime] - 1], orb_b[nu[ime] - 1], tt)
+                        else:
+                            data[:, ime] = table2c(seed, itype, si_, sj, orb_a[mu[ime] - 1],
+                                                   orb_b[nu[ime] - 1], t, asym_pi, isub)
                     with open(os.path.join(path, fname), "w") as f:
                         for ix in range(nx2c):
                             f.write(_fmt(data[ix]) + "\n")
                         f.write("\n")
                     fd.write("  %3d %3d %3d %-29s %3d %4d %9.6f\n"
-                             % (icell, itype, isub, fname, len(mu), nx2c, xmax))
+                             % (icell, itype, isub, fname, len(mu), nx2c, xm))
                     munu_records.setdefault(itype, []).append((mu, nu, mv))
             for itype, recs in munu_records.items():
                 with open(os.path.join(path, "%02d_munu_2c.%s.dat" % (itype, zz)), "w") as f:
@@ -559,7 +583,7 @@ def fdata_dir_for(workload, root=None, dogs=False):
     key = {"si64": "Si_rc50", "si512": "Si_rc50", "cho1536": "CHO_rc45_40_40",
            "sic4096": "SiC_rc50", "batch256": "SiC_rc50"}[workload]
     path = os.path.join(root, key + ("_DOGS" if dogs else ""))
-    stamp = os.path.join(path, ".complete")
+    stamp = os.path.join(path, ".complete_vnl")
     if not os.path.exists(stamp):
         write_fdata(path, species_for(workload), dogs=dogs)
         with open(stamp, "w") as f:
