@@ -76,6 +76,9 @@ extern "C" {
 #define FB_ALL 15u
 #define FB_KEEP_DBLOCKS 16u  /* fb_dassemble: also keep dS, dT Dblocks */
 #define FB_FORCES 32u        /* fb_assemble_graph / fb_autotune: the force pass too */
+#define FB_SVNL 128u         /* svnl blocks <basis i | projectors j> (assemble_svnl, M_assemble_PP_2c.f90:86) */
+#define FB_VNL2C 256u        /* vnl 2c: atom, ontop left / right (assemble_vnl_2c, M_assemble_PP_2c.f90:232) */
+#define FB_VNL3C 512u        /* vnl 3c (assemble_vnl_3c, M_assemble_PP_3c.f90:94); fb_dassemble: the vnl forces */
 #define FB_DIPOLE 64u        /* z-dipole blocks (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499);
                                 with FB_THEORY_DOGS, FB_VNA2C computes them and FB_S as well */
 
@@ -89,6 +92,10 @@ extern "C" {
 #define FB_BLOCK_RHO 6     /* s%denmat(i)%neighbors(k)%block (input) */
 #define FB_BLOCK_CAPE 7    /* s%capemat(i)%neighbors(k)%block (input) */
 #define FB_BLOCK_DIP 8     /* s%dipole_z(i)%neighbors(k)%block (FB_DIPOLE) */
+#define FB_BLOCK_SVNL 9    /* s%svnl(i)%neighbors(k)%block over PP pairs, norb_i x norb_PP_j */
+#define FB_BLOCK_VNL 10    /* s%vnl(i)%neighbors(k)%block over PPp pairs, norb_i x norb_j */
+#define FB_BLOCK_DSVNL 11  /* s%svnl(i)%neighbors(k)%Dblock (after the vnl force pass) */
+#define FB_BLOCK_RHO_PP 12 /* s%denmat_PP(i)%neighbors(k)%block (input, PPp pairs) */
 
 /* force arrays for fb_get_forces */
 #define FB_F_TOT 0         /* ftot: kinetic + vna + f3na(a+b+c) - pulay */
@@ -100,6 +107,12 @@ extern "C" {
 #define FB_F_F3NAC 6       /* forces(i)%f3nac */
 #define FB_F_VNA_ONTOP 7   /* forces(i)%vna_ontop(3, neighn), per pair */
 #define FB_F_VNA_ATOM 8    /* forces(i)%vna_atom(3, neighn), per pair */
+#define FB_F_VNL 9         /* forces(i)%vnl: the vnl atom and ontop pair sums */
+#define FB_F_F3NLA 10      /* forces(i)%f3nla */
+#define FB_F_F3NLB 11      /* forces(i)%f3nlb */
+#define FB_F_F3NLC 12      /* forces(i)%f3nlc */
+#define FB_F_VNL_ATOM 13   /* forces(i)%vnl_atom(3, neighn_PP), per PP pair */
+#define FB_F_VNL_ONTOP 14  /* forces(i)%vnl_ontop(3, neighn_PPx), per PPx pair (ontop left) */
 
 typedef struct fb_ctx fb_ctx;
 
@@ -339,6 +352,39 @@ long long fb_norbitals(const fb_ctx *ctx);
 int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts,
                     const void *extra_dev, void *Hk_dev, void *Sk_dev);
 int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
+
+/* Non-local pseudopotential (vnl).  fb_neighbors_pp replaces
+ * driver_neighbors_PP (c.SYSTEM/M_neighbors_PP.f90:98-151): the PP map
+ * (basis of i within rcA_i + rc_PP_j - 0.01 of the projectors of j), the PPx
+ * map (projectors of i, basis of j), the PPp map (atoms sharing a projector
+ * atom, in the reference's first-occurrence order) with the PP and PPx maps
+ * into it and the PPx points into PP(j), and the PP common-neighbor triplets
+ * (find_common_neighbors_PP with mpairnay's svnl indices).  Needs Fdata with
+ * the vnl tables (interaction 6) and projector shells of s, sp or spd; single
+ * structures.  fb_assemble with FB_SVNL / FB_VNL2C / FB_VNL3C assembles
+ * svnl over PP pairs and vnl over PPp pairs; fb_set_denmat_pp gives
+ * s%denmat_PP (PPp layout, FB_BLOCK_RHO_PP) and fb_dassemble with FB_VNL2C /
+ * FB_VNL3C computes Dassemble_svnl, Dassemble_vnl_2c (vnl_atom, vnl_ontop;
+ * the reference leaves the ontop-right force out, M_Dassemble_PP_2c.f90:
+ * 737-738, and build_forces doubles the left one), Dassemble_vnl_3c
+ * (f3nla/b/c) and the vnl terms of build_forces (M_build_forces.f90:395-461),
+ * added into FB_F_TOT.  The maps are returned 1-based as the reference
+ * numbers them: which = FB_PP_MAP (neighn, neigh_j, neigh_b, self, map into
+ * PPp), FB_PPX_MAP (also point into PP(j)) or FB_PPP_MAP (no map / point). */
+#define FB_PP_MAP 0
+#define FB_PPX_MAP 1
+#define FB_PPP_MAP 2
+int fb_neighbors_pp(fb_ctx *ctx);
+int fb_get_pp_sizes(fb_ctx *ctx, int *npp, int *nppx, int *nppp, int *ntrip,
+                    long long *nsvnl, long long *nvnl);
+int fb_get_pp_neighbors(fb_ctx *ctx, int which, int *neighn, int *neigh_j,
+                        int *neigh_b, int *self, int *map, int *point);
+int fb_get_pp_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j,
+                     int *iatom_common_b, int *jatom_common_j,
+                     int *jatom_common_b, int *neigh_common, int *m31,
+                     int *m32);
+int fb_set_denmat_pp(fb_ctx *ctx, const double *rho_pp);
+int fb_set_denmat_pp_device(fb_ctx *ctx, const void *rho_pp_dev);
 
 /* Theory of the neutral-atom terms.  FB_THEORY_HARRIS (the default):
  * assemble_vna_2c / assemble_vna_3c of the Harris functional

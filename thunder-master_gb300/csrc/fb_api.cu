@@ -14,6 +14,7 @@
 #include "../../include/fbgpu.h"
 #include "fb_fdata.h"
 #include "fb_launch.h"
+#include "fb_pp.h"
 #include "fb_devbuf.h"
 #include "fb_mlp.h"
 
@@ -26,11 +27,11 @@ std::atomic<long long> g_alloc_gen{0};
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
        KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
-       KT_BLOCH, KT_N };
+       KT_BLOCH, KT_PP_NEIGH, KT_PP, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
-                                     "dassemble_3c_mlp", "bloch"};
+                                     "dassemble_3c_mlp", "bloch", "pp_neighbors", "vnl"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -74,6 +75,18 @@ struct fb_ctx {
   // the DOGS shell charges dq[atom][MAXSUB]
   int theory = FB_THEORY_HARRIS;
   DevBuf d_dq, d_dogs_ps;
+  // non-local pseudopotential: maps (driver_neighbors_PP), blocks, forces
+  bool have_pp_neigh = false, have_rho_pp = false;
+  int npp = 0, nppx = 0, nppp = 0, ntrip_pp = 0;
+  long long nsvnl = 0, nvnl = 0;
+  std::vector<int> h_pp_off, h_ppx_off, h_ppp_off, h_ppc_off;
+  std::vector<long long> h_svnl_base, h_vnl_base;
+  DevBuf d_pp_cnt, d_pp_off, d_pp_j, d_pp_b, d_pp_self, d_pp_map, d_svnl_sum, d_svnl_base, d_svnl_off;
+  DevBuf d_ppx_cnt, d_ppx_off, d_ppx_j, d_ppx_b, d_ppx_self, d_ppx_map, d_ppx_point;
+  DevBuf d_ub, d_pslot_off, d_pslot_j, d_pslot_b, d_ppp_cnt, d_vnl_sum, d_ppp_off, d_vnl_base, d_ppp_j, d_ppp_b,
+      d_ppp_self, d_vnl_off;
+  DevBuf d_ppc_cnt, d_ppc_off, d_t_alpha, d_t_i, d_t_ib, d_t_j, d_t_jb, d_t_m, d_t_m31, d_t_m32;
+  DevBuf d_svnl, d_dsvnl, d_vnl, d_rho_pp, d_vnl_atom, d_vnl_ontop, d_f3nla, d_f3nlb, d_f3nlc, d_fvnl;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -89,6 +102,7 @@ struct fb_ctx {
   // maps of the same sizes reuse it).
   cudaGraphExec_t gexec = nullptr;
   unsigned g_what = 0;
+  int g_npp = -1, g_nppx = -1, g_nppp = -1, g_ntrip_pp = -1;
   int g_theory = -1, g_prec = -1, g_N = -1, g_P = -1, g_T = -1, g_have_d = -1, g_mlp_n = -1, g_mlp_mode = -1, g_mlp_engine = -1;
   long long g_nblock = -1, g_alloc = -1, g_launches = 0;
   cudaStream_t g_stream = nullptr;
@@ -110,6 +124,10 @@ struct fb_ctx {
   double kt_ms[KT_N] = {0};
   long long kt_n[KT_N] = {0};
 };
+
+static PPArgs pp_args(fb_ctx *ctx);
+template <typename T>
+static int host_scan(fb_ctx *ctx, const DevBuf &cnt, int n, std::vector<T> &off, DevBuf &d_off);
 
 static int fail(fb_ctx *c, int code, const char *fmt, ...) {
   char b[1024];
@@ -182,6 +200,12 @@ static int status_error(fb_ctx *ctx, unsigned st) {
     cudaMemcpy(info, ctx->d_errinfo.p, sizeof info, cudaMemcpyDeviceToHost);
     return fail(ctx, FB_ERR_ATOMS_CLOSE, "atoms dangerously close: iatom %d jatom %d mbeta %d", info[0] + 1,
                 info[1] + 1, info[2]);
+  }
+  if (st & DEVERR_CAP) {
+    int info[3] = {0, 0, 0};
+    cudaMemcpy(info, ctx->d_errinfo.p, sizeof info, cudaMemcpyDeviceToHost);
+    return fail(ctx, FB_ERR_CAPACITY, "PPp: the image of atom %d seen from atom %d lies outside the 9x9x9 image box",
+                info[1] + 1, info[0] + 1);
   }
   if (st & DEVERR_SELF) return fail(ctx, FB_ERR_NEIGH_SELF, "neigh_self missing");
   if (st & DEVERR_BACK) return fail(ctx, FB_ERR_NEIGH_BACK, "neigh_back missing or found twice");
@@ -283,6 +307,7 @@ int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies, const int *n
   CU(cudaMemcpy(ctx->d_gxy.p, f.gxy.data(), f.gxy.size() * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_fdata = true;
   ctx->have_neigh = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = false;
   return FB_OK;
 }
 
@@ -308,7 +333,8 @@ static void make_images(fb_ctx *ctx, int s, const double *ratom) {
   double D = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
                        (hi[2] - lo[2]) * (hi[2] - lo[2]));
   double rmax = 0.0;
-  for (int k = 0; k < ctx->fdh.nspecies; k++) rmax = std::max(rmax, ctx->fdh.sp[k].rcA);
+  for (int k = 0; k < ctx->fdh.nspecies; k++)
+    rmax = std::max(rmax, std::max(ctx->fdh.sp[k].rcA, ctx->fdh.sp[k].rc_pp));
   double reach = std::max(2.0 * rmax, 0.5) + D + 1.0;
   const double *X = &ctx->h_xl[(size_t)s * XL_STRIDE];
   for (int mb = 0; mb < NIMG; mb++) {
@@ -381,6 +407,7 @@ int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms, const double *rato
   CU(cudaMemcpy(ctx->d_satom_off.p, ctx->h_satom_off.data(), (nstruct + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_speriodic.p, per.data(), nstruct * sizeof(int), cudaMemcpyHostToDevice));
   ctx->have_neigh = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = false;
   return fb_update_positions(ctx, ratom);
 }
 
@@ -437,6 +464,7 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_neigh = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = false;
   return FB_OK;
 }
 
@@ -739,6 +767,170 @@ int fb_get_neighbors(fb_ctx *ctx, int *neighn, int *neigh_j, int *neigh_b, int *
   return FB_OK;
 }
 
+// driver_neighbors_PP (c.SYSTEM/M_neighbors_PP.f90:98-151) on the device
+int fb_neighbors_pp(fb_ctx *ctx) {
+  if (!ctx) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  if (!ctx->fdh.dev.have_pp)
+    return fail(ctx, FB_ERR_TABLE, "vnl: the Fdata lacks a vnl table or a projector basis of s, sp or spd shells");
+  if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "vnl maps: single structures (a batch of one)");
+  CU(cudaSetDevice(ctx->device));
+  int N = ctx->N;
+  ctx->have_pp_neigh = ctx->have_rho_pp = false;
+  ctx->assembled &= ~(unsigned)(FB_SVNL | FB_VNL2C | FB_VNL3C);
+  ctx->dassembled &= ~(unsigned)(FB_VNL2C | FB_VNL3C);
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  size_t ib = (size_t)N * sizeof(int) + 4, lb = (size_t)N * sizeof(long long) + 8;
+  DevBuf *ibufs[] = {&ctx->d_pp_cnt, &ctx->d_ppx_cnt, &ctx->d_ub, &ctx->d_ppp_cnt, &ctx->d_ppc_cnt, &ctx->d_pp_self,
+                     &ctx->d_ppx_self, &ctx->d_ppp_self};
+  for (DevBuf *b : ibufs) CHK(b->ensure(ib));
+  CHK(ctx->d_svnl_sum.ensure(lb));
+  CHK(ctx->d_vnl_sum.ensure(lb));
+  PPArgs a = pp_args(ctx);
+  // PP and PPx pairs: count, offsets, fill
+  KL(KT_PP_NEIGH, launch_pp_pairs(a, 0, false, ctx->stream));
+  KL(KT_PP_NEIGH, launch_pp_pairs(a, 1, false, ctx->stream));
+  CHK(host_scan<int>(ctx, ctx->d_pp_cnt, N, ctx->h_pp_off, ctx->d_pp_off));
+  CHK(host_scan<int>(ctx, ctx->d_ppx_cnt, N, ctx->h_ppx_off, ctx->d_ppx_off));
+  CHK(host_scan<long long>(ctx, ctx->d_svnl_sum, N, ctx->h_svnl_base, ctx->d_svnl_base));
+  ctx->npp = ctx->h_pp_off[N];
+  ctx->nppx = ctx->h_ppx_off[N];
+  ctx->nsvnl = ctx->h_svnl_base[N];
+  size_t pb = (size_t)ctx->npp * sizeof(int) + 4, xb = (size_t)ctx->nppx * sizeof(int) + 4;
+  CHK(ctx->d_pp_j.ensure(pb));
+  CHK(ctx->d_pp_b.ensure(pb));
+  CHK(ctx->d_pp_map.ensure(pb));
+  CHK(ctx->d_svnl_off.ensure((size_t)ctx->npp * sizeof(long long) + 8));
+  CHK(ctx->d_ppx_j.ensure(xb));
+  CHK(ctx->d_ppx_b.ensure(xb));
+  CHK(ctx->d_ppx_map.ensure(xb));
+  CHK(ctx->d_ppx_point.ensure(xb));
+  CU(cudaMemsetAsync(ctx->d_pp_self.p, 0xff, N * sizeof(int), ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_ppx_self.p, 0xff, N * sizeof(int), ctx->stream));
+  a = pp_args(ctx);
+  KL(KT_PP_NEIGH, launch_pp_pairs(a, 0, true, ctx->stream));
+  KL(KT_PP_NEIGH, launch_pp_pairs(a, 1, true, ctx->stream));
+  // PPp: candidate bounds, first occurrences into slots, compaction + maps
+  KL(KT_PP_NEIGH, launch_ppp_bounds(a, ctx->stream));
+  {
+    std::vector<int> ub(N);
+    CU(cudaMemcpyAsync(ub.data(), ctx->d_ub.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    std::vector<long long> so(N + 1, 0);
+    for (int i = 0; i < N; i++) so[i + 1] = so[i] + ub[i];
+    CHK(ctx->d_pslot_off.ensure((N + 1) * sizeof(long long)));
+    CHK(ctx->d_pslot_j.ensure((size_t)so[N] * sizeof(int) + 4));
+    CHK(ctx->d_pslot_b.ensure((size_t)so[N] * sizeof(int) + 4));
+    CU(cudaMemcpyAsync(ctx->d_pslot_off.p, so.data(), (N + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  }
+  a = pp_args(ctx);
+  KL(KT_PP_NEIGH, launch_ppp(a, ctx->stream));
+  CHK(host_scan<int>(ctx, ctx->d_ppp_cnt, N, ctx->h_ppp_off, ctx->d_ppp_off));
+  CHK(host_scan<long long>(ctx, ctx->d_vnl_sum, N, ctx->h_vnl_base, ctx->d_vnl_base));
+  ctx->nppp = ctx->h_ppp_off[N];
+  ctx->nvnl = ctx->h_vnl_base[N];
+  size_t kb = (size_t)ctx->nppp * sizeof(int) + 4;
+  CHK(ctx->d_ppp_j.ensure(kb));
+  CHK(ctx->d_ppp_b.ensure(kb));
+  CHK(ctx->d_vnl_off.ensure((size_t)ctx->nppp * sizeof(long long) + 8));
+  CU(cudaMemsetAsync(ctx->d_ppp_self.p, 0xff, N * sizeof(int), ctx->stream));
+  a = pp_args(ctx);
+  KL(KT_PP_NEIGH, launch_ppp_compact(a, ctx->npp, ctx->nppx, ctx->stream));
+  ctx->launches++;  // compaction + maps
+  // common PP triplets: count, offsets, fill
+  KL(KT_PP_NEIGH, launch_ppc(a, false, ctx->stream));
+  CHK(host_scan<int>(ctx, ctx->d_ppc_cnt, N, ctx->h_ppc_off, ctx->d_ppc_off));
+  ctx->ntrip_pp = ctx->h_ppc_off[N];
+  size_t tb = (size_t)ctx->ntrip_pp * sizeof(int) + 4;
+  DevBuf *tbufs[] = {&ctx->d_t_alpha, &ctx->d_t_i, &ctx->d_t_ib, &ctx->d_t_j, &ctx->d_t_jb, &ctx->d_t_m,
+                     &ctx->d_t_m31, &ctx->d_t_m32};
+  for (DevBuf *b : tbufs) CHK(b->ensure(tb));
+  a = pp_args(ctx);
+  KL(KT_PP_NEIGH, launch_ppc(a, true, ctx->stream));
+  unsigned st = 0;
+  CHK(sync_status(ctx, &st));
+  if (st) return status_error(ctx, st);
+  ctx->have_pp_neigh = true;
+  return FB_OK;
+}
+
+int fb_get_pp_sizes(fb_ctx *ctx, int *npp, int *nppx, int *nppp, int *ntrip, long long *nsvnl, long long *nvnl) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors_pp first");
+  if (npp) *npp = ctx->npp;
+  if (nppx) *nppx = ctx->nppx;
+  if (nppp) *nppp = ctx->nppp;
+  if (ntrip) *ntrip = ctx->ntrip_pp;
+  if (nsvnl) *nsvnl = ctx->nsvnl;
+  if (nvnl) *nvnl = ctx->nvnl;
+  return FB_OK;
+}
+
+int fb_get_pp_neighbors(fb_ctx *ctx, int which, int *neighn, int *neigh_j, int *neigh_b, int *self, int *map,
+                        int *point) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors_pp first");
+  if (which < FB_PP_MAP || which > FB_PPP_MAP) return fail(ctx, FB_ERR_ARG, "unknown PP map %d", which);
+  const std::vector<int> &off = which == FB_PP_MAP ? ctx->h_pp_off : which == FB_PPX_MAP ? ctx->h_ppx_off
+                                                                                              : ctx->h_ppp_off;
+  DevBuf &J = which == FB_PP_MAP ? ctx->d_pp_j : which == FB_PPX_MAP ? ctx->d_ppx_j : ctx->d_ppp_j;
+  DevBuf &B = which == FB_PP_MAP ? ctx->d_pp_b : which == FB_PPX_MAP ? ctx->d_ppx_b : ctx->d_ppp_b;
+  DevBuf &S = which == FB_PP_MAP ? ctx->d_pp_self : which == FB_PPX_MAP ? ctx->d_ppx_self : ctx->d_ppp_self;
+  int n = off[ctx->N];
+  if (neighn)
+    for (int i = 0; i < ctx->N; i++) neighn[i] = off[i + 1] - off[i];
+  CHK(d2h_int(ctx, neigh_j, J, n, 1));
+  CHK(d2h_int(ctx, neigh_b, B, n, 0));
+  CHK(d2h_int(ctx, self, S, ctx->N, 1));
+  if (which == FB_PP_MAP) CHK(d2h_int(ctx, map, ctx->d_pp_map, n, 1));
+  if (which == FB_PPX_MAP) {
+    CHK(d2h_int(ctx, map, ctx->d_ppx_map, n, 1));
+    CHK(d2h_int(ctx, point, ctx->d_ppx_point, n, 1));
+  }
+  return FB_OK;
+}
+
+int fb_get_pp_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_common_b, int *jatom_common_j,
+                     int *jatom_common_b, int *neigh_common, int *m31, int *m32) {
+  if (!ctx) return FB_ERR_ARG;
+  if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors_pp first");
+  int T = ctx->ntrip_pp;
+  if (ncommon)
+    for (int i = 0; i < ctx->N; i++) ncommon[i] = ctx->h_ppc_off[i + 1] - ctx->h_ppc_off[i];
+  CHK(d2h_int(ctx, iatom_common_j, ctx->d_t_i, T, 1));
+  CHK(d2h_int(ctx, iatom_common_b, ctx->d_t_ib, T, 0));
+  CHK(d2h_int(ctx, jatom_common_j, ctx->d_t_j, T, 1));
+  CHK(d2h_int(ctx, jatom_common_b, ctx->d_t_jb, T, 0));
+  CHK(d2h_int(ctx, neigh_common, ctx->d_t_m, T, 1));
+  CHK(d2h_int(ctx, m31, ctx->d_t_m31, T, 1));
+  CHK(d2h_int(ctx, m32, ctx->d_t_m32, T, 1));
+  return FB_OK;
+}
+
+int fb_set_denmat_pp(fb_ctx *ctx, const double *rho_pp) {
+  if (!ctx || !rho_pp) return FB_ERR_ARG;
+  if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors_pp first");
+  CU(cudaSetDevice(ctx->device));
+  size_t bb = (size_t)ctx->nvnl * sizeof(double);
+  CHK(ctx->d_rho_pp.ensure(bb + 8));
+  CU(cudaMemcpyAsync(ctx->d_rho_pp.p, rho_pp, bb, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_rho_pp = true;
+  return FB_OK;
+}
+
+int fb_set_denmat_pp_device(fb_ctx *ctx, const void *rho_pp_dev) {
+  if (!ctx || !rho_pp_dev) return FB_ERR_ARG;
+  if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors_pp first");
+  CU(cudaSetDevice(ctx->device));
+  size_t bb = (size_t)ctx->nvnl * sizeof(double);
+  CHK(ctx->d_rho_pp.ensure(bb + 8));
+  CU(cudaMemcpyAsync(ctx->d_rho_pp.p, rho_pp_dev, bb, cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->have_rho_pp = true;
+  return FB_OK;
+}
+
 int fb_get_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_common_b, int *jatom_common_j,
                   int *jatom_common_b, int *neigh_common) {
   if (!ctx) return FB_ERR_ARG;
@@ -831,6 +1023,102 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   return a;
 }
 
+extern "C++" {
+// device arguments of the vnl kernels
+static PPArgs pp_args(fb_ctx *ctx) {
+  PPArgs a{};
+  a.N = ctx->N;
+  a.ratom = ctx->d_ratom.as<double>();
+  a.pos4 = ctx->d_pos4.as<float4>();
+  a.sid = ctx->d_sid.as<int>();
+  a.isp = ctx->d_isp.as<int>();
+  a.fd = ctx->d_fd.as<FdataDev>();
+  a.table2c = ctx->d_tab2.as<double>();
+  a.xl = ctx->d_xl.as<double>();
+  a.xlf = ctx->d_xlf.as<float>();
+  a.satom_off = ctx->d_satom_off.as<int>();
+  a.simg_off = ctx->d_simg_off.as<int>();
+  a.imgs = ctx->d_imgs.as<int>();
+  a.sbbox = ctx->d_sbbox.as<float4>();
+  double ra = 0.0, rp = 0.0;
+  int have_d = ctx->fdh.have_d;
+  for (int k = 0; k < ctx->fdh.nspecies; k++) {
+    ra = std::max(ra, ctx->fdh.sp[k].rcA);
+    rp = std::max(rp, ctx->fdh.sp[k].rc_pp);
+    if (ctx->fdh.sp[k].pattern_pp() == PAT_SPD) have_d = 1;
+  }
+  a.reach = (float)(ra + rp);
+  a.have_d = have_d;
+  a.pp_cnt = ctx->d_pp_cnt.as<int>();
+  a.svnl_sum = ctx->d_svnl_sum.as<long long>();
+  a.pp_off = ctx->d_pp_off.as<int>();
+  a.svnl_base = ctx->d_svnl_base.as<long long>();
+  a.pp_j = ctx->d_pp_j.as<int>();
+  a.pp_b = ctx->d_pp_b.as<int>();
+  a.pp_self = ctx->d_pp_self.as<int>();
+  a.pp_map = ctx->d_pp_map.as<int>();
+  a.svnl_off = ctx->d_svnl_off.as<long long>();
+  a.ppx_cnt = ctx->d_ppx_cnt.as<int>();
+  a.ppx_off = ctx->d_ppx_off.as<int>();
+  a.ppx_j = ctx->d_ppx_j.as<int>();
+  a.ppx_b = ctx->d_ppx_b.as<int>();
+  a.ppx_self = ctx->d_ppx_self.as<int>();
+  a.ppx_map = ctx->d_ppx_map.as<int>();
+  a.ppx_point = ctx->d_ppx_point.as<int>();
+  a.ub = ctx->d_ub.as<int>();
+  a.slot_off = ctx->d_pslot_off.as<long long>();
+  a.slot_j = ctx->d_pslot_j.as<int>();
+  a.slot_b = ctx->d_pslot_b.as<int>();
+  a.ppp_cnt = ctx->d_ppp_cnt.as<int>();
+  a.vnl_sum = ctx->d_vnl_sum.as<long long>();
+  a.ppp_off = ctx->d_ppp_off.as<int>();
+  a.vnl_base = ctx->d_vnl_base.as<long long>();
+  a.ppp_j = ctx->d_ppp_j.as<int>();
+  a.ppp_b = ctx->d_ppp_b.as<int>();
+  a.ppp_self = ctx->d_ppp_self.as<int>();
+  a.vnl_off = ctx->d_vnl_off.as<long long>();
+  a.ppc_cnt = ctx->d_ppc_cnt.as<int>();
+  a.ppc_off = ctx->d_ppc_off.as<int>();
+  a.t_alpha = ctx->d_t_alpha.as<int>();
+  a.t_i = ctx->d_t_i.as<int>();
+  a.t_ib = ctx->d_t_ib.as<int>();
+  a.t_j = ctx->d_t_j.as<int>();
+  a.t_jb = ctx->d_t_jb.as<int>();
+  a.t_m = ctx->d_t_m.as<int>();
+  a.t_m31 = ctx->d_t_m31.as<int>();
+  a.t_m32 = ctx->d_t_m32.as<int>();
+  a.svnl = ctx->d_svnl.as<double>();
+  a.dsvnl = ctx->d_dsvnl.as<double>();
+  a.vnl = ctx->d_vnl.as<double>();
+  a.rho_pp = ctx->d_rho_pp.as<double>();
+  a.vnl_atom = ctx->d_vnl_atom.as<double>();
+  a.vnl_ontop = ctx->d_vnl_ontop.as<double>();
+  a.f3nla = ctx->d_f3nla.as<double>();
+  a.f3nlb = ctx->d_f3nlb.as<double>();
+  a.f3nlc = ctx->d_f3nlc.as<double>();
+  a.fvnl = ctx->d_fvnl.as<double>();
+  a.ftot = ctx->d_ftot.as<double>();
+  a.status = ctx->d_status.as<unsigned>();
+  a.errinfo = ctx->d_errinfo.as<int>();
+  return a;
+}
+}  // extern "C++"
+
+extern "C++" {
+// count -> host prefix sum -> offsets on the device (n + 1 entries)
+template <typename T>
+static int host_scan(fb_ctx *ctx, const DevBuf &cnt, int n, std::vector<T> &off, DevBuf &d_off) {
+  std::vector<T> c(n);
+  CU(cudaMemcpyAsync(c.data(), cnt.p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  off.assign(n + 1, 0);
+  for (int i = 0; i < n; i++) off[i + 1] = off[i] + c[i];
+  CHK(d_off.ensure((n + 1) * sizeof(T)));
+  CU(cudaMemcpyAsync(d_off.p, off.data(), (n + 1) * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  return FB_OK;
+}
+}  // extern "C++"
+
 // the double-float kernels carry the Harris terms only; DOGS runs in FP64
 static bool use_df(const fb_ctx *ctx) {
   return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d && ctx->theory == FB_THEORY_HARRIS;
@@ -918,6 +1206,12 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   // three-center terms read
   if (a.dogs && (w2 & FB_VNA2C)) w2 |= FB_S | FB_DIPOLE;
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
+  if (what & (FB_SVNL | FB_VNL2C | FB_VNL3C)) {
+    PPArgs pa = pp_args(ctx);
+    if (what & FB_SVNL) KL(KT_PP, launch_svnl(pa, ctx->npp, false, ctx->stream));
+    if (what & FB_VNL2C) KL(KT_PP, launch_vnl_2c(pa, ctx->stream));
+    if (what & FB_VNL3C) KL(KT_PP, launch_vnl_3c(pa, ctx->ntrip_pp, ctx->stream));
+  }
   if (what & FB_VNA3C) {
     // triplets of approved bins through the network, the rest through the tables
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
@@ -950,13 +1244,22 @@ static int check_assemble(fb_ctx *ctx, unsigned what) {
     return fail(ctx, FB_ERR_TABLE, "FB_DIPOLE: the Fdata has no z-dipole table (dipole_z)");
   if ((what & FB_DIPOLE) || (dogs && (what & FB_VNA2C)))
     CHK(ctx->d_dip.ensure((size_t)ctx->nblock * sizeof(double) + 8));
+  if (what & (FB_SVNL | FB_VNL2C | FB_VNL3C)) {
+    if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
+    if ((what & (FB_VNL2C | FB_VNL3C)) && !(what & FB_SVNL) && !(ctx->assembled & FB_SVNL))
+      return fail(ctx, FB_ERR_STATE, "assemble_vnl reads the svnl blocks: assemble FB_SVNL first");
+    if ((what & FB_VNL3C) && !(what & FB_VNL2C) && !(ctx->assembled & FB_VNL2C))
+      return fail(ctx, FB_ERR_STATE, "assemble_vnl_3c accumulates onto assemble_vnl_2c blocks: assemble FB_VNL2C first");
+    CHK(ctx->d_svnl.ensure((size_t)ctx->nsvnl * sizeof(double) + 8));
+    CHK(ctx->d_vnl.ensure((size_t)ctx->nvnl * sizeof(double) + 8));
+  }
   return FB_OK;
 }
 
 static void assemble_done(fb_ctx *ctx, unsigned what) {
   if (what & FB_VNA2C) ctx->have_vna2c = true;
   if ((what & FB_DIPOLE) || (ctx->theory == FB_THEORY_DOGS && (what & FB_VNA2C))) ctx->have_dip = true;
-  ctx->assembled |= what & (FB_ALL | FB_DIPOLE);
+  ctx->assembled |= what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C);
 }
 
 int fb_assemble(fb_ctx *ctx, unsigned what) {
@@ -985,6 +1288,10 @@ static DevBuf *block_buf(fb_ctx *ctx, int which, size_t *n) {
     case FB_BLOCK_RHO: return ctx->have_rho ? &ctx->d_rho : nullptr;
     case FB_BLOCK_CAPE: return ctx->have_rho ? &ctx->d_cape : nullptr;
     case FB_BLOCK_DIP: return ctx->have_dip ? &ctx->d_dip : nullptr;
+    case FB_BLOCK_SVNL: *n = (size_t)ctx->nsvnl; return (ctx->assembled & FB_SVNL) ? &ctx->d_svnl : nullptr;
+    case FB_BLOCK_VNL: *n = (size_t)ctx->nvnl; return (ctx->assembled & FB_VNL2C) ? &ctx->d_vnl : nullptr;
+    case FB_BLOCK_DSVNL: *n = (size_t)3 * ctx->nsvnl; return (ctx->dassembled & (FB_VNL2C | FB_VNL3C)) ? &ctx->d_dsvnl : nullptr;
+    case FB_BLOCK_RHO_PP: *n = (size_t)ctx->nvnl; return ctx->have_rho_pp ? &ctx->d_rho_pp : nullptr;
   }
   return nullptr;
 }
@@ -1043,7 +1350,18 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
 // a graph is being captured)
 static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
-  if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
+  if ((what & FB_ALL) && !ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
+  if (what & (FB_VNL2C | FB_VNL3C)) {
+    if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
+    if (!ctx->have_rho_pp) return fail(ctx, FB_ERR_STATE, "vnl: fb_set_denmat_pp first");
+    if (!(ctx->assembled & FB_SVNL)) return fail(ctx, FB_ERR_STATE, "Dassemble_vnl reads the svnl blocks: assemble FB_SVNL first");
+    size_t a3 = (size_t)3 * ctx->N * sizeof(double);
+    CHK(ctx->d_dsvnl.ensure((size_t)3 * ctx->nsvnl * sizeof(double) + 8));
+    CHK(ctx->d_vnl_atom.ensure((size_t)3 * ctx->npp * sizeof(double) + 8));
+    CHK(ctx->d_vnl_ontop.ensure((size_t)3 * ctx->nppx * sizeof(double) + 8));
+    DevBuf *bufs[] = {&ctx->d_f3nla, &ctx->d_f3nlb, &ctx->d_f3nlc, &ctx->d_fvnl};
+    for (DevBuf *b : bufs) CHK(b->ensure(a3));
+  }
   bool dogs = ctx->theory == FB_THEORY_DOGS;
   if (dogs && (what & (FB_VNA2C | FB_VNA3C)) && !ctx->have_charges)
     return fail(ctx, FB_ERR_STATE, "DOGS: fb_set_charges first");
@@ -1101,13 +1419,33 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     }
   }
   KL(KT_FORCES, launch_build_forces(a, what & FB_ALL, ctx->stream));
+  if (what & (FB_VNL2C | FB_VNL3C)) {
+    // vnl force pass (M_Dassemble_PP_2c.f90, M_Dassemble_PP_3c.f90) and its
+    // build_forces terms, added into ftot
+    PPArgs pa = pp_args(ctx);
+    size_t a3 = (size_t)3 * N * sizeof(double);
+    CU(cudaMemsetAsync(ctx->d_f3nla.p, 0, a3, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3nlb.p, 0, a3, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3nlc.p, 0, a3, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_fvnl.p, 0, a3, ctx->stream));
+    KL(KT_PP, launch_svnl(pa, ctx->npp, true, ctx->stream));
+    if (what & FB_VNL2C) {
+      KL(KT_PP, launch_dvnl_2c(pa, ctx->npp, ctx->nppx, ctx->stream));
+    } else {
+      CU(cudaMemsetAsync(ctx->d_vnl_atom.p, 0, (size_t)3 * ctx->npp * sizeof(double), ctx->stream));
+      CU(cudaMemsetAsync(ctx->d_vnl_ontop.p, 0, (size_t)3 * ctx->nppx * sizeof(double), ctx->stream));
+    }
+    if (what & FB_VNL3C) KL(KT_PP, launch_dvnl_3c(pa, ctx->ntrip_pp, ctx->stream));
+    KL(KT_PP, launch_pp_forces(pa, ctx->npp, ctx->nppx, ctx->stream));
+    ctx->launches++;  // two kernels
+  }
   return FB_OK;
 }
 
 static void dassemble_done(fb_ctx *ctx, unsigned what) {
   bool keep = (what & FB_KEEP_DBLOCKS) != 0;
   ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
-  ctx->dassembled = what & FB_ALL;
+  ctx->dassembled = what & (FB_ALL | FB_VNL2C | FB_VNL3C);
 }
 
 int fb_dassemble(fb_ctx *ctx, unsigned what) {
@@ -1143,7 +1481,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   int st = FB_OK;
   if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
     st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
-  if (!st && (what & (FB_ALL | FB_DIPOLE))) st = enqueue_assemble(ctx, what);
+  if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C))) st = enqueue_assemble(ctx, what);
   if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -1162,6 +1500,10 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   ctx->g_launches = ctx->launches - l0;
   ctx->launches = l0;
   ctx->g_what = what;
+  ctx->g_npp = ctx->npp;
+  ctx->g_nppx = ctx->nppx;
+  ctx->g_nppp = ctx->nppp;
+  ctx->g_ntrip_pp = ctx->ntrip_pp;
   ctx->g_theory = ctx->theory;
   ctx->g_prec = ctx->prec;
   ctx->g_N = ctx->N;
@@ -1180,13 +1522,16 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
 
 int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
-  if (!(what & (FB_ALL | FB_FORCES | FB_DIPOLE))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
+  const unsigned vals = FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C;
+  if (!(what & (vals | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
   CU(cudaSetDevice(ctx->device));
-  if (what & (FB_ALL | FB_DIPOLE)) CHK(check_assemble(ctx, what));
+  if (what & vals) CHK(check_assemble(ctx, what));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, (what & FB_FORCES) != 0));
   if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what));
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
-  bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_theory == ctx->theory && ctx->g_prec == ctx->prec && ctx->g_N == ctx->N &&
+  bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_theory == ctx->theory && ctx->g_prec == ctx->prec &&
+               ctx->g_npp == ctx->npp && ctx->g_nppx == ctx->nppx && ctx->g_nppp == ctx->nppp &&
+               ctx->g_ntrip_pp == ctx->ntrip_pp && ctx->g_N == ctx->N &&
                ctx->g_P == ctx->P && ctx->g_T == ctx->T && ctx->g_nblock == ctx->nblock &&
                ctx->g_have_d == ctx->fdh.have_d && ctx->g_alloc == g_alloc_gen.load() &&
                ctx->g_mlp_n == ctx->mlp_n && ctx->g_mlp_mode == ctx->mlp_mode &&
@@ -1348,8 +1693,16 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out) {
     case FB_F_F3NAC: b = &ctx->d_f3c; break;
     case FB_F_VNA_ONTOP: b = &ctx->d_ontop; n = (size_t)3 * ctx->P; break;
     case FB_F_VNA_ATOM: b = &ctx->d_atomf; n = (size_t)3 * ctx->P; break;
+    case FB_F_VNL: b = &ctx->d_fvnl; break;
+    case FB_F_F3NLA: b = &ctx->d_f3nla; break;
+    case FB_F_F3NLB: b = &ctx->d_f3nlb; break;
+    case FB_F_F3NLC: b = &ctx->d_f3nlc; break;
+    case FB_F_VNL_ATOM: b = &ctx->d_vnl_atom; n = (size_t)3 * ctx->npp; break;
+    case FB_F_VNL_ONTOP: b = &ctx->d_vnl_ontop; n = (size_t)3 * ctx->nppx; break;
     default: return fail(ctx, FB_ERR_ARG, "unknown force array %d", which);
   }
+  if (which >= FB_F_VNL && !(ctx->dassembled & (FB_VNL2C | FB_VNL3C)))
+    return fail(ctx, FB_ERR_STATE, "vnl forces: fb_dassemble with FB_VNL2C / FB_VNL3C first");
   CU(cudaMemcpyAsync(out, b->p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return FB_OK;

@@ -49,6 +49,19 @@ __device__ __forceinline__ double smoother(double r, double rend, double x) {
   return sm * sm;
 }
 
+// Integer cell shift (ix, iy, iz) of image mbeta in the make_cells order
+// (c.SYSTEM/make_cells.f90:125-144): iz outer, ix inner, the origin skipped.
+__device__ __forceinline__ void mbeta_shift(int mb, int &sx, int &sy, int &sz) {
+  int L = (mb == 0) ? 364 : (mb <= 364 ? mb - 1 : mb);
+  sx = L % 9 - 4;
+  sy = (L / 9) % 9 - 4;
+  sz = L / 81 - 4;
+}
+__device__ __forceinline__ int shift_mbeta(int sx, int sy, int sz) {
+  int L = (sz + 4) * 81 + (sy + 4) * 9 + (sx + 4);
+  return L == 364 ? 0 : (L < 364 ? L + 1 : L);
+}
+
 __device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
                                           double e[3][3]) {
   int j = c.neigh_j[p], mb = c.neigh_b[p];

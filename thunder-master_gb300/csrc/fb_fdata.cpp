@@ -184,6 +184,8 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
       if (!read_ints(t, 1, &sp.nssh_pp) || sp.nssh_pp < 0 || sp.nssh_pp > 8) goto bad_info;
       if (sp.nssh_pp > 0 && !read_ints(t, sp.nssh_pp, lpp)) goto bad_info;
       if (!read_dbls(t, 1, &rcpp)) goto bad_info;
+      sp.rc_pp = rcpp;  // M_species.f90:1147, used as read (M_neighbors_PP.f90:469)
+      for (int k = 0; k < sp.nssh_pp; k++) sp.lpp[k] = lpp[k];
       t.skip();
       t.skip();
       if (!read_dbls(t, 1, &ae)) goto bad_info;
@@ -212,6 +214,8 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
         return FB_ERR_UNSUPPORTED;
       }
       if (sp.pattern == PAT_SPD) out.have_d = 1;
+      sp.norb_pp = 0;
+      for (int k = 0; k < sp.nssh_pp; k++) sp.norb_pp += 2 * sp.lpp[k] + 1;
     }
     goto info_done;
   bad_info:
@@ -222,6 +226,7 @@ info_done:
 
   // ---- read_Fdata_2c --------------------------------------------------------
   bool dogs_ok = true;  // every DOGS sub-cell and z-dipole table found
+  bool pp_ok = true;    // every vnl table found
   for (int is = 0; is < nspecies; is++) {
     for (int js = 0; js < nspecies; js++) {
       std::string pz = zz(out.sp[is].nZ) + "." + zz(out.sp[js].nZ);
@@ -321,6 +326,31 @@ info_done:
         }
         if (r) return r;
       }
+      // non-local pseudopotential table (itype 6): basis of is, projectors of js
+      {
+        int PPB = out.sp[js].pattern_pp();
+        Cell2cDev &d = out.dev.c2vnl[is][js];
+        d.off = -1;
+        int k = index[6][0];
+        if (PPB < 0 || k < 1 || k > ncell) {
+          pp_ok = false;
+        } else {
+          const Cell2 &c = cells[k - 1];
+          if (!map_equal(c, make_munu(PA, PPB))) {
+            err = "2c table " + pz + " vnl has a non-canonical ME map";
+            return FB_ERR_UNSUPPORTED;
+          }
+          d.nx = c.nx;
+          d.nME = c.nME;
+          d.xmax = c.xmax;
+          d.dx = c.xmax / (c.nx - 1);
+          double dx3 = d.dx * d.dx * d.dx;
+          d.inv_dx6 = 1.0 / (dx3 * dx3);
+          d.off = (long long)out.table2c.size();
+          for (int ix = 0; ix < c.nx; ix++)
+            for (int e = 0; e < c.nME; e++) out.table2c.push_back(c.F[ix + (size_t)c.nx * e]);
+        }
+      }
       // DOGS: charged-shell sub-cells of vna ontop L (shells of the first
       // species), ontop R and atom (shells of the second), and dipole_z
       int nsub[3] = {out.sp[is].nssh, out.sp[js].nssh, out.sp[js].nssh};
@@ -353,6 +383,7 @@ info_done:
         err = "short " + path;
         return FB_ERR_IO;
       }
+      out.sp[is].cl_pp[k] = cl;
     }
   }
 
@@ -517,7 +548,17 @@ info_done:
     out.dev.sp[k].rcA = out.sp[k].rcA;
     out.dev.sp[k].nssh = out.sp[k].nssh;
     out.dev.sp[k].rcmin = out.sp[k].rcmin;
+    // cl (b.FUNCTIONS/cl.f90:50-90): the shell's cl for each of its 2l+1 projectors
+    const SpeciesHost &sh = out.sp[k];
+    out.dev.sp[k].pp_pattern = sh.pattern_pp();
+    out.dev.sp[k].norb_pp = sh.norb_pp;
+    out.dev.sp[k].rc_pp = sh.rc_pp;
+    int o = 0;
+    for (int q = 0; q < sh.nssh_pp && o < 9; q++)
+      for (int m = 0; m < 2 * sh.lpp[q] + 1 && o < 9; m++) out.dev.sp[k].cl[o++] = sh.cl_pp[q];
+    if (sh.pattern_pp() < 0) pp_ok = false;
   }
+  out.dev.have_pp = pp_ok ? 1 : 0;
   out.dev.have_dogs = dogs_ok ? 1 : 0;
   return FB_OK;
 }

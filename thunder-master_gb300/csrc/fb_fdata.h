@@ -11,6 +11,17 @@ struct SpeciesHost {
   int lssh[8] = {0};
   double rcA = 0.0;
   double rcmin = 99.0;
+  int lpp[8] = {0};
+  double rc_pp = 0.0;
+  double cl_pp[8] = {0};
+  int norb_pp = 0;
+  // projector shells as a basis pattern: s, sp or spd, else -1
+  int pattern_pp() const {
+    if (nssh_pp == 1 && lpp[0] == 0) return PAT_S;
+    if (nssh_pp == 2 && lpp[0] == 0 && lpp[1] == 1) return PAT_SP;
+    if (nssh_pp == 3 && lpp[0] == 0 && lpp[1] == 1 && lpp[2] == 2) return PAT_SPD;
+    return -1;
+  }
 };
 
 struct FdataHost {

@@ -143,6 +143,11 @@ struct SpeciesDev {
   int nssh;      // shells
   double rcA;    // max shell cutoff, Angstrom
   double rcmin;  // min shell cutoff from 99, Angstrom (the DOGS smoothing range)
+  // pseudopotential projectors: shell pattern (PAT_*, -1 if none of s, sp,
+  // spd), orbitals, cutoff (as info.dat gives it) and cl per projector orbital
+  int pp_pattern, norb_pp;
+  double rc_pp;
+  double cl[9];
 };
 
 // One 2c interaction cell (T_Fdata_cell_2c, e.FDATA/M_Fdata_2c.f90:83-96).
@@ -170,6 +175,7 @@ struct FdataDev {
   int nspecies;
   int have_d;
   int have_dogs;  // the DOGS sub-cells and the z-dipole table are present
+  int have_pp;    // every species pair has its vnl table and a supported projector basis
   SpeciesDev sp[MAXSP];
   Cell2cDev c2[MAXSP][MAXSP][5];       // itype 1..5 -> [itype-1]
   Cell3cDev c3[MAXSP][MAXSP][MAXSP];   // (in1, in2, indna)
@@ -177,6 +183,8 @@ struct FdataDev {
   // vna_atom ([0..2][isorp-1]) and bcna, and the z-dipole table (itype 10)
   Cell2cDev c2s[MAXSP][MAXSP][3][MAXSUB];
   Cell2cDev c2dip[MAXSP][MAXSP];
+  // non-local pseudopotential <basis of in1 | projector of in2> (itype 6)
+  Cell2cDev c2vnl[MAXSP][MAXSP];
   Cell3cDev c3s[MAXSP][MAXSP][MAXSP][MAXSUB];
 };
 

@@ -40,13 +40,18 @@ LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
 FB_DIPOLE = 64
+FB_SVNL, FB_VNL2C, FB_VNL3C = 128, 256, 512
+FB_VNL = FB_SVNL | FB_VNL2C | FB_VNL3C
+FB_PP_MAP, FB_PPX_MAP, FB_PPP_MAP = 0, 1, 2
 FB_THEORY_HARRIS, FB_THEORY_DOGS = 0, 1
 FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
 FB_MLP_ENGINE_MMA, FB_MLP_ENGINE_TC = 0, 1
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
-BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7, "dip": 8}
+BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7, "dip": 8,
+         "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
-         "vna_ontop": 7, "vna_atom": 8}
+         "vna_ontop": 7, "vna_atom": 8,
+         "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14}
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
           6: "ATOMS_CLOSE", 7: "NEIGH_SELF", 8: "NEIGH_BACK", 9: "CUDA", 10: "WATCHDOG",
           11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED"}
@@ -99,6 +104,12 @@ _SIGS = {
     "fb_get_neighbors": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
     "fb_get_common": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
+    "fb_neighbors_pp": (C.c_int, [C.c_void_p]),
+    "fb_get_pp_sizes": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
+    "fb_get_pp_neighbors": (C.c_int, [C.c_void_p, C.c_int] + [C.c_void_p] * 6),
+    "fb_get_pp_common": (C.c_int, [C.c_void_p] + [C.c_void_p] * 8),
+    "fb_set_denmat_pp": (C.c_int, [C.c_void_p, _dp]),
+    "fb_set_denmat_pp_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fb_assemble": (C.c_int, [C.c_void_p, C.c_uint]),
     "fb_get_blocks": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fb_device_blocks": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
@@ -283,6 +294,51 @@ class Context:
         return dict(neighn=neighn, neigh_j=nj[:P], neigh_b=nb[:P], neigh_back=nback[:P], neigh_self=nself,
                     blk_off=blk)
 
+    # ---- non-local pseudopotential (vnl) ----------------------------------
+    def driver_neighbors_PP(self):
+        """driver_neighbors_PP: PP, PPx, PPp maps and the PP common triplets."""
+        self._check(self.L.fb_neighbors_pp(self.h))
+        return self.pp_sizes()
+
+    def pp_sizes(self):
+        n = [C.c_int() for _ in range(4)]
+        b = [C.c_longlong() for _ in range(2)]
+        self._check(self.L.fb_get_pp_sizes(self.h, *[C.byref(x) for x in n], *[C.byref(x) for x in b]))
+        self.npp, self.nppx, self.nppp, self.ntrip_pp = (x.value for x in n)
+        self.nsvnl, self.nvnl = (x.value for x in b)
+        return dict(npp=self.npp, nppx=self.nppx, nppp=self.nppp, ntrip=self.ntrip_pp, nsvnl=self.nsvnl,
+                    nvnl=self.nvnl)
+
+    def pp_neighbors(self, which):
+        """One PP map (FB_PP_MAP, FB_PPX_MAP, FB_PPP_MAP), 1-based."""
+        N = self.natoms
+        cnt = {FB_PP_MAP: self.npp, FB_PPX_MAP: self.nppx, FB_PPP_MAP: self.nppp}[which]
+        neighn, self_ = np.zeros(N, np.int32), np.zeros(N, np.int32)
+        jj, bb, mp, pt = (np.zeros(max(cnt, 1), np.int32) for _ in range(4))
+        self._check(self.L.fb_get_pp_neighbors(self.h, which, _ptr(neighn), _ptr(jj), _ptr(bb), _ptr(self_),
+                                               _ptr(mp) if which != FB_PPP_MAP else None,
+                                               _ptr(pt) if which == FB_PPX_MAP else None))
+        d = dict(neighn=neighn, neigh_j=jj[:cnt], neigh_b=bb[:cnt], self=self_)
+        if which != FB_PPP_MAP:
+            d["map"] = mp[:cnt]
+        if which == FB_PPX_MAP:
+            d["point"] = pt[:cnt]
+        return d
+
+    def pp_common(self):
+        N, T = self.natoms, self.ntrip_pp
+        nc = np.zeros(N, np.int32)
+        arr = [np.zeros(max(T, 1), np.int32) for _ in range(7)]
+        self._check(self.L.fb_get_pp_common(self.h, _ptr(nc), *[_ptr(x) for x in arr]))
+        return dict(ncommon=nc, iatom_j=arr[0][:T], iatom_b=arr[1][:T], jatom_j=arr[2][:T], jatom_b=arr[3][:T],
+                    neigh_common=arr[4][:T], m31=arr[5][:T], m32=arr[6][:T])
+
+    def set_denmat_pp(self, rho_pp):
+        self._check(self.L.fb_set_denmat_pp(self.h, np.ascontiguousarray(rho_pp, np.float64)))
+
+    def set_denmat_pp_device(self, ptr):
+        self._check(self.L.fb_set_denmat_pp_device(self.h, C.c_void_p(ptr)))
+
     def common_neighbors(self):
         N, T = self.natoms, self.ntrip
         nc = np.zeros(N, np.int32)
@@ -444,7 +500,12 @@ class Context:
         return a.value, b.value
 
     def blocks(self, which):
-        n = self.nblock * (3 if which in ("dS", "dT") else 1)
+        if which in ("svnl", "dsvnl"):
+            n = self.nsvnl * (3 if which == "dsvnl" else 1)
+        elif which in ("vnl", "rho_pp"):
+            n = self.nvnl
+        else:
+            n = self.nblock * (3 if which in ("dS", "dT") else 1)
         out = np.zeros(max(n, 1))
         self._check(self.L.fb_get_blocks(self.h, BLOCK[which], out))
         return out[:n]
@@ -469,7 +530,11 @@ class Context:
         self._check(self.L.fb_dassemble(self.h, what | (FB_KEEP_DBLOCKS if keep_dblocks else 0)))
 
     def forces(self, which):
-        n = 3 * (self.npairs if which in ("vna_ontop", "vna_atom") else self.natoms)
+        n = 3 * {"vna_ontop": self.npairs, "vna_atom": self.npairs}.get(which, self.natoms)
+        if which == "vnl_atom":
+            n = 3 * self.npp
+        elif which == "vnl_ontop":
+            n = 3 * self.nppx
         out = np.zeros(max(n, 1))
         self._check(self.L.fb_get_forces(self.h, FORCE[which], out))
         return out[:n]
