@@ -460,6 +460,7 @@ def run_gpu(args):
     if rank == 0:
         line["bloch"] = bloch_measure(ctx, torch, stream, local)
         line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
+        line["vnl"] = vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=args.no_cpu)
     if args.mlp_epochs > 0:
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
@@ -564,6 +565,63 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
         out["max_abs_dftot_ev_per_A"] = float(np.abs(f_gpu - d["ftot"]).max())
         out["cpu_oracle"] = {"value": round(P / t, 1), "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": "1 DOGS step (neighbors + value + force pass), %.3f s" % t}
+    return out
+
+
+def vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=False):
+    """The non-local pseudopotential step on the same structure: the PP maps
+    (driver_neighbors_PP), svnl + vnl 2c/3c and the vnl force pass as one
+    graph launch, with a seeded density over the PPp pairs; its agreement
+    with the oracle and the oracle's time for the same step on one core."""
+    ctx = fbgpu.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    sz = ctx.driver_neighbors_PP()
+    rho_pp = np.random.default_rng(11).normal(0.0, 0.1, sz["nvnl"])
+    d_rho = torch.from_numpy(rho_pp).to(f"cuda:{local}")
+    ctx.set_denmat_pp_device(d_rho.data_ptr())
+    what = fbgpu.FB_VNL | fbgpu.FB_FORCES
+
+    def step():
+        ctx.driver_neighbors_PP()
+        ctx.set_denmat_pp_device(d_rho.data_ptr())
+        ctx.assemble_graph(what)
+
+    timed = make_timer(torch, ctx, stream, flush, 1, local)
+    for _ in range(max(3, args.warmup)):
+        step()
+    ms, launches = timed(step, args.steps)
+    ms_k, _ = timed(lambda: (ctx.driver_neighbors_PP(), ctx.set_denmat_pp_device(d_rho.data_ptr()),
+                             ctx.assemble(fbgpu.FB_VNL), ctx.Dassemble(fbgpu.FB_VNL2C | fbgpu.FB_VNL3C)),
+                    args.steps, timing=True)
+    kt = ctx.timing()
+    ctx.set_timing(False)
+    out = {"what": "vnl: PP/PPx/PPp maps + common triplets, svnl, vnl 2c + 3c, vnl forces (FP64)",
+           "sizes": sz, "ms_per_step": round(ms / args.steps, 4),
+           "value": round(sz["nppp"] * args.steps / (ms * 1e-3), 1), "unit": "vnl blocks (PPp pairs)/s",
+           "gpu_launches_per_step": launches // max(1, args.steps),
+           "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+    vnl = ctx.blocks("vnl")
+    ctx.set_denmat_pp(rho_pp)
+    ctx.Dassemble(fbgpu.FB_VNL2C | fbgpu.FB_VNL3C)
+    f_gpu = ctx.forces("ftot")
+    ctx.close()
+    if no_cpu or st.natoms > 1024:
+        out["cpu_oracle"] = "not run (single-core oracle bounded to systems of at most 1024 atoms)"
+    else:
+        from oracle import oracle as orc
+        fd = orc.Fdata(path, nZ)
+        t0 = time.perf_counter()
+        s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors().neighbors_pp()
+        _, vref = s.assemble_pp()
+        d = s.dassemble_pp(rho_pp)
+        t = time.perf_counter() - t0
+        out["max_abs_dvnl_ev"] = float(np.abs(vnl - vref).max())
+        out["max_abs_dftot_ev_per_A"] = float(np.abs(f_gpu - d["ftot_vnl"]).max())
+        out["cpu_oracle"] = {"value": round(s.nppp / t, 1), "unit": "vnl blocks (PPp pairs)/s", "cores": 1,
+                             "kind": "port", "sample": "1 vnl step (maps + value + force pass), %.3f s" % t}
     return out
 
 
