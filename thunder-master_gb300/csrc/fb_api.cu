@@ -1354,7 +1354,9 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if (what & (FB_VNL2C | FB_VNL3C)) {
     if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
     if (!ctx->have_rho_pp) return fail(ctx, FB_ERR_STATE, "vnl: fb_set_denmat_pp first");
-    if (!(ctx->assembled & FB_SVNL)) return fail(ctx, FB_ERR_STATE, "Dassemble_vnl reads the svnl blocks: assemble FB_SVNL first");
+    // the svnl blocks: assembled before, or by the same graph's value pass
+    if (!(what & FB_SVNL) && !(ctx->assembled & FB_SVNL))
+      return fail(ctx, FB_ERR_STATE, "Dassemble_vnl reads the svnl blocks: assemble FB_SVNL first");
     size_t a3 = (size_t)3 * ctx->N * sizeof(double);
     CHK(ctx->d_dsvnl.ensure((size_t)3 * ctx->nsvnl * sizeof(double) + 8));
     CHK(ctx->d_vnl_atom.ensure((size_t)3 * ctx->npp * sizeof(double) + 8));
@@ -1451,7 +1453,7 @@ static void dassemble_done(fb_ctx *ctx, unsigned what) {
 int fb_dassemble(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
   CU(cudaSetDevice(ctx->device));
-  CHK(prepare_dassemble(ctx, what));
+  CHK(prepare_dassemble(ctx, what & ~FB_SVNL));
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
   CHK(enqueue_dassemble(ctx, what));
   unsigned st = 0;
