@@ -435,7 +435,8 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * kernel: "neigh_count", "neigh_fill", "neigh_back", "common_count",
  * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
  * "dassemble_3c", "build_forces", "trip_bins", "split_rho", "mlp_eval",
- * "assemble_3c_mlp", "dassemble_3c_mlp", "bloch".  No reference counterpart (the reference
+ * "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common",
+ * "svnl", "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,

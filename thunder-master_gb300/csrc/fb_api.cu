@@ -27,11 +27,13 @@ std::atomic<long long> g_alloc_gen{0};
 // kernels timed by fb_set_timing / fb_get_timing
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
        KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
-       KT_BLOCH, KT_PP_NEIGH, KT_PP, KT_N };
+       KT_BLOCH, KT_PP_PAIRS, KT_PPP, KT_PPC, KT_SVNL, KT_VNL2C, KT_VNL3C, KT_DSVNL, KT_DVNL2C, KT_DVNL3C,
+       KT_VNLF, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
-                                     "dassemble_3c_mlp", "bloch", "pp_neighbors", "vnl"};
+                                     "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
+                                     "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -788,8 +790,8 @@ int fb_neighbors_pp(fb_ctx *ctx) {
   CHK(ctx->d_vnl_sum.ensure(lb));
   PPArgs a = pp_args(ctx);
   // PP and PPx pairs: count, offsets, fill
-  KL(KT_PP_NEIGH, launch_pp_pairs(a, 0, false, ctx->stream));
-  KL(KT_PP_NEIGH, launch_pp_pairs(a, 1, false, ctx->stream));
+  KL(KT_PP_PAIRS, launch_pp_pairs(a, 0, false, ctx->stream));
+  KL(KT_PP_PAIRS, launch_pp_pairs(a, 1, false, ctx->stream));
   CHK(host_scan<int>(ctx, ctx->d_pp_cnt, N, ctx->h_pp_off, ctx->d_pp_off));
   CHK(host_scan<int>(ctx, ctx->d_ppx_cnt, N, ctx->h_ppx_off, ctx->d_ppx_off));
   CHK(host_scan<long long>(ctx, ctx->d_svnl_sum, N, ctx->h_svnl_base, ctx->d_svnl_base));
@@ -808,10 +810,10 @@ int fb_neighbors_pp(fb_ctx *ctx) {
   CU(cudaMemsetAsync(ctx->d_pp_self.p, 0xff, N * sizeof(int), ctx->stream));
   CU(cudaMemsetAsync(ctx->d_ppx_self.p, 0xff, N * sizeof(int), ctx->stream));
   a = pp_args(ctx);
-  KL(KT_PP_NEIGH, launch_pp_pairs(a, 0, true, ctx->stream));
-  KL(KT_PP_NEIGH, launch_pp_pairs(a, 1, true, ctx->stream));
+  KL(KT_PP_PAIRS, launch_pp_pairs(a, 0, true, ctx->stream));
+  KL(KT_PP_PAIRS, launch_pp_pairs(a, 1, true, ctx->stream));
   // PPp: candidate bounds, first occurrences into slots, compaction + maps
-  KL(KT_PP_NEIGH, launch_ppp_bounds(a, ctx->stream));
+  KL(KT_PPP, launch_ppp_bounds(a, ctx->stream));
   {
     std::vector<int> ub(N);
     CU(cudaMemcpyAsync(ub.data(), ctx->d_ub.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -825,7 +827,7 @@ int fb_neighbors_pp(fb_ctx *ctx) {
                        ctx->stream));
   }
   a = pp_args(ctx);
-  KL(KT_PP_NEIGH, launch_ppp(a, ctx->stream));
+  KL(KT_PPP, launch_ppp(a, ctx->stream));
   CHK(host_scan<int>(ctx, ctx->d_ppp_cnt, N, ctx->h_ppp_off, ctx->d_ppp_off));
   CHK(host_scan<long long>(ctx, ctx->d_vnl_sum, N, ctx->h_vnl_base, ctx->d_vnl_base));
   ctx->nppp = ctx->h_ppp_off[N];
@@ -836,10 +838,10 @@ int fb_neighbors_pp(fb_ctx *ctx) {
   CHK(ctx->d_vnl_off.ensure((size_t)ctx->nppp * sizeof(long long) + 8));
   CU(cudaMemsetAsync(ctx->d_ppp_self.p, 0xff, N * sizeof(int), ctx->stream));
   a = pp_args(ctx);
-  KL(KT_PP_NEIGH, launch_ppp_compact(a, ctx->npp, ctx->nppx, ctx->stream));
+  KL(KT_PPP, launch_ppp_compact(a, ctx->npp, ctx->nppx, ctx->stream));
   ctx->launches++;  // compaction + maps
   // common PP triplets: count, offsets, fill
-  KL(KT_PP_NEIGH, launch_ppc(a, false, ctx->stream));
+  KL(KT_PPC, launch_ppc(a, false, ctx->stream));
   CHK(host_scan<int>(ctx, ctx->d_ppc_cnt, N, ctx->h_ppc_off, ctx->d_ppc_off));
   ctx->ntrip_pp = ctx->h_ppc_off[N];
   size_t tb = (size_t)ctx->ntrip_pp * sizeof(int) + 4;
@@ -847,7 +849,7 @@ int fb_neighbors_pp(fb_ctx *ctx) {
                      &ctx->d_t_m31, &ctx->d_t_m32};
   for (DevBuf *b : tbufs) CHK(b->ensure(tb));
   a = pp_args(ctx);
-  KL(KT_PP_NEIGH, launch_ppc(a, true, ctx->stream));
+  KL(KT_PPC, launch_ppc(a, true, ctx->stream));
   unsigned st = 0;
   CHK(sync_status(ctx, &st));
   if (st) return status_error(ctx, st);
@@ -1208,9 +1210,9 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   if (w2) KL(KT_ASM2C, launch_assemble_2c(a, w2, ctx->stream));
   if (what & (FB_SVNL | FB_VNL2C | FB_VNL3C)) {
     PPArgs pa = pp_args(ctx);
-    if (what & FB_SVNL) KL(KT_PP, launch_svnl(pa, ctx->npp, false, ctx->stream));
-    if (what & FB_VNL2C) KL(KT_PP, launch_vnl_2c(pa, ctx->stream));
-    if (what & FB_VNL3C) KL(KT_PP, launch_vnl_3c(pa, ctx->ntrip_pp, ctx->stream));
+    if (what & FB_SVNL) KL(KT_SVNL, launch_svnl(pa, ctx->npp, false, ctx->stream));
+    if (what & FB_VNL2C) KL(KT_VNL2C, launch_vnl_2c(pa, ctx->stream));
+    if (what & FB_VNL3C) KL(KT_VNL3C, launch_vnl_3c(pa, ctx->ntrip_pp, ctx->stream));
   }
   if (what & FB_VNA3C) {
     // triplets of approved bins through the network, the rest through the tables
@@ -1430,15 +1432,15 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     CU(cudaMemsetAsync(ctx->d_f3nlb.p, 0, a3, ctx->stream));
     CU(cudaMemsetAsync(ctx->d_f3nlc.p, 0, a3, ctx->stream));
     CU(cudaMemsetAsync(ctx->d_fvnl.p, 0, a3, ctx->stream));
-    KL(KT_PP, launch_svnl(pa, ctx->npp, true, ctx->stream));
+    KL(KT_DSVNL, launch_svnl(pa, ctx->npp, true, ctx->stream));
     if (what & FB_VNL2C) {
-      KL(KT_PP, launch_dvnl_2c(pa, ctx->npp, ctx->nppx, ctx->stream));
+      KL(KT_DVNL2C, launch_dvnl_2c(pa, ctx->npp, ctx->nppx, ctx->stream));
     } else {
       CU(cudaMemsetAsync(ctx->d_vnl_atom.p, 0, (size_t)3 * ctx->npp * sizeof(double), ctx->stream));
       CU(cudaMemsetAsync(ctx->d_vnl_ontop.p, 0, (size_t)3 * ctx->nppx * sizeof(double), ctx->stream));
     }
-    if (what & FB_VNL3C) KL(KT_PP, launch_dvnl_3c(pa, ctx->ntrip_pp, ctx->stream));
-    KL(KT_PP, launch_pp_forces(pa, ctx->npp, ctx->nppx, ctx->stream));
+    if (what & FB_VNL3C) KL(KT_DVNL3C, launch_dvnl_3c(pa, ctx->ntrip_pp, ctx->stream));
+    KL(KT_VNLF, launch_pp_forces(pa, ctx->npp, ctx->nppx, ctx->stream));
     ctx->launches++;  // two kernels
   }
   return FB_OK;

@@ -23,6 +23,9 @@ Context.set_theory     DOGS instead of Harris vna 2c / 3c             j.ASSEMBLE
                                                                       j.ASSEMBLERS/M_assemble_3c_DOGS.f90:158
 Context.assemble_dipole_z  assemble_dipole_z                          j.ASSEMBLERS/M_assemble_2c_DOGS.f90:376
 Context.bloch          Bloch sums into H(k), S(k)                     h.SOLVESH/M_kspace_Lowdin.f90:680
+Context.driver_neighbors_PP  driver_neighbors_PP                      c.SYSTEM/M_neighbors_PP.f90:98
+Context.assemble(FB_VNL)  assemble_svnl / vnl_2c / vnl_3c             j.ASSEMBLERS/M_assemble_PP_{2c,3c}.f90
+Context.Dassemble(FB_VNL2C | FB_VNL3C)  Dassemble_svnl / vnl_2c / vnl_3c  k.DASSEMBLERS/M_Dassemble_PP_{2c,3c}.f90
 =====================  =============================================  ====================================
 
 There is no CPU fallback: every call runs on the GPU through the native
@@ -133,7 +136,8 @@ FB_PREC_FP64, FB_PREC_DF = 0, 1
 
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
            "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
-           "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch")
+           "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
+           "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces")
 
 
 class FBError(RuntimeError):
