@@ -266,10 +266,33 @@ __global__ void k_pp_maps(PPArgs a) {
   }
 }
 
+// the image of the cell shift (sx, sy, sz), or -1 outside the 9 x 9 x 9 box
+__device__ __forceinline__ int image_of_shift(int sx, int sy, int sz) {
+  if (sx < -4 || sx > 4 || sy < -4 || sy > 4 || sz < -4 || sz > 4) return -1;
+  return shift_mbeta(sx, sy, sz);
+}
+
 // mpairnay (M_assemble_PP_3c.f90:266-365): the PP neighbor of atom `at` that
-// is atom al at the vector r12 = r_al - r_at(image); exactly one must match
+// is atom al at the vector r12 = r_al - r_at(image); exactly one must match.
+// The entry that can match is (al, mb_hint), mb_hint the image of the
+// negated shift of at's image: it is found by an integer search and then
+// tested exactly; only when that fails does the reference's full count run.
 __device__ __forceinline__ int mpairnay(const PPArgs &a, const double *X, int at, int al, const double *r12,
-                                        int &imatch) {
+                                        int mb_hint, int &imatch) {
+  if (mb_hint >= 0) {
+    for (int k = a.pp_off[at]; k < a.pp_off[at + 1]; k++) {
+      if (a.pp_j[k] != al || a.pp_b[k] != mb_hint) continue;
+      double r21[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        r21[c] = __dsub_rn(__dadd_rn(a.ratom[3 * al + c], X[3 * mb_hint + c]), a.ratom[3 * at + c]);
+      if (dist_rn(r12, r21) < 0.0001) {
+        imatch = 1;
+        return k - a.pp_off[at];
+      }
+      break;
+    }
+  }
   int m = -1;
   imatch = 0;
   for (int k = a.pp_off[at]; k < a.pp_off[at + 1]; k++) {
@@ -310,7 +333,9 @@ __global__ void k_ppc(PPArgs a) {
       r1[c] = __dadd_rn(a.ratom[3 * i + c], X[3 * ib + c]);
       r31[c] = __dsub_rn(rna[c], r1[c]);
     }
-    int im31 = 0, m31 = FILL ? mpairnay(a, X, i, al, r31, im31) : 0;
+    int ibx, iby, ibz;
+    mbeta_shift(ib, ibx, iby, ibz);
+    int im31 = 0, m31 = FILL ? mpairnay(a, X, i, al, r31, image_of_shift(-ibx, -iby, -ibz), im31) : 0;
     for (int qb0 = q0; qb0 < q1; qb0 += 32) {
       int qb = qb0 + lane;
       bool keep = false;
@@ -325,23 +350,41 @@ __global__ void k_ppc(PPArgs a) {
             r2[c] = __dadd_rn(a.ratom[3 * j + c], X[3 * jb + c]);
             r[c] = __dsub_rn(r2[c], r1[c]);
           }
-          for (int k = a.ppp_off[i]; k < a.ppp_off[i + 1]; k++) {
-            int ka = a.ppp_j[k], kb = a.ppp_b[k];
-            double r3[3];
+          // the entry that can match: (j, image of shift(jb) - shift(ib)),
+          // found by an integer search and tested exactly; otherwise the
+          // reference's scan (first k within 1e-4) decides
+          int jbx, jby, jbz;
+          mbeta_shift(jb, jbx, jby, jbz);
+          int kb0 = image_of_shift(jbx - ibx, jby - iby, jbz - ibz);
+          if (kb0 >= 0)
+            for (int k = a.ppp_off[i]; k < a.ppp_off[i + 1]; k++) {
+              if (a.ppp_j[k] != j || a.ppp_b[k] != kb0) continue;
+              double r3[3];
 #pragma unroll
-            for (int c = 0; c < 3; c++) r3[c] = __dsub_rn(__dadd_rn(X[3 * kb + c], a.ratom[3 * ka + c]), a.ratom[3 * i + c]);
-            if (dist_rn(r, r3) < 1.0e-4) {
-              m = k - a.ppp_off[i];
+              for (int c = 0; c < 3; c++)
+                r3[c] = __dsub_rn(__dadd_rn(X[3 * kb0 + c], a.ratom[3 * j + c]), a.ratom[3 * i + c]);
+              if (dist_rn(r, r3) < 1.0e-4) m = k - a.ppp_off[i];
               break;
             }
-          }
+          if (m < 0)
+            for (int k = a.ppp_off[i]; k < a.ppp_off[i + 1]; k++) {
+              int ka = a.ppp_j[k], kb = a.ppp_b[k];
+              double r3[3];
+#pragma unroll
+              for (int c = 0; c < 3; c++)
+                r3[c] = __dsub_rn(__dadd_rn(X[3 * kb + c], a.ratom[3 * ka + c]), a.ratom[3 * i + c]);
+              if (dist_rn(r, r3) < 1.0e-4) {
+                m = k - a.ppp_off[i];
+                break;
+              }
+            }
           keep = m >= 0;
           if (FILL && keep) {
             double r32[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) r32[c] = __dsub_rn(rna[c], r2[c]);
             int im32 = 0;
-            m32 = mpairnay(a, X, j, al, r32, im32);
+            m32 = mpairnay(a, X, j, al, r32, image_of_shift(-jbx, -jby, -jbz), im32);
             if (im32 != 1 || im31 != 1) {
               atomicOr(a.status, DEVERR_BACK);
               a.errinfo[0] = al;
