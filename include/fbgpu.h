@@ -79,6 +79,8 @@ extern "C" {
 #define FB_SVNL 128u         /* svnl blocks <basis i | projectors j> (assemble_svnl, M_assemble_PP_2c.f90:86) */
 #define FB_VNL2C 256u        /* vnl 2c: atom, ontop left / right (assemble_vnl_2c, M_assemble_PP_2c.f90:232) */
 #define FB_VNL3C 512u        /* vnl 3c (assemble_vnl_3c, M_assemble_PP_3c.f90:94); fb_dassemble: the vnl forces */
+#define FB_EWALD 1024u       /* DOGS Ewald: the matrix (assemble_ewald) and the ewaldsr / ewaldlr blocks
+                                (M_assemble_ewald_DOGS.f90:98, :404, :633) */
 #define FB_DIPOLE 64u        /* z-dipole blocks (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499);
                                 with FB_THEORY_DOGS, FB_VNA2C computes them and FB_S as well */
 
@@ -96,6 +98,8 @@ extern "C" {
 #define FB_BLOCK_VNL 10    /* s%vnl(i)%neighbors(k)%block over PPp pairs, norb_i x norb_j */
 #define FB_BLOCK_DSVNL 11  /* s%svnl(i)%neighbors(k)%Dblock (after the vnl force pass) */
 #define FB_BLOCK_RHO_PP 12 /* s%denmat_PP(i)%neighbors(k)%block (input, PPp pairs) */
+#define FB_BLOCK_EWALDSR 13 /* s%ewaldsr(i)%neighbors(k)%block (FB_EWALD) */
+#define FB_BLOCK_EWALDLR 14 /* s%ewaldlr(i)%neighbors(k)%block (FB_EWALD) */
 
 /* force arrays for fb_get_forces */
 #define FB_F_TOT 0         /* ftot: kinetic + vna + f3na(a+b+c) - pulay */
@@ -414,6 +418,17 @@ int fb_set_theory(fb_ctx *ctx, int theory);
  * M_assemble_3c_DOGS.f90:313). */
 int fb_set_charges(fb_ctx *ctx, const double *dq, int nssh_max);
 
+/* The DOGS Ewald terms (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90), assembled
+ * with FB_EWALD in DOGS after (or with) FB_VNA2C: the long-range Coulomb
+ * matrix s%ewald(i, j) of assemble_ewald (:633-918; reciprocal sum over the
+ * reference's g box, erfc-screened lattice sum, -2 kappa/sqrt(pi) on the
+ * diagonal; a cluster keeps only the bare 1/z of its own cell), the
+ * short-range correction s%ewaldsr (:98-378: atom, ontop and three-center
+ * terms from the overlap and z-dipole blocks and the atoms' total charges)
+ * and the long-range blocks s%ewaldlr (:404-592, with sum_ewald = ewald dQ).
+ * Single structures.  fb_get_ewald copies the N x N matrix (row-major). */
+int fb_get_ewald(fb_ctx *ctx, double *ewald);
+
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the
  * table contractions, rotations, frame derivatives and density contractions
  * run in double-float arithmetic on the FP32 pipe (two floats per value,
@@ -436,7 +451,8 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * "common_fill", "assemble_2c", "assemble_3c", "dassemble_2c",
  * "dassemble_3c", "build_forces", "trip_bins", "split_rho", "mlp_eval",
  * "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common",
- * "svnl", "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces".  No reference counterpart (the reference
+ * "svnl", "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald",
+ * "ewald_blocks".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,

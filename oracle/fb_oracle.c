@@ -2674,3 +2674,182 @@ int or_build_forces_vnl(or_sys *s, const double *vnl_atom, const double *vnl_ont
   for (int k = 0; k < 3 * N; k++) ftot_add[k] = vnl[k] + f3nla[k] + f3nlb[k] + f3nlc[k];
   return OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Ewald (DOGS): the long-range Coulomb matrix and the ewaldsr / ewaldlr     */
+/* blocks (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90)                           */
+/* ------------------------------------------------------------------------ */
+/* total charge of each atom, dQ(i) = sum over its shells of Qin - Qneutral */
+static void atom_dq(const or_sys *s, double *dq) {
+  for (int i = 0; i < s->natoms; i++) {
+    dq[i] = 0.0;
+    for (int k = 1; k <= s->fd->sp[s->imass[i]].nssh; k++) dq[i] = dq[i] + shell_dq(s, i, k);
+  }
+}
+
+/* assemble_ewald (:633-918): ewald(i, j) (row-major N x N here) */
+int or_assemble_ewald(or_sys *s, double *ewald) {
+  int N = s->natoms;
+  const double pi = 3.141592653589793238462643;
+  double a1[3], a2[3], a3[3], c[3], g1[3], g2[3], g3[3];
+  for (int k = 0; k < 3; k++) a1[k] = s->lattice[0][k], a2[k] = s->lattice[1][k], a3[k] = s->lattice[2][k];
+  for (long long k = 0; k < (long long)N * N; k++) ewald[k] = 0.0;
+  cross3(a2, a3, c);
+  double volume = a1[0] * c[0] + a1[1] * c[1] + a1[2] * c[2];
+  for (int k = 0; k < 3; k++) g1[k] = 2.0 * pi * c[k] / volume;
+  cross3(a3, a1, c);
+  for (int k = 0; k < 3; k++) g2[k] = 2.0 * pi * c[k] / volume;
+  cross3(a1, a2, c);
+  for (int k = 0; k < 3; k++) g3[k] = 2.0 * pi * c[k] / volume;
+  volume = fabs(volume);
+  double gmax = 5.0, rmax = 5.0;
+  double g1m2 = pow(magnitude3(g1), 2), g2m2 = pow(magnitude3(g2), 2), g3m2 = pow(magnitude3(g3), 2);
+  double r1m2 = pow(magnitude3(a1), 2), r2m2 = pow(magnitude3(a2), 2), r3m2 = pow(magnitude3(a3), 2);
+  double rmin2 = r1m2;
+  if (r2m2 < rmin2) rmin2 = r2m2;
+  if (r3m2 < rmin2) rmin2 = r3m2;
+  double gmin2 = g1m2;
+  if (g2m2 < gmin2) gmin2 = g2m2;
+  if (g3m2 < gmin2) gmin2 = g3m2;
+  double kappa = sqrt(sqrt(gmin2 / (4.0 * rmin2)));
+  int ig1 = (int)(gmax * sqrt(4.0 * kappa * kappa / g1m2) + 1.0);
+  int ig2 = (int)(gmax * sqrt(4.0 * kappa * kappa / g2m2) + 1.0);
+  int ig3 = (int)(gmax * sqrt(4.0 * kappa * kappa / g3m2) + 1.0);
+  if (ig1 <= 1) ig1 = 2;
+  if (ig2 <= 1) ig2 = 2;
+  if (ig3 <= 1) ig3 = 2;
+  int il1 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r1m2)) + 1.0);
+  int il2 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r2m2)) + 1.0);
+  int il3 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r3m2)) + 1.0);
+  if (il1 <= 1) il1 = 2;
+  if (il2 <= 1) il2 = 2;
+  if (il3 <= 1) il3 = 2;
+  if (s->icluster == 1) ig1 = ig2 = ig3 = 0;
+  for (int n1 = -ig1; n1 <= ig1; n1++)
+    for (int n2 = -ig2; n2 <= ig2; n2++)
+      for (int n3 = -ig3; n3 <= ig3; n3++) {
+        if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+        double g[3];
+        for (int k = 0; k < 3; k++) g[k] = n1 * g1[k] + n2 * g2[k] + n3 * g3[k];
+        double gm2 = pow(magnitude3(g), 2);
+        double argument = gm2 / (4.0 * kappa * kappa);
+        double stuff = 4.0 * pi * exp(-argument) / (gm2 * volume);
+        for (int i = 0; i < N; i++)
+          for (int j = i; j < N; j++) {
+            double factor = j == i ? 0.5 * stuff : 1.0 * stuff;
+            double gdotb = g[0] * (RAT(s, i)[0] - RAT(s, j)[0]) + g[1] * (RAT(s, i)[1] - RAT(s, j)[1]) +
+                           g[2] * (RAT(s, i)[2] - RAT(s, j)[2]);
+            ewald[(size_t)i * N + j] = ewald[(size_t)i * N + j] + factor * cos(gdotb);
+            ewald[(size_t)j * N + i] = ewald[(size_t)j * N + i] + factor * cos(gdotb);
+          }
+      }
+  if (s->icluster == 1) {
+    il1 = il2 = il3 = 0;
+    kappa = 0.0;
+  }
+  for (int n1 = -il1; n1 <= il1; n1++)
+    for (int n2 = -il2; n2 <= il2; n2++)
+      for (int n3 = -il3; n3 <= il3; n3++)
+        for (int i = 0; i < N; i++)
+          for (int j = i; j < N; j++) {
+            double factor = j == i ? 0.5 : 1.0;
+            double cv[3];
+            for (int k = 0; k < 3; k++) cv[k] = n1 * a1[k] + n2 * a2[k] + n3 * a3[k];
+            for (int k = 0; k < 3; k++) cv[k] = cv[k] + RAT(s, i)[k] - RAT(s, j)[k];
+            double z = sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
+            if (z > 0.0001) {
+              double argument = kappa * z;
+              ewald[(size_t)i * N + j] = ewald[(size_t)i * N + j] + factor * erfc(argument) / z;
+              ewald[(size_t)j * N + i] = ewald[(size_t)j * N + i] + factor * erfc(argument) / z;
+            }
+          }
+  for (int i = 0; i < N; i++) ewald[(size_t)i * N + i] = ewald[(size_t)i * N + i] - 2.0 * kappa / sqrt(pi);
+  return OK;
+}
+
+/* assemble_ewaldsr (:98-378): per pair of the neighbor map (S and dip are
+ * the overlap and z-dipole block sets), the atom term into the self block
+ * (dQ_j S(i,self)/z), the ontop terms (dQ_i (S/2z + dip/z^2) + dQ_j (S/2z -
+ * dip/z^2)) and the three-center terms over the common neighbors
+ * ((sterm - dterm)/d13 + (sterm + dterm)/d23 with sterm = dQ_alpha S/2,
+ * dterm = dQ_alpha dip/z), all times eq2 */
+int or_assemble_ewaldsr(or_sys *s, const double *S, const double *dip, double *sr) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double *dq = (double *)malloc(sizeof(double) * N);
+  atom_dq(s, dq);
+  for (long long k = 0; k < s->nblock; k++) sr[k] = 0.0;
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p];
+      if (i == j && s->neigh_b[p] == 0) continue;
+      double r2[3];
+      for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[s->neigh_b[p]][k];
+      double z = distance3(RAT(s, i), r2);
+      for (int k = 0; k < nmu * nmu; k++) sr[os + k] = sr[os + k] + dq[j] * (S[os + k] / z) * P_eq2;
+    }
+  }
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      long long o = s->blk_off[p];
+      double r2[3];
+      for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[s->neigh_b[p]][k];
+      double z = distance3(RAT(s, i), r2);
+      for (int k = 0; k < nmu * nnu; k++) {
+        double sterm = S[o + k] / (2.0 * z), dterm = dip[o + k] / (z * z);
+        sr[o + k] = sr[o + k] + dq[i] * (sterm + dterm) * P_eq2;
+        sr[o + k] = sr[o + k] + dq[j] * (sterm - dterm) * P_eq2;
+      }
+    }
+  }
+  for (int ia = 0; ia < N; ia++) {
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+      double d13 = distance3(g.rna, g.r1), d23 = distance3(g.rna, g.r2);
+      for (int k = 0; k < nmu * nnu; k++) {
+        double sterm = dq[ia] * S[o + k] / 2.0, dterm = dq[ia] * dip[o + k] / g.z;
+        sr[o + k] = sr[o + k] + ((sterm - dterm) / d13 + (sterm + dterm) / d23) * P_eq2;
+      }
+    }
+  }
+  free(dq);
+  return OK;
+}
+
+/* assemble_ewaldlr (:404-592): sum_ewald(i) = sum_j dQ_j ewald(i, j); per
+ * pair (S/2 - dip/z) sum_ewald(i) eq2 + (S/2 + dip/z) sum_ewald(j) eq2, the
+ * dipole term left out on the self pair */
+int or_assemble_ewaldlr(or_sys *s, const double *ewald, const double *S, const double *dip, double *lr) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double *dq = (double *)malloc(sizeof(double) * N), *se = (double *)calloc(N, sizeof(double));
+  atom_dq(s, dq);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) se[i] = se[i] + dq[j] * ewald[(size_t)i * N + j];
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      long long o = s->blk_off[p];
+      double r2[3];
+      for (int k = 0; k < 3; k++) r2[k] = RAT(s, j)[k] + s->xl[s->neigh_b[p]][k];
+      double z = distance3(RAT(s, i), r2);
+      int self = i == j && s->neigh_b[p] == 0;
+      for (int k = 0; k < nmu * nnu; k++) {
+        double sterm = S[o + k] / 2.0, dterm = self ? 0.0 : dip[o + k] / z;
+        lr[o + k] = 0.0 + (sterm - dterm) * se[i] * P_eq2 + (sterm + dterm) * se[j] * P_eq2;
+      }
+    }
+  }
+  free(dq);
+  free(se);
+  return OK;
+}

@@ -89,6 +89,15 @@ int or_assemble_vna_2c_dogs(or_sys *s, const double *S, double *vb,
                             double *vbo);
 int or_assemble_vna_3c_dogs(or_sys *s, const double *S, const double *dip,
                             double *vb);
+/* Ewald (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90): the N x N long-range
+ * Coulomb matrix (row-major), and the ewaldsr / ewaldlr block sets over the
+ * neighbor map from the overlap and z-dipole blocks and the atoms' total
+ * charges (the sum of the shell charges of or_set_charges) */
+int or_assemble_ewald(or_sys *s, double *ewald);
+int or_assemble_ewaldsr(or_sys *s, const double *S, const double *dip,
+                        double *sr);
+int or_assemble_ewaldlr(or_sys *s, const double *ewald, const double *S,
+                        const double *dip, double *lr);
 /* DOGS force derivatives (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90,
  * M_Dassemble_3c_DOGS.f90): z-dipole Dblocks; vna ontop / atom pair terms;
  * f3na{a,b,c} (neutral + charged; overwrites) from S, dS, dip, ddip */

@@ -60,6 +60,9 @@ def lib():
         L.or_assemble_vna_3c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_dassemble_dipole_z.argtypes = [C.c_void_p, _dp]
         L.or_neighbors_pp.argtypes = [C.c_void_p]
+        L.or_assemble_ewald.argtypes = [C.c_void_p, _dp]
+        L.or_assemble_ewaldsr.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.or_assemble_ewaldlr.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_pp_sizes.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_longlong)] * 2
         L.or_pp_sizes.restype = None
         L.or_get_pp.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, C.c_void_p, C.c_void_p]
@@ -253,6 +256,23 @@ class System:
         _check(L.or_build_forces(self.h, rho, cape, dS, dT, ontop, atom, fa, fb, fc, kin, vna, pul, ftot))
         return dict(dS=dS, dT=dT, ddip=ddip, vna_ontop=ontop, vna_atom=atom, f3naa=fa, f3nab=fb, f3nac=fc,
                     kinetic=kin, vna=vna, pulay=pul, ftot=ftot)
+
+    def assemble_ewald(self, dQ):
+        """DOGS Ewald: the N x N matrix ewald(i, j) and the ewaldsr and
+        ewaldlr block sets, with shell charges dQ (natoms, nssh_max)."""
+        L = lib()
+        N, nb = len(self.imass), self.nblock
+        d = np.ascontiguousarray(dQ, np.float64).reshape(N, -1)
+        _check(L.or_set_charges(self.h, np.ascontiguousarray(d.ravel()), d.shape[1]))
+        S, T, vb, vbo, dip = (np.zeros(nb) for _ in range(5))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        _check(L.or_assemble_dipole_z(self.h, dip))
+        ew = np.zeros(N * N)
+        _check(L.or_assemble_ewald(self.h, ew))
+        sr, lr = np.zeros(nb), np.zeros(nb)
+        _check(L.or_assemble_ewaldsr(self.h, S, dip, sr))
+        _check(L.or_assemble_ewaldlr(self.h, ew, S, dip, lr))
+        return ew.reshape(N, N), sr, lr
 
     # ---- non-local pseudopotential (vnl) --------------------------------
     def neighbors_pp(self):

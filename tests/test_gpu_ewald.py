@@ -1,0 +1,71 @@
+"""The DOGS Ewald terms on the GPU (fb_assemble with FB_EWALD) against the
+oracle's restatement of assemble_ewald / assemble_ewaldsr / assemble_ewaldlr
+(j.ASSEMBLERS/M_assemble_ewald_DOGS.f90): the N x N matrix to 1e-10 1/A and
+the ewaldsr / ewaldlr blocks to 1e-10 eV per element, periodic cells of one
+and two species, a vacancy cell and a cluster, plain and as one graph; the
+call-order errors."""
+import numpy as np
+import pytest
+
+import fbgpu
+from conftest import workload
+from fbgpu import synth
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = fbgpu.Context(0)
+    yield c
+    c.close()
+
+
+def case(fdata_root, name):
+    if name == "sic_cluster":
+        path, nZ, _ = workload("sic_small", fdata_root, dogs=True)
+        st = synth.diamond((1, 1, 1), 4.36, 0.1, 41, sp_a=1, sp_b=2, name="SiC8cluster")
+        st.icluster = 1
+        return path, [14, 6], st
+    return workload(name, fdata_root, dogs=True)
+
+
+@pytest.mark.parametrize("name", ["sic_small", "si64", "sic_vac", "cho_small", "sic_cluster"])
+def test_ewald_matches_oracle(ctx, fdata_root, name):
+    path, nZ, st = case(fdata_root, name)
+    dq = np.random.default_rng(13).uniform(-0.3, 0.3, (len(st.imass), 3))
+    s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
+    ew, sr, lr = s.assemble_ewald(dq)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice, st.icluster)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_DOGS)
+    ctx.set_charges(dq)
+    what = fbgpu.FB_ALL | fbgpu.FB_EWALD
+    ctx.assemble(what)
+    assert np.abs(ctx.ewald() - ew).max() <= TOL
+    assert np.abs(ctx.blocks("ewaldsr") - sr).max() <= TOL
+    assert np.abs(ctx.blocks("ewaldlr") - lr).max() <= TOL
+    for _ in range(2):  # as one graph, captured then replayed
+        ctx.assemble_graph(what)
+        assert np.abs(ctx.blocks("ewaldsr") - sr).max() <= TOL
+        assert np.abs(ctx.blocks("ewaldlr") - lr).max() <= TOL
+
+
+def test_ewald_errors(ctx, fdata_root):
+    path, nZ, st = case(fdata_root, "sic_small")
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    with pytest.raises(fbgpu.FBError) as e:      # DOGS only
+        ctx.assemble(fbgpu.FB_ALL | fbgpu.FB_EWALD)
+    assert e.value.code == 11
+    ctx.set_theory(fbgpu.FB_THEORY_DOGS)
+    ctx.set_charges(np.zeros((len(st.imass), 3)))
+    with pytest.raises(fbgpu.FBError) as e:      # the overlap and dipole blocks first
+        ctx.assemble(fbgpu.FB_EWALD)
+    assert e.value.code == 11

@@ -15,6 +15,7 @@
 #include "fb_fdata.h"
 #include "fb_launch.h"
 #include "fb_pp.h"
+#include "fb_ewald.h"
 #include "fb_devbuf.h"
 #include "fb_mlp.h"
 
@@ -28,12 +29,13 @@ std::atomic<long long> g_alloc_gen{0};
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
        KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
        KT_BLOCH, KT_PP_PAIRS, KT_PPP, KT_PPC, KT_SVNL, KT_VNL2C, KT_VNL3C, KT_DSVNL, KT_DVNL2C, KT_DVNL3C,
-       KT_VNLF, KT_N };
+       KT_VNLF, KT_EWALD, KT_EWALD_BLOCKS, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
                                      "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
-                                     "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces"};
+                                     "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald",
+                                     "ewald_blocks"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -89,6 +91,11 @@ struct fb_ctx {
       d_ppp_self, d_vnl_off;
   DevBuf d_ppc_cnt, d_ppc_off, d_t_alpha, d_t_i, d_t_ib, d_t_j, d_t_jb, d_t_m, d_t_m31, d_t_m32;
   DevBuf d_svnl, d_dsvnl, d_vnl, d_rho_pp, d_vnl_atom, d_vnl_ontop, d_f3nla, d_f3nlb, d_f3nlc, d_fvnl;
+  // DOGS Ewald: the N x N matrix, its g / L lists, atom charges, sr / lr blocks
+  bool have_ewald = false;
+  int ew_ng = 0, ew_nl = 0;
+  double ew_kappa = 0.0;
+  DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -128,6 +135,8 @@ struct fb_ctx {
 };
 
 static PPArgs pp_args(fb_ctx *ctx);
+static EwaldArgs ewald_args(fb_ctx *ctx);
+static int ewald_setup(fb_ctx *ctx);
 template <typename T>
 static int host_scan(fb_ctx *ctx, const DevBuf &cnt, int n, std::vector<T> &off, DevBuf &d_off);
 
@@ -309,7 +318,7 @@ int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies, const int *n
   CU(cudaMemcpy(ctx->d_gxy.p, f.gxy.data(), f.gxy.size() * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_fdata = true;
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
   return FB_OK;
 }
 
@@ -409,7 +418,7 @@ int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms, const double *rato
   CU(cudaMemcpy(ctx->d_satom_off.p, ctx->h_satom_off.data(), (nstruct + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_speriodic.p, per.data(), nstruct * sizeof(int), cudaMemcpyHostToDevice));
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
   return fb_update_positions(ctx, ratom);
 }
 
@@ -466,7 +475,7 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
   return FB_OK;
 }
 
@@ -778,7 +787,7 @@ int fb_neighbors_pp(fb_ctx *ctx) {
   if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "vnl maps: single structures (a batch of one)");
   CU(cudaSetDevice(ctx->device));
   int N = ctx->N;
-  ctx->have_pp_neigh = ctx->have_rho_pp = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
   ctx->assembled &= ~(unsigned)(FB_SVNL | FB_VNL2C | FB_VNL3C);
   ctx->dassembled &= ~(unsigned)(FB_VNL2C | FB_VNL3C);
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
@@ -907,6 +916,15 @@ int fb_get_pp_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_
   CHK(d2h_int(ctx, neigh_common, ctx->d_t_m, T, 1));
   CHK(d2h_int(ctx, m31, ctx->d_t_m31, T, 1));
   CHK(d2h_int(ctx, m32, ctx->d_t_m32, T, 1));
+  return FB_OK;
+}
+
+int fb_get_ewald(fb_ctx *ctx, double *ewald) {
+  if (!ctx || !ewald) return FB_ERR_ARG;
+  if (!ctx->have_ewald) return fail(ctx, FB_ERR_STATE, "fb_assemble with FB_EWALD first");
+  CU(cudaMemcpyAsync(ewald, ctx->d_ewald.p, (size_t)ctx->N * ctx->N * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
   return FB_OK;
 }
 
@@ -1107,6 +1125,119 @@ static PPArgs pp_args(fb_ctx *ctx) {
 }  // extern "C++"
 
 extern "C++" {
+extern "C++" {
+// the reciprocal and lattice sums of assemble_ewald (M_assemble_ewald_DOGS.f90:
+// 640-700), built on the host exactly as the reference builds them: the cell
+// volume and reciprocal vectors, kappa = (gmin^2 / (4 rmin^2))^(1/4), the
+// g box (g != 0) with stuff = 4 pi exp(-g^2 / 4 kappa^2) / (g^2 V), and the L
+// box; a cluster has no g terms, only L = 0 and kappa = 0.
+static int ewald_setup(fb_ctx *ctx) {
+  const double pi = 3.141592653589793238462643;
+  const double *lat = &ctx->h_lat[0];
+  double a1[3] = {lat[0], lat[1], lat[2]}, a2[3] = {lat[3], lat[4], lat[5]}, a3[3] = {lat[6], lat[7], lat[8]};
+  auto cross = [](const double *a, const double *b, double *c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  auto mag2 = [](const double *a) {
+    double m = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    return m * m;
+  };
+  double c[3], g1[3], g2[3], g3[3];
+  cross(a2, a3, c);
+  double volume = a1[0] * c[0] + a1[1] * c[1] + a1[2] * c[2];
+  for (int k = 0; k < 3; k++) g1[k] = 2.0 * pi * c[k] / volume;
+  cross(a3, a1, c);
+  for (int k = 0; k < 3; k++) g2[k] = 2.0 * pi * c[k] / volume;
+  cross(a1, a2, c);
+  for (int k = 0; k < 3; k++) g3[k] = 2.0 * pi * c[k] / volume;
+  volume = std::fabs(volume);
+  std::vector<double> gv, st, lv;
+  double kappa = 0.0;
+  if (ctx->h_icl[0] == 1) {
+    lv = {0.0, 0.0, 0.0};
+  } else {
+    double gmax = 5.0, rmax = 5.0;
+    double g1m2 = mag2(g1), g2m2 = mag2(g2), g3m2 = mag2(g3), r1m2 = mag2(a1), r2m2 = mag2(a2), r3m2 = mag2(a3);
+    double rmin2 = std::min(r1m2, std::min(r2m2, r3m2)), gmin2 = std::min(g1m2, std::min(g2m2, g3m2));
+    kappa = std::sqrt(std::sqrt(gmin2 / (4.0 * rmin2)));
+    auto box = [](double v) {
+      int n = (int)(v + 1.0);
+      return n <= 1 ? 2 : n;
+    };
+    int ig1 = box(gmax * std::sqrt(4.0 * kappa * kappa / g1m2)), ig2 = box(gmax * std::sqrt(4.0 * kappa * kappa / g2m2)),
+        ig3 = box(gmax * std::sqrt(4.0 * kappa * kappa / g3m2));
+    int il1 = box(rmax * std::sqrt(1.0 / (kappa * kappa * r1m2))), il2 = box(rmax * std::sqrt(1.0 / (kappa * kappa * r2m2))),
+        il3 = box(rmax * std::sqrt(1.0 / (kappa * kappa * r3m2)));
+    for (int n1 = -ig1; n1 <= ig1; n1++)
+      for (int n2 = -ig2; n2 <= ig2; n2++)
+        for (int n3 = -ig3; n3 <= ig3; n3++) {
+          if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+          double g[3];
+          for (int k = 0; k < 3; k++) g[k] = n1 * g1[k] + n2 * g2[k] + n3 * g3[k];
+          double gm2 = mag2(g);
+          gv.insert(gv.end(), g, g + 3);
+          st.push_back(4.0 * pi * std::exp(-gm2 / (4.0 * kappa * kappa)) / (gm2 * volume));
+        }
+    for (int n1 = -il1; n1 <= il1; n1++)
+      for (int n2 = -il2; n2 <= il2; n2++)
+        for (int n3 = -il3; n3 <= il3; n3++)
+          for (int k = 0; k < 3; k++) lv.push_back(n1 * a1[k] + n2 * a2[k] + n3 * a3[k]);
+  }
+  ctx->ew_ng = (int)st.size();
+  ctx->ew_nl = (int)(lv.size() / 3);
+  ctx->ew_kappa = kappa;
+  CHK(ctx->d_ew_g.ensure(gv.size() * sizeof(double) + 8));
+  CHK(ctx->d_ew_stuff.ensure(st.size() * sizeof(double) + 8));
+  CHK(ctx->d_ew_l.ensure(lv.size() * sizeof(double) + 8));
+  if (!gv.empty()) {
+    CU(cudaMemcpy(ctx->d_ew_g.p, gv.data(), gv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(ctx->d_ew_stuff.p, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CU(cudaMemcpy(ctx->d_ew_l.p, lv.data(), lv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return FB_OK;
+}
+
+static EwaldArgs ewald_args(fb_ctx *ctx) {
+  EwaldArgs e{};
+  e.N = ctx->N;
+  e.T = ctx->T;
+  e.ratom = ctx->d_ratom.as<double>();
+  e.sid = ctx->d_sid.as<int>();
+  e.isp = ctx->d_isp.as<int>();
+  e.fd = ctx->d_fd.as<FdataDev>();
+  e.xl = ctx->d_xl.as<double>();
+  e.ng = ctx->ew_ng;
+  e.nl = ctx->ew_nl;
+  e.gvec = ctx->d_ew_g.as<double>();
+  e.stuff = ctx->d_ew_stuff.as<double>();
+  e.lvec = ctx->d_ew_l.as<double>();
+  e.kappa = ctx->ew_kappa;
+  e.pair_off = ctx->d_pair_off.as<int>();
+  e.neigh_j = ctx->d_neigh_j.as<int>();
+  e.neigh_b = ctx->d_neigh_b.as<int>();
+  e.neigh_self = ctx->d_neigh_self.as<int>();
+  e.blk_off = ctx->d_blk_off.as<long long>();
+  e.trip_alpha = ctx->d_talpha.as<int>();
+  e.ci_j = ctx->d_ci_j.as<int>();
+  e.ci_b = ctx->d_ci_b.as<int>();
+  e.cj_j = ctx->d_cj_j.as<int>();
+  e.cj_b = ctx->d_cj_b.as<int>();
+  e.tdst = ctx->d_tdst.as<int>();
+  e.dq = ctx->d_dq.as<double>();
+  e.dqa = ctx->d_dqa.as<double>();
+  e.ewald = ctx->d_ewald.as<double>();
+  e.sum_ewald = ctx->d_sum_ewald.as<double>();
+  e.S = ctx->d_S.as<double>();
+  e.dip = ctx->d_dip.as<double>();
+  e.sr = ctx->d_ewsr.as<double>();
+  e.lr = ctx->d_ewlr.as<double>();
+  return e;
+}
+
+}  // extern "C++"
+
 // count -> host prefix sum -> offsets on the device (n + 1 entries)
 template <typename T>
 static int host_scan(fb_ctx *ctx, const DevBuf &cnt, int n, std::vector<T> &off, DevBuf &d_off) {
@@ -1214,6 +1345,12 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     if (what & FB_VNL2C) KL(KT_VNL2C, launch_vnl_2c(pa, ctx->stream));
     if (what & FB_VNL3C) KL(KT_VNL3C, launch_vnl_3c(pa, ctx->ntrip_pp, ctx->stream));
   }
+  if (what & FB_EWALD) {
+    EwaldArgs e = ewald_args(ctx);
+    KL(KT_EWALD, launch_ewald_matrix(e, ctx->stream));
+    KL(KT_EWALD_BLOCKS, launch_ewald_blocks(e, ctx->fdh.have_d, ctx->stream));
+    ctx->launches += e.T > 0 ? 3 : 2;
+  }
   if (what & FB_VNA3C) {
     // triplets of approved bins through the network, the rest through the tables
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
@@ -1246,6 +1383,20 @@ static int check_assemble(fb_ctx *ctx, unsigned what) {
     return fail(ctx, FB_ERR_TABLE, "FB_DIPOLE: the Fdata has no z-dipole table (dipole_z)");
   if ((what & FB_DIPOLE) || (dogs && (what & FB_VNA2C)))
     CHK(ctx->d_dip.ensure((size_t)ctx->nblock * sizeof(double) + 8));
+  if (what & FB_EWALD) {
+    if (!dogs) return fail(ctx, FB_ERR_STATE, "Ewald: the DOGS theory (fb_set_theory) first");
+    if (!ctx->have_charges) return fail(ctx, FB_ERR_STATE, "Ewald: fb_set_charges first");
+    if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "Ewald: single structures (a batch of one)");
+    if (!(what & FB_VNA2C) && !(ctx->have_dip && (ctx->assembled & FB_S)))
+      return fail(ctx, FB_ERR_STATE, "Ewald reads the overlap and dipole blocks: assemble FB_VNA2C (DOGS) first");
+    size_t nb = (size_t)ctx->nblock * sizeof(double) + 8, n = (size_t)ctx->N;
+    CHK(ctx->d_ewald.ensure(n * n * sizeof(double) + 8));
+    CHK(ctx->d_dqa.ensure(n * sizeof(double) + 8));
+    CHK(ctx->d_sum_ewald.ensure(n * sizeof(double) + 8));
+    CHK(ctx->d_ewsr.ensure(nb));
+    CHK(ctx->d_ewlr.ensure(nb));
+    CHK(ewald_setup(ctx));
+  }
   if (what & (FB_SVNL | FB_VNL2C | FB_VNL3C)) {
     if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
     if ((what & (FB_VNL2C | FB_VNL3C)) && !(what & FB_SVNL) && !(ctx->assembled & FB_SVNL))
@@ -1262,6 +1413,7 @@ static void assemble_done(fb_ctx *ctx, unsigned what) {
   if (what & FB_VNA2C) ctx->have_vna2c = true;
   if ((what & FB_DIPOLE) || (ctx->theory == FB_THEORY_DOGS && (what & FB_VNA2C))) ctx->have_dip = true;
   ctx->assembled |= what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C);
+  if (what & FB_EWALD) ctx->have_ewald = true;
 }
 
 int fb_assemble(fb_ctx *ctx, unsigned what) {
@@ -1294,6 +1446,8 @@ static DevBuf *block_buf(fb_ctx *ctx, int which, size_t *n) {
     case FB_BLOCK_VNL: *n = (size_t)ctx->nvnl; return (ctx->assembled & FB_VNL2C) ? &ctx->d_vnl : nullptr;
     case FB_BLOCK_DSVNL: *n = (size_t)3 * ctx->nsvnl; return (ctx->dassembled & (FB_VNL2C | FB_VNL3C)) ? &ctx->d_dsvnl : nullptr;
     case FB_BLOCK_RHO_PP: *n = (size_t)ctx->nvnl; return ctx->have_rho_pp ? &ctx->d_rho_pp : nullptr;
+    case FB_BLOCK_EWALDSR: return ctx->have_ewald ? &ctx->d_ewsr : nullptr;
+    case FB_BLOCK_EWALDLR: return ctx->have_ewald ? &ctx->d_ewlr : nullptr;
   }
   return nullptr;
 }
@@ -1485,7 +1639,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   int st = FB_OK;
   if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
     st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
-  if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C))) st = enqueue_assemble(ctx, what);
+  if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD))) st = enqueue_assemble(ctx, what);
   if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -1526,7 +1680,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
 
 int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
-  const unsigned vals = FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C;
+  const unsigned vals = FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD;
   if (!(what & (vals | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
   CU(cudaSetDevice(ctx->device));
   if (what & vals) CHK(check_assemble(ctx, what));

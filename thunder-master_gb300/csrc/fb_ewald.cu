@@ -1,0 +1,175 @@
+// fb_ewald.cu -- sm_103a kernels of the DOGS Ewald terms
+// (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90): the long-range Coulomb matrix
+// ewald(i, j) (assemble_ewald, :633-918), sum_ewald = ewald dQ, and the
+// ewaldsr / ewaldlr blocks over the neighbor map (:98-592).
+//
+// The matrix is the reference's sum: over the reciprocal vectors g != 0 of
+// the box it chooses, stuff(g) cos(g . (r_i - r_j)), plus over its lattice
+// vectors L the screened erfc(kappa z)/z with z = |L + r_i - r_j| > 1e-4,
+// minus 2 kappa / sqrt(pi) on the diagonal.  The g and L lists and kappa
+// are built on the host exactly as the reference builds them.  One thread
+// per (i, j) of the upper triangle, mirrored; FP64 throughout.
+#include "fb_common.cuh"
+#include "fb_ewald.h"
+
+namespace fb {
+
+namespace {
+
+__global__ void k_ewald(EwaldArgs e) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long N = e.N;
+  if (t >= N * (N + 1) / 2) return;
+  // t -> (i, j), j >= i, row-major over the upper triangle
+  long long i = (long long)((2.0 * N + 1.0 - sqrt((2.0 * N + 1.0) * (2.0 * N + 1.0) - 8.0 * (double)t)) / 2.0);
+  if (i < 0) i = 0;
+  while (i > 0 && i * (2 * N - i + 1) / 2 > t) i--;
+  while ((i + 1) * (2 * N - i) / 2 <= t) i++;
+  long long j = i + (t - i * (2 * N - i + 1) / 2);
+  double d[3] = {e.ratom[3 * i] - e.ratom[3 * j], e.ratom[3 * i + 1] - e.ratom[3 * j + 1],
+                 e.ratom[3 * i + 2] - e.ratom[3 * j + 2]};
+  double acc = 0.0;
+  for (int k = 0; k < e.ng; k++) {
+    const double *g = e.gvec + 3 * k;
+    double gdotb = g[0] * d[0] + g[1] * d[1] + g[2] * d[2];
+    acc += e.stuff[k] * cos(gdotb);
+  }
+  for (int k = 0; k < e.nl; k++) {
+    const double *L = e.lvec + 3 * k;
+    double c0 = L[0] + d[0], c1 = L[1] + d[1], c2 = L[2] + d[2];
+    double z = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    if (z > 0.0001) acc += erfc(e.kappa * z) / z;
+  }
+  if (i == j) acc -= 2.0 * e.kappa / sqrt(3.141592653589793238462643);
+  e.ewald[i * N + j] = acc;
+  e.ewald[j * N + i] = acc;
+}
+
+// sum_ewald(i) = sum_j dQ_j ewald(i, j): one warp per row
+__global__ void k_sum_ewald(EwaldArgs e) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= e.N) return;
+  double s = 0.0;
+  for (int j = lane; j < e.N; j += 32) s = fma(e.dqa[j], e.ewald[(long long)i * e.N + j], s);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+  if (lane == 0) e.sum_ewald[i] = s;
+}
+
+// ewaldsr two-center terms and ewaldlr, one warp per atom: the lanes write
+// the ontop and long-range terms of their pairs, then the atom term
+// (dQ_j S(i, self)/z eq2 over the neighbors) is reduced into the self block
+template <int PA>
+__device__ void atom_ewald_2c(const EwaldArgs &e, int i, int lane) {
+  constexpr int NA = pat_norb(PA);
+  const FdataDev &fd = *e.fd;
+  int p0 = e.pair_off[i], p1 = e.pair_off[i + 1];
+  const double *X = e.xl + (long long)e.sid[i] * XL_STRIDE;
+  long long os = e.blk_off[p0 + e.neigh_self[i]];
+  double ri[3] = {e.ratom[3 * i], e.ratom[3 * i + 1], e.ratom[3 * i + 2]};
+  double wsum = 0.0;  // sum over non-self neighbors of dQ_j / z
+  for (int p = p0 + lane; p < p1; p += 32) {
+    int j = e.neigh_j[p], mb = e.neigh_b[p];
+    int nj = fd.sp[e.isp[j]].norb;
+    long long o = e.blk_off[p];
+    bool self = (i == j && mb == 0);
+    double r2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) r2[k] = e.ratom[3 * j + k] + X[3 * mb + k];
+    double z = dist_rn(ri, r2);
+    double qi = e.dqa[i], qj = e.dqa[j], si = e.sum_ewald[i], sj = e.sum_ewald[j];
+    if (!self) wsum += qj / z;
+    for (int q = 0; q < NA * nj; q++) {
+      double Sv = e.S[o + q], Dv = e.dip[o + q];
+      // ewaldlr (:520-590): the dipole term left out on the self pair
+      double sterm = Sv / 2.0, dterm = self ? 0.0 : Dv / z;
+      e.lr[o + q] = (sterm - dterm) * si * P_eq2 + (sterm + dterm) * sj * P_eq2;
+      // ewaldsr ontop (:245-300)
+      if (!self) {
+        double st = Sv / (2.0 * z), dt = Dv / (z * z);
+        e.sr[o + q] = qi * (st + dt) * P_eq2 + qj * (st - dt) * P_eq2;
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
+  __syncwarp();
+  // ewaldsr atom term (:200-240) into the self block (the self pair has no ontop term)
+  for (int q = lane; q < NA * NA; q += 32) e.sr[os + q] = e.S[os + q] * wsum * P_eq2;
+}
+
+template <bool HASD>
+__global__ void k_ewald_2c(EwaldArgs e) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= e.N) return;
+  int pa = e.fd->sp[e.isp[i]].pattern;
+  if (pa == PAT_SP) atom_ewald_2c<PAT_SP>(e, i, lane);
+  else if (pa == PAT_S) atom_ewald_2c<PAT_S>(e, i, lane);
+  else if constexpr (HASD) atom_ewald_2c<PAT_SPD>(e, i, lane);
+}
+
+// ewaldsr three-center terms (:305-375): per common-neighbor triplet,
+// ((sterm - dterm)/d13 + (sterm + dterm)/d23) eq2 with sterm = dQ_alpha S/2
+// and dterm = dQ_alpha dip/z, FP64 atomics into block (i, mneigh)
+__global__ void k_ewald_3c(EwaldArgs e) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.T) return;
+  const FdataDev &fd = *e.fd;
+  int ia = e.trip_alpha[t], iat = e.ci_j[t], jat = e.cj_j[t];
+  const double *X = e.xl + (long long)e.sid[ia] * XL_STRIDE;
+  int ib = e.ci_b[t], jb = e.cj_b[t];
+  double r1[3], r2[3], rna[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r1[k] = e.ratom[3 * iat + k] + X[3 * ib + k];
+    r2[k] = e.ratom[3 * jat + k] + X[3 * jb + k];
+    rna[k] = e.ratom[3 * ia + k];
+  }
+  double z = dist_rn(r1, r2), d13 = dist_rn(rna, r1), d23 = dist_rn(rna, r2);
+  int ni = fd.sp[e.isp[iat]].norb, nj = fd.sp[e.isp[jat]].norb;
+  long long o = e.blk_off[e.tdst[t]];
+  double qa = e.dqa[ia];
+  for (int q = 0; q < ni * nj; q++) {
+    double sterm = qa * e.S[o + q] / 2.0, dterm = qa * e.dip[o + q] / z;
+    atomicAdd(e.sr + o + q, ((sterm - dterm) / d13 + (sterm + dterm) / d23) * P_eq2);
+  }
+}
+
+// dQ of each atom: the sum of its shell charges
+__global__ void k_atom_dq(EwaldArgs e) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e.N) return;
+  double s = 0.0;
+  int n = e.fd->sp[e.isp[i]].nssh;
+  for (int k = 0; k < n && k < MAXSUB; k++) s += e.dq[i * MAXSUB + k];
+  e.dqa[i] = s;
+}
+
+}  // namespace
+
+int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s) {
+  long long n = (long long)e.N * (e.N + 1) / 2;
+  k_ewald<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_ewald_blocks(const EwaldArgs &e, int have_d, cudaStream_t s) {
+  k_atom_dq<<<(e.N + 255) / 256, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  unsigned wg = (unsigned)(((long long)e.N * 32 + 255) / 256);
+  k_sum_ewald<<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  if (have_d) k_ewald_2c<true><<<wg, 256, 0, s>>>(e);
+  else k_ewald_2c<false><<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  if (e.T > 0) {
+    k_ewald_3c<<<(e.T + 255) / 256, 256, 0, s>>>(e);
+    FB_LAUNCH_CHECK();
+  }
+  return 0;
+}
+
+}  // namespace fb

@@ -1,0 +1,36 @@
+// fb_ewald.h -- device arguments and launchers of the DOGS Ewald terms
+// (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fb_internal.h"
+
+namespace fb {
+
+struct EwaldArgs {
+  int N, T;
+  const double *ratom;
+  const int *sid, *isp;
+  const FdataDev *fd;
+  const double *xl;
+  // the reciprocal vectors g != 0 with stuff(g), the lattice vectors L, kappa
+  int ng, nl;
+  const double *gvec, *stuff, *lvec;
+  double kappa;
+  // neighbor and common-neighbor maps, block offsets
+  const int *pair_off, *neigh_j, *neigh_b, *neigh_self;
+  const long long *blk_off;
+  const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
+  // charges: shell charges dq[atom][MAXSUB] -> atom totals dqa
+  const double *dq;
+  double *dqa;
+  // outputs and inputs
+  double *ewald, *sum_ewald;
+  const double *S, *dip;
+  double *sr, *lr;
+};
+
+int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s);
+int launch_ewald_blocks(const EwaldArgs &e, int have_d, cudaStream_t s);
+
+}  // namespace fb

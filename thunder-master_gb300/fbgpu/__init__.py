@@ -23,6 +23,7 @@ Context.set_theory     DOGS instead of Harris vna 2c / 3c             j.ASSEMBLE
                                                                       j.ASSEMBLERS/M_assemble_3c_DOGS.f90:158
 Context.assemble_dipole_z  assemble_dipole_z                          j.ASSEMBLERS/M_assemble_2c_DOGS.f90:376
 Context.bloch          Bloch sums into H(k), S(k)                     h.SOLVESH/M_kspace_Lowdin.f90:680
+Context.assemble(FB_EWALD)  assemble_ewald / ewaldsr / ewaldlr (DOGS)  j.ASSEMBLERS/M_assemble_ewald_DOGS.f90
 Context.driver_neighbors_PP  driver_neighbors_PP                      c.SYSTEM/M_neighbors_PP.f90:98
 Context.assemble(FB_VNL)  assemble_svnl / vnl_2c / vnl_3c             j.ASSEMBLERS/M_assemble_PP_{2c,3c}.f90
 Context.Dassemble(FB_VNL2C | FB_VNL3C)  Dassemble_svnl / vnl_2c / vnl_3c  k.DASSEMBLERS/M_Dassemble_PP_{2c,3c}.f90
@@ -43,6 +44,7 @@ LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
 FB_DIPOLE = 64
+FB_EWALD = 1024
 FB_SVNL, FB_VNL2C, FB_VNL3C = 128, 256, 512
 FB_VNL = FB_SVNL | FB_VNL2C | FB_VNL3C
 FB_PP_MAP, FB_PPX_MAP, FB_PPP_MAP = 0, 1, 2
@@ -51,7 +53,7 @@ FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
 FB_MLP_ENGINE_MMA, FB_MLP_ENGINE_TC = 0, 1
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
 BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7, "dip": 8,
-         "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12}
+         "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12, "ewaldsr": 13, "ewaldlr": 14}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8,
          "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14}
@@ -112,6 +114,7 @@ _SIGS = {
     "fb_get_pp_neighbors": (C.c_int, [C.c_void_p, C.c_int] + [C.c_void_p] * 6),
     "fb_get_pp_common": (C.c_int, [C.c_void_p] + [C.c_void_p] * 8),
     "fb_set_denmat_pp": (C.c_int, [C.c_void_p, _dp]),
+    "fb_get_ewald": (C.c_int, [C.c_void_p, _dp]),
     "fb_set_denmat_pp_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fb_assemble": (C.c_int, [C.c_void_p, C.c_uint]),
     "fb_get_blocks": (C.c_int, [C.c_void_p, C.c_int, _dp]),
@@ -137,7 +140,7 @@ FB_PREC_FP64, FB_PREC_DF = 0, 1
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
            "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
            "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
-           "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces")
+           "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald", "ewald_blocks")
 
 
 class FBError(RuntimeError):
@@ -336,6 +339,12 @@ class Context:
         self._check(self.L.fb_get_pp_common(self.h, _ptr(nc), *[_ptr(x) for x in arr]))
         return dict(ncommon=nc, iatom_j=arr[0][:T], iatom_b=arr[1][:T], jatom_j=arr[2][:T], jatom_b=arr[3][:T],
                     neigh_common=arr[4][:T], m31=arr[5][:T], m32=arr[6][:T])
+
+    def ewald(self):
+        """The N x N Ewald matrix of the last FB_EWALD assembly."""
+        out = np.zeros(self.natoms * self.natoms)
+        self._check(self.L.fb_get_ewald(self.h, out))
+        return out.reshape(self.natoms, self.natoms)
 
     def set_denmat_pp(self, rho_pp):
         self._check(self.L.fb_set_denmat_pp(self.h, np.ascontiguousarray(rho_pp, np.float64)))
