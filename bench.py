@@ -545,6 +545,20 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
            "unit": UNIT, "gpu_launches_per_step": launches // max(1, args.steps),
            "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
            "launch_shapes": shapes}
+    # the Ewald terms (matrix + ewaldsr + ewaldlr) on top of the DOGS value pass
+    ctx.assemble(fbgpu.FB_ALL)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.assemble(fbgpu.FB_EWALD)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.assemble(fbgpu.FB_EWALD)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["ewald"] = {"what": "DOGS Ewald: N x N matrix (reciprocal + screened lattice sums), ewaldsr, ewaldlr",
+                    "ms": round(e0.elapsed_time(e1) / args.steps, 4)}
+    ew_gpu = ctx.ewald()
+    sr_gpu, lr_gpu = ctx.blocks("ewaldsr"), ctx.blocks("ewaldlr")
     # agreement with the oracle and the oracle's single-core time
     got = {k: ctx.blocks(k) for k in ("vna", "vnao")}
     ctx.set_denmat(rho, cape)
@@ -562,6 +576,11 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
         d = s.dassemble_dogs(rho, cape, dq)
         t = time.perf_counter() - t0
         out["max_abs_dvna_ev"] = float(max(np.abs(got["vna"] - ref[2]).max(), np.abs(got["vnao"] - ref[3]).max()))
+        t0 = time.perf_counter()
+        ew, sr, lr = s.assemble_ewald(dq)
+        out["ewald"]["cpu_oracle_s"] = round(time.perf_counter() - t0, 3)
+        out["ewald"]["max_abs_dewald"] = float(np.abs(ew_gpu - ew).max())
+        out["ewald"]["max_abs_dsr_lr_ev"] = float(max(np.abs(sr_gpu - sr).max(), np.abs(lr_gpu - lr).max()))
         out["max_abs_dftot_ev_per_A"] = float(np.abs(f_gpu - d["ftot"]).max())
         out["cpu_oracle"] = {"value": round(P / t, 1), "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": "1 DOGS step (neighbors + value + force pass), %.3f s" % t}
