@@ -95,7 +95,7 @@ struct fb_ctx {
   bool have_ewald = false;
   int ew_ng = 0, ew_nl = 0;
   double ew_kappa = 0.0;
-  DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr;
+  DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -1188,6 +1188,8 @@ static int ewald_setup(fb_ctx *ctx) {
   ctx->ew_ng = (int)st.size();
   ctx->ew_nl = (int)(lv.size() / 3);
   ctx->ew_kappa = kappa;
+  CHK(ctx->d_ew_sfc.ensure((size_t)ctx->N * ctx->ew_ng * sizeof(double) + 8));
+  CHK(ctx->d_ew_sfs.ensure((size_t)ctx->N * ctx->ew_ng * sizeof(double) + 8));
   CHK(ctx->d_ew_g.ensure(gv.size() * sizeof(double) + 8));
   CHK(ctx->d_ew_stuff.ensure(st.size() * sizeof(double) + 8));
   CHK(ctx->d_ew_l.ensure(lv.size() * sizeof(double) + 8));
@@ -1227,6 +1229,8 @@ static EwaldArgs ewald_args(fb_ctx *ctx) {
   e.tdst = ctx->d_tdst.as<int>();
   e.dq = ctx->d_dq.as<double>();
   e.dqa = ctx->d_dqa.as<double>();
+  e.sfc = ctx->d_ew_sfc.as<double>();
+  e.sfs = ctx->d_ew_sfs.as<double>();
   e.ewald = ctx->d_ewald.as<double>();
   e.sum_ewald = ctx->d_sum_ewald.as<double>();
   e.S = ctx->d_S.as<double>();
@@ -1348,6 +1352,7 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   if (what & FB_EWALD) {
     EwaldArgs e = ewald_args(ctx);
     KL(KT_EWALD, launch_ewald_matrix(e, ctx->stream));
+    if (e.ng > 0) ctx->launches++;  // structure factors + tiles
     KL(KT_EWALD_BLOCKS, launch_ewald_blocks(e, ctx->fdh.have_d, ctx->stream));
     ctx->launches += e.T > 0 ? 3 : 2;
   }

@@ -7,8 +7,13 @@
 // the box it chooses, stuff(g) cos(g . (r_i - r_j)), plus over its lattice
 // vectors L the screened erfc(kappa z)/z with z = |L + r_i - r_j| > 1e-4,
 // minus 2 kappa / sqrt(pi) on the diagonal.  The g and L lists and kappa
-// are built on the host exactly as the reference builds them.  One thread
-// per (i, j) of the upper triangle, mirrored; FP64 throughout.
+// are built on the host exactly as the reference builds them; FP64
+// throughout.  The reciprocal half is evaluated as the structure-factor
+// product sum_g stuff(g) (cos g.r_i cos g.r_j + sin g.r_i sin g.r_j) over
+// 32 x 32 tiles of (i, j) with the per-atom cos / sin tables staged in shared
+// memory; the lattice half skips the terms with kappa z > 5.5, each below
+// erfc(5.5)/z < 1e-14 / z (the oracle keeps them; the difference stays far
+// below the 1e-10 parity tolerance).
 #include "fb_common.cuh"
 #include "fb_ewald.h"
 
@@ -16,33 +21,76 @@ namespace fb {
 
 namespace {
 
-__global__ void k_ewald(EwaldArgs e) {
+// per-atom cos(g . r_i), sin(g . r_i), [i * ng + k]
+__global__ void k_ewald_sf(EwaldArgs e) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long N = e.N;
-  if (t >= N * (N + 1) / 2) return;
-  // t -> (i, j), j >= i, row-major over the upper triangle
-  long long i = (long long)((2.0 * N + 1.0 - sqrt((2.0 * N + 1.0) * (2.0 * N + 1.0) - 8.0 * (double)t)) / 2.0);
-  if (i < 0) i = 0;
-  while (i > 0 && i * (2 * N - i + 1) / 2 > t) i--;
-  while ((i + 1) * (2 * N - i) / 2 <= t) i++;
-  long long j = i + (t - i * (2 * N - i + 1) / 2);
-  double d[3] = {e.ratom[3 * i] - e.ratom[3 * j], e.ratom[3 * i + 1] - e.ratom[3 * j + 1],
-                 e.ratom[3 * i + 2] - e.ratom[3 * j + 2]};
-  double acc = 0.0;
-  for (int k = 0; k < e.ng; k++) {
-    const double *g = e.gvec + 3 * k;
-    double gdotb = g[0] * d[0] + g[1] * d[1] + g[2] * d[2];
-    acc += e.stuff[k] * cos(gdotb);
+  if (t >= (long long)e.N * e.ng) return;
+  int i = (int)(t / e.ng), k = (int)(t % e.ng);
+  const double *g = e.gvec + 3 * k;
+  double gr = g[0] * e.ratom[3 * i] + g[1] * e.ratom[3 * i + 1] + g[2] * e.ratom[3 * i + 2];
+  double sn, cs;
+  sincos(gr, &sn, &cs);
+  e.sfc[t] = cs;
+  e.sfs[t] = sn;
+}
+
+// one 32 x 32 tile (bi <= bj) per block of 32 x 8 threads, 4 rows each
+__global__ void __launch_bounds__(256) k_ewald_tiles(EwaldArgs e) {
+  __shared__ double Ci[32][33], Si[32][33], Cj[32][33], Sj[32][33], St[32];
+  int nb = (e.N + 31) / 32;
+  // blockIdx.x -> (bi, bj), bj >= bi, row-major over the upper triangle of tiles
+  int t = blockIdx.x, bi = 0;
+  while (t >= nb - bi) {
+    t -= nb - bi;
+    bi++;
   }
-  for (int k = 0; k < e.nl; k++) {
-    const double *L = e.lvec + 3 * k;
-    double c0 = L[0] + d[0], c1 = L[1] + d[1], c2 = L[2] + d[2];
-    double z = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
-    if (z > 0.0001) acc += erfc(e.kappa * z) / z;
+  int bj = bi + t;
+  int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  int j = bj * 32 + tx;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k0 = 0; k0 < e.ng; k0 += 32) {
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      int ii = bi * 32 + r, jj = bj * 32 + r, k = k0 + tx;
+      bool kv = k < e.ng;
+      Ci[r][tx] = (kv && ii < e.N) ? e.sfc[(long long)ii * e.ng + k] : 0.0;
+      Si[r][tx] = (kv && ii < e.N) ? e.sfs[(long long)ii * e.ng + k] : 0.0;
+      Cj[r][tx] = (kv && jj < e.N) ? e.sfc[(long long)jj * e.ng + k] : 0.0;
+      Sj[r][tx] = (kv && jj < e.N) ? e.sfs[(long long)jj * e.ng + k] : 0.0;
+    }
+    if (ty == 0) St[tx] = (k0 + tx < e.ng) ? e.stuff[k0 + tx] : 0.0;
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < 32; k++) {
+      double cj = Cj[tx][k], sj = Sj[tx][k], st = St[k];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        int r = ty + 8 * q;
+        acc[q] = fma(st, fma(Ci[r][k], cj, Si[r][k] * sj), acc[q]);
+      }
+    }
   }
-  if (i == j) acc -= 2.0 * e.kappa / sqrt(3.141592653589793238462643);
-  e.ewald[i * N + j] = acc;
-  e.ewald[j * N + i] = acc;
+  if (j >= e.N) return;
+  double rcut2 = e.kappa > 0.0 ? (5.5 / e.kappa) * (5.5 / e.kappa) : 1.0e300;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    int i = bi * 32 + ty + 8 * q;
+    if (i >= e.N || (bi == bj && j < i)) continue;
+    double d[3] = {e.ratom[3 * i] - e.ratom[3 * j], e.ratom[3 * i + 1] - e.ratom[3 * j + 1],
+                   e.ratom[3 * i + 2] - e.ratom[3 * j + 2]};
+    double v = acc[q];
+    for (int k = 0; k < e.nl; k++) {
+      const double *L = e.lvec + 3 * k;
+      double c0 = L[0] + d[0], c1 = L[1] + d[1], c2 = L[2] + d[2];
+      double z2 = c0 * c0 + c1 * c1 + c2 * c2;
+      if (z2 > rcut2) continue;
+      double z = sqrt(z2);
+      if (z > 0.0001) v += erfc(e.kappa * z) / z;
+    }
+    if (i == j) v -= 2.0 * e.kappa / sqrt(3.141592653589793238462643);
+    e.ewald[(long long)i * e.N + j] = v;
+    e.ewald[(long long)j * e.N + i] = v;
+  }
 }
 
 // sum_ewald(i) = sum_j dQ_j ewald(i, j): one warp per row
@@ -150,8 +198,13 @@ __global__ void k_atom_dq(EwaldArgs e) {
 }  // namespace
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s) {
-  long long n = (long long)e.N * (e.N + 1) / 2;
-  k_ewald<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(e);
+  if (e.ng > 0) {
+    long long n = (long long)e.N * e.ng;
+    k_ewald_sf<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e);
+    FB_LAUNCH_CHECK();
+  }
+  long long nb = (e.N + 31) / 32;
+  k_ewald_tiles<<<(unsigned)(nb * (nb + 1) / 2), 256, 0, s>>>(e);
   FB_LAUNCH_CHECK();
   return 0;
 }

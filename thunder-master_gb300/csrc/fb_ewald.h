@@ -24,6 +24,8 @@ struct EwaldArgs {
   // charges: shell charges dq[atom][MAXSUB] -> atom totals dqa
   const double *dq;
   double *dqa;
+  // per-atom structure factors cos / sin(g . r_i), [i * ng + k]
+  double *sfc, *sfs;
   // outputs and inputs
   double *ewald, *sum_ewald;
   const double *S, *dip;
