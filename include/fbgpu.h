@@ -117,6 +117,9 @@ extern "C" {
 #define FB_F_F3NLC 12      /* forces(i)%f3nlc */
 #define FB_F_VNL_ATOM 13   /* forces(i)%vnl_atom(3, neighn_PP), per PP pair */
 #define FB_F_VNL_ONTOP 14  /* forces(i)%vnl_ontop(3, neighn_PPx), per PPx pair (ontop left) */
+#define FB_F_EWALDSR 15    /* forces(i)%ewaldsr(3, neighn), per pair (DOGS, FB_EWALD) */
+#define FB_F_EWALDLR 16    /* forces(i)%ewaldlr (DOGS, FB_EWALD) */
+#define FB_F_EWALD 17      /* forces(i)%ewald, the Ewald energy force of Dassemble_ewald (DOGS, FB_EWALD) */
 
 typedef struct fb_ctx fb_ctx;
 
@@ -426,7 +429,15 @@ int fb_set_charges(fb_ctx *ctx, const double *dq, int nssh_max);
  * short-range correction s%ewaldsr (:98-378: atom, ontop and three-center
  * terms from the overlap and z-dipole blocks and the atoms' total charges)
  * and the long-range blocks s%ewaldlr (:404-592, with sum_ewald = ewald dQ).
- * Single structures.  fb_get_ewald copies the N x N matrix (row-major). */
+ * Single structures.  fb_get_ewald copies the N x N matrix (row-major).
+ * fb_dassemble with FB_EWALD (after FB_EWALD was assembled, or in one
+ * fb_assemble_graph with it) computes the force pass of
+ * k.DASSEMBLERS/M_Dassemble_ewald_DOGS.f90: dewald and the Ewald energy
+ * force FB_F_EWALD (Dassemble_ewald, :878-1236), the ewaldsr pair forces
+ * FB_F_EWALDSR with their three-center terms added into f3na (:94-527),
+ * the ewaldlr atom forces FB_F_EWALDLR (:553-837), and the build_forces
+ * terms (ftot -= ewaldsr on i, += on j, += ewaldlr; M_build_forces.f90:
+ * 367-386) added into FB_F_TOT.  dewald is 3 N^2 doubles. */
 int fb_get_ewald(fb_ctx *ctx, double *ewald);
 
 /* Arithmetic of the three-center kernels.  FB_PREC_DF (the default): the

@@ -104,6 +104,7 @@ typedef struct {
   /* pseudopotential projectors: shells, orbitals, cutoff (as read), cl */
   int lssh_PP[MAXSH], norb_PP_max;
   double rcutoff_PP, cl_PP[MAXSH];
+  double Q0; /* sum of the shells' Qneutral */
 } species_t;
 
 struct or_fdata {
@@ -281,6 +282,8 @@ static int read_info(or_fdata *fd, const char *dir, const int *nZreq) {
     if (s->nssh_PP > 0 && read_ints(&t, s->nssh_PP, lpp)) goto bad;
     if (read_dbls(&t, 1, &rcpp)) goto bad;
     s->rcutoff_PP = rcpp; /* :1147, used as read (M_neighbors_PP.f90:469) */
+    s->Q0 = 0.0;
+    for (int i = 0; i < nssh; i++) s->Q0 = s->Q0 + qn[i];
     s->norb_PP_max = 0;   /* :1188-1194 */
     for (int i = 0; i < s->nssh_PP; i++) {
       if (lpp[i] < 0 || lpp[i] > 2) { seterr("unsupported PP l=%d", lpp[i]); txt_close(&t); return E_UNSUP; }
@@ -2851,5 +2854,248 @@ int or_assemble_ewaldlr(or_sys *s, const double *ewald, const double *S, const d
   }
   free(dq);
   free(se);
+  return OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Ewald force pass (DOGS, k.DASSEMBLERS/M_Dassemble_ewald_DOGS.f90)         */
+/* ------------------------------------------------------------------------ */
+/* Dassemble_ewald (:878-1236): dewald(:, i, j) = derivative of ewald(i, j)
+ * with respect to r_i ([(i * N + j) * 3 + c]), and the Ewald energy force
+ * fewald(i) with qq = Q_i Q_j - Q0_i Q0_j (Q = Q0 + dQ) */
+int or_dassemble_ewald(or_sys *s, double *dewald, double *fewald) {
+  int N = s->natoms;
+  const double pi = 3.141592653589793238462643;
+  double *dq = (double *)malloc(sizeof(double) * N), *Q = (double *)malloc(sizeof(double) * N),
+         *Q0 = (double *)malloc(sizeof(double) * N);
+  atom_dq(s, dq);
+  for (int i = 0; i < N; i++) Q0[i] = s->fd->sp[s->imass[i]].Q0, Q[i] = Q0[i] + dq[i];
+  for (long long k = 0; k < 3LL * N * N; k++) dewald[k] = 0.0;
+  for (int k = 0; k < 3 * N; k++) fewald[k] = 0.0;
+  double a1[3], a2[3], a3[3], c[3], g1[3], g2[3], g3[3];
+  for (int k = 0; k < 3; k++) a1[k] = s->lattice[0][k], a2[k] = s->lattice[1][k], a3[k] = s->lattice[2][k];
+  cross3(a2, a3, c);
+  double volume = a1[0] * c[0] + a1[1] * c[1] + a1[2] * c[2];
+  for (int k = 0; k < 3; k++) g1[k] = 2.0 * pi * c[k] / volume;
+  cross3(a3, a1, c);
+  for (int k = 0; k < 3; k++) g2[k] = 2.0 * pi * c[k] / volume;
+  cross3(a1, a2, c);
+  for (int k = 0; k < 3; k++) g3[k] = 2.0 * pi * c[k] / volume;
+  volume = fabs(volume);
+  double gmax = 5.0, rmax = 5.0;
+  double g1m2 = pow(magnitude3(g1), 2), g2m2 = pow(magnitude3(g2), 2), g3m2 = pow(magnitude3(g3), 2);
+  double r1m2 = pow(magnitude3(a1), 2), r2m2 = pow(magnitude3(a2), 2), r3m2 = pow(magnitude3(a3), 2);
+  double rmin2 = r1m2;
+  if (r2m2 < rmin2) rmin2 = r2m2;
+  if (r3m2 < rmin2) rmin2 = r3m2;
+  double gmin2 = g1m2;
+  if (g2m2 < gmin2) gmin2 = g2m2;
+  if (g3m2 < gmin2) gmin2 = g3m2;
+  double kappa = sqrt(sqrt(gmin2 / (4.0 * rmin2)));
+  int ig1 = (int)(gmax * sqrt(4.0 * kappa * kappa / g1m2) + 1.0);
+  int ig2 = (int)(gmax * sqrt(4.0 * kappa * kappa / g2m2) + 1.0);
+  int ig3 = (int)(gmax * sqrt(4.0 * kappa * kappa / g3m2) + 1.0);
+  if (ig1 <= 1) ig1 = 2;
+  if (ig2 <= 1) ig2 = 2;
+  if (ig3 <= 1) ig3 = 2;
+  int il1 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r1m2)) + 1.0);
+  int il2 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r2m2)) + 1.0);
+  int il3 = (int)(rmax * sqrt(1.0 / (kappa * kappa * r3m2)) + 1.0);
+  if (il1 <= 1) il1 = 2;
+  if (il2 <= 1) il2 = 2;
+  if (il3 <= 1) il3 = 2;
+  if (s->icluster == 1) ig1 = ig2 = ig3 = 0;
+  for (int n1 = -ig1; n1 <= ig1; n1++)
+    for (int n2 = -ig2; n2 <= ig2; n2++)
+      for (int n3 = -ig3; n3 <= ig3; n3++) {
+        if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+        double g[3];
+        for (int k = 0; k < 3; k++) g[k] = n1 * g1[k] + n2 * g2[k] + n3 * g3[k];
+        double gm2 = pow(magnitude3(g), 2);
+        double stuff = 4.0 * pi * exp(-gm2 / (4.0 * kappa * kappa)) / (gm2 * volume);
+        for (int i = 0; i < N; i++)
+          for (int j = i; j < N; j++) {
+            double factor = j == i ? 0.5 * stuff : 1.0 * stuff, factorf = 2.0 * stuff;
+            double gdotb = g[0] * (RAT(s, i)[0] - RAT(s, j)[0]) + g[1] * (RAT(s, i)[1] - RAT(s, j)[1]) +
+                           g[2] * (RAT(s, i)[2] - RAT(s, j)[2]);
+            double qq = Q[i] * Q[j] - Q0[i] * Q0[j], sn = sin(gdotb);
+            for (int k = 0; k < 3; k++) {
+              fewald[3 * i + k] = fewald[3 * i + k] + qq * factorf * sn * g[k];
+              fewald[3 * j + k] = fewald[3 * j + k] - qq * factorf * sn * g[k];
+              dewald[((size_t)i * N + j) * 3 + k] = dewald[((size_t)i * N + j) * 3 + k] - factor * sn * g[k];
+              dewald[((size_t)j * N + i) * 3 + k] = dewald[((size_t)j * N + i) * 3 + k] + factor * sn * g[k];
+            }
+          }
+      }
+  if (s->icluster == 1) {
+    il1 = il2 = il3 = 0;
+    kappa = 0.0;
+  }
+  for (int n1 = -il1; n1 <= il1; n1++)
+    for (int n2 = -il2; n2 <= il2; n2++)
+      for (int n3 = -il3; n3 <= il3; n3++)
+        for (int i = 0; i < N; i++)
+          for (int j = i; j < N; j++) {
+            double factor = j == i ? 0.5 : 1.0, factorf = 2.0;
+            double cv[3];
+            for (int k = 0; k < 3; k++) cv[k] = n1 * a1[k] + n2 * a2[k] + n3 * a3[k];
+            for (int k = 0; k < 3; k++) cv[k] = cv[k] + RAT(s, i)[k] - RAT(s, j)[k];
+            double z = sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
+            if (z > 0.0001) {
+              double argument = kappa * z, qq = Q[i] * Q[j] - Q0[i] * Q0[j];
+              double F = (2.0 * exp(-argument * argument) * kappa * z / sqrt(pi) + erfc(argument)) / (z * z * z);
+              for (int k = 0; k < 3; k++) {
+                fewald[3 * i + k] = fewald[3 * i + k] + qq * factorf * cv[k] * F;
+                fewald[3 * j + k] = fewald[3 * j + k] - qq * factorf * cv[k] * F;
+                dewald[((size_t)i * N + j) * 3 + k] = dewald[((size_t)i * N + j) * 3 + k] - factor * cv[k] * F;
+                dewald[((size_t)j * N + i) * 3 + k] = dewald[((size_t)j * N + i) * 3 + k] + factor * cv[k] * F;
+              }
+            }
+          }
+  free(dq); free(Q); free(Q0);
+  return OK;
+}
+
+/* Dassemble_ewaldsr (:94-527): per pair fsr(3, pair) (atom and ontop terms,
+ * the self pair zero) and the three-center terms added into f3naa/b/c */
+int or_dassemble_ewaldsr(or_sys *s, const double *rho, const double *S, const double *dS, const double *dip,
+                         const double *ddip, double *fsr, double *f3naa, double *f3nab, double *f3nac) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double *dq = (double *)malloc(sizeof(double) * N);
+  atom_dq(s, dq);
+  for (int k = 0; k < 3 * s->npairs; k++) fsr[k] = 0.0;
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    long long os = s->blk_off[s->pair_off[i] + s->neigh_self[i]];
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p];
+      double r1[3], r2[3], z, eps[9], sig[3];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      if (z < 1.0e-05) sig[0] = 0.0, sig[1] = 0.0, sig[2] = 1.0;
+      else for (int k = 0; k < 3; k++) sig[k] = (r2[k] - r1[k]) / z;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      for (int inu = 0; inu < nmu; inu++)
+        for (int imu = 0; imu < nmu; imu++)
+          for (int k = 0; k < 3; k++)
+            fsr[3 * p + k] = fsr[3 * p + k] - P_eq2 * rho[os + imu + nmu * inu] * dq[j] *
+                                                  (S[os + imu + nmu * inu] / (z * z)) * sig[k];
+    }
+  }
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      double r1[3], r2[3], z, eps[9], sig[3];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      if (z < 1.0e-05) sig[0] = 0.0, sig[1] = 0.0, sig[2] = 1.0;
+      else for (int k = 0; k < 3; k++) sig[k] = (r2[k] - r1[k]) / z;
+      long long o = s->blk_off[p];
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          long long e = o + imu + nmu * inu;
+          double r = rho[e], sterm = S[e] / (2.0 * z), dterm = dip[e] / (z * z);
+          for (int k = 0; k < 3; k++) {
+            double spterm = dS[3 * e + k] / (2.0 * z), dpterm = ddip[3 * e + k] / (z * z);
+            fsr[3 * p + k] = fsr[3 * p + k] - P_eq2 * r * dq[i] * (spterm + dpterm) -
+                             P_eq2 * r * dq[i] * (sterm + 2.0 * dterm) * (sig[k] / z) -
+                             P_eq2 * r * dq[j] * (spterm - dpterm) -
+                             P_eq2 * r * dq[j] * (sterm - 2.0 * dterm) * (sig[k] / z);
+          }
+        }
+    }
+  }
+  for (int ia = 0; ia < N; ia++) {
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      long long o = s->blk_off[s->pair_off[g.iatom] + g.mneigh];
+      double d13 = distance3(g.rna, g.r1), d23 = distance3(g.rna, g.r2), rA1[3] = {0, 0, 0}, rA2[3] = {0, 0, 0};
+      if (d13 > 1.0e-05) for (int k = 0; k < 3; k++) rA1[k] = (g.rna[k] - g.r1[k]) / d13;
+      if (d23 > 1.0e-05) for (int k = 0; k < 3; k++) rA2[k] = (g.rna[k] - g.r2[k]) / d23;
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          long long e = o + imu + nmu * inu;
+          double r = rho[e], sterm = S[e] / 2.0, dterm = dip[e] / g.z;
+          for (int k = 0; k < 3; k++) {
+            double spterm = dS[3 * e + k] / 2.0;
+            double dpterm = ddip[3 * e + k] / g.z + dterm * g.sighat[k] / g.z;
+            double A = -dq[ia] * (sterm - dterm) * rA1[k] / (d13 * d13) - dq[ia] * (sterm + dterm) * rA2[k] / (d23 * d23);
+            double B = dq[ia] * (sterm - dterm) * rA1[k] / (d13 * d13) + dq[ia] * (spterm - dpterm) / d13 +
+                       dq[ia] * (spterm + dpterm) / d23;
+            A = -A;
+            B = -B;
+            double Cc = -A - B;
+            f3naa[3 * ia + k] = f3naa[3 * ia + k] - P_eq2 * r * A;
+            f3nab[3 * g.iatom + k] = f3nab[3 * g.iatom + k] - P_eq2 * r * B;
+            f3nac[3 * g.jatom + k] = f3nac[3 * g.jatom + k] - P_eq2 * r * Cc;
+          }
+        }
+    }
+  }
+  free(dq);
+  return OK;
+}
+
+/* Dassemble_ewaldlr (:553-837): flr(3, atom), with sum_ewald = ewald dQ and
+ * sum_dewald = dewald dQ (dewald from or_dassemble_ewald) */
+int or_dassemble_ewaldlr(or_sys *s, const double *rho, const double *ewald, const double *dewald, const double *S,
+                         const double *dS, const double *dip, const double *ddip, double *flr) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms;
+  double *dq = (double *)malloc(sizeof(double) * N), *se = (double *)calloc(N, sizeof(double)),
+         *sd = (double *)calloc(3 * (size_t)N, sizeof(double));
+  atom_dq(s, dq);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      se[i] = se[i] + dq[j] * ewald[(size_t)i * N + j];
+      for (int k = 0; k < 3; k++) sd[3 * i + k] = sd[3 * i + k] + dq[j] * dewald[((size_t)i * N + j) * 3 + k];
+    }
+  for (int k = 0; k < 3 * N; k++) flr[k] = 0.0;
+#define DEW(a, b, k) dewald[((size_t)(a) * N + (b)) * 3 + (k)]
+  for (int i = 0; i < N; i++) {
+    int nmu = fd->sp[s->imass[i]].norb_max;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], nnu = fd->sp[s->imass[j]].norb_max;
+      double r1[3], r2[3], z, eps[9], sig[3];
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      if (z < 1.0e-05) sig[0] = 0.0, sig[1] = 0.0, sig[2] = 1.0;
+      else for (int k = 0; k < 3; k++) sig[k] = (r2[k] - r1[k]) / z;
+      long long o = s->blk_off[p];
+      int self = i == j && s->neigh_b[p] == 0;
+      for (int inu = 0; inu < nnu; inu++)
+        for (int imu = 0; imu < nmu; imu++) {
+          long long e = o + imu + nmu * inu;
+          double r = rho[e], sterm = S[e] / 2.0, dterm = self ? 0.0 : dip[e] / z;
+          for (int k = 0; k < 3; k++) {
+            if (self) {
+              flr[3 * i + k] = flr[3 * i + k] - P_eq2 * r * sterm * sd[3 * i + k];
+              flr[3 * j + k] = flr[3 * j + k] - P_eq2 * r * sterm * sd[3 * j + k];
+            } else {
+              double spterm = dS[3 * e + k] / 2.0;
+              double dpterm = ddip[3 * e + k] / z + dip[e] * sig[k] / (z * z);
+              flr[3 * i + k] = flr[3 * i + k] - P_eq2 * r * (sterm - dterm) * sd[3 * i + k] -
+                               P_eq2 * r * (spterm - dpterm) * se[i] -
+                               P_eq2 * r * (sterm + dterm) * dq[i] * DEW(i, j, k) -
+                               P_eq2 * r * (spterm + dpterm) * se[j];
+              flr[3 * j + k] = flr[3 * j + k] - P_eq2 * r * (sterm - dterm) * dq[j] * DEW(j, i, k) +
+                               P_eq2 * r * (spterm - dpterm) * se[i] -
+                               P_eq2 * r * (sterm + dterm) * sd[3 * j + k] +
+                               P_eq2 * r * (spterm + dpterm) * se[j];
+            }
+          }
+          for (int ka = 0; ka < N; ka++) {
+            if (ka == i || ka == j) continue;
+            for (int k = 0; k < 3; k++)
+              flr[3 * ka + k] = flr[3 * ka + k] - r * dq[ka] * P_eq2 * (sterm - dterm) * DEW(ka, i, k) -
+                                r * dq[ka] * P_eq2 * (sterm + dterm) * DEW(ka, j, k);
+          }
+        }
+    }
+  }
+#undef DEW
+  free(dq); free(se); free(sd);
   return OK;
 }

@@ -98,6 +98,20 @@ int or_assemble_ewaldsr(or_sys *s, const double *S, const double *dip,
                         double *sr);
 int or_assemble_ewaldlr(or_sys *s, const double *ewald, const double *S,
                         const double *dip, double *lr);
+/* Ewald force pass (k.DASSEMBLERS/M_Dassemble_ewald_DOGS.f90): dewald
+ * ([(i * N + j) * 3 + c], derivative of ewald(i, j) in r_i) and the Ewald
+ * energy force; the ewaldsr pair forces (3 per pair) with the three-center
+ * terms added into f3naa/b/c; the ewaldlr atom forces.  rho is the density
+ * matrix, dS / ddip the overlap and dipole Dblocks */
+int or_dassemble_ewald(or_sys *s, double *dewald, double *fewald);
+int or_dassemble_ewaldsr(or_sys *s, const double *rho, const double *S,
+                         const double *dS, const double *dip,
+                         const double *ddip, double *fsr, double *f3naa,
+                         double *f3nab, double *f3nac);
+int or_dassemble_ewaldlr(or_sys *s, const double *rho, const double *ewald,
+                         const double *dewald, const double *S,
+                         const double *dS, const double *dip,
+                         const double *ddip, double *flr);
 /* DOGS force derivatives (k.DASSEMBLERS/M_Dassemble_2c_DOGS.f90,
  * M_Dassemble_3c_DOGS.f90): z-dipole Dblocks; vna ontop / atom pair terms;
  * f3na{a,b,c} (neutral + charged; overwrites) from S, dS, dip, ddip */

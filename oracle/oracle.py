@@ -61,6 +61,9 @@ def lib():
         L.or_dassemble_dipole_z.argtypes = [C.c_void_p, _dp]
         L.or_neighbors_pp.argtypes = [C.c_void_p]
         L.or_assemble_ewald.argtypes = [C.c_void_p, _dp]
+        L.or_dassemble_ewald.argtypes = [C.c_void_p, _dp, _dp]
+        L.or_dassemble_ewaldsr.argtypes = [C.c_void_p] + [_dp] * 9
+        L.or_dassemble_ewaldlr.argtypes = [C.c_void_p] + [_dp] * 8
         L.or_assemble_ewaldsr.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.or_assemble_ewaldlr.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_pp_sizes.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_longlong)] * 2
@@ -273,6 +276,37 @@ class System:
         _check(L.or_assemble_ewaldsr(self.h, S, dip, sr))
         _check(L.or_assemble_ewaldlr(self.h, ew, S, dip, lr))
         return ew.reshape(N, N), sr, lr
+
+    def dassemble_ewald(self, rho, dQ):
+        """DOGS Ewald force pass: dewald (N, N, 3), the Ewald energy force,
+        the ewaldsr pair forces (3 per pair) with their three-center part
+        (f3naa/b/c), the ewaldlr atom forces, and their build_forces
+        addition to ftot (-ewaldsr on i, + on j, + ewaldlr, + the f3na part)."""
+        L = lib()
+        N, nb, P = len(self.imass), self.nblock, self.npairs
+        ew, _, _ = self.assemble_ewald(dQ)
+        S, T, vb, vbo, dip = (np.zeros(nb) for _ in range(5))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        _check(L.or_assemble_dipole_z(self.h, dip))
+        rho = np.ascontiguousarray(rho, np.float64)
+        dS, dT, ddip = np.zeros(3 * nb), np.zeros(3 * nb), np.zeros(3 * nb)
+        _check(L.or_dassemble_2c(self.h, rho, dS, dT, np.zeros(3 * P), np.zeros(3 * P)))
+        _check(L.or_dassemble_dipole_z(self.h, ddip))
+        dew, few = np.zeros(3 * N * N), np.zeros(3 * N)
+        _check(L.or_dassemble_ewald(self.h, dew, few))
+        fsr = np.zeros(3 * P)
+        fa, fb, fc = np.zeros(3 * N), np.zeros(3 * N), np.zeros(3 * N)
+        _check(L.or_dassemble_ewaldsr(self.h, rho, S, dS, dip, ddip, fsr, fa, fb, fc))
+        flr = np.zeros(3 * N)
+        _check(L.or_dassemble_ewaldlr(self.h, rho, np.ascontiguousarray(ew.ravel()), dew, S, dS, dip, ddip, flr))
+        add = (flr + fa + fb + fc).reshape(N, 3)
+        fs = fsr.reshape(P, 3)
+        for i in range(N):
+            for p in range(self.pair_off[i], self.pair_off[i + 1]):
+                add[i] -= fs[p]
+                add[self.neigh_j[p]] += fs[p]
+        return dict(ewald=ew, dewald=dew.reshape(N, N, 3), fewald=few, ewaldsr=fsr, f3na_add=(fa, fb, fc),
+                    ewaldlr=flr, ftot_add=add.ravel())
 
     # ---- non-local pseudopotential (vnl) --------------------------------
     def neighbors_pp(self):

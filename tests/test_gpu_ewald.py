@@ -55,6 +55,36 @@ def test_ewald_matches_oracle(ctx, fdata_root, name):
         assert np.abs(ctx.blocks("ewaldlr") - lr).max() <= TOL
 
 
+@pytest.mark.parametrize("name", ["sic_small", "sic_vac", "cho_small", "sic_cluster"])
+def test_ewald_forces_match_oracle(ctx, fdata_root, name):
+    from conftest import symmetric_denmat
+    path, nZ, st = case(fdata_root, name)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
+    norb = np.array([fd.norb(int(q)) for q in st.imass])
+    rho, cape = symmetric_denmat(s, norb, 5)
+    dq = np.random.default_rng(2).uniform(-0.3, 0.3, (len(st.imass), 3))
+    ref = s.dassemble_ewald(rho, dq)
+    dogs = s.dassemble_dogs(rho, cape, dq)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice, st.icluster)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_DOGS)
+    ctx.set_charges(dq)
+    ctx.set_denmat(rho, cape)
+    what = fbgpu.FB_ALL | fbgpu.FB_EWALD
+    ctx.assemble(what)
+    ctx.Dassemble(what)
+    assert np.abs(ctx.forces("ewald") - ref["fewald"]).max() <= TOL
+    assert np.abs(ctx.forces("ewaldsr") - ref["ewaldsr"]).max() <= TOL
+    assert np.abs(ctx.forces("ewaldlr") - ref["ewaldlr"]).max() <= TOL
+    want = dogs["ftot"] + ref["ftot_add"]
+    assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+    for _ in range(2):  # value and force pass as one graph
+        ctx.assemble_graph(what | fbgpu.FB_FORCES)
+        assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+
+
 def test_ewald_errors(ctx, fdata_root):
     path, nZ, st = case(fdata_root, "sic_small")
     ctx.read_Fdata(path, nZ)

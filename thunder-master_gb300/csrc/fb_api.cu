@@ -96,6 +96,7 @@ struct fb_ctx {
   int ew_ng = 0, ew_nl = 0;
   double ew_kappa = 0.0;
   DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs;
+  DevBuf d_q0a, d_dewald, d_ew_w, d_sum_dewald, d_ew_cw, d_fewald, d_fsr, d_flr;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -1237,6 +1238,21 @@ static EwaldArgs ewald_args(fb_ctx *ctx) {
   e.dip = ctx->d_dip.as<double>();
   e.sr = ctx->d_ewsr.as<double>();
   e.lr = ctx->d_ewlr.as<double>();
+  e.dogs_ps = ctx->d_dogs_ps.as<double>();
+  e.q0a = ctx->d_q0a.as<double>();
+  e.dewald = ctx->d_dewald.as<double>();
+  e.w = ctx->d_ew_w.as<double>();
+  e.sum_dewald = ctx->d_sum_dewald.as<double>();
+  e.cw = ctx->d_ew_cw.as<double>();
+  e.fewald = ctx->d_fewald.as<double>();
+  e.fsr = ctx->d_fsr.as<double>();
+  e.flr = ctx->d_flr.as<double>();
+  e.f3naa = ctx->d_f3a.as<double>();
+  e.f3nab = ctx->d_f3b.as<double>();
+  e.f3nac = ctx->d_f3c.as<double>();
+  e.ftot = ctx->d_ftot.as<double>();
+  e.pair_owner = ctx->d_pair_owner.as<int>();
+  e.P = ctx->P;
   return e;
 }
 
@@ -1509,7 +1525,7 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
 
 // device storage of the force pass (allocations happen here, never while
 // a graph is being captured)
-static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
+static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = false) {
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   if ((what & FB_ALL) && !ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
   if (what & (FB_VNL2C | FB_VNL3C)) {
@@ -1544,7 +1560,19 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what) {
   if ((what & FB_VNA3C) && (use_df(ctx) || mlp_routes(ctx)))
     CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, true));
-  if (dogs && (what & FB_VNA3C)) CHK(ctx->d_dogs_ps.ensure((size_t)8 * P * sizeof(double) + 8));
+  if (dogs && (what & (FB_VNA3C | FB_EWALD))) CHK(ctx->d_dogs_ps.ensure((size_t)8 * P * sizeof(double) + 8));
+  if (what & FB_EWALD) {
+    if (!dogs) return fail(ctx, FB_ERR_STATE, "Ewald forces: the DOGS theory (fb_set_theory) first");
+    if (!ctx->have_ewald && !(graph_values && (what & FB_EWALD)))
+      return fail(ctx, FB_ERR_STATE, "Ewald forces read the Ewald matrix: assemble FB_EWALD first");
+    size_t n = (size_t)N;
+    CHK(ctx->d_q0a.ensure(n * sizeof(double) + 8));
+    CHK(ctx->d_dewald.ensure(3 * n * n * sizeof(double) + 8));
+    CHK(ctx->d_ew_w.ensure(n * sizeof(double) + 8));
+    DevBuf *b3[] = {&ctx->d_sum_dewald, &ctx->d_ew_cw, &ctx->d_fewald, &ctx->d_flr};
+    for (DevBuf *b : b3) CHK(b->ensure(3 * n * sizeof(double) + 8));
+    CHK(ctx->d_fsr.ensure((size_t)3 * P * sizeof(double) + 8));
+  }
   return FB_OK;
 }
 
@@ -1562,9 +1590,18 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
   AsmArgs a = asm_args(ctx);
   a.keep_dblocks = (what & FB_KEEP_DBLOCKS) != 0;
   unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
-  // DOGS: the 2c kernel also leaves the per-pair sums the 3c kernel reads
-  if (a.dogs && (what & FB_VNA3C)) w2 |= 8u;
+  // DOGS: the 2c kernel also leaves the per-pair sums the 3c and Ewald kernels read
+  if (a.dogs && (what & (FB_VNA3C | FB_EWALD))) w2 |= 8u;
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
+  if (what & FB_EWALD) {
+    // Dassemble_ewald (dewald, the Ewald energy force, the katom sums) and
+    // the ewaldsr three-center terms into f3na, before build_forces sums them
+    EwaldArgs e = ewald_args(ctx);
+    CU(cudaMemsetAsync(ctx->d_ew_w.p, 0, (size_t)N * sizeof(double), ctx->stream));
+    KL(KT_EWALD, launch_dewald(e, ctx->stream));
+    ctx->launches += e.ng > 0 ? 4 : 3;
+    KL(KT_EWALD_BLOCKS, launch_ewald_f3c(e, ctx->stream));
+  }
   if (what & FB_VNA3C) {
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
     AsmArgs at = a;
@@ -1602,13 +1639,20 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     KL(KT_VNLF, launch_pp_forces(pa, ctx->npp, ctx->nppx, ctx->stream));
     ctx->launches++;  // two kernels
   }
+  if (what & FB_EWALD) {
+    // Dassemble_ewaldsr / ewaldlr pair and atom forces and their
+    // build_forces terms, added into ftot
+    EwaldArgs e = ewald_args(ctx);
+    KL(KT_EWALD_BLOCKS, launch_ewald_forces(e, ctx->stream));
+    ctx->launches++;
+  }
   return FB_OK;
 }
 
 static void dassemble_done(fb_ctx *ctx, unsigned what) {
   bool keep = (what & FB_KEEP_DBLOCKS) != 0;
   ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
-  ctx->dassembled = what & (FB_ALL | FB_VNL2C | FB_VNL3C);
+  ctx->dassembled = what & (FB_ALL | FB_VNL2C | FB_VNL3C | FB_EWALD);
 }
 
 int fb_dassemble(fb_ctx *ctx, unsigned what) {
@@ -1690,7 +1734,7 @@ int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   CU(cudaSetDevice(ctx->device));
   if (what & vals) CHK(check_assemble(ctx, what));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, (what & FB_FORCES) != 0));
-  if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what));
+  if (what & FB_FORCES) CHK(prepare_dassemble(ctx, what, true));
   if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   bool fresh = ctx->gexec && ctx->g_what == what && ctx->g_theory == ctx->theory && ctx->g_prec == ctx->prec &&
                ctx->g_npp == ctx->npp && ctx->g_nppx == ctx->nppx && ctx->g_nppp == ctx->nppp &&
@@ -1862,9 +1906,14 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out) {
     case FB_F_F3NLC: b = &ctx->d_f3nlc; break;
     case FB_F_VNL_ATOM: b = &ctx->d_vnl_atom; n = (size_t)3 * ctx->npp; break;
     case FB_F_VNL_ONTOP: b = &ctx->d_vnl_ontop; n = (size_t)3 * ctx->nppx; break;
+    case FB_F_EWALDSR: b = &ctx->d_fsr; n = (size_t)3 * ctx->P; break;
+    case FB_F_EWALDLR: b = &ctx->d_flr; break;
+    case FB_F_EWALD: b = &ctx->d_fewald; break;
     default: return fail(ctx, FB_ERR_ARG, "unknown force array %d", which);
   }
-  if (which >= FB_F_VNL && !(ctx->dassembled & (FB_VNL2C | FB_VNL3C)))
+  if (which >= FB_F_EWALDSR && !(ctx->dassembled & FB_EWALD))
+    return fail(ctx, FB_ERR_STATE, "Ewald forces: fb_dassemble with FB_EWALD first");
+  if (which >= FB_F_VNL && which <= FB_F_VNL_ONTOP && !(ctx->dassembled & (FB_VNL2C | FB_VNL3C)))
     return fail(ctx, FB_ERR_STATE, "vnl forces: fb_dassemble with FB_VNL2C / FB_VNL3C first");
   CU(cudaMemcpyAsync(out, b->p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));

@@ -195,7 +195,331 @@ __global__ void k_atom_dq(EwaldArgs e) {
   e.dqa[i] = s;
 }
 
+// ---------------------------------------------------------------------------
+// force pass (k.DASSEMBLERS/M_Dassemble_ewald_DOGS.f90)
+// ---------------------------------------------------------------------------
+// Dassemble_ewald (:878-1236): dewald(:, i, j) = d ewald(i, j) / d r_i =
+// - sum_g stuff g sin(g . (r_i - r_j)) - sum_L c (2 exp(-kappa^2 z^2) kappa z
+// / sqrt(pi) + erfc(kappa z)) / z^3, c = L + r_i - r_j; dewald(:, j, i) =
+// -dewald(:, i, j); the diagonal is zero.  sin(g . (r_i - r_j)) = s_i c_j -
+// c_i s_j from the structure-factor tables; the same kappa z > 5.5 cut as
+// the matrix.
+__global__ void __launch_bounds__(256) k_dewald_tiles(EwaldArgs e) {
+  __shared__ double Ci[32][33], Si[32][33], Cj[32][33], Sj[32][33], W[3][32];
+  int nb = (e.N + 31) / 32;
+  int t = blockIdx.x, bi = 0;
+  while (t >= nb - bi) {
+    t -= nb - bi;
+    bi++;
+  }
+  int bj = bi + t;
+  int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  int j = bj * 32 + tx;
+  double acc[4][3];
+#pragma unroll
+  for (int q = 0; q < 4; q++) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
+  for (int k0 = 0; k0 < e.ng; k0 += 32) {
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      int ii = bi * 32 + r, jj = bj * 32 + r, k = k0 + tx;
+      bool kv = k < e.ng;
+      Ci[r][tx] = (kv && ii < e.N) ? e.sfc[(long long)ii * e.ng + k] : 0.0;
+      Si[r][tx] = (kv && ii < e.N) ? e.sfs[(long long)ii * e.ng + k] : 0.0;
+      Cj[r][tx] = (kv && jj < e.N) ? e.sfc[(long long)jj * e.ng + k] : 0.0;
+      Sj[r][tx] = (kv && jj < e.N) ? e.sfs[(long long)jj * e.ng + k] : 0.0;
+    }
+    if (ty < 3) W[ty][tx] = (k0 + tx < e.ng) ? e.stuff[k0 + tx] * e.gvec[3 * (k0 + tx) + ty] : 0.0;
+    __syncthreads();
+#pragma unroll 2
+    for (int k = 0; k < 32; k++) {
+      double cj = Cj[tx][k], sj = Sj[tx][k], w0 = W[0][k], w1 = W[1][k], w2 = W[2][k];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        int r = ty + 8 * q;
+        double sn = fma(Si[r][k], cj, -Ci[r][k] * sj);  // sin(g . (r_i - r_j))
+        acc[q][0] = fma(-w0, sn, acc[q][0]);
+        acc[q][1] = fma(-w1, sn, acc[q][1]);
+        acc[q][2] = fma(-w2, sn, acc[q][2]);
+      }
+    }
+  }
+  if (j >= e.N) return;
+  double rcut2 = e.kappa > 0.0 ? (5.5 / e.kappa) * (5.5 / e.kappa) : 1.0e300;
+  const double rpi = 1.0 / sqrt(3.141592653589793238462643);
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    int i = bi * 32 + ty + 8 * q;
+    if (i >= e.N || (bi == bj && j < i)) continue;
+    double v[3] = {acc[q][0], acc[q][1], acc[q][2]};
+    if (i == j) {
+      v[0] = v[1] = v[2] = 0.0;
+    } else {
+      double d[3] = {e.ratom[3 * i] - e.ratom[3 * j], e.ratom[3 * i + 1] - e.ratom[3 * j + 1],
+                     e.ratom[3 * i + 2] - e.ratom[3 * j + 2]};
+      for (int k = 0; k < e.nl; k++) {
+        const double *L = e.lvec + 3 * k;
+        double c0 = L[0] + d[0], c1 = L[1] + d[1], c2 = L[2] + d[2];
+        double z2 = c0 * c0 + c1 * c1 + c2 * c2;
+        if (z2 > rcut2) continue;
+        double z = sqrt(z2);
+        if (z > 0.0001) {
+          double x = e.kappa * z;
+          double F = (2.0 * exp(-x * x) * x * rpi + erfc(x)) / (z2 * z);
+          v[0] -= c0 * F;
+          v[1] -= c1 * F;
+          v[2] -= c2 * F;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      e.dewald[((long long)i * e.N + j) * 3 + c] = v[c];
+      e.dewald[((long long)j * e.N + i) * 3 + c] = -v[c];
+    }
+  }
+}
+
+// per-pair weights of the ewaldlr katom term (:805-834): A = S/2 - dip/z
+// (dip term zero on the self pair) on iatom, B = S/2 + dip/z on jatom,
+// rho-contracted through the pair sums
+__global__ void k_ewald_w(EwaldArgs e) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= e.N) return;
+  const double *X = e.xl + (long long)e.sid[i] * XL_STRIDE;
+  double ri[3] = {e.ratom[3 * i], e.ratom[3 * i + 1], e.ratom[3 * i + 2]};
+  double wi = 0.0;
+  for (int p = e.pair_off[i] + lane; p < e.pair_off[i + 1]; p += 32) {
+    int j = e.neigh_j[p], mb = e.neigh_b[p];
+    const double *ps = e.dogs_ps + 8 * (long long)p;
+    double dt = 0.0;
+    if (!(i == j && mb == 0)) {
+      double r2[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) r2[k] = e.ratom[3 * j + k] + X[3 * mb + k];
+      dt = ps[1] / dist_rn(ri, r2);
+    }
+    wi += 0.5 * ps[0] - dt;
+    atomicAdd(e.w + j, 0.5 * ps[0] + dt);
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) wi += __shfl_xor_sync(0xffffffffu, wi, d);
+  if (lane == 0) atomicAdd(e.w + i, wi);
+}
+
+// one warp per row k: sum_dewald(:, k) = dewald(:, k, :) dQ, the katom sum
+// cw(:, k) = dewald(:, k, :) w, and the Ewald energy force
+// fewald(k) = -2 (Q_k sum_j Q_j dewald(:, k, j) - Q0_k sum_j Q0_j dewald(:, k, j))
+__global__ void k_ewald_rowsums(EwaldArgs e) {
+  int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (k >= e.N) return;
+  double sd[3] = {0, 0, 0}, sw[3] = {0, 0, 0}, sq[3] = {0, 0, 0}, s0[3] = {0, 0, 0};
+  for (int j = lane; j < e.N; j += 32) {
+    const double *D = e.dewald + ((long long)k * e.N + j) * 3;
+    double dq = e.dqa[j], q0 = e.q0a[j], wj = e.w[j];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double v = D[c];
+      sd[c] = fma(dq, v, sd[c]);
+      sw[c] = fma(wj, v, sw[c]);
+      sq[c] = fma(q0 + dq, v, sq[c]);
+      s0[c] = fma(q0, v, s0[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      sd[c] += __shfl_xor_sync(0xffffffffu, sd[c], d);
+      sw[c] += __shfl_xor_sync(0xffffffffu, sw[c], d);
+      sq[c] += __shfl_xor_sync(0xffffffffu, sq[c], d);
+      s0[c] += __shfl_xor_sync(0xffffffffu, s0[c], d);
+    }
+  if (lane == 0) {
+    double q0 = e.q0a[k], q = q0 + e.dqa[k];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      e.sum_dewald[3 * k + c] = sd[c];
+      e.cw[3 * k + c] = sw[c];
+      e.fewald[3 * k + c] = -2.0 * (q * sq[c] - q0 * s0[c]);
+      // the katom term of ewaldlr over every atom (the direct terms of the
+      // reference's iatom / jatom equal the two it leaves out of the loop)
+      e.flr[3 * k + c] = -P_eq2 * e.dqa[k] * sw[c];
+    }
+  }
+}
+
+// Dassemble_ewaldsr two-center terms (:150-300) per pair, and the
+// pair-local ewaldlr terms (:660-790); one warp per atom, lanes over pairs
+__global__ void k_ewald_f2c(EwaldArgs e) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= e.N) return;
+  const double *X = e.xl + (long long)e.sid[i] * XL_STRIDE;
+  double ri[3] = {e.ratom[3 * i], e.ratom[3 * i + 1], e.ratom[3 * i + 2]};
+  int pself = e.pair_off[i] + e.neigh_self[i];
+  double sself = e.dogs_ps[8 * (long long)pself];
+  double qi = e.dqa[i], sei = e.sum_ewald[i];
+  double fi[3] = {0, 0, 0};
+  for (int p = e.pair_off[i] + lane; p < e.pair_off[i + 1]; p += 32) {
+    int j = e.neigh_j[p], mb = e.neigh_b[p];
+    const double *ps = e.dogs_ps + 8 * (long long)p;
+    bool self = (i == j && mb == 0);
+    double sS = ps[0], sD = ps[1];
+    double fs[3] = {0, 0, 0}, fj[3] = {0, 0, 0};
+    double qj = e.dqa[j], sej = e.sum_ewald[j];
+    if (self) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) fi[c] -= P_eq2 * sS * e.sum_dewald[3 * i + c];  // two halves of 0.5 S
+    } else {
+      double r2[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) r2[k] = e.ratom[3 * j + k] + X[3 * mb + k];
+      double z = dist_rn(ri, r2), iz = 1.0 / z;
+      double sig[3];
+      if (z < 1.0e-05) {
+        sig[0] = 0.0;
+        sig[1] = 0.0;
+        sig[2] = 1.0;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) sig[k] = (r2[k] - ri[k]) * iz;
+      }
+      double A = 0.5 * sS - sD * iz, B = 0.5 * sS + sD * iz;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double sdS = ps[2 + c], sdD = ps[5 + c];
+        // ewaldsr: atom term, then ontop (:175, :270-290)
+        fs[c] = -P_eq2 * qj * (sself * iz * iz) * sig[c];
+        fs[c] -= P_eq2 * qi * (sdS / (2.0 * z) + sdD * iz * iz) + P_eq2 * qi * (sS / (2.0 * z) + 2.0 * sD * iz * iz) * (sig[c] * iz) +
+                 P_eq2 * qj * (sdS / (2.0 * z) - sdD * iz * iz) + P_eq2 * qj * (sS / (2.0 * z) - 2.0 * sD * iz * iz) * (sig[c] * iz);
+        // ewaldlr pair-local terms
+        double spt = 0.5 * sdS, dpt = sdD * iz + sD * sig[c] * iz * iz;
+        fi[c] -= P_eq2 * (A * e.sum_dewald[3 * i + c] + (spt - dpt) * sei + (spt + dpt) * sej);
+        fj[c] = -P_eq2 * (B * e.sum_dewald[3 * j + c] - (spt - dpt) * sei - (spt + dpt) * sej);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) atomicAdd(e.flr + 3 * j + c, fj[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) e.fsr[3 * (long long)p + c] = fs[c];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double v = fi[c];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    if (lane == 0) atomicAdd(e.flr + 3 * i + c, v);
+  }
+}
+
+// Dassemble_ewaldsr three-center terms (:305-520) into f3naa / f3nab /
+// f3nac, one thread per common-neighbor triplet
+__global__ void k_ewald_f3c_kernel(EwaldArgs e) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.T) return;
+  int ia = e.trip_alpha[t], iat = e.ci_j[t], jat = e.cj_j[t];
+  const double *X = e.xl + (long long)e.sid[ia] * XL_STRIDE;
+  int ib = e.ci_b[t], jb = e.cj_b[t];
+  double r1[3], r2[3], rna[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r1[k] = e.ratom[3 * iat + k] + X[3 * ib + k];
+    r2[k] = e.ratom[3 * jat + k] + X[3 * jb + k];
+    rna[k] = e.ratom[3 * ia + k];
+  }
+  double z = dist_rn(r1, r2), d13 = dist_rn(rna, r1), d23 = dist_rn(rna, r2);
+  double sig[3], rA1[3], rA2[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    sig[k] = z < 1.0e-05 ? (k == 2 ? 1.0 : 0.0) : (r2[k] - r1[k]) / z;
+    rA1[k] = d13 > 1.0e-05 ? (rna[k] - r1[k]) / d13 : 0.0;
+    rA2[k] = d23 > 1.0e-05 ? (rna[k] - r2[k]) / d23 : 0.0;
+  }
+  const double *ps = e.dogs_ps + 8 * (long long)e.tdst[t];
+  double qa = e.dqa[ia], st = 0.5 * ps[0], dt = ps[1] / z;
+  double i13 = 1.0 / (d13 * d13), i23 = 1.0 / (d23 * d23);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double spt = 0.5 * ps[2 + c], dpt = ps[5 + c] / z + dt * sig[c] / z;
+    double A = qa * ((st - dt) * rA1[c] * i13 + (st + dt) * rA2[c] * i23);
+    double B = -qa * ((st - dt) * rA1[c] * i13 + (spt - dpt) / d13 + (spt + dpt) / d23);
+    double C = -A - B;
+    atomicAdd(e.f3naa + 3 * ia + c, -P_eq2 * A);
+    atomicAdd(e.f3nab + 3 * iat + c, -P_eq2 * B);
+    atomicAdd(e.f3nac + 3 * jat + c, -P_eq2 * C);
+  }
+}
+
+// build_forces Ewald terms (M_build_forces.f90:367-386): ftot(i) -= ewaldsr,
+// ftot(j) += ewaldsr per pair, ftot += ewaldlr per atom
+__global__ void k_ewald_ftot(EwaldArgs e) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= e.N) return;
+  double fi[3] = {0, 0, 0};
+  for (int p = e.pair_off[i] + lane; p < e.pair_off[i + 1]; p += 32) {
+    int j = e.neigh_j[p];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double v = e.fsr[3 * (long long)p + c];
+      fi[c] -= v;
+      atomicAdd(e.ftot + 3 * j + c, v);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double v = fi[c];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    if (lane == 0) atomicAdd(e.ftot + 3 * i + c, v + e.flr[3 * i + c]);
+  }
+}
+
+// Q0 of each atom
+__global__ void k_atom_q0(EwaldArgs e) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e.N) return;
+  e.q0a[i] = e.fd->sp[e.isp[i]].q0;
+}
+
 }  // namespace
+
+int launch_dewald(const EwaldArgs &e, cudaStream_t s) {
+  if (e.ng > 0) {
+    long long n = (long long)e.N * e.ng;
+    k_ewald_sf<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e);
+    FB_LAUNCH_CHECK();
+  }
+  long long nb = (e.N + 31) / 32;
+  k_dewald_tiles<<<(unsigned)(nb * (nb + 1) / 2), 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  k_atom_q0<<<(e.N + 255) / 256, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  unsigned wg = (unsigned)(((long long)e.N * 32 + 255) / 256);
+  k_ewald_w<<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  k_ewald_rowsums<<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_ewald_f3c(const EwaldArgs &e, cudaStream_t s) {
+  if (e.T == 0) return 0;
+  k_ewald_f3c_kernel<<<(e.T + 255) / 256, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_ewald_forces(const EwaldArgs &e, cudaStream_t s) {
+  unsigned wg = (unsigned)(((long long)e.N * 32 + 255) / 256);
+  k_ewald_f2c<<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  k_ewald_ftot<<<wg, 256, 0, s>>>(e);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s) {
   if (e.ng > 0) {

@@ -30,9 +30,22 @@ struct EwaldArgs {
   double *ewald, *sum_ewald;
   const double *S, *dip;
   double *sr, *lr;
+  // force pass: per pair rho sums (S, dip, dS, ddip; 8 per pair), Q0 per
+  // atom, dewald [(i * N + j) * 3 + c], per-atom weights and sums, forces
+  const double *dogs_ps;
+  double *q0a, *dewald, *w, *sum_dewald, *cw, *fewald, *fsr, *flr;
+  double *f3naa, *f3nab, *f3nac, *ftot;
+  const int *pair_owner;
+  int P;
 };
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s);
 int launch_ewald_blocks(const EwaldArgs &e, int have_d, cudaStream_t s);
+// force pass: dewald and the Ewald energy force; the ewaldsr three-center
+// terms into f3na (before build_forces); the ewaldsr / ewaldlr forces added
+// into ftot (after build_forces)
+int launch_dewald(const EwaldArgs &e, cudaStream_t s);
+int launch_ewald_f3c(const EwaldArgs &e, cudaStream_t s);
+int launch_ewald_forces(const EwaldArgs &e, cudaStream_t s);
 
 }  // namespace fb

@@ -190,6 +190,8 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
       t.skip();
       if (!read_dbls(t, 1, &ae)) goto bad_info;
       t.skip();
+      sp.q0 = 0.0;
+      for (int k = 0; k < sp.nssh; k++) sp.q0 += q[k];
       sp.rcA = -99.0;
       sp.rcmin = 99.0;
       sp.norb = 0;
@@ -553,6 +555,7 @@ info_done:
     out.dev.sp[k].pp_pattern = sh.pattern_pp();
     out.dev.sp[k].norb_pp = sh.norb_pp;
     out.dev.sp[k].rc_pp = sh.rc_pp;
+    out.dev.sp[k].q0 = sh.q0;
     int o = 0;
     for (int q = 0; q < sh.nssh_pp && o < 9; q++)
       for (int m = 0; m < 2 * sh.lpp[q] + 1 && o < 9; m++) out.dev.sp[k].cl[o++] = sh.cl_pp[q];

@@ -13,6 +13,7 @@ struct SpeciesHost {
   double rcmin = 99.0;
   int lpp[8] = {0};
   double rc_pp = 0.0;
+  double q0 = 0.0;  // sum of the shells' Qneutral
   double cl_pp[8] = {0};
   int norb_pp = 0;
   // projector shells as a basis pattern: s, sp or spd, else -1

@@ -148,6 +148,7 @@ struct SpeciesDev {
   int pp_pattern, norb_pp;
   double rc_pp;
   double cl[9];
+  double q0;     // sum of the shells' Qneutral
 };
 
 // One 2c interaction cell (T_Fdata_cell_2c, e.FDATA/M_Fdata_2c.f90:83-96).

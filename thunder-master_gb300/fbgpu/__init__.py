@@ -56,7 +56,8 @@ BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape"
          "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12, "ewaldsr": 13, "ewaldlr": 14}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8,
-         "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14}
+         "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14,
+         "ewaldsr": 15, "ewaldlr": 16, "ewald": 17}
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
           6: "ATOMS_CLOSE", 7: "NEIGH_SELF", 8: "NEIGH_BACK", 9: "CUDA", 10: "WATCHDOG",
           11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED"}
@@ -543,7 +544,7 @@ class Context:
         self._check(self.L.fb_dassemble(self.h, what | (FB_KEEP_DBLOCKS if keep_dblocks else 0)))
 
     def forces(self, which):
-        n = 3 * {"vna_ontop": self.npairs, "vna_atom": self.npairs}.get(which, self.natoms)
+        n = 3 * {"vna_ontop": self.npairs, "vna_atom": self.npairs, "ewaldsr": self.npairs}.get(which, self.natoms)
         if which == "vnl_atom":
             n = 3 * self.npp
         elif which == "vnl_ontop":
