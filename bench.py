@@ -557,6 +557,17 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
     torch.cuda.synchronize()
     out["ewald"] = {"what": "DOGS Ewald: N x N matrix (reciprocal + screened lattice sums), ewaldsr, ewaldlr",
                     "ms": round(e0.elapsed_time(e1) / args.steps, 4)}
+    ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+    ctx.Dassemble(fbgpu.FB_EWALD)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.Dassemble(fbgpu.FB_EWALD)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["ewald"]["force_ms"] = round(e0.elapsed_time(e1) / args.steps, 4)
+    out["ewald"]["force_what"] = ("dewald + Ewald energy force, ewaldsr (pair + three-center) and ewaldlr forces, "
+                                  "build_forces terms")
     ew_gpu = ctx.ewald()
     sr_gpu, lr_gpu = ctx.blocks("ewaldsr"), ctx.blocks("ewaldlr")
     # agreement with the oracle and the oracle's single-core time
