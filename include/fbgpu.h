@@ -81,6 +81,10 @@ extern "C" {
 #define FB_VNL3C 512u        /* vnl 3c (assemble_vnl_3c, M_assemble_PP_3c.f90:94); fb_dassemble: the vnl forces */
 #define FB_EWALD 1024u       /* DOGS Ewald: the matrix (assemble_ewald) and the ewaldsr / ewaldlr blocks
                                 (M_assemble_ewald_DOGS.f90:98, :404, :633) */
+#define FB_VXC 2048u         /* McWEDA exchange-correlation, Harris (assemble_vxc,
+                                M_assemble_vxc_McWEDA_Harris.f90:102): the input densities
+                                (M_assemble_rho_McWEDA_Harris.f90) and the vxc blocks; reads the
+                                overlap (FB_S in the same or an earlier call) */
 #define FB_DIPOLE 64u        /* z-dipole blocks (assemble_dipole_z, M_assemble_2c_DOGS.f90:376-499);
                                 with FB_THEORY_DOGS, FB_VNA2C computes them and FB_S as well */
 
@@ -100,6 +104,12 @@ extern "C" {
 #define FB_BLOCK_RHO_PP 12 /* s%denmat_PP(i)%neighbors(k)%block (input, PPp pairs) */
 #define FB_BLOCK_EWALDSR 13 /* s%ewaldsr(i)%neighbors(k)%block (FB_EWALD) */
 #define FB_BLOCK_EWALDLR 14 /* s%ewaldlr(i)%neighbors(k)%block (FB_EWALD) */
+#define FB_BLOCK_VXC 15       /* s%vxc(i)%neighbors(k)%block (FB_VXC) */
+#define FB_BLOCK_RHO_IN 16    /* s%rho_in(i)%neighbors(k)%block (FB_VXC) */
+#define FB_BLOCK_RHO_BOND 17  /* s%rho_bond(i)%neighbors(k)%block (FB_VXC) */
+#define FB_BLOCK_WRHO_IN 18   /* s%rho_in_weighted(i)%neighbors(k)%block, nssh_i x nssh_j: 9 doubles
+                                 per pair, (issh, jssh) at [9 p + issh + nssh_i jssh] (FB_VXC) */
+#define FB_BLOCK_WRHO_BOND 19 /* s%rho_bond_weighted(i)%neighbors(k)%block, same layout (FB_VXC) */
 
 /* force arrays for fb_get_forces */
 #define FB_F_TOT 0         /* ftot: kinetic + vna + f3na(a+b+c) - pulay */

@@ -105,6 +105,11 @@ typedef struct {
   int lssh_PP[MAXSH], norb_PP_max;
   double rcutoff_PP, cl_PP[MAXSH];
   double Q0; /* sum of the shells' Qneutral */
+  double qn[MAXSH]; /* Qneutral per shell */
+  /* one-center McWEDA xc (e.FDATA/M_Fdata_1c_McWEDA_Harris.f90:58-61):
+   * E(issh, jssh), V(issh, jssh) at [issh * MAXSH + jssh], 0-based */
+  int have_vxc1c;
+  double vxc1c_E[MAXSH * MAXSH], vxc1c_V[MAXSH * MAXSH];
 } species_t;
 
 struct or_fdata {
@@ -283,7 +288,7 @@ static int read_info(or_fdata *fd, const char *dir, const int *nZreq) {
     if (read_dbls(&t, 1, &rcpp)) goto bad;
     s->rcutoff_PP = rcpp; /* :1147, used as read (M_neighbors_PP.f90:469) */
     s->Q0 = 0.0;
-    for (int i = 0; i < nssh; i++) s->Q0 = s->Q0 + qn[i];
+    for (int i = 0; i < nssh; i++) s->Q0 = s->Q0 + qn[i], s->qn[i] = qn[i];
     s->norb_PP_max = 0;   /* :1188-1194 */
     for (int i = 0; i < s->nssh_PP; i++) {
       if (lpp[i] < 0 || lpp[i] > 2) { seterr("unsupported PP l=%d", lpp[i]); txt_close(&t); return E_UNSUP; }
@@ -476,6 +481,30 @@ static int read_fdata_3c(or_fdata *fd, const char *dir) {
   return OK;
 }
 
+/* read_Fdata_1c (e.FDATA/M_Fdata_1c_McWEDA_Harris.f90:99-136): vxc_1c.ZZ.dat
+ * holds nssh records of E(issh, :) then nssh records of V(issh, :).  The
+ * file is optional here: only the McWEDA assembler reads it. */
+static int read_fdata_1c(or_fdata *fd, const char *dir) {
+  for (int k = 1; k <= fd->nspecies; k++) {
+    species_t *sp = &fd->sp[k];
+    char path[1024];
+    txt t;
+    snprintf(path, sizeof path, "%s/vxc_1c.%02d.dat", dir, sp->nZ);
+    sp->have_vxc1c = 0;
+    FILE *f = fopen(path, "rb");
+    if (!f) continue;
+    fclose(f);
+    if (txt_open(&t, path)) return E_IO;
+    int n = sp->nssh, bad = 0;
+    for (int a = 0; a < n && !bad; a++) bad = read_dbls(&t, n, &sp->vxc1c_E[a * MAXSH]);
+    for (int a = 0; a < n && !bad; a++) bad = read_dbls(&t, n, &sp->vxc1c_V[a * MAXSH]);
+    txt_close(&t);
+    if (bad) { seterr("parse error in %s", path); return E_IO; }
+    sp->have_vxc1c = 1;
+  }
+  return OK;
+}
+
 or_fdata *or_load_fdata(const char *dir, int nspecies, const int *nZ, char *err, int errlen) {
   if (nspecies < 1 || nspecies > MAXSP) {
     if (err) snprintf(err, (size_t)errlen, "nspecies out of range");
@@ -486,6 +515,7 @@ or_fdata *or_load_fdata(const char *dir, int nspecies, const int *nZ, char *err,
   int st = read_info(fd, dir, nZ);
   if (!st) st = read_fdata_2c(fd, dir);
   if (!st) st = read_fdata_3c(fd, dir);
+  if (!st) st = read_fdata_1c(fd, dir);
   if (st) {
     if (err) snprintf(err, (size_t)errlen, "%s", g_err);
     or_free_fdata(fd);
@@ -3098,4 +3128,308 @@ int or_dassemble_ewaldlr(or_sys *s, const double *rho, const double *ewald, cons
 #undef DEW
   free(dq); free(se); free(sd);
   return OK;
+}
+
+/* ======================================================================== */
+/* McWEDA exchange-correlation, Harris (PRB 71, 235101 (2005)):             */
+/* j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90 (input densities) and      */
+/* j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90 (the vxc blocks).          */
+/* Orbital blocks use the pair layout (blk_off); the shell-level weighted   */
+/* densities use 9 doubles per pair, element (issh, jssh) at                */
+/* [9 p + issh + nssh_i jssh] (column-major nssh_i x nssh_j).               */
+/* ======================================================================== */
+#define P_vxc_ontop 7
+#define P_rho_ontopL 15
+#define P_rho_ontopR 16
+#define P_rho_atom 17
+#define P_rhoS_ontopL 19
+#define P_rhoS_ontopR 20
+#define P_rhoS_atom 21
+#define P_rho_3c 1
+#define P_rhoS_3c 2
+#define P_Hartree (P_eq2 / P_abohr) /* include/constants.h:5 */
+#define WSH 9                       /* doubles per pair of a shell-level block */
+
+/* lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:56-190):
+ * out = exc, muxc, dexc, d2exc, dmuxc, d2muxc.  The low-density branch's
+ * d2dec keeps the reference's (dden*3) factor (:143-144). */
+void or_lda_ceperley_alder(double rh, double *out) {
+  const double delta_rh = 1.0e-6;
+  double exc, muxc, dexc, d2exc, dmuxc, d2muxc;
+  double dec, ddec, d2dec, den, dden, d2den, d3den, ex, rho_third, rho, rhx, rs, rsl, sqrs;
+  double d2nec, d2nex, d3nec, d3nex;
+  rhx = sqrt(rh * rh + delta_rh);
+  rho = rhx * (P_abohr * P_abohr * P_abohr);
+  rho_third = pow(rho, 1.0 / 3.0);
+  rs = 0.62035049 / rho_third;
+  if (rho < 0.23873241) {
+    sqrs = sqrt(rs);
+    den = 1.0 + 1.0529 * sqrs + 0.3334 * rs;
+    exc = -0.4581652 / rs - 0.1423 / den;
+    muxc = exc - rs * (0.15273333 / (rs * rs) + (0.02497128 / sqrs + 0.01581427) / (den * den));
+    dden = 1.0529 / (2.0 * sqrs) + 0.3334;
+    d2den = (-0.5) * 1.0529 / (2.0 * rs * sqrs);
+    d3den = (0.75) * 1.0529 / (2.0 * (rs * rs) * sqrs);
+    dec = 0.1423 * dden / (den * den);
+    ddec = -2.0 * 0.1423 * dden * dden / (den * den * den) + 0.1423 * d2den / (den * den);
+    d2dec = 6.0 * 0.1423 * (dden * 3) / (den * den * den * den) - 6.0 * 0.1423 * dden * d2den / (den * den * den) +
+            0.1423 * d3den / (den * den);
+  } else {
+    rsl = log(rs);
+    exc = -0.4581652 / rs - 0.0480 + 0.0311 * rsl - 0.0116 * rs + 0.002 * rs * rsl;
+    muxc = exc - rs * (0.15273333 / (rs * rs) + 0.01036667 / rs - 0.003866667 + 0.00066667 * (1.0 + rsl));
+    dec = 0.0311 / rs - 0.0116 + 0.0020 * (rsl + 1.0);
+    ddec = -0.0311 / (rs * rs) + 0.0020 / rs;
+    d2dec = 2.0 * 0.0311 / (rs * rs * rs) - 0.0020 / (rs * rs);
+  }
+  ex = -0.7385587664 * rho_third;
+  dexc = (muxc - exc) / rho;
+  d2nec = (4.0 * rs / (9.0 * rho * rho)) * dec + (rs * rs / (9.0 * rho * rho)) * ddec;
+  d2nex = -(2.0 / (9.0 * rho * rho)) * ex;
+  dmuxc = 2.0 * dexc + rho * (d2nex + d2nec);
+  d3nec = (-28.0 * rs / (27.0 * rho * rho * rho)) * dec + (-4.0 * rs * rs / (9.0 * rho * rho * rho)) * ddec +
+          ((rs * rs * rs) / (-27.0 * rho * rho * rho)) * d2dec;
+  d3nex = (10.0 / (27.0 * rho * rho * rho)) * ex;
+  d2muxc = 3.0 * (d2nex + d2nec) + rho * (d3nex + d3nec);
+  d2exc = d2nex + d2nec;
+  {
+    const double a3 = P_abohr * P_abohr * P_abohr, a6 = a3 * a3;
+    out[0] = exc * P_Hartree;
+    out[1] = muxc * P_Hartree;
+    out[2] = dexc * P_Hartree * a3;
+    out[3] = d2exc * P_Hartree * a6;
+    out[4] = dmuxc * P_Hartree * a3;
+    out[5] = d2muxc * P_Hartree * a6;
+  }
+}
+
+/* assemble_rho_2c (:81-276) and assemble_rho_weighted_2c (:427-622) of
+ * M_assemble_rho_McWEDA_Harris.f90: rho_in = rho_bond = sum over the shells
+ * of both atoms of Qneutral * <i|rho_shell|j> (ontop left + right) for
+ * i != j; into the self block sum over every neighbor j of the atom case
+ * <i|rho_shell(j)|i> rotated with (in1, in1), rho_bond taking only the self
+ * pair's term.  The weighted (shell-level) densities follow the same
+ * pattern without rotations. */
+int or_assemble_rho_2c(or_sys *s, double *rho_in, double *rho_bond, double *wrho_in, double *wrho_bond) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
+  for (int i = 0; i < N; i++) {
+    double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, ni = fd->sp[in1].nssh, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j], nnu = fd->sp[in2].norb_max;
+      int nj = fd->sp[in2].nssh;
+      long long o = s->blk_off[p];
+      for (int k = 0; k < nmu * nnu; k++) rho_in[o + k] = 0.0, rho_bond[o + k] = 0.0;
+      for (int k = 0; k < WSH; k++) wrho_in[WSH * p + k] = 0.0, wrho_bond[WSH * p + k] = 0.0;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      for (int isorp = 1; isorp <= ni; isorp++) { /* :189-200 */
+        double Q = fd->sp[in1].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rho_ontopL, isorp, z, nmu, nnu, mm))) { err = st; break; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        for (int k = 0; k < nmu * nnu; k++) rho_in[o + k] = rho_in[o + k] + xm[k] * Q;
+        for (int k = 0; k < nmu * nnu; k++) rho_bond[o + k] = rho_bond[o + k] + xm[k] * Q;
+      }
+      for (int isorp = 1; isorp <= nj; isorp++) { /* :206-217 */
+        double Q = fd->sp[in2].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rho_ontopR, isorp, z, nmu, nnu, mm))) { err = st; break; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        for (int k = 0; k < nmu * nnu; k++) rho_in[o + k] = rho_in[o + k] + xm[k] * Q;
+        for (int k = 0; k < nmu * nnu; k++) rho_bond[o + k] = rho_bond[o + k] + xm[k] * Q;
+      }
+      for (int isorp = 1; isorp <= ni; isorp++) { /* weighted :528-539 */
+        double Q = fd->sp[in1].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rhoS_ontopL, isorp, z, ni, nj, mm))) { err = st; break; }
+        for (int k = 0; k < ni * nj; k++) wrho_in[WSH * p + k] = wrho_in[WSH * p + k] + mm[k] * Q;
+        for (int k = 0; k < ni * nj; k++) wrho_bond[WSH * p + k] = wrho_bond[WSH * p + k] + mm[k] * Q;
+      }
+      for (int isorp = 1; isorp <= nj; isorp++) { /* :544-554 */
+        double Q = fd->sp[in2].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rhoS_ontopR, isorp, z, ni, nj, mm))) { err = st; break; }
+        for (int k = 0; k < ni * nj; k++) wrho_in[WSH * p + k] = wrho_in[WSH * p + k] + mm[k] * Q;
+        for (int k = 0; k < ni * nj; k++) wrho_bond[WSH * p + k] = wrho_bond[WSH * p + k] + mm[k] * Q;
+      }
+    }
+    /* self block: the atom case (:222-276, :560-621) */
+    int ps = s->pair_off[i] + s->neigh_self[i];
+    long long os = s->blk_off[ps];
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      int self = (i == j && s->neigh_b[p] == 0);
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      for (int isorp = 1; isorp <= fd->sp[in2].nssh; isorp++) {
+        double Q = fd->sp[in2].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rho_atom, isorp, z, nmu, nmu, mm))) { err = st; break; }
+        or_rotate(fd, in1, in1, eps, nmu, nmu, mm, xm);
+        for (int k = 0; k < nmu * nmu; k++) rho_in[os + k] = rho_in[os + k] + xm[k] * Q;
+        if (self)
+          for (int k = 0; k < nmu * nmu; k++) rho_bond[os + k] = rho_bond[os + k] + xm[k] * Q;
+      }
+      for (int isorp = 1; isorp <= fd->sp[in2].nssh; isorp++) {
+        double Q = fd->sp[in2].qn[isorp - 1];
+        if ((st = or_getMEs_2c(fd, in1, in2, P_rhoS_atom, isorp, z, ni, ni, mm))) { err = st; break; }
+        for (int k = 0; k < ni * ni; k++) wrho_in[WSH * ps + k] = wrho_in[WSH * ps + k] + mm[k] * Q;
+        if (self)
+          for (int k = 0; k < ni * ni; k++) wrho_bond[WSH * ps + k] = wrho_bond[WSH * ps + k] + mm[k] * Q;
+      }
+    }
+  }
+  return err;
+}
+
+/* assemble_rho_3c (:298-403) and assemble_rho_weighted_3c (:645-741):
+ * rho_in(iatom, mneigh) += sum over the shells of ialpha of Qneutral *
+ * rotate(den3), and the weighted density += Qneutral * denS3 (no rotation).
+ * Accumulates onto the 2c values. */
+int or_assemble_rho_3c(or_sys *s, double *rho_in, double *wrho_in) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+  /* serial over ialpha: the triplets of different ialpha write the same
+   * pair blocks */
+  for (int ia = 0; ia < N; ia++) {
+    double mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1]; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      int ni = fd->sp[g.in1].nssh, nj = fd->sp[g.in2].nssh, st;
+      int p = s->pair_off[g.iatom] + g.mneigh;
+      long long o = s->blk_off[p];
+      for (int isorp = 1; isorp <= fd->sp[g.indna].nssh; isorp++) {
+        double Q = fd->sp[g.indna].qn[isorp - 1];
+        st = or_getMEs_3c(fd, g.in1, g.in2, g.indna, P_rho_3c, isorp, g.x, g.z, nmu, nnu, g.cost, mm);
+        if (st) { err = st; break; }
+        or_rotate(fd, g.in1, g.in2, g.eps, nmu, nnu, mm, xm);
+        for (int k = 0; k < nmu * nnu; k++) rho_in[o + k] = rho_in[o + k] + xm[k] * Q;
+      }
+      for (int isorp = 1; isorp <= fd->sp[g.indna].nssh; isorp++) {
+        double Q = fd->sp[g.indna].qn[isorp - 1];
+        st = or_getMEs_3c(fd, g.in1, g.in2, g.indna, P_rhoS_3c, isorp, g.x, g.z, ni, nj, g.cost, mm);
+        if (st) { err = st; break; }
+        for (int k = 0; k < ni * nj; k++) wrho_in[WSH * p + k] = wrho_in[WSH * p + k] + mm[k] * Q;
+      }
+    }
+  }
+  return err;
+}
+
+/* orbital imu (0-based) of species sp: its shell, l and m
+ * (c.SYSTEM/M_species.f90:1196-1208) */
+static void orb_of(const species_t *sp, int imu, int *issh, int *l, int *m) {
+  int n = 0;
+  for (int a = 0; a < sp->nssh; a++) {
+    int w = 2 * sp->lssh[a] + 1;
+    if (imu < n + w) { *issh = a; *l = sp->lssh[a]; *m = imu - n - sp->lssh[a]; return; }
+    n += w;
+  }
+  *issh = -1; *l = -1; *m = 0;
+}
+
+/* assemble_vxc (M_assemble_vxc_McWEDA_Harris.f90:102-191): vxc = vxc_bond +
+ * vxc_SN - vxc_SN_bond, with assemble_vxc_SN (:212-486), the generalized
+ * Sankey-Niklewski terms at the weighted densities, and assemble_vxc_bond
+ * (:507-640), the one-center V for the self block and the rotated
+ * vxc_ontop table otherwise.  The optional outputs take vxc_SN,
+ * vxc_SN_bond and vxc_bond. */
+int or_assemble_vxc(or_sys *s, const double *S, const double *rho_in, const double *rho_bond,
+                    const double *wrho_in, const double *wrho_bond, double *vxc, double *sn, double *snb,
+                    double *bond) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, err = OK;
+  for (int k = 1; k <= fd->nspecies; k++)
+    if (!fd->sp[k].have_vxc1c) { seterr("no vxc_1c.%02d.dat", fd->sp[k].nZ); return E_TABLE; }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(g_threads) if (g_threads > 1)
+  for (int i = 0; i < N; i++) {
+    double r1[3], r2[3], z, eps[9], mm[MAXORB * MAXORB], xm[MAXORB * MAXORB];
+    double vsn[MAXORB * MAXORB], vsnb[MAXORB * MAXORB], vb[MAXORB * MAXORB];
+    double lin[6], lbo[6];
+    const species_t *A = &fd->sp[s->imass[i]];
+    int in1 = s->imass[i], nmu = A->norb_max, ni = A->nssh, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      const species_t *B = &fd->sp[in2];
+      int nnu = B->norb_max;
+      long long o = s->blk_off[p];
+      const double *Wi = wrho_in + WSH * p, *Wb = wrho_bond + WSH * p;
+      for (int k = 0; k < nmu * nnu; k++) vsn[k] = 0.0, vsnb[k] = 0.0, vb[k] = 0.0;
+      if (!(i == j && s->neigh_b[p] == 0)) {
+        /* off-site SN (:286-357) */
+        int n1 = 0;
+        for (int a = 0; a < ni; a++) {
+          int l1 = A->lssh[a];
+          n1 = n1 + l1 + 1;
+          int n2 = 0;
+          for (int b = 0; b < B->nssh; b++) {
+            int l2 = B->lssh[b];
+            n2 = n2 + l2 + 1;
+            double wi = Wi[a + ni * b], wb = Wb[a + ni * b];
+            or_lda_ceperley_alder(wi, lin);
+            or_lda_ceperley_alder(wb, lbo);
+            for (int m1 = -l1; m1 <= l1; m1++)
+              for (int m2 = -l2; m2 <= l2; m2++) {
+                int imu = n1 + m1 - 1, inu = n2 + m2 - 1, q = imu + nmu * inu;
+                double ov = S[o + q], ri = rho_in[o + q], rb = rho_bond[o + q];
+                vsn[q] = lin[1] * ov + lin[4] * (ri - wi * ov);
+                vsnb[q] = lbo[1] * ov + lbo[4] * (rb - wb * ov);
+              }
+            n2 = n2 + l2;
+          }
+          n1 = n1 + l1;
+        }
+        /* vxc_bond ontop (:612-627) */
+        pair_frame(s, i, p, r1, r2, &z, eps);
+        if ((st = or_getMEs_2c(fd, in1, in2, P_vxc_ontop, 0, z, nmu, nnu, mm))) { err = st; continue; }
+        or_rotate(fd, in1, in2, eps, nmu, nnu, mm, xm);
+        for (int k = 0; k < nmu * nnu; k++) vb[k] = xm[k];
+      } else {
+        /* on-site SN (:365-480) */
+        int n1 = 0;
+        for (int a = 0; a < ni; a++) {
+          int l1 = A->lssh[a];
+          n1 = n1 + l1 + 1;
+          double wi = Wi[a + ni * a], wb = Wb[a + ni * a];
+          or_lda_ceperley_alder(wi, lin);
+          or_lda_ceperley_alder(wb, lbo);
+          for (int m1 = -l1; m1 <= l1; m1++) {
+            int imu = n1 + m1 - 1, q = imu + nmu * imu;
+            vsn[q] = lin[1] + lin[4] * (rho_in[o + q] - wi);
+            vsnb[q] = lbo[1] + lbo[4] * (rho_bond[o + q] - wb);
+          }
+          int n2 = 0;
+          for (int b = 0; b < ni; b++) {
+            int l2 = A->lssh[b];
+            n2 = n2 + l2 + 1;
+            double wi2 = Wi[a + ni * b], wb2 = Wb[a + ni * b];
+            or_lda_ceperley_alder(wi2, lin);
+            or_lda_ceperley_alder(wb2, lbo);
+            for (int m1 = -l1; m1 <= l1; m1++)
+              for (int m2 = -l2; m2 <= l2; m2++) {
+                int imu = n1 + m1 - 1, inu = n2 + m2 - 1, q = imu + nmu * inu;
+                if (imu != inu) {
+                  vsn[q] = lin[4] * rho_in[o + q];
+                  vsnb[q] = lbo[4] * rho_bond[o + q];
+                }
+              }
+            n2 = n2 + l2;
+          }
+          n1 = n1 + l1;
+        }
+        /* vxc_bond on-site: V(issh, jssh) where l and m agree (:590-605) */
+        for (int inu = 0; inu < nmu; inu++)
+          for (int imu = 0; imu < nmu; imu++) {
+            int sa, la, ma, sb, lb, mb;
+            orb_of(A, imu, &sa, &la, &ma);
+            orb_of(A, inu, &sb, &lb, &mb);
+            if (la == lb && ma == mb) vb[imu + nmu * inu] = A->vxc1c_V[sa * MAXSH + sb];
+          }
+      }
+      for (int k = 0; k < nmu * nnu; k++) vxc[o + k] = vb[k] + vsn[k] - vsnb[k];
+      if (sn) for (int k = 0; k < nmu * nnu; k++) sn[o + k] = vsn[k];
+      if (snb) for (int k = 0; k < nmu * nnu; k++) snb[o + k] = vsnb[k];
+      if (bond) for (int k = 0; k < nmu * nnu; k++) bond[o + k] = vb[k];
+    }
+  }
+  return err;
 }

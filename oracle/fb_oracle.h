@@ -150,6 +150,23 @@ int or_build_forces_vnl(or_sys *s, const double *vnl_atom,
                         const double *f3nlb, const double *f3nlc, double *vnl,
                         double *ftot_add);
 
+/* McWEDA exchange-correlation, Harris (M_assemble_rho_McWEDA_Harris.f90,
+ * M_assemble_vxc_McWEDA_Harris.f90): the Ceperley-Alder LDA (out = exc,
+ * muxc, dexc, d2exc, dmuxc, d2muxc); the input densities rho_in / rho_bond
+ * (orbital blocks) and their shell-level weighted forms (9 doubles per pair,
+ * (issh, jssh) at [9 p + issh + nssh_i jssh]), 2c part (overwrites) and 3c
+ * part (accumulates onto rho_in and wrho_in); the vxc blocks from the
+ * overlap S and those densities (sn, snb, bond optional: vxc_SN,
+ * vxc_SN_bond, vxc_bond). */
+void or_lda_ceperley_alder(double rh, double *out);
+int or_assemble_rho_2c(or_sys *s, double *rho_in, double *rho_bond,
+                       double *wrho_in, double *wrho_bond);
+int or_assemble_rho_3c(or_sys *s, double *rho_in, double *wrho_in);
+int or_assemble_vxc(or_sys *s, const double *S, const double *rho_in,
+                    const double *rho_bond, const double *wrho_in,
+                    const double *wrho_bond, double *vxc, double *sn,
+                    double *snb, double *bond);
+
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */
 int or_getMEs_2c(or_fdata *fd, int isp, int jsp, int iint, int isub, double x,

@@ -81,6 +81,10 @@ def lib():
         L.or_build_forces_vnl.argtypes = [C.c_void_p] + [_dp] * 7
         L.or_dassemble_vna_2c_dogs.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.or_dassemble_vna_3c_dogs.argtypes = [C.c_void_p] + [_dp] * 8
+        L.or_lda_ceperley_alder.argtypes = [C.c_double, _dp]
+        L.or_assemble_rho_2c.argtypes = [C.c_void_p] + [_dp] * 4
+        L.or_assemble_rho_3c.argtypes = [C.c_void_p] + [_dp] * 2
+        L.or_assemble_vxc.argtypes = [C.c_void_p] + [_dp] * 6 + [C.c_void_p] * 3
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
         L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     _dp, _dp]
@@ -308,6 +312,33 @@ class System:
         return dict(ewald=ew, dewald=dew.reshape(N, N, 3), fewald=few, ewaldsr=fsr, f3na_add=(fa, fb, fc),
                     ewaldlr=flr, ftot_add=add.ravel())
 
+    # ---- McWEDA exchange-correlation (Harris) ---------------------------
+    def assemble_vxc(self, with3c=True, parts=False):
+        """McWEDA value pass: returns dict(S, rho_in, rho_bond, wrho_in,
+        wrho_bond, vxc) and with parts also vxc_SN, vxc_SN_bond, vxc_bond.
+        Weighted densities: (npairs, 9), element (issh, jssh) at
+        issh + nssh_i * jssh."""
+        L = lib()
+        L.or_set_threads(self.threads)
+        nb, P = self.nblock, self.npairs
+        S, T, vb, vbo = (np.zeros(nb) for _ in range(4))
+        _check(L.or_assemble_2c(self.h, S, T, vb, vbo))
+        ri, rb, wi, wb = np.zeros(nb), np.zeros(nb), np.zeros(9 * max(P, 1)), np.zeros(9 * max(P, 1))
+        _check(L.or_assemble_rho_2c(self.h, ri, rb, wi, wb))
+        if with3c:
+            _check(L.or_assemble_rho_3c(self.h, ri, wi))
+        vxc = np.zeros(nb)
+        out = dict(S=S, rho_in=ri, rho_bond=rb, wrho_in=wi.reshape(-1, 9)[:P], wrho_bond=wb.reshape(-1, 9)[:P],
+                   vxc=vxc)
+        if parts:
+            sn, snb, bond = np.zeros(nb), np.zeros(nb), np.zeros(nb)
+            _check(L.or_assemble_vxc(self.h, S, ri, rb, wi, wb, vxc, sn.ctypes.data, snb.ctypes.data,
+                                     bond.ctypes.data))
+            out.update(vxc_SN=sn, vxc_SN_bond=snb, vxc_bond=bond)
+        else:
+            _check(L.or_assemble_vxc(self.h, S, ri, rb, wi, wb, vxc, None, None, None))
+        return out
+
     # ---- non-local pseudopotential (vnl) --------------------------------
     def neighbors_pp(self):
         """driver_neighbors_PP: PP, PPx and PPp maps (0-based) and the PP
@@ -395,6 +426,13 @@ def getDMEs_3c(fd, isp, jsp, ksp, x, y, cost, nmu, nnu, iint=3, isub=0):
     _check(lib().or_getDMEs_3c(fd.h, isp, jsp, ksp, iint, isub, float(x), float(y), nmu, nnu, float(cost),
                                h, dp, dx, dy))
     return tuple(a.reshape(nnu, nmu).T for a in (h, dp, dx, dy))
+
+
+def lda_ceperley_alder(rh):
+    """(exc, muxc, dexc, d2exc, dmuxc, d2muxc) of lda_ceperley_alder."""
+    out = np.zeros(6)
+    lib().or_lda_ceperley_alder(float(rh), out)
+    return out
 
 
 def epsilon(r1, r2):

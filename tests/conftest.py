@@ -26,12 +26,13 @@ def fdata_root():
     return root
 
 
-def workload(name, root, dogs=False):
+def workload(name, root, dogs=False, vxc=False):
     """(fdata dir, nZ list, Structure) of a named synthetic workload; dogs:
-    the Fdata set with the DOGS charged-shell sub-cells and z-dipole table."""
+    the Fdata set with the DOGS charged-shell sub-cells and z-dipole table;
+    vxc: the one with the McWEDA exchange-correlation tables."""
     path = synth.fdata_dir_for(name if name in ("si64", "si512", "cho1536", "sic4096") else
                                {"cho_small": "cho1536", "sic_small": "sic4096", "si_vac": "si64",
-                                "sic_vac": "sic4096"}[name], root=root, dogs=dogs)
+                                "sic_vac": "sic4096"}[name], root=root, dogs=dogs, vxc=vxc)
     if name in ("si64", "si512", "cho1536", "sic4096"):
         st = synth.structure_for(name)
         nZ = [s.nZ for s in synth.species_for(name)]

@@ -1,0 +1,96 @@
+"""The McWEDA exchange-correlation value pass on the GPU (fb_assemble with
+FB_VXC) against the oracle's restatement of assemble_vxc
+(j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90) and the input densities
+(j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90): the vxc, rho_in and
+rho_bond blocks and the shell-level weighted densities to 1e-10 per element
+on cells of one and two species, with s-only hydrogen, vacancies and a
+cluster, plain and as one graph; the call-order and table errors."""
+import numpy as np
+import pytest
+
+import fbgpu
+from conftest import workload
+from fbgpu import synth
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = fbgpu.Context(0)
+    yield c
+    c.close()
+
+
+def case(fdata_root, name):
+    if name == "sic_cluster":
+        path, nZ, _ = workload("sic_small", fdata_root, vxc=True)
+        st = synth.diamond((1, 1, 1), 4.36, 0.1, 41, sp_a=1, sp_b=2, name="SiC8cluster")
+        st.icluster = 1
+        return path, [14, 6], st
+    return workload(name, fdata_root, vxc=True)
+
+
+def _check(ctx, ref, P):
+    assert np.abs(ctx.blocks("rho_in") - ref["rho_in"]).max() <= TOL
+    assert np.abs(ctx.blocks("rho_bond") - ref["rho_bond"]).max() <= TOL
+    assert np.abs(ctx.blocks("wrho_in").reshape(P, 9) - ref["wrho_in"]).max() <= TOL
+    assert np.abs(ctx.blocks("wrho_bond").reshape(P, 9) - ref["wrho_bond"]).max() <= TOL
+    assert np.abs(ctx.blocks("vxc") - ref["vxc"]).max() <= TOL
+
+
+@pytest.mark.parametrize("name", ["si64", "sic_small", "cho_small", "si_vac", "sic_vac", "sic_cluster"])
+def test_vxc_matches_oracle(ctx, fdata_root, name):
+    path, nZ, st = case(fdata_root, name)
+    s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
+    ref = s.assemble_vxc()
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice, st.icluster)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    what = fbgpu.FB_ALL | fbgpu.FB_VXC
+    ctx.assemble(what)
+    assert np.abs(ctx.blocks("S") - ref["S"]).max() <= TOL
+    _check(ctx, ref, s.npairs)
+    for _ in range(2):  # as one graph, captured then replayed
+        ctx.assemble_graph(what)
+        _check(ctx, ref, s.npairs)
+
+
+def test_vxc_after_overlap(ctx, fdata_root):
+    """FB_VXC alone reads the overlap of an earlier call."""
+    path, nZ, st = case(fdata_root, "sic_small")
+    s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice).neighbors()
+    ref = s.assemble_vxc()
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    ctx.assemble(fbgpu.FB_S)
+    ctx.assemble(fbgpu.FB_VXC)
+    _check(ctx, ref, s.npairs)
+
+
+def test_vxc_errors(ctx, fdata_root):
+    path, nZ, st = case(fdata_root, "sic_small")
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    with pytest.raises(fbgpu.FBError) as e:      # the overlap first
+        ctx.assemble(fbgpu.FB_VXC)
+    assert e.value.code == 11
+    ctx.set_theory(fbgpu.FB_THEORY_DOGS)
+    with pytest.raises(fbgpu.FBError) as e:      # McWEDA Harris only
+        ctx.assemble(fbgpu.FB_S | fbgpu.FB_VXC)
+    assert e.value.code == 13
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    plain, nZ2, st2 = workload("sic_small", fdata_root)  # no McWEDA tables
+    ctx.read_Fdata(plain, nZ2)
+    ctx.set_structure(st2.ratom, st2.imass, st2.lattice)
+    ctx.driver_neighbors()
+    with pytest.raises(fbgpu.FBError) as e:
+        ctx.assemble(fbgpu.FB_S | fbgpu.FB_VXC)
+    assert e.value.code == 3

@@ -1,0 +1,171 @@
+"""The oracle's restatement of the McWEDA exchange-correlation value pass
+(j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90,
+j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90,
+g.XC_FUNCTIONALS/lda_ceperley_alder.f90).
+
+The Ceperley-Alder functional is pinned to the published Perdew-Zunger
+parameterisation (an independent restatement below) and to its own
+derivative identities by central differences; the assembled densities and
+vxc blocks are checked for the symmetries the synthetic tables carry
+(Hermitian across neigh_back), for the structure of the formulas (rho_bond
+is rho_in without the three-center and the neighbors' atom terms; vxc =
+vxc_bond + vxc_SN - vxc_SN_bond), and for both branches of the functional
+being reached on the test systems."""
+import numpy as np
+import pytest
+
+from conftest import workload
+from oracle import oracle as orc
+
+P_ABOHR = 0.529177
+P_HARTREE = 14.39975 / P_ABOHR
+
+
+def pz81_exc(rs):
+    """Exchange + correlation energy per electron (Hartree) of the
+    Perdew-Zunger fit to Ceperley-Alder (PRB 23, 5048 (1981), Table XII)."""
+    ex = -0.4581652 / rs
+    if rs >= 1.0:
+        ec = -0.1423 / (1.0 + 1.0529 * np.sqrt(rs) + 0.3334 * rs)
+    else:
+        ec = -0.0480 + 0.0311 * np.log(rs) - 0.0116 * rs + 0.0020 * rs * np.log(rs)
+    return ex + ec
+
+
+def _rh_of_rs(rs):
+    """Density in 1/A^3 whose smoothed value sqrt(rh^2 + 1e-6) has radius rs."""
+    rho_au = 3.0 / (4.0 * np.pi * rs ** 3)
+    rhx = rho_au / P_ABOHR ** 3
+    return np.sqrt(rhx * rhx - 1.0e-6)
+
+
+@pytest.mark.parametrize("rs", [0.4, 0.8, 1.5, 3.0, 6.0])
+def test_lda_matches_published_fit(rs):
+    exc = orc.lda_ceperley_alder(_rh_of_rs(rs))[0]
+    assert abs(exc - pz81_exc(rs) * P_HARTREE) < 2e-6 * abs(exc)
+
+
+@pytest.mark.parametrize("rh", [0.02, 0.3, 1.2, 2.5, 8.0])
+def test_lda_derivative_identities(rh):
+    h = 1e-5 * rh
+    f = orc.lda_ceperley_alder
+    exc, muxc, dexc, d2exc, dmuxc, d2muxc = f(rh)
+    rhx = np.sqrt(rh * rh + 1e-6)
+    # muxc = d(rho exc)/d rho and dmuxc = d muxc / d rho, rho = sqrt(rh^2 + 1e-6)
+    drhx = np.sqrt((rh + h) ** 2 + 1e-6) - np.sqrt((rh - h) ** 2 + 1e-6)
+    fp, fm = f(rh + h), f(rh - h)
+    n_p, n_m = np.sqrt((rh + h) ** 2 + 1e-6), np.sqrt((rh - h) ** 2 + 1e-6)
+    # the fit's constants are rounded (0.15273333 for 0.4581652 / 3), so the
+    # identities hold to about 2e-5 (muxc) and 1e-4 (dmuxc, d2muxc)
+    assert abs((n_p * fp[0] - n_m * fm[0]) / drhx - muxc) < 5e-5 * abs(muxc)
+    assert abs((fp[1] - fm[1]) / drhx - dmuxc) < 2e-4 * abs(dmuxc)
+    assert abs(dexc - (muxc - exc) / rhx) < 1e-12 * abs(dexc)
+    # d2muxc = d dmuxc / d rho holds in the high-density branch; in the low
+    # density one the reference's d2dec carries (dden*3) where the
+    # derivative has dden**3, which the restatement keeps
+    fd2 = (fp[4] - fm[4]) / drhx
+    rho_au = rhx * P_ABOHR ** 3
+    if rho_au >= 0.23873241:
+        assert abs(fd2 - d2muxc) < 3e-4 * abs(d2muxc)
+    else:
+        assert abs(fd2 - d2muxc) > 1e-2 * abs(d2muxc)
+
+
+def _system(fdata_root, name):
+    path, nZ, st = workload(name, fdata_root, vxc=True)
+    fd = orc.Fdata(path, nZ)
+    return st, orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+
+
+@pytest.fixture(scope="module", params=["si64", "sic_small", "cho_small"])
+def vxc_case(request, fdata_root):
+    st, s = _system(fdata_root, request.param)
+    r3 = s.assemble_vxc(with3c=True, parts=True)
+    r2 = s.assemble_vxc(with3c=False)
+    return request.param, st, s, r3, r2
+
+
+def _norb(s, st):
+    return [s.fd.norb(int(k)) for k in st.imass]
+
+
+def _nssh(st, name):
+    # shells per species of the synthetic sets: Si, C, O sp; H s
+    return [1 if (name == "cho_small" and k == 2) else 2 for k in st.imass]
+
+
+def test_blocks_are_hermitian(vxc_case):
+    name, st, s, r, _ = vxc_case
+    norb, nsh = _norb(s, st), _nssh(st, name)
+    for key in ("S", "rho_in", "rho_bond", "vxc"):
+        x = r[key]
+        worst = 0.0
+        for i in range(len(st.imass)):
+            for p in range(s.pair_off[i], s.pair_off[i + 1]):
+                j = s.neigh_j[p]
+                q = s.pair_off[j] + s.neigh_back[p]
+                a = x[s.blk_off[p]:s.blk_off[p + 1]].reshape(norb[j], norb[i]).T
+                b = x[s.blk_off[q]:s.blk_off[q + 1]].reshape(norb[i], norb[j]).T
+                worst = max(worst, np.abs(a - b.T).max())
+        assert worst < 1e-12 * max(1.0, np.abs(x).max()), key
+    for key in ("wrho_in", "wrho_bond"):
+        w = r[key]
+        for i in range(len(st.imass)):
+            for p in range(s.pair_off[i], s.pair_off[i + 1]):
+                j = s.neigh_j[p]
+                q = s.pair_off[j] + s.neigh_back[p]
+                a = w[p][:nsh[i] * nsh[j]].reshape(nsh[j], nsh[i]).T
+                b = w[q][:nsh[i] * nsh[j]].reshape(nsh[i], nsh[j]).T
+                assert np.abs(a - b.T).max() < 1e-13
+                assert np.all(w[p][nsh[i] * nsh[j]:] == 0.0)
+
+
+def test_density_structure(vxc_case):
+    """rho_bond equals rho_in off site without the three-center part; on the
+    self block it holds only the atom's own term; the weighted densities
+    are positive with the synthetic tables."""
+    name, st, s, r3, r2 = vxc_case
+    N = len(st.imass)
+    self_p = s.pair_off[:-1] + s.neigh_self
+    off = np.ones(s.npairs, bool)
+    off[self_p] = False
+    for p in np.nonzero(off)[0][:400]:
+        sl = slice(s.blk_off[p], s.blk_off[p + 1])
+        assert np.array_equal(r2["rho_in"][sl], r2["rho_bond"][sl])
+        assert np.array_equal(r2["wrho_in"][p], r2["wrho_bond"][p])
+        assert np.array_equal(r3["rho_bond"][sl], r2["rho_bond"][sl])
+    assert np.all(r3["wrho_in"][:, 0] > 0.0)
+    # the three-center part reaches the pairs with common neighbours
+    assert np.abs(r3["rho_in"] - r2["rho_in"]).max() > 1e-6
+    assert np.abs(r3["wrho_in"] - r2["wrho_in"]).max() > 1e-6
+    # self block of rho_bond: only the self pair's atom term, so smaller
+    for i in range(min(N, 8)):
+        ps = self_p[i]
+        assert r3["wrho_bond"][ps][0] < r3["wrho_in"][ps][0]
+
+
+def test_vxc_is_the_sum_of_its_parts(vxc_case):
+    _, _, _, r, _ = vxc_case
+    assert np.array_equal(r["vxc"], r["vxc_bond"] + r["vxc_SN"] - r["vxc_SN_bond"])
+
+
+def test_both_lda_branches_are_reached(fdata_root):
+    """The on-site weighted densities of Si64 are above the density where
+    the Ceperley-Alder fit changes form (rs = 1, 1.61 / A^3), the off-site
+    ones below, so both branches feed the vxc blocks."""
+    st, s = _system(fdata_root, "si64")
+    r = s.assemble_vxc()
+    w = r["wrho_in"]
+    self_p = s.pair_off[:-1] + s.neigh_self
+    rho_rs1 = 0.23873241 / P_ABOHR ** 3
+    assert w[self_p, 0].max() > rho_rs1
+    off = np.setdiff1d(np.arange(s.npairs), self_p)
+    assert w[off, 0].max() < rho_rs1
+
+
+def test_translation_invariance(fdata_root):
+    path, nZ, st = workload("sic_small", fdata_root, vxc=True)
+    fd = orc.Fdata(path, nZ)
+    a = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors().assemble_vxc()
+    b = orc.System(fd, st.ratom + np.array([0.31, -0.17, 0.05]), st.imass, st.lattice).neighbors().assemble_vxc()
+    assert np.abs(a["vxc"] - b["vxc"]).max() < 1e-9

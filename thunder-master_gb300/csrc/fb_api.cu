@@ -16,6 +16,7 @@
 #include "fb_launch.h"
 #include "fb_pp.h"
 #include "fb_ewald.h"
+#include "fb_vxc.h"
 #include "fb_devbuf.h"
 #include "fb_mlp.h"
 
@@ -29,13 +30,13 @@ std::atomic<long long> g_alloc_gen{0};
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
        KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
        KT_BLOCH, KT_PP_PAIRS, KT_PPP, KT_PPC, KT_SVNL, KT_VNL2C, KT_VNL3C, KT_DSVNL, KT_DVNL2C, KT_DVNL3C,
-       KT_VNLF, KT_EWALD, KT_EWALD_BLOCKS, KT_N };
+       KT_VNLF, KT_EWALD, KT_EWALD_BLOCKS, KT_RHO2C, KT_RHO3C, KT_VXC, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
                                      "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
                                      "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald",
-                                     "ewald_blocks"};
+                                     "ewald_blocks", "rho_2c", "rho_3c", "vxc"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -97,6 +98,8 @@ struct fb_ctx {
   double ew_kappa = 0.0;
   DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs;
   DevBuf d_q0a, d_dewald, d_ew_w, d_sum_dewald, d_ew_cw, d_fewald, d_fsr, d_flr;
+  // McWEDA exchange-correlation (Harris): input densities and vxc blocks
+  DevBuf d_rho_in, d_rho_bond, d_wrho_in, d_wrho_bond, d_vxc;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -1044,6 +1047,17 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   return a;
 }
 
+static VxcArgs vxc_args(fb_ctx *ctx) {
+  VxcArgs v{};
+  v.a = asm_args(ctx);
+  v.rho_in = ctx->d_rho_in.as<double>();
+  v.rho_bond = ctx->d_rho_bond.as<double>();
+  v.wrho_in = ctx->d_wrho_in.as<double>();
+  v.wrho_bond = ctx->d_wrho_bond.as<double>();
+  v.vxc = ctx->d_vxc.as<double>();
+  return v;
+}
+
 extern "C++" {
 // device arguments of the vnl kernels
 static PPArgs pp_args(fb_ctx *ctx) {
@@ -1365,6 +1379,12 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     if (what & FB_VNL2C) KL(KT_VNL2C, launch_vnl_2c(pa, ctx->stream));
     if (what & FB_VNL3C) KL(KT_VNL3C, launch_vnl_3c(pa, ctx->ntrip_pp, ctx->stream));
   }
+  if (what & FB_VXC) {
+    VxcArgs v = vxc_args(ctx);
+    KL(KT_RHO2C, launch_rho_2c(v, ctx->stream));
+    if (a.ntrip > 0) KL(KT_RHO3C, launch_rho_3c(v, ctx->stream));
+    KL(KT_VXC, launch_vxc(v, ctx->stream));
+  }
   if (what & FB_EWALD) {
     EwaldArgs e = ewald_args(ctx);
     KL(KT_EWALD, launch_ewald_matrix(e, ctx->stream));
@@ -1418,6 +1438,19 @@ static int check_assemble(fb_ctx *ctx, unsigned what) {
     CHK(ctx->d_ewlr.ensure(nb));
     CHK(ewald_setup(ctx));
   }
+  if (what & FB_VXC) {
+    if (dogs) return fail(ctx, FB_ERR_UNSUPPORTED, "vxc: this build assembles the McWEDA Harris exchange-correlation only");
+    if (!ctx->fdh.dev.have_vxc)
+      return fail(ctx, FB_ERR_TABLE, "vxc: the Fdata lacks McWEDA tables (vxc_ontop, den_*, denS_*, den3, denS3, vxc_1c)");
+    if (!(what & FB_S) && !(ctx->assembled & FB_S))
+      return fail(ctx, FB_ERR_STATE, "assemble_vxc reads the overlap blocks: assemble FB_S first");
+    size_t nb = (size_t)ctx->nblock * sizeof(double) + 8, nw = (size_t)VXC_WSH * ctx->P * sizeof(double) + 8;
+    CHK(ctx->d_rho_in.ensure(nb));
+    CHK(ctx->d_rho_bond.ensure(nb));
+    CHK(ctx->d_vxc.ensure(nb));
+    CHK(ctx->d_wrho_in.ensure(nw));
+    CHK(ctx->d_wrho_bond.ensure(nw));
+  }
   if (what & (FB_SVNL | FB_VNL2C | FB_VNL3C)) {
     if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
     if ((what & (FB_VNL2C | FB_VNL3C)) && !(what & FB_SVNL) && !(ctx->assembled & FB_SVNL))
@@ -1433,7 +1466,7 @@ static int check_assemble(fb_ctx *ctx, unsigned what) {
 static void assemble_done(fb_ctx *ctx, unsigned what) {
   if (what & FB_VNA2C) ctx->have_vna2c = true;
   if ((what & FB_DIPOLE) || (ctx->theory == FB_THEORY_DOGS && (what & FB_VNA2C))) ctx->have_dip = true;
-  ctx->assembled |= what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C);
+  ctx->assembled |= what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_VXC);
   if (what & FB_EWALD) ctx->have_ewald = true;
 }
 
@@ -1469,6 +1502,11 @@ static DevBuf *block_buf(fb_ctx *ctx, int which, size_t *n) {
     case FB_BLOCK_RHO_PP: *n = (size_t)ctx->nvnl; return ctx->have_rho_pp ? &ctx->d_rho_pp : nullptr;
     case FB_BLOCK_EWALDSR: return ctx->have_ewald ? &ctx->d_ewsr : nullptr;
     case FB_BLOCK_EWALDLR: return ctx->have_ewald ? &ctx->d_ewlr : nullptr;
+    case FB_BLOCK_VXC: return (ctx->assembled & FB_VXC) ? &ctx->d_vxc : nullptr;
+    case FB_BLOCK_RHO_IN: return (ctx->assembled & FB_VXC) ? &ctx->d_rho_in : nullptr;
+    case FB_BLOCK_RHO_BOND: return (ctx->assembled & FB_VXC) ? &ctx->d_rho_bond : nullptr;
+    case FB_BLOCK_WRHO_IN: *n = (size_t)VXC_WSH * ctx->P; return (ctx->assembled & FB_VXC) ? &ctx->d_wrho_in : nullptr;
+    case FB_BLOCK_WRHO_BOND: *n = (size_t)VXC_WSH * ctx->P; return (ctx->assembled & FB_VXC) ? &ctx->d_wrho_bond : nullptr;
   }
   return nullptr;
 }
@@ -1688,7 +1726,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   int st = FB_OK;
   if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
     st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
-  if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD))) st = enqueue_assemble(ctx, what);
+  if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD | FB_VXC))) st = enqueue_assemble(ctx, what);
   if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -1729,7 +1767,7 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
 
 int fb_assemble_graph(fb_ctx *ctx, unsigned what) {
   if (!ctx) return FB_ERR_ARG;
-  const unsigned vals = FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD;
+  const unsigned vals = FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD | FB_VXC;
   if (!(what & (vals | FB_FORCES))) return fail(ctx, FB_ERR_ARG, "nothing to assemble");
   CU(cudaSetDevice(ctx->device));
   if (what & vals) CHK(check_assemble(ctx, what));

@@ -191,7 +191,7 @@ int fdata_read(const std::string &dir, int nspecies, const int *nZ, FdataHost &o
       if (!read_dbls(t, 1, &ae)) goto bad_info;
       t.skip();
       sp.q0 = 0.0;
-      for (int k = 0; k < sp.nssh; k++) sp.q0 += q[k];
+      for (int k = 0; k < sp.nssh; k++) sp.q0 += q[k], sp.qn[k] = q[k];
       sp.rcA = -99.0;
       sp.rcmin = 99.0;
       sp.norb = 0;
@@ -229,6 +229,7 @@ info_done:
   // ---- read_Fdata_2c --------------------------------------------------------
   bool dogs_ok = true;  // every DOGS sub-cell and z-dipole table found
   bool pp_ok = true;    // every vnl table found
+  bool vxc_ok = true;   // every McWEDA table found
   for (int is = 0; is < nspecies; is++) {
     for (int js = 0; js < nspecies; js++) {
       std::string pz = zz(out.sp[is].nZ) + "." + zz(out.sp[js].nZ);
@@ -297,12 +298,11 @@ info_done:
       }
       // stage cell (itype, isub) into d: 0 staged, 1 absent, else an error
       int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
-      auto stage = [&](int it, int isub, Cell2cDev &d) -> int {
+      auto stage_map = [&](int it, int isub, const MEMap &m, Cell2cDev &d) -> int {
         int k = index[it][isub];
         d.off = -1;
         if (k < 1 || k > ncell) return 1;
         const Cell2 &c = cells[k - 1];
-        MEMap m = make_munu(PA, it == 5 ? PA : PB);
         if (!map_equal(c, m)) {
           err = "2c table " + pz + " interaction " + std::to_string(it) + " sub " + std::to_string(isub) +
                 " has a non-canonical ME map";
@@ -318,6 +318,9 @@ info_done:
         for (int ix = 0; ix < c.nx; ix++)
           for (int e = 0; e < c.nME; e++) out.table2c.push_back(c.F[ix + (size_t)c.nx * e]);
         return 0;
+      };
+      auto stage = [&](int it, int isub, Cell2cDev &d) -> int {
+        return stage_map(it, isub, make_munu(PA, it == 5 ? PA : PB), d);
       };
       // the five Harris interactions (isub = 0)
       for (int it = 1; it <= 5; it++) {
@@ -370,6 +373,27 @@ info_done:
         int r = stage(10, 0, out.dev.c2dip[is][js]);
         if (r == 1) dogs_ok = false;
         else if (r) return r;
+      }
+      // McWEDA: vxc_ontop and the density sub-cells
+      {
+        int r = stage(7, 0, out.dev.c2vxc[is][js]);
+        if (r == 1) vxc_ok = false;
+        else if (r) return r;
+        const int its[6] = {15, 16, 17, 19, 20, 21};
+        const MEMap maps[6] = {make_munu(PA, PB), make_munu(PA, PB), make_munu(PA, PA),
+                               make_munu_s(PA, PB), make_munu_s(PA, PB), make_munu_s(PA, PA)};
+        int nsh[6] = {out.sp[is].nssh, out.sp[js].nssh, out.sp[js].nssh,
+                      out.sp[is].nssh, out.sp[js].nssh, out.sp[js].nssh};
+        for (int q = 0; q < 6; q++)
+          for (int isorp = 1; isorp <= MAXSUB; isorp++) {
+            Cell2cDev &d = out.dev.c2rho[is][js][q][isorp - 1];
+            d.off = -1;
+            if (isorp > nsh[q]) continue;
+            r = stage_map(its[q], isorp, maps[q], d);
+            if (r == 1) vxc_ok = false;
+            else if (r) return r;
+          }
+        if (nsh[0] > MAXSUB || nsh[1] > MAXSUB) vxc_ok = false;
       }
     }
     // clPP.ZZ.dat is opened unconditionally (M_Fdata_2c.f90:252-258)
@@ -466,12 +490,11 @@ info_done:
         // stage bcna (interaction 3) sub-cell isub, theta 1..5: 0 staged,
         // 1 absent, else an error
         int PA = out.sp[is].pattern, PB = out.sp[js].pattern;
-        MEMap m = make_munu_3c(PA, PB);
-        auto stage3 = [&](int isub, Cell3cDev &d) -> int {
+        auto stage3m = [&](int itype, int isub, const MEMap &m, Cell3cDev &d) -> int {
           d.off = -1;
           const Cell3 *th[NTHETA];
           for (int it = 1; it <= NTHETA; it++) {
-            int k = index[3][isub][it];
+            int k = index[itype][isub][it];
             if (k < 1 || k > ncell) return 1;
             th[it - 1] = &cells[k - 1];
             if (!map_equal3(*th[it - 1], m)) {
@@ -514,6 +537,7 @@ info_done:
             }
           return 0;
         };
+        auto stage3 = [&](int isub, Cell3cDev &d) -> int { return stage3m(3, isub, make_munu_3c(PA, PB), d); };
         int r = stage3(0, out.dev.c3[is][js][ks]);
         if (r == 1) {
           err = "3c table " + pz + " lacks bcna";
@@ -531,7 +555,39 @@ info_done:
           if (r == 1) dogs_ok = false;
           else if (r) return r;
         }
+        // McWEDA three-center densities den3 (itype 1) and denS3 (itype 2)
+        for (int q = 0; q < 2; q++)
+          for (int isorp = 1; isorp <= MAXSUB; isorp++) {
+            Cell3cDev &dd = out.dev.c3rho[is][js][ks][q][isorp - 1];
+            dd.off = -1;
+            if (isorp > nk) continue;
+            r = stage3m(q + 1, isorp, q == 0 ? make_munu_3c(PA, PB) : make_munu_s(PA, PB), dd);
+            if (r == 1) vxc_ok = false;
+            else if (r) return r;
+          }
+        if (nk > MAXSUB) vxc_ok = false;
       }
+
+  // one-center McWEDA xc (read_Fdata_1c, e.FDATA/M_Fdata_1c_McWEDA_Harris.f90:
+  // 99-136): vxc_1c.ZZ.dat, nssh records of E then nssh records of V
+  for (int k = 0; k < nspecies && vxc_ok; k++) {
+    Text t;
+    int n = out.sp[k].nssh;
+    if (n > MAXSUB || !t.load(dir + "/vxc_1c." + zz(out.sp[k].nZ) + ".dat")) {
+      vxc_ok = false;
+      break;
+    }
+    double row[8];
+    for (int a = 0; a < n && vxc_ok; a++) vxc_ok = read_dbls(t, n, row);  // E
+    for (int a = 0; a < n && vxc_ok; a++) {
+      vxc_ok = read_dbls(t, n, row);
+      for (int b = 0; b < n; b++) out.dev.vxc1c[k][a * MAXSUB + b] = row[b];
+    }
+    if (!vxc_ok) {
+      err = "parse error in vxc_1c." + zz(out.sp[k].nZ) + ".dat";
+      return FB_ERR_IO;
+    }
+  }
 
   // double-float copy of the 3c values: hi = nearest float, lo = nearest
   // float of the remainder (exact in double)
@@ -556,6 +612,7 @@ info_done:
     out.dev.sp[k].norb_pp = sh.norb_pp;
     out.dev.sp[k].rc_pp = sh.rc_pp;
     out.dev.sp[k].q0 = sh.q0;
+    for (int q = 0; q < MAXSUB; q++) out.dev.sp[k].qn[q] = q < sh.nssh ? sh.qn[q] : 0.0;
     int o = 0;
     for (int q = 0; q < sh.nssh_pp && o < 9; q++)
       for (int m = 0; m < 2 * sh.lpp[q] + 1 && o < 9; m++) out.dev.sp[k].cl[o++] = sh.cl_pp[q];
@@ -563,6 +620,7 @@ info_done:
   }
   out.dev.have_pp = pp_ok ? 1 : 0;
   out.dev.have_dogs = dogs_ok ? 1 : 0;
+  out.dev.have_vxc = vxc_ok ? 1 : 0;
   return FB_OK;
 }
 

@@ -14,6 +14,7 @@ struct SpeciesHost {
   int lpp[8] = {0};
   double rc_pp = 0.0;
   double q0 = 0.0;  // sum of the shells' Qneutral
+  double qn[8] = {0};  // Qneutral per shell
   double cl_pp[8] = {0};
   int norb_pp = 0;
   // projector shells as a basis pattern: s, sp or spd, else -1

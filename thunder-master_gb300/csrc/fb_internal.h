@@ -74,6 +74,21 @@ __host__ __device__ constexpr MEMap make_munu(int PA, int PB) {
 }
 
 // make_munu_3c (c.SYSTEM/M_integrals_3c.f90:230-587)
+// make_munuS / make_munuS_atom / make_munuS_3c (c.SYSTEM/M_integrals_2c.f90:
+// 521-755, M_integrals_3c.f90:623-753): one shell-level channel per shell
+// pair, issh outer, mvalue 0.
+__host__ __device__ constexpr MEMap make_munu_s(int PA, int PB) {
+  MEMap m{};
+  for (int a = 0; a < pat_nssh(PA); a++)
+    for (int b = 0; b < pat_nssh(PB); b++) {
+      m.mu[m.n] = a;
+      m.nu[m.n] = b;
+      m.mv[m.n] = 0;
+      m.n++;
+    }
+  return m;
+}
+
 __host__ __device__ constexpr MEMap make_munu_3c(int PA, int PB) {
   MEMap m = make_munu(PA, PB);
   int n1 = 0;
@@ -149,6 +164,7 @@ struct SpeciesDev {
   double rc_pp;
   double cl[9];
   double q0;     // sum of the shells' Qneutral
+  double qn[MAXSUB];  // Qneutral per shell
 };
 
 // One 2c interaction cell (T_Fdata_cell_2c, e.FDATA/M_Fdata_2c.f90:83-96).
@@ -187,6 +203,17 @@ struct FdataDev {
   // non-local pseudopotential <basis of in1 | projector of in2> (itype 6)
   Cell2cDev c2vnl[MAXSP][MAXSP];
   Cell3cDev c3s[MAXSP][MAXSP][MAXSP][MAXSUB];
+  // McWEDA exchange-correlation: vxc_ontop (itype 7); the density
+  // sub-cells isorp = 1..nssh of rho ontop L (shells of the first species),
+  // R, atom (shells of the second), and of their shell-level forms rhoS
+  // ([0..5] = itype 15, 16, 17, 19, 20, 21); the three-center densities
+  // den3 and denS3 ([0..1] = itype 1, 2; shells of the third species); the
+  // one-center V(issh, jssh) at [issh * MAXSUB + jssh]
+  int have_vxc;
+  Cell2cDev c2vxc[MAXSP][MAXSP];
+  Cell2cDev c2rho[MAXSP][MAXSP][6][MAXSUB];
+  Cell3cDev c3rho[MAXSP][MAXSP][MAXSP][2][MAXSUB];
+  double vxc1c[MAXSP][MAXSUB * MAXSUB];
 };
 
 // device status flags (bit mask, OR-ed by kernels)

@@ -1,0 +1,463 @@
+// fb_vxc.cu -- sm_103a kernels of the McWEDA exchange-correlation assembly,
+// Harris (PRB 71, 235101 (2005)):
+//   k_rho_2c  assemble_rho_2c + assemble_rho_weighted_2c
+//             (j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90:81-276, :427-622)
+//   k_rho_3c  assemble_rho_3c + assemble_rho_weighted_3c (:298-403, :645-741)
+//   k_vxc     assemble_vxc_SN + assemble_vxc_bond + vxc = bond + SN - SN_bond
+//             (j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90:102-640)
+// All FP64.  The density sub-cells of one pair share the pair's grid and
+// frame, so the Qneutral-weighted sum over the shells is taken in the
+// molecular frame and rotated once (the rotation is linear).
+#include "fb_common.cuh"
+#include "fb_vxc.h"
+
+namespace fb {
+
+namespace {
+
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+// lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:56-190):
+// muxc (eV), dmuxc and d2muxc (eV A^3, eV A^6).  The low-density branch's
+// d2dec keeps the reference's (dden*3) factor (:143-144).
+struct Lda {
+  double muxc, dmuxc, d2muxc;
+};
+
+__device__ __forceinline__ Lda lda_ca(double rh) {
+  const double a3 = P_abohr * P_abohr * P_abohr;
+  double rhx = sqrt(rh * rh + 1.0e-6);
+  double rho = rhx * a3;
+  double rho_third = pow(rho, 1.0 / 3.0);
+  double rs = 0.62035049 / rho_third;
+  double exc, muxc, dec, ddec, d2dec;
+  if (rho < 0.23873241) {
+    double sqrs = sqrt(rs);
+    double den = 1.0 + 1.0529 * sqrs + 0.3334 * rs;
+    exc = -0.4581652 / rs - 0.1423 / den;
+    muxc = exc - rs * (0.15273333 / (rs * rs) + (0.02497128 / sqrs + 0.01581427) / (den * den));
+    double dden = 1.0529 / (2.0 * sqrs) + 0.3334;
+    double d2den = (-0.5) * 1.0529 / (2.0 * rs * sqrs);
+    double d3den = 0.75 * 1.0529 / (2.0 * (rs * rs) * sqrs);
+    dec = 0.1423 * dden / (den * den);
+    ddec = -2.0 * 0.1423 * dden * dden / (den * den * den) + 0.1423 * d2den / (den * den);
+    d2dec = 6.0 * 0.1423 * (dden * 3) / (den * den * den * den) - 6.0 * 0.1423 * dden * d2den / (den * den * den) +
+            0.1423 * d3den / (den * den);
+  } else {
+    double rsl = log(rs);
+    exc = -0.4581652 / rs - 0.0480 + 0.0311 * rsl - 0.0116 * rs + 0.002 * rs * rsl;
+    muxc = exc - rs * (0.15273333 / (rs * rs) + 0.01036667 / rs - 0.003866667 + 0.00066667 * (1.0 + rsl));
+    dec = 0.0311 / rs - 0.0116 + 0.0020 * (rsl + 1.0);
+    ddec = -0.0311 / (rs * rs) + 0.0020 / rs;
+    d2dec = 2.0 * 0.0311 / (rs * rs * rs) - 0.0020 / (rs * rs);
+  }
+  double ex = -0.7385587664 * rho_third;
+  double dexc = (muxc - exc) / rho;
+  double r2 = rho * rho, r3 = r2 * rho;
+  double d2nec = (4.0 * rs / (9.0 * r2)) * dec + (rs * rs / (9.0 * r2)) * ddec;
+  double d2nex = -(2.0 / (9.0 * r2)) * ex;
+  double dmuxc = 2.0 * dexc + rho * (d2nex + d2nec);
+  double d3nec = (-28.0 * rs / (27.0 * r3)) * dec + (-4.0 * rs * rs / (9.0 * r3)) * ddec +
+                 ((rs * rs * rs) / (-27.0 * r3)) * d2dec;
+  double d3nex = (10.0 / (27.0 * r3)) * ex;
+  double d2muxc = 3.0 * (d2nex + d2nec) + rho * (d3nex + d3nec);
+  Lda o;
+  o.muxc = muxc * P_Hartree;
+  o.dmuxc = dmuxc * P_Hartree * a3;
+  o.d2muxc = d2muxc * P_Hartree * (a3 * a3);
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// rho 2c: one warp per atom i, one lane per pair
+// ---------------------------------------------------------------------------
+template <int PA, int PB, bool HASD>
+__device__ __forceinline__ void pair_rho2c(const Ctx2c &c, const VxcArgs &v, int i, int p, double *Xatom,
+                                           double *Watom) {
+  using PL = Plan<PA, PB, K2C>;
+  using PLA = Plan<PA, PA, K2C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
+  constexpr int SA = pat_nssh(PA), SB = pat_nssh(PB);
+  const FdataDev &fd = *c.fd;
+  int j = c.neigh_j[p];
+  int in1 = c.isp[i], in2 = c.isp[j];
+  double r1[3], r2[3], z, e[3][3];
+  pair_geom(c, i, p, r1, r2, z, e);
+  RotM R;
+  twister<HASD>(e, R);
+  bool self = (i == j && c.neigh_b[p] == 0);
+  constexpr int NT = cmax(cmax(NE, NEA), cmax(SA * SB, SA * SA));
+  double w[7], t[NT];
+  int i0 = 0;
+  const Cell2cDev *last = nullptr;
+  auto weights = [&](const Cell2cDev &cell) {
+    if (z > cell.xmax * (1.0 + 1.0e-5)) atomicOr(c.status, DEVERR_XLARGE);
+    if (!last || !same_grid(*last, cell)) lagrange7(z, cell, i0, w, nullptr);
+    last = &cell;
+  };
+  const double *qi = fd.sp[in1].qn, *qj = fd.sp[in2].qn;
+  double *W_in = v.wrho_in + (long long)VXC_WSH * p, *W_bo = v.wrho_bond + (long long)VXC_WSH * p;
+  if (!self) {
+    // ontop left (shells of i) + right (shells of j), :186-218
+    double m[NE];
+#pragma unroll
+    for (int q = 0; q < NE; q++) m[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SA; isorp++) {
+      const Cell2cDev &cl = fd.c2rho[in1][in2][0][isorp];
+      weights(cl);
+      interp2c<NE>(c.table2c, cl, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < NE; q++) m[q] = fma(t[q], qi[isorp], m[q]);
+    }
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      const Cell2cDev &cr = fd.c2rho[in1][in2][1][isorp];
+      weights(cr);
+      interp2c<NE>(c.table2c, cr, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < NE; q++) m[q] = fma(t[q], qj[isorp], m[q]);
+    }
+    double X[NA * NB];
+    rotate_plan<PA, PB, K2C>(R, m, X);
+    long long o = c.blk_off[p];
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) {
+      v.rho_in[o + q] = X[q];
+      v.rho_bond[o + q] = X[q];
+    }
+    // shell-level ontop (no rotation), :524-555
+    double ws[SA * SB];
+#pragma unroll
+    for (int q = 0; q < SA * SB; q++) ws[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SA; isorp++) {
+      const Cell2cDev &cl = fd.c2rho[in1][in2][3][isorp];
+      weights(cl);
+      interp2c<SA * SB>(c.table2c, cl, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < SA * SB; q++) ws[q] = fma(t[q], qi[isorp], ws[q]);
+    }
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      const Cell2cDev &cr = fd.c2rho[in1][in2][4][isorp];
+      weights(cr);
+      interp2c<SA * SB>(c.table2c, cr, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < SA * SB; q++) ws[q] = fma(t[q], qj[isorp], ws[q]);
+    }
+    // channel (a, b) of the shell map is element a + SA b of the block
+#pragma unroll
+    for (int q = 0; q < VXC_WSH; q++) {
+      double val = 0.0;
+      if (q < SA * SB) {
+        int a = q % SA, b = q / SA;
+        val = ws[a * SB + b];
+      }
+      W_in[q] = val;
+      W_bo[q] = val;
+    }
+  }
+  // atom case into the self block: <i|rho_shell(j)|i> rotated with (in1, in1)
+  {
+    double m[NEA];
+#pragma unroll
+    for (int q = 0; q < NEA; q++) m[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      const Cell2cDev &ca = fd.c2rho[in1][in2][2][isorp];
+      weights(ca);
+      interp2c<NEA>(c.table2c, ca, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < NEA; q++) m[q] = fma(t[q], qj[isorp], m[q]);
+    }
+    double XA[NA * NA];
+    rotate_plan<PA, PA, K2C>(R, m, XA);
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) Xatom[q] += XA[q];
+    double ws[SA * SA];
+#pragma unroll
+    for (int q = 0; q < SA * SA; q++) ws[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      const Cell2cDev &ca = fd.c2rho[in1][in2][5][isorp];
+      weights(ca);
+      interp2c<SA * SA>(c.table2c, ca, i0, w, t);
+#pragma unroll
+      for (int q = 0; q < SA * SA; q++) ws[q] = fma(t[q], qj[isorp], ws[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < SA * SA; q++) Watom[q] += ws[(q % SA) * SA + q / SA];
+    if (self) {
+      // rho_bond of the self block takes only the atom's own term
+      long long o = c.blk_off[p];
+#pragma unroll
+      for (int q = 0; q < NA * NA; q++) v.rho_bond[o + q] = XA[q];
+#pragma unroll
+      for (int q = 0; q < VXC_WSH; q++) W_bo[q] = q < SA * SA ? ws[(q % SA) * SA + q / SA] : 0.0;
+    }
+  }
+}
+
+template <int PA, bool HASD>
+__device__ void atom_rho2c(const Ctx2c &c, const VxcArgs &v, int i, int lane) {
+  constexpr int NA = pat_norb(PA), SA = pat_nssh(PA);
+  double Xatom[NA * NA], Watom[SA * SA];
+#pragma unroll
+  for (int q = 0; q < NA * NA; q++) Xatom[q] = 0.0;
+#pragma unroll
+  for (int q = 0; q < SA * SA; q++) Watom[q] = 0.0;
+  int p0 = c.pair_off[i], p1 = c.pair_off[i + 1];
+  for (int p = p0 + lane; p < p1; p += 32) {
+    int pb = c.fd->sp[c.isp[c.neigh_j[p]]].pattern;
+    if (pb == PAT_SP) pair_rho2c<PA, PAT_SP, HASD>(c, v, i, p, Xatom, Watom);
+    else if (pb == PAT_S) pair_rho2c<PA, PAT_S, HASD>(c, v, i, p, Xatom, Watom);
+    else if constexpr (HASD) pair_rho2c<PA, PAT_SPD, HASD>(c, v, i, p, Xatom, Watom);
+  }
+#pragma unroll
+  for (int q = 0; q < NA * NA; q++)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) Xatom[q] += __shfl_xor_sync(0xffffffffu, Xatom[q], off);
+#pragma unroll
+  for (int q = 0; q < SA * SA; q++)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) Watom[q] += __shfl_xor_sync(0xffffffffu, Watom[q], off);
+  if (lane == 0) {
+    int ps = p0 + c.neigh_self[i];
+    long long os = c.blk_off[ps];
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) v.rho_in[os + q] = Xatom[q];
+#pragma unroll
+    for (int q = 0; q < VXC_WSH; q++) v.wrho_in[(long long)VXC_WSH * ps + q] = q < SA * SA ? Watom[q] : 0.0;
+  }
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_rho_2c(Ctx2c c, VxcArgs v) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= c.N) return;
+  int pa = c.fd->sp[c.isp[i]].pattern;
+  if (pa == PAT_SP) atom_rho2c<PAT_SP, HASD>(c, v, i, lane);
+  else if (pa == PAT_S) atom_rho2c<PAT_S, HASD>(c, v, i, lane);
+  else if constexpr (HASD) atom_rho2c<PAT_SPD, HASD>(c, v, i, lane);
+}
+
+// ---------------------------------------------------------------------------
+// rho 3c: one thread per triplet, FP64 atomics into the pair (iatom, mneigh)
+// ---------------------------------------------------------------------------
+template <int PA, int PB, bool HASD>
+__device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int t) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
+  constexpr int SA = pat_nssh(PA), SB = pat_nssh(PB);
+  int ia, iat, jat;
+  TripGeom g;
+  trip_geom(c, t, ia, iat, jat, g);
+  const FdataDev &fd = *c.fd;
+  int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+  int nk = fd.sp[indna].nssh;
+  const double *qk = fd.sp[indna].qn;
+  double F[NE], m[NE];
+#pragma unroll
+  for (int q = 0; q < NE; q++) m[q] = 0.0;
+#pragma unroll 1
+  for (int isorp = 0; isorp < nk; isorp++) {
+    interp3c<NE, false>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, F, nullptr, nullptr, nullptr);
+#pragma unroll
+    for (int q = 0; q < NE; q++) m[q] = fma(F[q], qk[isorp], m[q]);
+  }
+  double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
+  sfor<NE>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    if constexpr (PL::m.mv[e] == 1) m[e] = m[e] * sint;
+  });
+  RotM R;
+  twister<HASD>(g.e, R);
+  double X[NA * NB];
+  rotate_plan<PA, PB, K3C>(R, m, X);
+  int p = c.tdst[t];
+  double *dst = v.rho_in + c.blk_off[p];
+#pragma unroll
+  for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, X[q]);
+  double Fs[SA * SB], ws[SA * SB];
+#pragma unroll
+  for (int q = 0; q < SA * SB; q++) ws[q] = 0.0;
+#pragma unroll 1
+  for (int isorp = 0; isorp < nk; isorp++) {
+    interp3c<SA * SB, false>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, Fs, nullptr, nullptr,
+                             nullptr);
+#pragma unroll
+    for (int q = 0; q < SA * SB; q++) ws[q] = fma(Fs[q], qk[isorp], ws[q]);
+  }
+  double *wd = v.wrho_in + (long long)VXC_WSH * p;
+#pragma unroll
+  for (int q = 0; q < SA * SB; q++) atomicAdd(wd + (q / SB) + SA * (q % SB), ws[q]);
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_rho_3c(Ctx3c c, VxcArgs v) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.T; t += gridDim.x * blockDim.x) {
+    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+    int key = pa * 3 + pb;
+    switch (key) {
+      case PAT_SP * 3 + PAT_SP: trip_rho3c<PAT_SP, PAT_SP, HASD>(c, v, t); break;
+      case PAT_SP * 3 + PAT_S: trip_rho3c<PAT_SP, PAT_S, HASD>(c, v, t); break;
+      case PAT_S * 3 + PAT_SP: trip_rho3c<PAT_S, PAT_SP, HASD>(c, v, t); break;
+      case PAT_S * 3 + PAT_S: trip_rho3c<PAT_S, PAT_S, HASD>(c, v, t); break;
+      default:
+        if constexpr (HASD) {
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_rho3c<PAT_SPD, PAT_SPD, HASD>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_rho3c<PAT_SPD, PAT_SP, HASD>(c, v, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_rho3c<PAT_SP, PAT_SPD, HASD>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_rho3c<PAT_SPD, PAT_S, HASD>(c, v, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_rho3c<PAT_S, PAT_SPD, HASD>(c, v, t);
+        }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vxc: one warp per atom, one lane per pair
+// ---------------------------------------------------------------------------
+template <int PA, int PB, bool HASD>
+__device__ __forceinline__ void pair_vxc(const Ctx2c &c, const VxcArgs &v, int i, int p) {
+  using PL = Plan<PA, PB, K2C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
+  constexpr int SA = pat_nssh(PA), SB = pat_nssh(PB);
+  const FdataDev &fd = *c.fd;
+  int j = c.neigh_j[p];
+  long long o = c.blk_off[p];
+  const double *Wi = v.wrho_in + (long long)VXC_WSH * p, *Wb = v.wrho_bond + (long long)VXC_WSH * p;
+  const double *S = c.S + o, *ri = v.rho_in + o, *rb = v.rho_bond + o;
+  double sn[NA * NB], snb[NA * NB], bond[NA * NB];
+  bool self = (i == j && c.neigh_b[p] == 0);
+  if (!self) {
+    // off-site generalized Sankey-Niklewski (vxc_SN :286-357)
+#pragma unroll
+    for (int a = 0; a < SA; a++)
+#pragma unroll
+      for (int b = 0; b < SB; b++) {
+        double wi = Wi[a + SA * b], wb = Wb[a + SA * b];
+        Lda li = lda_ca(wi), lb = lda_ca(wb);
+#pragma unroll
+        for (int imu = shell_off(a); imu < shell_off(a) + 2 * a + 1; imu++)
+#pragma unroll
+          for (int inu = shell_off(b); inu < shell_off(b) + 2 * b + 1; inu++) {
+            int q = imu + NA * inu;
+            double ov = S[q];
+            sn[q] = li.muxc * ov + li.dmuxc * (ri[q] - wi * ov);
+            snb[q] = lb.muxc * ov + lb.dmuxc * (rb[q] - wb * ov);
+          }
+      }
+    // vxc_bond: the rotated vxc_ontop table (:612-627)
+    double r1[3], r2[3], z, e[3][3];
+    pair_geom(c, i, p, r1, r2, z, e);
+    RotM R;
+    twister<HASD>(e, R);
+    const Cell2cDev &cell = fd.c2vxc[c.isp[i]][c.isp[j]];
+    if (z > cell.xmax * (1.0 + 1.0e-5)) atomicOr(c.status, DEVERR_XLARGE);
+    double w[7], m[NE];
+    int i0 = 0;
+    lagrange7(z, cell, i0, w, nullptr);
+    interp2c<NE>(c.table2c, cell, i0, w, m);
+    rotate_plan<PA, PB, K2C>(R, m, bond);
+  } else if constexpr (PA == PB) {
+    // on-site SN (:365-480): diagonal, then the off-diagonal imu != inu
+#pragma unroll
+    for (int q = 0; q < NA * NA; q++) sn[q] = snb[q] = bond[q] = 0.0;
+#pragma unroll
+    for (int a = 0; a < SA; a++) {
+      {
+        double wi = Wi[a + SA * a], wb = Wb[a + SA * a];
+        Lda li = lda_ca(wi), lb = lda_ca(wb);
+#pragma unroll
+        for (int imu = shell_off(a); imu < shell_off(a) + 2 * a + 1; imu++) {
+          int q = imu + NA * imu;
+          sn[q] = li.muxc + li.dmuxc * (ri[q] - wi);
+          snb[q] = lb.muxc + lb.dmuxc * (rb[q] - wb);
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < SA; b++) {
+        Lda li = lda_ca(Wi[a + SA * b]), lb = lda_ca(Wb[a + SA * b]);
+#pragma unroll
+        for (int imu = shell_off(a); imu < shell_off(a) + 2 * a + 1; imu++)
+#pragma unroll
+          for (int inu = shell_off(b); inu < shell_off(b) + 2 * b + 1; inu++)
+            if (imu != inu) {
+              int q = imu + NA * inu;
+              sn[q] = li.dmuxc * ri[q];
+              snb[q] = lb.dmuxc * rb[q];
+            }
+      }
+    }
+    // vxc_bond on-site: V(issh, jssh) where l and m agree (:590-605); with
+    // one shell per l in these bases that is the diagonal, V(issh, issh)
+    const double *V = fd.vxc1c[c.isp[i]];
+#pragma unroll
+    for (int imu = 0; imu < NA; imu++) {
+      int sa = orb_shell(imu);
+      bond[imu + NA * imu] = V[sa * MAXSUB + sa];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NA * NB; q++) v.vxc[o + q] = bond[q] + sn[q] - snb[q];
+}
+
+template <int PA, bool HASD>
+__device__ void atom_vxc(const Ctx2c &c, const VxcArgs &v, int i, int lane) {
+  for (int p = c.pair_off[i] + lane; p < c.pair_off[i + 1]; p += 32) {
+    int pb = c.fd->sp[c.isp[c.neigh_j[p]]].pattern;
+    if (pb == PAT_SP) pair_vxc<PA, PAT_SP, HASD>(c, v, i, p);
+    else if (pb == PAT_S) pair_vxc<PA, PAT_S, HASD>(c, v, i, p);
+    else if constexpr (HASD) pair_vxc<PA, PAT_SPD, HASD>(c, v, i, p);
+  }
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_vxc(Ctx2c c, VxcArgs v) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= c.N) return;
+  int pa = c.fd->sp[c.isp[i]].pattern;
+  if (pa == PAT_SP) atom_vxc<PAT_SP, HASD>(c, v, i, lane);
+  else if (pa == PAT_S) atom_vxc<PAT_S, HASD>(c, v, i, lane);
+  else if constexpr (HASD) atom_vxc<PAT_SPD, HASD>(c, v, i, lane);
+}
+
+}  // namespace
+
+int launch_rho_2c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.N == 0) return 0;
+  Ctx2c c = make2c(v.a);
+  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
+  if (v.a.have_d) k_rho_2c<true><<<blocks, threads, 0, s>>>(c, v);
+  else k_rho_2c<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_rho_3c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.ntrip == 0) return 0;
+  Ctx3c c = make3c(v.a);
+  int threads = 128;
+  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
+  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
+  if (v.a.have_d) k_rho_3c<true><<<blocks, threads, 0, s>>>(c, v);
+  else k_rho_3c<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_vxc(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.N == 0) return 0;
+  Ctx2c c = make2c(v.a);
+  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
+  if (v.a.have_d) k_vxc<true><<<blocks, threads, 0, s>>>(c, v);
+  else k_vxc<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+}  // namespace fb

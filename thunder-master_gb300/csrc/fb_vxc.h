@@ -1,0 +1,30 @@
+// fb_vxc.h -- device arguments and launchers of the McWEDA
+// exchange-correlation assembly, Harris (j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90,
+// M_assemble_rho_McWEDA_Harris.f90).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fb_launch.h"
+
+namespace fb {
+
+// Orbital blocks (rho_in, rho_bond, vxc) use the pair block layout
+// (blk_off); the shell-level weighted densities hold VXC_WSH doubles per
+// pair, element (issh, jssh) at [VXC_WSH p + issh + nssh_i jssh].
+constexpr int VXC_WSH = MAXSUB * MAXSUB;
+
+struct VxcArgs {
+  AsmArgs a;               // geometry, maps, tables; a.S is the overlap
+  double *rho_in, *rho_bond;
+  double *wrho_in, *wrho_bond;
+  double *vxc;
+};
+
+// assemble_rho_2c + assemble_rho_weighted_2c: writes all four density sets
+int launch_rho_2c(const VxcArgs &v, cudaStream_t s);
+// assemble_rho_3c + assemble_rho_weighted_3c: accumulates onto rho_in, wrho_in
+int launch_rho_3c(const VxcArgs &v, cudaStream_t s);
+// assemble_vxc_SN + assemble_vxc_bond + their sum: writes vxc
+int launch_vxc(const VxcArgs &v, cudaStream_t s);
+
+}  // namespace fb

@@ -27,6 +27,8 @@ Context.assemble(FB_EWALD)  assemble_ewald / ewaldsr / ewaldlr (DOGS)  j.ASSEMBL
 Context.driver_neighbors_PP  driver_neighbors_PP                      c.SYSTEM/M_neighbors_PP.f90:98
 Context.assemble(FB_VNL)  assemble_svnl / vnl_2c / vnl_3c             j.ASSEMBLERS/M_assemble_PP_{2c,3c}.f90
 Context.Dassemble(FB_VNL2C | FB_VNL3C)  Dassemble_svnl / vnl_2c / vnl_3c  k.DASSEMBLERS/M_Dassemble_PP_{2c,3c}.f90
+Context.assemble(FB_VXC)  assemble_vxc (McWEDA, Harris)               j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90:102,
+                                                                      j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90
 =====================  =============================================  ====================================
 
 There is no CPU fallback: every call runs on the GPU through the native
@@ -45,6 +47,7 @@ LIBPATH = os.path.join(_HERE, "_lib", "libfbgpu.so")
 FB_S, FB_T, FB_VNA2C, FB_VNA3C, FB_ALL, FB_KEEP_DBLOCKS, FB_FORCES = 1, 2, 4, 8, 15, 16, 32
 FB_DIPOLE = 64
 FB_EWALD = 1024
+FB_VXC = 2048
 FB_SVNL, FB_VNL2C, FB_VNL3C = 128, 256, 512
 FB_VNL = FB_SVNL | FB_VNL2C | FB_VNL3C
 FB_PP_MAP, FB_PPX_MAP, FB_PPP_MAP = 0, 1, 2
@@ -53,7 +56,8 @@ FB_MLP_OFF, FB_MLP_GATED, FB_MLP_ALL = 0, 1, 2
 FB_MLP_ENGINE_MMA, FB_MLP_ENGINE_TC = 0, 1
 TUNABLE = ("assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c")
 BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape": 7, "dip": 8,
-         "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12, "ewaldsr": 13, "ewaldlr": 14}
+         "svnl": 9, "vnl": 10, "dsvnl": 11, "rho_pp": 12, "ewaldsr": 13, "ewaldlr": 14,
+         "vxc": 15, "rho_in": 16, "rho_bond": 17, "wrho_in": 18, "wrho_bond": 19}
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8,
          "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14,
@@ -141,7 +145,8 @@ FB_PREC_FP64, FB_PREC_DF = 0, 1
 KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill", "assemble_2c",
            "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
            "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
-           "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald", "ewald_blocks")
+           "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald", "ewald_blocks",
+           "rho_2c", "rho_3c", "vxc")
 
 
 class FBError(RuntimeError):
@@ -518,6 +523,8 @@ class Context:
             n = self.nsvnl * (3 if which == "dsvnl" else 1)
         elif which in ("vnl", "rho_pp"):
             n = self.nvnl
+        elif which in ("wrho_in", "wrho_bond"):
+            n = 9 * self.npairs
         else:
             n = self.nblock * (3 if which in ("dS", "dT") else 1)
         out = np.zeros(max(n, 1))

@@ -39,6 +39,12 @@ P_VNL = 6           # include/interactions_2c.h:10
 P_DIPOLE_Z = 10     # include/interactions_2c.h:14
 P_BCNA = 3
 P_NTHETA = 5
+# McWEDA exchange-correlation (include/interactions_2c.h:11,20-26,
+# interactions_3c.h:6-7)
+P_VXC_ONTOP = 7
+P_RHO_ONTOPL, P_RHO_ONTOPR, P_RHO_ATOM = 15, 16, 17
+P_RHOS_ONTOPL, P_RHOS_ONTOPR, P_RHOS_ATOM = 19, 20, 21
+P_RHO_3C, P_RHOS_3C = 1, 2
 
 
 @dataclass
@@ -156,6 +162,19 @@ def make_munu_3c(ls_i, ls_j):
     return mu, nu, mv
 
 
+def make_munu_s(ls_i, ls_j):
+    """Shell-level map of make_munuS / make_munuS_atom / make_munuS_3c
+    (c.SYSTEM/M_integrals_2c.f90:521-755, M_integrals_3c.f90:623-753): one
+    channel per shell pair (issh outer, jssh inner), mvalue 0."""
+    mu, nu, mv = [], [], []
+    for a in range(len(ls_i)):
+        for b in range(len(ls_j)):
+            mu.append(a + 1)
+            nu.append(b + 1)
+            mv.append(0)
+    return mu, nu, mv
+
+
 def _orbital_lm(ls):
     """(shell index, l, m) for each orbital of a species, m = -l..l."""
     out = []
@@ -214,7 +233,13 @@ def _seed_of(*keys):
 
 
 _AMP2 = {P_OVERLAP: 0.6, P_KINETIC: 3.0, P_VNA_ONTOPL: 0.4, P_VNA_ONTOPR: 0.4, P_VNA_ATOM: 0.3,
-         P_DIPOLE_Z: 0.5, P_VNL: 0.5}
+         P_DIPOLE_Z: 0.5, P_VNL: 0.5, P_VXC_ONTOP: 0.8, P_RHO_ONTOPL: 0.25, P_RHO_ONTOPR: 0.25,
+         P_RHO_ATOM: 0.1}
+# ontop left / right pairs: <A|O_A|B> of (A, B) is <B|O_A|A> of (B, A)
+_SWAP_LR = {P_VNA_ONTOPL: P_VNA_ONTOPR, P_VNA_ONTOPR: P_VNA_ONTOPL,
+            P_RHO_ONTOPL: P_RHO_ONTOPR, P_RHO_ONTOPR: P_RHO_ONTOPL,
+            P_RHOS_ONTOPL: P_RHOS_ONTOPR, P_RHOS_ONTOPR: P_RHOS_ONTOPL}
+_RIGHT = (P_VNA_ONTOPR, P_RHO_ONTOPR, P_RHOS_ONTOPR)
 
 
 def _base2c(seed, itype, zA, zB, oa, ob, t, asym_pi, isub=0):
@@ -263,22 +288,51 @@ def table2c(seed, itype, A, B, oa, ob, t, asym_pi=False, isub=0):
     f^{BA}[nu, mu] = s(mu) s(nu) f^{AB}[mu, nu] (s = _flip_sign), so that
     S, T and the ontop potentials are Hermitian across neigh_back, and
     vna_ontopL of (B, A) is the transpose of vna_ontopR of (A, B)."""
-    if itype == P_VNA_ATOM:   # both orbitals on A: symmetric in (mu, nu)
+    if itype in (P_VNA_ATOM, P_RHO_ATOM):   # both orbitals on A: symmetric in (mu, nu)
         if (oa[0], oa[1]) > (ob[0], ob[1]):
             oa, ob = ob, oa
         return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi, isub)
     if _canonical(A.nZ, oa, B.nZ, ob):
-        if itype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
-            itype = P_VNA_ONTOPL
+        if itype in _RIGHT and A.nZ == B.nZ and oa == ob:
+            itype = _SWAP_LR[itype]
         return _base2c(seed, itype, A.nZ, B.nZ, oa, ob, t, asym_pi, isub)
     sign = _flip_sign(oa) * _flip_sign(ob)
-    rtype = {P_VNA_ONTOPL: P_VNA_ONTOPR, P_VNA_ONTOPR: P_VNA_ONTOPL}.get(itype, itype)
-    if rtype == P_VNA_ONTOPR and A.nZ == B.nZ and oa == ob:
-        rtype = P_VNA_ONTOPL
+    rtype = _SWAP_LR.get(itype, itype)
+    if rtype in _RIGHT and A.nZ == B.nZ and oa == ob:
+        rtype = _SWAP_LR[rtype]
     return sign * _base2c(seed, rtype, B.nZ, A.nZ, ob, oa, t, asym_pi, isub)
 
 
-def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0, isub=0):
+def _pos2c(seed, itype, zA, zB, sa, sb, t, isub):
+    """A positive shell-level density channel a exp(-c t^2) (1 + 0.2 sin(...))."""
+    rng = np.random.default_rng(_seed_of(seed, "2cS", itype, zA, zB, sa, sb, isub))
+    a = 0.02 + 0.04 * rng.random()
+    cc = 1.0 + 3.0 * rng.random()
+    k, ph = 2.0 + 3.0 * rng.random(), 6.2832 * rng.random()
+    return a * np.exp(-cc * t * t) * (1.0 + 0.2 * np.sin(k * t + ph))
+
+
+def table2c_shell(seed, itype, A, B, sa, sb, t, isub):
+    """Values of one shell-level density channel (rhoS ontop L / R, atom;
+    interactions 19-21) between shell sa of A and shell sb of B (of A for
+    the atom case).  Positive, and the ontop channels of the reversed pair
+    are the transposed ones (the weighted densities are then symmetric
+    across neigh_back)."""
+    if itype == P_RHOS_ATOM:
+        if sa > sb:
+            sa, sb = sb, sa
+        return _pos2c(seed, itype, A.nZ, B.nZ, sa, sb, t, isub)
+    if (A.nZ, sa) <= (B.nZ, sb):
+        if itype in _RIGHT and A.nZ == B.nZ and sa == sb:
+            itype = _SWAP_LR[itype]
+        return _pos2c(seed, itype, A.nZ, B.nZ, sa, sb, t, isub)
+    rtype = _SWAP_LR[itype]
+    if rtype in _RIGHT and A.nZ == B.nZ and sa == sb:
+        rtype = _SWAP_LR[rtype]
+    return _pos2c(seed, rtype, B.nZ, A.nZ, sb, sa, t, isub)
+
+
+def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0, isub=0, itype=P_BCNA):
     """Legendre coefficient itheta of the bcna channel <A oa| V_K |B ob>.
 
     c^{BAK}_l[nu, mu] = (-1)^l s(mu) s(nu) c^{ABK}_l[mu, nu] with l = itheta-1
@@ -297,10 +351,36 @@ def table3c(seed, A, B, K, oa, ob, mval, itheta, u, v, theta_decay=1.0, isub=0):
         key = (B.nZ, A.nZ, ob, oa)
         sign = (-1.0) ** l * _flip_sign(oa) * _flip_sign(ob)
     sub = () if isub == 0 else ("isorp", isub)
-    rng = np.random.default_rng(_seed_of(seed, "3c", key, K.nZ, mval, itheta, *sub))
+    tag = () if itype == P_BCNA else ("itype", itype)
+    rng = np.random.default_rng(_seed_of(seed, "3c", key, K.nZ, mval, itheta, *sub, *tag))
     coef = rng.normal(0.0, 1.0, 30)
     amp = 0.5 / (itheta ** theta_decay) * (1.0 if isub == 0 else 0.4)
+    if itype == P_RHO_3C:
+        amp *= 0.1
     return sign * _f2d(coef, u, v, amp)
+
+
+def table3c_shell(seed, A, B, K, sa, sb, itheta, u, v, isub):
+    """Legendre coefficient itheta of the shell-level three-center density
+    (rhoS_3c, interaction 2) between shell sa of A and shell sb of B, the
+    density of shell isub of K.  The isotropic term is positive; reversing
+    the bond transposes the shells and flips the odd terms."""
+    l = itheta - 1
+    if (A.nZ, sa) == (B.nZ, sb):
+        if l % 2 == 1:
+            return np.zeros(np.broadcast(u, v).shape)
+        key, sign = (A.nZ, B.nZ, sa, sb), 1.0
+    elif (A.nZ, sa) < (B.nZ, sb):
+        key, sign = (A.nZ, B.nZ, sa, sb), 1.0
+    else:
+        key, sign = (B.nZ, A.nZ, sb, sa), (-1.0) ** l
+    rng = np.random.default_rng(_seed_of(seed, "3cS", key, K.nZ, itheta, isub))
+    a = 0.004 + 0.008 * rng.random()
+    cu, cv = 1.0 + 2.0 * rng.random(), 0.5 + rng.random()
+    base = a * np.exp(-cu * u * u - cv * v * v)
+    if l == 0:
+        return base * (1.0 + 0.2 * np.sin(3.0 * u + 2.0 * v))
+    return sign * 0.15 / itheta * base * np.sin((2.0 + l) * u + v + rng.random())
 
 
 # ---------------------------------------------------------------------------
@@ -311,7 +391,7 @@ def _fmt(vals):
 
 
 def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
-                asym_pi=False, theta_decay=1.0, dogs=False):
+                asym_pi=False, theta_decay=1.0, dogs=False, vxc=False):
     """Write a complete Harris Fdata set for ``species`` into ``path``.
 
     nx2c: 2c grid points on [0, rcA_i + rcA_j] (200 points over 10 bohr for
@@ -324,6 +404,10 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
     table, which the DOGS assemblers read.  Cells of one interaction are
     consecutive and its munu file holds one record triple per cell (the
     reference re-opens the open unit, which keeps its position).
+    vxc: also the McWEDA exchange-correlation tables: vxc_ontop, the
+    density sub-cells isorp = 1..nssh of den_ontopl / den_ontopr / den_atom
+    and of their shell-level (spherical) forms, the three-center densities
+    den3 and denS3 (shells of the third atom), and vxc_1c.ZZ.dat.
     """
     os.makedirs(path, exist_ok=True)
     ns = len(species)
@@ -379,6 +463,16 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
                                   ma if itype == P_VNA_ATOM else mm))
             if dogs:
                 cells.append((P_DIPOLE_Z, 0, "dipole_z", mm))
+            if vxc:
+                ms_ = make_munu_s(si_.lssh, sj.lssh)
+                mas = make_munu_s(si_.lssh, si_.lssh)
+                ni, nj = len(si_.lssh), len(sj.lssh)
+                cells.append((P_VXC_ONTOP, 0, "vxc_ontop", mm))
+                for itype, n, stem, mp in ((P_RHO_ONTOPL, ni, "den_ontopl", mm), (P_RHO_ONTOPR, nj, "den_ontopr", mm),
+                                           (P_RHO_ATOM, nj, "den_atom", ma), (P_RHOS_ONTOPL, ni, "denS_ontopl", ms_),
+                                           (P_RHOS_ONTOPR, nj, "denS_ontopr", ms_), (P_RHOS_ATOM, nj, "denS_atom", mas)):
+                    for isub in range(1, n + 1):
+                        cells.append((itype, isub, "%s_%02d" % (stem, isub), mp))
             # non-local pseudopotential <basis i | projector j> (every Fdata set)
             cells.append((P_VNL, 0, "vnl", make_munu(si_.lssh, sj.lssh_pp)))
             with open(os.path.join(path, "2c.%s.dat" % zz), "w") as f:
@@ -387,7 +481,8 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
             with open(os.path.join(path, "2c.%s.dir" % zz), "w") as fd:
                 for icell, (itype, isub, stem, (mu, nu, mv)) in enumerate(cells, start=1):
                     fname = "%s.%s.dat" % (stem, zz)
-                    ls_b = si_.lssh if itype == P_VNA_ATOM else sj.lssh_pp if itype == P_VNL else sj.lssh
+                    atom_like = itype in (P_VNA_ATOM, P_RHO_ATOM, P_RHOS_ATOM)
+                    ls_b = si_.lssh if atom_like else sj.lssh_pp if itype == P_VNL else sj.lssh
                     orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(ls_b)
                     xm = si_.rcA + sj.rcutoff_pp if itype == P_VNL else xmax
                     tt = np.linspace(0.0, xm, nx2c) / xm
@@ -395,6 +490,8 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
                     for ime in range(len(mu)):
                         if itype == P_VNL:
                             data[:, ime] = table2c_vnl(seed, si_, sj, orb_a[mu[ime] - 1], orb_b[nu[ime] - 1], tt)
+                        elif itype in (P_RHOS_ONTOPL, P_RHOS_ONTOPR, P_RHOS_ATOM):
+                            data[:, ime] = table2c_shell(seed, itype, si_, sj, mu[ime] - 1, nu[ime] - 1, t, isub)
                         else:
                             data[:, ime] = table2c(seed, itype, si_, sj, orb_a[mu[ime] - 1],
                                                    orb_b[nu[ime] - 1], t, asym_pi, isub)
@@ -420,33 +517,61 @@ def write_fdata(path, species, seed=20261203, nx2c=200, n3c=31,
                 zzz = "%02d.%02d.%02d" % (si_.nZ, sj.nZ, sk.nZ)
                 ymax = si_.rcA + sj.rcA                       # dbc
                 xmax = sk.rcA + max(si_.rcA, sj.rcA)          # dna
-                mu, nu, mv = make_munu_3c(si_.lssh, sj.lssh)
+                m3 = make_munu_3c(si_.lssh, sj.lssh)
                 orb_a, orb_b = _orbital_lm(si_.lssh), _orbital_lm(sj.lssh)
                 u = np.linspace(0.0, 1.0, n3c)[None, :]       # x fastest
                 v = np.linspace(0.0, 1.0, n3c)[:, None]
-                subs = list(range(0, (len(sk.lssh) if dogs else 0) + 1))
+                nk = len(sk.lssh)
+                # (itype, isub, stem, map), cells of one interaction consecutive
+                cells = [(P_BCNA, isub, "bcna", m3) for isub in range(0, (nk if dogs else 0) + 1)]
+                if vxc:
+                    cells += [(P_RHO_3C, isub, "den3", m3) for isub in range(1, nk + 1)]
+                    cells += [(P_RHOS_3C, isub, "denS3", make_munu_s(si_.lssh, sj.lssh)) for isub in range(1, nk + 1)]
                 with open(os.path.join(path, "3c.%s.dat" % zzz), "w") as f:
-                    f.write("%d\n" % (P_NTHETA * len(subs)))
-                with open(os.path.join(path, "3c.%s.dir" % zzz), "w") as fd, \
-                        open(os.path.join(path, "%02d_munu_3c.%s.dat" % (P_BCNA, zzz)), "w") as fm:
-                    for isub in subs:
+                    f.write("%d\n" % (P_NTHETA * len(cells)))
+                munu3 = {}
+                icell = 0
+                with open(os.path.join(path, "3c.%s.dir" % zzz), "w") as fd:
+                    for itype, isub, stem, (mu, nu, mv) in cells:
                         for itheta in range(1, P_NTHETA + 1):
-                            fname = "bcna_%02d_%02d.%s.dat" % (itheta, isub, zzz)
+                            icell += 1
+                            fname = "%s_%02d_%02d.%s.dat" % (stem, itheta, isub, zzz)
                             data = np.zeros((n3c, n3c, len(mu)))
                             for ime in range(len(mu)):
-                                data[:, :, ime] = table3c(seed, si_, sj, sk, orb_a[mu[ime] - 1],
-                                                          orb_b[nu[ime] - 1], mv[ime], itheta, u, v,
-                                                          theta_decay, isub)
+                                if itype == P_RHOS_3C:
+                                    data[:, :, ime] = table3c_shell(seed, si_, sj, sk, mu[ime] - 1, nu[ime] - 1,
+                                                                    itheta, u, v, isub)
+                                else:
+                                    data[:, :, ime] = table3c(seed, si_, sj, sk, orb_a[mu[ime] - 1],
+                                                              orb_b[nu[ime] - 1], mv[ime], itheta, u, v,
+                                                              theta_decay, isub, itype)
                             with open(os.path.join(path, fname), "w") as f:
                                 for iy in range(n3c):
                                     for ix in range(n3c):
                                         f.write(_fmt(data[iy, ix]) + "\n")
                             fd.write("  %2d %2d %2d %3d %-29s %3d %4d %9.6f %4d %9.6f\n"
-                                     % (isub * P_NTHETA + itheta, P_BCNA, isub, itheta, fname, len(mu),
-                                        n3c, xmax, n3c, ymax))
+                                     % (icell, itype, isub, itheta, fname, len(mu), n3c, xmax, n3c, ymax))
+                            munu3.setdefault(itype, []).append((mu, nu, mv))
+                for itype, recs in munu3.items():
+                    with open(os.path.join(path, "%02d_munu_3c.%s.dat" % (itype, zzz)), "w") as fm:
+                        for mu, nu, mv in recs:
                             fm.write(" " + " ".join("%d" % q for q in mu) + "\n")
                             fm.write(" " + " ".join("%d" % q for q in nu) + "\n")
                             fm.write(" " + " ".join("%d" % q for q in mv) + "\n")
+    if vxc:
+        # one-center xc (read_Fdata_1c, e.FDATA/M_Fdata_1c_McWEDA_Harris.f90:118-136):
+        # nssh rows of E, then nssh rows of V
+        for s in species:
+            n = len(s.lssh)
+            rng = np.random.default_rng(_seed_of(seed, "1c", s.nZ))
+            E = rng.normal(0.0, 0.3, (n, n))
+            V = rng.normal(0.0, 0.3, (n, n))
+            E = 0.5 * (E + E.T) - 8.0 * np.eye(n)
+            V = 0.5 * (V + V.T) - 6.0 * np.eye(n)
+            with open(os.path.join(path, "vxc_1c.%02d.dat" % s.nZ), "w") as f:
+                for M in (E, V):
+                    for r in M:
+                        f.write(_fmt(r) + "\n")
     return path
 
 
@@ -575,17 +700,18 @@ def batch_structures(nstruct=256, seed=SEED_BATCH):
     return out
 
 
-def fdata_dir_for(workload, root=None, dogs=False):
+def fdata_dir_for(workload, root=None, dogs=False, vxc=False):
     """Generate (once) and return the Fdata directory of a workload (with
-    the DOGS sub-cells and dipole table when dogs is set)."""
+    the DOGS sub-cells and dipole table when dogs is set, the McWEDA
+    exchange-correlation tables when vxc is set)."""
     root = root or os.environ.get("FBGPU_FDATA_ROOT") or os.path.join(
         os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "_fdata")
     key = {"si64": "Si_rc50", "si512": "Si_rc50", "cho1536": "CHO_rc45_40_40",
            "sic4096": "SiC_rc50", "batch256": "SiC_rc50"}[workload]
-    path = os.path.join(root, key + ("_DOGS" if dogs else ""))
+    path = os.path.join(root, key + ("_DOGS" if dogs else "") + ("_VXC" if vxc else ""))
     stamp = os.path.join(path, ".complete_vnl")
     if not os.path.exists(stamp):
-        write_fdata(path, species_for(workload), dogs=dogs)
+        write_fdata(path, species_for(workload), dogs=dogs, vxc=vxc)
         with open(stamp, "w") as f:
             f.write("ok\n")
     return path
