@@ -461,6 +461,7 @@ def run_gpu(args):
         line["bloch"] = bloch_measure(ctx, torch, stream, local)
         line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
         line["vnl"] = vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=args.no_cpu)
+        line["vxc"] = vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=args.no_cpu)
     if args.mlp_epochs > 0:
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
@@ -652,6 +653,54 @@ def vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=F
         out["max_abs_dftot_ev_per_A"] = float(np.abs(f_gpu - d["ftot_vnl"]).max())
         out["cpu_oracle"] = {"value": round(s.nppp / t, 1), "unit": "vnl blocks (PPp pairs)/s", "cores": 1,
                              "kind": "port", "sample": "1 vnl step (maps + value + force pass), %.3f s" % t}
+    return out
+
+
+def vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=False):
+    """The McWEDA exchange-correlation step (Harris) on the same structure,
+    with the Fdata set that carries the McWEDA tables: neighbors, then the
+    overlap, the input densities (2c + 3c) and the vxc blocks as one graph
+    launch; its agreement with the oracle and the oracle's time for the
+    same step on one core."""
+    from fbgpu import synth
+    path = synth.fdata_dir_for(args.workload, root=fdata_root(), vxc=True)
+    ctx = fbgpu.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    P, T, _ = ctx.driver_neighbors()
+    what = fbgpu.FB_S | fbgpu.FB_VXC
+
+    def step():
+        ctx.driver_neighbors()
+        ctx.assemble_graph(what)
+
+    timed = make_timer(torch, ctx, stream, flush, 1, local)
+    for _ in range(max(3, args.warmup)):
+        step()
+    ms, launches = timed(step, args.steps)
+    timed(lambda: (ctx.driver_neighbors(), ctx.assemble(what)), args.steps, timing=True)
+    kt = ctx.timing()
+    ctx.set_timing(False)
+    out = {"what": "McWEDA vxc (Harris): overlap, rho_in / rho_bond and weighted densities (2c + 3c), "
+                   "Ceperley-Alder SN terms, vxc_bond; FP64",
+           "ms_per_step": round(ms / args.steps, 4), "value": round(P * args.steps / (ms * 1e-3), 1),
+           "unit": "neighbor blocks/s", "gpu_launches_per_step": launches // max(1, args.steps),
+           "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+    vxc = ctx.blocks("vxc")
+    ctx.close()
+    if no_cpu or st.natoms > 1024:
+        out["cpu_oracle"] = "not run (single-core oracle bounded to systems of at most 1024 atoms)"
+    else:
+        from oracle import oracle as orc
+        fd = orc.Fdata(path, nZ)
+        t0 = time.perf_counter()
+        s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+        ref = s.assemble_vxc()
+        t = time.perf_counter() - t0
+        out["max_abs_dvxc_ev"] = float(np.abs(vxc - ref["vxc"]).max())
+        out["cpu_oracle"] = {"value": round(s.npairs / t, 1), "unit": "neighbor blocks/s", "cores": 1,
+                             "kind": "port", "sample": "1 vxc step (neighbors + overlap + densities + vxc), %.3f s" % t}
     return out
 
 

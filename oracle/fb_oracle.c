@@ -55,6 +55,8 @@ enum {
 
 static __thread char g_err[512];
 static int g_threads = 1;
+/* test switch (or_set_exact_derivatives): 0 keeps the reference's forms */
+static int g_exact = 0;
 
 static void seterr(const char *fmt, ...) {
   va_list ap;
@@ -64,6 +66,7 @@ static void seterr(const char *fmt, ...) {
 }
 const char *or_last_error(void) { return g_err; }
 void or_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+void or_set_exact_derivatives(int on) { g_exact = on ? 1 : 0; }
 
 /* ------------------------------------------------------------------------ */
 /* data types: T_Fdata_cell_2c/bundle (e.FDATA/M_Fdata_2c.f90:83-109),       */
@@ -712,7 +715,7 @@ static int getMEs_3c_body(or_fdata *fd, int isp, int jsp, int ksp, int iint, int
     c = get_cell3c(fd, isp, jsp, ksp, iint, isub, it);
     if (!c || c->nME != nME) { seterr("missing 3c theta cell %d", it); return E_TABLE; }
     double pt = p[it - 1], Dpt = Dp[it - 1];
-    if (gg < P_tiny) {                                              /* :406-410, :684-691 */
+    if (!g_exact && gg < P_tiny) {                                  /* :406-410, :684-691 */
       for (int m = 0; m < nME; m++) {
         interim[m] = ((1.0 - px - py) * F3(c, ix, iy, m) + px * F3(c, ix + 1, iy, m) + py * F3(c, ix, iy + 1, m));
         Fd[m] = Fd[m] + pt * interim[m];
@@ -3172,7 +3175,8 @@ void or_lda_ceperley_alder(double rh, double *out) {
     d3den = (0.75) * 1.0529 / (2.0 * (rs * rs) * sqrs);
     dec = 0.1423 * dden / (den * den);
     ddec = -2.0 * 0.1423 * dden * dden / (den * den * den) + 0.1423 * d2den / (den * den);
-    d2dec = 6.0 * 0.1423 * (dden * 3) / (den * den * den * den) - 6.0 * 0.1423 * dden * d2den / (den * den * den) +
+    double dd3 = g_exact ? dden * dden * dden : dden * 3; /* the reference's form is (dden*3) */
+    d2dec = 6.0 * 0.1423 * dd3 / (den * den * den * den) - 6.0 * 0.1423 * dden * d2den / (den * den * den) +
             0.1423 * d3den / (den * den);
   } else {
     rsl = log(rs);
@@ -3431,5 +3435,283 @@ int or_assemble_vxc(or_sys *s, const double *S, const double *rho_in, const doub
       if (bond) for (int k = 0; k < nmu * nnu; k++) bond[o + k] = vb[k];
     }
   }
+  return err;
+}
+
+/* ------------------------------------------------------------------------ */
+/* McWEDA force pass (Harris): Dassemble_vxc                                 */
+/* (k.DASSEMBLERS/M_Dassemble_vxc_McWEDA_Harris.f90:102-810, with            */
+/* Dassemble_rho_2c / Dassemble_rho_weighted_2c of                           */
+/* k.DASSEMBLERS/M_Dassemble_rho_McWEDA_Harris.f90:96-710 and                */
+/* Dassemble_vxc_3c of k.DASSEMBLERS/M_Dassemble_vxc_3c_McWEDA_Harris.f90).  */
+/* Inputs: the density matrix, the overlap S and its Dblocks dS, and the     */
+/* value pass's rho_in, rho_bond and weighted densities.  Outputs: the pair  */
+/* forces vxc_off_site(3, p) and vxc_on_site(3, p) and the three-center     */
+/* forces f3xca/b/c (3 N, overwritten).                                      */
+/* ------------------------------------------------------------------------ */
+
+/* derivative of a 2c density interaction summed over the shells of the
+ * atom isp_q with Qneutral weights, rotated as (in1, in3): out(3, nmu, nnu) */
+static int d_rho_sum(or_fdata *fd, int in1, int in2, int in3, int iint, int qsp, double z, const double *eps,
+                     const double *deps, const double *eta, int nmu, int nnu, int rotate_it, double *out) {
+  double mm[MAXORB * MAXORB], dm[MAXORB * MAXORB], vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+  for (int k = 0; k < 3 * nmu * nnu; k++) out[k] = 0.0, vdm[k] = 0.0;
+  for (int isorp = 1; isorp <= fd->sp[qsp].nssh; isorp++) {
+    double Q = fd->sp[qsp].qn[isorp - 1];
+    int st = or_getDMEs_2c(fd, in1, in2, iint, isorp, z, nmu, nnu, mm, dm);
+    if (st) return st;
+    for (int inu = 0; inu < nnu; inu++)
+      for (int imu = 0; imu < nmu; imu++)
+        if (z > 1.0e-3)
+          for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+    if (rotate_it) {
+      drotate(fd, in1, in3, eps, deps, nmu, nnu, mm, vdm, vdx);
+      for (int k = 0; k < 3 * nmu * nnu; k++) out[k] = out[k] + vdx[k] * Q;
+    } else {
+      for (int k = 0; k < 3 * nmu * nnu; k++) out[k] = out[k] + vdm[k] * Q;
+    }
+  }
+  return OK;
+}
+
+int or_dassemble_vxc(or_sys *s, const double *rho, const double *S, const double *dS, const double *rho_in,
+                     const double *rho_bond, const double *wrho_in, const double *wrho_bond, double *off_site,
+                     double *on_site, double *f3xca, double *f3xcb, double *f3xcc) {
+  or_fdata *fd = s->fd;
+  int N = s->natoms, P = s->npairs, err = OK;
+  int mo = 1;
+  for (int k = 1; k <= fd->nspecies; k++) if (fd->sp[k].norb_max > mo) mo = fd->sp[k].norb_max;
+  size_t sa = (size_t)3 * mo * mo;
+  /* Dassemble_rho_2c: ontop Dblocko (blk layout, 3 per element; rho_in and
+   * rho_bond share it) and the atom case Dblock of each pair (3 nmu nmu) */
+  double *drho_o = (double *)calloc((size_t)3 * s->nblock + 1, sizeof(double));
+  double *drho_a = (double *)calloc(sa * P + 1, sizeof(double));
+  /* Dassemble_rho_weighted_2c: ontop Dblocko and atom Dblock, 3 x 9 per pair */
+  double *dw_o = (double *)calloc((size_t)27 * P + 1, sizeof(double));
+  double *dw_a = (double *)calloc((size_t)27 * P + 1, sizeof(double));
+  for (int i = 0; i < N && !err; i++) {
+    double r1[3], r2[3], z, eps[9], deps[27], eta[3], tmp[3 * MAXORB * MAXORB];
+    int in1 = s->imass[i], nmu = fd->sp[in1].norb_max, ni = fd->sp[in1].nssh, st;
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      int nnu = fd->sp[in2].norb_max, nj = fd->sp[in2].nssh;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      pair_frame(s, i, p, r1, r2, &z, eps);
+      or_depsilon_2c(r1, r2, z, eps, deps);
+      for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+      long long o = s->blk_off[p];
+      /* :141-196 ontop left + right */
+      if ((st = d_rho_sum(fd, in1, in2, in2, P_rho_ontopL, in1, z, eps, deps, eta, nmu, nnu, 1, tmp))) { err = st; break; }
+      for (int k = 0; k < 3 * nmu * nnu; k++) drho_o[3 * o + k] = drho_o[3 * o + k] + tmp[k];
+      if ((st = d_rho_sum(fd, in1, in2, in2, P_rho_ontopR, in2, z, eps, deps, eta, nmu, nnu, 1, tmp))) { err = st; break; }
+      for (int k = 0; k < 3 * nmu * nnu; k++) drho_o[3 * o + k] = drho_o[3 * o + k] + tmp[k];
+      /* :245-281 atom case of this neighbor */
+      if ((st = d_rho_sum(fd, in1, in2, in1, P_rho_atom, in2, z, eps, deps, eta, nmu, nmu, 1, tmp))) { err = st; break; }
+      memcpy(drho_a + sa * p, tmp, sizeof(double) * 3 * nmu * nmu);
+      /* weighted :505-551 and :610-636, no rotations */
+      if ((st = d_rho_sum(fd, in1, in2, in2, P_rhoS_ontopL, in1, z, eps, deps, eta, ni, nj, 0, tmp))) { err = st; break; }
+      for (int k = 0; k < 3 * ni * nj; k++) dw_o[27 * p + k] = dw_o[27 * p + k] + tmp[k];
+      if ((st = d_rho_sum(fd, in1, in2, in2, P_rhoS_ontopR, in2, z, eps, deps, eta, ni, nj, 0, tmp))) { err = st; break; }
+      for (int k = 0; k < 3 * ni * nj; k++) dw_o[27 * p + k] = dw_o[27 * p + k] + tmp[k];
+      if ((st = d_rho_sum(fd, in1, in2, in1, P_rhoS_atom, in2, z, eps, deps, eta, ni, ni, 0, tmp))) { err = st; break; }
+      memcpy(dw_a + 27 * p, tmp, sizeof(double) * 3 * ni * ni);
+    }
+  }
+  for (int k = 0; k < 3 * P; k++) off_site[k] = 0.0, on_site[k] = 0.0;
+  /* Dassemble_vxc_SN (:203-616) and Dassemble_vxc_bond (:638-810) */
+  for (int i = 0; i < N && !err; i++) {
+    const species_t *A = &fd->sp[s->imass[i]];
+    int in1 = s->imass[i], nmu = A->norb_max, ni = A->nssh, st;
+    int ps = s->pair_off[i] + s->neigh_self[i];
+    long long os = s->blk_off[ps];
+    double lin[6], lbo[6];
+    for (int in = 0; in < s->neighn[i]; in++) {
+      int p = s->pair_off[i] + in, j = s->neigh_j[p], in2 = s->imass[j];
+      const species_t *B = &fd->sp[in2];
+      int nnu = B->norb_max;
+      long long o = s->blk_off[p];
+      double *fo = off_site + 3 * (size_t)p, *fn = on_site + 3 * (size_t)p;
+      if (i == j && s->neigh_b[p] == 0) continue;
+      /* off-site SN (:289-356) */
+      int n1 = 0;
+      for (int a = 0; a < ni; a++) {
+        int l1 = A->lssh[a];
+        n1 = n1 + l1 + 1;
+        int n2 = 0;
+        for (int b = 0; b < B->nssh; b++) {
+          int l2 = B->lssh[b];
+          n2 = n2 + l2 + 1;
+          double wi = wrho_in[WSH * p + a + ni * b], wb = wrho_bond[WSH * p + a + ni * b];
+          const double *dwi = dw_o + 27 * (size_t)p + 3 * (a + ni * b), *dwb = dwi;
+          or_lda_ceperley_alder(wi, lin);
+          or_lda_ceperley_alder(wb, lbo);
+          for (int m1 = -l1; m1 <= l1; m1++)
+            for (int m2 = -l2; m2 <= l2; m2++) {
+              int imu = n1 + m1 - 1, inu = n2 + m2 - 1, q = imu + nmu * inu;
+              double ov = S[o + q], ri = rho_in[o + q], rb = rho_bond[o + q], r = rho[o + q];
+              const double *dov = dS + 3 * (o + q), *dri = drho_o + 3 * (o + q), *drb = dri;
+              for (int c = 0; c < 3; c++) {
+                fo[c] = fo[c] - r * (dov[c] * (lin[1] - lin[4] * wi) + dwi[c] * lin[5] * (ri - wi * ov) + lin[4] * dri[c]);
+                fo[c] = fo[c] + r * (dov[c] * (lbo[1] - lbo[4] * wb) + dwb[c] * lbo[5] * (rb - wb * ov) + lbo[4] * drb[c]);
+              }
+            }
+          n2 = n2 + l2;
+        }
+        n1 = n1 + l1;
+      }
+      /* on-site SN for this neighbor (:360-606) */
+      n1 = 0;
+      for (int a = 0; a < ni; a++) {
+        int l1 = A->lssh[a];
+        n1 = n1 + l1 + 1;
+        {
+          double wi = wrho_in[WSH * ps + a + ni * a], wb = wrho_bond[WSH * ps + a + ni * a];
+          /* Dblocko of the self pair: never assembled, zero */
+          const double *dwi = dw_o + 27 * (size_t)ps + 3 * (a + ni * a), *dwb = dwi;
+          or_lda_ceperley_alder(wi, lin);
+          or_lda_ceperley_alder(wb, lbo);
+          for (int m1 = -l1; m1 <= l1; m1++) {
+            int imu = n1 + m1 - 1, q = imu + nmu * imu;
+            double pri = rho_in[os + q], prb = rho_bond[os + q], r = rho[os + q];
+            const double *dri = drho_a + sa * p + 3 * q;
+            for (int c = 0; c < 3; c++) {
+              fn[c] = fn[c] - r * (lin[4] * dri[c] + dwi[c] * lin[5] * (pri - wi));
+              fn[c] = fn[c] + r * (lbo[4] * dwb[c] + dwb[c] * lbo[5] * (prb - wb));
+            }
+          }
+        }
+        int n2 = 0;
+        for (int b = 0; b < ni; b++) {
+          int l2 = A->lssh[b];
+          n2 = n2 + l2 + 1;
+          double wi = wrho_in[WSH * ps + a + ni * b], wb = wrho_bond[WSH * ps + a + ni * b];
+          const double *dwi = dw_a + 27 * (size_t)p + 3 * (a + ni * b), *dwb = dwi;
+          or_lda_ceperley_alder(wi, lin);
+          or_lda_ceperley_alder(wb, lbo);
+          for (int m1 = -l1; m1 <= l1; m1++)
+            for (int m2 = -l2; m2 <= l2; m2++) {
+              int imu = n1 + m1 - 1, inu = n2 + m2 - 1, q = imu + nmu * inu;
+              if (imu == inu) continue;
+              double pri = rho_in[os + q], prb = rho_bond[os + q], r = rho[os + q];
+              const double *dri = drho_a + sa * p + 3 * q, *drb = dri;
+              for (int c = 0; c < 3; c++) {
+                fn[c] = fn[c] - r * (dwi[c] * lin[5] * pri + lin[4] * dri[c]);
+                fn[c] = fn[c] + r * (dwb[c] * lbo[5] * prb + lbo[4] * drb[c]);
+              }
+            }
+          n2 = n2 + l2;
+        }
+        n1 = n1 + l1;
+      }
+      /* Dassemble_vxc_bond (:735-790) */
+      {
+        double r1[3], r2[3], z, eps[9], deps[27], eta[3], mm[MAXORB * MAXORB], dm[MAXORB * MAXORB];
+        double vdm[3 * MAXORB * MAXORB], vdx[3 * MAXORB * MAXORB];
+        pair_frame(s, i, p, r1, r2, &z, eps);
+        or_depsilon_2c(r1, r2, z, eps, deps);
+        for (int k = 0; k < 3; k++) eta[k] = E2(eps, k, 2);
+        for (int k = 0; k < 3 * nmu * nnu; k++) vdm[k] = 0.0;
+        if ((st = or_getDMEs_2c(fd, in1, in2, P_vxc_ontop, 0, z, nmu, nnu, mm, dm))) { err = st; break; }
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            if (z > 1.0e-3)
+              for (int c = 0; c < 3; c++) vdm[c + 3 * (imu + nmu * inu)] = -eta[c] * dm[imu + nmu * inu];
+        drotate(fd, in1, in2, eps, deps, nmu, nnu, mm, vdm, vdx);
+        for (int inu = 0; inu < nnu; inu++)
+          for (int imu = 0; imu < nmu; imu++)
+            for (int c = 0; c < 3; c++)
+              fo[c] = fo[c] - rho[o + imu + nmu * inu] * vdx[c + 3 * (imu + nmu * inu)];
+      }
+    }
+  }
+  /* Dassemble_vxc_3c (M_Dassemble_vxc_3c_McWEDA_Harris.f90:97-514) */
+  for (int k = 0; k < 3 * N; k++) f3xca[k] = f3xcb[k] = f3xcc[k] = 0.0;
+  for (int ia = 0; ia < N && !err; ia++) {
+    double mm[MAXORB * MAXORB], dpm[MAXORB * MAXORB], dxm[MAXORB * MAXORB], dym[MAXORB * MAXORB];
+    double Ma[3 * MAXORB * MAXORB], Mb[3 * MAXORB * MAXORB], Xa[3 * MAXORB * MAXORB], Xb[3 * MAXORB * MAXORB];
+    double rxa[3 * MAXORB * MAXORB], rxb[3 * MAXORB * MAXORB], rsa[27], rsb[27];
+    double depsA[27], depsB[27], amt[3], bmt[3], lin[6];
+    for (int t = s->trip_off[ia]; t < s->trip_off[ia + 1] && !err; t++) {
+      trip_t g;
+      trip_frame(s, ia, t, &g);
+      int nmu = fd->sp[g.in1].norb_max, nnu = fd->sp[g.in2].norb_max;
+      int ni = fd->sp[g.in1].nssh, nj = fd->sp[g.in2].nssh, nk = fd->sp[g.indna].nssh;
+      int p = s->pair_off[g.iatom] + g.mneigh;
+      long long o = s->blk_off[p];
+      or_depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.eps, depsA, depsB);
+      for (int k = 0; k < 3 * nmu * nnu; k++) rxa[k] = rxb[k] = 0.0;
+      for (int k = 0; k < 27; k++) rsa[k] = rsb[k] = 0.0;
+      for (int isorp = 1; isorp <= nk; isorp++) { /* :262-310 */
+        double Q = fd->sp[g.indna].qn[isorp - 1];
+        int st = or_getDMEs_3c(fd, g.in1, g.in2, g.indna, P_rho_3c, isorp, g.x, g.z, nmu, nnu, g.cost, mm, dpm, dxm,
+                               dym);
+        if (st) { err = st; break; }
+        if (g.x > 1.0e-5)
+          for (int k = 0; k < 3; k++) amt[k] = (g.sighat[k] - g.cost * g.rhat[k]) / g.x;
+        else
+          amt[0] = amt[1] = amt[2] = 0.0;
+        for (int k = 0; k < 3; k++) bmt[k] = (g.cost * g.sighat[k] - g.rhat[k]) / g.z;
+        for (int k = 0; k < 3 * nmu * nnu; k++) Ma[k] = Mb[k] = 0.0;
+        cell3c *c = get_cell3c(fd, g.in1, g.in2, g.indna, P_rho_3c, isorp, 1);
+        for (int m = 0; m < c->nME; m++) {
+          int k = (c->mu[m] - 1) + nmu * (c->nu[m] - 1);
+          for (int q = 0; q < 3; q++) Ma[q + 3 * k] = g.rhat[q] * dxm[k] + amt[q] * dpm[k];
+          for (int q = 0; q < 3; q++) Mb[q + 3 * k] = -g.sighat[q] * dym[k] + bmt[q] * dpm[k] - Ma[q + 3 * k] / 2.0;
+        }
+        drotate(fd, g.in1, g.in2, g.eps, depsA, nmu, nnu, mm, Ma, Xa);
+        drotate(fd, g.in1, g.in2, g.eps, depsB, nmu, nnu, mm, Mb, Xb);
+        for (int k = 0; k < 3 * nmu * nnu; k++) rxa[k] = rxa[k] + Xa[k] * Q, rxb[k] = rxb[k] + Xb[k] * Q;
+      }
+      if (err) break;
+      for (int isorp = 1; isorp <= nk; isorp++) { /* :330-368 */
+        double Q = fd->sp[g.indna].qn[isorp - 1];
+        int st = or_getDMEs_3c(fd, g.in1, g.in2, g.indna, P_rhoS_3c, isorp, g.x, g.z, ni, nj, g.cost, mm, dpm, dxm,
+                               dym);
+        if (st) { err = st; break; }
+        for (int a = 0; a < ni; a++)
+          for (int b = 0; b < nj; b++) {
+            int k = a + ni * b;
+            for (int q = 0; q < 3; q++) {
+              double va = g.rhat[q] * dxm[k] + amt[q] * dpm[k];
+              double bq = (g.cost * g.sighat[q] - g.rhat[q]) / g.z;
+              double vb = -g.sighat[q] * dym[k] + bq * dpm[k] - va / 2.0;
+              rsa[q + 3 * k] = rsa[q + 3 * k] + va * Q;
+              rsb[q + 3 * k] = rsb[q + 3 * k] + vb * Q;
+            }
+          }
+      }
+      if (err) break;
+      const species_t *A = &fd->sp[g.in1], *B = &fd->sp[g.in2];
+      int n1 = 0;
+      for (int a = 0; a < ni; a++) { /* :371-402 */
+        int l1 = A->lssh[a];
+        n1 = n1 + l1 + 1;
+        int n2 = 0;
+        for (int b = 0; b < nj; b++) {
+          int l2 = B->lssh[b];
+          n2 = n2 + l2 + 1;
+          double w = wrho_in[WSH * p + a + ni * b];
+          or_lda_ceperley_alder(w, lin);
+          const double *pa_ = rsa + 3 * (a + ni * b), *pb_ = rsb + 3 * (a + ni * b);
+          for (int m1 = -l1; m1 <= l1; m1++)
+            for (int m2 = -l2; m2 <= l2; m2++) {
+              int imu = n1 + m1 - 1, inu = n2 + m2 - 1, q = imu + nmu * inu;
+              double dev = rho_in[o + q] - w * S[o + q], r = rho[o + q];
+              for (int c = 0; c < 3; c++) {
+                double mxa = lin[4] * rxa[c + 3 * q] + pa_[c] * lin[5] * dev;
+                double mxb = lin[4] * rxb[c + 3 * q] + pb_[c] * lin[5] * dev;
+                double mxc = -mxa - mxb;
+                f3xca[3 * ia + c] = f3xca[3 * ia + c] - r * mxa;
+                f3xcb[3 * g.iatom + c] = f3xcb[3 * g.iatom + c] - r * mxb;
+                f3xcc[3 * g.jatom + c] = f3xcc[3 * g.jatom + c] - r * mxc;
+              }
+            }
+          n2 = n2 + l2;
+        }
+        n1 = n1 + l1;
+      }
+    }
+  }
+  free(drho_o); free(drho_a); free(dw_o); free(dw_a);
   return err;
 }

@@ -166,6 +166,16 @@ int or_assemble_vxc(or_sys *s, const double *S, const double *rho_in,
                     const double *rho_bond, const double *wrho_in,
                     const double *wrho_bond, double *vxc, double *sn,
                     double *snb, double *bond);
+/* McWEDA force pass (Dassemble_vxc, k.DASSEMBLERS/M_Dassemble_vxc_McWEDA_Harris.f90,
+ * with Dassemble_rho_2c / _weighted_2c and Dassemble_vxc_3c): from the density
+ * matrix, S and its Dblocks dS (3 per element) and the value pass's
+ * densities; vxc_off_site and vxc_on_site (3 per pair) and f3xca/b/c (3 N) */
+int or_dassemble_vxc(or_sys *s, const double *rho, const double *S,
+                     const double *dS, const double *rho_in,
+                     const double *rho_bond, const double *wrho_in,
+                     const double *wrho_bond, double *off_site,
+                     double *on_site, double *f3xca, double *f3xcb,
+                     double *f3xcc);
 
 /* pointwise interpolators (module M_Fdata_2c / M_Fdata_3c); hmbox etc are
  * norb_mu x norb_nu column-major */
@@ -189,6 +199,16 @@ void or_depsilon_3c(const double *r1, const double *r2, const double *r21,
                     const double *eps3, double *dera3, double *der13);
 void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu,
                int norb_nu, const double *mmatrix, double *xmatrix);
+
+/* Test switch, off by default: 1 replaces the reference's two forms that are
+ * not the derivative of its values -- the (dden*3) of d2dec in
+ * lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:143) and the
+ * three-point linear branch of getMEs/getDMEs_Fdata_3c
+ * (e.FDATA/M_Fdata_3c.f90:406-410, :684-691), whose x / y derivatives use
+ * one scalar gradient for every matrix element -- by exact ones (dden**3,
+ * the bicubic everywhere), so finite differences can check the rest of a
+ * force restatement. */
+void or_set_exact_derivatives(int on);
 
 /* OpenMP thread count for the assemblers (1 = serial reference order) */
 void or_set_threads(int n);

@@ -84,6 +84,7 @@ def lib():
         L.or_lda_ceperley_alder.argtypes = [C.c_double, _dp]
         L.or_assemble_rho_2c.argtypes = [C.c_void_p] + [_dp] * 4
         L.or_assemble_rho_3c.argtypes = [C.c_void_p] + [_dp] * 2
+        L.or_dassemble_vxc.argtypes = [C.c_void_p] + [_dp] * 12
         L.or_assemble_vxc.argtypes = [C.c_void_p] + [_dp] * 6 + [C.c_void_p] * 3
         L.or_getMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
         L.or_getDMEs_2c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
@@ -97,6 +98,7 @@ def lib():
         L.or_depsilon_3c.argtypes = [_dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp]
         L.or_rotate.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, C.c_int, _dp, _dp]
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_set_exact_derivatives.argtypes = [C.c_int]
         L.or_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -338,6 +340,30 @@ class System:
         else:
             _check(L.or_assemble_vxc(self.h, S, ri, rb, wi, wb, vxc, None, None, None))
         return out
+
+    def dassemble_vxc(self, rho):
+        """McWEDA force pass: dict(vxc_off_site, vxc_on_site (3 per pair),
+        f3xca, f3xcb, f3xcc, and vxc, the pair sums build_forces makes of
+        them (off + on site on i, minus on j), and ftot_add = vxc + f3xc)."""
+        L = lib()
+        N, nb, P = len(self.imass), self.nblock, self.npairs
+        r = self.assemble_vxc()
+        rho = np.ascontiguousarray(rho, np.float64)
+        dS, dT = np.zeros(3 * nb), np.zeros(3 * nb)
+        _check(L.or_dassemble_2c(self.h, rho, dS, dT, np.zeros(3 * P), np.zeros(3 * P)))
+        off, on = np.zeros(3 * P), np.zeros(3 * P)
+        fa, fb, fc = np.zeros(3 * N), np.zeros(3 * N), np.zeros(3 * N)
+        wi = np.ascontiguousarray(r["wrho_in"].ravel())
+        wb = np.ascontiguousarray(r["wrho_bond"].ravel())
+        _check(L.or_dassemble_vxc(self.h, rho, r["S"], dS, r["rho_in"], r["rho_bond"], wi, wb, off, on, fa, fb, fc))
+        pair = (off + on).reshape(P, 3)
+        vxc = np.zeros((N, 3))
+        for i in range(N):
+            for p in range(self.pair_off[i], self.pair_off[i + 1]):
+                vxc[i] += pair[p]
+                vxc[self.neigh_j[p]] -= pair[p]
+        return dict(vxc_off_site=off, vxc_on_site=on, f3xca=fa, f3xcb=fb, f3xcc=fc, vxc=vxc.ravel(),
+                    ftot_add=vxc.ravel() + fa + fb + fc, values=r)
 
     # ---- non-local pseudopotential (vnl) --------------------------------
     def neighbors_pp(self):

@@ -82,6 +82,10 @@ def test_vxc_errors(ctx, fdata_root):
     with pytest.raises(fbgpu.FBError) as e:      # the overlap first
         ctx.assemble(fbgpu.FB_VXC)
     assert e.value.code == 11
+    both, _, _ = workload("sic_small", fdata_root, dogs=True, vxc=True)  # DOGS and McWEDA tables
+    ctx.read_Fdata(both, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
     ctx.set_theory(fbgpu.FB_THEORY_DOGS)
     with pytest.raises(fbgpu.FBError) as e:      # McWEDA Harris only
         ctx.assemble(fbgpu.FB_S | fbgpu.FB_VXC)
