@@ -130,6 +130,12 @@ extern "C" {
 #define FB_F_EWALDSR 15    /* forces(i)%ewaldsr(3, neighn), per pair (DOGS, FB_EWALD) */
 #define FB_F_EWALDLR 16    /* forces(i)%ewaldlr (DOGS, FB_EWALD) */
 #define FB_F_EWALD 17      /* forces(i)%ewald, the Ewald energy force of Dassemble_ewald (DOGS, FB_EWALD) */
+#define FB_F_VXC 18        /* forces(i)%vxc: the vxc_off_site + vxc_on_site pair sums (FB_VXC) */
+#define FB_F_F3XCA 19      /* forces(i)%f3xca (FB_VXC) */
+#define FB_F_F3XCB 20      /* forces(i)%f3xcb (FB_VXC) */
+#define FB_F_F3XCC 21      /* forces(i)%f3xcc (FB_VXC) */
+#define FB_F_VXC_OFF_SITE 22 /* forces(i)%vxc_off_site(3, neighn), per pair (FB_VXC) */
+#define FB_F_VXC_ON_SITE 23  /* forces(i)%vxc_on_site(3, neighn), per pair (FB_VXC) */
 
 typedef struct fb_ctx fb_ctx;
 

@@ -74,6 +74,35 @@ def test_vxc_after_overlap(ctx, fdata_root):
     _check(ctx, ref, s.npairs)
 
 
+@pytest.mark.parametrize("name", ["sic_small", "si64", "cho_small", "sic_vac", "sic_cluster"])
+def test_vxc_forces_match_oracle(ctx, fdata_root, name):
+    """Dassemble_vxc: the pair forces vxc_off_site / vxc_on_site, f3xca/b/c,
+    the vxc pair sums and their addition to ftot, plain and as one graph."""
+    from conftest import symmetric_denmat
+    path, nZ, st = case(fdata_root, name)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
+    rho, cape = symmetric_denmat(s, np.array([fd.norb(int(q)) for q in st.imass]), 5)
+    ref = s.dassemble_vxc(rho)
+    harris = s.dassemble(rho, cape)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice, st.icluster)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    ctx.set_denmat(rho, cape)
+    what = fbgpu.FB_ALL | fbgpu.FB_VXC
+    ctx.assemble(what)
+    ctx.Dassemble(what)
+    for k in ("vxc_off_site", "vxc_on_site", "f3xca", "f3xcb", "f3xcc", "vxc"):
+        assert np.abs(ctx.forces(k) - ref[k]).max() <= TOL, k
+    want = harris["ftot"] + ref["ftot_add"]
+    assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+    for _ in range(2):  # value and force pass as one graph
+        ctx.assemble_graph(what | fbgpu.FB_FORCES)
+        assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+        assert np.abs(ctx.forces("vxc_on_site") - ref["vxc_on_site"]).max() <= TOL
+
+
 def test_vxc_errors(ctx, fdata_root):
     path, nZ, st = case(fdata_root, "sic_small")
     ctx.read_Fdata(path, nZ)

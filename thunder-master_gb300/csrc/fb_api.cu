@@ -30,13 +30,14 @@ std::atomic<long long> g_alloc_gen{0};
 enum { KT_NEIGH_COUNT, KT_NEIGH_FILL, KT_NEIGH_BACK, KT_COMMON_COUNT, KT_COMMON_FILL, KT_ASM2C, KT_ASM3C,
        KT_DASM2C, KT_DASM3C, KT_FORCES, KT_TRIP_BINS, KT_SPLIT_RHO, KT_MLP_EVAL, KT_ASM3C_MLP, KT_DASM3C_MLP,
        KT_BLOCH, KT_PP_PAIRS, KT_PPP, KT_PPC, KT_SVNL, KT_VNL2C, KT_VNL3C, KT_DSVNL, KT_DVNL2C, KT_DVNL3C,
-       KT_VNLF, KT_EWALD, KT_EWALD_BLOCKS, KT_RHO2C, KT_RHO3C, KT_VXC, KT_N };
+       KT_VNLF, KT_EWALD, KT_EWALD_BLOCKS, KT_RHO2C, KT_RHO3C, KT_VXC, KT_DVXC2C, KT_DVXC3C, KT_VXCF, KT_N };
 static const char *kt_names[KT_N] = {"neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fill",
                                      "assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c",
                                      "build_forces", "trip_bins", "split_rho", "mlp_eval", "assemble_3c_mlp",
                                      "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
                                      "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald",
-                                     "ewald_blocks", "rho_2c", "rho_3c", "vxc"};
+                                     "ewald_blocks", "rho_2c", "rho_3c", "vxc", "dvxc_2c", "dvxc_3c",
+                                     "vxc_forces"};
 // kernels with a tunable launch shape
 enum { TK_A2C, TK_A3C, TK_D2C, TK_D3C, TK_N };
 static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c", "dassemble_3c"};
@@ -100,6 +101,7 @@ struct fb_ctx {
   DevBuf d_q0a, d_dewald, d_ew_w, d_sum_dewald, d_ew_cw, d_fewald, d_fsr, d_flr;
   // McWEDA exchange-correlation (Harris): input densities and vxc blocks
   DevBuf d_rho_in, d_rho_bond, d_wrho_in, d_wrho_bond, d_vxc;
+  DevBuf d_vxc_off, d_vxc_on, d_vxc_wd, d_vxc_gd, d_f3xa, d_f3xb, d_f3xc, d_fvxc;
   bool have_charges = false, have_dip = false;
   bool have_vna2c = false, have_rho = false, have_cape = false, have_dblocks = false;
   unsigned assembled = 0, dassembled = 0;
@@ -1055,6 +1057,14 @@ static VxcArgs vxc_args(fb_ctx *ctx) {
   v.wrho_in = ctx->d_wrho_in.as<double>();
   v.wrho_bond = ctx->d_wrho_bond.as<double>();
   v.vxc = ctx->d_vxc.as<double>();
+  v.off = ctx->d_vxc_off.as<double>();
+  v.on = ctx->d_vxc_on.as<double>();
+  v.wd = ctx->d_vxc_wd.as<double>();
+  v.gd = ctx->d_vxc_gd.as<double>();
+  v.f3a = ctx->d_f3xa.as<double>();
+  v.f3b = ctx->d_f3xb.as<double>();
+  v.f3c = ctx->d_f3xc.as<double>();
+  v.fvxc = ctx->d_fvxc.as<double>();
   return v;
 }
 
@@ -1599,6 +1609,18 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = fal
     CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, true));
   if (dogs && (what & (FB_VNA3C | FB_EWALD))) CHK(ctx->d_dogs_ps.ensure((size_t)8 * P * sizeof(double) + 8));
+  if (what & FB_VXC) {
+    if (dogs) return fail(ctx, FB_ERR_UNSUPPORTED, "vxc forces: this build assembles the McWEDA Harris exchange-correlation only");
+    if (!ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
+    if (!(ctx->assembled & FB_VXC) && !(graph_values && (what & FB_VXC)))
+      return fail(ctx, FB_ERR_STATE, "Dassemble_vxc reads the value pass: assemble FB_VXC first");
+    CHK(ctx->d_vxc_off.ensure(pb));
+    CHK(ctx->d_vxc_on.ensure(pb));
+    CHK(ctx->d_vxc_wd.ensure((size_t)ctx->nblock * sizeof(double) + 8));
+    CHK(ctx->d_vxc_gd.ensure((size_t)VXC_WSH * P * sizeof(double) + 8));
+    DevBuf *b3[] = {&ctx->d_f3xa, &ctx->d_f3xb, &ctx->d_f3xc, &ctx->d_fvxc};
+    for (DevBuf *b : b3) CHK(b->ensure(ab + 8));
+  }
   if (what & FB_EWALD) {
     if (!dogs) return fail(ctx, FB_ERR_STATE, "Ewald forces: the DOGS theory (fb_set_theory) first");
     if (!ctx->have_ewald && !(graph_values && (what & FB_EWALD)))
@@ -1677,6 +1699,20 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     KL(KT_VNLF, launch_pp_forces(pa, ctx->npp, ctx->nppx, ctx->stream));
     ctx->launches++;  // two kernels
   }
+  if (what & FB_VXC) {
+    // Dassemble_vxc (2c pair terms, then the three-center terms with the
+    // per-pair weights the 2c kernel leaves) and its build_forces terms,
+    // added into ftot
+    VxcArgs v = vxc_args(ctx);
+    v.a = a;
+    KL(KT_DVXC2C, launch_dvxc_2c(v, ctx->stream));
+    size_t a3 = (size_t)3 * N * sizeof(double);
+    CU(cudaMemsetAsync(ctx->d_f3xa.p, 0, a3, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3xb.p, 0, a3, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3xc.p, 0, a3, ctx->stream));
+    if (a.ntrip > 0) KL(KT_DVXC3C, launch_dvxc_3c(v, ctx->stream));
+    KL(KT_VXCF, launch_vxc_forces(v, ctx->stream));
+  }
   if (what & FB_EWALD) {
     // Dassemble_ewaldsr / ewaldlr pair and atom forces and their
     // build_forces terms, added into ftot
@@ -1690,7 +1726,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
 static void dassemble_done(fb_ctx *ctx, unsigned what) {
   bool keep = (what & FB_KEEP_DBLOCKS) != 0;
   ctx->have_dblocks = keep && (what & FB_S) && (what & FB_T);
-  ctx->dassembled = what & (FB_ALL | FB_VNL2C | FB_VNL3C | FB_EWALD);
+  ctx->dassembled = what & (FB_ALL | FB_VNL2C | FB_VNL3C | FB_EWALD | FB_VXC);
 }
 
 int fb_dassemble(fb_ctx *ctx, unsigned what) {
@@ -1947,9 +1983,17 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out) {
     case FB_F_EWALDSR: b = &ctx->d_fsr; n = (size_t)3 * ctx->P; break;
     case FB_F_EWALDLR: b = &ctx->d_flr; break;
     case FB_F_EWALD: b = &ctx->d_fewald; break;
+    case FB_F_VXC: b = &ctx->d_fvxc; break;
+    case FB_F_F3XCA: b = &ctx->d_f3xa; break;
+    case FB_F_F3XCB: b = &ctx->d_f3xb; break;
+    case FB_F_F3XCC: b = &ctx->d_f3xc; break;
+    case FB_F_VXC_OFF_SITE: b = &ctx->d_vxc_off; n = (size_t)3 * ctx->P; break;
+    case FB_F_VXC_ON_SITE: b = &ctx->d_vxc_on; n = (size_t)3 * ctx->P; break;
     default: return fail(ctx, FB_ERR_ARG, "unknown force array %d", which);
   }
-  if (which >= FB_F_EWALDSR && !(ctx->dassembled & FB_EWALD))
+  if (which >= FB_F_VXC && !(ctx->dassembled & FB_VXC))
+    return fail(ctx, FB_ERR_STATE, "vxc forces: fb_dassemble with FB_VXC first");
+  if (which >= FB_F_EWALDSR && which <= FB_F_EWALD && !(ctx->dassembled & FB_EWALD))
     return fail(ctx, FB_ERR_STATE, "Ewald forces: fb_dassemble with FB_EWALD first");
   if (which >= FB_F_VNL && which <= FB_F_VNL_ONTOP && !(ctx->dassembled & (FB_VNL2C | FB_VNL3C)))
     return fail(ctx, FB_ERR_STATE, "vnl forces: fb_dassemble with FB_VNL2C / FB_VNL3C first");

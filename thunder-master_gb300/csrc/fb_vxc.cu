@@ -426,6 +426,427 @@ __global__ void __launch_bounds__(128) k_vxc(Ctx2c c, VxcArgs v) {
   else if constexpr (HASD) atom_vxc<PAT_SPD, HASD>(c, v, i, lane);
 }
 
+// ===========================================================================
+// force pass (k.DASSEMBLERS/M_Dassemble_vxc_McWEDA_Harris.f90,
+// M_Dassemble_rho_McWEDA_Harris.f90, M_Dassemble_vxc_3c_McWEDA_Harris.f90)
+// ===========================================================================
+// The reference accumulates rho(mu, nu) times per-element combinations of
+// the Dblocks of S, rho_in / rho_bond (ontop and atom case) and of the
+// weighted densities.  Each Dblock enters linearly, so the per-element
+// factors are gathered first into one weight block per Dblock, and every
+// weight block is contracted with its table's derivative rotation in the
+// molecular frame (contract), the same sums in a different order:
+//   off site   wS = rho ((muxc_b - dmuxc_b Wb) - (muxc_in - dmuxc_in Wi))  on dS
+//              wR = rho (dmuxc_b - dmuxc_in)                                on drho ontop
+//              gW(a,b) = sum rho (d2muxc_b (rho_b - Wb S) - d2muxc_in (rho_in - Wi S))
+//                                                                   on dW ontop
+//              - rho                                                on dvxc_ontop
+//   on site    wA(mu,mu) = -rho_s dmuxc_in(Wi_s(a,a)),
+//              wA(mu,nu) = rho_s (dmuxc_b - dmuxc_in)(W_s(a,b)), mu != nu  on drho atom
+//              gA(a,b) = sum_{mu != nu} rho_s (d2muxc_b rho_b_s - d2muxc_in rho_in_s)
+//                                                                   on dW atom
+// with the self block's Dblocko (the diagonal shell-density derivative of
+// :502-505, never assembled for the self pair) zero, and rho_bond's
+// off-diagonal derivatives taken as rho_in's (:572-575), as the reference
+// does.  The three-center pass contracts rho dmuxc_in and the shell sums
+// of rho d2muxc_in (rho_in - Wi S) left here per pair.
+template <int PA, int PB, bool HASD>
+__device__ __forceinline__ void pair_dvxc(const Ctx2c &c, const VxcArgs &v, int i, int p, const double *wA,
+                                          const double *gA) {
+  using PL = Plan<PA, PB, K2C>;
+  using PLA = Plan<PA, PA, K2C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
+  constexpr int SA = pat_nssh(PA), SB = pat_nssh(PB);
+  const FdataDev &fd = *c.fd;
+  int j = c.neigh_j[p];
+  int in1 = c.isp[i], in2 = c.isp[j];
+  long long o = c.blk_off[p];
+  double *gdp = v.gd + (long long)VXC_WSH * p;
+  if (i == j && c.neigh_b[p] == 0) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) v.off[3 * p + q] = v.on[3 * p + q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) v.wd[o + q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < VXC_WSH; q++) gdp[q] = 0.0;
+    return;
+  }
+  double r1[3], r2[3], z, e[3][3];
+  pair_geom(c, i, p, r1, r2, z, e);
+  double dd[3][3][3];
+  depsilon_2c(r1, r2, z, e, dd);
+  RotM R;
+  DRotM D;
+  twister<HASD>(e, R);
+  dtwister<HASD>(e, dd, D);
+  double eta[3] = {e[0][2], e[1][2], e[2][2]};
+  bool tiny = z < 1.0e-5;
+  bool on_eta = z > 1.0e-3;
+  // weights of the off-site terms and of the three-center pass
+  const double *rho = v.a.rho + o, *S = c.S + o, *ri = v.rho_in + o, *rb = v.rho_bond + o;
+  const double *Wi = v.wrho_in + (long long)VXC_WSH * p, *Wb = v.wrho_bond + (long long)VXC_WSH * p;
+  double wS[NA * NB], wR[NA * NB], gW[SA * SB];
+#pragma unroll
+  for (int a = 0; a < SA; a++)
+#pragma unroll
+    for (int b = 0; b < SB; b++) {
+      double wi = Wi[a + SA * b], wb = Wb[a + SA * b];
+      Lda li = lda_ca(wi), lb = lda_ca(wb);
+      double g = 0.0, gd = 0.0;
+#pragma unroll
+      for (int mu = shell_off(a); mu < shell_off(a) + 2 * a + 1; mu++)
+#pragma unroll
+        for (int nu = shell_off(b); nu < shell_off(b) + 2 * b + 1; nu++) {
+          int q = mu + NA * nu;
+          double r = rho[q], ov = S[q];
+          wS[q] = r * ((lb.muxc - lb.dmuxc * wb) - (li.muxc - li.dmuxc * wi));
+          wR[q] = r * (lb.dmuxc - li.dmuxc);
+          g += r * (lb.d2muxc * (rb[q] - wb * ov) - li.d2muxc * (ri[q] - wi * ov));
+          v.wd[o + q] = r * li.dmuxc;
+          gd += r * li.d2muxc * (ri[q] - wi * ov);
+        }
+      gW[a + SA * b] = g;
+      gdp[a + SA * b] = gd;
+    }
+#pragma unroll
+  for (int q = SA * SB; q < VXC_WSH; q++) gdp[q] = 0.0;
+  double f[3], out[3];
+  double val[NE > NEA ? NE : NEA], dv[NE > NEA ? NE : NEA], vd[3 * (NE > NEA ? NE : NEA)];
+  // d overlap
+  interp2c_d<NE>(c.table2c, fd.c2[in1][in2][0], z, tiny, val, dv, c.status);
+  vec2c<NE>(z, eta, dv, vd);
+  contract<PA, PB, K2C, HASD>(R, D, wS, val, vd, f);
+  // d rho ontop: the shells of i (left) and of j (right), Qneutral weighted
+  {
+    double m[NE], dm[NE], t[NE], dt[NE];
+#pragma unroll
+    for (int q = 0; q < NE; q++) m[q] = dm[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SA; isorp++) {
+      interp2c_d<NE>(c.table2c, fd.c2rho[in1][in2][0][isorp], z, tiny, t, dt, c.status);
+      double Q = fd.sp[in1].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < NE; q++) m[q] = fma(t[q], Q, m[q]), dm[q] = fma(dt[q], Q, dm[q]);
+    }
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      interp2c_d<NE>(c.table2c, fd.c2rho[in1][in2][1][isorp], z, tiny, t, dt, c.status);
+      double Q = fd.sp[in2].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < NE; q++) m[q] = fma(t[q], Q, m[q]), dm[q] = fma(dt[q], Q, dm[q]);
+    }
+    vec2c<NE>(z, eta, dm, vd);
+    contract<PA, PB, K2C, HASD>(R, D, wR, m, vd, out);
+#pragma unroll
+    for (int q = 0; q < 3; q++) f[q] += out[q];
+  }
+  // d W ontop (shell level, no rotation)
+  {
+    double dw[SA * SB], t[SA * SB], dt[SA * SB];
+#pragma unroll
+    for (int q = 0; q < SA * SB; q++) dw[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SA; isorp++) {
+      interp2c_d<SA * SB>(c.table2c, fd.c2rho[in1][in2][3][isorp], z, tiny, t, dt, c.status);
+      double Q = fd.sp[in1].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < SA * SB; q++) dw[q] = fma(dt[q], Q, dw[q]);
+    }
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      interp2c_d<SA * SB>(c.table2c, fd.c2rho[in1][in2][4][isorp], z, tiny, t, dt, c.status);
+      double Q = fd.sp[in2].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < SA * SB; q++) dw[q] = fma(dt[q], Q, dw[q]);
+    }
+    if (on_eta) {
+#pragma unroll
+      for (int a = 0; a < SA; a++)
+#pragma unroll
+        for (int b = 0; b < SB; b++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) f[k] += gW[a + SA * b] * (-eta[k] * dw[a * SB + b]);
+    }
+  }
+  // - rho . d vxc_ontop (Dassemble_vxc_bond)
+  interp2c_d<NE>(c.table2c, fd.c2vxc[in1][in2], z, tiny, val, dv, c.status);
+  vec2c<NE>(z, eta, dv, vd);
+  contract<PA, PB, K2C, HASD>(R, D, rho, val, vd, out);
+#pragma unroll
+  for (int q = 0; q < 3; q++) v.off[3 * p + q] = f[q] - out[q];
+  // on site: d rho atom and d W atom of this neighbor
+  {
+    double m[NEA], dm[NEA], t[NEA], dt[NEA];
+#pragma unroll
+    for (int q = 0; q < NEA; q++) m[q] = dm[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      interp2c_d<NEA>(c.table2c, fd.c2rho[in1][in2][2][isorp], z, tiny, t, dt, c.status);
+      double Q = fd.sp[in2].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < NEA; q++) m[q] = fma(t[q], Q, m[q]), dm[q] = fma(dt[q], Q, dm[q]);
+    }
+    vec2c<NEA>(z, eta, dm, vd);
+    contract<PA, PA, K2C, HASD>(R, D, wA, m, vd, f);
+    double dw[SA * SA], ts[SA * SA], dts[SA * SA];
+#pragma unroll
+    for (int q = 0; q < SA * SA; q++) dw[q] = 0.0;
+#pragma unroll
+    for (int isorp = 0; isorp < SB; isorp++) {
+      interp2c_d<SA * SA>(c.table2c, fd.c2rho[in1][in2][5][isorp], z, tiny, ts, dts, c.status);
+      double Q = fd.sp[in2].qn[isorp];
+#pragma unroll
+      for (int q = 0; q < SA * SA; q++) dw[q] = fma(dts[q], Q, dw[q]);
+    }
+    if (on_eta) {
+#pragma unroll
+      for (int a = 0; a < SA; a++)
+#pragma unroll
+        for (int b = 0; b < SA; b++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) f[k] += gA[a + SA * b] * (-eta[k] * dw[a * SA + b]);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) v.on[3 * p + q] = f[q];
+  }
+}
+
+template <int PA, bool HASD>
+__device__ void atom_dvxc(const Ctx2c &c, const VxcArgs &v, int i, int lane) {
+  constexpr int NA = pat_norb(PA), SA = pat_nssh(PA);
+  int p0 = c.pair_off[i], ps = p0 + c.neigh_self[i];
+  long long os = c.blk_off[ps];
+  // on-site weights from the self block (the same for every neighbor of i)
+  double wA[NA * NA], gA[SA * SA];
+  {
+    const double *Wi = v.wrho_in + (long long)VXC_WSH * ps, *Wb = v.wrho_bond + (long long)VXC_WSH * ps;
+    const double *rs = v.a.rho + os, *ri = v.rho_in + os, *rb = v.rho_bond + os;
+#pragma unroll
+    for (int a = 0; a < SA; a++) {
+      Lda ld = lda_ca(Wi[a + SA * a]);
+#pragma unroll
+      for (int b = 0; b < SA; b++) {
+        Lda li = lda_ca(Wi[a + SA * b]), lb = lda_ca(Wb[a + SA * b]);
+        double g = 0.0;
+#pragma unroll
+        for (int mu = shell_off(a); mu < shell_off(a) + 2 * a + 1; mu++)
+#pragma unroll
+          for (int nu = shell_off(b); nu < shell_off(b) + 2 * b + 1; nu++) {
+            int q = mu + NA * nu;
+            double r = rs[q];
+            if (mu == nu) {
+              wA[q] = -r * ld.dmuxc;
+            } else {
+              wA[q] = r * (lb.dmuxc - li.dmuxc);
+              g += r * (lb.d2muxc * rb[q] - li.d2muxc * ri[q]);
+            }
+          }
+        gA[a + SA * b] = g;
+      }
+    }
+  }
+  for (int p = p0 + lane; p < c.pair_off[i + 1]; p += 32) {
+    int pb = c.fd->sp[c.isp[c.neigh_j[p]]].pattern;
+    if (pb == PAT_SP) pair_dvxc<PA, PAT_SP, HASD>(c, v, i, p, wA, gA);
+    else if (pb == PAT_S) pair_dvxc<PA, PAT_S, HASD>(c, v, i, p, wA, gA);
+    else if constexpr (HASD) pair_dvxc<PA, PAT_SPD, HASD>(c, v, i, p, wA, gA);
+  }
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_dvxc_2c(Ctx2c c, VxcArgs v) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= c.N) return;
+  int pa = c.fd->sp[c.isp[i]].pattern;
+  if (pa == PAT_SP) atom_dvxc<PAT_SP, HASD>(c, v, i, lane);
+  else if (pa == PAT_S) atom_dvxc<PAT_S, HASD>(c, v, i, lane);
+  else if constexpr (HASD) atom_dvxc<PAT_SPD, HASD>(c, v, i, lane);
+}
+
+// Dassemble_vxc_3c: rhoxa/b = the Qneutral-weighted derivative rotations of
+// den3, rhoma/b the shell-level denS3 derivatives; mxca = dmuxc rhoxa +
+// rhoma d2muxc (rho_in - W S) (:371-402), contracted with rho of the pair:
+// sum rho mxca = contract(rho dmuxc, rhoxa) + sum_ab gd(a,b) rhoma(a,b).
+template <int PA, int PB, bool HASD>
+__device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
+  constexpr int SA = pat_nssh(PA), SB = pat_nssh(PB);
+  int ia, iat, jat;
+  TripGeom g;
+  trip_geom(c, t, ia, iat, jat, g);
+  const FdataDev &fd = *c.fd;
+  int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+  int nk = fd.sp[indna].nssh;
+  const double *qk = fd.sp[indna].qn;
+  double dA[3][3][3], dB[3][3][3];
+  depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
+  double amt[3], bmt[3];
+  if (g.x > 1.0e-5) {
+    double ix = 1.0 / g.x;
+#pragma unroll
+    for (int k = 0; k < 3; k++) amt[k] = (g.sighat[k] - g.cost * g.rhat[k]) * ix;
+  } else {
+    amt[0] = amt[1] = amt[2] = 0.0;
+  }
+  double iz = 1.0 / g.z;
+#pragma unroll
+  for (int k = 0; k < 3; k++) bmt[k] = (g.cost * g.sighat[k] - g.rhat[k]) * iz;
+  double F[NE], DpF[NE], DxF[NE], DyF[NE], t0[NE], t1[NE], t2[NE], t3[NE];
+#pragma unroll
+  for (int e = 0; e < NE; e++) F[e] = DpF[e] = DxF[e] = DyF[e] = 0.0;
+#pragma unroll 1
+  for (int isorp = 0; isorp < nk; isorp++) {
+    interp3c<NE, true>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, t0, t1, t2, t3);
+    double Q = qk[isorp];
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      F[e] = fma(t0[e], Q, F[e]);
+      DpF[e] = fma(t1[e], Q, DpF[e]);
+      DxF[e] = fma(t2[e], Q, DxF[e]);
+      DyF[e] = fma(t3[e], Q, DyF[e]);
+    }
+  }
+  double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
+  double M[NE], Ma[3 * NE], Mb[3 * NE];
+  sfor<NE>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    double m = F[e], dp = DpF[e], dx = DxF[e], dy = DyF[e];
+    if constexpr (PL::m.mv[e] == 1) {
+      dp = DpF[e] * sint - g.cost * F[e] / sint;
+      m = F[e] * sint;
+      dx = DxF[e] * sint;
+      dy = DyF[e] * sint;
+    }
+    M[e] = m;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double a = g.rhat[q] * dx + amt[q] * dp;
+      Ma[q + 3 * e] = a;
+      Mb[q + 3 * e] = -g.sighat[q] * dy + bmt[q] * dp - a * 0.5;
+    }
+  });
+  RotM R;
+  twister<HASD>(g.e, R);
+  DRotM DA, DB;
+  dtwister<HASD>(g.e, dA, DA);
+  dtwister<HASD>(g.e, dB, DB);
+  int p = c.tdst[t];
+  const double *wdp = v.wd + c.blk_off[p];
+  double wb[NA * NB];
+#pragma unroll
+  for (int q = 0; q < NA * NB; q++) wb[q] = __ldg(wdp + q);
+  MolRho<PA, PB, K3C> GA, GB;
+  mol_rho<PA, PB, K3C>(R, DA, wb, GA);
+  mol_rho<PA, PB, K3C>(R, DB, wb, GB);
+  double fa[3], fb[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    double sa = 0.0, sb = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      sa = fma(M[e], GA.H[q][e], sa);
+      sa = fma(Ma[q + 3 * e], GA.G[e], sa);
+      sb = fma(M[e], GB.H[q][e], sb);
+      sb = fma(Mb[q + 3 * e], GB.G[e], sb);
+    }
+    fa[q] = sa;
+    fb[q] = sb;
+  }
+  // shell level (denS3, no rotation, mvalue 0)
+  {
+    constexpr int NS = SA * SB;
+    double Dp[NS], Dx[NS], Dy[NS], s0[NS], s1[NS], s2[NS], s3[NS];
+#pragma unroll
+    for (int e = 0; e < NS; e++) Dp[e] = Dx[e] = Dy[e] = 0.0;
+#pragma unroll 1
+    for (int isorp = 0; isorp < nk; isorp++) {
+      interp3c<NS, true>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, s0, s1, s2, s3);
+      double Q = qk[isorp];
+#pragma unroll
+      for (int e = 0; e < NS; e++) {
+        Dp[e] = fma(s1[e], Q, Dp[e]);
+        Dx[e] = fma(s2[e], Q, Dx[e]);
+        Dy[e] = fma(s3[e], Q, Dy[e]);
+      }
+    }
+    const double *gd = v.gd + (long long)VXC_WSH * p;
+#pragma unroll
+    for (int a = 0; a < SA; a++)
+#pragma unroll
+      for (int b = 0; b < SB; b++) {
+        int e = a * SB + b;
+        double w = gd[a + SA * b];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          double ra = g.rhat[q] * Dx[e] + amt[q] * Dp[e];
+          double rb = -g.sighat[q] * Dy[e] + bmt[q] * Dp[e] - ra / 2.0;
+          fa[q] = fma(w, ra, fa[q]);
+          fb[q] = fma(w, rb, fb[q]);
+        }
+      }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    atomicAdd(v.f3a + 3 * ia + q, -fa[q]);
+    atomicAdd(v.f3b + 3 * iat + q, -fb[q]);
+    atomicAdd(v.f3c + 3 * jat + q, fa[q] + fb[q]);
+  }
+}
+
+template <bool HASD>
+__global__ void __launch_bounds__(128) k_dvxc_3c(Ctx3c c, VxcArgs v) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.T; t += gridDim.x * blockDim.x) {
+    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+    int key = pa * 3 + pb;
+    switch (key) {
+      case PAT_SP * 3 + PAT_SP: trip_dvxc<PAT_SP, PAT_SP, HASD>(c, v, t); break;
+      case PAT_SP * 3 + PAT_S: trip_dvxc<PAT_SP, PAT_S, HASD>(c, v, t); break;
+      case PAT_S * 3 + PAT_SP: trip_dvxc<PAT_S, PAT_SP, HASD>(c, v, t); break;
+      case PAT_S * 3 + PAT_S: trip_dvxc<PAT_S, PAT_S, HASD>(c, v, t); break;
+      default:
+        if constexpr (HASD) {
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_dvxc<PAT_SPD, PAT_SPD, HASD>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_dvxc<PAT_SPD, PAT_SP, HASD>(c, v, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_dvxc<PAT_SP, PAT_SPD, HASD>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_dvxc<PAT_SPD, PAT_S, HASD>(c, v, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_dvxc<PAT_S, PAT_SPD, HASD>(c, v, t);
+        }
+    }
+  }
+}
+
+// build_forces vxc terms (c.SYSTEM/M_build_forces.f90:345-365, :453-455):
+// f_i += off + on of i's pairs, f_j -= them, gathered by atom j through
+// neigh_back (one warp per atom); ftot += that + f3xca + f3xcb + f3xcc.
+__global__ void k_vxc_forces(int N, const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
+                             const int *__restrict__ neigh_back, const double *__restrict__ off,
+                             const double *__restrict__ on, const double *__restrict__ f3a,
+                             const double *__restrict__ f3b, const double *__restrict__ f3c,
+                             double *__restrict__ fvxc, double *__restrict__ ftot) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= N) return;
+  double f[3] = {0.0, 0.0, 0.0};
+  for (int p = pair_off[i] + lane; p < pair_off[i + 1]; p += 32) {
+    int pb = pair_off[neigh_j[p]] + neigh_back[p];  // pair (j -> i)
+#pragma unroll
+    for (int q = 0; q < 3; q++) f[q] += off[3 * p + q] + on[3 * p + q] - off[3 * pb + q] - on[3 * pb + q];
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) f[q] += __shfl_xor_sync(0xffffffffu, f[q], o);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      fvxc[3 * i + q] = f[q];
+      ftot[3 * i + q] += f[q] + f3a[3 * i + q] + f3b[3 * i + q] + f3c[3 * i + q];
+    }
+  }
+}
+
 }  // namespace
 
 int launch_rho_2c(const VxcArgs &v, cudaStream_t s) {
@@ -456,6 +877,37 @@ int launch_vxc(const VxcArgs &v, cudaStream_t s) {
   int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
   if (v.a.have_d) k_vxc<true><<<blocks, threads, 0, s>>>(c, v);
   else k_vxc<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_dvxc_2c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.N == 0) return 0;
+  Ctx2c c = make2c(v.a);
+  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
+  if (v.a.have_d) k_dvxc_2c<true><<<blocks, threads, 0, s>>>(c, v);
+  else k_dvxc_2c<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_dvxc_3c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.ntrip == 0) return 0;
+  Ctx3c c = make3c(v.a);
+  int threads = 128;
+  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
+  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
+  if (v.a.have_d) k_dvxc_3c<true><<<blocks, threads, 0, s>>>(c, v);
+  else k_dvxc_3c<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+int launch_vxc_forces(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.N == 0) return 0;
+  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
+  k_vxc_forces<<<blocks, threads, 0, s>>>(v.a.N, v.a.pair_off, v.a.neigh_j, v.a.neigh_back, v.off, v.on, v.f3a,
+                                          v.f3b, v.f3c, v.fvxc, v.a.ftot);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -29,6 +29,8 @@ Context.assemble(FB_VNL)  assemble_svnl / vnl_2c / vnl_3c             j.ASSEMBLE
 Context.Dassemble(FB_VNL2C | FB_VNL3C)  Dassemble_svnl / vnl_2c / vnl_3c  k.DASSEMBLERS/M_Dassemble_PP_{2c,3c}.f90
 Context.assemble(FB_VXC)  assemble_vxc (McWEDA, Harris)               j.ASSEMBLERS/M_assemble_vxc_McWEDA_Harris.f90:102,
                                                                       j.ASSEMBLERS/M_assemble_rho_McWEDA_Harris.f90
+Context.Dassemble(FB_VXC)  Dassemble_vxc (McWEDA, Harris)             k.DASSEMBLERS/M_Dassemble_vxc_McWEDA_Harris.f90:102,
+                                                                      k.DASSEMBLERS/M_Dassemble_vxc_3c_McWEDA_Harris.f90:97
 =====================  =============================================  ====================================
 
 There is no CPU fallback: every call runs on the GPU through the native
@@ -61,7 +63,8 @@ BLOCK = {"S": 0, "T": 1, "vna": 2, "vnao": 3, "dS": 4, "dT": 5, "rho": 6, "cape"
 FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, "f3nac": 6,
          "vna_ontop": 7, "vna_atom": 8,
          "vnl": 9, "f3nla": 10, "f3nlb": 11, "f3nlc": 12, "vnl_atom": 13, "vnl_ontop": 14,
-         "ewaldsr": 15, "ewaldlr": 16, "ewald": 17}
+         "ewaldsr": 15, "ewaldlr": 16, "ewald": 17,
+         "vxc": 18, "f3xca": 19, "f3xcb": 20, "f3xcc": 21, "vxc_off_site": 22, "vxc_on_site": 23}
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
           6: "ATOMS_CLOSE", 7: "NEIGH_SELF", 8: "NEIGH_BACK", 9: "CUDA", 10: "WATCHDOG",
           11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED"}
@@ -146,7 +149,7 @@ KERNELS = ("neigh_count", "neigh_fill", "neigh_back", "common_count", "common_fi
            "assemble_3c", "dassemble_2c", "dassemble_3c", "build_forces", "trip_bins", "split_rho",
            "mlp_eval", "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common", "svnl",
            "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald", "ewald_blocks",
-           "rho_2c", "rho_3c", "vxc")
+           "rho_2c", "rho_3c", "vxc", "dvxc_2c", "dvxc_3c", "vxc_forces")
 
 
 class FBError(RuntimeError):
@@ -551,7 +554,8 @@ class Context:
         self._check(self.L.fb_dassemble(self.h, what | (FB_KEEP_DBLOCKS if keep_dblocks else 0)))
 
     def forces(self, which):
-        n = 3 * {"vna_ontop": self.npairs, "vna_atom": self.npairs, "ewaldsr": self.npairs}.get(which, self.natoms)
+        n = 3 * {"vna_ontop": self.npairs, "vna_atom": self.npairs, "ewaldsr": self.npairs,
+                 "vxc_off_site": self.npairs, "vxc_on_site": self.npairs}.get(which, self.natoms)
         if which == "vnl_atom":
             n = 3 * self.npp
         elif which == "vnl_ontop":
