@@ -683,11 +683,37 @@ def vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=False):
     kt = ctx.timing()
     ctx.set_timing(False)
     out = {"what": "McWEDA vxc (Harris): overlap, rho_in / rho_bond and weighted densities (2c + 3c), "
-                   "Ceperley-Alder SN terms, vxc_bond; FP64",
+                   "Ceperley-Alder SN terms, vxc_bond; FP64 (three-center densities double-float)",
            "ms_per_step": round(ms / args.steps, 4), "value": round(P * args.steps / (ms * 1e-3), 1),
            "unit": "neighbor blocks/s", "gpu_launches_per_step": launches // max(1, args.steps),
            "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
     vxc = ctx.blocks("vxc")
+    # the force pass too (Dassemble_vxc with the S, T and vna force terms of
+    # build_forces), with a seeded density matrix, as one graph
+    nb = ctx.nblock
+    rng = np.random.default_rng(7)
+    d_rho = torch.from_numpy(rng.normal(0.0, 0.1, nb)).to(f"cuda:{local}")
+    d_cape = torch.from_numpy(rng.normal(0.0, 0.05, nb)).to(f"cuda:{local}")
+    ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
+    whatf = fbgpu.FB_ALL | fbgpu.FB_VXC | fbgpu.FB_FORCES
+
+    def stepf():
+        ctx.driver_neighbors()
+        ctx.assemble_graph(whatf)
+
+    for _ in range(max(3, args.warmup)):
+        stepf()
+    msf, lf = timed(stepf, args.steps)
+    timed(lambda: (ctx.driver_neighbors(), ctx.assemble(fbgpu.FB_ALL | fbgpu.FB_VXC),
+                   ctx.Dassemble(fbgpu.FB_ALL | fbgpu.FB_VXC)), args.steps, timing=True)
+    ktf = ctx.timing()
+    ctx.set_timing(False)
+    out["with_forces"] = {"what": "Harris S, T, vna + McWEDA vxc, value and force pass (Dassemble_vxc and the "
+                                  "build_forces terms), one graph",
+                          "ms_per_step": round(msf / args.steps, 4),
+                          "value": round(P * args.steps / (msf * 1e-3), 1), "unit": "neighbor blocks/s",
+                          "gpu_launches_per_step": lf // max(1, args.steps),
+                          "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktf.items() if v[1]}}
     ctx.close()
     if no_cpu or st.natoms > 1024:
         out["cpu_oracle"] = "not run (single-core oracle bounded to systems of at most 1024 atoms)"

@@ -42,8 +42,10 @@ def _check(ctx, ref, P):
     assert np.abs(ctx.blocks("vxc") - ref["vxc"]).max() <= TOL
 
 
+@pytest.mark.parametrize("prec", [0, 1])  # FP64 kernels, double-float three-center densities
 @pytest.mark.parametrize("name", ["si64", "sic_small", "cho_small", "si_vac", "sic_vac", "sic_cluster"])
-def test_vxc_matches_oracle(ctx, fdata_root, name):
+def test_vxc_matches_oracle(ctx, fdata_root, name, prec):
+    ctx.set_precision(prec)
     path, nZ, st = case(fdata_root, name)
     s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
     ref = s.assemble_vxc()
@@ -52,12 +54,15 @@ def test_vxc_matches_oracle(ctx, fdata_root, name):
     ctx.driver_neighbors()
     ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
     what = fbgpu.FB_ALL | fbgpu.FB_VXC
-    ctx.assemble(what)
-    assert np.abs(ctx.blocks("S") - ref["S"]).max() <= TOL
-    _check(ctx, ref, s.npairs)
-    for _ in range(2):  # as one graph, captured then replayed
-        ctx.assemble_graph(what)
+    try:
+        ctx.assemble(what)
+        assert np.abs(ctx.blocks("S") - ref["S"]).max() <= TOL
         _check(ctx, ref, s.npairs)
+        for _ in range(2):  # as one graph, captured then replayed
+            ctx.assemble_graph(what)
+            _check(ctx, ref, s.npairs)
+    finally:
+        ctx.set_precision(1)
 
 
 def test_vxc_after_overlap(ctx, fdata_root):

@@ -1392,7 +1392,10 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   if (what & FB_VXC) {
     VxcArgs v = vxc_args(ctx);
     KL(KT_RHO2C, launch_rho_2c(v, ctx->stream));
-    if (a.ntrip > 0) KL(KT_RHO3C, launch_rho_3c(v, ctx->stream));
+    if (a.ntrip > 0) {
+      if (use_df(ctx)) KL(KT_RHO3C, launch_rho_3c_df(v, ctx->stream));
+      else KL(KT_RHO3C, launch_rho_3c(v, ctx->stream));
+    }
     KL(KT_VXC, launch_vxc(v, ctx->stream));
   }
   if (what & FB_EWALD) {

@@ -31,6 +31,8 @@ struct VxcArgs {
 int launch_rho_2c(const VxcArgs &v, cudaStream_t s);
 // assemble_rho_3c + assemble_rho_weighted_3c: accumulates onto rho_in, wrho_in
 int launch_rho_3c(const VxcArgs &v, cudaStream_t s);
+// the same in double-float on the FP32 pipe (s and sp bases)
+int launch_rho_3c_df(const VxcArgs &v, cudaStream_t s);
 // assemble_vxc_SN + assemble_vxc_bond + their sum: writes vxc
 int launch_vxc(const VxcArgs &v, cudaStream_t s);
 // Dassemble_vxc_SN + Dassemble_vxc_bond (with the rho 2c derivatives): the
