@@ -1065,6 +1065,7 @@ static VxcArgs vxc_args(fb_ctx *ctx) {
   v.f3b = ctx->d_f3xb.as<double>();
   v.f3c = ctx->d_f3xc.as<double>();
   v.fvxc = ctx->d_fvxc.as<double>();
+  v.qsum_all = ctx->fdh.dev.vxc_qsum_all;
   return v;
 }
 
@@ -1395,6 +1396,7 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     if (a.ntrip > 0) {
       if (use_df(ctx)) KL(KT_RHO3C, launch_rho_3c_df(v, ctx->stream));
       else KL(KT_RHO3C, launch_rho_3c(v, ctx->stream));
+      if (!v.qsum_all) ctx->launches++;  // the triples without summed cells
     }
     KL(KT_VXC, launch_vxc(v, ctx->stream));
   }
@@ -1713,7 +1715,10 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     CU(cudaMemsetAsync(ctx->d_f3xa.p, 0, a3, ctx->stream));
     CU(cudaMemsetAsync(ctx->d_f3xb.p, 0, a3, ctx->stream));
     CU(cudaMemsetAsync(ctx->d_f3xc.p, 0, a3, ctx->stream));
-    if (a.ntrip > 0) KL(KT_DVXC3C, launch_dvxc_3c(v, ctx->stream));
+    if (a.ntrip > 0) {
+      KL(KT_DVXC3C, launch_dvxc_3c(v, ctx->stream));
+      if (!v.qsum_all) ctx->launches++;
+    }
     KL(KT_VXCF, launch_vxc_forces(v, ctx->stream));
   }
   if (what & FB_EWALD) {

@@ -566,6 +566,43 @@ info_done:
             else if (r) return r;
           }
         if (nk > MAXSUB) vxc_ok = false;
+        // Qneutral-weighted sums of the sub-cells
+        for (int q = 0; q < 2; q++) {
+          Cell3cDev &dq = out.dev.c3rhoq[is][js][ks][q];
+          dq.off = -1;
+          if (nk < 1 || nk > MAXSUB) continue;
+          const Cell3cDev &c0 = out.dev.c3rho[is][js][ks][q][0];
+          bool ok = c0.off >= 0;
+          for (int k = 1; k < nk && ok; k++) {
+            const Cell3cDev &ck = out.dev.c3rho[is][js][ks][q][k];
+            ok = ck.off >= 0 && ck.nx == c0.nx && ck.ny == c0.ny && ck.nME == c0.nME && ck.dx == c0.dx && ck.dy == c0.dy;
+          }
+          long long nn = (long long)c0.nx * c0.ny;
+          for (long long n = 0; n < nn && ok; n++)
+            for (int k = 1; k < nk && ok; k++)
+              ok = out.lin[out.dev.c3rho[is][js][ks][q][k].node_off + n] == out.lin[c0.node_off + n];
+          if (!ok) continue;
+          dq = c0;
+          dq.off = (long long)out.table3c.size();
+          dq.node_off = (long long)out.lin.size();
+          long long nv = nn * NTHETA * c0.nME;
+          for (long long k = 0; k < nv; k++) {
+            double acc = 0.0;
+            for (int i = 0; i < nk; i++)
+              acc += out.sp[ks].qn[i] * out.table3c[out.dev.c3rho[is][js][ks][q][i].off + k];
+            out.table3c.push_back(acc);
+          }
+          for (long long n = 0; n < nn; n++) {
+            unsigned char l0 = out.lin[c0.node_off + n];
+            out.lin.push_back(l0);
+            for (int d = 0; d < 2; d++) {
+              double acc = 0.0;
+              for (int i = 0; i < nk; i++)
+                acc += out.sp[ks].qn[i] * out.gxy[2 * (out.dev.c3rho[is][js][ks][q][i].node_off + n) + d];
+              out.gxy.push_back(acc);
+            }
+          }
+        }
       }
 
   // one-center McWEDA xc (read_Fdata_1c, e.FDATA/M_Fdata_1c_McWEDA_Harris.f90:
@@ -621,6 +658,12 @@ info_done:
   out.dev.have_pp = pp_ok ? 1 : 0;
   out.dev.have_dogs = dogs_ok ? 1 : 0;
   out.dev.have_vxc = vxc_ok ? 1 : 0;
+  out.dev.vxc_qsum_all = 1;
+  for (int is = 0; is < nspecies; is++)
+    for (int js = 0; js < nspecies; js++)
+      for (int ks = 0; ks < nspecies; ks++)
+        for (int q = 0; q < 2; q++)
+          if (out.dev.c3rhoq[is][js][ks][q].off < 0) out.dev.vxc_qsum_all = 0;
   return FB_OK;
 }
 

@@ -213,6 +213,12 @@ struct FdataDev {
   Cell2cDev c2vxc[MAXSP][MAXSP];
   Cell2cDev c2rho[MAXSP][MAXSP][6][MAXSUB];
   Cell3cDev c3rho[MAXSP][MAXSP][MAXSP][2][MAXSUB];
+  // the same tables summed over isorp with the third species' Qneutral
+  // weights (interpolation is linear in the table values and in the
+  // linear-branch gradients), where every sub-cell shares the grid and the
+  // gradient switch at every node; off = -1 where they do not
+  Cell3cDev c3rhoq[MAXSP][MAXSP][MAXSP][2];
+  int vxc_qsum_all;  // every species triple has both summed cells
   double vxc1c[MAXSP][MAXSUB * MAXSUB];
 };
 

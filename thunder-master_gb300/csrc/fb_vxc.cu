@@ -246,7 +246,12 @@ __global__ void __launch_bounds__(128) k_rho_2c(Ctx2c c, VxcArgs v) {
 // ---------------------------------------------------------------------------
 // rho 3c: one thread per triplet, FP64 atomics into the pair (iatom, mneigh)
 // ---------------------------------------------------------------------------
-template <int PA, int PB, bool HASD>
+// true when the triple's Qneutral-summed density cells exist
+__device__ __forceinline__ bool qsum_triple(const FdataDev &fd, int in1, int in2, int in3) {
+  return fd.c3rhoq[in1][in2][in3][0].off >= 0 && fd.c3rhoq[in1][in2][in3][1].off >= 0;
+}
+
+template <int PA, int PB, bool HASD, bool QSUM>
 __device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int t) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
@@ -258,14 +263,19 @@ __device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int
   int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
-  double F[NE], m[NE];
+  double m[NE];
+  if constexpr (QSUM) {
+    interp3c<NE, false>(c, fd.c3rhoq[in1][in2][indna][0], g.x, g.z, g.cost, m, nullptr, nullptr, nullptr);
+  } else {
+    double F[NE];
 #pragma unroll
-  for (int q = 0; q < NE; q++) m[q] = 0.0;
+    for (int q = 0; q < NE; q++) m[q] = 0.0;
 #pragma unroll 1
-  for (int isorp = 0; isorp < nk; isorp++) {
-    interp3c<NE, false>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, F, nullptr, nullptr, nullptr);
+    for (int isorp = 0; isorp < nk; isorp++) {
+      interp3c<NE, false>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, F, nullptr, nullptr, nullptr);
 #pragma unroll
-    for (int q = 0; q < NE; q++) m[q] = fma(F[q], qk[isorp], m[q]);
+      for (int q = 0; q < NE; q++) m[q] = fma(F[q], qk[isorp], m[q]);
+    }
   }
   double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
   sfor<NE>([&](auto E) {
@@ -280,38 +290,48 @@ __device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int
   double *dst = v.rho_in + c.blk_off[p];
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, X[q]);
-  double Fs[SA * SB], ws[SA * SB];
+  double ws[SA * SB];
+  if constexpr (QSUM) {
+    interp3c<SA * SB, false>(c, fd.c3rhoq[in1][in2][indna][1], g.x, g.z, g.cost, ws, nullptr, nullptr, nullptr);
+  } else {
+    double Fs[SA * SB];
 #pragma unroll
-  for (int q = 0; q < SA * SB; q++) ws[q] = 0.0;
+    for (int q = 0; q < SA * SB; q++) ws[q] = 0.0;
 #pragma unroll 1
-  for (int isorp = 0; isorp < nk; isorp++) {
-    interp3c<SA * SB, false>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, Fs, nullptr, nullptr,
-                             nullptr);
+    for (int isorp = 0; isorp < nk; isorp++) {
+      interp3c<SA * SB, false>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, Fs, nullptr, nullptr,
+                               nullptr);
 #pragma unroll
-    for (int q = 0; q < SA * SB; q++) ws[q] = fma(Fs[q], qk[isorp], ws[q]);
+      for (int q = 0; q < SA * SB; q++) ws[q] = fma(Fs[q], qk[isorp], ws[q]);
+    }
   }
   double *wd = v.wrho_in + (long long)VXC_WSH * p;
 #pragma unroll
   for (int q = 0; q < SA * SB; q++) atomicAdd(wd + (q / SB) + SA * (q % SB), ws[q]);
 }
 
-template <bool HASD>
+// triplets in the binned order (tperm) for table locality; QSUM: the
+// triplets whose triple has summed cells, else the others
+template <bool HASD, bool QSUM>
 __global__ void __launch_bounds__(128) k_rho_3c(Ctx3c c, VxcArgs v) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.T; t += gridDim.x * blockDim.x) {
-    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
+    int t = c.tperm ? c.tperm[i] : i;
+    int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
+    if (qsum_triple(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
+    int pa = c.fd->sp[in1].pattern, pb = c.fd->sp[in2].pattern;
     int key = pa * 3 + pb;
     switch (key) {
-      case PAT_SP * 3 + PAT_SP: trip_rho3c<PAT_SP, PAT_SP, HASD>(c, v, t); break;
-      case PAT_SP * 3 + PAT_S: trip_rho3c<PAT_SP, PAT_S, HASD>(c, v, t); break;
-      case PAT_S * 3 + PAT_SP: trip_rho3c<PAT_S, PAT_SP, HASD>(c, v, t); break;
-      case PAT_S * 3 + PAT_S: trip_rho3c<PAT_S, PAT_S, HASD>(c, v, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_rho3c<PAT_SP, PAT_SP, HASD, QSUM>(c, v, t); break;
+      case PAT_SP * 3 + PAT_S: trip_rho3c<PAT_SP, PAT_S, HASD, QSUM>(c, v, t); break;
+      case PAT_S * 3 + PAT_SP: trip_rho3c<PAT_S, PAT_SP, HASD, QSUM>(c, v, t); break;
+      case PAT_S * 3 + PAT_S: trip_rho3c<PAT_S, PAT_S, HASD, QSUM>(c, v, t); break;
       default:
         if constexpr (HASD) {
-          if (key == PAT_SPD * 3 + PAT_SPD) trip_rho3c<PAT_SPD, PAT_SPD, HASD>(c, v, t);
-          else if (key == PAT_SPD * 3 + PAT_SP) trip_rho3c<PAT_SPD, PAT_SP, HASD>(c, v, t);
-          else if (key == PAT_SP * 3 + PAT_SPD) trip_rho3c<PAT_SP, PAT_SPD, HASD>(c, v, t);
-          else if (key == PAT_SPD * 3 + PAT_S) trip_rho3c<PAT_SPD, PAT_S, HASD>(c, v, t);
-          else if (key == PAT_S * 3 + PAT_SPD) trip_rho3c<PAT_S, PAT_SPD, HASD>(c, v, t);
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_rho3c<PAT_SPD, PAT_SPD, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_rho3c<PAT_SPD, PAT_SP, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_rho3c<PAT_SP, PAT_SPD, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_rho3c<PAT_SPD, PAT_S, HASD, QSUM>(c, v, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_rho3c<PAT_S, PAT_SPD, HASD, QSUM>(c, v, t);
         }
     }
   }
@@ -668,7 +688,7 @@ __global__ void __launch_bounds__(128) k_dvxc_2c(Ctx2c c, VxcArgs v) {
 // den3, rhoma/b the shell-level denS3 derivatives; mxca = dmuxc rhoxa +
 // rhoma d2muxc (rho_in - W S) (:371-402), contracted with rho of the pair:
 // sum rho mxca = contract(rho dmuxc, rhoxa) + sum_ab gd(a,b) rhoma(a,b).
-template <int PA, int PB, bool HASD>
+template <int PA, int PB, bool HASD, bool QSUM>
 __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
@@ -680,8 +700,7 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
   int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
-  double dA[3][3][3], dB[3][3][3];
-  depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
+  int p = c.tdst[t];
   double amt[3], bmt[3];
   if (g.x > 1.0e-5) {
     double ix = 1.0 / g.x;
@@ -693,82 +712,29 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
   double iz = 1.0 / g.z;
 #pragma unroll
   for (int k = 0; k < 3; k++) bmt[k] = (g.cost * g.sighat[k] - g.rhat[k]) * iz;
-  double F[NE], DpF[NE], DxF[NE], DyF[NE], t0[NE], t1[NE], t2[NE], t3[NE];
-#pragma unroll
-  for (int e = 0; e < NE; e++) F[e] = DpF[e] = DxF[e] = DyF[e] = 0.0;
-#pragma unroll 1
-  for (int isorp = 0; isorp < nk; isorp++) {
-    interp3c<NE, true>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, t0, t1, t2, t3);
-    double Q = qk[isorp];
-#pragma unroll
-    for (int e = 0; e < NE; e++) {
-      F[e] = fma(t0[e], Q, F[e]);
-      DpF[e] = fma(t1[e], Q, DpF[e]);
-      DxF[e] = fma(t2[e], Q, DxF[e]);
-      DyF[e] = fma(t3[e], Q, DyF[e]);
-    }
-  }
-  double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
-  double M[NE], Ma[3 * NE], Mb[3 * NE];
-  sfor<NE>([&](auto E) {
-    constexpr int e = decltype(E)::value;
-    double m = F[e], dp = DpF[e], dx = DxF[e], dy = DyF[e];
-    if constexpr (PL::m.mv[e] == 1) {
-      dp = DpF[e] * sint - g.cost * F[e] / sint;
-      m = F[e] * sint;
-      dx = DxF[e] * sint;
-      dy = DyF[e] * sint;
-    }
-    M[e] = m;
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      double a = g.rhat[q] * dx + amt[q] * dp;
-      Ma[q + 3 * e] = a;
-      Mb[q + 3 * e] = -g.sighat[q] * dy + bmt[q] * dp - a * 0.5;
-    }
-  });
-  RotM R;
-  twister<HASD>(g.e, R);
-  DRotM DA, DB;
-  dtwister<HASD>(g.e, dA, DA);
-  dtwister<HASD>(g.e, dB, DB);
-  int p = c.tdst[t];
-  const double *wdp = v.wd + c.blk_off[p];
-  double wb[NA * NB];
-#pragma unroll
-  for (int q = 0; q < NA * NB; q++) wb[q] = __ldg(wdp + q);
-  MolRho<PA, PB, K3C> GA, GB;
-  mol_rho<PA, PB, K3C>(R, DA, wb, GA);
-  mol_rho<PA, PB, K3C>(R, DB, wb, GB);
-  double fa[3], fb[3];
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    double sa = 0.0, sb = 0.0;
-#pragma unroll
-    for (int e = 0; e < NE; e++) {
-      sa = fma(M[e], GA.H[q][e], sa);
-      sa = fma(Ma[q + 3 * e], GA.G[e], sa);
-      sb = fma(M[e], GB.H[q][e], sb);
-      sb = fma(Mb[q + 3 * e], GB.G[e], sb);
-    }
-    fa[q] = sa;
-    fb[q] = sb;
-  }
-  // shell level (denS3, no rotation, mvalue 0)
+  // shell level first (denS3, no rotation, mvalue 0): with rhoma = rhat dx +
+  // amt dp and rhomb = -sighat dy + bmt dp - rhoma / 2, only the gd-weighted
+  // sums of dp, dx, dy enter
+  double gp = 0.0, gx = 0.0, gy = 0.0;
   {
     constexpr int NS = SA * SB;
-    double Dp[NS], Dx[NS], Dy[NS], s0[NS], s1[NS], s2[NS], s3[NS];
+    double Dp[NS], Dx[NS], Dy[NS], s0[NS];
+    if constexpr (QSUM) {
+      interp3c<NS, true>(c, fd.c3rhoq[in1][in2][indna][1], g.x, g.z, g.cost, s0, Dp, Dx, Dy);
+    } else {
+      double s1[NS], s2[NS], s3[NS];
 #pragma unroll
-    for (int e = 0; e < NS; e++) Dp[e] = Dx[e] = Dy[e] = 0.0;
+      for (int e = 0; e < NS; e++) Dp[e] = Dx[e] = Dy[e] = 0.0;
 #pragma unroll 1
-    for (int isorp = 0; isorp < nk; isorp++) {
-      interp3c<NS, true>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, s0, s1, s2, s3);
-      double Q = qk[isorp];
+      for (int isorp = 0; isorp < nk; isorp++) {
+        interp3c<NS, true>(c, fd.c3rho[in1][in2][indna][1][isorp], g.x, g.z, g.cost, s0, s1, s2, s3);
+        double Q = qk[isorp];
 #pragma unroll
-      for (int e = 0; e < NS; e++) {
-        Dp[e] = fma(s1[e], Q, Dp[e]);
-        Dx[e] = fma(s2[e], Q, Dx[e]);
-        Dy[e] = fma(s3[e], Q, Dy[e]);
+        for (int e = 0; e < NS; e++) {
+          Dp[e] = fma(s1[e], Q, Dp[e]);
+          Dx[e] = fma(s2[e], Q, Dx[e]);
+          Dy[e] = fma(s3[e], Q, Dy[e]);
+        }
       }
     }
     const double *gd = v.gd + (long long)VXC_WSH * p;
@@ -778,14 +744,88 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
       for (int b = 0; b < SB; b++) {
         int e = a * SB + b;
         double w = gd[a + SA * b];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          double ra = g.rhat[q] * Dx[e] + amt[q] * Dp[e];
-          double rb = -g.sighat[q] * Dy[e] + bmt[q] * Dp[e] - ra / 2.0;
-          fa[q] = fma(w, ra, fa[q]);
-          fb[q] = fma(w, rb, fb[q]);
-        }
+        gp = fma(w, Dp[e], gp);
+        gx = fma(w, Dx[e], gx);
+        gy = fma(w, Dy[e], gy);
       }
+  }
+  // orbital level (den3): value and derivatives, Qneutral-summed
+  double F[NE], DpF[NE], DxF[NE], DyF[NE];
+  if constexpr (QSUM) {
+    interp3c<NE, true>(c, fd.c3rhoq[in1][in2][indna][0], g.x, g.z, g.cost, F, DpF, DxF, DyF);
+  } else {
+    double t0[NE], t1[NE], t2[NE], t3[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) F[e] = DpF[e] = DxF[e] = DyF[e] = 0.0;
+#pragma unroll 1
+    for (int isorp = 0; isorp < nk; isorp++) {
+      interp3c<NE, true>(c, fd.c3rho[in1][in2][indna][0][isorp], g.x, g.z, g.cost, t0, t1, t2, t3);
+      double Q = qk[isorp];
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        F[e] = fma(t0[e], Q, F[e]);
+        DpF[e] = fma(t1[e], Q, DpF[e]);
+        DxF[e] = fma(t2[e], Q, DxF[e]);
+        DyF[e] = fma(t3[e], Q, DyF[e]);
+      }
+    }
+  }
+  // the sin(theta) factor of the mvalue = 1 channels (getDMEs_Fdata_3c
+  // :827-832), in place
+  double sint = sqrt(fmax(1.0e-5, 1.0 - g.cost * g.cost));
+  sfor<NE>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    if constexpr (PL::m.mv[e] == 1) {
+      DpF[e] = DpF[e] * sint - g.cost * F[e] / sint;
+      F[e] = F[e] * sint;
+      DxF[e] = DxF[e] * sint;
+      DyF[e] = DyF[e] * sint;
+    }
+  });
+  // vdxcMa = rhat dx + amt dp, vdxcMb = -sighat dy + bmt dp - vdxcMa / 2
+  // (:285-301): contracted with the molecular-frame weights G only through
+  // the sums of dx G, dp G, dy G
+  RotM R;
+  twister<HASD>(g.e, R);
+  const double *wdp = v.wd + c.blk_off[p];
+  double wb[NA * NB];
+#pragma unroll
+  for (int q = 0; q < NA * NB; q++) wb[q] = __ldg(wdp + q);
+  double fa[3], fb[3];
+  {
+    double dA[3][3][3], dB[3][3][3];
+    depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
+    DRotM DA;
+    dtwister<HASD>(g.e, dA, DA);
+    MolRho<PA, PB, K3C> G;
+    mol_rho<PA, PB, K3C>(R, DA, wb, G);
+    double sx = 0.0, sp = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) sx = fma(DxF[e], G.G[e], sx), sp = fma(DpF[e], G.G[e], sp);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double h = 0.0;
+#pragma unroll
+      for (int e = 0; e < NE; e++) h = fma(F[e], G.H[q][e], h);
+      fa[q] = h + g.rhat[q] * (sx + gx) + amt[q] * (sp + gp);
+    }
+    DRotM DB;
+    dtwister<HASD>(g.e, dB, DB);
+    mol_rho<PA, PB, K3C>(R, DB, wb, G);
+    double tx = 0.0, tp = 0.0, ty = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      tx = fma(DxF[e], G.G[e], tx);
+      tp = fma(DpF[e], G.G[e], tp);
+      ty = fma(DyF[e], G.G[e], ty);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double h = 0.0;
+#pragma unroll
+      for (int e = 0; e < NE; e++) h = fma(F[e], G.H[q][e], h);
+      fb[q] = h - g.sighat[q] * (ty + gy) + bmt[q] * (tp + gp) - 0.5 * (g.rhat[q] * (tx + gx) + amt[q] * (tp + gp));
+    }
   }
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -795,23 +835,26 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
   }
 }
 
-template <bool HASD>
+template <bool HASD, bool QSUM>
 __global__ void __launch_bounds__(128) k_dvxc_3c(Ctx3c c, VxcArgs v) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.T; t += gridDim.x * blockDim.x) {
-    int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
+    int t = c.tperm ? c.tperm[i] : i;
+    int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
+    if (qsum_triple(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
+    int pa = c.fd->sp[in1].pattern, pb = c.fd->sp[in2].pattern;
     int key = pa * 3 + pb;
     switch (key) {
-      case PAT_SP * 3 + PAT_SP: trip_dvxc<PAT_SP, PAT_SP, HASD>(c, v, t); break;
-      case PAT_SP * 3 + PAT_S: trip_dvxc<PAT_SP, PAT_S, HASD>(c, v, t); break;
-      case PAT_S * 3 + PAT_SP: trip_dvxc<PAT_S, PAT_SP, HASD>(c, v, t); break;
-      case PAT_S * 3 + PAT_S: trip_dvxc<PAT_S, PAT_S, HASD>(c, v, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_dvxc<PAT_SP, PAT_SP, HASD, QSUM>(c, v, t); break;
+      case PAT_SP * 3 + PAT_S: trip_dvxc<PAT_SP, PAT_S, HASD, QSUM>(c, v, t); break;
+      case PAT_S * 3 + PAT_SP: trip_dvxc<PAT_S, PAT_SP, HASD, QSUM>(c, v, t); break;
+      case PAT_S * 3 + PAT_S: trip_dvxc<PAT_S, PAT_S, HASD, QSUM>(c, v, t); break;
       default:
         if constexpr (HASD) {
-          if (key == PAT_SPD * 3 + PAT_SPD) trip_dvxc<PAT_SPD, PAT_SPD, HASD>(c, v, t);
-          else if (key == PAT_SPD * 3 + PAT_SP) trip_dvxc<PAT_SPD, PAT_SP, HASD>(c, v, t);
-          else if (key == PAT_SP * 3 + PAT_SPD) trip_dvxc<PAT_SP, PAT_SPD, HASD>(c, v, t);
-          else if (key == PAT_SPD * 3 + PAT_S) trip_dvxc<PAT_SPD, PAT_S, HASD>(c, v, t);
-          else if (key == PAT_S * 3 + PAT_SPD) trip_dvxc<PAT_S, PAT_SPD, HASD>(c, v, t);
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_dvxc<PAT_SPD, PAT_SPD, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_dvxc<PAT_SPD, PAT_SP, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_dvxc<PAT_SP, PAT_SPD, HASD, QSUM>(c, v, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_dvxc<PAT_SPD, PAT_S, HASD, QSUM>(c, v, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_dvxc<PAT_S, PAT_SPD, HASD, QSUM>(c, v, t);
         }
     }
   }
@@ -865,8 +908,13 @@ int launch_rho_3c(const VxcArgs &v, cudaStream_t s) {
   int threads = 128;
   long long need = ((long long)v.a.ntrip + threads - 1) / threads;
   int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
-  if (v.a.have_d) k_rho_3c<true><<<blocks, threads, 0, s>>>(c, v);
-  else k_rho_3c<false><<<blocks, threads, 0, s>>>(c, v);
+  if (v.a.have_d) {
+    k_rho_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
+    if (!v.qsum_all) k_rho_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
+  } else {
+    k_rho_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
+    if (!v.qsum_all) k_rho_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
+  }
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -897,8 +945,13 @@ int launch_dvxc_3c(const VxcArgs &v, cudaStream_t s) {
   int threads = 128;
   long long need = ((long long)v.a.ntrip + threads - 1) / threads;
   int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
-  if (v.a.have_d) k_dvxc_3c<true><<<blocks, threads, 0, s>>>(c, v);
-  else k_dvxc_3c<false><<<blocks, threads, 0, s>>>(c, v);
+  if (v.a.have_d) {
+    k_dvxc_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
+    if (!v.qsum_all) k_dvxc_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
+  } else {
+    k_dvxc_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
+    if (!v.qsum_all) k_dvxc_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
+  }
   FB_LAUNCH_CHECK();
   return 0;
 }

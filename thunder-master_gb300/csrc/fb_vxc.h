@@ -25,6 +25,9 @@ struct VxcArgs {
   double *off, *on;
   double *wd, *gd;
   double *f3a, *f3b, *f3c, *fvxc;
+  // every species triple has Qneutral-summed three-center cells (one kernel
+  // launch; otherwise a second one takes the triples that lack them)
+  int qsum_all;
 };
 
 // assemble_rho_2c + assemble_rho_weighted_2c: writes all four density sets
