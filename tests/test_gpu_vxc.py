@@ -79,8 +79,9 @@ def test_vxc_after_overlap(ctx, fdata_root):
     _check(ctx, ref, s.npairs)
 
 
+@pytest.mark.parametrize("prec", [0, 1])  # FP64 kernels, double-float three-center kernels
 @pytest.mark.parametrize("name", ["sic_small", "si64", "cho_small", "sic_vac", "sic_cluster"])
-def test_vxc_forces_match_oracle(ctx, fdata_root, name):
+def test_vxc_forces_match_oracle(ctx, fdata_root, name, prec):
     """Dassemble_vxc: the pair forces vxc_off_site / vxc_on_site, f3xca/b/c,
     the vxc pair sums and their addition to ftot, plain and as one graph."""
     from conftest import symmetric_denmat
@@ -95,17 +96,21 @@ def test_vxc_forces_match_oracle(ctx, fdata_root, name):
     ctx.driver_neighbors()
     ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
     ctx.set_denmat(rho, cape)
+    ctx.set_precision(prec)
     what = fbgpu.FB_ALL | fbgpu.FB_VXC
-    ctx.assemble(what)
-    ctx.Dassemble(what)
-    for k in ("vxc_off_site", "vxc_on_site", "f3xca", "f3xcb", "f3xcc", "vxc"):
-        assert np.abs(ctx.forces(k) - ref[k]).max() <= TOL, k
-    want = harris["ftot"] + ref["ftot_add"]
-    assert np.abs(ctx.forces("ftot") - want).max() <= TOL
-    for _ in range(2):  # value and force pass as one graph
-        ctx.assemble_graph(what | fbgpu.FB_FORCES)
+    try:
+        ctx.assemble(what)
+        ctx.Dassemble(what)
+        for k in ("vxc_off_site", "vxc_on_site", "f3xca", "f3xcb", "f3xcc", "vxc"):
+            assert np.abs(ctx.forces(k) - ref[k]).max() <= TOL, k
+        want = harris["ftot"] + ref["ftot_add"]
         assert np.abs(ctx.forces("ftot") - want).max() <= TOL
-        assert np.abs(ctx.forces("vxc_on_site") - ref["vxc_on_site"]).max() <= TOL
+        for _ in range(2):  # value and force pass as one graph
+            ctx.assemble_graph(what | fbgpu.FB_FORCES)
+            assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+            assert np.abs(ctx.forces("vxc_on_site") - ref["vxc_on_site"]).max() <= TOL
+    finally:
+        ctx.set_precision(1)
 
 
 def test_vxc_errors(ctx, fdata_root):

@@ -1716,7 +1716,8 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     CU(cudaMemsetAsync(ctx->d_f3xb.p, 0, a3, ctx->stream));
     CU(cudaMemsetAsync(ctx->d_f3xc.p, 0, a3, ctx->stream));
     if (a.ntrip > 0) {
-      KL(KT_DVXC3C, launch_dvxc_3c(v, ctx->stream));
+      if (use_df(ctx)) KL(KT_DVXC3C, launch_dvxc_3c_df(v, ctx->stream));
+      else KL(KT_DVXC3C, launch_dvxc_3c(v, ctx->stream));
       if (!v.qsum_all) ctx->launches++;
     }
     KL(KT_VXCF, launch_vxc_forces(v, ctx->stream));

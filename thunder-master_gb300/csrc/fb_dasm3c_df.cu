@@ -6,108 +6,6 @@
 
 namespace fb {
 
-// Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189) in df, evaluated with the
-// origin at atom 1.  Its expressions are translation invariant (the three
-// coefficients of each bracket sum to zero), and relative coordinates avoid
-// the cancellation of absolute squared norms: u = r2 - r1, v = ratm - r1.
-// The quantities shared by the three Cartesian components:
-struct DepsPre {
-  df ic, A1, A2, B1, B2;
-  df vu[3];
-  bool zero;  // sighat x rnabc below 1e-3: all derivatives vanish
-};
-
-__device__ __forceinline__ void depsilon_pre_df(const df u[3], const df v[3], DepsPre &p) {
-  df rn[3] = {v[0] - u[0] * 0.5f, v[1] - u[1] * 0.5f, v[2] - u[2] * 0.5f};
-  df c0 = u[1] * rn[2] - u[2] * rn[1];
-  df c1 = u[2] * rn[0] - u[0] * rn[2];
-  df c2 = u[0] * rn[1] - u[1] * rn[0];
-  df cm = df_sqrt(c0 * c0 + c1 * c1 + c2 * c2);
-  p.zero = cm.h < 1.0e-3f;
-  p.ic = p.zero ? df_zero() : df_rcp(cm);
-#pragma unroll
-  for (int k = 0; k < 3; k++) p.vu[k] = v[k] - u[k];
-  p.A1 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-  p.A2 = -(u[0] * v[0] + u[1] * v[1] + u[2] * v[2]);
-  p.B1 = u[0] * p.vu[0] + u[1] * p.vu[1] + u[2] * p.vu[2];
-  p.B2 = -(v[0] * p.vu[0] + v[1] * p.vu[1] + v[2] * p.vu[2]);
-}
-
-// component ix of deps/dratm (dA[imu][k]) and deps/dr1 (dB[imu][k])
-__device__ __forceinline__ void depsilon_comp_df(int ix, const df u[3], const df v[3], df iz, const df e[3][3],
-                                                 const DepsPre &p, df dA[3][3], df dB[3][3]) {
-#pragma unroll
-  for (int a = 0; a < 3; a++)
-#pragma unroll
-    for (int b = 0; b < 3; b++) dA[a][b] = dB[a][b] = df_zero();
-  if (p.zero) return;
-#pragma unroll
-  for (int imu = 0; imu < 3; imu++) {
-    df sa = df_zero(), sb = df_zero();
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      double lv = levi(ix, imu, k);
-      if (lv > 0.0) {
-        sa = sa + u[k];
-        sb = sb + p.vu[k];
-      } else if (lv < 0.0) {
-        sa = sa - u[k];
-        sb = sb - p.vu[k];
-      }
-    }
-    df ei = e[imu][1] * p.ic;
-    dA[imu][1] = p.ic * (sa - ei * (p.A1 * v[ix] + p.A2 * u[ix]));
-    dB[imu][1] = p.ic * (sb - ei * (p.B1 * v[ix] + p.B2 * u[ix]));
-    df t = e[imu][2] * e[ix][2];
-    dB[imu][2] = iz * ((ix == imu) ? t - df_one() : t);
-  }
-  dA[0][0] = e[2][2] * dA[1][1] - e[1][2] * dA[2][1];
-  dA[1][0] = e[0][2] * dA[2][1] - e[2][2] * dA[0][1];
-  dA[2][0] = e[1][2] * dA[0][1] - e[0][2] * dA[1][1];
-  dB[0][0] = e[2][2] * dB[1][1] - e[2][1] * dB[1][2] - e[1][2] * dB[2][1] + e[1][1] * dB[2][2];
-  dB[1][0] = e[0][2] * dB[2][1] - e[0][1] * dB[2][2] - e[2][2] * dB[0][1] + e[2][1] * dB[0][2];
-  dB[2][0] = e[1][2] * dB[0][1] - e[1][1] * dB[0][2] - e[0][2] * dB[1][1] + e[0][1] * dB[1][2];
-}
-
-// sum_e M_e H(e) for one Cartesian component, H = dL^T rho R + L^T rho dR at
-// the ME positions (the dL M R^T and L M dR^T terms of Dmatrix,
-// M_Drotations.f90:456-471, contracted with rho); dP is that component of
-// the p-shell rotation derivative (Dtwister, :236-249): dP[a][b] =
-// deps(perm a, perm b)
-template <int PA, int PB>
-__device__ __forceinline__ df mol_HM_df(const RotDF &R, const df dP[3][3], const df *rho, const df *rR,
-                                        const df *M) {
-  using PL = Plan<PA, PB, K3C>;
-  constexpr int NA = PL::NA;
-  df acc = df_zero();
-  sfor<PL::m.n>([&](auto E) {
-    constexpr int e = decltype(E)::value;
-    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
-    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
-    constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
-    df h = df_zero();
-    if constexpr (sa > 0) {
-      sfor<3>([&](auto KK) {
-        constexpr int k = decltype(KK)::value;
-        h = h + dP[k][ma] * rR[(oa + k) + NA * b];
-      });
-    }
-    if constexpr (sb > 0) {
-      sfor<2 * sa + 1>([&](auto KK) {
-        constexpr int k = decltype(KK)::value;
-        df t = df_zero();
-        sfor<3>([&](auto NU) {
-          constexpr int q = decltype(NU)::value;
-          t = t + rho[(oa + k) + NA * (ob + q)] * dP[q][mb];
-        });
-        h = h + ((sa == 0) ? t : Lrot_df<sa>(R, k, ma) * t);
-      });
-    }
-    acc = acc + M[e] * h;
-  });
-  return acc;
-}
-
 // MLP: F and its cos / x / y derivatives come from the MLP-3c results of
 // list position i instead of the tables
 template <int PA, int PB, bool MLP>

@@ -43,6 +43,8 @@ int launch_vxc(const VxcArgs &v, cudaStream_t s);
 int launch_dvxc_2c(const VxcArgs &v, cudaStream_t s);
 // Dassemble_vxc_3c: accumulates onto f3a/b/c (cleared by the caller)
 int launch_dvxc_3c(const VxcArgs &v, cudaStream_t s);
+// the same in double-float on the FP32 pipe (s and sp bases)
+int launch_dvxc_3c_df(const VxcArgs &v, cudaStream_t s);
 // build_forces vxc terms: fvxc and ftot += fvxc + f3xca + f3xcb + f3xcc
 int launch_vxc_forces(const VxcArgs &v, cudaStream_t s);
 
