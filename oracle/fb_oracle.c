@@ -3155,7 +3155,7 @@ int or_dassemble_ewaldlr(or_sys *s, const double *rho, const double *ewald, cons
 
 /* lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:56-190):
  * out = exc, muxc, dexc, d2exc, dmuxc, d2muxc.  The low-density branch's
- * d2dec keeps the reference's (dden*3) factor (:143-144). */
+ * d2dec keeps the reference's (dden*3) factor (:142). */
 void or_lda_ceperley_alder(double rh, double *out) {
   const double delta_rh = 1.0e-6;
   double exc, muxc, dexc, d2exc, dmuxc, d2muxc;

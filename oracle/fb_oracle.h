@@ -202,7 +202,7 @@ void or_rotate(or_fdata *fd, int in1, int in3, const double *eps, int norb_mu,
 
 /* Test switch, off by default: 1 replaces the reference's two forms that are
  * not the derivative of its values -- the (dden*3) of d2dec in
- * lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:143) and the
+ * lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:142) and the
  * three-point linear branch of getMEs/getDMEs_Fdata_3c
  * (e.FDATA/M_Fdata_3c.f90:406-410, :684-691), whose x / y derivatives use
  * one scalar gradient for every matrix element -- by exact ones (dden**3,

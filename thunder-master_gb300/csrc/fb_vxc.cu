@@ -19,7 +19,7 @@ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
 // lda_ceperley_alder (g.XC_FUNCTIONALS/lda_ceperley_alder.f90:56-190):
 // muxc (eV), dmuxc and d2muxc (eV A^3, eV A^6).  The low-density branch's
-// d2dec keeps the reference's (dden*3) factor (:143-144).
+// d2dec keeps the reference's (dden*3) factor (:142).
 struct Lda {
   double muxc, dmuxc, d2muxc;
 };
@@ -466,8 +466,8 @@ __global__ void __launch_bounds__(128) k_vxc(Ctx2c c, VxcArgs v) {
 //              gA(a,b) = sum_{mu != nu} rho_s (d2muxc_b rho_b_s - d2muxc_in rho_in_s)
 //                                                                   on dW atom
 // with the self block's Dblocko (the diagonal shell-density derivative of
-// :502-505, never assembled for the self pair) zero, and rho_bond's
-// off-diagonal derivatives taken as rho_in's (:572-575), as the reference
+// :498-509, never assembled for the self pair) zero, and rho_bond's
+// off-diagonal derivatives taken as rho_in's (:566, :582), as the reference
 // does.  The three-center pass contracts rho dmuxc_in and the shell sums
 // of rho d2muxc_in (rho_in - Wi S) left here per pair.
 template <int PA, int PB, bool HASD>
