@@ -80,7 +80,8 @@ extern "C" {
 #define FB_VNL2C 256u        /* vnl 2c: atom, ontop left / right (assemble_vnl_2c, M_assemble_PP_2c.f90:232) */
 #define FB_VNL3C 512u        /* vnl 3c (assemble_vnl_3c, M_assemble_PP_3c.f90:94); fb_dassemble: the vnl forces */
 #define FB_EWALD 1024u       /* DOGS Ewald: the matrix (assemble_ewald) and the ewaldsr / ewaldlr blocks
-                                (M_assemble_ewald_DOGS.f90:98, :404, :633) */
+                                (M_assemble_ewald_DOGS.f90:98, :404, :633); Harris: zero ewaldsr /
+                                ewaldlr blocks and forces (M_assemble_ewald_Harris.f90:92-239) */
 #define FB_VXC 2048u         /* McWEDA exchange-correlation, Harris (assemble_vxc,
                                 M_assemble_vxc_McWEDA_Harris.f90:102): the input densities
                                 (M_assemble_rho_McWEDA_Harris.f90) and the vxc blocks; reads the

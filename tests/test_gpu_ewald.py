@@ -85,14 +85,44 @@ def test_ewald_forces_match_oracle(ctx, fdata_root, name):
         assert np.abs(ctx.forces("ftot") - want).max() <= TOL
 
 
+def test_harris_ewald_is_zero(ctx, fdata_root):
+    """The Harris assemble_ewaldsr / assemble_ewaldlr allocate zero blocks and
+    Dassemble_ewaldsr zero pair forces (j.ASSEMBLERS/M_assemble_ewald_Harris.f90,
+    k.DASSEMBLERS/M_Dassemble_ewald_Harris.f90); there is no Ewald matrix, and
+    ftot is the Harris one."""
+    from conftest import symmetric_denmat
+    path, nZ, st = case(fdata_root, "sic_small")
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+    rho, cape = symmetric_denmat(s, np.array([fd.norb(int(q)) for q in st.imass]), 3)
+    ref = s.dassemble(rho, cape)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    ctx.set_denmat(rho, cape)
+    what = fbgpu.FB_ALL | fbgpu.FB_EWALD
+    ctx.assemble(what)
+    assert not ctx.blocks("ewaldsr").any() and not ctx.blocks("ewaldlr").any()
+    with pytest.raises(fbgpu.FBError) as e:
+        ctx.ewald()
+    assert e.value.code == 11
+    ctx.Dassemble(what)
+    for k in ("ewaldsr", "ewaldlr", "ewald"):
+        assert not ctx.forces(k).any()
+    assert np.abs(ctx.forces("ftot") - ref["ftot"]).max() <= TOL
+    ctx.assemble_graph(what | fbgpu.FB_FORCES)
+    assert np.abs(ctx.forces("ftot") - ref["ftot"]).max() <= TOL
+
+
 def test_ewald_errors(ctx, fdata_root):
     path, nZ, st = case(fdata_root, "sic_small")
     ctx.read_Fdata(path, nZ)
     ctx.set_structure(st.ratom, st.imass, st.lattice)
     ctx.driver_neighbors()
     ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
-    with pytest.raises(fbgpu.FBError) as e:      # DOGS only
-        ctx.assemble(fbgpu.FB_ALL | fbgpu.FB_EWALD)
+    with pytest.raises(fbgpu.FBError) as e:      # no Ewald matrix yet
+        ctx.ewald()
     assert e.value.code == 11
     ctx.set_theory(fbgpu.FB_THEORY_DOGS)
     ctx.set_charges(np.zeros((len(st.imass), 3)))

@@ -95,6 +95,7 @@ struct fb_ctx {
   DevBuf d_svnl, d_dsvnl, d_vnl, d_rho_pp, d_vnl_atom, d_vnl_ontop, d_f3nla, d_f3nlb, d_f3nlc, d_fvnl;
   // DOGS Ewald: the N x N matrix, its g / L lists, atom charges, sr / lr blocks
   bool have_ewald = false;
+  bool ewald_matrix = false;  // the DOGS Ewald matrix (Harris assembles zero blocks only)
   int ew_ng = 0, ew_nl = 0;
   double ew_kappa = 0.0;
   DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs;
@@ -324,7 +325,7 @@ int fb_load_fdata(fb_ctx *ctx, const char *fdata_dir, int nspecies, const int *n
   CU(cudaMemcpy(ctx->d_gxy.p, f.gxy.data(), f.gxy.size() * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_fdata = true;
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = ctx->ewald_matrix = false;
   return FB_OK;
 }
 
@@ -424,7 +425,7 @@ int fb_set_batch(fb_ctx *ctx, int nstruct, const int *natoms, const double *rato
   CU(cudaMemcpy(ctx->d_satom_off.p, ctx->h_satom_off.data(), (nstruct + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_speriodic.p, per.data(), nstruct * sizeof(int), cudaMemcpyHostToDevice));
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = ctx->ewald_matrix = false;
   return fb_update_positions(ctx, ratom);
 }
 
@@ -481,7 +482,7 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_neigh = false;
-  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = ctx->ewald_matrix = false;
   return FB_OK;
 }
 
@@ -793,7 +794,7 @@ int fb_neighbors_pp(fb_ctx *ctx) {
   if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "vnl maps: single structures (a batch of one)");
   CU(cudaSetDevice(ctx->device));
   int N = ctx->N;
-  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = false;
+  ctx->have_pp_neigh = ctx->have_rho_pp = ctx->have_ewald = ctx->ewald_matrix = false;
   ctx->assembled &= ~(unsigned)(FB_SVNL | FB_VNL2C | FB_VNL3C);
   ctx->dassembled &= ~(unsigned)(FB_VNL2C | FB_VNL3C);
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
@@ -928,6 +929,8 @@ int fb_get_pp_common(fb_ctx *ctx, int *ncommon, int *iatom_common_j, int *iatom_
 int fb_get_ewald(fb_ctx *ctx, double *ewald) {
   if (!ctx || !ewald) return FB_ERR_ARG;
   if (!ctx->have_ewald) return fail(ctx, FB_ERR_STATE, "fb_assemble with FB_EWALD first");
+  if (!ctx->ewald_matrix)
+    return fail(ctx, FB_ERR_STATE, "no Ewald matrix: the Harris assemble_ewald only allocates zero ewaldsr / ewaldlr blocks");
   CU(cudaMemcpyAsync(ewald, ctx->d_ewald.p, (size_t)ctx->N * ctx->N * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -1400,7 +1403,13 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     }
     KL(KT_VXC, launch_vxc(v, ctx->stream));
   }
-  if (what & FB_EWALD) {
+  if ((what & FB_EWALD) && !a.dogs) {
+    // Harris: assemble_ewaldsr / assemble_ewaldlr allocate zero blocks
+    // (j.ASSEMBLERS/M_assemble_ewald_Harris.f90:92-239)
+    size_t nb = (size_t)ctx->nblock * sizeof(double);
+    CU(cudaMemsetAsync(ctx->d_ewsr.p, 0, nb, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_ewlr.p, 0, nb, ctx->stream));
+  } else if (what & FB_EWALD) {
     EwaldArgs e = ewald_args(ctx);
     KL(KT_EWALD, launch_ewald_matrix(e, ctx->stream));
     if (e.ng > 0) ctx->launches++;  // structure factors + tiles
@@ -1439,8 +1448,11 @@ static int check_assemble(fb_ctx *ctx, unsigned what) {
     return fail(ctx, FB_ERR_TABLE, "FB_DIPOLE: the Fdata has no z-dipole table (dipole_z)");
   if ((what & FB_DIPOLE) || (dogs && (what & FB_VNA2C)))
     CHK(ctx->d_dip.ensure((size_t)ctx->nblock * sizeof(double) + 8));
-  if (what & FB_EWALD) {
-    if (!dogs) return fail(ctx, FB_ERR_STATE, "Ewald: the DOGS theory (fb_set_theory) first");
+  if ((what & FB_EWALD) && !dogs) {
+    size_t nb = (size_t)ctx->nblock * sizeof(double) + 8;
+    CHK(ctx->d_ewsr.ensure(nb));
+    CHK(ctx->d_ewlr.ensure(nb));
+  } else if (what & FB_EWALD) {
     if (!ctx->have_charges) return fail(ctx, FB_ERR_STATE, "Ewald: fb_set_charges first");
     if (ctx->nstruct != 1) return fail(ctx, FB_ERR_UNSUPPORTED, "Ewald: single structures (a batch of one)");
     if (!(what & FB_VNA2C) && !(ctx->have_dip && (ctx->assembled & FB_S)))
@@ -1482,7 +1494,10 @@ static void assemble_done(fb_ctx *ctx, unsigned what) {
   if (what & FB_VNA2C) ctx->have_vna2c = true;
   if ((what & FB_DIPOLE) || (ctx->theory == FB_THEORY_DOGS && (what & FB_VNA2C))) ctx->have_dip = true;
   ctx->assembled |= what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_VXC);
-  if (what & FB_EWALD) ctx->have_ewald = true;
+  if (what & FB_EWALD) {
+    ctx->have_ewald = true;
+    ctx->ewald_matrix = ctx->theory == FB_THEORY_DOGS;
+  }
 }
 
 int fb_assemble(fb_ctx *ctx, unsigned what) {
@@ -1626,8 +1641,13 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = fal
     DevBuf *b3[] = {&ctx->d_f3xa, &ctx->d_f3xb, &ctx->d_f3xc, &ctx->d_fvxc};
     for (DevBuf *b : b3) CHK(b->ensure(ab + 8));
   }
-  if (what & FB_EWALD) {
-    if (!dogs) return fail(ctx, FB_ERR_STATE, "Ewald forces: the DOGS theory (fb_set_theory) first");
+  if ((what & FB_EWALD) && !dogs) {
+    // Harris: Dassemble_ewaldsr allocates zero pair forces, Dassemble_ewaldlr
+    // does nothing (k.DASSEMBLERS/M_Dassemble_ewald_Harris.f90:94-160)
+    CHK(ctx->d_fsr.ensure((size_t)3 * P * sizeof(double) + 8));
+    CHK(ctx->d_flr.ensure((size_t)3 * N * sizeof(double) + 8));
+    CHK(ctx->d_fewald.ensure((size_t)3 * N * sizeof(double) + 8));
+  } else if (what & FB_EWALD) {
     if (!ctx->have_ewald && !(graph_values && (what & FB_EWALD)))
       return fail(ctx, FB_ERR_STATE, "Ewald forces read the Ewald matrix: assemble FB_EWALD first");
     size_t n = (size_t)N;
@@ -1658,7 +1678,12 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
   // DOGS: the 2c kernel also leaves the per-pair sums the 3c and Ewald kernels read
   if (a.dogs && (what & (FB_VNA3C | FB_EWALD))) w2 |= 8u;
   if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
-  if (what & FB_EWALD) {
+  if ((what & FB_EWALD) && !a.dogs) {
+    CU(cudaMemsetAsync(ctx->d_fsr.p, 0, (size_t)3 * P * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_flr.p, 0, (size_t)3 * N * sizeof(double), ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_fewald.p, 0, (size_t)3 * N * sizeof(double), ctx->stream));
+  }
+  if ((what & FB_EWALD) && a.dogs) {
     // Dassemble_ewald (dewald, the Ewald energy force, the katom sums) and
     // the ewaldsr three-center terms into f3na, before build_forces sums them
     EwaldArgs e = ewald_args(ctx);
@@ -1722,7 +1747,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     }
     KL(KT_VXCF, launch_vxc_forces(v, ctx->stream));
   }
-  if (what & FB_EWALD) {
+  if ((what & FB_EWALD) && a.dogs) {
     // Dassemble_ewaldsr / ewaldlr pair and atom forces and their
     // build_forces terms, added into ftot
     EwaldArgs e = ewald_args(ctx);
