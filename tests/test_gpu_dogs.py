@@ -54,8 +54,9 @@ def gpu_dogs_forces(ctx, rho, cape, graph=False):
     return {k: ctx.forces(k) for k in FORCES}
 
 
+@pytest.mark.parametrize("prec", [0, 1])  # FP64, double-float three-center kernels
 @pytest.mark.parametrize("name", ["sic_small", "cho_small", "si64", "sic_vac"])
-def test_dogs_forces_match_oracle(ctx, fdata_root, name):
+def test_dogs_forces_match_oracle(ctx, fdata_root, name, prec):
     from conftest import symmetric_denmat
     path, nZ, st = workload(name, fdata_root, dogs=True)
     fd = orc.Fdata(path, nZ)
@@ -64,25 +65,34 @@ def test_dogs_forces_match_oracle(ctx, fdata_root, name):
     rho, cape = symmetric_denmat(s, norb, 23)
     dq = charges(len(st.imass), 29)
     ref = s.dassemble_dogs(rho, cape, dq)
-    gpu_dogs(ctx, path, nZ, st, dq)
-    got = gpu_dogs_forces(ctx, rho, cape)
-    for k in FORCES:
-        assert np.abs(got[k] - ref[k]).max() <= TOL_FORCE, (k, np.abs(got[k] - ref[k]).max())
-    # the same step as one graph (value and force pass), replayed
-    for _ in range(2):
-        g = gpu_dogs_forces(ctx, rho, cape, graph=True)
+    ctx.set_precision(prec)
+    try:
+        gpu_dogs(ctx, path, nZ, st, dq)
+        got = gpu_dogs_forces(ctx, rho, cape)
         for k in FORCES:
-            assert np.abs(g[k] - ref[k]).max() <= TOL_FORCE, ("graph", k)
+            assert np.abs(got[k] - ref[k]).max() <= TOL_FORCE, (k, np.abs(got[k] - ref[k]).max())
+        # the same step as one graph (value and force pass), replayed
+        for _ in range(2):
+            g = gpu_dogs_forces(ctx, rho, cape, graph=True)
+            for k in FORCES:
+                assert np.abs(g[k] - ref[k]).max() <= TOL_FORCE, ("graph", k)
+    finally:
+        ctx.set_precision(fbgpu.FB_PREC_DF)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("name", ["sic_small", "cho_small", "si64", "sic_vac"])
-def test_dogs_matches_oracle(ctx, fdata_root, name):
+def test_dogs_matches_oracle(ctx, fdata_root, name, prec):
     path, nZ, st = workload(name, fdata_root, dogs=True)
     fd = orc.Fdata(path, nZ)
     s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
     dq = charges(len(st.imass), 17)
     ref = s.assemble_dogs(dq)
-    got = gpu_dogs(ctx, path, nZ, st, dq)
+    ctx.set_precision(prec)
+    try:
+        got = gpu_dogs(ctx, path, nZ, st, dq)
+    finally:
+        ctx.set_precision(fbgpu.FB_PREC_DF)
     for g, r, w in zip(got, ref, ("S", "T", "vna", "vnao", "dip")):
         assert g.shape == r.shape, w
         assert np.abs(g - r).max() <= TOL, (w, np.abs(g - r).max())

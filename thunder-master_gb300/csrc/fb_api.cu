@@ -1304,6 +1304,10 @@ static int host_scan(fb_ctx *ctx, const DevBuf &cnt, int n, std::vector<T> &off,
 static bool use_df(const fb_ctx *ctx) {
   return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d && ctx->theory == FB_THEORY_HARRIS;
 }
+// the DOGS three-center kernels in double-float
+static bool use_df_dogs(const fb_ctx *ctx) {
+  return ctx->prec == FB_PREC_DF && !ctx->fdh.have_d && ctx->theory == FB_THEORY_DOGS;
+}
 
 int fb_set_theory(fb_ctx *ctx, int theory) {
   if (!ctx || (theory != FB_THEORY_HARRIS && theory != FB_THEORY_DOGS)) return FB_ERR_ARG;
@@ -1423,6 +1427,7 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     at.tperm = a.tperm + nm;
     at.ntrip = a.ntrip - nm;
     if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
+    else if (use_df_dogs(ctx)) KL(KT_ASM3C, launch_assemble_3c_dogs_df(at, ctx->stream));
     else KL(KT_ASM3C, launch_assemble_3c(at, ctx->stream));
     if (nm > 0) {
       KL(KT_MLP_EVAL, mlp_launch(ctx, mlp_eval_args(ctx), a, false));
@@ -1625,7 +1630,7 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = fal
     CHK(ctx->d_dS.ensure(db));
     CHK(ctx->d_dT.ensure(db));
   }
-  if ((what & FB_VNA3C) && (use_df(ctx) || mlp_routes(ctx)))
+  if ((what & FB_VNA3C) && (use_df(ctx) || use_df_dogs(ctx) || mlp_routes(ctx)))
     CHK(ctx->d_rho_df.ensure((size_t)ctx->nblock * sizeof(float2) + 16));
   if (what & FB_VNA3C) CHK(prepare_mlp(ctx, true));
   if (dogs && (what & (FB_VNA3C | FB_EWALD))) CHK(ctx->d_dogs_ps.ensure((size_t)8 * P * sizeof(double) + 8));
@@ -1697,8 +1702,9 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     AsmArgs at = a;
     at.tperm = a.tperm + nm;
     at.ntrip = a.ntrip - nm;
-    if (use_df(ctx) || nm > 0) KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
+    if (use_df(ctx) || use_df_dogs(ctx) || nm > 0) KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
     if (use_df(ctx)) KL(KT_DASM3C, launch_dassemble_3c_df(at, ctx->stream));
+    else if (use_df_dogs(ctx)) KL(KT_DASM3C, launch_dassemble_3c_dogs_df(at, ctx->stream));
     else KL(KT_DASM3C, launch_dassemble_3c(at, ctx->stream));
     if (nm > 0) {
       KL(KT_MLP_EVAL, mlp_launch(ctx, mlp_eval_args(ctx), a, true));

@@ -112,6 +112,9 @@ int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s);
 // double-float three-center kernels (s and sp bases) and the rho split
 int launch_assemble_3c_df(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s);
+// DOGS three-center value and force kernels in double-float (s and sp bases)
+int launch_assemble_3c_dogs_df(const AsmArgs &a, cudaStream_t s);
+int launch_dassemble_3c_dogs_df(const AsmArgs &a, cudaStream_t s);
 int launch_split_rho(const AsmArgs &a, long long nblock, cudaStream_t s);
 // three-center kernels fed by MLP-3c results (a.mlpF) instead of the tables:
 // list positions 0 .. a.ntrip-1 of a.tperm

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
 SOURCES = ["fb_api.cu", "fb_fdata.cpp", "fb_neigh.cu", "fb_asm2c.cu", "fb_asm3c.cu", "fb_dasm2c.cu", "fb_dasm3c.cu",
-           "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu", "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu"]
+           "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu", "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu"]
 
 
 def nvcc():
