@@ -578,9 +578,6 @@ info_done:
             ok = ck.off >= 0 && ck.nx == c0.nx && ck.ny == c0.ny && ck.nME == c0.nME && ck.dx == c0.dx && ck.dy == c0.dy;
           }
           long long nn = (long long)c0.nx * c0.ny;
-          for (long long n = 0; n < nn && ok; n++)
-            for (int k = 1; k < nk && ok; k++)
-              ok = out.lin[out.dev.c3rho[is][js][ks][q][k].node_off + n] == out.lin[c0.node_off + n];
           if (!ok) continue;
           dq = c0;
           dq.off = (long long)out.table3c.size();
@@ -593,7 +590,11 @@ info_done:
             out.table3c.push_back(acc);
           }
           for (long long n = 0; n < nn; n++) {
+            // the common gradient switch, or 2 where the sub-cells disagree
+            // (a triplet on such a node takes the sub-cells one by one)
             unsigned char l0 = out.lin[c0.node_off + n];
+            for (int k = 1; k < nk; k++)
+              if (out.lin[out.dev.c3rho[is][js][ks][q][k].node_off + n] != l0) l0 = 2;
             out.lin.push_back(l0);
             for (int d = 0; d < 2; d++) {
               double acc = 0.0;
@@ -662,8 +663,15 @@ info_done:
   for (int is = 0; is < nspecies; is++)
     for (int js = 0; js < nspecies; js++)
       for (int ks = 0; ks < nspecies; ks++)
-        for (int q = 0; q < 2; q++)
-          if (out.dev.c3rhoq[is][js][ks][q].off < 0) out.dev.vxc_qsum_all = 0;
+        for (int q = 0; q < 2; q++) {
+          const Cell3cDev &cq = out.dev.c3rhoq[is][js][ks][q];
+          if (cq.off < 0) {
+            out.dev.vxc_qsum_all = 0;
+            continue;
+          }
+          for (long long n = 0; n < (long long)cq.nx * cq.ny; n++)
+            if (out.lin[cq.node_off + n] == 2) out.dev.vxc_qsum_all = 0;
+        }
   return FB_OK;
 }
 

@@ -215,10 +215,11 @@ struct FdataDev {
   Cell3cDev c3rho[MAXSP][MAXSP][MAXSP][2][MAXSUB];
   // the same tables summed over isorp with the third species' Qneutral
   // weights (interpolation is linear in the table values and in the
-  // linear-branch gradients), where every sub-cell shares the grid and the
-  // gradient switch at every node; off = -1 where they do not
+  // linear-branch gradients) where the sub-cells share the grid (off = -1
+  // where they do not); the gradient switch of a node is 2 where the
+  // sub-cells disagree on it, and a triplet there takes them one by one
   Cell3cDev c3rhoq[MAXSP][MAXSP][MAXSP][2];
-  int vxc_qsum_all;  // every species triple has both summed cells
+  int vxc_qsum_all;  // every triple has both summed cells and no node is 2
   double vxc1c[MAXSP][MAXSUB * MAXSUB];
 };
 

@@ -246,9 +246,22 @@ __global__ void __launch_bounds__(128) k_rho_2c(Ctx2c c, VxcArgs v) {
 // ---------------------------------------------------------------------------
 // rho 3c: one thread per triplet, FP64 atomics into the pair (iatom, mneigh)
 // ---------------------------------------------------------------------------
-// true when the triple's Qneutral-summed density cells exist
-__device__ __forceinline__ bool qsum_triple(const FdataDev &fd, int in1, int in2, int in3) {
-  return fd.c3rhoq[in1][in2][in3][0].off >= 0 && fd.c3rhoq[in1][in2][in3][1].off >= 0;
+// true when the triplet's Qneutral-summed density cells exist and its
+// stencil node (the one interp3c takes the gradient switch from) has one
+// switch for every sub-cell
+__device__ __forceinline__ bool qsum_node_ok(const unsigned char *lin, const Cell3cDev &cell, double x, double y) {
+  if (cell.off < 0) return false;
+  int ix = (int)(x / cell.dx) + 1, iy = (int)(y / cell.dy) + 1;
+  if (ix < 2) ix = 2;
+  if (iy < 2) iy = 2;
+  if (ix > cell.nx - 2) ix = cell.nx - 2;
+  if (iy > cell.ny - 2) iy = cell.ny - 2;
+  return lin[cell.node_off + (long long)(iy - 1) * cell.nx + (ix - 1)] != 2;
+}
+__device__ __forceinline__ bool qsum_fast(const Ctx3c &c, int in1, int in2, int in3, double x, double y) {
+  const FdataDev &fd = *c.fd;
+  return qsum_node_ok(c.lin, fd.c3rhoq[in1][in2][in3][0], x, y) &&
+         qsum_node_ok(c.lin, fd.c3rhoq[in1][in2][in3][1], x, y);
 }
 
 template <int PA, int PB, bool HASD, bool QSUM>
@@ -261,6 +274,7 @@ __device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int
   trip_geom(c, t, ia, iat, jat, g);
   const FdataDev &fd = *c.fd;
   int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+  if (qsum_fast(c, in1, in2, indna, g.x, g.z) != QSUM) return;
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
   double m[NE];
@@ -311,13 +325,12 @@ __device__ __forceinline__ void trip_rho3c(const Ctx3c &c, const VxcArgs &v, int
 }
 
 // triplets in the binned order (tperm) for table locality; QSUM: the
-// triplets whose triple has summed cells, else the others
+// triplets the summed cells serve (qsum_fast), else the others
 template <bool HASD, bool QSUM>
 __global__ void __launch_bounds__(128) k_rho_3c(Ctx3c c, VxcArgs v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
     int t = c.tperm ? c.tperm[i] : i;
     int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
-    if (qsum_triple(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
     int pa = c.fd->sp[in1].pattern, pb = c.fd->sp[in2].pattern;
     int key = pa * 3 + pb;
     switch (key) {
@@ -698,6 +711,7 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
   trip_geom(c, t, ia, iat, jat, g);
   const FdataDev &fd = *c.fd;
   int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+  if (qsum_fast(c, in1, in2, indna, g.x, g.z) != QSUM) return;
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
   int p = c.tdst[t];
@@ -840,7 +854,6 @@ __global__ void __launch_bounds__(128) k_dvxc_3c(Ctx3c c, VxcArgs v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
     int t = c.tperm ? c.tperm[i] : i;
     int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
-    if (qsum_triple(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
     int pa = c.fd->sp[in1].pattern, pb = c.fd->sp[in2].pattern;
     int key = pa * 3 + pb;
     switch (key) {

@@ -11,8 +11,21 @@ namespace fb {
 
 namespace {
 
-__device__ __forceinline__ bool qsum_triple_df(const FdataDev &fd, int in1, int in2, int in3) {
-  return fd.c3rhoq[in1][in2][in3][0].off >= 0 && fd.c3rhoq[in1][in2][in3][1].off >= 0;
+// as qsum_fast of the FP64 kernels: the summed cells exist and the
+// triplet's stencil node has one gradient switch for every sub-cell
+__device__ __forceinline__ bool qsum_node_ok_df(const unsigned char *lin, const Cell3cDev &cell, double x, double y) {
+  if (cell.off < 0) return false;
+  int ix = (int)__ddiv_rn(x, cell.dx) + 1, iy = (int)__ddiv_rn(y, cell.dy) + 1;
+  if (ix < 2) ix = 2;
+  if (iy < 2) iy = 2;
+  if (ix > cell.nx - 2) ix = cell.nx - 2;
+  if (iy > cell.ny - 2) iy = cell.ny - 2;
+  return lin[cell.node_off + (long long)(iy - 1) * cell.nx + (ix - 1)] != 2;
+}
+__device__ __forceinline__ bool qsum_fast_df(const Ctx3c &c, int in1, int in2, int in3, double x, double y) {
+  const FdataDev &fd = *c.fd;
+  return qsum_node_ok_df(c.lin, fd.c3rhoq[in1][in2][in3][0], x, y) &&
+         qsum_node_ok_df(c.lin, fd.c3rhoq[in1][in2][in3][1], x, y);
 }
 
 template <int PA, int PB, bool QSUM>
@@ -24,6 +37,7 @@ __device__ __forceinline__ void trip_rho3c_df(const Ctx3c &c, const VxcArgs &v, 
   trip_geom_df(c, t, g);
   const FdataDev &fd = *c.fd;
   int in1 = c.isp[g.iat], in2 = c.isp[g.jat], indna = c.isp[g.ia];
+  if (qsum_fast_df(c, in1, in2, indna, g.x, g.z) != QSUM) return;
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
   df m[NE];
@@ -87,7 +101,6 @@ __global__ void __launch_bounds__(128) k_rho_3c_df(Ctx3c c, VxcArgs v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
     int t = c.tperm ? c.tperm[i] : i;
     int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
-    if (qsum_triple_df(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
     switch (c.fd->sp[in1].pattern * 3 + c.fd->sp[in2].pattern) {
       case PAT_SP * 3 + PAT_SP: trip_rho3c_df<PAT_SP, PAT_SP, QSUM>(c, v, t); break;
       case PAT_SP * 3 + PAT_S: trip_rho3c_df<PAT_SP, PAT_S, QSUM>(c, v, t); break;
@@ -114,6 +127,7 @@ __device__ void trip_dvxc_df(const Ctx3c &c, const VxcArgs &v, int t) {
   const int ia = h.ia, iat = h.iat, jat = h.jat;
   const FdataDev &fd = *c.fd;
   int in1 = c.isp[iat], in2 = c.isp[jat], indna = c.isp[ia];
+  if (qsum_fast_df(c, in1, in2, indna, h.x, h.z) != QSUM) return;
   int nk = fd.sp[indna].nssh;
   const double *qk = fd.sp[indna].qn;
   int p = c.tdst[t];
@@ -246,7 +260,6 @@ __global__ void __launch_bounds__(128) k_dvxc_3c_df(Ctx3c c, VxcArgs v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c.T; i += gridDim.x * blockDim.x) {
     int t = c.tperm ? c.tperm[i] : i;
     int in1 = c.isp[c.ci_j[t]], in2 = c.isp[c.cj_j[t]];
-    if (qsum_triple_df(*c.fd, in1, in2, c.isp[c.trip_alpha[t]]) != QSUM) continue;
     switch (c.fd->sp[in1].pattern * 3 + c.fd->sp[in2].pattern) {
       case PAT_SP * 3 + PAT_SP: trip_dvxc_df<PAT_SP, PAT_SP, QSUM>(c, v, t); break;
       case PAT_SP * 3 + PAT_S: trip_dvxc_df<PAT_SP, PAT_S, QSUM>(c, v, t); break;
