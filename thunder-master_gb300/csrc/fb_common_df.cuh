@@ -239,7 +239,7 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
   lagrange4_df(px, wx, DERIV ? dwx : nullptr);
   lagrange4_df(py, wy, DERIV ? dwy : nullptr);
   if (DERIV) {
-    df idx = df_from(1.0 / cell.dx), idy = df_from(1.0 / cell.dy);
+    df idx = df_make(cell.idx_h, cell.idx_l), idy = df_make(cell.idy_h, cell.idy_l);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       dwx[k] = dwx[k] * idx;
@@ -254,9 +254,9 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
       for (int k = 0; k < 4; k++) W[4 * j + k] = wx[k] * wy[j];
   }
   const df *Tb = tab + (node0 - nx - 1) * NTHETA * NE;
-  // pass 1: the value contraction I_theta -> F and dF/dcos(theta); with
-  // derivatives the theta loop is kept rolled (code size, registers)
-#pragma unroll(DERIV ? 1 : NTHETA)
+  // pass 1: the value contraction I_theta -> F and dF/dcos(theta); the
+  // theta loop is kept rolled (instruction-cache footprint, registers)
+#pragma unroll 1
   for (int th = 0; th < NTHETA; th++) {
     const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
     dacc I[NE];

@@ -514,6 +514,13 @@ info_done:
           d.ymax = c1.ymax;
           d.dx = c1.xmax / (c1.nx - 1.0);  // M_Fdata_3c.f90:367-368
           d.dy = c1.ymax / (c1.ny - 1.0);
+          {
+            double ix = 1.0 / d.dx, iy = 1.0 / d.dy;
+            d.idx_h = (float)ix;
+            d.idx_l = (float)(ix - (double)d.idx_h);
+            d.idy_h = (float)iy;
+            d.idy_l = (float)(iy - (double)d.idy_h);
+          }
           d.off = (long long)out.table3c.size();
           d.node_off = (long long)out.lin.size();
           for (int iy = 0; iy < c1.ny; iy++)
