@@ -162,6 +162,16 @@ __device__ __forceinline__ df sel3(const df *a, int k) {
   return r;
 }
 
+// element j of a 4-array by selects (keeps the array in registers when j
+// is a loop variable)
+__device__ __forceinline__ df sel4(const df *a, int j) {
+  df r = a[0];
+  r = j == 1 ? a[1] : r;
+  r = j == 2 ? a[2] : r;
+  r = j == 3 ? a[3] : r;
+  return r;
+}
+
 // element th of a 5-array by selects (keeps the array in registers when th
 // is a loop variable)
 __device__ __forceinline__ df sel5(const df *a, int th) {
@@ -260,18 +270,35 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
   for (int th = 0; th < NTHETA; th++) {
     const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
     dacc I[NE];
+    if constexpr (DERIV) {
+      // stencil rows rolled as well (the force kernels' code footprint)
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+      for (int e = 0; e < NE; e++) I[e] = dacc{0.0f, 0.0f};
+#pragma unroll 1
+      for (int j = 0; j < 4; j++) {
+        const df wyj = sel4(wy, j);
+        const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
-        df w = DERIV ? wx[k] * wy[j] : W[4 * j + k];
+        for (int k = 0; k < 4; k++) {
+          df w = wx[k] * wyj;
 #pragma unroll
-        for (int e = 0; e < NE; e++) {
-          if (j == 0 && k == 0) dacc_first(I[e], w, Tn[e]);
-          else dacc_add(I[e], w, Tn[e]);
+          for (int e = 0; e < NE; e++) dacc_add(I[e], w, Tr[k * NTHETA * NE + e]);
         }
       }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
+          df w = W[4 * j + k];
+#pragma unroll
+          for (int e = 0; e < NE; e++) {
+            if (j == 0 && k == 0) dacc_first(I[e], w, Tn[e]);
+            else dacc_add(I[e], w, Tn[e]);
+          }
+        }
+    }
 #pragma unroll
     for (int e = 0; e < NE; e++) {
       df iv = dacc_val(I[e]);
@@ -287,22 +314,22 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
     const df plt = sel5(pl, th);
     dacc Ix[NE], Iy[NE];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int e = 0; e < NE; e++) Ix[e] = Iy[e] = dacc{0.0f, 0.0f};
+#pragma unroll 1
+    for (int j = 0; j < 4; j++) {
+      const df wyj = sel4(wy, j), dwyj = sel4(dwy, j);
+      const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
-        df wxd = dwx[k] * wy[j], wyd = wx[k] * dwy[j];
+        df wxd = dwx[k] * wyj, wyd = wx[k] * dwyj;
 #pragma unroll
         for (int e = 0; e < NE; e++) {
-          if (j == 0 && k == 0) {
-            dacc_first(Ix[e], wxd, Tn[e]);
-            dacc_first(Iy[e], wyd, Tn[e]);
-          } else {
-            dacc_add(Ix[e], wxd, Tn[e]);
-            dacc_add(Iy[e], wyd, Tn[e]);
-          }
+          df tv = Tr[k * NTHETA * NE + e];
+          dacc_add(Ix[e], wxd, tv);
+          dacc_add(Iy[e], wyd, tv);
         }
       }
+    }
 #pragma unroll
     for (int e = 0; e < NE; e++) {
       DxF[e] = DxF[e] + plt * dacc_val(Ix[e]);
