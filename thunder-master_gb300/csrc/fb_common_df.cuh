@@ -256,13 +256,6 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
       dwy[k] = dwy[k] * idy;
     }
   }
-  df W[16];
-  if (!DERIV) {
-#pragma unroll
-    for (int j = 0; j < 4; j++)
-#pragma unroll
-      for (int k = 0; k < 4; k++) W[4 * j + k] = wx[k] * wy[j];
-  }
   const df *Tb = tab + (node0 - nx - 1) * NTHETA * NE;
   // pass 1: the value contraction I_theta -> F and dF/dcos(theta); the
   // theta loop is kept rolled (instruction-cache footprint, registers)
@@ -270,34 +263,19 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
   for (int th = 0; th < NTHETA; th++) {
     const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
     dacc I[NE];
-    if constexpr (DERIV) {
-      // stencil rows rolled as well (the force kernels' code footprint)
+    // stencil rows rolled (instruction-cache footprint)
 #pragma unroll
-      for (int e = 0; e < NE; e++) I[e] = dacc{0.0f, 0.0f};
+    for (int e = 0; e < NE; e++) I[e] = dacc{0.0f, 0.0f};
 #pragma unroll 1
-      for (int j = 0; j < 4; j++) {
-        const df wyj = sel4(wy, j);
-        const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
+    for (int j = 0; j < 4; j++) {
+      const df wyj = sel4(wy, j);
+      const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-          df w = wx[k] * wyj;
+      for (int k = 0; k < 4; k++) {
+        df w = wx[k] * wyj;
 #pragma unroll
-          for (int e = 0; e < NE; e++) dacc_add(I[e], w, Tr[k * NTHETA * NE + e]);
-        }
+        for (int e = 0; e < NE; e++) dacc_add(I[e], w, Tr[k * NTHETA * NE + e]);
       }
-    } else {
-#pragma unroll
-      for (int j = 0; j < 4; j++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-          const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE + th * NE;
-          df w = W[4 * j + k];
-#pragma unroll
-          for (int e = 0; e < NE; e++) {
-            if (j == 0 && k == 0) dacc_first(I[e], w, Tn[e]);
-            else dacc_add(I[e], w, Tn[e]);
-          }
-        }
     }
 #pragma unroll
     for (int e = 0; e < NE; e++) {
