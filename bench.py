@@ -218,10 +218,12 @@ def tuned_shapes(ctx, fbgpu, autotune):
 
 
 # Executed FP32 work of the double-float three-center kernels per sp3 x sp3
-# triplet (2 FFMA + FADD + FMUL thread instructions), and the DRAM bytes per
-# triplet of one launch, from ncu on SiC4096 (profiles/): the df
-# formulation's arithmetic is what the FP32 pipe must execute.
-DF_FP32_FLOP = {"dassemble_3c": 55932.0, "assemble_3c": 15224.0}
+# triplet (2 FFMA + FADD + FMUL thread instructions, ncu on Si512: the count
+# per triplet does not depend on the system size), and the DRAM bytes per
+# triplet of one launch (ncu on SiC4096, where the launch's working set
+# exceeds what L2 keeps between launches) (profiles/): the df formulation's
+# arithmetic is what the FP32 pipe must execute.
+DF_FP32_FLOP = {"dassemble_3c": 59053.0, "assemble_3c": 16284.0}
 DF_DRAM_BYTES = {"dassemble_3c": 93.4, "assemble_3c": 89.7}
 
 
@@ -260,7 +262,7 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
                 "peak_source": "of measured: fb_probe_fp32 FFMA chains in this run",
                 "flops_per_launch": fl32,
                 "flops_source": "executed FP32 FLOPs of the double-float kernel (2 FFMA + FADD + FMUL per "
-                                "triplet, ncu on SiC4096)",
+                                "triplet, ncu on Si512)",
                 "avg_launch_ms": round(dom_ms, 4),
                 "fp64_equivalent": {"algorithmic_flops_per_launch": fl64, "achieved": round(ach64, 4),
                                     "fp64_peak": round(fp64_peak, 4), "unit": "TFLOP/s",
