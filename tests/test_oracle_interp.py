@@ -206,6 +206,62 @@ def test_rotate_is_L_M_Rt(si_fdata):
         assert np.allclose(X, L @ M @ L.T, atol=1e-13)
 
 
+def test_rotation_reproduces_slater_koster_table(si_fdata):
+    """Known answer: the rotation of the molecular-frame sigma / pi elements
+    into the crystal frame, in the frame the 2c assemblers build
+    (epsilon(r2, sighat), M_assemble_2c_Harris.f90:177), gives the s, p
+    entries of the Slater-Koster table (Phys. Rev. 94, 1498 (1954), Table I)
+    for the bond direction cosines (l, m, n).  Orbital order s, py, pz, px."""
+    fd = orc.Fdata(si_fdata, [14])
+    rng = np.random.default_rng(21)
+    for _ in range(20):
+        r1, r2 = rng.normal(size=3) * 2.0, rng.normal(size=3) * 2.0
+        d = r2 - r1
+        l, m, n = d / np.linalg.norm(d)
+        e = orc.epsilon(r2, d / np.linalg.norm(d))
+        ss, sp, ps, pps, ppp = rng.normal(size=5)
+        M = np.zeros((4, 4))
+        M[0, 0], M[0, 2], M[2, 0] = ss, sp, ps
+        M[1, 1], M[2, 2], M[3, 3] = ppp, pps, ppp
+        X = orc.rotate(fd, 1, 1, e, M)
+        c = {1: m, 2: n, 3: l}   # the direction cosine of each p orbital
+        want = np.zeros((4, 4))
+        want[0, 0] = ss
+        for a in (1, 2, 3):
+            want[0, a] = c[a] * sp
+            want[a, 0] = c[a] * ps
+            for b in (1, 2, 3):
+                want[a, b] = c[a] * c[b] * (pps - ppp) + (ppp if a == b else 0.0)
+        assert np.abs(X - want).max() < 1e-13
+
+
+def test_d_rotation_reproduces_slater_koster_sigma_entries(tmp_path):
+    """The same known answer for d orbitals (order xy, yz, 3z^2 - r^2, xz,
+    x^2 - y^2): a molecular-frame s-d sigma element gives the Table I
+    entries sqrt(3) lm, sqrt(3) mn, n^2 - (l^2 + m^2)/2, sqrt(3) ln,
+    sqrt(3)/2 (l^2 - m^2) times V_sd sigma, and a p-d sigma element the same
+    factors times the direction cosine of the p orbital."""
+    path = str(tmp_path / "fdata_ti")
+    synth.write_fdata(path, [synth.ti()])
+    fd = orc.Fdata(path, [22])
+    rng = np.random.default_rng(22)
+    s3 = np.sqrt(3.0)
+    for _ in range(10):
+        r1, r2 = rng.normal(size=3) * 2.0, rng.normal(size=3) * 2.0
+        d = r2 - r1
+        l, m, n = d / np.linalg.norm(d)
+        e = orc.epsilon(r2, d / np.linalg.norm(d))
+        sd, pd = rng.normal(size=2)
+        M = np.zeros((9, 9))
+        M[0, 6] = sd          # <s | d_z2>
+        M[2, 6] = pd          # <p_z | d_z2>
+        X = orc.rotate(fd, 1, 1, e, M)
+        f = np.array([s3 * l * m, s3 * m * n, n * n - 0.5 * (l * l + m * m), s3 * l * n, 0.5 * s3 * (l * l - m * m)])
+        assert np.abs(X[0, 4:9] - sd * f).max() < 1e-13
+        for a, ca in ((1, m), (2, n), (3, l)):
+            assert np.abs(X[a, 4:9] - pd * ca * f).max() < 1e-13
+
+
 def test_x_beyond_table_is_an_error(si_fdata):
     fd = orc.Fdata(si_fdata, [14])
     with pytest.raises(orc.OracleError) as ei:
