@@ -113,6 +113,60 @@ def test_vxc_forces_match_oracle(ctx, fdata_root, name, prec):
         ctx.set_precision(1)
 
 
+def test_vxc_batch_matches_oracle(ctx, fdata_root):
+    """A batch of three structures (one a cluster, one with a vacancy) in
+    one FB_VXC assembly: each structure's densities and vxc blocks as the
+    oracle gives them for that structure alone."""
+    path = synth.fdata_dir_for("batch256", root=fdata_root, vxc=True)
+    nZ = [14, 6]
+    structs = [synth.diamond((1, 1, 2), 4.36, 0.1, 31, sp_a=1, sp_b=2, name="SiC16"),
+               synth.diamond((2, 2, 1), 5.43, 0.1, 32, vacancy=0.05, name="Si32v"),
+               synth.diamond((1, 1, 1), 4.36, 0.1, 33, sp_a=1, sp_b=2, name="SiC8cluster")]
+    structs[2].icluster = 1
+    fd = orc.Fdata(path, nZ)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_batch([(st.ratom, st.imass, st.lattice, st.icluster) for st in structs])
+    ctx.driver_neighbors()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    ctx.assemble(fbgpu.FB_ALL | fbgpu.FB_VXC)
+    got = {w: ctx.blocks(w) for w in ("rho_in", "rho_bond", "vxc")}
+    off = ctx.batch_offsets()["block"]
+    for k, st in enumerate(structs):
+        s = orc.System(fd, st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
+        ref = s.assemble_vxc()
+        for w in ("rho_in", "rho_bond", "vxc"):
+            assert np.abs(got[w][off[k]:off[k + 1]] - ref[w]).max() <= TOL, (k, w)
+
+
+def test_all_terms_in_one_graph(ctx, fdata_root):
+    """Harris S, T, vna, the vnl terms and McWEDA vxc, value and force
+    pass as one graph: ftot is the sum of the oracle's three contributions."""
+    from conftest import symmetric_denmat
+    path, nZ, st = case(fdata_root, "sic_small")
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice).neighbors()
+    rho, cape = symmetric_denmat(s, np.array([fd.norb(int(q)) for q in st.imass]), 6)
+    harris = s.dassemble(rho, cape)
+    vxc = s.dassemble_vxc(rho)
+    s.neighbors_pp()
+    from test_oracle_pp import _sym_rho
+    rho_pp = _sym_rho(s, fd, st, 12)
+    vnl = s.dassemble_pp(rho_pp)
+    want = harris["ftot"] + vxc["ftot_add"] + vnl["ftot_vnl"]
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    ctx.driver_neighbors_PP()
+    ctx.set_theory(fbgpu.FB_THEORY_HARRIS)
+    ctx.set_denmat(rho, cape)
+    ctx.set_denmat_pp(rho_pp)
+    what = fbgpu.FB_ALL | fbgpu.FB_VXC | fbgpu.FB_VNL | fbgpu.FB_FORCES
+    for _ in range(2):
+        ctx.assemble_graph(what)
+        assert np.abs(ctx.forces("ftot") - want).max() <= TOL
+        assert np.abs(ctx.blocks("vxc") - vxc["values"]["vxc"]).max() <= TOL
+
+
 def test_vxc_errors(ctx, fdata_root):
     path, nZ, st = case(fdata_root, "sic_small")
     ctx.read_Fdata(path, nZ)
