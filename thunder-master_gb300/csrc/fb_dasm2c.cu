@@ -68,6 +68,10 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
   if (what & 4u) {
     double f[3] = {0.0, 0.0, 0.0};
     if (!self) {
+      // ontop left + right are summed before one contraction (linear)
+      double m[NE], dm[NE];
+#pragma unroll
+      for (int e = 0; e < NE; e++) m[e] = dm[e] = 0.0;
 #pragma unroll
       for (int w2 = 2; w2 <= 3; w2++) {
         interp2c_d<NE>(b.table2c, fd.c2[in1][in2][w2], z, tiny, v, dv, b.status);
@@ -85,11 +89,13 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
             }
           }
         }
-        vec2c<NE>(z, eta, dv, vd);
-        contract<PA, PB, K2C, HASD>(R, D, rb, v, vd, out);
 #pragma unroll
-        for (int q = 0; q < 3; q++) f[q] -= out[q] * P_eq2;
+        for (int e = 0; e < NE; e++) m[e] += v[e], dm[e] += dv[e];
       }
+      vec2c<NE>(z, eta, dm, vd);
+      contract<PA, PB, K2C, HASD>(R, D, rb, m, vd, out);
+#pragma unroll
+      for (int q = 0; q < 3; q++) f[q] -= out[q] * P_eq2;
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) c.ontop[3 * p + q] = f[q];
