@@ -141,7 +141,10 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % device)
+        # the raw samples go to FBGPU_CLOCKS_DIR (default: the system temp dir)
+        import tempfile
+        out = os.environ.get("FBGPU_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, "clocks_rank%d.csv" % device)
 
     def start(self):
         try:
@@ -190,7 +193,7 @@ def dist_env():
 
 
 # ---------------------------------------------------------------------------
-# algorithmic work per unit (see DESIGN.md "Measurement")
+# algorithmic work per unit
 # ---------------------------------------------------------------------------
 def flops_dassemble_3c(nme):
     # value + x + y derivative table contractions (5 theta x 16 nodes x nME FMA
