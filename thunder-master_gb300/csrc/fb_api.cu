@@ -72,7 +72,7 @@ struct fb_ctx {
   DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
-  DevBuf d_slot_off, d_slot_nn, d_slot_found;
+  DevBuf d_slot_off, d_slot_nn, d_slot_found, d_rcnt;
   DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
   DevBuf d_status, d_errinfo;
   // blocks
@@ -274,7 +274,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
                     &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm,
-                    &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
+                    &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_rcnt, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
@@ -517,6 +517,7 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.pair_owner = ctx->d_pair_owner.as<int>();
   a.r3v = ctx->d_r3v.as<double>();
   a.tcnt = ctx->d_tcnt.as<int>();
+  a.rcnt = ctx->d_rcnt.as<int>();
   a.trip_off = ctx->d_trip_off.as<int>();
   a.ci_j = ctx->d_ci_j.as<int>();
   a.ci_b = ctx->d_ci_b.as<int>();
@@ -578,7 +579,8 @@ static int finish_neighbors(fb_ctx *ctx) {
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
   NeighArgs a = neigh_args(ctx);
   KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
-  // common neighbors: slots for every ordered pair of ialpha's non-self neighbors
+  // common neighbors: slots for every ordered pair of ialpha's non-self
+  // neighbors, one row of n - 1 per non-self neighbor (n of them)
   std::vector<long long> soff(N + 1, 0);
   for (int i = 0; i < N; i++) {
     long long n = ctx->h_pair_off[i + 1] - ctx->h_pair_off[i] - 1;  // non-self neighbors
@@ -586,6 +588,7 @@ static int finish_neighbors(fb_ctx *ctx) {
     soff[i + 1] = soff[i] + (n > 1 ? n * (n - 1) : 0);
   }
   CHK(ctx->d_tcnt.ensure(N * sizeof(int)));
+  CHK(ctx->d_rcnt.ensure((size_t)P * sizeof(int) + 4));
   CHK(ctx->d_slot_off.ensure((N + 1) * sizeof(long long)));
   CHK(ctx->d_slot_nn.ensure((size_t)soff[N] * sizeof(unsigned) + 4));
   CHK(ctx->d_slot_found.ensure((size_t)soff[N] * sizeof(int) + 4));

@@ -46,6 +46,7 @@ struct NeighArgs {
   const int *pair_owner;
   double *r3v;
   int *tcnt;
+  int *rcnt;  // kept (ineigh, jneigh) pairs of each pair row (ialpha, ineigh)
   const int *trip_off;
   int *ci_j, *ci_b, *cj_j, *cj_b, *cneigh, *tdst;
   // common-neighbor slots: ialpha's kept (ineigh, jneigh) pairs and matches

@@ -146,132 +146,169 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
          fabs(__dadd_rn(__dsub_rn(r3[2], r2[2]), r1[2])) < 1.0e-4;
 }
 
-// find_common_max / find_common_neighbors: one warp per ialpha; for each
-// non-self ineigh (warp-uniform), lanes sweep jneigh; a candidate (i, j)
+// find_common_max / find_common_neighbors: one warp per pair row
+// (ialpha, ineigh), ineigh non-self; lanes sweep jneigh; a candidate (i, j)
 // with |r1 - r2| < rc_i + rc_j - 0.01 is kept only if j is found in i's
 // list by the reference's vector match (first kneigh with
 // |r3 - r2 + r1| < 1e-4 per component).  The entry that can match is
 // (jatom, shift(jbeta) - shift(ibeta)); i's list is sorted by (mbeta, jatom),
 // so it is found by binary search and then tested exactly.  When that entry
 // is absent or fails the test, the full scan of the reference decides.
-// Output order matches the reference loops.  One pass: every kept pair
-// (ineigh, jneigh) and its match go to ialpha's slots (slot_off[ialpha],
-// room for all ordered pairs of its non-self neighbors) and the count to
-// tcnt; k_common_compact then packs the slots into the CSR triplet lists.
-__global__ void k_common(int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
+// Each row writes its kept pairs (ineigh, jneigh) and matches, in jneigh
+// order, to its own run of slots: ialpha's slots start at slot_off[ialpha]
+// and hold n_ns rows of n_ns - 1 (n_ns non-self neighbors), row k for the
+// k-th non-self ineigh.  rcnt gets the row's count and tcnt[ialpha] (zeroed
+// by the caller) the sum over the rows; k_common_compact packs the rows in
+// ineigh order, so the triplets come out in the reference's loop order.
+__global__ void k_common(int P, int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
                          const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
-                         const double *__restrict__ xl0,
+                         const double *__restrict__ xl0, const int *__restrict__ pair_owner,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                          const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
-                         const double *__restrict__ r3v, int *__restrict__ tcnt,
+                         const double *__restrict__ r3v, int *__restrict__ tcnt, int *__restrict__ rcnt,
                          const long long *__restrict__ slot_off, unsigned *__restrict__ slot_nn,
                          int *__restrict__ slot_found) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
-  if (warp >= N) return;
-  int ia = warp;
+  if (pi >= P) return;
+  int ia = pair_owner[pi];
+  int p0 = pair_off[ia], n = pair_off[ia + 1] - p0, self = neigh_self[ia];
+  int in = pi - p0;
+  if (self < 0 || in == self) {
+    if (lane == 0) rcnt[pi] = 0;
+    return;
+  }
   const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
   int periodic = speriodic[sid[ia]];
-  int p0 = pair_off[ia], n = pair_off[ia + 1] - p0, self = neigh_self[ia];
+  int kidx = in - (in > self ? 1 : 0);
+  long long base = slot_off[ia] + (long long)kidx * (n - 2);
   int num = 0;
-  long long base = slot_off[ia];
-  for (int in = 0; in < n; in++) {
-    if (in == self) continue;
-    int pi = p0 + in, iat = neigh_j[pi], ib = neigh_b[pi];
-    double r1[3];
+  int iat = neigh_j[pi], ib = neigh_b[pi];
+  double r1[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
-    double rci = fd->sp[isp[iat]].rcA;
-    int q0 = pair_off[iat], qn = pair_off[iat + 1];
-    int ibx, iby, ibz;
-    mbeta_shift(ib, ibx, iby, ibz);
-    for (int j0 = 0; j0 < n; j0 += 32) {
-      int jn = j0 + lane;
-      bool keep = false;
-      int found = -1;
-      int jat = 0, jb = 0;
-      if (jn < n && jn != self && jn != in) {
-        int pj = p0 + jn;
-        jat = neigh_j[pj];
-        jb = neigh_b[pj];
-        double r2[3];
+  for (int k = 0; k < 3; k++) r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
+  double rci = fd->sp[isp[iat]].rcA;
+  int q0 = pair_off[iat], qn = pair_off[iat + 1];
+  int ibx, iby, ibz;
+  mbeta_shift(ib, ibx, iby, ibz);
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    int jn = j0 + lane;
+    bool keep = false;
+    int found = -1;
+    int jat = 0, jb = 0;
+    if (jn < n && jn != self && jn != in) {
+      int pj = p0 + jn;
+      jat = neigh_j[pj];
+      jb = neigh_b[pj];
+      double r2[3];
 #pragma unroll
-        for (int k = 0; k < 3; k++) r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
-        double z = dist_rn(r1, r2);
-        double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
-        if (z < range) {
-          int tmb = 0;
-          bool inbox = true;
-          if (periodic) {
-            int jbx, jby, jbz;
-            mbeta_shift(jb, jbx, jby, jbz);
-            int tx = jbx - ibx, ty = jby - iby, tz = jbz - ibz;
-            inbox = tx >= -4 && tx <= 4 && ty >= -4 && ty <= 4 && tz >= -4 && tz <= 4;
-            if (inbox) tmb = shift_mbeta(tx, ty, tz);
-          }
-          if (inbox) {
-            long long key = (long long)tmb * N + jat;
-            int lo = q0, hi = qn - 1;
-            while (lo <= hi) {
-              int mid = (lo + hi) >> 1;
-              long long km = (long long)neigh_b[mid] * N + neigh_j[mid];
-              if (km < key) lo = mid + 1;
-              else if (km > key) hi = mid - 1;
-              else {
-                if (common_match(r3v + 3 * mid, r1, r2)) found = mid - q0;
-                break;
-              }
+      for (int k = 0; k < 3; k++) r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
+      double z = dist_rn(r1, r2);
+      double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
+      if (z < range) {
+        int tmb = 0;
+        bool inbox = true;
+        if (periodic) {
+          int jbx, jby, jbz;
+          mbeta_shift(jb, jbx, jby, jbz);
+          int tx = jbx - ibx, ty = jby - iby, tz = jbz - ibz;
+          inbox = tx >= -4 && tx <= 4 && ty >= -4 && ty <= 4 && tz >= -4 && tz <= 4;
+          if (inbox) tmb = shift_mbeta(tx, ty, tz);
+        }
+        if (inbox) {
+          long long key = (long long)tmb * N + jat;
+          int lo = q0, hi = qn - 1;
+          while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            long long km = (long long)neigh_b[mid] * N + neigh_j[mid];
+            if (km < key) lo = mid + 1;
+            else if (km > key) hi = mid - 1;
+            else {
+              if (common_match(r3v + 3 * mid, r1, r2)) found = mid - q0;
+              break;
             }
           }
-          if (found < 0) {
-            // rare: candidate at the cutoff edge; decide by the reference scan
-            for (int q = q0; q < qn; q++)
-              if (common_match(r3v + 3 * q, r1, r2)) {
-                found = q - q0;
-                break;
-              }
-          }
-          keep = found >= 0;
         }
+        if (found < 0) {
+          // rare: candidate at the cutoff edge; decide by the reference scan
+          for (int q = q0; q < qn; q++)
+            if (common_match(r3v + 3 * q, r1, r2)) {
+              found = q - q0;
+              break;
+            }
+        }
+        keep = found >= 0;
       }
-      unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) {
-        long long t = base + num + __popc(m & ((1u << lane) - 1u));
-        slot_nn[t] = (unsigned)in | ((unsigned)jn << 16);
-        slot_found[t] = found;
-      }
-      num += __popc(m);
     }
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      long long t = base + num + __popc(m & ((1u << lane) - 1u));
+      slot_nn[t] = (unsigned)in | ((unsigned)jn << 16);
+      slot_found[t] = found;
+    }
+    num += __popc(m);
   }
-  if (lane == 0) tcnt[ia] = num;
+  if (lane == 0) {
+    rcnt[pi] = num;
+    if (num) atomicAdd(tcnt + ia, num);
+  }
 }
 
-// slots -> CSR triplet lists in the reference's field layout (one warp per ialpha)
+// slots -> CSR triplet lists in the reference's field layout (one warp per
+// ialpha): 32 rows at a time, an inclusive scan of their counts places each
+// row's run; each lane finds the row of its output entry by binary search
+// over the scan.
 __global__ void k_common_compact(int N, const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
-                                 const int *__restrict__ neigh_b, const int *__restrict__ tcnt,
-                                 const long long *__restrict__ slot_off, const unsigned *__restrict__ slot_nn,
-                                 const int *__restrict__ slot_found, const int *__restrict__ trip_off,
-                                 int *__restrict__ ci_j, int *__restrict__ ci_b, int *__restrict__ cj_j,
-                                 int *__restrict__ cj_b, int *__restrict__ cneigh, int *__restrict__ tdst,
-                                 int *__restrict__ talpha) {
+                                 const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
+                                 const int *__restrict__ rcnt, const long long *__restrict__ slot_off,
+                                 const unsigned *__restrict__ slot_nn, const int *__restrict__ slot_found,
+                                 const int *__restrict__ trip_off, int *__restrict__ ci_j, int *__restrict__ ci_b,
+                                 int *__restrict__ cj_j, int *__restrict__ cj_b, int *__restrict__ cneigh,
+                                 int *__restrict__ tdst, int *__restrict__ talpha) {
   int ia = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (ia >= N) return;
-  int p0 = pair_off[ia], cnt = tcnt[ia], t0 = trip_off[ia];
+  int p0 = pair_off[ia], n = pair_off[ia + 1] - p0, self = neigh_self[ia];
+  if (self < 0) return;
+  int t = trip_off[ia];
   long long s0 = slot_off[ia];
-  for (int k = lane; k < cnt; k += 32) {
-    unsigned nn = slot_nn[s0 + k];
-    int found = slot_found[s0 + k];
-    int pi = p0 + (int)(nn & 0xffffu), pj = p0 + (int)(nn >> 16);
-    int iat = neigh_j[pi];
-    int t = t0 + k;
-    ci_j[t] = iat;
-    ci_b[t] = neigh_b[pi];
-    cj_j[t] = neigh_j[pj];
-    cj_b[t] = neigh_b[pj];
-    cneigh[t] = found;
-    tdst[t] = pair_off[iat] + found;
-    talpha[t] = ia;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    int c = r0 + lane < n ? rcnt[p0 + r0 + lane] : 0;
+    int x = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    int ex = x - c;
+    int total = __shfl_sync(0xffffffffu, x, 31);
+    for (int e0 = 0; e0 < total; e0 += 32) {
+      int e = e0 + lane;
+      int k = 0;  // first row of the chunk whose inclusive count exceeds e
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        int v = __shfl_sync(0xffffffffu, x, k + step - 1);
+        if (v <= e) k += step;
+      }
+      int rex = __shfl_sync(0xffffffffu, ex, k);
+      if (e < total) {
+        int in = r0 + k;
+        long long s = s0 + (long long)(in - (in > self ? 1 : 0)) * (n - 2) + (e - rex);
+        unsigned nn = slot_nn[s];
+        int found = slot_found[s];
+        int pi = p0 + (int)(nn & 0xffffu), pj = p0 + (int)(nn >> 16);
+        int iat = neigh_j[pi];
+        int o = t + e;
+        ci_j[o] = iat;
+        ci_b[o] = neigh_b[pi];
+        cj_j[o] = neigh_j[pj];
+        cj_b[o] = neigh_b[pj];
+        cneigh[o] = found;
+        tdst[o] = pair_off[iat] + found;
+        talpha[o] = ia;
+      }
+    }
+    t += total;
   }
 }
 
@@ -394,18 +431,23 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
 }
 
 int launch_common(const NeighArgs &a, cudaStream_t s) {
-  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
-  k_common<<<blocks, threads, 0, s>>>(a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl, a.pair_off, a.neigh_j,
-                                      a.neigh_b, a.neigh_self, a.r3v, a.tcnt, a.slot_off, a.slot_nn, a.slot_found);
+  cudaError_t e = cudaMemsetAsync(a.tcnt, 0, (size_t)a.N * sizeof(int), s);
+  if (e != cudaSuccess) return (int)e;
+  if (a.P == 0) return 0;
+  int threads = 256;
+  long long blocks = ((long long)a.P * 32 + threads - 1) / threads;
+  k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl,
+                                                a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.r3v,
+                                                a.tcnt, a.rcnt, a.slot_off, a.slot_nn, a.slot_found);
   FB_LAUNCH_CHECK();
   return 0;
 }
 
 int launch_common_compact(const NeighArgs &a, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
-  k_common_compact<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_b, a.tcnt, a.slot_off, a.slot_nn,
-                                              a.slot_found, a.trip_off, a.ci_j, a.ci_b, a.cj_j, a.cj_b, a.cneigh,
-                                              a.tdst, a.talpha);
+  k_common_compact<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.rcnt,
+                                              a.slot_off, a.slot_nn, a.slot_found, a.trip_off, a.ci_j, a.ci_b,
+                                              a.cj_j, a.cj_b, a.cneigh, a.tdst, a.talpha);
   FB_LAUNCH_CHECK();
   return 0;
 }
