@@ -6,102 +6,178 @@ namespace fb {
 // ===========================================================================
 // neighbor maps (c.SYSTEM/M_neighbors.f90:356-519, :681-812)
 // ===========================================================================
-// One warp per atom i; lanes sweep jatom inside each periodic image, images
-// in increasing mbeta, so hits come out in the reference order (mbeta
-// outer, jatom inner).  In a batch, j runs over the atoms of i's own
-// structure and the images are that structure's.  A float prefilter with a
-// 1e-2 A margin discards far pairs; every candidate is decided by the
-// uncontracted FP64 test of the reference:
-// z = distance(r1, r2) < rc_i + rc_j - 0.01.
-template <bool FILL>
-__global__ void k_neigh(int N, const double *__restrict__ ratom, const float4 *__restrict__ pos4,
-                        const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
-                        const int *__restrict__ satom_off, const int *__restrict__ simg_off,
-                        const float4 *__restrict__ sbbox, float rcmax, const double *__restrict__ xl,
-                        const float *__restrict__ xlf, const int *__restrict__ imgs, int *__restrict__ cnt,
-                        long long *__restrict__ bsum, const int *__restrict__ pair_off,
-                        const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
-                        int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
-                        unsigned *__restrict__ status, int *__restrict__ errinfo) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= N) return;
-  int i = warp;
-  int s = sid[i];
-  int a0 = satom_off[s], a1 = satom_off[s + 1];
-  const double *X = xl + (long long)s * XL_STRIDE;
-  const float *Xf = xlf + (long long)s * XL_STRIDE;
-  float4 bbox_lo = sbbox[2 * s], bbox_hi = sbbox[2 * s + 1];
-  double ri[3] = {ratom[3 * i], ratom[3 * i + 1], ratom[3 * i + 2]};
-  float4 pi = pos4[i];  // (x, y, z, float cutoff of species)
-  double rci = fd->sp[isp[i]].rcA;
-  // float reach of atom i: its cutoff + the largest cutoff + margin
-  float reach = pi.w + rcmax + 1.0e-2f;
-  int num = 0, base = FILL ? pair_off[i] : 0;
-  long long norbsum = 0;  // sum of norb_j over the hits so far
-  long long bbase = FILL ? blk_base[i] : 0;
-  int ni = fd->sp[isp[i]].norb;
-  for (int ii = simg_off[s]; ii < simg_off[s + 1]; ii++) {
-    int mb = imgs[ii];
-    float L0 = Xf[3 * mb], L1 = Xf[3 * mb + 1], L2 = Xf[3 * mb + 2];
-    // skip an image whose shifted bounding box lies beyond reach (warp-uniform)
-    float ox = fmaxf(fmaxf(bbox_lo.x + L0 - pi.x, pi.x - (bbox_hi.x + L0)), 0.0f);
-    float oy = fmaxf(fmaxf(bbox_lo.y + L1 - pi.y, pi.y - (bbox_hi.y + L1)), 0.0f);
-    float oz = fmaxf(fmaxf(bbox_lo.z + L2 - pi.z, pi.z - (bbox_hi.z + L2)), 0.0f);
-    if (ox * ox + oy * oy + oz * oz > reach * reach) continue;
-    double X0 = X[3 * mb], X1 = X[3 * mb + 1], X2 = X[3 * mb + 2];
-    for (int j0 = a0; j0 < a1; j0 += 32) {
-      int j = j0 + lane;
-      bool hit = false;
-      if (j < a1) {
-        float4 pj = pos4[j];
-        float d0 = (pj.x + L0) - pi.x, d1 = (pj.y + L1) - pi.y, d2 = (pj.z + L2) - pi.z;
-        float lim = pi.w + pj.w + 1.0e-2f;
-        if (d0 * d0 + d1 * d1 + d2 * d2 < lim * lim) {
-          // the reference's test, uncontracted FP64
-          double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[j]].rcA), 0.01);
-          double r2[3] = {__dadd_rn(ratom[3 * j], X0), __dadd_rn(ratom[3 * j + 1], X1),
-                          __dadd_rn(ratom[3 * j + 2], X2)};
-          double z = dist_rn(ri, r2);
-          if (!FILL && i != j && z < 0.5) {
-            atomicOr(status, DEVERR_CLOSE);
-            errinfo[0] = i;
-            errinfo[1] = j;
-            errinfo[2] = mb;
-          }
-          hit = z < range;
+// One CTA per atom i.  Its warps take the periodic images in turn; in an
+// image, lanes sweep jatom.  A first sweep counts each image's hits (and
+// their norb sum) into shared memory, warp 0 scans the counts in increasing
+// mbeta, and the fill pass sweeps again, writing each image's hits from its
+// scanned offset: the list comes out in the reference order (mbeta outer,
+// jatom inner).  In a batch, j runs over the atoms of i's own structure and
+// the images are that structure's.  A float prefilter with a 1e-2 A margin
+// discards far pairs; every candidate is decided by the uncontracted FP64
+// test of the reference: z = distance(r1, r2) < rc_i + rc_j - 0.01.
+constexpr int NEIGH_THREADS = 256;
+
+struct NeighAtom {
+  int i, a0, a1, ni;
+  double ri[3], rci;
+  float4 pi;    // (x, y, z, float cutoff of species)
+  float reach;  // float reach of atom i: its cutoff + the largest cutoff + margin
+  float4 lo, hi;
+  const double *X;
+  const float *Xf;
+};
+
+// one image mb swept by one warp: returns the hit count (warp-uniform) and
+// adds their norb sum to orb.  CHECK flags atoms closer than 0.5 A; WRITE
+// stores the hits from slot off of i's list, block offsets from orb.
+template <bool CHECK, bool WRITE>
+__device__ __forceinline__ int neigh_sweep(const NeighAtom &A, int mb, int lane, int off, long long &orb,
+                                           const double *__restrict__ ratom, const float4 *__restrict__ pos4,
+                                           const int *__restrict__ isp, const FdataDev *__restrict__ fd, int base,
+                                           long long bbase, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
+                                           int *__restrict__ neigh_self, int *__restrict__ pair_owner,
+                                           long long *__restrict__ blk_off, unsigned *__restrict__ status,
+                                           int *__restrict__ errinfo) {
+  float L0 = A.Xf[3 * mb], L1 = A.Xf[3 * mb + 1], L2 = A.Xf[3 * mb + 2];
+  // skip an image whose shifted bounding box lies beyond reach (warp-uniform)
+  float ox = fmaxf(fmaxf(A.lo.x + L0 - A.pi.x, A.pi.x - (A.hi.x + L0)), 0.0f);
+  float oy = fmaxf(fmaxf(A.lo.y + L1 - A.pi.y, A.pi.y - (A.hi.y + L1)), 0.0f);
+  float oz = fmaxf(fmaxf(A.lo.z + L2 - A.pi.z, A.pi.z - (A.hi.z + L2)), 0.0f);
+  if (ox * ox + oy * oy + oz * oz > A.reach * A.reach) return 0;
+  double X0 = A.X[3 * mb], X1 = A.X[3 * mb + 1], X2 = A.X[3 * mb + 2];
+  int num = 0;
+  for (int j0 = A.a0; j0 < A.a1; j0 += 32) {
+    int j = j0 + lane;
+    bool hit = false;
+    if (j < A.a1) {
+      float4 pj = pos4[j];
+      float d0 = (pj.x + L0) - A.pi.x, d1 = (pj.y + L1) - A.pi.y, d2 = (pj.z + L2) - A.pi.z;
+      float lim = A.pi.w + pj.w + 1.0e-2f;
+      if (d0 * d0 + d1 * d1 + d2 * d2 < lim * lim) {
+        // the reference's test, uncontracted FP64
+        double range = __dsub_rn(__dadd_rn(A.rci, fd->sp[isp[j]].rcA), 0.01);
+        double r2[3] = {__dadd_rn(ratom[3 * j], X0), __dadd_rn(ratom[3 * j + 1], X1),
+                        __dadd_rn(ratom[3 * j + 2], X2)};
+        double z = dist_rn(A.ri, r2);
+        if (CHECK && A.i != j && z < 0.5) {
+          atomicOr(status, DEVERR_CLOSE);
+          errinfo[0] = A.i;
+          errinfo[1] = j;
+          errinfo[2] = mb;
         }
+        hit = z < range;
       }
-      unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (m == 0u) continue;
-      // inclusive warp scan of norb_j over the hit lanes -> block offsets
-      int nj = hit ? fd->sp[isp[j]].norb : 0;
-      int incl = nj;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m == 0u) continue;
+    // inclusive warp scan of norb_j over the hit lanes -> block offsets
+    int nj = hit ? fd->sp[isp[j]].norb : 0;
+    int incl = nj;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        int u = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += u;
-      }
-      if (FILL && hit) {
-        int idx = num + __popc(m & ((1u << lane) - 1u));
-        neigh_j[base + idx] = j;
-        neigh_b[base + idx] = mb;
-        pair_owner[base + idx] = i;
-        blk_off[base + idx] = bbase + (long long)ni * (norbsum + incl - nj);
-        if (j == i && mb == 0) neigh_self[i] = idx;
-      }
-      num += __popc(m);
-      norbsum += __shfl_sync(0xffffffffu, incl, 31);
+    for (int d = 1; d < 32; d <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += u;
+    }
+    if (WRITE && hit) {
+      int idx = off + num + __popc(m & ((1u << lane) - 1u));
+      neigh_j[base + idx] = j;
+      neigh_b[base + idx] = mb;
+      pair_owner[base + idx] = A.i;
+      blk_off[base + idx] = bbase + (long long)A.ni * (orb + incl - nj);
+      if (j == A.i && mb == 0) neigh_self[A.i] = idx;
+    }
+    num += __popc(m);
+    orb += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  return num;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(NEIGH_THREADS)
+    k_neigh(int N, const double *__restrict__ ratom, const float4 *__restrict__ pos4, const int *__restrict__ isp,
+            const FdataDev *__restrict__ fd, const int *__restrict__ sid, const int *__restrict__ satom_off,
+            const int *__restrict__ simg_off, const float4 *__restrict__ sbbox, float rcmax,
+            const double *__restrict__ xl, const float *__restrict__ xlf, const int *__restrict__ imgs,
+            int *__restrict__ cnt, long long *__restrict__ bsum, const int *__restrict__ pair_off,
+            const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
+            int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
+            unsigned *__restrict__ status, int *__restrict__ errinfo) {
+  __shared__ int s_cnt[NIMG];         // hits of each image, then their first slot
+  __shared__ long long s_orb[NIMG];   // norb sum of each image's hits, then its running start
+  int i = blockIdx.x;
+  if (i >= N) return;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  NeighAtom A;
+  A.i = i;
+  int s = sid[i];
+  A.a0 = satom_off[s];
+  A.a1 = satom_off[s + 1];
+  A.X = xl + (long long)s * XL_STRIDE;
+  A.Xf = xlf + (long long)s * XL_STRIDE;
+  A.lo = sbbox[2 * s];
+  A.hi = sbbox[2 * s + 1];
+#pragma unroll
+  for (int k = 0; k < 3; k++) A.ri[k] = ratom[3 * i + k];
+  A.pi = pos4[i];
+  A.rci = fd->sp[isp[i]].rcA;
+  A.reach = A.pi.w + rcmax + 1.0e-2f;
+  A.ni = fd->sp[isp[i]].norb;
+  int g0 = simg_off[s], nimg = simg_off[s + 1] - g0;
+  if (nimg > NIMG) {  // the image list holds each mbeta at most once
+    if (threadIdx.x == 0) atomicOr(status, DEVERR_CAP);
+    return;
+  }
+  int base = FILL ? pair_off[i] : 0;
+  long long bbase = FILL ? blk_base[i] : 0;
+  for (int k = warp; k < nimg; k += nw) {
+    long long orb = 0;
+    int c = neigh_sweep<!FILL, false>(A, imgs[g0 + k], lane, 0, orb, ratom, pos4, isp, fd, base, bbase, neigh_j,
+                                      neigh_b, neigh_self, pair_owner, blk_off, status, errinfo);
+    if (lane == 0) {
+      s_cnt[k] = c;
+      s_orb[k] = orb;
     }
   }
-  if (!FILL && lane == 0) {
-    cnt[i] = num;
-    bsum[i] = (long long)ni * norbsum;
+  __syncthreads();
+  if (warp == 0) {  // exclusive scan over the images, in list order
+    int carry = 0;
+    long long corb = 0;
+    for (int k0 = 0; k0 < nimg; k0 += 32) {
+      int k = k0 + lane;
+      int c = k < nimg ? s_cnt[k] : 0;
+      long long o = k < nimg ? s_orb[k] : 0;
+      int x = c;
+      long long y = o;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, x, d);
+        long long v = __shfl_up_sync(0xffffffffu, y, d);
+        if (lane >= d) {
+          x += u;
+          y += v;
+        }
+      }
+      if (k < nimg) {
+        s_cnt[k] = carry + x - c;
+        s_orb[k] = corb + y - o;
+      }
+      carry += __shfl_sync(0xffffffffu, x, 31);
+      corb += __shfl_sync(0xffffffffu, y, 31);
+    }
+    if (!FILL && lane == 0) {
+      cnt[i] = carry;
+      bsum[i] = (long long)A.ni * corb;
+    }
   }
-  if (FILL) {
-    __syncwarp();
-    if (lane == 0 && neigh_self[i] < 0) atomicOr(status, DEVERR_SELF);
+  if (!FILL) return;
+  __syncthreads();
+  for (int k = warp; k < nimg; k += nw) {
+    long long orb = s_orb[k];
+    neigh_sweep<false, true>(A, imgs[g0 + k], lane, s_cnt[k], orb, ratom, pos4, isp, fd, base, bbase, neigh_j,
+                             neigh_b, neigh_self, pair_owner, blk_off, status, errinfo);
   }
+  __syncthreads();
+  if (threadIdx.x == 0 && neigh_self[i] < 0) atomicOr(status, DEVERR_SELF);
 }
 
 // neigh_back (M_neighbors.f90:469-486) and the per-pair vectors
@@ -405,7 +481,8 @@ int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsign
 }
 
 int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
-  int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
+  if (a.N == 0) return 0;
+  int threads = NEIGH_THREADS, blocks = a.N;
   if (fill)
     k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
                                              a.sbbox, a.rcmax, a.xl, a.xlf, a.imgs, nullptr, nullptr, a.pair_off,
