@@ -55,6 +55,112 @@ def test_neighbors_match_brute_force(fdata_root, name):
             assert np.allclose(xl[s.neigh_b[p]] + xl[s.neigh_b[q]], 0.0, atol=1e-9)
 
 
+def _rc(name, st):
+    sp = synth.species_for(name)
+    return np.array([max(r * 0.529177 for r in x.rcutoff) for x in sp])[st.imass - 1]
+
+
+def _common_brute(s, st, xl, rc):
+    """find_common_neighbors (c.SYSTEM/M_neighbors.f90:548-812) as plain
+    loops: for each ialpha, ineigh then jneigh over its non-self neighbors,
+    i != j index, kept when |r1 - r2| < rc_i + rc_j - 0.01 and j is found in
+    i's list by the vector match (first kneigh, 1e-4 per component)."""
+    out = []
+    for a in range(st.natoms):
+        p0, p1 = s.pair_off[a], s.pair_off[a + 1]
+        pself = p0 + s.neigh_self[a]
+        for pi in range(p0, p1):
+            if pi == pself:
+                continue
+            i, ib = s.neigh_j[pi], s.neigh_b[pi]
+            r1 = st.ratom[i] + xl[ib]
+            q0, q1 = s.pair_off[i], s.pair_off[i + 1]
+            r3 = st.ratom[s.neigh_j[q0:q1]] + xl[s.neigh_b[q0:q1]] - st.ratom[i]
+            for pj in range(p0, p1):
+                if pj == pself or pj == pi:
+                    continue
+                j, jb = s.neigh_j[pj], s.neigh_b[pj]
+                r2 = st.ratom[j] + xl[jb]
+                if not np.linalg.norm(r2 - r1) < rc[i] + rc[j] - 0.01:
+                    continue
+                hit = np.nonzero(np.all(np.abs(r3 - r2 + r1) < 1e-4, axis=1))[0]
+                if len(hit):
+                    out.append((a, i, ib, j, jb, int(hit[0])))
+    return out
+
+
+def _common_got(s):
+    return [(a, s.ci_j[t], s.ci_b[t], s.cj_j[t], s.cj_b[t], s.cneigh[t])
+            for a in range(len(s.trip_off) - 1) for t in range(s.trip_off[a], s.trip_off[a + 1])]
+
+
+@pytest.mark.parametrize("name", ["si_vac", "sic_vac"])
+def test_common_neighbors_match_brute_force(fdata_root, name):
+    """Every triplet of the reference loops, in their order, and no other."""
+    fd, s, st, norb = _system(name, fdata_root)
+    rc = _rc({"si_vac": "si64", "sic_vac": "sic4096"}[name], st)
+    want = _common_brute(s, st, _xl(st.lattice), rc)
+    assert s.ntrip == len(want) > 0
+    assert _common_got(s) == want
+
+
+def _cluster(ratom):
+    ratom = np.asarray(ratom, float)
+    return synth.Structure(ratom=ratom, imass=np.ones(len(ratom), np.int32), lattice=20.0 * np.eye(3),
+                           icluster=1, name="cluster")
+
+
+@pytest.mark.parametrize("kind", ["atom", "dimer", "isolated"])
+def test_sparse_clusters(fdata_root, kind):
+    """Ragged neighbor lists: one atom (only its self pair, no triplets), a
+    dimer (rows without a partner, no triplets) and a cluster with one atom
+    far from the rest (a self-only list among full ones).  Neighbors and
+    triplets as the brute force gives them; blocks Hermitian; the total
+    force on the cluster vanishes (zero on a lone atom)."""
+    path, nZ, base = workload("sic_vac", fdata_root)
+    if kind == "atom":
+        st = _cluster([[0.0, 0.0, 0.0]])
+    elif kind == "dimer":
+        st = _cluster([[0.0, 0.0, 0.0], [0.3, -0.2, 2.3]])
+    else:
+        si8 = synth.diamond((1, 1, 1), 5.43, 0.1, 21, name="Si8")
+        st = _cluster(np.vstack([si8.ratom, [[30.0, 30.0, 30.0]]]))
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice, icluster=1).neighbors()
+    rc = _rc("sic4096", st)
+    xl = np.zeros((1, 3))
+    N = st.natoms
+    for i in range(N):
+        d = np.linalg.norm(st.ratom - st.ratom[i], axis=1)
+        want = [(j, 0) for j in np.nonzero(d < rc[i] + rc - 0.01)[0]]
+        got = list(zip(s.neigh_j[s.pair_off[i]:s.pair_off[i + 1]], s.neigh_b[s.pair_off[i]:s.pair_off[i + 1]]))
+        assert got == want
+    assert _common_got(s) == _common_brute(s, st, xl, rc)
+    if kind == "atom":
+        assert (s.npairs, s.ntrip) == (1, 0)
+    elif kind == "dimer":
+        assert (s.npairs, s.ntrip) == (4, 0)
+    else:
+        assert np.diff(s.pair_off)[-1] == 1 and s.ntrip > 0
+    S, T, vb, vbo = s.assemble()
+    assert np.all(np.isfinite(S)) and np.all(np.isfinite(T + vb + vbo))
+    norb = np.array([fd.norb(int(k)) for k in st.imass])
+    for i in range(N):
+        for p in range(s.pair_off[i], s.pair_off[i + 1]):
+            j = s.neigh_j[p]
+            q = s.pair_off[j] + s.neigh_back[p]
+            a = S[s.blk_off[p]:s.blk_off[p + 1]].reshape(norb[j], norb[i]).T
+            b = S[s.blk_off[q]:s.blk_off[q + 1]].reshape(norb[i], norb[j]).T
+            assert np.abs(a - b.T).max() < 1e-13
+    rho, cape = symmetric_denmat(s, norb, 3)
+    f = s.dassemble(rho, cape)["ftot"].reshape(N, 3)
+    assert np.all(np.isfinite(f))
+    if kind == "atom":
+        assert np.abs(f).max() < 1e-12
+    else:
+        assert np.abs(f.sum(axis=0)).max() < 1e-9 * max(1.0, np.abs(f).max())
+
+
 def test_common_neighbors_are_pairs_within_cutoff(fdata_root):
     fd, s, st, norb = _system("si64", fdata_root)
     xl = _xl(st.lattice)
