@@ -480,7 +480,8 @@ long long fb_kernel_launches(const fb_ctx *ctx);
  * "dassemble_3c", "build_forces", "trip_bins", "split_rho", "mlp_eval",
  * "assemble_3c_mlp", "dassemble_3c_mlp", "bloch", "pp_pairs", "ppp", "pp_common",
  * "svnl", "vnl_2c", "vnl_3c", "dsvnl", "dvnl_2c", "dvnl_3c", "vnl_forces", "ewald",
- * "ewald_blocks".  No reference counterpart (the reference
+ * "ewald_blocks", "rho_2c", "rho_3c", "vxc", "dvxc_2c", "dvxc_3c",
+ * "vxc_forces".  No reference counterpart (the reference
  * has no timers on this path). */
 int fb_set_timing(fb_ctx *ctx, int enable);
 int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,
