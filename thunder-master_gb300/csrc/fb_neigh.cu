@@ -16,6 +16,8 @@ namespace fb {
 // discards far pairs; every candidate is decided by the uncontracted FP64
 // test of the reference: z = distance(r1, r2) < rc_i + rc_j - 0.01.
 constexpr int NEIGH_THREADS = 256;
+// per-image counts and norb sums of one atom live in static shared memory
+static_assert(NIMG * (sizeof(int) + sizeof(long long)) <= 48 * 1024, "image box too large for k_neigh");
 
 struct NeighAtom {
   int i, a0, a1, ni;
