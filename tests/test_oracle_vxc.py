@@ -264,3 +264,46 @@ def test_vxc_forces_conserve_momentum(cluster):
     st, at, s, rho = cluster
     d = s.dassemble_vxc(rho)
     assert np.abs(d["ftot_add"].reshape(-1, 3).sum(0)).max() < 1e-11
+
+
+@pytest.mark.parametrize("kind", ["atom", "dimer", "isolated"])
+def test_sparse_clusters(fdata_root, kind):
+    """Ragged lists under McWEDA: a lone Si atom (its self pair only: the
+    density and vxc come from the atom term and vxc_1c), a Si dimer, and a
+    Si8 cluster with one atom far away.  Blocks finite and Hermitian, the
+    lone atom's density block the same with and without three-center terms,
+    and the vxc forces summing to zero."""
+    from conftest import symmetric_denmat
+    from fbgpu import synth
+    path, nZ, _ = workload("sic_small", fdata_root, vxc=True)
+    if kind == "atom":
+        r = np.zeros((1, 3))
+    elif kind == "dimer":
+        r = np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 2.3]])
+    else:
+        r = np.vstack([synth.diamond((1, 1, 1), 5.43, 0.1, 21).ratom, [[30.0, 30.0, 30.0]]])
+    imass = np.ones(len(r), np.int32)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, r, imass, 20.0 * np.eye(3), icluster=1).neighbors()
+    v3 = s.assemble_vxc()
+    v2 = s.assemble_vxc(with3c=False)
+    norb = [fd.norb(1)] * len(r)
+    for key in ("rho_in", "rho_bond", "vxc"):
+        x = v3[key]
+        assert np.all(np.isfinite(x)), key
+        for i in range(len(r)):
+            for p in range(s.pair_off[i], s.pair_off[i + 1]):
+                j = s.neigh_j[p]
+                q = s.pair_off[j] + s.neigh_back[p]
+                a = x[s.blk_off[p]:s.blk_off[p + 1]].reshape(norb[j], norb[i]).T
+                b = x[s.blk_off[q]:s.blk_off[q + 1]].reshape(norb[i], norb[j]).T
+                assert np.abs(a - b.T).max() < 1e-12 * max(1.0, np.abs(x).max()), key
+    if kind in ("atom", "dimer"):  # no triplets: the three-center terms add nothing
+        assert s.ntrip == 0
+        for key in ("rho_in", "vxc"):
+            assert np.array_equal(v3[key], v2[key]), key
+    rho, _ = symmetric_denmat(s, norb, 5)
+    d = s.dassemble_vxc(rho)
+    f = d["ftot_add"].reshape(-1, 3)
+    assert np.all(np.isfinite(f))
+    assert np.abs(f.sum(0)).max() < 1e-11 * max(1.0, np.abs(f).max())
