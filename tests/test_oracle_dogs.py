@@ -115,3 +115,34 @@ def test_dogs_charged_forces_linear(systems):
     b = s.dassemble_dogs(rho, cape, 2.0 * dq)["ftot"] - z
     assert np.abs(a).max() > 1e-3
     assert np.abs(b - 2.0 * a).max() <= 1e-9 * max(1.0, np.abs(b).max())
+
+
+@pytest.mark.parametrize("kind", ["atom", "dimer", "isolated"])
+def test_dogs_sparse_clusters(fdata_root, kind):
+    """A lone atom, a dimer and a cluster with one isolated atom under DOGS
+    with random shell charges: zero charges give the Harris blocks, the
+    blocks are finite, and the total force vanishes."""
+    from conftest import symmetric_denmat
+    from fbgpu import synth
+    if kind == "atom":
+        r = np.zeros((1, 3))
+    elif kind == "dimer":
+        r = np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 2.3]])
+    else:
+        r = np.vstack([synth.diamond((1, 1, 1), 5.43, 0.1, 21).ratom, [[30.0, 30.0, 30.0]]])
+    imass = np.ones(len(r), np.int32)
+    path, nZ, _ = workload("sic_vac", fdata_root, dogs=True)
+    path0, _, _ = workload("sic_vac", fdata_root)
+    fd, fd0 = orc.Fdata(path, nZ), orc.Fdata(path0, nZ)
+    s = orc.System(fd, r, imass, 20.0 * np.eye(3), icluster=1).neighbors()
+    s0 = orc.System(fd0, r, imass, 20.0 * np.eye(3), icluster=1).neighbors()
+    zero = np.zeros((len(r), 3))
+    for a, b in zip(s0.assemble(), s.assemble_dogs(zero)[:4]):
+        assert np.array_equal(a, b)
+    dq = np.random.default_rng(7).uniform(-0.3, 0.3, (len(r), 3))
+    blocks = s.assemble_dogs(dq)
+    assert all(np.all(np.isfinite(x)) for x in blocks)
+    rho, cape = symmetric_denmat(s, [fd.norb(1)] * len(r), 2)
+    f = s.dassemble_dogs(rho, cape, dq)["ftot"].reshape(-1, 3)
+    assert np.all(np.isfinite(f))
+    assert np.abs(f.sum(0)).max() < 1e-9 * max(1.0, np.abs(f).max())

@@ -156,3 +156,91 @@ def test_vnl_forces_are_minus_gradient(pp_system):
             rm[i, k] -= h
             g = -(energy(rp) - energy(rm)) / (2 * h)
             assert abs(g - f[i, k]) < 1e-5 * max(1.0, abs(g)), (i, k, g, f[i, k])
+
+
+# clusters sit off the origin: the 2c frames are built from absolute
+# positions (epsilon(r2_absolute, sighat), M_assemble_2c_Harris.f90:177), and
+# an atom at the origin takes the degenerate frame whose derivative
+# Depsilon_2c sets to zero (b.FUNCTIONS/Depsilon_2c.f90:99-107)
+_OFF = np.array([1.1, 0.7, -0.4])
+
+
+def _sparse(kind):
+    if kind == "atom":
+        r = np.zeros((1, 3))
+    elif kind == "dimer":
+        r = np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 2.3]])
+    else:
+        r = np.vstack([synth.diamond((1, 1, 1), 5.43, 0.1, 21).ratom, [[30.0, 30.0, 30.0]]])
+    return synth.Structure(ratom=r + _OFF, imass=np.ones(len(r), np.int32), lattice=20.0 * np.eye(3),
+                           icluster=1)
+
+
+@pytest.mark.parametrize("kind", ["atom", "dimer", "isolated"])
+def test_vnl_sparse_clusters(fdata_root, kind):
+    """A lone atom (its own projector only), a dimer and a cluster with one
+    isolated atom: vnl blocks Hermitian, the vnl forces sum to zero, and on
+    the dimer they are minus the gradient of sum rho_pp . vnl."""
+    path, nZ, _ = workload("sic_vac", fdata_root)
+    fd = orc.Fdata(path, nZ)
+    st = _sparse(kind)
+
+    def build(r):
+        return orc.System(fd, r, st.imass, st.lattice, icluster=1).neighbors().neighbors_pp()
+
+    s = build(st.ratom)
+    xl = _xl(st.lattice)
+    _, vnl = s.assemble_pp()
+    back = _back(s, st, xl)
+    off, norb = _vnl_off(s, fd, st)
+    ppp = s.pp["PPp"]
+    assert np.all(np.isfinite(vnl)) and off[-1] == len(vnl)
+    for i in range(len(st.imass)):
+        for p in range(ppp["off"][i], ppp["off"][i + 1]):
+            j, q = ppp["j"][p], back[p]
+            a = vnl[off[p]:off[p + 1]].reshape(norb[j], norb[i]).T
+            b = vnl[off[q]:off[q + 1]].reshape(norb[i], norb[j]).T
+            assert np.abs(a - b.T).max() < 1e-12
+    rho = _sym_rho(s, fd, st, 6)
+    f = s.dassemble_pp(rho)["ftot_vnl"].reshape(-1, 3)
+    assert np.all(np.isfinite(f))
+    assert np.abs(f.sum(0)).max() < 1e-10 * max(1.0, np.abs(f).max())
+    if kind == "dimer":
+        h = 1e-5
+        for k in range(3):
+            rp, rm = st.ratom.copy(), st.ratom.copy()
+            rp[1, k] += h
+            rm[1, k] -= h
+            g = -(float(rho @ build(rp).assemble_pp()[1]) - float(rho @ build(rm).assemble_pp()[1])) / (2 * h)
+            assert abs(g - f[1, k]) < 1e-5 * max(1.0, abs(g)), (k, g, f[1, k])
+
+
+def test_vnl_frame_derivative_vanishes_at_the_origin(fdata_root):
+    """The reference's quirk, kept: a dimer along z with one atom at the
+    origin.  Its 2c frames come from absolute positions; at the origin
+    Depsilon_2c returns zero, so the vnl force keeps the component along the
+    bond (equal to minus the gradient) and loses the frame-rotation part
+    that the gradient of a non-rotation-invariant rho_pp . vnl has across it."""
+    path, nZ, _ = workload("sic_vac", fdata_root)
+    fd = orc.Fdata(path, nZ)
+    imass = np.ones(2, np.int32)
+
+    def build(r):
+        return orc.System(fd, r, imass, 20.0 * np.eye(3), icluster=1).neighbors().neighbors_pp()
+
+    r = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 2.35]])
+    st = synth.Structure(ratom=r, imass=imass, lattice=20.0 * np.eye(3), icluster=1)
+    s = build(r)
+    rho = _sym_rho(s, fd, st, 6)
+    f = s.dassemble_pp(rho)["ftot_vnl"].reshape(-1, 3)
+    h = 1e-5
+    g = np.zeros(3)
+    for k in range(3):
+        rp, rm = r.copy(), r.copy()
+        rp[1, k] += h
+        rm[1, k] -= h
+        g[k] = -(float(rho @ build(rp).assemble_pp()[1]) - float(rho @ build(rm).assemble_pp()[1])) / (2 * h)
+    assert abs(g[2] - f[1, 2]) < 1e-5 * max(1.0, abs(g[2]))
+    assert np.abs(f[1, :2]).max() == 0.0
+    assert np.abs(g[:2]).max() > 1e-3
+
