@@ -252,3 +252,33 @@ def test_parallel_oracle_matches_serial(fdata_root):
     f1 = s1.dassemble(rho, cape)["ftot"]
     f4 = s4.dassemble(rho, cape)["ftot"]
     assert np.abs(f1 - f4).max() < 1e-11
+
+
+def test_cluster_forces_are_minus_gradient(fdata_root):
+    """The same derivative check on a cluster (icluster = 1: no images),
+    placed off the origin, with one isolated atom: ftot = -dE/dR."""
+    path, nZ, _ = workload("sic_vac", fdata_root)
+    fd = orc.Fdata(path, nZ)
+    r = np.vstack([synth.diamond((1, 1, 1), 5.43, 0.1, 21).ratom, [[30.0, 30.0, 30.0]]]) + [1.1, 0.7, -0.4]
+    imass = np.ones(len(r), np.int32)
+    lat = 20.0 * np.eye(3)
+    s = orc.System(fd, r, imass, lat, icluster=1).neighbors()
+    norb = np.array([fd.norb(1)] * len(r))
+    rho, cape = symmetric_denmat(s, norb, 12)
+    f = s.dassemble(rho, cape)["ftot"].reshape(-1, 3)
+    assert np.abs(f[-1]).max() == 0.0  # the isolated atom feels nothing
+
+    def energy(x):
+        t = orc.System(fd, x, imass, lat, icluster=1).neighbors()
+        assert t.npairs == s.npairs and t.ntrip == s.ntrip
+        S, T, vb, vbo = t.assemble()
+        return float(rho @ (T + vb + vbo) - cape @ S)
+
+    h = 1e-5
+    for i in (0, 3, 6):
+        for k in range(3):
+            rp, rm = r.copy(), r.copy()
+            rp[i, k] += h
+            rm[i, k] -= h
+            g = (energy(rp) - energy(rm)) / (2 * h)
+            assert abs(-g - f[i, k]) < 1e-5 * max(1.0, abs(g)), (i, k, -g, f[i, k])
