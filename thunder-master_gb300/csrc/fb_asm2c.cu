@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(256) k_assemble_2c(Ctx2c c, unsigned what, Sch
   });
 }
 
+#if FB_IN_PART(0)
 // build_forces, assembly terms (c.SYSTEM/M_build_forces.f90:172-588).  The
 // j-side contribution of pair (i -> j) is gathered by atom j through
 // neigh_back, which maps j's own pair list one-to-one onto the pairs whose
@@ -235,6 +236,26 @@ __global__ void k_build_forces(int N, const int *__restrict__ pair_off, const in
     }
   }
 }
+#endif
+
+// The four instantiations (HASD, DOGS) of k_assemble_2c build as four parts of
+// this source (FB_IN_PART); part 0 also holds the launcher.
+int launch_assemble_2c_v(int v, const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_assemble_2c_v0(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_assemble_2c_v1(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_assemble_2c_v2(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_assemble_2c_v3(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+
+#if FB_IN_PART(0)
+int launch_assemble_2c_v(int v, const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  switch (v) {
+    case 0: return launch_assemble_2c_v0(c, what, q, grid, block, s);
+    case 1: return launch_assemble_2c_v1(c, what, q, grid, block, s);
+    case 2: return launch_assemble_2c_v2(c, what, q, grid, block, s);
+    case 3: return launch_assemble_2c_v3(c, what, q, grid, block, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
 
 int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   Ctx2c c = make2c(a);
@@ -243,17 +264,44 @@ int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   int e = sched_launch(a.cfg_a2c, (long long)a.N * 32, a.queue ? a.queue + 0 : nullptr, s, grid, block, q);
   if (e) return e;
   bool dogs = a.dogs && (what & 4u);
-  if (a.have_d) {
-    if (dogs) k_assemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
-    else k_assemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
-  } else {
-    if (dogs) k_assemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
-    else k_assemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
-  }
+  int v = (a.have_d ? 2 : 0) + (dogs ? 1 : 0);
+  return launch_assemble_2c_v(v, c, what, q, grid, block, s);
+}
+#endif
+
+#if FB_IN_PART(0)
+int launch_assemble_2c_v0(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_assemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
+#endif
 
+#if FB_IN_PART(1)
+int launch_assemble_2c_v1(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_assemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(2)
+int launch_assemble_2c_v2(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_assemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(3)
+int launch_assemble_2c_v3(const Ctx2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_assemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(0)
 int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s) {
   int threads = 128, blocks = (a.N * 32 + threads - 1) / threads;
   k_build_forces<<<blocks, threads, 0, s>>>(a.N, a.pair_off, a.neigh_j, a.neigh_back, a.sumT, a.sumS, a.ontop,
@@ -261,5 +309,6 @@ int launch_build_forces(const AsmArgs &a, unsigned what, cudaStream_t s) {
   FB_LAUNCH_CHECK();
   return 0;
 }
+#endif
 
 }  // namespace fb

@@ -229,6 +229,25 @@ __global__ void __launch_bounds__(256) k_dassemble_2c(CtxD2c c, unsigned what, S
   });
 }
 
+// The four instantiations (HASD, DOGS) of k_dassemble_2c build as four parts of
+// this source (FB_IN_PART); part 0 also holds the launcher.
+int launch_dassemble_2c_v(int v, const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_2c_v0(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_2c_v1(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_2c_v2(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_2c_v3(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+
+#if FB_IN_PART(0)
+int launch_dassemble_2c_v(int v, const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  switch (v) {
+    case 0: return launch_dassemble_2c_v0(c, what, q, grid, block, s);
+    case 1: return launch_dassemble_2c_v1(c, what, q, grid, block, s);
+    case 2: return launch_dassemble_2c_v2(c, what, q, grid, block, s);
+    case 3: return launch_dassemble_2c_v3(c, what, q, grid, block, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   CtxD2c c;
   c.b = make2c(a);
@@ -246,15 +265,41 @@ int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d2c, (long long)a.N * 32, a.queue ? a.queue + 2 : nullptr, s, grid, block, q);
   if (e) return e;
-  if (a.have_d) {
-    if (a.dogs) k_dassemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
-    else k_dassemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
-  } else {
-    if (a.dogs) k_dassemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
-    else k_dassemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
-  }
+  int v = (a.have_d ? 2 : 0) + (a.dogs ? 1 : 0);
+  return launch_dassemble_2c_v(v, c, what, q, grid, block, s);
+}
+#endif
+
+#if FB_IN_PART(0)
+int launch_dassemble_2c_v0(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_2c<false, false><<<grid, block, 0, s>>>(c, what, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
+#endif
+
+#if FB_IN_PART(1)
+int launch_dassemble_2c_v1(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_2c<false, true><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(2)
+int launch_dassemble_2c_v2(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_2c<true, false><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(3)
+int launch_dassemble_2c_v3(const CtxD2c &c, unsigned what, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_2c<true, true><<<grid, block, 0, s>>>(c, what, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
 
 }  // namespace fb

@@ -186,6 +186,25 @@ __global__ void __launch_bounds__(256) k_dassemble_3c(Ctx3c c, Sched q) {
   });
 }
 
+// The four instantiations (HASD, DOGS) of k_dassemble_3c build as four parts of
+// this source (FB_IN_PART); part 0 also holds the launcher.
+int launch_dassemble_3c_v(int v, const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v0(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v1(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v2(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v3(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+
+#if FB_IN_PART(0)
+int launch_dassemble_3c_v(int v, const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  switch (v) {
+    case 0: return launch_dassemble_3c_v0(c, q, grid, block, s);
+    case 1: return launch_dassemble_3c_v1(c, q, grid, block, s);
+    case 2: return launch_dassemble_3c_v2(c, q, grid, block, s);
+    case 3: return launch_dassemble_3c_v3(c, q, grid, block, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
 int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s) {
   if (a.ntrip == 0) return 0;
   Ctx3c c = make3c(a);
@@ -193,15 +212,41 @@ int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  if (a.have_d) {
-    if (a.dogs) k_dassemble_3c<true, true><<<grid, block, 0, s>>>(c, q);
-    else k_dassemble_3c<true, false><<<grid, block, 0, s>>>(c, q);
-  } else {
-    if (a.dogs) k_dassemble_3c<false, true><<<grid, block, 0, s>>>(c, q);
-    else k_dassemble_3c<false, false><<<grid, block, 0, s>>>(c, q);
-  }
+  int v = (a.have_d ? 2 : 0) + (a.dogs ? 1 : 0);
+  return launch_dassemble_3c_v(v, c, q, grid, block, s);
+}
+#endif
+
+#if FB_IN_PART(0)
+int launch_dassemble_3c_v0(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<false, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
+#endif
+
+#if FB_IN_PART(1)
+int launch_dassemble_3c_v1(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<false, true><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(2)
+int launch_dassemble_3c_v2(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<true, false><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(3)
+int launch_dassemble_3c_v3(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<true, true><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
 
 }  // namespace fb

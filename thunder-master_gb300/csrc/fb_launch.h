@@ -3,6 +3,16 @@
 #include <cuda_runtime.h>
 #include "fb_internal.h"
 
+// A source whose template instantiations take long to compile is built in
+// parts: the build compiles it once per part with -DFB_PART=k, and part k
+// holds only the launchers marked FB_IN_PART(k), so the parts compile in
+// parallel.  Compiled without FB_PART, a source holds every part.
+#ifdef FB_PART
+#define FB_IN_PART(k) (FB_PART == (k))
+#else
+#define FB_IN_PART(k) 1
+#endif
+
 namespace fb {
 
 // Launch shape of one kernel: threads per CTA; ctas_per_sm > 0 selects the

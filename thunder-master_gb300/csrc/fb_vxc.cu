@@ -873,6 +873,7 @@ __global__ void __launch_bounds__(128) k_dvxc_3c(Ctx3c c, VxcArgs v) {
   }
 }
 
+#if FB_IN_PART(0)
 // build_forces vxc terms (c.SYSTEM/M_build_forces.f90:345-365, :453-455):
 // f_i += off + on of i's pairs, f_j -= them, gathered by atom j through
 // neigh_back (one warp per atom); ftot += that + f3xca + f3xcb + f3xcc.
@@ -902,32 +903,24 @@ __global__ void k_vxc_forces(int N, const int *__restrict__ pair_off, const int 
     }
   }
 }
+#endif
 
 }  // namespace
 
+// The launchers are split over eight parts of this source (FB_IN_PART): the
+// d-shell (HASD) instantiations build apart from the s/p ones.
+int launch_dvxc_3c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s);
+int launch_dvxc_3c_d_split(const VxcArgs &v, int blocks, int threads, cudaStream_t s);
+int launch_rho_3c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s);
+int launch_dvxc_2c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s);
+
+#if FB_IN_PART(0)
 int launch_rho_2c(const VxcArgs &v, cudaStream_t s) {
   if (v.a.N == 0) return 0;
   Ctx2c c = make2c(v.a);
   int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
   if (v.a.have_d) k_rho_2c<true><<<blocks, threads, 0, s>>>(c, v);
   else k_rho_2c<false><<<blocks, threads, 0, s>>>(c, v);
-  FB_LAUNCH_CHECK();
-  return 0;
-}
-
-int launch_rho_3c(const VxcArgs &v, cudaStream_t s) {
-  if (v.a.ntrip == 0) return 0;
-  Ctx3c c = make3c(v.a);
-  int threads = 128;
-  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
-  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
-  if (v.a.have_d) {
-    k_rho_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
-    if (!v.qsum_all) k_rho_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
-  } else {
-    k_rho_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
-    if (!v.qsum_all) k_rho_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
-  }
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -942,33 +935,6 @@ int launch_vxc(const VxcArgs &v, cudaStream_t s) {
   return 0;
 }
 
-int launch_dvxc_2c(const VxcArgs &v, cudaStream_t s) {
-  if (v.a.N == 0) return 0;
-  Ctx2c c = make2c(v.a);
-  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
-  if (v.a.have_d) k_dvxc_2c<true><<<blocks, threads, 0, s>>>(c, v);
-  else k_dvxc_2c<false><<<blocks, threads, 0, s>>>(c, v);
-  FB_LAUNCH_CHECK();
-  return 0;
-}
-
-int launch_dvxc_3c(const VxcArgs &v, cudaStream_t s) {
-  if (v.a.ntrip == 0) return 0;
-  Ctx3c c = make3c(v.a);
-  int threads = 128;
-  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
-  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
-  if (v.a.have_d) {
-    k_dvxc_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
-    if (!v.qsum_all) k_dvxc_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
-  } else {
-    k_dvxc_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
-    if (!v.qsum_all) k_dvxc_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
-  }
-  FB_LAUNCH_CHECK();
-  return 0;
-}
-
 int launch_vxc_forces(const VxcArgs &v, cudaStream_t s) {
   if (v.a.N == 0) return 0;
   int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
@@ -977,5 +943,87 @@ int launch_vxc_forces(const VxcArgs &v, cudaStream_t s) {
   FB_LAUNCH_CHECK();
   return 0;
 }
+#endif
+
+#if FB_IN_PART(1)
+int launch_rho_3c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.ntrip == 0) return 0;
+  int threads = 128;
+  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
+  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
+  if (v.a.have_d) return launch_rho_3c_d(v, blocks, threads, s);
+  Ctx3c c = make3c(v.a);
+  k_rho_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
+  if (!v.qsum_all) k_rho_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(2)
+int launch_rho_3c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s) {
+  Ctx3c c = make3c(v.a);
+  k_rho_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
+  if (!v.qsum_all) k_rho_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
+#endif
+
+#if FB_IN_PART(3)
+int launch_dvxc_2c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.N == 0) return 0;
+  int threads = 128, blocks = (int)(((long long)v.a.N * 32 + threads - 1) / threads);
+  if (v.a.have_d) return launch_dvxc_2c_d(v, blocks, threads, s);
+  Ctx2c c = make2c(v.a);
+  k_dvxc_2c<false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(4)
+int launch_dvxc_2c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s) {
+  Ctx2c c = make2c(v.a);
+  k_dvxc_2c<true><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(5)
+int launch_dvxc_3c(const VxcArgs &v, cudaStream_t s) {
+  if (v.a.ntrip == 0) return 0;
+  int threads = 128;
+  long long need = ((long long)v.a.ntrip + threads - 1) / threads;
+  int blocks = (int)(need < 152LL * 64 ? need : 152LL * 64);
+  if (v.a.have_d) return launch_dvxc_3c_d(v, blocks, threads, s);
+  Ctx3c c = make3c(v.a);
+  k_dvxc_3c<false, true><<<blocks, threads, 0, s>>>(c, v);
+  if (!v.qsum_all) k_dvxc_3c<false, false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(6)
+int launch_dvxc_3c_d(const VxcArgs &v, int blocks, int threads, cudaStream_t s) {
+  Ctx3c c = make3c(v.a);
+  k_dvxc_3c<true, true><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  if (!v.qsum_all) return launch_dvxc_3c_d_split(v, blocks, threads, s);
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(7)
+int launch_dvxc_3c_d_split(const VxcArgs &v, int blocks, int threads, cudaStream_t s) {
+  Ctx3c c = make3c(v.a);
+  k_dvxc_3c<true, false><<<blocks, threads, 0, s>>>(c, v);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
 
 }  // namespace fb

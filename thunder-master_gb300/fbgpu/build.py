@@ -24,7 +24,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
 SOURCES = ["fb_api.cu", "fb_fdata.cpp", "fb_neigh.cu", "fb_asm2c.cu", "fb_asm3c.cu", "fb_dasm2c.cu", "fb_dasm3c.cu",
-           "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu", "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu"]
+           "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu",
+           "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu"]
+# Sources compiled in parts (-DFB_PART=k, k < count): their slow template
+# instantiations compile in parallel (FB_IN_PART in fb_launch.h).
+PARTS = {"fb_asm2c.cu": 4, "fb_asm3c.cu": 4, "fb_dasm2c.cu": 4, "fb_dasm3c.cu": 4, "fb_vxc.cu": 8}
 
 
 def nvcc():
@@ -36,6 +40,16 @@ def nvcc():
 
 def _sources():
     return [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+
+
+def _units():
+    """(source, part or None) per compile job, slowest sources first."""
+    units = []
+    for s in _sources():
+        n = PARTS.get(s)
+        units += [(s, k) for k in range(n)] if n else [(s, None)]
+    units.sort(key=lambda u: u[1] is None)
+    return units
 
 
 def _deps():
@@ -59,16 +73,19 @@ def build(force=False, verbose=False):
     cc = nvcc()
     objs = []
 
-    def compile_one(src):
-        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
-        cmd = [cc] + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+    def compile_one(unit):
+        src, part = unit
+        stem = os.path.splitext(src)[0] + ("" if part is None else ".p%d" % part)
+        obj = os.path.join(OUT, stem + ".o")
+        extra = [] if part is None else ["-DFB_PART=%d" % part, "-diag-suppress=177"]
+        cmd = [cc] + NVFLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
         return obj, r.stderr
 
-    with ThreadPoolExecutor(max_workers=8) as ex:
-        results = list(ex.map(compile_one, _sources()))
+    with ThreadPoolExecutor(max_workers=max(8, os.cpu_count() or 8)) as ex:
+        results = list(ex.map(compile_one, _units()))
     logs = []
     for obj, log in results:
         objs.append(obj)
