@@ -9,13 +9,18 @@ force kernels run as one CUDA graph launch per step, with launch shapes
 picked by the library's autotuner.  The density matrices the solver would
 supply are seeded synthetic blocks.
 
+Default workload: SiC4096, the 4,096-atom zincblende SiC cell (8x8x8 cells,
+a = 4.36 A, N(0, 0.1 A) jitter, sp3, rc = 5.0 bohr), synthetic Gaussian-
+polynomial Fdata, every kernel in FP64 (--prec fp64).  The same step with
+the double-float three-center kernels, its agreement with the FP64 result
+and with the oracle, the table vs MLP-3c comparison, the DOGS, vnl, Ewald,
+McWEDA and Bloch-sum steps, and the Si512, C/H/O 1536 and 256-structure
+batch workloads at both precisions ride along as extra keys of the line.
+
 --workload batch256: 256 independent Si / SiC structures of 32..512 atoms in
 one batch (one neighbor build + one graph launch per step), compared with
 the same 256 structures assembled one after another through the
 single-structure calls.
-
-Default workload: 512-atom Si (4x4x4 diamond cells, a = 5.43 A, N(0, 0.15 A)
-jitter, sp3, rc = 5.0 bohr), synthetic Gaussian-polynomial Fdata.
 
   value  neighbor blocks/s with inputs resident in HBM (device timing, CUDA
          events on the library's stream, L2 flushed between steps)
@@ -39,7 +44,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "thunder-master_gb300")
-for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
+for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
@@ -73,62 +78,8 @@ def load_workload(name):
 
 
 def denmat_fast(neighn, neigh_j0, neigh_back0, blk_off, norb_of, seed=42):
-    """Seeded density matrices symmetric across neigh_back (vectorized):
-    rho_ji(nu, mu) = rho_ij(mu, nu).  neigh_j0 and neigh_back0 are 0-based
-    global indices."""
-    rng = np.random.default_rng(seed)
-    NB = int(blk_off[-1])
-    raw_r = rng.normal(0.0, 0.1, NB)
-    raw_c = rng.normal(0.0, 0.05, NB)
-    P = len(neigh_j0)
-    pair_off = np.concatenate([[0], np.cumsum(neighn)]).astype(np.int64)
-    owner = np.repeat(np.arange(len(neighn)), neighn)
-    ni = norb_of[owner]
-    nj = norb_of[neigh_j0]
-    q = pair_off[neigh_j0] + neigh_back0
-    # every element e of pair p: (mu, nu) column-major, mu fastest
-    size = ni * nj
-    pe = np.repeat(np.arange(P), size)
-    loc = np.arange(NB) - np.repeat(blk_off[:P], size)
-    mu = loc % np.repeat(ni, size)
-    nu = loc // np.repeat(ni, size)
-    # the mirrored element (nu, mu) of pair q (an nj x ni block)
-    mirror = np.repeat(blk_off[q], size) + nu + np.repeat(nj, size) * mu
-    lead = pe <= np.repeat(q, size)  # the pair with the smaller index supplies the values
-    rho = np.where(lead, raw_r, raw_r[mirror])
-    cape = np.where(lead, raw_c, raw_c[mirror])
-    selfp = pe == np.repeat(q, size)
-    rho[selfp] = 0.5 * (raw_r[selfp] + raw_r[mirror[selfp]])
-    cape[selfp] = 0.5 * (raw_c[selfp] + raw_c[mirror[selfp]])
-    return rho, cape
-
-
-def denmat_for(ctx_or_sys, st, nZ, norb_of, seed=42):
-    """Seeded density matrices symmetric across neigh_back."""
-    rng = np.random.default_rng(seed)
-    nb = ctx_or_sys["blk_off"]
-    P = len(ctx_or_sys["neigh_j"])
-    rho = np.zeros(int(nb[-1]))
-    cape = np.zeros(int(nb[-1]))
-    pair_off = np.concatenate([[0], np.cumsum(ctx_or_sys["neighn"])])
-    owner = np.repeat(np.arange(len(ctx_or_sys["neighn"])), ctx_or_sys["neighn"])
-    for p in range(P):
-        i = owner[p]
-        j = ctx_or_sys["neigh_j"][p] - 1
-        q = pair_off[j] + ctx_or_sys["neigh_back"][p] - 1
-        if q < p:
-            continue
-        ni, nj = norb_of[i], norb_of[j]
-        a = rng.normal(0.0, 0.1, (ni, nj))
-        b = rng.normal(0.0, 0.05, (ni, nj))
-        if p == q:
-            a = 0.5 * (a + a.T)
-            b = 0.5 * (b + b.T)
-        rho[nb[p]:nb[p + 1]] = a.T.ravel()
-        cape[nb[p]:nb[p + 1]] = b.T.ravel()
-        rho[nb[q]:nb[q + 1]] = a.ravel()
-        cape[nb[q]:nb[q + 1]] = b.ravel()
-    return rho, cape
+    from fbgpu import synth
+    return synth.symmetric_denmat(neighn, neigh_j0, neigh_back0, blk_off, norb_of, seed)
 
 
 class ClockSampler:
@@ -363,32 +314,19 @@ def mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T
     return res
 
 
-def run_gpu(args):
-    import torch
-    import fbgpu
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    if args.workload == "batch256":
-        return run_batch(args, torch, fbgpu, ws, rank, local)
-    path, nZ, st = load_workload(args.workload)
-    ctx = fbgpu.Context(local)
-    stream = torch.cuda.Stream(device=local)
-    ctx.set_stream(stream.cuda_stream)
-    ctx.read_Fdata(path, nZ)
-    ctx.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
-    ctx.set_structure(st.ratom, st.imass, st.lattice)
-    P, T, NB = ctx.driver_neighbors()
-    nbm = ctx.neighbors()
-    norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
-    rho, cape = denmat_fast(nbm["neighn"], nbm["neigh_j"] - 1, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
-    d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
-    d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+PREC_NAME = {0: "fp64", 1: "df"}
+
+
+def measure_single(args, ctx, fbgpu, torch, stream, flush, ws, local, st, NB, rho, cape, d_rho, d_cape, prec,
+                   steps, warmup, e2e=True, clocks=False, autotune=True):
+    """Time one step of the path on the structure already on ctx, at one
+    precision of the three-center kernels: the device step (inputs in HBM),
+    the end-to-end step through the C ABI with pinned host buffers, and the
+    separate calls with per-kernel CUDA-event timing.  Returns the timings
+    and the step's outputs (S, T, vna, vnao, ftot)."""
+    ctx.set_precision(prec)
     ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
-    shapes = tuned_shapes(ctx, fbgpu, not args.no_autotune)
+    shapes = tuned_shapes(ctx, fbgpu, autotune)
     step_what = fbgpu.FB_ALL | fbgpu.FB_FORCES
 
     def device_step():
@@ -403,7 +341,6 @@ def run_gpu(args):
         ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
         ctx.Dassemble(fbgpu.FB_ALL)
 
-    # pinned host buffers for the end-to-end leg
     pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
     h_pos = pin(3 * st.natoms)
     h_pos[:] = st.ratom.ravel()
@@ -422,62 +359,160 @@ def run_gpu(args):
             ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
         ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
 
-    h2d = 3 * st.natoms * 8 + 2 * NB * 8
-    d2h = 4 * NB * 8 + 3 * st.natoms * 8
     timed = make_timer(torch, ctx, stream, flush, ws, local)
-
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         device_step()
-        e2e_step()
+        if e2e:
+            e2e_step()
         kernel_step()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ms, launches = timed(device_step, args.steps)
-    ms_e2e, _ = timed(e2e_step, args.steps)
-    clk = clocks.stop()
-    ms_k, _ = timed(kernel_step, args.steps, timing=True)
+    sampler = ClockSampler(local) if clocks else None
+    if sampler:
+        sampler.start()
+    ms, launches = timed(device_step, steps)
+    ms_e2e = timed(e2e_step, steps)[0] if e2e else None
+    clk = sampler.stop() if sampler else None
+    out = {k: ctx.blocks(k) for k in ("S", "T", "vna", "vnao")}
+    out["ftot"] = ctx.forces("ftot")
+    ms_k, _ = timed(kernel_step, steps, timing=True)
     ktimes = ctx.timing()
     ctx.set_timing(False)
+    return {"ms": ms, "ms_e2e": ms_e2e, "launches": launches, "ktimes": ktimes, "ms_k": ms_k, "clocks": clk,
+            "shapes": shapes, "out": out, "prec": PREC_NAME[prec]}
 
-    per_step = ms / args.steps
-    value = ws * P * args.steps / (ms * 1e-3)
-    e2e_value = ws * P * args.steps / (ms_e2e * 1e-3)
-    roof = roofline_for(ctx, ktimes, T, P, st.natoms, nZ, args.steps, args.prec)
+
+def max_abs_diffs(a, b):
+    """Largest |a - b| per output: blocks in eV, ftot in eV/Angstrom."""
+    return {k: float(np.abs(a[k] - b[k]).max()) for k in ("S", "T", "vna", "vnao", "ftot")}
+
+
+def run_gpu(args):
+    import torch
+    import fbgpu
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "batch256":
+        return run_batch(args, torch, fbgpu, ws, rank, local)
+    path, nZ, st = load_workload(args.workload)
+    ctx = fbgpu.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    P, T, NB = ctx.driver_neighbors()
+    nbm = ctx.neighbors()
+    norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
+    rho, cape = denmat_fast(nbm["neighn"], nbm["neigh_j"] - 1, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
+    d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
+    d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    prec_main = fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF
+    prec_other = fbgpu.FB_PREC_DF if prec_main == fbgpu.FB_PREC_FP64 else fbgpu.FB_PREC_FP64
+    common = (args, ctx, fbgpu, torch, stream, flush, ws, local, st, NB, rho, cape, d_rho, d_cape)
+    m = measure_single(*common, prec_main, args.steps, args.warmup, e2e=True, clocks=True,
+                       autotune=not args.no_autotune)
+    o = measure_single(*common, prec_other, args.steps, max(3, min(args.warmup, 3)), e2e=True,
+                       autotune=not args.no_autotune)
+    ctx.set_precision(prec_main)
+
+    per_step = m["ms"] / args.steps
+    value = ws * P * args.steps / (m["ms"] * 1e-3)
+    e2e_value = ws * P * args.steps / (m["ms_e2e"] * 1e-3)
+    h2d = 3 * st.natoms * 8 + 2 * NB * 8
+    d2h = 4 * NB * 8 + 3 * st.natoms * 8
+    roof = roofline_for(ctx, m["ktimes"], T, P, st.natoms, nZ, args.steps, m["prec"])
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f64 (three-center: double-float f32x2)",
+        "vs_baseline": None, "dtype": "f64" if m["prec"] == "fp64" else "f64 (three-center: double-float f32x2)",
         "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "natoms": st.natoms, "pairs": P, "triplets": T,
-                   "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
+                   "three_center_arithmetic": "fp64" if m["prec"] == "fp64" else "double-float (FP32 pipe)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MiB write)", "forces": True,
                    "step": "fb_neighbors + one CUDA graph launch (assembly + forces)",
-                   "launch_shapes": shapes, "autotuned": not args.no_autotune},
+                   "launch_shapes": m["shapes"], "autotuned": not args.no_autotune},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(ms_e2e / args.steps, 4)},
-        "gpu_launches": launches,
-        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
-        "separate_calls_ms_per_step": round(ms_k / args.steps, 4),
+                "ms_per_step": round(m["ms_e2e"] / args.steps, 4)},
+        "gpu_launches": m["launches"],
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in m["ktimes"].items() if v[1]},
+        "separate_calls_ms_per_step": round(m["ms_k"] / args.steps, 4),
         "roofline": roof,
-        "clocks": clk,
+        "clocks": m["clocks"],
     }
+    # the same step with the other precision of the three-center kernels
+    line["double_float" if o["prec"] == "df" else "fp64_path"] = {
+        "what": ("three-center kernels in double-float (f32 pairs, 48-bit significand) on the FP32 pipe; every "
+                 "data-selecting decision in FP64") if o["prec"] == "df" else "every kernel in FP64",
+        "ms_per_step": round(o["ms"] / args.steps, 4), "value": round(ws * P * args.steps / (o["ms"] * 1e-3), 1),
+        "unit": UNIT, "e2e": {"value": round(ws * P * args.steps / (o["ms_e2e"] * 1e-3), 1),
+                              "ms_per_step": round(o["ms_e2e"] / args.steps, 4)},
+        "speedup_vs_headline": round(m["ms"] / o["ms"], 4),
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in o["ktimes"].items() if v[1]},
+        "roofline": roofline_for(ctx, o["ktimes"], T, P, st.natoms, nZ, args.steps, o["prec"]),
+        "launch_shapes": o["shapes"],
+        "max_abs_diff_vs_headline": max_abs_diffs(o["out"], m["out"])}
     if rank == 0:
         line["bloch"] = bloch_measure(ctx, torch, stream, local)
         line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
         line["vnl"] = vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=args.no_cpu)
         line["vxc"] = vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=args.no_cpu)
     if args.mlp_epochs > 0:
+        ctx.set_precision(prec_main)
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
+    if rank == 0 and args.extra_workloads:
+        line["workloads"] = {}
+        for name in args.extra_workloads.split(","):
+            if name and name != args.workload:
+                line["workloads"][name] = (measure_batch_extra(args, torch, fbgpu, local) if name == "batch256"
+                                           else measure_other_workload(args, name, fbgpu, torch, stream, flush,
+                                                                       local))
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(args.workload, path, nZ, st, P)
+        cb, ref = cpu_baseline(args.workload, path, nZ, st, P, keep=True)
+        line["cpu_baseline"] = cb
+        if ref is not None:
+            line["parity_vs_oracle"] = {
+                "what": "max |GPU - oracle| in this run, same structure and density matrices (eV, eV/Angstrom)",
+                m["prec"]: max_abs_diffs(m["out"], ref), o["prec"]: max_abs_diffs(o["out"], ref),
+                "tolerance": 1e-10}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def measure_other_workload(args, name, fbgpu, torch, stream, flush, local):
+    """Device step of another single-structure workload at both precisions
+    (neighbors + one graph launch of assembly and forces)."""
+    path, nZ, st = load_workload(name)
+    ctx = fbgpu.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    P, T, NB = ctx.driver_neighbors()
+    nbm = ctx.neighbors()
+    norb_of = np.array([ctx.norb_species[k - 1] for k in st.imass])
+    rho, cape = denmat_fast(nbm["neighn"], nbm["neigh_j"] - 1, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
+    d_rho = torch.from_numpy(rho).to(f"cuda:{local}")
+    d_cape = torch.from_numpy(cape).to(f"cuda:{local}")
+    out = {"workload": WORKLOADS[name], "natoms": st.natoms, "pairs": P, "triplets": T}
+    res = {}
+    for prec in (fbgpu.FB_PREC_FP64, fbgpu.FB_PREC_DF):
+        r = measure_single(args, ctx, fbgpu, torch, stream, flush, 1, local, st, NB, rho, cape, d_rho, d_cape,
+                           prec, args.steps, 3, e2e=False, autotune=not args.no_autotune)
+        res[r["prec"]] = r
+        out[r["prec"]] = {"ms_per_step": round(r["ms"] / args.steps, 4),
+                          "value": round(P * args.steps / (r["ms"] * 1e-3), 1), "unit": UNIT,
+                          "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in r["ktimes"].items()
+                                                  if v[1]}}
+    out["df_max_abs_diff_vs_fp64"] = max_abs_diffs(res["df"]["out"], res["fp64"]["out"])
+    ctx.close()
+    return out
 
 
 def bloch_measure(ctx, torch, stream, local, reps=5):
@@ -780,9 +815,10 @@ def batch_inputs(structs, ctx, fbgpu):
     return denmat_fast(nbm["neighn"], jg, nbm["neigh_back"] - 1, nbm["blk_off"], norb_of)
 
 
-def run_batch(args, torch, fbgpu, ws, rank, local):
-    """Config: 256 structures of uneven size in one batch, against the same
-    structures assembled one at a time."""
+def measure_batch(args, torch, fbgpu, ws, local, prec, steps, warmup, e2e=True, clocks=False, seq_steps=3):
+    """Config 4: 256 structures of uneven size in one batch (one neighbor
+    build + one graph launch per step), against the same structures
+    assembled one at a time through the single-structure calls."""
     from fbgpu import synth
     path = synth.fdata_dir_for("batch256", root=fdata_root())
     nZ = [s.nZ for s in synth.species_for("batch256")]
@@ -791,7 +827,7 @@ def run_batch(args, torch, fbgpu, ws, rank, local):
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
     ctx.read_Fdata(path, nZ)
-    ctx.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
+    ctx.set_precision(prec)
     ctx.set_batch([(st.ratom, st.imass, st.lattice, 0) for st in structs])
     P, T, NB = ctx.driver_neighbors()
     off = ctx.batch_offsets()
@@ -814,7 +850,7 @@ def run_batch(args, torch, fbgpu, ws, rank, local):
     seq = fbgpu.Context(local)
     seq.set_stream(stream.cuda_stream)
     seq.read_Fdata(path, nZ)
-    seq.set_precision(fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF)
+    seq.set_precision(prec)
     bo = off["block"]
 
     def sequential_step():
@@ -843,72 +879,117 @@ def run_batch(args, torch, fbgpu, ws, rank, local):
             ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
         ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
 
-    h2d = 3 * natoms * 8 + 2 * NB * 8
-    d2h = 4 * NB * 8 + 3 * natoms * 8
     timed = make_timer(torch, ctx, stream, flush, ws, local)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch_step()
-        e2e_step()
+        if e2e:
+            e2e_step()
     sequential_step()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ms, launches = timed(batch_step, args.steps)
-    ms_e2e, _ = timed(e2e_step, args.steps)
-    clk = clocks.stop()
-    seq_steps = max(1, min(args.steps, 3))
+    sampler = ClockSampler(local) if clocks else None
+    if sampler:
+        sampler.start()
+    ms, launches = timed(batch_step, steps)
+    ms_e2e = timed(e2e_step, steps)[0] if e2e else None
+    clk = sampler.stop() if sampler else None
+    ftot_batch = ctx.forces("ftot")
     ms_seq, seq_launches = make_timer(torch, seq, stream, flush, ws, local)(sequential_step, seq_steps)
-    # per-kernel times of the batch through the separate calls
+    # the last structure of the sequential pass against its slice of the batch
+    last = len(structs) - 1
+    f_last = seq.forces("ftot")
+    seq_diff = float(np.abs(f_last - ftot_batch[3 * int(off["atom"][last]):3 * int(off["atom"][last + 1])]).max())
+
     def kernel_step():
         ctx.driver_neighbors()
         ctx.assemble(fbgpu.FB_ALL)
         ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
         ctx.Dassemble(fbgpu.FB_ALL)
     kernel_step()
-    ms_k, _ = timed(kernel_step, args.steps, timing=True)
+    ms_k, _ = timed(kernel_step, steps, timing=True)
     ktimes = ctx.timing()
     ctx.set_timing(False)
-    roof = roofline_for(ctx, ktimes, T, P, natoms, nZ, args.steps, args.prec)
-    per_step = ms / args.steps
+    roof = roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, PREC_NAME[prec])
     sizes = np.diff(off["atom"])
+    seq.close()
+    ctx.close()
+    return {"structs": structs, "path": path, "nZ": nZ, "P": P, "T": T, "NB": NB, "natoms": natoms,
+            "sizes": sizes, "ms": ms, "ms_e2e": ms_e2e, "launches": launches, "clocks": clk, "shapes": shapes,
+            "ms_seq": ms_seq, "seq_steps": seq_steps, "seq_launches": seq_launches, "ktimes": ktimes,
+            "ms_k": ms_k, "roofline": roof, "seq_vs_batch_max_abs_dftot": seq_diff, "prec": PREC_NAME[prec],
+            "ftot": ftot_batch}
+
+
+def measure_batch_extra(args, torch, fbgpu, local):
+    """The batch configuration as an extra key of the single-structure
+    line, at both precisions."""
+    out = {"workload": WORKLOADS["batch256"]}
+    ft = {}
+    for prec in (fbgpu.FB_PREC_FP64, fbgpu.FB_PREC_DF):
+        r = measure_batch(args, torch, fbgpu, 1, local, prec, args.steps, 3, e2e=False)
+        out.update(structures=256, natoms=r["natoms"], pairs=r["P"], triplets=r["T"],
+                   atoms_min_max=[int(r["sizes"].min()), int(r["sizes"].max())])
+        ft[r["prec"]] = r["ftot"]
+        per = r["ms"] / args.steps
+        seq = r["ms_seq"] / r["seq_steps"]
+        out[r["prec"]] = {"batch_ms_per_step": round(per, 4),
+                          "value": round(r["P"] * args.steps / (r["ms"] * 1e-3), 1), "unit": UNIT,
+                          "sequential_ms_per_step": round(seq, 4), "batch_speedup": round(seq / per, 3),
+                          "sequential_launches_per_step": r["seq_launches"] // r["seq_steps"],
+                          "batch_launches_per_step": r["launches"] // args.steps,
+                          "last_structure_sequential_vs_batch_max_abs_dftot": r["seq_vs_batch_max_abs_dftot"],
+                          "launch_shapes": r["shapes"]}
+    out["df_max_abs_dftot_vs_fp64"] = float(np.abs(ft["df"] - ft["fp64"]).max())
+    return out
+
+
+def run_batch(args, torch, fbgpu, ws, rank, local):
+    """Config: 256 structures of uneven size in one batch, against the same
+    structures assembled one at a time."""
+    prec = fbgpu.FB_PREC_FP64 if args.prec == "fp64" else fbgpu.FB_PREC_DF
+    r = measure_batch(args, torch, fbgpu, ws, local, prec, args.steps, args.warmup, e2e=True, clocks=True,
+                      seq_steps=max(1, min(args.steps, 3)))
+    P, T, NB, natoms = r["P"], r["T"], r["NB"], r["natoms"]
+    h2d = 3 * natoms * 8 + 2 * NB * 8
+    d2h = 4 * NB * 8 + 3 * natoms * 8
+    per_step = r["ms"] / args.steps
+    ms_seq, seq_steps = r["ms_seq"], r["seq_steps"]
     line = {
-        "metric": METRIC, "value": round(ws * P * args.steps / (ms * 1e-3), 1), "unit": UNIT, "n_gpus": ws,
+        "metric": METRIC, "value": round(ws * P * args.steps / (r["ms"] * 1e-3), 1), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS["batch256"], "structures": len(structs), "natoms": natoms,
-                   "atoms_min_max": [int(sizes.min()), int(sizes.max())], "pairs": P, "triplets": T,
-                   "three_center_arithmetic": "double-float (FP32 pipe)" if args.prec == "df" else "fp64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if r["prec"] == "fp64" else "f64 (three-center: double-float f32x2)", "data": "synthetic",
+        "config": {"workload": WORKLOADS["batch256"], "structures": len(r["structs"]), "natoms": natoms,
+                   "atoms_min_max": [int(r["sizes"].min()), int(r["sizes"].max())], "pairs": P, "triplets": T,
+                   "three_center_arithmetic": "double-float (FP32 pipe)" if r["prec"] == "df" else "fp64",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 and flushed between steps (256 MiB write)", "forces": True,
                    "step": "fb_neighbors over the batch + one CUDA graph launch (assembly + forces)",
-                   "launch_shapes": shapes, "autotuned": not args.no_autotune},
-        "e2e": {"value": round(ws * P * args.steps / (ms_e2e * 1e-3), 1), "unit": UNIT,
+                   "launch_shapes": r["shapes"], "autotuned": not args.no_autotune},
+        "e2e": {"value": round(ws * P * args.steps / (r["ms_e2e"] * 1e-3), 1), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(ms_e2e / args.steps, 4)},
+                "ms_per_step": round(r["ms_e2e"] / args.steps, 4)},
         "sequential": {"ms_per_step": round(ms_seq / seq_steps, 4),
                        "value": round(P * seq_steps / (ms_seq * 1e-3), 1), "unit": UNIT,
-                       "gpu_launches_per_step": seq_launches // seq_steps,
+                       "gpu_launches_per_step": r["seq_launches"] // seq_steps,
                        "how": "the 256 structures one after another: fb_set_structure + fb_neighbors + "
                               "fb_assemble + fb_dassemble each (device-resident density matrices)",
-                       "batch_speedup": round((ms_seq / seq_steps) / per_step, 3)},
-        "gpu_launches": launches,
-        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
-        "separate_calls_ms_per_step": round(ms_k / args.steps, 4),
-        "roofline": roof,
-        "clocks": clk,
+                       "batch_speedup": round((ms_seq / seq_steps) / per_step, 3),
+                       "last_structure_max_abs_dftot_vs_batch": r["seq_vs_batch_max_abs_dftot"]},
+        "gpu_launches": r["launches"],
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in r["ktimes"].items() if v[1]},
+        "separate_calls_ms_per_step": round(r["ms_k"] / args.steps, 4),
+        "roofline": r["roofline"],
+        "clocks": r["clocks"],
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_batch(path, nZ, structs, P)
+        line["cpu_baseline"] = cpu_baseline_batch(r["path"], r["nZ"], r["structs"], P)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    seq.close()
-    ctx.close()
 
 
 def cpu_baseline_batch(path, nZ, structs, P_total, nsample=16):
     """The oracle on a bounded sample of the batch (the first nsample
     structures), scaled to blocks/s."""
     from oracle import oracle as orc
-    from conftest import symmetric_denmat
     cores = os.cpu_count() or 1
     fd = orc.Fdata(path, nZ)
     t_tot, p_tot = 0.0, 0
@@ -918,7 +999,7 @@ def cpu_baseline_batch(path, nZ, structs, P_total, nsample=16):
         s.assemble()
         t1 = time.perf_counter()
         norb = np.array([fd.norb(int(k)) for k in st.imass])
-        rho, cape = symmetric_denmat(s, norb, 42)
+        rho, cape = denmat_fast(np.diff(s.pair_off), s.neigh_j[:s.npairs], s.neigh_back[:s.npairs], s.blk_off, norb)
         t2 = time.perf_counter()
         s.dassemble(rho, cape)
         t3 = time.perf_counter()
@@ -929,31 +1010,37 @@ def cpu_baseline_batch(path, nZ, structs, P_total, nsample=16):
                       "%.3f s" % (nsample, p_tot, t_tot)}
 
 
-def cpu_baseline(workload, path, nZ, st, P_expect=None, steps=1):
+def cpu_baseline(workload, path, nZ, st, P_expect=None, steps=1, keep=False):
     """The oracle (C restatement, OpenMP on every host core) on one full step
-    of the same workload: neighbors, 2c + 3c assembly, forces."""
+    of the same workload: neighbors, 2c + 3c assembly, forces.  keep: also
+    return the last step's S, T, vna, vnao and ftot (same density matrices
+    as the GPU step: the same generator over bit-identical neighbor maps)."""
     from oracle import oracle as orc
-    from conftest import symmetric_denmat
     cores = os.cpu_count() or 1
     fd = orc.Fdata(path, nZ)
     times = []
     P = None
+    ref = None
     for _ in range(steps):
         t0 = time.perf_counter()
         s = orc.System(fd, st.ratom, st.imass, st.lattice, threads=cores).neighbors()
-        s.assemble()
+        blocks = s.assemble()
         t1 = time.perf_counter()
         norb = np.array([fd.norb(int(k)) for k in st.imass])
-        rho, cape = symmetric_denmat(s, norb, 42)
+        rho, cape = denmat_fast(np.diff(s.pair_off), s.neigh_j[:s.npairs], s.neigh_back[:s.npairs], s.blk_off, norb)
         t2 = time.perf_counter()
-        s.dassemble(rho, cape)
+        d = s.dassemble(rho, cape)
         t3 = time.perf_counter()
         times.append((t1 - t0) + (t3 - t2))
         P = s.npairs
+        if keep:
+            ref = dict(zip(("S", "T", "vna", "vnao"), blocks))
+            ref["ftot"] = d["ftot"]
     t = float(np.median(times))
-    return {"value": round(P / t, 1), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d full step(s) of the same workload (neighbors + 2c + 3c assembly + forces), median "
-                      "%.3f s/step" % (steps, t)}
+    rec = {"value": round(P / t, 1), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": "%d full step(s) of the same workload (neighbors + 2c + 3c assembly + forces), median "
+                     "%.3f s/step" % (steps, t)}
+    return (rec, ref) if keep else rec
 
 
 def run_reference(args):
@@ -1005,14 +1092,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fbgpu", choices=["fbgpu", "reference"])
-    ap.add_argument("--workload", default="si512", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sic4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--extra-workloads", default="si512,cho1536,batch256",
+                    help="comma-separated workloads also measured (both precisions) as extra keys of the line")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--mlp-epochs", type=int, default=12,
                     help="train the MLP-3c surrogate this many epochs over 2^22 samples and compare it with the "
                          "table path (0: skip)")
-    ap.add_argument("--prec", default="df", choices=["df", "fp64"],
-                    help="three-center arithmetic: double-float on the FP32 pipe (default) or FP64")
+    ap.add_argument("--prec", default="fp64", choices=["df", "fp64"],
+                    help="three-center arithmetic of the headline: FP64 (default) or double-float on the FP32 pipe "
+                         "(the other one is measured too, as an extra key)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -493,21 +493,27 @@ int fb_get_timing(fb_ctx *ctx, const char *kernel, double *total_ms,
  * or an MD loop that must not call the CUDA allocator between steps (an
  * allocation synchronizes the device and can fail once memory fragments).
  *
- * Computes what fb_dassemble(ctx, FB_ALL) + fb_get_forces(ctx, FB_F_TOT)
- * compute, for the structure and neighbor maps already on the context:
+ * Computes the Harris forces that fb_dassemble(ctx, FB_ALL) +
+ * fb_get_forces(ctx, FB_F_TOT) compute, for the structure and neighbor maps
+ * already on the context, from the density matrices passed here (not the
+ * ones fb_set_denmat stored on the context):
  *   rho_dev, cape_dev  device pointers, nblock doubles each, block layout;
  *                      cape_dev may be NULL (no Pulay term)
  *   ftot_dev           device pointer, 3*natoms doubles, written
+ * It always runs the FP64 three-center kernel from the tables, whatever
+ * fb_set_precision and the MLP-3c mode say (on GB300 that kernel is about
+ * 2.7x slower than the double-float one that fb_dassemble runs by default).
  * The call makes no cudaMalloc, cudaFree or other allocating call.  Its
  * intermediate per-pair and per-atom terms live in one statically sized
  * device array of the library, which every GPU that loads the library holds
  * until the process exits (8.25 MiB); systems with more than
  * FB_NOALLOC_MAX_PAIRS pairs or FB_NOALLOC_MAX_ATOMS atoms are rejected with
- * FB_ERR_CAPACITY.  All calls share that array and it keeps the last call's
- * contents, so calls that overlap on the GPU (two streams, two contexts on
- * one device) race and must be serialized by the caller.  The first call on
- * each device looks up the array's device address; make that first call
- * before any stream capture.  Returns after the work completes. */
+ * FB_ERR_CAPACITY.  fb_create looks up that array's device address for its
+ * device, so the module that holds the array is loaded then, not inside
+ * this call.  All calls share the array and it keeps the last call's
+ * contents (the call clears what it accumulates), so calls that overlap on
+ * the GPU (two streams, two contexts on one device) race and must be
+ * serialized by the caller.  Returns after the work completes. */
 #define FB_NOALLOC_MAX_PAIRS 65536
 #define FB_NOALLOC_MAX_ATOMS 16384
 int fb_dassemble_noalloc(fb_ctx *ctx, const double *rho_dev,

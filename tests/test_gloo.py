@@ -61,3 +61,33 @@ def test_shard_covers_each_item_once():
         assert got == list(range(37))
     with pytest.raises(ValueError):
         batch.shard(4, 2, 2)
+
+
+def test_weighted_shard_balances_the_batch():
+    """Longest-first sharding of the 256-structure batch by its three-center
+    work estimate: every item once, the same partition on every rank, and
+    the largest rank load within the greedy rule's bound (at most the mean
+    load plus the largest item), well below the round-robin split's."""
+    from fbgpu import batch, synth
+    structs = synth.batch_structures(256)
+    w = np.array([batch.work_estimate(s.ratom, s.lattice) for s in structs])
+    for world in (2, 4, 8):
+        parts = [batch.shard(len(w), r, world, weights=w) for r in range(world)]
+        assert sorted(i for p in parts for i in p) == list(range(len(w)))
+        loads = np.array([w[p].sum() for p in parts])
+        assert loads.max() <= w.sum() / world + w.max() + 1e-9
+        rr = np.array([w[batch.shard(len(w), r, world)].sum() for r in range(world)])
+        assert loads.max() <= rr.max()
+        assert loads.max() / loads.mean() < 1.02
+
+
+def test_work_estimate_tracks_triplets(fdata_root):
+    """The estimate orders structures like their actual triplet counts."""
+    from fbgpu import batch, synth
+    from oracle import oracle as orc
+    structs = synth.batch_structures(12)
+    fd = orc.Fdata(synth.fdata_dir_for("batch256", root=fdata_root), [14, 6])
+    est = np.array([batch.work_estimate(s.ratom, s.lattice) for s in structs])
+    trip = np.array([orc.System(fd, s.ratom, s.imass, s.lattice).neighbors().ntrip for s in structs])
+    ratio = trip / est
+    assert ratio.max() / ratio.min() < 1.5

@@ -1,0 +1,79 @@
+"""GPU parity at the full sizes of the two largest single-structure workloads.
+
+SiC4096 (8x8x8 zincblende SiC, 4,096 atoms, 225,214 pairs, 5.12 M common
+-neighbor triplets) and C/H/O 1536 (mixed 4- and 1-orbital blocks, 60 k
+pairs, 1.0 M triplets), through the C ABI, against the oracle run on every
+host core: the neighbor maps and common-neighbor lists bit-exact, and S, T,
+vna, vnao, ftot and its terms within 1e-10 eV (eV/Angstrom) per element, in
+both precision modes of the three-center kernels.  This checks the triplet
+binning, the atomics and the launch shapes at the sizes the benchmark runs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import workload
+from oracle import oracle as orc
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+TOL = 1e-10
+PRECS = [0, 1]  # FB_PREC_FP64, FB_PREC_DF
+
+
+def _full_size(name, fdata_root):
+    import fbgpu
+    from fbgpu import synth
+    path, nZ, st = workload(name, fdata_root)
+    fd = orc.Fdata(path, nZ)
+    s = orc.System(fd, st.ratom, st.imass, st.lattice, threads=os.cpu_count() or 1).neighbors()
+    ref_blocks = s.assemble()
+    norb = np.array([fd.norb(int(k)) for k in st.imass])
+    rho, cape = synth.symmetric_denmat(np.diff(s.pair_off), s.neigh_j[:s.npairs], s.neigh_back[:s.npairs],
+                                       s.blk_off, norb, seed=77)
+    ref_f = s.dassemble(rho, cape)
+    ctx = fbgpu.Context(0)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    assert ctx.driver_neighbors() == (s.npairs, s.ntrip, s.nblock)
+    P, T = s.npairs, s.ntrip
+    nb = ctx.neighbors()
+    assert np.array_equal(nb["neighn"], np.diff(s.pair_off))
+    assert np.array_equal(nb["neigh_j"], s.neigh_j[:P] + 1)
+    assert np.array_equal(nb["neigh_b"], s.neigh_b[:P])
+    assert np.array_equal(nb["neigh_back"], s.neigh_back[:P] + 1)
+    assert np.array_equal(nb["neigh_self"], s.neigh_self + 1)
+    assert np.array_equal(nb["blk_off"], s.blk_off)
+    cm = ctx.common_neighbors()
+    assert np.array_equal(cm["ncommon"], np.diff(s.trip_off))
+    assert np.array_equal(cm["iatom_common_j"], s.ci_j[:T] + 1)
+    assert np.array_equal(cm["iatom_common_b"], s.ci_b[:T])
+    assert np.array_equal(cm["jatom_common_j"], s.cj_j[:T] + 1)
+    assert np.array_equal(cm["jatom_common_b"], s.cj_b[:T])
+    assert np.array_equal(cm["neigh_common"], s.cneigh[:T] + 1)
+    for prec in PRECS:
+        ctx.set_precision(prec)
+        ctx.assemble()
+        for key, r in zip(("S", "T", "vna", "vnao"), ref_blocks):
+            err = np.abs(ctx.blocks(key) - r).max()
+            assert err <= TOL, "%s prec %d %s max |diff| %.3e" % (name, prec, key, err)
+        ctx.set_denmat(rho, cape)
+        ctx.Dassemble()
+        for key in ("ftot", "kinetic", "vna", "pulay", "f3naa", "f3nab", "f3nac", "vna_ontop", "vna_atom"):
+            err = np.abs(ctx.forces(key) - ref_f[key]).max()
+            assert err <= TOL, "%s prec %d %s max |diff| %.3e" % (name, prec, key, err)
+    # the graph step (autotuned launch shapes) gives the same forces
+    ctx.autotune(fbgpu.FB_ALL | fbgpu.FB_FORCES, reps=1)
+    ctx.assemble_graph(fbgpu.FB_ALL | fbgpu.FB_FORCES)
+    assert np.abs(ctx.forces("ftot") - ref_f["ftot"]).max() <= TOL
+    assert np.abs(ctx.blocks("vna") - ref_blocks[2]).max() <= TOL
+    ctx.close()
+
+
+def test_sic4096_full_size_parity(fdata_root):
+    _full_size("sic4096", fdata_root)
+
+
+def test_cho1536_full_size_parity(fdata_root):
+    _full_size("cho1536", fdata_root)

@@ -282,3 +282,20 @@ def test_cluster_forces_are_minus_gradient(fdata_root):
             rm[i, k] -= h
             g = (energy(rp) - energy(rm)) / (2 * h)
             assert abs(-g - f[i, k]) < 1e-5 * max(1.0, abs(g)), (i, k, -g, f[i, k])
+
+
+def test_synthetic_denmat_symmetric_across_neigh_back(fdata_root):
+    """The vectorised density-matrix generator the benchmark and the
+    full-size tests use: rho_ij(mu, nu) = rho_ji(nu, mu) for every pair of
+    mixed-size blocks, self blocks symmetric."""
+    fd, s, st, norb = _system("cho_small", fdata_root)
+    rho, cape = synth.symmetric_denmat(np.diff(s.pair_off), s.neigh_j[:s.npairs], s.neigh_back[:s.npairs],
+                                       s.blk_off, norb, seed=3)
+    for i in range(len(norb)):
+        for p in range(s.pair_off[i], s.pair_off[i + 1]):
+            j = s.neigh_j[p]
+            q = s.pair_off[j] + s.neigh_back[p]
+            for m in (rho, cape):
+                a = m[s.blk_off[p]:s.blk_off[p + 1]].reshape(norb[j], norb[i]).T
+                b = m[s.blk_off[q]:s.blk_off[q + 1]].reshape(norb[i], norb[j]).T
+                assert np.array_equal(a, b.T)

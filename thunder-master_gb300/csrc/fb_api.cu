@@ -233,6 +233,8 @@ static int status_error(fb_ctx *ctx, unsigned st) {
   return FB_OK;
 }
 
+static int noalloc_scratch(fb_ctx *ctx, double **out);
+
 extern "C" {
 
 const char *fb_version(void) { return "fbgpu 0.1 sm_103a fp64"; }
@@ -258,6 +260,14 @@ int fb_create(int device, fb_ctx **out) {
     return FB_ERR_CUDA;
   }
   for (int k = 0; k < TK_N; k++) ctx->cfg[k] = KCfg{128, 0, 1, ctx->nsm};
+  // the device address of fb_dassemble_noalloc's static scratch, looked up
+  // here so that the entry point itself never loads a module or reserves
+  // memory
+  double *scr = nullptr;
+  if (noalloc_scratch(ctx, &scr) != FB_OK) {
+    fb_destroy(ctx);
+    return FB_ERR_CUDA;
+  }
   *out = ctx;
   return FB_OK;
 }
@@ -2120,7 +2130,7 @@ static __device__ __align__(256) double
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_ptr[128];  // device address per device ordinal
 
-// once per device, with that device current
+// once per device, with that device current (fb_create calls it)
 static int noalloc_scratch(fb_ctx *ctx, double **out) {
   if (ctx->device < 0 || ctx->device >= 128) return fail(ctx, FB_ERR_ARG, "device ordinal %d", ctx->device);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);

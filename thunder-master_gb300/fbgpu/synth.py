@@ -715,3 +715,40 @@ def fdata_dir_for(workload, root=None, dogs=False, vxc=False):
         with open(stamp, "w") as f:
             f.write("ok\n")
     return path
+
+
+def symmetric_denmat(neighn, neigh_j0, neigh_back0, blk_off, norb_of, seed=42):
+    """Seeded stand-ins for the density matrices rho and cape that the
+    solver supplies, symmetric across neigh_back as the solver's are:
+    rho_ji(nu, mu) = rho_ij(mu, nu).  neigh_j0 and neigh_back0 are 0-based
+    (global atom index, position in j's list); blocks are column-major
+    norb_i x norb_j at blk_off."""
+    rng = np.random.default_rng(seed)
+    NB = int(blk_off[-1])
+    raw_r = rng.normal(0.0, 0.1, NB)
+    raw_c = rng.normal(0.0, 0.05, NB)
+    neigh_j0 = np.asarray(neigh_j0, np.int64)
+    neigh_back0 = np.asarray(neigh_back0, np.int64)
+    blk_off = np.asarray(blk_off, np.int64)
+    norb_of = np.asarray(norb_of, np.int64)
+    P = len(neigh_j0)
+    pair_off = np.concatenate([[0], np.cumsum(neighn)]).astype(np.int64)
+    owner = np.repeat(np.arange(len(neighn)), neighn)
+    ni = norb_of[owner]
+    nj = norb_of[neigh_j0]
+    q = pair_off[neigh_j0] + neigh_back0
+    # every element e of pair p: (mu, nu) column-major, mu fastest
+    size = ni * nj
+    pe = np.repeat(np.arange(P), size)
+    loc = np.arange(NB) - np.repeat(blk_off[:P], size)
+    mu = loc % np.repeat(ni, size)
+    nu = loc // np.repeat(ni, size)
+    # the mirrored element (nu, mu) of pair q (an nj x ni block)
+    mirror = np.repeat(blk_off[q], size) + nu + np.repeat(nj, size) * mu
+    lead = pe <= np.repeat(q, size)  # the pair with the smaller index supplies the values
+    rho = np.where(lead, raw_r, raw_r[mirror])
+    cape = np.where(lead, raw_c, raw_c[mirror])
+    selfp = pe == np.repeat(q, size)
+    rho[selfp] = 0.5 * (raw_r[selfp] + raw_r[mirror[selfp]])
+    cape[selfp] = 0.5 * (raw_c[selfp] + raw_c[mirror[selfp]])
+    return rho, cape
