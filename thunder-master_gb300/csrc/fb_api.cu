@@ -45,6 +45,10 @@ static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c
 struct fb_ctx {
   int device = 0;
   cudaStream_t own = nullptr, stream = nullptr;
+  // set while a graph of a value + force pass is captured: the force pass's
+  // three-center table kernel also adds the value-pass vna terms, and the
+  // value pass skips its three-center table kernel
+  bool fuse3c = false;
   std::string err;
   long long launches = 0;
   // Fdata
@@ -1439,7 +1443,9 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     AsmArgs at = a;
     at.tperm = a.tperm + nm;
     at.ntrip = a.ntrip - nm;
-    if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
+    if (ctx->fuse3c) {
+      // the force pass adds these triplets' value terms (enqueue_dassemble)
+    } else if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
     else if (use_df_dogs(ctx)) KL(KT_ASM3C, launch_assemble_3c_dogs_df(at, ctx->stream));
     else KL(KT_ASM3C, launch_assemble_3c(at, ctx->stream));
     if (nm > 0) {
@@ -1715,6 +1721,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
     AsmArgs at = a;
     at.tperm = a.tperm + nm;
     at.ntrip = a.ntrip - nm;
+    at.fuse_value = ctx->fuse3c;
     if (use_df(ctx) || use_df_dogs(ctx) || nm > 0) KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
     if (use_df(ctx)) KL(KT_DASM3C, launch_dassemble_3c_df(at, ctx->stream));
     else if (use_df_dogs(ctx)) KL(KT_DASM3C, launch_dassemble_3c_dogs_df(at, ctx->stream));
@@ -1815,8 +1822,11 @@ static int capture_graph(fb_ctx *ctx, unsigned what) {
   int st = FB_OK;
   if (cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream) != cudaSuccess)
     st = fail(ctx, FB_ERR_CUDA, "graph capture: status clear");
+  // one interpolation per triplet when the step computes values and forces
+  ctx->fuse3c = (what & FB_VNA3C) && (what & FB_FORCES) && ctx->theory == FB_THEORY_HARRIS;
   if (!st && (what & (FB_ALL | FB_DIPOLE | FB_SVNL | FB_VNL2C | FB_VNL3C | FB_EWALD | FB_VXC))) st = enqueue_assemble(ctx, what);
   if (!st && (what & FB_FORCES)) st = enqueue_dassemble(ctx, what);
+  ctx->fuse3c = false;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   ctx->timing = timing;

@@ -228,8 +228,48 @@ __device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, 
       }
     return;
   }
-  // METHOD 3, 16-point bicubic (:425-481, :721-798) as a tensor product of
-  // 4-point Lagrange weights
+  const double *Tb = tab + (node0 - nx - 1) * NTHETA * NE;  // node (ix-1, iy-1)
+  if constexpr (DERIV) {
+    // METHOD 3 with derivatives (:721-798).  The interpolation is linear in
+    // the table values, so the Legendre sums are taken first at each of the
+    // 16 stencil nodes, g = sum_th P_th T_th and gp = sum_th P'_th T_th, and
+    // the stencil weights then contract g (value, d/dx, d/dy) and gp
+    // (d/dcos): 11 FP64 FMAs per node and element instead of 15 + 20/16
+    // for the per-theta contraction.  The sums differ from the reference's
+    // order only by rounding.
+    double wx[4], wy[4], dwx[4], dwy[4];
+    lagrange4(px, wx, dwx);
+    lagrange4(py, wy, dwy);
+    double idx = 1.0 / cell.dx, idy = 1.0 / cell.dy;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      dwx[k] *= idx;
+      dwy[k] *= idy;
+    }
+#pragma unroll 1
+    for (int j = 0; j < 4; j++) {
+      double wyj = wy[j], dwyj = dwy[j];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        double W = wx[k] * wyj, Wx = dwx[k] * wyj, Wy = wx[k] * dwyj;
+        const double *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE;
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          double t0 = __ldg(Tn + e), t1 = __ldg(Tn + NE + e), t2 = __ldg(Tn + 2 * NE + e);
+          double t3 = __ldg(Tn + 3 * NE + e), t4 = __ldg(Tn + 4 * NE + e);
+          double g = fma(pl[4], t4, fma(pl[3], t3, fma(pl[2], t2, fma(pl[1], t1, t0))));
+          double gp = fma(dpl[4], t4, fma(dpl[3], t3, fma(dpl[2], t2, t1)));
+          F[e] = fma(W, g, F[e]);
+          DxF[e] = fma(Wx, g, DxF[e]);
+          DyF[e] = fma(Wy, g, DyF[e]);
+          DpF[e] = fma(W, gp, DpF[e]);
+        }
+      }
+    }
+    return;
+  }
+  // METHOD 3, 16-point bicubic (:425-481) as a tensor product of 4-point
+  // Lagrange weights
   double wx[4], wy[4], dwx[4], dwy[4];
   lagrange4(px, wx, DERIV ? dwx : nullptr);
   lagrange4(py, wy, DERIV ? dwy : nullptr);
@@ -244,7 +284,6 @@ __device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, 
         Wy[4 * j + k] = wx[k] * dwy[j] / cell.dy;
       }
     }
-  const double *Tb = tab + (node0 - nx - 1) * NTHETA * NE;  // node (ix-1, iy-1)
 #pragma unroll
   for (int th = 0; th < NTHETA; th++) {
     double I[NE], Ix[NE], Iy[NE];

@@ -13,7 +13,11 @@ namespace fb {
 // neutral term (scaled by stinky); the smoother and monopole terms are
 // contracted with rho through the per-pair sums of rho S, rho dip, rho dS
 // and rho ddip the 2c kernel left in dogs_ps.
-template <int PA, int PB, bool HASD, bool DOGS>
+// FUSE (Harris only): the same triplet's value-pass term of assemble_vna_3c
+// (j.ASSEMBLERS/M_assemble_3c_Harris.f90:82-227), rot(F sint^mvalue) P_eq2
+// into the vna block (i, mneigh), is added from the F this kernel
+// interpolates anyway, so a step with forces interpolates every triplet once.
+template <int PA, int PB, bool HASD, bool DOGS, bool FUSE>
 __device__ void trip_3c_force(const Ctx3c &c, int t) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
@@ -109,6 +113,13 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   });
   RotM R;
   twister<HASD>(g.e, R);
+  if constexpr (FUSE) {
+    double X[NA * NB];
+    rotate_plan<PA, PB, K3C>(R, M, X);
+    double *dst = c.vb + c.blk_off[c.tdst[t]];
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, X[q] * P_eq2);
+  }
   DRotM DA, DB;
   dtwister<HASD>(g.e, dA, DA);
   dtwister<HASD>(g.e, dB, DB);
@@ -163,36 +174,39 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   }
 }
 
-template <bool HASD, bool DOGS>
+template <bool HASD, bool DOGS, bool FUSE>
 __global__ void __launch_bounds__(256) k_dassemble_3c(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
     if (c.tperm) t = c.tperm[t];
     int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
     int key = pa * 3 + pb;
     switch (key) {
-      case PAT_SP * 3 + PAT_SP: trip_3c_force<PAT_SP, PAT_SP, HASD, DOGS>(c, t); break;
-      case PAT_SP * 3 + PAT_S: trip_3c_force<PAT_SP, PAT_S, HASD, DOGS>(c, t); break;
-      case PAT_S * 3 + PAT_SP: trip_3c_force<PAT_S, PAT_SP, HASD, DOGS>(c, t); break;
-      case PAT_S * 3 + PAT_S: trip_3c_force<PAT_S, PAT_S, HASD, DOGS>(c, t); break;
+      case PAT_SP * 3 + PAT_SP: trip_3c_force<PAT_SP, PAT_SP, HASD, DOGS, FUSE>(c, t); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_force<PAT_SP, PAT_S, HASD, DOGS, FUSE>(c, t); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_force<PAT_S, PAT_SP, HASD, DOGS, FUSE>(c, t); break;
+      case PAT_S * 3 + PAT_S: trip_3c_force<PAT_S, PAT_S, HASD, DOGS, FUSE>(c, t); break;
       default:
         if constexpr (HASD) {
-          if (key == PAT_SPD * 3 + PAT_SPD) trip_3c_force<PAT_SPD, PAT_SPD, HASD, DOGS>(c, t);
-          else if (key == PAT_SPD * 3 + PAT_SP) trip_3c_force<PAT_SPD, PAT_SP, HASD, DOGS>(c, t);
-          else if (key == PAT_SP * 3 + PAT_SPD) trip_3c_force<PAT_SP, PAT_SPD, HASD, DOGS>(c, t);
-          else if (key == PAT_SPD * 3 + PAT_S) trip_3c_force<PAT_SPD, PAT_S, HASD, DOGS>(c, t);
-          else if (key == PAT_S * 3 + PAT_SPD) trip_3c_force<PAT_S, PAT_SPD, HASD, DOGS>(c, t);
+          if (key == PAT_SPD * 3 + PAT_SPD) trip_3c_force<PAT_SPD, PAT_SPD, HASD, DOGS, FUSE>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_SP) trip_3c_force<PAT_SPD, PAT_SP, HASD, DOGS, FUSE>(c, t);
+          else if (key == PAT_SP * 3 + PAT_SPD) trip_3c_force<PAT_SP, PAT_SPD, HASD, DOGS, FUSE>(c, t);
+          else if (key == PAT_SPD * 3 + PAT_S) trip_3c_force<PAT_SPD, PAT_S, HASD, DOGS, FUSE>(c, t);
+          else if (key == PAT_S * 3 + PAT_SPD) trip_3c_force<PAT_S, PAT_SPD, HASD, DOGS, FUSE>(c, t);
         }
     }
   });
 }
 
-// The four instantiations (HASD, DOGS) of k_dassemble_3c build as four parts of
-// this source (FB_IN_PART); part 0 also holds the launcher.
+// The instantiations (HASD, DOGS) and the fused Harris value + force
+// kernels (HASD) of k_dassemble_3c build as six parts of this source
+// (FB_IN_PART); part 0 also holds the launcher.
 int launch_dassemble_3c_v(int v, const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
 int launch_dassemble_3c_v0(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
 int launch_dassemble_3c_v1(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
 int launch_dassemble_3c_v2(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
 int launch_dassemble_3c_v3(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v4(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
+int launch_dassemble_3c_v5(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s);
 
 #if FB_IN_PART(0)
 int launch_dassemble_3c_v(int v, const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
@@ -201,6 +215,8 @@ int launch_dassemble_3c_v(int v, const Ctx3c &c, Sched q, dim3 grid, dim3 block,
     case 1: return launch_dassemble_3c_v1(c, q, grid, block, s);
     case 2: return launch_dassemble_3c_v2(c, q, grid, block, s);
     case 3: return launch_dassemble_3c_v3(c, q, grid, block, s);
+    case 4: return launch_dassemble_3c_v4(c, q, grid, block, s);
+    case 5: return launch_dassemble_3c_v5(c, q, grid, block, s);
   }
   return (int)cudaErrorInvalidValue;
 }
@@ -213,13 +229,14 @@ int launch_dassemble_3c(const AsmArgs &a, cudaStream_t s) {
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
   int v = (a.have_d ? 2 : 0) + (a.dogs ? 1 : 0);
+  if (a.fuse_value && !a.dogs) v = a.have_d ? 5 : 4;
   return launch_dassemble_3c_v(v, c, q, grid, block, s);
 }
 #endif
 
 #if FB_IN_PART(0)
 int launch_dassemble_3c_v0(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
-  k_dassemble_3c<false, false><<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c<false, false, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -227,7 +244,7 @@ int launch_dassemble_3c_v0(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaS
 
 #if FB_IN_PART(1)
 int launch_dassemble_3c_v1(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
-  k_dassemble_3c<false, true><<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c<false, true, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -235,7 +252,7 @@ int launch_dassemble_3c_v1(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaS
 
 #if FB_IN_PART(2)
 int launch_dassemble_3c_v2(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
-  k_dassemble_3c<true, false><<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c<true, false, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -243,7 +260,23 @@ int launch_dassemble_3c_v2(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaS
 
 #if FB_IN_PART(3)
 int launch_dassemble_3c_v3(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
-  k_dassemble_3c<true, true><<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c<true, true, false><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(4)
+int launch_dassemble_3c_v4(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<false, false, true><<<grid, block, 0, s>>>(c, q);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+#endif
+
+#if FB_IN_PART(5)
+int launch_dassemble_3c_v5(const Ctx3c &c, Sched q, dim3 grid, dim3 block, cudaStream_t s) {
+  k_dassemble_3c<true, false, true><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

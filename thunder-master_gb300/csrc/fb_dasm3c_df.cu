@@ -7,8 +7,10 @@
 namespace fb {
 
 // MLP: F and its cos / x / y derivatives come from the MLP-3c results of
-// list position i instead of the tables
-template <int PA, int PB, bool MLP>
+// list position i instead of the tables.  FUSE: also the triplet's
+// value-pass term of assemble_vna_3c (M_assemble_3c_Harris.f90:82-227),
+// rot(F sint^mvalue) P_eq2 into the vna block, from the same F.
+template <int PA, int PB, bool MLP, bool FUSE>
 __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n;
@@ -51,6 +53,14 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
   for (int a = 0; a < 3; a++)
 #pragma unroll
     for (int b = 0; b < 3; b++) R.p[a][b] = g.e[pperm(a)][pperm(b)];
+  if constexpr (FUSE) {
+    df X[NA * NB];
+    rotate_plan_df<PA, PB, K3C>(R, F, X);
+    double *dst = c.vb + c.blk_off[c.tdst[t]];
+    const df pe = peq2_df();
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, df_to(X[q] * pe));
+  }
   const df *rho = c.rho_df + c.blk_off[c.tdst[t]];
   df rb[NA * NB], rR[NA * NB], G[NE];
 #pragma unroll
@@ -104,17 +114,17 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
   }
 }
 
-template <bool MLP>
+template <bool MLP, bool FUSE>
 __global__ void __launch_bounds__(256) k_dassemble_3c_df(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
     int i = t;
     if (c.tperm) t = c.tperm[t];
     int pa = c.fd->sp[c.isp[c.ci_j[t]]].pattern, pb = c.fd->sp[c.isp[c.cj_j[t]]].pattern;
     switch (pa * 3 + pb) {
-      case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP, MLP>(c, t, i); break;
-      case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S, MLP>(c, t, i); break;
-      case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP, MLP>(c, t, i); break;
-      case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S, MLP>(c, t, i); break;
+      case PAT_SP * 3 + PAT_SP: trip_3c_force_df<PAT_SP, PAT_SP, MLP, FUSE>(c, t, i); break;
+      case PAT_SP * 3 + PAT_S: trip_3c_force_df<PAT_SP, PAT_S, MLP, FUSE>(c, t, i); break;
+      case PAT_S * 3 + PAT_SP: trip_3c_force_df<PAT_S, PAT_SP, MLP, FUSE>(c, t, i); break;
+      case PAT_S * 3 + PAT_S: trip_3c_force_df<PAT_S, PAT_S, MLP, FUSE>(c, t, i); break;
       default: break;
     }
   });
@@ -127,7 +137,8 @@ int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  k_dassemble_3c_df<false><<<grid, block, 0, s>>>(c, q);
+  if (a.fuse_value) k_dassemble_3c_df<false, true><<<grid, block, 0, s>>>(c, q);
+  else k_dassemble_3c_df<false, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -139,7 +150,7 @@ int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  k_dassemble_3c_df<true><<<grid, block, 0, s>>>(c, q);
+  k_dassemble_3c_df<true, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }

@@ -80,6 +80,9 @@ struct AsmArgs {
   const long long *blk_off;
   const int *trip_alpha, *ci_j, *ci_b, *cj_j, *cj_b, *tdst;
   const int *tperm;  // triplet processing order (binned), or null
+  // force pass: the three-center kernel also adds the value-pass vna terms
+  // of its triplets (a step that computes both interpolates each once)
+  int fuse_value;
   double *S, *T, *vb, *vbo;
   const double *rho, *cape;
   double *dS, *dT;

@@ -28,7 +28,7 @@ SOURCES = ["fb_api.cu", "fb_fdata.cpp", "fb_neigh.cu", "fb_asm2c.cu", "fb_asm3c.
            "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu"]
 # Sources compiled in parts (-DFB_PART=k, k < count): their slow template
 # instantiations compile in parallel (FB_IN_PART in fb_launch.h).
-PARTS = {"fb_asm2c.cu": 4, "fb_asm3c.cu": 4, "fb_dasm2c.cu": 4, "fb_dasm3c.cu": 4, "fb_vxc.cu": 8}
+PARTS = {"fb_asm2c.cu": 4, "fb_asm3c.cu": 4, "fb_dasm2c.cu": 4, "fb_dasm3c.cu": 6, "fb_vxc.cu": 8}
 
 
 def nvcc():
