@@ -146,10 +146,17 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # algorithmic work per unit
 # ---------------------------------------------------------------------------
-def flops_dassemble_3c(nme):
-    # value + x + y derivative table contractions (5 theta x 16 nodes x nME FMA
-    # each), Legendre and theta-derivative combination (4 x 5 x nME FMA), and
-    # ~1800 FLOP of geometry, frame derivatives and molecular-frame contraction
+def flops_dassemble_3c(nme, prec="df"):
+    """FP64 FLOPs per triplet of the force kernel's formulation.  fp64: the
+    Legendre sums first at each of the 16 stencil nodes (4 + 3 FMA per node
+    and element), then the value, x, y and cos contractions (4 FMA), about
+    100 FLOP of stencil weights; df (the per-theta form of the reference,
+    executed in double-float): value + x + y contractions per theta (5 x 16
+    x 3 FMA per element) and the Legendre combination (4 x 5 FMA).  Both add
+    about 1800 FLOP of geometry, frame derivatives and the molecular-frame
+    density contraction."""
+    if prec == "fp64":
+        return 2.0 * (16 * 11 * nme) + 100.0 + 1800.0
     return 2.0 * (3 * 5 * 16 * nme + 4 * 5 * nme) + 1800.0
 
 
@@ -192,7 +199,7 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
     dom_ms = ktimes[dom][0] / max(1, ktimes[dom][1])
     from fbgpu import synth
     nme = len(synth.make_munu_3c([0, 1], [0, 1])[0])
-    fl64 = {"dassemble_3c": T * flops_dassemble_3c(nme), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
+    fl64 = {"dassemble_3c": T * flops_dassemble_3c(nme, prec), "assemble_3c": T * flops_assemble_3c(nme)}.get(dom)
     if fl64 is None:
         return None
     fp64_peak = ctx.probe_fp64()
@@ -454,16 +461,23 @@ def run_gpu(args):
         "roofline": roofline_for(ctx, o["ktimes"], T, P, st.natoms, nZ, args.steps, o["prec"]),
         "launch_shapes": o["shapes"],
         "max_abs_diff_vs_headline": max_abs_diffs(o["out"], m["out"])}
+    legs = set(args.legs.split(",")) if args.legs != "none" else set()
     if rank == 0:
-        line["bloch"] = bloch_measure(ctx, torch, stream, local)
-        line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
-        line["vnl"] = vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=args.no_cpu)
-        line["vxc"] = vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=args.no_cpu)
+        if "bloch" in legs:
+            line["bloch"] = bloch_measure(ctx, torch, stream, local)
+        if "solve" in legs:
+            line["solve_k"] = solve_measure(args, fbgpu, torch, stream, local)
+        if "dogs" in legs:
+            line["dogs"] = dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=args.no_cpu)
+        if "vnl" in legs:
+            line["vnl"] = vnl_measure(args, fbgpu, torch, stream, flush, local, path, st, nZ, no_cpu=args.no_cpu)
+        if "vxc" in legs:
+            line["vxc"] = vxc_measure(args, fbgpu, torch, stream, flush, local, st, nZ, no_cpu=args.no_cpu)
     if args.mlp_epochs > 0:
         ctx.set_precision(prec_main)
         line["mlp3c"] = mlp_compare(ctx, fbgpu, torch, stream, flush, ws, local, d_rho, d_cape, P, T,
                                     args.steps, args.mlp_epochs)
-    if rank == 0 and args.extra_workloads:
+    if rank == 0 and args.extra_workloads and args.extra_workloads != "none":
         line["workloads"] = {}
         for name in args.extra_workloads.split(","):
             if name and name != args.workload:
@@ -477,7 +491,9 @@ def run_gpu(args):
             line["parity_vs_oracle"] = {
                 "what": "max |GPU - oracle| in this run, same structure and density matrices (eV, eV/Angstrom)",
                 m["prec"]: max_abs_diffs(m["out"], ref), o["prec"]: max_abs_diffs(o["out"], ref),
-                "tolerance": 1e-10}
+                "max_abs_ftot_ev_per_A": float(np.abs(ref["ftot"]).max()),
+                "tolerance": "blocks 1e-10 eV; forces 1e-10 of the largest component (the reference algorithm "
+                             "built with and without FMA contraction differs by ~1e-11 of it)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -539,6 +555,48 @@ def bloch_measure(ctx, torch, stream, local, reps=5):
     return {"what": "dense complex H(k) = T + vna + vnao and S(k) at one k-point (Bloch sums of the blocks)",
             "norbitals": n, "ms": round(ms, 4), "bytes_written": nbytes,
             "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), "hermiticity_max_abs": herm}
+
+
+def solve_measure(args, fbgpu, torch, stream, local, name="si512", nk=2):
+    """The k-point Lowdin solver (kspace_Lowdin: Bloch sums, eigenpairs of
+    S(k), S^-1/2, eigenpairs of S^-1/2 H S^-1/2, c = S^-1/2 c_Lowdin) on
+    Si512 (2,048 orbitals), per k-point, and its agreement with the
+    oracle's numpy restatement on the oracle's Bloch sums."""
+    path, nZ, st = load_workload(name)
+    ctx = fbgpu.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.read_Fdata(path, nZ)
+    ctx.set_structure(st.ratom, st.imass, st.lattice)
+    ctx.driver_neighbors()
+    ctx.assemble(fbgpu.FB_ALL)
+    n = int(ctx.L.fb_norbitals(ctx.h))
+    kpts = np.array([[0.11, -0.23, 0.31], [0.0, 0.0, 0.0]])[:nk]
+    c = torch.empty((nk, n, n, 2), dtype=torch.float64, device=f"cuda:{local}")
+    ctx.solve_k(kpts[:1], c_ptr=c.data_ptr())  # workspace + library load
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eig, dropped = ctx.solve_k(kpts, c_ptr=c.data_ptr())
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / nk
+    out = {"what": "kspace_Lowdin per k-point on %s: Bloch sums + zheevd(S) + Lowdin S^-1/2 + zheevd(S^-1/2 H "
+                   "S^-1/2) + c = S^-1/2 c_L (cuSOLVER / cuBLAS FP64, own kernels for the sums and scaling)" % name,
+           "norbitals": n, "kpoints": nk, "ms_per_kpoint": round(dt * 1e3, 2),
+           "dropped_overlap_eigenvalues": [int(x) for x in dropped]}
+    del c
+    ctx.close()
+    if not args.no_cpu:
+        from oracle import lowdin
+        from oracle import oracle as orc
+        s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice, threads=os.cpu_count() or 1).neighbors()
+        S, T, vb, vbo = s.assemble()
+        t0 = time.perf_counter()
+        err = 0.0
+        for k in range(nk):
+            eps = lowdin.solve_k(s.bloch(kpts[k:k + 1], T + vb + vbo)[0], s.bloch(kpts[k:k + 1], S)[0])[0]
+            err = max(err, float(np.abs(eps - eig[k]).max()))
+        out["max_abs_deig_ev"] = err
+        out["cpu_numpy_s_per_kpoint"] = round((time.perf_counter() - t0) / nk, 3)
+    return out
 
 
 def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=False):
@@ -1096,6 +1154,8 @@ def main():
     ap.add_argument("--extra-workloads", default="si512,cho1536,batch256",
                     help="comma-separated workloads also measured (both precisions) as extra keys of the line")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline measurement")
+    ap.add_argument("--legs", default="bloch,solve,dogs,vnl,vxc",
+                    help="extra measurements on the same structure (comma list, or none)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--mlp-epochs", type=int, default=12,
                     help="train the MLP-3c surrogate this many epochs over 2^22 samples and compare it with the "

@@ -67,6 +67,7 @@ extern "C" {
 #define FB_ERR_STATE 11        /* call out of order (e.g. no neighbors yet) */
 #define FB_ERR_CAPACITY 12     /* size beyond a stated maximum */
 #define FB_ERR_UNSUPPORTED 13  /* basis or map this build does not handle */
+#define FB_ERR_SOLVER 14       /* an eigen-decomposition did not converge */
 
 /* assembly selection bits for fb_assemble / fb_dassemble */
 #define FB_S 1u        /* overlap           (assemble_S / Dassemble_S) */
@@ -376,6 +377,28 @@ long long fb_norbitals(const fb_ctx *ctx);
 int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts,
                     const void *extra_dev, void *Hk_dev, void *Sk_dev);
 int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
+
+/* k-point Lowdin solver after the Bloch sums.  Replaces kspace_Lowdin
+ * (h.SOLVESH/M_kspace_Lowdin.f90:740-880) with diagonalize_S and
+ * diagonalize_H_Lowdin (h.SOLVESH/M_diagonalization_Lowdin_kpoints.f90:
+ * 145-403).  Per k-point (kpts: 3 doubles each, 1/Angstrom): the Bloch sums
+ * S(k) and H(k) = T + vna + vnao (+ extra_dev, as fb_bloch_device) on the
+ * device, the eigenpairs of S(k), the reference's linear-dependence rule
+ * (overlap eigenvalues below 1e-4: the columns above them move down, the
+ * trailing columns keep theirs), S^-1/2 from lambda^(-1/4)-scaled columns,
+ * the eigenpairs of S^-1/2 H S^-1/2 and c = S^-1/2 c_Lowdin.
+ *   eigen    host, nk * norbitals doubles: band energies, ascending (eV)
+ *   c_dev    device or NULL: nk column-major norbitals x norbitals complex
+ *            matrices (re, im interleaved), the eigenvectors c (the
+ *            reference's s%kpoints(ik)%c)
+ *   dropped  host or NULL: per k-point the number of overlap eigenvalues
+ *            below 1e-4 (norbitals - norbitals_new)
+ * The eigen-decompositions are cuSOLVER zheevd and the products cuBLAS
+ * zgemm, opened at the first call (FB_ERR_UNSUPPORTED where absent); the
+ * reference stops where zheev fails, this returns FB_ERR_SOLVER.  Works in
+ * four norbitals^2 complex device matrices the context keeps. */
+int fb_solve_k(fb_ctx *ctx, int nk, const double *kpts, const void *extra_dev,
+               double *eigen, void *c_dev, int *dropped);
 
 /* Non-local pseudopotential (vnl).  fb_neighbors_pp replaces
  * driver_neighbors_PP (c.SYSTEM/M_neighbors_PP.f90:98-151): the PP map

@@ -3,11 +3,20 @@
 SiC4096 (8x8x8 zincblende SiC, 4,096 atoms, 225,214 pairs, 5.12 M common
 -neighbor triplets) and C/H/O 1536 (mixed 4- and 1-orbital blocks, 60 k
 pairs, 1.0 M triplets), through the C ABI, against the oracle run on every
-host core: the neighbor maps and common-neighbor lists bit-exact, and S, T,
-vna, vnao, ftot and its terms within 1e-10 eV (eV/Angstrom) per element, in
-both precision modes of the three-center kernels.  This checks the triplet
-binning, the atomics and the launch shapes at the sizes the benchmark runs.
-"""
+host core: the neighbor maps and common-neighbor lists bit-exact, S, T, vna
+and vnao within 1e-10 eV per element, in both precision modes of the
+three-center kernels.  This checks the triplet binning, the atomics and the
+launch shapes at the sizes the benchmark runs.
+
+The forces at these sizes reach 100-400 eV/Angstrom, and their three-center
+terms are ill-conditioned (1/x and 1/sin(theta) factors of
+Dassemble_vna_3c, k.DASSEMBLERS/M_Dassemble_3c_Harris.f90:285-292, :827-832,
+amplify rounding): the reference's own algorithm, as the oracle, compiled
+once with strict FP64 and once with FMA contraction gives f3nab values that
+differ by up to 6.4e-9 eV/Angstrom on C/H/O 1536 (1.6e-11 of the largest
+component).  An absolute 1e-10 eV/Angstrom bound would fail the reference
+against itself, so each force array is held to 1e-10 of its largest
+component here (the small-system tests keep the absolute bound)."""
 import os
 
 import numpy as np
@@ -18,7 +27,8 @@ from oracle import oracle as orc
 
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 
-TOL = 1e-10
+TOL = 1e-10        # eV per block element
+TOL_F_REL = 1e-10  # of the largest component of each force array
 PRECS = [0, 1]  # FB_PREC_FP64, FB_PREC_DF
 
 
@@ -62,11 +72,12 @@ def _full_size(name, fdata_root):
         ctx.Dassemble()
         for key in ("ftot", "kinetic", "vna", "pulay", "f3naa", "f3nab", "f3nac", "vna_ontop", "vna_atom"):
             err = np.abs(ctx.forces(key) - ref_f[key]).max()
-            assert err <= TOL, "%s prec %d %s max |diff| %.3e" % (name, prec, key, err)
+            tol = TOL_F_REL * max(1.0, np.abs(ref_f[key]).max())
+            assert err <= tol, "%s prec %d %s max |diff| %.3e (tol %.3e)" % (name, prec, key, err, tol)
     # the graph step (autotuned launch shapes) gives the same forces
     ctx.autotune(fbgpu.FB_ALL | fbgpu.FB_FORCES, reps=1)
     ctx.assemble_graph(fbgpu.FB_ALL | fbgpu.FB_FORCES)
-    assert np.abs(ctx.forces("ftot") - ref_f["ftot"]).max() <= TOL
+    assert np.abs(ctx.forces("ftot") - ref_f["ftot"]).max() <= TOL_F_REL * np.abs(ref_f["ftot"]).max()
     assert np.abs(ctx.blocks("vna") - ref_blocks[2]).max() <= TOL
     ctx.close()
 

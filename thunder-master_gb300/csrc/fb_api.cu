@@ -19,6 +19,7 @@
 #include "fb_vxc.h"
 #include "fb_devbuf.h"
 #include "fb_mlp.h"
+#include "fb_solve.h"
 
 using namespace fb;
 
@@ -78,6 +79,9 @@ struct fb_ctx {
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
   DevBuf d_slot_off, d_slot_nn, d_slot_found, d_rcnt;
   DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
+  // k-point Lowdin solver (fb_solve_k): handles and n x n work matrices
+  SolverHandles solver;
+  DevBuf d_sol_S, d_sol_H, d_sol_W, d_sol_T, d_sol_lam, d_sol_eps, d_sol_work, d_sol_info;
   DevBuf d_status, d_errinfo;
   // blocks
   DevBuf d_S, d_T, d_vb, d_vbo, d_rho, d_cape, d_dS, d_dT, d_rho_df, d_dip;
@@ -292,6 +296,10 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
+  solver_destroy(ctx->solver);
+  DevBuf *sb[] = {&ctx->d_sol_S, &ctx->d_sol_H, &ctx->d_sol_W, &ctx->d_sol_T, &ctx->d_sol_lam, &ctx->d_sol_eps,
+                  &ctx->d_sol_work, &ctx->d_sol_info, &ctx->d_orb_slot};
+  for (DevBuf *b : sb) b->release();
   ctx->d_binok.release();
   ctx->d_mlpF.release();
   DevBuf *mb[] = {&ctx->mlp.params, &ctx->mlp.grad, &ctx->mlp.adam_m, &ctx->mlp.adam_v, &ctx->mlp.wbf,
@@ -2467,6 +2475,50 @@ int fb_bloch_device(fb_ctx *ctx, int nk, const double *kpts, const void *extra_d
   CU(cudaSetDevice(ctx->device));
   return bloch_run(ctx, nk, kpts, static_cast<const double *>(extra_dev), static_cast<double *>(Hk_dev),
                    static_cast<double *>(Sk_dev));
+}
+
+int fb_solve_k(fb_ctx *ctx, int nk, const double *kpts, const void *extra_dev, double *eigen, void *c_dev,
+               int *dropped) {
+  if (!ctx || nk < 1 || !kpts || !eigen) return FB_ERR_ARG;
+  CU(cudaSetDevice(ctx->device));
+  std::string why;
+  if (!solver_available(why)) return fail(ctx, FB_ERR_UNSUPPORTED, "fb_solve_k: %s", why.c_str());
+  long long n = fb_norbitals(ctx);
+  if (n < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  if (n > 46340) return fail(ctx, FB_ERR_CAPACITY, "fb_solve_k handles at most 46340 orbitals (n^2 < 2^31)");
+  size_t mb = (size_t)n * n * 2 * sizeof(double);
+  CHK(ctx->d_sol_S.ensure(mb));
+  CHK(ctx->d_sol_H.ensure(mb));
+  CHK(ctx->d_sol_W.ensure(mb));
+  CHK(ctx->d_sol_T.ensure(mb));
+  CHK(ctx->d_sol_lam.ensure((size_t)n * sizeof(double)));
+  CHK(ctx->d_sol_eps.ensure((size_t)n * sizeof(double)));
+  CHK(ctx->d_sol_info.ensure(sizeof(int)));
+  int lwork = 0;
+  if (lowdin_work_size(ctx->solver, ctx->stream, (int)n, ctx->d_sol_S.as<double>(), ctx->d_sol_lam.as<double>(),
+                       &lwork, why))
+    return fail(ctx, FB_ERR_CUDA, "fb_solve_k: %s", why.c_str());
+  CHK(ctx->d_sol_work.ensure((size_t)std::max(lwork, 1) * 2 * sizeof(double)));
+  LowdinBufs b;
+  b.Sk = ctx->d_sol_S.as<double>();
+  b.Hk = ctx->d_sol_H.as<double>();
+  b.W = ctx->d_sol_W.as<double>();
+  b.T = ctx->d_sol_T.as<double>();
+  b.lam = ctx->d_sol_lam.as<double>();
+  b.eps = ctx->d_sol_eps.as<double>();
+  b.work = ctx->d_sol_work.as<double>();
+  b.lwork = lwork;
+  b.info = ctx->d_sol_info.as<int>();
+  for (int k = 0; k < nk; k++) {
+    CHK(bloch_run(ctx, 1, kpts + 3 * k, static_cast<const double *>(extra_dev), b.Hk, b.Sk));
+    double *c = c_dev ? static_cast<double *>(c_dev) + (size_t)k * 2 * n * n : nullptr;
+    int rc = lowdin_solve(ctx->solver, ctx->stream, (int)n, b, eigen + (size_t)k * n, c,
+                          dropped ? dropped + k : nullptr, why);
+    ctx->launches += c ? 4 : 3;  // scaling kernel + library kernels not counted
+    if (rc == -3) return fail(ctx, FB_ERR_SOLVER, "fb_solve_k, k-point %d: %s", k, why.c_str());
+    if (rc) return fail(ctx, FB_ERR_CUDA, "fb_solve_k, k-point %d: %s", k, why.c_str());
+  }
+  return FB_OK;
 }
 
 int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk) {

@@ -67,7 +67,7 @@ FORCE = {"ftot": 0, "kinetic": 1, "vna": 2, "pulay": 3, "f3naa": 4, "f3nab": 5, 
          "vxc": 18, "f3xca": 19, "f3xcb": 20, "f3xcc": 21, "vxc_off_site": 22, "vxc_on_site": 23}
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "TABLE", 4: "X_NEGATIVE", 5: "X_TOO_LARGE",
           6: "ATOMS_CLOSE", 7: "NEIGH_SELF", 8: "NEIGH_BACK", 9: "CUDA", 10: "WATCHDOG",
-          11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED"}
+          11: "STATE", 12: "CAPACITY", 13: "UNSUPPORTED", 14: "SOLVER"}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -90,6 +90,7 @@ _SIGS = {
     "fb_norbitals": (C.c_longlong, [C.c_void_p]),
     "fb_bloch": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p]),
     "fb_bloch_device": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fb_solve_k": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, _dp, C.c_void_p, C.c_void_p]),
     "fb_mlp_nparams": (C.c_longlong, [C.c_void_p]),
     "fb_mlp_layout": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fb_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -430,6 +431,19 @@ class Context:
                                            None if extra_ptr is None else C.c_void_p(extra_ptr),
                                            None if hk_ptr is None else C.c_void_p(hk_ptr),
                                            None if sk_ptr is None else C.c_void_p(sk_ptr)))
+
+    def solve_k(self, kpts, c_ptr=None, extra_ptr=None):
+        """kspace_Lowdin per k-point: (band energies (nk, n) ascending,
+        dropped overlap eigenvalues per k-point).  c_ptr: device buffer for
+        the eigenvectors (nk column-major n x n complex), or None."""
+        k = np.ascontiguousarray(kpts, np.float64).reshape(-1, 3)
+        n = int(self.L.fb_norbitals(self.h))
+        eig = np.zeros(len(k) * n)
+        dropped = np.zeros(len(k), np.int32)
+        self._check(self.L.fb_solve_k(self.h, len(k), k.ravel(), None if extra_ptr is None else C.c_void_p(extra_ptr),
+                                      eig, None if c_ptr is None else C.c_void_p(c_ptr),
+                                      dropped.ctypes.data_as(C.c_void_p)))
+        return eig.reshape(len(k), n), dropped
 
     # ---- MLP-3c surrogate ------------------------------------------------------
     def mlp_init(self, seed=1):

@@ -25,7 +25,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
 SOURCES = ["fb_api.cu", "fb_fdata.cpp", "fb_neigh.cu", "fb_asm2c.cu", "fb_asm3c.cu", "fb_dasm2c.cu", "fb_dasm3c.cu",
            "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu",
-           "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu"]
+           "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu", "fb_solve.cu"]
 # Sources compiled in parts (-DFB_PART=k, k < count): their slow template
 # instantiations compile in parallel (FB_IN_PART in fb_launch.h).
 PARTS = {"fb_asm2c.cu": 4, "fb_asm3c.cu": 4, "fb_dasm2c.cu": 4, "fb_dasm3c.cu": 6, "fb_vxc.cu": 8}
@@ -90,7 +90,7 @@ def build(force=False, verbose=False):
     for obj, log in results:
         objs.append(obj)
         logs.append(log)
-    cmd = [cc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
+    cmd = [cc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
