@@ -2,8 +2,10 @@
 oracle's restatement of assemble_ewald / assemble_ewaldsr / assemble_ewaldlr
 (j.ASSEMBLERS/M_assemble_ewald_DOGS.f90): the N x N matrix to 1e-10 1/A and
 the ewaldsr / ewaldlr blocks to 1e-10 eV per element, periodic cells of one
-and two species, a vacancy cell and a cluster, plain and as one graph; the
-call-order errors."""
+and two species, a vacancy cell, a cluster and the 512-atom Si cell (343
+lattice vectors, most of them inside the screened cutoff), plain and as one
+graph, with the lattice and reciprocal sums in FP64 (precision 0) and in
+double-float (precision 1, the default); the call-order errors."""
 import numpy as np
 import pytest
 
@@ -33,8 +35,10 @@ def case(fdata_root, name):
     return workload(name, fdata_root, dogs=True)
 
 
-@pytest.mark.parametrize("name", ["sic_small", "si64", "sic_vac", "cho_small", "sic_cluster"])
-def test_ewald_matches_oracle(ctx, fdata_root, name):
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("name", ["sic_small", "si64", "sic_vac", "cho_small", "sic_cluster", "si512"])
+def test_ewald_matches_oracle(ctx, fdata_root, name, prec):
+    ctx.set_precision(prec)
     path, nZ, st = case(fdata_root, name)
     dq = np.random.default_rng(13).uniform(-0.3, 0.3, (len(st.imass), 3))
     s = orc.System(orc.Fdata(path, nZ), st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()
@@ -55,9 +59,11 @@ def test_ewald_matches_oracle(ctx, fdata_root, name):
         assert np.abs(ctx.blocks("ewaldlr") - lr).max() <= TOL
 
 
-@pytest.mark.parametrize("name", ["sic_small", "sic_vac", "cho_small", "sic_cluster"])
-def test_ewald_forces_match_oracle(ctx, fdata_root, name):
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("name", ["sic_small", "sic_vac", "cho_small", "sic_cluster", "si512"])
+def test_ewald_forces_match_oracle(ctx, fdata_root, name, prec):
     from conftest import symmetric_denmat
+    ctx.set_precision(prec)
     path, nZ, st = case(fdata_root, name)
     fd = orc.Fdata(path, nZ)
     s = orc.System(fd, st.ratom, st.imass, st.lattice, icluster=st.icluster).neighbors()

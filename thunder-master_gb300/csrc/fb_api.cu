@@ -1266,6 +1266,7 @@ static EwaldArgs ewald_args(fb_ctx *ctx) {
   e.xl = ctx->d_xl.as<double>();
   e.ng = ctx->ew_ng;
   e.nl = ctx->ew_nl;
+  e.df = ctx->prec == FB_PREC_DF;
   e.gvec = ctx->d_ew_g.as<double>();
   e.stuff = ctx->d_ew_stuff.as<double>();
   e.lvec = ctx->d_ew_l.as<double>();

@@ -487,14 +487,19 @@ __global__ void k_atom_q0(EwaldArgs e) {
 }  // namespace
 
 int launch_dewald(const EwaldArgs &e, cudaStream_t s) {
-  if (e.ng > 0) {
-    long long n = (long long)e.N * e.ng;
-    k_ewald_sf<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e);
+  if (e.df) {
+    int rc = launch_dewald_tiles_df(e, s);
+    if (rc) return rc;
+  } else {
+    if (e.ng > 0) {
+      long long n = (long long)e.N * e.ng;
+      k_ewald_sf<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e);
+      FB_LAUNCH_CHECK();
+    }
+    long long nb = (e.N + 31) / 32;
+    k_dewald_tiles<<<(unsigned)(nb * (nb + 1) / 2), 256, 0, s>>>(e);
     FB_LAUNCH_CHECK();
   }
-  long long nb = (e.N + 31) / 32;
-  k_dewald_tiles<<<(unsigned)(nb * (nb + 1) / 2), 256, 0, s>>>(e);
-  FB_LAUNCH_CHECK();
   k_atom_q0<<<(e.N + 255) / 256, 256, 0, s>>>(e);
   FB_LAUNCH_CHECK();
   unsigned wg = (unsigned)(((long long)e.N * 32 + 255) / 256);
@@ -522,6 +527,7 @@ int launch_ewald_forces(const EwaldArgs &e, cudaStream_t s) {
 }
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s) {
+  if (e.df) return launch_ewald_matrix_df(e, s);
   if (e.ng > 0) {
     long long n = (long long)e.N * e.ng;
     k_ewald_sf<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(e);

@@ -37,6 +37,9 @@ struct EwaldArgs {
   double *f3naa, *f3nab, *f3nac, *ftot;
   const int *pair_owner;
   int P;
+  // the lattice and reciprocal sums of the matrix and its derivative in
+  // double-float (fb_ewald_df.cu) instead of FP64
+  int df;
 };
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s);
@@ -46,6 +49,9 @@ int launch_ewald_blocks(const EwaldArgs &e, int have_d, cudaStream_t s);
 // into ftot (after build_forces)
 int launch_dewald(const EwaldArgs &e, cudaStream_t s);
 int launch_ewald_f3c(const EwaldArgs &e, cudaStream_t s);
+// the double-float matrix and derivative sums (structure factors + tiles)
+int launch_ewald_matrix_df(const EwaldArgs &e, cudaStream_t s);
+int launch_dewald_tiles_df(const EwaldArgs &e, cudaStream_t s);
 int launch_ewald_forces(const EwaldArgs &e, cudaStream_t s);
 
 }  // namespace fb

@@ -25,7 +25,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
 SOURCES = ["fb_api.cu", "fb_fdata.cpp", "fb_neigh.cu", "fb_asm2c.cu", "fb_asm3c.cu", "fb_dasm2c.cu", "fb_dasm3c.cu",
            "fb_probe.cu", "fb_asm3c_df.cu", "fb_dasm3c_df.cu", "fb_mlp.cu", "fb_mlp_eval.cu", "fb_mlp_tc.cu", "fb_bloch.cu",
-           "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu", "fb_solve.cu"]
+           "fb_pp.cu", "fb_ewald.cu", "fb_vxc.cu", "fb_vxc_df.cu", "fb_dogs_df.cu", "fb_solve.cu", "fb_ewald_df.cu"]
 # Sources compiled in parts (-DFB_PART=k, k < count): their slow template
 # instantiations compile in parallel (FB_IN_PART in fb_launch.h).
 PARTS = {"fb_asm2c.cu": 4, "fb_asm3c.cu": 4, "fb_dasm2c.cu": 4, "fb_dasm3c.cu": 6, "fb_vxc.cu": 8}
