@@ -395,7 +395,10 @@ int fb_bloch(fb_ctx *ctx, int nk, const double *kpts, double *Hk, double *Sk);
  *            below 1e-4 (norbitals - norbitals_new)
  * The eigen-decompositions are cuSOLVER zheevd and the products cuBLAS
  * zgemm, opened at the first call (FB_ERR_UNSUPPORTED where absent); the
- * reference stops where zheev fails, this returns FB_ERR_SOLVER.  Works in
+ * reference stops where zheev fails, this returns FB_ERR_SOLVER; it also
+ * returns FB_ERR_SOLVER where more than half of the overlap eigenvalues
+ * fall below 1e-4, where the reference's column shift leaves eigenvalues
+ * below 1e-4 (negative ones among them) in S^-1/2 and its result is NaN.  Works in
  * four norbitals^2 complex device matrices the context keeps. */
 int fb_solve_k(fb_ctx *ctx, int nk, const double *kpts, const void *extra_dev,
                double *eigen, void *c_dev, int *dropped);

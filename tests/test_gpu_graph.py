@@ -82,7 +82,9 @@ def test_graph_step_and_replay(gpu_ctx, fdata_root, prec):
     l0 = ctx.kernel_launches()
     ctx.assemble_graph(fbgpu.FB_ALL | fbgpu.FB_FORCES)
     per_graph = ctx.kernel_launches() - l0
-    assert per_graph >= 5
+    # 2c value, 2c force, three-center force (which also adds the
+    # three-center value terms) and build_forces at least
+    assert per_graph >= 4
     _check(ctx, blocks, fref, "graph prec %d" % prec)
     ctx.set_denmat(rho2, cape2)
     ctx.assemble_graph(fbgpu.FB_ALL | fbgpu.FB_FORCES)

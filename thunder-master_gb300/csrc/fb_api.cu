@@ -77,6 +77,10 @@ struct fb_ctx {
   DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
+  // the triplet lists in the binned order (6 x T ints) for the table
+  // kernels, valid for tbin_T triplets
+  DevBuf d_tbin;
+  int tbin_T = -1;
   DevBuf d_slot_off, d_slot_nn, d_slot_found, d_rcnt;
   DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
   // k-point Lowdin solver (fb_solve_k): handles and n x n work matrices
@@ -291,7 +295,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
-                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm,
+                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm, &ctx->d_tbin,
                     &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_rcnt, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
@@ -570,6 +574,28 @@ static bool mlp_routes(const fb_ctx *ctx) {
 
 // counting sort of the triplets by interpolation bin, approved MLP-3c bins
 // first; mlp_n = triplets the network takes
+// the three-center table kernels' view of list positions nm .. T-1: the
+// binned copies of the triplet lists, read in order
+static AsmArgs table3c_view(const fb_ctx *ctx, const AsmArgs &a, int nm) {
+  AsmArgs at = a;
+  int T = ctx->T;
+  at.ntrip = T - nm;
+  if (ctx->tbin_T == T && ctx->d_tbin.p) {
+    const int *b = ctx->d_tbin.as<int>();
+    long long n = T;
+    at.trip_alpha = b + nm;
+    at.ci_j = b + n + nm;
+    at.ci_b = b + 2 * n + nm;
+    at.cj_j = b + 3 * n + nm;
+    at.cj_b = b + 4 * n + nm;
+    at.tdst = b + 5 * n + nm;
+    at.tperm = nullptr;
+  } else {
+    at.tperm = a.tperm ? a.tperm + nm : nullptr;
+  }
+  return at;
+}
+
 static int bin_triplets(fb_ctx *ctx) {
   int T = ctx->T, nsp = ctx->fdh.nspecies, cells = trip_cells(ctx);
   size_t nbins = (size_t)nsp * nsp * nsp * cells;
@@ -578,11 +604,13 @@ static int bin_triplets(fb_ctx *ctx) {
   CHK(ctx->d_trank.ensure(tb));
   CHK(ctx->d_tperm.ensure(tb));
   CHK(ctx->d_thist.ensure(2 * nbins * sizeof(int)));
+  CHK(ctx->d_tbin.ensure(6 * (size_t)T * sizeof(int) + 4));
   bool gated = mlp_routes(ctx) && ctx->mlp_mode == FB_MLP_GATED && ctx->d_binok.p;
   NeighArgs a = neigh_args(ctx);
   KL(KT_TRIP_BINS, launch_trip_bins(a, T, nsp, cells, gated ? ctx->d_binok.as<unsigned char>() : nullptr,
                                     ctx->d_tkey.as<int>(), ctx->d_trank.as<int>(), ctx->d_thist.as<int>(),
-                                    ctx->d_tperm.as<int>(), ctx->stream));
+                                    ctx->d_tperm.as<int>(), ctx->d_tbin.as<int>(), ctx->stream));
+  ctx->tbin_T = T;
   ctx->mlp_n = 0;
   if (mlp_routes(ctx) && ctx->mlp_mode == FB_MLP_ALL) ctx->mlp_n = T;
   if (gated && T > 0) {
@@ -1449,9 +1477,7 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
   if (what & FB_VNA3C) {
     // triplets of approved bins through the network, the rest through the tables
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
-    AsmArgs at = a;
-    at.tperm = a.tperm + nm;
-    at.ntrip = a.ntrip - nm;
+    AsmArgs at = table3c_view(ctx, a, nm);
     if (ctx->fuse3c) {
       // the force pass adds these triplets' value terms (enqueue_dassemble)
     } else if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
@@ -1727,9 +1753,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
   }
   if (what & FB_VNA3C) {
     int nm = mlp_routes(ctx) ? ctx->mlp_n : 0;
-    AsmArgs at = a;
-    at.tperm = a.tperm + nm;
-    at.ntrip = a.ntrip - nm;
+    AsmArgs at = table3c_view(ctx, a, nm);
     at.fuse_value = ctx->fuse3c;
     if (use_df(ctx) || use_df_dogs(ctx) || nm > 0) KL(KT_SPLIT_RHO, launch_split_rho(a, ctx->nblock, ctx->stream));
     if (use_df(ctx)) KL(KT_DASM3C, launch_dassemble_3c_df(at, ctx->stream));
@@ -1945,6 +1969,7 @@ static int tune_launch(fb_ctx *ctx, int k, const KCfg &c, unsigned what) {
       return launch_assemble_2c(a, w2, ctx->stream);
     }
     case TK_A3C:
+      a = table3c_view(ctx, a, 0);
       a.cfg_a3c = c;
       return use_df(ctx) ? launch_assemble_3c_df(a, ctx->stream) : launch_assemble_3c(a, ctx->stream);
     case TK_D2C: {
@@ -1954,6 +1979,7 @@ static int tune_launch(fb_ctx *ctx, int k, const KCfg &c, unsigned what) {
       return launch_dassemble_2c(a, w2, ctx->stream);
     }
     case TK_D3C:
+      a = table3c_view(ctx, a, 0);
       a.cfg_d3c = c;
       return use_df(ctx) ? launch_dassemble_3c_df(a, ctx->stream) : launch_dassemble_3c(a, ctx->stream);
   }

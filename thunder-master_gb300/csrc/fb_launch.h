@@ -115,9 +115,10 @@ int launch_common(const NeighArgs &a, cudaStream_t s);
 int launch_common_compact(const NeighArgs &a, cudaStream_t s);
 // counting sort of the triplets by (species triple, 3c grid cell) -> perm;
 // bins with binok[bin] set (may be null) come first; hist has 2 x nbins
-// entries and holds the exclusive bin starts afterwards
+// entries and holds the exclusive bin starts afterwards; binned (may be
+// null): 6 x T ints, the triplet lists copied into the binned order
 int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsigned char *binok, int *key, int *rank,
-                     int *hist, int *perm, cudaStream_t s);
+                     int *hist, int *perm, int *binned, cudaStream_t s);
 int launch_assemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);
 int launch_assemble_3c(const AsmArgs &a, cudaStream_t s);
 int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s);

@@ -465,8 +465,27 @@ __global__ void k_trip_scatter(int T, const int *__restrict__ key, const int *__
   perm[start[key[t]] + rank[t]] = t;
 }
 
+// the triplet lists in the binned order, list position i holding triplet
+// perm[i] (six arrays of T: talpha, ci_j, ci_b, cj_j, cj_b, tdst): the
+// three-center kernels read these in order instead of gathering through
+// perm, which cost one 32-byte sector per array and triplet
+__global__ void k_trip_gather(int T, const int *__restrict__ perm, const int *__restrict__ talpha,
+                              const int *__restrict__ ci_j, const int *__restrict__ ci_b, const int *__restrict__ cj_j,
+                              const int *__restrict__ cj_b, const int *__restrict__ tdst, int *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= T) return;
+  int t = perm[i];
+  long long n = T;
+  out[i] = talpha[t];
+  out[n + i] = ci_j[t];
+  out[2 * n + i] = ci_b[t];
+  out[3 * n + i] = cj_j[t];
+  out[4 * n + i] = cj_b[t];
+  out[5 * n + i] = tdst[t];
+}
+
 int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsigned char *binok, int *key, int *rank,
-                     int *hist, int *perm, cudaStream_t s) {
+                     int *hist, int *perm, int *binned, cudaStream_t s) {
   if (T == 0) return 0;
   int nbins = 2 * nsp * nsp * nsp * cells;
   cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), s);
@@ -479,6 +498,10 @@ int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsign
   FB_LAUNCH_CHECK();
   k_trip_scatter<<<blocks, threads, 0, s>>>(T, key, rank, hist, perm);
   FB_LAUNCH_CHECK();
+  if (binned) {
+    k_trip_gather<<<blocks, threads, 0, s>>>(T, perm, a.talpha, a.ci_j, a.ci_b, a.cj_j, a.cj_b, a.tdst, binned);
+    FB_LAUNCH_CHECK();
+  }
   return 0;
 }
 

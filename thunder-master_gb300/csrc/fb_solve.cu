@@ -165,6 +165,15 @@ int lowdin_solve(SolverHandles &h, cudaStream_t s, int n, const LowdinBufs &b, d
   for (int k = 0; k < n; k++)
     if (lam[k] < LOWDIN_OVERTOL) m = k + 1;
   if (dropped) *dropped = m;
+  // with more than half of the eigenvalues dropped, the trailing columns
+  // that keep their place include eigenvalues below overtol: the reference
+  // raises them to the power -1/4 (a NaN for the negative ones) and goes on
+  // with a meaningless S^-1/2; report it instead
+  if (2 * m > n) {
+    err = std::to_string(m) + " of " + std::to_string(n) +
+          " overlap eigenvalues are below 1e-4: the Lowdin S^-1/2 is undefined (S(k) is far from positive definite)";
+    return -3;
+  }
   // 3. W = shifted, scaled eigenvectors; S12 = W W^H (into Tmp)
   long long nn = (long long)n * n;
   int threads = 256;

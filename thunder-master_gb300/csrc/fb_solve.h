@@ -32,7 +32,8 @@ int lowdin_work_size(SolverHandles &h, cudaStream_t s, int n, double *A, double 
 // energies to eps_host (n, ascending), eigenvectors c to c_dev (n x n
 // complex, may be null), the number of dropped overlap eigenvalues to
 // dropped (may be null).  Returns 0, -1 (libraries absent), -2 (a call
-// failed) or -3 (no convergence), with err set.
+// failed) or -3 (no convergence, or more than half of the overlap
+// eigenvalues below overtol), with err set.
 int lowdin_solve(SolverHandles &h, cudaStream_t s, int n, const LowdinBufs &b, double *eps_host, double *c_dev,
                  int *dropped, std::string &err);
 void solver_destroy(SolverHandles &h);
