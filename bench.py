@@ -656,6 +656,11 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
     torch.cuda.synchronize()
     out["ewald"] = {"what": "DOGS Ewald: N x N matrix (reciprocal + screened lattice sums), ewaldsr, ewaldlr",
                     "ms": round(e0.elapsed_time(e1) / args.steps, 4)}
+    ctx.set_timing(True)
+    ctx.assemble(fbgpu.FB_EWALD)
+    torch.cuda.synchronize()
+    out["ewald"]["kernels_ms"] = {k: round(v[0], 4) for k, v in ctx.timing().items() if v[1]}
+    ctx.set_timing(False)
     ctx.set_denmat_device(d_rho.data_ptr(), d_cape.data_ptr())
     ctx.Dassemble(fbgpu.FB_EWALD)
     torch.cuda.synchronize()
@@ -665,10 +670,31 @@ def dogs_measure(args, fbgpu, torch, stream, flush, ws, local, st, nZ, no_cpu=Fa
     e1.record(stream)
     torch.cuda.synchronize()
     out["ewald"]["force_ms"] = round(e0.elapsed_time(e1) / args.steps, 4)
+    ctx.set_timing(True)
+    ctx.Dassemble(fbgpu.FB_EWALD)
+    torch.cuda.synchronize()
+    out["ewald"]["force_kernels_ms"] = {k: round(v[0], 4) for k, v in ctx.timing().items() if v[1]}
+    ctx.set_timing(False)
     out["ewald"]["force_what"] = ("dewald + Ewald energy force, ewaldsr (pair + three-center) and ewaldlr forces, "
                                   "build_forces terms")
     ew_gpu = ctx.ewald()
     sr_gpu, lr_gpu = ctx.blocks("ewaldsr"), ctx.blocks("ewaldlr")
+    # the same Ewald passes with the FP64 lattice and reciprocal sums
+    ctx.set_precision(fbgpu.FB_PREC_FP64)
+    ctx.assemble(fbgpu.FB_EWALD)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx.assemble(fbgpu.FB_EWALD)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["ewald"]["fp64_ms"] = round(e0.elapsed_time(e1), 4)
+    out["ewald"]["fp64_max_abs_dewald_matrix_vs_df"] = float(np.abs(ctx.ewald() - ew_gpu).max())
+    e0.record(stream)
+    ctx.Dassemble(fbgpu.FB_EWALD)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["ewald"]["fp64_force_ms"] = round(e0.elapsed_time(e1), 4)
+    ctx.set_precision(fbgpu.FB_PREC_DF)
     # agreement with the oracle and the oracle's single-core time
     got = {k: ctx.blocks(k) for k in ("vna", "vnao")}
     ctx.set_denmat(rho, cape)

@@ -45,11 +45,12 @@ __device__ __forceinline__ df ld(const float2 *p) {
   return df_make(v.x, v.y);
 }
 
-// fit f of fb_ewald_fit.h at x in [0, 5.5] (staged in shared memory)
+// fit f of fb_ewald_fit.h at x in [0, 5.5] (staged in shared memory):
+// interval k = floor(4 x), local t = 8 (x - k/4) - 1 = 8 x - (2k + 1)
 __device__ __forceinline__ df ew_fit(const float2 *fit, df x) {
   int k = (int)(x.h * 4.0f);
   k = k < 0 ? 0 : (k >= EW_FIT_NINT ? EW_FIT_NINT - 1 : k);
-  df t = df_make(__fmul_rn(x.h, 8.0f), __fmul_rn(x.l, 8.0f)) + df_make(-(float)(8 * k + 1));
+  df t = df_make(__fmul_rn(x.h, 8.0f), __fmul_rn(x.l, 8.0f)) + df_make(-(float)(2 * k + 1));
   const float2 *c = fit + k * EW_FIT_NC;
   float pt = c[EW_FIT_NC - 1].x;
 #pragma unroll
