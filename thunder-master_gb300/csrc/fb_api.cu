@@ -110,7 +110,7 @@ struct fb_ctx {
   bool ewald_matrix = false;  // the DOGS Ewald matrix (Harris assembles zero blocks only)
   int ew_ng = 0, ew_nl = 0;
   double ew_kappa = 0.0;
-  DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs;
+  DevBuf d_ewald, d_ew_g, d_ew_stuff, d_ew_l, d_dqa, d_sum_ewald, d_ewsr, d_ewlr, d_ew_sfc, d_ew_sfs, d_ew_ldf;
   DevBuf d_q0a, d_dewald, d_ew_w, d_sum_dewald, d_ew_cw, d_fewald, d_fsr, d_flr;
   // McWEDA exchange-correlation (Harris): input densities and vxc blocks
   DevBuf d_rho_in, d_rho_bond, d_wrho_in, d_wrho_bond, d_vxc;
@@ -1280,6 +1280,15 @@ static int ewald_setup(fb_ctx *ctx) {
     CU(cudaMemcpy(ctx->d_ew_stuff.p, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   CU(cudaMemcpy(ctx->d_ew_l.p, lv.data(), lv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // hi/lo float pairs of the lattice vectors for the double-float sums
+  std::vector<float> lf(2 * lv.size());
+  for (size_t q = 0; q < lv.size(); q++) {
+    float hi = (float)lv[q];
+    lf[2 * q] = hi;
+    lf[2 * q + 1] = (float)(lv[q] - (double)hi);
+  }
+  CHK(ctx->d_ew_ldf.ensure(lf.size() * sizeof(float) + 8));
+  CU(cudaMemcpy(ctx->d_ew_ldf.p, lf.data(), lf.size() * sizeof(float), cudaMemcpyHostToDevice));
   return FB_OK;
 }
 
@@ -1295,6 +1304,7 @@ static EwaldArgs ewald_args(fb_ctx *ctx) {
   e.ng = ctx->ew_ng;
   e.nl = ctx->ew_nl;
   e.df = ctx->prec == FB_PREC_DF;
+  e.lvec_df = ctx->d_ew_ldf.as<float2>();
   e.gvec = ctx->d_ew_g.as<double>();
   e.stuff = ctx->d_ew_stuff.as<double>();
   e.lvec = ctx->d_ew_l.as<double>();

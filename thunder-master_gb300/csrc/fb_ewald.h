@@ -38,8 +38,10 @@ struct EwaldArgs {
   const int *pair_owner;
   int P;
   // the lattice and reciprocal sums of the matrix and its derivative in
-  // double-float (fb_ewald_df.cu) instead of FP64
+  // double-float (fb_ewald_df.cu) instead of FP64, with the lattice
+  // vectors as hi/lo float pairs [3 * nl]
   int df;
+  const float2 *lvec_df;
 };
 
 int launch_ewald_matrix(const EwaldArgs &e, cudaStream_t s);

@@ -71,18 +71,20 @@ __device__ __forceinline__ void stage_fit(float2 *fit, int f) {
 // fails it, every other z is at least 0.5 A), or nl
 __device__ __forceinline__ int next_lattice(const EwaldArgs &e, int k, const float *d, float rcut2) {
   for (; k < e.nl; k++) {
-    const double *L = e.lvec + 3 * k;
-    float c0 = __fadd_rn((float)L[0], d[0]), c1 = __fadd_rn((float)L[1], d[1]), c2 = __fadd_rn((float)L[2], d[2]);
+    const float2 *L = e.lvec_df + 3 * k;
+    float c0 = __fadd_rn(L[0].x, d[0]), c1 = __fadd_rn(L[1].x, d[1]), c2 = __fadd_rn(L[2].x, d[2]);
     float z2 = __fmaf_rn(c0, c0, __fmaf_rn(c1, c1, __fmul_rn(c2, c2)));
     if (z2 <= rcut2 && z2 > 1.0e-6f) return k;
   }
   return e.nl;
 }
 
+// c = L + r_i - r_j in df from the hi/lo copy of L (no FP64 operation: at
+// FP64's rate the conversions alone would cost more than the df terms)
 __device__ __forceinline__ void lattice_vec(const EwaldArgs &e, int k, const df *dd, df *c, df &z2) {
-  const double *L = e.lvec + 3 * k;
+  const float2 *L = e.lvec_df + 3 * k;
 #pragma unroll
-  for (int a = 0; a < 3; a++) c[a] = df_from(L[a]) + dd[a];
+  for (int a = 0; a < 3; a++) c[a] = ld(L + a) + dd[a];
   z2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
 }
 
