@@ -185,7 +185,11 @@ def tuned_shapes(ctx, fbgpu, autotune):
 # exceeds what L2 keeps between launches) (profiles/): the df formulation's
 # arithmetic is what the FP32 pipe must execute.
 DF_FP32_FLOP = {"dassemble_3c": 59053.0, "assemble_3c": 16284.0}
-DF_DRAM_BYTES = {"dassemble_3c": 93.4, "assemble_3c": 89.7}
+# DRAM read + write bytes per triplet of one force-kernel launch, ncu on
+# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 160.64 MB per launch;
+# profiles/k_dassemble_3c_df_sic4096.md, 159.78 MB), over 5,125,854 triplets
+DRAM_BYTES_PER_TRIPLET = {"fp64": 160.639232e6 / 5125854, "df": 159.777792e6 / 5125854}
+TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
 def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
@@ -217,9 +221,9 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
         ach = fl32 / (dom_ms * 1e-3) / 1e12
         return {"bound": "fp32", "kernel": dom, "achieved": round(ach, 4), "peak": round(fp32_peak, 4),
                 "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4),
-                "traffic": round(T * DF_DRAM_BYTES[dom]),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on SiC4096, "
-                                  "scaled by triplets",
+                "traffic": round(T * DRAM_BYTES_PER_TRIPLET["df"]) if dom == "dassemble_3c" else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on SiC4096 (%s), "
+                                  "scaled by triplets" % TRAFFIC_SOURCE["df"],
                 "peak_source": "of measured: fb_probe_fp32 FFMA chains in this run",
                 "flops_per_launch": fl32,
                 "flops_source": "executed FP32 FLOPs of the double-float kernel (2 FFMA + FADD + FMUL per "
@@ -230,7 +234,12 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
                                     "ratio_to_fp64_peak": round(ach64 / fp64_peak, 4)},
                 "hbm": hbm}
     return {"bound": "fp64", "kernel": dom, "achieved": round(ach64, 4), "peak": round(fp64_peak, 4),
-            "unit": "TFLOP/s", "frac": round(ach64 / fp64_peak, 4), "traffic": None,
+            "unit": "TFLOP/s", "frac": round(ach64 / fp64_peak, 4),
+            "traffic": round(T * DRAM_BYTES_PER_TRIPLET["fp64"]) if dom == "dassemble_3c" else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on SiC4096 (%s), "
+                              "scaled by triplets" % TRAFFIC_SOURCE["fp64"],
+            "flops_source": "FP64 FLOPs of the kernel's formulation per sp3 x sp3 triplet (Legendre sums at the "
+                            "stencil nodes first), x triplets",
             "peak_source": "of measured: fb_probe_fp64 DFMA chains in this run",
             "flops_per_launch": fl64, "avg_launch_ms": round(dom_ms, 4), "hbm": hbm}
 
