@@ -239,6 +239,7 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
 // by the caller) the sum over the rows; k_common_compact packs the rows in
 // ineigh order, so the triplets come out in the reference's loop order.
 __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
+                         const float4 *__restrict__ pos4, const float *__restrict__ xlf0,
                          const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                          const double *__restrict__ xl0, const int *__restrict__ pair_owner,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
@@ -257,6 +258,7 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
     return;
   }
   const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
+  const float *xlf = xlf0 + (long long)sid[ia] * XL_STRIDE;
   int periodic = speriodic[sid[ia]];
   int kidx = in - (in > self ? 1 : 0);
   long long base = slot_off[ia] + (long long)kidx * (n - 2);
@@ -266,6 +268,8 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
 #pragma unroll
   for (int k = 0; k < 3; k++) r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
   double rci = fd->sp[isp[iat]].rcA;
+  float4 pi4 = pos4[iat];
+  float r1f[3] = {pi4.x + xlf[3 * ib], pi4.y + xlf[3 * ib + 1], pi4.z + xlf[3 * ib + 2]};
   int q0 = pair_off[iat], qn = pair_off[iat + 1];
   int ibx, iby, ibz;
   mbeta_shift(ib, ibx, iby, ibz);
@@ -278,12 +282,30 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
       int pj = p0 + jn;
       jat = neigh_j[pj];
       jb = neigh_b[pj];
+      // float pre-test (the positions' float copies carry the species
+      // cutoff in .w): clearly beyond the range -> rejected, clearly inside
+      // (0.01 A of margin against ~1e-5 A of float error) -> kept without
+      // the FP64 distance; only the band between takes the reference's
+      // uncontracted FP64 test
+      float4 pj4 = pos4[jat];
+      float d0 = (pj4.x + xlf[3 * jb]) - r1f[0], d1 = (pj4.y + xlf[3 * jb + 1]) - r1f[1];
+      float d2 = (pj4.z + xlf[3 * jb + 2]) - r1f[2];
+      float dd = d0 * d0 + d1 * d1 + d2 * d2;
+      float lim = pi4.w + pj4.w + 1.0e-2f, sure = pi4.w + pj4.w - 2.0e-2f;
+      bool inside = false;
       double r2[3];
+      if (dd < lim * lim) {
 #pragma unroll
-      for (int k = 0; k < 3; k++) r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
-      double z = dist_rn(r1, r2);
-      double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
-      if (z < range) {
+        for (int k = 0; k < 3; k++) r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
+        if (dd < sure * sure) {
+          inside = true;
+        } else {
+          double z = dist_rn(r1, r2);
+          double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
+          inside = z < range;
+        }
+      }
+      if (inside) {
         int tmb = 0;
         bool inbox = true;
         if (periodic) {
@@ -538,7 +560,7 @@ int launch_common(const NeighArgs &a, cudaStream_t s) {
   if (a.P == 0) return 0;
   int threads = 256;
   long long blocks = ((long long)a.P * 32 + threads - 1) / threads;
-  k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl,
+  k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.pos4, a.xlf, a.isp, a.fd, a.sid, a.xl,
                                                 a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.r3v,
                                                 a.tcnt, a.rcnt, a.slot_off, a.slot_nn, a.slot_found);
   FB_LAUNCH_CHECK();
