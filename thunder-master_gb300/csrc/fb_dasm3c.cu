@@ -93,22 +93,20 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
       if constexpr (PL::m.mv[e] == 1) Fq[e] = Fq[e] * sint;
     });
   }
-  double M[NE], Ma[3 * NE], Mb[3 * NE];
+  // molecular-frame value and derivatives with the sin(theta) factor of
+  // the mvalue = 1 channels (M_Fdata_3c.f90:814-833)
+  double M[NE], Dp[NE], Dx[NE], Dy[NE];
   sfor<NE>([&](auto E) {
     constexpr int e = decltype(E)::value;
-    double m = F[e], dp = DpF[e], dx = DxF[e], dy = DyF[e];
+    M[e] = F[e];
+    Dp[e] = DpF[e];
+    Dx[e] = DxF[e];
+    Dy[e] = DyF[e];
     if constexpr (PL::m.mv[e] == 1) {
-      dp = DpF[e] * sint - g.cost * F[e] / sint;
-      m = F[e] * sint;
-      dx = DxF[e] * sint;
-      dy = DyF[e] * sint;
-    }
-    M[e] = m;
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      double a = g.rhat[q] * dx + amt[q] * dp;
-      Ma[q + 3 * e] = a;
-      Mb[q + 3 * e] = -g.sighat[q] * dy + bmt[q] * dp - a * 0.5;
+      Dp[e] = DpF[e] * sint - g.cost * F[e] / sint;
+      M[e] = F[e] * sint;
+      Dx[e] = DxF[e] * sint;
+      Dy[e] = DyF[e] * sint;
     }
   });
   RotM R;
@@ -130,16 +128,26 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   MolRho<PA, PB, K3C> GA, GB;
   mol_rho<PA, PB, K3C>(R, DA, rb, GA);
   mol_rho<PA, PB, K3C>(R, DB, rb, GB);
+  // f3naMa(q, e) = rhat_q dx + amt_q dp and f3naMb(q, e) = -sighat_q dy +
+  // bmt_q dp - f3naMa(q, e) / 2 (:334-344) enter only through their sums
+  // with G(e): sum_e Ma(q, e) G(e) = rhat_q Sx + amt_q Sp, and
+  // sum_e Mb(q, e) G(e) = -sighat_q Sy + bmt_q Sp - (rhat_q Sx + amt_q Sp) / 2
+  double Sx = 0.0, Sy = 0.0, Sp = 0.0;
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    Sx = fma(Dx[e], GA.G[e], Sx);
+    Sy = fma(Dy[e], GA.G[e], Sy);
+    Sp = fma(Dp[e], GA.G[e], Sp);
+  }
   double fa[3], fb[3];
 #pragma unroll
   for (int q = 0; q < 3; q++) {
-    double sa = 0.0, sb = 0.0;
+    double ga = fma(g.rhat[q], Sx, amt[q] * Sp);
+    double sa = ga, sb = fma(-g.sighat[q], Sy, fma(bmt[q], Sp, -0.5 * ga));
 #pragma unroll
     for (int e = 0; e < NE; e++) {
       sa = fma(M[e], GA.H[q][e], sa);
-      sa = fma(Ma[q + 3 * e], GA.G[e], sa);
       sb = fma(M[e], GB.H[q][e], sb);
-      sb = fma(Mb[q + 3 * e], GB.G[e], sb);
     }
     fa[q] = -sa * P_eq2;
     fb[q] = -sb * P_eq2;

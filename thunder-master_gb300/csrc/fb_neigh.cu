@@ -422,7 +422,14 @@ __global__ void k_common_compact(int N, const int *__restrict__ pair_off, const 
 // (M_assemble_3c_Harris.f90:160-186) and the index rule of getMEs_Fdata_3c
 // (M_Fdata_3c.f90:367-376); it only orders the work.
 // ---------------------------------------------------------------------------
-__global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__ ratom, const int *__restrict__ isp,
+// The bin is a sort key for table locality (and, with an MLP gate, the
+// routing unit): without a gate the float positions decide it (a triplet
+// within ~1e-5 A of a grid line may land in the neighboring bin, which only
+// changes its place in the order); with a gate the key is computed in FP64.
+template <bool EXACT>
+__global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__ ratom,
+                           const float4 *__restrict__ pos4, const float *__restrict__ xlf0,
+                           const int *__restrict__ isp,
                            const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                            const double *__restrict__ xl0,
                            const int *__restrict__ talpha, const int *__restrict__ ci_j, const int *__restrict__ ci_b,
@@ -432,20 +439,39 @@ __global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int ia = talpha[t], i = ci_j[t], j = cj_j[t], ib = ci_b[t], jb = cj_b[t];
-  const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
-  double r1[3], r2[3], rn[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    r1[k] = ratom[3 * i + k] + xl[3 * ib + k];
-    r2[k] = ratom[3 * j + k] + xl[3 * jb + k];
-    rn[k] = ratom[3 * ia + k] - 0.5 * (r1[k] + r2[k]);
-  }
-  double z = sqrt((r2[0] - r1[0]) * (r2[0] - r1[0]) + (r2[1] - r1[1]) * (r2[1] - r1[1]) +
-                  (r2[2] - r1[2]) * (r2[2] - r1[2]));
-  double x = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
   int a = isp[i], b = isp[j], c = isp[ia];
   const Cell3cDev &cell = fd->c3[a][b][c];
-  int ix = (int)(x / cell.dx) + 1, iy = (int)(z / cell.dy) + 1;
+  int ix, iy;
+  if constexpr (EXACT) {
+    const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
+    double r1[3], r2[3], rn[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      r1[k] = ratom[3 * i + k] + xl[3 * ib + k];
+      r2[k] = ratom[3 * j + k] + xl[3 * jb + k];
+      rn[k] = ratom[3 * ia + k] - 0.5 * (r1[k] + r2[k]);
+    }
+    double z = sqrt((r2[0] - r1[0]) * (r2[0] - r1[0]) + (r2[1] - r1[1]) * (r2[1] - r1[1]) +
+                    (r2[2] - r1[2]) * (r2[2] - r1[2]));
+    double x = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+    ix = (int)(x / cell.dx) + 1;
+    iy = (int)(z / cell.dy) + 1;
+  } else {
+    const float *xl = xlf0 + (long long)sid[ia] * XL_STRIDE;
+    float4 pi = pos4[i], pj = pos4[j], pa = pos4[ia];
+    float r1[3] = {pi.x + xl[3 * ib], pi.y + xl[3 * ib + 1], pi.z + xl[3 * ib + 2]};
+    float r2[3] = {pj.x + xl[3 * jb], pj.y + xl[3 * jb + 1], pj.z + xl[3 * jb + 2]};
+    float pn[3] = {pa.x, pa.y, pa.z};
+    float zz = 0.0f, xx = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      float d = r2[k] - r1[k], n = pn[k] - 0.5f * (r1[k] + r2[k]);
+      zz += d * d;
+      xx += n * n;
+    }
+    ix = (int)(sqrtf(xx) * cell.idx_h) + 1;
+    iy = (int)(sqrtf(zz) * cell.idy_h) + 1;
+  }
   ix = min(max(ix, 2), cell.nx - 2);
   iy = min(max(iy, 2), cell.ny - 2);
   int node = (iy - 1) * cell.nx + (ix - 1);
@@ -513,8 +539,12 @@ int launch_trip_bins(const NeighArgs &a, int T, int nsp, int cells, const unsign
   cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
   int threads = 256, blocks = (T + threads - 1) / threads;
-  k_trip_key<<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.isp, a.fd, a.sid, a.xl, a.talpha, a.ci_j, a.ci_b,
-                                        a.cj_j, a.cj_b, binok, key, rank, hist);
+  if (binok)
+    k_trip_key<true><<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.pos4, a.xlf, a.isp, a.fd, a.sid, a.xl,
+                                                a.talpha, a.ci_j, a.ci_b, a.cj_j, a.cj_b, binok, key, rank, hist);
+  else
+    k_trip_key<false><<<blocks, threads, 0, s>>>(T, nsp, cells, a.ratom, a.pos4, a.xlf, a.isp, a.fd, a.sid, a.xl,
+                                                 a.talpha, a.ci_j, a.ci_b, a.cj_j, a.cj_b, binok, key, rank, hist);
   FB_LAUNCH_CHECK();
   k_scan_bins<<<1, 1024, 0, s>>>(nbins, hist);
   FB_LAUNCH_CHECK();
