@@ -126,8 +126,7 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) rb[q] = __ldg(rho + q);
   MolRho<PA, PB, K3C> GA, GB;
-  mol_rho<PA, PB, K3C>(R, DA, rb, GA);
-  mol_rho<PA, PB, K3C>(R, DB, rb, GB);
+  mol_rho_ab<PA, PB, K3C>(R, DA, DB, rb, GA, GB);
   // f3naMa(q, e) = rhat_q dx + amt_q dp and f3naMb(q, e) = -sighat_q dy +
   // bmt_q dp - f3naMa(q, e) / 2 (:334-344) enter only through their sums
   // with G(e): sum_e Ma(q, e) G(e) = rhat_q Sx + amt_q Sp, and

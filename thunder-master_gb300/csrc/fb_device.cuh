@@ -411,6 +411,78 @@ __device__ __forceinline__ void mol_rho(const RotM &R, const DRotM &D, const dou
   });
 }
 
+// mol_rho for the two frame derivatives of a triplet (the neutral atom's and
+// atom 1's) at once: rho R and G are computed once, and rho dR_c is formed
+// once per column and component, then contracted with L^T.  The same sums as
+// two mol_rho calls, with the shared terms taken once.
+template <int PA, int PB, int K>
+__device__ __forceinline__ void mol_rho_ab(const RotM &R, const DRotM &DA, const DRotM &DB, const double *rho,
+                                           MolRho<PA, PB, K> &A, MolRho<PA, PB, K> &Bo) {
+  using PL = Plan<PA, PB, K>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  double rR[NA * NB], rdA[3][NA * NB], rdB[3][NA * NB];
+  sfor<NA>([&](auto MU) {
+    constexpr int mu = decltype(MU)::value;
+    sfor<NB>([&](auto B) {
+      constexpr int b = decltype(B)::value;
+      constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
+      double acc = 0.0;
+      sfor<2 * sb + 1>([&](auto NU) {
+        constexpr int k = decltype(NU)::value;
+        double t = rho[mu + NA * (ob + k)] * Lrot<sb>(R, k, mb);
+        acc = (k == 0) ? t : acc + t;
+      });
+      rR[mu + NA * b] = acc;
+      if constexpr (sb > 0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          double ta = 0.0, tb = 0.0;
+          sfor<2 * sb + 1>([&](auto NU) {
+            constexpr int q = decltype(NU)::value;
+            ta = fma(rho[mu + NA * (ob + q)], DLrot<sb>(DA, c, q, mb), ta);
+            tb = fma(rho[mu + NA * (ob + q)], DLrot<sb>(DB, c, q, mb), tb);
+          });
+          rdA[c][mu + NA * b] = ta;
+          rdB[c][mu + NA * b] = tb;
+        }
+      }
+    });
+  });
+  sfor<PL::m.n>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
+    constexpr int sb = orb_shell(b);
+    double g = 0.0;
+    sfor<2 * sa + 1>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      g = fma(Lrot<sa>(R, k, ma), rR[(oa + k) + NA * b], g);
+    });
+    A.G[e] = g;
+    Bo.G[e] = g;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double ha = 0.0, hb = 0.0;
+      if constexpr (sa > 0) {
+        sfor<2 * sa + 1>([&](auto KK) {
+          constexpr int k = decltype(KK)::value;
+          ha = fma(DLrot<sa>(DA, c, k, ma), rR[(oa + k) + NA * b], ha);
+          hb = fma(DLrot<sa>(DB, c, k, ma), rR[(oa + k) + NA * b], hb);
+        });
+      }
+      if constexpr (sb > 0) {
+        sfor<2 * sa + 1>([&](auto KK) {
+          constexpr int k = decltype(KK)::value;
+          ha = fma(Lrot<sa>(R, k, ma), rdA[c][(oa + k) + NA * b], ha);
+          hb = fma(Lrot<sa>(R, k, ma), rdB[c][(oa + k) + NA * b], hb);
+        });
+      }
+      A.H[c][e] = ha;
+      Bo.H[c][e] = hb;
+    }
+  });
+}
+
 // Explicit Drotate (M_Drotations.f90:102-153, Dmatrix :389-482):
 // Xd[c + 3*(mu + NA*nu)]
 template <int PA, int PB, int K>
