@@ -80,6 +80,7 @@ struct fb_ctx {
   // the triplet lists in the binned order (6 x T ints) for the table
   // kernels, valid for tbin_T triplets
   DevBuf d_tbin;
+  DevBuf d_mlp_pts, d_mlp_ptrip;  // network inputs per routed triplet (tensor-core engine)
   int tbin_T = -1;
   DevBuf d_slot_off, d_slot_nn, d_slot_found, d_rcnt;
   DevBuf d_orb_slot;  // first orbital of each atom (iblock_slot)
@@ -295,7 +296,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
-                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm, &ctx->d_tbin,
+                    &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm, &ctx->d_tbin, &ctx->d_mlp_pts, &ctx->d_mlp_ptrip,
                     &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_rcnt, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
@@ -1437,13 +1438,27 @@ static MlpEvalArgs mlp_eval_args(fb_ctx *ctx) {
 }
 
 static int mlp_launch(fb_ctx *ctx, const MlpEvalArgs &m, const AsmArgs &a, bool tangents) {
+  if (ctx->mlp_engine == FB_MLP_ENGINE_TC && !m.pts) {
+    // inputs first, at full occupancy; the tensor-core kernel reads them
+    MlpEvalArgs mp = m;
+    mp.pts = ctx->d_mlp_pts.as<float>();
+    mp.ptrip = ctx->d_mlp_ptrip.as<int>();
+    int e = launch_mlp_points(m, a, ctx->d_pos4.as<float4>(), ctx->d_xlf.as<float>(), ctx->d_mlp_pts.as<float>(),
+                              ctx->d_mlp_ptrip.as<int>(), ctx->stream);
+    if (e) return e;
+    ctx->launches++;
+    return launch_mlp_tc(mp, a, tangents, ctx->nsm, ctx->stream);
+  }
   if (ctx->mlp_engine == FB_MLP_ENGINE_TC) return launch_mlp_tc(m, a, tangents, ctx->nsm, ctx->stream);
   return launch_mlp_eval(m, a, tangents, ctx->nsm, ctx->stream);
 }
 
 static int prepare_mlp(fb_ctx *ctx, bool forces) {
-  if (mlp_routes(ctx) && ctx->mlp_n > 0)
+  if (mlp_routes(ctx) && ctx->mlp_n > 0) {
     CHK(ctx->d_mlpF.ensure((size_t)ctx->mlp_n * (forces ? 4 : 1) * MLP_ME_STRIDE * sizeof(float)));
+    CHK(ctx->d_mlp_pts.ensure((size_t)ctx->mlp_n * 3 * sizeof(float) + 16));
+    CHK(ctx->d_mlp_ptrip.ensure((size_t)ctx->mlp_n * sizeof(int) + 16));
+  }
   return FB_OK;
 }
 

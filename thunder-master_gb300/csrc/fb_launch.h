@@ -139,6 +139,9 @@ struct MlpEvalArgs;
 int launch_mlp_eval(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
 // the same on the tcgen05 tensor cores (TMEM accumulators)
 int launch_mlp_tc(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s);
+// the network's inputs (x, y, cos; species triple) per list position in float
+int launch_mlp_points(const MlpEvalArgs &m, const AsmArgs &a, const float4 *pos4, const float *xlf, float *pts,
+                      int *ptrip, cudaStream_t s);
 // Bloch sums of up to three block sets (B, C may be null) into nk dense
 // complex n x n matrices at out (column-major, re/im interleaved)
 int launch_bloch(const AsmArgs &a, int P, int nk, const double *kpts, const int *pair_owner, const double *r3v,

@@ -385,6 +385,58 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
   if (warp == 0) tmem_dealloc(tmem, S::cols);
 }
 
+// The network's inputs per list position, ahead of the tensor-core kernel:
+// (x, y, cos theta) of the triplet in float and its species triple.  The
+// inputs enter the network as BF16 hi/lo pairs (16 bits), so float geometry
+// from the float copies of the positions is exact enough, and a thread per
+// triplet at full occupancy takes the position gathers off the
+// one-CTA-per-SM tensor-core kernel (where they were its leading stall).
+// The tails recompute the geometry exactly (fb_dasm3c_df.cu, fb_asm3c_df.cu).
+__global__ void k_mlp_points(int n, const int *__restrict__ list, const int *__restrict__ talpha,
+                             const int *__restrict__ ci_j, const int *__restrict__ ci_b,
+                             const int *__restrict__ cj_j, const int *__restrict__ cj_b, const int *__restrict__ sid,
+                             const int *__restrict__ isp, int nsp, const float4 *__restrict__ pos4,
+                             const float *__restrict__ xlf0, float *__restrict__ pts, int *__restrict__ ptrip) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int t = list[i];
+  int ia = talpha[t], iat = ci_j[t], jat = cj_j[t], ib = ci_b[t], jb = cj_b[t];
+  const float *xl = xlf0 + (long long)sid[ia] * XL_STRIDE;
+  float4 p1 = pos4[iat], p2 = pos4[jat], pa = pos4[ia];
+  float r1[3] = {p1.x + xl[3 * ib], p1.y + xl[3 * ib + 1], p1.z + xl[3 * ib + 2]};
+  float r2[3] = {p2.x + xl[3 * jb], p2.y + xl[3 * jb + 1], p2.z + xl[3 * jb + 2]};
+  float rn[3] = {pa.x, pa.y, pa.z};
+  float r21[3], rc[3], z2 = 0.0f, x2 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r21[k] = r2[k] - r1[k];
+    rc[k] = rn[k] - (r1[k] + 0.5f * r21[k]);
+    z2 += r21[k] * r21[k];
+    x2 += rc[k] * rc[k];
+  }
+  float z = sqrtf(z2), x = sqrtf(x2);
+  float cost = 0.0f;
+  if (x > 1.0e-5f) {
+    if (z < 1.0e-5f) cost = rc[2] / x;  // sighat = (0, 0, 1)
+    else cost = (r21[0] * rc[0] + r21[1] * rc[1] + r21[2] * rc[2]) / (z * x);
+  }
+  pts[3 * i] = x;
+  pts[3 * i + 1] = z;
+  pts[3 * i + 2] = cost;
+  ptrip[i] = (isp[iat] * nsp + isp[jat]) * nsp + isp[ia];
+}
+
+int launch_mlp_points(const MlpEvalArgs &m, const AsmArgs &a, const float4 *pos4, const float *xlf, float *pts,
+                      int *ptrip, cudaStream_t s) {
+  if (m.n == 0) return 0;
+  int threads = 256;
+  k_mlp_points<<<(m.n + threads - 1) / threads, threads, 0, s>>>(m.n, m.list, a.trip_alpha, a.ci_j, a.ci_b, a.cj_j,
+                                                                  a.cj_b, a.sid, a.isp, m.nsp, pos4, xlf, pts,
+                                                                  ptrip);
+  FB_LAUNCH_CHECK();
+  return 0;
+}
+
 int launch_mlp_tc(const MlpEvalArgs &m, const AsmArgs &a, bool tangents, int nsm, cudaStream_t s) {
   if (m.n == 0) return 0;
   Ctx3c c = make3c(a);
