@@ -146,17 +146,25 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # algorithmic work per unit
 # ---------------------------------------------------------------------------
+# Executed FP64 FLOPs per sp3 x sp3 triplet of the FP64 force kernel
+# (2 DFMA + DADD + DMUL: 2,564 + 96 + 311 thread instructions, ncu on
+# SiC4096, profiles/k_dassemble_3c_sic4096.md; the divisions and square roots
+# are DFMA sequences and count in DFMA)
+FP64_FLOP_PER_TRIPLET = 2 * 2563.955 + 96.0 + 310.998
+
+
 def flops_dassemble_3c(nme, prec="df"):
-    """FP64 FLOPs per triplet of the force kernel's formulation.  fp64: the
-    Legendre sums first at each of the 16 stencil nodes (4 + 3 FMA per node
-    and element), then the value, x, y and cos contractions (4 FMA), about
-    100 FLOP of stencil weights; df (the per-theta form of the reference,
-    executed in double-float): value + x + y contractions per theta (5 x 16
-    x 3 FMA per element) and the Legendre combination (4 x 5 FMA).  Both add
-    about 1800 FLOP of geometry, frame derivatives and the molecular-frame
-    density contraction."""
+    """FP64 FLOPs per triplet of the force kernel.  fp64: the FP64 kernel's
+    executed count (ncu), about 3,500 of them the interpolation (Legendre
+    sums first at each of the 16 stencil nodes, 4 + 3 FMA per node and
+    element, then the value, x, y and cos contractions, 4 FMA).  df: the FP64
+    formulation of the per-theta form the double-float kernel executes on
+    the FP32 pipe, value + x + y contractions per theta (5 x 16 x 3 FMA per
+    element), the Legendre combination (4 x 5 FMA) and about 1,800 FLOP of
+    geometry, frame derivatives and the molecular-frame density
+    contraction (its "FP64-equivalent" rate)."""
     if prec == "fp64":
-        return 2.0 * (16 * 11 * nme) + 100.0 + 1800.0
+        return FP64_FLOP_PER_TRIPLET * (nme / 10.0)
     return 2.0 * (3 * 5 * 16 * nme + 4 * 5 * nme) + 1800.0
 
 
@@ -238,8 +246,10 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
             "traffic": round(T * DRAM_BYTES_PER_TRIPLET["fp64"]) if dom == "dassemble_3c" else None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on SiC4096 (%s), "
                               "scaled by triplets" % TRAFFIC_SOURCE["fp64"],
-            "flops_source": "FP64 FLOPs of the kernel's formulation per sp3 x sp3 triplet (Legendre sums at the "
-                            "stencil nodes first), x triplets",
+            "flops_source": "executed FP64 FLOPs per sp3 x sp3 triplet (2 DFMA + DADD + DMUL, ncu on SiC4096, "
+                            "profiles/k_dassemble_3c_sic4096.md) x triplets",
+            "peak_nominal": {"value": round(2.0 * 2.0 * 152 * 2.07e9 / 1e12, 4), "unit": "TFLOP/s",
+                             "what": "2 FP64 lanes per SM per clock x 152 SMs x 2.07 GHz, FMA as 2 FLOP"},
             "peak_source": "of measured: fb_probe_fp64 DFMA chains in this run",
             "flops_per_launch": fl64, "avg_launch_ms": round(dom_ms, 4), "hbm": hbm}
 

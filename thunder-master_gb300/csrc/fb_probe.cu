@@ -3,20 +3,24 @@
 
 namespace fb {
 
-// Each thread runs 8 independent DFMA chains; the result is written only if
-// it is impossible (never), so the chains are not removed.
+// Each thread runs 16 independent DFMA chains, unrolled four iterations
+// deep, so neither the chains' latency nor the loop's own instructions hold
+// the FP64 pipe back; the result is written only if it is impossible
+// (never), so the chains are not removed.
+constexpr int PROBE_CHAINS = 16;
 __global__ void __launch_bounds__(256) k_probe_dfma(int iters, double seed, double *sink) {
-  double a[8];
+  double a[PROBE_CHAINS];
 #pragma unroll
-  for (int k = 0; k < 8; k++) a[k] = seed + 1e-3 * (threadIdx.x + k);
+  for (int k = 0; k < PROBE_CHAINS; k++) a[k] = seed + 1e-3 * (threadIdx.x + k);
   const double m = 0.999999, c = 1e-7;
+#pragma unroll 4
   for (int it = 0; it < iters; it++) {
 #pragma unroll
-    for (int k = 0; k < 8; k++) a[k] = fma(a[k], m, c);
+    for (int k = 0; k < PROBE_CHAINS; k++) a[k] = fma(a[k], m, c);
   }
   double s = 0.0;
 #pragma unroll
-  for (int k = 0; k < 8; k++) s += a[k];
+  for (int k = 0; k < PROBE_CHAINS; k++) s += a[k];
   if (s == -1.2345678e300) sink[0] = s;
 }
 
@@ -24,7 +28,7 @@ int probe_dfma(cudaStream_t s, double *ms, double *flops) {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int blocks = nsm * 8, threads = 256, iters = 8192;
+  int blocks = nsm * 8, threads = 256, iters = 4096;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -41,7 +45,7 @@ int probe_dfma(cudaStream_t s, double *ms, double *flops) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   *ms = t;
-  *flops = 2.0 * 8.0 * (double)iters * (double)blocks * threads;
+  *flops = 2.0 * PROBE_CHAINS * (double)iters * (double)blocks * threads;
   return 0;
 }
 
