@@ -194,9 +194,9 @@ def tuned_shapes(ctx, fbgpu, autotune):
 # arithmetic is what the FP32 pipe must execute.
 DF_FP32_FLOP = {"dassemble_3c": 59053.0, "assemble_3c": 16284.0}
 # DRAM read + write bytes per triplet of one force-kernel launch, ncu on
-# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 160.64 MB per launch;
+# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 159.82 MB per launch;
 # profiles/k_dassemble_3c_df_sic4096.md, 159.78 MB), over 5,125,854 triplets
-DRAM_BYTES_PER_TRIPLET = {"fp64": 160.639232e6 / 5125854, "df": 159.777792e6 / 5125854}
+DRAM_BYTES_PER_TRIPLET = {"fp64": 159.824896e6 / 5125854, "df": 159.777792e6 / 5125854}
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
