@@ -376,7 +376,16 @@ def measure_single(args, ctx, fbgpu, torch, stream, flush, ws, local, st, NB, rh
     h_out = [pin(NB) for _ in range(4)]
     h_f = pin(3 * st.natoms)
 
+    import ctypes as C
+    ptrs = [C.c_void_p(a.ctypes.data) for a in (h_pos, h_rho, h_cape, *h_out, h_f)]
+
     def e2e_step():
+        # one call: positions and density matrices in, S, T, vna, vnao and
+        # ftot out, the copies overlapped with the kernels (fb_step_forces)
+        ctx._check(ctx.L.fb_step_forces(ctx.h, *ptrs))
+
+    def e2e_calls_step():
+        # the same through the separate calls (each copy synchronous)
         ctx.update_positions(h_pos)
         ctx.driver_neighbors()
         ctx.set_denmat(h_rho, h_cape)
@@ -390,20 +399,22 @@ def measure_single(args, ctx, fbgpu, torch, stream, flush, ws, local, st, NB, rh
         device_step()
         if e2e:
             e2e_step()
+            e2e_calls_step()
         kernel_step()
     sampler = ClockSampler(local) if clocks else None
     if sampler:
         sampler.start()
     ms, launches = timed(device_step, steps)
     ms_e2e = timed(e2e_step, steps)[0] if e2e else None
+    ms_e2e_calls = timed(e2e_calls_step, steps)[0] if e2e else None
     clk = sampler.stop() if sampler else None
     out = {k: ctx.blocks(k) for k in ("S", "T", "vna", "vnao")}
     out["ftot"] = ctx.forces("ftot")
     ms_k, _ = timed(kernel_step, steps, timing=True)
     ktimes = ctx.timing()
     ctx.set_timing(False)
-    return {"ms": ms, "ms_e2e": ms_e2e, "launches": launches, "ktimes": ktimes, "ms_k": ms_k, "clocks": clk,
-            "shapes": shapes, "out": out, "prec": PREC_NAME[prec]}
+    return {"ms": ms, "ms_e2e": ms_e2e, "ms_e2e_calls": ms_e2e_calls, "launches": launches, "ktimes": ktimes,
+            "ms_k": ms_k, "clocks": clk, "shapes": shapes, "out": out, "prec": PREC_NAME[prec]}
 
 
 def max_abs_diffs(a, b):
@@ -461,7 +472,13 @@ def run_gpu(args):
                    "step": "fb_neighbors + one CUDA graph launch (assembly + forces)",
                    "launch_shapes": m["shapes"], "autotuned": not args.no_autotune},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(m["ms_e2e"] / args.steps, 4)},
+                "ms_per_step": round(m["ms_e2e"] / args.steps, 4),
+                "how": "fb_step_forces: positions and rho/cape in from pinned host memory, S, T, vna, vnao and "
+                       "ftot out, every step, the copies overlapped with the kernels",
+                "separate_calls": {"value": round(ws * P * args.steps / (m["ms_e2e_calls"] * 1e-3), 1),
+                                   "ms_per_step": round(m["ms_e2e_calls"] / args.steps, 4),
+                                   "how": "fb_update_positions, fb_neighbors, fb_set_denmat, fb_assemble_graph, "
+                                          "fb_get_blocks x 4, fb_get_forces (each copy synchronous)"}},
         "gpu_launches": m["launches"],
         "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in m["ktimes"].items() if v[1]},
         "separate_calls_ms_per_step": round(m["ms_k"] / args.steps, 4),
@@ -973,14 +990,11 @@ def measure_batch(args, torch, fbgpu, ws, local, prec, steps, warmup, e2e=True, 
     h_out = [pin(NB) for _ in range(4)]
     h_f = pin(3 * natoms)
 
+    import ctypes as C
+    ptrs = [C.c_void_p(a.ctypes.data) for a in (h_pos, h_rho, h_cape, *h_out, h_f)]
+
     def e2e_step():
-        ctx.update_positions(h_pos)
-        ctx.driver_neighbors()
-        ctx.set_denmat(h_rho, h_cape)
-        ctx.assemble_graph(step_what)
-        for key, buf in zip(("S", "T", "vna", "vnao"), h_out):
-            ctx._check(ctx.L.fb_get_blocks(ctx.h, fbgpu.BLOCK[key], buf))
-        ctx._check(ctx.L.fb_get_forces(ctx.h, fbgpu.FORCE["ftot"], h_f))
+        ctx._check(ctx.L.fb_step_forces(ctx.h, *ptrs))
 
     timed = make_timer(torch, ctx, stream, flush, ws, local)
     for _ in range(warmup):

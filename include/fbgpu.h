@@ -240,6 +240,23 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out);
 /* End-to-end H/S step through host buffers: upload positions, build the
  * neighbor maps, assemble S, T, vna (2c + 3c) and copy the four block sets
  * back.  Any output may be NULL. */
+/* One step with forces through host buffers, the copies overlapped with the
+ * kernels: upload the positions (ratom may be NULL: unchanged), build the
+ * neighbor maps, then the value pass (assemble_S, assemble_T,
+ * assemble_vna_2c/3c) while rho and cape (nblock doubles each, block layout
+ * of the maps just built; cape may be NULL) travel on a copy stream, then the
+ * force pass (Dassemble_S/T/vna_2c/vna_3c, build_forces) while S, T and vnao
+ * travel back; vna and ftot (3*natoms) follow.  Any output may be NULL.  The
+ * same results as fb_neighbors + fb_set_denmat + fb_assemble_graph(FB_ALL |
+ * FB_FORCES) + fb_get_blocks + fb_get_forces; pinned host buffers let the
+ * copies overlap.  Harris only.  Replaces one SCF/MD step's calls of
+ * assemble_S/T/vna_2c/vna_3c (j.ASSEMBLERS/M_assemble_2c_Harris.f90:89-649,
+ * M_assemble_3c_Harris.f90:82-227) and Dassemble_* + build_forces
+ * (k.DASSEMBLERS/M_Dassemble_2c_Harris.f90:96-869,
+ * M_Dassemble_3c_Harris.f90:136-408, c.SYSTEM/M_build_forces.f90:172-588). */
+int fb_step_forces(fb_ctx *ctx, const double *ratom, const double *rho,
+                   const double *cape, double *S, double *T, double *vna,
+                   double *vnao, double *ftot);
 int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T,
                      double *vna, double *vnao);
 

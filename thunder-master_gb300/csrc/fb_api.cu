@@ -46,6 +46,10 @@ static const char *tk_names[TK_N] = {"assemble_2c", "assemble_3c", "dassemble_2c
 struct fb_ctx {
   int device = 0;
   cudaStream_t own = nullptr, stream = nullptr;
+  // fb_step_forces: a copy stream and its events (host <-> device copies
+  // overlapped with the kernels)
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_val = nullptr, ev_frc = nullptr;
   // set while a graph of a value + force pass is captured: the force pass's
   // three-center table kernel also adds the value-pass vna terms, and the
   // value pass skips its three-center table kernel
@@ -318,6 +322,10 @@ void fb_destroy(fb_ctx *ctx) {
     cudaEventDestroy(e.second);
   }
   if (ctx->own) cudaStreamDestroy(ctx->own);
+  if (ctx->cstream) cudaStreamDestroy(ctx->cstream);
+  cudaEvent_t evs[] = {ctx->ev_in, ctx->ev_val, ctx->ev_frc};
+  for (cudaEvent_t e : evs)
+    if (e) cudaEventDestroy(e);
   delete ctx;
 }
 
@@ -2135,6 +2143,64 @@ int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T, dou
   if (T && (st = fb_get_blocks(ctx, FB_BLOCK_T, T))) return st;
   if (vna && (st = fb_get_blocks(ctx, FB_BLOCK_VNA, vna))) return st;
   if (vnao && (st = fb_get_blocks(ctx, FB_BLOCK_VNAO, vnao))) return st;
+  return FB_OK;
+}
+
+int fb_step_forces(fb_ctx *ctx, const double *ratom, const double *rho, const double *cape, double *S, double *T,
+                   double *vna, double *vnao, double *ftot) {
+  if (!ctx || !rho) return FB_ERR_ARG;
+  if (ctx->theory != FB_THEORY_HARRIS) return fail(ctx, FB_ERR_UNSUPPORTED, "fb_step_forces: Harris only");
+  CU(cudaSetDevice(ctx->device));
+  if (!ctx->cstream) CU(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
+  cudaEvent_t *evs[] = {&ctx->ev_in, &ctx->ev_val, &ctx->ev_frc};
+  for (cudaEvent_t *e : evs)
+    if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  int st;
+  if (ratom && (st = fb_update_positions(ctx, ratom))) return st;
+  if ((st = fb_neighbors(ctx))) return st;
+  size_t bb = (size_t)ctx->nblock * sizeof(double);
+  CHK(ctx->d_rho.ensure(bb + 8));
+  CHK(ctx->d_cape.ensure(bb + 8));
+  const unsigned what = FB_ALL;
+  CHK(check_assemble(ctx, what));
+  CHK(prepare_mlp(ctx, true));
+  ctx->have_rho = true;
+  CHK(prepare_dassemble(ctx, what, true));
+  // the density matrices travel on the copy stream while the value pass runs
+  CU(cudaMemcpyAsync(ctx->d_rho.p, rho, bb, cudaMemcpyHostToDevice, ctx->cstream));
+  if (cape) CU(cudaMemcpyAsync(ctx->d_cape.p, cape, bb, cudaMemcpyHostToDevice, ctx->cstream));
+  else CU(cudaMemsetAsync(ctx->d_cape.p, 0, bb, ctx->cstream));
+  CU(cudaEventRecord(ctx->ev_in, ctx->cstream));
+  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+  ctx->fuse3c = true;  // one interpolation per triplet, as in the graph step
+  st = enqueue_assemble(ctx, what);
+  if (!st && cudaEventRecord(ctx->ev_val, ctx->stream) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event record");
+  if (!st && cudaStreamWaitEvent(ctx->stream, ctx->ev_in, 0) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event wait");
+  if (!st) st = enqueue_dassemble(ctx, what);
+  ctx->fuse3c = false;
+  if (st) {
+    cudaStreamSynchronize(ctx->cstream);
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+  }
+  CU(cudaEventRecord(ctx->ev_frc, ctx->stream));
+  // S, T and vnao are final after the value pass: they travel back while
+  // the force pass runs; vna (2c + 3c) and ftot after it
+  CU(cudaStreamWaitEvent(ctx->cstream, ctx->ev_val, 0));
+  if (S) CU(cudaMemcpyAsync(S, ctx->d_S.p, bb, cudaMemcpyDeviceToHost, ctx->cstream));
+  if (T) CU(cudaMemcpyAsync(T, ctx->d_T.p, bb, cudaMemcpyDeviceToHost, ctx->cstream));
+  if (vnao) CU(cudaMemcpyAsync(vnao, ctx->d_vbo.p, bb, cudaMemcpyDeviceToHost, ctx->cstream));
+  CU(cudaStreamWaitEvent(ctx->cstream, ctx->ev_frc, 0));
+  if (vna) CU(cudaMemcpyAsync(vna, ctx->d_vb.p, bb, cudaMemcpyDeviceToHost, ctx->cstream));
+  if (ftot)
+    CU(cudaMemcpyAsync(ftot, ctx->d_ftot.p, (size_t)3 * ctx->N * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->cstream));
+  CU(cudaStreamSynchronize(ctx->cstream));
+  unsigned stt = 0;
+  CHK(sync_status(ctx, &stt));
+  if (stt) return status_error(ctx, stt);
+  assemble_done(ctx, what);
+  dassemble_done(ctx, what);
   return FB_OK;
 }
 

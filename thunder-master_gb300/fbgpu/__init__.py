@@ -91,6 +91,7 @@ _SIGS = {
     "fb_bloch": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p]),
     "fb_bloch_device": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fb_solve_k": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_void_p, _dp, C.c_void_p, C.c_void_p]),
+    "fb_step_forces": (C.c_int, [C.c_void_p] + [C.c_void_p] * 8),
     "fb_mlp_nparams": (C.c_longlong, [C.c_void_p]),
     "fb_mlp_layout": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fb_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -431,6 +432,18 @@ class Context:
                                            None if extra_ptr is None else C.c_void_p(extra_ptr),
                                            None if hk_ptr is None else C.c_void_p(hk_ptr),
                                            None if sk_ptr is None else C.c_void_p(sk_ptr)))
+
+    def step_forces(self, ratom, rho, cape, S=None, T=None, vna=None, vnao=None, ftot=None):
+        """One value + force step through host arrays (fb_step_forces).  The
+        outputs (C-contiguous float64 arrays of nblock or 3*natoms, or None)
+        are filled in place; pinned arrays let the copies overlap."""
+        ins = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (ratom, rho, cape)]
+        outs = (S, T, vna, vnao, ftot)
+        for o in outs:
+            if o is not None and not (o.dtype == np.float64 and o.flags.c_contiguous):
+                raise ValueError("outputs must be C-contiguous float64 arrays")
+        ptr = lambda x: None if x is None else C.c_void_p(x.ctypes.data)
+        self._check(self.L.fb_step_forces(self.h, *[ptr(x) for x in ins], *[ptr(o) for o in outs]))
 
     def solve_k(self, kpts, c_ptr=None, extra_ptr=None):
         """kspace_Lowdin per k-point: (band energies (nk, n) ascending,
