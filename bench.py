@@ -200,7 +200,7 @@ DRAM_BYTES_PER_TRIPLET = {"fp64": 159.824896e6 / 5125854, "df": 159.777792e6 / 5
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
-def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
+def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df", sm_mhz=None):
     """Roofline of the dominant kernel from its CUDA-event launch times.
     Double-float kernels run on the FP32 pipe: achieved = executed FP32
     FLOPs per launch / launch time against the FP32 FFMA peak probed in the
@@ -241,16 +241,25 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df"):
                                     "fp64_peak": round(fp64_peak, 4), "unit": "TFLOP/s",
                                     "ratio_to_fp64_peak": round(ach64 / fp64_peak, 4)},
                 "hbm": hbm}
-    return {"bound": "fp64", "kernel": dom, "achieved": round(ach64, 4), "peak": round(fp64_peak, 4),
-            "unit": "TFLOP/s", "frac": round(ach64 / fp64_peak, 4),
+    # The FP64 pipe executes 2 lanes per SM per clock (an FMA counting as 2
+    # FLOP): its rate at the clock sampled under load is the peak.  The
+    # DFMA-chain probe is reported beside it; it reaches about 84 % of that
+    # rate, below what this kernel's mix of DFMA, DMUL and DADD issues.
+    import torch
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    pipe_peak = 4.0 * nsm * (sm_mhz or 2070.0) * 1e6 / 1e12
+    return {"bound": "fp64", "kernel": dom, "achieved": round(ach64, 4), "peak": round(pipe_peak, 4),
+            "unit": "TFLOP/s", "frac": round(ach64 / pipe_peak, 4),
             "traffic": round(T * DRAM_BYTES_PER_TRIPLET["fp64"]) if dom == "dassemble_3c" else None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on SiC4096 (%s), "
                               "scaled by triplets" % TRAFFIC_SOURCE["fp64"],
             "flops_source": "executed FP64 FLOPs per sp3 x sp3 triplet (2 DFMA + DADD + DMUL, ncu on SiC4096, "
                             "profiles/k_dassemble_3c_sic4096.md) x triplets",
-            "peak_nominal": {"value": round(2.0 * 2.0 * 152 * 2.07e9 / 1e12, 4), "unit": "TFLOP/s",
-                             "what": "2 FP64 lanes per SM per clock x 152 SMs x 2.07 GHz, FMA as 2 FLOP"},
-            "peak_source": "of measured: fb_probe_fp64 DFMA chains in this run",
+            "peak_source": "FP64 pipe rate: 2 lanes per SM per clock x %d SMs x %.0f MHz (median SM clock sampled "
+                           "during the timed region), FMA as 2 FLOP; no FP64 figure in MEASURED_PEAKS.json"
+                           % (nsm, sm_mhz or 2070.0),
+            "probe": {"value": round(fp64_peak, 4), "unit": "TFLOP/s", "frac": round(ach64 / fp64_peak, 4),
+                      "what": "fb_probe_fp64: 16 independent DFMA chains per thread, 64 warps per SM, in this run"},
             "flops_per_launch": fl64, "avg_launch_ms": round(dom_ms, 4), "hbm": hbm}
 
 
@@ -459,7 +468,8 @@ def run_gpu(args):
     e2e_value = ws * P * args.steps / (m["ms_e2e"] * 1e-3)
     h2d = 3 * st.natoms * 8 + 2 * NB * 8
     d2h = 4 * NB * 8 + 3 * st.natoms * 8
-    roof = roofline_for(ctx, m["ktimes"], T, P, st.natoms, nZ, args.steps, m["prec"])
+    roof = roofline_for(ctx, m["ktimes"], T, P, st.natoms, nZ, args.steps, m["prec"],
+                        (m["clocks"] or {}).get("sm_mhz"))
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_step, 4), "higher_is_better": True, "scaling": "weak",
@@ -494,7 +504,8 @@ def run_gpu(args):
                               "ms_per_step": round(o["ms_e2e"] / args.steps, 4)},
         "speedup_vs_headline": round(m["ms"] / o["ms"], 4),
         "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in o["ktimes"].items() if v[1]},
-        "roofline": roofline_for(ctx, o["ktimes"], T, P, st.natoms, nZ, args.steps, o["prec"]),
+        "roofline": roofline_for(ctx, o["ktimes"], T, P, st.natoms, nZ, args.steps, o["prec"],
+                                 (m["clocks"] or {}).get("sm_mhz")),
         "launch_shapes": o["shapes"],
         "max_abs_diff_vs_headline": max_abs_diffs(o["out"], m["out"])}
     legs = set(args.legs.split(",")) if args.legs != "none" else set()
