@@ -1516,7 +1516,9 @@ static int enqueue_assemble(fb_ctx *ctx, unsigned what) {
     } else if (use_df(ctx)) KL(KT_ASM3C, launch_assemble_3c_df(at, ctx->stream));
     else if (use_df_dogs(ctx)) KL(KT_ASM3C, launch_assemble_3c_dogs_df(at, ctx->stream));
     else KL(KT_ASM3C, launch_assemble_3c(at, ctx->stream));
-    if (nm > 0) {
+    if (nm > 0 && !ctx->fuse3c) {
+      // (fused step: the force pass's network evaluation gives the values
+      // too, and its tail adds the value terms)
       KL(KT_MLP_EVAL, mlp_launch(ctx, mlp_eval_args(ctx), a, false));
       AsmArgs am = a;
       am.ntrip = nm;
@@ -1797,6 +1799,7 @@ static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
       AsmArgs am = a;
       am.ntrip = nm;
       am.mlpF = ctx->d_mlpF.as<float>();
+      am.fuse_value = ctx->fuse3c;
       KL(KT_DASM3C_MLP, launch_dassemble_3c_mlp(am, ctx->stream));
     }
   }

@@ -150,7 +150,8 @@ int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s) {
   Sched q;
   int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
   if (e) return e;
-  k_dassemble_3c_df<true, false><<<grid, block, 0, s>>>(c, q);
+  if (a.fuse_value) k_dassemble_3c_df<true, true><<<grid, block, 0, s>>>(c, q);
+  else k_dassemble_3c_df<true, false><<<grid, block, 0, s>>>(c, q);
   FB_LAUNCH_CHECK();
   return 0;
 }
