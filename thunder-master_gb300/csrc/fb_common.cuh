@@ -139,6 +139,7 @@ struct Ctx3c {
 struct TripGeom {
   double r1[3], r2[3], rna[3], r21[3], rnabc[3], sighat[3], rhat[3], z, x, cost;
   double e[3][3];
+  bool estd;  // e has its y axis along sighat x rhat (not the collinear fallback)
 };
 
 // set-up of M_assemble_3c_Harris.f90:154-189
@@ -177,7 +178,39 @@ __device__ __forceinline__ void trip_geom(const Ctx3c &c, int t, int &ia, int &i
     for (int k = 0; k < 3; k++) g.rhat[k] = g.rnabc[k] * ix;
   }
   g.cost = g.sighat[0] * g.rhat[0] + g.sighat[1] * g.rhat[1] + g.sighat[2] * g.rhat[2];
-  epsilon_fn(g.rhat, g.sighat, g.e);
+  g.estd = epsilon_fn(g.rhat, g.sighat, g.e);
+}
+
+// The frame-derivative terms of a triplet's three-center forces for s and p
+// shells: hA_c = sum_e M_e H_c(e) for d/dratm and hB_c for d/dr1, H the
+// Dtwister derivative (M_Drotations.f90:456-471) contracted with the
+// density, through the rotation rates of the frame (frame_rates_3c; the
+// collinear fallback frame through frame_extra_3c).  Gf is L^T rho L over
+// the whole block (mol_G_full), M the molecular-frame block at the ME
+// positions.
+template <int PA, int PB>
+__device__ __forceinline__ void frame_terms_3c(const TripGeom &g, const double *Gf, const double *M, double hA[3],
+                                               double hB[3]) {
+  double tau[3];
+  mol_tau<PA, PB>(Gf, M, tau);
+  FrameRates3c w;
+  frame_rates_3c(g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, w);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    hA[q] = w.axy[q] * tau[0];
+    hB[q] = fma(w.bxz[q], tau[2], fma(w.byz[q], tau[1], w.bxy[q] * tau[0]));
+  }
+  if (!g.estd) {
+    FrameExtra3c x;
+    frame_extra_3c(g.r1, g.r2, g.r21, g.rna, g.rnabc, g.e, x);
+    double kd, kzy;
+    mol_kappa_extra<PA, PB>(Gf, M, kd, kzy);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      hA[q] = fma(x.psiA[q], kd, hA[q]);
+      hB[q] = fma(x.chiB[q] + w.byz[q], kzy, fma(x.psiB[q], kd, hB[q]));
+    }
+  }
 }
 
 // getMEs_Fdata_3c / getDMEs_Fdata_3c (e.FDATA/M_Fdata_3c.f90:293-846):

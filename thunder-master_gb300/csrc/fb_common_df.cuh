@@ -36,6 +36,7 @@ struct GeomDF {
   df rh[3];   // rhat
   df cost, iz, ix;
   df e[3][3];  // epsilon(rhat, sighat)
+  bool estd;   // e has its y axis along sighat x rhat (not the collinear fallback)
 };
 
 // FP64 part of the set-up: what the table cell depends on, and the exact
@@ -119,7 +120,8 @@ __device__ __forceinline__ void trip_geom_df_from(const GeomFP64 &h, GeomDF &g) 
     for (int k = 0; k < 3; k++) yp[k] = cross_df(g.sig, g.rh, k);
     ypm2 = (yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]).h;
   }
-  if (!hasr || ypm2 < 1.0e-8f) {
+  g.estd = hasr && !(ypm2 < 1.0e-8f);
+  if (!g.estd) {
     // colinear fallback (:148-168), first non-zero component of zphat
     if (fabsf(g.sig[0].h) > 1.0e-4f) {
       yp[0] = -(g.sig[1] + g.sig[2]) * df_rcp(g.sig[0]);
@@ -320,11 +322,11 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
 // ---------------------------------------------------------------------------
 // three-center force helpers shared by the df force kernels
 // ---------------------------------------------------------------------------
-// Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189) in df, evaluated with the
-// origin at atom 1.  Its expressions are translation invariant (the three
-// coefficients of each bracket sum to zero), and relative coordinates avoid
-// the cancellation of absolute squared norms: u = r2 - r1, v = ratm - r1.
-// The quantities shared by the three Cartesian components:
+// The scalars of Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189) in df,
+// evaluated with the origin at atom 1.  Its expressions are translation
+// invariant (the three coefficients of each bracket sum to zero), and
+// relative coordinates avoid the cancellation of absolute squared norms:
+// u = r2 - r1, v = ratm - r1.
 struct DepsPre {
   df ic, A1, A2, B1, B2;
   df vu[3];
@@ -347,79 +349,61 @@ __device__ __forceinline__ void depsilon_pre_df(const df u[3], const df v[3], De
   p.B2 = -(v[0] * p.vu[0] + v[1] * p.vu[1] + v[2] * p.vu[2]);
 }
 
-// component ix of deps/dratm (dA[imu][k]) and deps/dr1 (dB[imu][k])
-__device__ __forceinline__ void depsilon_comp_df(int ix, const df u[3], const df v[3], df iz, const df e[3][3],
-                                                 const DepsPre &p, df dA[3][3], df dB[3][3]) {
-#pragma unroll
-  for (int a = 0; a < 3; a++)
-#pragma unroll
-    for (int b = 0; b < 3; b++) dA[a][b] = dB[a][b] = df_zero();
-  if (p.zero) return;
-#pragma unroll
-  for (int imu = 0; imu < 3; imu++) {
-    df sa = df_zero(), sb = df_zero();
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      double lv = levi(ix, imu, k);
-      if (lv > 0.0) {
-        sa = sa + u[k];
-        sb = sb + p.vu[k];
-      } else if (lv < 0.0) {
-        sa = sa - u[k];
-        sb = sb - p.vu[k];
-      }
-    }
-    df ei = e[imu][1] * p.ic;
-    dA[imu][1] = p.ic * (sa - ei * (p.A1 * v[ix] + p.A2 * u[ix]));
-    dB[imu][1] = p.ic * (sb - ei * (p.B1 * v[ix] + p.B2 * u[ix]));
-    df t = e[imu][2] * e[ix][2];
-    dB[imu][2] = iz * ((ix == imu) ? t - df_one() : t);
-  }
-  dA[0][0] = e[2][2] * dA[1][1] - e[1][2] * dA[2][1];
-  dA[1][0] = e[0][2] * dA[2][1] - e[2][2] * dA[0][1];
-  dA[2][0] = e[1][2] * dA[0][1] - e[0][2] * dA[1][1];
-  dB[0][0] = e[2][2] * dB[1][1] - e[2][1] * dB[1][2] - e[1][2] * dB[2][1] + e[1][1] * dB[2][2];
-  dB[1][0] = e[0][2] * dB[2][1] - e[0][1] * dB[2][2] - e[2][2] * dB[0][1] + e[2][1] * dB[0][2];
-  dB[2][0] = e[1][2] * dB[0][1] - e[1][1] * dB[0][2] - e[0][2] * dB[1][1] + e[0][1] * dB[1][2];
-}
-
-// sum_e M_e H(e) for one Cartesian component, H = dL^T rho R + L^T rho dR at
-// the ME positions (the dL M R^T and L M dR^T terms of Dmatrix,
-// M_Drotations.f90:456-471, contracted with rho); dP is that component of
-// the p-shell rotation derivative (Dtwister, :236-249): dP[a][b] =
-// deps(perm a, perm b)
+// Molecular-frame density of a triplet's block: Gf = L^T rho L over the
+// whole block and G at the ME positions
 template <int PA, int PB>
-__device__ __forceinline__ df mol_HM_df(const RotDF &R, const df dP[3][3], const df *rho, const df *rR,
-                                        const df *M) {
+__device__ __forceinline__ void mol_density_df(const RotDF &R, const df *rb, df *Gf, df *G) {
   using PL = Plan<PA, PB, K3C>;
   constexpr int NA = PL::NA;
-  df acc = df_zero();
+  mol_G_full_df<PA, PB>(R, rb, Gf);
   sfor<PL::m.n>([&](auto E) {
     constexpr int e = decltype(E)::value;
-    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
-    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
-    constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
-    df h = df_zero();
-    if constexpr (sa > 0) {
-      sfor<3>([&](auto KK) {
-        constexpr int k = decltype(KK)::value;
-        h = h + dP[k][ma] * rR[(oa + k) + NA * b];
-      });
-    }
-    if constexpr (sb > 0) {
-      sfor<2 * sa + 1>([&](auto KK) {
-        constexpr int k = decltype(KK)::value;
-        df t = df_zero();
-        sfor<3>([&](auto NU) {
-          constexpr int q = decltype(NU)::value;
-          t = t + rho[(oa + k) + NA * (ob + q)] * dP[q][mb];
-        });
-        h = h + ((sa == 0) ? t : Lrot_df<sa>(R, k, ma) * t);
-      });
-    }
-    acc = acc + M[e] * h;
+    constexpr int at = PL::m.mu[e] + NA * PL::m.nu[e];
+    G[e] = Gf[at];
   });
-  return acc;
+}
+
+// The frame-derivative terms of a triplet's three-center forces (s and p
+// shells) in df: hA_c = sum_e M_e H_c(e) for d/dratm, hB_c for d/dr1, H the
+// Dtwister derivative contracted with the density, through the rotation
+// rates of the frame (frame_rates_3c and frame_extra_3c in fb_device.cuh),
+// with the origin at atom 1: u = r21, v = ratm - r1, ratm - r2 = v - u.
+template <int PA, int PB>
+__device__ __forceinline__ void frame_terms_3c_df(const GeomDF &g, const df *Gf, const df *M, df hA[3], df hB[3]) {
+  df tau[3];
+  mol_tau_df<PA, PB>(Gf, M, tau);
+  DepsPre pre;
+  depsilon_pre_df(g.u, g.v, pre);
+  const df izr = pre.zero ? df_zero() : g.iz;
+  df ex[3], ey[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ex[k] = g.e[k][0];
+    ey[k] = g.e[k][1];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    df axy = pre.ic * cross_df(ex, g.u, k);
+    df bxy = pre.ic * cross_df(ex, pre.vu, k);
+    hA[k] = axy * tau[0];
+    hB[k] = bxy * tau[0] - (izr * ey[k]) * tau[1] - (izr * ex[k]) * tau[2];
+  }
+  if (!g.estd) {
+    // epsilon's collinear fallback frame: V = A1 v + A2 u, V' = B1 v + B2 u
+    df kd, kzy;
+    mol_kappa_extra_df<PA, PB>(Gf, M, kd, kzy);
+    df ez[3] = {g.e[0][2], g.e[1][2], g.e[2][2]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      df V = pre.A1 * g.v[k] + pre.A2 * g.u[k];
+      df Vb = pre.B1 * g.v[k] + pre.B2 * g.u[k];
+      df psiA = pre.ic * (cross_df(ey, g.u, k) - pre.ic * V);
+      df psiB = pre.ic * (cross_df(ey, pre.vu, k) - pre.ic * Vb);
+      df chiB = pre.ic * cross_df(ez, pre.vu, k);
+      hA[k] = hA[k] + psiA * kd;
+      hB[k] = hB[k] + psiB * kd + (chiB - izr * ey[k]) * kzy;
+    }
+  }
 }
 
 }  // namespace fb

@@ -25,8 +25,6 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   TripGeom g;
   trip_geom(c, t, ia, iat, jat, g);
   const Cell3cDev &cell = c.fd->c3[c.isp[iat]][c.isp[jat]][c.isp[ia]];
-  double dA[3][3][3], dB[3][3][3];
-  depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
   double amt[3], bmt[3];
   if (g.x > 1.0e-5) {
     double ix = 1.0 / g.x;
@@ -118,15 +116,46 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
 #pragma unroll
     for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, X[q] * P_eq2);
   }
-  DRotM DA, DB;
-  dtwister<HASD>(g.e, dA, DA);
-  dtwister<HASD>(g.e, dB, DB);
   const double *rho = c.rho + c.blk_off[c.tdst[t]];
   double rb[NA * NB];
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) rb[q] = __ldg(rho + q);
-  MolRho<PA, PB, K3C> GA, GB;
-  mol_rho_ab<PA, PB, K3C>(R, DA, DB, rb, GA, GB);
+  // G(e): the density in the molecular frame at the ME positions; hA, hB:
+  // sum_e M_e H_c(e), the frame-derivative terms of the neutral atom's and
+  // atom 1's coordinates (Dtwister, M_Drotations.f90:456-471, contracted
+  // with rho)
+  double Ge[NE], hA[3], hB[3];
+  if constexpr (NA <= 4 && NB <= 4) {
+    double Gf[NA * NB];
+    mol_G_full<PA, PB>(R, rb, Gf);
+    sfor<NE>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      constexpr int at = PL::m.mu[e] + NA * PL::m.nu[e];
+      Ge[e] = Gf[at];
+    });
+    frame_terms_3c<PA, PB>(g, Gf, M, hA, hB);
+  } else {
+    double dA[3][3][3], dB[3][3][3];
+    depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
+    DRotM DA, DB;
+    dtwister<HASD>(g.e, dA, DA);
+    dtwister<HASD>(g.e, dB, DB);
+    MolRho<PA, PB, K3C> GA, GB;
+    mol_rho_ab<PA, PB, K3C>(R, DA, DB, rb, GA, GB);
+#pragma unroll
+    for (int e = 0; e < NE; e++) Ge[e] = GA.G[e];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double sa = 0.0, sb = 0.0;
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        sa = fma(M[e], GA.H[q][e], sa);
+        sb = fma(M[e], GB.H[q][e], sb);
+      }
+      hA[q] = sa;
+      hB[q] = sb;
+    }
+  }
   // f3naMa(q, e) = rhat_q dx + amt_q dp and f3naMb(q, e) = -sighat_q dy +
   // bmt_q dp - f3naMa(q, e) / 2 (:334-344) enter only through their sums
   // with G(e): sum_e Ma(q, e) G(e) = rhat_q Sx + amt_q Sp, and
@@ -134,20 +163,16 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   double Sx = 0.0, Sy = 0.0, Sp = 0.0;
 #pragma unroll
   for (int e = 0; e < NE; e++) {
-    Sx = fma(Dx[e], GA.G[e], Sx);
-    Sy = fma(Dy[e], GA.G[e], Sy);
-    Sp = fma(Dp[e], GA.G[e], Sp);
+    Sx = fma(Dx[e], Ge[e], Sx);
+    Sy = fma(Dy[e], Ge[e], Sy);
+    Sp = fma(Dp[e], Ge[e], Sp);
   }
   double fa[3], fb[3];
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     double ga = fma(g.rhat[q], Sx, amt[q] * Sp);
-    double sa = ga, sb = fma(-g.sighat[q], Sy, fma(bmt[q], Sp, -0.5 * ga));
-#pragma unroll
-    for (int e = 0; e < NE; e++) {
-      sa = fma(M[e], GA.H[q][e], sa);
-      sb = fma(M[e], GB.H[q][e], sb);
-    }
+    double sa = ga + hA[q];
+    double sb = fma(-g.sighat[q], Sy, fma(bmt[q], Sp, -0.5 * ga)) + hB[q];
     fa[q] = -sa * P_eq2;
     fb[q] = -sb * P_eq2;
   }
@@ -157,7 +182,7 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
     // contracted with rho of the pair
     double cx = 0.0;
 #pragma unroll
-    for (int e = 0; e < NE; e++) cx = fma(Fq[e], GA.G[e], cx);
+    for (int e = 0; e < NE; e++) cx = fma(Fq[e], Ge[e], cx);
     const double *ps = c.dogs_ps + 8 * (long long)c.tdst[t];
     double sterm = 0.5 * ps[0], dterm = ps[1] / g.z;
     double am = sterm - dterm, ap = sterm + dterm;

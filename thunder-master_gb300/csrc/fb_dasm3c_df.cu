@@ -62,11 +62,10 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
     for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, df_to(X[q] * pe));
   }
   const df *rho = c.rho_df + c.blk_off[c.tdst[t]];
-  df rb[NA * NB], rR[NA * NB], G[NE];
+  df rb[NA * NB], Gf[NA * NB], G[NE];
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) rb[q] = rho[q];
-  mol_rR_df<PA, PB, K3C>(R, rb, rR);
-  mol_G_df<PA, PB, K3C>(R, rR, G);
+  mol_density_df<PA, PB>(R, rb, Gf, G);
   // the f3naMa / f3naMb terms (:334-344) enter only through
   // sum_e Ma(q,e) G(e) = rhat_q Sx + amt_q Sp and
   // sum_e Mb(q,e) G(e) = bmt_q Sp - sighat_q Sy - (rhat_q Sx + amt_q Sp)/2
@@ -77,34 +76,21 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
     Sy = Sy + DyF[e] * G[e];
     Sp = Sp + DpF[e] * G[e];
   }
-  DepsPre pre;
-  depsilon_pre_df(g.u, g.v, pre);
+  // frame-derivative terms (Dtwister contracted with rho) through the
+  // rotation rates of the frame
+  df hA[3], hB[3];
+  frame_terms_3c_df<PA, PB>(g, Gf, F, hA, hB);
   const df peq2 = peq2_df();
   double fa[3], fb[3];
-#pragma unroll 1
+#pragma unroll
   for (int q = 0; q < 3; q++) {
-    df dA[3][3], dB[3][3];
-    depsilon_comp_df(q, g.u, g.v, iz, g.e, pre, dA, dB);
-    df dPA[3][3], dPB[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-        dPA[a][b] = dA[pperm(a)][pperm(b)];
-        dPB[a][b] = dB[pperm(a)][pperm(b)];
-      }
-    df amt = (g.x > 1.0e-5) ? (sel3(g.sig, q) - cost * sel3(g.rh, q)) * g.ix : df_zero();
-    df bmt = (cost * sel3(g.sig, q) - sel3(g.rh, q)) * iz;
-    df ga = sel3(g.rh, q) * Sx + amt * Sp;
-    df sa = mol_HM_df<PA, PB>(R, dPA, rb, rR, F) + ga;
-    df sb = mol_HM_df<PA, PB>(R, dPB, rb, rR, F) + ((bmt * Sp - sel3(g.sig, q) * Sy) - ga * 0.5f);
-    double va = -df_to(sa * peq2), vb = -df_to(sb * peq2);
-    fa[0] = q == 0 ? va : fa[0];
-    fa[1] = q == 1 ? va : fa[1];
-    fa[2] = q == 2 ? va : fa[2];
-    fb[0] = q == 0 ? vb : fb[0];
-    fb[1] = q == 1 ? vb : fb[1];
-    fb[2] = q == 2 ? vb : fb[2];
+    df amt = (g.x > 1.0e-5) ? (g.sig[q] - cost * g.rh[q]) * g.ix : df_zero();
+    df bmt = (cost * g.sig[q] - g.rh[q]) * iz;
+    df ga = g.rh[q] * Sx + amt * Sp;
+    df sa = ga + hA[q];
+    df sb = ((bmt * Sp - g.sig[q] * Sy) - ga * 0.5f) + hB[q];
+    fa[q] = -df_to(sa * peq2);
+    fb[q] = -df_to(sb * peq2);
   }
 #pragma unroll
   for (int q = 0; q < 3; q++) {

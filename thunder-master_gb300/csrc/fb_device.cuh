@@ -58,7 +58,9 @@ __device__ __forceinline__ double dist_rn(const double *a, const double *b) {
 // ---------------------------------------------------------------------------
 // epsilon_function (b.FUNCTIONS/epsilon.f90:73-202): e[i][j] = spe(i+1,j+1)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void epsilon_fn(const double *r1, const double *r2, double e[3][3]) {
+// Returns true when the y axis is r2 x r1 normalised (the standard frame),
+// false for the identity or the fallback y axis of a collinear pair.
+__device__ __forceinline__ bool epsilon_fn(const double *r1, const double *r2, double e[3][3]) {
   double r1m = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
   double r2m = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
   if (r2m < 1.0e-4) {
@@ -66,7 +68,7 @@ __device__ __forceinline__ void epsilon_fn(const double *r1, const double *r2, d
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) e[i][j] = (i == j) ? 1.0 : 0.0;
-    return;
+    return false;
   }
   double inv2 = 1.0 / r2m;
   double zp[3] = {r2[0] * inv2, r2[1] * inv2, r2[2] * inv2};
@@ -79,7 +81,8 @@ __device__ __forceinline__ void epsilon_fn(const double *r1, const double *r2, d
     yp[2] = zp[0] * h1 - zp[1] * h0;
     ypm = sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]);
   }
-  if (ypm < 1.0e-4) {
+  const bool standard = !(ypm < 1.0e-4);
+  if (!standard) {
     if (fabs(zp[0]) > 1.0e-4) {
       yp[0] = -(zp[1] + zp[2]) / zp[0];
       yp[1] = 1.0;
@@ -106,6 +109,7 @@ __device__ __forceinline__ void epsilon_fn(const double *r1, const double *r2, d
     e[k][1] = yp[k];
     e[k][2] = zp[k];
   }
+  return standard;
 }
 
 __device__ __forceinline__ constexpr double levi(int i, int j, int k) {
@@ -481,6 +485,186 @@ __device__ __forceinline__ void mol_rho_ab(const RotM &R, const DRotM &DA, const
       Bo.H[c][e] = hb;
     }
   });
+}
+
+// ---------------------------------------------------------------------------
+// Frame-derivative terms through rotation rates (s and p shells).
+//
+// The three-center frame e (columns x, y, z) is orthonormal, so its
+// derivative along any coordinate is de = e W with W = e^T de skew: three
+// rates W^xy, W^yz, W^xz.  The p block of the rotation is L_p = P e P^T (p
+// order y, z, x), so dL = L Omega with Omega the same rates in p order, and
+// for X = L M L^T
+//   sum rho (dL M L^T + L M dL^T) = sum_e M_e [G, Omega](e),   G = L^T rho L,
+// which is W^xy tau^xy + W^yz tau^yz + W^xz tau^xz with
+// tau^ij = sum_e M_e [G, J^ij](e), J^ij = E(p_i, p_j) - E(p_j, p_i).  This is
+// the same sum as contracting Dtwister's dL (M_Drotations.f90:456-471) with
+// rho, without forming dL: the rates come from Depsilon_3c in closed form
+// (frame_rates_3c).
+// ---------------------------------------------------------------------------
+// p orbital of frame axis i (x, y, z) in the order (y, z, x)
+__host__ __device__ constexpr int p_of_axis(int i) { return 1 + (i == 0 ? 2 : i - 1); }
+
+// G = L^T rho L over the whole block (rho and G column-major, NA rows)
+template <int PA, int PB>
+__device__ __forceinline__ void mol_G_full(const RotM &R, const double *rho, double *G) {
+  constexpr int NA = pat_norb(PA), NB = pat_norb(PB);
+  static_assert(NA <= 4 && NB <= 4, "s and p shells only");
+  double rR[NA * NB];
+  sfor<NA>([&](auto MU) {
+    constexpr int mu = decltype(MU)::value;
+    sfor<NB>([&](auto B) {
+      constexpr int b = decltype(B)::value;
+      constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
+      if constexpr (sb == 0) {
+        rR[mu + NA * b] = rho[mu + NA * b];
+      } else {
+        double acc = rho[mu + NA * ob] * R.p[0][mb];
+        acc = fma(rho[mu + NA * (ob + 1)], R.p[1][mb], acc);
+        rR[mu + NA * b] = fma(rho[mu + NA * (ob + 2)], R.p[2][mb], acc);
+      }
+    });
+  });
+  sfor<NB>([&](auto B) {
+    constexpr int b = decltype(B)::value;
+    sfor<NA>([&](auto A) {
+      constexpr int a = decltype(A)::value;
+      constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
+      if constexpr (sa == 0) {
+        G[a + NA * b] = rR[a + NA * b];
+      } else {
+        double acc = R.p[0][ma] * rR[oa + NA * b];
+        acc = fma(R.p[1][ma], rR[(oa + 1) + NA * b], acc);
+        G[a + NA * b] = fma(R.p[2][ma], rR[(oa + 2) + NA * b], acc);
+      }
+    });
+  });
+}
+
+// tau^xy, tau^yz, tau^xz of the molecular-frame block M (values at the ME
+// positions of the plan) against the full molecular-frame density G
+template <int PA, int PB>
+__device__ __forceinline__ void mol_tau(const double *G, const double *M, double tau[3]) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  constexpr bool pa = NA >= 4, pb = NB >= 4;
+  sfor<3>([&](auto PR) {
+    constexpr int pr = decltype(PR)::value;
+    constexpr int ai = pr == 1 ? 1 : 0, aj = pr == 0 ? 1 : 2;  // (x,y), (y,z), (x,z)
+    constexpr int Pi = p_of_axis(ai), Pj = p_of_axis(aj);
+    double acc = 0.0;
+    sfor<PL::m.n>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+      // [G, J]_ab = G(a,Pi)[b=Pj] - G(a,Pj)[b=Pi] - [a=Pi] G(Pj,b) + [a=Pj] G(Pi,b)
+      if constexpr (pb && b == Pj) acc = fma(M[e], G[a + NA * Pi], acc);
+      if constexpr (pb && b == Pi) acc = fma(-M[e], G[a + NA * Pj], acc);
+      if constexpr (pa && a == Pi) acc = fma(-M[e], G[Pj + NA * b], acc);
+      if constexpr (pa && a == Pj) acc = fma(M[e], G[Pi + NA * b], acc);
+    });
+    tau[pr] = acc;
+  });
+}
+
+// Rotation rates of the three-center frame, component c of d/dratm (a*) and
+// d/dr1 (b*).  Depsilon_3c (b.FUNCTIONS/Depsilon_3c.f90:49-189) gives, with
+// u = r21, ic = 1 / |r21 x rnabc| and iz = 1 / z,
+//   e_x . de_y/dratm_c = ic (e_x x u)_c             (de_z/dratm = 0)
+//   e_x . de_y/dr1_c   = ic (e_x x (ratm - r2))_c
+//   e_y . de_z/dr1_c   = -iz e_y,c,   e_x . de_z/dr1_c = -iz e_x,c
+// (its terms along e_x . e_y and e_y . e_z vanish).  Valid for the standard
+// frame (y along r21 x rnabc); every rate is zero where Depsilon_3c returns
+// zeros (|r21 x rnabc| < 1e-3).
+struct FrameRates3c {
+  double axy[3];
+  double bxy[3], byz[3], bxz[3];
+};
+
+__device__ __forceinline__ void frame_rates_3c(const double *r2, const double *r21, double z, const double *ratm,
+                                               const double *rnabc, const double e[3][3], FrameRates3c &w) {
+  double c0 = r21[1] * rnabc[2] - r21[2] * rnabc[1];
+  double c1 = r21[2] * rnabc[0] - r21[0] * rnabc[2];
+  double c2 = r21[0] * rnabc[1] - r21[1] * rnabc[0];
+  double cm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  bool zero = fabs(cm) < 1.0e-3;
+  double ic = zero ? 0.0 : 1.0 / cm, iz = zero ? 0.0 : 1.0 / z;
+  double ex[3] = {e[0][0], e[1][0], e[2][0]}, ey[3] = {e[0][1], e[1][1], e[2][1]};
+  double s[3] = {ratm[0] - r2[0], ratm[1] - r2[1], ratm[2] - r2[2]};
+  w.axy[0] = ic * (ex[1] * r21[2] - ex[2] * r21[1]);
+  w.axy[1] = ic * (ex[2] * r21[0] - ex[0] * r21[2]);
+  w.axy[2] = ic * (ex[0] * r21[1] - ex[1] * r21[0]);
+  w.bxy[0] = ic * (ex[1] * s[2] - ex[2] * s[1]);
+  w.bxy[1] = ic * (ex[2] * s[0] - ex[0] * s[2]);
+  w.bxy[2] = ic * (ex[0] * s[1] - ex[1] * s[0]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    w.byz[k] = -iz * ey[k];
+    w.bxz[k] = -iz * ex[k];
+  }
+}
+
+// epsilon's collinear fallback frame (y axis not along r21 x rnabc) is not
+// the frame Depsilon_3c differentiates.  Its de_y then has a component along
+// e_y, psi = e_y . de_y, and e_z . de_y (chi) is no longer -e_y . de_z, so the
+// rates of the literal derivatives gain psi (E_xx + E_yy) and, for d/dr1,
+// (chi - e_y . de_z) E_zy.  From Depsilon_3c's expressions, with
+// V = A1 ratm + A2 r2 + A3 r1 and V' = B1 ratm + B2 r2 + B3 r1 as there:
+//   psiA = ic ((e_y x u) - ic V),  psiB = ic ((e_y x (ratm - r2)) - ic V'),
+//   chiB = ic (e_z x (ratm - r2))
+struct FrameExtra3c {
+  double psiA[3], psiB[3], chiB[3];
+};
+
+__device__ __forceinline__ void frame_extra_3c(const double *r1, const double *r2, const double *r21,
+                                               const double *ratm, const double *rnabc, const double e[3][3],
+                                               FrameExtra3c &x) {
+  double c0 = r21[1] * rnabc[2] - r21[2] * rnabc[1];
+  double c1 = r21[2] * rnabc[0] - r21[0] * rnabc[2];
+  double c2 = r21[0] * rnabc[1] - r21[1] * rnabc[0];
+  double cm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  double ic = fabs(cm) < 1.0e-3 ? 0.0 : 1.0 / cm;
+  double r2m2 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+  double r1m2 = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+  double ram2 = ratm[0] * ratm[0] + ratm[1] * ratm[1] + ratm[2] * ratm[2];
+  double r12 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+  double r2a = r2[0] * ratm[0] + r2[1] * ratm[1] + r2[2] * ratm[2];
+  double r1a = r1[0] * ratm[0] + r1[1] * ratm[1] + r1[2] * ratm[2];
+  double A1 = r1m2 + r2m2 - 2.0 * r12, A2 = r12 - r1m2 - r2a + r1a, A3 = r12 - r2m2 + r2a - r1a;
+  double B1 = r2a - r1a + r12 - r2m2, B2 = r2a + r1a - r12 - ram2, B3 = ram2 - 2.0 * r2a + r2m2;
+  double ey[3] = {e[0][1], e[1][1], e[2][1]}, ez[3] = {e[0][2], e[1][2], e[2][2]};
+  double s[3] = {ratm[0] - r2[0], ratm[1] - r2[1], ratm[2] - r2[2]};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const int c1i = (c + 1) % 3, c2i = (c + 2) % 3;
+    double V = A1 * ratm[c] + A2 * r2[c] + A3 * r1[c];
+    double Vb = B1 * ratm[c] + B2 * r2[c] + B3 * r1[c];
+    x.psiA[c] = ic * ((ey[c1i] * r21[c2i] - ey[c2i] * r21[c1i]) - ic * V);
+    x.psiB[c] = ic * ((ey[c1i] * s[c2i] - ey[c2i] * s[c1i]) - ic * Vb);
+    x.chiB[c] = ic * (ez[c1i] * s[c2i] - ez[c2i] * s[c1i]);
+  }
+}
+
+// kappa_ij = sum_e M_e ([a = p_j] G(p_i, b) + [b = p_j] G(a, p_i)), the
+// coefficient of Omega_ij; returns kappa_xx + kappa_yy and kappa_zy
+template <int PA, int PB>
+__device__ __forceinline__ void mol_kappa_extra(const double *G, const double *M, double &kd, double &kzy) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  constexpr bool pa = NA >= 4, pb = NB >= 4;
+  constexpr int Px = p_of_axis(0), Py = p_of_axis(1), Pz = p_of_axis(2);
+  double d = 0.0, zy = 0.0;
+  sfor<PL::m.n>([&](auto E) {
+    constexpr int e = decltype(E)::value;
+    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+    if constexpr (pa && a == Px) d = fma(M[e], G[Px + NA * b], d);
+    if constexpr (pa && a == Py) d = fma(M[e], G[Py + NA * b], d);
+    if constexpr (pb && b == Px) d = fma(M[e], G[a + NA * Px], d);
+    if constexpr (pb && b == Py) d = fma(M[e], G[a + NA * Py], d);
+    if constexpr (pa && a == Py) zy = fma(M[e], G[Pz + NA * b], zy);
+    if constexpr (pb && b == Py) zy = fma(M[e], G[a + NA * Pz], zy);
+  });
+  kd = d;
+  kzy = zy;
 }
 
 // Explicit Drotate (M_Drotations.f90:102-153, Dmatrix :389-482):

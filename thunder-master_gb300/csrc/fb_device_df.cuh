@@ -1,8 +1,9 @@
 // fb_device_df.cuh -- double-float (FP32-pipe) forms of the Slater-Koster
-// rotation, the molecular-frame density contraction and the bicubic table
-// contraction used by the three-center kernels.  Same mathematics and same
-// operation structure as the FP64 forms in fb_device.cuh (rotate_plan,
-// mol_rho) and fb_common.cuh (interp3c); s and p shells only.
+// rotation, the molecular-frame density and rotation-rate sums and the
+// bicubic table contraction used by the three-center kernels.  Same
+// mathematics and same operation structure as the FP64 forms in
+// fb_device.cuh (rotate_plan, mol_G_full, mol_tau) and fb_common.cuh
+// (interp3c); s and p shells only.
 #pragma once
 #include "fb_df.cuh"
 #include "fb_device.cuh"
@@ -12,10 +13,6 @@ namespace fb {
 struct RotDF {
   df p[3][3];
 };
-struct DRotDF {
-  df p[3][3][3];
-};
-
 __device__ __forceinline__ df df_zero() { return df{0.0f, 0.0f}; }
 __device__ __forceinline__ df df_one() { return df{1.0f, 0.0f}; }
 
@@ -27,24 +24,10 @@ __device__ __forceinline__ void twister_df(const double e[3][3], RotDF &R) {
 #pragma unroll
     for (int b = 0; b < 3; b++) R.p[a][b] = df_from(e[pperm(a)][pperm(b)]);
 }
-__device__ __forceinline__ void dtwister_df(const df dd[3][3][3], DRotDF &D) {
-#pragma unroll
-  for (int c = 0; c < 3; c++)
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) D.p[c][a][b] = dd[c][pperm(a)][pperm(b)];
-}
-
 template <int S>
 __device__ __forceinline__ df Lrot_df(const RotDF &R, int k, int m) {
   if constexpr (S == 0) return df_one();
   else return R.p[k][m];
-}
-template <int S>
-__device__ __forceinline__ df DLrot_df(const DRotDF &D, int c, int k, int m) {
-  if constexpr (S == 0) return df_zero();
-  else return D.p[c][k][m];
 }
 
 // rotate (M_rotations.f90:98-177) in df: X = L M R^T, structural zeros
@@ -90,79 +73,83 @@ __device__ __forceinline__ void rotate_plan_df(const RotDF &R, const df *v, df *
   });
 }
 
-// molecular-frame density contraction (see mol_rho in fb_device.cuh):
-// rR = rho R, G(e) = (L^T rho R)(e), H_c(e) = (dL_c^T rho R + L^T rho dR_c)(e)
-template <int PA, int PB, int K>
-__device__ __forceinline__ void mol_rR_df(const RotDF &R, const df *rho, df *rR) {
-  using PL = Plan<PA, PB, K>;
-  constexpr int NA = PL::NA, NB = PL::NB;
+// G = L^T rho L over the whole block and the rotation-rate sums tau^xy,
+// tau^yz, tau^xz of M against it (mol_G_full / mol_tau in fb_device.cuh)
+template <int PA, int PB>
+__device__ __forceinline__ void mol_G_full_df(const RotDF &R, const df *rho, df *G) {
+  constexpr int NA = pat_norb(PA), NB = pat_norb(PB);
+  static_assert(NA <= 4 && NB <= 4, "s and p shells only");
+  df rR[NA * NB];
   sfor<NA>([&](auto MU) {
     constexpr int mu = decltype(MU)::value;
     sfor<NB>([&](auto B) {
       constexpr int b = decltype(B)::value;
       constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
-      df acc = df_zero();
-      sfor<2 * sb + 1>([&](auto NU) {
-        constexpr int k = decltype(NU)::value;
-        df t = (sb == 0) ? rho[mu + NA * (ob + k)] : rho[mu + NA * (ob + k)] * Lrot_df<sb>(R, k, mb);
-        acc = (k == 0) ? t : acc + t;
-      });
-      rR[mu + NA * b] = acc;
+      if constexpr (sb == 0) {
+        rR[mu + NA * b] = rho[mu + NA * b];
+      } else {
+        rR[mu + NA * b] = rho[mu + NA * ob] * R.p[0][mb] + rho[mu + NA * (ob + 1)] * R.p[1][mb] +
+                          rho[mu + NA * (ob + 2)] * R.p[2][mb];
+      }
+    });
+  });
+  sfor<NB>([&](auto B) {
+    constexpr int b = decltype(B)::value;
+    sfor<NA>([&](auto A) {
+      constexpr int a = decltype(A)::value;
+      constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
+      if constexpr (sa == 0) {
+        G[a + NA * b] = rR[a + NA * b];
+      } else {
+        G[a + NA * b] = R.p[0][ma] * rR[oa + NA * b] + R.p[1][ma] * rR[(oa + 1) + NA * b] +
+                        R.p[2][ma] * rR[(oa + 2) + NA * b];
+      }
     });
   });
 }
 
-template <int PA, int PB, int K>
-__device__ __forceinline__ void mol_G_df(const RotDF &R, const df *rR, df *G) {
-  using PL = Plan<PA, PB, K>;
-  constexpr int NA = PL::NA;
-  sfor<PL::m.n>([&](auto E) {
-    constexpr int e = decltype(E)::value;
-    constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
-    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
-    df g = df_zero();
-    sfor<2 * sa + 1>([&](auto KK) {
-      constexpr int k = decltype(KK)::value;
-      df t = (sa == 0) ? rR[(oa + k) + NA * b] : Lrot_df<sa>(R, k, ma) * rR[(oa + k) + NA * b];
-      g = (k == 0) ? t : g + t;
+template <int PA, int PB>
+__device__ __forceinline__ void mol_tau_df(const df *G, const df *M, df tau[3]) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  constexpr bool pa = NA >= 4, pb = NB >= 4;
+  sfor<3>([&](auto PR) {
+    constexpr int pr = decltype(PR)::value;
+    constexpr int ai = pr == 1 ? 1 : 0, aj = pr == 0 ? 1 : 2;
+    constexpr int Pi = p_of_axis(ai), Pj = p_of_axis(aj);
+    df acc = df_zero();
+    sfor<PL::m.n>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
+      if constexpr (pb && b == Pj) acc = acc + M[e] * G[a + NA * Pi];
+      if constexpr (pb && b == Pi) acc = acc - M[e] * G[a + NA * Pj];
+      if constexpr (pa && a == Pi) acc = acc - M[e] * G[Pj + NA * b];
+      if constexpr (pa && a == Pj) acc = acc + M[e] * G[Pi + NA * b];
     });
-    G[e] = g;
+    tau[pr] = acc;
   });
 }
 
-template <int PA, int PB, int K>
-__device__ __forceinline__ void mol_H_df(const RotDF &R, const DRotDF &D, const df *rho, const df *rR,
-                                         df (*H)[Plan<PA, PB, K>::m.n]) {
-  using PL = Plan<PA, PB, K>;
-  constexpr int NA = PL::NA;
+// kappa_xx + kappa_yy and kappa_zy (mol_kappa_extra in fb_device.cuh)
+template <int PA, int PB>
+__device__ __forceinline__ void mol_kappa_extra_df(const df *G, const df *M, df &kd, df &kzy) {
+  using PL = Plan<PA, PB, K3C>;
+  constexpr int NA = PL::NA, NB = PL::NB;
+  constexpr bool pa = NA >= 4, pb = NB >= 4;
+  constexpr int Px = p_of_axis(0), Py = p_of_axis(1), Pz = p_of_axis(2);
+  df d = df_zero(), zy = df_zero();
   sfor<PL::m.n>([&](auto E) {
     constexpr int e = decltype(E)::value;
     constexpr int a = PL::m.mu[e], b = PL::m.nu[e];
-    constexpr int sa = orb_shell(a), ma = orb_m(a), oa = shell_off(sa);
-    constexpr int sb = orb_shell(b), mb = orb_m(b), ob = shell_off(sb);
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      df h = df_zero();
-      if constexpr (sa > 0) {
-        sfor<2 * sa + 1>([&](auto KK) {
-          constexpr int k = decltype(KK)::value;
-          h = h + DLrot_df<sa>(D, c, k, ma) * rR[(oa + k) + NA * b];
-        });
-      }
-      if constexpr (sb > 0) {
-        sfor<2 * sa + 1>([&](auto KK) {
-          constexpr int k = decltype(KK)::value;
-          df t = df_zero();
-          sfor<2 * sb + 1>([&](auto NU) {
-            constexpr int q = decltype(NU)::value;
-            t = t + rho[(oa + k) + NA * (ob + q)] * DLrot_df<sb>(D, c, q, mb);
-          });
-          h = h + ((sa == 0) ? t : Lrot_df<sa>(R, k, ma) * t);
-        });
-      }
-      H[c][e] = h;
-    }
+    if constexpr (pa && a == Px) d = d + M[e] * G[Px + NA * b];
+    if constexpr (pa && a == Py) d = d + M[e] * G[Py + NA * b];
+    if constexpr (pb && b == Px) d = d + M[e] * G[a + NA * Px];
+    if constexpr (pb && b == Py) d = d + M[e] * G[a + NA * Py];
+    if constexpr (pa && a == Py) zy = zy + M[e] * G[Pz + NA * b];
+    if constexpr (pb && b == Py) zy = zy + M[e] * G[a + NA * Pz];
   });
+  kd = d;
+  kzy = zy;
 }
 
 // 4-point Lagrange weights on nodes -1, 0, 1, 2 and their derivatives in df

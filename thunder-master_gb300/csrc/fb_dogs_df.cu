@@ -172,11 +172,10 @@ __device__ void trip_3c_force_dogs_df(const Ctx3c &c, int t) {
     for (int b = 0; b < 3; b++) R.p[a][b] = g.e[pperm(a)][pperm(b)];
   int p = c.tdst[t];
   const df *rho = c.rho_df + c.blk_off[p];
-  df rb[NA * NB], rR[NA * NB], G[NE];
+  df rb[NA * NB], Gf[NA * NB], G[NE];
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) rb[q] = rho[q];
-  mol_rR_df<PA, PB, K3C>(R, rb, rR);
-  mol_G_df<PA, PB, K3C>(R, rR, G);
+  mol_density_df<PA, PB>(R, rb, Gf, G);
   df Sx = df_zero(), Sy = df_zero(), Sp = df_zero(), Cx = df_zero();
 #pragma unroll
   for (int e = 0; e < NE; e++) {
@@ -193,27 +192,17 @@ __device__ void trip_3c_force_dogs_df(const Ctx3c &c, int t) {
   double am = sterm - dterm, ap = sterm + dterm;
   double emnpl = am / sk.d13 + ap / sk.d23;
   double i13 = 1.0 / (sk.d13 * sk.d13), i23 = 1.0 / (sk.d23 * sk.d23);
-  DepsPre pre;
-  depsilon_pre_df(g.u, g.v, pre);
+  df hA[3], hB[3];
+  frame_terms_3c_df<PA, PB>(g, Gf, F, hA, hB);
   const df peq2 = peq2_df();
   double fa[3], fb[3];
 #pragma unroll 1
   for (int q = 0; q < 3; q++) {
-    df dA[3][3], dB[3][3];
-    depsilon_comp_df(q, g.u, g.v, iz, g.e, pre, dA, dB);
-    df dPA[3][3], dPB[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-        dPA[a][b] = dA[pperm(a)][pperm(b)];
-        dPB[a][b] = dB[pperm(a)][pperm(b)];
-      }
     df amt = (g.x > 1.0e-5) ? (sel3(g.sig, q) - cost * sel3(g.rh, q)) * g.ix : df_zero();
     df bmt = (cost * sel3(g.sig, q) - sel3(g.rh, q)) * iz;
     df ga = sel3(g.rh, q) * Sx + amt * Sp;
-    df sa = mol_HM_df<PA, PB>(R, dPA, rb, rR, F) + ga;
-    df sb = mol_HM_df<PA, PB>(R, dPB, rb, rR, F) + ((bmt * Sp - sel3(g.sig, q) * Sy) - ga * 0.5f);
+    df sa = sel3(hA, q) + ga;
+    df sb = sel3(hB, q) + ((bmt * Sp - sel3(g.sig, q) * Sy) - ga * 0.5f);
     double va = -df_to(sa * peq2), vb = -df_to(sb * peq2);
     // DOGS extras
     double spterm = 0.5 * ps[2 + q];

@@ -806,7 +806,31 @@ __device__ void trip_dvxc(const Ctx3c &c, const VxcArgs &v, int t) {
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) wb[q] = __ldg(wdp + q);
   double fa[3], fb[3];
-  {
+  if constexpr (NA <= 4 && NB <= 4) {
+    // frame-derivative terms through the rotation rates of the frame
+    // (frame_terms_3c); G(e) from the whole molecular-frame block
+    double Gf[NA * NB], Ge[NE], hA[3], hB[3];
+    mol_G_full<PA, PB>(R, wb, Gf);
+    sfor<NE>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      constexpr int at = PL::m.mu[e] + NA * PL::m.nu[e];
+      Ge[e] = Gf[at];
+    });
+    frame_terms_3c<PA, PB>(g, Gf, F, hA, hB);
+    double sx = 0.0, sp = 0.0, sy = 0.0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      sx = fma(DxF[e], Ge[e], sx);
+      sp = fma(DpF[e], Ge[e], sp);
+      sy = fma(DyF[e], Ge[e], sy);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      double ga = g.rhat[q] * (sx + gx) + amt[q] * (sp + gp);
+      fa[q] = hA[q] + ga;
+      fb[q] = hB[q] - g.sighat[q] * (sy + gy) + bmt[q] * (sp + gp) - 0.5 * ga;
+    }
+  } else {
     double dA[3][3][3], dB[3][3][3];
     depsilon_3c(g.r1, g.r2, g.r21, g.z, g.rna, g.rnabc, g.e, dA, dB);
     DRotM DA;

@@ -207,11 +207,10 @@ __device__ void trip_dvxc_df(const Ctx3c &c, const VxcArgs &v, int t) {
 #pragma unroll
     for (int b = 0; b < 3; b++) R.p[a][b] = g.e[pperm(a)][pperm(b)];
   const double *wdp = v.wd + c.blk_off[p];
-  df rb[NA * NB], rR[NA * NB], G[NE];
+  df rb[NA * NB], Gf[NA * NB], G[NE];
 #pragma unroll
   for (int q = 0; q < NA * NB; q++) rb[q] = df_from(__ldg(wdp + q));
-  mol_rR_df<PA, PB, K3C>(R, rb, rR);
-  mol_G_df<PA, PB, K3C>(R, rR, G);
+  mol_density_df<PA, PB>(R, rb, Gf, G);
   df Sx = gx, Sy = gy, Sp = gp;
 #pragma unroll
   for (int e = 0; e < NE; e++) {
@@ -219,26 +218,16 @@ __device__ void trip_dvxc_df(const Ctx3c &c, const VxcArgs &v, int t) {
     Sy = Sy + DyF[e] * G[e];
     Sp = Sp + DpF[e] * G[e];
   }
-  DepsPre pre;
-  depsilon_pre_df(g.u, g.v, pre);
+  df hA[3], hB[3];
+  frame_terms_3c_df<PA, PB>(g, Gf, F, hA, hB);
   double fa[3], fb[3];
 #pragma unroll 1
   for (int q = 0; q < 3; q++) {
-    df dA[3][3], dB[3][3];
-    depsilon_comp_df(q, g.u, g.v, iz, g.e, pre, dA, dB);
-    df dPA[3][3], dPB[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-        dPA[a][b] = dA[pperm(a)][pperm(b)];
-        dPB[a][b] = dB[pperm(a)][pperm(b)];
-      }
     df amt = (g.x > 1.0e-5) ? (sel3(g.sig, q) - cost * sel3(g.rh, q)) * g.ix : df_zero();
     df bmt = (cost * sel3(g.sig, q) - sel3(g.rh, q)) * iz;
     df ga = sel3(g.rh, q) * Sx + amt * Sp;
-    df sa = mol_HM_df<PA, PB>(R, dPA, rb, rR, F) + ga;
-    df sb = mol_HM_df<PA, PB>(R, dPB, rb, rR, F) + ((bmt * Sp - sel3(g.sig, q) * Sy) - ga * 0.5f);
+    df sa = sel3(hA, q) + ga;
+    df sb = sel3(hB, q) + ((bmt * Sp - sel3(g.sig, q) * Sy) - ga * 0.5f);
     double va = -df_to(sa), vb = -df_to(sb);
     fa[0] = q == 0 ? va : fa[0];
     fa[1] = q == 1 ? va : fa[1];
