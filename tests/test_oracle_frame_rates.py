@@ -11,14 +11,10 @@ with the rates in the closed forms the kernels use (frame_rates_3c,
 frame_extra_3c), for the standard frame and for epsilon's collinear fallback
 frame.  The numpy here restates the kernels' formulas; the literal side is
 the oracle's Depsilon_3c."""
-import os
-import sys
-
 import numpy as np
 import pytest
 
-sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "oracle"))
-import oracle as O  # noqa: E402
+from oracle import oracle as O
 
 PPERM = [1, 2, 0]          # p order (y, z, x): orbital slot -> frame axis
 P_OF_AXIS = {0: 3, 1: 1, 2: 2}  # frame axis x, y, z -> orbital of an s+p block

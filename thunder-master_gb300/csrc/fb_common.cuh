@@ -267,9 +267,12 @@ __device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, 
     // the table values, so the Legendre sums are taken first at each of the
     // 16 stencil nodes, g = sum_th P_th T_th and gp = sum_th P'_th T_th, and
     // the stencil weights then contract g (value, d/dx, d/dy) and gp
-    // (d/dcos): 11 FP64 FMAs per node and element instead of 15 + 20/16
-    // for the per-theta contraction.  The sums differ from the reference's
-    // order only by rounding.
+    // (d/dcos), as a tensor product: along each stencil row the x weights
+    // give A = sum_k wx g, B = sum_k wx' g, C = sum_k wx gp, and the row's y
+    // weight adds wy A, wy B, wy' A, wy C.  11 FP64 FMAs per node and element
+    // instead of 15 + 20/16 for the per-theta contraction, and no products of
+    // the x and y weights.  The sums differ from the reference's order only
+    // by rounding.
     double wx[4], wy[4], dwx[4], dwy[4];
     lagrange4(px, wx, dwx);
     lagrange4(py, wy, dwy);
@@ -282,21 +285,31 @@ __device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, 
 #pragma unroll 1
     for (int j = 0; j < 4; j++) {
       double wyj = wy[j], dwyj = dwy[j];
+      const double *Tr = Tb + (long long)j * nx * NTHETA * NE;
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        double W = wx[k] * wyj, Wx = dwx[k] * wyj, Wy = wx[k] * dwyj;
-        const double *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE;
+      for (int e = 0; e < NE; e++) {
+        double A = 0.0, B = 0.0, C = 0.0;
 #pragma unroll
-        for (int e = 0; e < NE; e++) {
-          double t0 = __ldg(Tn + e), t1 = __ldg(Tn + NE + e), t2 = __ldg(Tn + 2 * NE + e);
-          double t3 = __ldg(Tn + 3 * NE + e), t4 = __ldg(Tn + 4 * NE + e);
+        for (int k = 0; k < 4; k++) {
+          const double *Tn = Tr + k * NTHETA * NE + e;
+          double t0 = __ldg(Tn), t1 = __ldg(Tn + NE), t2 = __ldg(Tn + 2 * NE);
+          double t3 = __ldg(Tn + 3 * NE), t4 = __ldg(Tn + 4 * NE);
           double g = fma(pl[4], t4, fma(pl[3], t3, fma(pl[2], t2, fma(pl[1], t1, t0))));
           double gp = fma(dpl[4], t4, fma(dpl[3], t3, fma(dpl[2], t2, t1)));
-          F[e] = fma(W, g, F[e]);
-          DxF[e] = fma(Wx, g, DxF[e]);
-          DyF[e] = fma(Wy, g, DyF[e]);
-          DpF[e] = fma(W, gp, DpF[e]);
+          if (k == 0) {
+            A = wx[0] * g;
+            B = dwx[0] * g;
+            C = wx[0] * gp;
+          } else {
+            A = fma(wx[k], g, A);
+            B = fma(dwx[k], g, B);
+            C = fma(wx[k], gp, C);
+          }
         }
+        F[e] = fma(wyj, A, F[e]);
+        DxF[e] = fma(wyj, B, DxF[e]);
+        DyF[e] = fma(dwyj, A, DyF[e]);
+        DpF[e] = fma(wyj, C, DpF[e]);
       }
     }
     return;

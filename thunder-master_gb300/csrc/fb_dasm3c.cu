@@ -94,6 +94,7 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
   // molecular-frame value and derivatives with the sin(theta) factor of
   // the mvalue = 1 channels (M_Fdata_3c.f90:814-833)
   double M[NE], Dp[NE], Dx[NE], Dy[NE];
+  const double cs = g.cost / sint;
   sfor<NE>([&](auto E) {
     constexpr int e = decltype(E)::value;
     M[e] = F[e];
@@ -101,7 +102,7 @@ __device__ void trip_3c_force(const Ctx3c &c, int t) {
     Dx[e] = DxF[e];
     Dy[e] = DyF[e];
     if constexpr (PL::m.mv[e] == 1) {
-      Dp[e] = DpF[e] * sint - g.cost * F[e] / sint;
+      Dp[e] = fma(DpF[e], sint, -cs * F[e]);
       M[e] = F[e] * sint;
       Dx[e] = DxF[e] * sint;
       Dy[e] = DyF[e] * sint;
