@@ -147,17 +147,18 @@ def dist_env():
 # algorithmic work per unit
 # ---------------------------------------------------------------------------
 # Executed FP64 FLOPs per sp3 x sp3 triplet of the FP64 force kernel
-# (2 DFMA + DADD + DMUL: 2,564 + 96 + 311 thread instructions, ncu on
+# (2 DFMA + DADD + DMUL: 1,944 + 64 + 347 thread instructions, ncu on
 # SiC4096, profiles/k_dassemble_3c_sic4096.md; the divisions and square roots
 # are DFMA sequences and count in DFMA)
-FP64_FLOP_PER_TRIPLET = 2 * 2563.955 + 96.0 + 310.998
+FP64_FLOP_PER_TRIPLET = 2 * 1943.959 + 64.0 + 346.996
 
 
 def flops_dassemble_3c(nme, prec="df"):
     """FP64 FLOPs per triplet of the force kernel.  fp64: the FP64 kernel's
     executed count (ncu), about 3,500 of them the interpolation (Legendre
     sums first at each of the 16 stencil nodes, 4 + 3 FMA per node and
-    element, then the value, x, y and cos contractions, 4 FMA).  df: the FP64
+    element, then the x contractions along each stencil row, 3 FMA per node,
+    and the row's y weights, 4 FMA per row).  df: the FP64
     formulation of the per-theta form the double-float kernel executes on
     the FP32 pipe, value + x + y contractions per theta (5 x 16 x 3 FMA per
     element), the Legendre combination (4 x 5 FMA) and about 1,800 FLOP of
@@ -187,16 +188,18 @@ def tuned_shapes(ctx, fbgpu, autotune):
 
 
 # Executed FP32 work of the double-float three-center kernels per sp3 x sp3
-# triplet (2 FFMA + FADD + FMUL thread instructions, ncu on Si512: the count
+# triplet (2 FFMA + FADD + FMUL thread instructions: the force kernel
+# 9,546 + 26,981 + 3,192, ncu on SiC4096; the value kernel on Si512, the count
 # per triplet does not depend on the system size), and the DRAM bytes per
 # triplet of one launch (ncu on SiC4096, where the launch's working set
 # exceeds what L2 keeps between launches) (profiles/): the df formulation's
 # arithmetic is what the FP32 pipe must execute.
-DF_FP32_FLOP = {"dassemble_3c": 59053.0, "assemble_3c": 16284.0}
+DF_FP32_FLOP = {"dassemble_3c": 2 * 9545.781 + 26981.411 + 3191.927, "assemble_3c": 16284.0}
 # DRAM read + write bytes per triplet of one force-kernel launch, ncu on
-# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 159.82 MB per launch;
-# profiles/k_dassemble_3c_df_sic4096.md, 159.78 MB), over 5,125,854 triplets
-DRAM_BYTES_PER_TRIPLET = {"fp64": 159.824896e6 / 5125854, "df": 159.777792e6 / 5125854}
+# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 160.10 MB per launch;
+# profiles/k_dassemble_3c_df_sic4096.md, 159.59 MB; means of three launches),
+# over 5,125,854 triplets
+DRAM_BYTES_PER_TRIPLET = {"fp64": 160.100523e6 / 5125854, "df": 159.594240e6 / 5125854}
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
@@ -235,7 +238,7 @@ def roofline_for(ctx, ktimes, T, P, natoms, nZ, steps, prec="df", sm_mhz=None):
                 "peak_source": "of measured: fb_probe_fp32 FFMA chains in this run",
                 "flops_per_launch": fl32,
                 "flops_source": "executed FP32 FLOPs of the double-float kernel (2 FFMA + FADD + FMUL per "
-                                "triplet, ncu on Si512)",
+                                "triplet, ncu on SiC4096)",
                 "avg_launch_ms": round(dom_ms, 4),
                 "fp64_equivalent": {"algorithmic_flops_per_launch": fl64, "achieved": round(ach64, 4),
                                     "fp64_peak": round(fp64_peak, 4), "unit": "TFLOP/s",
