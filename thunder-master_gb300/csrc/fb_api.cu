@@ -78,7 +78,7 @@ struct fb_ctx {
   std::vector<int> h_pair_off, h_trip_off;
   std::vector<long long> h_blk_base;  // first block element of each atom's pairs (+ total)
   DevBuf d_bsum, d_blk_base;
-  DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v,
+  DevBuf d_cnt, d_pair_off, d_neigh_j, d_neigh_b, d_neigh_self, d_neigh_back, d_pair_owner, d_r3v, d_r3f,
       d_blk_off, d_tcnt, d_trip_off, d_ci_j, d_ci_b, d_cj_j, d_cj_b, d_cneigh, d_tdst, d_talpha;
   DevBuf d_tkey, d_trank, d_tperm, d_thist;
   // the triplet lists in the binned order (6 x T ints) for the table
@@ -295,7 +295,7 @@ void fb_destroy(fb_ctx *ctx) {
   DevBuf *bufs[] = {&ctx->d_fd, &ctx->d_tab2, &ctx->d_tab3, &ctx->d_lin, &ctx->d_gxy, &ctx->d_ratom,
                     &ctx->d_pos4, &ctx->d_isp, &ctx->d_xl, &ctx->d_xlf, &ctx->d_imgs, &ctx->d_cnt,
                     &ctx->d_pair_off, &ctx->d_neigh_j, &ctx->d_neigh_b, &ctx->d_neigh_self, &ctx->d_neigh_back,
-                    &ctx->d_pair_owner, &ctx->d_r3v, &ctx->d_blk_off, &ctx->d_tcnt,
+                    &ctx->d_pair_owner, &ctx->d_r3v, &ctx->d_r3f, &ctx->d_blk_off, &ctx->d_tcnt,
                     &ctx->d_trip_off, &ctx->d_ci_j, &ctx->d_ci_b, &ctx->d_cj_j, &ctx->d_cj_b, &ctx->d_cneigh,
                     &ctx->d_tdst, &ctx->d_talpha, &ctx->d_status, &ctx->d_errinfo, &ctx->d_S, &ctx->d_T,
                     &ctx->d_vb, &ctx->d_vbo, &ctx->d_rho, &ctx->d_cape, &ctx->d_dS, &ctx->d_dT, &ctx->d_sumT,
@@ -551,6 +551,7 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.neigh_back = ctx->d_neigh_back.as<int>();
   a.pair_owner = ctx->d_pair_owner.as<int>();
   a.r3v = ctx->d_r3v.as<double>();
+  a.r3f = ctx->d_r3f.as<float4>();
   a.tcnt = ctx->d_tcnt.as<int>();
   a.rcnt = ctx->d_rcnt.as<int>();
   a.trip_off = ctx->d_trip_off.as<int>();
@@ -636,6 +637,7 @@ static int finish_neighbors(fb_ctx *ctx) {
   int N = ctx->N, P = ctx->P;
   CHK(ctx->d_neigh_back.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
+  CHK(ctx->d_r3f.ensure(P * sizeof(float4) + 16));
   NeighArgs a = neigh_args(ctx);
   KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
   // common neighbors: slots for every ordered pair of ialpha's non-self

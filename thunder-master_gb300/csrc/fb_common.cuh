@@ -437,11 +437,12 @@ __device__ __forceinline__ void vec2c(double z, const double *eta, const double 
     for (int k = 0; k < 3; k++) vd[k + 3 * e] = on ? -eta[k] * dv[e] : 0.0;
 }
 
-template <int PA, int PB, int K, bool HASD>
-__device__ __forceinline__ void contract(const RotM &R, const DRotM &D, const double *blk, const double *v,
-                                         const double *vd, double out[3]) {
-  MolRho<PA, PB, K> G;
-  mol_rho<PA, PB, K>(R, D, blk, G);
+// sum_{mu,nu} blk(mu,nu) d/dr_q [L M R^T](mu,nu) for M given by v (values)
+// and vd (its Cartesian derivatives) at the ME positions, from the
+// molecular-frame density G of the block (mol_rho)
+template <int PA, int PB, int K>
+__device__ __forceinline__ void contract_g(const MolRho<PA, PB, K> &G, const double *v, const double *vd,
+                                           double out[3]) {
   constexpr int NE = Plan<PA, PB, K>::m.n;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -453,6 +454,14 @@ __device__ __forceinline__ void contract(const RotM &R, const DRotM &D, const do
     }
     out[q] = s;
   }
+}
+
+template <int PA, int PB, int K, bool HASD>
+__device__ __forceinline__ void contract(const RotM &R, const DRotM &D, const double *blk, const double *v,
+                                         const double *vd, double out[3]) {
+  MolRho<PA, PB, K> G;
+  mol_rho<PA, PB, K>(R, D, blk, G);
+  contract_g<PA, PB, K>(G, v, vd, out);
 }
 
 inline Ctx2c make2c(const AsmArgs &a) {

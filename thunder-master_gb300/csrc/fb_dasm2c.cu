@@ -52,6 +52,10 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
 #pragma unroll
     for (int q = 0; q < 3; q++) c.sumS[3 * p + q] = out[q];
   }
+  // the kinetic and on-top vna terms contract with the same density block:
+  // its molecular-frame form is taken once
+  MolRho<PA, PB, K2C> Grb;
+  if ((what & 2u) || ((what & 4u) && !self)) mol_rho<PA, PB, K2C>(R, D, rb, Grb);
   if (what & 2u) {
     interp2c_d<NE>(b.table2c, fd.c2[in1][in2][1], z, tiny, v, dv, b.status);
     vec2c<NE>(z, eta, dv, vd);
@@ -61,7 +65,7 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
 #pragma unroll
       for (int q = 0; q < 3 * NA * NB; q++) c.dT[3 * o + q] = Xd[q];
     }
-    contract<PA, PB, K2C, HASD>(R, D, rb, v, vd, out);
+    contract_g<PA, PB, K2C>(Grb, v, vd, out);
 #pragma unroll
     for (int q = 0; q < 3; q++) c.sumT[3 * p + q] = out[q];
   }
@@ -93,7 +97,7 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
         for (int e = 0; e < NE; e++) m[e] += v[e], dm[e] += dv[e];
       }
       vec2c<NE>(z, eta, dm, vd);
-      contract<PA, PB, K2C, HASD>(R, D, rb, m, vd, out);
+      contract_g<PA, PB, K2C>(Grb, m, vd, out);
 #pragma unroll
       for (int q = 0; q < 3; q++) f[q] -= out[q] * P_eq2;
     }

@@ -55,6 +55,7 @@ struct NeighArgs {
   int *neigh_j, *neigh_b, *neigh_self, *neigh_back;
   const int *pair_owner;
   double *r3v;
+  float4 *r3f;  // float r3v with the neighbor's species cutoff in .w
   int *tcnt;
   int *rcnt;  // kept (ineigh, jneigh) pairs of each pair row (ialpha, ineigh)
   const int *trip_off;

@@ -184,12 +184,12 @@ __global__ void __launch_bounds__(NEIGH_THREADS)
 
 // neigh_back (M_neighbors.f90:469-486) and the per-pair vectors
 // r3 = xl(mbeta) + ratom(j) - ratom(i) used by find_common_neighbors
-// (:776-779); one thread per pair.
+// (:776-779), and its float copy; one thread per pair.
 __global__ void k_neigh_back(int N, int P, const int *__restrict__ pair_owner, const int *__restrict__ pair_off,
                              const int *__restrict__ neigh_j, const int *__restrict__ neigh_b,
                              const int *__restrict__ sid, const double *__restrict__ xl0,
-                             const double *__restrict__ ratom,
-                             int *__restrict__ neigh_back, double *__restrict__ r3v,
+                             const double *__restrict__ ratom, const float4 *__restrict__ pos4,
+                             int *__restrict__ neigh_back, double *__restrict__ r3v, float4 *__restrict__ r3f,
                              unsigned *__restrict__ status) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
@@ -208,11 +208,16 @@ __global__ void k_neigh_back(int N, int P, const int *__restrict__ pair_owner, c
   }
   if (nfound != 1) atomicOr(status, DEVERR_BACK);
   neigh_back[p] = found;
+  float f[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     double v = __dsub_rn(__dadd_rn(xl[3 * mb + k], ratom[3 * j + k]), ratom[3 * i + k]);
     r3v[3 * p + k] = v;
+    f[k] = __double2float_rn(v);
   }
+  // float copy for the pre-tests of the common-neighbor search, with the
+  // neighbor's species cutoff (rcA) in .w
+  r3f[p] = make_float4(f[0], f[1], f[2], pos4[j].w);
 }
 
 
@@ -222,6 +227,29 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
   return fabs(__dadd_rn(__dsub_rn(r3[0], r2[0]), r1[0])) < 1.0e-4 &&
          fabs(__dadd_rn(__dsub_rn(r3[1], r2[1]), r1[1])) < 1.0e-4 &&
          fabs(__dadd_rn(__dsub_rn(r3[2], r2[2]), r1[2])) < 1.0e-4;
+}
+
+// The same match decided in float where it is certain: r2 - r1 is the
+// difference b - a of two relative vectors of ialpha's list and r3 = c is a
+// relative vector of iat's list, all a few bohr long, so the float value of
+// r3 - (r2 - r1) is within 2 u (|a| + |b| + |c|) of the exact one (u = 2^-24;
+// the FP64 values differ from the exact ones by ~1e-15).  Returns 1 when every
+// component is certainly below 1e-4, -1 when one is certainly not, and 0 in
+// the band between (8 u (|a| + |b| + |c| + 1) wide each side), where the FP64
+// test decides.
+__device__ __forceinline__ int common_match_f(float4 c, float4 a, float d0, float d1, float d2, float4 b) {
+  const float u8 = 4.76837158e-7f;  // 8 * 2^-24
+  float e[3] = {c.x - d0, c.y - d1, c.z - d2};
+  float t[3] = {u8 * (fabsf(a.x) + fabsf(b.x) + fabsf(c.x) + 1.0f), u8 * (fabsf(a.y) + fabsf(b.y) + fabsf(c.y) + 1.0f),
+                u8 * (fabsf(a.z) + fabsf(b.z) + fabsf(c.z) + 1.0f)};
+  bool sure = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float m = fabsf(e[k]);
+    if (m >= 1.0e-4f + t[k]) return -1;
+    sure = sure && m < 1.0e-4f - t[k];
+  }
+  return sure ? 1 : 0;
 }
 
 // find_common_max / find_common_neighbors: one warp per pair row
@@ -239,12 +267,12 @@ __device__ __forceinline__ bool common_match(const double *r3, const double *r1,
 // by the caller) the sum over the rows; k_common_compact packs the rows in
 // ineigh order, so the triplets come out in the reference's loop order.
 __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
-                         const float4 *__restrict__ pos4, const float *__restrict__ xlf0,
                          const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                          const double *__restrict__ xl0, const int *__restrict__ pair_owner,
                          const int *__restrict__ pair_off, const int *__restrict__ neigh_j,
                          const int *__restrict__ neigh_b, const int *__restrict__ neigh_self,
-                         const double *__restrict__ r3v, int *__restrict__ tcnt, int *__restrict__ rcnt,
+                         const double *__restrict__ r3v, const float4 *__restrict__ r3f, int *__restrict__ tcnt,
+                         int *__restrict__ rcnt,
                          const long long *__restrict__ slot_off, unsigned *__restrict__ slot_nn,
                          int *__restrict__ slot_found) {
   int pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -258,18 +286,15 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
     return;
   }
   const double *xl = xl0 + (long long)sid[ia] * XL_STRIDE;
-  const float *xlf = xlf0 + (long long)sid[ia] * XL_STRIDE;
   int periodic = speriodic[sid[ia]];
   int kidx = in - (in > self ? 1 : 0);
   long long base = slot_off[ia] + (long long)kidx * (n - 2);
   int num = 0;
   int iat = neigh_j[pi], ib = neigh_b[pi];
-  double r1[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
-  double rci = fd->sp[isp[iat]].rcA;
-  float4 pi4 = pos4[iat];
-  float r1f[3] = {pi4.x + xlf[3 * ib], pi4.y + xlf[3 * ib + 1], pi4.z + xlf[3 * ib + 2]};
+  // ialpha -> (iat, ib) as a float relative vector, iat's cutoff in .w; the
+  // FP64 positions r1 (iat shifted by ib) and r2 (jat shifted by jb) are
+  // formed only in the bands where the FP64 tests decide
+  const float4 a4 = r3f[pi];
   int q0 = pair_off[iat], qn = pair_off[iat + 1];
   int ibx, iby, ibz;
   mbeta_shift(ib, ibx, iby, ibz);
@@ -282,30 +307,45 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
       int pj = p0 + jn;
       jat = neigh_j[pj];
       jb = neigh_b[pj];
-      // float pre-test (the positions' float copies carry the species
-      // cutoff in .w): clearly beyond the range -> rejected, clearly inside
-      // (0.01 A of margin against ~1e-5 A of float error) -> kept without
-      // the FP64 distance; only the band between takes the reference's
-      // uncontracted FP64 test
-      float4 pj4 = pos4[jat];
-      float d0 = (pj4.x + xlf[3 * jb]) - r1f[0], d1 = (pj4.y + xlf[3 * jb + 1]) - r1f[1];
-      float d2 = (pj4.z + xlf[3 * jb + 2]) - r1f[2];
+      // float pre-test on the relative vectors r2 - r1 = b - a (error
+      // ~1e-6 bohr; the species cutoffs in .w): clearly beyond the range ->
+      // rejected, clearly inside (0.01 of margin) -> kept without the FP64
+      // distance; only the band between takes the reference's uncontracted
+      // FP64 test
+      const float4 b4 = r3f[pj];
+      float d0 = b4.x - a4.x, d1 = b4.y - a4.y, d2 = b4.z - a4.z;
       float dd = d0 * d0 + d1 * d1 + d2 * d2;
-      float lim = pi4.w + pj4.w + 1.0e-2f, sure = pi4.w + pj4.w - 2.0e-2f;
+      float lim = a4.w + b4.w + 1.0e-2f, sure = a4.w + b4.w - 2.0e-2f;
       bool inside = false;
-      double r2[3];
       if (dd < lim * lim) {
-#pragma unroll
-        for (int k = 0; k < 3; k++) r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
         if (dd < sure * sure) {
           inside = true;
         } else {
+          double r1[3], r2[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
+            r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
+          }
           double z = dist_rn(r1, r2);
-          double range = __dsub_rn(__dadd_rn(rci, fd->sp[isp[jat]].rcA), 0.01);
+          double range = __dsub_rn(__dadd_rn(fd->sp[isp[iat]].rcA, fd->sp[isp[jat]].rcA), 0.01);
           inside = z < range;
         }
       }
       if (inside) {
+        // the vector match, in float where certain (common_match_f) and in
+        // FP64 in its band
+        auto match = [&](int q) {
+          int m = common_match_f(r3f[q], a4, d0, d1, d2, b4);
+          if (m != 0) return m > 0;
+          double r1[3], r2[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            r1[k] = __dadd_rn(ratom[3 * iat + k], xl[3 * ib + k]);
+            r2[k] = __dadd_rn(ratom[3 * jat + k], xl[3 * jb + k]);
+          }
+          return common_match(r3v + 3 * q, r1, r2);
+        };
         int tmb = 0;
         bool inbox = true;
         if (periodic) {
@@ -324,7 +364,7 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
             if (km < key) lo = mid + 1;
             else if (km > key) hi = mid - 1;
             else {
-              if (common_match(r3v + 3 * mid, r1, r2)) found = mid - q0;
+              if (match(mid)) found = mid - q0;
               break;
             }
           }
@@ -332,7 +372,7 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
         if (found < 0) {
           // rare: candidate at the cutoff edge; decide by the reference scan
           for (int q = q0; q < qn; q++)
-            if (common_match(r3v + 3 * q, r1, r2)) {
+            if (match(q)) {
               found = q - q0;
               break;
             }
@@ -579,7 +619,7 @@ int launch_neigh_back(const NeighArgs &a, cudaStream_t s) {
   if (a.P == 0) return 0;
   int threads = 256, blocks = (a.P + threads - 1) / threads;
   k_neigh_back<<<blocks, threads, 0, s>>>(a.N, a.P, a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.sid, a.xl,
-                                          a.ratom, a.neigh_back, a.r3v, a.status);
+                                          a.ratom, a.pos4, a.neigh_back, a.r3v, a.r3f, a.status);
   FB_LAUNCH_CHECK();
   return 0;
 }
@@ -590,9 +630,9 @@ int launch_common(const NeighArgs &a, cudaStream_t s) {
   if (a.P == 0) return 0;
   int threads = 256;
   long long blocks = ((long long)a.P * 32 + threads - 1) / threads;
-  k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.pos4, a.xlf, a.isp, a.fd, a.sid, a.xl,
+  k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl,
                                                 a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.r3v,
-                                                a.tcnt, a.rcnt, a.slot_off, a.slot_nn, a.slot_found);
+                                                a.r3f, a.tcnt, a.rcnt, a.slot_off, a.slot_nn, a.slot_found);
   FB_LAUNCH_CHECK();
   return 0;
 }
