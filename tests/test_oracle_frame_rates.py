@@ -165,3 +165,33 @@ def test_degenerate_triplet_has_no_frame_terms(seed):
     assert np.all(hA == 0.0) and np.all(hB == 0.0)
     assert np.abs(_literal(e, dA, M, rho)).max() == 0.0
     assert np.abs(_literal(e, dB, M, rho)).max() == 0.0
+
+
+def _frame2(r1, r2):
+    z = np.linalg.norm(r2 - r1)
+    sig = (r2 - r1) / z
+    e = O.epsilon(r2, sig)
+    d = np.zeros(27)
+    O.lib().or_depsilon_2c(np.ascontiguousarray(r1), np.ascontiguousarray(r2), float(z),
+                           np.ascontiguousarray(e.T.ravel()), d)
+    return e, d.reshape(3, 3, 3, order="F"), z
+
+
+def test_two_center_rates_match_depsilon_2c():
+    """The two-center force kernel's rates (frame_rates_2c) against the
+    oracle's Depsilon_2c in the standard frame: e^T de is skew with
+    W^xy = (e_x x r2)_q / |r2 x r1|, W^yz = -e_y,q / z, W^xz = -e_x,q / z."""
+    rng = np.random.default_rng(3)
+    worst = 0.0
+    for _ in range(200):
+        r1 = rng.normal(size=3) * 20.0
+        r2 = r1 + rng.normal(size=3) * 2.0
+        e, d, z = _frame2(r1, r2)
+        ic, iz = 1.0 / np.linalg.norm(np.cross(r2, r1)), 1.0 / z
+        ex, ey = e[:, 0], e[:, 1]
+        wxy = ic * np.cross(ex, r2)
+        for q in range(3):
+            W = np.array([[0.0, wxy[q], -iz * ex[q]], [-wxy[q], 0.0, -iz * ey[q]], [iz * ex[q], iz * ey[q], 0.0]])
+            Om = e.T @ d[q]
+            worst = max(worst, np.abs(Om - W).max() / (1.0 + np.abs(Om).max()))
+    assert worst < 1e-12, worst

@@ -62,7 +62,8 @@ __device__ __forceinline__ int shift_mbeta(int sx, int sy, int sz) {
   return L == 364 ? 0 : (L < 364 ? L + 1 : L);
 }
 
-__device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
+// returns true when epsilon's frame is the standard one (y along r2 x sighat)
+__device__ __forceinline__ bool pair_geom(const Ctx2c &c, int i, int p, double *r1, double *r2, double &z,
                                           double e[3][3]) {
   int j = c.neigh_j[p], mb = c.neigh_b[p];
   const double *xl = c.xl + (long long)c.sid[i] * XL_STRIDE;
@@ -82,7 +83,7 @@ __device__ __forceinline__ void pair_geom(const Ctx2c &c, int i, int p, double *
 #pragma unroll
     for (int k = 0; k < 3; k++) sig[k] = (r2[k] - r1[k]) * iz;
   }
-  epsilon_fn(r2, sig, e);
+  return epsilon_fn(r2, sig, e);
 }
 
 // interpolate one 2c cell at the weights (getMEs_Fdata_2c :378-401)
@@ -462,6 +463,29 @@ __device__ __forceinline__ void contract(const RotM &R, const DRotM &D, const do
   MolRho<PA, PB, K> G;
   mol_rho<PA, PB, K>(R, D, blk, G);
   contract_g<PA, PB, K>(G, v, vd, out);
+}
+
+// The same contraction (s and p shells) through the rotation rates of the
+// frame: Gf = L^T blk L over the whole block (mol_G_full), W[pair][q] the
+// rates W^xy, W^yz, W^xz of component q (frame_rates_2c):
+// out_q = sum_pair W[pair][q] tau^pair + sum_e vd_q(e) G(e)
+template <int PA, int PB, int K>
+__device__ __forceinline__ void contract_rates(const double *Gf, const double (*W)[3], const double *v,
+                                               const double *vd, double out[3]) {
+  using PL = Plan<PA, PB, K>;
+  constexpr int NA = PL::NA;
+  double tau[3];
+  mol_tau<PA, PB, K>(Gf, v, tau);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    double s = fma(W[2][q], tau[2], fma(W[1][q], tau[1], W[0][q] * tau[0]));
+    sfor<PL::m.n>([&](auto E) {
+      constexpr int e = decltype(E)::value;
+      constexpr int at = PL::m.mu[e] + NA * PL::m.nu[e];
+      s = fma(vd[q + 3 * e], Gf[at], s);
+    });
+    out[q] = s;
+  }
 }
 
 inline Ctx2c make2c(const AsmArgs &a) {

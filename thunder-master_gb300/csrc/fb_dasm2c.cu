@@ -9,22 +9,36 @@ namespace fb {
 // go through one derivative rotation), and the atom term adds the smoothed
 // charged shells with the smoother and monopole derivatives
 // (M_Dassemble_2c_DOGS.f90:780-1196); sig = sum rho(i,self) S(i,self).
-template <int PA, int PB, bool HASD, bool DOGS>
-__device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned what, double sig) {
+// RATES (s and p shells, no DOGS, no explicit derivative blocks): the
+// frame-derivative terms through the rotation rates of the pair frame
+// (frame_rates_2c, contract_rates) instead of Depsilon_2c and Dtwister's dL.
+// Pairs in epsilon's collinear fallback frame, and calls that keep the
+// derivative blocks (FB_KEEP_DBLOCKS), take the literal path (pair_d2c_at).
+template <int PA, int PB, bool HASD, bool DOGS, bool RATES>
+__device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned what, double sig,
+                                         const double *r1, const double *r2, double z, const double (*e)[3]) {
   using PL = Plan<PA, PB, K2C>;
   using PLA = Plan<PA, PA, K2C>;
   constexpr int NA = PL::NA, NB = PL::NB, NE = PL::m.n, NEA = PLA::m.n;
+  static_assert(!RATES || (!HASD && !DOGS), "rotation rates: s and p shells, no DOGS terms");
   const Ctx2c &b = c.b;
   int j = b.neigh_j[p];
   int in1 = b.isp[i], in2 = b.isp[j];
-  double r1[3], r2[3], z, e[3][3];
-  pair_geom(b, i, p, r1, r2, z, e);
-  double dd[3][3][3];
-  depsilon_2c(r1, r2, z, e, dd);
+  double ee[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) ee[a][k] = e[a][k];
   RotM R;
   DRotM D;
-  twister<HASD>(e, R);
-  dtwister<HASD>(e, dd, D);
+  twister<HASD>(ee, R);
+  if constexpr (!RATES) {
+    double dd[3][3][3];
+    depsilon_2c(r1, r2, z, ee, dd);
+    dtwister<HASD>(ee, dd, D);
+  }
+  double W[3][3];
+  if constexpr (RATES) frame_rates_2c(r1, r2, z, ee, W);
   double eta[3] = {e[0][2], e[1][2], e[2][2]};
   const FdataDev &fd = *b.fd;
   long long o = b.blk_off[p];
@@ -39,7 +53,7 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
   if (what & 1u) {
     interp2c_d<NE>(b.table2c, fd.c2[in1][in2][0], z, tiny, v, dv, b.status);
     vec2c<NE>(z, eta, dv, vd);
-    if (c.keep) {
+    if (!RATES && c.keep) {
       double Xd[3 * NA * NB];
       drotate_plan<PA, PB, K2C>(R, D, v, vd, Xd);
 #pragma unroll
@@ -48,24 +62,39 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
     double cb[NA * NB];
 #pragma unroll
     for (int q = 0; q < NA * NB; q++) cb[q] = __ldg(c.cape + o + q);
-    contract<PA, PB, K2C, HASD>(R, D, cb, v, vd, out);
+    if constexpr (RATES) {
+      double Gf[NA * NB];
+      mol_G_full<PA, PB>(R, cb, Gf);
+      contract_rates<PA, PB, K2C>(Gf, W, v, vd, out);
+    } else {
+      contract<PA, PB, K2C, HASD>(R, D, cb, v, vd, out);
+    }
 #pragma unroll
     for (int q = 0; q < 3; q++) c.sumS[3 * p + q] = out[q];
   }
   // the kinetic and on-top vna terms contract with the same density block:
-  // its molecular-frame form is taken once
+  // the literal form takes its molecular-frame form (with H) once; the
+  // rotation-rate form recomputes the cheaper L^T rho L at each use (fewer
+  // live registers)
   MolRho<PA, PB, K2C> Grb;
-  if ((what & 2u) || ((what & 4u) && !self)) mol_rho<PA, PB, K2C>(R, D, rb, Grb);
+  if constexpr (!RATES)
+    if ((what & 2u) || ((what & 4u) && !self)) mol_rho<PA, PB, K2C>(R, D, rb, Grb);
   if (what & 2u) {
     interp2c_d<NE>(b.table2c, fd.c2[in1][in2][1], z, tiny, v, dv, b.status);
     vec2c<NE>(z, eta, dv, vd);
-    if (c.keep) {
+    if (!RATES && c.keep) {
       double Xd[3 * NA * NB];
       drotate_plan<PA, PB, K2C>(R, D, v, vd, Xd);
 #pragma unroll
       for (int q = 0; q < 3 * NA * NB; q++) c.dT[3 * o + q] = Xd[q];
     }
-    contract_g<PA, PB, K2C>(Grb, v, vd, out);
+    if constexpr (RATES) {
+      double Grf[NA * NB];
+      mol_G_full<PA, PB>(R, rb, Grf);
+      contract_rates<PA, PB, K2C>(Grf, W, v, vd, out);
+    } else {
+      contract_g<PA, PB, K2C>(Grb, v, vd, out);
+    }
 #pragma unroll
     for (int q = 0; q < 3; q++) c.sumT[3 * p + q] = out[q];
   }
@@ -97,7 +126,13 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
         for (int e = 0; e < NE; e++) m[e] += v[e], dm[e] += dv[e];
       }
       vec2c<NE>(z, eta, dm, vd);
-      contract_g<PA, PB, K2C>(Grb, m, vd, out);
+      if constexpr (RATES) {
+        double Grf[NA * NB];
+        mol_G_full<PA, PB>(R, rb, Grf);
+        contract_rates<PA, PB, K2C>(Grf, W, m, vd, out);
+      } else {
+        contract_g<PA, PB, K2C>(Grb, m, vd, out);
+      }
 #pragma unroll
       for (int q = 0; q < 3; q++) f[q] -= out[q] * P_eq2;
     }
@@ -110,7 +145,13 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
     long long os = b.blk_off[b.pair_off[i] + b.neigh_self[i]];
 #pragma unroll
     for (int q = 0; q < NA * NA; q++) rs[q] = __ldg(c.rho + os + q);
-    contract<PA, PA, K2C, HASD>(R, D, rs, v, vd, out);
+    if constexpr (RATES) {
+      double Gs[NA * NA];
+      mol_G_full<PA, PA>(R, rs, Gs);
+      contract_rates<PA, PA, K2C>(Gs, W, v, vd, out);
+    } else {
+      contract<PA, PA, K2C, HASD>(R, D, rs, v, vd, out);
+    }
     if constexpr (DOGS) {
       // charged shells of jatom, smoothed: sum of dq * (smooth dX - eta
       // dsmooth X + (1 - smooth) d(S/z) + eta dsmooth S/z) contracted with
@@ -191,6 +232,34 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
   }
 }
 
+// the literal form out of line: it runs only for the rare collinear fallback
+// frame and for FB_KEEP_DBLOCKS, and a call keeps its registers off the
+// rotation-rate path
+template <int PA, int PB, bool HASD, bool DOGS>
+__device__ __noinline__ void pair_d2c_literal(const CtxD2c &c, int i, int p, unsigned what, double sig) {
+  double r1[3], r2[3], z, e[3][3];
+  pair_geom(c.b, i, p, r1, r2, z, e);
+  pair_d2c<PA, PB, HASD, DOGS, false>(c, i, p, what, sig, r1, r2, z, e);
+}
+
+// one pair: its geometry, then the rotation-rate form unless the pair frame is
+// epsilon's collinear fallback with non-zero Depsilon_2c derivatives
+template <int PA, int PB, bool HASD, bool DOGS>
+__device__ __forceinline__ void pair_d2c_at(const CtxD2c &c, int i, int p, unsigned what, double sig) {
+  double r1[3], r2[3], z, e[3][3];
+  bool estd = pair_geom(c.b, i, p, r1, r2, z, e);
+  if constexpr (!HASD && !DOGS) {
+    double cm;
+    if (!c.keep && (estd || frame2c_degenerate(r1, r2, z, cm))) {
+      pair_d2c<PA, PB, HASD, DOGS, true>(c, i, p, what, sig, r1, r2, z, e);
+    } else {
+      pair_d2c_literal<PA, PB, HASD, DOGS>(c, i, p, what, sig);
+    }
+  } else {
+    pair_d2c<PA, PB, HASD, DOGS, false>(c, i, p, what, sig, r1, r2, z, e);
+  }
+}
+
 template <int PA, bool HASD, bool DOGS>
 __device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
   int p0 = c.b.pair_off[i], p1 = c.b.pair_off[i + 1];
@@ -217,9 +286,9 @@ __device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
   }
   for (int p = p0 + lane; p < p1; p += 32) {
     int pb = c.b.fd->sp[c.b.isp[c.b.neigh_j[p]]].pattern;
-    if (pb == PAT_SP) pair_d2c<PA, PAT_SP, HASD, DOGS>(c, i, p, what, sig);
-    else if (pb == PAT_S) pair_d2c<PA, PAT_S, HASD, DOGS>(c, i, p, what, sig);
-    else if constexpr (HASD) pair_d2c<PA, PAT_SPD, HASD, DOGS>(c, i, p, what, sig);
+    if (pb == PAT_SP) pair_d2c_at<PA, PAT_SP, HASD, DOGS>(c, i, p, what, sig);
+    else if (pb == PAT_S) pair_d2c_at<PA, PAT_S, HASD, DOGS>(c, i, p, what, sig);
+    else if constexpr (HASD) pair_d2c_at<PA, PAT_SPD, HASD, DOGS>(c, i, p, what, sig);
   }
 }
 

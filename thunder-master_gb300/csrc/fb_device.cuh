@@ -543,9 +543,9 @@ __device__ __forceinline__ void mol_G_full(const RotM &R, const double *rho, dou
 
 // tau^xy, tau^yz, tau^xz of the molecular-frame block M (values at the ME
 // positions of the plan) against the full molecular-frame density G
-template <int PA, int PB>
+template <int PA, int PB, int K = K3C>
 __device__ __forceinline__ void mol_tau(const double *G, const double *M, double tau[3]) {
-  using PL = Plan<PA, PB, K3C>;
+  using PL = Plan<PA, PB, K>;
   constexpr int NA = PL::NA, NB = PL::NB;
   constexpr bool pa = NA >= 4, pb = NB >= 4;
   sfor<3>([&](auto PR) {
@@ -600,6 +600,37 @@ __device__ __forceinline__ void frame_rates_3c(const double *r2, const double *r
   for (int k = 0; k < 3; k++) {
     w.byz[k] = -iz * ey[k];
     w.bxz[k] = -iz * ex[k];
+  }
+}
+
+// Rotation rates of the two-center frame epsilon(r2, sighat), component q of
+// d/dr1 (Depsilon_2c, b.FUNCTIONS/Depsilon_2c.f90:46-140, with
+// ic = 1 / |r2 x r1| and iz = 1 / z):
+//   W^xy = e_x . de_y = ic (e_x x r2)_q,  W^yz = e_y . de_z = -iz e_y,q,
+//   W^xz = e_x . de_z = -iz e_x,q
+// (its terms along e_x . e_y vanish).  Valid for the standard frame; all zero
+// where Depsilon_2c returns zeros (z < 1e-5 or |r2 x r1| < 1e-3).  W[pair][q],
+// pairs (x,y), (y,z), (x,z).
+__device__ __forceinline__ bool frame2c_degenerate(const double *r1, const double *r2, double z, double &cm) {
+  double c0 = r2[1] * r1[2] - r2[2] * r1[1];
+  double c1 = r2[2] * r1[0] - r2[0] * r1[2];
+  double c2 = r2[0] * r1[1] - r2[1] * r1[0];
+  cm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  return z < 1.0e-5 || fabs(cm) < 1.0e-3;
+}
+__device__ __forceinline__ void frame_rates_2c(const double *r1, const double *r2, double z, const double e[3][3],
+                                               double W[3][3]) {
+  double cm;
+  bool zero = frame2c_degenerate(r1, r2, z, cm);
+  double ic = zero ? 0.0 : 1.0 / cm, iz = zero ? 0.0 : 1.0 / z;
+  double ex[3] = {e[0][0], e[1][0], e[2][0]};
+  W[0][0] = ic * (ex[1] * r2[2] - ex[2] * r2[1]);
+  W[0][1] = ic * (ex[2] * r2[0] - ex[0] * r2[2]);
+  W[0][2] = ic * (ex[0] * r2[1] - ex[1] * r2[0]);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    W[1][q] = -iz * e[q][1];
+    W[2][q] = -iz * ex[q];
   }
 }
 
