@@ -259,8 +259,57 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
     }
   }
   const df *Tb = tab + (node0 - nx - 1) * NTHETA * NE;
-  // pass 1: the value contraction I_theta -> F and dF/dcos(theta); the
-  // theta loop is kept rolled (instruction-cache footprint, registers)
+  if constexpr (DERIV) {
+    // The interpolation is linear in the table values, so the Legendre sums
+    // come first at each of the 16 stencil nodes, g = sum_th P_th T_th and
+    // gp = sum_th P'_th T_th (dacc sums, the P_0 = 1 and P'_1 = 1 terms as
+    // their starting values), and the stencil weights then accumulate g
+    // (value, d/dx, d/dy) and gp (d/dcos) in four dacc sums per element:
+    // 4 + 3 + 4 accumulations per node and element instead of the 15 of the
+    // per-theta contraction.  The sums differ from the reference's order by
+    // rounding only.  Stencil rows and columns are rolled
+    // (instruction-cache footprint), the matrix elements unrolled.
+    dacc aF[NE], aDp[NE], aDx[NE], aDy[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) aF[e] = aDp[e] = aDx[e] = aDy[e] = dacc{0.0f, 0.0f};
+#pragma unroll 1
+    for (int j = 0; j < 4; j++) {
+      const df wyj = sel4(wy, j), dwyj = sel4(dwy, j);
+#pragma unroll 1
+      for (int k = 0; k < 4; k++) {
+        const df wxk = sel4(wx, k), dwxk = sel4(dwx, k);
+        const df W = wxk * wyj, Wx = dwxk * wyj, Wy = wxk * dwyj;
+        const df *Tn = Tb + ((long long)j * nx + k) * NTHETA * NE;
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          const df t0 = Tn[e], t1 = Tn[NE + e], t2 = Tn[2 * NE + e], t3 = Tn[3 * NE + e], t4 = Tn[4 * NE + e];
+          dacc g{t0.h, t0.l}, gp{t1.h, t1.l};
+          dacc_add(g, pl[1], t1);
+          dacc_add(g, pl[2], t2);
+          dacc_add(g, pl[3], t3);
+          dacc_add(g, pl[4], t4);
+          dacc_add(gp, dpl[2], t2);
+          dacc_add(gp, dpl[3], t3);
+          dacc_add(gp, dpl[4], t4);
+          const df gv = dacc_val(g), gpv = dacc_val(gp);
+          dacc_add(aF[e], W, gv);
+          dacc_add(aDx[e], Wx, gv);
+          dacc_add(aDy[e], Wy, gv);
+          dacc_add(aDp[e], W, gpv);
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      F[e] = dacc_val(aF[e]);
+      DpF[e] = dacc_val(aDp[e]);
+      DxF[e] = dacc_val(aDx[e]);
+      DyF[e] = dacc_val(aDy[e]);
+    }
+    return;
+  }
+  // value only: the per-theta contraction I_theta -> F; the theta loop is
+  // kept rolled (instruction-cache footprint, registers)
 #pragma unroll 1
   for (int th = 0; th < NTHETA; th++) {
     const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
