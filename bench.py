@@ -154,19 +154,13 @@ FP64_FLOP_PER_TRIPLET = 2 * 1943.959 + 64.0 + 346.996
 
 
 def flops_dassemble_3c(nme, prec="df"):
-    """FP64 FLOPs per triplet of the force kernel.  fp64: the FP64 kernel's
-    executed count (ncu), about 3,500 of them the interpolation (Legendre
-    sums first at each of the 16 stencil nodes, 4 + 3 FMA per node and
-    element, then the x contractions along each stencil row, 3 FMA per node,
-    and the row's y weights, 4 FMA per row).  df: the FP64
-    formulation of the per-theta form the double-float kernel executes on
-    the FP32 pipe, value + x + y contractions per theta (5 x 16 x 3 FMA per
-    element), the Legendre combination (4 x 5 FMA) and about 1,800 FLOP of
-    geometry, frame derivatives and the molecular-frame density
-    contraction (its "FP64-equivalent" rate)."""
-    if prec == "fp64":
-        return FP64_FLOP_PER_TRIPLET * (nme / 10.0)
-    return 2.0 * (3 * 5 * 16 * nme + 4 * 5 * nme) + 1800.0
+    """FP64 FLOPs per triplet of the force kernel: the FP64 kernel's executed
+    count (ncu), about 3,500 of them the interpolation (Legendre sums first at
+    each of the 16 stencil nodes, 4 + 3 FMA per node and element, then the x
+    contractions along each stencil row, 3 FMA per node, and the row's y
+    weights, 4 FMA per row).  The double-float kernel runs the same
+    formulation on the FP32 pipe; this count is its "FP64-equivalent" work."""
+    return FP64_FLOP_PER_TRIPLET * (nme / 10.0)
 
 
 def flops_assemble_3c(nme):
@@ -189,17 +183,17 @@ def tuned_shapes(ctx, fbgpu, autotune):
 
 # Executed FP32 work of the double-float three-center kernels per sp3 x sp3
 # triplet (2 FFMA + FADD + FMUL thread instructions: the force kernel
-# 9,546 + 26,981 + 3,192, ncu on SiC4096; the value kernel on Si512, the count
+# 6,417 + 19,682 + 2,149, ncu on SiC4096; the value kernel on Si512, the count
 # per triplet does not depend on the system size), and the DRAM bytes per
 # triplet of one launch (ncu on SiC4096, where the launch's working set
 # exceeds what L2 keeps between launches) (profiles/): the df formulation's
 # arithmetic is what the FP32 pipe must execute.
-DF_FP32_FLOP = {"dassemble_3c": 2 * 9545.781 + 26981.411 + 3191.927, "assemble_3c": 16284.0}
+DF_FP32_FLOP = {"dassemble_3c": 2 * 6416.868 + 19681.613 + 2148.956, "assemble_3c": 16284.0}
 # DRAM read + write bytes per triplet of one force-kernel launch, ncu on
 # SiC4096 (profiles/k_dassemble_3c_sic4096.md, 160.10 MB per launch;
-# profiles/k_dassemble_3c_df_sic4096.md, 159.59 MB; means of three launches),
+# profiles/k_dassemble_3c_df_sic4096.md, 159.88 MB; means of three launches),
 # over 5,125,854 triplets
-DRAM_BYTES_PER_TRIPLET = {"fp64": 160.100523e6 / 5125854, "df": 159.594240e6 / 5125854}
+DRAM_BYTES_PER_TRIPLET = {"fp64": 160.100523e6 / 5125854, "df": 159.876693e6 / 5125854}
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
