@@ -69,8 +69,11 @@ struct fb_ctx {
   std::vector<double> h_lat;   // 9 per structure, rows a1, a2, a3
   std::vector<double> h_xl;    // XL_STRIDE per structure
   std::vector<float4> h_sbbox; // lo, hi per structure
+  std::vector<float4> h_cbox;  // lo, hi per chunk of 32 consecutive atoms of a structure
+  std::vector<int> h_cb_off;   // first chunk of each structure
   float rcmax = 0.0f;
   DevBuf d_ratom, d_pos4, d_isp, d_xl, d_xlf, d_imgs, d_sid, d_satom_off, d_simg_off, d_sbbox, d_speriodic;
+  DevBuf d_cbox, d_cb_off;
   // neighbors
   bool have_neigh = false;
   int P = 0, T = 0;
@@ -302,6 +305,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
                     &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm, &ctx->d_tbin, &ctx->d_mlp_pts, &ctx->d_mlp_ptrip,
                     &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_rcnt, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
+                    &ctx->d_cbox, &ctx->d_cb_off,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
   ctx->d_queue.release();
@@ -502,11 +506,38 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
     ctx->h_sbbox[2 * s] = lo;
     ctx->h_sbbox[2 * s + 1] = hi;
   }
+  // bounding boxes of the chunks of 32 consecutive atoms the neighbor sweep
+  // takes per warp step: a chunk whose shifted box lies beyond reach of atom
+  // i is skipped whole, which keeps the (mbeta, jatom) order
+  ctx->h_cb_off.assign(ns + 1, 0);
+  for (int s = 0; s < ns; s++) {
+    int na = ctx->h_satom_off[s + 1] - ctx->h_satom_off[s];
+    ctx->h_cb_off[s + 1] = ctx->h_cb_off[s] + (na + 31) / 32;
+  }
+  ctx->h_cbox.assign(2 * (size_t)ctx->h_cb_off[ns], make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  for (int s = 0; s < ns; s++) {
+    int a0 = ctx->h_satom_off[s], a1 = ctx->h_satom_off[s + 1];
+    for (int k = 0; a0 + 32 * k < a1; k++) {
+      float4 lo = make_float4(1e30f, 1e30f, 1e30f, 0.0f), hi = make_float4(-1e30f, -1e30f, -1e30f, 0.0f);
+      for (int i = a0 + 32 * k; i < std::min(a1, a0 + 32 * k + 32); i++) {
+        lo.x = std::min(lo.x, p4[i].x);
+        lo.y = std::min(lo.y, p4[i].y);
+        lo.z = std::min(lo.z, p4[i].z);
+        hi.x = std::max(hi.x, p4[i].x);
+        hi.y = std::max(hi.y, p4[i].y);
+        hi.z = std::max(hi.z, p4[i].z);
+      }
+      ctx->h_cbox[2 * (size_t)(ctx->h_cb_off[s] + k)] = lo;
+      ctx->h_cbox[2 * (size_t)(ctx->h_cb_off[s] + k) + 1] = hi;
+    }
+  }
   CHK(ctx->d_ratom.ensure(3 * (size_t)N * sizeof(double)));
   CHK(ctx->d_pos4.ensure(N * sizeof(float4)));
   CHK(ctx->d_imgs.ensure(ctx->h_imgs.size() * sizeof(int)));
   CHK(ctx->d_simg_off.ensure((ns + 1) * sizeof(int)));
   CHK(ctx->d_sbbox.ensure(2 * (size_t)ns * sizeof(float4)));
+  CHK(ctx->d_cbox.ensure(ctx->h_cbox.size() * sizeof(float4)));
+  CHK(ctx->d_cb_off.ensure((ns + 1) * sizeof(int)));
   CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_pos4.p, p4.data(), N * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_imgs.p, ctx->h_imgs.data(), ctx->h_imgs.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -514,6 +545,10 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
   CU(cudaMemcpyAsync(ctx->d_simg_off.p, ctx->h_simg_off.data(), (ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_sbbox.p, ctx->h_sbbox.data(), 2 * (size_t)ns * sizeof(float4), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_cbox.p, ctx->h_cbox.data(), ctx->h_cbox.size() * sizeof(float4), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_cb_off.p, ctx->h_cb_off.data(), (ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_neigh = false;
@@ -531,6 +566,8 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.satom_off = ctx->d_satom_off.as<int>();
   a.simg_off = ctx->d_simg_off.as<int>();
   a.sbbox = ctx->d_sbbox.as<float4>();
+  a.cbox = ctx->d_cbox.as<float4>();
+  a.cb_off = ctx->d_cb_off.as<int>();
   a.speriodic = ctx->d_speriodic.as<int>();
   a.rcmax = ctx->rcmax;
   a.isp = ctx->d_isp.as<int>();

@@ -54,12 +54,21 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
 #pragma unroll
     for (int b = 0; b < 3; b++) R.p[a][b] = g.e[pperm(a)][pperm(b)];
   if constexpr (FUSE) {
-    df X[NA * NB];
-    rotate_plan_df<PA, PB, K3C>(R, F, X);
-    double *dst = c.vb + c.blk_off[c.tdst[t]];
-    const df pe = peq2_df();
+    // the value-pass term in FP64 on the otherwise idle FP64 pipe: a few
+    // dozen instructions instead of the double-float rotation's several
+    // hundred (code size, issue slots), from the df values and frame
+    RotM Rd;
 #pragma unroll
-    for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, df_to(X[q] * pe));
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) Rd.p[a][b] = df_to(R.p[a][b]);
+    double Md[NE], X[NA * NB];
+#pragma unroll
+    for (int e = 0; e < NE; e++) Md[e] = df_to(F[e]) * P_eq2;
+    rotate_plan<PA, PB, K3C>(Rd, Md, X);
+    double *dst = c.vb + c.blk_off[c.tdst[t]];
+#pragma unroll
+    for (int q = 0; q < NA * NB; q++) atomicAdd(dst + q, X[q]);
   }
   const df *rho = c.rho_df + c.blk_off[c.tdst[t]];
   df rb[NA * NB], Gf[NA * NB], G[NE];

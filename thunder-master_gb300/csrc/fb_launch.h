@@ -38,6 +38,8 @@ struct NeighArgs {
   const int *satom_off;   // first atom of each structure (+ end)
   const int *simg_off;    // images of structure s: imgs[simg_off[s] .. simg_off[s+1]-1]
   const float4 *sbbox;    // bounding box (lo, hi) of each structure's positions
+  const float4 *cbox;     // bounding box (lo, hi) of each chunk of 32 consecutive atoms
+  const int *cb_off;      // first chunk of each structure
   const int *speriodic;   // 1 for a periodic structure, 0 for a cluster
   float rcmax;            // largest species cutoff
   const int *isp;

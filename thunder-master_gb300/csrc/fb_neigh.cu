@@ -25,6 +25,7 @@ struct NeighAtom {
   float4 pi;    // (x, y, z, float cutoff of species)
   float reach;  // float reach of atom i: its cutoff + the largest cutoff + margin
   float4 lo, hi;
+  const float4 *cb;  // chunk boxes of the structure
   const double *X;
   const float *Xf;
 };
@@ -49,6 +50,14 @@ __device__ __forceinline__ int neigh_sweep(const NeighAtom &A, int mb, int lane,
   double X0 = A.X[3 * mb], X1 = A.X[3 * mb + 1], X2 = A.X[3 * mb + 2];
   int num = 0;
   for (int j0 = A.a0; j0 < A.a1; j0 += 32) {
+    // skip the chunk of 32 atoms whose shifted box lies beyond reach (warp-uniform)
+    {
+      const float4 clo = A.cb[2 * ((j0 - A.a0) >> 5)], chi = A.cb[2 * ((j0 - A.a0) >> 5) + 1];
+      float cx = fmaxf(fmaxf(clo.x + L0 - A.pi.x, A.pi.x - (chi.x + L0)), 0.0f);
+      float cy = fmaxf(fmaxf(clo.y + L1 - A.pi.y, A.pi.y - (chi.y + L1)), 0.0f);
+      float cz = fmaxf(fmaxf(clo.z + L2 - A.pi.z, A.pi.z - (chi.z + L2)), 0.0f);
+      if (cx * cx + cy * cy + cz * cz > A.reach * A.reach) continue;
+    }
     int j = j0 + lane;
     bool hit = false;
     if (j < A.a1) {
@@ -98,7 +107,8 @@ template <bool FILL>
 __global__ void __launch_bounds__(NEIGH_THREADS)
     k_neigh(int N, const double *__restrict__ ratom, const float4 *__restrict__ pos4, const int *__restrict__ isp,
             const FdataDev *__restrict__ fd, const int *__restrict__ sid, const int *__restrict__ satom_off,
-            const int *__restrict__ simg_off, const float4 *__restrict__ sbbox, float rcmax,
+            const int *__restrict__ simg_off, const float4 *__restrict__ sbbox, const float4 *__restrict__ cbox,
+            const int *__restrict__ cb_off, float rcmax,
             const double *__restrict__ xl, const float *__restrict__ xlf, const int *__restrict__ imgs,
             int *__restrict__ cnt, long long *__restrict__ bsum, const int *__restrict__ pair_off,
             const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
@@ -118,6 +128,7 @@ __global__ void __launch_bounds__(NEIGH_THREADS)
   A.Xf = xlf + (long long)s * XL_STRIDE;
   A.lo = sbbox[2 * s];
   A.hi = sbbox[2 * s + 1];
+  A.cb = cbox + 2 * (long long)cb_off[s];
 #pragma unroll
   for (int k = 0; k < 3; k++) A.ri[k] = ratom[3 * i + k];
   A.pi = pos4[i];
@@ -602,13 +613,15 @@ int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
   int threads = NEIGH_THREADS, blocks = a.N;
   if (fill)
     k_neigh<true><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
-                                             a.sbbox, a.rcmax, a.xl, a.xlf, a.imgs, nullptr, nullptr, a.pair_off,
+                                             a.sbbox, a.cbox, a.cb_off, a.rcmax, a.xl, a.xlf, a.imgs, nullptr, nullptr,
+                                             a.pair_off,
                                              a.blk_base,
                                              a.neigh_j, a.neigh_b, a.neigh_self, a.pair_owner_w, a.blk_off_w,
                                              a.status, a.errinfo);
   else
     k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
-                                              a.sbbox, a.rcmax, a.xl, a.xlf, a.imgs, a.cnt, a.bsum, nullptr, nullptr,
+                                              a.sbbox, a.cbox, a.cb_off, a.rcmax, a.xl, a.xlf, a.imgs, a.cnt, a.bsum,
+                                              nullptr, nullptr,
                                               nullptr,
                                               nullptr, nullptr, nullptr, nullptr, a.status, a.errinfo);
   FB_LAUNCH_CHECK();
