@@ -306,64 +306,29 @@ __device__ __forceinline__ void interp3c_df(const Ctx3c &c, const Cell3cDev &cel
       DxF[e] = dacc_val(aDx[e]);
       DyF[e] = dacc_val(aDy[e]);
     }
-    return;
-  }
-  // value only: the per-theta contraction I_theta -> F; the theta loop is
-  // kept rolled (instruction-cache footprint, registers)
-#pragma unroll 1
-  for (int th = 0; th < NTHETA; th++) {
-    const df plt = sel5(pl, th), dplt = DERIV ? sel5(dpl, th) : df_zero();
-    dacc I[NE];
-    // stencil rows rolled (instruction-cache footprint)
-#pragma unroll
-    for (int e = 0; e < NE; e++) I[e] = dacc{0.0f, 0.0f};
-#pragma unroll 1
-    for (int j = 0; j < 4; j++) {
-      const df wyj = sel4(wy, j);
-      const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        df w = wx[k] * wyj;
-#pragma unroll
-        for (int e = 0; e < NE; e++) dacc_add(I[e], w, Tr[k * NTHETA * NE + e]);
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < NE; e++) {
-      df iv = dacc_val(I[e]);
-      F[e] = F[e] + plt * iv;
-      if (DERIV) DpF[e] = DpF[e] + dplt * iv;
-    }
-  }
-  if constexpr (DERIV) {
-    // pass 2: the x and y derivative contractions (fewer live accumulators
-    // than one fused pass; the stencil is re-read from L1)
+  } else {
+    // value only: the per-theta contraction I_theta -> F; the theta loop is
+    // kept rolled (instruction-cache footprint, registers)
 #pragma unroll 1
     for (int th = 0; th < NTHETA; th++) {
       const df plt = sel5(pl, th);
-      dacc Ix[NE], Iy[NE];
+      dacc I[NE];
+      // stencil rows rolled (instruction-cache footprint)
 #pragma unroll
-      for (int e = 0; e < NE; e++) Ix[e] = Iy[e] = dacc{0.0f, 0.0f};
+      for (int e = 0; e < NE; e++) I[e] = dacc{0.0f, 0.0f};
 #pragma unroll 1
       for (int j = 0; j < 4; j++) {
-        const df wyj = sel4(wy, j), dwyj = sel4(dwy, j);
+        const df wyj = sel4(wy, j);
         const df *Tr = Tb + (long long)j * nx * NTHETA * NE + th * NE;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          df wxd = dwx[k] * wyj, wyd = wx[k] * dwyj;
+          df w = wx[k] * wyj;
 #pragma unroll
-          for (int e = 0; e < NE; e++) {
-            df tv = Tr[k * NTHETA * NE + e];
-            dacc_add(Ix[e], wxd, tv);
-            dacc_add(Iy[e], wyd, tv);
-          }
+          for (int e = 0; e < NE; e++) dacc_add(I[e], w, Tr[k * NTHETA * NE + e]);
         }
       }
 #pragma unroll
-      for (int e = 0; e < NE; e++) {
-        DxF[e] = DxF[e] + plt * dacc_val(Ix[e]);
-        DyF[e] = DyF[e] + plt * dacc_val(Iy[e]);
-      }
+      for (int e = 0; e < NE; e++) F[e] = F[e] + plt * dacc_val(I[e]);
     }
   }
 }
