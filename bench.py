@@ -147,10 +147,10 @@ def dist_env():
 # algorithmic work per unit
 # ---------------------------------------------------------------------------
 # Executed FP64 FLOPs per sp3 x sp3 triplet of the FP64 force kernel
-# (2 DFMA + DADD + DMUL: 1,944 + 64 + 347 thread instructions, ncu on
+# (2 DFMA + DADD + DMUL: 1,912 + 64 + 334 thread instructions, ncu on
 # SiC4096, profiles/k_dassemble_3c_sic4096.md; the divisions and square roots
 # are DFMA sequences and count in DFMA)
-FP64_FLOP_PER_TRIPLET = 2 * 1943.959 + 64.0 + 346.996
+FP64_FLOP_PER_TRIPLET = 2 * 1911.959 + 64.0 + 333.996
 
 
 def flops_dassemble_3c(nme, prec="df"):
@@ -190,10 +190,10 @@ def tuned_shapes(ctx, fbgpu, autotune):
 # arithmetic is what the FP32 pipe must execute.
 DF_FP32_FLOP = {"dassemble_3c": 2 * 6416.868 + 19681.613 + 2148.956, "assemble_3c": 16284.0}
 # DRAM read + write bytes per triplet of one force-kernel launch, ncu on
-# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 160.10 MB per launch;
+# SiC4096 (profiles/k_dassemble_3c_sic4096.md, 159.30 MB per launch;
 # profiles/k_dassemble_3c_df_sic4096.md, 159.88 MB; means of three launches),
 # over 5,125,854 triplets
-DRAM_BYTES_PER_TRIPLET = {"fp64": 160.100523e6 / 5125854, "df": 159.876693e6 / 5125854}
+DRAM_BYTES_PER_TRIPLET = {"fp64": 159.295317e6 / 5125854, "df": 159.876693e6 / 5125854}
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 

@@ -179,7 +179,7 @@ __device__ __forceinline__ void trip_geom(const Ctx3c &c, int t, int &ia, int &i
     for (int k = 0; k < 3; k++) g.rhat[k] = g.rnabc[k] * ix;
   }
   g.cost = g.sighat[0] * g.rhat[0] + g.sighat[1] * g.rhat[1] + g.sighat[2] * g.rhat[2];
-  g.estd = epsilon_fn(g.rhat, g.sighat, g.e);
+  g.estd = epsilon_unit(g.rhat, g.sighat, g.e);
 }
 
 // The frame-derivative terms of a triplet's three-center forces for s and p
@@ -277,7 +277,7 @@ __device__ __forceinline__ void interp3c(const Ctx3c &c, const Cell3cDev &cell, 
     double wx[4], wy[4], dwx[4], dwy[4];
     lagrange4(px, wx, dwx);
     lagrange4(py, wy, dwy);
-    double idx = 1.0 / cell.dx, idy = 1.0 / cell.dy;
+    const double idx = cell.idxd, idy = cell.idyd;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       dwx[k] *= idx;

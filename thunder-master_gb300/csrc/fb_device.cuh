@@ -112,6 +112,50 @@ __device__ __forceinline__ bool epsilon_fn(const double *r1, const double *r2, d
   return standard;
 }
 
+// epsilon_fn for arguments that are unit vectors already (or r1 = 0): the
+// three-center frame epsilon(rhat, sighat).  The normalisations of r1 and r2
+// are the identity to within an ulp and are skipped; the decisions are the
+// same (r1 = 0 or |r2 x r1| < 1e-4 takes the fallback y axis).
+__device__ __forceinline__ bool epsilon_unit(const double *r1, const double *r2, double e[3][3]) {
+  const double zp[3] = {r2[0], r2[1], r2[2]};
+  double yp[3] = {0.0, 0.0, 0.0}, ypm = 0.0;
+  if (r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2] > 1.0e-8) {
+    yp[0] = zp[1] * r1[2] - zp[2] * r1[1];
+    yp[1] = zp[2] * r1[0] - zp[0] * r1[2];
+    yp[2] = zp[0] * r1[1] - zp[1] * r1[0];
+    ypm = sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]);
+  }
+  const bool standard = !(ypm < 1.0e-4);
+  if (!standard) {
+    if (fabs(zp[0]) > 1.0e-4) {
+      yp[0] = -(zp[1] + zp[2]) / zp[0];
+      yp[1] = 1.0;
+      yp[2] = 1.0;
+    } else if (fabs(zp[1]) > 1.0e-4) {
+      yp[0] = 1.0;
+      yp[1] = -(zp[0] + zp[2]) / zp[1];
+      yp[2] = 1.0;
+    } else {
+      yp[0] = 1.0;
+      yp[1] = 1.0;
+      yp[2] = -(zp[0] + zp[1]) / zp[2];
+    }
+    ypm = sqrt(yp[0] * yp[0] + yp[1] * yp[1] + yp[2] * yp[2]);
+  }
+  double iy = 1.0 / ypm;
+  yp[0] *= iy;
+  yp[1] *= iy;
+  yp[2] *= iy;
+  double xp[3] = {yp[1] * zp[2] - yp[2] * zp[1], yp[2] * zp[0] - yp[0] * zp[2], yp[0] * zp[1] - yp[1] * zp[0]};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    e[k][0] = xp[k];
+    e[k][1] = yp[k];
+    e[k][2] = zp[k];
+  }
+  return standard;
+}
+
 __device__ __forceinline__ constexpr double levi(int i, int j, int k) {
   return (i == j || j == k || i == k) ? 0.0
          : ((i == 0 && j == 1) || (i == 1 && j == 2) || (i == 2 && j == 0)) ? 1.0

@@ -516,6 +516,8 @@ info_done:
           d.dy = c1.ymax / (c1.ny - 1.0);
           {
             double ix = 1.0 / d.dx, iy = 1.0 / d.dy;
+            d.idxd = ix;
+            d.idyd = iy;
             d.idx_h = (float)ix;
             d.idx_l = (float)(ix - (double)d.idx_h);
             d.idy_h = (float)iy;

@@ -184,6 +184,7 @@ struct Cell2cDev {
 struct Cell3cDev {
   int nx, ny, nME;
   double dx, dy, xmax, ymax;
+  double idxd, idyd;                 // 1/dx, 1/dy (the FP64 derivative weights)
   float idx_h, idx_l, idy_h, idy_l;  // 1/dx, 1/dy as hi + lo floats (the df derivative weights)
   long long off;      // -1 if absent
   long long node_off; // into lin / gxy
