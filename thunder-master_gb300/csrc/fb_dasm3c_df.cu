@@ -109,8 +109,14 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
   }
 }
 
+// At most 128 threads per CTA and 3 CTAs per SM: 168 registers per thread,
+// 12 warps per SM instead of the 8 that 255 registers allow.  The kernel is
+// issue- and latency-bound: the extra warps are worth more than the
+// 0.7-1 KB of spills per thread the cap costs (7.42 -> 6.71 ms on SiC4096,
+// the fused form 9.03 -> 7.41 ms).
+constexpr int DF_FORCE_THREADS = 128;
 template <bool MLP, bool FUSE>
-__global__ void __launch_bounds__(256) k_dassemble_3c_df(Ctx3c c, Sched q) {
+__global__ void __launch_bounds__(DF_FORCE_THREADS, 3) k_dassemble_3c_df(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
     int i = t;
     if (c.tperm) t = c.tperm[t];
@@ -125,12 +131,21 @@ __global__ void __launch_bounds__(256) k_dassemble_3c_df(Ctx3c c, Sched q) {
   });
 }
 
+// the three-center force shape, with the block size capped at the df
+// kernels' launch bound
+static KCfg df_force_cfg(const KCfg &cfg) {
+  KCfg k = cfg;
+  if (k.threads <= 0 || k.threads > DF_FORCE_THREADS) k.threads = DF_FORCE_THREADS;
+  return k;
+}
+
 int launch_dassemble_3c_df(const AsmArgs &a, cudaStream_t s) {
   if (a.ntrip == 0) return 0;
   Ctx3c c = make3c(a);
   dim3 grid, block;
   Sched q;
-  int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
+  int e = sched_launch(df_force_cfg(a.cfg_d3c), (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block,
+                       q);
   if (e) return e;
   if (a.fuse_value) k_dassemble_3c_df<false, true><<<grid, block, 0, s>>>(c, q);
   else k_dassemble_3c_df<false, false><<<grid, block, 0, s>>>(c, q);
@@ -143,7 +158,8 @@ int launch_dassemble_3c_mlp(const AsmArgs &a, cudaStream_t s) {
   Ctx3c c = make3c(a);
   dim3 grid, block;
   Sched q;
-  int e = sched_launch(a.cfg_d3c, (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block, q);
+  int e = sched_launch(df_force_cfg(a.cfg_d3c), (long long)a.ntrip, a.queue ? a.queue + 3 : nullptr, s, grid, block,
+                       q);
   if (e) return e;
   if (a.fuse_value) k_dassemble_3c_df<true, true><<<grid, block, 0, s>>>(c, q);
   else k_dassemble_3c_df<true, false><<<grid, block, 0, s>>>(c, q);
