@@ -191,9 +191,9 @@ def tuned_shapes(ctx, fbgpu, autotune):
 DF_FP32_FLOP = {"dassemble_3c": 2 * 6416.868 + 19681.613 + 2148.956, "assemble_3c": 16284.0}
 # DRAM read + write bytes per triplet of one force-kernel launch, ncu on
 # SiC4096 (profiles/k_dassemble_3c_sic4096.md, 159.30 MB per launch;
-# profiles/k_dassemble_3c_df_sic4096.md, 159.88 MB; means of three launches),
+# profiles/k_dassemble_3c_df_sic4096.md, 159.65 MB; means of three launches),
 # over 5,125,854 triplets
-DRAM_BYTES_PER_TRIPLET = {"fp64": 159.295317e6 / 5125854, "df": 159.876693e6 / 5125854}
+DRAM_BYTES_PER_TRIPLET = {"fp64": 159.295317e6 / 5125854, "df": 159.650645e6 / 5125854}
 TRAFFIC_SOURCE = {"fp64": "profiles/k_dassemble_3c_sic4096.md", "df": "profiles/k_dassemble_3c_df_sic4096.md"}
 
 
