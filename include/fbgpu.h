@@ -279,7 +279,10 @@ int fb_assemble_graph(fb_ctx *ctx, unsigned what);
  * 32), ctas_per_sm = 0 for a grid that covers the work (one triplet per
  * thread, one atom per warp), or > 0 for a persistent grid of
  * ctas_per_sm CTAs per SM whose warps take `chunk` groups of work (32
- * triplets, or one atom, per group) at a time from a device counter. */
+ * triplets, or one atom, per group) at a time from a device counter.  The
+ * double-float three-center force kernels run at most 128 threads per CTA
+ * (their register budget): a "dassemble_3c" shape of 256 threads runs them
+ * with 128. */
 int fb_set_launch(fb_ctx *ctx, const char *kernel, int threads,
                   int ctas_per_sm, int chunk);
 int fb_get_launch(const fb_ctx *ctx, const char *kernel, int *threads,
