@@ -50,6 +50,10 @@ struct fb_ctx {
   // overlapped with the kernels)
   cudaStream_t cstream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_val = nullptr, ev_frc = nullptr;
+  // and a second kernel stream: the two-center kernels run on it while the
+  // common-neighbor stage runs on the main stream
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_nb = nullptr, ev_2c = nullptr;
   // set while a graph of a value + force pass is captured: the force pass's
   // three-center table kernel also adds the value-pass vna terms, and the
   // value pass skips its three-center table kernel
@@ -327,7 +331,8 @@ void fb_destroy(fb_ctx *ctx) {
   }
   if (ctx->own) cudaStreamDestroy(ctx->own);
   if (ctx->cstream) cudaStreamDestroy(ctx->cstream);
-  cudaEvent_t evs[] = {ctx->ev_in, ctx->ev_val, ctx->ev_frc};
+  if (ctx->s2) cudaStreamDestroy(ctx->s2);
+  cudaEvent_t evs[] = {ctx->ev_in, ctx->ev_val, ctx->ev_frc, ctx->ev_nb, ctx->ev_2c};
   for (cudaEvent_t e : evs)
     if (e) cudaEventDestroy(e);
   delete ctx;
@@ -668,15 +673,27 @@ static int bin_triplets(fb_ctx *ctx) {
   return FB_OK;
 }
 
-// everything after the pair lists exist on the device: neigh_back, common
-// neighbors, block storage
-static int finish_neighbors(fb_ctx *ctx) {
-  int N = ctx->N, P = ctx->P;
+// after the pair lists exist on the device: neigh_back and the block storage
+static int finish_pairs(fb_ctx *ctx) {
+  int P = ctx->P;
   CHK(ctx->d_neigh_back.ensure(P * sizeof(int) + 4));
   CHK(ctx->d_r3v.ensure(3 * P * sizeof(double) + 8));
   CHK(ctx->d_r3f.ensure(P * sizeof(float4) + 16));
   NeighArgs a = neigh_args(ctx);
   KL(KT_NEIGH_BACK, launch_neigh_back(a, ctx->stream));
+  size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
+  CHK(ctx->d_S.ensure(bb));
+  CHK(ctx->d_T.ensure(bb));
+  CHK(ctx->d_vb.ensure(bb));
+  CHK(ctx->d_vbo.ensure(bb));
+  return FB_OK;
+}
+
+// after neigh_back: the common neighbors and the triplet binning (one host
+// synchronization with ctx->stream for the triplet count)
+static int finish_common(fb_ctx *ctx) {
+  int N = ctx->N, P = ctx->P;
+  NeighArgs a = neigh_args(ctx);
   // common neighbors: slots for every ordered pair of ialpha's non-self
   // neighbors, one row of n - 1 per non-self neighbor (n of them)
   std::vector<long long> soff(N + 1, 0);
@@ -719,22 +736,19 @@ static int finish_neighbors(fb_ctx *ctx) {
   ctx->mlp_cells = trip_cells(ctx);
   // triplet processing order, binned by (species triple, 3c grid cell)
   CHK(bin_triplets(ctx));
-  // block storage
-  size_t bb = (size_t)ctx->nblock * sizeof(double) + 8;
-  CHK(ctx->d_S.ensure(bb));
-  CHK(ctx->d_T.ensure(bb));
-  CHK(ctx->d_vb.ensure(bb));
-  CHK(ctx->d_vbo.ensure(bb));
   ctx->have_neigh = true;
   ctx->have_vna2c = ctx->have_rho = ctx->have_cape = ctx->have_dblocks = ctx->have_dip = false;
   ctx->assembled = ctx->dassembled = 0;
   return FB_OK;
 }
 
-int fb_neighbors(fb_ctx *ctx) {
-  if (!ctx) return FB_ERR_ARG;
-  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
-  CU(cudaSetDevice(ctx->device));
+static int finish_neighbors(fb_ctx *ctx) {
+  CHK(finish_pairs(ctx));
+  return finish_common(ctx);
+}
+
+// the pair stage of fb_neighbors: counts, pair lists, neigh_back, block storage
+static int neighbors_pairs(fb_ctx *ctx) {
   int N = ctx->N;
   CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
   CHK(ctx->d_cnt.ensure(N * sizeof(int)));
@@ -776,7 +790,15 @@ int fb_neighbors(fb_ctx *ctx) {
   CU(cudaMemsetAsync(ctx->d_neigh_self.p, 0xff, N * sizeof(int), ctx->stream));
   a = neigh_args(ctx);
   KL(KT_NEIGH_FILL, launch_neigh(a, true, ctx->stream));
-  return finish_neighbors(ctx);
+  return finish_pairs(ctx);
+}
+
+int fb_neighbors(fb_ctx *ctx) {
+  if (!ctx) return FB_ERR_ARG;
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  CU(cudaSetDevice(ctx->device));
+  CHK(neighbors_pairs(ctx));
+  return finish_common(ctx);
 }
 
 int fb_set_neighbors(fb_ctx *ctx, const int *neighn, const int *neigh_j, const int *neigh_b) {
@@ -1726,8 +1748,10 @@ int fb_set_denmat_device(fb_ctx *ctx, const void *rho_dev, const void *cape_dev)
 
 // device storage of the force pass (allocations happen here, never while
 // a graph is being captured)
-static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = false) {
-  if (!ctx->have_neigh) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
+static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = false, bool pairs_only = false) {
+  // (pairs_only: the pair lists exist, the common-neighbor stage is still to
+  // come; the storage allocated here depends on the pairs only)
+  if (!ctx->have_neigh && !pairs_only) return fail(ctx, FB_ERR_STATE, "fb_neighbors first");
   if ((what & FB_ALL) && !ctx->have_rho) return fail(ctx, FB_ERR_STATE, "fb_set_denmat first");
   if (what & (FB_VNL2C | FB_VNL3C)) {
     if (!ctx->have_pp_neigh) return fail(ctx, FB_ERR_STATE, "vnl: fb_neighbors_pp first");
@@ -1794,23 +1818,28 @@ static int prepare_dassemble(fb_ctx *ctx, unsigned what, bool graph_values = fal
   return FB_OK;
 }
 
-// clears and launches of the force pass (no synchronization)
-static int enqueue_dassemble(fb_ctx *ctx, unsigned what) {
+// clears and launches of the force pass (no synchronization).  phase 1 is
+// the clears and the two-center kernel, which read the pair lists only;
+// phase 2 the rest; phase 0 both.
+static int enqueue_dassemble(fb_ctx *ctx, unsigned what, int phase = 0) {
   int N = ctx->N, P = ctx->P;
   size_t pb = (size_t)3 * P * sizeof(double) + 8, ab = (size_t)3 * N * sizeof(double);
-  CU(cudaMemsetAsync(ctx->d_f3a.p, 0, ab, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_f3b.p, 0, ab, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_f3c.p, 0, ab, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_sumT.p, 0, pb, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_sumS.p, 0, pb, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_ontop.p, 0, pb, ctx->stream));
-  CU(cudaMemsetAsync(ctx->d_atomf.p, 0, pb, ctx->stream));
   AsmArgs a = asm_args(ctx);
   a.keep_dblocks = (what & FB_KEEP_DBLOCKS) != 0;
-  unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
-  // DOGS: the 2c kernel also leaves the per-pair sums the 3c and Ewald kernels read
-  if (a.dogs && (what & (FB_VNA3C | FB_EWALD))) w2 |= 8u;
-  if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
+  if (phase != 2) {
+    CU(cudaMemsetAsync(ctx->d_f3a.p, 0, ab, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3b.p, 0, ab, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_f3c.p, 0, ab, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_sumT.p, 0, pb, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_sumS.p, 0, pb, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_ontop.p, 0, pb, ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_atomf.p, 0, pb, ctx->stream));
+    unsigned w2 = what & (FB_S | FB_T | FB_VNA2C);
+    // DOGS: the 2c kernel also leaves the per-pair sums the 3c and Ewald kernels read
+    if (a.dogs && (what & (FB_VNA3C | FB_EWALD))) w2 |= 8u;
+    if (w2) KL(KT_DASM2C, launch_dassemble_2c(a, w2, ctx->stream));
+  }
+  if (phase == 1) return FB_OK;
   if ((what & FB_EWALD) && !a.dogs) {
     CU(cudaMemsetAsync(ctx->d_fsr.p, 0, (size_t)3 * P * sizeof(double), ctx->stream));
     CU(cudaMemsetAsync(ctx->d_flr.p, 0, (size_t)3 * N * sizeof(double), ctx->stream));
@@ -2188,42 +2217,99 @@ int fb_assemble_step(fb_ctx *ctx, const double *ratom, double *S, double *T, dou
   return FB_OK;
 }
 
-int fb_step_forces(fb_ctx *ctx, const double *ratom, const double *rho, const double *cape, double *S, double *T,
-                   double *vna, double *vnao, double *ftot) {
-  if (!ctx || !rho) return FB_ERR_ARG;
-  if (ctx->theory != FB_THEORY_HARRIS) return fail(ctx, FB_ERR_UNSUPPORTED, "fb_step_forces: Harris only");
-  CU(cudaSetDevice(ctx->device));
-  if (!ctx->cstream) CU(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
-  cudaEvent_t *evs[] = {&ctx->ev_in, &ctx->ev_val, &ctx->ev_frc};
-  for (cudaEvent_t *e : evs)
-    if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-  int st;
-  if (ratom && (st = fb_update_positions(ctx, ratom))) return st;
-  if ((st = fb_neighbors(ctx))) return st;
+// the overlapped form of fb_step_forces: after the pair stage of the
+// neighbor build, the two-center value and force kernels (which read the
+// pair lists only) run on a second stream while the main stream runs the
+// common-neighbor stage and its host synchronization; the fused three-center
+// kernel and build_forces wait for both
+static int step_overlapped(fb_ctx *ctx, const double *rho, const double *cape, unsigned what) {
   size_t bb = (size_t)ctx->nblock * sizeof(double);
-  CHK(ctx->d_rho.ensure(bb + 8));
-  CHK(ctx->d_cape.ensure(bb + 8));
-  const unsigned what = FB_ALL;
-  CHK(check_assemble(ctx, what));
-  CHK(prepare_mlp(ctx, true));
-  ctx->have_rho = true;
-  CHK(prepare_dassemble(ctx, what, true));
-  // the density matrices travel on the copy stream while the value pass runs
+  cudaStream_t main = ctx->stream;
+  // (the status word keeps the pair stage's flags: finish_common checks them)
+  CU(cudaEventRecord(ctx->ev_nb, main));
+  // the density matrices travel on the copy stream
   CU(cudaMemcpyAsync(ctx->d_rho.p, rho, bb, cudaMemcpyHostToDevice, ctx->cstream));
   if (cape) CU(cudaMemcpyAsync(ctx->d_cape.p, cape, bb, cudaMemcpyHostToDevice, ctx->cstream));
   else CU(cudaMemsetAsync(ctx->d_cape.p, 0, bb, ctx->cstream));
   CU(cudaEventRecord(ctx->ev_in, ctx->cstream));
-  CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
-  ctx->fuse3c = true;  // one interpolation per triplet, as in the graph step
-  st = enqueue_assemble(ctx, what);
-  if (!st && cudaEventRecord(ctx->ev_val, ctx->stream) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event record");
-  if (!st && cudaStreamWaitEvent(ctx->stream, ctx->ev_in, 0) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event wait");
-  if (!st) st = enqueue_dassemble(ctx, what);
+  // second stream: two-center value pass, then (with rho) the two-center
+  // force kernel and the clears of the force accumulators
+  ctx->stream = ctx->s2;
+  int st = cudaStreamWaitEvent(ctx->s2, ctx->ev_nb, 0) == cudaSuccess ? FB_OK : fail(ctx, FB_ERR_CUDA, "event wait");
+  if (!st) st = enqueue_assemble(ctx, what & (FB_S | FB_T | FB_VNA2C));
+  if (!st && cudaEventRecord(ctx->ev_val, ctx->s2) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event record");
+  if (!st && cudaStreamWaitEvent(ctx->s2, ctx->ev_in, 0) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event wait");
+  if (!st) st = enqueue_dassemble(ctx, what, 1);
+  if (!st && cudaEventRecord(ctx->ev_2c, ctx->s2) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event record");
+  ctx->stream = main;
+  // main stream: common neighbors and triplet bins, then the three-center
+  // force kernel (with the value-pass terms) and build_forces
+  if (!st) st = finish_common(ctx);
+  ctx->have_rho = true;
+  if (!st) st = check_assemble(ctx, what);
+  if (!st && cudaStreamWaitEvent(main, ctx->ev_2c, 0) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event wait");
+  ctx->fuse3c = true;
+  if (!st) st = enqueue_dassemble(ctx, what, 2);
   ctx->fuse3c = false;
   if (st) {
+    cudaStreamSynchronize(ctx->s2);
     cudaStreamSynchronize(ctx->cstream);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(main);
+  }
+  return st;
+}
+
+int fb_step_forces(fb_ctx *ctx, const double *ratom, const double *rho, const double *cape, double *S, double *T,
+                   double *vna, double *vnao, double *ftot) {
+  if (!ctx || !rho) return FB_ERR_ARG;
+  if (ctx->theory != FB_THEORY_HARRIS) return fail(ctx, FB_ERR_UNSUPPORTED, "fb_step_forces: Harris only");
+  if (ctx->N < 1) return fail(ctx, FB_ERR_STATE, "fb_set_structure first");
+  CU(cudaSetDevice(ctx->device));
+  if (!ctx->cstream) CU(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
+  if (!ctx->s2) CU(cudaStreamCreateWithFlags(&ctx->s2, cudaStreamNonBlocking));
+  cudaEvent_t *evs[] = {&ctx->ev_in, &ctx->ev_val, &ctx->ev_frc, &ctx->ev_nb, &ctx->ev_2c};
+  for (cudaEvent_t *e : evs)
+    if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  int st;
+  if (ratom && (st = fb_update_positions(ctx, ratom))) return st;
+  const unsigned what = FB_ALL;
+  // per-kernel timing drains its events at each host synchronization of the
+  // main stream, and the network routing sizes its storage from the triplet
+  // bins: both take the serial order
+  bool overlap = !ctx->timing && !mlp_routes(ctx);
+  if (overlap) {
+    if ((st = neighbors_pairs(ctx))) return st;
+  } else if ((st = fb_neighbors(ctx))) {
     return st;
+  }
+  size_t bb = (size_t)ctx->nblock * sizeof(double);
+  CHK(ctx->d_rho.ensure(bb + 8));
+  CHK(ctx->d_cape.ensure(bb + 8));
+  ctx->have_rho = true;
+  if (overlap) {
+    CHK(prepare_dassemble(ctx, what, true, true));
+    if ((st = step_overlapped(ctx, rho, cape, what))) return st;
+  } else {
+    CHK(check_assemble(ctx, what));
+    CHK(prepare_mlp(ctx, true));
+    CHK(prepare_dassemble(ctx, what, true));
+    // the density matrices travel on the copy stream while the value pass runs
+    CU(cudaMemcpyAsync(ctx->d_rho.p, rho, bb, cudaMemcpyHostToDevice, ctx->cstream));
+    if (cape) CU(cudaMemcpyAsync(ctx->d_cape.p, cape, bb, cudaMemcpyHostToDevice, ctx->cstream));
+    else CU(cudaMemsetAsync(ctx->d_cape.p, 0, bb, ctx->cstream));
+    CU(cudaEventRecord(ctx->ev_in, ctx->cstream));
+    CU(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+    ctx->fuse3c = true;  // one interpolation per triplet, as in the graph step
+    st = enqueue_assemble(ctx, what);
+    if (!st && cudaEventRecord(ctx->ev_val, ctx->stream) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event record");
+    if (!st && cudaStreamWaitEvent(ctx->stream, ctx->ev_in, 0) != cudaSuccess) st = fail(ctx, FB_ERR_CUDA, "event wait");
+    if (!st) st = enqueue_dassemble(ctx, what);
+    ctx->fuse3c = false;
+    if (st) {
+      cudaStreamSynchronize(ctx->cstream);
+      cudaStreamSynchronize(ctx->stream);
+      return st;
+    }
   }
   CU(cudaEventRecord(ctx->ev_frc, ctx->stream));
   // S, T and vnao are final after the value pass: they travel back while

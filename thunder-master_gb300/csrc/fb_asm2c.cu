@@ -173,7 +173,8 @@ __device__ void atom_2c(const Ctx2c &c, int i, int lane, unsigned what) {
       Xatom[q] = v;
     }
     if (lane == 0) {
-      long long os = c.blk_off[p0 + c.neigh_self[i]];
+      // (a missing self pair is reported by the neighbor fill; stay in bounds)
+      long long os = c.blk_off[p0 + max(c.neigh_self[i], 0)];
 #pragma unroll
       for (int q = 0; q < NA * NA; q++) c.vb[os + q] = Xatom[q];
     }

@@ -142,7 +142,7 @@ __device__ __forceinline__ void pair_d2c(const CtxD2c &c, int i, int p, unsigned
     interp2c_d<NEA>(b.table2c, fd.c2[in1][in2][4], z, tiny, v, dv, b.status);
     vec2c<NEA>(z, eta, dv, vd);
     double rs[NA * NA];
-    long long os = b.blk_off[b.pair_off[i] + b.neigh_self[i]];
+    long long os = b.blk_off[b.pair_off[i] + max(b.neigh_self[i], 0)];
 #pragma unroll
     for (int q = 0; q < NA * NA; q++) rs[q] = __ldg(c.rho + os + q);
     if constexpr (RATES) {
@@ -269,7 +269,7 @@ __device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
     // rotated as the overlap pass does, contracted with rho of the self block
     using PLA = Plan<PA, PA, K2C>;
     constexpr int NA = PLA::NA;
-    int ps = p0 + c.b.neigh_self[i];
+    int ps = p0 + max(c.b.neigh_self[i], 0);
     double r1[3], r2[3], z, e[3][3];
     pair_geom(c.b, i, ps, r1, r2, z, e);
     RotM R;
