@@ -1119,6 +1119,8 @@ static AsmArgs asm_args(fb_ctx *ctx) {
   a.N = ctx->N;
   a.ntrip = ctx->T;
   a.have_d = ctx->fdh.have_d;
+  a.P = ctx->P;
+  a.pair_owner = ctx->d_pair_owner.as<int>();
   a.ratom = ctx->d_ratom.as<double>();
   a.sid = ctx->d_sid.as<int>();
   a.isp = ctx->d_isp.as<int>();

@@ -22,7 +22,8 @@ namespace fb {
 // a warp reduction into i's self block.
 // ===========================================================================
 struct Ctx2c {
-  int N;
+  int N, P;
+  const int *pair_owner;
   const double *ratom;
   const int *sid;
   const int *isp;
@@ -491,6 +492,8 @@ __device__ __forceinline__ void contract_rates(const double *Gf, const double (*
 inline Ctx2c make2c(const AsmArgs &a) {
   Ctx2c c;
   c.N = a.N;
+  c.P = a.P;
+  c.pair_owner = a.pair_owner;
   c.ratom = a.ratom;
   c.sid = a.sid;
   c.isp = a.isp;

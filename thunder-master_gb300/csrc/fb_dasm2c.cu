@@ -292,14 +292,35 @@ __device__ void atom_d2c(const CtxD2c &c, int i, int lane, unsigned what) {
   }
 }
 
+template <int PA, bool HASD>
+__device__ __forceinline__ void pair_d2c_pb(const CtxD2c &c, int i, int p, unsigned what) {
+  int pb = c.b.fd->sp[c.b.isp[c.b.neigh_j[p]]].pattern;
+  if (pb == PAT_SP) pair_d2c_at<PA, PAT_SP, HASD, false>(c, i, p, what, 0.0);
+  else if (pb == PAT_S) pair_d2c_at<PA, PAT_S, HASD, false>(c, i, p, what, 0.0);
+  else if constexpr (HASD) pair_d2c_at<PA, PAT_SPD, HASD, false>(c, i, p, what, 0.0);
+}
+
+// DOGS: a warp per atom (the atom's self-overlap sum sig enters every pair);
+// otherwise a thread per pair, so that no lane idles past the end of an
+// atom's pair list
 template <bool HASD, bool DOGS>
 __global__ void __launch_bounds__(256) k_dassemble_2c(CtxD2c c, unsigned what, Sched q) {
-  for_each_warp_item(c.b.N, q, [&](int i, int lane) {
-    int pa = c.b.fd->sp[c.b.isp[i]].pattern;
-    if (pa == PAT_SP) atom_d2c<PAT_SP, HASD, DOGS>(c, i, lane, what);
-    else if (pa == PAT_S) atom_d2c<PAT_S, HASD, DOGS>(c, i, lane, what);
-    else if constexpr (HASD) atom_d2c<PAT_SPD, HASD, DOGS>(c, i, lane, what);
-  });
+  if constexpr (DOGS) {
+    for_each_warp_item(c.b.N, q, [&](int i, int lane) {
+      int pa = c.b.fd->sp[c.b.isp[i]].pattern;
+      if (pa == PAT_SP) atom_d2c<PAT_SP, HASD, DOGS>(c, i, lane, what);
+      else if (pa == PAT_S) atom_d2c<PAT_S, HASD, DOGS>(c, i, lane, what);
+      else if constexpr (HASD) atom_d2c<PAT_SPD, HASD, DOGS>(c, i, lane, what);
+    });
+  } else {
+    for_each_item(c.b.P, q, [&](int p) {
+      int i = c.b.pair_owner[p];
+      int pa = c.b.fd->sp[c.b.isp[i]].pattern;
+      if (pa == PAT_SP) pair_d2c_pb<PAT_SP, HASD>(c, i, p, what);
+      else if (pa == PAT_S) pair_d2c_pb<PAT_S, HASD>(c, i, p, what);
+      else if constexpr (HASD) pair_d2c_pb<PAT_SPD, HASD>(c, i, p, what);
+    });
+  }
 }
 
 // The four instantiations (HASD, DOGS) of k_dassemble_2c build as four parts of
@@ -336,7 +357,8 @@ int launch_dassemble_2c(const AsmArgs &a, unsigned what, cudaStream_t s) {
   c.dogs_ps = a.dogs_ps;
   dim3 grid, block;
   Sched q;
-  int e = sched_launch(a.cfg_d2c, (long long)a.N * 32, a.queue ? a.queue + 2 : nullptr, s, grid, block, q);
+  long long work = a.dogs ? (long long)a.N * 32 : (long long)a.P;
+  int e = sched_launch(a.cfg_d2c, work, a.queue ? a.queue + 2 : nullptr, s, grid, block, q);
   if (e) return e;
   int v = (a.have_d ? 2 : 0) + (a.dogs ? 1 : 0);
   return launch_dassemble_2c_v(v, c, what, q, grid, block, s);

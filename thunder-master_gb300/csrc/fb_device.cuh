@@ -800,18 +800,20 @@ __device__ __forceinline__ void lagrange7(double x, const Cell2cDev &c, int &i0,
 #pragma unroll
   for (int k = 0; k < 7; k++) w[k] = pre[k] * suf[k] * (Ck[k] * c.inv_dx6);
   if (dw) {
-    // derivative of prod_{p != k} t_p by running (value, derivative) pairs
+    // derivative of prod_{p != k} t_p = pre_k suf_k (every dt_p/dx = 1):
+    // the prefix and suffix products' derivatives by the product rule,
+    // dpre_{k+1} = dpre_k t_k + pre_k, dsuf_{k-1} = dsuf_k t_k + suf_k
+    double dpre[7], dsuf[7];
+    dpre[0] = 0.0;
+    dpre[1] = 1.0;
 #pragma unroll
-    for (int k = 0; k < 7; k++) {
-      double P = 1.0, dP = 0.0;
+    for (int p = 2; p < 7; p++) dpre[p] = fma(dpre[p - 1], t[p - 1], pre[p - 1]);
+    dsuf[6] = 0.0;
+    dsuf[5] = 1.0;
 #pragma unroll
-      for (int p = 0; p < 7; p++)
-        if (p != k) {
-          dP = fma(dP, t[p], P);
-          P = P * t[p];
-        }
-      dw[k] = dP * (Ck[k] * c.inv_dx6);
-    }
+    for (int p = 4; p >= 0; p--) dsuf[p] = fma(dsuf[p + 1], t[p + 1], suf[p + 1]);
+#pragma unroll
+    for (int k = 0; k < 7; k++) dw[k] = fma(dpre[k], suf[k], pre[k] * dsuf[k]) * (Ck[k] * c.inv_dx6);
   }
 }
 

@@ -72,6 +72,8 @@ struct NeighArgs {
 
 struct AsmArgs {
   int N, ntrip, have_d;
+  int P;                   // pairs (neighbor blocks)
+  const int *pair_owner;   // atom of each pair
   const double *ratom;
   const int *sid;  // structure of each atom (image vectors at xl + sid * XL_STRIDE)
   const int *isp;
