@@ -70,6 +70,7 @@ struct fb_ctx {
   // batch of one); structure s holds atoms h_satom_off[s] .. h_satom_off[s+1]-1
   int N = 0, nstruct = 0;
   std::vector<int> h_satom_off, h_sid, h_icl, h_simg_off, h_isp, h_imgs;
+  std::vector<long long> h_img_off;  // per structure: first (atom, image) entry of d_img_start / d_img_orb
   std::vector<double> h_lat;   // 9 per structure, rows a1, a2, a3
   std::vector<double> h_xl;    // XL_STRIDE per structure
   std::vector<float4> h_sbbox; // lo, hi per structure
@@ -77,6 +78,7 @@ struct fb_ctx {
   std::vector<int> h_cb_off;   // first chunk of each structure
   float rcmax = 0.0f;
   DevBuf d_ratom, d_pos4, d_isp, d_xl, d_xlf, d_imgs, d_sid, d_satom_off, d_simg_off, d_sbbox, d_speriodic;
+  DevBuf d_img_off, d_img_start, d_img_orb;
   DevBuf d_cbox, d_cb_off;
   // neighbors
   bool have_neigh = false;
@@ -309,6 +311,7 @@ void fb_destroy(fb_ctx *ctx) {
                     &ctx->d_sumS, &ctx->d_ontop, &ctx->d_atomf, &ctx->d_f3a, &ctx->d_f3b, &ctx->d_f3c,
                     &ctx->d_kin, &ctx->d_vna, &ctx->d_pul, &ctx->d_ftot, &ctx->d_bsum, &ctx->d_blk_base, &ctx->d_tab3df, &ctx->d_rho_df, &ctx->d_tkey, &ctx->d_trank, &ctx->d_tperm, &ctx->d_tbin, &ctx->d_mlp_pts, &ctx->d_mlp_ptrip,
                     &ctx->d_thist, &ctx->d_slot_off, &ctx->d_slot_nn, &ctx->d_slot_found, &ctx->d_rcnt, &ctx->d_sid, &ctx->d_satom_off, &ctx->d_simg_off, &ctx->d_sbbox,
+                    &ctx->d_img_off, &ctx->d_img_start, &ctx->d_img_orb,
                     &ctx->d_cbox, &ctx->d_cb_off,
                     &ctx->d_speriodic};
   for (DevBuf *b : bufs) b->release();
@@ -486,9 +489,12 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
   int N = ctx->N, ns = ctx->nstruct;
   ctx->h_imgs.clear();
   ctx->h_simg_off.assign(ns + 1, 0);
+  ctx->h_img_off.assign(ns + 1, 0);
   for (int s = 0; s < ns; s++) {
     make_images(ctx, s, ratom);
     ctx->h_simg_off[s + 1] = (int)ctx->h_imgs.size();
+    long long na = ctx->h_satom_off[s + 1] - ctx->h_satom_off[s];
+    ctx->h_img_off[s + 1] = ctx->h_img_off[s] + na * (ctx->h_simg_off[s + 1] - ctx->h_simg_off[s]);
   }
   // float positions with the species cutoff in .w, and the bounding boxes
   std::vector<float4> p4(N);
@@ -543,6 +549,11 @@ int fb_update_positions(fb_ctx *ctx, const double *ratom) {
   CHK(ctx->d_sbbox.ensure(2 * (size_t)ns * sizeof(float4)));
   CHK(ctx->d_cbox.ensure(ctx->h_cbox.size() * sizeof(float4)));
   CHK(ctx->d_cb_off.ensure((ns + 1) * sizeof(int)));
+  CHK(ctx->d_img_off.ensure((ns + 1) * sizeof(long long)));
+  CHK(ctx->d_img_start.ensure((size_t)ctx->h_img_off[ns] * sizeof(int) + 4));
+  CHK(ctx->d_img_orb.ensure((size_t)ctx->h_img_off[ns] * sizeof(long long) + 8));
+  CU(cudaMemcpyAsync(ctx->d_img_off.p, ctx->h_img_off.data(), (ns + 1) * sizeof(long long), cudaMemcpyHostToDevice,
+                     ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_ratom.p, ratom, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_pos4.p, p4.data(), N * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_imgs.p, ctx->h_imgs.data(), ctx->h_imgs.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -580,6 +591,9 @@ static NeighArgs neigh_args(fb_ctx *ctx) {
   a.xl = ctx->d_xl.as<double>();
   a.xlf = ctx->d_xlf.as<float>();
   a.imgs = ctx->d_imgs.as<int>();
+  a.img_off = ctx->d_img_off.as<long long>();
+  a.img_start = ctx->d_img_start.as<int>();
+  a.img_orb = ctx->d_img_orb.as<long long>();
   a.cnt = ctx->d_cnt.as<int>();
   a.bsum = ctx->d_bsum.as<long long>();
   a.blk_base = ctx->d_blk_base.as<long long>();

@@ -47,6 +47,12 @@ struct NeighArgs {
   const double *xl;
   const float *xlf;
   const int *imgs;
+  // per atom and image (from img_off[s] + (i - first atom of s) * images of
+  // s): the image's first slot in i's list and its norb start, written by the
+  // count pass for the fill pass
+  const long long *img_off;
+  int *img_start;
+  long long *img_orb;
   int *cnt;
   long long *bsum;
   const long long *blk_base;

@@ -7,11 +7,11 @@ namespace fb {
 // neighbor maps (c.SYSTEM/M_neighbors.f90:356-519, :681-812)
 // ===========================================================================
 // One CTA per atom i.  Its warps take the periodic images in turn; in an
-// image, lanes sweep jatom.  A first sweep counts each image's hits (and
+// image, lanes sweep jatom.  The count pass counts each image's hits (and
 // their norb sum) into shared memory, warp 0 scans the counts in increasing
-// mbeta, and the fill pass sweeps again, writing each image's hits from its
-// scanned offset: the list comes out in the reference order (mbeta outer,
-// jatom inner).  In a batch, j runs over the atoms of i's own structure and
+// mbeta and stores each image's first slot and norb start; the fill pass
+// sweeps again, writing each image's hits from those starts: the list comes
+// out in the reference order (mbeta outer, jatom inner).  In a batch, j runs over the atoms of i's own structure and
 // the images are that structure's.  A float prefilter with a 1e-2 A margin
 // discards far pairs; every candidate is decided by the uncontracted FP64
 // test of the reference: z = distance(r1, r2) < rc_i + rc_j - 0.01.
@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(NEIGH_THREADS)
             int *__restrict__ cnt, long long *__restrict__ bsum, const int *__restrict__ pair_off,
             const long long *__restrict__ blk_base, int *__restrict__ neigh_j, int *__restrict__ neigh_b,
             int *__restrict__ neigh_self, int *__restrict__ pair_owner, long long *__restrict__ blk_off,
+            const long long *__restrict__ img_off, int *__restrict__ img_start, long long *__restrict__ img_orb,
             unsigned *__restrict__ status, int *__restrict__ errinfo) {
   __shared__ int s_cnt[NIMG];         // hits of each image, then their first slot
   __shared__ long long s_orb[NIMG];   // norb sum of each image's hits, then its running start
@@ -142,6 +143,18 @@ __global__ void __launch_bounds__(NEIGH_THREADS)
   }
   int base = FILL ? pair_off[i] : 0;
   long long bbase = FILL ? blk_base[i] : 0;
+  // this atom's per-image first slots and norb starts (count pass -> fill pass)
+  long long ibase = img_off[s] + (long long)(i - A.a0) * nimg;
+  if constexpr (FILL) {
+    for (int k = warp; k < nimg; k += nw) {
+      long long orb = img_orb[ibase + k];
+      neigh_sweep<false, true>(A, imgs[g0 + k], lane, img_start[ibase + k], orb, ratom, pos4, isp, fd, base, bbase,
+                               neigh_j, neigh_b, neigh_self, pair_owner, blk_off, status, errinfo);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && neigh_self[i] < 0) atomicOr(status, DEVERR_SELF);
+    return;
+  }
   for (int k = warp; k < nimg; k += nw) {
     long long orb = 0;
     int c = neigh_sweep<!FILL, false>(A, imgs[g0 + k], lane, 0, orb, ratom, pos4, isp, fd, base, bbase, neigh_j,
@@ -171,26 +184,17 @@ __global__ void __launch_bounds__(NEIGH_THREADS)
         }
       }
       if (k < nimg) {
-        s_cnt[k] = carry + x - c;
-        s_orb[k] = corb + y - o;
+        img_start[ibase + k] = carry + x - c;
+        img_orb[ibase + k] = corb + y - o;
       }
       carry += __shfl_sync(0xffffffffu, x, 31);
       corb += __shfl_sync(0xffffffffu, y, 31);
     }
-    if (!FILL && lane == 0) {
+    if (lane == 0) {
       cnt[i] = carry;
       bsum[i] = (long long)A.ni * corb;
     }
   }
-  if (!FILL) return;
-  __syncthreads();
-  for (int k = warp; k < nimg; k += nw) {
-    long long orb = s_orb[k];
-    neigh_sweep<false, true>(A, imgs[g0 + k], lane, s_cnt[k], orb, ratom, pos4, isp, fd, base, bbase, neigh_j,
-                             neigh_b, neigh_self, pair_owner, blk_off, status, errinfo);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0 && neigh_self[i] < 0) atomicOr(status, DEVERR_SELF);
 }
 
 // neigh_back (M_neighbors.f90:469-486) and the per-pair vectors
@@ -530,7 +534,15 @@ __global__ void k_trip_key(int T, int nsp, int cells, const double *__restrict__
   // bins approved for the MLP-3c surrogate come first
   if (!(binok && binok[k])) k += nsp * nsp * nsp * cells;
   key[t] = k;
-  rank[t] = atomicAdd(hist + k, 1);
+  // neighboring triplets share bins: one atomic per bin and warp, the lanes
+  // of a bin ranked in lane order after the slots it reserves
+  unsigned act = __activemask();
+  unsigned peers = __match_any_sync(act, k);
+  int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+  int r0 = 0;
+  if (lane == leader) r0 = atomicAdd(hist + k, __popc(peers));
+  r0 = __shfl_sync(peers, r0, leader);
+  rank[t] = r0 + __popc(peers & ((1u << lane) - 1u));
 }
 
 // exclusive scan of the bin counts, one block
@@ -617,13 +629,14 @@ int launch_neigh(const NeighArgs &a, bool fill, cudaStream_t s) {
                                              a.pair_off,
                                              a.blk_base,
                                              a.neigh_j, a.neigh_b, a.neigh_self, a.pair_owner_w, a.blk_off_w,
-                                             a.status, a.errinfo);
+                                             a.img_off, a.img_start, a.img_orb, a.status, a.errinfo);
   else
     k_neigh<false><<<blocks, threads, 0, s>>>(a.N, a.ratom, a.pos4, a.isp, a.fd, a.sid, a.satom_off, a.simg_off,
                                               a.sbbox, a.cbox, a.cb_off, a.rcmax, a.xl, a.xlf, a.imgs, a.cnt, a.bsum,
                                               nullptr, nullptr,
                                               nullptr,
-                                              nullptr, nullptr, nullptr, nullptr, a.status, a.errinfo);
+                                              nullptr, nullptr, nullptr, nullptr, a.img_off, a.img_start, a.img_orb,
+                                              a.status, a.errinfo);
   FB_LAUNCH_CHECK();
   return 0;
 }
