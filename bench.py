@@ -97,6 +97,17 @@ class ClockSampler:
         out = os.environ.get("FBGPU_CLOCKS_DIR") or tempfile.gettempdir()
         self.path = os.path.join(out, "clocks_rank%d.csv" % device)
 
+    @classmethod
+    def warm(cls, device):
+        """One query ahead of every sampler: the first nvidia-smi start of a
+        process (binary and NVML state loaded cold) is the slow one."""
+        try:
+            subprocess.run(["nvidia-smi", "-i", str(device), "--query-gpu=" + cls.FIELDS,
+                            "--format=csv,noheader,nounits"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                           timeout=60)
+        except (OSError, subprocess.SubprocessError):
+            pass
+
     def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
@@ -423,6 +434,8 @@ def measure_single(args, ctx, fbgpu, torch, stream, flush, ws, local, st, NB, rh
     if sampler:
         sampler.start()
     ms, launches = timed(device_step, steps)
+    if e2e:
+        e2e_step()  # (one more untimed step right before the timed ones)
     ms_e2e = timed(e2e_step, steps)[0] if e2e else None
     ms_e2e_calls = timed(e2e_calls_step, steps)[0] if e2e else None
     clk = sampler.stop() if sampler else None
@@ -445,6 +458,7 @@ def run_gpu(args):
     import fbgpu
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
+    ClockSampler.warm(local)
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
