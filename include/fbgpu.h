@@ -246,7 +246,11 @@ int fb_get_forces(fb_ctx *ctx, int which, double *out);
  * assemble_vna_2c/3c) while rho and cape (nblock doubles each, block layout
  * of the maps just built; cape may be NULL) travel on a copy stream, then the
  * force pass (Dassemble_S/T/vna_2c/vna_3c, build_forces) while S, T and vnao
- * travel back; vna and ftot (3*natoms) follow.  Any output may be NULL.  The
+ * travel back; vna and ftot (3*natoms) follow.  The two-center kernels run
+ * on a second internal stream beside the common-neighbor search (unless
+ * per-kernel timing is on or MLP-3c routes triplets); the call returns after
+ * both internal streams and the context's stream are done.  Any output may
+ * be NULL.  The
  * same results as fb_neighbors + fb_set_denmat + fb_assemble_graph(FB_ALL |
  * FB_FORCES) + fb_get_blocks + fb_get_forces; pinned host buffers let the
  * copies overlap.  Harris only.  Replaces one SCF/MD step's calls of
