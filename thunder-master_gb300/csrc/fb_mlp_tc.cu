@@ -42,8 +42,8 @@ struct TcShape {
   static constexpr int consts = NTAN ? h + hsize : x + TILES * 128 * MLP_IN * 2;
   static constexpr int nconst = 3 * MLP_H + MLP_OUT + 3 * MLP_H;  // b1 b2 b3 b4, W1 columns 0..2
   static constexpr int rinfo = consts + nconst * 4;
-  static constexpr int bar = rinfo + TILES * 128 * 16;
-  static constexpr int smem = bar + 16;
+  static constexpr int bar = rinfo + TILES * 128 * 16;  // mbarrier, TMEM slot, tangents' mbarrier
+  static constexpr int smem = bar + 24;
   static constexpr int threads = 128 * TILES * SPLIT;
   static constexpr int cols = TILES * MT * 128;  // TMEM columns (a power of 2)
 };
@@ -86,6 +86,9 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
   float *rinfo = reinterpret_cast<float *>(smem + S::rinfo);  // [TILES * 128][4]: triple, cos, 2/xmax, 2/ymax
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S::bar);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::bar + 8);
+  // with tangents, the primal products commit to `bar` and the tangents'
+  // to `bart`, so that each half's epilogue overlaps the other's products
+  uint64_t *bart = reinterpret_cast<uint64_t *>(smem + S::bar + 16);
   const float *b1 = cst, *b2 = cst + MLP_H, *b3 = cst + 2 * MLP_H, *b4 = cst + 3 * MLP_H;
   const float *w1c = cst + 3 * MLP_H + MLP_OUT;  // [3][128]
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -112,6 +115,7 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
   for (int i = tid; i < MLP_OUT; i += S::threads) cst[3 * MLP_H + i] = a.params[a.o_b4 + i];
   if (tid == 0) {
     mbar_init(bar, 1);
+    mbar_init(bart, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) tmem_alloc(tslot, S::cols);
@@ -123,8 +127,8 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
   const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
   const FdataDev &fd = *c.fd;
   constexpr uint32_t ID128 = umma_idesc_bf16(128, MLP_H), ID64 = umma_idesc_bf16(128, MLP_OUT);
-  uint32_t phase = 0;
-  bool ok = true;
+  uint32_t phase = 0, phaset = 0;
+  bool ok = true, pend = false, pendt = false;  // commits not yet waited for
   const int ntiles = (a.n + 127) / 128;
   float *ri = rinfo + 4 * (tt * 128 + row);
 
@@ -190,9 +194,11 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
       }
       umma_commit(bar);
     }
+    pend = true;
     ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
-    phase ^= 1;
     if (!ok) break;
+    phase ^= 1;
+    pend = false;
     tc_fence_after();
     const float sx = ri[2], sy = ri[3];
     __nv_bfloat16 *H = Hs + tt * MT * 128 * MLP_H;
@@ -229,76 +235,194 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    // ---- layers 2 and 3 (K = N = 128) ----------------------------------------
+    // MMAs of one layer for operands [op0, op1) of every tile into their
+    // accumulators (the output layer: N = 64, accumulators 64 columns apart)
+    auto issue = [&](const __nv_bfloat16 *W, int op0, int op1, bool out_layer) {
+      uint32_t wb = smem_u32(W);
+      for (int q = 0; q < TILES; q++)
+        for (int op = op0; op < op1; op++) {
+          uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
+          uint32_t d = tmem + (q * MT + op) * (out_layer ? MLP_OUT : 128);
+          for (int ks = 0; ks < MLP_H / 16; ks++)
+            umma_bf16(d, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
+                      umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), out_layer ? ID64 : ID128, ks > 0);
+        }
+    };
+    if constexpr (NTAN == 0) {
+      // ---- layers 2 and 3 (K = N = 128) ----------------------------------------
 #pragma unroll 1
-    for (int l = 0; l < 2; l++) {
-      const __nv_bfloat16 *W = l == 0 ? W2s : W3s;
-      const float *bl = l == 0 ? b2 : b3;
+      for (int l = 0; l < 2; l++) {
+        const __nv_bfloat16 *W = l == 0 ? W2s : W3s;
+        const float *bl = l == 0 ? b2 : b3;
+        if (tid == 0) {
+          uint32_t wb = smem_u32(W);
+          for (int q = 0; q < TILES; q++)
+            for (int op = 0; op < MT; op++) {
+              uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
+              for (int ks = 0; ks < MLP_H / 16; ks++)
+                umma_bf16(tmem + (q * MT + op) * 128, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
+                          umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID128, ks > 0);
+            }
+          umma_commit(bar);
+        }
+        pend = true;
+        ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+        if (!ok) break;
+        phase ^= 1;
+        pend = false;
+        tc_fence_after();
+#pragma unroll 1
+        for (int c0 = part * HALF; c0 < (part + 1) * HALF; c0 += 16) {
+          float z[16], ds[16];
+          tmem_ld16(dbase + c0, z);
+#pragma unroll
+          for (int hh = 0; hh < 2; hh++) {
+            float hv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+              float zz = z[8 * hh + j] + bl[c0 + 8 * hh + j];
+              float sg = sigmoid_fast(zz);
+              hv[j] = zz * sg;
+              ds[8 * hh + j] = sg * (1.0f + zz * (1.0f - sg));
+            }
+            st_row8(H, row, c0 + 8 * hh, MLP_H, hv);
+          }
+#pragma unroll
+          for (int op = 1; op < MT; op++) {
+            float dz[16];
+            tmem_ld16(dbase + op * 128 + c0, dz);
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+              float tv[8];
+#pragma unroll
+              for (int j = 0; j < 8; j++) tv[j] = ds[8 * hh + j] * dz[8 * hh + j];
+              st_row8(H + op * 128 * MLP_H, row, c0 + 8 * hh, MLP_H, tv);
+            }
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+      }
+      if (!ok) break;
+      // ---- layer 4 (N = 64, 50 used) --------------------------------------------
       if (tid == 0) {
-        uint32_t wb = smem_u32(W);
+        uint32_t wb = smem_u32(W4s);
         for (int q = 0; q < TILES; q++)
           for (int op = 0; op < MT; op++) {
             uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
             for (int ks = 0; ks < MLP_H / 16; ks++)
-              umma_bf16(tmem + (q * MT + op) * 128, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
-                        umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID128, ks > 0);
+              umma_bf16(tmem + (q * MT + op) * MLP_OUT, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
+                        umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID64, ks > 0);
           }
         umma_commit(bar);
       }
+      pend = true;
       ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
-      phase ^= 1;
       if (!ok) break;
-      tc_fence_after();
+      phase ^= 1;
+      pend = false;
+    } else {
+      // Layers 2 and 3 with tangents, pipelined: the primal products commit
+      // to `bar`, the tangent products to `bart`.  The primal epilogue
+      // (SiLU and silu') runs while the tangent products of its layer run;
+      // the next layer's primal product (it reads only the primal operand
+      // and writes only the primal accumulator) is issued as soon as the
+      // primal operand is written, and runs while the tangent epilogue reads
+      // the tangent accumulators.  TMEM: layer l's accumulators at columns
+      // op * 128; the output layer's at op * 64, its primal (columns 0..63)
+      // issued during layer 3's tangent epilogue (columns 128..511), its
+      // tangents (64..255) only after it.
+      if (tid == 0) {
+        issue(W2s, 0, 1, false);
+        umma_commit(bar);
+        issue(W2s, 1, MT, false);
+        umma_commit(bart);
+      }
+      pend = pendt = true;
 #pragma unroll 1
-      for (int c0 = part * HALF; c0 < (part + 1) * HALF; c0 += 16) {
-        float z[16], ds[16];
-        tmem_ld16(dbase + c0, z);
+      for (int l = 0; l < 2; l++) {
+        const float *bl = l == 0 ? b2 : b3;
+        ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+        if (!ok) break;
+        phase ^= 1;
+        pend = false;
+        tc_fence_after();
+        float ds[HALF];  // silu'(z) of this thread's columns
 #pragma unroll
-        for (int hh = 0; hh < 2; hh++) {
-          float hv[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            float zz = z[8 * hh + j] + bl[c0 + 8 * hh + j];
-            float sg = sigmoid_fast(zz);
-            hv[j] = zz * sg;
-            ds[8 * hh + j] = sg * (1.0f + zz * (1.0f - sg));
-          }
-          st_row8(H, row, c0 + 8 * hh, MLP_H, hv);
-        }
-#pragma unroll
-        for (int op = 1; op < MT; op++) {
-          float dz[16];
-          tmem_ld16(dbase + op * 128 + c0, dz);
+        for (int cc = 0; cc < HALF / 16; cc++) {
+          const int c0 = part * HALF + 16 * cc;
+          float z[16];
+          tmem_ld16(dbase + c0, z);
 #pragma unroll
           for (int hh = 0; hh < 2; hh++) {
-            float tv[8];
+            float hv[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) tv[j] = ds[8 * hh + j] * dz[8 * hh + j];
-            st_row8(H + op * 128 * MLP_H, row, c0 + 8 * hh, MLP_H, tv);
+            for (int j = 0; j < 8; j++) {
+              float zz = z[8 * hh + j] + bl[c0 + 8 * hh + j];
+              float sg = sigmoid_fast(zz);
+              hv[j] = zz * sg;
+              ds[16 * cc + 8 * hh + j] = sg * (1.0f + zz * (1.0f - sg));
+            }
+            st_row8(H, row, c0 + 8 * hh, MLP_H, hv);
           }
         }
-      }
-      fence_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      tc_fence_after();
-    }
-    if (!ok) break;
-    // ---- layer 4 (N = 64, 50 used) --------------------------------------------
-    if (tid == 0) {
-      uint32_t wb = smem_u32(W4s);
-      for (int q = 0; q < TILES; q++)
-        for (int op = 0; op < MT; op++) {
-          uint32_t ha = smem_u32(Hs + (q * MT + op) * 128 * MLP_H);
-          for (int ks = 0; ks < MLP_H / 16; ks++)
-            umma_bf16(tmem + (q * MT + op) * MLP_OUT, umma_desc(ha + ks * 256, 128, (MLP_H / 8) * 128),
-                      umma_desc(wb + ks * 256, 128, (MLP_H / 8) * 128), ID64, ks > 0);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+          issue(l == 0 ? W3s : W4s, 0, 1, l == 1);
+          umma_commit(bar);
         }
-      umma_commit(bar);
+        pend = true;
+        ok = __syncthreads_and(mbar_wait(bart, phaset, TC_WAIT_LIMIT) ? 1 : 0) != 0;
+        if (!ok) break;
+        phaset ^= 1;
+        pendt = false;
+        tc_fence_after();
+#pragma unroll
+        for (int cc = 0; cc < HALF / 16; cc++) {
+          const int c0 = part * HALF + 16 * cc;
+#pragma unroll
+          for (int op = 1; op < MT; op++) {
+            float dz[16];
+            tmem_ld16(dbase + op * 128 + c0, dz);
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+              float tv[8];
+#pragma unroll
+              for (int j = 0; j < 8; j++) tv[j] = ds[16 * cc + 8 * hh + j] * dz[8 * hh + j];
+              st_row8(H + op * 128 * MLP_H, row, c0 + 8 * hh, MLP_H, tv);
+            }
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+          issue(l == 0 ? W3s : W4s, 1, MT, l == 1);
+          umma_commit(bart);
+        }
+        pendt = true;
+      }
+      if (!ok) break;
+      // the output layer's products, both halves
+      bool w = mbar_wait(bar, phase, TC_WAIT_LIMIT);
+      if (w) {
+        phase ^= 1;
+        pend = false;
+        w = mbar_wait(bart, phaset, TC_WAIT_LIMIT);
+        if (w) {
+          phaset ^= 1;
+          pendt = false;
+        }
+      }
+      ok = __syncthreads_and(w ? 1 : 0) != 0;
+      if (!ok) break;
     }
-    ok = __syncthreads_and(mbar_wait(bar, phase, TC_WAIT_LIMIT) ? 1 : 0) != 0;
-    phase ^= 1;
-    if (!ok) break;
     tc_fence_after();
     // ---- Legendre combination: each part sums its share of the output
     // columns, parts 1.. hand their partial sums to part 0 ------------------
@@ -377,7 +501,8 @@ __global__ void __launch_bounds__(TcShape<NTAN, TILES, SPLIT>::threads, 1)
   if (!ok) {
     // a product never completed: report it, give it one more bounded wait, release TMEM
     if (tid == 0) atomicOr(status, DEVERR_WATCHDOG);
-    mbar_wait(bar, phase ^ 1, TC_WAIT_LIMIT);
+    if (pend) mbar_wait(bar, phase, TC_WAIT_LIMIT);
+    if (pendt) mbar_wait(bart, phaset, TC_WAIT_LIMIT);
   }
   tc_fence_before();
   __syncthreads();
