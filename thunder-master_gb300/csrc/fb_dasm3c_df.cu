@@ -114,9 +114,11 @@ __device__ void trip_3c_force_df(const Ctx3c &c, int t, int i) {
 // issue- and latency-bound: the extra warps are worth more than the
 // 0.7-1 KB of spills per thread the cap costs (7.42 -> 6.71 ms on SiC4096,
 // the fused form 9.03 -> 7.41 ms).
+// The network-fed tail (MLP) has no interpolation and fewer live values: 4
+// CTAs per SM (128 registers, 16 warps) for 0.4-0.65 KB of spills.
 constexpr int DF_FORCE_THREADS = 128;
 template <bool MLP, bool FUSE>
-__global__ void __launch_bounds__(DF_FORCE_THREADS, 3) k_dassemble_3c_df(Ctx3c c, Sched q) {
+__global__ void __launch_bounds__(DF_FORCE_THREADS, MLP ? 4 : 3) k_dassemble_3c_df(Ctx3c c, Sched q) {
   for_each_item(c.T, q, [&](int t) {
     int i = t;
     if (c.tperm) t = c.tperm[t];
