@@ -281,6 +281,9 @@ __device__ __forceinline__ int common_match_f(float4 c, float4 a, float d0, floa
 // k-th non-self ineigh.  rcnt gets the row's count and tcnt[ialpha] (zeroed
 // by the caller) the sum over the rows; k_common_compact packs the rows in
 // ineigh order, so the triplets come out in the reference's loop order.
+constexpr int COMMON_THREADS = 256;  // k_common's block: 8 pair rows
+constexpr int COMMON_KEYS = 128;     // longest neighbor list staged in shared memory
+
 __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const double *__restrict__ ratom,
                          const int *__restrict__ isp, const FdataDev *__restrict__ fd, const int *__restrict__ sid,
                          const double *__restrict__ xl0, const int *__restrict__ pair_owner,
@@ -311,6 +314,14 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
   // formed only in the bands where the FP64 tests decide
   const float4 a4 = r3f[pi];
   int q0 = pair_off[iat], qn = pair_off[iat + 1];
+  // iat's list keys (mbeta * N + jatom), which the binary searches below
+  // probe, staged once per row in shared memory (lists up to COMMON_KEYS)
+  __shared__ long long s_key[COMMON_THREADS / 32][COMMON_KEYS];
+  long long *key_s = s_key[threadIdx.x >> 5];
+  const bool kshared = qn - q0 <= COMMON_KEYS;
+  if (kshared)
+    for (int k = lane; k < qn - q0; k += 32) key_s[k] = (long long)neigh_b[q0 + k] * N + neigh_j[q0 + k];
+  __syncwarp();
   int ibx, iby, ibz;
   mbeta_shift(ib, ibx, iby, ibz);
   for (int j0 = 0; j0 < n; j0 += 32) {
@@ -375,7 +386,7 @@ __global__ void k_common(int P, int N, const int *__restrict__ speriodic, const 
           int lo = q0, hi = qn - 1;
           while (lo <= hi) {
             int mid = (lo + hi) >> 1;
-            long long km = (long long)neigh_b[mid] * N + neigh_j[mid];
+            long long km = kshared ? key_s[mid - q0] : (long long)neigh_b[mid] * N + neigh_j[mid];
             if (km < key) lo = mid + 1;
             else if (km > key) hi = mid - 1;
             else {
@@ -654,7 +665,7 @@ int launch_common(const NeighArgs &a, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(a.tcnt, 0, (size_t)a.N * sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
   if (a.P == 0) return 0;
-  int threads = 256;
+  int threads = COMMON_THREADS;
   long long blocks = ((long long)a.P * 32 + threads - 1) / threads;
   k_common<<<(unsigned)blocks, threads, 0, s>>>(a.P, a.N, a.speriodic, a.ratom, a.isp, a.fd, a.sid, a.xl,
                                                 a.pair_owner, a.pair_off, a.neigh_j, a.neigh_b, a.neigh_self, a.r3v,
